@@ -1,0 +1,50 @@
+"""The oracle (oracle/ffno_oracle.py) against the reference's own float64 outputs and VJPs (tests/golden/)."""
+import pytest
+import torch
+
+from golden_io import CASES, load, model_config
+from oracle.ffno_oracle import OracleFFNO3D, lte_tables, vjp
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_forward_matches_reference(name):
+    meta, state, a = load(name)
+    oracle = OracleFFNO3D(state, model_config(meta), torch.float64)
+    with torch.no_grad():
+        y = oracle.forward(a["x"], a["z"], meta["dx"], meta["dy"])
+    assert (y - a["y64"]).abs().max().item() < 1e-10
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_vjp_matches_reference(name):
+    meta, state, a = load(name)
+    oracle = OracleFFNO3D(state, model_config(meta), torch.float64)
+    _, xb, zb = vjp(oracle, a["x"], a["z"], meta["dx"], meta["dy"], a["cot"])
+    assert ((xb - a["xbar"]).abs().max() / a["xbar"].abs().max()).item() < 1e-9
+    assert ((zb - a["zbar"]).abs().max() / a["zbar"].abs().max()).item() < 1e-8
+
+
+def test_oracle_float32_is_within_the_reference_float32_envelope():
+    meta, state, a = load("w32_m16")
+    oracle = OracleFFNO3D(state, model_config(meta), torch.float32)
+    with torch.no_grad():
+        y = oracle.forward(a["x"].float(), a["z"].float(), meta["dx"], meta["dy"]).double()
+    ref_err = (a["y32"] - a["y64"]).abs().max().item()
+    assert (y - a["y64"]).abs().max().item() < max(2 * ref_err, 1e-5)
+
+
+def test_head_matches_reference():
+    meta, state, a = load("head")
+    cfg = model_config(dict(width=16, n_layers=1, hidden_spectral=16, hidden_vertical=16, z_min_wavelength=0.5,
+                            atoms=meta["atoms"]))
+    oracle = OracleFFNO3D(state, cfg, torch.float64)
+    y = oracle.head(a["head"], a["x"])
+    assert (y - a["y64"]).abs().max().item() < 1e-12
+
+
+def test_lte_debye_stage_table():
+    # MULTI3D's ndxi after the shift by ion_1 (models/ffno_model.py:121-128): H (ion 1, 2) and Ca II (ion 2, 3)
+    _, _, ndxi_h, dion_h = lte_tables(dict(g=[2.0, 1.0], ev=[0.0, 13.6], ion=[1, 2]), 2)
+    assert ndxi_h == [0.0, 1.0] and dion_h == [0.0, 1.0]
+    _, _, ndxi_ca, dion_ca = lte_tables(dict(g=[2.0, 1.0], ev=[0.0, 11.9], ion=[2, 3]), 2)
+    assert ndxi_ca == [0.0, 3.0] and dion_ca == [0.0, 1.0]
