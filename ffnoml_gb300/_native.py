@@ -1,0 +1,103 @@
+"""ctypes binding of libffnoml_gb300.so (the C ABI declared in include/ffnoml_gb300.h).
+
+The library is built in-tree by ffnoml_gb300.build (or __graft_entry__.build()). There is no fallback: if the library
+is missing or fails to load, every operation raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libffnoml_gb300.so")
+
+P = ctypes.c_void_p
+I = ctypes.c_int
+L = ctypes.c_long
+F = ctypes.c_float
+D = ctypes.c_double
+
+FFNO_MAX_LEVELS = 32
+FFNO_MAX_SPECIES = 4
+
+ERRORS = {1: "invalid argument", 2: "kernel launch failed", 3: "workspace too small", 4: "device wait timed out"}
+
+
+class HeadParams(ctypes.Structure):
+    _fields_ = [
+        ("nspecies", I),
+        ("levels", I * FFNO_MAX_SPECIES),
+        ("rho_channel", I), ("temperature_channel", I), ("ne_channel", I),
+        ("in_channels", I),
+        ("total_bound", F),
+        ("log10_particle_mass", F * FFNO_MAX_SPECIES),
+        ("mean_x", F * 8), ("std_x", F * 8),
+        ("mean_y", F * FFNO_MAX_LEVELS), ("std_y", F * FFNO_MAX_LEVELS),
+        ("log_g", D * FFNO_MAX_LEVELS), ("ev", D * FFNO_MAX_LEVELS), ("ndxi", D * FFNO_MAX_LEVELS),
+        ("dion", D * FFNO_MAX_LEVELS),
+    ]
+
+
+class XformDesc(ctypes.Structure):
+    _fields_ = [
+        ("nb", L), ("nb2", L),
+        ("in_b1", L), ("in_b2", L), ("out_b1", L), ("out_b2", L),
+        ("K", I), ("M", I),
+        ("N", L),
+        ("in_split", I),
+        ("in_hi", L), ("in_lo", L),
+        ("out_split", I),
+        ("out_hi", L), ("out_lo", L),
+    ]
+
+
+# name -> argument types (all return int status)
+PROTOTYPES = {
+    "ffno_stats_parts": [L],
+    "ffno_depth_weights": [P, I, L, P, P],
+    "ffno_column_info": [P, I, L, P, P],
+    "ffno_lift_fwd": [P, I, L, I, P, P, P, P, I, I, P],
+    "ffno_gn_finalize": [P, I, I, I, P, P, F, P, P, P],
+    "ffno_gn_act": [P, P, L, I, I, P, P],
+    "ffno_gate_fwd": [P, L, I, P, P, P, P, P, P],
+    "ffno_mlp2_fwd": [I, P, P, P, F, P, L, I, P, P, P, P, P, I, I, P],
+    "ffno_fuse_fwd": [P, P, P, P, P, L, I, P, P, P, P, P, P, P, P, I, I, P],
+    "ffno_resid_out": [P, P, P, F, L, I, P, P],
+    "ffno_head_fwd": [P, P, L, I, P, P, P, I, I, ctypes.POINTER(HeadParams), P, P, P],
+    "ffno_xform": [P, P, P, ctypes.POINTER(XformDesc), I, P],
+    "ffno_spectral_mix": [P, P, L, L, L, L, L, I, P, P, P, P, I, P],
+}
+
+_lib = None
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+def lib():
+    """The loaded library; raises if it was not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise NativeError(f"{LIB_PATH} is missing: build it with `python -m ffnoml_gb300.build` "
+                              "(or __graft_entry__.build()); ffnoml_gb300 has no fallback path")
+        handle = ctypes.CDLL(LIB_PATH)
+        for name, args in PROTOTYPES.items():
+            fn = getattr(handle, name)
+            fn.argtypes = args
+            fn.restype = I
+        handle.ffno_version.restype = ctypes.c_char_p
+        handle.ffno_version.argtypes = []
+        _lib = handle
+    return _lib
+
+
+def call(name, *args):
+    """Call an entry point and raise on a non-zero status."""
+    status = getattr(lib(), name)(*args)
+    if status:
+        raise NativeError(f"{name} failed: {ERRORS.get(status, status)} (status {status})")
+    return status
+
+
+def exported_symbols():
+    return list(PROTOTYPES) + ["ffno_version"]

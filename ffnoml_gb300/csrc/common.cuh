@@ -1,0 +1,178 @@
+// Shared device helpers for the FFNO3D kernels: activations, the FP32 SIMT tile GEMM used by the pointwise (1x1x1
+// convolution) chains, and the deterministic depth-weighted GroupNorm statistics.
+//
+// Activation layout: channels last, one row of C floats per voxel, voxel v = (d * H + h) * W + w of one cube.
+// A "tile" is BM = 64 consecutive voxels processed by one CTA of NT = 256 threads; thread (ty, tx) = (tid / 16,
+// tid % 16) owns rows ty + 16 i (i < 4) and columns tx + 16 j (j < N / 16) of every tile GEMM output.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ffnoml_gb300.h"
+
+namespace ffno {
+
+constexpr int BM = 64;
+constexpr int NT = 256;
+constexpr int GMAX = 8;  // DepthWeightedGroupNorm uses at most 8 groups (models/ffno_model.py:21-25)
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752440f)); }
+
+// d gelu / dx = Phi(x) + x phi(x)
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752440f));
+  const float pdf = 0.39894228040143267794f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+__device__ __forceinline__ float sigmoid(float x) { return 1.f / (1.f + expf(-x)); }
+
+// acc[i][j] = sum_k A[(ty + 16 i) * lda + k] * W[k * N + tx + 16 j]; A in shared memory, W (row-major K x N) in
+// global memory (read through L1; every CTA reads the same small weight matrix).
+template <int K, int N>
+__device__ __forceinline__ void tile_mm(const float* __restrict__ A, int lda, const float* __restrict__ W,
+                                        float (&acc)[4][N / 16]) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < N / 16; ++j) acc[i][j] = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < K; ++k) {
+    float a[4], b[N / 16];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = A[(ty + 16 * i) * lda + k];
+#pragma unroll
+    for (int j = 0; j < N / 16; ++j) b[j] = __ldg(W + k * N + tx + 16 * j);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < N / 16; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+  }
+}
+
+// Copy rows v0 .. v0 + BM - 1 (C floats each, row-major, contiguous) into shared memory with row stride lds; rows at or
+// beyond V are zero.
+template <int C>
+__device__ __forceinline__ void load_rows(float* __restrict__ s, int lds, const float* __restrict__ g, long v0, long V) {
+  constexpr int Q = C / 4;  // float4 per row
+  for (int e = threadIdx.x; e < BM * Q; e += NT) {
+    const int r = e / Q, q = e % Q;
+    float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (v0 + r < V) val = __ldg(reinterpret_cast<const float4*>(g + (v0 + r) * C) + q);
+    float* d = s + r * lds + 4 * q;
+    d[0] = val.x; d[1] = val.y; d[2] = val.z; d[3] = val.w;
+  }
+}
+
+// Running weighted group statistics (total weight, mean, M2) of one CTA, merged tile by tile with Chan's parallel
+// update so that no long single-precision sum and no E[x^2] - E[x]^2 cancellation occurs.
+struct GroupAcc {
+  double w, mean, m2;
+};
+
+__device__ __forceinline__ void chan_merge(GroupAcc& a, double wt, double mt, double m2t) {
+  if (wt <= 0.0) return;
+  const double wn = a.w + wt;
+  const double delta = mt - a.mean;
+  a.mean += delta * (wt / wn);
+  a.m2 += m2t + delta * delta * (a.w * wt / wn);
+  a.w = wn;
+}
+
+// Scratch (shared memory) for tile_group_stats: colsum [16][N], col [N], gmean [GMAX], gw (1)
+template <int N>
+struct StatsSmem {
+  float part[16 * N];
+  float col[N];
+  float gmean[GMAX];
+  float wsum;
+};
+
+// Accumulate the depth-weighted statistics of one tile's values val (rows ty + 16 i, columns tx + 16 j) into acc[g]
+// (held by thread g < groups). wr[i] is the weight of row i, zero for rows past the cube. Column c belongs to group
+// c / cpg. Deterministic: fixed summation order.
+template <int N>
+__device__ __forceinline__ void tile_group_stats(const float (&val)[4][N / 16], const float (&wr)[4], int cpg,
+                                                 int groups, StatsSmem<N>& sm, GroupAcc& acc) {
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  // tile weight: sum of the row weights (each row counted once: the threads with tx == 0 hold rows ty + 16 i)
+  if (tx == 0) {
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) s += wr[i];
+    sm.part[ty] = s;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    float s = 0.f;
+    for (int t = 0; t < 16; ++t) s += sm.part[t];
+    sm.wsum = s;
+  }
+  __syncthreads();
+  // pass 1: weighted sums
+#pragma unroll
+  for (int j = 0; j < N / 16; ++j) {
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) s = fmaf(wr[i], val[i][j], s);
+    sm.part[ty * N + tx + 16 * j] = s;
+  }
+  __syncthreads();
+  for (int c = tid; c < N; c += NT) {
+    float s = 0.f;
+    for (int t = 0; t < 16; ++t) s += sm.part[t * N + c];
+    sm.col[c] = s;
+  }
+  __syncthreads();
+  if (tid < groups) {
+    float s = 0.f;
+    for (int c = tid * cpg; c < (tid + 1) * cpg; ++c) s += sm.col[c];
+    const float wt = sm.wsum * cpg;
+    sm.gmean[tid] = wt > 0.f ? s / wt : 0.f;
+  }
+  __syncthreads();
+  // pass 2: weighted squared deviations from the tile mean
+#pragma unroll
+  for (int j = 0; j < N / 16; ++j) {
+    const float m = sm.gmean[(tx + 16 * j) / cpg];
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float d = val[i][j] - m;
+      s = fmaf(wr[i] * d, d, s);
+    }
+    sm.part[ty * N + tx + 16 * j] = s;
+  }
+  __syncthreads();
+  for (int c = tid; c < N; c += NT) {
+    float s = 0.f;
+    for (int t = 0; t < 16; ++t) s += sm.part[t * N + c];
+    sm.col[c] = s;
+  }
+  __syncthreads();
+  if (tid < groups) {
+    float s = 0.f;
+    for (int c = tid * cpg; c < (tid + 1) * cpg; ++c) s += sm.col[c];
+    chan_merge(acc, (double)sm.wsum * cpg, (double)sm.gmean[tid], (double)s);
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void write_partial(double* partials, int groups, const GroupAcc& acc) {
+  const int tid = threadIdx.x;
+  if (tid < groups) {
+    double* p = partials + ((long)blockIdx.x * groups + tid) * 3;
+    p[0] = acc.w;
+    p[1] = acc.mean;
+    p[2] = acc.m2;
+  }
+}
+
+}  // namespace ffno
+
+#define FFNO_CHECK_LAUNCH()                                   \
+  do {                                                        \
+    cudaError_t e_ = cudaGetLastError();                      \
+    if (e_ != cudaSuccess) return FFNO_ELAUNCH;               \
+  } while (0)

@@ -1,0 +1,149 @@
+/* ffnoml_gb300 — C ABI of the GB300 (sm_103a) FFNO3D forward and input-VJP kernels.
+ *
+ * The reference (harshmathur1990/FFNOML) exposes this path only as the PyTorch module FFNO3D
+ * (models/ffno_model.py:614-832) behind ffno_model_factory.create_ffno3d (ffno_model_factory.py:6-19) and the
+ * protocol-v2 service (ffno_fsdp_service.py). Each entry point below replaces one stage of FFNO3D.forward / its
+ * autograd backward; the comment on each names the reference code it stands for. The Python host code in
+ * ffnoml_gb300/ (module, executor, service) calls these through ctypes.
+ *
+ * Conventions
+ *  - Every pointer is a device pointer unless noted; every call is asynchronous on `stream` (a cudaStream_t, NULL =
+ *    legacy default stream) and allocates nothing: all workspace is passed in by the caller.
+ *  - Activations are channels-last: one contiguous row of C floats per voxel, voxel v = (d*H + h)*W + w of one cube,
+ *    V = D*H*W voxels. The model input x_in and the output are channels-first [channels][V], as FFNO3D's [B,C,D,H,W].
+ *  - Weight matrices are row-major [K][N] (input channel k, output channel n): the transpose of a Conv3d weight
+ *    [N][K][1][1][1].
+ *  - GroupNorm coefficients `coefs` are [3][C] floats: per channel the group mean, gamma*rstd and beta; the
+ *    normalised value is (x - coefs[0][c]) * coefs[1][c] + coefs[2][c].
+ *  - GroupNorm partial statistics `partials` are [nparts][groups][3] doubles (total weight, mean, M2), one row per
+ *    CTA of the producing kernel, which is launched with exactly nparts CTAs.
+ *  - Return value: FFNO_OK (0) or an error code; no call traps, aborts or throws.
+ *  - Supported widths C: 16, 32, 64, 96.
+ */
+#ifndef FFNOML_GB300_H
+#define FFNOML_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFNO_OK 0
+#define FFNO_EINVAL 1      /* unsupported size, null pointer, inconsistent arguments */
+#define FFNO_ELAUNCH 2     /* a kernel launch failed (cudaGetLastError) */
+#define FFNO_ENOMEM 3      /* the caller's workspace is too small */
+#define FFNO_ETIMEOUT 4    /* a bounded device wait ran out */
+
+typedef void* ffno_stream_t; /* cudaStream_t */
+
+/* Level-fraction head constants (FFNO3D.head_output, models/ffno_model.py:730-749; MULTI3D tables :116-141). */
+#define FFNO_MAX_LEVELS 32
+#define FFNO_MAX_SPECIES 4
+typedef struct {
+  int nspecies;
+  int levels[FFNO_MAX_SPECIES];
+  int rho_channel, temperature_channel, ne_channel;
+  int in_channels;
+  float total_bound;
+  float log10_particle_mass[FFNO_MAX_SPECIES];
+  float mean_x[8], std_x[8];
+  float mean_y[FFNO_MAX_LEVELS], std_y[FFNO_MAX_LEVELS];
+  double log_g[FFNO_MAX_LEVELS], ev[FFNO_MAX_LEVELS], ndxi[FFNO_MAX_LEVELS], dion[FFNO_MAX_LEVELS];
+} ffno_head_params;
+
+/* library version string */
+const char* ffno_version(void);
+
+/* Number of CTAs the statistics-producing kernels use for V voxels (= nparts of their partials). */
+int ffno_stats_parts(long V);
+
+/* depth_weights (models/ffno_model.py:28-34, 67-74): z [D][HW] heights (any units) -> w [D][HW] trapezoid |dz| over
+ * the column mean. */
+int ffno_depth_weights(const float* z, int D, long HW, float* w, ffno_stream_t stream);
+
+/* Column analysis for HeightSpectralConv.box/shared-grid check (models/ffno_model.py:248-259, 266-269): out[0] = 1.0f
+ * if every column shifted by its own minimum equals column 0 shifted by its minimum (exact float equality), else 0;
+ * out[1] = the largest column span max - min. out is 2 floats of device memory. */
+int ffno_column_info(const float* z, int D, long HW, float* out, ffno_stream_t stream);
+
+/* lift: pre = x_in (channels-first [cin][V]) @ w_lift [cin][C] (FFNO3D.lift[0], models/ffno_model.py:688-692),
+ * with the depth-weighted GroupNorm partials of pre (lift[1]). */
+int ffno_lift_fwd(const float* x_in, int cin, long V, int C, const float* w_lift, const float* dw, float* pre,
+                  double* partials, int nparts, int groups, ffno_stream_t stream);
+
+/* DepthWeightedGroupNorm statistics (models/ffno_model.py:77-95): partials -> coefs [3][C] and gstats [groups][2]
+ * (mean, rstd as doubles). */
+int ffno_gn_finalize(const double* partials, int nparts, int C, int groups, const float* gamma, const float* beta,
+                     float eps, float* coefs, double* gstats, ffno_stream_t stream);
+
+/* out = act(GroupNorm(pre)), act 0 = identity, 1 = GELU (lift[1:3], models/ffno_model.py:782-783). */
+int ffno_gn_act(const float* pre, const float* coefs, long V, int C, int act, float* out, ffno_stream_t stream);
+
+/* Input gate of both branches (SpectralConv2dFull.input_gate :336-341, HeightSpectralConv.input_gate :205-210 and
+ * z_proj :211, :265): out = x * sigmoid(gelu(x @ w1) @ w2) [+ zp[c] * z[v]] (zp, z may be NULL). */
+int ffno_gate_fwd(const float* x, long V, int C, const float* w1, const float* w2, const float* zp, const float* z,
+                  float* out, ffno_stream_t stream);
+
+/* Pointwise 2-layer MLP C -> 2C -> C (post :367-373, :221-225; pw :489-493; mlp :495) with a residual prologue and
+ * the GroupNorm partials of its output:
+ *   mode 0: a = in
+ *   mode 1: a = in + res * gelu(GN(prev_pre))    (x1 = x + res_fused * fused, :545)
+ *   mode 2: a = in + res * GN(prev_pre)          (x2 = x1 + res_pw * pw, :548)
+ * modes 1 and 2 also write a to xout. pre = gelu(a @ w1) @ w2. */
+int ffno_mlp2_fwd(int mode, const float* in, const float* prev_pre, const float* prev_coefs, float res, float* xout,
+                  long V, int C, const float* w1, const float* w2, const float* dw, float* pre, double* partials,
+                  int nparts, int groups, ffno_stream_t stream);
+
+/* Branch gate + fuse (FFNOBlock3dBalanced._fuse_branches, models/ffno_model.py:524-534) on
+ * spec = gelu(GN_spec(spec_pre)), vert = gelu(GN_vert(vert_pre)):
+ *   gates = sigmoid(gelu([x, spec, vert] @ wg1) @ wg2 + bg2); smix = spec*gates[:C]; vmix = vert*gates[C:]
+ *   pre = gelu([smix, vmix] @ wf1) @ wf2 + 0.5 (smix + vmix), with the GroupNorm partials of pre. */
+int ffno_fuse_fwd(const float* x, const float* spec_pre, const float* spec_coefs, const float* vert_pre,
+                  const float* vert_coefs, long V, int C, const float* wg1, const float* wg2, const float* bg2,
+                  const float* wf1, const float* wf2, const float* dw, float* pre, double* partials, int nparts,
+                  int groups, ffno_stream_t stream);
+
+/* Block output out = x2 + res * GN(pre) (models/ffno_model.py:550-551). */
+int ffno_resid_out(const float* x2, const float* pre, const float* coefs, float res, long V, int C, float* out,
+                   ffno_stream_t stream);
+
+/* Projection + level-fraction head (FFNO3D._run_head + head_output, models/ffno_model.py:790-798, 730-749):
+ * h = gelu(x @ p1) @ p2 + b2 (p2, b2 padded to nhp = 16 or 32 columns), then per voxel the MULTI3D LTE weights of
+ * T, ne from x_in, per-species log-softmax and total correction -> out channels-first [levels][V], normalised
+ * log10 n. If head_out is not NULL the raw head channels are also written there channels-first [nh][V]. */
+int ffno_head_fwd(const float* x, const float* x_in, long V, int C, const float* p1, const float* p2, const float* b2,
+                  int nh, int nhp, const ffno_head_params* params, float* out, float* head_out, ffno_stream_t stream);
+
+/* Batched transform GEMM: out[b][m][n] = sum_k T[m][k] * in[b][k][n], the DFT-as-contraction of both spectral
+ * operators (rfft2/irfft2 of SpectralConv2dFull.forward :441-448; the Filon height transform and its inverse of
+ * HeightSpectralConv.forward :270-275, :303-305). Batch b = b1 * nb2 + b2; a row index r of in (k) or out (m) is
+ * addressed as (r / split) * s_hi + (r % split) * s_lo. n is contiguous. */
+typedef struct {
+  long nb, nb2;
+  long in_b1, in_b2, out_b1, out_b2;
+  int K, M;
+  long N;
+  int in_split;
+  long in_hi, in_lo;
+  int out_split;
+  long out_hi, out_lo;
+} ffno_xform_desc;
+int ffno_xform(const float* T, const float* in, float* out, const ffno_xform_desc* desc, int accumulate,
+               ffno_stream_t stream);
+
+/* Per-frequency complex channel mixing (SpectralConv2dFull.mix_spectrum :394-429; HeightSpectralConv mode mixing
+ * :282-300): for each frequency f < F and row b < nb, with xhat = re + i im at offset f*sf + b*sb (im at +s_im):
+ *   out = g_f * (xhat @ (w_re + i w_im)) + U_f (V_f xhat)
+ * wbig [2C][2C] = [[w_re, w_im], [-w_im, w_re]], g [F][2], U [F][C][rank], Vm [F][rank][C]. in and out must not
+ * overlap. */
+int ffno_spectral_mix(const float* in, float* out, long F, long nb, long sf, long sb, long s_im, int C,
+                      const float* wbig, const float* g, const float* U, const float* Vm, int rank,
+                      ffno_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FFNOML_GB300_H */
