@@ -64,6 +64,17 @@ PROTOTYPES = {
     "ffno_head_fwd": [P, P, L, I, P, P, P, I, I, ctypes.POINTER(HeadParams), P, P, P],
     "ffno_xform": [P, P, P, ctypes.POINTER(XformDesc), I, P],
     "ffno_spectral_mix": [P, P, L, L, L, L, L, I, P, P, P, P, I, P],
+    "ffno_gn_bwd_stats": [I, P, F, P, P, P, P, L, I, I, P, I, P],
+    "ffno_gn_bwd_final": [P, I, I, P, P],
+    "ffno_gn_bwd_apply": [I, P, F, P, P, P, P, P, P, L, I, I, F, P, P, P],
+    "ffno_mlp2_bwd": [P, P, P, L, I, P, P, P, P, P],
+    "ffno_fuse_bwd": [P, P, P, P, P, P, P, L, I, P, P, P, P, P, P, P, P, P, P, P, P],
+    "ffno_gate_bwd": [P, P, P, P, L, I, P, P, P, P, P, P, P, P, P, P, P, P],
+    "ffno_lift_bwd": [P, I, L, I, P, P, P],
+    "ffno_head_bwd": [P, P, P, L, I, P, P, P, P, P, I, ctypes.POINTER(HeadParams), P, P, P],
+    "ffno_depth_weights_bwd": [P, P, I, L, P, P],
+    "ffno_outer_parts": [I, I, L],
+    "ffno_outer": [P, L, I, P, L, I, L, P, I, P, I, P],
 }
 
 _lib = None

@@ -27,36 +27,38 @@ __device__ __forceinline__ float gelu_grad(float x) {
 
 __device__ __forceinline__ float sigmoid(float x) { return 1.f / (1.f + expf(-x)); }
 
-// acc[i][j] = sum_k A[(ty + 16 i) * lda + k] * W[k * N + tx + 16 j]; A in shared memory, W (row-major K x N) in
-// global memory (read through L1; every CTA reads the same small weight matrix).
-template <int K, int N>
+// acc[i][j] = sum_k A[(ty + 16 i) * lda + k] * W[k * N + tx + 16 j] for i < RM rows per thread (a tile of 16 RM
+// rows); A in shared memory, W (row-major K x N) in global memory (read through L1; every CTA reads the same small
+// weight matrix).
+template <int K, int N, int RM = 4>
 __device__ __forceinline__ void tile_mm(const float* __restrict__ A, int lda, const float* __restrict__ W,
-                                        float (&acc)[4][N / 16]) {
+                                        float (&acc)[RM][N / 16]) {
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < RM; ++i)
 #pragma unroll
     for (int j = 0; j < N / 16; ++j) acc[i][j] = 0.f;
 #pragma unroll 4
   for (int k = 0; k < K; ++k) {
-    float a[4], b[N / 16];
+    float a[RM], b[N / 16];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) a[i] = A[(ty + 16 * i) * lda + k];
+    for (int i = 0; i < RM; ++i) a[i] = A[(ty + 16 * i) * lda + k];
 #pragma unroll
     for (int j = 0; j < N / 16; ++j) b[j] = __ldg(W + k * N + tx + 16 * j);
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < RM; ++i)
 #pragma unroll
       for (int j = 0; j < N / 16; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
   }
 }
 
-// Copy rows v0 .. v0 + BM - 1 (C floats each, row-major, contiguous) into shared memory with row stride lds; rows at or
-// beyond V are zero.
+// Copy rows v0 .. v0 + rows - 1 (C floats each, row-major, contiguous) into shared memory with row stride lds; rows at
+// or beyond V are zero.
 template <int C>
-__device__ __forceinline__ void load_rows(float* __restrict__ s, int lds, const float* __restrict__ g, long v0, long V) {
+__device__ __forceinline__ void load_rows(float* __restrict__ s, int lds, const float* __restrict__ g, long v0, long V,
+                                          int rows = BM) {
   constexpr int Q = C / 4;  // float4 per row
-  for (int e = threadIdx.x; e < BM * Q; e += NT) {
+  for (int e = threadIdx.x; e < rows * Q; e += NT) {
     const int r = e / Q, q = e % Q;
     float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
     if (v0 + r < V) val = __ldg(reinterpret_cast<const float4*>(g + (v0 + r) * C) + q);
@@ -92,15 +94,15 @@ struct StatsSmem {
 // Accumulate the depth-weighted statistics of one tile's values val (rows ty + 16 i, columns tx + 16 j) into acc[g]
 // (held by thread g < groups). wr[i] is the weight of row i, zero for rows past the cube. Column c belongs to group
 // c / cpg. Deterministic: fixed summation order.
-template <int N>
-__device__ __forceinline__ void tile_group_stats(const float (&val)[4][N / 16], const float (&wr)[4], int cpg,
+template <int N, int RM = 4>
+__device__ __forceinline__ void tile_group_stats(const float (&val)[RM][N / 16], const float (&wr)[RM], int cpg,
                                                  int groups, StatsSmem<N>& sm, GroupAcc& acc) {
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   // tile weight: sum of the row weights (each row counted once: the threads with tx == 0 hold rows ty + 16 i)
   if (tx == 0) {
     float s = 0.f;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) s += wr[i];
+    for (int i = 0; i < RM; ++i) s += wr[i];
     sm.part[ty] = s;
   }
   __syncthreads();
@@ -115,7 +117,7 @@ __device__ __forceinline__ void tile_group_stats(const float (&val)[4][N / 16], 
   for (int j = 0; j < N / 16; ++j) {
     float s = 0.f;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) s = fmaf(wr[i], val[i][j], s);
+    for (int i = 0; i < RM; ++i) s = fmaf(wr[i], val[i][j], s);
     sm.part[ty * N + tx + 16 * j] = s;
   }
   __syncthreads();
@@ -138,7 +140,7 @@ __device__ __forceinline__ void tile_group_stats(const float (&val)[4][N / 16], 
     const float m = sm.gmean[(tx + 16 * j) / cpg];
     float s = 0.f;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < RM; ++i) {
       const float d = val[i][j] - m;
       s = fmaf(wr[i] * d, d, s);
     }
@@ -155,6 +157,53 @@ __device__ __forceinline__ void tile_group_stats(const float (&val)[4][N / 16], 
     float s = 0.f;
     for (int c = tid * cpg; c < (tid + 1) * cpg; ++c) s += sm.col[c];
     chan_merge(acc, (double)sm.wsum * cpg, (double)sm.gmean[tid], (double)s);
+  }
+  __syncthreads();
+}
+
+// Per-group sums of two per-element quantities a, b of one tile (rows ty + 16 i, columns tx + 16 j), added in a fixed
+// order into the double accumulators s1, s2 held by thread g < groups. Used by the GroupNorm backward.
+template <int N, int RM = 4>
+__device__ __forceinline__ void tile_group_sums(const float (&a)[RM][N / 16], const float (&b)[RM][N / 16], int cpg,
+                                                int groups, float* part /* [16][N] */, float* col /* [2][N] */,
+                                                double& s1, double& s2) {
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+#pragma unroll
+  for (int j = 0; j < N / 16; ++j) {
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < RM; ++i) s += a[i][j];
+    part[ty * N + tx + 16 * j] = s;
+  }
+  __syncthreads();
+  for (int c = tid; c < N; c += NT) {
+    float s = 0.f;
+    for (int t = 0; t < 16; ++t) s += part[t * N + c];
+    col[c] = s;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < N / 16; ++j) {
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < RM; ++i) s += b[i][j];
+    part[ty * N + tx + 16 * j] = s;
+  }
+  __syncthreads();
+  for (int c = tid; c < N; c += NT) {
+    float s = 0.f;
+    for (int t = 0; t < 16; ++t) s += part[t * N + c];
+    col[N + c] = s;
+  }
+  __syncthreads();
+  if (tid < groups) {
+    float x = 0.f, y = 0.f;
+    for (int c = tid * cpg; c < (tid + 1) * cpg; ++c) {
+      x += col[c];
+      y += col[N + c];
+    }
+    s1 += (double)x;
+    s2 += (double)y;
   }
   __syncthreads();
 }

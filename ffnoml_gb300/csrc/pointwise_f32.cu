@@ -149,8 +149,9 @@ __global__ void k_gn_finalize(const double* __restrict__ partials, int nparts, i
     gm[tid] = a.mean;
     gr[tid] = rstd;
     if (gstats) {
-      gstats[2 * tid] = a.mean;
-      gstats[2 * tid + 1] = rstd;
+      gstats[3 * tid] = a.mean;
+      gstats[3 * tid + 1] = rstd;
+      gstats[3 * tid + 2] = a.w;
     }
   }
   __syncthreads();

@@ -1,17 +1,21 @@
-"""Executor of the FFNO3D forward pass (and, in executor_bwd, its input VJP) on one GPU.
+"""Executor of the FFNO3D forward pass and its input VJP on one GPU.
 
 It packs the module's weights into device buffers in the kernels' layouts (once per weight version), keeps the
 shape-constant tables resident (DFT matrices per (H, W); frequency-MLP tables per (H, W, dx, dy); height tables per
 height grid), and issues the C-ABI kernels of libffnoml_gb300 on the current CUDA stream.
 
-Per cube (batch element), the block is (FFNOBlock3dBalanced.forward, models/ffno_model.py:536-553):
+Per cube (batch element), a block is (FFNOBlock3dBalanced.forward, models/ffno_model.py:536-553):
   xs = gate_s(x); xv = gate_v(x) + z_proj z
-  spec_pre = post_s(irfft2(mix_s(rfft2(xs))))                       -> GroupNorm statistics
-  vert_pre = post_v(iDFT_z(mix_v(DFT_z(xv))))                       -> GroupNorm statistics
-  fused_pre = fuse(gate([x, gelu(GN spec_pre), gelu(GN vert_pre)]))   -> statistics
-  x1 = x + r_f gelu(GN fused_pre); pw_pre = pw(x1)                    -> statistics
-  x2 = x1 + r_pw GN(pw_pre);      mlp_pre = mlp(x2)                   -> statistics
+  spec_pre = post_s(irfft2(mix_s(rfft2(xs))))                        -> GroupNorm statistics
+  vert_pre = post_v(iDFT_z(mix_v(DFT_z(xv))))                        -> GroupNorm statistics
+  fused_pre = fuse(gate([x, gelu(GN spec_pre), gelu(GN vert_pre)]))  -> statistics
+  x1 = x + r_f gelu(GN fused_pre); pw_pre = pw(x1)                   -> statistics
+  x2 = x1 + r_pw GN(pw_pre);      mlp_pre = mlp(x2)                  -> statistics
   out = x2 + r_mlp GN(mlp_pre)
+
+The input VJP keeps only the block inputs from the forward pass and recomputes each block's intermediates before
+back-propagating through it (the reference's per-block activation checkpointing, models/ffno_model.py:751-780).
+Parameter gradients are not computed: the service's VJP discards them (ffno_fsdp_runtime.py:319-344).
 """
 import math
 
@@ -23,6 +27,7 @@ from . import tables as tb
 
 EPS = 1e-5  # nn.GroupNorm default, DepthWeightedGroupNorm's eps (models/ffno_model.py:77-95)
 SUPPORTED_WIDTHS = (16, 32, 64, 96)
+NORMS = ("spec", "vert", "fuse", "pw", "mlp")
 
 
 def _ptr(t):
@@ -45,7 +50,7 @@ def _wbig(wr, wi):
 
 
 class Packed:
-    """Device copies of one model's weights in kernel layouts."""
+    """Device copies of one model's weights in kernel layouts (and their transposes for the VJP)."""
 
     def __init__(self, model, device):
         self.device = device
@@ -57,21 +62,22 @@ class Packed:
         self.blocks = []
         for b in model.blocks:
             s, v = b.spec, b.vertical
-            pk = dict(
-                s_g1=dev(_conv_t(s.input_gate[0])), s_g2=dev(_conv_t(s.input_gate[2])),
-                s_wbig=dev(_wbig(s.weight_real, s.weight_imag)),
-                s_p1=dev(_conv_t(s.post[0])), s_p2=dev(_conv_t(s.post[2])),
-                v_g1=dev(_conv_t(v.input_gate[0])), v_g2=dev(_conv_t(v.input_gate[2])),
-                v_zp=dev(v.z_proj.weight.detach().reshape(C)),
-                v_wbig=dev(_wbig(v.weight_real, v.weight_imag)),
-                v_p1=dev(_conv_t(v.post[0])), v_p2=dev(_conv_t(v.post[2])),
-                bg1=dev(_conv_t(b.branch_gate[0])), bg2=dev(_conv_t(b.branch_gate[2])),
-                bgb=dev(b.branch_gate[2].bias.detach()),
-                f1=dev(_conv_t(b.fuse[0])), f2=dev(_conv_t(b.fuse[2])),
-                pw1=dev(_conv_t(b.pw[0])), pw2=dev(_conv_t(b.pw[2])),
-                m1=dev(_conv_t(b.mlp.net[0])), m2=dev(_conv_t(b.mlp.net[3])),
+            mats = dict(
+                s_g1=_conv_t(s.input_gate[0]), s_g2=_conv_t(s.input_gate[2]),
+                s_p1=_conv_t(s.post[0]), s_p2=_conv_t(s.post[2]),
+                v_g1=_conv_t(v.input_gate[0]), v_g2=_conv_t(v.input_gate[2]),
+                v_p1=_conv_t(v.post[0]), v_p2=_conv_t(v.post[2]),
+                bg1=_conv_t(b.branch_gate[0]), bg2=_conv_t(b.branch_gate[2]),
+                f1=_conv_t(b.fuse[0]), f2=_conv_t(b.fuse[2]),
+                pw1=_conv_t(b.pw[0]), pw2=_conv_t(b.pw[2]),
+                m1=_conv_t(b.mlp.net[0]), m2=_conv_t(b.mlp.net[3]),
+                s_wbig=_wbig(s.weight_real, s.weight_imag), v_wbig=_wbig(v.weight_real, v.weight_imag),
             )
-            for n in ("spec", "vert", "fuse", "pw", "mlp"):
+            pk = {k: dev(m) for k, m in mats.items()}
+            pk.update({k + "t": dev(m.t()) for k, m in mats.items()})               # transposes for the VJP
+            pk["v_zp"] = dev(v.z_proj.weight.detach().reshape(C))
+            pk["bgb"] = dev(b.branch_gate[2].bias.detach())
+            for n in NORMS:
                 norm = getattr(b, "norm_" + n)
                 pk[n + "_g"] = dev(norm.weight.detach())
                 pk[n + "_b"] = dev(norm.bias.detach())
@@ -83,16 +89,16 @@ class Packed:
         if nh > 32:
             raise ValueError("at most 32 head channels are supported")
         self.p1 = dev(_conv_t(model.proj1))
+        self.p1t = dev(_conv_t(model.proj1).t())
         p2 = torch.zeros(2 * C, self.nhp)
         p2[:, :nh] = _conv_t(model.proj2)
         self.p2 = dev(p2)
+        self.p2t = dev(p2.t())
         b2 = torch.zeros(self.nhp)
         b2[:nh] = model.proj2.bias.detach().float()
         self.b2 = dev(b2)
         self.head = self._head_params(model)
-        # host copies of the parameters the frequency MLPs need (tables are built in float64 on the host)
-        self.freq_params = {k: v.detach().cpu() for k, v in model.state_dict().items()
-                            if ".freq_" in k}
+        self.freq_params = {k: v.detach().cpu() for k, v in model.state_dict().items() if ".freq_" in k}
 
     @staticmethod
     def _head_params(model):
@@ -128,6 +134,46 @@ def _weights_key(model):
     return tuple(items)
 
 
+class FreqTables:
+    """g, U, V of one operator of one block on the device, with the adjoint forms (conj g, V^T as U, U^T as V)."""
+
+    def __init__(self, g, u, v, device):
+        f = lambda a: None if a is None else a.to(device=device, dtype=torch.float32).contiguous()
+        self.g, self.u, self.v = f(g), f(u), f(v)
+        self.g_adj = f(torch.stack([g[:, 0], -g[:, 1]], 1))
+        self.u_adj = None if v is None else f(v.transpose(1, 2))     # [F][C][r] = V^T
+        self.v_adj = None if u is None else f(u.transpose(1, 2))     # [F][r][C] = U^T
+
+
+class Geometry:
+    def __init__(self, shared, span, column, column_raw, length, k):
+        self.shared, self.span, self.column, self.column_raw, self.length, self.k = (shared, span, column, column_raw,
+                                                                                     length, k)
+
+
+class Workspace:
+    """Device buffers for one cube of shape (D, H, W) at width C."""
+
+    def __init__(self, D, H, W, C, live, groups, device):
+        V = D * H * W
+        HW = H * W
+        Wf = W // 2 + 1
+        f32 = dict(dtype=torch.float32, device=device)
+        self.V = V
+        self.nparts = nat.lib().ffno_stats_parts(V)
+        nb = lambda *s: torch.empty(*s, **f32)
+        self.dw = nb(V)
+        self.partials = torch.empty(max(self.nparts, 1) * groups * 3, dtype=torch.float64, device=device)
+        self.coefs = {n: nb(3 * C) for n in ("lift",) + NORMS}
+        self.gstats = {n: torch.empty(groups * 3, dtype=torch.float64, device=device) for n in ("lift",) + NORMS}
+        for n in ("x", "pre", "xs", "xv", "ys", "yv", "spec_pre", "vert_pre", "fused_pre", "pw_pre", "mlp_pre",
+                  "x1", "x2"):
+            setattr(self, n, nb(V, C))
+        spec_len = D * 2 * H * Wf * C
+        self.sa, self.sb = nb(spec_len), nb(spec_len)
+        self.va, self.vb = nb(2 * live * HW * C), nb(2 * live * HW * C)
+
+
 class Executor:
     def __init__(self, model):
         self.model = model
@@ -151,8 +197,10 @@ class Executor:
         key = (H, W, str(device))
         if key not in self._plane:
             twf, thf, thi, twi = tb.plane_dft(H, W)
-            f = lambda a: torch.as_tensor(a, dtype=torch.float32, device=device).contiguous()
-            self._plane[key] = (f(twf), f(thf), f(thi), f(twi))
+            f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device=device)
+            # forward tables and the transposes the VJP applies (rows/cols swapped)
+            self._plane[key] = dict(twf=f(twf), thf=f(thf), thi=f(thi), twi=f(twi), twf_t=f(twf.T), thf_t=f(thf.T),
+                                    thi_t=f(thi.T), twi_t=f(twi.T))
         return self._plane[key]
 
     def plane_freq(self, pk, H, W, dx, dy, device):
@@ -160,206 +208,349 @@ class Executor:
         if key not in self._plane_freq:
             feats = tb.plane_features(H, W, dx, dy)
             rank = self.model.freq_mix_rank
-            per_block = []
-            for i in range(self.model.n_layers):
-                g, u, v = tb.freq_tables(pk.freq_params, f"blocks.{i}.spec", feats, rank)
-                per_block.append(self._upload_freq(g, u, v, device))
-            self._plane_freq[key] = per_block
+            self._plane_freq[key] = [FreqTables(*tb.freq_tables(pk.freq_params, f"blocks.{i}.spec", feats, rank), device)
+                                     for i in range(self.model.n_layers)]
         return self._plane_freq[key]
 
-    def height(self, pk, column, length, k, device):
-        key = (column.tobytes(), float(length), k.numel())
+    def height(self, pk, geo, device):
+        key = (geo.column.tobytes(), float(geo.length), geo.k.numel())
         if key not in self._height:
-            live, tzf, tzi = tb.height_tables(column, length, k)
-            feats = tb.height_features(k[:live], self.model.z_feature_wavelength)
+            live, tzf, tzi = tb.height_tables(geo.column, geo.length, geo.k)
+            feats = tb.height_features(geo.k[:live], self.model.z_feature_wavelength)
             rank = self.model.freq_mix_rank
-            per_block = []
-            for i in range(self.model.n_layers):
-                g, u, v = tb.freq_tables(pk.freq_params, f"blocks.{i}.vertical", feats, rank)
-                per_block.append(self._upload_freq(g, u, v, device))
-            f = lambda a: torch.as_tensor(a, dtype=torch.float32, device=device).contiguous()
-            self._height[key] = (live, f(tzf), f(tzi), per_block)
+            per_block = [FreqTables(*tb.freq_tables(pk.freq_params, f"blocks.{i}.vertical", feats, rank), device)
+                         for i in range(self.model.n_layers)]
+            f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device=device)
+            self._height[key] = dict(live=live, tzf=f(tzf), tzi=f(tzi), tzf_t=f(tzf.T), tzi_t=f(tzi.T),
+                                     freq=per_block)
         return self._height[key]
-
-    @staticmethod
-    def _upload_freq(g, u, v, device):
-        f = lambda a: None if a is None else a.to(device=device, dtype=torch.float32).contiguous()
-        return f(g), f(u), f(v)
 
     # -------------------------------------------------------------------------------------------- geometry
     def geometry(self, z_scale):
-        """Per-batch height analysis: (shared, span, column of sample 0 shifted to 0 as float64 numpy)."""
+        """Per-batch height analysis (HeightSpectralConv.box and shared-grid test, models/ffno_model.py:248-269)."""
         B, D = z_scale.shape[0], z_scale.shape[1]
         HW = z_scale.shape[2] * z_scale.shape[3]
         info = torch.empty(B, 2, dtype=torch.float32, device=z_scale.device)
         s = _stream()
         for b in range(B):
             nat.call("ffno_column_info", z_scale[b].data_ptr(), D, HW, info[b].data_ptr(), s)
-        col = z_scale[:, :, 0, 0]                                   # [B, D]
+        col = z_scale[:, :, 0, 0]
         host = torch.cat([info.reshape(-1), col.reshape(-1)]).cpu()
         info_h = host[:2 * B].reshape(B, 2)
         cols = host[2 * B:].reshape(B, D).double().numpy()
         shared_each = bool((info_h[:, 0] > 0.5).all())
-        span = float(info_h[:, 1].view(torch.float32).max()) if B else 0.0
+        span = float(info_h[:, 1].max())
         shifted = cols - cols.min(axis=1, keepdims=True)
         shared = shared_each and bool((shifted == shifted[:1]).all())
-        return shared, span, shifted[0]
-
-    def box(self, span):
         m = self.model
         modes = int(math.floor(m.z_reference_length / m.z_min_wavelength)) + 1
-        return tb.height_box(span, m.z_reference_length, m.z_min_wavelength, modes)
+        length, k = tb.height_box(span, m.z_reference_length, m.z_min_wavelength, modes)
+        return Geometry(shared, span, shifted[0], cols[0], length, k)
 
-    # -------------------------------------------------------------------------------------------- forward
-    def forward(self, x, z_scale, dx, dy):
-        """x [B, Cin, D, H, W], z_scale [B, D, H, W] (Mm), float32 CUDA -> [B, L, D, H, W] float32."""
+    # -------------------------------------------------------------------------------------------- setup
+    def _setup(self, x, z_scale, dx, dy):
         m = self.model
-        if not x.is_cuda:
+        if not x.is_cuda or not z_scale.is_cuda:
             raise RuntimeError("ffnoml_gb300 runs on CUDA tensors only")
         if x.dtype != torch.float32 or z_scale.dtype != torch.float32:
             raise TypeError("ffnoml_gb300 FFNO3D takes float32 inputs")
         if m.width not in SUPPORTED_WIDTHS:
             raise ValueError(f"width {m.width} is not supported (supported: {SUPPORTED_WIDTHS})")
-        B, Cin, D, H, W = x.shape
-        if Cin != m.in_channels:
-            raise ValueError(f"expected {m.in_channels} input channels, got {Cin}")
+        if x.dim() != 5 or z_scale.dim() != 4 or z_scale.shape != (x.shape[0],) + tuple(x.shape[2:]):
+            raise ValueError(f"x must be [B, Cin, D, H, W] and z_scale [B, D, H, W]; got {tuple(x.shape)}, "
+                             f"{tuple(z_scale.shape)}")
+        if x.shape[1] != m.in_channels:
+            raise ValueError(f"expected {m.in_channels} input channels, got {x.shape[1]}")
+        if x.shape[2] < 2:
+            raise ValueError("the height operator needs at least two levels")
         device = x.device
         pk = self.packed(device)
-        x = x.contiguous()
-        z_scale = z_scale.contiguous()
-        shared, span, column = self.geometry(z_scale)
-        if not shared:
+        geo = self.geometry(z_scale)
+        if not geo.shared:
             raise NotImplementedError("per-column height grids are not supported by the GB300 path yet")
-        length, k = self.box(span)
-        hgt = self.height(pk, column, length, k, device)
+        hgt = self.height(pk, geo, device)
+        B, _, D, H, W = x.shape
         pln = self.plane(H, W, device)
         pfr = self.plane_freq(pk, H, W, dx, dy, device)
-        out = torch.empty(B, m.out_channels, D, H, W, dtype=torch.float32, device=device)
-        for b in range(B):
-            self._forward_cube(pk, x[b], z_scale[b], out[b], D, H, W, hgt, pln, pfr)
-        return out
+        return pk, geo, hgt, pln, pfr
 
-    def _forward_cube(self, pk, xin, z, out, D, H, W, hgt, pln, pfr):
+    # -------------------------------------------------------------------------------------------- forward
+    def forward(self, x, z_scale, dx, dy, keep=False):
+        """x [B, Cin, D, H, W], z_scale [B, D, H, W] (Mm), float32 CUDA -> [B, L, D, H, W] float32. With keep=True
+        also returns the state the VJP needs (block inputs per cube)."""
         m = self.model
-        C = m.width
-        V = D * H * W
-        HW = H * W
-        Wf = W // 2 + 1
-        dev = xin.device
+        x = x.contiguous()
+        z_scale = z_scale.contiguous()
+        pk, geo, hgt, pln, pfr = self._setup(x, z_scale, dx, dy)
+        B, _, D, H, W = x.shape
+        out = torch.empty(B, m.out_channels, D, H, W, dtype=torch.float32, device=x.device)
+        ws = Workspace(D, H, W, m.width, hgt["live"], pk.groups, x.device)
+        saved = []
+        for b in range(B):
+            xin, z = x[b], z_scale[b]
+            self._depth_weights(ws, z, D, H * W)
+            self._lift(pk, ws, xin)
+            inputs = [ws.x.clone()] if keep else None
+            for i in range(m.n_layers):
+                self._block(pk, ws, i, z, D, H, W, hgt, pln, pfr[i])
+                if keep:
+                    inputs.append(ws.x.clone())
+            self._head(pk, ws.x, xin, out[b])
+            if keep:
+                saved.append(inputs)
+        state = dict(x=x, z=z_scale, dx=dx, dy=dy, inputs=saved, geo=geo) if keep else None
+        return out, state
+
+    def _depth_weights(self, ws, z, D, HW):
+        nat.call("ffno_depth_weights", z.data_ptr(), D, HW, ws.dw.data_ptr(), _stream())
+
+    def _finalize(self, ws, name, gamma, beta):
+        m = self.model
+        nat.call("ffno_gn_finalize", ws.partials.data_ptr(), ws.nparts, m.width, self._packed.groups,
+                 gamma.data_ptr(), beta.data_ptr(), EPS, ws.coefs[name].data_ptr(), ws.gstats[name].data_ptr(),
+                 _stream())
+
+    def _lift(self, pk, ws, xin):
+        m = self.model
+        V, C, s = ws.V, m.width, _stream()
+        nat.call("ffno_lift_fwd", xin.data_ptr(), m.in_channels, V, C, pk.lift_w.data_ptr(), ws.dw.data_ptr(),
+                 ws.pre.data_ptr(), ws.partials.data_ptr(), ws.nparts, pk.groups, s)
+        self._finalize(ws, "lift", pk.lift_g, pk.lift_b)
+        nat.call("ffno_gn_act", ws.pre.data_ptr(), ws.coefs["lift"].data_ptr(), V, C, 1, ws.x.data_ptr(), s)
+
+    def _block(self, pk, ws, i, z, D, H, W, hgt, pln, fq, x_in=None):
+        """Block i on ws.x (or x_in), leaving every intermediate in ws and the block output in ws.x."""
+        m = self.model
+        C, V, HW, Wf = m.width, ws.V, H * W, W // 2 + 1
         s = _stream()
+        bp = pk.blocks[i]
+        G, P = pk.groups, ws.nparts
+        x = ws.x if x_in is None else x_in
+        live = hgt["live"]
+        d = _descs(D, H, W, C, live)
+        nat.call("ffno_gate_fwd", x.data_ptr(), V, C, bp["s_g1"].data_ptr(), bp["s_g2"].data_ptr(), None, None,
+                 ws.xs.data_ptr(), s)
+        nat.call("ffno_gate_fwd", x.data_ptr(), V, C, bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(),
+                 bp["v_zp"].data_ptr(), z.data_ptr(), ws.xv.data_ptr(), s)
+        # horizontal spectral branch: rfft2 -> mix -> irfft2 as contractions
+        nat.call("ffno_xform", pln["twf"].data_ptr(), ws.xs.data_ptr(), ws.sa.data_ptr(), d["wf"], 0, s)
+        nat.call("ffno_xform", pln["thf"].data_ptr(), ws.sa.data_ptr(), ws.sb.data_ptr(), d["hf"], 0, s)
+        nat.call("ffno_spectral_mix", ws.sb.data_ptr(), ws.sa.data_ptr(), H * Wf, D, C, 2 * H * Wf * C, H * Wf * C, C,
+                 bp["s_wbig"].data_ptr(), fq.g.data_ptr(), _ptr(fq.u), _ptr(fq.v), m.freq_mix_rank, s)
+        nat.call("ffno_xform", pln["thi"].data_ptr(), ws.sa.data_ptr(), ws.sb.data_ptr(), d["hf"], 0, s)
+        nat.call("ffno_xform", pln["twi"].data_ptr(), ws.sb.data_ptr(), ws.ys.data_ptr(), d["wi"], 0, s)
+        nat.call("ffno_mlp2_fwd", 0, ws.ys.data_ptr(), None, None, 0.0, None, V, C, bp["s_p1"].data_ptr(),
+                 bp["s_p2"].data_ptr(), ws.dw.data_ptr(), ws.spec_pre.data_ptr(), ws.partials.data_ptr(), P, G, s)
+        self._finalize(ws, "spec", bp["spec_g"], bp["spec_b"])
+        # vertical (height) branch
+        hq = hgt["freq"][i]
+        nat.call("ffno_xform", hgt["tzf"].data_ptr(), ws.xv.data_ptr(), ws.va.data_ptr(), d["zf"], 0, s)
+        nat.call("ffno_spectral_mix", ws.va.data_ptr(), ws.vb.data_ptr(), live, HW, HW * C, C, live * HW * C, C,
+                 bp["v_wbig"].data_ptr(), hq.g.data_ptr(), _ptr(hq.u), _ptr(hq.v), m.freq_mix_rank, s)
+        nat.call("ffno_xform", hgt["tzi"].data_ptr(), ws.vb.data_ptr(), ws.yv.data_ptr(), d["zi"], 0, s)
+        nat.call("ffno_mlp2_fwd", 0, ws.yv.data_ptr(), None, None, 0.0, None, V, C, bp["v_p1"].data_ptr(),
+                 bp["v_p2"].data_ptr(), ws.dw.data_ptr(), ws.vert_pre.data_ptr(), ws.partials.data_ptr(), P, G, s)
+        self._finalize(ws, "vert", bp["vert_g"], bp["vert_b"])
+        # gate + fuse
+        nat.call("ffno_fuse_fwd", x.data_ptr(), ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(),
+                 ws.vert_pre.data_ptr(), ws.coefs["vert"].data_ptr(), V, C, bp["bg1"].data_ptr(),
+                 bp["bg2"].data_ptr(), bp["bgb"].data_ptr(), bp["f1"].data_ptr(), bp["f2"].data_ptr(),
+                 ws.dw.data_ptr(), ws.fused_pre.data_ptr(), ws.partials.data_ptr(), P, G, s)
+        self._finalize(ws, "fuse", bp["fuse_g"], bp["fuse_b"])
+        r_f, r_pw, r_mlp = bp["res"]
+        nat.call("ffno_mlp2_fwd", 1, x.data_ptr(), ws.fused_pre.data_ptr(), ws.coefs["fuse"].data_ptr(), r_f,
+                 ws.x1.data_ptr(), V, C, bp["pw1"].data_ptr(), bp["pw2"].data_ptr(), ws.dw.data_ptr(),
+                 ws.pw_pre.data_ptr(), ws.partials.data_ptr(), P, G, s)
+        self._finalize(ws, "pw", bp["pw_g"], bp["pw_b"])
+        nat.call("ffno_mlp2_fwd", 2, ws.x1.data_ptr(), ws.pw_pre.data_ptr(), ws.coefs["pw"].data_ptr(), r_pw,
+                 ws.x2.data_ptr(), V, C, bp["m1"].data_ptr(), bp["m2"].data_ptr(), ws.dw.data_ptr(),
+                 ws.mlp_pre.data_ptr(), ws.partials.data_ptr(), P, G, s)
+        self._finalize(ws, "mlp", bp["mlp_g"], bp["mlp_b"])
+        nat.call("ffno_resid_out", ws.x2.data_ptr(), ws.mlp_pre.data_ptr(), ws.coefs["mlp"].data_ptr(), r_mlp, V, C,
+                 ws.x.data_ptr(), s)
+
+    def _head(self, pk, x, xin, out):
+        m = self.model
+        V = x.shape[0]
+        nat.call("ffno_head_fwd", x.data_ptr(), xin.data_ptr(), V, m.width, pk.p1.data_ptr(), pk.p2.data_ptr(),
+                 pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head, out.data_ptr(), None, _stream())
+
+    # -------------------------------------------------------------------------------------------- VJP
+    def backward(self, state, ybar):
+        """Input VJP: ybar [B, L, D, H, W] -> (x_bar [B, Cin, D, H, W], z_bar [B, D, H, W])."""
+        m = self.model
+        x, z_scale, dx, dy = state["x"], state["z"], state["dx"], state["dy"]
+        pk, geo, hgt, pln, pfr = self._setup(x, z_scale, dx, dy)
+        B, Cin, D, H, W = x.shape
+        C, V, HW = m.width, D * H * W, H * W
+        dev = x.device
+        s = _stream()
+        ybar = ybar.contiguous()
+        xbar_in = torch.zeros_like(x)
+        zbar = torch.zeros_like(z_scale)
+        live = hgt["live"]
+        ws = Workspace(D, H, W, C, live, pk.groups, dev)
+        gb = _GradBuffers(D, H, W, C, live, pk.groups, ws.nparts, dev)
+        tzf_bar = torch.zeros(2 * live, D, dtype=torch.float64, device=dev)
+        tzi_bar = torch.zeros(D, 2 * live, dtype=torch.float64, device=dev)
+        for b in range(B):
+            xin, z = x[b], z_scale[b]
+            inputs = state["inputs"][b]
+            self._depth_weights(ws, z, D, HW)
+            gb.wbar.zero_()
+            # head
+            nat.call("ffno_head_bwd", inputs[-1].data_ptr(), xin.data_ptr(), ybar[b].data_ptr(), V, C,
+                     pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.p2t.data_ptr(), pk.p1t.data_ptr(),
+                     pk.nhp, pk.head, gb.xbar.data_ptr(), xbar_in[b].data_ptr(), s)
+            for i in reversed(range(m.n_layers)):
+                self._block(pk, ws, i, z, D, H, W, hgt, pln, pfr[i], x_in=inputs[i])
+                self._block_bwd(pk, ws, gb, i, inputs[i], z, zbar[b], D, H, W, hgt, pln, pfr[i], tzf_bar, tzi_bar)
+            # lift: x0 = gelu(GN(pre0))
+            self._lift(pk, ws, xin)
+            self._gn_bwd(ws, gb, 1, gb.xbar, 1.0, ws.pre, pk.lift_g, pk.lift_b, "lift", gb.pbar)
+            nat.call("ffno_lift_bwd", gb.pbar.data_ptr(), Cin, V, C, pk.lift_w.data_ptr(), xbar_in[b].data_ptr(), s)
+            nat.call("ffno_depth_weights_bwd", z.data_ptr(), gb.wbar.data_ptr(), D, HW, zbar[b].data_ptr(), s)
+        # the height tables depend on the shared column (sample 0, column (0, 0)): their gradient goes there
+        gcol = tb.height_tables_vjp(geo.column_raw, geo.length, geo.k, live, tzf_bar.cpu().numpy(),
+                                    tzi_bar.cpu().numpy())
+        zbar[0, :, 0, 0] += torch.as_tensor(gcol, dtype=torch.float32, device=dev)
+        return xbar_in, zbar
+
+    def _gn_bwd(self, ws, gb, mode, u, r, pre, gamma, beta, name, pbar):
+        m = self.model
+        C, V, s = m.width, ws.V, _stream()
+        G = self._packed.groups
+        nat.call("ffno_gn_bwd_stats", mode, u.data_ptr(), r, pre.data_ptr(), gamma.data_ptr(), beta.data_ptr(),
+                 ws.gstats[name].data_ptr(), V, C, G, gb.bpart.data_ptr(), ws.nparts, s)
+        nat.call("ffno_gn_bwd_final", gb.bpart.data_ptr(), ws.nparts, G, gb.sums.data_ptr(), s)
+        nat.call("ffno_gn_bwd_apply", mode, u.data_ptr(), r, pre.data_ptr(), gamma.data_ptr(), beta.data_ptr(),
+                 ws.gstats[name].data_ptr(), gb.sums.data_ptr(), ws.dw.data_ptr(), V, C, G, EPS, pbar.data_ptr(),
+                 gb.wbar.data_ptr(), s)
+
+    def _block_bwd(self, pk, ws, gb, i, x, z, zbar, D, H, W, hgt, pln, fq, tzf_bar, tzi_bar):
+        """gb.xbar (gradient of the block output) -> gb.xbar (gradient of the block input x); accumulates the
+        depth-weight gradient in gb.wbar, the z_proj gradient in zbar and the height-table gradients."""
+        m = self.model
+        C, V, HW, Wf = m.width, ws.V, H * W, W // 2 + 1
+        s = _stream()
+        bp = pk.blocks[i]
+        r_f, r_pw, r_mlp = bp["res"]
+        live = hgt["live"]
+        d = _descs(D, H, W, C, live)
+        # out = x2 + r_mlp GN(mlp_pre); mlp_pre = mlp(x2)
+        self._gn_bwd(ws, gb, 0, gb.xbar, r_mlp, ws.mlp_pre, bp["mlp_g"], bp["mlp_b"], "mlp", gb.pbar)
+        nat.call("ffno_mlp2_bwd", ws.x2.data_ptr(), gb.pbar.data_ptr(), gb.xbar.data_ptr(), V, C, bp["m1"].data_ptr(),
+                 bp["m2t"].data_ptr(), bp["m1t"].data_ptr(), gb.g2.data_ptr(), s)
+        # x2 = x1 + r_pw GN(pw_pre); pw_pre = pw(x1)
+        self._gn_bwd(ws, gb, 0, gb.g2, r_pw, ws.pw_pre, bp["pw_g"], bp["pw_b"], "pw", gb.pbar)
+        nat.call("ffno_mlp2_bwd", ws.x1.data_ptr(), gb.pbar.data_ptr(), gb.g2.data_ptr(), V, C,
+                 bp["pw1"].data_ptr(), bp["pw2t"].data_ptr(), bp["pw1t"].data_ptr(), gb.g1.data_ptr(), s)
+        # x1 = x + r_f gelu(GN(fused_pre)); fused_pre = fuse(x, spec, vert)
+        self._gn_bwd(ws, gb, 1, gb.g1, r_f, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], "fuse", gb.pbar)
+        nat.call("ffno_fuse_bwd", x.data_ptr(), ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(),
+                 ws.vert_pre.data_ptr(), ws.coefs["vert"].data_ptr(), gb.pbar.data_ptr(), gb.g1.data_ptr(), V, C,
+                 bp["bg1"].data_ptr(), bp["bg2"].data_ptr(), bp["bgb"].data_ptr(), bp["f1"].data_ptr(),
+                 bp["f2t"].data_ptr(), bp["f1t"].data_ptr(), bp["bg2t"].data_ptr(), bp["bg1t"].data_ptr(),
+                 gb.xacc.data_ptr(), gb.sbar.data_ptr(), gb.vbar.data_ptr(), s)
+        # spec = gelu(GN(spec_pre)), spec_pre = post_s(ys); vert likewise
+        self._gn_bwd(ws, gb, 1, gb.sbar, 1.0, ws.spec_pre, bp["spec_g"], bp["spec_b"], "spec", gb.pbar)
+        nat.call("ffno_mlp2_bwd", ws.ys.data_ptr(), gb.pbar.data_ptr(), None, V, C, bp["s_p1"].data_ptr(),
+                 bp["s_p2t"].data_ptr(), bp["s_p1t"].data_ptr(), gb.ysb.data_ptr(), s)
+        self._gn_bwd(ws, gb, 1, gb.vbar, 1.0, ws.vert_pre, bp["vert_g"], bp["vert_b"], "vert", gb.pbar)
+        nat.call("ffno_mlp2_bwd", ws.yv.data_ptr(), gb.pbar.data_ptr(), None, V, C, bp["v_p1"].data_ptr(),
+                 bp["v_p2t"].data_ptr(), bp["v_p1t"].data_ptr(), gb.yvb.data_ptr(), s)
+        # horizontal transposes: ys = twi thi mix thf twf xs  ->  xs_bar = twf^T thf^T mix^T thi^T twi^T ys_bar
+        nat.call("ffno_xform", pln["twi_t"].data_ptr(), gb.ysb.data_ptr(), ws.sa.data_ptr(), d["wf"], 0, s)
+        nat.call("ffno_xform", pln["thi_t"].data_ptr(), ws.sa.data_ptr(), ws.sb.data_ptr(), d["hf"], 0, s)
+        nat.call("ffno_spectral_mix", ws.sb.data_ptr(), ws.sa.data_ptr(), H * Wf, D, C, 2 * H * Wf * C, H * Wf * C, C,
+                 bp["s_wbigt"].data_ptr(), fq.g_adj.data_ptr(), _ptr(fq.u_adj), _ptr(fq.v_adj), m.freq_mix_rank, s)
+        nat.call("ffno_xform", pln["thf_t"].data_ptr(), ws.sa.data_ptr(), ws.sb.data_ptr(), d["hf"], 0, s)
+        nat.call("ffno_xform", pln["twf_t"].data_ptr(), ws.sb.data_ptr(), gb.xsb.data_ptr(), d["wi"], 0, s)
+        # vertical transposes (ws.vb holds the mixed modes, ws.xv the transform input)
+        hq = hgt["freq"][i]
+        N = HW * C
+        nat.call("ffno_outer", gb.yvb.data_ptr(), N, D, ws.vb.data_ptr(), N, 2 * live, N, gb.opart.data_ptr(),
+                 gb.osplit_i, tzi_bar.data_ptr(), 1, s)
+        nat.call("ffno_xform", hgt["tzi_t"].data_ptr(), gb.yvb.data_ptr(), ws.va.data_ptr(), d["zf"], 0, s)
+        nat.call("ffno_spectral_mix", ws.va.data_ptr(), ws.vb.data_ptr(), live, HW, HW * C, C, live * HW * C, C,
+                 bp["v_wbigt"].data_ptr(), hq.g_adj.data_ptr(), _ptr(hq.u_adj), _ptr(hq.v_adj), m.freq_mix_rank, s)
+        nat.call("ffno_outer", ws.vb.data_ptr(), N, 2 * live, ws.xv.data_ptr(), N, D, N, gb.opart.data_ptr(),
+                 gb.osplit_f, tzf_bar.data_ptr(), 1, s)
+        nat.call("ffno_xform", hgt["tzf_t"].data_ptr(), ws.vb.data_ptr(), gb.xvb.data_ptr(), d["zi"], 0, s)
+        # input gates (and z_proj)
+        nat.call("ffno_gate_bwd", x.data_ptr(), gb.xsb.data_ptr(), gb.xvb.data_ptr(), gb.xacc.data_ptr(), V, C,
+                 bp["s_g1"].data_ptr(), bp["s_g2"].data_ptr(), bp["s_g2t"].data_ptr(), bp["s_g1t"].data_ptr(),
+                 bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(), bp["v_g2t"].data_ptr(), bp["v_g1t"].data_ptr(),
+                 bp["v_zp"].data_ptr(), gb.xbar.data_ptr(), zbar.data_ptr(), s)
+
+
+class _GradBuffers:
+    def __init__(self, D, H, W, C, live, groups, nparts, device):
+        V = D * H * W
+        f32 = dict(dtype=torch.float32, device=device)
+        for n in ("xbar", "g2", "g1", "xacc", "sbar", "vbar", "pbar", "ysb", "yvb", "xsb", "xvb"):
+            setattr(self, n, torch.empty(V, C, **f32))
+        self.wbar = torch.zeros(V, **f32)
+        self.bpart = torch.empty(max(nparts, 1) * groups * 2, dtype=torch.float64, device=device)
+        self.sums = torch.empty(groups * 2, dtype=torch.float64, device=device)
+        N = H * W * C
         lib = nat.lib()
-        nparts = lib.ffno_stats_parts(V)
-        G = pk.groups
-        f32 = dict(dtype=torch.float32, device=dev)
-        buf = lambda *shape: torch.empty(*shape, **f32)
-        dw = buf(V)
-        nat.call("ffno_depth_weights", z.data_ptr(), D, HW, dw.data_ptr(), s)
-        partials = torch.empty(nparts * G * 3, dtype=torch.float64, device=dev)
-        coefs = {n: buf(3 * C) for n in ("lift", "spec", "vert", "fuse", "pw", "mlp")}
+        self.osplit_i = lib.ffno_outer_parts(D, 2 * live, N)
+        self.osplit_f = lib.ffno_outer_parts(2 * live, D, N)
+        self.opart = torch.empty(max(self.osplit_i, self.osplit_f) * D * 2 * live, **f32)
 
-        x = buf(V, C)
-        pre = buf(V, C)
-        nat.call("ffno_lift_fwd", xin.data_ptr(), m.in_channels, V, C, pk.lift_w.data_ptr(), dw.data_ptr(),
-                 pre.data_ptr(), partials.data_ptr(), nparts, G, s)
-        nat.call("ffno_gn_finalize", partials.data_ptr(), nparts, C, G, pk.lift_g.data_ptr(), pk.lift_b.data_ptr(),
-                 EPS, coefs["lift"].data_ptr(), None, s)
-        nat.call("ffno_gn_act", pre.data_ptr(), coefs["lift"].data_ptr(), V, C, 1, x.data_ptr(), s)
 
-        live, tzf, tzi, hfreq = hgt
-        twf, thf, thi, twi = pln
-        spec_len = D * 2 * H * Wf * C
-        sa, sb_ = buf(spec_len), buf(spec_len)
-        xs, xv, y = buf(V, C), buf(V, C), buf(V, C)
-        va, vb = buf(2 * live * HW * C), buf(2 * live * HW * C)
-        spec_pre, vert_pre, fused_pre, pw_pre, mlp_pre = (buf(V, C) for _ in range(5))
-        x1, x2 = buf(V, C), buf(V, C)
-        descs = self._descs(D, H, W, C, live)
-        for i, bp in enumerate(pk.blocks):
-            # ---- input gates
-            nat.call("ffno_gate_fwd", x.data_ptr(), V, C, bp["s_g1"].data_ptr(), bp["s_g2"].data_ptr(), None, None,
-                     xs.data_ptr(), s)
-            nat.call("ffno_gate_fwd", x.data_ptr(), V, C, bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(),
-                     bp["v_zp"].data_ptr(), z.data_ptr(), xv.data_ptr(), s)
-            # ---- horizontal spectral branch
-            g, u, v = pfr[i]
-            nat.call("ffno_xform", twf.data_ptr(), xs.data_ptr(), sa.data_ptr(), descs["wf"], 0, s)
-            nat.call("ffno_xform", thf.data_ptr(), sa.data_ptr(), sb_.data_ptr(), descs["hf"], 0, s)
-            nat.call("ffno_spectral_mix", sb_.data_ptr(), sa.data_ptr(), H * Wf, D, C, 2 * H * Wf * C, H * Wf * C, C,
-                     bp["s_wbig"].data_ptr(), g.data_ptr(), _ptr(u), _ptr(v), m.freq_mix_rank, s)
-            nat.call("ffno_xform", thi.data_ptr(), sa.data_ptr(), sb_.data_ptr(), descs["hi"], 0, s)
-            nat.call("ffno_xform", twi.data_ptr(), sb_.data_ptr(), y.data_ptr(), descs["wi"], 0, s)
-            nat.call("ffno_mlp2_fwd", 0, y.data_ptr(), None, None, 0.0, None, V, C, bp["s_p1"].data_ptr(),
-                     bp["s_p2"].data_ptr(), dw.data_ptr(), spec_pre.data_ptr(), partials.data_ptr(), nparts, G, s)
-            nat.call("ffno_gn_finalize", partials.data_ptr(), nparts, C, G, bp["spec_g"].data_ptr(),
-                     bp["spec_b"].data_ptr(), EPS, coefs["spec"].data_ptr(), None, s)
-            # ---- vertical (height) branch
-            g, u, v = hfreq[i]
-            nat.call("ffno_xform", tzf.data_ptr(), xv.data_ptr(), va.data_ptr(), descs["zf"], 0, s)
-            nat.call("ffno_spectral_mix", va.data_ptr(), vb.data_ptr(), live, HW, HW * C, C, live * HW * C, C,
-                     bp["v_wbig"].data_ptr(), g.data_ptr(), _ptr(u), _ptr(v), m.freq_mix_rank, s)
-            nat.call("ffno_xform", tzi.data_ptr(), vb.data_ptr(), y.data_ptr(), descs["zi"], 0, s)
-            nat.call("ffno_mlp2_fwd", 0, y.data_ptr(), None, None, 0.0, None, V, C, bp["v_p1"].data_ptr(),
-                     bp["v_p2"].data_ptr(), dw.data_ptr(), vert_pre.data_ptr(), partials.data_ptr(), nparts, G, s)
-            nat.call("ffno_gn_finalize", partials.data_ptr(), nparts, C, G, bp["vert_g"].data_ptr(),
-                     bp["vert_b"].data_ptr(), EPS, coefs["vert"].data_ptr(), None, s)
-            # ---- gate + fuse
-            nat.call("ffno_fuse_fwd", x.data_ptr(), spec_pre.data_ptr(), coefs["spec"].data_ptr(),
-                     vert_pre.data_ptr(), coefs["vert"].data_ptr(), V, C, bp["bg1"].data_ptr(),
-                     bp["bg2"].data_ptr(), bp["bgb"].data_ptr(), bp["f1"].data_ptr(), bp["f2"].data_ptr(),
-                     dw.data_ptr(), fused_pre.data_ptr(), partials.data_ptr(), nparts, G, s)
-            nat.call("ffno_gn_finalize", partials.data_ptr(), nparts, C, G, bp["fuse_g"].data_ptr(),
-                     bp["fuse_b"].data_ptr(), EPS, coefs["fuse"].data_ptr(), None, s)
-            # ---- residual MLPs
-            r_f, r_pw, r_mlp = bp["res"]
-            nat.call("ffno_mlp2_fwd", 1, x.data_ptr(), fused_pre.data_ptr(), coefs["fuse"].data_ptr(), r_f,
-                     x1.data_ptr(), V, C, bp["pw1"].data_ptr(), bp["pw2"].data_ptr(), dw.data_ptr(),
-                     pw_pre.data_ptr(), partials.data_ptr(), nparts, G, s)
-            nat.call("ffno_gn_finalize", partials.data_ptr(), nparts, C, G, bp["pw_g"].data_ptr(),
-                     bp["pw_b"].data_ptr(), EPS, coefs["pw"].data_ptr(), None, s)
-            nat.call("ffno_mlp2_fwd", 2, x1.data_ptr(), pw_pre.data_ptr(), coefs["pw"].data_ptr(), r_pw,
-                     x2.data_ptr(), V, C, bp["m1"].data_ptr(), bp["m2"].data_ptr(), dw.data_ptr(),
-                     mlp_pre.data_ptr(), partials.data_ptr(), nparts, G, s)
-            nat.call("ffno_gn_finalize", partials.data_ptr(), nparts, C, G, bp["mlp_g"].data_ptr(),
-                     bp["mlp_b"].data_ptr(), EPS, coefs["mlp"].data_ptr(), None, s)
-            nat.call("ffno_resid_out", x2.data_ptr(), mlp_pre.data_ptr(), coefs["mlp"].data_ptr(), r_mlp, V, C,
-                     x.data_ptr(), s)
-        hp = pk.head
-        nat.call("ffno_head_fwd", x.data_ptr(), xin.data_ptr(), V, C, pk.p1.data_ptr(), pk.p2.data_ptr(),
-                 pk.b2.data_ptr(), pk.nh, pk.nhp, hp, out.data_ptr(), None, s)
+def _descs(D, H, W, C, live):
+    Wf = W // 2 + 1
+    HW = H * W
+    XD = nat.XformDesc
+    big = 1 << 30
+    d = {}
+    # rfft along W: per (d, h) row [W][C] -> [2][Wf] rows of the [D][2][H][Wf][C] spectrum
+    d["wf"] = XD(nb=D * H, nb2=H, in_b1=H * W * C, in_b2=W * C, out_b1=2 * H * Wf * C, out_b2=Wf * C,
+                 K=W, M=2 * Wf, N=C, in_split=big, in_hi=0, in_lo=C, out_split=Wf, out_hi=H * Wf * C, out_lo=C)
+    # complex DFT along H on [2H][Wf*C] per depth
+    d["hf"] = XD(nb=D, nb2=1, in_b1=2 * H * Wf * C, in_b2=0, out_b1=2 * H * Wf * C, out_b2=0, K=2 * H, M=2 * H,
+                 N=Wf * C, in_split=big, in_hi=0, in_lo=Wf * C, out_split=big, out_hi=0, out_lo=Wf * C)
+    # c2r along W: [2][Wf] rows -> [W][C]
+    d["wi"] = XD(nb=D * H, nb2=H, in_b1=2 * H * Wf * C, in_b2=Wf * C, out_b1=H * W * C, out_b2=W * C,
+                 K=2 * Wf, M=W, N=C, in_split=Wf, in_hi=H * Wf * C, in_lo=C, out_split=big, out_hi=0, out_lo=C)
+    # height transform [D][HW*C] -> [2M'][HW*C] and back
+    d["zf"] = XD(nb=1, nb2=1, in_b1=0, in_b2=0, out_b1=0, out_b2=0, K=D, M=2 * live, N=HW * C,
+                 in_split=big, in_hi=0, in_lo=HW * C, out_split=big, out_hi=0, out_lo=HW * C)
+    d["zi"] = XD(nb=1, nb2=1, in_b1=0, in_b2=0, out_b1=0, out_b2=0, K=2 * live, M=D, N=HW * C,
+                 in_split=big, in_hi=0, in_lo=HW * C, out_split=big, out_hi=0, out_lo=HW * C)
+    return d
+
+
+class _FFNOFunction(torch.autograd.Function):
+    """FFNO3D.forward with the hand-written input VJP."""
 
     @staticmethod
-    def _descs(D, H, W, C, live):
-        Wf = W // 2 + 1
-        HW = H * W
-        XD = nat.XformDesc
-        big = 1 << 30
-        d = {}
-        # rfft along W: per (d, h) row [W][C] -> [2][Wf] rows of the [D][2][H][Wf][C] spectrum
-        d["wf"] = XD(nb=D * H, nb2=H, in_b1=H * W * C, in_b2=W * C, out_b1=2 * H * Wf * C, out_b2=Wf * C,
-                     K=W, M=2 * Wf, N=C, in_split=big, in_hi=0, in_lo=C, out_split=Wf, out_hi=H * Wf * C, out_lo=C)
-        # complex DFT along H on [2H][Wf*C] per depth
-        hd = dict(nb=D, nb2=1, in_b1=2 * H * Wf * C, in_b2=0, out_b1=2 * H * Wf * C, out_b2=0, K=2 * H, M=2 * H,
-                  N=Wf * C, in_split=big, in_hi=0, in_lo=Wf * C, out_split=big, out_hi=0, out_lo=Wf * C)
-        d["hf"] = XD(**hd)
-        d["hi"] = XD(**hd)
-        # c2r along W: [2][Wf] rows -> [W][C]
-        d["wi"] = XD(nb=D * H, nb2=H, in_b1=2 * H * Wf * C, in_b2=Wf * C, out_b1=H * W * C, out_b2=W * C,
-                     K=2 * Wf, M=W, N=C, in_split=Wf, in_hi=H * Wf * C, in_lo=C, out_split=big, out_hi=0, out_lo=C)
-        # height transform [D][HW*C] -> [2M'][HW*C] and back
-        d["zf"] = XD(nb=1, nb2=1, in_b1=0, in_b2=0, out_b1=0, out_b2=0, K=D, M=2 * live, N=HW * C,
-                     in_split=big, in_hi=0, in_lo=HW * C, out_split=big, out_hi=0, out_lo=HW * C)
-        d["zi"] = XD(nb=1, nb2=1, in_b1=0, in_b2=0, out_b1=0, out_b2=0, K=2 * live, M=D, N=HW * C,
-                     in_split=big, in_hi=0, in_lo=HW * C, out_split=big, out_hi=0, out_lo=HW * C)
-        return {k: v for k, v in d.items()}
+    def forward(ctx, x, z_scale, executor, dx, dy):
+        y, state = executor.forward(x, z_scale, dx, dy, keep=True)
+        ctx.executor = executor
+        ctx.state = state
+        return y
+
+    @staticmethod
+    def backward(ctx, ybar):
+        xbar, zbar = ctx.executor.backward(ctx.state, ybar)
+        ctx.state = None
+        return xbar, zbar, None, None, None
 
 
 def ffno_apply(model, x, z_scale, dx, dy):
-    """FFNO3D.forward on the GB300 path (autograd-aware once the VJP is registered)."""
+    """FFNO3D.forward on the GB300 path; differentiable in x and z_scale."""
     if z_scale.ndim == 5:
         z_scale = z_scale[:, 0]
     dx = _spacing(dx)
     dy = _spacing(dy)
-    return model.executor().forward(x, z_scale, dx, dy)
+    ex = model.executor()
+    if torch.is_grad_enabled() and (x.requires_grad or z_scale.requires_grad):
+        return _FFNOFunction.apply(x, z_scale, ex, dx, dy)
+    y, _ = ex.forward(x, z_scale, dx, dy)
+    return y
 
 
 def _spacing(v):

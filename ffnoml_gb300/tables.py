@@ -160,3 +160,57 @@ def freq_tables(params, prefix, features, rank):
     u = lin("freq_u", h).reshape(n, -1, rank)
     v = lin("freq_v", h).reshape(n, rank, -1)
     return g, u, v
+
+
+# ------------------------------------------------------------------------------------------------ table adjoint
+def _filon_torch(z, k):
+    """filon() in torch float64 (differentiable in z)."""
+    za, zb = z[:-1, None], z[1:, None]
+    lo = torch.minimum(za, zb)
+    h = (zb - za).abs()
+    th = h * k
+    small = th.abs() < 1e-2
+    t = torch.where(small, torch.ones_like(th), th)
+    c, s = torch.cos(t), torch.sin(t)
+    r_re = torch.where(small, 0.5 - th ** 2 / 8, (c + t * s - 1) / t ** 2)
+    r_im = torch.where(small, -th / 3 + th ** 3 / 30, (t * c - s) / t ** 2)
+    l_re = torch.where(small, 0.5 - th ** 2 / 24, s / t - r_re)
+    l_im = torch.where(small, -th / 6 + th ** 3 / 120, (c - 1) / t - r_im)
+    ph = lo * k
+    e_re, e_im = h * torch.cos(ph), -h * torch.sin(ph)
+    lo_re, lo_im = e_re * l_re - e_im * l_im, e_re * l_im + e_im * l_re
+    hi_re, hi_im = e_re * r_re - e_im * r_im, e_re * r_im + e_im * r_re
+    up = za <= zb
+    a_re, a_im = torch.where(up, lo_re, hi_re), torch.where(up, lo_im, hi_im)
+    b_re, b_im = torch.where(up, hi_re, lo_re), torch.where(up, hi_im, lo_im)
+    pad_end, pad_start = (0, 0, 0, 1), (0, 0, 1, 0)
+    return (F.pad(a_re, pad_end) + F.pad(b_re, pad_start), F.pad(a_im, pad_end) + F.pad(b_im, pad_start))
+
+
+def height_tables_vjp(column_raw, length, k, live, tzf_bar, tzi_bar):
+    """Gradient w.r.t. the raw (unshifted) shared column of heights [D] of the height tables (tzf, tzi) along
+    (tzf_bar [2M'][D], tzi_bar [D][2M']), by autograd through the float64 table builder: the column shift by its
+    minimum, the Filon weights, the inverse phases and the taper's median spacing (models/ffno_model.py:37-64,
+    239-246, 266-275, 302-305)."""
+    with torch.enable_grad():
+        return _height_tables_vjp(column_raw, length, k, live, tzf_bar, tzi_bar)
+
+
+def _height_tables_vjp(column_raw, length, k, live, tzf_bar, tzi_bar):
+    col_raw = torch.as_tensor(np.asarray(column_raw, dtype=np.float64)).requires_grad_(True)
+    col = col_raw - col_raw.amin()
+    kk = k[:live].double()
+    dz = (col[1:] - col[:-1]).abs().median(dim=-1).values
+    kn = math.pi / dz
+    u = ((kk - 2 * kn / 3) / (kn / 3)).clamp(0, 1)
+    tap = 0.5 * (1 + torch.cos(math.pi * u))
+    factor = torch.full((live,), 2.0, dtype=torch.float64)
+    factor[0] = 1.0
+    f = factor * tap / length
+    q_re, q_im = _filon_torch(col, kk)
+    ph = col[:, None] * kk[None]
+    tzf = torch.cat([q_re.t(), q_im.t()], 0)
+    tzi = torch.cat([torch.cos(ph) * f, -torch.sin(ph) * f], 1)
+    (g,) = torch.autograd.grad((tzf * torch.as_tensor(tzf_bar)).sum() + (tzi * torch.as_tensor(tzi_bar)).sum(),
+                               col_raw)
+    return g.numpy()

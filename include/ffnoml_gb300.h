@@ -73,8 +73,8 @@ int ffno_column_info(const float* z, int D, long HW, float* out, ffno_stream_t s
 int ffno_lift_fwd(const float* x_in, int cin, long V, int C, const float* w_lift, const float* dw, float* pre,
                   double* partials, int nparts, int groups, ffno_stream_t stream);
 
-/* DepthWeightedGroupNorm statistics (models/ffno_model.py:77-95): partials -> coefs [3][C] and gstats [groups][2]
- * (mean, rstd as doubles). */
+/* DepthWeightedGroupNorm statistics (models/ffno_model.py:77-95): partials -> coefs [3][C] and, if gstats is not
+ * NULL, gstats [groups][3] doubles (mean, rstd, total weight T). */
 int ffno_gn_finalize(const double* partials, int nparts, int C, int groups, const float* gamma, const float* beta,
                      float eps, float* coefs, double* gstats, ffno_stream_t stream);
 
@@ -141,6 +141,66 @@ int ffno_xform(const float* T, const float* in, float* out, const ffno_xform_des
 int ffno_spectral_mix(const float* in, float* out, long F, long nb, long sf, long sb, long s_im, int C,
                       const float* wbig, const float* g, const float* U, const float* Vm, int rank,
                       ffno_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------------------------------
+ * Input VJP (the hand-written replacement of torch.autograd.backward through FFNO3D.forward under per-block
+ * checkpointing, ffno_fsdp_runtime.py:306-348 and models/ffno_model.py:751-780). u is the gradient arriving at a
+ * GroupNorm's consumer: mode 0 means dL/dy = r*u (y = GN(pre)), mode 1 means dL/dy = r*u*gelu'(y) (GELU after GN).
+ * ------------------------------------------------------------------------------------------------------------------ */
+
+/* Per-group sums S1 = sum ghat, S2 = sum ghat*xhat of the GroupNorm backward, ghat = dL/dy * gamma, as partials
+ * [nparts][groups][2] doubles (one row per CTA; any nparts >= 1). */
+int ffno_gn_bwd_stats(int mode, const float* u, float r, const float* pre, const float* gamma, const float* beta,
+                      const double* gstats, long V, int C, int groups, double* partials, int nparts,
+                      ffno_stream_t stream);
+/* partials -> sums [groups][2] doubles (fixed order). */
+int ffno_gn_bwd_final(const double* partials, int nparts, int groups, double* sums, ffno_stream_t stream);
+/* pre_bar = rstd (ghat - (w/T)(S1 + xhat S2)); w_bar[v] += the depth-weight gradient of this GroupNorm's statistics. */
+int ffno_gn_bwd_apply(int mode, const float* u, float r, const float* pre, const float* gamma, const float* beta,
+                      const double* gstats, const double* sums, const float* dw, long V, int C, int groups, float eps,
+                      float* pre_bar, float* w_bar, ffno_stream_t stream);
+
+/* Backward of pre = gelu(a @ w1) @ w2 (the C -> 2C -> C MLPs): a_bar = base + ((pre_bar @ w2t) * gelu'(a @ w1)) @ w1t,
+ * recomputing a @ w1; w2t [C][2C], w1t [2C][C] are the transposed weights; base may be NULL. */
+int ffno_mlp2_bwd(const float* a, const float* pre_bar, const float* base, long V, int C, const float* w1,
+                  const float* w2t, const float* w1t, float* a_bar, ffno_stream_t stream);
+
+/* Backward of ffno_fuse_fwd given fused_pre_bar: x_bar = base + d/dx, spec_bar and vert_bar = gradients w.r.t.
+ * spec = gelu(GN_spec(spec_pre)) and vert (before their GroupNorm backward). Transposed weights: wf2t [C][2C],
+ * wf1t [2C][2C], wg2t [2C][C], wg1t [C][3C]. */
+int ffno_fuse_bwd(const float* x, const float* spec_pre, const float* spec_coefs, const float* vert_pre,
+                  const float* vert_coefs, const float* fused_pre_bar, const float* base, long V, int C,
+                  const float* wg1, const float* wg2, const float* bg2, const float* wf1, const float* wf2t,
+                  const float* wf1t, const float* wg2t, const float* wg1t, float* x_bar, float* spec_bar,
+                  float* vert_bar, ffno_stream_t stream);
+
+/* Backward of both input gates (ffno_gate_fwd): x_bar = base + gate_s'(xs_bar) + gate_v'(xv_bar);
+ * z_bar[v] += sum_c xv_bar[v][c] * zp[c] (z_proj). */
+int ffno_gate_bwd(const float* x, const float* xs_bar, const float* xv_bar, const float* base, long V, int C,
+                  const float* s_w1, const float* s_w2, const float* s_w2t, const float* s_w1t, const float* v_w1,
+                  const float* v_w2, const float* v_w2t, const float* v_w1t, const float* zp, float* x_bar,
+                  float* z_bar, ffno_stream_t stream);
+
+/* Backward of the lift convolution: x_in_bar [cin][V] += pre_bar @ w_lift^T. */
+int ffno_lift_bwd(const float* pre_bar, int cin, long V, int C, const float* w_lift, float* x_in_bar,
+                  ffno_stream_t stream);
+
+/* Backward of ffno_head_fwd given y_bar [levels][V]: x_bar [V][C] (gradient of the last block's output) and the
+ * head's direct input gradient x_in_bar [cin][V] (written, not accumulated: T, ne and rho channels). p2t [nhp][2C]
+ * and p1t [2C][C] are the transposed, zero-padded projection weights. */
+int ffno_head_bwd(const float* x, const float* x_in, const float* y_bar, long V, int C, const float* p1,
+                  const float* p2, const float* b2, const float* p2t, const float* p1t, int nhp,
+                  const ffno_head_params* params, float* x_bar, float* x_in_bar, ffno_stream_t stream);
+
+/* Backward of ffno_depth_weights: z_bar [D][HW] += d w / d z applied to w_bar. */
+int ffno_depth_weights_bwd(const float* z, const float* w_bar, int D, long HW, float* z_bar, ffno_stream_t stream);
+
+/* out [Ma][Mb] (double; = or +=) = A [Ma][N] (row stride lda) @ B [Mb][N]^T (row stride ldb), split over N into
+ * nsplit partial sums held in part [nsplit][Ma][Mb] floats and reduced in a fixed order: the gradients of the height
+ * operator's transform tables. ffno_outer_parts gives the nsplit to use. */
+int ffno_outer_parts(int Ma, int Mb, long N);
+int ffno_outer(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, float* part, int nsplit,
+               double* out, int accumulate, ffno_stream_t stream);
 
 #ifdef __cplusplus
 }
