@@ -1,0 +1,369 @@
+#!/usr/bin/env python3
+"""FFNO3D forward + input-VJP throughput on GB300 (voxels/s).
+
+Workload (the scaled configuration): FFNO3D width 64, 8 blocks, height operator with M = 32 modes
+(z_min_wavelength = 40/31), H + Ca II level-fraction head (12 levels), one cube [1, 6, 256, 128, 128] = 4.19 M voxels,
+synthetic seeded inputs with the reference's channel distributions, random-init weights of that architecture.
+
+A step is one forward pass plus one input VJP (per-block recompute) over the cube, inputs resident in HBM (value);
+e2e is the same step through the service backend's vjp_local with host numpy buffers (host<->device copies inside the
+timed region). The cube (GBs of activations) is far larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--precision fp32|bf16]
+
+--impl reference times the reference algorithm's CPU implementation (the oracle port of the reference FFNO3D, float32
+torch on the host cores) on a bounded sub-cube per step, same metric and unit.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WIDTH, LAYERS, MODES = 64, 8, 32
+SHAPE = (256, 128, 128)
+ATOMS = ["H", "CA"]
+DXY = 48e3
+MEAN_X = np.array([4.75, 0.0, 0.0, 0.0, 17.5, -8.0], np.float32)
+STD_X = np.array([2.5 / math.sqrt(12), 5.0, 5.0, 5.0, 7.0 / math.sqrt(12), 8.0 / math.sqrt(12)], np.float32)
+CPU_SAMPLE = (32, 16, 16)       # bounded sub-cube per step of the reference arm (same C, L, M)
+CPU_BASELINE_SAMPLE = (64, 32, 32)  # the cpu_baseline sub-cube (about 10-30 s of fwd+VJP on the host cores)
+KERNELS_PER_CALL = {"ffno_column_info": 3, "ffno_outer": 2}
+
+
+def model_config():
+    return dict(width=WIDTH, n_layers=LAYERS, z_min_wavelength=40.0 / (MODES - 1))
+
+
+def build_model(seed=0):
+    import torch
+    from ffnoml_gb300 import create_ffno3d
+    torch.manual_seed(seed)
+    m = create_ffno3d(6, 12, atoms=ATOMS, **model_config())
+    with torch.no_grad():
+        for name, p in m.named_parameters():
+            if ".freq_u." in name:
+                p.normal_(0.0, 0.1)
+        c = 0
+        for lv in m.species_levels:
+            m.proj2.weight[c + lv].normal_(0.0, 0.3)
+            m.proj2.bias[c + lv].normal_(0.0, 0.3)
+            c += lv + 1
+    m.set_normalization(MEAN_X, STD_X, np.zeros(12), np.ones(12))
+    return m.eval()
+
+
+def synthetic_si(shape, seed=1):
+    """SI features (6, D, H, W), heights (D, H, W) in metres, as the service receives them."""
+    D, H, W = shape
+    g = np.random.default_rng(seed)
+    f = np.empty((6, D, H, W), np.float32)
+    f[0] = 10.0 ** g.uniform(3.5, 6.0, (D, H, W))
+    f[1:4] = g.normal(0.0, 5e3, (3, D, H, W))
+    f[4] = g.uniform(14.0, 21.0, (D, H, W))
+    f[5] = g.uniform(-12.0, -4.0, (D, H, W))
+    z = np.broadcast_to(np.linspace(14.0, -1.0, D, dtype=np.float32)[:, None, None] * 1e6, (D, H, W)).copy()
+    return f, z
+
+
+def normalised(f, z):
+    """Model-unit, normalised inputs [1, 6, D, H, W] and z [1, D, H, W] in Mm (ffno_fsdp_runtime._model_inputs)."""
+    m = f.astype(np.float64).copy()
+    m[0] = np.log10(m[0])
+    m[1:4] /= 1e3
+    x = (m - MEAN_X[:, None, None, None]) / STD_X[:, None, None, None]
+    return x[None].astype(np.float32), (z / 1e6)[None].astype(np.float32)
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.out = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.out = [line.split(",") for line in out.strip().splitlines() if line.strip()]
+
+    def summary(self):
+        rows = [[c.strip() for c in r] for r in self.out if len(r) >= 9]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------------------------------- CPU arms
+def cpu_rate(model_state, shape, steps=1, warmup=0):
+    """fwd+VJP voxels/s of the oracle port (float32 torch on the host cores) on a sub-cube."""
+    import torch
+    from ffnoml_gb300.config import species_of
+    from oracle.ffno_oracle import OracleFFNO3D
+    cfg = dict(model_config(), species=species_of(ATOMS), in_channels=6, out_channels=12)
+    oracle = OracleFFNO3D(model_state, cfg, torch.float32, checkpoint_blocks=True)
+    f, z = synthetic_si(shape, seed=3)
+    x, zz = normalised(f, z)
+    x = torch.from_numpy(x)
+    zz = torch.from_numpy(zz)
+    cot = torch.from_numpy(np.random.default_rng(4).normal(size=(1, 12) + shape).astype(np.float32))
+
+    def step():
+        xr = x.clone().requires_grad_(True)
+        zr = zz.clone().requires_grad_(True)
+        y = oracle.forward(xr, zr, DXY, DXY)
+        torch.autograd.backward(y, cot)
+
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = time.perf_counter() - t0
+    vox = shape[0] * shape[1] * shape[2]
+    return vox * steps / dt, dt, torch.get_num_threads()
+
+
+def run_reference(args):
+    import torch
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    torch.set_num_threads(len(os.sched_getaffinity(0)))
+    model = build_model()
+    state = {k: v.detach().clone() for k, v in model.state_dict().items()}
+    rate, dt, cores = cpu_rate(state, CPU_SAMPLE, steps=args.steps, warmup=args.warmup)
+    sample = f"{CPU_SAMPLE[0]}x{CPU_SAMPLE[1]}x{CPU_SAMPLE[2]} sub-cube of the same model per step, fwd+VJP"
+    line = {"impl": "reference", "metric": "FFNO3D fwd+VJP voxels/s", "value": rate, "unit": "voxels/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "FFNO3D w64 L8 M32 H+CaII, [1,6,256,128,128], per-step sample " + sample,
+                       "parallelism": "cpu"},
+            "cpu_baseline": {"value": rate, "unit": "voxels/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": rate, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------------------- GPU arm
+def algorithmic_flops_per_voxel(C, L, D, H, W, M, levels, species, r=8):
+    """Forward MACs x 2 per voxel of the path (shared grid), the per-unit figure of the roofline."""
+    Wf = W // 2 + 1
+    per_block = (31 * C * C + C + (4 * C * C + 4 * r * C) * Wf / W + 4 * M * C + (4 * C * C + 4 * r * C) * M / D)
+    head = 6 * C + 2 * C * C + 2 * C * (levels + species)
+    return 2 * (L * per_block + head)
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+    from ffnoml_gb300 import _native as nat
+    from ffnoml_gb300.runtime import GB300Backend
+
+    rank, world, local = dist_info()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    model = build_model().to(dev).set_precision(args.precision)
+    D, H, W = args.shape
+    V = D * H * W
+    f_np, z_np = synthetic_si((D, H, W), seed=1 + rank)
+    x_np, z_mm = normalised(f_np, z_np)
+    x = torch.from_numpy(x_np).to(dev)
+    z = torch.from_numpy(z_mm).to(dev)
+    cot = torch.from_numpy(np.random.default_rng(2 + rank).normal(size=(1, 12, D, H, W)).astype(np.float32)).to(dev)
+    ex = model.executor()
+
+    def fwd_vjp():
+        y, st = ex.forward(x, z, DXY, DXY, keep=True)
+        ex.backward(st, cot)
+
+    def fwd():
+        ex.forward(x, z, DXY, DXY)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        barrier()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        calls0 = nat.counter.calls
+        a.record()
+        for _ in range(steps):
+            fn()
+        b.record()
+        barrier()
+        ms = a.elapsed_time(b)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t)
+        return ms / steps, nat.counter.calls - calls0
+
+    # fwd+VJP, device-resident (the headline)
+    with ClockSampler(local) as clk:
+        ms_step, calls = timed(fwd_vjp, args.steps, args.warmup)
+    clocks = clk.summary()
+    ms_fwd, _ = timed(fwd, max(args.steps, 3), 1)
+
+    # kernel breakdown of one fwd+VJP step (CUDA events around every entry point, on the launching stream)
+    nat.counter.timing = []
+    fwd_vjp()
+    torch.cuda.synchronize()
+    per = {}
+    for name, e0, e1 in nat.counter.timing:
+        t, n = per.get(name, (0.0, 0))
+        per[name] = (t + e0.elapsed_time(e1), n + 1)
+    nat.counter.timing = None
+    total = sum(t for t, _ in per.values())
+    top = max(per, key=lambda k: per[k][0])
+    breakdown = {k: {"ms": round(t, 3), "launches": n, "share": round(t / total, 4)}
+                 for k, (t, n) in sorted(per.items(), key=lambda kv: -kv[1][0])}
+
+    # roofline of the dominant kernel: algorithmic bytes (or flops) per launch / measured launch time
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    roof = roofline_of(top, per[top], D, H, W, WIDTH, hbm, peaks)
+
+    # e2e through the service backend with host buffers
+    e2e = None
+    if not args.no_e2e:
+        backend = GB300Backend(model, [f"l{i}" for i in range(12)], device=dev)
+        cot_np = np.random.default_rng(5).normal(size=(D, H, W, 12)).astype(np.float32)
+        for _ in range(max(1, min(args.warmup, 2))):
+            backend.vjp_local(f_np, z_np, DXY, DXY, cot_np)
+        barrier()
+        t0 = time.perf_counter()
+        n_e2e = max(1, min(args.steps, 3))
+        for _ in range(n_e2e):
+            backend.vjp_local(f_np, z_np, DXY, DXY, cot_np)
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / n_e2e
+        if world > 1:
+            t = torch.tensor([e2e_s], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t)
+        e2e = {"value": world * V / e2e_s, "unit": "voxels/s", "h2d_bytes_per_step": int(f_np.nbytes + z_np.nbytes +
+                                                                                            cot_np.nbytes),
+               "d2h_bytes_per_step": int(f_np.nbytes + z_np.nbytes), "ms_per_step": 1e3 * e2e_s}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        torch.set_num_threads(len(os.sched_getaffinity(0)))
+        state = {k: v.detach().cpu().clone() for k, v in model.state_dict().items()}
+        S = CPU_BASELINE_SAMPLE
+        rate, dt, cores = cpu_rate(state, S, steps=1, warmup=0)
+        cpu = {"value": rate, "unit": "voxels/s", "cores": cores, "kind": "port",
+               "sample": f"{S[0]}x{S[1]}x{S[2]} sub-cube of the same model, one fwd+VJP "
+                         f"({dt:.1f} s), oracle port of the reference FFNO3D in float32 torch"}
+
+    flops_vox = algorithmic_flops_per_voxel(WIDTH, LAYERS, D, H, W, MODES, 12, 2)
+    if rank == 0:
+        launches = sum(KERNELS_PER_CALL.get(k, 1) * n for k, (_, n) in per.items())
+        line = {
+            "metric": "FFNO3D fwd+VJP voxels/s", "value": world * V / (ms_step / 1e3), "unit": "voxels/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == "fp32" else "bf16", "data": "synthetic",
+            "config": {"workload": f"FFNO3D w{WIDTH} L{LAYERS} M{MODES} H+CaII, [1,6,{D},{H},{W}] fwd + input VJP "
+                                   "(per-block recompute)", "voxels_per_step": V, "parallelism": f"replicas{world}",
+                       "l2": "working set (GBs) >> L2; no flush needed", "precision": args.precision},
+            "fwd": {"value": world * V / (ms_fwd / 1e3), "unit": "voxels/s", "ms_per_step": ms_fwd},
+            "algorithmic_tflops": {"fwd+vjp": 2 * flops_vox * V / (ms_step / 1e3) / 1e12,
+                                   "fwd": flops_vox * V / (ms_fwd / 1e3) / 1e12},
+            "roofline": roof, "kernel_breakdown_ms": breakdown,
+            "clocks": clocks, "gpu_launches": launches * args.steps, "e2e": e2e, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def roofline_of(name, timing, D, H, W, C, hbm, peaks):
+    """Algorithmic traffic/work of one launch of the dominant entry point over its measured average duration."""
+    t_ms, n = timing
+    avg_s = t_ms / n / 1e3
+    V = D * H * W
+    Wf = W // 2 + 1
+    spec = D * 2 * H * Wf * C * 4
+    # algorithmic bytes per launch (FP32): inputs read once + outputs written once
+    bytes_per = {
+        "ffno_xform": None,
+        "ffno_mlp2_fwd": 2 * V * C * 4, "ffno_mlp2_bwd": 3 * V * C * 4, "ffno_fuse_fwd": 4 * V * C * 4,
+        "ffno_fuse_bwd": 7 * V * C * 4, "ffno_gate_fwd": 2 * V * C * 4, "ffno_gate_bwd": 5 * V * C * 4,
+        "ffno_spectral_mix": 2 * spec, "ffno_gn_bwd_stats": 2 * V * C * 4, "ffno_gn_bwd_apply": 3 * V * C * 4,
+    }.get(name)
+    if bytes_per is None:
+        bytes_per = 2 * V * C * 4
+    achieved = bytes_per / avg_s / 1e9
+    return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": None, "avg_launch_ms": t_ms / n,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16"])
+    ap.add_argument("--shape", default="256,128,128")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.shape = tuple(int(v) for v in args.shape.split(","))
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -75,6 +75,10 @@ PROTOTYPES = {
     "ffno_depth_weights_bwd": [P, P, I, L, P, P],
     "ffno_outer_parts": [I, I, L],
     "ffno_outer": [P, L, I, P, L, I, L, P, I, P, I, P],
+    "ffno_si_inputs": [P, P, L, P, P, P, P, P, P],
+    "ffno_si_populations": [P, L, I, P, P, P, P, P],
+    "ffno_si_population_cotangent": [P, P, L, I, P, P, P, P, P],
+    "ffno_si_input_grads": [P, P, P, L, P, P, P, P, P],
 }
 
 _lib = None
@@ -102,9 +106,30 @@ def lib():
     return _lib
 
 
+class _Counter:
+    """Launch accounting: number of entry-point calls, and optional per-call CUDA-event timing (for the benchmark's
+    kernel breakdown)."""
+
+    def __init__(self):
+        self.calls = 0
+        self.timing = None      # list of (name, start_event, end_event) while timing is on
+
+
+counter = _Counter()
+
+
 def call(name, *args):
     """Call an entry point and raise on a non-zero status."""
-    status = getattr(lib(), name)(*args)
+    counter.calls += 1
+    if counter.timing is not None:
+        import torch
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        status = getattr(lib(), name)(*args)
+        b.record()
+        counter.timing.append((name, a, b))
+    else:
+        status = getattr(lib(), name)(*args)
     if status:
         raise NativeError(f"{name} failed: {ERRORS.get(status, status)} (status {status})")
     return status

@@ -1,0 +1,178 @@
+"""Single-GPU persistent backend: the drop-in for DistributedFSDPBackend's predict_local / vjp_local
+(ffno_fsdp_runtime.py:81-348) with the same argument meaning, units, layouts and errors, on one GB300.
+
+Arrays cross the host boundary as numpy float32 in the service's layouts: features (6, nz, nx, ny) in SI (T [K],
+vx, vy, vz [m/s], log10 ne [m^-3], log10 rho [kg m^-3]), z (nz, nx, ny) in metres, populations (nz, nx, ny, L) in
+m^-3. The model sees D = nz, H = nx, W = ny. Weights and tables stay resident; host<->device copies go through
+pinned staging buffers that are reused per shape.
+"""
+import hashlib
+from pathlib import Path
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .executor import _stream
+
+INPUT_CHANNELS = ("temperature", "vx", "vy", "vz", "log10_ne", "log10_rho")
+
+
+def load_checkpoint(path, map_location="cpu"):
+    """The training checkpoint dict (model_state, normalization_stats, io_metadata), weights_only first
+    (train_utils.load_checkpoint, train_utils.py:20-92)."""
+    try:
+        return torch.load(path, map_location=map_location, weights_only=True)
+    except Exception:
+        return torch.load(path, map_location=map_location, weights_only=False)
+
+
+def _check(flags, what):
+    f = int(flags)
+    if f & 1:
+        raise ValueError(f"{what} contains NaN or Inf")
+    if f & 2:
+        raise ValueError(f"{what} temperature must be positive")
+    if f & 4:
+        raise RuntimeError("FFNO returned non-positive or non-finite populations")
+    if f & 8:
+        raise RuntimeError("FFNO VJP returned NaN or Inf")
+
+
+class GB300Backend:
+    """One resident FFNO3D on one GPU.
+
+    GB300Backend(model, level_names, normalization=None): model is an ffnoml_gb300.FFNO3D (moved to the device here);
+    normalization (mean_X, std_X, mean_Y, std_Y) defaults to the model's buffers. from_checkpoint builds it from a
+    training checkpoint the way DistributedFSDPBackend does (ffno_fsdp_runtime.py:116-165)."""
+
+    def __init__(self, model, level_names, normalization=None, device="cuda", name="model"):
+        if not torch.cuda.is_available():
+            raise RuntimeError("the GB300 backend requires CUDA")
+        self.device = torch.device(device)
+        self.model = model.to(self.device).eval()
+        self.level_names = tuple(str(v) for v in level_names)
+        if len(self.level_names) != model.out_channels:
+            raise RuntimeError("checkpoint Cout differs from configured level_names")
+        norm = normalization or {k: getattr(model, k).detach().cpu().numpy() for k in
+                                 ("mean_X", "std_X", "mean_Y", "std_Y")}
+        f = lambda k: torch.as_tensor(np.asarray(norm[k], dtype=np.float32), device=self.device).contiguous()
+        self.mean_x, self.std_x, self.mean_y, self.std_y = f("mean_X"), f("std_X"), f("mean_Y"), f("std_Y")
+        if torch.any(self.std_x <= 0) or torch.any(self.std_y <= 0):
+            raise RuntimeError("checkpoint normalization standard deviations must be positive")
+        self.name = name
+        self.call_count = 0
+        self._flags = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._staging = {}
+
+    @classmethod
+    def from_checkpoint(cls, checkpoint_path, factory, level_names, factory_kwargs=None, device="cuda"):
+        ck = load_checkpoint(checkpoint_path)
+        norm, io = ck.get("normalization_stats"), ck.get("io_metadata")
+        if norm is None or io is None:
+            raise RuntimeError("checkpoint must contain normalization_stats and io_metadata")
+        if int(io["Cin"]) != len(INPUT_CHANNELS):
+            raise RuntimeError(f"checkpoint Cin={io['Cin']} does not match {INPUT_CHANNELS}")
+        model = factory(Cin=int(io["Cin"]), Cout=int(io["Cout"]), device="cpu", **dict(factory_kwargs or {}))
+        model.load_state_dict(ck["model_state"], strict=True)
+        backend = cls(model, level_names, normalization=norm, device=device)
+        backend.checkpoint_hash = hashlib.sha256(Path(checkpoint_path).read_bytes()).hexdigest()
+        return backend
+
+    def describe(self):
+        return {"backend": "gb300_single_gpu", "input_channels": INPUT_CHANNELS, "level_names": self.level_names,
+                "device": str(self.device), "world_size": 1,
+                "full_parameter_count": sum(p.numel() for p in self.model.parameters()),
+                "output_representation": "linear_population_m3", "precision": self.model.precision}
+
+    # ------------------------------------------------------------------------------------------------ staging
+    def _stage(self, key, shape):
+        """(pinned host buffer, device buffer) of this shape, reused across calls."""
+        k = (key, tuple(shape))
+        if k not in self._staging:
+            host = torch.empty(shape, dtype=torch.float32, pin_memory=True)
+            dev = torch.empty(shape, dtype=torch.float32, device=self.device)
+            self._staging[k] = (host, dev)
+        return self._staging[k]
+
+    def _upload(self, key, array):
+        host, dev = self._stage(key, array.shape)
+        host.numpy()[...] = array
+        dev.copy_(host, non_blocking=True)
+        return dev
+
+    def _download(self, key, tensor):
+        host, _ = self._stage(key + "_out", tensor.shape)
+        host.copy_(tensor, non_blocking=True)
+        return host
+
+    def _validate(self, features, z_scale):
+        features = np.asarray(features, dtype=np.float32)
+        z_scale = np.asarray(z_scale, dtype=np.float32)
+        if features.ndim != 4 or features.shape[0] != len(INPUT_CHANNELS):
+            raise ValueError("local features must have shape (6,nz,nx_local,ny)")
+        if tuple(features.shape[1:]) != tuple(z_scale.shape):
+            raise ValueError("local z_scale must have shape (nz,nx_local,ny)")
+        return features, z_scale
+
+    def _prepare(self, features, z_scale):
+        nz, nx, ny = z_scale.shape
+        V = nz * nx * ny
+        f_dev = self._upload("features", features)
+        z_dev = self._upload("z", z_scale)
+        x = torch.empty(1, 6, nz, nx, ny, dtype=torch.float32, device=self.device)
+        zmm = torch.empty(1, nz, nx, ny, dtype=torch.float32, device=self.device)
+        self._flags.zero_()
+        nat.call("ffno_si_inputs", f_dev.data_ptr(), z_dev.data_ptr(), V, self.mean_x.data_ptr(),
+                 self.std_x.data_ptr(), x.data_ptr(), zmm.data_ptr(), self._flags.data_ptr(), _stream())
+        _check(self._flags.item(), "FFNO request")
+        return f_dev, x, zmm, V
+
+    # ------------------------------------------------------------------------------------------------ API
+    def predict_local(self, features, z_scale, dx, dy):
+        """(6,nz,nx,ny) SI features, (nz,nx,ny) heights [m] -> (nz,nx,ny,L) populations [m^-3]
+        (ffno_fsdp_runtime.py:294-304)."""
+        features, z_scale = self._validate(features, z_scale)
+        _, x, zmm, V = self._prepare(features, z_scale)
+        L = self.model.out_channels
+        with torch.no_grad():
+            y = self.model(x, zmm, float(dx), float(dy))
+        pop = torch.empty(*z_scale.shape, L, dtype=torch.float32, device=self.device)
+        nat.call("ffno_si_populations", y.data_ptr(), V, L, self.mean_y.data_ptr(), self.std_y.data_ptr(),
+                 pop.data_ptr(), self._flags.data_ptr(), _stream())
+        host = self._download("pop", pop)
+        torch.cuda.current_stream().synchronize()
+        _check(self._flags.item(), "FFNO output")
+        self.call_count += 1
+        return host.numpy().copy()
+
+    def vjp_local(self, features, z_scale, dx, dy, population_cotangent):
+        """Input VJP along the population cotangent (nz,nx,ny,L): {"features": (6,nz,nx,ny), "z_scale": (nz,nx,ny)}
+        per SI unit (ffno_fsdp_runtime.py:306-348)."""
+        features, z_scale = self._validate(features, z_scale)
+        cot = np.asarray(population_cotangent, dtype=np.float32)
+        L = self.model.out_channels
+        expected = tuple(z_scale.shape) + (L,)
+        if tuple(cot.shape) != expected:
+            raise ValueError(f"local population_cotangent has shape {cot.shape}; expected {expected}")
+        f_dev, x, zmm, V = self._prepare(features, z_scale)
+        cot_dev = self._upload("cot", cot)
+        ex = self.model.executor()
+        y, state = ex.forward(x, zmm, float(dx), float(dy), keep=True)
+        ybar = torch.empty_like(y)
+        nat.call("ffno_si_population_cotangent", y.data_ptr(), cot_dev.data_ptr(), V, L, self.mean_y.data_ptr(),
+                 self.std_y.data_ptr(), ybar.data_ptr(), self._flags.data_ptr(), _stream())
+        xbar, zbar = ex.backward(state, ybar)
+        fbar = torch.empty(6, *z_scale.shape, dtype=torch.float32, device=self.device)
+        zbar_m = torch.empty(*z_scale.shape, dtype=torch.float32, device=self.device)
+        nat.call("ffno_si_input_grads", f_dev.data_ptr(), xbar.data_ptr(), zbar.data_ptr(), V,
+                 self.std_x.data_ptr(), fbar.data_ptr(), zbar_m.data_ptr(), self._flags.data_ptr(), _stream())
+        hf = self._download("fbar", fbar)
+        hz = self._download("zbar", zbar_m)
+        torch.cuda.current_stream().synchronize()
+        flags = int(self._flags.item())
+        if flags & 1:
+            raise ValueError("FFNO VJP cotangent contains NaN or Inf")
+        _check(flags, "FFNO VJP")
+        self.call_count += 1
+        return {"features": hf.numpy().copy(), "z_scale": hz.numpy().copy()}

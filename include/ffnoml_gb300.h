@@ -202,6 +202,25 @@ int ffno_outer_parts(int Ma, int Mb, long N);
 int ffno_outer(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, float* part, int nsplit,
                double* out, int accumulate, ffno_stream_t stream);
 
+/* ------------------------------------------------------------------------------------------------------------------
+ * Service conversions (ffno_fsdp_runtime.py). flags is one device int, OR-ed: 1 non-finite input, 2 T <= 0,
+ * 4 non-positive or non-finite population, 8 non-finite gradient.
+ * ------------------------------------------------------------------------------------------------------------------ */
+
+/* _model_inputs + normalisation (:48-58, :274-276): SI features [6][V] (T, vx, vy, vz, log10 ne, log10 rho) and z [V]
+ * in metres -> normalised inputs x [6][V] and z_mm [V] in Mm. */
+int ffno_si_inputs(const float* features, const float* z_m, long V, const float* mean_x, const float* std_x,
+                   float* x, float* z_mm, int* flags, ffno_stream_t stream);
+/* linear_populations + _canonical_populations (:76-78, :277-292): normalised log10 n y [L][V] -> pop [V][L] m^-3. */
+int ffno_si_populations(const float* y, long V, int L, const float* mean_y, const float* std_y, float* pop,
+                        int* flags, ffno_stream_t stream);
+/* VJP of ffno_si_populations: pop_bar [V][L] -> y_bar [L][V]. */
+int ffno_si_population_cotangent(const float* y, const float* pop_bar, long V, int L, const float* mean_y,
+                                 const float* std_y, float* y_bar, int* flags, ffno_stream_t stream);
+/* VJP of ffno_si_inputs: x_bar [6][V], z_bar_mm [V] -> features_bar [6][V] (per K, per m/s, per dex), z_bar_m [V]. */
+int ffno_si_input_grads(const float* features, const float* x_bar, const float* z_bar_mm, long V, const float* std_x,
+                        float* features_bar, float* z_bar_m, int* flags, ffno_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

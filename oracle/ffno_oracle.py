@@ -129,7 +129,7 @@ def base_wavenumbers(modes, reference_length):
 
 def height_box(z_scale, reference_length, min_wavelength, base_k, dtype):
     """(length, k, mode factors) for these columns (models/ffno_model.py:248-259)."""
-    span = float((z_scale.amax(dim=-3) - z_scale.amin(dim=-3)).max())
+    span = float((z_scale.amax(dim=-3) - z_scale.amin(dim=-3)).max().detach())
     if 2 * span <= reference_length:
         k = base_k.to(dtype)
         length = reference_length
