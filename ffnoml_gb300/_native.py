@@ -79,6 +79,17 @@ PROTOTYPES = {
     "ffno_si_populations": [P, L, I, P, P, P, P, P],
     "ffno_si_population_cotangent": [P, P, L, I, P, P, P, P, P],
     "ffno_si_input_grads": [P, P, P, L, P, P, P, P, P],
+    "ffno_tc_selftest": [P, P, I, I, P, P, P],
+    "ffno_tc_parts": [L],
+    "ffno_tc_width_supported": [I],
+    "ffno_mlp2_fwd_tc": [I, P, P, P, F, P, L, I, P, P, P, P, I, I, P, P],
+    "ffno_gate_fwd_tc": [P, L, I, P, P, P, P, P, P],
+    "ffno_fuse1_tc": [P, P, P, P, P, L, I, P, P, P, P, P, P],
+    "ffno_fuse2_tc": [P, P, P, P, P, L, I, P, P, P, P, I, I, P, P],
+    "ffno_mlp2_bwd_tc": [P, P, P, L, I, P, P, P, P],
+    "ffno_gate_bwd_tc": [P, P, P, L, I, P, P, P, P, P, P],
+    "ffno_fuse_bwd_a_tc": [P, P, P, P, P, P, L, I, P, P, P, P],
+    "ffno_fuse_bwd_b_tc": [P, P, P, P, P, P, P, P, P, L, I, P, P, P, P, P, P],
 }
 
 _lib = None

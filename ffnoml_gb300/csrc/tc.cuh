@@ -1,0 +1,174 @@
+// Blackwell (sm_103a) tensor-core primitives for the BF16 kernels, written as inline PTX: tensor-memory allocation,
+// tcgen05.mma (kind::f16, BF16 operands, FP32 accumulators in TMEM), tcgen05.commit to an mbarrier, tcgen05.ld,
+// bulk (TMA) copies, and bounded mbarrier waits.
+//
+// Operand layout in shared memory: the canonical K-major, non-swizzled layout. An R x K operand (R = rows of A or of
+// B^T) is stored as 8 x 8 "core matrices" (8 rows x 16 bytes): element (r, k) sits at byte
+//   (r / 8) * SBO + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2,      SBO = K * 16
+// i.e. the K-chunks of one 8-row group are adjacent (LBO = 128 bytes) and the row groups follow each other.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <cuda_bf16.h>
+
+namespace ffno {
+namespace tc {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// byte offset of element (r, k) in a canonical K-major tile with K columns
+__device__ __forceinline__ uint32_t kmajor_offset(int r, int k, int K) {
+  return (uint32_t)((r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// shared-memory matrix descriptor, K-major, no swizzle (version bits 46..48 = 0b001)
+__device__ __forceinline__ uint64_t kmajor_desc(uint32_t saddr, uint32_t lbo_bytes, uint32_t sbo_bytes) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo_bytes >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo_bytes >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// instruction descriptor of tcgen05.mma kind::f16: D (F32) [M x N] += A (BF16, K-major) * B (BF16, K-major)
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4)                       // D format: F32
+         | (1u << 7)                     // A format: BF16
+         | (1u << 10)                    // B format: BF16
+         | ((uint32_t)(N >> 3) << 17)    // N / 8
+         | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
+// ---------------------------------------------------------------------------------------------------- mbarrier
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for the phase with this parity to complete, at most `limit` polls. Returns false if it ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = (1u << 26)) {
+  for (uint32_t i = 0; i < limit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// ---------------------------------------------------------------------------------------------------- bulk copy
+// 1-D bulk copy global -> shared completing on an mbarrier (cp.async.bulk, the TMA engine's untiled form). Both
+// addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// ---------------------------------------------------------------------------------------------------- fences
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------------------------------- TMEM
+// Allocate ncols (power of two >= 32) tensor-memory columns; one full warp calls it; the base address lands in *dst.
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_free(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// ---------------------------------------------------------------------------------------------------- MMA
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Arrive on bar when every tcgen05.mma issued so far by this thread has completed.
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// D [128 x N] += A [128 x K] * B [N x K]^T for canonical K-major tiles at a_base / b_base (shared addresses), K a
+// multiple of 16. Issued by one thread.
+__device__ __forceinline__ void gemm_128xN(uint32_t tmem_d, uint32_t a_base, uint32_t b_base, int K, int N,
+                                           bool accumulate) {
+  const uint32_t idesc = idesc_bf16(128, N);
+  for (int k = 0; k < K; k += 16) {
+    const uint64_t ad = kmajor_desc(a_base + (uint32_t)(k / 8) * 128u, 128u, (uint32_t)K * 16u);
+    const uint64_t bd = kmajor_desc(b_base + (uint32_t)(k / 8) * 128u, 128u, (uint32_t)K * 16u);
+    mma_bf16(tmem_d, ad, bd, idesc, (accumulate || k > 0) ? 1u : 0u);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------------- TMEM -> regs
+// 16 consecutive FP32 columns of this thread's lane (32x32b shape: warp w reads lanes 32w .. 32w+31).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %2, %1;" : "=r"(r) : "f"(a), "f"(b));
+  return r;
+}
+
+__device__ __forceinline__ float bf16_round(float a) { return __bfloat162float(__float2bfloat16_rn(a)); }
+
+// Split-BF16 pair of two values: hi = bf16(a), lo = bf16(a - hi), packed as (a, b) pairs.
+__device__ __forceinline__ void split_pack(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const float ah = bf16_round(a), bh = bf16_round(b);
+  hi = pack_bf16(ah, bh);
+  lo = pack_bf16(a - ah, b - bh);
+}
+
+// D [128 x N] = A B^T with split-BF16 operands (A = Ah + Al, B = Bh + Bl): Ah Bh + Ah Bl + Al Bh, FP32 accumulation.
+// Relative error about 2^-16, against 2^-8 for one BF16 product. Issued by one thread.
+__device__ __forceinline__ void gemm3_128xN(uint32_t tmem_d, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi,
+                                            uint32_t b_lo, int K, int N) {
+  gemm_128xN(tmem_d, a_hi, b_hi, K, N, false);
+  gemm_128xN(tmem_d, a_hi, b_lo, K, N, true);
+  gemm_128xN(tmem_d, a_lo, b_hi, K, N, true);
+}
+
+// Prefetch bytes of global memory into L2 (bulk, no shared-memory destination).
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+}  // namespace tc
+}  // namespace ffno

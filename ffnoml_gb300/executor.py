@@ -49,6 +49,32 @@ def _wbig(wr, wi):
     return torch.cat([torch.cat([wr, wi], 1), torch.cat([-wi, wr], 1)], 0).contiguous()
 
 
+def pack_kmajor(w):
+    """A [R][K] matrix (a Conv3d weight [out][in]) as BF16 in the tensor-core canonical K-major order: 8 x 8 core
+    matrices, each 8 rows x 16 bytes, the K-blocks of one 8-row group adjacent."""
+    R, K = w.shape
+    if R % 8 or K % 8:
+        raise ValueError("tensor-core operands need dimensions that are multiples of 8")
+    return w.detach().float().reshape(R // 8, 8, K // 8, 8).permute(0, 2, 1, 3).contiguous().to(torch.bfloat16)
+
+
+def _w(conv):
+    """Conv3d weight as the [out][in] matrix M of out = in @ M^T."""
+    return conv.weight.detach()[:, :, 0, 0, 0].float()
+
+
+def tc_pack(device, *mats):
+    """Split-BF16 packs of matrices [R][K] back to back: per matrix hi = bf16(M) then lo = bf16(M - hi), each in the
+    canonical K-major order (the layout the tensor-core kernels bulk-copy into shared memory)."""
+    parts = []
+    for m in mats:
+        m = m.detach().float().cpu()
+        hi = m.to(torch.bfloat16)
+        lo = (m - hi.float()).to(torch.bfloat16)
+        parts += [pack_kmajor(hi.float()).reshape(-1), pack_kmajor(lo.float()).reshape(-1)]
+    return torch.cat(parts).to(device).contiguous()
+
+
 class Packed:
     """Device copies of one model's weights in kernel layouts (and their transposes for the VJP)."""
 
@@ -59,6 +85,7 @@ class Packed:
         self.lift_w = dev(model.lift[0].weight.detach()[:, :, 0, 0, 0].t())          # [cin][C]
         self.lift_g, self.lift_b = dev(model.lift[1].weight.detach()), dev(model.lift[1].bias.detach())
         self.groups = model.lift[1].num_groups
+        self.tc = bool(nat.lib().ffno_tc_width_supported(C)) and self.groups == 8
         self.blocks = []
         for b in model.blocks:
             s, v = b.spec, b.vertical
@@ -82,6 +109,8 @@ class Packed:
                 pk[n + "_g"] = dev(norm.weight.detach())
                 pk[n + "_b"] = dev(norm.bias.detach())
             pk["res"] = (float(b.res_fused.detach()), float(b.res_pw.detach()), float(b.res_mlp.detach()))
+            if self.tc:
+                self._tc_block(pk, b, device)
             self.blocks.append(pk)
         nh = model.proj2.out_channels
         self.nh = nh
@@ -99,6 +128,25 @@ class Packed:
         self.b2 = dev(b2)
         self.head = self._head_params(model)
         self.freq_params = {k: v.detach().cpu() for k, v in model.state_dict().items() if ".freq_" in k}
+
+    @staticmethod
+    def _tc_block(pk, b, device):
+        """Split-BF16 packs of one block for the tensor-core kernels (matrix order of each entry point)."""
+        s, v = b.spec, b.vertical
+        for name, (c1, c2) in dict(s_post=(s.post[0], s.post[2]), v_post=(v.post[0], v.post[2]),
+                                   pw=(b.pw[0], b.pw[2]), mlp=(b.mlp.net[0], b.mlp.net[3])).items():
+            w1, w2 = _w(c1), _w(c2)
+            pk["tc_" + name] = tc_pack(device, w1, w2)
+            pk["tcb_" + name] = tc_pack(device, w1, w2.t(), w1.t())
+        for name, gate in (("s_gate", s.input_gate), ("v_gate", v.input_gate)):
+            g1, g2 = _w(gate[0]), _w(gate[2])
+            pk["tc_" + name] = tc_pack(device, g1, g2)
+            pk["tcb_" + name] = tc_pack(device, g1, g2, g2.t(), g1.t())
+        bg0, bg2, f0, f2 = _w(b.branch_gate[0]), _w(b.branch_gate[2]), _w(b.fuse[0]), _w(b.fuse[2])
+        pk["tc_fuse1"] = tc_pack(device, bg0, bg2)
+        pk["tc_fuse2"] = tc_pack(device, f0, f2)
+        pk["tcb_fuse_a"] = tc_pack(device, f0, f2.t())
+        pk["tcb_fuse_b"] = tc_pack(device, f0.t(), bg2.t(), bg0.t())
 
     @staticmethod
     def _head_params(model):
@@ -161,9 +209,12 @@ class Workspace:
         f32 = dict(dtype=torch.float32, device=device)
         self.V = V
         self.nparts = nat.lib().ffno_stats_parts(V)
+        self.nparts_tc = nat.lib().ffno_tc_parts(V)
         nb = lambda *s: torch.empty(*s, **f32)
         self.dw = nb(V)
-        self.partials = torch.empty(max(self.nparts, 1) * groups * 3, dtype=torch.float64, device=device)
+        self.partials = torch.empty(max(self.nparts, self.nparts_tc, 1) * groups * 3, dtype=torch.float64,
+                                    device=device)
+        self.err = torch.zeros(1, dtype=torch.int32, device=device)
         self.coefs = {n: nb(3 * C) for n in ("lift",) + NORMS}
         self.gstats = {n: torch.empty(groups * 3, dtype=torch.float64, device=device) for n in ("lift",) + NORMS}
         for n in ("x", "pre", "xs", "xv", "ys", "yv", "spec_pre", "vert_pre", "fused_pre", "pw_pre", "mlp_pre",
@@ -171,6 +222,7 @@ class Workspace:
             setattr(self, n, nb(V, C))
         spec_len = D * 2 * H * Wf * C
         self.sa, self.sb = nb(spec_len), nb(spec_len)
+        self.gates = nb(V, 2 * C)     # branch gates between the two tensor-core fuse stages
         self.va, self.vb = nb(2 * live * HW * C), nb(2 * live * HW * C)
 
 
@@ -298,15 +350,22 @@ class Executor:
             self._head(pk, ws.x, xin, out[b])
             if keep:
                 saved.append(inputs)
+        self._check(ws)
         state = dict(x=x, z=z_scale, dx=dx, dy=dy, inputs=saved, geo=geo) if keep else None
         return out, state
+
+    @staticmethod
+    def _check(ws):
+        if m_err := int(ws.err.item()):
+            raise nat.NativeError(f"a tensor-core kernel's bounded wait ran out (code {m_err})")
 
     def _depth_weights(self, ws, z, D, HW):
         nat.call("ffno_depth_weights", z.data_ptr(), D, HW, ws.dw.data_ptr(), _stream())
 
-    def _finalize(self, ws, name, gamma, beta):
+    def _finalize(self, ws, name, gamma, beta, tc=False):
         m = self.model
-        nat.call("ffno_gn_finalize", ws.partials.data_ptr(), ws.nparts, m.width, self._packed.groups,
+        nat.call("ffno_gn_finalize", ws.partials.data_ptr(), ws.nparts_tc if tc else ws.nparts, m.width,
+                 self._packed.groups,
                  gamma.data_ptr(), beta.data_ptr(), EPS, ws.coefs[name].data_ptr(), ws.gstats[name].data_ptr(),
                  _stream())
 
@@ -328,10 +387,16 @@ class Executor:
         x = ws.x if x_in is None else x_in
         live = hgt["live"]
         d = _descs(D, H, W, C, live)
-        nat.call("ffno_gate_fwd", x.data_ptr(), V, C, bp["s_g1"].data_ptr(), bp["s_g2"].data_ptr(), None, None,
-                 ws.xs.data_ptr(), s)
-        nat.call("ffno_gate_fwd", x.data_ptr(), V, C, bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(),
-                 bp["v_zp"].data_ptr(), z.data_ptr(), ws.xv.data_ptr(), s)
+        if self._tc():
+            nat.call("ffno_gate_fwd_tc", x.data_ptr(), V, C, bp["tc_s_gate"].data_ptr(), None, None, ws.xs.data_ptr(),
+                     ws.err.data_ptr(), s)
+            nat.call("ffno_gate_fwd_tc", x.data_ptr(), V, C, bp["tc_v_gate"].data_ptr(), bp["v_zp"].data_ptr(),
+                     z.data_ptr(), ws.xv.data_ptr(), ws.err.data_ptr(), s)
+        else:
+            nat.call("ffno_gate_fwd", x.data_ptr(), V, C, bp["s_g1"].data_ptr(), bp["s_g2"].data_ptr(), None, None,
+                     ws.xs.data_ptr(), s)
+            nat.call("ffno_gate_fwd", x.data_ptr(), V, C, bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(),
+                     bp["v_zp"].data_ptr(), z.data_ptr(), ws.xv.data_ptr(), s)
         # horizontal spectral branch: rfft2 -> mix -> irfft2 as contractions
         nat.call("ffno_xform", pln["twf"].data_ptr(), ws.xs.data_ptr(), ws.sa.data_ptr(), d["wf"], 0, s)
         nat.call("ffno_xform", pln["thf"].data_ptr(), ws.sa.data_ptr(), ws.sb.data_ptr(), d["hf"], 0, s)
@@ -339,35 +404,65 @@ class Executor:
                  bp["s_wbig"].data_ptr(), fq.g.data_ptr(), _ptr(fq.u), _ptr(fq.v), m.freq_mix_rank, s)
         nat.call("ffno_xform", pln["thi"].data_ptr(), ws.sa.data_ptr(), ws.sb.data_ptr(), d["hf"], 0, s)
         nat.call("ffno_xform", pln["twi"].data_ptr(), ws.sb.data_ptr(), ws.ys.data_ptr(), d["wi"], 0, s)
-        nat.call("ffno_mlp2_fwd", 0, ws.ys.data_ptr(), None, None, 0.0, None, V, C, bp["s_p1"].data_ptr(),
-                 bp["s_p2"].data_ptr(), ws.dw.data_ptr(), ws.spec_pre.data_ptr(), ws.partials.data_ptr(), P, G, s)
-        self._finalize(ws, "spec", bp["spec_g"], bp["spec_b"])
+        tc = self._mlp2(ws, 0, ws.ys, None, None, 0.0, None, bp["s_p1"], bp["s_p2"], bp.get("tc_s_post"),
+                        ws.spec_pre)
+        self._finalize(ws, "spec", bp["spec_g"], bp["spec_b"], tc)
         # vertical (height) branch
         hq = hgt["freq"][i]
         nat.call("ffno_xform", hgt["tzf"].data_ptr(), ws.xv.data_ptr(), ws.va.data_ptr(), d["zf"], 0, s)
         nat.call("ffno_spectral_mix", ws.va.data_ptr(), ws.vb.data_ptr(), live, HW, HW * C, C, live * HW * C, C,
                  bp["v_wbig"].data_ptr(), hq.g.data_ptr(), _ptr(hq.u), _ptr(hq.v), m.freq_mix_rank, s)
         nat.call("ffno_xform", hgt["tzi"].data_ptr(), ws.vb.data_ptr(), ws.yv.data_ptr(), d["zi"], 0, s)
-        nat.call("ffno_mlp2_fwd", 0, ws.yv.data_ptr(), None, None, 0.0, None, V, C, bp["v_p1"].data_ptr(),
-                 bp["v_p2"].data_ptr(), ws.dw.data_ptr(), ws.vert_pre.data_ptr(), ws.partials.data_ptr(), P, G, s)
-        self._finalize(ws, "vert", bp["vert_g"], bp["vert_b"])
+        tc = self._mlp2(ws, 0, ws.yv, None, None, 0.0, None, bp["v_p1"], bp["v_p2"], bp.get("tc_v_post"),
+                        ws.vert_pre)
+        self._finalize(ws, "vert", bp["vert_g"], bp["vert_b"], tc)
         # gate + fuse
-        nat.call("ffno_fuse_fwd", x.data_ptr(), ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(),
-                 ws.vert_pre.data_ptr(), ws.coefs["vert"].data_ptr(), V, C, bp["bg1"].data_ptr(),
-                 bp["bg2"].data_ptr(), bp["bgb"].data_ptr(), bp["f1"].data_ptr(), bp["f2"].data_ptr(),
-                 ws.dw.data_ptr(), ws.fused_pre.data_ptr(), ws.partials.data_ptr(), P, G, s)
-        self._finalize(ws, "fuse", bp["fuse_g"], bp["fuse_b"])
+        if self._tc():
+            self._fuse1_tc(ws, bp, x, None)
+            nat.call("ffno_fuse2_tc", ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(), ws.vert_pre.data_ptr(),
+                     ws.coefs["vert"].data_ptr(), ws.gates.data_ptr(), V, C, bp["tc_fuse2"].data_ptr(),
+                     ws.dw.data_ptr(), ws.fused_pre.data_ptr(), ws.partials.data_ptr(), ws.nparts_tc, G,
+                     ws.err.data_ptr(), s)
+            self._finalize(ws, "fuse", bp["fuse_g"], bp["fuse_b"], True)
+        else:
+            nat.call("ffno_fuse_fwd", x.data_ptr(), ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(),
+                     ws.vert_pre.data_ptr(), ws.coefs["vert"].data_ptr(), V, C, bp["bg1"].data_ptr(),
+                     bp["bg2"].data_ptr(), bp["bgb"].data_ptr(), bp["f1"].data_ptr(), bp["f2"].data_ptr(),
+                     ws.dw.data_ptr(), ws.fused_pre.data_ptr(), ws.partials.data_ptr(), P, G, s)
+            self._finalize(ws, "fuse", bp["fuse_g"], bp["fuse_b"])
         r_f, r_pw, r_mlp = bp["res"]
-        nat.call("ffno_mlp2_fwd", 1, x.data_ptr(), ws.fused_pre.data_ptr(), ws.coefs["fuse"].data_ptr(), r_f,
-                 ws.x1.data_ptr(), V, C, bp["pw1"].data_ptr(), bp["pw2"].data_ptr(), ws.dw.data_ptr(),
-                 ws.pw_pre.data_ptr(), ws.partials.data_ptr(), P, G, s)
-        self._finalize(ws, "pw", bp["pw_g"], bp["pw_b"])
-        nat.call("ffno_mlp2_fwd", 2, ws.x1.data_ptr(), ws.pw_pre.data_ptr(), ws.coefs["pw"].data_ptr(), r_pw,
-                 ws.x2.data_ptr(), V, C, bp["m1"].data_ptr(), bp["m2"].data_ptr(), ws.dw.data_ptr(),
-                 ws.mlp_pre.data_ptr(), ws.partials.data_ptr(), P, G, s)
-        self._finalize(ws, "mlp", bp["mlp_g"], bp["mlp_b"])
+        tc = self._mlp2(ws, 1, x, ws.fused_pre, ws.coefs["fuse"], r_f, ws.x1, bp["pw1"], bp["pw2"], bp.get("tc_pw"),
+                        ws.pw_pre)
+        self._finalize(ws, "pw", bp["pw_g"], bp["pw_b"], tc)
+        tc = self._mlp2(ws, 2, ws.x1, ws.pw_pre, ws.coefs["pw"], r_pw, ws.x2, bp["m1"], bp["m2"], bp.get("tc_mlp"),
+                        ws.mlp_pre)
+        self._finalize(ws, "mlp", bp["mlp_g"], bp["mlp_b"], tc)
         nat.call("ffno_resid_out", ws.x2.data_ptr(), ws.mlp_pre.data_ptr(), ws.coefs["mlp"].data_ptr(), r_mlp, V, C,
                  ws.x.data_ptr(), s)
+
+    def _tc(self):
+        """Whether the split-BF16 tensor-core kernels run (precision 'bf16' at a width they support)."""
+        return self.model.precision == "bf16" and self._packed.tc
+
+    def _fuse1_tc(self, ws, bp, x, hg):
+        m = self.model
+        nat.call("ffno_fuse1_tc", x.data_ptr(), ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(),
+                 ws.vert_pre.data_ptr(), ws.coefs["vert"].data_ptr(), ws.V, m.width, bp["tc_fuse1"].data_ptr(),
+                 bp["bgb"].data_ptr(), ws.gates.data_ptr(), _ptr(hg), ws.err.data_ptr(), _stream())
+
+    def _mlp2(self, ws, mode, inp, prev, pcoefs, res, xout, w1, w2, pack, pre):
+        """ffno_mlp2_fwd (FP32) or its tensor-core twin; returns whether the tensor-core path ran."""
+        m = self.model
+        C, V, s, G = m.width, ws.V, _stream(), self._packed.groups
+        if self._tc():
+            nat.call("ffno_mlp2_fwd_tc", mode, inp.data_ptr(), _ptr(prev), _ptr(pcoefs), res, _ptr(xout), V, C,
+                     pack.data_ptr(), ws.dw.data_ptr(), pre.data_ptr(), ws.partials.data_ptr(), ws.nparts_tc, G,
+                     ws.err.data_ptr(), s)
+            return True
+        nat.call("ffno_mlp2_fwd", mode, inp.data_ptr(), _ptr(prev), _ptr(pcoefs), res, _ptr(xout), V, C,
+                 w1.data_ptr(), w2.data_ptr(), ws.dw.data_ptr(), pre.data_ptr(), ws.partials.data_ptr(), ws.nparts,
+                 G, s)
+        return False
 
     def _head(self, pk, x, xin, out):
         m = self.model
@@ -414,6 +509,7 @@ class Executor:
         gcol = tb.height_tables_vjp(geo.column_raw, geo.length, geo.k, live, tzf_bar.cpu().numpy(),
                                     tzi_bar.cpu().numpy())
         zbar[0, :, 0, 0] += torch.as_tensor(gcol, dtype=torch.float32, device=dev)
+        self._check(ws)
         return xbar_in, zbar
 
     def _gn_bwd(self, ws, gb, mode, u, r, pre, gamma, beta, name, pbar):
@@ -437,28 +533,46 @@ class Executor:
         r_f, r_pw, r_mlp = bp["res"]
         live = hgt["live"]
         d = _descs(D, H, W, C, live)
+        tc = self._tc()
+        err = ws.err.data_ptr()
+
+        def mlp_bwd(a, pb, base, out, w1, w2t, w1t, pack):
+            if tc:
+                nat.call("ffno_mlp2_bwd_tc", a.data_ptr(), pb.data_ptr(), _ptr(base), V, C, bp[pack].data_ptr(),
+                         out.data_ptr(), err, s)
+            else:
+                nat.call("ffno_mlp2_bwd", a.data_ptr(), pb.data_ptr(), _ptr(base), V, C, bp[w1].data_ptr(),
+                         bp[w2t].data_ptr(), bp[w1t].data_ptr(), out.data_ptr(), s)
+
         # out = x2 + r_mlp GN(mlp_pre); mlp_pre = mlp(x2)
         self._gn_bwd(ws, gb, 0, gb.xbar, r_mlp, ws.mlp_pre, bp["mlp_g"], bp["mlp_b"], "mlp", gb.pbar)
-        nat.call("ffno_mlp2_bwd", ws.x2.data_ptr(), gb.pbar.data_ptr(), gb.xbar.data_ptr(), V, C, bp["m1"].data_ptr(),
-                 bp["m2t"].data_ptr(), bp["m1t"].data_ptr(), gb.g2.data_ptr(), s)
+        mlp_bwd(ws.x2, gb.pbar, gb.xbar, gb.g2, "m1", "m2t", "m1t", "tcb_mlp")
         # x2 = x1 + r_pw GN(pw_pre); pw_pre = pw(x1)
         self._gn_bwd(ws, gb, 0, gb.g2, r_pw, ws.pw_pre, bp["pw_g"], bp["pw_b"], "pw", gb.pbar)
-        nat.call("ffno_mlp2_bwd", ws.x1.data_ptr(), gb.pbar.data_ptr(), gb.g2.data_ptr(), V, C,
-                 bp["pw1"].data_ptr(), bp["pw2t"].data_ptr(), bp["pw1t"].data_ptr(), gb.g1.data_ptr(), s)
+        mlp_bwd(ws.x1, gb.pbar, gb.g2, gb.g1, "pw1", "pw2t", "pw1t", "tcb_pw")
         # x1 = x + r_f gelu(GN(fused_pre)); fused_pre = fuse(x, spec, vert)
         self._gn_bwd(ws, gb, 1, gb.g1, r_f, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], "fuse", gb.pbar)
-        nat.call("ffno_fuse_bwd", x.data_ptr(), ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(),
-                 ws.vert_pre.data_ptr(), ws.coefs["vert"].data_ptr(), gb.pbar.data_ptr(), gb.g1.data_ptr(), V, C,
-                 bp["bg1"].data_ptr(), bp["bg2"].data_ptr(), bp["bgb"].data_ptr(), bp["f1"].data_ptr(),
-                 bp["f2t"].data_ptr(), bp["f1t"].data_ptr(), bp["bg2t"].data_ptr(), bp["bg1t"].data_ptr(),
-                 gb.xacc.data_ptr(), gb.sbar.data_ptr(), gb.vbar.data_ptr(), s)
+        if tc:
+            self._fuse1_tc(ws, bp, x, gb.hg)
+            cs, cv = ws.coefs["spec"].data_ptr(), ws.coefs["vert"].data_ptr()
+            nat.call("ffno_fuse_bwd_a_tc", ws.spec_pre.data_ptr(), cs, ws.vert_pre.data_ptr(), cv,
+                     ws.gates.data_ptr(), gb.pbar.data_ptr(), V, C, bp["tcb_fuse_a"].data_ptr(), gb.hfb.data_ptr(),
+                     err, s)
+            nat.call("ffno_fuse_bwd_b_tc", ws.spec_pre.data_ptr(), cs, ws.vert_pre.data_ptr(), cv,
+                     ws.gates.data_ptr(), gb.hg.data_ptr(), gb.pbar.data_ptr(), gb.hfb.data_ptr(), gb.g1.data_ptr(),
+                     V, C, bp["tcb_fuse_b"].data_ptr(), gb.xacc.data_ptr(), gb.sbar.data_ptr(), gb.vbar.data_ptr(),
+                     err, s)
+        else:
+            nat.call("ffno_fuse_bwd", x.data_ptr(), ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(),
+                     ws.vert_pre.data_ptr(), ws.coefs["vert"].data_ptr(), gb.pbar.data_ptr(), gb.g1.data_ptr(), V, C,
+                     bp["bg1"].data_ptr(), bp["bg2"].data_ptr(), bp["bgb"].data_ptr(), bp["f1"].data_ptr(),
+                     bp["f2t"].data_ptr(), bp["f1t"].data_ptr(), bp["bg2t"].data_ptr(), bp["bg1t"].data_ptr(),
+                     gb.xacc.data_ptr(), gb.sbar.data_ptr(), gb.vbar.data_ptr(), s)
         # spec = gelu(GN(spec_pre)), spec_pre = post_s(ys); vert likewise
         self._gn_bwd(ws, gb, 1, gb.sbar, 1.0, ws.spec_pre, bp["spec_g"], bp["spec_b"], "spec", gb.pbar)
-        nat.call("ffno_mlp2_bwd", ws.ys.data_ptr(), gb.pbar.data_ptr(), None, V, C, bp["s_p1"].data_ptr(),
-                 bp["s_p2t"].data_ptr(), bp["s_p1t"].data_ptr(), gb.ysb.data_ptr(), s)
+        mlp_bwd(ws.ys, gb.pbar, None, gb.ysb, "s_p1", "s_p2t", "s_p1t", "tcb_s_post")
         self._gn_bwd(ws, gb, 1, gb.vbar, 1.0, ws.vert_pre, bp["vert_g"], bp["vert_b"], "vert", gb.pbar)
-        nat.call("ffno_mlp2_bwd", ws.yv.data_ptr(), gb.pbar.data_ptr(), None, V, C, bp["v_p1"].data_ptr(),
-                 bp["v_p2t"].data_ptr(), bp["v_p1t"].data_ptr(), gb.yvb.data_ptr(), s)
+        mlp_bwd(ws.yv, gb.pbar, None, gb.yvb, "v_p1", "v_p2t", "v_p1t", "tcb_v_post")
         # horizontal transposes: ys = twi thi mix thf twf xs  ->  xs_bar = twf^T thf^T mix^T thi^T twi^T ys_bar
         nat.call("ffno_xform", pln["twi_t"].data_ptr(), gb.ysb.data_ptr(), ws.sa.data_ptr(), d["wf"], 0, s)
         nat.call("ffno_xform", pln["thi_t"].data_ptr(), ws.sa.data_ptr(), ws.sb.data_ptr(), d["hf"], 0, s)
@@ -478,18 +592,25 @@ class Executor:
                  gb.osplit_f, tzf_bar.data_ptr(), 1, s)
         nat.call("ffno_xform", hgt["tzf_t"].data_ptr(), ws.vb.data_ptr(), gb.xvb.data_ptr(), d["zi"], 0, s)
         # input gates (and z_proj)
-        nat.call("ffno_gate_bwd", x.data_ptr(), gb.xsb.data_ptr(), gb.xvb.data_ptr(), gb.xacc.data_ptr(), V, C,
-                 bp["s_g1"].data_ptr(), bp["s_g2"].data_ptr(), bp["s_g2t"].data_ptr(), bp["s_g1t"].data_ptr(),
-                 bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(), bp["v_g2t"].data_ptr(), bp["v_g1t"].data_ptr(),
-                 bp["v_zp"].data_ptr(), gb.xbar.data_ptr(), zbar.data_ptr(), s)
+        if tc:
+            nat.call("ffno_gate_bwd_tc", x.data_ptr(), gb.xsb.data_ptr(), gb.xacc.data_ptr(), V, C,
+                     bp["tcb_s_gate"].data_ptr(), None, gb.xbar.data_ptr(), None, err, s)
+            nat.call("ffno_gate_bwd_tc", x.data_ptr(), gb.xvb.data_ptr(), gb.xbar.data_ptr(), V, C,
+                     bp["tcb_v_gate"].data_ptr(), bp["v_zp"].data_ptr(), gb.xbar.data_ptr(), zbar.data_ptr(), err, s)
+        else:
+            nat.call("ffno_gate_bwd", x.data_ptr(), gb.xsb.data_ptr(), gb.xvb.data_ptr(), gb.xacc.data_ptr(), V, C,
+                     bp["s_g1"].data_ptr(), bp["s_g2"].data_ptr(), bp["s_g2t"].data_ptr(), bp["s_g1t"].data_ptr(),
+                     bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(), bp["v_g2t"].data_ptr(), bp["v_g1t"].data_ptr(),
+                     bp["v_zp"].data_ptr(), gb.xbar.data_ptr(), zbar.data_ptr(), s)
 
 
 class _GradBuffers:
     def __init__(self, D, H, W, C, live, groups, nparts, device):
         V = D * H * W
         f32 = dict(dtype=torch.float32, device=device)
-        for n in ("xbar", "g2", "g1", "xacc", "sbar", "vbar", "pbar", "ysb", "yvb", "xsb", "xvb"):
+        for n in ("xbar", "g2", "g1", "xacc", "sbar", "vbar", "pbar", "ysb", "yvb", "xsb", "xvb", "hg"):
             setattr(self, n, torch.empty(V, C, **f32))
+        self.hfb = torch.empty(V, 2 * C, **f32)
         self.wbar = torch.zeros(V, **f32)
         self.bpart = torch.empty(max(nparts, 1) * groups * 2, dtype=torch.float64, device=device)
         self.sums = torch.empty(groups * 2, dtype=torch.float64, device=device)

@@ -221,6 +221,59 @@ int ffno_si_population_cotangent(const float* y, const float* pop_bar, long V, i
 int ffno_si_input_grads(const float* features, const float* x_bar, const float* z_bar_mm, long V, const float* std_x,
                         float* features_bar, float* z_bar_m, int* flags, ffno_stream_t stream);
 
+/* ------------------------------------------------------------------------------------------------------------------
+ * Tensor-core (tcgen05) kernels in split-BF16: each GEMM operand x is carried as hi = bf16(x), lo = bf16(x - hi) and
+ * each product as hi*hi + hi*lo + lo*hi on the BF16 tensor cores with FP32 accumulation in tensor memory. FP32
+ * activations and statistics in HBM, so each has the contract of the FP32 entry point (or stage) it names. Weights
+ * come pre-packed in `wpack` (16-byte aligned): for each matrix, in the order listed, its hi then its lo half, each
+ * [R][K] BF16 in the canonical K-major core-matrix order (8 x 8 blocks; the 8 rows of a block 16 bytes apart; the
+ * K-blocks of one 8-row group 128 bytes apart; row groups K*16 bytes apart). The matrix of a GEMM out = in @ M^T is
+ * M [out][in] (a Conv3d weight, or a transposed one in the backward). err: one device int, set non-zero if a bounded
+ * wait ran out. Widths C = 16, 32, 64. Statistics partials: nparts = ffno_tc_parts(V).
+ * ------------------------------------------------------------------------------------------------------------------ */
+int ffno_tc_parts(long V);
+int ffno_tc_width_supported(int C);
+
+/* ffno_mlp2_fwd; wpack = [w1 (2C x C), w2 (C x 2C)]. */
+int ffno_mlp2_fwd_tc(int mode, const float* in, const float* prev_pre, const float* prev_coefs, float res, float* xout,
+                     long V, int C, const void* wpack, const float* dw, float* pre, double* partials, int nparts,
+                     int groups, int* err, ffno_stream_t stream);
+/* ffno_gate_fwd for one branch; wpack = [g1, g2] (C x C). */
+int ffno_gate_fwd_tc(const float* x, long V, int C, const void* wpack, const float* zp, const float* z, float* out,
+                     int* err, ffno_stream_t stream);
+/* First stage of ffno_fuse_fwd: gates [V][2C] = sigmoid(gelu([x, spec, vert] wg1^T) wg2^T + bias), and (if hg is not
+ * NULL) the hidden pre-activation hg [V][C]; wpack = [wg1 (C x 3C), wg2 (2C x C)]. */
+int ffno_fuse1_tc(const float* x, const float* spec_pre, const float* spec_coefs, const float* vert_pre,
+                  const float* vert_coefs, long V, int C, const void* wpack, const float* bias, float* gates,
+                  float* hg, int* err, ffno_stream_t stream);
+/* Second stage of ffno_fuse_fwd: pre = gelu(B wf1^T) wf2^T + (B[:, :C] + B[:, C:]) / 2, B = [spec gs, vert gv], with
+ * GroupNorm partials; wpack = [wf1 (2C x 2C), wf2 (C x 2C)]. */
+int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
+                  const float* gates, long V, int C, const void* wpack, const float* dw, float* pre, double* partials,
+                  int nparts, int groups, int* err, ffno_stream_t stream);
+/* ffno_mlp2_bwd; wpack = [w1 (2C x C), w2^T (2C x C), w1^T (C x 2C)]. */
+int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack,
+                     float* a_bar, int* err, ffno_stream_t stream);
+/* One branch of ffno_gate_bwd: x_bar = base + d/dx applied to g_bar, z_bar += g_bar . zp if zp; wpack = [g1, g2,
+ * g2^T, g1^T]. base may equal x_bar. */
+int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long V, int C, const void* wpack,
+                     const float* zp, float* x_bar, float* z_bar, int* err, ffno_stream_t stream);
+/* ffno_fuse_bwd in two stages after ffno_fuse1_tc has recomputed gates and hg:
+ * a: hf_bar [V][2C] = (fused_pre_bar wf2) * gelu'(B wf1^T); wpack = [wf1 (2C x 2C), wf2^T (2C x C)]
+ * b: the rest, writing x_bar, spec_bar, vert_bar; wpack = [wf1^T (2C x 2C), wg2^T (C x 2C), wg1^T (3C x C)]. */
+int ffno_fuse_bwd_a_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
+                       const float* gates, const float* fused_pre_bar, long V, int C, const void* wpack,
+                       float* hf_bar, int* err, ffno_stream_t stream);
+int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
+                       const float* gates, const float* hg, const float* fused_pre_bar, const float* hf_bar,
+                       const float* base, long V, int C, const void* wpack, float* x_bar, float* spec_bar,
+                       float* vert_bar, int* err, ffno_stream_t stream);
+
+/* Self-test of the tensor-core primitives (no reference counterpart: it pins this library's tcgen05 descriptor and
+ * tensor-memory conventions): D [128][N] = bf16(A [128][K]) @ bf16(B [N][K])^T in FP32, one CTA; K, N multiples of 16
+ * up to 256. *status (device int) is set to 1 if the MMA completion wait ran out. */
+int ffno_tc_selftest(const float* A, const float* B, int K, int N, float* D, int* status, ffno_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,223 @@
+"""Each split-BF16 tensor-core kernel against its FP32 counterpart, through the C ABI, on a ragged voxel count (V not
+a multiple of the 128-voxel tile). Split-BF16 products carry ~2^-16 relative error, so the bar is 2e-4 relative."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+V = 1000
+G = 8
+
+
+def _nat():
+    from ffnoml_gb300 import _native as nat
+    return nat
+
+
+def _s():
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _rand(*shape, seed=0, scale=1.0):
+    g = torch.Generator().manual_seed(seed)
+    return (torch.randn(*shape, generator=g) * scale).cuda().contiguous()
+
+
+_KEEP = []
+
+
+def _hold(t):
+    """data_ptr of a tensor kept alive until the test ends (kernels run asynchronously after the call returns)."""
+    _KEEP.append(t)
+    return t.data_ptr()
+
+
+@pytest.fixture(autouse=True)
+def _release():
+    yield
+    torch.cuda.synchronize()
+    _KEEP.clear()
+
+
+def _close(a, b, tol=2e-4):
+    err = ((a - b).abs().max() / b.abs().max().clamp_min(1e-12)).item()
+    assert err < tol, err
+
+
+class _Packed:
+    def __init__(self, t):
+        self.t = t
+
+    def data_ptr(self):
+        return _hold(self.t)
+
+
+def _pack(*mats):
+    from ffnoml_gb300.executor import tc_pack
+    return _Packed(tc_pack(torch.device("cuda"), *[m.cpu() for m in mats]))
+
+
+def _coefs(C, seed):
+    g = torch.Generator().manual_seed(seed)
+    c = torch.stack([torch.randn(C, generator=g) * 0.1, 1 + 0.2 * torch.randn(C, generator=g),
+                     0.1 * torch.randn(C, generator=g)])
+    return c.reshape(-1).cuda().contiguous()
+
+
+@pytest.mark.parametrize("C", [16, 32, 64])
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_mlp2_fwd_tc(C, mode):
+    nat = _nat()
+    x, prev = _rand(V, C, seed=1), _rand(V, C, seed=2)
+    pc = _coefs(C, 3)
+    w1, w2 = _rand(2 * C, C, seed=4, scale=C ** -0.5), _rand(C, 2 * C, seed=5, scale=(2 * C) ** -0.5)
+    dw = (1 + 0.1 * _rand(V, seed=6)).contiguous()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    outs = []
+    for tc in (False, True):
+        pre, xo = torch.empty(V, C, device="cuda"), torch.zeros(V, C, device="cuda")
+        P = nat.lib().ffno_tc_parts(V) if tc else nat.lib().ffno_stats_parts(V)
+        part = torch.empty(P * G * 3, dtype=torch.float64, device="cuda")
+        coefs = torch.empty(3 * C, device="cuda")
+        gst = torch.empty(G * 3, dtype=torch.float64, device="cuda")
+        args = (mode, x.data_ptr(), prev.data_ptr(), pc.data_ptr(), 0.7, xo.data_ptr(), V, C)
+        if tc:
+            nat.call("ffno_mlp2_fwd_tc", *args, _pack(w1, w2).data_ptr(), dw.data_ptr(), pre.data_ptr(),
+                     part.data_ptr(), P, G, err.data_ptr(), _s())
+        else:
+            nat.call("ffno_mlp2_fwd", *args, _hold(w1.t().contiguous()), _hold(w2.t().contiguous()),
+                     dw.data_ptr(), pre.data_ptr(), part.data_ptr(), P, G, _s())
+        ones = torch.ones(C, device="cuda")
+        zeros = torch.zeros(C, device="cuda")
+        nat.call("ffno_gn_finalize", part.data_ptr(), P, C, G, ones.data_ptr(), zeros.data_ptr(), 1e-5,
+                 coefs.data_ptr(), gst.data_ptr(), _s())
+        torch.cuda.synchronize()
+        outs.append((pre, xo, gst))
+    assert int(err.item()) == 0
+    _close(outs[1][0], outs[0][0])
+    if mode:
+        _close(outs[1][1], outs[0][1], 1e-6)
+    assert torch.allclose(outs[1][2], outs[0][2], rtol=1e-4, atol=1e-6)
+
+
+@pytest.mark.parametrize("C", [16, 32, 64])
+@pytest.mark.parametrize("with_z", [False, True])
+def test_gate_fwd_tc(C, with_z):
+    nat = _nat()
+    x = _rand(V, C, seed=1)
+    g1, g2 = _rand(C, C, seed=2, scale=C ** -0.5), _rand(C, C, seed=3, scale=C ** -0.5)
+    zp, z = (_rand(C, seed=4), _rand(V, seed=5)) if with_z else (None, None)
+    ptr = lambda t: None if t is None else t.data_ptr()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    a, b = torch.empty(V, C, device="cuda"), torch.empty(V, C, device="cuda")
+    nat.call("ffno_gate_fwd", x.data_ptr(), V, C, _hold(g1.t().contiguous()), _hold(g2.t().contiguous()),
+             ptr(zp), ptr(z), a.data_ptr(), _s())
+    nat.call("ffno_gate_fwd_tc", x.data_ptr(), V, C, _pack(g1, g2).data_ptr(), ptr(zp), ptr(z), b.data_ptr(),
+             err.data_ptr(), _s())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    _close(b, a)
+
+
+def _fuse_weights(C):
+    return (_rand(C, 3 * C, seed=11, scale=(3 * C) ** -0.5), _rand(2 * C, C, seed=12, scale=C ** -0.5),
+            _rand(2 * C, seed=13), _rand(2 * C, 2 * C, seed=14, scale=(2 * C) ** -0.5),
+            _rand(C, 2 * C, seed=15, scale=(2 * C) ** -0.5))
+
+
+@pytest.mark.parametrize("C", [16, 32, 64])
+def test_fuse_fwd_tc(C):
+    nat = _nat()
+    x, sp, vp = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3)
+    sc, vc = _coefs(C, 4), _coefs(C, 5)
+    bg0, bg2, bb, f0, f2 = _fuse_weights(C)
+    dw = (1 + 0.1 * _rand(V, seed=6)).contiguous()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    P0, P1 = nat.lib().ffno_stats_parts(V), nat.lib().ffno_tc_parts(V)
+    part0 = torch.empty(P0 * G * 3, dtype=torch.float64, device="cuda")
+    part1 = torch.empty(P1 * G * 3, dtype=torch.float64, device="cuda")
+    a, b = torch.empty(V, C, device="cuda"), torch.empty(V, C, device="cuda")
+    T = lambda m: _hold(m.t().contiguous())
+    nat.call("ffno_fuse_fwd", x.data_ptr(), sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), V, C, T(bg0),
+             T(bg2), bb.data_ptr(), T(f0), T(f2), dw.data_ptr(), a.data_ptr(), part0.data_ptr(), P0, G, _s())
+    gates = torch.empty(V, 2 * C, device="cuda")
+    nat.call("ffno_fuse1_tc", x.data_ptr(), sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), V, C,
+             _pack(bg0, bg2).data_ptr(), bb.data_ptr(), gates.data_ptr(), None, err.data_ptr(), _s())
+    nat.call("ffno_fuse2_tc", sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), gates.data_ptr(), V, C,
+             _pack(f0, f2).data_ptr(), dw.data_ptr(), b.data_ptr(), part1.data_ptr(), P1, G, err.data_ptr(), _s())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    _close(b, a)
+
+
+@pytest.mark.parametrize("C", [16, 32, 64])
+def test_mlp2_bwd_tc(C):
+    nat = _nat()
+    a, pb, base = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3)
+    w1, w2 = _rand(2 * C, C, seed=4, scale=C ** -0.5), _rand(C, 2 * C, seed=5, scale=(2 * C) ** -0.5)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    r0, r1 = torch.empty(V, C, device="cuda"), torch.empty(V, C, device="cuda")
+    # FP32 kernel wants w1 [C][2C] (in x out), w2t = W2^T laid [C][2C], w1t [2C][C]
+    nat.call("ffno_mlp2_bwd", a.data_ptr(), pb.data_ptr(), base.data_ptr(), V, C, _hold(w1.t().contiguous()),
+             _hold(w2.contiguous()), _hold(w1.contiguous()), r0.data_ptr(), _s())
+    nat.call("ffno_mlp2_bwd_tc", a.data_ptr(), pb.data_ptr(), base.data_ptr(), V, C,
+             _pack(w1, w2.t(), w1.t()).data_ptr(), r1.data_ptr(), err.data_ptr(), _s())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    _close(r1, r0)
+
+
+@pytest.mark.parametrize("C", [16, 32, 64])
+def test_gate_bwd_tc(C):
+    nat = _nat()
+    x, xsb, xvb, base = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3), _rand(V, C, seed=4)
+    s1, s2 = _rand(C, C, seed=5, scale=C ** -0.5), _rand(C, C, seed=6, scale=C ** -0.5)
+    v1, v2 = _rand(C, C, seed=7, scale=C ** -0.5), _rand(C, C, seed=8, scale=C ** -0.5)
+    zp = _rand(C, seed=9)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    r0, r1 = torch.empty(V, C, device="cuda"), torch.empty(V, C, device="cuda")
+    z0, z1 = torch.zeros(V, device="cuda"), torch.zeros(V, device="cuda")
+    T = lambda m: _hold(m.t().contiguous())
+    Nn = lambda m: _hold(m.contiguous())
+    nat.call("ffno_gate_bwd", x.data_ptr(), xsb.data_ptr(), xvb.data_ptr(), base.data_ptr(), V, C, T(s1), T(s2),
+             Nn(s2), Nn(s1), T(v1), T(v2), Nn(v2), Nn(v1), zp.data_ptr(), r0.data_ptr(), z0.data_ptr(), _s())
+    nat.call("ffno_gate_bwd_tc", x.data_ptr(), xsb.data_ptr(), base.data_ptr(), V, C,
+             _pack(s1, s2, s2.t(), s1.t()).data_ptr(), None, r1.data_ptr(), None, err.data_ptr(), _s())
+    nat.call("ffno_gate_bwd_tc", x.data_ptr(), xvb.data_ptr(), r1.data_ptr(), V, C,
+             _pack(v1, v2, v2.t(), v1.t()).data_ptr(), zp.data_ptr(), r1.data_ptr(), z1.data_ptr(), err.data_ptr(),
+             _s())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    _close(r1, r0)
+    _close(z1, z0, 1e-5)
+
+
+@pytest.mark.parametrize("C", [16, 32, 64])
+def test_fuse_bwd_tc(C):
+    nat = _nat()
+    x, sp, vp = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3)
+    sc, vc = _coefs(C, 4), _coefs(C, 5)
+    fb, base = _rand(V, C, seed=6), _rand(V, C, seed=7)
+    bg0, bg2, bb, f0, f2 = _fuse_weights(C)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    o = [torch.empty(V, C, device="cuda") for _ in range(6)]
+    T = lambda m: _hold(m.t().contiguous())
+    Nn = lambda m: _hold(m.contiguous())
+    nat.call("ffno_fuse_bwd", x.data_ptr(), sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), fb.data_ptr(),
+             base.data_ptr(), V, C, T(bg0), T(bg2), bb.data_ptr(), T(f0), Nn(f2), Nn(f0), Nn(bg2), Nn(bg0),
+             o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(), _s())
+    gates, hg, hfb = (torch.empty(V, 2 * C, device="cuda"), torch.empty(V, C, device="cuda"),
+                      torch.empty(V, 2 * C, device="cuda"))
+    nat.call("ffno_fuse1_tc", x.data_ptr(), sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), V, C,
+             _pack(bg0, bg2).data_ptr(), bb.data_ptr(), gates.data_ptr(), hg.data_ptr(), err.data_ptr(), _s())
+    nat.call("ffno_fuse_bwd_a_tc", sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), gates.data_ptr(),
+             fb.data_ptr(), V, C, _pack(f0, f2.t()).data_ptr(), hfb.data_ptr(), err.data_ptr(), _s())
+    nat.call("ffno_fuse_bwd_b_tc", sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), gates.data_ptr(),
+             hg.data_ptr(), fb.data_ptr(), hfb.data_ptr(), base.data_ptr(), V, C,
+             _pack(f0.t(), bg2.t(), bg0.t()).data_ptr(), o[3].data_ptr(), o[4].data_ptr(), o[5].data_ptr(),
+             err.data_ptr(), _s())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    for i in range(3):
+        _close(o[3 + i], o[i])
