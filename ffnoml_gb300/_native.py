@@ -79,7 +79,7 @@ PROTOTYPES = {
     "ffno_si_populations": [P, L, I, P, P, P, P, P],
     "ffno_si_population_cotangent": [P, P, L, I, P, P, P, P, P],
     "ffno_si_input_grads": [P, P, P, L, P, P, P, P, P],
-    "ffno_tc_selftest": [P, P, I, I, P, P, P],
+    "ffno_tc_selftest": [P, P, I, I, I, P, P, P],
     "ffno_tc_parts": [L],
     "ffno_tc_width_supported": [I],
     "ffno_mlp2_fwd_tc": [I, P, P, P, F, P, L, I, P, P, P, P, I, I, P, P],
@@ -90,6 +90,9 @@ PROTOTYPES = {
     "ffno_gate_bwd_tc": [P, P, P, L, I, P, P, P, P, P, P],
     "ffno_fuse_bwd_a_tc": [P, P, P, P, P, P, L, I, P, P, P, P],
     "ffno_fuse_bwd_b_tc": [P, P, P, P, P, P, P, P, P, L, I, P, P, P, P, P, P],
+    "ffno_xform_tc_pack_bytes": [I, I],
+    "ffno_xform_tc": [P, P, P, ctypes.POINTER(XformDesc), I, P, P],
+    "ffno_spectral_mix_tc": [P, P, L, L, L, L, L, I, P, P, P, P, I, P, P],
 }
 
 _lib = None
@@ -129,8 +132,8 @@ class _Counter:
 counter = _Counter()
 
 
-def call(name, *args):
-    """Call an entry point and raise on a non-zero status."""
+def call(name, *args, tag=None):
+    """Call an entry point and raise on a non-zero status. tag names the call site in the timing breakdown."""
     counter.calls += 1
     if counter.timing is not None:
         import torch
@@ -138,7 +141,7 @@ def call(name, *args):
         a.record()
         status = getattr(lib(), name)(*args)
         b.record()
-        counter.timing.append((name, a, b))
+        counter.timing.append((name + (":" + tag if tag else ""), a, b))
     else:
         status = getattr(lib(), name)(*args)
     if status:

@@ -42,43 +42,117 @@ __device__ __forceinline__ float upstream(int mode, float u, float r, float y) {
 }
 
 // ------------------------------------------------------------------------------------------------ GN backward
-// Per group: S1 = sum ghat, S2 = sum ghat xhat, ghat = dL/dy * gamma, xhat = (pre - mean) rstd.
+// Lane layout of the two GroupNorm-backward kernels: each voxel's C channels are C/4 float4s held by LPV consecutive
+// lanes (LPV = C/4, or 24 lanes of a warp for C = 96); a warp covers VPW voxels per step.
 template <int C>
-__global__ void __launch_bounds__(NT) k_gn_bwd_stats(int mode, const float* __restrict__ u, float r,
-                                                     const float* __restrict__ pre, const float* __restrict__ gamma,
-                                                     const float* __restrict__ beta, const double* __restrict__ gst,
-                                                     long V, double* __restrict__ partials, int cpg, int groups) {
-  __shared__ float part[16 * C];
-  __shared__ float col[2 * C];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  double s1 = 0.0, s2 = 0.0;
-  const long nt = ntiles(V, BM);
-  for (long t = blockIdx.x; t < nt; t += gridDim.x) {
-    const long v0 = t * BM;
-    float a[4][C / 16], b[4][C / 16];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const long v = v0 + ty + 16 * i;
-#pragma unroll
-      for (int j = 0; j < C / 16; ++j) {
-        const int c = tx + 16 * j;
-        float ga = 0.f, gb = 0.f;
-        if (v < V) {
-          const int g = c / cpg;
-          const float xh = (__ldg(pre + v * C + c) - (float)gst[3 * g]) * (float)gst[3 * g + 1];
-          const float gm = __ldg(gamma + c);
-          ga = upstream(mode, __ldg(u + v * C + c), r, xh * gm + __ldg(beta + c)) * gm;
-          gb = ga * xh;
-        }
-        a[i][j] = ga;
-        b[i][j] = gb;
-      }
-    }
-    tile_group_sums<C>(a, b, cpg, groups, part, col, s1, s2);
-  }
+struct GnLanes {
+  static constexpr int LPV = C / 4;
+  static constexpr int VPW = LPV <= 32 ? 32 / LPV : 1;
+};
+
+// Per-group constants of one GroupNorm, as floats in shared memory: mean, rstd, 1/T, S1, S2, var*rstd^2.
+struct GnConst {
+  float mean[GMAX], rstd[GMAX], invT[GMAX], s1[GMAX], s2[GMAX], vr2[GMAX];
+};
+
+__device__ __forceinline__ void load_gn_const(GnConst& k, const double* gst, const double* sums, int groups,
+                                              float eps) {
   if (threadIdx.x < groups) {
-    partials[((long)blockIdx.x * groups + threadIdx.x) * 2] = s1;
-    partials[((long)blockIdx.x * groups + threadIdx.x) * 2 + 1] = s2;
+    const int g = threadIdx.x;
+    const double rs = gst[3 * g + 1];
+    k.mean[g] = (float)gst[3 * g];
+    k.rstd[g] = (float)rs;
+    k.invT[g] = (float)(1.0 / gst[3 * g + 2]);
+    k.s1[g] = sums ? (float)sums[2 * g] : 0.f;
+    k.s2[g] = sums ? (float)sums[2 * g + 1] : 0.f;
+    k.vr2[g] = (float)(1.0 - (double)eps * rs * rs);
+  }
+  __syncthreads();
+}
+
+// Per group: S1 = sum ghat, S2 = sum ghat xhat, ghat = dL/dy * gamma, xhat = (pre - mean) rstd, as per-CTA partials.
+template <int C>
+__global__ void __launch_bounds__(256) k_gn_bwd_stats(int mode, const float* __restrict__ u, float r,
+                                                      const float* __restrict__ pre, const float* __restrict__ gamma,
+                                                      const float* __restrict__ beta,
+                                                      const double* __restrict__ gst, long V,
+                                                      double* __restrict__ partials, int cpg, int groups) {
+  using Ln = GnLanes<C>;
+  __shared__ GnConst k;
+  __shared__ double red[8][GMAX][2];
+  load_gn_const(k, gst, nullptr, groups, 0.f);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / Ln::LPV, q = lane % Ln::LPV;
+  const bool active = sub < Ln::VPW;
+  const int c = 4 * q;
+  float gm[4], bt[4];
+  int grp[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    gm[j] = active ? __ldg(gamma + c + j) : 0.f;
+    bt[j] = active ? __ldg(beta + c + j) : 0.f;
+    grp[j] = (c + j) / cpg;
+  }
+  double d1[4] = {0, 0, 0, 0}, d2[4] = {0, 0, 0, 0};   // per element slot (groups of slot j fixed per thread)
+  float f1[4] = {0, 0, 0, 0}, f2[4] = {0, 0, 0, 0};
+  int n = 0;
+  const long step = (long)gridDim.x * 8 * Ln::VPW;
+  for (long v = ((long)blockIdx.x * 8 + warp) * Ln::VPW + sub; v < V; v += step) {
+    if (!active) break;
+    const float4 pu = __ldg(reinterpret_cast<const float4*>(u + v * C + c));
+    const float4 pp = __ldg(reinterpret_cast<const float4*>(pre + v * C + c));
+    const float uu[4] = {pu.x, pu.y, pu.z, pu.w}, xx[4] = {pp.x, pp.y, pp.z, pp.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int g = grp[j];
+      const float xh = (xx[j] - k.mean[g]) * k.rstd[g];
+      const float gh = upstream(mode, uu[j], r, xh * gm[j] + bt[j]) * gm[j];
+      f1[j] += gh;
+      f2[j] += gh * xh;
+    }
+    if (++n == 16) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        d1[j] += f1[j];
+        d2[j] += f2[j];
+        f1[j] = f2[j] = 0.f;
+      }
+      n = 0;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    d1[j] += f1[j];
+    d2[j] += f2[j];
+  }
+  // per group: warp reduce (lanes of other groups contribute 0), then warps in order
+  for (int g = 0; g < groups; ++g) {
+    double a = 0.0, b = 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (active && grp[j] == g) {
+        a += d1[j];
+        b += d2[j];
+      }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+      red[warp][g][0] = a;
+      red[warp][g][1] = b;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < groups) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < 8; ++w) {
+      a += red[w][threadIdx.x][0];
+      b += red[w][threadIdx.x][1];
+    }
+    partials[((long)blockIdx.x * groups + threadIdx.x) * 2] = a;
+    partials[((long)blockIdx.x * groups + threadIdx.x) * 2 + 1] = b;
   }
 }
 
@@ -94,40 +168,62 @@ __global__ void k_gn_bwd_final(const double* __restrict__ partials, int nparts, 
   sums[2 * g + 1] = s2;
 }
 
-// pre_bar = rstd (ghat - (w / T)(S1 + xhat S2)); w_bar += sum_c (1/T)(-S1 xhat - S2 (xhat^2 - var rstd^2) / 2).
-// Four threads per voxel, each over C/4 consecutive channels.
+// pre_bar = rstd (ghat - (w / T)(S1 + xhat S2)); w_bar[v] += sum_c (1/T)(-S1 xhat - S2 (xhat^2 - var rstd^2) / 2).
 template <int C>
-__global__ void k_gn_bwd_apply(int mode, const float* __restrict__ u, float r, const float* __restrict__ pre,
-                               const float* __restrict__ gamma, const float* __restrict__ beta,
-                               const double* __restrict__ gst, const double* __restrict__ sums,
-                               const float* __restrict__ dw, long V, float* __restrict__ pre_bar,
-                               float* __restrict__ w_bar, int cpg, float eps) {
-  constexpr int Q = C / 4;
-  const long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const long v = gid >> 2;
-  const int q = (int)(gid & 3);
-  const bool ok = v < V;
-  float wc = 0.f;
-  if (ok) {
-    const float wv = __ldg(dw + v);
-#pragma unroll 4
-    for (int cc = 0; cc < Q; ++cc) {
-      const int c = q * Q + cc;
-      const int g = c / cpg;
-      const float mean = (float)gst[3 * g], rs = (float)gst[3 * g + 1];
-      const float invT = (float)(1.0 / gst[3 * g + 2]);
-      const float S1 = (float)sums[2 * g], S2 = (float)sums[2 * g + 1];
-      const float xh = (__ldg(pre + v * C + c) - mean) * rs;
-      const float gm = __ldg(gamma + c);
-      const float gh = upstream(mode, __ldg(u + v * C + c), r, xh * gm + __ldg(beta + c)) * gm;
-      pre_bar[v * C + c] = rs * (gh - wv * invT * (S1 + xh * S2));
-      const float vr2 = 1.f - eps * rs * rs;
-      wc += invT * (-S1 * xh - 0.5f * S2 * (xh * xh - vr2));
-    }
+__global__ void __launch_bounds__(256) k_gn_bwd_apply(int mode, const float* __restrict__ u, float r,
+                                                      const float* __restrict__ pre, const float* __restrict__ gamma,
+                                                      const float* __restrict__ beta,
+                                                      const double* __restrict__ gst, const double* __restrict__ sums,
+                                                      const float* __restrict__ dw, long V,
+                                                      float* __restrict__ pre_bar, float* __restrict__ w_bar, int cpg,
+                                                      int groups, float eps) {
+  using Ln = GnLanes<C>;
+  __shared__ GnConst k;
+  load_gn_const(k, gst, sums, groups, eps);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / Ln::LPV, q = lane % Ln::LPV;
+  const bool active = sub < Ln::VPW;
+  const int c = 4 * q;
+  float gm[4], bt[4];
+  int grp[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    gm[j] = active ? __ldg(gamma + c + j) : 0.f;
+    bt[j] = active ? __ldg(beta + c + j) : 0.f;
+    grp[j] = (c + j) / cpg;
   }
-  wc += __shfl_xor_sync(0xffffffffu, wc, 1);
-  wc += __shfl_xor_sync(0xffffffffu, wc, 2);
-  if (ok && q == 0) w_bar[v] += wc;
+  const long step = (long)gridDim.x * 8 * Ln::VPW;
+  const long first = ((long)blockIdx.x * 8 + warp) * Ln::VPW;
+  for (long vb = first; vb < V; vb += step) {   // warp-uniform loop
+    const long v = vb + sub;
+    const bool ok = active && v < V;
+    float wc = 0.f;
+    if (ok) {
+      const float wv = __ldg(dw + v);
+      const float4 pu = __ldg(reinterpret_cast<const float4*>(u + v * C + c));
+      const float4 pp = __ldg(reinterpret_cast<const float4*>(pre + v * C + c));
+      const float uu[4] = {pu.x, pu.y, pu.z, pu.w}, xx[4] = {pp.x, pp.y, pp.z, pp.w};
+      float o[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int g = grp[j];
+        const float xh = (xx[j] - k.mean[g]) * k.rstd[g];
+        const float gh = upstream(mode, uu[j], r, xh * gm[j] + bt[j]) * gm[j];
+        o[j] = k.rstd[g] * (gh - wv * k.invT[g] * (k.s1[g] + xh * k.s2[g]));
+        wc += k.invT[g] * (-k.s1[g] * xh - 0.5f * k.s2[g] * (xh * xh - k.vr2[g]));
+      }
+      *reinterpret_cast<float4*>(pre_bar + v * C + c) = make_float4(o[0], o[1], o[2], o[3]);
+    }
+    // sum over the LPV lanes of this voxel (segments of a power-of-two LPV, or the whole warp for C = 96)
+    if (Ln::LPV >= 32 || (Ln::LPV & (Ln::LPV - 1))) {
+#pragma unroll
+      for (int off = 16; off; off >>= 1) wc += __shfl_xor_sync(0xffffffffu, wc, off);
+    } else {
+#pragma unroll
+      for (int off = Ln::LPV / 2; off; off >>= 1) wc += __shfl_xor_sync(0xffffffffu, wc, off);
+    }
+    if (ok && q == 0) w_bar[v] += wc;
+  }
 }
 
 // ------------------------------------------------------------------------------------------------ MLP backward
@@ -718,7 +814,7 @@ int ffno_gn_bwd_stats(int mode, const float* u, float r, const float* pre, const
   cudaStream_t s = (cudaStream_t)stream;
   const int cpg = C / groups;
   switch (C) {
-#define L(CC) case CC: k_gn_bwd_stats<CC><<<nparts, NT, 0, s>>>(mode, u, r, pre, gamma, beta, gstats, V, partials, cpg, groups); break;
+#define L(CC) case CC: k_gn_bwd_stats<CC><<<nparts, 256, 0, s>>>(mode, u, r, pre, gamma, beta, gstats, V, partials, cpg, groups); break;
     L(16) L(32) L(64) L(96)
 #undef L
   }
@@ -739,10 +835,9 @@ int ffno_gn_bwd_apply(int mode, const float* u, float r, const float* pre, const
   if (!width_ok(C) || V < 1 || groups < 1 || groups > GMAX || C % groups) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   const int cpg = C / groups;
-  const long threads = 4 * V;
-  const unsigned blocks = (unsigned)((threads + 255) / 256);
+  const int blocks = grid_of(V, 8 * 8, 4);
   switch (C) {
-#define L(CC) case CC: k_gn_bwd_apply<CC><<<blocks, 256, 0, s>>>(mode, u, r, pre, gamma, beta, gstats, sums, dw, V, pre_bar, w_bar, cpg, eps); break;
+#define L(CC) case CC: k_gn_bwd_apply<CC><<<blocks, 256, 0, s>>>(mode, u, r, pre, gamma, beta, gstats, sums, dw, V, pre_bar, w_bar, cpg, groups, eps); break;
     L(16) L(32) L(64) L(96)
 #undef L
   }

@@ -20,7 +20,7 @@ namespace {
 
 constexpr int TM = 128;  // voxels per tile = MMA M
 constexpr int TT = 256;  // threads per CTA (two warpgroups)
-constexpr int FB = 4;    // fill: independent loads in flight per thread
+constexpr int FB = 8;    // fill: independent loads in flight per thread
 
 __host__ __device__ constexpr uint32_t tmem_cols(int n) {
   return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : n <= 256 ? 256 : 512;
@@ -348,6 +348,9 @@ __global__ void __launch_bounds__(TT) k_gate_tc(const float* __restrict__ x, lon
   cx.ok = load_weights(smem, wpack, 2 * B1, cx, err);
   for (long t = blockIdx.x; cx.ok && t < nt; t += gridDim.x) {
     const long v0 = t * TM;
+    if (tid == 0) {
+      prefetch_rows(x, (t + gridDim.x) * TM, V, C);
+    }
     fill_tile<C>(A, v0, V, [&](long v, int k) { return ld4(x + v * C + k); });
     if (!gemms(cx, err, tmem, A, g1, C, C)) break;
 #pragma unroll
@@ -406,6 +409,11 @@ __global__ void __launch_bounds__(TT) k_fuse1_tc(const float* __restrict__ x, co
   cx.ok = load_weights(smem, wpack, B1 + B2, cx, err);
   for (long t = blockIdx.x; cx.ok && t < nt; t += gridDim.x) {
     const long v0 = t * TM;
+    if (tid == 0) {
+      prefetch_rows(x, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(sp, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(vp, (t + gridDim.x) * TM, V, C);
+    }
     fill_tile<3 * C>(A, v0, V, [&](long v, int k) {
       if (k < C) return ld4(x + v * C + k);
       if (k < 2 * C) return gn4<true>(ld4(sp + v * C + k - C), sc, C, k - C);
@@ -467,6 +475,11 @@ __global__ void __launch_bounds__(TT) k_fuse2_tc(const float* __restrict__ sp, c
   };
   for (long t = blockIdx.x; cx.ok && t < nt; t += gridDim.x) {
     const long v0 = t * TM;
+    if (tid == 0) {
+      prefetch_rows(sp, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(vp, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(gates, (t + gridDim.x) * TM, V, 2 * C);
+    }
     fill_tile<2 * C>(A, v0, V, mixed);
     if (!gemms(cx, err, tmem, A, wf1, 2 * C, 2 * C)) break;
 #pragma unroll
@@ -525,6 +538,11 @@ __global__ void __launch_bounds__(TT) k_mlp2_bwd_tc(const float* __restrict__ a,
   cx.ok = load_weights(smem, wpack, 3 * B1, cx, err);
   for (long t = blockIdx.x; cx.ok && t < nt; t += gridDim.x) {
     const long v0 = t * TM;
+    if (tid == 0) {
+      prefetch_rows(a, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(pb, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(base, (t + gridDim.x) * TM, V, C);
+    }
     fill_tile<C>(A, v0, V, [&](long v, int k) { return ld4(a + v * C + k); });
     fill_tile<C>(P, v0, V, [&](long v, int k) { return ld4(pb + v * C + k); });
     if (!gemms(cx, err, tmem, A, w1, C, 2 * C, tmem + 2 * C, P, w2t, C, 2 * C)) break;
@@ -582,6 +600,11 @@ __global__ void __launch_bounds__(TT) k_gate_bwd_tc(const float* __restrict__ x,
   cx.ok = load_weights(smem, wpack, 4 * B1, cx, err);
   for (long t = blockIdx.x; cx.ok && t < nt; t += gridDim.x) {
     const long v0 = t * TM;
+    if (tid == 0) {
+      prefetch_rows(x, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(gbar, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(base, (t + gridDim.x) * TM, V, C);
+    }
     const long v = v0 + row;
     fill_tile<C>(X, v0, V, [&](long vv, int k) { return ld4(x + vv * C + k); });
     if (!gemms(cx, err, D1, X, g1, C, C)) break;
@@ -681,6 +704,12 @@ __global__ void __launch_bounds__(TT) k_fuse_bwd_a_tc(const float* __restrict__ 
   cx.ok = load_weights(smem, wpack, B1 + B2, cx, err);
   for (long t = blockIdx.x; cx.ok && t < nt; t += gridDim.x) {
     const long v0 = t * TM;
+    if (tid == 0) {
+      prefetch_rows(sp, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(vp, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(gates, (t + gridDim.x) * TM, V, 2 * C);
+      prefetch_rows(fb, (t + gridDim.x) * TM, V, C);
+    }
     fill_tile<2 * C>(Bt, v0, V, [&](long v, int k) {
       const float4 g = ld4(gates + v * 2 * C + k);
       const float4 s =
@@ -729,6 +758,15 @@ __global__ void __launch_bounds__(TT) k_fuse_bwd_b_tc(const float* __restrict__ 
   cx.ok = load_weights(smem, wpack, B1 + B2 + B3, cx, err);
   for (long t = blockIdx.x; cx.ok && t < nt; t += gridDim.x) {
     const long v0 = t * TM;
+    if (tid == 0) {
+      prefetch_rows(hfb, (t + gridDim.x) * TM, V, 2 * C);
+      prefetch_rows(fb, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(gates, (t + gridDim.x) * TM, V, 2 * C);
+      prefetch_rows(sp, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(vp, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(hg, (t + gridDim.x) * TM, V, C);
+      prefetch_rows(base, (t + gridDim.x) * TM, V, C);
+    }
     const long v = v0 + row;
     fill_tile<2 * C>(A2, v0, V, [&](long vv, int k) { return ld4(hfb + vv * 2 * C + k); });
     if (!gemms(cx, err, tmem, A2, wf1t, 2 * C, 2 * C)) break;
@@ -746,12 +784,18 @@ __global__ void __launch_bounds__(TT) k_fuse_bwd_b_tc(const float* __restrict__ 
         const float* cf = is_s ? sc : vc;
         float* gout = is_s ? sbar : vbar;
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const float b = bb[i] + 0.5f * __ldg(fb + v * C + cc + i);
-          const float g = __ldg(gates + v * 2 * C + c0 + i);
-          const float s = gn1gelu(__ldg(pre + v * C + cc + i), cf, C, cc + i);
-          gout[v * C + cc + i] = b * g;
-          q[i] = b * s * g * (1.f - g);
+        for (int i = 0; i < 16; i += 4) {
+          const float4 f4 = ld4(fb + v * C + cc + i), g4 = ld4(gates + v * 2 * C + c0 + i);
+          const float4 s4 = gn4<true>(ld4(pre + v * C + cc + i), cf, C, cc + i);
+          const float ff[4] = {f4.x, f4.y, f4.z, f4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w}, ss[4] = {s4.x, s4.y, s4.z, s4.w};
+          float o[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float b = bb[i + j] + 0.5f * ff[j];
+            o[j] = b * gg[j];
+            q[i + j] = b * ss[j] * gg[j] * (1.f - gg[j]);
+          }
+          *reinterpret_cast<float4*>(gout + v * C + cc + i) = make_float4(o[0], o[1], o[2], o[3]);
         }
       }
       put16(A2, row, c0, 2 * C, q);
@@ -764,7 +808,13 @@ __global__ void __launch_bounds__(TT) k_fuse_bwd_b_tc(const float* __restrict__ 
       tc::tmem_ld16(tmem + lb + 2 * C + c0, hb);
       if (v < V)
 #pragma unroll
-        for (int i = 0; i < 16; ++i) hb[i] *= gelu_grad(__ldg(hg + v * C + c0 + i));
+        for (int i = 0; i < 16; i += 4) {
+          const float4 h4 = ld4(hg + v * C + c0 + i);
+          hb[i] *= gelu_grad(h4.x);
+          hb[i + 1] *= gelu_grad(h4.y);
+          hb[i + 2] *= gelu_grad(h4.z);
+          hb[i + 3] *= gelu_grad(h4.w);
+        }
       put16(A1, row, c0, C, hb);
     }
     if (!gemms(cx, err, tmem, A1, wg1t, C, 3 * C)) break;
@@ -776,12 +826,30 @@ __global__ void __launch_bounds__(TT) k_fuse_bwd_b_tc(const float* __restrict__ 
       if (v < V) {
         if (c0 < C) {
 #pragma unroll
-          for (int i = 0; i < 16; ++i) xbar[v * C + c0 + i] = r[i] + (base ? __ldg(base + v * C + c0 + i) : 0.f);
+          for (int i = 0; i < 16; i += 4) {
+            float4 o = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
+            if (base) {
+              const float4 b4 = ld4(base + v * C + c0 + i);
+              o.x += b4.x;
+              o.y += b4.y;
+              o.z += b4.z;
+              o.w += b4.w;
+            }
+            *reinterpret_cast<float4*>(xbar + v * C + c0 + i) = o;
+          }
         } else {
           float* g = c0 < 2 * C ? sbar : vbar;
           const int cc = c0 < 2 * C ? c0 - C : c0 - 2 * C;
 #pragma unroll
-          for (int i = 0; i < 16; ++i) g[v * C + cc + i] += r[i];
+          for (int i = 0; i < 16; i += 4) {
+            float4* p = reinterpret_cast<float4*>(g + v * C + cc + i);
+            float4 o = *p;
+            o.x += r[i];
+            o.y += r[i + 1];
+            o.z += r[i + 2];
+            o.w += r[i + 3];
+            *p = o;
+          }
         }
       }
     }

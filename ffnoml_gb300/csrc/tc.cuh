@@ -33,13 +33,26 @@ __device__ __forceinline__ uint64_t kmajor_desc(uint32_t saddr, uint32_t lbo_byt
   return d;
 }
 
-// instruction descriptor of tcgen05.mma kind::f16: D (F32) [M x N] += A (BF16, K-major) * B (BF16, K-major)
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+// instruction descriptor of tcgen05.mma kind::f16: D (F32) [M x N] += A (BF16, K-major) * B (BF16, K-major, or
+// MN-major with b_mn)
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, bool b_mn = false) {
   return (1u << 4)                       // D format: F32
          | (1u << 7)                     // A format: BF16
          | (1u << 10)                    // B format: BF16
+         | ((b_mn ? 1u : 0u) << 16)      // B major-ness: 0 K-major, 1 MN-major
          | ((uint32_t)(N >> 3) << 17)    // N / 8
          | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
+// byte offset of element (n, k) of an N x K operand stored MN-major (n contiguous): 8 (k) x 16-byte core matrices,
+// n-groups adjacent (SBO = 128 bytes), k-groups N * 16 bytes apart (LBO)
+__device__ __forceinline__ uint32_t mnmajor_offset(int n, int k, int N) {
+  return (uint32_t)((k >> 3) * (N * 16) + (n >> 3) * 128 + (k & 7) * 16 + (n & 7) * 2);
+}
+
+// shared-memory matrix descriptor of an MN-major operand (no swizzle): LBO = K-group stride, SBO = MN-group stride
+__device__ __forceinline__ uint64_t mnmajor_desc(uint32_t saddr, uint32_t lbo_bytes, uint32_t sbo_bytes) {
+  return kmajor_desc(saddr, lbo_bytes, sbo_bytes);
 }
 
 // ---------------------------------------------------------------------------------------------------- mbarrier
@@ -123,6 +136,17 @@ __device__ __forceinline__ void gemm_128xN(uint32_t tmem_d, uint32_t a_base, uin
   for (int k = 0; k < K; k += 16) {
     const uint64_t ad = kmajor_desc(a_base + (uint32_t)(k / 8) * 128u, 128u, (uint32_t)K * 16u);
     const uint64_t bd = kmajor_desc(b_base + (uint32_t)(k / 8) * 128u, 128u, (uint32_t)K * 16u);
+    mma_bf16(tmem_d, ad, bd, idesc, (accumulate || k > 0) ? 1u : 0u);
+  }
+}
+
+// D [128 x N] (+)= A [128 x K] (K-major) * B [N x K] with B stored MN-major (n contiguous, mnmajor_offset with N).
+__device__ __forceinline__ void gemm_128xN_bmn(uint32_t tmem_d, uint32_t a_base, uint32_t b_base, int K, int N,
+                                               bool accumulate) {
+  const uint32_t idesc = idesc_bf16(128, N, true);
+  for (int k = 0; k < K; k += 16) {
+    const uint64_t ad = kmajor_desc(a_base + (uint32_t)(k / 8) * 128u, 128u, (uint32_t)K * 16u);
+    const uint64_t bd = mnmajor_desc(b_base + (uint32_t)(k / 8) * (uint32_t)N * 16u, (uint32_t)N * 16u, 128u);
     mma_bf16(tmem_d, ad, bd, idesc, (accumulate || k > 0) ? 1u : 0u);
   }
 }

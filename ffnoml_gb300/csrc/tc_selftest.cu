@@ -9,7 +9,8 @@ using namespace ffno;
 namespace {
 
 __global__ void __launch_bounds__(128) k_tc_selftest(const float* __restrict__ A, const float* __restrict__ B, int K,
-                                                     int N, float* __restrict__ D, int* __restrict__ status) {
+                                                     int N, int b_mn, float* __restrict__ D,
+                                                     int* __restrict__ status) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint64_t bar;
   __shared__ uint32_t tslot;
@@ -22,7 +23,8 @@ __global__ void __launch_bounds__(128) k_tc_selftest(const float* __restrict__ A
   }
   for (int e = tid; e < N * K; e += 128) {
     const int r = e / K, k = e % K;
-    *reinterpret_cast<__nv_bfloat16*>(sb + tc::kmajor_offset(r, k, K)) = __float2bfloat16_rn(B[e]);
+    const uint32_t off = b_mn ? tc::mnmajor_offset(r, k, N) : tc::kmajor_offset(r, k, K);
+    *reinterpret_cast<__nv_bfloat16*>(sb + off) = __float2bfloat16_rn(B[e]);
   }
   if (warp == 0) tc::tmem_alloc(&tslot, 512);
   if (tid == 0) {
@@ -35,7 +37,10 @@ __global__ void __launch_bounds__(128) k_tc_selftest(const float* __restrict__ A
   tc::tc_after_sync();
   const uint32_t taddr = tslot;
   if (tid == 0) {
-    tc::gemm_128xN(taddr, tc::smem_u32(sa), tc::smem_u32(sb), K, N, false);
+    if (b_mn)
+      tc::gemm_128xN_bmn(taddr, tc::smem_u32(sa), tc::smem_u32(sb), K, N, false);
+    else
+      tc::gemm_128xN(taddr, tc::smem_u32(sa), tc::smem_u32(sb), K, N, false);
     tc::mma_commit(&bar);
   }
   const bool ok = tc::mbar_wait(&bar, 0);
@@ -57,13 +62,13 @@ __global__ void __launch_bounds__(128) k_tc_selftest(const float* __restrict__ A
 
 }  // namespace
 
-extern "C" int ffno_tc_selftest(const float* A, const float* B, int K, int N, float* D, int* status,
+extern "C" int ffno_tc_selftest(const float* A, const float* B, int K, int N, int b_mn, float* D, int* status,
                                 ffno_stream_t stream) {
   if (!A || !B || !D || !status || K < 16 || K % 16 || K > 256 || N < 16 || N % 16 || N > 256) return FFNO_EINVAL;
   const size_t smem = (size_t)(128 + N) * K * 2 + 1024;
   if (cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return FFNO_ELAUNCH;
-  k_tc_selftest<<<1, 128, smem, (cudaStream_t)stream>>>(A, B, K, N, D, status);
+  k_tc_selftest<<<1, 128, smem, (cudaStream_t)stream>>>(A, B, K, N, b_mn, D, status);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

@@ -75,6 +75,33 @@ def tc_pack(device, *mats):
     return torch.cat(parts).to(device).contiguous()
 
 
+class TcXform:
+    """A transform table T [M][K] (float64 numpy) packed for ffno_xform_tc: split-BF16 per 128-row m-tile and 64-wide
+    k-chunk, in slices of at most 256 rows (one kernel call each)."""
+
+    def __init__(self, T, device):
+        T = np.asarray(T, dtype=np.float64)
+        self.M, self.K = T.shape
+        Kp = (self.K + 15) // 16 * 16
+        self.slices = []
+        for r0 in range(0, self.M, 256):
+            rows = min(256, self.M - r0)
+            mt = (rows + 127) // 128
+            pad = np.zeros((mt * 128, Kp))
+            pad[:rows, :self.K] = T[r0:r0 + rows]
+            parts = []
+            for t in range(mt):
+                for k0 in range(0, Kp, 64):
+                    sub = torch.from_numpy(pad[t * 128:(t + 1) * 128, k0:min(Kp, k0 + 64)].copy())
+                    hi = sub.to(torch.bfloat16)
+                    lo = (sub - hi.double()).to(torch.bfloat16)
+                    parts += [pack_kmajor(hi.float()).reshape(-1), pack_kmajor(lo.float()).reshape(-1)]
+            packed = torch.cat(parts).to(device).contiguous()
+            if packed.numel() * 2 != nat.lib().ffno_xform_tc_pack_bytes(rows, self.K):
+                raise RuntimeError("transform pack size mismatch")
+            self.slices.append((r0, rows, packed))
+
+
 class Packed:
     """Device copies of one model's weights in kernel layouts (and their transposes for the VJP)."""
 
@@ -147,6 +174,10 @@ class Packed:
         pk["tc_fuse2"] = tc_pack(device, f0, f2)
         pk["tcb_fuse_a"] = tc_pack(device, f0, f2.t())
         pk["tcb_fuse_b"] = tc_pack(device, f0.t(), bg2.t(), bg0.t())
+        for name, conv in (("s", s), ("v", v)):
+            wb = _wbig(conv.weight_real, conv.weight_imag)
+            pk[f"tc_{name}_mix"] = tc_pack(device, wb.t())      # out = xhat @ wbig -> matrix wbig^T
+            pk[f"tcb_{name}_mix"] = tc_pack(device, wb)         # adjoint: xhat_bar = y_bar @ wbig^T
 
     @staticmethod
     def _head_params(model):
@@ -252,7 +283,8 @@ class Executor:
             f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device=device)
             # forward tables and the transposes the VJP applies (rows/cols swapped)
             self._plane[key] = dict(twf=f(twf), thf=f(thf), thi=f(thi), twi=f(twi), twf_t=f(twf.T), thf_t=f(thf.T),
-                                    thi_t=f(thi.T), twi_t=f(twi.T))
+                                    thi_t=f(thi.T), twi_t=f(twi.T), np=dict(twf=twf, thf=thf, thi=thi, twi=twi),
+                                    device=device)
         return self._plane[key]
 
     def plane_freq(self, pk, H, W, dx, dy, device):
@@ -274,8 +306,32 @@ class Executor:
                          for i in range(self.model.n_layers)]
             f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device=device)
             self._height[key] = dict(live=live, tzf=f(tzf), tzi=f(tzi), tzf_t=f(tzf.T), tzi_t=f(tzi.T),
-                                     freq=per_block)
+                                     freq=per_block, np=dict(tzf=tzf, tzi=tzi), device=device)
         return self._height[key]
+
+    @staticmethod
+    def tc_table(tabs, name):
+        """The split-BF16 pack of table `name` (a key of the plane or height dict; suffix _t = transposed), built once."""
+        key = "tc_" + name
+        if key not in tabs:
+            base = tabs["np"][name[:-2] if name.endswith("_t") else name]
+            tabs[key] = TcXform(base.T if name.endswith("_t") else base, tabs["device"])
+        return tabs[key]
+
+    def _xf(self, tabs, name, inp, out, desc, ws):
+        """out = T_name applied by ffno_xform (FP32) or ffno_xform_tc (split-BF16 tensor cores)."""
+        s = _stream()
+        if not self._tc():
+            nat.call("ffno_xform", tabs[name].data_ptr(), inp.data_ptr(), out.data_ptr(), desc, 0, s, tag=name)
+            return
+        tx = self.tc_table(tabs, name)
+        if len(tx.slices) > 1 and desc.out_split < desc.M:
+            raise ValueError("a transform taller than 256 rows needs single-level output addressing")
+        for r0, rows, packed in tx.slices:
+            d = nat.XformDesc.from_buffer_copy(desc)
+            d.M = rows
+            nat.call("ffno_xform_tc", packed.data_ptr(), inp.data_ptr(), out.data_ptr() + 4 * r0 * desc.out_lo, d, 0,
+                     ws.err.data_ptr(), s, tag=name)
 
     # -------------------------------------------------------------------------------------------- geometry
     def geometry(self, z_scale):
@@ -398,21 +454,19 @@ class Executor:
             nat.call("ffno_gate_fwd", x.data_ptr(), V, C, bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(),
                      bp["v_zp"].data_ptr(), z.data_ptr(), ws.xv.data_ptr(), s)
         # horizontal spectral branch: rfft2 -> mix -> irfft2 as contractions
-        nat.call("ffno_xform", pln["twf"].data_ptr(), ws.xs.data_ptr(), ws.sa.data_ptr(), d["wf"], 0, s)
-        nat.call("ffno_xform", pln["thf"].data_ptr(), ws.sa.data_ptr(), ws.sb.data_ptr(), d["hf"], 0, s)
-        nat.call("ffno_spectral_mix", ws.sb.data_ptr(), ws.sa.data_ptr(), H * Wf, D, C, 2 * H * Wf * C, H * Wf * C, C,
-                 bp["s_wbig"].data_ptr(), fq.g.data_ptr(), _ptr(fq.u), _ptr(fq.v), m.freq_mix_rank, s)
-        nat.call("ffno_xform", pln["thi"].data_ptr(), ws.sa.data_ptr(), ws.sb.data_ptr(), d["hf"], 0, s)
-        nat.call("ffno_xform", pln["twi"].data_ptr(), ws.sb.data_ptr(), ws.ys.data_ptr(), d["wi"], 0, s)
+        self._xf(pln, "twf", ws.xs, ws.sa, d["wf"], ws)
+        self._xf(pln, "thf", ws.sa, ws.sb, d["hf"], ws)
+        self._mix(ws, "s", bp, fq, ws.sb, ws.sa, H * Wf, D, C, 2 * H * Wf * C, H * Wf * C, False)
+        self._xf(pln, "thi", ws.sa, ws.sb, d["hf"], ws)
+        self._xf(pln, "twi", ws.sb, ws.ys, d["wi"], ws)
         tc = self._mlp2(ws, 0, ws.ys, None, None, 0.0, None, bp["s_p1"], bp["s_p2"], bp.get("tc_s_post"),
                         ws.spec_pre)
         self._finalize(ws, "spec", bp["spec_g"], bp["spec_b"], tc)
         # vertical (height) branch
         hq = hgt["freq"][i]
-        nat.call("ffno_xform", hgt["tzf"].data_ptr(), ws.xv.data_ptr(), ws.va.data_ptr(), d["zf"], 0, s)
-        nat.call("ffno_spectral_mix", ws.va.data_ptr(), ws.vb.data_ptr(), live, HW, HW * C, C, live * HW * C, C,
-                 bp["v_wbig"].data_ptr(), hq.g.data_ptr(), _ptr(hq.u), _ptr(hq.v), m.freq_mix_rank, s)
-        nat.call("ffno_xform", hgt["tzi"].data_ptr(), ws.vb.data_ptr(), ws.yv.data_ptr(), d["zi"], 0, s)
+        self._xf(hgt, "tzf", ws.xv, ws.va, d["zf"], ws)
+        self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, False)
+        self._xf(hgt, "tzi", ws.vb, ws.yv, d["zi"], ws)
         tc = self._mlp2(ws, 0, ws.yv, None, None, 0.0, None, bp["v_p1"], bp["v_p2"], bp.get("tc_v_post"),
                         ws.vert_pre)
         self._finalize(ws, "vert", bp["vert_g"], bp["vert_b"], tc)
@@ -439,6 +493,20 @@ class Executor:
         self._finalize(ws, "mlp", bp["mlp_g"], bp["mlp_b"], tc)
         nat.call("ffno_resid_out", ws.x2.data_ptr(), ws.mlp_pre.data_ptr(), ws.coefs["mlp"].data_ptr(), r_mlp, V, C,
                  ws.x.data_ptr(), s)
+
+    def _mix(self, ws, branch, bp, fq, inp, out, F, nb, sf, sb, s_im, adjoint):
+        """Per-frequency channel mixing (or its adjoint) on FP32 cores or tensor cores."""
+        m = self.model
+        s = _stream()
+        g, u, v = (fq.g_adj, fq.u_adj, fq.v_adj) if adjoint else (fq.g, fq.u, fq.v)
+        if self._tc():
+            w = bp[("tcb_" if adjoint else "tc_") + branch + "_mix"]
+            nat.call("ffno_spectral_mix_tc", inp.data_ptr(), out.data_ptr(), F, nb, sf, sb, s_im, m.width,
+                     w.data_ptr(), g.data_ptr(), _ptr(u), _ptr(v), m.freq_mix_rank, ws.err.data_ptr(), s)
+        else:
+            w = bp[branch + "_wbig" + ("t" if adjoint else "")]
+            nat.call("ffno_spectral_mix", inp.data_ptr(), out.data_ptr(), F, nb, sf, sb, s_im, m.width, w.data_ptr(),
+                     g.data_ptr(), _ptr(u), _ptr(v), m.freq_mix_rank, s)
 
     def _tc(self):
         """Whether the split-BF16 tensor-core kernels run (precision 'bf16' at a width they support)."""
@@ -574,23 +642,21 @@ class Executor:
         self._gn_bwd(ws, gb, 1, gb.vbar, 1.0, ws.vert_pre, bp["vert_g"], bp["vert_b"], "vert", gb.pbar)
         mlp_bwd(ws.yv, gb.pbar, None, gb.yvb, "v_p1", "v_p2t", "v_p1t", "tcb_v_post")
         # horizontal transposes: ys = twi thi mix thf twf xs  ->  xs_bar = twf^T thf^T mix^T thi^T twi^T ys_bar
-        nat.call("ffno_xform", pln["twi_t"].data_ptr(), gb.ysb.data_ptr(), ws.sa.data_ptr(), d["wf"], 0, s)
-        nat.call("ffno_xform", pln["thi_t"].data_ptr(), ws.sa.data_ptr(), ws.sb.data_ptr(), d["hf"], 0, s)
-        nat.call("ffno_spectral_mix", ws.sb.data_ptr(), ws.sa.data_ptr(), H * Wf, D, C, 2 * H * Wf * C, H * Wf * C, C,
-                 bp["s_wbigt"].data_ptr(), fq.g_adj.data_ptr(), _ptr(fq.u_adj), _ptr(fq.v_adj), m.freq_mix_rank, s)
-        nat.call("ffno_xform", pln["thf_t"].data_ptr(), ws.sa.data_ptr(), ws.sb.data_ptr(), d["hf"], 0, s)
-        nat.call("ffno_xform", pln["twf_t"].data_ptr(), ws.sb.data_ptr(), gb.xsb.data_ptr(), d["wi"], 0, s)
+        self._xf(pln, "twi_t", gb.ysb, ws.sa, d["wf"], ws)
+        self._xf(pln, "thi_t", ws.sa, ws.sb, d["hf"], ws)
+        self._mix(ws, "s", bp, fq, ws.sb, ws.sa, H * Wf, D, C, 2 * H * Wf * C, H * Wf * C, True)
+        self._xf(pln, "thf_t", ws.sa, ws.sb, d["hf"], ws)
+        self._xf(pln, "twf_t", ws.sb, gb.xsb, d["wi"], ws)
         # vertical transposes (ws.vb holds the mixed modes, ws.xv the transform input)
         hq = hgt["freq"][i]
         N = HW * C
         nat.call("ffno_outer", gb.yvb.data_ptr(), N, D, ws.vb.data_ptr(), N, 2 * live, N, gb.opart.data_ptr(),
                  gb.osplit_i, tzi_bar.data_ptr(), 1, s)
-        nat.call("ffno_xform", hgt["tzi_t"].data_ptr(), gb.yvb.data_ptr(), ws.va.data_ptr(), d["zf"], 0, s)
-        nat.call("ffno_spectral_mix", ws.va.data_ptr(), ws.vb.data_ptr(), live, HW, HW * C, C, live * HW * C, C,
-                 bp["v_wbigt"].data_ptr(), hq.g_adj.data_ptr(), _ptr(hq.u_adj), _ptr(hq.v_adj), m.freq_mix_rank, s)
+        self._xf(hgt, "tzi_t", gb.yvb, ws.va, d["zf"], ws)
+        self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, True)
         nat.call("ffno_outer", ws.vb.data_ptr(), N, 2 * live, ws.xv.data_ptr(), N, D, N, gb.opart.data_ptr(),
                  gb.osplit_f, tzf_bar.data_ptr(), 1, s)
-        nat.call("ffno_xform", hgt["tzf_t"].data_ptr(), ws.vb.data_ptr(), gb.xvb.data_ptr(), d["zi"], 0, s)
+        self._xf(hgt, "tzf_t", ws.vb, gb.xvb, d["zi"], ws)
         # input gates (and z_proj)
         if tc:
             nat.call("ffno_gate_bwd_tc", x.data_ptr(), gb.xsb.data_ptr(), gb.xacc.data_ptr(), V, C,

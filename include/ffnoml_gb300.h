@@ -269,10 +269,25 @@ int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const flo
                        const float* base, long V, int C, const void* wpack, float* x_bar, float* spec_bar,
                        float* vert_bar, int* err, ffno_stream_t stream);
 
+/* ffno_xform on tensor cores (split-BF16), same descriptor; M <= 256, every stride and N multiples of 4 floats.
+ * tpack: T [M][K] packed per 128-row m-tile (rows past M zero) and, within it, per 64-wide k-chunk (K padded with
+ * zeros to a multiple of 16; the last chunk narrower), each chunk its hi then lo half in the canonical K-major order
+ * with the chunk's own width; ffno_xform_tc_pack_bytes gives the size. */
+int ffno_xform_tc_pack_bytes(int M, int K);
+int ffno_xform_tc(const void* tpack, const float* in, float* out, const ffno_xform_desc* desc, int accumulate, int* err,
+                  ffno_stream_t stream);
+/* ffno_spectral_mix on tensor cores (split-BF16); wpack = [wbig^T (2C x 2C)]; C = 16, 32, 64; strides multiples of 4
+ * floats. */
+int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, long sb, long s_im, int C,
+                         const void* wpack, const float* g, const float* U, const float* Vm, int rank, int* err,
+                         ffno_stream_t stream);
+
 /* Self-test of the tensor-core primitives (no reference counterpart: it pins this library's tcgen05 descriptor and
- * tensor-memory conventions): D [128][N] = bf16(A [128][K]) @ bf16(B [N][K])^T in FP32, one CTA; K, N multiples of 16
- * up to 256. *status (device int) is set to 1 if the MMA completion wait ran out. */
-int ffno_tc_selftest(const float* A, const float* B, int K, int N, float* D, int* status, ffno_stream_t stream);
+ * tensor-memory conventions): D [128][N] = bf16(A [128][K]) @ bf16(B [N][K])^T in FP32, one CTA, with B staged
+ * K-major (b_mn = 0) or MN-major (b_mn = 1); K, N multiples of 16 up to 256. *status (device int) is set to 1 if the
+ * MMA completion wait ran out. */
+int ffno_tc_selftest(const float* A, const float* B, int K, int N, int b_mn, float* D, int* status,
+                     ffno_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -221,3 +221,61 @@ def test_fuse_bwd_tc(C):
     assert int(err.item()) == 0
     for i in range(3):
         _close(o[3 + i], o[i])
+
+
+@pytest.mark.parametrize("which", ["wf", "hf", "wi", "zf", "zi"])
+def test_xform_tc_matches_fp32(which):
+    from ffnoml_gb300 import tables as tb
+    from ffnoml_gb300.executor import TcXform, _descs
+    nat = _nat()
+    D, H, W, C, live = 12, 24, 20, 16, 13
+    Wf = W // 2 + 1
+    twf, thf, thi, twi = tb.plane_dft(H, W)
+    g = np.random.default_rng(3)
+    tzf, tzi = g.normal(size=(2 * live, D)), g.normal(size=(D, 2 * live))
+    T = dict(wf=twf, hf=thf, wi=twi, zf=tzf, zi=tzi)[which]
+    d = _descs(D, H, W, C, live)[which]
+    n_in = {"wf": D * H * W * C, "hf": D * 2 * H * Wf * C, "wi": D * 2 * H * Wf * C, "zf": D * H * W * C,
+            "zi": 2 * live * H * W * C}[which]
+    n_out = {"wf": D * 2 * H * Wf * C, "hf": D * 2 * H * Wf * C, "wi": D * H * W * C, "zf": 2 * live * H * W * C,
+             "zi": D * H * W * C}[which]
+    x = _rand(n_in, seed=7)
+    a, b = torch.zeros(n_out, device="cuda"), torch.zeros(n_out, device="cuda")
+    Tf = torch.as_tensor(T, dtype=torch.float32).cuda().contiguous()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nat.call("ffno_xform", Tf.data_ptr(), x.data_ptr(), a.data_ptr(), d, 0, _s())
+    tx = TcXform(T, torch.device("cuda"))
+    for r0, rows, packed in tx.slices:
+        dd = nat.XformDesc.from_buffer_copy(d)
+        dd.M = rows
+        nat.call("ffno_xform_tc", _hold(packed), x.data_ptr(), b.data_ptr() + 4 * r0 * d.out_lo, dd, 0,
+                 err.data_ptr(), _s())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    _close(b, a)
+
+
+@pytest.mark.parametrize("C", [16, 32, 64])
+@pytest.mark.parametrize("rank", [0, 4, 8])
+def test_spectral_mix_tc(C, rank):
+    from ffnoml_gb300.executor import tc_pack
+    nat = _nat()
+    F, nb = 37, 150
+    sf, sb, s_im = C, 2 * F * C, F * C            # the horizontal layout [b][2][F][C]
+    x = _rand(nb * 2 * F * C, seed=1)
+    wr, wi = _rand(C, C, seed=2, scale=C ** -0.5), _rand(C, C, seed=3, scale=C ** -0.5)
+    wbig = torch.cat([torch.cat([wr, wi], 1), torch.cat([-wi, wr], 1)], 0).contiguous()
+    gg = _rand(F, 2, seed=4)
+    U = _rand(F, C, max(rank, 1), seed=5) if rank else None
+    Vm = _rand(F, max(rank, 1), C, seed=6) if rank else None
+    ptr = lambda t: None if t is None else t.data_ptr()
+    a, b = torch.zeros_like(x), torch.zeros_like(x)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nat.call("ffno_spectral_mix", x.data_ptr(), a.data_ptr(), F, nb, sf, sb, s_im, C, wbig.data_ptr(), gg.data_ptr(),
+             ptr(U), ptr(Vm), rank, _s())
+    nat.call("ffno_spectral_mix_tc", x.data_ptr(), b.data_ptr(), F, nb, sf, sb, s_im, C,
+             _hold(tc_pack(torch.device("cuda"), wbig.t().cpu())), gg.data_ptr(), ptr(U), ptr(Vm), rank,
+             err.data_ptr(), _s())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    _close(b, a)
