@@ -303,6 +303,10 @@ def run_gb300(args):
                "sample": f"{S[0]}x{S[1]}x{S[2]} sub-cube of the same model, one fwd+VJP "
                          f"({dt:.1f} s), oracle port of the reference FFNO3D in float32 torch"}
 
+    serving = None
+    if rank == 0 and not args.no_serve:
+        serving = serving_stream(model, args.serve_requests, 40.0)
+
     flops_vox = algorithmic_flops_per_voxel(WIDTH, LAYERS, D, H, W, MODES, 12, 2)
     if rank == 0:
         launches = sum(KERNELS_PER_CALL.get(k, 1) * n for k, (_, n) in per.items())
@@ -319,10 +323,75 @@ def run_gb300(args):
                                    "fwd": flops_vox * V / (ms_fwd / 1e3) / 1e12},
             "roofline": roof, "kernel_breakdown_ms": breakdown,
             "clocks": clocks, "gpu_launches": launches * args.steps, "e2e": e2e, "cpu_baseline": cpu,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def serving_stream(model, n_requests, rate, seed=7, slots=4, connections=8):
+    """The mixed-size request stream: Poisson arrivals at `rate` per second, D in {128, 192, 256}, H = W in
+    {32, 64, 96, 128}, PREDICT over the protocol-v2 service (each request on one of `connections` client connections).
+    Returns p50 / p99 latency (send to reply) and aggregate voxels/s."""
+    import threading
+    import queue as q
+
+    from ffnoml_gb300.runtime import GB300Backend
+    from ffnoml_gb300.service import Client, Server
+
+    backend = GB300Backend(model, [f"l{i}" for i in range(12)])
+    srv = Server({"HCA": backend}, "bench", slots=slots)
+    srv.start()
+    g = np.random.default_rng(seed)
+    sizes = [(int(g.choice([128, 192, 256])), int(s), int(s)) for s in g.choice([32, 64, 96, 128], n_requests)]
+    gaps = g.exponential(1.0 / rate, n_requests)
+    inputs = {}
+    for sh in set(sizes):
+        inputs[sh] = synthetic_si(sh, seed=11)
+    # warm every shape once (tables and packs are built on first use)
+    c = Client(srv.port, "bench")
+    for sh in set(sizes):
+        c.request("PREDICT", "HCA", inputs[sh][0], inputs[sh][1], DXY, DXY, 12)
+    c.close()
+    work = q.Queue()
+    lat = [None] * n_requests
+
+    def client_loop():
+        cl = Client(srv.port, "bench")
+        while True:
+            item = work.get()
+            if item is None:
+                break
+            i, t_send = item
+            f, z = inputs[sizes[i]]
+            wait = t_send - time.perf_counter()
+            if wait > 0:
+                time.sleep(wait)
+            t0 = time.perf_counter()
+            cl.request("PREDICT", "HCA", f, z, DXY, DXY, 12)
+            lat[i] = time.perf_counter() - t0
+        cl.close()
+
+    threads = [threading.Thread(target=client_loop) for _ in range(connections)]
+    for t in threads:
+        t.start()
+    t_begin = time.perf_counter()
+    t = t_begin
+    for i in range(n_requests):
+        t += gaps[i]
+        work.put((i, t))
+    for _ in threads:
+        work.put(None)
+    for t_ in threads:
+        t_.join()
+    elapsed = time.perf_counter() - t_begin
+    srv.shutdown()
+    vox = sum(d * h * w for d, h, w in sizes)
+    lat_ms = np.array(lat) * 1e3
+    return {"requests": n_requests, "rate_per_s": rate, "slots": slots, "op": "PREDICT",
+            "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
+            "voxels_per_s": vox / elapsed, "wall_s": elapsed}
 
 
 def roofline_of(name, timing, D, H, W, C, hbm, peaks):
@@ -357,6 +426,8 @@ def main():
     ap.add_argument("--shape", default="256,128,128")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=256)
     args = ap.parse_args()
     args.shape = tuple(int(v) for v in args.shape.split(","))
     if args.impl == "reference":

@@ -18,6 +18,7 @@ back-propagating through it (the reference's per-block activation checkpointing,
 Parameter gradients are not computed: the service's VJP discards them (ffno_fsdp_runtime.py:319-344).
 """
 import math
+import threading
 
 import numpy as np
 import torch
@@ -265,9 +266,14 @@ class Executor:
         self._plane = {}
         self._plane_freq = {}
         self._height = {}
+        self._lock = threading.RLock()        # caches are shared by concurrent service slots
 
     # -------------------------------------------------------------------------------------------- caches
     def packed(self, device):
+        with self._lock:
+            return self._packed_locked(device)
+
+    def _packed_locked(self, device):
         key = (_weights_key(self.model), str(device))
         if self._packed_key != key:
             self._packed = Packed(self.model, device)
@@ -277,6 +283,10 @@ class Executor:
         return self._packed
 
     def plane(self, H, W, device):
+        with self._lock:
+            return self._plane_locked(H, W, device)
+
+    def _plane_locked(self, H, W, device):
         key = (H, W, str(device))
         if key not in self._plane:
             twf, thf, thi, twi = tb.plane_dft(H, W)
@@ -288,6 +298,10 @@ class Executor:
         return self._plane[key]
 
     def plane_freq(self, pk, H, W, dx, dy, device):
+        with self._lock:
+            return self._plane_freq_locked(pk, H, W, dx, dy, device)
+
+    def _plane_freq_locked(self, pk, H, W, dx, dy, device):
         key = (H, W, float(dx), float(dy))
         if key not in self._plane_freq:
             feats = tb.plane_features(H, W, dx, dy)
@@ -297,6 +311,10 @@ class Executor:
         return self._plane_freq[key]
 
     def height(self, pk, geo, device):
+        with self._lock:
+            return self._height_locked(pk, geo, device)
+
+    def _height_locked(self, pk, geo, device):
         key = (geo.column.tobytes(), float(geo.length), geo.k.numel())
         if key not in self._height:
             live, tzf, tzi = tb.height_tables(geo.column, geo.length, geo.k)
@@ -309,13 +327,13 @@ class Executor:
                                      freq=per_block, np=dict(tzf=tzf, tzi=tzi), device=device)
         return self._height[key]
 
-    @staticmethod
-    def tc_table(tabs, name):
+    def tc_table(self, tabs, name):
         """The split-BF16 pack of table `name` (a key of the plane or height dict; suffix _t = transposed), built once."""
         key = "tc_" + name
-        if key not in tabs:
-            base = tabs["np"][name[:-2] if name.endswith("_t") else name]
-            tabs[key] = TcXform(base.T if name.endswith("_t") else base, tabs["device"])
+        with self._lock:
+            if key not in tabs:
+                base = tabs["np"][name[:-2] if name.endswith("_t") else name]
+                tabs[key] = TcXform(base.T if name.endswith("_t") else base, tabs["device"])
         return tabs[key]
 
     def _xf(self, tabs, name, inp, out, desc, ws):

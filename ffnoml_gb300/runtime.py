@@ -7,6 +7,7 @@ m^-3. The model sees D = nz, H = nx, W = ny. Weights and tables stay resident; h
 pinned staging buffers that are reused per shape.
 """
 import hashlib
+import threading
 from pathlib import Path
 
 import numpy as np
@@ -62,8 +63,21 @@ class GB300Backend:
             raise RuntimeError("checkpoint normalization standard deviations must be positive")
         self.name = name
         self.call_count = 0
-        self._flags = torch.zeros(1, dtype=torch.int32, device=self.device)
-        self._staging = {}
+        self._local = threading.local()       # staging buffers and flags per calling thread (service slots)
+
+    @property
+    def _flags(self):
+        loc = self._local
+        if not hasattr(loc, "flags"):
+            loc.flags = torch.zeros(1, dtype=torch.int32, device=self.device)
+        return loc.flags
+
+    @property
+    def _staging(self):
+        loc = self._local
+        if not hasattr(loc, "staging"):
+            loc.staging = {}
+        return loc.staging
 
     @classmethod
     def from_checkpoint(cls, checkpoint_path, factory, level_names, factory_kwargs=None, device="cuda"):
