@@ -35,7 +35,7 @@ DXY = 48e3
 MEAN_X = np.array([4.75, 0.0, 0.0, 0.0, 17.5, -8.0], np.float32)
 STD_X = np.array([2.5 / math.sqrt(12), 5.0, 5.0, 5.0, 7.0 / math.sqrt(12), 8.0 / math.sqrt(12)], np.float32)
 CPU_SAMPLE = (32, 16, 16)       # bounded sub-cube per step of the reference arm (same C, L, M)
-CPU_BASELINE_SAMPLE = (64, 32, 32)  # the cpu_baseline sub-cube (about 10-30 s of fwd+VJP on the host cores)
+CPU_SAMPLE_FULL = (64, 32, 32)  # the cpu_baseline sub-cube (about 10-30 s of fwd+VJP on the host cores)
 KERNELS_PER_CALL = {"ffno_column_info": 3, "ffno_outer": 2}
 
 
@@ -297,7 +297,7 @@ def run_gb300(args):
     if rank == 0 and not args.no_cpu_baseline:
         torch.set_num_threads(len(os.sched_getaffinity(0)))
         state = {k: v.detach().cpu().clone() for k, v in model.state_dict().items()}
-        S = CPU_BASELINE_SAMPLE
+        S = CPU_SAMPLE_FULL
         rate, dt, cores = cpu_rate(state, S, steps=1, warmup=0)
         cpu = {"value": rate, "unit": "voxels/s", "cores": cores, "kind": "port",
                "sample": f"{S[0]}x{S[1]}x{S[2]} sub-cube of the same model, one fwd+VJP "
