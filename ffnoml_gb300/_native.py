@@ -18,7 +18,8 @@ D = ctypes.c_double
 FFNO_MAX_LEVELS = 32
 FFNO_MAX_SPECIES = 4
 
-ERRORS = {1: "invalid argument", 2: "kernel launch failed", 3: "workspace too small", 4: "device wait timed out"}
+ERRORS = {1: "invalid argument", 2: "kernel launch failed", 3: "workspace too small", 4: "device wait timed out",
+          5: "request exceeds the fixed capacity of a non-allocating entry point"}
 
 
 class HeadParams(ctypes.Structure):
@@ -75,6 +76,7 @@ PROTOTYPES = {
     "ffno_depth_weights_bwd": [P, P, I, L, P, P],
     "ffno_outer_parts": [I, I, L],
     "ffno_outer": [P, L, I, P, L, I, L, P, I, P, I, P],
+    "ffno_outer_noalloc": [P, L, I, P, L, I, L, P, I, P],
     "ffno_si_inputs": [P, P, L, P, P, P, P, P, P],
     "ffno_si_populations": [P, L, I, P, P, P, P, P],
     "ffno_si_population_cotangent": [P, P, L, I, P, P, P, P, P],

@@ -3,6 +3,8 @@
 // block's saved inputs instead of storing them.
 #include <math.h>
 
+#include <mutex>
+
 #include "common.cuh"
 
 using namespace ffno;
@@ -972,6 +974,58 @@ int ffno_outer(const float* A, long lda, int Ma, const float* B, long ldb, int M
   k_outer<<<(unsigned)((long)ti * tj * nsplit), NT, 0, s>>>(A, lda, Ma, B, ldb, Mb, N, chunk, ti, tj, part);
   const long n = (long)Ma * Mb;
   k_outer_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(part, nsplit, n, out, accumulate);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+// ---------------------------------------------------------------------------------------------- no-allocation variant
+// ffno_outer_noalloc: the same product as ffno_outer for hosts that cannot hand this library a scratch buffer on every
+// call. A process that binds the C ABI from its own runtime (a Julia, Go or Java host whose device memory belongs to
+// that runtime's own pool allocator, or a service that must not grow its footprint after start-up) often has no way to
+// call cudaMalloc for us, and the split-K partial sums need somewhere to live. They live here instead: a fixed array in
+// the library's own device memory, present on every GPU that loads the library until the process exits.
+}  // extern "C"
+
+namespace {
+
+constexpr long kOuterScratchFloats = 4L << 20;  // 16 MiB: Ma * Mb * nsplit partial sums at most
+__device__ __align__(256) float g_outer_scratch[kOuterScratchFloats];
+
+std::mutex g_outer_scratch_mutex;
+float* g_outer_scratch_ptr[256] = {};  // device address of g_outer_scratch per device ordinal, set on first use
+
+}  // namespace
+
+extern "C" {
+
+int ffno_outer_noalloc(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, double* out,
+                       int accumulate, ffno_stream_t stream) {
+  if (!A || !B || !out || Ma < 1 || Mb < 1 || N < 1) return FFNO_EINVAL;
+  const long n = (long)Ma * Mb;
+  if (n > kOuterScratchFloats) return FFNO_ETOOBIG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return FFNO_EINVAL;
+  float* scratch = nullptr;
+  {
+    // The host-side name g_outer_scratch is not a device address: ask the runtime for it once per device, with that
+    // device current.
+    std::lock_guard<std::mutex> lock(g_outer_scratch_mutex);
+    if (!g_outer_scratch_ptr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_outer_scratch) != cudaSuccess || !p) return FFNO_ELAUNCH;
+      g_outer_scratch_ptr[dev] = static_cast<float*>(p);
+    }
+    scratch = g_outer_scratch_ptr[dev];
+  }
+  long nsplit = ffno_outer_parts(Ma, Mb, N);
+  if (nsplit > kOuterScratchFloats / n) nsplit = kOuterScratchFloats / n;
+  const int ti = (Ma + 63) / 64, tj = (Mb + 63) / 64;
+  long chunk = (N + nsplit - 1) / nsplit;
+  chunk = (chunk + 15) / 16 * 16;
+  cudaStream_t s = (cudaStream_t)stream;
+  // every partial sum the reduction reads is written first by k_outer: nothing in the scratch has to start at zero
+  k_outer<<<(unsigned)((long)ti * tj * nsplit), NT, 0, s>>>(A, lda, Ma, B, ldb, Mb, N, chunk, ti, tj, scratch);
+  k_outer_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(scratch, nsplit, n, out, accumulate);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

@@ -35,6 +35,7 @@ extern "C" {
 #define FFNO_ELAUNCH 2     /* a kernel launch failed (cudaGetLastError) */
 #define FFNO_ENOMEM 3      /* the caller's workspace is too small */
 #define FFNO_ETIMEOUT 4    /* a bounded device wait ran out */
+#define FFNO_ETOOBIG 5     /* the request exceeds the fixed capacity of a non-allocating entry point */
 
 typedef void* ffno_stream_t; /* cudaStream_t */
 
@@ -201,6 +202,18 @@ int ffno_depth_weights_bwd(const float* z, const float* w_bar, int D, long HW, f
 int ffno_outer_parts(int Ma, int Mb, long N);
 int ffno_outer(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, float* part, int nsplit,
                double* out, int accumulate, ffno_stream_t stream);
+
+/* ffno_outer without a caller-provided scratch buffer. No counterpart in the reference: it exists for hosts that bind
+ * this C ABI but cannot allocate device memory for the library on each call (their device memory belongs to their own
+ * runtime's allocator, or they must not allocate after start-up). The partial sums live in a fixed 16 MiB array inside
+ * the library (held on every GPU that loads it until the process exits), so Ma * Mb may be at most 4 Mi (4194304);
+ * larger requests return FFNO_ETOOBIG without touching the device. Allocates nothing. The first call on each device
+ * looks up the array's device address (with that device current); make that first call before any stream capture.
+ * Every call shares the one array, so calls that overlap on the GPU (other streams, other threads) race; nothing in it
+ * needs to start at zero. Same result as ffno_outer with the same nsplit; fewer splits when the array is too small
+ * for the usual count (the sums are then added in a different order). */
+int ffno_outer_noalloc(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, double* out,
+                       int accumulate, ffno_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------------------------------
  * Service conversions (ffno_fsdp_runtime.py). flags is one device int, OR-ed: 1 non-finite input, 2 T <= 0,

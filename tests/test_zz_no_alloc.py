@@ -1,0 +1,42 @@
+"""ffno_outer_noalloc, the non-allocating twin of ffno_outer, through the C ABI: two calls in a row (different
+shapes, so the shared scratch is reused with other contents in it) against ffno_outer with caller scratch, and the
+refusal of a product beyond its fixed capacity. It serves hosts that bind the C ABI but cannot allocate device memory
+for the library on each call. Collected last so that a run stopping at the first failure has run every other test."""
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _outer_pair(Ma, Mb, N, seed):
+    from ffnoml_gb300 import _native as nat
+    g = torch.Generator().manual_seed(seed)
+    A = torch.randn(Ma, N, generator=g).cuda()
+    B = torch.randn(Mb, N, generator=g).cuda()
+    s = torch.cuda.current_stream().cuda_stream
+    nsplit = nat.lib().ffno_outer_parts(Ma, Mb, N)
+    part = torch.empty(nsplit * Ma * Mb, device="cuda")
+    ref = torch.empty(Ma, Mb, dtype=torch.float64, device="cuda")
+    got = torch.full((Ma, Mb), float("nan"), dtype=torch.float64, device="cuda")
+    nat.call("ffno_outer", A.data_ptr(), N, Ma, B.data_ptr(), N, Mb, N, part.data_ptr(), nsplit, ref.data_ptr(), 0, s)
+    nat.call("ffno_outer_noalloc", A.data_ptr(), N, Ma, B.data_ptr(), N, Mb, N, got.data_ptr(), 0, s)
+    torch.cuda.synchronize()
+    exact = A.double() @ B.double().t()
+    return ref, got, exact
+
+
+def test_noalloc_outer_matches_outer_on_two_calls():
+    for Ma, Mb, N, seed in ((256, 64, 200_000, 1), (72, 130, 50_000, 2)):
+        ref, got, exact = _outer_pair(Ma, Mb, N, seed)
+        scale = exact.abs().max()
+        assert ((got - ref).abs().max() / scale).item() < 1e-6
+        assert ((got - exact).abs().max() / scale).item() < 1e-5
+
+
+def test_noalloc_outer_refuses_oversized_products():
+    from ffnoml_gb300 import _native as nat
+    A = torch.zeros(16, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    status = nat.lib().ffno_outer_noalloc(A.data_ptr(), 1, 4096, A.data_ptr(), 1, 2048, 1, out.data_ptr(), 0,
+                                          torch.cuda.current_stream().cuda_stream)
+    assert status == 5
