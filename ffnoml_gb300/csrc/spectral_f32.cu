@@ -13,7 +13,7 @@ constexpr int XM = 64, XN = 64, XK = 16;
 // (rows ty + 16 i, columns tx + 16 j).
 __global__ void __launch_bounds__(NT) k_xform(const float* __restrict__ T, const float* __restrict__ in,
                                               float* __restrict__ out, ffno_xform_desc d, long ntn, long ntm,
-                                              int accumulate) {
+                                              int accumulate, long t_b) {
   __shared__ float ts[XM][XK + 1];
   __shared__ float is[XK][XN + 4];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -26,6 +26,7 @@ __global__ void __launch_bounds__(NT) k_xform(const float* __restrict__ T, const
   const long b1 = b / d.nb2, b2 = b % d.nb2;
   const float* ib = in + b1 * d.in_b1 + b2 * d.in_b2;
   float* ob = out + b1 * d.out_b1 + b2 * d.out_b2;
+  T += b * t_b;  // a table per batch element (t_b = 0: one shared table)
   const int m0 = (int)(tm * XM);
   const long n0 = tn * XN;
   float acc[4][4];
@@ -179,7 +180,46 @@ int ffno_xform(const float* T, const float* in, float* out, const ffno_xform_des
   const long ntn = (d.N + XN - 1) / XN, ntm = (d.M + XM - 1) / XM;
   const long blocks = ntn * ntm * d.nb;
   if (blocks > 0x7fffffffL) return FFNO_EINVAL;
-  k_xform<<<(unsigned)blocks, NT, 0, (cudaStream_t)stream>>>(T, in, out, d, ntn, ntm, accumulate);
+  k_xform<<<(unsigned)blocks, NT, 0, (cudaStream_t)stream>>>(T, in, out, d, ntn, ntm, accumulate, 0L);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_xform_pt(const float* T, long t_b, const float* in, float* out, const ffno_xform_desc* desc, int accumulate,
+                  ffno_stream_t stream) {
+  if (!T || !in || !out || !desc || t_b < 0) return FFNO_EINVAL;
+  const ffno_xform_desc& d = *desc;
+  if (d.nb < 1 || d.nb2 < 1 || d.K < 1 || d.M < 1 || d.N < 1 || d.in_split < 1 || d.out_split < 1)
+    return FFNO_EINVAL;
+  const long ntn = (d.N + XN - 1) / XN, ntm = (d.M + XM - 1) / XM;
+  const long blocks = ntn * ntm * d.nb;
+  if (blocks > 0x7fffffffL) return FFNO_EINVAL;
+  k_xform<<<(unsigned)blocks, NT, 0, (cudaStream_t)stream>>>(T, in, out, d, ntn, ntm, accumulate, t_b);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+// out[col][i][j] (+)= sum_c A[i*rs + col*C + c] * B[j*rs + col*C + c] (double), one CTA per column: the per-column
+// height-table gradients.
+__global__ void k_col_outer(const float* __restrict__ A, int Ra, const float* __restrict__ B, int Rb, long ncol, int C,
+                            long rs, double* __restrict__ out, int accumulate) {
+  const long col = blockIdx.x;
+  if (col >= ncol) return;
+  for (int e = threadIdx.x; e < Ra * Rb; e += blockDim.x) {
+    const int i = e / Rb, j = e % Rb;
+    const float* a = A + (long)i * rs + col * C;
+    const float* b = B + (long)j * rs + col * C;
+    double s = 0.0;
+    for (int c = 0; c < C; ++c) s += (double)a[c] * (double)b[c];
+    double* o = out + (col * Ra + i) * (long)Rb + j;
+    *o = accumulate ? *o + s : s;
+  }
+}
+
+int ffno_col_outer(const float* A, int Ra, const float* B, int Rb, long ncol, int C, long row_stride, double* out,
+                   int accumulate, ffno_stream_t stream) {
+  if (!A || !B || !out || Ra < 1 || Rb < 1 || ncol < 1 || C < 1 || ncol > 0x7fffffffL) return FFNO_EINVAL;
+  k_col_outer<<<(unsigned)ncol, 256, 0, (cudaStream_t)stream>>>(A, Ra, B, Rb, ncol, C, row_stride, out, accumulate);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

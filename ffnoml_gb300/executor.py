@@ -17,6 +17,7 @@ The input VJP keeps only the block inputs from the forward pass and recomputes e
 back-propagating through it (the reference's per-block activation checkpointing, models/ffno_model.py:751-780).
 Parameter gradients are not computed: the service's VJP discards them (ffno_fsdp_runtime.py:319-344).
 """
+import hashlib
 import math
 import threading
 
@@ -226,9 +227,10 @@ class FreqTables:
 
 
 class Geometry:
-    def __init__(self, shared, span, column, column_raw, length, k):
+    def __init__(self, shared, span, column, column_raw, length, k, columns=None):
         self.shared, self.span, self.column, self.column_raw, self.length, self.k = (shared, span, column, column_raw,
                                                                                      length, k)
+        self.columns = columns      # non-shared grids: every sample's columns [B][H*W][D] (float64, unshifted)
 
 
 class Workspace:
@@ -240,6 +242,7 @@ class Workspace:
         Wf = W // 2 + 1
         f32 = dict(dtype=torch.float32, device=device)
         self.V = V
+        self.live = live
         self.nparts = nat.lib().ffno_stats_parts(V)
         self.nparts_tc = nat.lib().ffno_tc_parts(V)
         nb = lambda *s: torch.empty(*s, **f32)
@@ -363,15 +366,41 @@ class Executor:
         col = z_scale[:, :, 0, 0]
         host = torch.cat([info.reshape(-1), col.reshape(-1)]).cpu()
         info_h = host[:2 * B].reshape(B, 2)
-        cols = host[2 * B:].reshape(B, D).double().numpy()
+        cols32 = host[2 * B:].reshape(B, D).numpy()
+        cols = cols32.astype(np.float64)
         shared_each = bool((info_h[:, 0] > 0.5).all())
         span = float(info_h[:, 1].max())
+        shifted32 = cols32 - cols32.min(axis=1, keepdims=True)       # the test in the model's float32
+        shared = shared_each and bool((shifted32 == shifted32[:1]).all())
         shifted = cols - cols.min(axis=1, keepdims=True)
-        shared = shared_each and bool((shifted == shifted[:1]).all())
         m = self.model
         modes = int(math.floor(m.z_reference_length / m.z_min_wavelength)) + 1
         length, k = tb.height_box(span, m.z_reference_length, m.z_min_wavelength, modes)
-        return Geometry(shared, span, shifted[0], cols[0], length, k)
+        columns = None
+        if not shared:
+            columns = z_scale.reshape(B, D, HW).transpose(1, 2).double().cpu().numpy()
+        return Geometry(shared, span, shifted[0], cols[0], length, k, columns)
+
+    def height_percol(self, pk, geo, b, device):
+        """Per-column tables of sample b when the height grids differ (cached by the sample's heights)."""
+        cols = geo.columns[b]
+        key = ("percol", hashlib.sha1(cols.tobytes()).hexdigest(), cols.shape, float(geo.length), geo.k.numel())
+        with self._lock:
+            if key not in self._height:
+                # per-column tables are large ([H*W][2M'][D] each): keep only the two most recent samples
+                old = [k for k in self._height if k[0] == "percol"]
+                for k in old[:-1]:
+                    del self._height[k]
+                live, tzf, tzi = tb.percolumn_tables(cols, geo.length, geo.k)
+                feats = tb.height_features(geo.k[:live], self.model.z_feature_wavelength)
+                rank = self.model.freq_mix_rank
+                per_block = [FreqTables(*tb.freq_tables(pk.freq_params, f"blocks.{i}.vertical", feats, rank), device)
+                             for i in range(self.model.n_layers)]
+                f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device=device)
+                self._height[key] = dict(live=live, percol=True, tzf=f(tzf), tzi=f(tzi),
+                                         tzf_t=f(tzf.transpose(0, 2, 1)), tzi_t=f(tzi.transpose(0, 2, 1)),
+                                         freq=per_block, columns=cols)
+            return self._height[key]
 
     # -------------------------------------------------------------------------------------------- setup
     def _setup(self, x, z_scale, dx, dy):
@@ -392,9 +421,7 @@ class Executor:
         device = x.device
         pk = self.packed(device)
         geo = self.geometry(z_scale)
-        if not geo.shared:
-            raise NotImplementedError("per-column height grids are not supported by the GB300 path yet")
-        hgt = self.height(pk, geo, device)
+        hgt = self.height(pk, geo, device) if geo.shared else None
         B, _, D, H, W = x.shape
         pln = self.plane(H, W, device)
         pfr = self.plane_freq(pk, H, W, dx, dy, device)
@@ -410,15 +437,18 @@ class Executor:
         pk, geo, hgt, pln, pfr = self._setup(x, z_scale, dx, dy)
         B, _, D, H, W = x.shape
         out = torch.empty(B, m.out_channels, D, H, W, dtype=torch.float32, device=x.device)
-        ws = Workspace(D, H, W, m.width, hgt["live"], pk.groups, x.device)
         saved = []
+        ws = None
         for b in range(B):
+            hgt_b = hgt if geo.shared else self.height_percol(pk, geo, b, x.device)
+            if ws is None or ws.live != hgt_b["live"]:
+                ws = Workspace(D, H, W, m.width, hgt_b["live"], pk.groups, x.device)
             xin, z = x[b], z_scale[b]
             self._depth_weights(ws, z, D, H * W)
             self._lift(pk, ws, xin)
             inputs = [ws.x.clone()] if keep else None
             for i in range(m.n_layers):
-                self._block(pk, ws, i, z, D, H, W, hgt, pln, pfr[i])
+                self._block(pk, ws, i, z, D, H, W, hgt_b, pln, pfr[i])
                 if keep:
                     inputs.append(ws.x.clone())
             self._head(pk, ws.x, xin, out[b])
@@ -482,9 +512,16 @@ class Executor:
         self._finalize(ws, "spec", bp["spec_g"], bp["spec_b"], tc)
         # vertical (height) branch
         hq = hgt["freq"][i]
-        self._xf(hgt, "tzf", ws.xv, ws.va, d["zf"], ws)
-        self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, False)
-        self._xf(hgt, "tzi", ws.vb, ws.yv, d["zi"], ws)
+        if hgt.get("percol"):
+            nat.call("ffno_xform_pt", hgt["tzf"].data_ptr(), 2 * live * D, ws.xv.data_ptr(), ws.va.data_ptr(),
+                     d["pcf"], 0, s)
+            self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, False)
+            nat.call("ffno_xform_pt", hgt["tzi"].data_ptr(), 2 * live * D, ws.vb.data_ptr(), ws.yv.data_ptr(),
+                     d["pci"], 0, s)
+        else:
+            self._xf(hgt, "tzf", ws.xv, ws.va, d["zf"], ws)
+            self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, False)
+            self._xf(hgt, "tzi", ws.vb, ws.yv, d["zi"], ws)
         tc = self._mlp2(ws, 0, ws.yv, None, None, 0.0, None, bp["v_p1"], bp["v_p2"], bp.get("tc_v_post"),
                         ws.vert_pre)
         self._finalize(ws, "vert", bp["vert_g"], bp["vert_b"], tc)
@@ -569,12 +606,21 @@ class Executor:
         ybar = ybar.contiguous()
         xbar_in = torch.zeros_like(x)
         zbar = torch.zeros_like(z_scale)
-        live = hgt["live"]
-        ws = Workspace(D, H, W, C, live, pk.groups, dev)
-        gb = _GradBuffers(D, H, W, C, live, pk.groups, ws.nparts, dev)
-        tzf_bar = torch.zeros(2 * live, D, dtype=torch.float64, device=dev)
-        tzi_bar = torch.zeros(D, 2 * live, dtype=torch.float64, device=dev)
+        ws = gb = None
+        if geo.shared:
+            live = hgt["live"]
+            tzf_bar = torch.zeros(2 * live, D, dtype=torch.float64, device=dev)
+            tzi_bar = torch.zeros(D, 2 * live, dtype=torch.float64, device=dev)
         for b in range(B):
+            hgt_b = hgt if geo.shared else self.height_percol(pk, geo, b, dev)
+            live = hgt_b["live"]
+            if ws is None or ws.live != live:
+                ws = Workspace(D, H, W, C, live, pk.groups, dev)
+                gb = _GradBuffers(D, H, W, C, live, pk.groups, ws.nparts, dev)
+            if not geo.shared:
+                # this sample's per-column table gradients: [HW][2M'][D] and [HW][D][2M']
+                tzf_bar = torch.zeros(HW, 2 * live, D, dtype=torch.float64, device=dev)
+                tzi_bar = torch.zeros(HW, D, 2 * live, dtype=torch.float64, device=dev)
             xin, z = x[b], z_scale[b]
             inputs = state["inputs"][b]
             self._depth_weights(ws, z, D, HW)
@@ -584,17 +630,23 @@ class Executor:
                      pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.p2t.data_ptr(), pk.p1t.data_ptr(),
                      pk.nhp, pk.head, gb.xbar.data_ptr(), xbar_in[b].data_ptr(), s)
             for i in reversed(range(m.n_layers)):
-                self._block(pk, ws, i, z, D, H, W, hgt, pln, pfr[i], x_in=inputs[i])
-                self._block_bwd(pk, ws, gb, i, inputs[i], z, zbar[b], D, H, W, hgt, pln, pfr[i], tzf_bar, tzi_bar)
+                self._block(pk, ws, i, z, D, H, W, hgt_b, pln, pfr[i], x_in=inputs[i])
+                self._block_bwd(pk, ws, gb, i, inputs[i], z, zbar[b], D, H, W, hgt_b, pln, pfr[i], tzf_bar, tzi_bar)
             # lift: x0 = gelu(GN(pre0))
             self._lift(pk, ws, xin)
             self._gn_bwd(ws, gb, 1, gb.xbar, 1.0, ws.pre, pk.lift_g, pk.lift_b, "lift", gb.pbar)
             nat.call("ffno_lift_bwd", gb.pbar.data_ptr(), Cin, V, C, pk.lift_w.data_ptr(), xbar_in[b].data_ptr(), s)
             nat.call("ffno_depth_weights_bwd", z.data_ptr(), gb.wbar.data_ptr(), D, HW, zbar[b].data_ptr(), s)
-        # the height tables depend on the shared column (sample 0, column (0, 0)): their gradient goes there
-        gcol = tb.height_tables_vjp(geo.column_raw, geo.length, geo.k, live, tzf_bar.cpu().numpy(),
-                                    tzi_bar.cpu().numpy())
-        zbar[0, :, 0, 0] += torch.as_tensor(gcol, dtype=torch.float32, device=dev)
+            if not geo.shared:
+                # every column's own tables depend on that column's heights
+                gcols = tb.percolumn_tables_vjp(geo.columns[b], geo.length, geo.k, live, tzf_bar.cpu().numpy(),
+                                                tzi_bar.cpu().numpy())                     # [HW][D]
+                zbar[b] += torch.as_tensor(gcols.T.reshape(D, H, W), dtype=torch.float32, device=dev)
+        if geo.shared:
+            # the height tables depend on the shared column (sample 0, column (0, 0)): their gradient goes there
+            gcol = tb.height_tables_vjp(geo.column_raw, geo.length, geo.k, live, tzf_bar.cpu().numpy(),
+                                        tzi_bar.cpu().numpy())
+            zbar[0, :, 0, 0] += torch.as_tensor(gcol, dtype=torch.float32, device=dev)
         self._check(ws)
         return xbar_in, zbar
 
@@ -668,13 +720,24 @@ class Executor:
         # vertical transposes (ws.vb holds the mixed modes, ws.xv the transform input)
         hq = hgt["freq"][i]
         N = HW * C
-        nat.call("ffno_outer", gb.yvb.data_ptr(), N, D, ws.vb.data_ptr(), N, 2 * live, N, gb.opart.data_ptr(),
-                 gb.osplit_i, tzi_bar.data_ptr(), 1, s)
-        self._xf(hgt, "tzi_t", gb.yvb, ws.va, d["zf"], ws)
-        self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, True)
-        nat.call("ffno_outer", ws.vb.data_ptr(), N, 2 * live, ws.xv.data_ptr(), N, D, N, gb.opart.data_ptr(),
-                 gb.osplit_f, tzf_bar.data_ptr(), 1, s)
-        self._xf(hgt, "tzf_t", ws.vb, gb.xvb, d["zi"], ws)
+        if hgt.get("percol"):
+            nat.call("ffno_col_outer", gb.yvb.data_ptr(), D, ws.vb.data_ptr(), 2 * live, HW, C, N,
+                     tzi_bar.data_ptr(), 1, s)
+            nat.call("ffno_xform_pt", hgt["tzi_t"].data_ptr(), 2 * live * D, gb.yvb.data_ptr(), ws.va.data_ptr(),
+                     d["pcf"], 0, s)
+            self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, True)
+            nat.call("ffno_col_outer", ws.vb.data_ptr(), 2 * live, ws.xv.data_ptr(), D, HW, C, N,
+                     tzf_bar.data_ptr(), 1, s)
+            nat.call("ffno_xform_pt", hgt["tzf_t"].data_ptr(), 2 * live * D, ws.vb.data_ptr(), gb.xvb.data_ptr(),
+                     d["pci"], 0, s)
+        else:
+            nat.call("ffno_outer", gb.yvb.data_ptr(), N, D, ws.vb.data_ptr(), N, 2 * live, N, gb.opart.data_ptr(),
+                     gb.osplit_i, tzi_bar.data_ptr(), 1, s)
+            self._xf(hgt, "tzi_t", gb.yvb, ws.va, d["zf"], ws)
+            self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, True)
+            nat.call("ffno_outer", ws.vb.data_ptr(), N, 2 * live, ws.xv.data_ptr(), N, D, N, gb.opart.data_ptr(),
+                     gb.osplit_f, tzf_bar.data_ptr(), 1, s)
+            self._xf(hgt, "tzf_t", ws.vb, gb.xvb, d["zi"], ws)
         # input gates (and z_proj)
         if tc:
             nat.call("ffno_gate_bwd_tc", x.data_ptr(), gb.xsb.data_ptr(), gb.xacc.data_ptr(), V, C,
@@ -725,6 +788,11 @@ def _descs(D, H, W, C, live):
                  in_split=big, in_hi=0, in_lo=HW * C, out_split=big, out_hi=0, out_lo=HW * C)
     d["zi"] = XD(nb=1, nb2=1, in_b1=0, in_b2=0, out_b1=0, out_b2=0, K=2 * live, M=D, N=HW * C,
                  in_split=big, in_hi=0, in_lo=HW * C, out_split=big, out_hi=0, out_lo=HW * C)
+    # per-column height transforms (a table per column, batch = column, n = channel)
+    d["pcf"] = XD(nb=HW, nb2=1, in_b1=C, in_b2=0, out_b1=C, out_b2=0, K=D, M=2 * live, N=C,
+                  in_split=big, in_hi=0, in_lo=HW * C, out_split=big, out_hi=0, out_lo=HW * C)
+    d["pci"] = XD(nb=HW, nb2=1, in_b1=C, in_b2=0, out_b1=C, out_b2=0, K=2 * live, M=D, N=C,
+                  in_split=big, in_hi=0, in_lo=HW * C, out_split=big, out_hi=0, out_lo=HW * C)
     return d
 
 

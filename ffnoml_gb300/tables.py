@@ -95,11 +95,11 @@ def taper(column, k):
 
 
 def filon(z, k):
-    """Filon weights (q_re, q_im) [D][M] of the piecewise-linear column z [D] at wavenumbers k [M], float64
+    """Filon weights (q_re, q_im) [..., D, M] of piecewise-linear columns z [..., D] at wavenumbers k [M], float64
     (height_fourier_weights, models/ffno_model.py:37-64): sum_j x_j q_jm = integral of x(z) e^{-i k_m z} dz."""
     z = np.asarray(z, dtype=np.float64)
     k = np.asarray(k, dtype=np.float64)
-    za, zb = z[:-1, None], z[1:, None]
+    za, zb = z[..., :-1, None], z[..., 1:, None]
     lo = np.minimum(za, zb)
     h = np.abs(zb - za)
     th = h * k
@@ -118,13 +118,42 @@ def filon(z, k):
     up = za <= zb
     a_re, a_im = np.where(up, lo_re, hi_re), np.where(up, lo_im, hi_im)
     b_re, b_im = np.where(up, hi_re, lo_re), np.where(up, hi_im, lo_im)
-    D, M = len(z), len(k)
-    q_re, q_im = np.zeros((D, M)), np.zeros((D, M))
-    q_re[:-1] += a_re
-    q_im[:-1] += a_im
-    q_re[1:] += b_re
-    q_im[1:] += b_im
+    shape = z.shape + (len(k),)
+    q_re, q_im = np.zeros(shape), np.zeros(shape)
+    q_re[..., :-1, :] += a_re
+    q_im[..., :-1, :] += a_im
+    q_re[..., 1:, :] += b_re
+    q_im[..., 1:, :] += b_im
     return q_re, q_im
+
+
+def column_tapers(columns, k):
+    """taper() for many columns [ncol, D] at once: [ncol, M]."""
+    cols = np.asarray(columns, dtype=np.float64)
+    dz = np.sort(np.abs(np.diff(cols, axis=-1)), axis=-1)[..., (cols.shape[-1] - 2) // 2]
+    kn = math.pi / dz[..., None]
+    u = np.clip((k.numpy()[None] - 2 * kn / 3) / (kn / 3), 0.0, 1.0)
+    return 0.5 * (1 + np.cos(math.pi * u))
+
+
+def percolumn_tables(z_raw, length, k):
+    """Per-column tables when the columns' height grids differ (the reference's non-shared path,
+    models/ffno_model.py:276-280, 306-308): z_raw [ncol, D] heights of each column (unshifted). Returns live modes M'
+    (the largest live count over the columns), tzf [ncol][2M'][D] and tzi [ncol][D][2M'] with each column's own
+    taper, float64."""
+    z = np.asarray(z_raw, dtype=np.float64)
+    z = z - z.min(axis=-1, keepdims=True)
+    tap = column_tapers(z, k)
+    live = max(1, int((tap > 0).sum(axis=-1).max()))
+    kk = k.numpy()[:live]
+    q_re, q_im = filon(z, kk)                                   # [ncol, D, M']
+    factor = np.full(live, 2.0)
+    factor[0] = 1.0
+    f = factor[None] * tap[:, :live] / length                   # [ncol, M']
+    ph = z[..., None] * kk                                      # [ncol, D, M']
+    tzf = np.concatenate([q_re.transpose(0, 2, 1), q_im.transpose(0, 2, 1)], axis=1)
+    tzi = np.concatenate([np.cos(ph) * f[:, None], -np.sin(ph) * f[:, None]], axis=2)
+    return live, tzf, tzi
 
 
 def height_tables(column, length, k):
@@ -164,8 +193,8 @@ def freq_tables(params, prefix, features, rank):
 
 # ------------------------------------------------------------------------------------------------ table adjoint
 def _filon_torch(z, k):
-    """filon() in torch float64 (differentiable in z)."""
-    za, zb = z[:-1, None], z[1:, None]
+    """filon() in torch float64 (differentiable in z), columns z [..., D]."""
+    za, zb = z[..., :-1, None], z[..., 1:, None]
     lo = torch.minimum(za, zb)
     h = (zb - za).abs()
     th = h * k
@@ -185,6 +214,29 @@ def _filon_torch(z, k):
     b_re, b_im = torch.where(up, hi_re, lo_re), torch.where(up, hi_im, lo_im)
     pad_end, pad_start = (0, 0, 0, 1), (0, 0, 1, 0)
     return (F.pad(a_re, pad_end) + F.pad(b_re, pad_start), F.pad(a_im, pad_end) + F.pad(b_im, pad_start))
+
+
+def percolumn_tables_vjp(z_raw, length, k, live, tzf_bar, tzi_bar):
+    """Gradient w.r.t. z_raw [ncol, D] of percolumn_tables along (tzf_bar [ncol][2M'][D], tzi_bar [ncol][D][2M']),
+    by float64 autograd: each column's shift by its minimum, Filon weights, phases and taper."""
+    with torch.enable_grad():
+        zr = torch.as_tensor(np.asarray(z_raw, dtype=np.float64)).requires_grad_(True)
+        z = zr - zr.amin(dim=-1, keepdim=True)
+        kk = k[:live].double()
+        dz = (z[..., 1:] - z[..., :-1]).abs().median(dim=-1).values[..., None]
+        kn = math.pi / dz
+        u = ((kk - 2 * kn / 3) / (kn / 3)).clamp(0, 1)
+        tap = 0.5 * (1 + torch.cos(math.pi * u))                  # [ncol, M']
+        factor = torch.full((live,), 2.0, dtype=torch.float64)
+        factor[0] = 1.0
+        f = factor * tap / length
+        q_re, q_im = _filon_torch(z, kk)                          # [ncol, D, M']
+        ph = z[..., None] * kk
+        tzf = torch.cat([q_re.transpose(1, 2), q_im.transpose(1, 2)], 1)
+        tzi = torch.cat([torch.cos(ph) * f[:, None], -torch.sin(ph) * f[:, None]], 2)
+        loss = (tzf * torch.as_tensor(tzf_bar)).sum() + (tzi * torch.as_tensor(tzi_bar)).sum()
+        (g,) = torch.autograd.grad(loss, zr)
+    return g.numpy()
 
 
 def height_tables_vjp(column_raw, length, k, live, tzf_bar, tzi_bar):

@@ -133,6 +133,14 @@ typedef struct {
 } ffno_xform_desc;
 int ffno_xform(const float* T, const float* in, float* out, const ffno_xform_desc* desc, int accumulate,
                ffno_stream_t stream);
+/* ffno_xform with a table per batch element: batch b uses T + b * t_b (b = b1 * nb2 + b2): the per-column Filon
+ * transforms of HeightSpectralConv when the columns' height grids differ (models/ffno_model.py:276-280, 306-308). */
+int ffno_xform_pt(const float* T, long t_b, const float* in, float* out, const ffno_xform_desc* desc, int accumulate,
+                  ffno_stream_t stream);
+/* Per-column table gradients: out [ncol][Ra][Rb] (double; = or +=) with out[col][i][j] = sum_c A[i][col][c] *
+ * B[j][col][c], A and B laid [rows][ncol][C] with row stride row_stride floats. */
+int ffno_col_outer(const float* A, int Ra, const float* B, int Rb, long ncol, int C, long row_stride, double* out,
+                   int accumulate, ffno_stream_t stream);
 
 /* Per-frequency complex channel mixing (SpectralConv2dFull.mix_spectrum :394-429; HeightSpectralConv mode mixing
  * :282-300): for each frequency f < F and row b < nb, with xhat = re + i im at offset f*sf + b*sb (im at +s_im):

@@ -7,8 +7,6 @@ from golden_io import CASES, load, model_config
 
 pytestmark = pytest.mark.gpu
 
-SHARED = [c for c in CASES if c != "per_column"]
-
 
 def _model(meta, state):
     from ffnoml_gb300 import FFNO3D
@@ -17,7 +15,7 @@ def _model(meta, state):
     return m.cuda().eval().set_precision("bf16")
 
 
-@pytest.mark.parametrize("name", SHARED)
+@pytest.mark.parametrize("name", CASES)
 def test_bf16_forward_and_vjp(name):
     meta, state, a = load(name)
     model = _model(meta, state)

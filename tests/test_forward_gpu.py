@@ -7,8 +7,6 @@ from golden_io import CASES, load, model_config
 
 pytestmark = pytest.mark.gpu
 
-SHARED = [c for c in CASES if c != "per_column"]
-
 
 def _model(meta, state):
     from ffnoml_gb300 import FFNO3D
@@ -18,7 +16,7 @@ def _model(meta, state):
     return m.cuda().eval()
 
 
-@pytest.mark.parametrize("name", SHARED)
+@pytest.mark.parametrize("name", CASES)
 def test_forward_matches_reference_float64(name):
     meta, state, a = load(name)
     model = _model(meta, state)
