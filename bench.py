@@ -5,9 +5,11 @@ Workload (the scaled configuration): FFNO3D width 64, 8 blocks, height operator 
 (z_min_wavelength = 40/31), H + Ca II level-fraction head (12 levels), one cube [1, 6, 256, 128, 128] = 4.19 M voxels,
 synthetic seeded inputs with the reference's channel distributions, random-init weights of that architecture.
 
-A step is one forward pass plus one input VJP (per-block recompute) over the cube, inputs resident in HBM (value);
+A step is one forward pass plus one input VJP (per-block recompute) over the cube, inputs resident in HBM (value), in
+the BF16 tensor-core form by default; the plain FP32 drop-in runs on the same cube for the speed-up and the BF16 error.
 e2e is the same step through the service backend's vjp_local with host numpy buffers (host<->device copies inside the
-timed region). The cube (GBs of activations) is far larger than L2, so no flush is needed between steps.
+timed region). The cube (GBs of activations) is far larger than L2, so no flush is needed between steps. The serving
+stream (256 mixed-size PREDICT requests, Poisson arrivals at 40 per second) reports p50 / p99 latency.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--precision fp32|bf16]
 
@@ -37,6 +39,7 @@ STD_X = np.array([2.5 / math.sqrt(12), 5.0, 5.0, 5.0, 7.0 / math.sqrt(12), 8.0 /
 CPU_SAMPLE = (32, 16, 16)       # bounded sub-cube per step of the reference arm (same C, L, M)
 CPU_SAMPLE_FULL = (64, 32, 32)  # the cpu_baseline sub-cube (about 10-30 s of fwd+VJP on the host cores)
 KERNELS_PER_CALL = {"ffno_column_info": 3, "ffno_outer": 2}
+METRIC = "FFNO3D voxels/s fwd & fwd+VJP, BF16 vs FP32 @ |\u0394log n|\u22642e-3; p50/p99 latency"
 
 
 def model_config():
@@ -170,7 +173,7 @@ def run_reference(args):
     state = {k: v.detach().clone() for k, v in model.state_dict().items()}
     rate, dt, cores = cpu_rate(state, CPU_SAMPLE, steps=args.steps, warmup=args.warmup)
     sample = f"{CPU_SAMPLE[0]}x{CPU_SAMPLE[1]}x{CPU_SAMPLE[2]} sub-cube of the same model per step, fwd+VJP"
-    line = {"impl": "reference", "metric": "FFNO3D fwd+VJP voxels/s", "value": rate, "unit": "voxels/s",
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "voxels/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -183,11 +186,93 @@ def run_reference(args):
 
 # ---------------------------------------------------------------------------------------------------- GPU arm
 def algorithmic_flops_per_voxel(C, L, D, H, W, M, levels, species, r=8):
-    """Forward MACs x 2 per voxel of the path (shared grid), the per-unit figure of the roofline."""
+    """Forward MACs x 2 per voxel of the path (shared grid), the per-unit figure of the whole-step rate."""
     Wf = W // 2 + 1
     per_block = (31 * C * C + C + (4 * C * C + 4 * r * C) * Wf / W + 4 * M * C + (4 * C * C + 4 * r * C) * M / D)
     head = 6 * C + 2 * C * C + 2 * C * (levels + species)
     return 2 * (L * per_block + head)
+
+
+def algorithmic(name, args):
+    """(bytes, flops) one launch of entry point `name` must move and compute, from its own arguments: FP32 tensors read
+    once and written once (weights and statistics omitted), GEMM flops counted once (the split-BF16 form issues three
+    BF16 MMAs per product; that is not counted). None when the entry point has no formula here."""
+    base = name.split(":")[0]
+    nz = lambda a: 1 if a else 0
+    if base in ("ffno_spectral_mix", "ffno_spectral_mix_tc"):
+        F, nb, C, rank = args[2], args[3], args[7], args[12]
+        rows = F * nb
+        return 2 * rows * 2 * C * 4, rows * (8 * C * C + 8 * rank * C)
+    if base in ("ffno_xform", "ffno_xform_tc"):
+        d = args[3]
+        batches = d.nb
+        return 4 * batches * (d.K + d.M) * d.N, 2 * batches * d.M * d.K * d.N
+    if base == "ffno_xform_pt":
+        d = args[4]
+        batches = d.nb
+        return 4 * batches * ((d.K + d.M) * d.N + d.M * d.K), 2 * batches * d.M * d.K * d.N
+    if base == "ffno_mlp2_fwd_tc":
+        V, C = args[6], args[7]
+        return 4 * V * C * (1 + nz(args[2]) + 1 + nz(args[5])), 8 * V * C * C
+    if base == "ffno_gate_fwd_tc":
+        V, C = args[1], args[2]
+        return 4 * V * C * 2 + 4 * V * nz(args[4]), 4 * V * C * C
+    if base == "ffno_fuse1_tc":
+        V, C = args[5], args[6]
+        return 4 * V * C * (3 + 2 + nz(args[10])), 10 * V * C * C
+    if base == "ffno_fuse2_tc":
+        V, C = args[5], args[6]
+        return 4 * V * C * (4 + 1), 12 * V * C * C
+    if base == "ffno_mlp2_bwd_tc":
+        V, C = args[3], args[4]
+        return 4 * V * C * (2 + nz(args[2]) + 1), 12 * V * C * C
+    if base == "ffno_gate_bwd_tc":
+        V, C = args[3], args[4]
+        return 4 * V * C * (2 + nz(args[2]) + 1) + 4 * V * 2 * nz(args[6]), 8 * V * C * C
+    if base == "ffno_fuse_bwd_a_tc":
+        V, C = args[6], args[7]
+        return 4 * V * C * (5 + 2), 12 * V * C * C
+    if base == "ffno_fuse_bwd_b_tc":
+        V, C = args[9], args[10]
+        return 4 * V * C * (9 + 3), 18 * V * C * C
+    if base == "ffno_outer":
+        R1, R2, N = args[2], args[5], args[6]
+        return 4 * N * (R1 + R2), 2 * N * R1 * R2
+    return None
+
+
+def roofline_rows(per, peaks):
+    """Achieved algorithmic GB/s and TFLOP/s of every entry point with a formula, its bound (the larger of bytes at
+    the HBM peak and flops at the sustained BF16 peak) and the fraction of that peak."""
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    tf = float(peaks.get("bf16_tflops_sustained", 1700.0))
+    rows = {}
+    for name, (t_ms, n, nbytes, nflops) in per.items():
+        if nbytes is None:
+            continue
+        sec = t_ms / 1e3
+        gbs, tfs = nbytes / sec / 1e9, nflops / sec / 1e12
+        hbm_bound = nbytes / (hbm * 1e9) >= nflops / (tf * 1e12)
+        rows[name] = {"bound": "hbm" if hbm_bound else "tensor", "GB/s": round(gbs, 1), "TFLOP/s": round(tfs, 2),
+                      "frac": round(gbs / hbm if hbm_bound else tfs / tf, 4), "avg_launch_ms": round(t_ms / n, 4),
+                      "launches": n, "bytes_per_launch": int(nbytes / n), "flops_per_launch": int(nflops / n)}
+    return rows
+
+
+def dram_traffic(kernel, nbytes_per_launch):
+    """DRAM bytes per launch of `kernel` at the benchmark's size: the ratio of ncu's dram__bytes_read + write to the
+    algorithmic bytes measured on a smaller capture (profiles/dram_traffic.json), times this launch's algorithmic
+    bytes (the traffic of these kernels grows in proportion to the rows they process). None without a capture."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as fh:
+            table = json.load(fh)
+    except (OSError, ValueError):
+        return None, None
+    rec = table.get(kernel.split(":")[0])
+    if not rec:
+        return None, None
+    ratio = rec["dram_bytes"] / rec["algorithmic_bytes"]
+    return ratio * nbytes_per_launch, rec.get("case")
 
 
 def run_gb300(args):
@@ -241,35 +326,66 @@ def run_gb300(args):
             ms = float(t)
         return ms / steps, nat.counter.calls - calls0
 
-    # fwd+VJP, device-resident (the headline)
+    # fwd+VJP at the headline precision, device-resident (--fwd-only: the forward alone, a profiling case)
+    step = fwd if args.fwd_only else fwd_vjp
     with ClockSampler(local) as clk:
-        ms_step, calls = timed(fwd_vjp, args.steps, args.warmup)
+        ms_step, calls = timed(step, args.steps, args.warmup)
     clocks = clk.summary()
-    ms_fwd, _ = timed(fwd, max(args.steps, 3), 1)
+    ms_fwd = ms_step if args.fwd_only else timed(fwd, max(args.steps, 3), 1)[0]
 
-    # kernel breakdown of one fwd+VJP step (CUDA events around every entry point, on the launching stream)
+    # kernel breakdown of one step (CUDA events around every entry point on the launching stream)
     nat.counter.timing = []
-    fwd_vjp()
+    step()
     torch.cuda.synchronize()
     per = {}
-    for name, e0, e1 in nat.counter.timing:
-        t, n = per.get(name, (0.0, 0))
-        per[name] = (t + e0.elapsed_time(e1), n + 1)
+    for name, e0, e1, cargs in nat.counter.timing:
+        t, n, nb, nf = per.get(name, (0.0, 0, 0, 0))
+        alg = algorithmic(name, cargs)
+        per[name] = (t + e0.elapsed_time(e1), n + 1, None if alg is None or nb is None else nb + alg[0],
+                     None if alg is None or nf is None else nf + alg[1])
     nat.counter.timing = None
-    total = sum(t for t, _ in per.values())
-    top = max(per, key=lambda k: per[k][0])
-    breakdown = {k: {"ms": round(t, 3), "launches": n, "share": round(t / total, 4)}
-                 for k, (t, n) in sorted(per.items(), key=lambda kv: -kv[1][0])}
+    launches = sum(KERNELS_PER_CALL.get(k.split(":")[0], 1) * v[1] for k, v in per.items())
+    total = sum(v[0] for v in per.values())
+    breakdown = {k: {"ms": round(v[0], 3), "launches": v[1], "share": round(v[0] / total, 4)}
+                 for k, v in sorted(per.items(), key=lambda kv: -kv[1][0])}
 
-    # roofline of the dominant kernel: algorithmic bytes (or flops) per launch / measured launch time
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
             peaks = json.load(fh)
     except OSError:
         pass
-    hbm = float(peaks.get("hbm_gbs", 6800.0))
-    roof = roofline_of(top, per[top], D, H, W, WIDTH, hbm, peaks)
+    rows = roofline_rows(per, peaks)
+    top = max(rows, key=lambda k: per[k][0])
+    r = rows[top]
+    hbm_b = r["bound"] == "hbm"
+    traffic, traffic_case = dram_traffic(top, r["bytes_per_launch"])
+    roof = {"kernel": top, "bound": r["bound"], "achieved": r["GB/s"] if hbm_b else r["TFLOP/s"],
+            "peak": float(peaks.get("hbm_gbs", 6800.0)) if hbm_b else float(peaks.get("bf16_tflops_sustained", 1700.0)),
+            "unit": "GB/s" if hbm_b else "TFLOP/s", "frac": r["frac"], "traffic": traffic,
+            "traffic_source": traffic_case, "algorithmic_bytes_per_launch": r["bytes_per_launch"],
+            "avg_launch_ms": r["avg_launch_ms"],
+            "peak_source": ("of measured (hbm_gbs)" if hbm_b else "of measured (bf16_tflops_sustained)")
+            if peaks else "of fallback"}
+
+    # the plain FP32 drop-in on the same cube, and the BF16 error against it
+    fp32 = None
+    if args.fwd_only:
+        args.no_fp32 = args.no_e2e = args.no_cpu_baseline = args.no_serve = True
+    if args.precision == "bf16" and not args.no_fp32:
+        with torch.no_grad():
+            y16 = ex.forward(x, z, DXY, DXY)[0]
+            model.set_precision("fp32")
+            y32 = ex.forward(x, z, DXY, DXY)[0]
+            dlog = float((y16 - y32).abs().max())
+        del y16, y32
+        ms32, _ = timed(fwd_vjp, max(2, args.steps // 2), 1)
+        ms32f, _ = timed(fwd, max(2, args.steps // 2), 1)
+        model.set_precision("bf16")
+        fp32 = {"fwd+vjp": {"value": world * V / (ms32 / 1e3), "unit": "voxels/s", "ms_per_step": ms32},
+                "fwd": {"value": world * V / (ms32f / 1e3), "unit": "voxels/s", "ms_per_step": ms32f},
+                "bf16_speedup_fwd+vjp": ms32 / ms_step, "bf16_speedup_fwd": ms32f / ms_fwd,
+                "max_abs_dlog10n_bf16_vs_fp32": dlog}
 
     # e2e through the service backend with host buffers
     e2e = None
@@ -309,19 +425,21 @@ def run_gb300(args):
 
     flops_vox = algorithmic_flops_per_voxel(WIDTH, LAYERS, D, H, W, MODES, 12, 2)
     if rank == 0:
-        launches = sum(KERNELS_PER_CALL.get(k, 1) * n for k, (_, n) in per.items())
         line = {
-            "metric": "FFNO3D fwd+VJP voxels/s", "value": world * V / (ms_step / 1e3), "unit": "voxels/s",
+            "metric": METRIC, "value": world * V / (ms_step / 1e3), "unit": "voxels/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if args.precision == "fp32" else "bf16", "data": "synthetic",
-            "config": {"workload": f"FFNO3D w{WIDTH} L{LAYERS} M{MODES} H+CaII, [1,6,{D},{H},{W}] fwd + input VJP "
-                                   "(per-block recompute)", "voxels_per_step": V, "parallelism": f"replicas{world}",
+            "config": {"workload": f"FFNO3D w{WIDTH} L{LAYERS} M{MODES} H+CaII, [1,6,{D},{H},{W}] " +
+                                   ("forward only" if args.fwd_only else "fwd + input VJP (per-block recompute)"),
+                       "voxels_per_step": V, "parallelism": f"replicas{world}",
                        "l2": "working set (GBs) >> L2; no flush needed", "precision": args.precision},
             "fwd": {"value": world * V / (ms_fwd / 1e3), "unit": "voxels/s", "ms_per_step": ms_fwd},
+            "fp32": fp32,
             "algorithmic_tflops": {"fwd+vjp": 2 * flops_vox * V / (ms_step / 1e3) / 1e12,
                                    "fwd": flops_vox * V / (ms_fwd / 1e3) / 1e12},
-            "roofline": roof, "kernel_breakdown_ms": breakdown,
+            "roofline": roof, "roofline_by_entry": dict(sorted(rows.items(), key=lambda kv: -per[kv[0]][0])[:12]),
+            "kernel_breakdown_ms": breakdown,
             "clocks": clocks, "gpu_launches": launches * args.steps, "e2e": e2e, "cpu_baseline": cpu,
             "serving": serving,
         }
@@ -394,35 +512,15 @@ def serving_stream(model, n_requests, rate, seed=7, slots=4, connections=8):
             "voxels_per_s": vox / elapsed, "wall_s": elapsed}
 
 
-def roofline_of(name, timing, D, H, W, C, hbm, peaks):
-    """Algorithmic traffic/work of one launch of the dominant entry point over its measured average duration."""
-    t_ms, n = timing
-    avg_s = t_ms / n / 1e3
-    V = D * H * W
-    Wf = W // 2 + 1
-    spec = D * 2 * H * Wf * C * 4
-    # algorithmic bytes per launch (FP32): inputs read once + outputs written once
-    bytes_per = {
-        "ffno_xform": None,
-        "ffno_mlp2_fwd": 2 * V * C * 4, "ffno_mlp2_bwd": 3 * V * C * 4, "ffno_fuse_fwd": 4 * V * C * 4,
-        "ffno_fuse_bwd": 7 * V * C * 4, "ffno_gate_fwd": 2 * V * C * 4, "ffno_gate_bwd": 5 * V * C * 4,
-        "ffno_spectral_mix": 2 * spec, "ffno_gn_bwd_stats": 2 * V * C * 4, "ffno_gn_bwd_apply": 3 * V * C * 4,
-    }.get(name)
-    if bytes_per is None:
-        bytes_per = 2 * V * C * 4
-    achieved = bytes_per / avg_s / 1e9
-    return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "traffic": None, "avg_launch_ms": t_ms / n,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"}
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16"])
+    ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16"])
+    ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 comparison run")
+    ap.add_argument("--fwd-only", action="store_true", help="time the forward pass alone (profiling cases)")
     ap.add_argument("--shape", default="256,128,128")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -145,7 +145,7 @@ def call(name, *args, tag=None):
         a.record()
         status = getattr(lib(), name)(*args)
         b.record()
-        counter.timing.append((name + (":" + tag if tag else ""), a, b))
+        counter.timing.append((name + (":" + tag if tag else ""), a, b, args))
     else:
         status = getattr(lib(), name)(*args)
     if status:
