@@ -159,15 +159,24 @@ __global__ void __launch_bounds__(256) k_gn_bwd_stats(int mode, const float* __r
 }
 
 __global__ void k_gn_bwd_final(const double* __restrict__ partials, int nparts, int groups, double* __restrict__ sums) {
-  const int g = threadIdx.x;
-  if (g >= groups) return;
-  double s1 = 0.0, s2 = 0.0;
-  for (int p = 0; p < nparts; ++p) {
-    s1 += partials[((long)p * groups + g) * 2];
-    s2 += partials[((long)p * groups + g) * 2 + 1];
+  // one warp per group: strided partial sums per lane, then a fixed shuffle tree (deterministic)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int g = warp; g < groups; g += nw) {
+    double s1 = 0.0, s2 = 0.0;
+    for (int p = lane; p < nparts; p += 32) {
+      s1 += partials[((long)p * groups + g) * 2];
+      s2 += partials[((long)p * groups + g) * 2 + 1];
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      s1 += __shfl_down_sync(0xffffffffu, s1, off);
+      s2 += __shfl_down_sync(0xffffffffu, s2, off);
+    }
+    if (lane == 0) {
+      sums[2 * g] = s1;
+      sums[2 * g + 1] = s2;
+    }
   }
-  sums[2 * g] = s1;
-  sums[2 * g + 1] = s2;
 }
 
 // pre_bar = rstd (ghat - (w / T)(S1 + xhat S2)); w_bar[v] += sum_c (1/T)(-S1 xhat - S2 (xhat^2 - var rstd^2) / 2).
@@ -826,7 +835,7 @@ int ffno_gn_bwd_stats(int mode, const float* u, float r, const float* pre, const
 
 int ffno_gn_bwd_final(const double* partials, int nparts, int groups, double* sums, ffno_stream_t stream) {
   if (nparts < 1 || groups < 1 || groups > GMAX) return FFNO_EINVAL;
-  k_gn_bwd_final<<<1, 32, 0, (cudaStream_t)stream>>>(partials, nparts, groups, sums);
+  k_gn_bwd_final<<<1, 512, 0, (cudaStream_t)stream>>>(partials, nparts, groups, sums);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

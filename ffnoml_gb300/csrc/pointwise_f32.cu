@@ -137,21 +137,31 @@ __global__ void k_gn_finalize(const double* __restrict__ partials, int nparts, i
                               const float* __restrict__ gamma, const float* __restrict__ beta, float eps,
                               float* __restrict__ coefs, double* __restrict__ gstats) {
   __shared__ double gm[GMAX], gr[GMAX];
-  const int tid = threadIdx.x;
-  if (tid < groups) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  // one warp per group: lane l merges partials l, l + 32, ... in order, then a fixed shuffle tree (deterministic)
+  for (int g = warp; g < groups; g += nw) {
     GroupAcc a{0.0, 0.0, 0.0};
-    for (int p = 0; p < nparts; ++p) {
-      const double* q = partials + ((long)p * groups + tid) * 3;
+    for (int p = lane; p < nparts; p += 32) {
+      const double* q = partials + ((long)p * groups + g) * 3;
       chan_merge(a, q[0], q[1], q[2]);
     }
-    const double var = a.w > 0.0 ? a.m2 / a.w : 0.0;
-    const double rstd = 1.0 / sqrt(var + (double)eps);
-    gm[tid] = a.mean;
-    gr[tid] = rstd;
-    if (gstats) {
-      gstats[3 * tid] = a.mean;
-      gstats[3 * tid + 1] = rstd;
-      gstats[3 * tid + 2] = a.w;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const double w = __shfl_down_sync(0xffffffffu, a.w, off);
+      const double m = __shfl_down_sync(0xffffffffu, a.mean, off);
+      const double m2 = __shfl_down_sync(0xffffffffu, a.m2, off);
+      if (lane < off) chan_merge(a, w, m, m2);
+    }
+    if (lane == 0) {
+      const double var = a.w > 0.0 ? a.m2 / a.w : 0.0;
+      const double rstd = 1.0 / sqrt(var + (double)eps);
+      gm[g] = a.mean;
+      gr[g] = rstd;
+      if (gstats) {
+        gstats[3 * g] = a.mean;
+        gstats[3 * g + 1] = rstd;
+        gstats[3 * g + 2] = a.w;
+      }
     }
   }
   __syncthreads();
@@ -506,7 +516,7 @@ int ffno_lift_fwd(const float* x_in, int cin, long V, int C, const float* w_lift
 int ffno_gn_finalize(const double* partials, int nparts, int C, int groups, const float* gamma, const float* beta,
                      float eps, float* coefs, double* gstats, ffno_stream_t stream) {
   if (nparts < 1 || C < 1 || groups < 1 || groups > GMAX || C % groups) return FFNO_EINVAL;
-  k_gn_finalize<<<1, 128, 0, (cudaStream_t)stream>>>(partials, nparts, C, groups, gamma, beta, eps, coefs, gstats);
+  k_gn_finalize<<<1, 512, 0, (cudaStream_t)stream>>>(partials, nparts, C, groups, gamma, beta, eps, coefs, gstats);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

@@ -6,6 +6,8 @@
 // pre-packed per (m-tile, k-chunk) in the canonical K-major order) arrives by bulk copy while the threads convert the
 // FP32 data chunk into a split MN-major tile (n contiguous, as it lies in HBM); the MMAs of chunk c run while chunk
 // c + 1 is staged. Accumulators live in tensor memory (<= 2 x 128 columns).
+#include <cudaTypedefs.h>
+
 #include "common.cuh"
 #include "tc.cuh"
 
@@ -194,153 +196,273 @@ __global__ void __launch_bounds__(XT) k_xform_tc(const uint8_t* __restrict__ tpa
 }
 
 // ---------------------------------------------------------------------------------------------------- mixing
-// Per-frequency mixing on tensor cores: a CTA item = 128 rows b of one frequency f. A = [re | im] rows (split, K-major
-// [128][2C]); B = wbig^T (split, [2C][2C]) resident; D [128][2C] in tensor memory; epilogue: g_f scaling and the
-// rank-r term U_f (V_f xhat) from FP32 values.
+// Per-frequency mixing on tensor cores: out_f = g_f (W x_f) + U_f (V_f x_f) for every row b of frequency f, with
+// x = [re | im] (2C values), W the [2C x 2C] channel map and g_f complex. A CTA item = 128 rows b of one frequency;
+// the grid is persistent.
+//   * The item's FP32 rows arrive by tiled TMA loads (a 4-D tensor map over channel, f, b and re/im, the outer three
+//     sorted by stride; 128-byte swizzle) into a staging buffer, issued one item ahead.
+//   * The threads split them into X (split BF16, K-major [128 b][2C]) and the item's V_f into a block-diagonal
+//     [16][2C] operand (rows 0..7 act on the re half, rows 8..15 on the im half).
+//   * MMAs: D^T [2C (padded to 128) x 128 b] = W X^T (W resident in shared memory as the A operand) and the low-rank
+//     projections T [128 b x 16] = X Vblk^T, into double-buffered tensor memory, so the epilogue of item i-1 runs
+//     while the MMAs of item i do.
+//   * Epilogue: thread = output channel p (TMEM lane; lanes < C hold re, lanes C..2C-1 im of the same channels),
+//     columns = rows b. The re and im lanes of a channel swap their values through shared memory (a shuffle when
+//     C = 16) to apply g_f; y = g_f D + sum_r U_f[p][r] t[b][r]; one warp's stores cover 32 consecutive channels of
+//     one row.
+constexpr int MIX_RANK_TC = 8;   // low-rank terms carried by the tensor-core mixing (larger ranks use k_mix)
+
+struct MixGeom {
+  int mul_b, mul_ri;   // staging row of (b, re/im) inside a box: b * mul_b + ri * mul_ri
+  int o1, o2, o3;      // logical dimension (0 f, 1 b, 2 re/im) of tensor-map dimensions 1..3
+};
+
+__device__ __forceinline__ void pair_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+
 template <int C>
-__global__ void __launch_bounds__(XT) k_mix_tc(const float* __restrict__ in, float* __restrict__ out, long F, long nb,
-                                               long sf, long sb, long s_im, const uint8_t* __restrict__ wpack,
-                                               const float* __restrict__ g, const float* __restrict__ U,
-                                               const float* __restrict__ Vm, int rank, int* __restrict__ err) {
-  extern __shared__ __align__(1024) uint8_t smem[];
+__global__ void __launch_bounds__(XT, 1)
+    k_mix_tc(const __grid_constant__ CUtensorMap tmap, float* __restrict__ out, long F, long nb, long sf, long sb,
+             long s_im, const uint8_t* __restrict__ wpack, const float* __restrict__ g, const float* __restrict__ U,
+             const float* __restrict__ Vm, int rank, MixGeom geo, int* __restrict__ err) {
   constexpr int K2 = 2 * C;
-  constexpr uint32_t WB = (uint32_t)K2 * K2 * 2 * 2;
-  uint8_t* sW = smem;
-  uint8_t* sA = smem + WB;
-  float* sT = reinterpret_cast<float*>(sA + 128u * K2 * 2 * 2);   // [128][33] low-rank projections (padded)
-  float* sU = sT + 128 * 33;                                      // [C][rank]
-  float* sV = sU + C * 16;                                        // [rank][C]
-  __shared__ uint64_t bar;
+  constexpr int CB = C < 32 ? C : 32;       // channels per staging row (one box row)
+  constexpr int NH = C / CB;                // boxes per item
+  constexpr int CPR = CB / 4;               // 16-byte chunks per staging row
+  constexpr uint32_t ROWB = CB * 4;
+  constexpr uint32_t HALF = 256u * ROWB;    // one box: 128 rows b x (re, im)
+  constexpr bool SWZ = (CB == 32);
+  constexpr uint32_t WB = 128u * K2 * 2;    // one split half (hi or lo) of a 128-row operand
+  constexpr uint32_t WP = (uint32_t)K2 * K2 * 2;   // one split half of the packed [2C][2C] weight
+  constexpr int NT = 16;                    // low-rank operand rows
+  constexpr int PW = C / 32;                // warp distance between the re and im lanes of a channel (0: same warp)
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+  uint8_t* sW = base;                  // hi [0, WB), lo [WB, 2 WB)
+  uint8_t* sX = base + 2 * WB;
+  uint8_t* sS = base + 4 * WB;         // staging, 1024-byte aligned (WB is a multiple of 1024)
+  uint8_t* sV = sS + NH * HALF;        // hi [NT][K2], lo after
+  float* sT = reinterpret_cast<float*>(sV + 2u * NT * K2 * 2);   // [128 b][16], 16-byte chunks swizzled by b
+  float4* sE = reinterpret_cast<float4*>(sT + 128 * 16);          // exchange: [8 warps][4][32 lanes] float4
+  __shared__ uint64_t bar_w, bar_s, bar_m[2];
   __shared__ uint32_t tslot;
-  const int tid = threadIdx.x, row = tid & 127, wg = tid >> 7;
-  if (tid < 32) tc::tmem_alloc(&tslot, K2 <= 32 ? 32 : (K2 <= 64 ? 64 : 128));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, q = warp & 3, wg = warp >> 2;
+  if (warp == 0) tc::tmem_alloc(&tslot, 512);
   if (tid == 0) {
-    tc::mbar_init(&bar, 1);
+    tc::mbar_init(&bar_w, 1);
+    tc::mbar_init(&bar_s, 1);
+    tc::mbar_init(&bar_m[0], 1);
+    tc::mbar_init(&bar_m[1], 1);
     tc::mbar_init_fence();
   }
+  // zero the padding rows 2C..127 of W (hi and lo); they are contiguous at the end of each half
+  for (uint32_t e = 2u * C * K2 * 2 + tid * 16u; e < WB; e += XT * 16u) {
+    *reinterpret_cast<uint4*>(sW + e) = make_uint4(0u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4*>(sW + WB + e) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  tc::fence_async_smem();
   tc::tc_before_sync();
   __syncthreads();
   tc::tc_after_sync();
   const uint32_t tmem = tslot;
-  const uint32_t lb = (uint32_t)(32 * ((tid >> 5) & 3)) << 16;
-  uint32_t phase = 0;
+  const uint32_t lq = (uint32_t)(32 * q) << 16;
+  const long nbt = (nb + 127) / 128, items = F * nbt;
+  auto issue_load = [&](long item) {
+    const long f = item / nbt, b0 = (item % nbt) * 128;
+    int c[4];
+    const int oo[3] = {geo.o1, geo.o2, geo.o3};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) c[k + 1] = oo[k] == 0 ? (int)f : (oo[k] == 1 ? (int)b0 : 0);
+    tc::mbar_arrive_expect_tx(&bar_s, NH * HALF);
+#pragma unroll
+    for (int h = 0; h < NH; ++h) tc::tma_load_4d(sS + h * HALF, &tmap, h * CB, c[1], c[2], c[3], &bar_s);
+  };
+  long it = blockIdx.x;
   if (tid == 0) {
-    tc::mbar_arrive_expect_tx(&bar, WB);
-    for (uint32_t off = 0; off < WB; off += 65536u)
-      tc::bulk_g2s(sW + off, wpack + off, (WB - off) < 65536u ? (WB - off) : 65536u, &bar);
+    tc::mbar_arrive_expect_tx(&bar_w, 2 * WP);
+    tc::bulk_g2s(sW, wpack, WP, &bar_w);
+    tc::bulk_g2s(sW + WB, wpack + WP, WP, &bar_w);
+    if (it < items) issue_load(it);
   }
-  bool ok = bounded(tc::mbar_wait(&bar, phase), err, 1);
-  phase ^= 1u;
-  const long nbt = (nb + 127) / 128;
-  for (long it = blockIdx.x; ok && it < F * nbt; it += gridDim.x) {
-    const long f = it / nbt, b0 = (it % nbt) * 128;
-    const float* fin = in + f * sf;
-    {  // L2 prefetch of the next item's rows (re and im halves)
-      const long nx = it + gridDim.x;
-      if (nx < F * nbt && tid < 128) {
-        const long fn = nx / nbt, bn = (nx % nbt) * 128 + tid;
-        if (bn < nb) {
-          tc::prefetch_l2(in + fn * sf + bn * sb, C * 4);
-          tc::prefetch_l2(in + fn * sf + bn * sb + s_im, C * 4);
+  bool ok = bounded(tc::mbar_wait(&bar_w, 0), err, 1);
+  bool load_pending = it < items;         // the load of the next item to process is in flight
+  float ucur[MIX_RANK_TC], uprev[MIX_RANK_TC];
+  long pf = 0, pb0 = 0;
+  float pgr = 0.f, pgi = 0.f;
+  const int p = 32 * q + lane;            // output channel slot of this thread in the epilogue
+  const bool live = p < 2 * C;
+  const int part = p >= C ? 1 : 0, pc = p - part * C;
+  const int pair_id = 1 + 2 * wg + (PW ? q % PW : 0);
+
+  auto epilogue = [&](uint32_t buf, long f, long b0, float gr, float gi) {
+    if (rank) {
+      if (wg == 0) {   // low-rank rows t[b][0..16) from tensor memory (lane = b) to shared memory
+        const int bl = 32 * q + lane;
+        float t[16];
+        tc::tmem_ld16(tmem + lq + 256u + buf * 16u, t);
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+          *reinterpret_cast<float4*>(sT + bl * 16 + ((m ^ (bl & 3)) << 2)) =
+              make_float4(t[4 * m], t[4 * m + 1], t[4 * m + 2], t[4 * m + 3]);
+      }
+      __syncthreads();
+    }
+    float* ob = out + f * sf + part * s_im + pc;
+    const float ga = part ? gr : gr, gb = part ? gi : -gi;   // y = ga * own + gb * partner
+#pragma unroll 1
+    for (int cch = 0; cch < 4; ++cch) {
+      const int col = 64 * wg + 16 * cch;
+      float v[16], w[16];
+      tc::tmem_ld16(tmem + lq + buf * 128u + (uint32_t)col, v);
+      if (PW == 0) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = __shfl_xor_sync(0xffffffffu, v[i], 16);
+      } else if (live) {
+        float4* mine = sE + warp * 128;
+        const float4* theirs = sE + (part ? warp - PW : warp + PW) * 128;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) mine[m * 32 + lane] = make_float4(v[4 * m], v[4 * m + 1], v[4 * m + 2], v[4 * m + 3]);
+        pair_sync(pair_id);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          const float4 t4 = theirs[m * 32 + lane];
+          w[4 * m] = t4.x;
+          w[4 * m + 1] = t4.y;
+          w[4 * m + 2] = t4.z;
+          w[4 * m + 3] = t4.w;
+        }
+        pair_sync(pair_id);
+      }
+      if (live) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const long b = b0 + col + i;
+          if (b < nb) {
+            float y = fmaf(ga, v[i], gb * w[i]);
+            if (rank) {
+              const int bl = col + i;
+              const float* tr = sT + bl * 16;
+#pragma unroll
+              for (int m = 0; m < 2; ++m) {
+                if (4 * m < rank) {
+                  const float4 tv = *reinterpret_cast<const float4*>(tr + (((2 * part + m) ^ (bl & 3)) << 2));
+                  y = fmaf(uprev[4 * m], tv.x, y);
+                  if (4 * m + 1 < rank) y = fmaf(uprev[4 * m + 1], tv.y, y);
+                  if (4 * m + 2 < rank) y = fmaf(uprev[4 * m + 2], tv.z, y);
+                  if (4 * m + 3 < rank) y = fmaf(uprev[4 * m + 3], tv.w, y);
+                }
+              }
+            }
+            ob[b * sb] = y;
+          }
         }
       }
     }
-    // A tile (split, K-major [128][2C]): row b = [re | im]
-    for (int e = tid; e < 128 * K2 / 4; e += XT) {
-      const int h = e & 1, r8 = (e >> 1) & 7, q = e >> 4;
-      const int kb = q % (K2 / 8), rb = q / (K2 / 8);
-      const int r = rb * 8 + r8, k = kb * 8 + h * 4;
-      const long b = b0 + r;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (b < nb) v = __ldg(reinterpret_cast<const float4*>(fin + b * sb + (k < C ? k : s_im + k - C)));
+    tc::tc_before_sync();
+    __syncthreads();
+    tc::tc_after_sync();
+  };
+
+  uint32_t j = 0;
+  for (; ok && it < items; it += gridDim.x, ++j) {
+    const long f = it / nbt, b0 = (it % nbt) * 128;
+    const bool w1 = tc::mbar_wait(&bar_s, j & 1u);
+    const bool w2 = j ? tc::mbar_wait(&bar_m[(j - 1) & 1u], ((j - 1) >> 1) & 1u) : true;
+    if (!(ok = bounded(w1 && w2, err, 2))) break;
+    load_pending = false;
+    tc::tc_after_sync();
+    // split the staged rows into X
+    for (int e = tid; e < 128 * NH * CPR; e += XT) {
+      const int c4 = e % CPR, rest = e / CPR;
+      const int b = rest & 127, h = rest >> 7;
+      const int rre = b * geo.mul_b, rim = rre + geo.mul_ri;
+      const uint8_t* hb = sS + h * HALF;
+      const float4 xr = *reinterpret_cast<const float4*>(hb + rre * ROWB + ((SWZ ? (c4 ^ (rre & 7)) : c4) << 4));
+      const float4 xi = *reinterpret_cast<const float4*>(hb + rim * ROWB + ((SWZ ? (c4 ^ (rim & 7)) : c4) << 4));
+      const int k = h * CB + c4 * 4;
       uint32_t h0, l0, h1, l1;
-      tc::split_pack(v.x, v.y, h0, l0);
-      tc::split_pack(v.z, v.w, h1, l1);
-      *reinterpret_cast<uint2*>(sA + (size_t)e * 8) = make_uint2(h0, h1);
-      *reinterpret_cast<uint2*>(sA + 128u * K2 * 2 + (size_t)e * 8) = make_uint2(l0, l1);
+      tc::split_pack(xr.x, xr.y, h0, l0);
+      tc::split_pack(xr.z, xr.w, h1, l1);
+      *reinterpret_cast<uint2*>(sX + tc::kmajor_offset(b, k, K2)) = make_uint2(h0, h1);
+      *reinterpret_cast<uint2*>(sX + WB + tc::kmajor_offset(b, k, K2)) = make_uint2(l0, l1);
+      tc::split_pack(xi.x, xi.y, h0, l0);
+      tc::split_pack(xi.z, xi.w, h1, l1);
+      *reinterpret_cast<uint2*>(sX + tc::kmajor_offset(b, C + k, K2)) = make_uint2(h0, h1);
+      *reinterpret_cast<uint2*>(sX + WB + tc::kmajor_offset(b, C + k, K2)) = make_uint2(l0, l1);
     }
     if (rank) {
-      for (int e = tid; e < C * rank; e += XT) {
-        sU[e] = __ldg(U + f * C * rank + e);
-        sV[e] = __ldg(Vm + f * C * rank + e);
+      // block-diagonal V_f: rows 0..r-1 act on the re half, rows 8..8+r-1 on the im half, the others are zero
+      for (int e = tid; e < NT * K2 / 2; e += XT) {
+        const int n = e / (K2 / 2), k = (e % (K2 / 2)) * 2;
+        const int kp = k >= C ? 1 : 0, c = k - kp * C;
+        const int r = n & 7;
+        float v0 = 0.f, v1 = 0.f;
+        if (r < rank && (n >> 3) == kp) {
+          const float* vr = Vm + (f * rank + r) * (long)C + c;
+          v0 = __ldg(vr);
+          v1 = __ldg(vr + 1);
+        }
+        uint32_t hi, lo;
+        tc::split_pack(v0, v1, hi, lo);
+        *reinterpret_cast<uint32_t*>(sV + tc::kmajor_offset(n, k, K2)) = hi;
+        *reinterpret_cast<uint32_t*>(sV + (uint32_t)NT * K2 * 2 + tc::kmajor_offset(n, k, K2)) = lo;
       }
+#pragma unroll
+      for (int r = 0; r < MIX_RANK_TC; ++r)
+        ucur[r] = (live && r < rank) ? __ldg(U + (f * C + pc) * (long)rank + r) : 0.f;
     }
     tc::fence_async_smem();
     tc::tc_before_sync();
     __syncthreads();
     tc::tc_after_sync();
+    load_pending = it + gridDim.x < items;
     if (tid == 0) {
-      const uint32_t ah = tc::smem_u32(sA), al = ah + 128u * K2 * 2;
-      const uint32_t bh = tc::smem_u32(sW), bl = bh + (uint32_t)K2 * K2 * 2;
-      tc::gemm3_128xN(tmem, ah, al, bh, bl, K2, K2);
-      tc::mma_commit(&bar);
-    }
-    // low-rank projections t[row][q] = sum_i V[r][i] xhat[row][i] (FP32, from the source rows) while the MMA runs
-    if (rank) {
-      for (int e = tid; e < 128 * 2 * rank; e += XT) {
-        const int r = e / (2 * rank), q = e % (2 * rank);
-        const int rr = q % rank, part = q / rank;
-        const long b = b0 + r;
-        float s = 0.f;
-        if (b < nb) {
-          const float* src = fin + b * sb + (part ? s_im : 0);
-          for (int i = 0; i < C; i += 4) {
-            const float4 x = __ldg(reinterpret_cast<const float4*>(src + i));
-            s = fmaf(sV[rr * C + i], x.x, s);
-            s = fmaf(sV[rr * C + i + 1], x.y, s);
-            s = fmaf(sV[rr * C + i + 2], x.z, s);
-            s = fmaf(sV[rr * C + i + 3], x.w, s);
-          }
-        }
-        sT[r * 33 + q] = s;
+      if (load_pending) issue_load(it + gridDim.x);
+      const uint32_t buf = j & 1u;
+      const uint32_t w_hi = tc::smem_u32(sW), x_hi = tc::smem_u32(sX);
+      tc::gemm3_128xN(tmem + buf * 128u, w_hi, w_hi + WB, x_hi, x_hi + WB, K2, 128);
+      if (rank) {
+        const uint32_t v_hi = tc::smem_u32(sV);
+        tc::gemm3_128xN(tmem + 256u + buf * 16u, x_hi, x_hi + WB, v_hi, v_hi + (uint32_t)NT * K2 * 2, K2, NT);
       }
+      tc::mma_commit(&bar_m[buf]);
     }
-    const bool w = tc::mbar_wait(&bar, phase);
-    phase ^= 1u;
-    tc::tc_before_sync();
-    if (!(ok = bounded(w, err, 2))) break;
-    tc::tc_after_sync();
-    const float gr = __ldg(g + 2 * f), gi = __ldg(g + 2 * f + 1);
-    const long b = b0 + row;
-    // re chunk j pairs with im chunk j + C/16; warpgroup wg takes j of its parity
+    if (j) epilogue((j - 1) & 1u, pf, pb0, pgr, pgi);
+    pf = f;
+    pb0 = b0;
+    pgr = __ldg(g + 2 * f);
+    pgi = __ldg(g + 2 * f + 1);
 #pragma unroll
-    for (int j = 0; j < C / 16; ++j) {
-      if ((C / 16 > 1) && (j & 1) != wg) continue;
-      if ((C / 16 == 1) && wg != 0) continue;
-      float ar[16], ai[16];
-      tc::tmem_ld16(tmem + lb + 16 * j, ar);
-      tc::tmem_ld16(tmem + lb + C + 16 * j, ai);
-      if (b < nb) {
-        float* fo = out + f * sf + b * sb;
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int o = 16 * j + i;
-          float yr = ar[i] * gr - ai[i] * gi;
-          float yi = ar[i] * gi + ai[i] * gr;
-          if (rank) {
-            float lr = 0.f, li = 0.f;
-            for (int r = 0; r < rank; ++r) {
-              const float u = sU[o * rank + r];
-              lr = fmaf(u, sT[row * 33 + r], lr);
-              li = fmaf(u, sT[row * 33 + rank + r], li);
-            }
-            yr += lr;
-            yi += li;
-          }
-          fo[o] = yr;
-          fo[s_im + o] = yi;
-        }
-      }
-    }
-    tc::tc_before_sync();
-    __syncthreads();
-    tc::tc_after_sync();
+    for (int r = 0; r < MIX_RANK_TC; ++r) uprev[r] = ucur[r];
   }
-  if (!ok) tc::mbar_wait(&bar, phase ^ 1u);
+  if (ok && j) {
+    const bool w = tc::mbar_wait(&bar_m[(j - 1) & 1u], ((j - 1) >> 1) & 1u);
+    if ((ok = bounded(w, err, 3))) {
+      tc::tc_after_sync();
+      epilogue((j - 1) & 1u, pf, pb0, pgr, pgi);
+    }
+  }
+  if (!ok) {   // leave no bulk copy or MMA in flight before freeing tensor memory
+    tc::mbar_wait(&bar_w, 0);
+    if (load_pending) tc::mbar_wait(&bar_s, j & 1u);
+    if (j) tc::mbar_wait(&bar_m[(j - 1) & 1u], ((j - 1) >> 1) & 1u);
+  }
   tc::tc_before_sync();
   __syncthreads();
   tc::tc_after_sync();
-  if (tid < 32) tc::tmem_free(tmem, K2 <= 32 ? 32 : (K2 <= 64 ? 64 : 128));
+  if (warp == 0) tc::tmem_free(tmem, 512);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the library does not link the driver directly)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
 }
 
 int g_sms = 0;
@@ -390,24 +512,61 @@ int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, 
                          ffno_stream_t stream) {
   if (!in || !out || !wpack || !g || !err || F < 1 || nb < 1 || rank < 0 || rank > 16) return FFNO_EINVAL;
   if (rank && (!U || !Vm)) return FFNO_EINVAL;
-  if ((reinterpret_cast<uintptr_t>(wpack) % 16) || sf % 4 || sb % 4 || s_im % 4) return FFNO_EINVAL;
+  if ((reinterpret_cast<uintptr_t>(wpack) % 16) || (reinterpret_cast<uintptr_t>(in) % 16)) return FFNO_EINVAL;
+  if (rank > MIX_RANK_TC) return FFNO_EINVAL;
+  if (sf < 1 || sb < 1 || s_im < 1 || sf % 4 || sb % 4 || s_im % 4) return FFNO_EINVAL;
+  if (F > 0x7fffffffL || nb > 0x7fffffffL) return FFNO_EINVAL;
+  if (C != 16 && C != 32 && C != 64) return FFNO_EINVAL;
+  // tensor map over (channel, then f / b / re-im sorted by stride); boxes of (min(C, 32), 1, 128, 2)
+  struct Dim { int logical; uint64_t extent, stride; uint32_t box; } d[3] = {
+      {0, (uint64_t)F, (uint64_t)sf * 4, 1u}, {1, (uint64_t)nb, (uint64_t)sb * 4, 128u}, {2, 2u, (uint64_t)s_im * 4, 2u}};
+  for (int i = 1; i < 3; ++i)
+    for (int k = i; k > 0 && d[k].stride < d[k - 1].stride; --k) {
+      const Dim t = d[k];
+      d[k] = d[k - 1];
+      d[k - 1] = t;
+    }
+  const int CB = C < 32 ? C : 32;
+  cuuint64_t gdim[4] = {(cuuint64_t)C, d[0].extent, d[1].extent, d[2].extent};
+  cuuint64_t gstr[3] = {d[0].stride, d[1].stride, d[2].stride};
+  cuuint32_t box[4] = {(cuuint32_t)CB, d[0].box, d[1].box, d[2].box};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUtensorMap map;
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  if (!encode) return FFNO_ELAUNCH;
+  if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(in), gdim, gstr, box, estr,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CB == 32 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return FFNO_EINVAL;
+  MixGeom geo{};
+  int run = 1;
+  for (int k = 0; k < 3; ++k) {
+    if (d[k].logical == 1) geo.mul_b = run;
+    if (d[k].logical == 2) geo.mul_ri = run;
+    run *= (int)d[k].box;
+  }
+  geo.o1 = d[0].logical;
+  geo.o2 = d[1].logical;
+  geo.o3 = d[2].logical;
   const long items = F * ((nb + 127) / 128);
   const long grid = items < sms() ? items : sms();
+  const size_t K2 = 2 * (size_t)C;
+  size_t smem = 1024 + 4 * 128 * K2 * 2 + (size_t)(C / CB) * 256 * CB * 4 + 2 * 16 * K2 * 2 + 128 * 16 * 4 +
+                8 * 128 * 16;
+  if (smem < 120 * 1024) smem = 120 * 1024;   // one CTA per SM: each CTA holds all 512 tensor-memory columns
   cudaStream_t s = (cudaStream_t)stream;
   switch (C) {
 #define L(CC)                                                                                                     \
   case CC: {                                                                                                      \
-    const size_t smem = (size_t)(2 * CC) * (2 * CC) * 4 + 128u * (2 * CC) * 4 + (128 * 33 + 2 * CC * 16) * 4;      \
     if (cudaFuncSetAttribute(k_mix_tc<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) \
       return FFNO_ELAUNCH;                                                                                        \
-    k_mix_tc<CC><<<(unsigned)grid, XT, smem, s>>>(in, out, F, nb, sf, sb, s_im, static_cast<const uint8_t*>(wpack), \
-                                                 g, U, Vm, rank, err);                                            \
+    k_mix_tc<CC><<<(unsigned)grid, XT, smem, s>>>(map, out, F, nb, sf, sb, s_im, static_cast<const uint8_t*>(wpack), \
+                                                 g, U, Vm, rank, geo, err);                                       \
     break;                                                                                                        \
   }
     L(16) L(32) L(64)
 #undef L
-    default:
-      return FFNO_EINVAL;
   }
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;

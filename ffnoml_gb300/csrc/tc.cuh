@@ -7,6 +7,7 @@
 //   (r / 8) * SBO + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2,      SBO = K * 16
 // i.e. the K-chunks of one 8-row group are adjacent (LBO = 128 bytes) and the row groups follow each other.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <cuda_bf16.h>
@@ -93,6 +94,17 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                    smem_u32(dst)),
                "l"(src), "r"(bytes), "r"(smem_u32(bar))
                : "memory");
+}
+
+// Tiled 4-D TMA load of one box of the tensor map into shared memory, completing on an mbarrier. The innermost
+// coordinate c0 times the element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
 }
 
 // ---------------------------------------------------------------------------------------------------- fences

@@ -29,6 +29,7 @@ from . import tables as tb
 
 EPS = 1e-5  # nn.GroupNorm default, DepthWeightedGroupNorm's eps (models/ffno_model.py:77-95)
 SUPPORTED_WIDTHS = (16, 32, 64, 96)
+MIX_RANK_TC = 8     # low-rank terms the tensor-core mixing carries; larger ranks mix on the FP32 kernel
 NORMS = ("spec", "vert", "fuse", "pw", "mlp")
 
 
@@ -554,7 +555,7 @@ class Executor:
         m = self.model
         s = _stream()
         g, u, v = (fq.g_adj, fq.u_adj, fq.v_adj) if adjoint else (fq.g, fq.u, fq.v)
-        if self._tc():
+        if self._tc() and m.freq_mix_rank <= MIX_RANK_TC:
             w = bp[("tcb_" if adjoint else "tc_") + branch + "_mix"]
             nat.call("ffno_spectral_mix_tc", inp.data_ptr(), out.data_ptr(), F, nb, sf, sb, s_im, m.width,
                      w.data_ptr(), g.data_ptr(), _ptr(u), _ptr(v), m.freq_mix_rank, ws.err.data_ptr(), s)

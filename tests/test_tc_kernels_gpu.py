@@ -256,12 +256,16 @@ def test_xform_tc_matches_fp32(which):
 
 
 @pytest.mark.parametrize("C", [16, 32, 64])
-@pytest.mark.parametrize("rank", [0, 4, 8])
-def test_spectral_mix_tc(C, rank):
+@pytest.mark.parametrize("rank", [0, 3, 8])
+@pytest.mark.parametrize("layout", ["horizontal", "height"])
+def test_spectral_mix_tc(C, rank, layout):
     from ffnoml_gb300.executor import tc_pack
     nat = _nat()
     F, nb = 37, 150
-    sf, sb, s_im = C, 2 * F * C, F * C            # the horizontal layout [b][2][F][C]
+    if layout == "horizontal":
+        sf, sb, s_im = C, 2 * F * C, F * C        # [b][2][F][C]
+    else:
+        sf, sb, s_im = nb * C, C, F * nb * C      # [2][F][b][C]
     x = _rand(nb * 2 * F * C, seed=1)
     wr, wi = _rand(C, C, seed=2, scale=C ** -0.5), _rand(C, C, seed=3, scale=C ** -0.5)
     wbig = torch.cat([torch.cat([wr, wi], 1), torch.cat([-wi, wr], 1)], 0).contiguous()
