@@ -207,6 +207,9 @@ def algorithmic(name, args):
         d = args[3]
         batches = d.nb
         return 4 * batches * (d.K + d.M) * d.N, 2 * batches * d.M * d.K * d.N
+    if base == "ffno_xform_tcr":
+        d = args[5]
+        return 4 * d.nb * (d.K + d.M) * d.N, 2 * d.nb * d.M * d.K * d.N
     if base == "ffno_xform_pt":
         d = args[4]
         batches = d.nb

@@ -95,6 +95,8 @@ PROTOTYPES = {
     "ffno_fuse_bwd_a_tc": [P, P, P, P, P, P, L, I, P, P, P, P],
     "ffno_fuse_bwd_b_tc": [P, P, P, P, P, P, P, P, P, L, I, P, P, P, P, P, P],
     "ffno_xform_tc_pack_bytes": [I, I],
+    "ffno_xform_tcr_max_table_bytes": [],
+    "ffno_xform_tcr": [P, I, I, P, P, ctypes.POINTER(XformDesc), I, P, P],
     "ffno_xform_tc": [P, P, P, ctypes.POINTER(XformDesc), I, P, P],
     "ffno_spectral_mix_tc": [P, P, L, L, L, L, L, I, P, P, P, P, I, P, P],
 }

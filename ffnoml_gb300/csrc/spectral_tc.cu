@@ -195,6 +195,189 @@ __global__ void __launch_bounds__(XT) k_xform_tc(const uint8_t* __restrict__ tpa
   if (tid < 32) tc::tmem_free(tmem, 256);
 }
 
+// ------------------------------------------------------------------------------------------- resident table
+// The transform GEMM with the whole split table resident in shared memory, in the transposed orientation:
+// D^T [128 data columns n][M rows m] = X^T T^T, with X a chunk of 64 data rows k x 128 columns n (A operand, MN-major:
+// n contiguous, as in HBM) and T the table [Mp][Kp] (B operand, K-major). The tensor-memory lane is the data column
+// n, so the stores of one warp cover 32 consecutive columns of one output row. An item is 128 columns: one n-tile of
+// one batch, or 128 / N whole batches when N divides 128 (the W transforms, N = C). Two pipelines of 256 threads per
+// CTA take alternate items, each with two data stages (double-buffered against the MMAs), 256 tensor-memory columns
+// and its own mbarriers; the table is shared. Every wait is bounded.
+constexpr int RT = 256;                     // threads per pipeline
+constexpr int RKC = 64;                     // data rows k per chunk
+constexpr uint32_t RSB = 128u * RKC * 2;    // one split half of a data stage
+
+__device__ __forceinline__ void rt_sync(int pipe) { asm volatile("bar.sync %0, %1;" ::"r"(1 + pipe), "n"(RT) : "memory"); }
+__device__ __forceinline__ bool rt_sync_and(int pipe, bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.and.pred po, %2, %3, pi;\n selp.u32 %0, 1, 0, po;\n}"
+      : "=r"(r)
+      : "r"((uint32_t)p), "r"(1 + pipe), "n"(RT)
+      : "memory");
+  return r != 0;
+}
+
+__global__ void __launch_bounds__(2 * RT, 1)
+    k_xform_rt(const uint8_t* __restrict__ tpack, int Mp, int Kp, const float* __restrict__ in, float* __restrict__ out,
+               ffno_xform_desc d, int nbi, int nshift, long ntn, long items, int accumulate, int* __restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t TB = (uint32_t)Mp * Kp * 2;                 // one split half of the table
+  uint8_t* sT = base;
+  uint8_t* sD = base + ((2 * TB + 1023u) & ~1023u);          // [pipe][stage][hi | lo]
+  __shared__ uint64_t bar_t, bar_m[2][2];
+  __shared__ uint32_t tslot;
+  const int tid = threadIdx.x, pipe = tid / RT, ptid = tid % RT, warp = tid >> 5, lane = tid & 31;
+  const int q = warp & 3, half = ptid >> 7;
+  if (warp == 0) tc::tmem_alloc(&tslot, 512);
+  if (tid == 0) {
+    tc::mbar_init(&bar_t, 1);
+    for (int i = 0; i < 4; ++i) tc::mbar_init(&bar_m[i >> 1][i & 1], 1);
+    tc::mbar_init_fence();
+    tc::mbar_arrive_expect_tx(&bar_t, 2 * TB);
+    for (uint32_t off = 0; off < 2 * TB; off += 32768u)
+      tc::bulk_g2s(sT + off, tpack + off, (2 * TB - off) < 32768u ? (2 * TB - off) : 32768u, &bar_t);
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  const uint32_t tmem = tslot + (uint32_t)pipe * 256u;
+  const uint32_t lq = (uint32_t)(32 * q) << 16;
+  bool ok = __syncthreads_and(tc::mbar_wait(&bar_t, 0)) != 0;
+  if (!ok && tid == 0) atomicExch(err, 1);
+  const int nch = (Kp + RKC - 1) / RKC;
+  const uint32_t idesc = tc::idesc_bf16_ab(128, Mp, true, false);
+  const uint32_t t_hi = tc::smem_u32(sT), t_lo = t_hi + TB;
+  uint32_t g = 0;                                            // chunks issued by this pipeline
+  const int n_ep = 32 * q + lane;                            // epilogue column of this thread
+  for (long it = 2L * blockIdx.x + pipe; ok && it < items; it += 2L * gridDim.x) {
+    long bfirst, n0;
+    if (nbi > 1) {
+      bfirst = it * nbi;
+      n0 = 0;
+    } else {
+      bfirst = it / ntn;
+      n0 = (it % ntn) * 128;
+    }
+    // source / destination offsets of column n of this item (-1: no such column)
+    auto col_in = [&](int n, long& off) -> bool {
+      long b, c;
+      if (nbi > 1) {
+        b = bfirst + (n >> nshift);
+        c = n & ((1 << nshift) - 1);
+      } else {
+        b = bfirst;
+        c = n0 + n;
+      }
+      if (b >= d.nb || c >= d.N) return false;
+      off = (b / d.nb2) * d.in_b1 + (b % d.nb2) * d.in_b2 + c;
+      return true;
+    };
+    for (int ch = 0; ch < nch; ++ch, ++g) {
+      const int s = (int)(g & 1u);
+      const int k0 = ch * RKC, kc = (Kp - k0) < RKC ? (Kp - k0) : RKC;
+      if (g >= 2) {
+        const bool w = tc::mbar_wait(&bar_m[pipe][s], ((g - 2) >> 1) & 1u);
+        if (!(ok = rt_sync_and(pipe, w))) break;
+      }
+      uint8_t* st = sD + (uint32_t)(pipe * 2 + s) * 2u * RSB;
+      // fill: piece = 4 consecutive columns of one row k; a warp covers 8 rows x 64 contiguous bytes of each
+      for (int e0 = ptid; e0 < kc * 32; e0 += 4 * RT) {
+        float4 v[4];
+        int kk[4], nn[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = e0 + u * RT;
+          const int ln = e & 31, grp = e >> 5;
+          kk[u] = 8 * (grp >> 3) + (ln & 7);
+          nn[u] = 8 * (2 * (grp & 7) + (ln >> 4)) + 4 * ((ln >> 3) & 1);
+          v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+          const int k = k0 + kk[u];
+          long off;
+          if (e < kc * 32 && k < d.K && col_in(nn[u], off))
+            v[u] = __ldg(reinterpret_cast<const float4*>(in + off + (long)(k / d.in_split) * d.in_hi +
+                                                        (long)(k % d.in_split) * d.in_lo));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = e0 + u * RT;
+          if (e >= kc * 32) break;
+          uint32_t h0, l0, h1, l1;
+          tc::split_pack(v[u].x, v[u].y, h0, l0);
+          tc::split_pack(v[u].z, v[u].w, h1, l1);
+          const uint32_t o = tc::mnmajor_offset(nn[u], kk[u], 128);
+          *reinterpret_cast<uint2*>(st + o) = make_uint2(h0, h1);
+          *reinterpret_cast<uint2*>(st + RSB + o) = make_uint2(l0, l1);
+        }
+      }
+      tc::fence_async_smem();
+      tc::tc_before_sync();
+      rt_sync(pipe);
+      tc::tc_after_sync();
+      if (ptid == 0) {
+        const uint32_t x_hi = tc::smem_u32(st), x_lo = x_hi + RSB;
+        const uint32_t as[3] = {x_hi, x_hi, x_lo}, bs[3] = {t_hi, t_lo, t_hi};
+#pragma unroll
+        for (int ps = 0; ps < 3; ++ps)
+          for (int kk = 0; kk < kc; kk += 16) {
+            const uint64_t ad = tc::mnmajor_desc(as[ps] + (uint32_t)(kk / 8) * 2048u, 2048u, 128u);
+            const uint64_t bd = tc::kmajor_desc(bs[ps] + (uint32_t)((k0 + kk) / 8) * 128u, 128u, (uint32_t)Kp * 16u);
+            tc::mma_bf16(tmem, ad, bd, idesc, (ch > 0 || ps > 0 || kk > 0) ? 1u : 0u);
+          }
+        tc::mma_commit(&bar_m[pipe][s]);
+      }
+    }
+    if (!ok) break;
+    {
+      const uint32_t gl = g - 1;
+      const bool w = tc::mbar_wait(&bar_m[pipe][gl & 1u], (gl >> 1) & 1u);
+      if (!(ok = rt_sync_and(pipe, w))) break;
+      tc::tc_after_sync();
+    }
+    // epilogue: lane = column n; the two halves of the pipeline take alternate 16-row chunks of m
+    long obase = 0;
+    bool nv;
+    {
+      long b, c;
+      if (nbi > 1) {
+        b = bfirst + (n_ep >> nshift);
+        c = n_ep & ((1 << nshift) - 1);
+      } else {
+        b = bfirst;
+        c = n0 + n_ep;
+      }
+      nv = b < d.nb && c < d.N;
+      if (nv) obase = (b / d.nb2) * d.out_b1 + (b % d.nb2) * d.out_b2 + c;
+    }
+    for (int jj = half; jj < Mp / 16; jj += 2) {
+      float v[16];
+      tc::tmem_ld16(tmem + lq + 16u * jj, v);
+      if (nv) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int m = 16 * jj + i;
+          if (m < d.M) {
+            float* p = out + obase + (long)(m / d.out_split) * d.out_hi + (long)(m % d.out_split) * d.out_lo;
+            *p = accumulate ? *p + v[i] : v[i];
+          }
+        }
+      }
+    }
+    tc::tc_before_sync();
+    rt_sync(pipe);
+    tc::tc_after_sync();
+  }
+  if (!ok) {   // leave no MMA in flight before freeing tensor memory
+    if (g >= 1) tc::mbar_wait(&bar_m[pipe][(g - 1) & 1u], ((g - 1) >> 1) & 1u);
+    if (g >= 2) tc::mbar_wait(&bar_m[pipe][g & 1u], ((g - 2) >> 1) & 1u);
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  if (warp == 0) tc::tmem_free(tslot, 512);
+}
+
 // ---------------------------------------------------------------------------------------------------- mixing
 // Per-frequency mixing on tensor cores: out_f = g_f (W x_f) + U_f (V_f x_f) for every row b of frequency f, with
 // x = [re | im] (2C values), W the [2C x 2C] channel map and g_f complex. A CTA item = 128 rows b of one frequency;
@@ -506,6 +689,35 @@ int ffno_xform_tc(const void* tpack, const float* in, float* out, const ffno_xfo
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }
+
+int ffno_xform_tcr(const void* tpack, int Mp, int Kp, const float* in, float* out, const ffno_xform_desc* desc,
+                   int accumulate, int* err, ffno_stream_t stream) {
+  if (!tpack || !in || !out || !desc || !err || (reinterpret_cast<uintptr_t>(tpack) % 16)) return FFNO_EINVAL;
+  const ffno_xform_desc& d = *desc;
+  if (d.nb < 1 || d.nb2 < 1 || d.K < 1 || d.M < 1 || d.N < 1 || d.in_split < 1 || d.out_split < 1) return FFNO_EINVAL;
+  if (Mp % 16 || Mp < d.M || Mp > 256 || Kp % 16 || Kp < d.K) return FFNO_EINVAL;
+  if ((size_t)Mp * Kp * 4 > ffno_xform_tcr_max_table_bytes()) return FFNO_EINVAL;
+  if (d.N % 4 || d.in_lo % 4 || d.in_hi % 4 || d.in_b1 % 4 || d.in_b2 % 4) return FFNO_EINVAL;   // float4 loads
+  if (reinterpret_cast<uintptr_t>(in) % 16) return FFNO_EINVAL;
+  int nbi = 1, nshift = 0;
+  if (d.N < 128 && 128 % d.N == 0) {
+    nbi = 128 / (int)d.N;
+    while ((1 << nshift) < d.N) ++nshift;
+  }
+  const long ntn = (d.N + 127) / 128;
+  const long items = nbi > 1 ? (d.nb + nbi - 1) / nbi : d.nb * ntn;
+  const size_t smem = 1024 + (((size_t)Mp * Kp * 4 + 1023) & ~(size_t)1023) + 4 * 2 * (size_t)RSB;
+  if (cudaFuncSetAttribute(k_xform_rt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return FFNO_ELAUNCH;
+  const long pairs = (items + 1) / 2;
+  const long grid = pairs < sms() ? pairs : sms();
+  k_xform_rt<<<(unsigned)grid, 2 * RT, smem, (cudaStream_t)stream>>>(static_cast<const uint8_t*>(tpack), Mp, Kp, in,
+                                                                    out, d, nbi, nshift, ntn, items, accumulate, err);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_xform_tcr_max_table_bytes(void) { return 96 * 1024; }
 
 int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, long sb, long s_im, int C,
                          const void* wpack, const float* g, const float* U, const float* Vm, int rank, int* err,

@@ -45,6 +45,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, bool b_mn = fals
          | ((uint32_t)(M >> 4) << 24);   // M / 16
 }
 
+// the same with either operand MN-major (A: bit 15, B: bit 16)
+__host__ __device__ constexpr uint32_t idesc_bf16_ab(int M, int N, bool a_mn, bool b_mn) {
+  return idesc_bf16(M, N, b_mn) | ((a_mn ? 1u : 0u) << 15);
+}
+
 // byte offset of element (n, k) of an N x K operand stored MN-major (n contiguous): 8 (k) x 16-byte core matrices,
 // n-groups adjacent (SBO = 128 bytes), k-groups N * 16 bytes apart (LBO)
 __device__ __forceinline__ uint32_t mnmajor_offset(int n, int k, int N) {

@@ -78,31 +78,42 @@ def tc_pack(device, *mats):
     return torch.cat(parts).to(device).contiguous()
 
 
+def _split_kmajor(m):
+    """hi = bf16(m), lo = bf16(m - hi) of a float64 [R][K] array, each in the canonical K-major order, as one flat
+    BF16 tensor (hi then lo)."""
+    t = torch.from_numpy(np.ascontiguousarray(m))
+    hi = t.to(torch.bfloat16)
+    lo = (t - hi.double()).to(torch.bfloat16)
+    return torch.cat([pack_kmajor(hi.float()).reshape(-1), pack_kmajor(lo.float()).reshape(-1)])
+
+
 class TcXform:
-    """A transform table T [M][K] (float64 numpy) packed for ffno_xform_tc: split-BF16 per 128-row m-tile and 64-wide
-    k-chunk, in slices of at most 256 rows (one kernel call each)."""
+    """A transform table T [M][K] (float64 numpy) packed for the tensor-core transforms, in slices of at most 256 rows
+    (one kernel call each): per slice the streamed pack of ffno_xform_tc (split-BF16 per 128-row m-tile and 64-wide
+    k-chunk) and, when the slice fits in shared memory, the resident pack of ffno_xform_tcr (the whole [Mp][Kp] table
+    as one canonical operand, Mp and Kp rounded up to 16)."""
 
     def __init__(self, T, device):
         T = np.asarray(T, dtype=np.float64)
         self.M, self.K = T.shape
         Kp = (self.K + 15) // 16 * 16
+        limit = nat.lib().ffno_xform_tcr_max_table_bytes()
         self.slices = []
         for r0 in range(0, self.M, 256):
             rows = min(256, self.M - r0)
             mt = (rows + 127) // 128
             pad = np.zeros((mt * 128, Kp))
             pad[:rows, :self.K] = T[r0:r0 + rows]
-            parts = []
-            for t in range(mt):
-                for k0 in range(0, Kp, 64):
-                    sub = torch.from_numpy(pad[t * 128:(t + 1) * 128, k0:min(Kp, k0 + 64)].copy())
-                    hi = sub.to(torch.bfloat16)
-                    lo = (sub - hi.double()).to(torch.bfloat16)
-                    parts += [pack_kmajor(hi.float()).reshape(-1), pack_kmajor(lo.float()).reshape(-1)]
+            parts = [_split_kmajor(pad[t * 128:(t + 1) * 128, k0:min(Kp, k0 + 64)])
+                     for t in range(mt) for k0 in range(0, Kp, 64)]
             packed = torch.cat(parts).to(device).contiguous()
             if packed.numel() * 2 != nat.lib().ffno_xform_tc_pack_bytes(rows, self.K):
                 raise RuntimeError("transform pack size mismatch")
-            self.slices.append((r0, rows, packed))
+            res = None
+            Mp = (rows + 15) // 16 * 16
+            if 4 * Mp * Kp <= limit:
+                res = (_split_kmajor(pad[:Mp]).to(device).contiguous(), Mp, Kp)
+            self.slices.append((r0, rows, packed, res))
 
 
 class Packed:
@@ -349,11 +360,15 @@ class Executor:
         tx = self.tc_table(tabs, name)
         if len(tx.slices) > 1 and desc.out_split < desc.M:
             raise ValueError("a transform taller than 256 rows needs single-level output addressing")
-        for r0, rows, packed in tx.slices:
+        for r0, rows, packed, res in tx.slices:
             d = nat.XformDesc.from_buffer_copy(desc)
             d.M = rows
-            nat.call("ffno_xform_tc", packed.data_ptr(), inp.data_ptr(), out.data_ptr() + 4 * r0 * desc.out_lo, d, 0,
-                     ws.err.data_ptr(), s, tag=name)
+            dst = out.data_ptr() + 4 * r0 * desc.out_lo
+            if res is not None:
+                nat.call("ffno_xform_tcr", res[0].data_ptr(), res[1], res[2], inp.data_ptr(), dst, d, 0,
+                         ws.err.data_ptr(), s, tag=name)
+            else:
+                nat.call("ffno_xform_tc", packed.data_ptr(), inp.data_ptr(), dst, d, 0, ws.err.data_ptr(), s, tag=name)
 
     # -------------------------------------------------------------------------------------------- geometry
     def geometry(self, z_scale):

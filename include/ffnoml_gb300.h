@@ -297,6 +297,12 @@ int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const flo
 int ffno_xform_tc_pack_bytes(int M, int K);
 int ffno_xform_tc(const void* tpack, const float* in, float* out, const ffno_xform_desc* desc, int accumulate, int* err,
                   ffno_stream_t stream);
+/* ffno_xform on tensor cores with the whole table resident in shared memory (the split table [Mp][Kp] packed as one
+ * canonical K-major operand, hi then lo; Mp a multiple of 16 <= 256, Kp a multiple of 16, 4 Mp Kp <=
+ * ffno_xform_tcr_max_table_bytes()). N, the input strides and the input pointer must be float4-aligned. */
+int ffno_xform_tcr_max_table_bytes(void);
+int ffno_xform_tcr(const void* tpack, int Mp, int Kp, const float* in, float* out, const ffno_xform_desc* desc,
+                   int accumulate, int* err, ffno_stream_t stream);
 /* ffno_spectral_mix on tensor cores (split-BF16); wpack = [wbig^T (2C x 2C)]; C = 16, 32, 64; strides multiples of 4
  * floats. */
 int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, long sb, long s_im, int C,

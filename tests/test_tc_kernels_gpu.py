@@ -224,11 +224,13 @@ def test_fuse_bwd_tc(C):
 
 
 @pytest.mark.parametrize("which", ["wf", "hf", "wi", "zf", "zi"])
-def test_xform_tc_matches_fp32(which):
+@pytest.mark.parametrize("C", [16, 64])
+@pytest.mark.parametrize("kind", ["streamed", "resident"])
+def test_xform_tc_matches_fp32(which, C, kind):
     from ffnoml_gb300 import tables as tb
     from ffnoml_gb300.executor import TcXform, _descs
     nat = _nat()
-    D, H, W, C, live = 12, 24, 20, 16, 13
+    D, H, W, live = 12, 24, 20, 13
     Wf = W // 2 + 1
     twf, thf, thi, twi = tb.plane_dft(H, W)
     g = np.random.default_rng(3)
@@ -245,11 +247,16 @@ def test_xform_tc_matches_fp32(which):
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     nat.call("ffno_xform", Tf.data_ptr(), x.data_ptr(), a.data_ptr(), d, 0, _s())
     tx = TcXform(T, torch.device("cuda"))
-    for r0, rows, packed in tx.slices:
+    for r0, rows, packed, res in tx.slices:
         dd = nat.XformDesc.from_buffer_copy(d)
         dd.M = rows
-        nat.call("ffno_xform_tc", _hold(packed), x.data_ptr(), b.data_ptr() + 4 * r0 * d.out_lo, dd, 0,
-                 err.data_ptr(), _s())
+        if kind == "resident":
+            assert res is not None
+            nat.call("ffno_xform_tcr", _hold(res[0]), res[1], res[2], x.data_ptr(), b.data_ptr() + 4 * r0 * d.out_lo,
+                     dd, 0, err.data_ptr(), _s())
+        else:
+            nat.call("ffno_xform_tc", _hold(packed), x.data_ptr(), b.data_ptr() + 4 * r0 * d.out_lo, dd, 0,
+                     err.data_ptr(), _s())
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     _close(b, a)
