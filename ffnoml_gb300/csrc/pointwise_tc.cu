@@ -4,11 +4,20 @@
 // Activations, residuals and GroupNorm statistics stay FP32 in HBM, so every kernel has the contract of an FP32 entry
 // point of pointwise_f32.cu / backward_f32.cu (or of a stage of one).
 //
-// CTA = 256 threads = two warpgroups over one tile of 128 voxels: thread t serves voxel row t % 128 (tensor-memory lane
-// t % 128), warpgroup t / 128 the even or odd 16-column chunks of every accumulator. The split weights
-// (packed on the host in the canonical K-major order) are bulk-copied (TMA) into shared memory once per persistent
-// CTA. Each GEMM is issued by thread 0 and completes on an mbarrier; every wait is bounded: a timeout sets *err, all
-// threads leave the tile loop together, and the CTA frees its tensor memory after one more bounded wait.
+// Orientation: every GEMM is computed transposed, D^T [features][128 voxels] = W X^T, with the split weights
+// (packed on the host in the canonical K-major order, [out][in]) as the A operand and the voxel tile as the B operand.
+// A tensor-memory lane is then an output feature and a column a voxel, so in every epilogue a warp's loads and stores
+// cover 32 consecutive channels of one voxel (128-byte runs), and intermediate activations are written back as
+// MN-major B tiles (voxels contiguous) with conflict-free 16-byte stores. Weight matrices with fewer than 128 rows
+// are read as 128-row A operands whose extra rows (the bytes that follow in shared memory) land in accumulator lanes
+// no epilogue reads. Input tiles arrive as split K-major tiles [128 voxels][K], filled from FP32 HBM.
+//
+// A CTA holds two pipelines of 256 threads (eight warps each) that take alternate 128-voxel tiles; each has its own
+// operand tiles, tensor-memory columns, MMA mbarrier and named barrier, so one pipeline's fills and epilogues overlap
+// the other's MMAs. In an epilogue, warp w of a pipeline reads lanes 32 (w % 4) .. + 31 and the voxel columns of its
+// half (w / 4). MMAs are issued by one thread of the pipeline and complete on its mbarrier; every wait is bounded: a
+// timeout sets *err, the pipeline leaves its tile loop, and the CTA frees its tensor memory after one more bounded
+// wait.
 #include <math.h>
 
 #include "common.cuh"
@@ -18,8 +27,9 @@ using namespace ffno;
 
 namespace {
 
-constexpr int TM = 128;  // voxels per tile = MMA M
-constexpr int TT = 256;  // threads per CTA (two warpgroups)
+constexpr int TM = 128;  // voxels per tile = accumulator columns
+constexpr int PT = 256;  // threads per pipeline
+constexpr int CT = 512;  // threads per CTA (two pipelines)
 constexpr int FB = 8;    // fill: independent loads in flight per thread
 
 __host__ __device__ constexpr uint32_t tmem_cols(int n) {
@@ -28,7 +38,7 @@ __host__ __device__ constexpr uint32_t tmem_cols(int n) {
 
 // bytes of one split matrix (hi + lo) of R x K
 __host__ __device__ constexpr uint32_t mat_bytes(int R, int K) { return (uint32_t)R * K * 2 * 2; }
-// bytes of one split activation tile of 128 x K
+// bytes of one split voxel tile of 128 x K
 __host__ __device__ constexpr uint32_t tile_bytes(int K) { return (uint32_t)TM * K * 2 * 2; }
 
 struct Ctx {
@@ -63,82 +73,6 @@ __device__ __forceinline__ bool load_weights(void* dst, const void* src, uint32_
   return ok;
 }
 
-// Issue up to two split GEMMs D_i = A_i B_i^T (thread 0) behind one commit and wait for them (all threads).
-__device__ __forceinline__ bool gemms(Ctx& cx, int* err, uint32_t d0, Split a0, Split b0, int k0, int n0,
-                                      uint32_t d1 = 0, Split a1 = Split{nullptr, 0}, Split b1 = Split{nullptr, 0},
-                                      int k1 = 0, int n1 = 0) {
-  tc::fence_async_smem();
-  tc::tc_before_sync();
-  __syncthreads();
-  tc::tc_after_sync();
-  if (threadIdx.x == 0) {
-    tc::gemm3_128xN(d0, tc::smem_u32(a0.hi()), tc::smem_u32(a0.lo()), tc::smem_u32(b0.hi()), tc::smem_u32(b0.lo()),
-                    k0, n0);
-    if (a1.p)
-      tc::gemm3_128xN(d1, tc::smem_u32(a1.hi()), tc::smem_u32(a1.lo()), tc::smem_u32(b1.hi()), tc::smem_u32(b1.lo()),
-                      k1, n1);
-    tc::mma_commit(cx.bar);
-  }
-  const bool ok = __syncthreads_and(tc::mbar_wait(cx.bar, cx.phase)) != 0;
-  cx.phase ^= 1u;
-  tc::tc_after_sync();
-  if (!ok && threadIdx.x == 0) atomicExch(err, 2);
-  cx.ok = ok;
-  return ok;
-}
-
-__device__ __forceinline__ void finish(Ctx& cx, uint32_t tmem, uint32_t ncol) {
-  if (!cx.ok) tc::mbar_wait(cx.bar, cx.phase ^ 1u);
-  tc::tc_before_sync();
-  __syncthreads();
-  tc::tc_after_sync();
-  if (threadIdx.x < 32) tc::tmem_free(tmem, ncol);
-}
-
-// Fill a split tile [128][KW] from FP32 sources: f(v, k) returns columns k..k+3 of voxel v (v < V); rows past the
-// cube are zero. Consecutive threads fill consecutive 8-byte pieces of the canonical layout.
-template <int KW, typename F>
-__device__ __forceinline__ void fill_tile(Split t, long v0, long V, F f) {
-  constexpr int NE = TM * KW / 4;
-  for (int e0 = threadIdx.x; e0 < NE; e0 += TT * FB) {
-    float4 a[FB];
-#pragma unroll
-    for (int u = 0; u < FB; ++u) {  // issue the loads of FB pieces before converting any of them
-      const int e = e0 + u * TT;
-      const int h = e & 1, r8 = (e >> 1) & 7, q = e >> 4;
-      const int kb = q % (KW / 8), rb = q / (KW / 8);
-      const long v = v0 + rb * 8 + r8;
-      a[u] = (e < NE && v < V) ? f(v, kb * 8 + h * 4) : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-#pragma unroll
-    for (int u = 0; u < FB; ++u) {
-      const int e = e0 + u * TT;
-      if (e >= NE) break;
-      uint32_t h0, l0, h1, l1;
-      tc::split_pack(a[u].x, a[u].y, h0, l0);
-      tc::split_pack(a[u].z, a[u].w, h1, l1);
-      *reinterpret_cast<uint2*>(t.hi() + (size_t)e * 8) = make_uint2(h0, h1);
-      *reinterpret_cast<uint2*>(t.lo() + (size_t)e * 8) = make_uint2(l0, l1);
-    }
-  }
-}
-
-// Write 16 values of this thread's row into a split tile with K columns at columns c0..c0+15.
-__device__ __forceinline__ void put16(Split t, int r, int c0, int K, const float (&v)[16]) {
-  uint32_t h[8], l[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) tc::split_pack(v[2 * i], v[2 * i + 1], h[i], l[i]);
-  const uint32_t o0 = tc::kmajor_offset(r, c0, K), o1 = tc::kmajor_offset(r, c0 + 8, K);
-  *reinterpret_cast<uint4*>(t.hi() + o0) = make_uint4(h[0], h[1], h[2], h[3]);
-  *reinterpret_cast<uint4*>(t.hi() + o1) = make_uint4(h[4], h[5], h[6], h[7]);
-  *reinterpret_cast<uint4*>(t.lo() + o0) = make_uint4(l[0], l[1], l[2], l[3]);
-  *reinterpret_cast<uint4*>(t.lo() + o1) = make_uint4(l[4], l[5], l[6], l[7]);
-}
-
-__device__ __forceinline__ uint32_t lane_base() { return (uint32_t)(32 * ((threadIdx.x >> 5) & 3)) << 16; }
-__device__ __forceinline__ int row_of() { return threadIdx.x & (TM - 1); }
-__device__ __forceinline__ int wg_of() { return threadIdx.x >> 7; }
-
 // L2 prefetch of rows [n0, n0 + 128) of a [V][width] FP32 array, by one thread
 __device__ __forceinline__ void prefetch_rows(const float* base, long n0, long V, int width) {
   if (!base || n0 >= V) return;
@@ -148,190 +82,140 @@ __device__ __forceinline__ void prefetch_rows(const float* base, long n0, long V
 
 __device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
-// GroupNorm apply (+ GELU) of 4 consecutive channels k..k+3 with coefs [3][C]
+// GroupNorm coefficients (mean, gamma * rstd, beta) of 4 consecutive channels, and their application (+ GELU)
+struct Gn4 {
+  float4 m, s, b;
+};
+__device__ __forceinline__ Gn4 gn_coefs(const float* __restrict__ cf, int C, int k) {
+  return Gn4{ld4(cf + k), ld4(cf + C + k), ld4(cf + 2 * C + k)};
+}
 template <bool GELU>
-__device__ __forceinline__ float4 gn4(float4 p, const float* __restrict__ cf, int C, int k) {
-  float4 y;
-  y.x = (p.x - __ldg(cf + k)) * __ldg(cf + C + k) + __ldg(cf + 2 * C + k);
-  y.y = (p.y - __ldg(cf + k + 1)) * __ldg(cf + C + k + 1) + __ldg(cf + 2 * C + k + 1);
-  y.z = (p.z - __ldg(cf + k + 2)) * __ldg(cf + C + k + 2) + __ldg(cf + 2 * C + k + 2);
-  y.w = (p.w - __ldg(cf + k + 3)) * __ldg(cf + C + k + 3) + __ldg(cf + 2 * C + k + 3);
-  if (GELU) {
-    y.x = gelu(y.x);
-    y.y = gelu(y.y);
-    y.z = gelu(y.z);
-    y.w = gelu(y.w);
-  }
+__device__ __forceinline__ float4 gn_apply(float4 p, const Gn4& g) {
+  float4 y = make_float4((p.x - g.m.x) * g.s.x + g.b.x, (p.y - g.m.y) * g.s.y + g.b.y, (p.z - g.m.z) * g.s.z + g.b.z,
+                         (p.w - g.m.w) * g.s.w + g.b.w);
+  if (GELU) y = make_float4(gelu(y.x), gelu(y.y), gelu(y.z), gelu(y.w));
   return y;
 }
 
-__device__ __forceinline__ float gn1gelu(float p, const float* __restrict__ cf, int C, int k) {
-  return gelu((p - __ldg(cf + k)) * __ldg(cf + C + k) + __ldg(cf + 2 * C + k));
+// ---------------------------------------------------------------------------------------------------- pipelines
+struct Pipe {
+  uint64_t* bar;   // MMA completion
+  uint32_t phase;
+  bool ok;
+  int id, ptid, lane, q, half;
+  uint32_t tmem;   // this pipeline's first tensor-memory column (lane 0)
+  uint32_t lq;     // lane-quadrant offset of this warp
+  __device__ int feat() const { return 32 * q + lane; }   // accumulator lane = output feature of this thread
+};
+
+__device__ __forceinline__ void pipe_sync(int id) {
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + id), "n"(PT) : "memory");
 }
 
-// Per-tile depth-weighted group statistics of the tile's values, merged with Chan's update into acc (threads
-// g < GMAX). Each thread holds, in v[C], the columns of the 16-column chunks of its warpgroup (chunk j belongs to
-// warpgroup j % 2; a group never straddles two chunks); w is its row's weight (0 past the cube). Fixed reduction order.
-template <int C>
-__device__ __forceinline__ void row_group_stats(const float (&v)[C], float w, float* red, float* gm, float* wsum,
-                                                GroupAcc& acc) {
-  constexpr int CPG = C / GMAX;
-  constexpr int NW = TT / 32;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, wg = wg_of();
-  float ws = wg == 0 ? w : 0.f;
-#pragma unroll
-  for (int o = 16; o; o >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, o);
-  float s[GMAX];
-#pragma unroll
-  for (int g = 0; g < GMAX; ++g) s[g] = 0.f;
-#pragma unroll
-  for (int c = 0; c < C; ++c)
-    if (((c >> 4) & 1) == wg) s[c / CPG] += v[c];
-#pragma unroll
-  for (int g = 0; g < GMAX; ++g) {
-    float x = w * s[g];
-#pragma unroll
-    for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    s[g] = x;
-  }
-  if (lane == 0) {
-    red[warp * (GMAX + 1) + GMAX] = ws;
-#pragma unroll
-    for (int g = 0; g < GMAX; ++g) red[warp * (GMAX + 1) + g] = s[g];
-  }
-  __syncthreads();
-  if (tid == 0) {
-    float t = 0.f;
-    for (int q = 0; q < NW; ++q) t += red[q * (GMAX + 1) + GMAX];
-    *wsum = t;
-  }
-  if (tid < GMAX) {
-    float t = 0.f, wt = 0.f;
-    for (int q = 0; q < NW; ++q) {
-      t += red[q * (GMAX + 1) + tid];
-      wt += red[q * (GMAX + 1) + GMAX];
-    }
-    wt *= CPG;
-    gm[tid] = wt > 0.f ? t / wt : 0.f;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int g = 0; g < GMAX; ++g) s[g] = 0.f;
-#pragma unroll
-  for (int c = 0; c < C; ++c)
-    if (((c >> 4) & 1) == wg) {
-      const float d = v[c] - gm[c / CPG];
-      s[c / CPG] += d * d;
-    }
-#pragma unroll
-  for (int g = 0; g < GMAX; ++g) {
-    float x = w * s[g];
-#pragma unroll
-    for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    s[g] = x;
-  }
-  __syncthreads();
-  if (lane == 0)
-#pragma unroll
-    for (int g = 0; g < GMAX; ++g) red[warp * (GMAX + 1) + g] = s[g];
-  __syncthreads();
-  if (tid < GMAX) {
-    float t = 0.f;
-    for (int q = 0; q < NW; ++q) t += red[q * (GMAX + 1) + tid];
-    chan_merge(acc, (double)*wsum * CPG, (double)gm[tid], (double)t);
-  }
-  __syncthreads();
-}
-
-// ---------------------------------------------------------------------------------------------------- ping-pong
-// Two warpgroups of a CTA run independent tile pipelines over alternate tiles (warpgroup w takes tiles
-// 2 * blockIdx.x + w, then every 2 * gridDim.x): each has its own operand tiles in shared memory, its own tensor-memory
-// columns and MMA mbarrier, and synchronises with a named barrier of its 128 threads, so one warpgroup's loads and
-// epilogue overlap the other's MMAs and waits. Thread t of a warpgroup serves voxel row t (tensor-memory lane t) and
-// every column of it. The split weights are shared.
-constexpr int WGT = 256;              // threads per pipeline
-constexpr int SPL = WGT / TM;         // threads per voxel row (each takes every SPL-th 16-column chunk)
-constexpr int CT = 2 * WGT;           // threads per CTA (two pipelines)
-
-__device__ __forceinline__ void wg_sync(int wg) { asm volatile("bar.sync %0, %1;" ::"r"(1 + wg), "n"(WGT) : "memory"); }
-
-// whether this thread's part of the row owns 16-column chunk jj
-__device__ __forceinline__ bool owns(int jj, int half) { return SPL == 1 || (jj % SPL) == half; }
-
-// Named-barrier AND over the warpgroup's predicates.
-__device__ __forceinline__ bool wg_sync_and(int wg, bool p) {
+__device__ __forceinline__ bool pipe_sync_and(int id, bool p) {
   uint32_t r;
   asm volatile(
       "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.and.pred po, %2, %3, pi;\n selp.u32 %0, 1, 0, po;\n}"
       : "=r"(r)
-      : "r"((uint32_t)p), "r"(1 + wg), "n"(WGT)
+      : "r"((uint32_t)p), "r"(1 + id), "n"(PT)
       : "memory");
   return r != 0;
 }
 
-struct WCtx {
-  uint64_t* bar;  // this warpgroup's MMA barrier
-  uint32_t phase;
-  bool ok;
-  int wg, wtid;
-};
-
-// A split operand in shared memory for the MMA: hi and lo shared-space addresses and the row-group stride.
+// An MMA operand in shared memory: hi / lo shared addresses, descriptor strides, bytes per 16-wide k step.
 struct Op {
-  uint32_t hi, lo, sbo;
+  uint32_t hi, lo, lbo, sbo, step;
+  bool mn;
 };
-__device__ __forceinline__ Op op_of(Split s, int K) {
-  return Op{tc::smem_u32(s.hi()), tc::smem_u32(s.lo()), (uint32_t)K * 16u};
+// weight matrix [R][K] (K-major) from row r0 (a multiple of 8) and column k0 (a multiple of 8); read as 128 rows
+__device__ __forceinline__ Op wop(const uint8_t* p, int R, int K, int r0 = 0, int k0 = 0) {
+  const uint32_t h = tc::smem_u32(p) + (uint32_t)(r0 / 8) * (uint32_t)K * 16u + (uint32_t)(k0 / 8) * 128u;
+  return Op{h, h + (uint32_t)R * K * 2, 128u, (uint32_t)K * 16u, 256u, false};
 }
-// Columns k0.. of a split operand with Ktot columns (a K-slice; k0 a multiple of 8).
-__device__ __forceinline__ Op op_kslice(Split s, int Ktot, int k0) {
+// voxel tile [128][K] stored K-major (filled from HBM), optionally the K-slice from column k0
+__device__ __forceinline__ Op kop(Split t, int K, int k0 = 0) {
   const uint32_t o = (uint32_t)(k0 / 8) * 128u;
-  return Op{tc::smem_u32(s.hi()) + o, tc::smem_u32(s.lo()) + o, (uint32_t)Ktot * 16u};
+  return Op{tc::smem_u32(t.hi()) + o, tc::smem_u32(t.lo()) + o, 128u, (uint32_t)K * 16u, 256u, false};
+}
+// voxel tile [128][K] stored MN-major (voxels contiguous; written by epilogues)
+__device__ __forceinline__ Op mop(Split t) {
+  return Op{tc::smem_u32(t.hi()), tc::smem_u32(t.lo()), 2048u, 128u, 4096u, true};
 }
 
-// D [128 x N] (+)= A B^T over K columns, split-BF16 (Ah Bh + Ah Bl + Al Bh); accumulates onto D when acc.
-__device__ __forceinline__ void gemm3_op(uint32_t tmem_d, Op a, Op b, int K, int N, bool acc) {
-  const uint32_t idesc = tc::idesc_bf16(128, N);
+// D^T [128 x 128] (+)= A B^T over K, split-BF16 (Ah Bh + Ah Bl + Al Bh); A K-major, B K- or MN-major
+__device__ __forceinline__ void mma3(uint32_t d, const Op& a, const Op& b, int K, bool acc) {
+  const uint32_t idesc = tc::idesc_bf16_ab(128, 128, false, b.mn);
   const uint32_t as[3] = {a.hi, a.hi, a.lo}, bs[3] = {b.hi, b.lo, b.hi};
 #pragma unroll
   for (int s = 0; s < 3; ++s)
     for (int k = 0; k < K; k += 16) {
-      const uint64_t ad = tc::kmajor_desc(as[s] + (uint32_t)(k / 8) * 128u, 128u, a.sbo);
-      const uint64_t bd = tc::kmajor_desc(bs[s] + (uint32_t)(k / 8) * 128u, 128u, b.sbo);
-      tc::mma_bf16(tmem_d, ad, bd, idesc, (acc || s > 0 || k > 0) ? 1u : 0u);
+      const uint64_t ad = tc::kmajor_desc(as[s] + (uint32_t)(k / 16) * a.step, a.lbo, a.sbo);
+      const uint64_t bd = tc::kmajor_desc(bs[s] + (uint32_t)(k / 16) * b.step, b.lbo, b.sbo);
+      tc::mma_bf16(d, ad, bd, idesc, (acc || s > 0 || k > 0) ? 1u : 0u);
     }
 }
 
-// Issue up to two split GEMMs (the warpgroup's thread 0) behind one commit and wait for them (the warpgroup).
-__device__ __forceinline__ bool wg_gemms(WCtx& cx, int* err, uint32_t d0, Op a0, Op b0, int k0, int n0,
-                                         bool acc0 = false, uint32_t d1 = 0, Op a1 = Op{0, 0, 0},
-                                         Op b1 = Op{0, 0, 0}, int k1 = 0, int n1 = 0) {
+struct Gemm {
+  uint32_t d;
+  Op a, b;
+  int K;
+  bool acc;
+};
+
+// Issue up to three split GEMMs (the pipeline's thread 0) behind one commit and wait for them (the pipeline).
+__device__ __forceinline__ bool pipe_gemms(Pipe& p, int* err, const Gemm& g0, const Gemm* g1 = nullptr,
+                                           const Gemm* g2 = nullptr) {
   tc::fence_async_smem();
   tc::tc_before_sync();
-  wg_sync(cx.wg);
+  pipe_sync(p.id);
   tc::tc_after_sync();
-  if (cx.wtid == 0) {
-    gemm3_op(d0, a0, b0, k0, n0, acc0);
-    if (k1) gemm3_op(d1, a1, b1, k1, n1, false);
-    tc::mma_commit(cx.bar);
+  if (p.ptid == 0) {
+    mma3(g0.d, g0.a, g0.b, g0.K, g0.acc);
+    if (g1) mma3(g1->d, g1->a, g1->b, g1->K, g1->acc);
+    if (g2) mma3(g2->d, g2->a, g2->b, g2->K, g2->acc);
+    tc::mma_commit(p.bar);
   }
-  const bool ok = wg_sync_and(cx.wg, tc::mbar_wait(cx.bar, cx.phase));
-  cx.phase ^= 1u;
+  const bool ok = pipe_sync_and(p.id, tc::mbar_wait(p.bar, p.phase));
+  p.phase ^= 1u;
   tc::tc_after_sync();
-  if (!ok && cx.wtid == 0) atomicExch(err, 2);
-  cx.ok = ok;
+  if (!ok && p.ptid == 0) atomicExch(err, 2);
+  p.ok = ok;
   return ok;
 }
 
-// fill_tile for one warpgroup (wtid = thread within it)
+// 16 accumulator columns (voxels 64 half + 16 c .. + 15) of this thread's lane, from accumulator base column d
+__device__ __forceinline__ void tld(const Pipe& p, uint32_t d, int c, float (&v)[16]) {
+  tc::tmem_ld16(p.tmem + p.lq + d + (uint32_t)(64 * p.half + 16 * c), v);
+}
+
+// Write 16 values of feature j for voxels vl .. vl + 15 (vl a multiple of 8) into an MN-major split tile [128][K]
+__device__ __forceinline__ void put_mn(Split t, int j, int vl, const float (&v)[16]) {
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) tc::split_pack(v[8 * g + 2 * i], v[8 * g + 2 * i + 1], h[i], l[i]);
+    const uint32_t o = tc::mnmajor_offset(vl + 8 * g, j, TM);
+    *reinterpret_cast<uint4*>(t.hi() + o) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(t.lo() + o) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+}
+
+// Fill a split K-major tile [128][KW] from FP32 sources: f(v, k) returns columns k..k+3 of voxel v (v < V); rows past
+// the cube are zero. With 256 threads, thread t always serves columns fill_col<KW>(t) .. + 3.
+template <int KW>
+__device__ __forceinline__ int fill_col(int ptid) {
+  return ((ptid >> 4) % (KW / 8)) * 8 + (ptid & 1) * 4;
+}
 template <int KW, typename F>
-__device__ __forceinline__ void wg_fill_tile(Split t, long v0, long V, int wtid, F f) {
+__device__ __forceinline__ void fill_tile(Split t, long v0, long V, int ptid, F f) {
+  static_assert(16 % (KW / 8) == 0 || (KW / 8) % 16 == 0, "fill columns must be fixed per thread");
   constexpr int NE = TM * KW / 4;
-  for (int e0 = wtid; e0 < NE; e0 += WGT * FB) {
+  for (int e0 = ptid; e0 < NE; e0 += PT * FB) {
     float4 a[FB];
 #pragma unroll
     for (int u = 0; u < FB; ++u) {  // issue the loads of FB pieces before converting any of them
-      const int e = e0 + u * WGT;
+      const int e = e0 + u * PT;
       const int h = e & 1, r8 = (e >> 1) & 7, q = e >> 4;
       const int kb = q % (KW / 8), rb = q / (KW / 8);
       const long v = v0 + rb * 8 + r8;
@@ -339,7 +223,7 @@ __device__ __forceinline__ void wg_fill_tile(Split t, long v0, long V, int wtid,
     }
 #pragma unroll
     for (int u = 0; u < FB; ++u) {
-      const int e = e0 + u * WGT;
+      const int e = e0 + u * PT;
       if (e >= NE) break;
       uint32_t h0, l0, h1, l1;
       tc::split_pack(a[u].x, a[u].y, h0, l0);
@@ -350,768 +234,697 @@ __device__ __forceinline__ void wg_fill_tile(Split t, long v0, long V, int wtid,
   }
 }
 
-// Per-tile depth-weighted group statistics of one warpgroup's tile (every thread holds all C values of its row in
-// v, weight w; 0 past the cube), merged with Chan's update into acc (threads wtid < GMAX). Fixed reduction order.
-// red: [4][GMAX + 1] of this warpgroup.
+// The tile's depth weights into shared memory (wt[128]) and their warp partial sums (wpart[4]); threads ptid < 128.
+__device__ __forceinline__ void load_tile_weights(const Pipe& p, const float* __restrict__ dw, long v0, long V,
+                                                  float* wt, float* wpart) {
+  if (p.ptid < TM) {
+    const long v = v0 + p.ptid;
+    float w = v < V ? __ldg(dw + v) : 0.f;
+    wt[p.ptid] = w;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    if (p.lane == 0) wpart[p.ptid >> 5] = w;
+  }
+}
+
+// Depth-weighted statistics of the tile's output features (lanes < C of the accumulator at column d; the tile's
+// weights wt[128], partial sums wpart[4] written before the last pipeline barrier), merged with Chan's update into
+// acc[g] = (w, mean, m2) by the thread holding the group's first lane. Fixed order throughout.
 template <int C>
-__device__ __forceinline__ void wg_row_group_stats(const float (&v)[C], float w, float* red, float* gm, float* wsum,
-                                                   GroupAcc& acc, int wg, int wtid) {
+__device__ __forceinline__ void tile_stats(const Pipe& p, uint32_t d, const float* wt, const float* wpart,
+                                           float* red /* [2][2][GMAX] */, double* acc /* [GMAX][3] */) {
   constexpr int CPG = C / GMAX;
-  const int lane = wtid & 31, wl = wtid >> 5, half = wtid / TM;
-  float ws = half == 0 ? w : 0.f;
+  const int f = p.feat(), g = f / CPG;
+  const bool live = f < C;
+  const float wsum = (wpart[0] + wpart[1]) + (wpart[2] + wpart[3]);
+  float s = 0.f;
 #pragma unroll
-  for (int o = 16; o; o >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, o);
-  float s[GMAX];
+  for (int c = 0; c < 4; ++c) {
+    float v[16];
+    tld(p, d, c, v);
 #pragma unroll
-  for (int g = 0; g < GMAX; ++g) s[g] = 0.f;
-#pragma unroll
-  for (int c = 0; c < C; ++c)
-    if (owns(c / 16, half)) s[c / CPG] += v[c];
-#pragma unroll
-  for (int g = 0; g < GMAX; ++g) {
-    float x = w * s[g];
-#pragma unroll
-    for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    s[g] = x;
+    for (int i = 0; i < 16; ++i) s = fmaf(wt[64 * p.half + 16 * c + i], v[i], s);
   }
-  if (lane == 0) {
-    red[wl * (GMAX + 1) + GMAX] = ws;
 #pragma unroll
-    for (int g = 0; g < GMAX; ++g) red[wl * (GMAX + 1) + g] = s[g];
-  }
-  wg_sync(wg);
-  if (wtid == 0) {
-    float t = 0.f;
-    for (int q = 0; q < WGT / 32; ++q) t += red[q * (GMAX + 1) + GMAX];
-    *wsum = t;
-  }
-  if (wtid < GMAX) {
-    float t = 0.f, wt = 0.f;
-    for (int q = 0; q < WGT / 32; ++q) {
-      t += red[q * (GMAX + 1) + wtid];
-      wt += red[q * (GMAX + 1) + GMAX];
+  for (int o = 1; o < CPG; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (live && f % CPG == 0) red[p.half * GMAX + g] = s;
+  pipe_sync(p.id);
+  const float wt_g = wsum * CPG;
+  const float mean = live && wt_g > 0.f ? (red[g] + red[GMAX + g]) / wt_g : 0.f;
+  float s2 = 0.f;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float v[16];
+    tld(p, d, c, v);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const float e = v[i] - mean;
+      s2 = fmaf(wt[64 * p.half + 16 * c + i] * e, e, s2);
     }
-    wt *= CPG;
-    gm[wtid] = wt > 0.f ? t / wt : 0.f;
   }
-  wg_sync(wg);
 #pragma unroll
-  for (int g = 0; g < GMAX; ++g) s[g] = 0.f;
-#pragma unroll
-  for (int c = 0; c < C; ++c)
-    if (owns(c / 16, half)) {
-      const float d = v[c] - gm[c / CPG];
-      s[c / CPG] += d * d;
-    }
-#pragma unroll
-  for (int g = 0; g < GMAX; ++g) {
-    float x = w * s[g];
-#pragma unroll
-    for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    s[g] = x;
+  for (int o = 1; o < CPG; o <<= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  if (live && f % CPG == 0) red[2 * GMAX + p.half * GMAX + g] = s2;
+  pipe_sync(p.id);
+  if (live && f % CPG == 0 && p.half == 0) {
+    double* a = acc + 3 * g;
+    GroupAcc ga{a[0], a[1], a[2]};
+    chan_merge(ga, (double)wt_g, (double)mean, (double)(red[2 * GMAX + g] + red[3 * GMAX + g]));
+    a[0] = ga.w;
+    a[1] = ga.mean;
+    a[2] = ga.m2;
   }
-  if (lane == 0)
-#pragma unroll
-    for (int g = 0; g < GMAX; ++g) red[wl * (GMAX + 1) + g] = s[g];
-  wg_sync(wg);
-  if (wtid < GMAX) {
-    float t = 0.f;
-    for (int q = 0; q < WGT / 32; ++q) t += red[q * (GMAX + 1) + wtid];
-    chan_merge(acc, (double)*wsum * CPG, (double)gm[wtid], (double)t);
-  }
-  wg_sync(wg);
+  pipe_sync(p.id);
 }
 
-// The CTA's GroupNorm partial: warpgroup 1's statistics merged into warpgroup 0's (fixed order). All threads call it.
-__device__ __forceinline__ void wg_write_partial(double* partials, GroupAcc acc, double* xs, int wg, int wtid) {
-  if (wg == 1 && wtid < GMAX) {
-    xs[3 * wtid] = acc.w;
-    xs[3 * wtid + 1] = acc.mean;
-    xs[3 * wtid + 2] = acc.m2;
-  }
+// The CTA's GroupNorm partial: pipeline 1's statistics merged into pipeline 0's (fixed order). All threads call it.
+__device__ __forceinline__ void write_partial2(double* partials, const double* acc /* [2][GMAX][3] */) {
   __syncthreads();
-  if (wg == 0 && wtid < GMAX) {
-    chan_merge(acc, xs[3 * wtid], xs[3 * wtid + 1], xs[3 * wtid + 2]);
-    double* p = partials + ((long)blockIdx.x * GMAX + wtid) * 3;
-    p[0] = acc.w;
-    p[1] = acc.mean;
-    p[2] = acc.m2;
+  const int t = threadIdx.x;
+  if (t < GMAX) {
+    GroupAcc a{acc[3 * t], acc[3 * t + 1], acc[3 * t + 2]};
+    chan_merge(a, acc[3 * GMAX + 3 * t], acc[3 * GMAX + 3 * t + 1], acc[3 * GMAX + 3 * t + 2]);
+    double* o = partials + ((long)blockIdx.x * GMAX + t) * 3;
+    o[0] = a.w;
+    o[1] = a.mean;
+    o[2] = a.m2;
   }
 }
 
-// After both warpgroups left their loops: wait once more (bounded) for an MMA of a failed wait, free tensor memory.
-__device__ __forceinline__ void wg_finish(const WCtx& cx, uint32_t tmem_all, uint32_t ncol_all) {
-  if (!cx.ok) tc::mbar_wait(cx.bar, cx.phase ^ 1u);
+// After both pipelines left their loops: wait once more (bounded) for an MMA of a failed wait, free tensor memory.
+__device__ __forceinline__ void pipe_finish(const Pipe& p, uint32_t tmem_all, uint32_t ncol_all) {
+  if (!p.ok) tc::mbar_wait(p.bar, p.phase ^ 1u);
   tc::tc_before_sync();
   __syncthreads();
   tc::tc_after_sync();
   if (threadIdx.x < 32) tc::tmem_free(tmem_all, ncol_all);
 }
 
-#define TC_PROLOGUE_WG(NCOLS)                                                            \
+// Prologue: tensor memory (NCOLS columns per pipeline), barriers, the pipeline of this thread; NP pipelines per CTA.
+#define PIPE_PROLOGUE(NCOLS, NP)                                                         \
   __shared__ uint64_t bars[3];                                                           \
   __shared__ uint32_t tslot;                                                             \
-  const int tid = threadIdx.x, wg = tid / WGT, wtid = tid % WGT, half = wtid / TM;      \
   constexpr uint32_t NCOL = tmem_cols(NCOLS);                                            \
-  static_assert(2 * NCOL <= 512, "two warpgroups' accumulators exceed tensor memory");   \
-  if (tid < 32) tc::tmem_alloc(&tslot, 2 * NCOL);                                        \
+  static_assert((NP) * NCOL <= 512, "accumulators exceed tensor memory");                \
+  const int tid = threadIdx.x;                                                           \
+  if (tid < 32) tc::tmem_alloc(&tslot, (NP) * NCOL);                                     \
   if (tid == 0) {                                                                        \
-    tc::mbar_init(&bars[0], 1);                                                          \
-    tc::mbar_init(&bars[1], 1);                                                          \
-    tc::mbar_init(&bars[2], 1);                                                          \
+    for (int i = 0; i < 3; ++i) tc::mbar_init(&bars[i], 1);                              \
     tc::mbar_init_fence();                                                               \
   }                                                                                      \
   tc::tc_before_sync();                                                                  \
   __syncthreads();                                                                       \
   tc::tc_after_sync();                                                                   \
-  const uint32_t tmem_all = tslot, tmem = tslot + (uint32_t)wg * NCOL;                   \
+  const int pid = tid / PT;                                                              \
+  Pipe P{&bars[1 + pid], 0u, true, pid, tid % PT, tid & 31, (tid >> 5) & 3, (tid % PT) / 128, \
+         tslot + (uint32_t)pid * NCOL, (uint32_t)(32 * ((tid >> 5) & 3)) << 16};          \
   Ctx wcx{&bars[0], 0u, true};                                                           \
-  WCtx cx{&bars[1 + wg], 0u, true, wg, wtid};                                            \
-  const uint32_t lb = lane_base();                                                       \
-  const int row = wtid % TM;                                                             \
   const long nt = (V + TM - 1) / TM;                                                     \
-  const long tstep = 2L * gridDim.x;                                                     \
-  (void)row;                                                                             \
-  (void)half;
-
-#define TC_PROLOGUE(NCOLS)                    \
-  __shared__ uint64_t bar;                    \
-  __shared__ uint32_t tslot;                  \
-  const int tid = threadIdx.x;                \
-  constexpr uint32_t NCOL = tmem_cols(NCOLS); \
-  if (tid < 32) tc::tmem_alloc(&tslot, NCOL); \
-  if (tid == 0) {                             \
-    tc::mbar_init(&bar, 1);                   \
-    tc::mbar_init_fence();                    \
-  }                                           \
-  tc::tc_before_sync();                       \
-  __syncthreads();                            \
-  tc::tc_after_sync();                        \
-  const uint32_t tmem = tslot;                \
-  Ctx cx{&bar, 0u, true};                     \
-  const uint32_t lb = lane_base();            \
-  const int row = row_of(), wg = wg_of();     \
-  (void)row;                                  \
-  (void)wg;                                   \
-  const long nt = (V + TM - 1) / TM;
+  const long tstep = (long)(NP) * gridDim.x;                                             \
+  const long t0 = (long)(NP) * blockIdx.x + pid;
 
 // ============================================================================================== forward
 // 2-layer MLP C -> 2C -> C with the residual prologue of ffno_mlp2_fwd and GroupNorm partials of the output.
-// Weights: [w1 (2C x C), w2 (C x 2C)]. Per warpgroup: the input tile, then (aliased) the hidden tile.
+// Weights: [w1 (2C x C), w2 (C x 2C)]. Per pipeline: the input tile, then (aliased) the hidden tile.
 template <int C, int MODE>
 __global__ void __launch_bounds__(CT, 1) k_mlp2_tc(const float* __restrict__ in, const float* __restrict__ prev,
-                                                const float* __restrict__ pc, float res, float* __restrict__ xout,
-                                                long V, const uint8_t* __restrict__ wpack,
-                                                const float* __restrict__ dw, float* __restrict__ pre,
-                                                double* __restrict__ partials, int* __restrict__ err) {
+                                                   const float* __restrict__ pc, float res, float* __restrict__ xout,
+                                                   long V, const uint8_t* __restrict__ wpack,
+                                                   const float* __restrict__ dw, float* __restrict__ pre,
+                                                   double* __restrict__ partials, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t B1 = mat_bytes(2 * C, C), B2 = mat_bytes(C, 2 * C), RB = tile_bytes(2 * C);
-  Split w1 = split_at(smem, 2 * C, C), w2 = split_at(smem + B1, C, 2 * C);
-  __shared__ float red[2][(WGT / 32) * (GMAX + 1)], gmean[2][GMAX], wsum[2];
-  __shared__ double xs[3 * GMAX];
-  TC_PROLOGUE_WG(2 * C)
-  uint8_t* region = smem + B1 + B2 + wg * RB;
-  Split A = split_at(region, TM, C), H = split_at(region, TM, 2 * C);
-  GroupAcc acc{0.0, 0.0, 0.0};
-  cx.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
-  for (long t = 2L * blockIdx.x + wg; cx.ok && t < nt; t += tstep) {
+  __shared__ float wt[2][TM], wpart[2][4], red[2][4 * GMAX];
+  __shared__ double acc[2 * GMAX * 3];
+  PIPE_PROLOGUE(TM, 2)
+  uint8_t* region = smem + B1 + B2 + pid * RB;
+  const Split X = split_at(region, TM, C), H = split_at(region, TM, 2 * C);
+  if (tid < 2 * GMAX * 3) acc[tid] = 0.0;
+  P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
+  const Op w1 = wop(smem, 2 * C, C), w2 = wop(smem + B1, C, 2 * C);
+  Gn4 gc{};
+  if (MODE != 0) gc = gn_coefs(pc, C, fill_col<C>(P.ptid));
+  const int f = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (wtid == 0) {
+    if (P.ptid == 0) {
       prefetch_rows(in, (t + tstep) * TM, V, C);
       if (MODE != 0) prefetch_rows(prev, (t + tstep) * TM, V, C);
     }
-    wg_fill_tile<C>(A, v0, V, wtid, [&](long v, int k) {
+    load_tile_weights(P, dw, v0, V, wt[pid], wpart[pid]);
+    fill_tile<C>(X, v0, V, P.ptid, [&](long v, int k) {
       float4 a = ld4(in + v * C + k);
       if (MODE != 0) {
-        const float4 y = gn4<MODE == 1>(ld4(prev + v * C + k), pc, C, k);
-        a.x += res * y.x;
-        a.y += res * y.y;
-        a.z += res * y.z;
-        a.w += res * y.w;
+        const float4 y = gn_apply<MODE == 1>(ld4(prev + v * C + k), gc);
+        a = make_float4(fmaf(res, y.x, a.x), fmaf(res, y.y, a.y), fmaf(res, y.z, a.z), fmaf(res, y.w, a.w));
         *reinterpret_cast<float4*>(xout + v * C + k) = a;
       }
       return a;
     });
-    if (!wg_gemms(cx, err, tmem, op_of(A, C), op_of(w1, C), C, 2 * C)) break;
-#pragma unroll
-    for (int jj = 0; jj < (2 * C) / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+    if (!pipe_gemms(P, err, Gemm{P.tmem, w1, kop(X, C), C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float v[16];
-      tc::tmem_ld16(tmem + lb + c0, v);
+      tld(P, 0, c, v);
 #pragma unroll
       for (int i = 0; i < 16; ++i) v[i] = gelu(v[i]);
-      put16(H, row, c0, 2 * C, v);
+      if (f < 2 * C) put_mn(H, f, 64 * P.half + 16 * c, v);
     }
-    if (!wg_gemms(cx, err, tmem, op_of(H, 2 * C), op_of(w2, 2 * C), 2 * C, C)) break;
-    float o[C];
-#pragma unroll
-    for (int jj = 0; jj < C / 16; ++jj) {
-      if (!owns(jj, half)) continue;
+    if (!pipe_gemms(P, err, Gemm{P.tmem, w2, mop(H), 2 * C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float v[16];
-      tc::tmem_ld16(tmem + lb + 16 * jj, v);
+      tld(P, 0, c, v);
+      const long vb = v0 + 64 * P.half + 16 * c;
+      if (f < C)
 #pragma unroll
-      for (int i = 0; i < 16; ++i) o[16 * jj + i] = v[i];
+        for (int i = 0; i < 16; ++i)
+          if (vb + i < V) pre[(vb + i) * C + f] = v[i];
     }
-    const long v = v0 + row;
-    float w = 0.f;
-    if (v < V) {
-      w = __ldg(dw + v);
-      float4* dst = reinterpret_cast<float4*>(pre + v * C);
-#pragma unroll
-      for (int c = 0; c < C; c += 4)
-        if (owns(c / 16, half)) dst[c / 4] = make_float4(o[c], o[c + 1], o[c + 2], o[c + 3]);
-    }
-    wg_row_group_stats<C>(o, w, red[wg], gmean[wg], &wsum[wg], acc, wg, wtid);
+    tile_stats<C>(P, 0, wt[pid], wpart[pid], red[pid], acc + pid * GMAX * 3);
   }
-  wg_write_partial(partials, acc, xs, wg, wtid);
-  wg_finish(cx, tmem_all, 2 * NCOL);
+  write_partial2(partials, acc);
+  pipe_finish(P, tslot, 2 * NCOL);
 }
 
 // Input gate of one branch: out = x sigmoid(gelu(x G1) G2) [+ zp z]. Weights: [g1 (C x C), g2 (C x C)].
 template <int C>
 __global__ void __launch_bounds__(CT, 1) k_gate_tc(const float* __restrict__ x, long V, const uint8_t* __restrict__ wpack,
-                                                const float* __restrict__ zp, const float* __restrict__ z,
-                                                float* __restrict__ out, int* __restrict__ err) {
+                                                   const float* __restrict__ zp, const float* __restrict__ z,
+                                                   float* __restrict__ out, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t B1 = mat_bytes(C, C), RB = tile_bytes(C);
-  Split g1 = split_at(smem, C, C), g2 = split_at(smem + B1, C, C);
-  TC_PROLOGUE_WG(C)
-  Split A = split_at(smem + 2 * B1 + wg * RB, TM, C);
-  cx.ok = load_weights(smem, wpack, 2 * B1, wcx, err);
-  for (long t = 2L * blockIdx.x + wg; cx.ok && t < nt; t += tstep) {
+  PIPE_PROLOGUE(TM, 2)
+  const Split X = split_at(smem + 2 * B1 + pid * RB, TM, C);
+  P.ok = load_weights(smem, wpack, 2 * B1, wcx, err);
+  const Op g1 = wop(smem, C, C), g2 = wop(smem + B1, C, C);
+  const int f = P.feat();
+  const float zf = (zp && f < C) ? __ldg(zp + f) : 0.f;
+  for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (wtid == 0) prefetch_rows(x, (t + tstep) * TM, V, C);
-    wg_fill_tile<C>(A, v0, V, wtid, [&](long v, int k) { return ld4(x + v * C + k); });
-    if (!wg_gemms(cx, err, tmem, op_of(A, C), op_of(g1, C), C, C)) break;
-#pragma unroll
-    for (int jj = 0; jj < C / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+    if (P.ptid == 0) prefetch_rows(x, (t + tstep) * TM, V, C);
+    fill_tile<C>(X, v0, V, P.ptid, [&](long v, int k) { return ld4(x + v * C + k); });
+    if (!pipe_gemms(P, err, Gemm{P.tmem, g1, kop(X, C), C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float v[16];
-      tc::tmem_ld16(tmem + lb + c0, v);
+      tld(P, 0, c, v);
 #pragma unroll
       for (int i = 0; i < 16; ++i) v[i] = gelu(v[i]);
-      put16(A, row, c0, C, v);
+      if (f < C) put_mn(X, f, 64 * P.half + 16 * c, v);
     }
-    if (!wg_gemms(cx, err, tmem, op_of(A, C), op_of(g2, C), C, C)) break;
-    const long v = v0 + row;
-    const float zv = (zp && v < V) ? __ldg(z + v) : 0.f;
-#pragma unroll
-    for (int jj = 0; jj < C / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+    if (!pipe_gemms(P, err, Gemm{P.tmem, g2, mop(X), C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float g[16];
-      tc::tmem_ld16(tmem + lb + c0, g);
-      if (v < V) {
+      tld(P, 0, c, g);
+      const long vb = v0 + 64 * P.half + 16 * c;
+      if (f < C)
 #pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          const float4 xv = ld4(x + v * C + c0 + i);
-          float4 o = make_float4(xv.x * sigmoid(g[i]), xv.y * sigmoid(g[i + 1]), xv.z * sigmoid(g[i + 2]),
-                                 xv.w * sigmoid(g[i + 3]));
-          if (zp) {
-            o.x += __ldg(zp + c0 + i) * zv;
-            o.y += __ldg(zp + c0 + i + 1) * zv;
-            o.z += __ldg(zp + c0 + i + 2) * zv;
-            o.w += __ldg(zp + c0 + i + 3) * zv;
+        for (int i = 0; i < 16; ++i) {
+          const long v = vb + i;
+          if (v < V) {
+            float o = __ldg(x + v * C + f) * sigmoid(g[i]);
+            if (zp) o = fmaf(zf, __ldg(z + v), o);
+            out[v * C + f] = o;
           }
-          *reinterpret_cast<float4*>(out + v * C + c0 + i) = o;
         }
-      }
     }
   }
-  wg_finish(cx, tmem_all, 2 * NCOL);
+  pipe_finish(P, tslot, 2 * NCOL);
 }
 
 // Branch gates (first half of _fuse_branches): gates = sigmoid(gelu([x, spec, vert] Wg1) Wg2 + b), spec =
 // gelu(GN(spec_pre)) etc.; optionally the hidden pre-activation [x, spec, vert] Wg1 to hg. Weights: [wg1 (C x 3C),
-// wg2 (2C x C)]. The first GEMM runs over three K-slices of C columns (x, spec, vert) through one tile per warpgroup.
+// wg2 (2C x C)]. The first GEMM runs over three K-slices of C columns (x, spec, vert) through one tile per pipeline.
 template <int C>
 __global__ void __launch_bounds__(CT, 1) k_fuse1_tc(const float* __restrict__ x, const float* __restrict__ sp,
-                                                 const float* __restrict__ sc, const float* __restrict__ vp,
-                                                 const float* __restrict__ vc, long V,
-                                                 const uint8_t* __restrict__ wpack, const float* __restrict__ bias,
-                                                 float* __restrict__ gates, float* __restrict__ hg,
-                                                 int* __restrict__ err) {
+                                                    const float* __restrict__ sc, const float* __restrict__ vp,
+                                                    const float* __restrict__ vc, long V,
+                                                    const uint8_t* __restrict__ wpack, const float* __restrict__ bias,
+                                                    float* __restrict__ gates, float* __restrict__ hg,
+                                                    int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t B1 = mat_bytes(C, 3 * C), B2 = mat_bytes(2 * C, C), RB = tile_bytes(C);
-  Split wg1 = split_at(smem, C, 3 * C), wg2 = split_at(smem + B1, 2 * C, C);
-  TC_PROLOGUE_WG(2 * C)
-  Split A = split_at(smem + B1 + B2 + wg * RB, TM, C);
-  cx.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
-  for (long t = 2L * blockIdx.x + wg; cx.ok && t < nt; t += tstep) {
+  PIPE_PROLOGUE(TM, 2)
+  const Split A = split_at(smem + B1 + B2 + pid * RB, TM, C);
+  P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
+  const Op wg2 = wop(smem + B1, 2 * C, C);
+  const int kf = fill_col<C>(P.ptid);
+  const Gn4 gs = gn_coefs(sc, C, kf), gv = gn_coefs(vc, C, kf);
+  const int f = P.feat();
+  const float bf = f < 2 * C ? __ldg(bias + f) : 0.f;
+  for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (wtid == 0) {
+    if (P.ptid == 0) {
       prefetch_rows(x, (t + tstep) * TM, V, C);
       prefetch_rows(sp, (t + tstep) * TM, V, C);
       prefetch_rows(vp, (t + tstep) * TM, V, C);
     }
     for (int kc = 0; kc < 3; ++kc) {
-      wg_fill_tile<C>(A, v0, V, wtid, [&](long v, int k) {
-        if (kc == 0) return ld4(x + v * C + k);
-        if (kc == 1) return gn4<true>(ld4(sp + v * C + k), sc, C, k);
-        return gn4<true>(ld4(vp + v * C + k), vc, C, k);
-      });
-      if (!wg_gemms(cx, err, tmem, op_of(A, C), op_kslice(wg1, 3 * C, kc * C), C, C, kc > 0)) break;
+      if (kc == 0)
+        fill_tile<C>(A, v0, V, P.ptid, [&](long v, int k) { return ld4(x + v * C + k); });
+      else if (kc == 1)
+        fill_tile<C>(A, v0, V, P.ptid, [&](long v, int k) { return gn_apply<true>(ld4(sp + v * C + k), gs); });
+      else
+        fill_tile<C>(A, v0, V, P.ptid, [&](long v, int k) { return gn_apply<true>(ld4(vp + v * C + k), gv); });
+      if (!pipe_gemms(P, err, Gemm{P.tmem, wop(smem, C, 3 * C, 0, kc * C), kop(A, C), C, kc > 0})) break;
     }
-    if (!cx.ok) break;
-    const long v = v0 + row;
-#pragma unroll
-    for (int jj = 0; jj < C / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+    if (!P.ok) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float h[16];
-      tc::tmem_ld16(tmem + lb + c0, h);
-      if (hg && v < V)
+      tld(P, 0, c, h);
+      const long vb = v0 + 64 * P.half + 16 * c;
+      if (hg && f < C)
 #pragma unroll
-        for (int i = 0; i < 16; i += 4)
-          *reinterpret_cast<float4*>(hg + v * C + c0 + i) = make_float4(h[i], h[i + 1], h[i + 2], h[i + 3]);
+        for (int i = 0; i < 16; ++i)
+          if (vb + i < V) hg[(vb + i) * C + f] = h[i];
 #pragma unroll
       for (int i = 0; i < 16; ++i) h[i] = gelu(h[i]);
-      put16(A, row, c0, C, h);
+      if (f < C) put_mn(A, f, 64 * P.half + 16 * c, h);
     }
-    if (!wg_gemms(cx, err, tmem, op_of(A, C), op_of(wg2, C), C, 2 * C)) break;
-#pragma unroll
-    for (int jj = 0; jj < (2 * C) / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+    if (!pipe_gemms(P, err, Gemm{P.tmem, wg2, mop(A), C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float g[16];
-      tc::tmem_ld16(tmem + lb + c0, g);
-      if (v < V)
+      tld(P, 0, c, g);
+      const long vb = v0 + 64 * P.half + 16 * c;
+      if (f < 2 * C)
 #pragma unroll
-        for (int i = 0; i < 16; i += 4)
-          *reinterpret_cast<float4*>(gates + v * 2 * C + c0 + i) =
-              make_float4(sigmoid(g[i] + __ldg(bias + c0 + i)), sigmoid(g[i + 1] + __ldg(bias + c0 + i + 1)),
-                          sigmoid(g[i + 2] + __ldg(bias + c0 + i + 2)), sigmoid(g[i + 3] + __ldg(bias + c0 + i + 3)));
+        for (int i = 0; i < 16; ++i)
+          if (vb + i < V) gates[(vb + i) * 2 * C + f] = sigmoid(g[i] + bf);
     }
   }
-  wg_finish(cx, tmem_all, 2 * NCOL);
+  pipe_finish(P, tslot, 2 * NCOL);
 }
 
 // Fuse (second half of _fuse_branches): B = [spec gs, vert gv], pre = gelu(B Wf1) Wf2 + (spec gs + vert gv) / 2, with
 // the GroupNorm partials of pre. Weights: [wf1 (2C x 2C), wf2 (C x 2C)].
 template <int C>
 __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp, const float* __restrict__ sc,
-                                                 const float* __restrict__ vp, const float* __restrict__ vc,
-                                                 const float* __restrict__ gates, long V,
-                                                 const uint8_t* __restrict__ wpack, const float* __restrict__ dw,
-                                                 float* __restrict__ pre, double* __restrict__ partials,
-                                                 int* __restrict__ err) {
+                                                    const float* __restrict__ vp, const float* __restrict__ vc,
+                                                    const float* __restrict__ gates, long V,
+                                                    const uint8_t* __restrict__ wpack, const float* __restrict__ dw,
+                                                    float* __restrict__ pre, double* __restrict__ partials,
+                                                    int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t B1 = mat_bytes(2 * C, 2 * C), B2 = mat_bytes(C, 2 * C), RB = tile_bytes(2 * C);
-  Split wf1 = split_at(smem, 2 * C, 2 * C), wf2 = split_at(smem + B1, C, 2 * C);
-  __shared__ float red[2][(WGT / 32) * (GMAX + 1)], gmean[2][GMAX], wsum[2];
-  __shared__ double xs[3 * GMAX];
-  TC_PROLOGUE_WG(2 * C)
-  Split A = split_at(smem + B1 + B2 + wg * RB, TM, 2 * C);
-  GroupAcc acc{0.0, 0.0, 0.0};
-  cx.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
-  auto mixed = [&](long v, int k) {  // columns k..k+3 of B
-    const float4 g = ld4(gates + v * 2 * C + k);
-    const float4 s = (k < C) ? gn4<true>(ld4(sp + v * C + k), sc, C, k) : gn4<true>(ld4(vp + v * C + k - C), vc, C, k - C);
-    return make_float4(s.x * g.x, s.y * g.y, s.z * g.z, s.w * g.w);
-  };
-  for (long t = 2L * blockIdx.x + wg; cx.ok && t < nt; t += tstep) {
+  __shared__ float wt[2][TM], wpart[2][4], red[2][4 * GMAX];
+  __shared__ double acc[2 * GMAX * 3];
+  PIPE_PROLOGUE(TM, 2)
+  const Split A = split_at(smem + B1 + B2 + pid * RB, TM, 2 * C);
+  if (tid < 2 * GMAX * 3) acc[tid] = 0.0;
+  P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
+  const Op wf1 = wop(smem, 2 * C, 2 * C), wf2 = wop(smem + B1, C, 2 * C);
+  const int kf = fill_col<2 * C>(P.ptid);
+  const Gn4 gk = kf < C ? gn_coefs(sc, C, kf) : gn_coefs(vc, C, kf - C);
+  const float* src = kf < C ? sp : vp;
+  const int ks = kf < C ? kf : kf - C;
+  const int f = P.feat();
+  const int fc = f < C ? f : 0;   // this thread's output channel (epilogue) and its GroupNorm coefficients
+  const float sm = __ldg(sc + fc), ss = __ldg(sc + C + fc), sb = __ldg(sc + 2 * C + fc);
+  const float vm = __ldg(vc + fc), vs = __ldg(vc + C + fc), vbb = __ldg(vc + 2 * C + fc);
+  for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (wtid == 0) {
+    if (P.ptid == 0) {
       prefetch_rows(sp, (t + tstep) * TM, V, C);
       prefetch_rows(vp, (t + tstep) * TM, V, C);
       prefetch_rows(gates, (t + tstep) * TM, V, 2 * C);
     }
-    wg_fill_tile<2 * C>(A, v0, V, wtid, mixed);
-    if (!wg_gemms(cx, err, tmem, op_of(A, 2 * C), op_of(wf1, 2 * C), 2 * C, 2 * C)) break;
-#pragma unroll
-    for (int jj = 0; jj < (2 * C) / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+    load_tile_weights(P, dw, v0, V, wt[pid], wpart[pid]);
+    fill_tile<2 * C>(A, v0, V, P.ptid, [&](long v, int k) {
+      const float4 g = ld4(gates + v * 2 * C + k);
+      const float4 s = gn_apply<true>(ld4(src + v * C + ks), gk);
+      return make_float4(s.x * g.x, s.y * g.y, s.z * g.z, s.w * g.w);
+    });
+    if (!pipe_gemms(P, err, Gemm{P.tmem, wf1, kop(A, 2 * C), 2 * C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float h[16];
-      tc::tmem_ld16(tmem + lb + c0, h);
+      tld(P, 0, c, h);
 #pragma unroll
       for (int i = 0; i < 16; ++i) h[i] = gelu(h[i]);
-      put16(A, row, c0, 2 * C, h);
+      if (f < 2 * C) put_mn(A, f, 64 * P.half + 16 * c, h);
     }
-    if (!wg_gemms(cx, err, tmem, op_of(A, 2 * C), op_of(wf2, 2 * C), 2 * C, C)) break;
-    const long v = v0 + row;
-    float o[C];
+    if (!pipe_gemms(P, err, Gemm{P.tmem, wf2, mop(A), 2 * C, false})) break;
+    // pre = gelu(B Wf1) Wf2 + (spec gs + vert gv) / 2, written to HBM and back to tensor memory for the statistics
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+      float o[16];
+      tld(P, 0, c, o);
+      const long vb = v0 + 64 * P.half + 16 * c;
+      if (f < C)
 #pragma unroll
-    for (int jj = 0; jj < C / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      float f[16];
-      tc::tmem_ld16(tmem + lb + 16 * jj, f);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) o[16 * jj + i] = f[i];
+        for (int i = 0; i < 16; ++i) {
+          const long v = vb + i;
+          if (v < V) {
+            const float s = gelu((__ldg(sp + v * C + f) - sm) * ss + sb) * __ldg(gates + v * 2 * C + f);
+            const float u = gelu((__ldg(vp + v * C + f) - vm) * vs + vbb) * __ldg(gates + v * 2 * C + C + f);
+            o[i] += 0.5f * (s + u);
+            pre[v * C + f] = o[i];
+          }
+        }
+      tc::tmem_st16(P.tmem + P.lq + (uint32_t)(64 * P.half + 16 * c), o);
     }
-    float w = 0.f;
-    if (v < V) {
-      w = __ldg(dw + v);
-#pragma unroll
-      for (int c = 0; c < C; c += 4) {
-        if (!owns(c / 16, half)) continue;
-        const float4 a = mixed(v, c), b = mixed(v, C + c);
-        o[c] += 0.5f * (a.x + b.x);
-        o[c + 1] += 0.5f * (a.y + b.y);
-        o[c + 2] += 0.5f * (a.z + b.z);
-        o[c + 3] += 0.5f * (a.w + b.w);
-        *reinterpret_cast<float4*>(pre + v * C + c) = make_float4(o[c], o[c + 1], o[c + 2], o[c + 3]);
-      }
-    }
-    wg_row_group_stats<C>(o, w, red[wg], gmean[wg], &wsum[wg], acc, wg, wtid);
+    tc::tc_before_sync();
+    pipe_sync(P.id);
+    tc::tc_after_sync();
+    tile_stats<C>(P, 0, wt[pid], wpart[pid], red[pid], acc + pid * GMAX * 3);
   }
-  wg_write_partial(partials, acc, xs, wg, wtid);
-  wg_finish(cx, tmem_all, 2 * NCOL);
+  write_partial2(partials, acc);
+  pipe_finish(P, tslot, 2 * NCOL);
 }
 
 // ============================================================================================== backward
 // a_bar = base + ((pre_bar W2^T) * gelu'(a W1)) W1^T. Weights: [w1 (2C x C), w2t (2C x C), w1t (C x 2C)].
-// Per warpgroup: the tiles of a and pre_bar, then (aliased) the hidden tile.
+// Per pipeline: the tiles of a and pre_bar, then (aliased) the hidden tile.
 template <int C>
 __global__ void __launch_bounds__(CT, 1) k_mlp2_bwd_tc(const float* __restrict__ a, const float* __restrict__ pb,
-                                                    const float* __restrict__ base, long V,
-                                                    const uint8_t* __restrict__ wpack, float* __restrict__ abar,
-                                                    int* __restrict__ err) {
+                                                       const float* __restrict__ base, long V,
+                                                       const uint8_t* __restrict__ wpack, float* __restrict__ abar,
+                                                       int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t B1 = mat_bytes(2 * C, C), RB = tile_bytes(2 * C);
-  Split w1 = split_at(smem, 2 * C, C), w2t = split_at(smem + B1, 2 * C, C), w1t = split_at(smem + 2 * B1, C, 2 * C);
-  TC_PROLOGUE_WG(4 * C)
-  uint8_t* region = smem + 3 * B1 + wg * RB;
-  Split A = split_at(region, TM, C), P = split_at(region + tile_bytes(C), TM, C), H = split_at(region, TM, 2 * C);
-  cx.ok = load_weights(smem, wpack, 3 * B1, wcx, err);
-  for (long t = 2L * blockIdx.x + wg; cx.ok && t < nt; t += tstep) {
+  PIPE_PROLOGUE(2 * TM, 2)
+  uint8_t* region = smem + 3 * B1 + pid * RB;
+  const Split A = split_at(region, TM, C), Pt = split_at(region + tile_bytes(C), TM, C),
+              H = split_at(region, TM, 2 * C);
+  P.ok = load_weights(smem, wpack, 3 * B1, wcx, err);
+  const Op w1 = wop(smem, 2 * C, C), w2t = wop(smem + B1, 2 * C, C), w1t = wop(smem + 2 * B1, C, 2 * C);
+  const int f = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (wtid == 0) {
+    if (P.ptid == 0) {
       prefetch_rows(a, (t + tstep) * TM, V, C);
       prefetch_rows(pb, (t + tstep) * TM, V, C);
       prefetch_rows(base, (t + tstep) * TM, V, C);
     }
-    wg_fill_tile<C>(A, v0, V, wtid, [&](long v, int k) { return ld4(a + v * C + k); });
-    wg_fill_tile<C>(P, v0, V, wtid, [&](long v, int k) { return ld4(pb + v * C + k); });
-    if (!wg_gemms(cx, err, tmem, op_of(A, C), op_of(w1, C), C, 2 * C, false, tmem + 2 * C, op_of(P, C), op_of(w2t, C),
-                  C, 2 * C))
-      break;
-#pragma unroll
-    for (int jj = 0; jj < (2 * C) / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+    fill_tile<C>(A, v0, V, P.ptid, [&](long v, int k) { return ld4(a + v * C + k); });
+    fill_tile<C>(Pt, v0, V, P.ptid, [&](long v, int k) { return ld4(pb + v * C + k); });
+    const Gemm g2{P.tmem + TM, w2t, kop(Pt, C), C, false};
+    if (!pipe_gemms(P, err, Gemm{P.tmem, w1, kop(A, C), C, false}, &g2)) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float hp[16], gb[16];
-      tc::tmem_ld16(tmem + lb + c0, hp);
-      tc::tmem_ld16(tmem + lb + 2 * C + c0, gb);
+      tld(P, 0, c, hp);
+      tld(P, TM, c, gb);
 #pragma unroll
       for (int i = 0; i < 16; ++i) gb[i] *= gelu_grad(hp[i]);
-      put16(H, row, c0, 2 * C, gb);
+      if (f < 2 * C) put_mn(H, f, 64 * P.half + 16 * c, gb);
     }
-    if (!wg_gemms(cx, err, tmem, op_of(H, 2 * C), op_of(w1t, 2 * C), 2 * C, C)) break;
-    const long v = v0 + row;
-#pragma unroll
-    for (int jj = 0; jj < C / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+    if (!pipe_gemms(P, err, Gemm{P.tmem, w1t, mop(H), 2 * C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float r[16];
-      tc::tmem_ld16(tmem + lb + c0, r);
-      if (v < V)
+      tld(P, 0, c, r);
+      const long vb = v0 + 64 * P.half + 16 * c;
+      if (f < C)
 #pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          float4 o = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
-          if (base) {
-            const float4 b = ld4(base + v * C + c0 + i);
-            o.x += b.x;
-            o.y += b.y;
-            o.z += b.z;
-            o.w += b.w;
-          }
-          *reinterpret_cast<float4*>(abar + v * C + c0 + i) = o;
+        for (int i = 0; i < 16; ++i) {
+          const long v = vb + i;
+          if (v < V) abar[v * C + f] = base ? r[i] + __ldg(base + v * C + f) : r[i];
         }
     }
   }
-  wg_finish(cx, tmem_all, 2 * NCOL);
+  pipe_finish(P, tslot, 2 * NCOL);
+}
+
+// Sums of 16 per-voxel values over the 32 lanes of a warp: afterwards lanes 2i and 2i + 1 hold the sum for voxel
+// vox_of(lane) (a fixed butterfly, deterministic).
+__device__ __forceinline__ float warp_sum16(float (&v)[16], int lane) {
+#pragma unroll
+  for (int m = 16, n = 8; m >= 2; m >>= 1, n >>= 1) {
+    const bool up = (lane & m) != 0;
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+      const float send = up ? v[i] : v[i + n];
+      const float keep = up ? v[i + n] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, m);
+    }
+  }
+  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+__device__ __forceinline__ int vox_of(int lane) {
+  return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
 }
 
 // One input gate's backward: x_bar = base + d/dx [x sigmoid(gelu(x G1) G2)] applied to gbar; with zp, z_bar[v] +=
-// sum_c gbar zp. Weights: [g1, g2, g2t, g1t] (each C x C).
+// sum_c gbar zp. Weights: [g1, g2, g2t, g1t] (each C x C). One tile region per pipeline, reused by the input tile
+// and the three MN-major intermediates.
 template <int C>
 __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__ x, const float* __restrict__ gbar,
-                                                    const float* __restrict__ base, long V,
-                                                    const uint8_t* __restrict__ wpack, const float* __restrict__ zp,
-                                                    float* __restrict__ xbar, float* __restrict__ zbar,
-                                                    int* __restrict__ err) {
+                                                       const float* __restrict__ base, long V,
+                                                       const uint8_t* __restrict__ wpack, const float* __restrict__ zp,
+                                                       float* __restrict__ xbar, float* __restrict__ zbar,
+                                                       int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  constexpr uint32_t B1 = mat_bytes(C, C), RB = 2 * tile_bytes(C);
-  Split g1 = split_at(smem, C, C), g2 = split_at(smem + B1, C, C), g2t = split_at(smem + 2 * B1, C, C),
-        g1t = split_at(smem + 3 * B1, C, C);
-  TC_PROLOGUE_WG(4 * C)
-  Split X = split_at(smem + 4 * B1 + wg * RB, TM, C), T = split_at(smem + 4 * B1 + wg * RB + tile_bytes(C), TM, C);
-  __shared__ float zsh[2][TM];
-  const uint32_t D1 = tmem, D2 = tmem + C, D3 = tmem + 2 * C, D4 = tmem + 3 * C;
-  cx.ok = load_weights(smem, wpack, 4 * B1, wcx, err);
-  for (long t = 2L * blockIdx.x + wg; cx.ok && t < nt; t += tstep) {
+  constexpr uint32_t B1 = mat_bytes(C, C), RB = tile_bytes(C);
+  constexpr int NQ = (C + 31) / 32;   // warps of a half holding live channels
+  __shared__ float zq[2][2][NQ][64];  // [pipeline][half][warp][voxel of the half]
+  PIPE_PROLOGUE(2 * TM, 2)
+  const Split T = split_at(smem + 4 * B1 + pid * RB, TM, C);
+  P.ok = load_weights(smem, wpack, 4 * B1, wcx, err);
+  const Op g1 = wop(smem, C, C), g2 = wop(smem + B1, C, C), g2t = wop(smem + 2 * B1, C, C),
+           g1t = wop(smem + 3 * B1, C, C);
+  const int f = P.feat();
+  const float zf = (zp && f < C) ? __ldg(zp + f) : 0.f;
+  const uint32_t D1 = 0, D2 = TM;
+  for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (wtid == 0) {
+    if (P.ptid == 0) {
       prefetch_rows(x, (t + tstep) * TM, V, C);
       prefetch_rows(gbar, (t + tstep) * TM, V, C);
       prefetch_rows(base, (t + tstep) * TM, V, C);
     }
-    const long v = v0 + row;
-    wg_fill_tile<C>(X, v0, V, wtid, [&](long vv, int k) { return ld4(x + vv * C + k); });
-    if (!wg_gemms(cx, err, D1, op_of(X, C), op_of(g1, C), C, C)) break;
-#pragma unroll
-    for (int jj = 0; jj < C / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+    fill_tile<C>(T, v0, V, P.ptid, [&](long vv, int k) { return ld4(x + vv * C + k); });
+    if (!pipe_gemms(P, err, Gemm{P.tmem + D1, g1, kop(T, C), C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float h[16];
-      tc::tmem_ld16(D1 + lb + c0, h);
+      tld(P, D1, c, h);
 #pragma unroll
       for (int i = 0; i < 16; ++i) h[i] = gelu(h[i]);
-      put16(T, row, c0, C, h);
+      if (f < C) put_mn(T, f, 64 * P.half + 16 * c, h);
     }
-    if (!wg_gemms(cx, err, D2, op_of(T, C), op_of(g2, C), C, C)) break;
-    float zs = 0.f;
+    if (!pipe_gemms(P, err, Gemm{P.tmem + D2, g2, mop(T), C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+      float g[16], q[16], zs[16];
+      tld(P, D2, c, g);
+      const long vb = v0 + 64 * P.half + 16 * c;
 #pragma unroll
-    for (int jj = 0; jj < C / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
-      float g[16], q[16];
-      tc::tmem_ld16(D2 + lb + c0, g);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) q[i] = 0.f;
-      if (v < V) {
-#pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          const float4 b = ld4(gbar + v * C + c0 + i), xv = ld4(x + v * C + c0 + i);
-          const float bb[4] = {b.x, b.y, b.z, b.w}, xx[4] = {xv.x, xv.y, xv.z, xv.w};
-          float o[4];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const float s = sigmoid(g[i + j]);
-            o[j] = bb[j] * s;
-            q[i + j] = bb[j] * xx[j] * s * (1.f - s);
-            if (zp) zs += bb[j] * __ldg(zp + c0 + i + j);
-          }
-          float4 r = make_float4(o[0], o[1], o[2], o[3]);
-          if (base) {
-            const float4 bs = ld4(base + v * C + c0 + i);
-            r.x += bs.x;
-            r.y += bs.y;
-            r.z += bs.z;
-            r.w += bs.w;
-          }
-          *reinterpret_cast<float4*>(xbar + v * C + c0 + i) = r;
+      for (int i = 0; i < 16; ++i) {
+        const long v = vb + i;
+        q[i] = 0.f;
+        zs[i] = 0.f;
+        if (f < C && v < V) {
+          const float b = __ldg(gbar + v * C + f), xv = __ldg(x + v * C + f);
+          const float s = sigmoid(g[i]);
+          xbar[v * C + f] = base ? fmaf(b, s, __ldg(base + v * C + f)) : b * s;
+          q[i] = b * xv * s * (1.f - s);
+          zs[i] = b * zf;
         }
       }
-      put16(T, row, c0, C, q);
+      if (f < C) put_mn(T, f, 64 * P.half + 16 * c, q);
+      if (zp && P.q < NQ) {
+        const float sum = warp_sum16(zs, P.lane);
+        if ((P.lane & 1) == 0) zq[pid][P.half][P.q][16 * c + vox_of(P.lane)] = sum;
+      }
     }
-    if (SPL > 1) {   // the two halves of the row add their parts of z_bar in a fixed order
-      if (half == 1) zsh[wg][row] = zs;
-      wg_sync(wg);
-      if (half == 0) zs += zsh[wg][row];
-    }
-    if (zp && half == 0 && v < V) zbar[v] += zs;
-    if (!wg_gemms(cx, err, D3, op_of(T, C), op_of(g2t, C), C, C)) break;
+    if (zp) {   // z_bar: the warps' partial sums per voxel, added in a fixed order
+      pipe_sync(P.id);
+      if (P.ptid < TM) {
+        const int hh = P.ptid >> 6, vl = P.ptid & 63;
+        const long v = v0 + P.ptid;
+        float s = 0.f;
 #pragma unroll
-    for (int jj = 0; jj < C / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+        for (int w = 0; w < NQ; ++w) s += zq[pid][hh][w][vl];
+        if (v < V) zbar[v] += s;
+      }
+    }
+    if (!pipe_gemms(P, err, Gemm{P.tmem + D2, g2t, mop(T), C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float hb[16], hp[16];
-      tc::tmem_ld16(D3 + lb + c0, hb);
-      tc::tmem_ld16(D1 + lb + c0, hp);
+      tld(P, D2, c, hb);
+      tld(P, D1, c, hp);
 #pragma unroll
       for (int i = 0; i < 16; ++i) hb[i] *= gelu_grad(hp[i]);
-      put16(T, row, c0, C, hb);
+      if (f < C) put_mn(T, f, 64 * P.half + 16 * c, hb);
     }
-    if (!wg_gemms(cx, err, D4, op_of(T, C), op_of(g1t, C), C, C)) break;
-#pragma unroll
-    for (int jj = 0; jj < C / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+    if (!pipe_gemms(P, err, Gemm{P.tmem + D2, g1t, mop(T), C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float r[16];
-      tc::tmem_ld16(D4 + lb + c0, r);
-      if (v < V)
+      tld(P, D2, c, r);
+      const long vb = v0 + 64 * P.half + 16 * c;
+      if (f < C)
 #pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          float4* p = reinterpret_cast<float4*>(xbar + v * C + c0 + i);
-          float4 o = *p;
-          o.x += r[i];
-          o.y += r[i + 1];
-          o.z += r[i + 2];
-          o.w += r[i + 3];
-          *p = o;
-        }
+        for (int i = 0; i < 16; ++i)
+          if (vb + i < V) xbar[(vb + i) * C + f] += r[i];
     }
   }
-  wg_finish(cx, tmem_all, 2 * NCOL);
+  pipe_finish(P, tslot, 2 * NCOL);
 }
 
 // Fuse backward, stage a: hf_bar_pre = (F_bar Wf2^T) * gelu'(B Wf1) with B = [spec gs, vert gv], F_bar =
-// fused_pre_bar. Weights: [wf1 (2C x 2C), wf2t (2C x C)]. Per warpgroup one tile: B, then (after its GEMM) F_bar.
+// fused_pre_bar. Weights: [wf1 (2C x 2C), wf2t (2C x C)]. Per pipeline one tile: B, then (after its GEMM) F_bar.
 template <int C>
 __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_a_tc(const float* __restrict__ sp, const float* __restrict__ sc,
-                                                      const float* __restrict__ vp, const float* __restrict__ vc,
-                                                      const float* __restrict__ gates, const float* __restrict__ fb,
-                                                      long V, const uint8_t* __restrict__ wpack,
-                                                      float* __restrict__ hfb, int* __restrict__ err) {
+                                                         const float* __restrict__ vp, const float* __restrict__ vc,
+                                                         const float* __restrict__ gates, const float* __restrict__ fb,
+                                                         long V, const uint8_t* __restrict__ wpack,
+                                                         float* __restrict__ hfb, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t B1 = mat_bytes(2 * C, 2 * C), B2 = mat_bytes(2 * C, C), RB = tile_bytes(2 * C);
-  Split wf1 = split_at(smem, 2 * C, 2 * C), wf2t = split_at(smem + B1, 2 * C, C);
-  TC_PROLOGUE_WG(4 * C)
-  Split Bt = split_at(smem + B1 + B2 + wg * RB, TM, 2 * C), Ft = split_at(smem + B1 + B2 + wg * RB, TM, C);
-  cx.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
-  for (long t = 2L * blockIdx.x + wg; cx.ok && t < nt; t += tstep) {
+  PIPE_PROLOGUE(2 * TM, 2)
+  const Split Bt = split_at(smem + B1 + B2 + pid * RB, TM, 2 * C), Ft = split_at(smem + B1 + B2 + pid * RB, TM, C);
+  P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
+  const Op wf1 = wop(smem, 2 * C, 2 * C), wf2t = wop(smem + B1, 2 * C, C);
+  const int kf = fill_col<2 * C>(P.ptid);
+  const Gn4 gk = kf < C ? gn_coefs(sc, C, kf) : gn_coefs(vc, C, kf - C);
+  const float* src = kf < C ? sp : vp;
+  const int ks = kf < C ? kf : kf - C;
+  const int f = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (wtid == 0) {
+    if (P.ptid == 0) {
       prefetch_rows(sp, (t + tstep) * TM, V, C);
       prefetch_rows(vp, (t + tstep) * TM, V, C);
       prefetch_rows(gates, (t + tstep) * TM, V, 2 * C);
       prefetch_rows(fb, (t + tstep) * TM, V, C);
     }
-    wg_fill_tile<2 * C>(Bt, v0, V, wtid, [&](long v, int k) {
+    fill_tile<2 * C>(Bt, v0, V, P.ptid, [&](long v, int k) {
       const float4 g = ld4(gates + v * 2 * C + k);
-      const float4 s =
-          (k < C) ? gn4<true>(ld4(sp + v * C + k), sc, C, k) : gn4<true>(ld4(vp + v * C + k - C), vc, C, k - C);
+      const float4 s = gn_apply<true>(ld4(src + v * C + ks), gk);
       return make_float4(s.x * g.x, s.y * g.y, s.z * g.z, s.w * g.w);
     });
-    if (!wg_gemms(cx, err, tmem, op_of(Bt, 2 * C), op_of(wf1, 2 * C), 2 * C, 2 * C)) break;
-    wg_fill_tile<C>(Ft, v0, V, wtid, [&](long v, int k) { return ld4(fb + v * C + k); });
-    if (!wg_gemms(cx, err, tmem + 2 * C, op_of(Ft, C), op_of(wf2t, C), C, 2 * C)) break;
-    const long v = v0 + row;
-#pragma unroll
-    for (int jj = 0; jj < (2 * C) / 16; ++jj) {
-      if (!owns(jj, half)) continue;
-      const int c0 = 16 * jj;
+    if (!pipe_gemms(P, err, Gemm{P.tmem, wf1, kop(Bt, 2 * C), 2 * C, false})) break;
+    fill_tile<C>(Ft, v0, V, P.ptid, [&](long v, int k) { return ld4(fb + v * C + k); });
+    if (!pipe_gemms(P, err, Gemm{P.tmem + TM, wf2t, kop(Ft, C), C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float hp[16], hb[16];
-      tc::tmem_ld16(tmem + lb + c0, hp);
-      tc::tmem_ld16(tmem + lb + 2 * C + c0, hb);
-      if (v < V)
+      tld(P, 0, c, hp);
+      tld(P, TM, c, hb);
+      const long vb = v0 + 64 * P.half + 16 * c;
+      if (f < 2 * C)
 #pragma unroll
-        for (int i = 0; i < 16; i += 4)
-          *reinterpret_cast<float4*>(hfb + v * 2 * C + c0 + i) =
-              make_float4(hb[i] * gelu_grad(hp[i]), hb[i + 1] * gelu_grad(hp[i + 1]), hb[i + 2] * gelu_grad(hp[i + 2]),
-                          hb[i + 3] * gelu_grad(hp[i + 3]));
+        for (int i = 0; i < 16; ++i)
+          if (vb + i < V) hfb[(vb + i) * 2 * C + f] = hb[i] * gelu_grad(hp[i]);
     }
   }
-  wg_finish(cx, tmem_all, 2 * NCOL);
+  pipe_finish(P, tslot, 2 * NCOL);
 }
 
 // Fuse backward, stage b: B_bar = hfb Wf1^T + [F_bar, F_bar] / 2; spec/vert grads B_bar g (+ the gate path);
 // gate pre-activation grad q = B_bar [spec, vert] g (1 - g); hg_bar = (q Wg2^T) * gelu'(hg); A_bar = hg_bar Wg1^T:
 // x_bar = base + A_bar[:C], spec_bar = B_bar_s g_s + A_bar[C:2C], vert_bar likewise.
-// Weights: [wf1t (2C x 2C), wg2t (C x 2C), wg1t (3C x C)].
+// Weights: [wf1t (2C x 2C), wg2t (C x 2C), wg1t (3C x C)]. One pipeline per CTA (the weights leave room for one tile).
 template <int C>
-__global__ void __launch_bounds__(TT) k_fuse_bwd_b_tc(const float* __restrict__ sp, const float* __restrict__ sc,
-                                                      const float* __restrict__ vp, const float* __restrict__ vc,
-                                                      const float* __restrict__ gates, const float* __restrict__ hg,
-                                                      const float* __restrict__ fb, const float* __restrict__ hfb,
-                                                      const float* __restrict__ base, long V,
-                                                      const uint8_t* __restrict__ wpack, float* __restrict__ xbar,
-                                                      float* __restrict__ sbar, float* __restrict__ vbar,
-                                                      int* __restrict__ err) {
+__global__ void __launch_bounds__(PT, 1) k_fuse_bwd_b_tc(const float* __restrict__ sp, const float* __restrict__ sc,
+                                                         const float* __restrict__ vp, const float* __restrict__ vc,
+                                                         const float* __restrict__ gates, const float* __restrict__ hg,
+                                                         const float* __restrict__ fb, const float* __restrict__ hfb,
+                                                         const float* __restrict__ base, long V,
+                                                         const uint8_t* __restrict__ wpack, float* __restrict__ xbar,
+                                                         float* __restrict__ sbar, float* __restrict__ vbar,
+                                                         int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t B1 = mat_bytes(2 * C, 2 * C), B2 = mat_bytes(C, 2 * C), B3 = mat_bytes(3 * C, C);
-  Split wf1t = split_at(smem, 2 * C, 2 * C), wg2t = split_at(smem + B1, C, 2 * C), wg1t = split_at(smem + B1 + B2, 3 * C, C);
-  uint8_t* region = smem + B1 + B2 + B3;
-  Split A2 = split_at(region, TM, 2 * C), A1 = split_at(region, TM, C);
-  TC_PROLOGUE(3 * C)
-  cx.ok = load_weights(smem, wpack, B1 + B2 + B3, cx, err);
-  for (long t = blockIdx.x; cx.ok && t < nt; t += gridDim.x) {
+  PIPE_PROLOGUE(2 * TM, 1)
+  const Split T2 = split_at(smem + B1 + B2 + B3, TM, 2 * C), T1 = split_at(smem + B1 + B2 + B3, TM, C);
+  P.ok = load_weights(smem, wpack, B1 + B2 + B3, wcx, err);
+  const Op wf1t = wop(smem, 2 * C, 2 * C), wg2t = wop(smem + B1, C, 2 * C);
+  const Op wg1a = wop(smem + B1 + B2, 3 * C, C, 0), wg1b = wop(smem + B1 + B2, 3 * C, C, TM);
+  const int f = P.feat();
+  // epilogue 1: feature f of B_bar is channel fc of the spec (f < C) or vert (f >= C) branch
+  const bool fs = f < C;
+  const int fc = fs ? f : (f < 2 * C ? f - C : 0);
+  const float* pre = fs ? sp : vp;
+  const float* cf = fs ? sc : vc;
+  float* gout = fs ? sbar : vbar;
+  const float gm = __ldg(cf + fc), gsc = __ldg(cf + C + fc), gbi = __ldg(cf + 2 * C + fc);
+  for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (tid == 0) {
-      prefetch_rows(hfb, (t + gridDim.x) * TM, V, 2 * C);
-      prefetch_rows(fb, (t + gridDim.x) * TM, V, C);
-      prefetch_rows(gates, (t + gridDim.x) * TM, V, 2 * C);
-      prefetch_rows(sp, (t + gridDim.x) * TM, V, C);
-      prefetch_rows(vp, (t + gridDim.x) * TM, V, C);
-      prefetch_rows(hg, (t + gridDim.x) * TM, V, C);
-      prefetch_rows(base, (t + gridDim.x) * TM, V, C);
+    if (P.ptid == 0) {
+      prefetch_rows(hfb, (t + tstep) * TM, V, 2 * C);
+      prefetch_rows(fb, (t + tstep) * TM, V, C);
+      prefetch_rows(gates, (t + tstep) * TM, V, 2 * C);
+      prefetch_rows(sp, (t + tstep) * TM, V, C);
+      prefetch_rows(vp, (t + tstep) * TM, V, C);
+      prefetch_rows(hg, (t + tstep) * TM, V, C);
+      prefetch_rows(base, (t + tstep) * TM, V, C);
     }
-    const long v = v0 + row;
-    fill_tile<2 * C>(A2, v0, V, [&](long vv, int k) { return ld4(hfb + vv * 2 * C + k); });
-    if (!gemms(cx, err, tmem, A2, wf1t, 2 * C, 2 * C)) break;
-#pragma unroll
-    for (int jj = 0; jj < (2 * C) / 16; ++jj) if ((jj & 1) == wg) {
-      const int c0 = 16 * jj;
+    fill_tile<2 * C>(T2, v0, V, P.ptid, [&](long vv, int k) { return ld4(hfb + vv * 2 * C + k); });
+    if (!pipe_gemms(P, err, Gemm{P.tmem, wf1t, kop(T2, 2 * C), 2 * C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float bb[16], q[16];
-      tc::tmem_ld16(tmem + lb + c0, bb);
+      tld(P, 0, c, bb);
+      const long vb = v0 + 64 * P.half + 16 * c;
 #pragma unroll
-      for (int i = 0; i < 16; ++i) q[i] = 0.f;
-      if (v < V) {
-        const bool is_s = c0 < C;
-        const int cc = is_s ? c0 : c0 - C;
-        const float* pre = is_s ? sp : vp;
-        const float* cf = is_s ? sc : vc;
-        float* gout = is_s ? sbar : vbar;
-#pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          const float4 f4 = ld4(fb + v * C + cc + i), g4 = ld4(gates + v * 2 * C + c0 + i);
-          const float4 s4 = gn4<true>(ld4(pre + v * C + cc + i), cf, C, cc + i);
-          const float ff[4] = {f4.x, f4.y, f4.z, f4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w}, ss[4] = {s4.x, s4.y, s4.z, s4.w};
-          float o[4];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const float b = bb[i + j] + 0.5f * ff[j];
-            o[j] = b * gg[j];
-            q[i + j] = b * ss[j] * gg[j] * (1.f - gg[j]);
-          }
-          *reinterpret_cast<float4*>(gout + v * C + cc + i) = make_float4(o[0], o[1], o[2], o[3]);
+      for (int i = 0; i < 16; ++i) {
+        const long v = vb + i;
+        q[i] = 0.f;
+        if (f < 2 * C && v < V) {
+          const float b = bb[i] + 0.5f * __ldg(fb + v * C + fc);
+          const float g = __ldg(gates + v * 2 * C + f);
+          const float s = gelu((__ldg(pre + v * C + fc) - gm) * gsc + gbi);
+          gout[v * C + fc] = b * g;
+          q[i] = b * s * g * (1.f - g);
         }
       }
-      put16(A2, row, c0, 2 * C, q);
+      if (f < 2 * C) put_mn(T2, f, 64 * P.half + 16 * c, q);
     }
-    if (!gemms(cx, err, tmem + 2 * C, A2, wg2t, 2 * C, C)) break;
-#pragma unroll
-    for (int jj = 0; jj < (C) / 16; ++jj) if ((jj & 1) == wg) {
-      const int c0 = 16 * jj;
+    if (!pipe_gemms(P, err, Gemm{P.tmem + TM, wg2t, mop(T2), 2 * C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
       float hb[16];
-      tc::tmem_ld16(tmem + lb + 2 * C + c0, hb);
-      if (v < V)
+      tld(P, TM, c, hb);
+      const long vb = v0 + 64 * P.half + 16 * c;
 #pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          const float4 h4 = ld4(hg + v * C + c0 + i);
-          hb[i] *= gelu_grad(h4.x);
-          hb[i + 1] *= gelu_grad(h4.y);
-          hb[i + 2] *= gelu_grad(h4.z);
-          hb[i + 3] *= gelu_grad(h4.w);
-        }
-      put16(A1, row, c0, C, hb);
+      for (int i = 0; i < 16; ++i) {
+        const long v = vb + i;
+        hb[i] = (f < C && v < V) ? hb[i] * gelu_grad(__ldg(hg + v * C + f)) : 0.f;
+      }
+      if (f < C) put_mn(T1, f, 64 * P.half + 16 * c, hb);
     }
-    if (!gemms(cx, err, tmem, A1, wg1t, C, 3 * C)) break;
+    {
+      const Gemm gb{P.tmem + TM, wg1b, mop(T1), C, false};
+      if (!pipe_gemms(P, err, Gemm{P.tmem, wg1a, mop(T1), C, false}, 3 * C > TM ? &gb : nullptr)) break;
+    }
+    // rows r of A_bar: r < C -> x_bar, r < 2C -> spec_bar, r < 3C -> vert_bar; accumulator rows 0..127 then 128..
+#pragma unroll 1
+    for (int part = 0; part < 2; ++part) {
+      const int r = f + TM * part;
+      if (part == 1 && 3 * C <= TM) break;
+#pragma unroll 1
+      for (int c = 0; c < 4; ++c) {
+        float a[16];
+        tld(P, TM * part, c, a);
+        const long vb = v0 + 64 * P.half + 16 * c;
+        if (r < 3 * C)
 #pragma unroll
-    for (int jj = 0; jj < (3 * C) / 16; ++jj) if ((jj & 1) == wg) {
-      const int c0 = 16 * jj;
-      float r[16];
-      tc::tmem_ld16(tmem + lb + c0, r);
-      if (v < V) {
-        if (c0 < C) {
-#pragma unroll
-          for (int i = 0; i < 16; i += 4) {
-            float4 o = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
-            if (base) {
-              const float4 b4 = ld4(base + v * C + c0 + i);
-              o.x += b4.x;
-              o.y += b4.y;
-              o.z += b4.z;
-              o.w += b4.w;
+          for (int i = 0; i < 16; ++i) {
+            const long v = vb + i;
+            if (v < V) {
+              if (r < C)
+                xbar[v * C + r] = base ? a[i] + __ldg(base + v * C + r) : a[i];
+              else if (r < 2 * C)
+                sbar[v * C + r - C] += a[i];
+              else
+                vbar[v * C + r - 2 * C] += a[i];
             }
-            *reinterpret_cast<float4*>(xbar + v * C + c0 + i) = o;
           }
-        } else {
-          float* g = c0 < 2 * C ? sbar : vbar;
-          const int cc = c0 < 2 * C ? c0 - C : c0 - 2 * C;
-#pragma unroll
-          for (int i = 0; i < 16; i += 4) {
-            float4* p = reinterpret_cast<float4*>(g + v * C + cc + i);
-            float4 o = *p;
-            o.x += r[i];
-            o.y += r[i + 1];
-            o.z += r[i + 2];
-            o.w += r[i + 3];
-            *p = o;
-          }
-        }
       }
     }
   }
-  finish(cx, tmem, NCOL);
+  pipe_finish(P, tslot, NCOL);
 }
 
-#undef TC_PROLOGUE
-#undef TC_PROLOGUE_WG
+#undef PIPE_PROLOGUE
 
 int g_sms = 0;
 int sms() {
@@ -1126,6 +939,12 @@ int sms() {
 
 int grid_tc(long V) {
   const long t = ((V + TM - 1) / TM + 1) / 2;   // two warpgroup pipelines per CTA
+  const long g = (long)sms();
+  return (int)(t < g ? (t > 0 ? t : 1) : g);
+}
+
+int grid_tc1(long V) {   // one pipeline per CTA
+  const long t = (V + TM - 1) / TM;
   const long g = (long)sms();
   return (int)(t < g ? (t > 0 ? t : 1) : g);
 }
@@ -1256,7 +1075,7 @@ int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z_bar)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   TC_DISPATCH(C, {
-    const size_t smem = 4 * mat_bytes(CC, CC) + 4 * tile_bytes(CC);
+    const size_t smem = 4 * mat_bytes(CC, CC) + 2 * tile_bytes(CC);
     if (!launch_prep(k_gate_bwd_tc<CC>, smem)) return FFNO_ELAUNCH;
     k_gate_bwd_tc<CC><<<grid_tc(V), CT, smem, s>>>(x, g_bar, base, V, static_cast<const uint8_t*>(wpack), zp, x_bar,
                                                   z_bar, err);
@@ -1290,7 +1109,7 @@ int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const flo
     const size_t smem =
         mat_bytes(2 * CC, 2 * CC) + mat_bytes(CC, 2 * CC) + mat_bytes(3 * CC, CC) + tile_bytes(2 * CC);
     if (!launch_prep(k_fuse_bwd_b_tc<CC>, smem)) return FFNO_ELAUNCH;
-    k_fuse_bwd_b_tc<CC><<<grid_tc(V), TT, smem, s>>>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, hg,
+    k_fuse_bwd_b_tc<CC><<<grid_tc1(V), PT, smem, s>>>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, hg,
                                                     fused_pre_bar, hf_bar, base, V,
                                                     static_cast<const uint8_t*>(wpack), x_bar, spec_bar, vert_bar,
                                                     err);

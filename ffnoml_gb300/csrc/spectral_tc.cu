@@ -206,6 +206,7 @@ __global__ void __launch_bounds__(XT) k_xform_tc(const uint8_t* __restrict__ tpa
 constexpr int RT = 256;                     // threads per pipeline
 constexpr int RKC = 64;                     // data rows k per chunk
 constexpr uint32_t RSB = 128u * RKC * 2;    // one split half of a data stage
+constexpr int RT_MAXK = 512;                // largest padded K of a resident table
 
 __device__ __forceinline__ void rt_sync(int pipe) { asm volatile("bar.sync %0, %1;" ::"r"(1 + pipe), "n"(RT) : "memory"); }
 __device__ __forceinline__ bool rt_sync_and(int pipe, bool p) {
@@ -228,8 +229,12 @@ __global__ void __launch_bounds__(2 * RT, 1)
   uint8_t* sD = base + ((2 * TB + 1023u) & ~1023u);          // [pipe][stage][hi | lo]
   __shared__ uint64_t bar_t, bar_m[2][2];
   __shared__ uint32_t tslot;
+  __shared__ long row_in[RT_MAXK], row_out[256];   // element offsets of data row k and output row m
   const int tid = threadIdx.x, pipe = tid / RT, ptid = tid % RT, warp = tid >> 5, lane = tid & 31;
   const int q = warp & 3, half = ptid >> 7;
+  for (int k = tid; k < Kp; k += 2 * RT) row_in[k] = (long)(k / d.in_split) * d.in_hi + (long)(k % d.in_split) * d.in_lo;
+  for (int m = tid; m < Mp; m += 2 * RT)
+    row_out[m] = (long)(m / d.out_split) * d.out_hi + (long)(m % d.out_split) * d.out_lo;
   if (warp == 0) tc::tmem_alloc(&tslot, 512);
   if (tid == 0) {
     tc::mbar_init(&bar_t, 1);
@@ -260,20 +265,23 @@ __global__ void __launch_bounds__(2 * RT, 1)
       bfirst = it / ntn;
       n0 = (it % ntn) * 128;
     }
-    // source / destination offsets of column n of this item (-1: no such column)
-    auto col_in = [&](int n, long& off) -> bool {
+    // every fill piece of this thread covers the same 4 columns nf..nf+3 (see the piece mapping below)
+    const int nf = 8 * (2 * ((ptid >> 5) & 7) + (lane >> 4)) + 4 * ((lane >> 3) & 1);
+    long foff = 0;
+    bool fv;
+    {
       long b, c;
       if (nbi > 1) {
-        b = bfirst + (n >> nshift);
-        c = n & ((1 << nshift) - 1);
+        b = bfirst + (nf >> nshift);
+        c = nf & ((1 << nshift) - 1);
       } else {
         b = bfirst;
-        c = n0 + n;
+        c = n0 + nf;
       }
-      if (b >= d.nb || c >= d.N) return false;
-      off = (b / d.nb2) * d.in_b1 + (b % d.nb2) * d.in_b2 + c;
-      return true;
-    };
+      fv = b < d.nb && c < d.N;
+      if (fv) foff = (b / d.nb2) * d.in_b1 + (b % d.nb2) * d.in_b2 + c;
+    }
+    const float* fsrc = in + foff;
     for (int ch = 0; ch < nch; ++ch, ++g) {
       const int s = (int)(g & 1u);
       const int k0 = ch * RKC, kc = (Kp - k0) < RKC ? (Kp - k0) : RKC;
@@ -282,22 +290,17 @@ __global__ void __launch_bounds__(2 * RT, 1)
         if (!(ok = rt_sync_and(pipe, w))) break;
       }
       uint8_t* st = sD + (uint32_t)(pipe * 2 + s) * 2u * RSB;
-      // fill: piece = 4 consecutive columns of one row k; a warp covers 8 rows x 64 contiguous bytes of each
+      // fill: piece e = 4 consecutive columns of one row k; lanes take 8 rows x 2 column pairs, so a warp reads 8
+      // rows x 64 contiguous bytes and writes conflict-free 8-byte slots of the MN-major tile. Row k of piece e is
+      // 8 (e / 256) + (lane & 7); its columns nf..nf+3 depend on the thread only.
       for (int e0 = ptid; e0 < kc * 32; e0 += 4 * RT) {
         float4 v[4];
-        int kk[4], nn[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int e = e0 + u * RT;
-          const int ln = e & 31, grp = e >> 5;
-          kk[u] = 8 * (grp >> 3) + (ln & 7);
-          nn[u] = 8 * (2 * (grp & 7) + (ln >> 4)) + 4 * ((ln >> 3) & 1);
-          v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-          const int k = k0 + kk[u];
-          long off;
-          if (e < kc * 32 && k < d.K && col_in(nn[u], off))
-            v[u] = __ldg(reinterpret_cast<const float4*>(in + off + (long)(k / d.in_split) * d.in_hi +
-                                                        (long)(k % d.in_split) * d.in_lo));
+          const int k = k0 + 8 * (e >> 8) + (lane & 7);
+          v[u] = (e < kc * 32 && k < d.K && fv) ? __ldg(reinterpret_cast<const float4*>(fsrc + row_in[k]))
+                                                : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -306,7 +309,7 @@ __global__ void __launch_bounds__(2 * RT, 1)
           uint32_t h0, l0, h1, l1;
           tc::split_pack(v[u].x, v[u].y, h0, l0);
           tc::split_pack(v[u].z, v[u].w, h1, l1);
-          const uint32_t o = tc::mnmajor_offset(nn[u], kk[u], 128);
+          const uint32_t o = tc::mnmajor_offset(nf, 8 * (e >> 8) + (lane & 7), 128);
           *reinterpret_cast<uint2*>(st + o) = make_uint2(h0, h1);
           *reinterpret_cast<uint2*>(st + RSB + o) = make_uint2(l0, l1);
         }
@@ -358,7 +361,7 @@ __global__ void __launch_bounds__(2 * RT, 1)
         for (int i = 0; i < 16; ++i) {
           const int m = 16 * jj + i;
           if (m < d.M) {
-            float* p = out + obase + (long)(m / d.out_split) * d.out_hi + (long)(m % d.out_split) * d.out_lo;
+            float* p = out + obase + row_out[m];
             *p = accumulate ? *p + v[i] : v[i];
           }
         }
@@ -695,7 +698,7 @@ int ffno_xform_tcr(const void* tpack, int Mp, int Kp, const float* in, float* ou
   if (!tpack || !in || !out || !desc || !err || (reinterpret_cast<uintptr_t>(tpack) % 16)) return FFNO_EINVAL;
   const ffno_xform_desc& d = *desc;
   if (d.nb < 1 || d.nb2 < 1 || d.K < 1 || d.M < 1 || d.N < 1 || d.in_split < 1 || d.out_split < 1) return FFNO_EINVAL;
-  if (Mp % 16 || Mp < d.M || Mp > 256 || Kp % 16 || Kp < d.K) return FFNO_EINVAL;
+  if (Mp % 16 || Mp < d.M || Mp > 256 || Kp % 16 || Kp < d.K || Kp > RT_MAXK) return FFNO_EINVAL;
   if ((size_t)Mp * Kp * 4 > ffno_xform_tcr_max_table_bytes()) return FFNO_EINVAL;
   if (d.N % 4 || d.in_lo % 4 || d.in_hi % 4 || d.in_b1 % 4 || d.in_b2 % 4) return FFNO_EINVAL;   // float4 loads
   if (reinterpret_cast<uintptr_t>(in) % 16) return FFNO_EINVAL;
@@ -717,7 +720,7 @@ int ffno_xform_tcr(const void* tpack, int Mp, int Kp, const float* in, float* ou
   return FFNO_OK;
 }
 
-int ffno_xform_tcr_max_table_bytes(void) { return 96 * 1024; }
+int ffno_xform_tcr_max_table_bytes(void) { return 80 * 1024; }
 
 int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, long sb, long s_im, int C,
                          const void* wpack, const float* g, const float* U, const float* Vm, int rank, int* err,
