@@ -142,9 +142,9 @@ __device__ __forceinline__ Op mop(Split t) {
   return Op{tc::smem_u32(t.hi()), tc::smem_u32(t.lo()), 2048u, 128u, 4096u, true};
 }
 
-// D^T [128 x 128] (+)= A B^T over K, split-BF16 (Ah Bh + Ah Bl + Al Bh); A K-major, B K- or MN-major
-__device__ __forceinline__ void mma3(uint32_t d, const Op& a, const Op& b, int K, bool acc) {
-  const uint32_t idesc = tc::idesc_bf16_ab(128, 128, false, b.mn);
+// D [128 x N] (+)= A B^T over K, split-BF16 (Ah Bh + Ah Bl + Al Bh); either operand K- or MN-major
+__device__ __forceinline__ void mma3(uint32_t d, const Op& a, const Op& b, int K, int N, bool acc) {
+  const uint32_t idesc = tc::idesc_bf16_ab(128, N, a.mn, b.mn);
   const uint32_t as[3] = {a.hi, a.hi, a.lo}, bs[3] = {b.hi, b.lo, b.hi};
 #pragma unroll
   for (int s = 0; s < 3; ++s)
@@ -160,6 +160,7 @@ struct Gemm {
   Op a, b;
   int K;
   bool acc;
+  int N = 128;
 };
 
 // Issue up to three split GEMMs (the pipeline's thread 0) behind one commit and wait for them (the pipeline).
@@ -170,9 +171,9 @@ __device__ __forceinline__ bool pipe_gemms(Pipe& p, int* err, const Gemm& g0, co
   pipe_sync(p.id);
   tc::tc_after_sync();
   if (p.ptid == 0) {
-    mma3(g0.d, g0.a, g0.b, g0.K, g0.acc);
-    if (g1) mma3(g1->d, g1->a, g1->b, g1->K, g1->acc);
-    if (g2) mma3(g2->d, g2->a, g2->b, g2->K, g2->acc);
+    mma3(g0.d, g0.a, g0.b, g0.K, g0.N, g0.acc);
+    if (g1) mma3(g1->d, g1->a, g1->b, g1->K, g1->N, g1->acc);
+    if (g2) mma3(g2->d, g2->a, g2->b, g2->K, g2->N, g2->acc);
     tc::mma_commit(p.bar);
   }
   const bool ok = pipe_sync_and(p.id, tc::mbar_wait(p.bar, p.phase));
@@ -297,6 +298,105 @@ __device__ __forceinline__ void tile_stats(const Pipe& p, uint32_t d, const floa
   pipe_sync(p.id);
 }
 
+// ---------------------------------------------------------------------------------------------- row orientation
+// GEMMs with C outputs run untransposed, D [128 voxels][C] = X W^T (the voxel tile as the A operand, K- or MN-major,
+// the weights as the B operand), so that every accumulator lane is live: thread feat() of a pipeline serves voxel
+// row feat() and the 16-column chunks j with j % 2 == half.
+__device__ __forceinline__ bool owns(int j, int half) { return (j & 1) == half; }
+
+__device__ __forceinline__ void rld(const Pipe& p, uint32_t d, int j, float (&v)[16]) {
+  tc::tmem_ld16(p.tmem + p.lq + d + (uint32_t)(16 * j), v);
+}
+
+// Write 16 values of row r into a split K-major tile with K columns at columns c0..c0+15.
+__device__ __forceinline__ void put16(Split t, int r, int c0, int K, const float (&v)[16]) {
+  uint32_t h[8], l[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) tc::split_pack(v[2 * i], v[2 * i + 1], h[i], l[i]);
+  const uint32_t o0 = tc::kmajor_offset(r, c0, K), o1 = tc::kmajor_offset(r, c0 + 8, K);
+  *reinterpret_cast<uint4*>(t.hi() + o0) = make_uint4(h[0], h[1], h[2], h[3]);
+  *reinterpret_cast<uint4*>(t.hi() + o1) = make_uint4(h[4], h[5], h[6], h[7]);
+  *reinterpret_cast<uint4*>(t.lo() + o0) = make_uint4(l[0], l[1], l[2], l[3]);
+  *reinterpret_cast<uint4*>(t.lo() + o1) = make_uint4(l[4], l[5], l[6], l[7]);
+}
+
+// Depth-weighted statistics of a row-oriented tile: every thread holds, in v[C], the chunks of its row it owns and
+// the row's weight w (0 past the cube). Merged with Chan's update into acc[g] by thread g < GMAX; fixed order.
+// red: [8][GMAX + 1] of this pipeline.
+template <int C>
+__device__ __forceinline__ void row_stats(const Pipe& p, const float (&v)[C], float w, float* red, float* gm,
+                                          float* wsum, double* acc) {
+  constexpr int CPG = C / GMAX, NW = PT / 32;
+  const int lane = p.lane, wl = p.ptid >> 5;
+  float ws = p.half == 0 ? w : 0.f;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, o);
+  float s[GMAX];
+#pragma unroll
+  for (int g = 0; g < GMAX; ++g) s[g] = 0.f;
+#pragma unroll
+  for (int c = 0; c < C; ++c)
+    if (owns(c / 16, p.half)) s[c / CPG] += v[c];
+#pragma unroll
+  for (int g = 0; g < GMAX; ++g) {
+    float x = w * s[g];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    s[g] = x;
+  }
+  if (lane == 0) {
+    red[wl * (GMAX + 1) + GMAX] = ws;
+#pragma unroll
+    for (int g = 0; g < GMAX; ++g) red[wl * (GMAX + 1) + g] = s[g];
+  }
+  pipe_sync(p.id);
+  if (p.ptid == 0) {
+    float t = 0.f;
+    for (int q = 0; q < NW; ++q) t += red[q * (GMAX + 1) + GMAX];
+    *wsum = t;
+  }
+  if (p.ptid < GMAX) {
+    float t = 0.f, wt = 0.f;
+    for (int q = 0; q < NW; ++q) {
+      t += red[q * (GMAX + 1) + p.ptid];
+      wt += red[q * (GMAX + 1) + GMAX];
+    }
+    wt *= CPG;
+    gm[p.ptid] = wt > 0.f ? t / wt : 0.f;
+  }
+  pipe_sync(p.id);
+#pragma unroll
+  for (int g = 0; g < GMAX; ++g) s[g] = 0.f;
+#pragma unroll
+  for (int c = 0; c < C; ++c)
+    if (owns(c / 16, p.half)) {
+      const float d = v[c] - gm[c / CPG];
+      s[c / CPG] += d * d;
+    }
+#pragma unroll
+  for (int g = 0; g < GMAX; ++g) {
+    float x = w * s[g];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    s[g] = x;
+  }
+  if (lane == 0)
+#pragma unroll
+    for (int g = 0; g < GMAX; ++g) red[wl * (GMAX + 1) + g] = s[g];
+  pipe_sync(p.id);
+  if (p.ptid < GMAX) {
+    float t = 0.f;
+    for (int q = 0; q < NW; ++q) t += red[q * (GMAX + 1) + p.ptid];
+    double* a = acc + 3 * p.ptid;
+    GroupAcc ga{a[0], a[1], a[2]};
+    chan_merge(ga, (double)*wsum * CPG, (double)gm[p.ptid], (double)t);
+    a[0] = ga.w;
+    a[1] = ga.mean;
+    a[2] = ga.m2;
+  }
+  pipe_sync(p.id);
+}
+
 // The CTA's GroupNorm partial: pipeline 1's statistics merged into pipeline 0's (fixed order). All threads call it.
 __device__ __forceinline__ void write_partial2(double* partials, const double* acc /* [2][GMAX][3] */) {
   __syncthreads();
@@ -407,48 +507,55 @@ __global__ void __launch_bounds__(CT, 1) k_mlp2_tc(const float* __restrict__ in,
   pipe_finish(P, tslot, 2 * NCOL);
 }
 
-// Input gate of one branch: out = x sigmoid(gelu(x G1) G2) [+ zp z]. Weights: [g1 (C x C), g2 (C x C)].
+// Input gate of one branch: out = x sigmoid(gelu(x G1) G2) [+ zp z]. Weights: [g1 (C x C), g2 (C x C)]. Both GEMMs
+// have C outputs and run untransposed (lane = voxel).
 template <int C>
 __global__ void __launch_bounds__(CT, 1) k_gate_tc(const float* __restrict__ x, long V, const uint8_t* __restrict__ wpack,
                                                    const float* __restrict__ zp, const float* __restrict__ z,
                                                    float* __restrict__ out, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t B1 = mat_bytes(C, C), RB = tile_bytes(C);
-  PIPE_PROLOGUE(TM, 2)
+  PIPE_PROLOGUE(C, 2)
   const Split X = split_at(smem + 2 * B1 + pid * RB, TM, C);
   P.ok = load_weights(smem, wpack, 2 * B1, wcx, err);
   const Op g1 = wop(smem, C, C), g2 = wop(smem + B1, C, C);
-  const int f = P.feat();
-  const float zf = (zp && f < C) ? __ldg(zp + f) : 0.f;
+  const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
     if (P.ptid == 0) prefetch_rows(x, (t + tstep) * TM, V, C);
     fill_tile<C>(X, v0, V, P.ptid, [&](long v, int k) { return ld4(x + v * C + k); });
-    if (!pipe_gemms(P, err, Gemm{P.tmem, g1, kop(X, C), C, false})) break;
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
+    if (!pipe_gemms(P, err, Gemm{P.tmem, kop(X, C), g1, C, false, C})) break;
+#pragma unroll
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
       float v[16];
-      tld(P, 0, c, v);
+      rld(P, 0, j, v);
 #pragma unroll
       for (int i = 0; i < 16; ++i) v[i] = gelu(v[i]);
-      if (f < C) put_mn(X, f, 64 * P.half + 16 * c, v);
+      put16(X, row, 16 * j, C, v);
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem, g2, mop(X), C, false})) break;
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      float g[16];
-      tld(P, 0, c, g);
-      const long vb = v0 + 64 * P.half + 16 * c;
-      if (f < C)
+    if (!pipe_gemms(P, err, Gemm{P.tmem, kop(X, C), g2, C, false, C})) break;
+    const long v = v0 + row;
+    const float zv = (zp && v < V) ? __ldg(z + v) : 0.f;
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const long v = vb + i;
-          if (v < V) {
-            float o = __ldg(x + v * C + f) * sigmoid(g[i]);
-            if (zp) o = fmaf(zf, __ldg(z + v), o);
-            out[v * C + f] = o;
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      const int c0 = 16 * j;
+      float g[16];
+      rld(P, 0, j, g);
+      if (v < V) {
+#pragma unroll
+        for (int i = 0; i < 16; i += 4) {
+          const float4 xv = ld4(x + v * C + c0 + i);
+          float4 o = make_float4(xv.x * sigmoid(g[i]), xv.y * sigmoid(g[i + 1]), xv.z * sigmoid(g[i + 2]),
+                                 xv.w * sigmoid(g[i + 3]));
+          if (zp) {
+            const float4 zz = ld4(zp + c0 + i);
+            o = make_float4(fmaf(zz.x, zv, o.x), fmaf(zz.y, zv, o.y), fmaf(zz.z, zv, o.z), fmaf(zz.w, zv, o.w));
           }
+          *reinterpret_cast<float4*>(out + v * C + c0 + i) = o;
         }
+      }
     }
   }
   pipe_finish(P, tslot, 2 * NCOL);
@@ -456,7 +563,8 @@ __global__ void __launch_bounds__(CT, 1) k_gate_tc(const float* __restrict__ x, 
 
 // Branch gates (first half of _fuse_branches): gates = sigmoid(gelu([x, spec, vert] Wg1) Wg2 + b), spec =
 // gelu(GN(spec_pre)) etc.; optionally the hidden pre-activation [x, spec, vert] Wg1 to hg. Weights: [wg1 (C x 3C),
-// wg2 (2C x C)]. The first GEMM runs over three K-slices of C columns (x, spec, vert) through one tile per pipeline.
+// wg2 (2C x C)]. The first GEMM (C outputs, untransposed) runs over three K-slices of C columns (x, spec, vert) through
+// one tile per pipeline; the second (2C outputs) is transposed.
 template <int C>
 __global__ void __launch_bounds__(CT, 1) k_fuse1_tc(const float* __restrict__ x, const float* __restrict__ sp,
                                                     const float* __restrict__ sc, const float* __restrict__ vp,
@@ -488,23 +596,25 @@ __global__ void __launch_bounds__(CT, 1) k_fuse1_tc(const float* __restrict__ x,
         fill_tile<C>(A, v0, V, P.ptid, [&](long v, int k) { return gn_apply<true>(ld4(sp + v * C + k), gs); });
       else
         fill_tile<C>(A, v0, V, P.ptid, [&](long v, int k) { return gn_apply<true>(ld4(vp + v * C + k), gv); });
-      if (!pipe_gemms(P, err, Gemm{P.tmem, wop(smem, C, 3 * C, 0, kc * C), kop(A, C), C, kc > 0})) break;
+      if (!pipe_gemms(P, err, Gemm{P.tmem, kop(A, C), wop(smem, C, 3 * C, 0, kc * C), C, kc > 0, C})) break;
     }
     if (!P.ok) break;
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      float h[16];
-      tld(P, 0, c, h);
-      const long vb = v0 + 64 * P.half + 16 * c;
-      if (hg && f < C)
+    const long v = v0 + f;
 #pragma unroll
-        for (int i = 0; i < 16; ++i)
-          if (vb + i < V) hg[(vb + i) * C + f] = h[i];
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      const int c0 = 16 * j;
+      float h[16];
+      rld(P, 0, j, h);
+      if (hg && v < V)
+#pragma unroll
+        for (int i = 0; i < 16; i += 4)
+          *reinterpret_cast<float4*>(hg + v * C + c0 + i) = make_float4(h[i], h[i + 1], h[i + 2], h[i + 3]);
 #pragma unroll
       for (int i = 0; i < 16; ++i) h[i] = gelu(h[i]);
-      if (f < C) put_mn(A, f, 64 * P.half + 16 * c, h);
+      put16(A, f, c0, C, h);
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem, wg2, mop(A), C, false})) break;
+    if (!pipe_gemms(P, err, Gemm{P.tmem, wg2, kop(A, C), C, false})) break;
 #pragma unroll 1
     for (int c = 0; c < 4; ++c) {
       float g[16];
@@ -598,7 +708,7 @@ __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp
 
 // ============================================================================================== backward
 // a_bar = base + ((pre_bar W2^T) * gelu'(a W1)) W1^T. Weights: [w1 (2C x C), w2t (2C x C), w1t (C x 2C)].
-// Per pipeline: the tiles of a and pre_bar, then (aliased) the hidden tile.
+// Per pipeline: the tiles of a and pre_bar, then (aliased) the hidden tile; the last GEMM (C outputs) untransposed.
 template <int C>
 __global__ void __launch_bounds__(CT, 1) k_mlp2_bwd_tc(const float* __restrict__ a, const float* __restrict__ pb,
                                                        const float* __restrict__ base, long V,
@@ -633,45 +743,31 @@ __global__ void __launch_bounds__(CT, 1) k_mlp2_bwd_tc(const float* __restrict__
       for (int i = 0; i < 16; ++i) gb[i] *= gelu_grad(hp[i]);
       if (f < 2 * C) put_mn(H, f, 64 * P.half + 16 * c, gb);
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem, w1t, mop(H), 2 * C, false})) break;
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      float r[16];
-      tld(P, 0, c, r);
-      const long vb = v0 + 64 * P.half + 16 * c;
-      if (f < C)
+    if (!pipe_gemms(P, err, Gemm{P.tmem, mop(H), w1t, 2 * C, false, C})) break;
+    const long v = v0 + f;
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const long v = vb + i;
-          if (v < V) abar[v * C + f] = base ? r[i] + __ldg(base + v * C + f) : r[i];
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      const int c0 = 16 * j;
+      float r[16];
+      rld(P, 0, j, r);
+      if (v < V)
+#pragma unroll
+        for (int i = 0; i < 16; i += 4) {
+          float4 o = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
+          if (base) {
+            const float4 b = ld4(base + v * C + c0 + i);
+            o = make_float4(o.x + b.x, o.y + b.y, o.z + b.z, o.w + b.w);
+          }
+          *reinterpret_cast<float4*>(abar + v * C + c0 + i) = o;
         }
     }
   }
   pipe_finish(P, tslot, 2 * NCOL);
 }
 
-// Sums of 16 per-voxel values over the 32 lanes of a warp: afterwards lanes 2i and 2i + 1 hold the sum for voxel
-// vox_of(lane) (a fixed butterfly, deterministic).
-__device__ __forceinline__ float warp_sum16(float (&v)[16], int lane) {
-#pragma unroll
-  for (int m = 16, n = 8; m >= 2; m >>= 1, n >>= 1) {
-    const bool up = (lane & m) != 0;
-#pragma unroll
-    for (int i = 0; i < n; ++i) {
-      const float send = up ? v[i] : v[i + n];
-      const float keep = up ? v[i + n] : v[i];
-      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, m);
-    }
-  }
-  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
-}
-__device__ __forceinline__ int vox_of(int lane) {
-  return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
-}
-
 // One input gate's backward: x_bar = base + d/dx [x sigmoid(gelu(x G1) G2)] applied to gbar; with zp, z_bar[v] +=
-// sum_c gbar zp. Weights: [g1, g2, g2t, g1t] (each C x C). One tile region per pipeline, reused by the input tile
-// and the three MN-major intermediates.
+// sum_c gbar zp. Weights: [g1, g2, g2t, g1t] (each C x C). All four GEMMs have C outputs and run untransposed.
 template <int C>
 __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__ x, const float* __restrict__ gbar,
                                                        const float* __restrict__ base, long V,
@@ -679,17 +775,15 @@ __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__
                                                        float* __restrict__ xbar, float* __restrict__ zbar,
                                                        int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  constexpr uint32_t B1 = mat_bytes(C, C), RB = tile_bytes(C);
-  constexpr int NQ = (C + 31) / 32;   // warps of a half holding live channels
-  __shared__ float zq[2][2][NQ][64];  // [pipeline][half][warp][voxel of the half]
-  PIPE_PROLOGUE(2 * TM, 2)
-  const Split T = split_at(smem + 4 * B1 + pid * RB, TM, C);
+  constexpr uint32_t B1 = mat_bytes(C, C), RB = 2 * tile_bytes(C);
+  __shared__ float zsh[2][TM];
+  PIPE_PROLOGUE(4 * C, 2)
+  const Split X = split_at(smem + 4 * B1 + pid * RB, TM, C), T = split_at(smem + 4 * B1 + pid * RB + tile_bytes(C), TM, C);
   P.ok = load_weights(smem, wpack, 4 * B1, wcx, err);
   const Op g1 = wop(smem, C, C), g2 = wop(smem + B1, C, C), g2t = wop(smem + 2 * B1, C, C),
            g1t = wop(smem + 3 * B1, C, C);
-  const int f = P.feat();
-  const float zf = (zp && f < C) ? __ldg(zp + f) : 0.f;
-  const uint32_t D1 = 0, D2 = TM;
+  const uint32_t D1 = 0, D2 = C, D3 = 2 * C, D4 = 3 * C;
+  const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
     if (P.ptid == 0) {
@@ -697,72 +791,82 @@ __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__
       prefetch_rows(gbar, (t + tstep) * TM, V, C);
       prefetch_rows(base, (t + tstep) * TM, V, C);
     }
-    fill_tile<C>(T, v0, V, P.ptid, [&](long vv, int k) { return ld4(x + vv * C + k); });
-    if (!pipe_gemms(P, err, Gemm{P.tmem + D1, g1, kop(T, C), C, false})) break;
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
+    const long v = v0 + row;
+    fill_tile<C>(X, v0, V, P.ptid, [&](long vv, int k) { return ld4(x + vv * C + k); });
+    if (!pipe_gemms(P, err, Gemm{P.tmem + D1, kop(X, C), g1, C, false, C})) break;
+#pragma unroll
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
       float h[16];
-      tld(P, D1, c, h);
+      rld(P, D1, j, h);
 #pragma unroll
       for (int i = 0; i < 16; ++i) h[i] = gelu(h[i]);
-      if (f < C) put_mn(T, f, 64 * P.half + 16 * c, h);
+      put16(T, row, 16 * j, C, h);
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem + D2, g2, mop(T), C, false})) break;
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      float g[16], q[16], zs[16];
-      tld(P, D2, c, g);
-      const long vb = v0 + 64 * P.half + 16 * c;
+    if (!pipe_gemms(P, err, Gemm{P.tmem + D2, kop(T, C), g2, C, false, C})) break;
+    float zs = 0.f;
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const long v = vb + i;
-        q[i] = 0.f;
-        zs[i] = 0.f;
-        if (f < C && v < V) {
-          const float b = __ldg(gbar + v * C + f), xv = __ldg(x + v * C + f);
-          const float s = sigmoid(g[i]);
-          xbar[v * C + f] = base ? fmaf(b, s, __ldg(base + v * C + f)) : b * s;
-          q[i] = b * xv * s * (1.f - s);
-          zs[i] = b * zf;
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      const int c0 = 16 * j;
+      float g[16], q[16];
+      rld(P, D2, j, g);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) q[i] = 0.f;
+      if (v < V) {
+#pragma unroll
+        for (int i = 0; i < 16; i += 4) {
+          const float4 b = ld4(gbar + v * C + c0 + i), xv = ld4(x + v * C + c0 + i);
+          const float bb[4] = {b.x, b.y, b.z, b.w}, xx[4] = {xv.x, xv.y, xv.z, xv.w};
+          float o[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const float s = sigmoid(g[i + u]);
+            o[u] = bb[u] * s;
+            q[i + u] = bb[u] * xx[u] * s * (1.f - s);
+            if (zp) zs = fmaf(bb[u], __ldg(zp + c0 + i + u), zs);
+          }
+          float4 r = make_float4(o[0], o[1], o[2], o[3]);
+          if (base) {
+            const float4 bs = ld4(base + v * C + c0 + i);
+            r = make_float4(r.x + bs.x, r.y + bs.y, r.z + bs.z, r.w + bs.w);
+          }
+          *reinterpret_cast<float4*>(xbar + v * C + c0 + i) = r;
         }
       }
-      if (f < C) put_mn(T, f, 64 * P.half + 16 * c, q);
-      if (zp && P.q < NQ) {
-        const float sum = warp_sum16(zs, P.lane);
-        if ((P.lane & 1) == 0) zq[pid][P.half][P.q][16 * c + vox_of(P.lane)] = sum;
-      }
+      put16(T, row, c0, C, q);
     }
-    if (zp) {   // z_bar: the warps' partial sums per voxel, added in a fixed order
+    if (zp) {   // the two halves of the row add their parts of z_bar in a fixed order
+      if (P.half == 1) zsh[pid][row] = zs;
       pipe_sync(P.id);
-      if (P.ptid < TM) {
-        const int hh = P.ptid >> 6, vl = P.ptid & 63;
-        const long v = v0 + P.ptid;
-        float s = 0.f;
-#pragma unroll
-        for (int w = 0; w < NQ; ++w) s += zq[pid][hh][w][vl];
-        if (v < V) zbar[v] += s;
-      }
+      if (P.half == 0 && v < V) zbar[v] += zs + zsh[pid][row];
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem + D2, g2t, mop(T), C, false})) break;
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
+    if (!pipe_gemms(P, err, Gemm{P.tmem + D3, kop(T, C), g2t, C, false, C})) break;
+#pragma unroll
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
       float hb[16], hp[16];
-      tld(P, D2, c, hb);
-      tld(P, D1, c, hp);
+      rld(P, D3, j, hb);
+      rld(P, D1, j, hp);
 #pragma unroll
       for (int i = 0; i < 16; ++i) hb[i] *= gelu_grad(hp[i]);
-      if (f < C) put_mn(T, f, 64 * P.half + 16 * c, hb);
+      put16(T, row, 16 * j, C, hb);
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem + D2, g1t, mop(T), C, false})) break;
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      float r[16];
-      tld(P, D2, c, r);
-      const long vb = v0 + 64 * P.half + 16 * c;
-      if (f < C)
+    if (!pipe_gemms(P, err, Gemm{P.tmem + D4, kop(T, C), g1t, C, false, C})) break;
 #pragma unroll
-        for (int i = 0; i < 16; ++i)
-          if (vb + i < V) xbar[(vb + i) * C + f] += r[i];
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      const int c0 = 16 * j;
+      float r[16];
+      rld(P, D4, j, r);
+      if (v < V)
+#pragma unroll
+        for (int i = 0; i < 16; i += 4) {
+          float4* pp = reinterpret_cast<float4*>(xbar + v * C + c0 + i);
+          float4 o = *pp;
+          o = make_float4(o.x + r[i], o.y + r[i + 1], o.z + r[i + 2], o.w + r[i + 3]);
+          *pp = o;
+        }
     }
   }
   pipe_finish(P, tslot, 2 * NCOL);
@@ -821,7 +925,8 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_a_tc(const float* __restrict
 // Fuse backward, stage b: B_bar = hfb Wf1^T + [F_bar, F_bar] / 2; spec/vert grads B_bar g (+ the gate path);
 // gate pre-activation grad q = B_bar [spec, vert] g (1 - g); hg_bar = (q Wg2^T) * gelu'(hg); A_bar = hg_bar Wg1^T:
 // x_bar = base + A_bar[:C], spec_bar = B_bar_s g_s + A_bar[C:2C], vert_bar likewise.
-// Weights: [wf1t (2C x 2C), wg2t (C x 2C), wg1t (3C x C)]. One pipeline per CTA (the weights leave room for one tile).
+// Weights: [wf1t (2C x 2C), wg2t (C x 2C), wg1t (3C x C)]. One pipeline per CTA (the weights leave room for one tile);
+// all three GEMMs run untransposed (lane = voxel; its epilogues read and write several tensors per voxel).
 template <int C>
 __global__ void __launch_bounds__(PT, 1) k_fuse_bwd_b_tc(const float* __restrict__ sp, const float* __restrict__ sc,
                                                          const float* __restrict__ vp, const float* __restrict__ vc,
@@ -833,19 +938,11 @@ __global__ void __launch_bounds__(PT, 1) k_fuse_bwd_b_tc(const float* __restrict
                                                          int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t B1 = mat_bytes(2 * C, 2 * C), B2 = mat_bytes(C, 2 * C), B3 = mat_bytes(3 * C, C);
-  PIPE_PROLOGUE(2 * TM, 1)
+  PIPE_PROLOGUE(3 * C, 1)
   const Split T2 = split_at(smem + B1 + B2 + B3, TM, 2 * C), T1 = split_at(smem + B1 + B2 + B3, TM, C);
   P.ok = load_weights(smem, wpack, B1 + B2 + B3, wcx, err);
-  const Op wf1t = wop(smem, 2 * C, 2 * C), wg2t = wop(smem + B1, C, 2 * C);
-  const Op wg1a = wop(smem + B1 + B2, 3 * C, C, 0), wg1b = wop(smem + B1 + B2, 3 * C, C, TM);
-  const int f = P.feat();
-  // epilogue 1: feature f of B_bar is channel fc of the spec (f < C) or vert (f >= C) branch
-  const bool fs = f < C;
-  const int fc = fs ? f : (f < 2 * C ? f - C : 0);
-  const float* pre = fs ? sp : vp;
-  const float* cf = fs ? sc : vc;
-  float* gout = fs ? sbar : vbar;
-  const float gm = __ldg(cf + fc), gsc = __ldg(cf + C + fc), gbi = __ldg(cf + 2 * C + fc);
+  const Op wf1t = wop(smem, 2 * C, 2 * C), wg2t = wop(smem + B1, C, 2 * C), wg1t = wop(smem + B1 + B2, 3 * C, C);
+  const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
     if (P.ptid == 0) {
@@ -857,67 +954,87 @@ __global__ void __launch_bounds__(PT, 1) k_fuse_bwd_b_tc(const float* __restrict
       prefetch_rows(hg, (t + tstep) * TM, V, C);
       prefetch_rows(base, (t + tstep) * TM, V, C);
     }
+    const long v = v0 + row;
     fill_tile<2 * C>(T2, v0, V, P.ptid, [&](long vv, int k) { return ld4(hfb + vv * 2 * C + k); });
-    if (!pipe_gemms(P, err, Gemm{P.tmem, wf1t, kop(T2, 2 * C), 2 * C, false})) break;
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      float bb[16], q[16];
-      tld(P, 0, c, bb);
-      const long vb = v0 + 64 * P.half + 16 * c;
+    if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T2, 2 * C), wf1t, 2 * C, false, 2 * C})) break;
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const long v = vb + i;
-        q[i] = 0.f;
-        if (f < 2 * C && v < V) {
-          const float b = bb[i] + 0.5f * __ldg(fb + v * C + fc);
-          const float g = __ldg(gates + v * 2 * C + f);
-          const float s = gelu((__ldg(pre + v * C + fc) - gm) * gsc + gbi);
-          gout[v * C + fc] = b * g;
-          q[i] = b * s * g * (1.f - g);
+    for (int j = 0; j < (2 * C) / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      const int c0 = 16 * j;
+      float bb[16], q[16];
+      rld(P, 0, j, bb);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) q[i] = 0.f;
+      if (v < V) {
+        const bool is_s = c0 < C;
+        const int cc = is_s ? c0 : c0 - C;
+        const float* pre = is_s ? sp : vp;
+        const float* cf = is_s ? sc : vc;
+        float* gout = is_s ? sbar : vbar;
+#pragma unroll
+        for (int i = 0; i < 16; i += 4) {
+          const float4 f4 = ld4(fb + v * C + cc + i), g4 = ld4(gates + v * 2 * C + c0 + i);
+          const float4 s4 = gn_apply<true>(ld4(pre + v * C + cc + i), gn_coefs(cf, C, cc + i));
+          const float ff[4] = {f4.x, f4.y, f4.z, f4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w},
+                      ss[4] = {s4.x, s4.y, s4.z, s4.w};
+          float o[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const float b = bb[i + u] + 0.5f * ff[u];
+            o[u] = b * gg[u];
+            q[i + u] = b * ss[u] * gg[u] * (1.f - gg[u]);
+          }
+          *reinterpret_cast<float4*>(gout + v * C + cc + i) = make_float4(o[0], o[1], o[2], o[3]);
         }
       }
-      if (f < 2 * C) put_mn(T2, f, 64 * P.half + 16 * c, q);
+      put16(T2, row, c0, 2 * C, q);
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem + TM, wg2t, mop(T2), 2 * C, false})) break;
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
+    if (!pipe_gemms(P, err, Gemm{P.tmem + 2 * C, kop(T2, 2 * C), wg2t, 2 * C, false, C})) break;
+#pragma unroll
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      const int c0 = 16 * j;
       float hb[16];
-      tld(P, TM, c, hb);
-      const long vb = v0 + 64 * P.half + 16 * c;
+      rld(P, 2 * C, j, hb);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const long v = vb + i;
-        hb[i] = (f < C && v < V) ? hb[i] * gelu_grad(__ldg(hg + v * C + f)) : 0.f;
+      for (int i = 0; i < 16; i += 4) {
+        const float4 h4 = v < V ? ld4(hg + v * C + c0 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        hb[i] *= gelu_grad(h4.x);
+        hb[i + 1] *= gelu_grad(h4.y);
+        hb[i + 2] *= gelu_grad(h4.z);
+        hb[i + 3] *= gelu_grad(h4.w);
       }
-      if (f < C) put_mn(T1, f, 64 * P.half + 16 * c, hb);
+      put16(T1, row, c0, C, hb);
     }
-    {
-      const Gemm gb{P.tmem + TM, wg1b, mop(T1), C, false};
-      if (!pipe_gemms(P, err, Gemm{P.tmem, wg1a, mop(T1), C, false}, 3 * C > TM ? &gb : nullptr)) break;
-    }
-    // rows r of A_bar: r < C -> x_bar, r < 2C -> spec_bar, r < 3C -> vert_bar; accumulator rows 0..127 then 128..
-#pragma unroll 1
-    for (int part = 0; part < 2; ++part) {
-      const int r = f + TM * part;
-      if (part == 1 && 3 * C <= TM) break;
-#pragma unroll 1
-      for (int c = 0; c < 4; ++c) {
-        float a[16];
-        tld(P, TM * part, c, a);
-        const long vb = v0 + 64 * P.half + 16 * c;
-        if (r < 3 * C)
+    if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T1, C), wg1t, C, false, 3 * C})) break;
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const long v = vb + i;
-            if (v < V) {
-              if (r < C)
-                xbar[v * C + r] = base ? a[i] + __ldg(base + v * C + r) : a[i];
-              else if (r < 2 * C)
-                sbar[v * C + r - C] += a[i];
-              else
-                vbar[v * C + r - 2 * C] += a[i];
+    for (int j = 0; j < (3 * C) / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      const int c0 = 16 * j;
+      float r[16];
+      rld(P, 0, j, r);
+      if (v < V) {
+        if (c0 < C) {
+#pragma unroll
+          for (int i = 0; i < 16; i += 4) {
+            float4 o = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
+            if (base) {
+              const float4 b4 = ld4(base + v * C + c0 + i);
+              o = make_float4(o.x + b4.x, o.y + b4.y, o.z + b4.z, o.w + b4.w);
             }
+            *reinterpret_cast<float4*>(xbar + v * C + c0 + i) = o;
           }
+        } else {
+          float* g = c0 < 2 * C ? sbar : vbar;
+          const int cc = c0 < 2 * C ? c0 - C : c0 - 2 * C;
+#pragma unroll
+          for (int i = 0; i < 16; i += 4) {
+            float4* pp = reinterpret_cast<float4*>(g + v * C + cc + i);
+            float4 o = *pp;
+            o = make_float4(o.x + r[i], o.y + r[i + 1], o.z + r[i + 2], o.w + r[i + 3]);
+            *pp = o;
+          }
+        }
       }
     }
   }
@@ -1075,7 +1192,7 @@ int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z_bar)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   TC_DISPATCH(C, {
-    const size_t smem = 4 * mat_bytes(CC, CC) + 2 * tile_bytes(CC);
+    const size_t smem = 4 * mat_bytes(CC, CC) + 4 * tile_bytes(CC);
     if (!launch_prep(k_gate_bwd_tc<CC>, smem)) return FFNO_ELAUNCH;
     k_gate_bwd_tc<CC><<<grid_tc(V), CT, smem, s>>>(x, g_bar, base, V, static_cast<const uint8_t*>(wpack), zp, x_bar,
                                                   z_bar, err);
