@@ -753,8 +753,9 @@ __global__ void k_depth_weights_bwd(const float* __restrict__ z, const float* __
 __global__ void __launch_bounds__(NT) k_outer(const float* __restrict__ A, long lda, int Ma,
                                               const float* __restrict__ B, long ldb, int Mb, long N, long chunk,
                                               int ti, int tj, float* __restrict__ part) {
-  __shared__ float as[64][17];
-  __shared__ float bs[64][17];
+  // 64 x 64 output tile, k in chunks of 64 read as float4 (16 threads per row: 256 contiguous bytes)
+  __shared__ float as[64][65];
+  __shared__ float bs[64][65];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   long bid = blockIdx.x;
   const int bi = (int)(bid % ti);
@@ -768,17 +769,39 @@ __global__ void __launch_bounds__(NT) k_outer(const float* __restrict__ A, long 
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
-  for (long k0 = n0; k0 < n1; k0 += 16) {
-    for (int e = threadIdx.x; e < 64 * 16; e += NT) {
-      const int r = e / 16, c = e % 16;
+  for (long k0 = n0; k0 < n1; k0 += 64) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = threadIdx.x + u * NT;
+      const int r = e >> 4, c = (e & 15) * 4;
       const long n = k0 + c;
       const int i = bi * 64 + r, j = bj * 64 + r;
-      as[r][c] = (i < Ma && n < n1) ? __ldg(A + (long)i * lda + n) : 0.f;
-      bs[r][c] = (j < Mb && n < n1) ? __ldg(B + (long)j * ldb + n) : 0.f;
+      float4 va = make_float4(0.f, 0.f, 0.f, 0.f), vb = va;
+      if (n + 3 < n1) {
+        if (i < Ma) va = __ldg(reinterpret_cast<const float4*>(A + (long)i * lda + n));
+        if (j < Mb) vb = __ldg(reinterpret_cast<const float4*>(B + (long)j * ldb + n));
+      } else {
+        float ta[4] = {0.f, 0.f, 0.f, 0.f}, tb[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int q = 0; q < 4; ++q)
+          if (n + q < n1) {
+            if (i < Ma) ta[q] = __ldg(A + (long)i * lda + n + q);
+            if (j < Mb) tb[q] = __ldg(B + (long)j * ldb + n + q);
+          }
+        va = make_float4(ta[0], ta[1], ta[2], ta[3]);
+        vb = make_float4(tb[0], tb[1], tb[2], tb[3]);
+      }
+      as[r][c] = va.x;
+      as[r][c + 1] = va.y;
+      as[r][c + 2] = va.z;
+      as[r][c + 3] = va.w;
+      bs[r][c] = vb.x;
+      bs[r][c + 1] = vb.y;
+      bs[r][c + 2] = vb.z;
+      bs[r][c + 3] = vb.w;
     }
     __syncthreads();
-#pragma unroll
-    for (int k = 0; k < 16; ++k) {
+#pragma unroll 16
+    for (int k = 0; k < 64; ++k) {
       float a[4], b[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
@@ -966,7 +989,7 @@ int ffno_depth_weights_bwd(const float* z, const float* w_bar, int D, long HW, f
 
 int ffno_outer_parts(int Ma, int Mb, long N) {
   const long tiles = (long)((Ma + 63) / 64) * ((Mb + 63) / 64);
-  long nsplit = (2L * sms() + tiles - 1) / tiles;
+  long nsplit = (4L * sms() + tiles - 1) / tiles;
   const long maxs = (N + 1023) / 1024;
   if (nsplit > maxs) nsplit = maxs;
   if (nsplit < 1) nsplit = 1;
@@ -977,8 +1000,10 @@ int ffno_outer(const float* A, long lda, int Ma, const float* B, long ldb, int M
                double* out, int accumulate, ffno_stream_t stream) {
   if (!A || !B || !part || !out || Ma < 1 || Mb < 1 || N < 1 || nsplit < 1) return FFNO_EINVAL;
   const int ti = (Ma + 63) / 64, tj = (Mb + 63) / 64;
+  if (lda % 4 || ldb % 4 || (reinterpret_cast<uintptr_t>(A) % 16) || (reinterpret_cast<uintptr_t>(B) % 16))
+    return FFNO_EINVAL;   // float4 loads
   long chunk = (N + nsplit - 1) / nsplit;
-  chunk = (chunk + 15) / 16 * 16;
+  chunk = (chunk + 63) / 64 * 64;
   cudaStream_t s = (cudaStream_t)stream;
   k_outer<<<(unsigned)((long)ti * tj * nsplit), NT, 0, s>>>(A, lda, Ma, B, ldb, Mb, N, chunk, ti, tj, part);
   const long n = (long)Ma * Mb;
@@ -1012,6 +1037,8 @@ int ffno_outer_noalloc(const float* A, long lda, int Ma, const float* B, long ld
   if (!A || !B || !out || Ma < 1 || Mb < 1 || N < 1) return FFNO_EINVAL;
   const long n = (long)Ma * Mb;
   if (n > kOuterScratchFloats) return FFNO_ETOOBIG;
+  if (lda % 4 || ldb % 4 || (reinterpret_cast<uintptr_t>(A) % 16) || (reinterpret_cast<uintptr_t>(B) % 16))
+    return FFNO_EINVAL;   // k_outer reads float4
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return FFNO_EINVAL;
   float* scratch = nullptr;
@@ -1030,7 +1057,7 @@ int ffno_outer_noalloc(const float* A, long lda, int Ma, const float* B, long ld
   if (nsplit > kOuterScratchFloats / n) nsplit = kOuterScratchFloats / n;
   const int ti = (Ma + 63) / 64, tj = (Mb + 63) / 64;
   long chunk = (N + nsplit - 1) / nsplit;
-  chunk = (chunk + 15) / 16 * 16;
+  chunk = (chunk + 63) / 64 * 64;
   cudaStream_t s = (cudaStream_t)stream;
   // every partial sum the reduction reads is written first by k_outer: nothing in the scratch has to start at zero
   k_outer<<<(unsigned)((long)ti * tj * nsplit), NT, 0, s>>>(A, lda, Ma, B, ldb, Mb, N, chunk, ti, tj, scratch);

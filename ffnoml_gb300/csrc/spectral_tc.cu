@@ -1,11 +1,12 @@
 // Tensor-core (tcgen05, split-BF16) versions of the spectral kernels: the batched transform GEMM that carries every
 // DFT of the path (same ffno_xform_desc contract as spectral_f32.cu) and the per-frequency channel mixing.
 //
-// Transform GEMM: out[b][m][n] = sum_k T[m][k] in[b][k][n]. A CTA owns one (batch, 128-column n-tile) and all of M
-// (at most two 128-row MMA tiles). K runs in chunks of 64 through a two-stage pipeline: the T chunk (split BF16,
-// pre-packed per (m-tile, k-chunk) in the canonical K-major order) arrives by bulk copy while the threads convert the
-// FP32 data chunk into a split MN-major tile (n contiguous, as it lies in HBM); the MMAs of chunk c run while chunk
-// c + 1 is staged. Accumulators live in tensor memory (<= 2 x 128 columns).
+// Transform GEMM: out[b][m][n] = sum_k T[m][k] in[b][k][n], computed transposed, D^T [128 data columns][M] = X^T T^T,
+// so that tensor-memory lanes are data columns and the stores of a warp cover 32 consecutive columns of one output
+// row. Data chunks of 64 rows k are converted from FP32 HBM into split MN-major tiles (the columns are contiguous in
+// HBM); the split table is either resident in shared memory (k_xform_rt, tables up to 80 KB: the W and height
+// transforms) or streamed per k-chunk next to the data (k_xform_st: the H transforms). Accumulators live in tensor
+// memory (<= 256 columns per pipeline).
 #include <cudaTypedefs.h>
 
 #include "common.cuh"
@@ -15,184 +16,17 @@ using namespace ffno;
 
 namespace {
 
-constexpr int XT = 256;    // threads
-constexpr int XNT = 128;   // n columns per tile
-constexpr int XKC = 64;    // k per chunk
-constexpr int XMT = 2;     // max m tiles of 128
+constexpr int XT = 256;    // threads of the mixing kernel
+constexpr int XKC = 64;    // k per chunk of the streamed table pack
+constexpr int XMT = 2;     // max m tiles of 128 (a transform call has at most 256 output rows)
 
-__host__ __device__ constexpr uint32_t a_chunk_bytes(int kc) { return 128u * kc * 2 * 2; }  // split hi + lo
-__host__ __device__ constexpr uint32_t b_chunk_bytes(int kc) { return (uint32_t)XNT * kc * 2 * 2; }
-
-struct XPipe {
-  uint64_t* bar_a;    // [2] T chunk arrived
-  uint64_t* bar_m;    // [2] MMAs of the chunk in this buffer finished
-};
+// one (m-tile, k-chunk) block of the streamed table pack: 128 rows x kc, split hi + lo
+__host__ __device__ constexpr uint32_t a_chunk_bytes(int kc) { return 128u * kc * 2 * 2; }
 
 __device__ __forceinline__ bool bounded(bool ok, int* err, int code) {
   const bool all = __syncthreads_and(ok) != 0;
   if (!all && threadIdx.x == 0) atomicExch(err, code);
   return all;
-}
-
-__global__ void __launch_bounds__(XT) k_xform_tc(const uint8_t* __restrict__ tpack, const float* __restrict__ in,
-                                                 float* __restrict__ out, ffno_xform_desc d, int Kp, long ntn,
-                                                 int accumulate, int* __restrict__ err) {
-  extern __shared__ __align__(1024) uint8_t smem[];
-  const int MT = (d.M + 127) / 128;
-  const int nchunks = (Kp + XKC - 1) / XKC;
-  const uint32_t stageA = XMT * a_chunk_bytes(XKC), stageB = b_chunk_bytes(XKC);
-  uint8_t* sA[2] = {smem, smem + stageA + stageB};
-  uint8_t* sB[2] = {smem + stageA, smem + 2 * stageA + stageB};
-  __shared__ uint64_t bars[4];
-  __shared__ uint32_t tslot;
-  const int tid = threadIdx.x;
-  if (tid < 32) tc::tmem_alloc(&tslot, 256);
-  if (tid == 0) {
-    for (int i = 0; i < 4; ++i) tc::mbar_init(&bars[i], 1);
-    tc::mbar_init_fence();
-  }
-  tc::tc_before_sync();
-  __syncthreads();
-  tc::tc_after_sync();
-  const uint32_t tmem = tslot;
-  XPipe P{bars, bars + 2};
-  const long items = ntn * d.nb;
-  long g = 0;  // global chunk counter: buffer g & 1, use (g >> 1) of that buffer
-  bool ok = true;
-  const int row = tid & 127, wg = tid >> 7;
-  const uint32_t lb = (uint32_t)(32 * ((tid >> 5) & 3)) << 16;
-  const uint32_t mt_bytes = (uint32_t)128 * Kp * 2 * 2;  // one m-tile of the pack (all chunks)
-  for (long it = blockIdx.x; ok && it < items; it += gridDim.x) {
-    const long b = it / ntn, tn = it % ntn;
-    const long b1 = b / d.nb2, b2 = b % d.nb2;
-    const float* ib = in + b1 * d.in_b1 + b2 * d.in_b2;
-    float* ob = out + b1 * d.out_b1 + b2 * d.out_b2;
-    const long n0 = tn * XNT;
-    {  // L2 prefetch of the next item's rows (one row of up to 128 columns per thread)
-      const long nx = it + gridDim.x;
-      if (nx < items && tid < d.K) {
-        const long bn = nx / ntn, tnn = nx % ntn;
-        const long nn0 = tnn * XNT, cols = (d.N - nn0) < XNT ? (d.N - nn0) : XNT;
-        const float* src = in + (bn / d.nb2) * d.in_b1 + (bn % d.nb2) * d.in_b2 +
-                           (long)(tid / d.in_split) * d.in_hi + (long)(tid % d.in_split) * d.in_lo + nn0;
-        tc::prefetch_l2(src, (uint32_t)(cols * 4));
-      }
-    }
-    for (int c = 0; c < nchunks; ++c, ++g) {
-      const int s = (int)(g & 1);
-      const int k0 = c * XKC, kc = (Kp - k0) < XKC ? (Kp - k0) : XKC;
-      // buffer s is free once the MMAs of chunk g - 2 are done
-      if (g >= 2) {
-        const bool w = tc::mbar_wait(&P.bar_m[s], (uint32_t)(((g - 2) >> 1) & 1));
-        if (!(ok = bounded(w, err, 3))) break;
-      }
-      if (tid == 0) {
-        const uint32_t bytes = a_chunk_bytes(kc);
-        tc::mbar_arrive_expect_tx(&P.bar_a[s], bytes * MT);
-        for (int mt = 0; mt < MT; ++mt)
-          tc::bulk_g2s(sA[s] + mt * a_chunk_bytes(XKC), tpack + (size_t)mt * mt_bytes + (size_t)c * a_chunk_bytes(XKC),
-                       bytes, &P.bar_a[s]);
-      }
-      // data chunk: rows k0 .. k0 + kc (zero past K), columns n0 .. n0 + 127 (zero past N) -> split MN-major tile;
-      // four independent loads in flight per thread before any conversion
-      {
-        const uint32_t half = (uint32_t)XNT * kc * 2;
-        const int ne = kc * XNT / 4;
-        for (int e0 = tid; e0 < ne; e0 += 4 * XT) {
-          float4 v[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const int e = e0 + u * XT;
-            const int kk = e / (XNT / 4), nn = 4 * (e % (XNT / 4));
-            const int k = k0 + kk;
-            const long n = n0 + nn;
-            v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (e < ne && k < d.K && n < d.N)
-              v[u] = __ldg(reinterpret_cast<const float4*>(ib + (long)(k / d.in_split) * d.in_hi +
-                                                           (long)(k % d.in_split) * d.in_lo + n));
-          }
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const int e = e0 + u * XT;
-            if (e >= ne) break;
-            const int kk = e / (XNT / 4), nn = 4 * (e % (XNT / 4));
-            uint32_t h0, l0, h1, l1;
-            tc::split_pack(v[u].x, v[u].y, h0, l0);
-            tc::split_pack(v[u].z, v[u].w, h1, l1);
-            const uint32_t off = tc::mnmajor_offset(nn, kk, XNT);
-            *reinterpret_cast<uint2*>(sB[s] + off) = make_uint2(h0, h1);
-            *reinterpret_cast<uint2*>(sB[s] + half + off) = make_uint2(l0, l1);
-          }
-        }
-      }
-      tc::fence_async_smem();
-      const bool wa = tc::mbar_wait(&P.bar_a[s], (uint32_t)((g >> 1) & 1));
-      tc::tc_before_sync();
-      if (!(ok = bounded(wa, err, 1))) break;
-      tc::tc_after_sync();
-      if (tid == 0) {
-        const uint32_t bh = tc::smem_u32(sB[s]), bl = bh + (uint32_t)XNT * kc * 2;
-        for (int mt = 0; mt < MT; ++mt) {
-          const uint32_t ah = tc::smem_u32(sA[s] + mt * a_chunk_bytes(XKC)), al = ah + 128u * kc * 2;
-          const uint32_t dcol = tmem + mt * XNT;
-          tc::gemm_128xN_bmn(dcol, ah, bh, kc, XNT, c > 0);
-          tc::gemm_128xN_bmn(dcol, ah, bl, kc, XNT, true);
-          tc::gemm_128xN_bmn(dcol, al, bh, kc, XNT, true);
-        }
-        tc::mma_commit(&P.bar_m[s]);
-      }
-    }
-    if (!ok) break;
-    // all MMAs of this item: the last chunk's commit covers every earlier MMA of this thread
-    {
-      const long gl = g - 1;
-      const bool w = tc::mbar_wait(&P.bar_m[gl & 1], (uint32_t)((gl >> 1) & 1));
-      if (!(ok = bounded(w, err, 3))) break;
-      tc::tc_after_sync();
-    }
-    for (int mt = 0; mt < MT; ++mt) {
-      const int m = mt * 128 + row;
-      const long off = (long)(m / d.out_split) * d.out_hi + (long)(m % d.out_split) * d.out_lo;
-#pragma unroll
-      for (int jj = 0; jj < XNT / 16; ++jj) {
-        if ((jj & 1) != wg) continue;
-        float v[16];
-        tc::tmem_ld16(tmem + mt * XNT + lb + 16 * jj, v);
-        const long n = n0 + 16 * jj;
-        if (m < d.M) {
-          float* dst = ob + off + n;
-          if (n + 15 < d.N) {
-#pragma unroll
-            for (int i = 0; i < 16; i += 4) {
-              float4 o = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-              if (accumulate) {
-                const float4 p = *reinterpret_cast<float4*>(dst + i);
-                o.x += p.x;
-                o.y += p.y;
-                o.z += p.z;
-                o.w += p.w;
-              }
-              *reinterpret_cast<float4*>(dst + i) = o;
-            }
-          } else {
-            for (int i = 0; i < 16 && n + i < d.N; ++i) dst[i] = accumulate ? dst[i] + v[i] : v[i];
-          }
-        }
-      }
-    }
-    tc::tc_before_sync();
-    __syncthreads();
-    tc::tc_after_sync();
-  }
-  // leave no bulk copy or MMA in flight before freeing tensor memory
-  if (!ok) {
-    tc::mbar_wait(&P.bar_m[0], 0);
-    tc::mbar_wait(&P.bar_m[1], 0);
-  }
-  tc::tc_before_sync();
-  __syncthreads();
-  tc::tc_after_sync();
-  if (tid < 32) tc::tmem_free(tmem, 256);
 }
 
 // ------------------------------------------------------------------------------------------- resident table
@@ -379,6 +213,179 @@ __global__ void __launch_bounds__(2 * RT, 1)
   __syncthreads();
   tc::tc_after_sync();
   if (warp == 0) tc::tmem_free(tslot, 512);
+}
+
+// ------------------------------------------------------------------------------------------- streamed table
+// The transposed transform GEMM of k_xform_rt for tables too large to keep resident (the H transforms, K = M = 2H):
+// per 64-row k-chunk the table slice [MT * 128][kc] (from the m-tile / k-chunk pack of ffno_xform_tc) arrives by
+// bulk copies into the stage next to the data chunk, both double-buffered against the MMAs. One pipeline of 256
+// threads per CTA (the table stages fill shared memory).
+__global__ void __launch_bounds__(RT, 1)
+    k_xform_st(const uint8_t* __restrict__ tpack, int MT, int Kp, const float* __restrict__ in, float* __restrict__ out,
+               ffno_xform_desc d, int nbi, int nshift, long ntn, long items, int accumulate, int* __restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t TSB = (uint32_t)MT * 128u * RKC * 2;        // one split half of a table stage
+  uint8_t* sD = base;                                        // [stage][hi | lo], 2 * RSB each
+  uint8_t* sT = base + 4 * RSB;                              // [stage][hi | lo], 2 * TSB each
+  __shared__ uint64_t bar_t[2], bar_m[2];
+  __shared__ uint32_t tslot;
+  __shared__ long row_in[RT_MAXK], row_out[256];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, q = warp & 3, half = tid >> 7;
+  const int Mp = MT * 128;
+  for (int k = tid; k < Kp; k += RT) row_in[k] = (long)(k / d.in_split) * d.in_hi + (long)(k % d.in_split) * d.in_lo;
+  for (int m = tid; m < Mp; m += RT) row_out[m] = (long)(m / d.out_split) * d.out_hi + (long)(m % d.out_split) * d.out_lo;
+  if (warp == 0) tc::tmem_alloc(&tslot, 256);
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&bar_t[i], 1);
+      tc::mbar_init(&bar_m[i], 1);
+    }
+    tc::mbar_init_fence();
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  const uint32_t tmem = tslot;
+  const uint32_t lq = (uint32_t)(32 * q) << 16;
+  const int nch = (Kp + RKC - 1) / RKC;
+  const uint32_t idesc = tc::idesc_bf16_ab(128, Mp, true, false);
+  const uint32_t mt_bytes = (uint32_t)128 * Kp * 2 * 2;
+  bool ok = true;
+  uint32_t g = 0;
+  const int n_ep = 32 * q + lane;
+  for (long it = blockIdx.x; ok && it < items; it += gridDim.x) {
+    long bfirst, n0;
+    if (nbi > 1) {
+      bfirst = it * nbi;
+      n0 = 0;
+    } else {
+      bfirst = it / ntn;
+      n0 = (it % ntn) * 128;
+    }
+    const int nf = 8 * (2 * ((tid >> 5) & 7) + (lane >> 4)) + 4 * ((lane >> 3) & 1);
+    long foff = 0;
+    bool fv;
+    {
+      long b, c;
+      if (nbi > 1) {
+        b = bfirst + (nf >> nshift);
+        c = nf & ((1 << nshift) - 1);
+      } else {
+        b = bfirst;
+        c = n0 + nf;
+      }
+      fv = b < d.nb && c < d.N;
+      if (fv) foff = (b / d.nb2) * d.in_b1 + (b % d.nb2) * d.in_b2 + c;
+    }
+    const float* fsrc = in + foff;
+    for (int ch = 0; ch < nch; ++ch, ++g) {
+      const int s = (int)(g & 1u);
+      const int k0 = ch * RKC, kc = (Kp - k0) < RKC ? (Kp - k0) : RKC;
+      if (g >= 2) {
+        const bool w = tc::mbar_wait(&bar_m[s], ((g - 2) >> 1) & 1u);
+        if (!(ok = bounded(w, err, 3))) break;
+      }
+      uint8_t* st = sD + (uint32_t)s * 2u * RSB;
+      uint8_t* tt = sT + (uint32_t)s * 2u * TSB;
+      if (tid == 0) {   // the table slice of this chunk: m-tiles stacked, hi then lo
+        const uint32_t part = 128u * kc * 2;
+        tc::mbar_arrive_expect_tx(&bar_t[s], 2u * MT * part);
+        for (int mt = 0; mt < MT; ++mt) {
+          const uint8_t* src = tpack + (size_t)mt * mt_bytes + (size_t)ch * a_chunk_bytes(XKC);
+          tc::bulk_g2s(tt + mt * part, src, part, &bar_t[s]);
+          tc::bulk_g2s(tt + (uint32_t)MT * part + mt * part, src + part, part, &bar_t[s]);
+        }
+      }
+      for (int e0 = tid; e0 < kc * 32; e0 += 4 * RT) {
+        float4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = e0 + u * RT;
+          const int k = k0 + 8 * (e >> 8) + (lane & 7);
+          v[u] = (e < kc * 32 && k < d.K && fv) ? __ldg(reinterpret_cast<const float4*>(fsrc + row_in[k]))
+                                                : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = e0 + u * RT;
+          if (e >= kc * 32) break;
+          uint32_t h0, l0, h1, l1;
+          tc::split_pack(v[u].x, v[u].y, h0, l0);
+          tc::split_pack(v[u].z, v[u].w, h1, l1);
+          const uint32_t o = tc::mnmajor_offset(nf, 8 * (e >> 8) + (lane & 7), 128);
+          *reinterpret_cast<uint2*>(st + o) = make_uint2(h0, h1);
+          *reinterpret_cast<uint2*>(st + RSB + o) = make_uint2(l0, l1);
+        }
+      }
+      tc::fence_async_smem();
+      const bool wt = tc::mbar_wait(&bar_t[s], (g >> 1) & 1u);
+      tc::tc_before_sync();
+      if (!(ok = bounded(wt, err, 1))) break;
+      tc::tc_after_sync();
+      if (tid == 0) {
+        const uint32_t x_hi = tc::smem_u32(st), x_lo = x_hi + RSB;
+        const uint32_t t_hi = tc::smem_u32(tt), t_lo = t_hi + (uint32_t)MT * 128u * kc * 2;
+        const uint32_t as[3] = {x_hi, x_hi, x_lo}, bs[3] = {t_hi, t_lo, t_hi};
+#pragma unroll
+        for (int ps = 0; ps < 3; ++ps)
+          for (int kk = 0; kk < kc; kk += 16) {
+            const uint64_t ad = tc::mnmajor_desc(as[ps] + (uint32_t)(kk / 8) * 2048u, 2048u, 128u);
+            const uint64_t bd = tc::kmajor_desc(bs[ps] + (uint32_t)(kk / 8) * 128u, 128u, (uint32_t)kc * 16u);
+            tc::mma_bf16(tmem, ad, bd, idesc, (ch > 0 || ps > 0 || kk > 0) ? 1u : 0u);
+          }
+        tc::mma_commit(&bar_m[s]);
+      }
+    }
+    if (!ok) break;
+    {
+      const uint32_t gl = g - 1;
+      const bool w = tc::mbar_wait(&bar_m[gl & 1u], (gl >> 1) & 1u);
+      if (!(ok = bounded(w, err, 3))) break;
+      tc::tc_after_sync();
+    }
+    long obase = 0;
+    bool nv;
+    {
+      long b, c;
+      if (nbi > 1) {
+        b = bfirst + (n_ep >> nshift);
+        c = n_ep & ((1 << nshift) - 1);
+      } else {
+        b = bfirst;
+        c = n0 + n_ep;
+      }
+      nv = b < d.nb && c < d.N;
+      if (nv) obase = (b / d.nb2) * d.out_b1 + (b % d.nb2) * d.out_b2 + c;
+    }
+    for (int jj = half; jj < Mp / 16; jj += 2) {
+      float v[16];
+      tc::tmem_ld16(tmem + lq + 16u * jj, v);
+      if (nv) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int m = 16 * jj + i;
+          if (m < d.M) {
+            float* p = out + obase + row_out[m];
+            *p = accumulate ? *p + v[i] : v[i];
+          }
+        }
+      }
+    }
+    tc::tc_before_sync();
+    __syncthreads();
+    tc::tc_after_sync();
+  }
+  if (!ok) {   // leave no bulk copy or MMA in flight before freeing tensor memory
+    tc::mbar_wait(&bar_t[0], 0);
+    tc::mbar_wait(&bar_t[1], 0);
+    if (g >= 1) tc::mbar_wait(&bar_m[(g - 1) & 1u], ((g - 1) >> 1) & 1u);
+    if (g >= 2) tc::mbar_wait(&bar_m[g & 1u], ((g - 2) >> 1) & 1u);
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  if (warp == 0) tc::tmem_free(tmem, 256);
 }
 
 // ---------------------------------------------------------------------------------------------------- mixing
@@ -679,16 +686,23 @@ int ffno_xform_tc(const void* tpack, const float* in, float* out, const ffno_xfo
       d.out_split < 1)
     return FFNO_EINVAL;
   if (d.N % 4 || d.in_lo % 4 || d.in_hi % 4 || d.in_b1 % 4 || d.in_b2 % 4) return FFNO_EINVAL;  // float4 loads
-  if (d.out_lo % 4 || d.out_hi % 4 || d.out_b1 % 4 || d.out_b2 % 4) return FFNO_EINVAL;
+  if (reinterpret_cast<uintptr_t>(in) % 16) return FFNO_EINVAL;
   const int Kp = (d.K + 15) / 16 * 16;
-  const long ntn = (d.N + XNT - 1) / XNT;
-  const long items = ntn * d.nb;
-  const size_t smem = 2 * ((size_t)XMT * a_chunk_bytes(XKC) + b_chunk_bytes(XKC));
-  if (cudaFuncSetAttribute(k_xform_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (Kp > RT_MAXK) return FFNO_EINVAL;
+  const int MT = (d.M + 127) / 128;
+  int nbi = 1, nshift = 0;
+  if (d.N < 128 && 128 % d.N == 0) {
+    nbi = 128 / (int)d.N;
+    while ((1 << nshift) < d.N) ++nshift;
+  }
+  const long ntn = (d.N + 127) / 128;
+  const long items = nbi > 1 ? (d.nb + nbi - 1) / nbi : d.nb * ntn;
+  const size_t smem = 1024 + 4 * (size_t)RSB + 2 * 2 * (size_t)MT * 128 * RKC * 2;
+  if (cudaFuncSetAttribute(k_xform_st, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return FFNO_ELAUNCH;
   const long grid = items < sms() ? items : sms();
-  k_xform_tc<<<(unsigned)grid, XT, smem, (cudaStream_t)stream>>>(static_cast<const uint8_t*>(tpack), in, out, d, Kp,
-                                                                 ntn, accumulate, err);
+  k_xform_st<<<(unsigned)grid, RT, smem, (cudaStream_t)stream>>>(static_cast<const uint8_t*>(tpack), MT, Kp, in, out,
+                                                                d, nbi, nshift, ntn, items, accumulate, err);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

@@ -206,7 +206,8 @@ int ffno_depth_weights_bwd(const float* z, const float* w_bar, int D, long HW, f
 
 /* out [Ma][Mb] (double; = or +=) = A [Ma][N] (row stride lda) @ B [Mb][N]^T (row stride ldb), split over N into
  * nsplit partial sums held in part [nsplit][Ma][Mb] floats and reduced in a fixed order: the gradients of the height
- * operator's transform tables. ffno_outer_parts gives the nsplit to use. */
+ * operator's transform tables. ffno_outer_parts gives the nsplit to use. A and B 16-byte aligned, lda and ldb
+ * multiples of 4 (the rows are read as float4). */
 int ffno_outer_parts(int Ma, int Mb, long N);
 int ffno_outer(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, float* part, int nsplit,
                double* out, int accumulate, ffno_stream_t stream);
