@@ -90,6 +90,22 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(value, world, device):
+    """The largest of every rank's value (a time: the job ends when its slowest replica does)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t)
+
+
+def job_rate(units_per_rank, world, seconds):
+    """Whole-job throughput of `world` replicas that each processed units_per_rank in (max-over-ranks) seconds."""
+    return world * units_per_rank / seconds
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
 
@@ -322,11 +338,7 @@ def run_gb300(args):
             fn()
         b.record()
         barrier()
-        ms = a.elapsed_time(b)
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t)
+        ms = max_over_ranks(a.elapsed_time(b), world, dev)
         return ms / steps, nat.counter.calls - calls0
 
     # fwd+VJP at the headline precision, device-resident (--fwd-only: the forward alone, a profiling case)
@@ -385,8 +397,8 @@ def run_gb300(args):
         ms32, _ = timed(fwd_vjp, max(2, args.steps // 2), 1)
         ms32f, _ = timed(fwd, max(2, args.steps // 2), 1)
         model.set_precision("bf16")
-        fp32 = {"fwd+vjp": {"value": world * V / (ms32 / 1e3), "unit": "voxels/s", "ms_per_step": ms32},
-                "fwd": {"value": world * V / (ms32f / 1e3), "unit": "voxels/s", "ms_per_step": ms32f},
+        fp32 = {"fwd+vjp": {"value": job_rate(V, world, ms32 / 1e3), "unit": "voxels/s", "ms_per_step": ms32},
+                "fwd": {"value": job_rate(V, world, ms32f / 1e3), "unit": "voxels/s", "ms_per_step": ms32f},
                 "bf16_speedup_fwd+vjp": ms32 / ms_step, "bf16_speedup_fwd": ms32f / ms_fwd,
                 "max_abs_dlog10n_bf16_vs_fp32": dlog}
 
@@ -403,12 +415,8 @@ def run_gb300(args):
         for _ in range(n_e2e):
             backend.vjp_local(f_np, z_np, DXY, DXY, cot_np)
         barrier()
-        e2e_s = (time.perf_counter() - t0) / n_e2e
-        if world > 1:
-            t = torch.tensor([e2e_s], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t)
-        e2e = {"value": world * V / e2e_s, "unit": "voxels/s", "h2d_bytes_per_step": int(f_np.nbytes + z_np.nbytes +
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / n_e2e, world, dev)
+        e2e = {"value": job_rate(V, world, e2e_s), "unit": "voxels/s", "h2d_bytes_per_step": int(f_np.nbytes + z_np.nbytes +
                                                                                             cot_np.nbytes),
                "d2h_bytes_per_step": int(f_np.nbytes + z_np.nbytes), "ms_per_step": 1e3 * e2e_s}
 
@@ -429,7 +437,7 @@ def run_gb300(args):
     flops_vox = algorithmic_flops_per_voxel(WIDTH, LAYERS, D, H, W, MODES, 12, 2)
     if rank == 0:
         line = {
-            "metric": METRIC, "value": world * V / (ms_step / 1e3), "unit": "voxels/s",
+            "metric": METRIC, "value": job_rate(V, world, ms_step / 1e3), "unit": "voxels/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if args.precision == "fp32" else "bf16", "data": "synthetic",
@@ -437,7 +445,7 @@ def run_gb300(args):
                                    ("forward only" if args.fwd_only else "fwd + input VJP (per-block recompute)"),
                        "voxels_per_step": V, "parallelism": f"replicas{world}",
                        "l2": "working set (GBs) >> L2; no flush needed", "precision": args.precision},
-            "fwd": {"value": world * V / (ms_fwd / 1e3), "unit": "voxels/s", "ms_per_step": ms_fwd},
+            "fwd": {"value": job_rate(V, world, ms_fwd / 1e3), "unit": "voxels/s", "ms_per_step": ms_fwd},
             "fp32": fp32,
             "algorithmic_tflops": {"fwd+vjp": 2 * flops_vox * V / (ms_step / 1e3) / 1e12,
                                    "fwd": flops_vox * V / (ms_fwd / 1e3) / 1e12},
