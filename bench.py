@@ -343,9 +343,12 @@ def run_gb300(args):
 
     # fwd+VJP at the headline precision, device-resident (--fwd-only: the forward alone, a profiling case)
     step = fwd if args.fwd_only else fwd_vjp
+    torch.cuda.reset_peak_memory_stats(dev)
     with ClockSampler(local) as clk:
         ms_step, calls = timed(step, args.steps, args.warmup)
     clocks = clk.summary()
+    memory = {"peak_allocated_gib": torch.cuda.max_memory_allocated(dev) / 2 ** 30,
+              "device_total_gib": torch.cuda.get_device_properties(dev).total_memory / 2 ** 30}
     ms_fwd = ms_step if args.fwd_only else timed(fwd, max(args.steps, 3), 1)[0]
 
     # kernel breakdown of one step (CUDA events around every entry point on the launching stream)
@@ -451,7 +454,8 @@ def run_gb300(args):
                                    "fwd": flops_vox * V / (ms_fwd / 1e3) / 1e12},
             "roofline": roof, "roofline_by_entry": dict(sorted(rows.items(), key=lambda kv: -per[kv[0]][0])[:12]),
             "kernel_breakdown_ms": breakdown,
-            "clocks": clocks, "gpu_launches": launches * args.steps, "e2e": e2e, "cpu_baseline": cpu,
+            "clocks": clocks, "memory": memory, "gpu_launches": launches * args.steps, "e2e": e2e,
+            "cpu_baseline": cpu,
             "serving": serving,
         }
         print(json.dumps(line), flush=True)

@@ -264,9 +264,13 @@ class Workspace:
         self.err = torch.zeros(1, dtype=torch.int32, device=device)
         self.coefs = {n: nb(3 * C) for n in ("lift",) + NORMS}
         self.gstats = {n: torch.empty(groups * 3, dtype=torch.float64, device=device) for n in ("lift",) + NORMS}
-        for n in ("x", "pre", "xs", "xv", "ys", "yv", "spec_pre", "vert_pre", "fused_pre", "pw_pre", "mlp_pre",
-                  "x1", "x2"):
+        for n in ("x", "xs", "xv", "yv", "spec_pre", "vert_pre", "fused_pre", "pw_pre", "mlp_pre", "x1", "x2"):
             setattr(self, n, nb(V, C))
+        # buffers whose lives do not overlap share storage: the lift pre-activation is dead before block 0 writes
+        # spec_pre (and, in the VJP, spec_pre is dead when the lift is recomputed); the gated input xs is dead once
+        # the W transform has read it, before the spectral branch writes ys
+        self.pre = self.spec_pre
+        self.ys = self.xs
         spec_len = D * 2 * H * Wf * C
         self.sa, self.sb = nb(spec_len), nb(spec_len)
         self.gates = nb(V, 2 * C)     # branch gates between the two tensor-core fuse stages
@@ -771,9 +775,13 @@ class _GradBuffers:
     def __init__(self, D, H, W, C, live, groups, nparts, device):
         V = D * H * W
         f32 = dict(dtype=torch.float32, device=device)
-        for n in ("xbar", "g2", "g1", "xacc", "sbar", "vbar", "pbar", "ysb", "yvb", "xsb", "xvb", "hg"):
+        for n in ("xbar", "g2", "g1", "xacc", "sbar", "vbar", "pbar", "hg"):
             setattr(self, n, torch.empty(V, C, **f32))
         self.hfb = torch.empty(V, 2 * C, **f32)
+        # within a block's VJP g2 and g1 are dead (after the pw and fuse stages) before the branch post-MLP gradients
+        # ysb, yvb are written, and hg, hfb (fuse stage) before the transform gradients xsb, xvb
+        self.ysb, self.yvb = self.g2, self.g1
+        self.xsb, self.xvb = self.hg, self.hfb.reshape(-1)[:V * C].view(V, C)
         self.wbar = torch.zeros(V, **f32)
         self.bpart = torch.empty(max(nparts, 1) * groups * 2, dtype=torch.float64, device=device)
         self.sums = torch.empty(groups * 2, dtype=torch.float64, device=device)
