@@ -94,6 +94,14 @@ PROTOTYPES = {
     "ffno_gate_bwd_tc": [P, P, P, L, I, P, P, P, P, P, P],
     "ffno_fuse_bwd_a_tc": [P, P, P, P, P, P, L, I, P, P, P, P],
     "ffno_fuse_bwd_b_tc": [P, P, P, P, P, P, P, P, P, L, I, P, P, P, P, P, P],
+    "ffno_gn_jvp_stats": [P, P, P, P, L, I, I, P, I, P],
+    "ffno_gn_jvp_apply": [P, P, P, P, P, P, I, P, F, L, I, I, P, P],
+    "ffno_gate_jvp": [P, P, L, I, P, P, P, P],
+    "ffno_mlp2_jvp": [P, P, L, I, P, P, P, P],
+    "ffno_fuse_jvp": [P, P, P, P, P, P, P, P, L, I, P, P, P, P, P, P, P],
+    "ffno_head_jvp": [P, P, P, P, L, I, P, P, P, I, ctypes.POINTER(HeadParams), P, P],
+    "ffno_si_input_tangent": [P, P, L, P, P, P, P],
+    "ffno_si_population_tangent": [P, P, L, I, P, P, P, P, P],
     "ffno_xform_tc_pack_bytes": [I, I],
     "ffno_xform_tcr_max_table_bytes": [],
     "ffno_xform_tcr": [P, I, I, P, P, ctypes.POINTER(XformDesc), I, P, P],

@@ -574,14 +574,6 @@ __global__ void __launch_bounds__(NT) k_lift_bwd(const float* __restrict__ pb, i
 }
 
 // ------------------------------------------------------------------------------------------------ head backward
-constexpr double kEE = 1.602189e-12, kBK = 1.380662e-16;
-constexpr double kLN10 = 2.302585092994045684;
-
-__device__ __forceinline__ double ln_ccon() {
-  const double hh = 6.626176e-27, em = 9.109534e-28, pi = 3.14159265359;
-  const double a = hh / sqrt(2.0 * pi * em) / sqrt(kBK);
-  return log(0.5 * a * a * a);
-}
 
 template <int C, int NHP>
 __global__ void __launch_bounds__(NT) k_head_bwd(const float* __restrict__ x, const float* __restrict__ xin,

@@ -27,6 +27,17 @@ __device__ __forceinline__ float gelu_grad(float x) {
 
 __device__ __forceinline__ float sigmoid(float x) { return 1.f / (1.f + expf(-x)); }
 
+// MULTI3D constants, cgs (models/ffno_model.py:111-112)
+constexpr double kEE = 1.602189e-12, kBK = 1.380662e-16;
+constexpr double kLN10 = 2.302585092994045684;
+
+__device__ __forceinline__ double ln_ccon() {
+  // log(0.5 * (HH / sqrt(2 pi EM) / sqrt(BK))^3), MULTI3D's Saha constant (models/ffno_model.py:112)
+  const double hh = 6.626176e-27, em = 9.109534e-28, pi = 3.14159265359;
+  const double a = hh / sqrt(2.0 * pi * em) / sqrt(kBK);
+  return log(0.5 * a * a * a);
+}
+
 // acc[i][j] = sum_k A[(ty + 16 i) * lda + k] * W[k * N + tx + 16 j] for i < RM rows per thread (a tile of 16 RM
 // rows); A in shared memory, W (row-major K x N) in global memory (read through L1; every CTA reads the same small
 // weight matrix).

@@ -286,6 +286,7 @@ class Executor:
         self._plane_freq = {}
         self._height = {}
         self._lock = threading.RLock()        # caches are shared by concurrent service slots
+        self._tls = threading.local()         # per-thread mode (a JVP forces the FP32 kernels)
 
     # -------------------------------------------------------------------------------------------- caches
     def packed(self, device):
@@ -584,8 +585,9 @@ class Executor:
                      g.data_ptr(), _ptr(u), _ptr(v), m.freq_mix_rank, s)
 
     def _tc(self):
-        """Whether the split-BF16 tensor-core kernels run (precision 'bf16' at a width they support)."""
-        return self.model.precision == "bf16" and self._packed.tc
+        """Whether the split-BF16 tensor-core kernels run (precision 'bf16' at a width they support; never inside a
+        JVP, which is FP32)."""
+        return self.model.precision == "bf16" and self._packed.tc and not getattr(self._tls, "fp32", False)
 
     def _fuse1_tc(self, ws, bp, x, hg):
         m = self.model
@@ -612,6 +614,111 @@ class Executor:
         V = x.shape[0]
         nat.call("ffno_head_fwd", x.data_ptr(), xin.data_ptr(), V, m.width, pk.p1.data_ptr(), pk.p2.data_ptr(),
                  pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head, out.data_ptr(), None, _stream())
+
+    # -------------------------------------------------------------------------------------------- JVP
+    def jvp(self, x, z_scale, dx, dy, x_dot):
+        """Forward-mode derivative of FFNO3D.forward along the input tangent x_dot (heights fixed; what jvp_local gets
+        from dual tensors, ffno_fsdp_runtime.py:350-372): x, x_dot [B, Cin, D, H, W], z_scale [B, D, H, W] ->
+        (y, y_dot) [B, L, D, H, W] (normalised log10 n). FP32 kernels whatever the model's precision; the primal
+        is computed block by block next to its tangent."""
+        m = self.model
+        x = x.contiguous()
+        z_scale = z_scale.contiguous()
+        x_dot = x_dot.contiguous()
+        if x_dot.shape != x.shape or x_dot.dtype != torch.float32 or x_dot.device != x.device:
+            raise ValueError(f"x_dot must match x: {tuple(x_dot.shape)} {x_dot.dtype} vs {tuple(x.shape)}")
+        self._tls.fp32 = True
+        try:
+            pk, geo, hgt, pln, pfr = self._setup(x, z_scale, dx, dy)
+            B, Cin, D, H, W = x.shape
+            C, V, HW = m.width, D * H * W, H * W
+            dev, s = x.device, _stream()
+            y = torch.empty(B, m.out_channels, D, H, W, dtype=torch.float32, device=dev)
+            out = torch.empty_like(y)
+            ws = tw = None
+            for b in range(B):
+                hgt_b = hgt if geo.shared else self.height_percol(pk, geo, b, dev)
+                if ws is None or ws.live != hgt_b["live"]:
+                    ws = Workspace(D, H, W, C, hgt_b["live"], pk.groups, dev)
+                    tw = _TangentBuffers(D, H, W, C, hgt_b["live"], pk.groups, ws.nparts, dev)
+                xin, z, xin_dot = x[b], z_scale[b], x_dot[b]
+                self._depth_weights(ws, z, D, HW)
+                self._lift(pk, ws, xin)
+                nat.call("ffno_lift_fwd", xin_dot.data_ptr(), Cin, V, C, pk.lift_w.data_ptr(), ws.dw.data_ptr(),
+                         tw.pre.data_ptr(), tw.scratch_parts.data_ptr(), ws.nparts, pk.groups, s)
+                self._gn_jvp(ws, tw, ws.pre, tw.pre, pk.lift_g, pk.lift_b, "lift", 1, None, 1.0, tw.x)
+                for i in range(m.n_layers):
+                    tw.xp.copy_(ws.x)
+                    self._block(pk, ws, i, z, D, H, W, hgt_b, pln, pfr[i], x_in=tw.xp)
+                    self._block_jvp(pk, ws, tw, i, tw.xp, D, H, W, hgt_b, pln, pfr[i])
+                self._head(pk, ws.x, xin, y[b])
+                nat.call("ffno_head_jvp", ws.x.data_ptr(), tw.x.data_ptr(), xin.data_ptr(), xin_dot.data_ptr(), V, C,
+                         pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.nhp, pk.head, out[b].data_ptr(), s)
+            self._check(ws)
+        finally:
+            self._tls.fp32 = False
+        return y, out
+
+    def _gn_jvp(self, ws, tw, pre, pre_dot, gamma, beta, name, act, base, res, out):
+        m = self.model
+        G, s = self._packed.groups, _stream()
+        nat.call("ffno_gn_jvp_stats", pre.data_ptr(), pre_dot.data_ptr(), ws.gstats[name].data_ptr(),
+                 ws.dw.data_ptr(), ws.V, m.width, G, tw.parts.data_ptr(), ws.nparts, s)
+        nat.call("ffno_gn_bwd_final", tw.parts.data_ptr(), ws.nparts, G, tw.sums.data_ptr(), s)
+        nat.call("ffno_gn_jvp_apply", pre.data_ptr(), pre_dot.data_ptr(), gamma.data_ptr(), beta.data_ptr(),
+                 ws.gstats[name].data_ptr(), tw.sums.data_ptr(), act, _ptr(base), res, ws.V, m.width, G,
+                 out.data_ptr(), s)
+
+    def _block_jvp(self, pk, ws, tw, i, x, D, H, W, hgt, pln, fq):
+        """Tangent of block i: tw.x (tangent of its input x) -> tw.x (tangent of its output), with the primal
+        intermediates of the same block in ws."""
+        m = self.model
+        C, V, HW, Wf = m.width, ws.V, H * W, W // 2 + 1
+        s = _stream()
+        bp = pk.blocks[i]
+        r_f, r_pw, r_mlp = bp["res"]
+        live = hgt["live"]
+        d = _descs(D, H, W, C, live)
+        nat.call("ffno_gate_jvp", x.data_ptr(), tw.x.data_ptr(), V, C, bp["s_g1"].data_ptr(), bp["s_g2"].data_ptr(),
+                 tw.xs.data_ptr(), s)
+        nat.call("ffno_gate_jvp", x.data_ptr(), tw.x.data_ptr(), V, C, bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(),
+                 tw.xv.data_ptr(), s)
+        # the spectral operators are linear in their input: the forward kernels on the tangent
+        self._xf(pln, "twf", tw.xs, tw.sa, d["wf"], ws)
+        self._xf(pln, "thf", tw.sa, tw.sb, d["hf"], ws)
+        self._mix(ws, "s", bp, fq, tw.sb, tw.sa, H * Wf, D, C, 2 * H * Wf * C, H * Wf * C, False)
+        self._xf(pln, "thi", tw.sa, tw.sb, d["hf"], ws)
+        self._xf(pln, "twi", tw.sb, tw.ys, d["wi"], ws)
+        nat.call("ffno_mlp2_jvp", ws.ys.data_ptr(), tw.ys.data_ptr(), V, C, bp["s_p1"].data_ptr(),
+                 bp["s_p2"].data_ptr(), tw.spec_pre.data_ptr(), s)
+        hq = hgt["freq"][i]
+        if hgt.get("percol"):
+            nat.call("ffno_xform_pt", hgt["tzf"].data_ptr(), 2 * live * D, tw.xv.data_ptr(), tw.va.data_ptr(),
+                     d["pcf"], 0, s)
+            self._mix(ws, "v", bp, hq, tw.va, tw.vb, live, HW, HW * C, C, live * HW * C, False)
+            nat.call("ffno_xform_pt", hgt["tzi"].data_ptr(), 2 * live * D, tw.vb.data_ptr(), tw.yv.data_ptr(),
+                     d["pci"], 0, s)
+        else:
+            self._xf(hgt, "tzf", tw.xv, tw.va, d["zf"], ws)
+            self._mix(ws, "v", bp, hq, tw.va, tw.vb, live, HW, HW * C, C, live * HW * C, False)
+            self._xf(hgt, "tzi", tw.vb, tw.yv, d["zi"], ws)
+        nat.call("ffno_mlp2_jvp", ws.yv.data_ptr(), tw.yv.data_ptr(), V, C, bp["v_p1"].data_ptr(),
+                 bp["v_p2"].data_ptr(), tw.vert_pre.data_ptr(), s)
+        # branch outputs gelu(GN(.)), then gate + fuse
+        self._gn_jvp(ws, tw, ws.spec_pre, tw.spec_pre, bp["spec_g"], bp["spec_b"], "spec", 1, None, 1.0, tw.sd)
+        self._gn_jvp(ws, tw, ws.vert_pre, tw.vert_pre, bp["vert_g"], bp["vert_b"], "vert", 1, None, 1.0, tw.vd)
+        nat.call("ffno_fuse_jvp", x.data_ptr(), tw.x.data_ptr(), ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(),
+                 ws.vert_pre.data_ptr(), ws.coefs["vert"].data_ptr(), tw.sd.data_ptr(), tw.vd.data_ptr(), V, C,
+                 bp["bg1"].data_ptr(), bp["bg2"].data_ptr(), bp["bgb"].data_ptr(), bp["f1"].data_ptr(),
+                 bp["f2"].data_ptr(), tw.fused.data_ptr(), s)
+        # residual tail: x1 = x + r_f gelu(GN(fused)), x2 = x1 + r_pw GN(pw(x1)), out = x2 + r_mlp GN(mlp(x2))
+        self._gn_jvp(ws, tw, ws.fused_pre, tw.fused, bp["fuse_g"], bp["fuse_b"], "fuse", 1, tw.x, r_f, tw.x1)
+        nat.call("ffno_mlp2_jvp", ws.x1.data_ptr(), tw.x1.data_ptr(), V, C, bp["pw1"].data_ptr(), bp["pw2"].data_ptr(),
+                 tw.pw.data_ptr(), s)
+        self._gn_jvp(ws, tw, ws.pw_pre, tw.pw, bp["pw_g"], bp["pw_b"], "pw", 0, tw.x1, r_pw, tw.x2)
+        nat.call("ffno_mlp2_jvp", ws.x2.data_ptr(), tw.x2.data_ptr(), V, C, bp["m1"].data_ptr(), bp["m2"].data_ptr(),
+                 tw.mlp.data_ptr(), s)
+        self._gn_jvp(ws, tw, ws.mlp_pre, tw.mlp, bp["mlp_g"], bp["mlp_b"], "mlp", 0, tw.x2, r_mlp, tw.x)
 
     # -------------------------------------------------------------------------------------------- VJP
     def backward(self, state, ybar):
@@ -792,6 +899,28 @@ class _GradBuffers:
         self.opart = torch.empty(max(self.osplit_i, self.osplit_f) * D * 2 * live, **f32)
 
 
+class _TangentBuffers:
+    """Tangent twins of the forward intermediates of one cube (JVP), with buffers whose lives do not overlap
+    sharing storage."""
+
+    def __init__(self, D, H, W, C, live, groups, nparts, device):
+        V, HW, Wf = D * H * W, H * W, W // 2 + 1
+        f32 = dict(dtype=torch.float32, device=device)
+        nb = lambda *s: torch.empty(*s, **f32)
+        for n in ("x", "xp", "xs", "xv", "yv", "spec_pre", "vert_pre", "sd", "vd", "fused", "x1", "x2"):
+            setattr(self, n, nb(V, C))
+        self.pre = self.spec_pre      # the lift tangent is dead before block 0 writes spec_pre
+        self.ys = self.xs             # xs is dead once the W transform has read it
+        self.pw = self.spec_pre       # spec_pre (and its GN tangent sd) are consumed by the fuse tangent
+        self.mlp = self.vert_pre
+        spec_len = D * 2 * H * Wf * C
+        self.sa, self.sb = nb(spec_len), nb(spec_len)
+        self.va, self.vb = nb(2 * live * HW * C), nb(2 * live * HW * C)
+        self.parts = torch.empty(max(nparts, 1) * groups * 2, dtype=torch.float64, device=device)
+        self.sums = torch.empty(groups * 2, dtype=torch.float64, device=device)
+        self.scratch_parts = torch.empty(max(nparts, 1) * groups * 3, dtype=torch.float64, device=device)
+
+
 def _descs(D, H, W, C, live):
     Wf = W // 2 + 1
     HW = H * W
@@ -838,12 +967,23 @@ class _FFNOFunction(torch.autograd.Function):
 
 
 def ffno_apply(model, x, z_scale, dx, dy):
-    """FFNO3D.forward on the GB300 path; differentiable in x and z_scale."""
+    """FFNO3D.forward on the GB300 path; differentiable in x and z_scale (reverse mode: autograd) and in x (forward
+    mode: a dual x under torch.autograd.forward_ad gives a dual output, as the reference's jvp_local uses it)."""
+    import torch.autograd.forward_ad as fwAD
     if z_scale.ndim == 5:
         z_scale = z_scale[:, 0]
     dx = _spacing(dx)
     dy = _spacing(dy)
     ex = model.executor()
+    x_primal, x_tangent = fwAD.unpack_dual(x)
+    z_primal, z_tangent = fwAD.unpack_dual(z_scale)
+    if x_tangent is not None or z_tangent is not None:
+        if z_tangent is not None:
+            raise NotImplementedError("forward-mode derivatives along z_scale are not supported (heights are fixed)")
+        if torch.is_grad_enabled() and (x_primal.requires_grad or z_primal.requires_grad):
+            raise NotImplementedError("forward- and reverse-mode derivatives in one call are not supported")
+        y, y_dot = ex.jvp(x_primal, z_primal, dx, dy, x_tangent.float())
+        return fwAD.make_dual(y, y_dot)
     if torch.is_grad_enabled() and (x.requires_grad or z_scale.requires_grad):
         return _FFNOFunction.apply(x, z_scale, ex, dx, dy)
     y, _ = ex.forward(x, z_scale, dx, dy)

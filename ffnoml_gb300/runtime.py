@@ -160,6 +160,37 @@ class GB300Backend:
         self.call_count += 1
         return host.numpy().copy()
 
+    def jvp_local(self, features, z_scale, dx, dy, feature_tangent):
+        """Forward-mode derivative of the populations along feature_tangent (6,nz,nx,ny) in the SI units of features
+        (the heights stay fixed): (nz,nx,ny,L) in m^-3 (ffno_fsdp_runtime.py:350-372). FP32 whatever the model's
+        precision."""
+        features, z_scale = self._validate(features, z_scale)
+        tangent = np.asarray(feature_tangent, dtype=np.float32)
+        if tangent.shape != features.shape:
+            raise ValueError(f"local feature_tangent has shape {tangent.shape}; expected {features.shape}")
+        if not np.isfinite(tangent).all():
+            raise ValueError("FFNO JVP tangent contains NaN or Inf")
+        f_dev, x, zmm, V = self._prepare(features, z_scale)
+        t_dev = self._upload("tangent", tangent)
+        x_dot = torch.empty_like(x)
+        nat.call("ffno_si_input_tangent", f_dev.data_ptr(), t_dev.data_ptr(), V, self.std_x.data_ptr(),
+                 x_dot.data_ptr(), self._flags.data_ptr(), _stream())
+        y, y_dot = self.model.executor().jvp(x, zmm, float(dx), float(dy), x_dot)
+        L = self.model.out_channels
+        pop_dot = torch.empty(*z_scale.shape, L, dtype=torch.float32, device=self.device)
+        nat.call("ffno_si_population_tangent", y.data_ptr(), y_dot.data_ptr(), V, L, self.mean_y.data_ptr(),
+                 self.std_y.data_ptr(), pop_dot.data_ptr(), self._flags.data_ptr(), _stream())
+        host = self._download("pop_dot", pop_dot)
+        torch.cuda.current_stream().synchronize()
+        flags = int(self._flags.item())
+        if flags & 1:
+            raise ValueError("FFNO JVP tangent contains NaN or Inf")
+        if flags & 8:
+            raise RuntimeError("FFNO JVP returned NaN or Inf")
+        _check(flags, "FFNO JVP")
+        self.call_count += 1
+        return host.numpy().copy()
+
     def vjp_local(self, features, z_scale, dx, dy, population_cotangent):
         """Input VJP along the population cotangent (nz,nx,ny,L): {"features": (6,nz,nx,ny), "z_scale": (nz,nx,ny)}
         per SI unit (ffno_fsdp_runtime.py:306-348)."""

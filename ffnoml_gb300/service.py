@@ -91,7 +91,7 @@ class Request:
 
 def workspace_bytes(op, voxels, width, levels):
     """Upper estimate of the device memory one request needs (activations, spectral buffers, VJP state), bytes."""
-    per_voxel = 4 * width * (22 if op == "PREDICT" else 48) + 4 * (20 + 3 * levels)
+    per_voxel = 4 * width * {"PREDICT": 22, "VJP": 48, "JVP": 42}[op] + 4 * (20 + 3 * levels)
     return int(voxels * per_voxel * 1.25) + (64 << 20)
 
 
@@ -199,7 +199,8 @@ def execute(backends, req):
     if req.op == "VJP":
         out = backend.vjp_local(req.arrays[0], req.arrays[1], req.dx, req.dy, req.arrays[2])
         return head + array_bytes(out["features"]) + array_bytes(out["z_scale"])
-    raise NotImplementedError("JVP is not available in this service")
+    pop_dot = backend.jvp_local(req.arrays[0], req.arrays[1], req.dx, req.dy, req.arrays[2])
+    return head + array_bytes(pop_dot)
 
 
 # ---------------------------------------------------------------------------------------------------- server

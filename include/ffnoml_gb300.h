@@ -310,6 +310,42 @@ int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, 
                          const void* wpack, const float* g, const float* U, const float* Vm, int rank, int* err,
                          ffno_stream_t stream);
 
+/* ---- forward-mode derivative (JVP): jvp_local (ffno_fsdp_runtime.py:350-372), the tangent of FFNO3D.forward along
+ * an input tangent with the heights fixed. The linear stages reuse the forward entry points on the tangent (the lift
+ * convolution ffno_lift_fwd, the DFTs ffno_xform / ffno_xform_pt, the mixing ffno_spectral_mix); these linearise the
+ * nonlinear ones next to their primal inputs. FP32. */
+/* GroupNorm tangent (DepthWeightedGroupNorm :77-95): per-CTA partials [nparts][groups][2] of S1 = sum w pre_dot and
+ * S2 = sum w xhat pre_dot (reduce with ffno_gn_bwd_final), then out = base + res * gamma r (pre_dot - S1/T - xhat
+ * S2/T) [* gelu'(y) with act = 1]. gstats as written by ffno_gn_finalize for the primal. base may be NULL. */
+int ffno_gn_jvp_stats(const float* pre, const float* pre_dot, const double* gstats, const float* dw, long V, int C,
+                      int groups, double* partials, int nparts, ffno_stream_t stream);
+int ffno_gn_jvp_apply(const float* pre, const float* pre_dot, const float* gamma, const float* beta,
+                      const double* gstats, const double* sums, int act, const float* base, float res, long V, int C,
+                      int groups, float* out, ffno_stream_t stream);
+/* Tangent of ffno_gate_fwd (the z_proj term is constant): same weights [K][N]. */
+int ffno_gate_jvp(const float* x, const float* x_dot, long V, int C, const float* w1, const float* w2, float* out_dot,
+                  ffno_stream_t stream);
+/* Tangent of the MLP C -> 2C -> C of ffno_mlp2_fwd at input a (the residual prologue is applied by the caller). */
+int ffno_mlp2_jvp(const float* a, const float* a_dot, long V, int C, const float* w1, const float* w2, float* out_dot,
+                  ffno_stream_t stream);
+/* Tangent of ffno_fuse_fwd's fused pre-activation (_fuse_branches :524-534) given the tangents spec_dot / vert_dot of
+ * the branch outputs gelu(GN(spec_pre)), gelu(GN(vert_pre)). */
+int ffno_fuse_jvp(const float* x, const float* x_dot, const float* spec_pre, const float* spec_coefs,
+                  const float* vert_pre, const float* vert_coefs, const float* spec_dot, const float* vert_dot, long V,
+                  int C, const float* wg1, const float* wg2, const float* bg2, const float* wf1, const float* wf2,
+                  float* fused_dot, ffno_stream_t stream);
+/* Tangent of ffno_head_fwd along the last block's tangent x_dot [V][C] and the input tangent x_in_dot [cin][V]:
+ * out_dot [levels][V] (normalised log10 n). */
+int ffno_head_jvp(const float* x, const float* x_dot, const float* x_in, const float* x_in_dot, long V, int C,
+                  const float* p1, const float* p2, const float* b2, int nhp, const ffno_head_params* params,
+                  float* out_dot, ffno_stream_t stream);
+/* Service units: SI feature tangent (6, nz, nx, ny) -> normalised model-input tangent; model-output tangent ->
+ * population tangent (nz, nx, ny, L) in m^-3 (0 where the +-37 clamp is active). flags as ffno_si_*. */
+int ffno_si_input_tangent(const float* features, const float* tangent, long V, const float* std_x, float* x_dot,
+                          int* flags, ffno_stream_t stream);
+int ffno_si_population_tangent(const float* y, const float* y_dot, long V, int L, const float* mean_y,
+                               const float* std_y, float* out, int* flags, ffno_stream_t stream);
+
 /* Self-test of the tensor-core primitives (no reference counterpart: it pins this library's tcgen05 descriptor and
  * tensor-memory conventions): D [128][N] = bf16(A [128][K]) @ bf16(B [N][K])^T in FP32, one CTA, with B staged
  * K-major (b_mn = 0) or MN-major (b_mn = 1); K, N multiples of 16 up to 256. *status (device int) is set to 1 if the

@@ -370,3 +370,16 @@ def vjp(oracle, x, z_scale, dx, dy, cotangent):
     y = oracle.forward(x, z, dx, dy)
     xb, zb = torch.autograd.grad(y, (x, z), cotangent)
     return y.detach(), xb, zb
+
+
+def jvp(oracle, x, z_scale, dx, dy, x_dot):
+    """Forward-mode derivative of oracle.forward at (x, z_scale) along x_dot with the heights fixed (what jvp_local
+    computes with dual tensors, ffno_fsdp_runtime.py:350-372): (y, y_dot)."""
+    fn = lambda xx: oracle.forward(xx, z_scale, dx, dy)
+    return torch.func.jvp(fn, (x,), (x_dot,))
+
+
+def jvp_si(oracle, features, z_m, dx, dy, feature_tangent):
+    """The same at the service level: SI features and their tangent -> (populations, population tangent)."""
+    fn = lambda ff: oracle.forward_si(ff, z_m, dx, dy)
+    return torch.func.jvp(fn, (features,), (feature_tangent,))

@@ -40,6 +40,11 @@ class FakeBackend:
         s = cot.sum(axis=-1)
         return {"features": np.broadcast_to(s, features.shape).astype(np.float32) * 2, "z_scale": s.astype(np.float32)}
 
+    def jvp_local(self, features, z, dx, dy, tangent):
+        self._check(features, z)
+        base = tangent.sum(axis=0)
+        return np.stack([base * (l + 1) for l in range(len(self.level_names))], axis=-1).astype(np.float32)
+
 
 def _server(backend, slots=2):
     srv = Server({"H": backend}, "tok", port=0, slots=slots, budget_bytes=1 << 40, device="cpu")
@@ -127,4 +132,16 @@ def test_two_connections_run_concurrently():
     assert elapsed < 0.55                               # the two 0.3 s requests overlapped
     for pop, f, z in results.values():
         assert np.allclose(pop[..., 1], f.sum(0) + z + 1, atol=1e-5)
+    srv.shutdown()
+
+
+def test_jvp_request_round_trip():
+    srv = _server(FakeBackend())
+    c = Client(srv.port, "tok")
+    f, z = _inputs((3, 4, 5), 4)
+    t = np.random.default_rng(5).normal(size=f.shape).astype(np.float32)
+    got = c.request("JVP", "H", f, z, 48e3, 48e3, 6, t)
+    assert got.shape == (3, 4, 5, 6)
+    np.testing.assert_allclose(got[..., 2], 3 * t.sum(axis=0), rtol=1e-6)
+    c.close()
     srv.shutdown()
