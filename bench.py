@@ -405,6 +405,14 @@ def run_gb300(args):
                 "bf16_speedup_fwd+vjp": ms32 / ms_step, "bf16_speedup_fwd": ms32f / ms_fwd,
                 "max_abs_dlog10n_bf16_vs_fp32": dlog}
 
+    # forward-mode derivative (JVP, FP32 tangent kernels) along a seeded input tangent, inputs resident
+    jvp = None
+    if not args.no_jvp and not args.fwd_only:
+        xdot = torch.from_numpy(np.random.default_rng(6 + rank).normal(size=x.shape).astype(np.float32)).to(dev)
+        ms_jvp, _ = timed(lambda: ex.jvp(x, z, DXY, DXY, xdot), 2, 1)
+        jvp = {"value": job_rate(V, world, ms_jvp / 1e3), "unit": "voxels/s", "ms_per_step": ms_jvp,
+               "dtype": "f32"}
+
     # e2e through the service backend with host buffers
     e2e = None
     if not args.no_e2e:
@@ -449,7 +457,7 @@ def run_gb300(args):
                        "voxels_per_step": V, "parallelism": f"replicas{world}",
                        "l2": "working set (GBs) >> L2; no flush needed", "precision": args.precision},
             "fwd": {"value": job_rate(V, world, ms_fwd / 1e3), "unit": "voxels/s", "ms_per_step": ms_fwd},
-            "fp32": fp32,
+            "fp32": fp32, "jvp": jvp,
             "algorithmic_tflops": {"fwd+vjp": 2 * flops_vox * V / (ms_step / 1e3) / 1e12,
                                    "fwd": flops_vox * V / (ms_fwd / 1e3) / 1e12},
             "roofline": roof, "roofline_by_entry": dict(sorted(rows.items(), key=lambda kv: -per[kv[0]][0])[:12]),
@@ -536,6 +544,7 @@ def main():
     ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16"])
     ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 comparison run")
     ap.add_argument("--fwd-only", action="store_true", help="time the forward pass alone (profiling cases)")
+    ap.add_argument("--no-jvp", action="store_true", help="skip the forward-mode derivative timing")
     ap.add_argument("--shape", default="256,128,128")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
