@@ -5,7 +5,8 @@ Workload (the scaled configuration): FFNO3D width 64, 8 blocks, height operator 
 (z_min_wavelength = 40/31), H + Ca II level-fraction head (12 levels), one cube [1, 6, 256, 128, 128] = 4.19 M voxels,
 synthetic seeded inputs with the reference's channel distributions, random-init weights of that architecture.
 
-A step is one forward pass plus one input VJP (per-block recompute) over the cube, inputs resident in HBM (value), in
+A step is one forward pass plus one input VJP over the cube (each block's intermediates kept from the forward when
+they fit in half the free HBM, else recomputed block by block in the backward), inputs resident in HBM (value), in
 the BF16 tensor-core form by default; the plain FP32 drop-in runs on the same cube for the speed-up and the BF16 error.
 e2e is the same step through the service backend's vjp_local with host numpy buffers (host<->device copies inside the
 timed region). The cube (GBs of activations) is far larger than L2, so no flush is needed between steps. The serving
@@ -347,6 +348,7 @@ def run_gb300(args):
     with ClockSampler(local) as clk:
         ms_step, calls = timed(step, args.steps, args.warmup)
     clocks = clk.summary()
+    cached_states = ex.last_cached
     memory = {"peak_allocated_gib": torch.cuda.max_memory_allocated(dev) / 2 ** 30,
               "device_total_gib": torch.cuda.get_device_properties(dev).total_memory / 2 ** 30}
     ms_fwd = ms_step if args.fwd_only else timed(fwd, max(args.steps, 3), 1)[0]
@@ -453,7 +455,8 @@ def run_gb300(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if args.precision == "fp32" else "bf16", "data": "synthetic",
             "config": {"workload": f"FFNO3D w{WIDTH} L{LAYERS} M{MODES} H+CaII, [1,6,{D},{H},{W}] " +
-                                   ("forward only" if args.fwd_only else "fwd + input VJP (per-block recompute)"),
+                                   ("forward only" if args.fwd_only else "fwd + input VJP (block states " +
+                                    ("kept from the forward)" if cached_states else "recomputed per block)")),
                        "voxels_per_step": V, "parallelism": f"replicas{world}",
                        "l2": "working set (GBs) >> L2; no flush needed", "precision": args.precision},
             "fwd": {"value": job_rate(V, world, ms_fwd / 1e3), "unit": "voxels/s", "ms_per_step": ms_fwd},

@@ -17,6 +17,7 @@ The input VJP keeps only the block inputs from the forward pass and recomputes e
 back-propagating through it (the reference's per-block activation checkpointing, models/ffno_model.py:751-780).
 Parameter gradients are not computed: the service's VJP discards them (ffno_fsdp_runtime.py:319-344).
 """
+import copy
 import hashlib
 import math
 import threading
@@ -276,6 +277,39 @@ class Workspace:
         self.gates = nb(V, 2 * C)     # branch gates between the two tensor-core fuse stages
         self.va, self.vb = nb(2 * live * HW * C), nb(2 * live * HW * C)
 
+    # the intermediates a block's VJP reads (kept per block when the forward caches block states)
+    CACHED = ("xs", "xv", "yv", "spec_pre", "vert_pre", "fused_pre", "pw_pre", "mlp_pre", "x1", "x2", "vb")
+
+    def state_bytes(self):
+        """Device bytes of one block's cached intermediates."""
+        return sum(getattr(self, n).numel() * 4 for n in self.CACHED) + 2 * len(NORMS) * 8 * 64
+
+    def fork(self):
+        """A view of this workspace with its own copies of the cached intermediates and GroupNorm statistics (the
+        scratch buffers stay shared): block i of a caching forward writes its state there."""
+        w = copy.copy(self)
+        for n in self.CACHED:
+            setattr(w, n, torch.empty_like(getattr(self, n)))
+        w.ys = w.xs
+        w.coefs = dict(self.coefs)
+        w.gstats = dict(self.gstats)
+        for n in NORMS:
+            w.coefs[n] = torch.empty_like(self.coefs[n])
+            w.gstats[n] = torch.empty_like(self.gstats[n])
+        return w
+
+    def bind(self, state):
+        """This workspace's scratch with a block's cached intermediates and statistics (from fork)."""
+        w = copy.copy(self)
+        for n in self.CACHED + ("ys",):
+            setattr(w, n, getattr(state, n))
+        w.coefs = dict(self.coefs)
+        w.gstats = dict(self.gstats)
+        for n in NORMS:
+            w.coefs[n] = state.coefs[n]
+            w.gstats[n] = state.gstats[n]
+        return w
+
 
 class Executor:
     def __init__(self, model):
@@ -287,6 +321,12 @@ class Executor:
         self._height = {}
         self._lock = threading.RLock()        # caches are shared by concurrent service slots
         self._tls = threading.local()         # per-thread mode (a JVP forces the FP32 kernels)
+        # A forward for the VJP keeps every block's intermediates instead of recomputing them in the backward when
+        # they fit in half the free device memory (models/ffno_model.py:786-791 recomputes each block under
+        # checkpoint_blocks). A host that runs several requests at once on the device turns this off (the service
+        # does).
+        self.cache_states = True
+        self.last_cached = False              # whether the last forward for a VJP kept its block states
 
     # -------------------------------------------------------------------------------------------- caches
     def packed(self, device):
@@ -458,26 +498,43 @@ class Executor:
         pk, geo, hgt, pln, pfr = self._setup(x, z_scale, dx, dy)
         B, _, D, H, W = x.shape
         out = torch.empty(B, m.out_channels, D, H, W, dtype=torch.float32, device=x.device)
-        saved = []
+        saved, states = [], []
         ws = None
+        cache = None
         for b in range(B):
             hgt_b = hgt if geo.shared else self.height_percol(pk, geo, b, x.device)
             if ws is None or ws.live != hgt_b["live"]:
                 ws = Workspace(D, H, W, m.width, hgt_b["live"], pk.groups, x.device)
+            if keep and cache is None:
+                cache = self.cache_states and self._fits(B * m.n_layers * ws.state_bytes(), x.device)
+                self.last_cached = cache
             xin, z = x[b], z_scale[b]
             self._depth_weights(ws, z, D, H * W)
             self._lift(pk, ws, xin)
             inputs = [ws.x.clone()] if keep else None
+            blocks = [] if cache else None
             for i in range(m.n_layers):
-                self._block(pk, ws, i, z, D, H, W, hgt_b, pln, pfr[i])
+                wb = ws.fork() if cache else ws
+                self._block(pk, wb, i, z, D, H, W, hgt_b, pln, pfr[i])
                 if keep:
                     inputs.append(ws.x.clone())
+                if cache:
+                    blocks.append(wb)
             self._head(pk, ws.x, xin, out[b])
             if keep:
                 saved.append(inputs)
+                states.append(blocks)
         self._check(ws)
-        state = dict(x=x, z=z_scale, dx=dx, dy=dy, inputs=saved, geo=geo) if keep else None
+        state = dict(x=x, z=z_scale, dx=dx, dy=dy, inputs=saved, geo=geo, blocks=states if cache else None) \
+            if keep else None
         return out, state
+
+    @staticmethod
+    def _fits(nbytes, device):
+        free, _ = torch.cuda.mem_get_info(device)
+        # memory PyTorch's allocator holds but no tensor uses is free for this process too
+        free += torch.cuda.memory_reserved(device) - torch.cuda.memory_allocated(device)
+        return nbytes <= 0.5 * free
 
     @staticmethod
     def _check(ws):
@@ -756,9 +813,17 @@ class Executor:
             nat.call("ffno_head_bwd", inputs[-1].data_ptr(), xin.data_ptr(), ybar[b].data_ptr(), V, C,
                      pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.p2t.data_ptr(), pk.p1t.data_ptr(),
                      pk.nhp, pk.head, gb.xbar.data_ptr(), xbar_in[b].data_ptr(), s)
+            cached = state.get("blocks")
             for i in reversed(range(m.n_layers)):
-                self._block(pk, ws, i, z, D, H, W, hgt_b, pln, pfr[i], x_in=inputs[i])
-                self._block_bwd(pk, ws, gb, i, inputs[i], z, zbar[b], D, H, W, hgt_b, pln, pfr[i], tzf_bar, tzi_bar)
+                if cached and cached[b][i] is not None:
+                    # a block's cached state is consumed by its VJP (a second backward over the same state
+                    # recomputes the block)
+                    wb = ws.bind(cached[b][i])
+                    cached[b][i] = None
+                else:
+                    wb = ws
+                    self._block(pk, ws, i, z, D, H, W, hgt_b, pln, pfr[i], x_in=inputs[i])
+                self._block_bwd(pk, wb, gb, i, inputs[i], z, zbar[b], D, H, W, hgt_b, pln, pfr[i], tzf_bar, tzi_bar)
             # lift: x0 = gelu(GN(pre0))
             self._lift(pk, ws, xin)
             self._gn_bwd(ws, gb, 1, gb.xbar, 1.0, ws.pre, pk.lift_g, pk.lift_b, "lift", gb.pbar)

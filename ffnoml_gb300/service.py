@@ -101,6 +101,12 @@ class Scheduler:
     def __init__(self, backends, slots=4, memory_fraction=0.8, budget_bytes=None, device=None):
         self.backends = backends
         self.slots = max(1, int(slots))
+        # a VJP recomputes each block in its backward: its workspace stays within the admission estimate while
+        # other requests run beside it
+        for b in backends.values():
+            model = getattr(b, "model", None)
+            if model is not None and hasattr(model, "executor"):
+                model.executor().cache_states = False
         self.device = torch.device(device or "cuda")
         if self.device.type == "cuda" and self.device.index is None:
             self.device = torch.device("cuda", torch.cuda.current_device())
