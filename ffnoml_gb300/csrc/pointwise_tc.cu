@@ -73,6 +73,10 @@ __device__ __forceinline__ bool load_weights(void* dst, const void* src, uint32_
   return ok;
 }
 
+// Tiles of L2 prefetch lookahead per pipeline: at tile t a pipeline prefetches the inputs of its tile t + c_pf steps
+// ahead (0: none). Set by ffno_tc_set_prefetch_tiles.
+__constant__ int c_pf = 1;
+
 // L2 prefetch of rows [n0, n0 + 128) of a [V][width] FP32 array, by one thread
 __device__ __forceinline__ void prefetch_rows(const float* base, long n0, long V, int width) {
   if (!base || n0 >= V) return;
@@ -465,11 +469,18 @@ __global__ void __launch_bounds__(CT, 1) k_mlp2_tc(const float* __restrict__ in,
   Gn4 gc{};
   if (MODE != 0) gc = gn_coefs(pc, C, fill_col<C>(P.ptid));
   const int f = P.feat();
+  const int pf = c_pf;
+  for (int k = 1; P.ptid == 0 && k < pf; ++k) {
+    const long tp = t0 + k * tstep;
+    prefetch_rows(in, tp * TM, V, C);
+    if (MODE != 0) prefetch_rows(prev, tp * TM, V, C);
+  }
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (P.ptid == 0) {
-      prefetch_rows(in, (t + tstep) * TM, V, C);
-      if (MODE != 0) prefetch_rows(prev, (t + tstep) * TM, V, C);
+    if (P.ptid == 0 && pf > 0) {
+      const long tp = t + pf * tstep;
+      prefetch_rows(in, tp * TM, V, C);
+      if (MODE != 0) prefetch_rows(prev, tp * TM, V, C);
     }
     load_tile_weights(P, dw, v0, V, wt[pid], wpart[pid]);
     fill_tile<C>(X, v0, V, P.ptid, [&](long v, int k) {
@@ -520,9 +531,17 @@ __global__ void __launch_bounds__(CT, 1) k_gate_tc(const float* __restrict__ x, 
   P.ok = load_weights(smem, wpack, 2 * B1, wcx, err);
   const Op g1 = wop(smem, C, C), g2 = wop(smem + B1, C, C);
   const int row = P.feat();
+  const int pf = c_pf;
+  for (int k = 1; P.ptid == 0 && k < pf; ++k) {
+    const long tp = t0 + k * tstep;
+    prefetch_rows(x, tp * TM, V, C);
+  }
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (P.ptid == 0) prefetch_rows(x, (t + tstep) * TM, V, C);
+    if (P.ptid == 0 && pf > 0) {
+      const long tp = t + pf * tstep;
+      prefetch_rows(x, tp * TM, V, C);
+    }
     fill_tile<C>(X, v0, V, P.ptid, [&](long v, int k) { return ld4(x + v * C + k); });
     if (!pipe_gemms(P, err, Gemm{P.tmem, kop(X, C), g1, C, false, C})) break;
 #pragma unroll
@@ -582,12 +601,20 @@ __global__ void __launch_bounds__(CT, 1) k_fuse1_tc(const float* __restrict__ x,
   const Gn4 gs = gn_coefs(sc, C, kf), gv = gn_coefs(vc, C, kf);
   const int f = P.feat();
   const float bf = f < 2 * C ? __ldg(bias + f) : 0.f;
+  const int pf = c_pf;
+  for (int k = 1; P.ptid == 0 && k < pf; ++k) {
+    const long tp = t0 + k * tstep;
+    prefetch_rows(x, tp * TM, V, C);
+    prefetch_rows(sp, tp * TM, V, C);
+    prefetch_rows(vp, tp * TM, V, C);
+  }
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (P.ptid == 0) {
-      prefetch_rows(x, (t + tstep) * TM, V, C);
-      prefetch_rows(sp, (t + tstep) * TM, V, C);
-      prefetch_rows(vp, (t + tstep) * TM, V, C);
+    if (P.ptid == 0 && pf > 0) {
+      const long tp = t + pf * tstep;
+      prefetch_rows(x, tp * TM, V, C);
+      prefetch_rows(sp, tp * TM, V, C);
+      prefetch_rows(vp, tp * TM, V, C);
     }
     for (int kc = 0; kc < 3; ++kc) {
       if (kc == 0)
@@ -655,12 +682,20 @@ __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp
   const int fc = f < C ? f : 0;   // this thread's output channel (epilogue) and its GroupNorm coefficients
   const float sm = __ldg(sc + fc), ss = __ldg(sc + C + fc), sb = __ldg(sc + 2 * C + fc);
   const float vm = __ldg(vc + fc), vs = __ldg(vc + C + fc), vbb = __ldg(vc + 2 * C + fc);
+  const int pf = c_pf;
+  for (int k = 1; P.ptid == 0 && k < pf; ++k) {
+    const long tp = t0 + k * tstep;
+    prefetch_rows(sp, tp * TM, V, C);
+    prefetch_rows(vp, tp * TM, V, C);
+    prefetch_rows(gates, tp * TM, V, 2 * C);
+  }
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (P.ptid == 0) {
-      prefetch_rows(sp, (t + tstep) * TM, V, C);
-      prefetch_rows(vp, (t + tstep) * TM, V, C);
-      prefetch_rows(gates, (t + tstep) * TM, V, 2 * C);
+    if (P.ptid == 0 && pf > 0) {
+      const long tp = t + pf * tstep;
+      prefetch_rows(sp, tp * TM, V, C);
+      prefetch_rows(vp, tp * TM, V, C);
+      prefetch_rows(gates, tp * TM, V, 2 * C);
     }
     load_tile_weights(P, dw, v0, V, wt[pid], wpart[pid]);
     fill_tile<2 * C>(A, v0, V, P.ptid, [&](long v, int k) {
@@ -723,12 +758,20 @@ __global__ void __launch_bounds__(CT, 1) k_mlp2_bwd_tc(const float* __restrict__
   P.ok = load_weights(smem, wpack, 3 * B1, wcx, err);
   const Op w1 = wop(smem, 2 * C, C), w2t = wop(smem + B1, 2 * C, C), w1t = wop(smem + 2 * B1, C, 2 * C);
   const int f = P.feat();
+  const int pf = c_pf;
+  for (int k = 1; P.ptid == 0 && k < pf; ++k) {
+    const long tp = t0 + k * tstep;
+    prefetch_rows(a, tp * TM, V, C);
+    prefetch_rows(pb, tp * TM, V, C);
+    prefetch_rows(base, tp * TM, V, C);
+  }
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (P.ptid == 0) {
-      prefetch_rows(a, (t + tstep) * TM, V, C);
-      prefetch_rows(pb, (t + tstep) * TM, V, C);
-      prefetch_rows(base, (t + tstep) * TM, V, C);
+    if (P.ptid == 0 && pf > 0) {
+      const long tp = t + pf * tstep;
+      prefetch_rows(a, tp * TM, V, C);
+      prefetch_rows(pb, tp * TM, V, C);
+      prefetch_rows(base, tp * TM, V, C);
     }
     fill_tile<C>(A, v0, V, P.ptid, [&](long v, int k) { return ld4(a + v * C + k); });
     fill_tile<C>(Pt, v0, V, P.ptid, [&](long v, int k) { return ld4(pb + v * C + k); });
@@ -784,12 +827,20 @@ __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__
            g1t = wop(smem + 3 * B1, C, C);
   const uint32_t D1 = 0, D2 = C, D3 = 2 * C, D4 = 3 * C;
   const int row = P.feat();
+  const int pf = c_pf;
+  for (int k = 1; P.ptid == 0 && k < pf; ++k) {
+    const long tp = t0 + k * tstep;
+    prefetch_rows(x, tp * TM, V, C);
+    prefetch_rows(gbar, tp * TM, V, C);
+    prefetch_rows(base, tp * TM, V, C);
+  }
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (P.ptid == 0) {
-      prefetch_rows(x, (t + tstep) * TM, V, C);
-      prefetch_rows(gbar, (t + tstep) * TM, V, C);
-      prefetch_rows(base, (t + tstep) * TM, V, C);
+    if (P.ptid == 0 && pf > 0) {
+      const long tp = t + pf * tstep;
+      prefetch_rows(x, tp * TM, V, C);
+      prefetch_rows(gbar, tp * TM, V, C);
+      prefetch_rows(base, tp * TM, V, C);
     }
     const long v = v0 + row;
     fill_tile<C>(X, v0, V, P.ptid, [&](long vv, int k) { return ld4(x + vv * C + k); });
@@ -891,13 +942,22 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_a_tc(const float* __restrict
   const float* src = kf < C ? sp : vp;
   const int ks = kf < C ? kf : kf - C;
   const int f = P.feat();
+  const int pf = c_pf;
+  for (int k = 1; P.ptid == 0 && k < pf; ++k) {
+    const long tp = t0 + k * tstep;
+    prefetch_rows(sp, tp * TM, V, C);
+    prefetch_rows(vp, tp * TM, V, C);
+    prefetch_rows(gates, tp * TM, V, 2 * C);
+    prefetch_rows(fb, tp * TM, V, C);
+  }
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (P.ptid == 0) {
-      prefetch_rows(sp, (t + tstep) * TM, V, C);
-      prefetch_rows(vp, (t + tstep) * TM, V, C);
-      prefetch_rows(gates, (t + tstep) * TM, V, 2 * C);
-      prefetch_rows(fb, (t + tstep) * TM, V, C);
+    if (P.ptid == 0 && pf > 0) {
+      const long tp = t + pf * tstep;
+      prefetch_rows(sp, tp * TM, V, C);
+      prefetch_rows(vp, tp * TM, V, C);
+      prefetch_rows(gates, tp * TM, V, 2 * C);
+      prefetch_rows(fb, tp * TM, V, C);
     }
     fill_tile<2 * C>(Bt, v0, V, P.ptid, [&](long v, int k) {
       const float4 g = ld4(gates + v * 2 * C + k);
@@ -925,10 +985,12 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_a_tc(const float* __restrict
 // Fuse backward, stage b: B_bar = hfb Wf1^T + [F_bar, F_bar] / 2; spec/vert grads B_bar g (+ the gate path);
 // gate pre-activation grad q = B_bar [spec, vert] g (1 - g); hg_bar = (q Wg2^T) * gelu'(hg); A_bar = hg_bar Wg1^T:
 // x_bar = base + A_bar[:C], spec_bar = B_bar_s g_s + A_bar[C:2C], vert_bar likewise.
-// Weights: [wf1t (2C x 2C), wg2t (C x 2C), wg1t (3C x C)]. One pipeline per CTA (the weights leave room for one tile);
-// all three GEMMs run untransposed (lane = voxel; its epilogues read and write several tensors per voxel).
+// Weights: [wf1t (2C x 2C), wg2t (C x 2C), wg1t (3C x C)]. All three GEMMs run untransposed (lane = voxel; the
+// epilogues read and write several tensors per voxel). Each of the two pipelines has one [128][C] operand tile, so the
+// K = 2C products run as two K-slices: hfb's spec and vert halves, then q's spec and vert halves (each slice's
+// epilogue fills the tile while the other pipeline's MMAs run).
 template <int C>
-__global__ void __launch_bounds__(PT, 1) k_fuse_bwd_b_tc(const float* __restrict__ sp, const float* __restrict__ sc,
+__global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict__ sp, const float* __restrict__ sc,
                                                          const float* __restrict__ vp, const float* __restrict__ vc,
                                                          const float* __restrict__ gates, const float* __restrict__ hg,
                                                          const float* __restrict__ fb, const float* __restrict__ hfb,
@@ -937,59 +999,80 @@ __global__ void __launch_bounds__(PT, 1) k_fuse_bwd_b_tc(const float* __restrict
                                                          float* __restrict__ sbar, float* __restrict__ vbar,
                                                          int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  constexpr uint32_t B1 = mat_bytes(2 * C, 2 * C), B2 = mat_bytes(C, 2 * C), B3 = mat_bytes(3 * C, C);
-  PIPE_PROLOGUE(3 * C, 1)
-  const Split T2 = split_at(smem + B1 + B2 + B3, TM, 2 * C), T1 = split_at(smem + B1 + B2 + B3, TM, C);
+  constexpr uint32_t B1 = mat_bytes(2 * C, 2 * C), B2 = mat_bytes(C, 2 * C), B3 = mat_bytes(3 * C, C),
+                     RB = tile_bytes(C);
+  PIPE_PROLOGUE(3 * C, 2)
+  const Split T = split_at(smem + B1 + B2 + B3 + pid * RB, TM, C);
   P.ok = load_weights(smem, wpack, B1 + B2 + B3, wcx, err);
-  const Op wf1t = wop(smem, 2 * C, 2 * C), wg2t = wop(smem + B1, C, 2 * C), wg1t = wop(smem + B1 + B2, 3 * C, C);
+  const Op wg1t = wop(smem + B1 + B2, 3 * C, C);
   const int row = P.feat();
+  const int pf = c_pf;
+  for (int k = 1; P.ptid == 0 && k < pf; ++k) {
+    const long tp = t0 + k * tstep;
+    prefetch_rows(hfb, tp * TM, V, 2 * C);
+    prefetch_rows(fb, tp * TM, V, C);
+    prefetch_rows(gates, tp * TM, V, 2 * C);
+    prefetch_rows(sp, tp * TM, V, C);
+    prefetch_rows(vp, tp * TM, V, C);
+    prefetch_rows(hg, tp * TM, V, C);
+    prefetch_rows(base, tp * TM, V, C);
+  }
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
-    if (P.ptid == 0) {
-      prefetch_rows(hfb, (t + tstep) * TM, V, 2 * C);
-      prefetch_rows(fb, (t + tstep) * TM, V, C);
-      prefetch_rows(gates, (t + tstep) * TM, V, 2 * C);
-      prefetch_rows(sp, (t + tstep) * TM, V, C);
-      prefetch_rows(vp, (t + tstep) * TM, V, C);
-      prefetch_rows(hg, (t + tstep) * TM, V, C);
-      prefetch_rows(base, (t + tstep) * TM, V, C);
+    if (P.ptid == 0 && pf > 0) {
+      const long tp = t + pf * tstep;
+      prefetch_rows(hfb, tp * TM, V, 2 * C);
+      prefetch_rows(fb, tp * TM, V, C);
+      prefetch_rows(gates, tp * TM, V, 2 * C);
+      prefetch_rows(sp, tp * TM, V, C);
+      prefetch_rows(vp, tp * TM, V, C);
+      prefetch_rows(hg, tp * TM, V, C);
+      prefetch_rows(base, tp * TM, V, C);
     }
     const long v = v0 + row;
-    fill_tile<2 * C>(T2, v0, V, P.ptid, [&](long vv, int k) { return ld4(hfb + vv * 2 * C + k); });
-    if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T2, 2 * C), wf1t, 2 * C, false, 2 * C})) break;
-#pragma unroll
-    for (int j = 0; j < (2 * C) / 16; ++j) {
-      if (!owns(j, P.half)) continue;
-      const int c0 = 16 * j;
-      float bb[16], q[16];
-      rld(P, 0, j, bb);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) q[i] = 0.f;
-      if (v < V) {
-        const bool is_s = c0 < C;
-        const int cc = is_s ? c0 : c0 - C;
-        const float* pre = is_s ? sp : vp;
-        const float* cf = is_s ? sc : vc;
-        float* gout = is_s ? sbar : vbar;
-#pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          const float4 f4 = ld4(fb + v * C + cc + i), g4 = ld4(gates + v * 2 * C + c0 + i);
-          const float4 s4 = gn_apply<true>(ld4(pre + v * C + cc + i), gn_coefs(cf, C, cc + i));
-          const float ff[4] = {f4.x, f4.y, f4.z, f4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w},
-                      ss[4] = {s4.x, s4.y, s4.z, s4.w};
-          float o[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const float b = bb[i + u] + 0.5f * ff[u];
-            o[u] = b * gg[u];
-            q[i + u] = b * ss[u] * gg[u] * (1.f - gg[u]);
-          }
-          *reinterpret_cast<float4*>(gout + v * C + cc + i) = make_float4(o[0], o[1], o[2], o[3]);
-        }
-      }
-      put16(T2, row, c0, 2 * C, q);
+    // B_bar (without the F_bar term) = hfb Wf1^T over the spec and vert halves of hfb
+    for (int kh = 0; kh < 2; ++kh) {
+      fill_tile<C>(T, v0, V, P.ptid, [&](long vv, int k) { return ld4(hfb + vv * 2 * C + kh * C + k); });
+      if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, C), wop(smem, 2 * C, 2 * C, 0, kh * C), C, kh > 0, 2 * C})) break;
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem + 2 * C, kop(T2, 2 * C), wg2t, 2 * C, false, C})) break;
+    if (!P.ok) break;
+    // per branch half: the direct spec/vert gradients, q, and its slice of q Wg2^T
+    for (int kh = 0; kh < 2; ++kh) {
+      const float* pre = kh == 0 ? sp : vp;
+      const float* cf = kh == 0 ? sc : vc;
+      float* gout = kh == 0 ? sbar : vbar;
+#pragma unroll 1
+      for (int jj = 0; jj < C / 16; ++jj) {
+        const int j = kh * (C / 16) + jj;
+        if (!owns(j, P.half)) continue;
+        const int cc = 16 * jj;
+        float bb[16], q[16];
+        rld(P, 0, j, bb);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) q[i] = 0.f;
+        if (v < V) {
+#pragma unroll
+          for (int i = 0; i < 16; i += 4) {
+            const float4 f4 = ld4(fb + v * C + cc + i), g4 = ld4(gates + v * 2 * C + kh * C + cc + i);
+            const float4 s4 = gn_apply<true>(ld4(pre + v * C + cc + i), gn_coefs(cf, C, cc + i));
+            const float ff[4] = {f4.x, f4.y, f4.z, f4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w},
+                        ss[4] = {s4.x, s4.y, s4.z, s4.w};
+            float o[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const float b = bb[i + u] + 0.5f * ff[u];
+              o[u] = b * gg[u];
+              q[i + u] = b * ss[u] * gg[u] * (1.f - gg[u]);
+            }
+            *reinterpret_cast<float4*>(gout + v * C + cc + i) = make_float4(o[0], o[1], o[2], o[3]);
+          }
+        }
+        put16(T, row, cc, C, q);
+      }
+      if (!pipe_gemms(P, err, Gemm{P.tmem + 2 * C, kop(T, C), wop(smem + B1, C, 2 * C, 0, kh * C), C, kh > 0, C}))
+        break;
+    }
+    if (!P.ok) break;
 #pragma unroll
     for (int j = 0; j < C / 16; ++j) {
       if (!owns(j, P.half)) continue;
@@ -1004,9 +1087,9 @@ __global__ void __launch_bounds__(PT, 1) k_fuse_bwd_b_tc(const float* __restrict
         hb[i + 2] *= gelu_grad(h4.z);
         hb[i + 3] *= gelu_grad(h4.w);
       }
-      put16(T1, row, c0, C, hb);
+      put16(T, row, c0, C, hb);
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T1, C), wg1t, C, false, 3 * C})) break;
+    if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, C), wg1t, C, false, 3 * C})) break;
 #pragma unroll
     for (int j = 0; j < (3 * C) / 16; ++j) {
       if (!owns(j, P.half)) continue;
@@ -1038,7 +1121,7 @@ __global__ void __launch_bounds__(PT, 1) k_fuse_bwd_b_tc(const float* __restrict
       }
     }
   }
-  pipe_finish(P, tslot, NCOL);
+  pipe_finish(P, tslot, 2 * NCOL);
 }
 
 #undef PIPE_PROLOGUE
@@ -1060,12 +1143,6 @@ int grid_tc(long V) {
   return (int)(t < g ? (t > 0 ? t : 1) : g);
 }
 
-int grid_tc1(long V) {   // one pipeline per CTA
-  const long t = (V + TM - 1) / TM;
-  const long g = (long)sms();
-  return (int)(t < g ? (t > 0 ? t : 1) : g);
-}
-
 template <typename K>
 bool launch_prep(K kernel, size_t bytes) {
   if (bytes > 227 * 1024 - 1024) return false;   // leave room for the kernels' static shared memory
@@ -1083,6 +1160,11 @@ extern "C" {
 int ffno_tc_parts(long V) { return grid_tc(V); }
 
 int ffno_tc_width_supported(int C) { return tc_width(C) ? 1 : 0; }
+
+int ffno_tc_set_prefetch_tiles(int tiles) {
+  if (tiles < 0 || tiles > 4) return FFNO_EINVAL;
+  return cudaMemcpyToSymbol(c_pf, &tiles, sizeof(int)) == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
+}
 
 #define TC_DISPATCH(C, ...)  \
   switch (C) {               \
@@ -1224,9 +1306,9 @@ int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const flo
   cudaStream_t s = (cudaStream_t)stream;
   TC_DISPATCH(C, {
     const size_t smem =
-        mat_bytes(2 * CC, 2 * CC) + mat_bytes(CC, 2 * CC) + mat_bytes(3 * CC, CC) + tile_bytes(2 * CC);
+        mat_bytes(2 * CC, 2 * CC) + mat_bytes(CC, 2 * CC) + mat_bytes(3 * CC, CC) + 2 * tile_bytes(CC);
     if (!launch_prep(k_fuse_bwd_b_tc<CC>, smem)) return FFNO_ELAUNCH;
-    k_fuse_bwd_b_tc<CC><<<grid_tc1(V), PT, smem, s>>>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, hg,
+    k_fuse_bwd_b_tc<CC><<<grid_tc(V), CT, smem, s>>>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, hg,
                                                     fused_pre_bar, hf_bar, base, V,
                                                     static_cast<const uint8_t*>(wpack), x_bar, spec_bar, vert_bar,
                                                     err);

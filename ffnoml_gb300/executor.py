@@ -276,20 +276,26 @@ class Workspace:
         self.sa, self.sb = nb(spec_len), nb(spec_len)
         self.gates = nb(V, 2 * C)     # branch gates between the two tensor-core fuse stages
         self.va, self.vb = nb(2 * live * HW * C), nb(2 * live * HW * C)
+        self.hg = None                # the gate MLP's hidden pre-activation, kept only by a caching forward
 
     # the intermediates a block's VJP reads (kept per block when the forward caches block states)
     CACHED = ("xs", "xv", "yv", "spec_pre", "vert_pre", "fused_pre", "pw_pre", "mlp_pre", "x1", "x2", "vb")
 
-    def state_bytes(self):
-        """Device bytes of one block's cached intermediates."""
-        return sum(getattr(self, n).numel() * 4 for n in self.CACHED) + 2 * len(NORMS) * 8 * 64
+    def state_bytes(self, gates):
+        """Device bytes of one block's cached intermediates (gates: also the branch gates and the gate MLP's hidden
+        layer of the tensor-core fuse)."""
+        n = sum(getattr(self, n).numel() for n in self.CACHED) + (3 * self.x.numel() if gates else 0)
+        return 4 * n + 2 * len(NORMS) * 8 * 64
 
-    def fork(self):
+    def fork(self, gates):
         """A view of this workspace with its own copies of the cached intermediates and GroupNorm statistics (the
         scratch buffers stay shared): block i of a caching forward writes its state there."""
         w = copy.copy(self)
         for n in self.CACHED:
             setattr(w, n, torch.empty_like(getattr(self, n)))
+        if gates:
+            w.gates = torch.empty_like(self.gates)
+            w.hg = torch.empty_like(self.x)
         w.ys = w.xs
         w.coefs = dict(self.coefs)
         w.gstats = dict(self.gstats)
@@ -303,6 +309,8 @@ class Workspace:
         w = copy.copy(self)
         for n in self.CACHED + ("ys",):
             setattr(w, n, getattr(state, n))
+        if state.hg is not None:
+            w.gates, w.hg = state.gates, state.hg
         w.coefs = dict(self.coefs)
         w.gstats = dict(self.gstats)
         for n in NORMS:
@@ -506,7 +514,7 @@ class Executor:
             if ws is None or ws.live != hgt_b["live"]:
                 ws = Workspace(D, H, W, m.width, hgt_b["live"], pk.groups, x.device)
             if keep and cache is None:
-                cache = self.cache_states and self._fits(B * m.n_layers * ws.state_bytes(), x.device)
+                cache = self.cache_states and self._fits(B * m.n_layers * ws.state_bytes(self._tc()), x.device)
                 self.last_cached = cache
             xin, z = x[b], z_scale[b]
             self._depth_weights(ws, z, D, H * W)
@@ -514,7 +522,7 @@ class Executor:
             inputs = [ws.x.clone()] if keep else None
             blocks = [] if cache else None
             for i in range(m.n_layers):
-                wb = ws.fork() if cache else ws
+                wb = ws.fork(self._tc()) if cache else ws
                 self._block(pk, wb, i, z, D, H, W, hgt_b, pln, pfr[i])
                 if keep:
                     inputs.append(ws.x.clone())
@@ -605,7 +613,7 @@ class Executor:
         self._finalize(ws, "vert", bp["vert_g"], bp["vert_b"], tc)
         # gate + fuse
         if self._tc():
-            self._fuse1_tc(ws, bp, x, None)
+            self._fuse1_tc(ws, bp, x, ws.hg)
             nat.call("ffno_fuse2_tc", ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(), ws.vert_pre.data_ptr(),
                      ws.coefs["vert"].data_ptr(), ws.gates.data_ptr(), V, C, bp["tc_fuse2"].data_ptr(),
                      ws.dw.data_ptr(), ws.fused_pre.data_ptr(), ws.partials.data_ptr(), ws.nparts_tc, G,
@@ -883,13 +891,16 @@ class Executor:
         # x1 = x + r_f gelu(GN(fused_pre)); fused_pre = fuse(x, spec, vert)
         self._gn_bwd(ws, gb, 1, gb.g1, r_f, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], "fuse", gb.pbar)
         if tc:
-            self._fuse1_tc(ws, bp, x, gb.hg)
+            hg = ws.hg                     # gates and hidden layer kept from the forward, else recomputed
+            if hg is None:
+                hg = gb.hg
+                self._fuse1_tc(ws, bp, x, hg)
             cs, cv = ws.coefs["spec"].data_ptr(), ws.coefs["vert"].data_ptr()
             nat.call("ffno_fuse_bwd_a_tc", ws.spec_pre.data_ptr(), cs, ws.vert_pre.data_ptr(), cv,
                      ws.gates.data_ptr(), gb.pbar.data_ptr(), V, C, bp["tcb_fuse_a"].data_ptr(), gb.hfb.data_ptr(),
                      err, s)
             nat.call("ffno_fuse_bwd_b_tc", ws.spec_pre.data_ptr(), cs, ws.vert_pre.data_ptr(), cv,
-                     ws.gates.data_ptr(), gb.hg.data_ptr(), gb.pbar.data_ptr(), gb.hfb.data_ptr(), gb.g1.data_ptr(),
+                     ws.gates.data_ptr(), hg.data_ptr(), gb.pbar.data_ptr(), gb.hfb.data_ptr(), gb.g1.data_ptr(),
                      V, C, bp["tcb_fuse_b"].data_ptr(), gb.xacc.data_ptr(), gb.sbar.data_ptr(), gb.vbar.data_ptr(),
                      err, s)
         else:

@@ -255,6 +255,9 @@ int ffno_si_input_grads(const float* features, const float* x_bar, const float* 
  * ------------------------------------------------------------------------------------------------------------------ */
 int ffno_tc_parts(long V);
 int ffno_tc_width_supported(int C);
+/* L2 prefetch lookahead of the tensor-core pointwise kernels on the current device, in tiles of 128 voxels per
+ * pipeline (0..4; default 1): a tuning knob, synchronous, not to be called while those kernels run. */
+int ffno_tc_set_prefetch_tiles(int tiles);
 
 /* ffno_mlp2_fwd; wpack = [w1 (2C x C), w2 (C x 2C)]. */
 int ffno_mlp2_fwd_tc(int mode, const float* in, const float* prev_pre, const float* prev_coefs, float res, float* xout,
