@@ -97,7 +97,7 @@ template <bool GELU>
 __device__ __forceinline__ float4 gn_apply(float4 p, const Gn4& g) {
   float4 y = make_float4((p.x - g.m.x) * g.s.x + g.b.x, (p.y - g.m.y) * g.s.y + g.b.y, (p.z - g.m.z) * g.s.z + g.b.z,
                          (p.w - g.m.w) * g.s.w + g.b.w);
-  if (GELU) y = make_float4(gelu(y.x), gelu(y.y), gelu(y.z), gelu(y.w));
+  if (GELU) y = make_float4(gelu_tc(y.x), gelu_tc(y.y), gelu_tc(y.z), gelu_tc(y.w));
   return y;
 }
 
@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(CT, 1) k_mlp2_tc(const float* __restrict__ in,
       float v[16];
       tld(P, 0, c, v);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = gelu(v[i]);
+      for (int i = 0; i < 16; ++i) v[i] = gelu_tc(v[i]);
       if (f < 2 * C) put_mn(H, f, 64 * P.half + 16 * c, v);
     }
     if (!pipe_gemms(P, err, Gemm{P.tmem, w2, mop(H), 2 * C, false})) break;
@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(CT, 1) k_gate_tc(const float* __restrict__ x, 
       float v[16];
       rld(P, 0, j, v);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = gelu(v[i]);
+      for (int i = 0; i < 16; ++i) v[i] = gelu_tc(v[i]);
       put16(X, row, 16 * j, C, v);
     }
     if (!pipe_gemms(P, err, Gemm{P.tmem, kop(X, C), g2, C, false, C})) break;
@@ -566,8 +566,8 @@ __global__ void __launch_bounds__(CT, 1) k_gate_tc(const float* __restrict__ x, 
 #pragma unroll
         for (int i = 0; i < 16; i += 4) {
           const float4 xv = ld4(x + v * C + c0 + i);
-          float4 o = make_float4(xv.x * sigmoid(g[i]), xv.y * sigmoid(g[i + 1]), xv.z * sigmoid(g[i + 2]),
-                                 xv.w * sigmoid(g[i + 3]));
+          float4 o = make_float4(xv.x * sigmoid_tc(g[i]), xv.y * sigmoid_tc(g[i + 1]), xv.z * sigmoid_tc(g[i + 2]),
+                                 xv.w * sigmoid_tc(g[i + 3]));
           if (zp) {
             const float4 zz = ld4(zp + c0 + i);
             o = make_float4(fmaf(zz.x, zv, o.x), fmaf(zz.y, zv, o.y), fmaf(zz.z, zv, o.z), fmaf(zz.w, zv, o.w));
@@ -638,7 +638,7 @@ __global__ void __launch_bounds__(CT, 1) k_fuse1_tc(const float* __restrict__ x,
         for (int i = 0; i < 16; i += 4)
           *reinterpret_cast<float4*>(hg + v * C + c0 + i) = make_float4(h[i], h[i + 1], h[i + 2], h[i + 3]);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) h[i] = gelu(h[i]);
+      for (int i = 0; i < 16; ++i) h[i] = gelu_tc(h[i]);
       put16(A, f, c0, C, h);
     }
     if (!pipe_gemms(P, err, Gemm{P.tmem, wg2, kop(A, C), C, false})) break;
@@ -650,7 +650,7 @@ __global__ void __launch_bounds__(CT, 1) k_fuse1_tc(const float* __restrict__ x,
       if (f < 2 * C)
 #pragma unroll
         for (int i = 0; i < 16; ++i)
-          if (vb + i < V) gates[(vb + i) * 2 * C + f] = sigmoid(g[i] + bf);
+          if (vb + i < V) gates[(vb + i) * 2 * C + f] = sigmoid_tc(g[i] + bf);
     }
   }
   pipe_finish(P, tslot, 2 * NCOL);
@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp
       float h[16];
       tld(P, 0, c, h);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) h[i] = gelu(h[i]);
+      for (int i = 0; i < 16; ++i) h[i] = gelu_tc(h[i]);
       if (f < 2 * C) put_mn(A, f, 64 * P.half + 16 * c, h);
     }
     if (!pipe_gemms(P, err, Gemm{P.tmem, wf2, mop(A), 2 * C, false})) break;
@@ -724,8 +724,8 @@ __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp
         for (int i = 0; i < 16; ++i) {
           const long v = vb + i;
           if (v < V) {
-            const float s = gelu((__ldg(sp + v * C + f) - sm) * ss + sb) * __ldg(gates + v * 2 * C + f);
-            const float u = gelu((__ldg(vp + v * C + f) - vm) * vs + vbb) * __ldg(gates + v * 2 * C + C + f);
+            const float s = gelu_tc((__ldg(sp + v * C + f) - sm) * ss + sb) * __ldg(gates + v * 2 * C + f);
+            const float u = gelu_tc((__ldg(vp + v * C + f) - vm) * vs + vbb) * __ldg(gates + v * 2 * C + C + f);
             o[i] += 0.5f * (s + u);
             pre[v * C + f] = o[i];
           }
@@ -783,7 +783,7 @@ __global__ void __launch_bounds__(CT, 1) k_mlp2_bwd_tc(const float* __restrict__
       tld(P, 0, c, hp);
       tld(P, TM, c, gb);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) gb[i] *= gelu_grad(hp[i]);
+      for (int i = 0; i < 16; ++i) gb[i] *= gelu_grad_tc(hp[i]);
       if (f < 2 * C) put_mn(H, f, 64 * P.half + 16 * c, gb);
     }
     if (!pipe_gemms(P, err, Gemm{P.tmem, mop(H), w1t, 2 * C, false, C})) break;
@@ -851,7 +851,7 @@ __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__
       float h[16];
       rld(P, D1, j, h);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) h[i] = gelu(h[i]);
+      for (int i = 0; i < 16; ++i) h[i] = gelu_tc(h[i]);
       put16(T, row, 16 * j, C, h);
     }
     if (!pipe_gemms(P, err, Gemm{P.tmem + D2, kop(T, C), g2, C, false, C})) break;
@@ -872,7 +872,7 @@ __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__
           float o[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
-            const float s = sigmoid(g[i + u]);
+            const float s = sigmoid_tc(g[i + u]);
             o[u] = bb[u] * s;
             q[i + u] = bb[u] * xx[u] * s * (1.f - s);
             if (zp) zs = fmaf(bb[u], __ldg(zp + c0 + i + u), zs);
@@ -900,7 +900,7 @@ __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__
       rld(P, D3, j, hb);
       rld(P, D1, j, hp);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) hb[i] *= gelu_grad(hp[i]);
+      for (int i = 0; i < 16; ++i) hb[i] *= gelu_grad_tc(hp[i]);
       put16(T, row, 16 * j, C, hb);
     }
     if (!pipe_gemms(P, err, Gemm{P.tmem + D4, kop(T, C), g1t, C, false, C})) break;
@@ -976,7 +976,7 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_a_tc(const float* __restrict
       if (f < 2 * C)
 #pragma unroll
         for (int i = 0; i < 16; ++i)
-          if (vb + i < V) hfb[(vb + i) * 2 * C + f] = hb[i] * gelu_grad(hp[i]);
+          if (vb + i < V) hfb[(vb + i) * 2 * C + f] = hb[i] * gelu_grad_tc(hp[i]);
     }
   }
   pipe_finish(P, tslot, 2 * NCOL);
@@ -1082,10 +1082,10 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
 #pragma unroll
       for (int i = 0; i < 16; i += 4) {
         const float4 h4 = v < V ? ld4(hg + v * C + c0 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-        hb[i] *= gelu_grad(h4.x);
-        hb[i + 1] *= gelu_grad(h4.y);
-        hb[i + 2] *= gelu_grad(h4.z);
-        hb[i + 3] *= gelu_grad(h4.w);
+        hb[i] *= gelu_grad_tc(h4.x);
+        hb[i + 1] *= gelu_grad_tc(h4.y);
+        hb[i + 2] *= gelu_grad_tc(h4.z);
+        hb[i + 3] *= gelu_grad_tc(h4.w);
       }
       put16(T, row, c0, C, hb);
     }
