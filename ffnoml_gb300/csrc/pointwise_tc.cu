@@ -22,6 +22,7 @@
 
 #include "common.cuh"
 #include "tc.cuh"
+#include "ws.h"
 
 using namespace ffno;
 
@@ -1259,6 +1260,7 @@ int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, lo
                      float* a_bar, int* err, ffno_stream_t stream) {
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
+  if (ws::mlp2_bwd_supported(C)) return ws::mlp2_bwd(a, pre_bar, base, V, C, wpack, a_bar, err, s);
   TC_DISPATCH(C, {
     const size_t smem = 3 * mat_bytes(2 * CC, CC) + 2 * tile_bytes(2 * CC);
     if (!launch_prep(k_mlp2_bwd_tc<CC>, smem)) return FFNO_ELAUNCH;

@@ -1,0 +1,326 @@
+// Warp-specialised tensor-core form of the channel-MLP backward (the ffno_mlp2_bwd contract):
+//   a_bar = base + ((pre_bar W2^T) * gelu'(a W1)) W1^T,   W1: [2C][C], W2: [C][2C], split-BF16 products.
+//
+// One persistent CTA per SM walks 128-voxel tiles with five roles that hand work to each other through mbarriers, so
+// HBM reads, format conversion, tensor-core MMAs and the two epilogues of different tiles overlap:
+//   warp 0       TMA: FP32 tiles of a and pre_bar ([128 voxels][32 channels] boxes, 128-byte swizzle) into a
+//                two-stage shared-memory ring;
+//   warp 1       MMA issue (one thread): GEMM1 D1 = a W1^T and GEMM2 D2 = pre_bar W2, then GEMM3 D3 = G W1;
+//   warps 2-5    conversion: FP32 rows from the ring -> split BF16 (hi = bf16(x), lo = bf16(x - hi)) written straight
+//                into tensor memory, where they are the A operands of GEMM1/2 (lane = voxel);
+//   warps 6-13   epilogue 1: G = D2 * gelu'(D1), split and written back over D1 (per 16-feature chunk: 8 columns hi,
+//                8 columns lo), the A operand of GEMM3;
+//   warps 14-17  epilogue 2: a_bar = base + D3 to HBM.
+// Tensor memory (512 columns): two A stages of 128 columns [a hi | a lo | pre_bar hi | pre_bar lo] (D3 of the stage's
+// tile lands over its a half), D1 at 256, D2 at 384. Every wait is bounded; a time-out records a code in *err, the
+// role stops, the others run into their own bounded waits, and the CTA frees tensor memory only after the last MMA
+// commit and every issued TMA copy have been waited for.
+#include "common.cuh"
+#include "tc.cuh"
+#include "ws.h"
+
+using namespace ffno;
+
+namespace {
+
+constexpr int TM = 128;
+constexpr int NWARPS = 18;
+constexpr int NTHREADS = NWARPS * 32;
+constexpr int W_TMA = 0, W_MMA = 1, W_CVT = 2, W_E1 = 6, W_E2 = 14;
+constexpr uint32_t BOX_BYTES = TM * 32 * 4;   // one [128][32] FP32 box
+constexpr uint32_t D1 = 256, D2 = 384;        // accumulator columns
+
+__host__ __device__ constexpr uint32_t mat_bytes(int R, int K) { return (uint32_t)R * K * 2 * 2; }
+
+struct Bars {
+  uint64_t stg_full[2], stg_empty[2], a_full[2], a_empty[2], d3_full[2], d_full, g_full, w;
+};
+
+constexpr uint64_t WAIT_NS = 1000000000ull;   // one second: every legitimate wait here lasts microseconds
+
+__device__ __forceinline__ bool wait_or_flag(uint64_t* bar, uint32_t parity, int* err, int code) {
+  if (tc::mbar_wait_for(bar, parity, WAIT_NS)) return true;
+  atomicExch(err, code);
+  return false;
+}
+
+// The same for a whole warp (tcgen05.ld / st are warp-collective): the warp goes on only if every lane saw the phase.
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+  const bool ok = __all_sync(0xffffffffu, tc::mbar_wait_for(bar, parity, WAIT_NS)) != 0;
+  if (!ok && (threadIdx.x & 31) == 0) atomicExch(err, code);
+  return ok;
+}
+
+// three split products into d: (A hi, B hi), (A hi, B lo), (A lo, B hi) for one 16-wide k step
+__device__ __forceinline__ void mma3_ta(uint32_t d, uint32_t a_hi, uint32_t a_lo, uint64_t b_hi, uint64_t b_lo,
+                                        uint32_t idesc, bool acc) {
+  tc::mma_bf16_ta(d, a_hi, b_hi, idesc, acc ? 1u : 0u);
+  tc::mma_bf16_ta(d, a_hi, b_lo, idesc, 1u);
+  tc::mma_bf16_ta(d, a_lo, b_hi, idesc, 1u);
+}
+
+template <int C>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_mlp2_bwd_ws(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_pb,
+                  const float* __restrict__ base, long V, const uint8_t* __restrict__ wpack, float* __restrict__ abar,
+                  int* __restrict__ err) {
+  static_assert(C == 32 || C == 64, "widths 32 and 64");
+  constexpr uint32_t B1 = mat_bytes(2 * C, C);   // each of w1 (2C x C), w2t (2C x C), w1t (C x 2C)
+  constexpr uint32_t WB = 3 * B1;
+  constexpr int NB = C / 32;                     // TMA boxes per tensor tile
+  constexpr uint32_t XB = NB * BOX_BYTES;        // one tensor's FP32 tile
+  constexpr uint32_t SB = 2 * XB;                // one ring stage: a, pre_bar
+  static_assert(WB % 1024 == 0, "the ring must stay 1024-byte aligned (128-byte swizzle)");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* ring = smem + WB;
+  __shared__ Bars bars;
+  __shared__ uint32_t tslot;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) tc::tmem_alloc(&tslot, 512);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; ++s) {
+      tc::mbar_init(&bars.stg_full[s], 1);
+      tc::mbar_init(&bars.stg_empty[s], 128);
+      tc::mbar_init(&bars.a_full[s], 128);
+      tc::mbar_init(&bars.a_empty[s], 128);
+      tc::mbar_init(&bars.d3_full[s], 1);
+    }
+    tc::mbar_init(&bars.d_full, 1);
+    tc::mbar_init(&bars.g_full, 256);
+    tc::mbar_init(&bars.w, 1);
+    tc::mbar_init_fence();
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  const uint32_t tmem = tslot;
+  if (threadIdx.x == 0) {
+    tc::mbar_arrive_expect_tx(&bars.w, WB);
+    for (uint32_t off = 0; off < WB; off += 32768u)
+      tc::bulk_g2s(smem + off, wpack + off, WB - off < 32768u ? WB - off : 32768u, &bars.w);
+  }
+  const bool ok = __syncthreads_and(tc::mbar_wait_for(&bars.w, 0, WAIT_NS)) != 0;
+  if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+
+  const long nt = (V + TM - 1) / TM;
+  const int niter = (long)blockIdx.x < nt ? (int)((nt - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  auto tile_of = [&](int i) { return (long)blockIdx.x + (long)i * gridDim.x; };
+
+  if (ok && warp == W_TMA && lane == 0) {
+    int issued[2] = {0, 0};
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!wait_or_flag(&bars.stg_empty[s], (n & 1u) ^ 1u, err, 3)) break;
+      const int row = (int)(tile_of(i) * TM);
+      tc::mbar_arrive_expect_tx(&bars.stg_full[s], SB);
+      uint8_t* st = ring + s * SB;
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        tc::tma_load_2d(st + b * BOX_BYTES, &map_a, 32 * b, row, &bars.stg_full[s]);
+        tc::tma_load_2d(st + XB + b * BOX_BYTES, &map_pb, 32 * b, row, &bars.stg_full[s]);
+      }
+      ++issued[s];
+    }
+    for (int s = 0; s < 2; ++s)   // every copy has landed before the CTA may exit
+      if (issued[s]) tc::mbar_wait_for(&bars.stg_full[s], (uint32_t)(issued[s] - 1) & 1u, WAIT_NS);
+  } else if (ok && warp == W_MMA && lane == 0) {
+    const uint32_t i12 = tc::idesc_bf16(128, 2 * C), i3 = tc::idesc_bf16(128, C);
+    const uint32_t w1 = tc::smem_u32(smem), w2t = w1 + B1, w1t = w1 + 2 * B1, LO = B1 / 2;
+    uint64_t* last = nullptr;   // the last commit's barrier and phase parity, waited for before exit
+    uint32_t last_par = 0;
+    bool last_seen = true;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!wait_or_flag(&bars.a_full[s], n & 1u, err, 4)) break;
+      if (i > 0) {   // GEMM3 of the previous tile has read G out of D1
+        if (!wait_or_flag(&bars.d3_full[(i - 1) & 1], ((uint32_t)(i - 1) >> 1) & 1u, err, 5)) break;
+        last_seen = true;
+      }
+      tc::tc_after_sync();
+      const uint32_t A = tmem + (uint32_t)(128 * s);
+#pragma unroll 1
+      for (int k = 0; k < C / 16; ++k) {
+        const uint32_t ah = A + 8u * k, al = A + C / 2 + 8u * k;
+        const uint32_t ph = A + C + 8u * k, pl = A + C + C / 2 + 8u * k;
+        const uint32_t bo = 256u * k;
+        mma3_ta(tmem + D1, ah, al, tc::kmajor_desc(w1 + bo, 128u, C * 16u), tc::kmajor_desc(w1 + LO + bo, 128u, C * 16u),
+                i12, k > 0);
+        mma3_ta(tmem + D2, ph, pl, tc::kmajor_desc(w2t + bo, 128u, C * 16u),
+                tc::kmajor_desc(w2t + LO + bo, 128u, C * 16u), i12, k > 0);
+      }
+      tc::mma_commit(&bars.d_full);
+      last = &bars.d_full;
+      last_par = (uint32_t)i & 1u;
+      last_seen = false;
+      if (!wait_or_flag(&bars.g_full, (uint32_t)i & 1u, err, 6)) break;
+      tc::tc_after_sync();
+#pragma unroll 1
+      for (int j = 0; j < 2 * C / 16; ++j) {
+        const uint32_t bo = 256u * j;
+        mma3_ta(tmem + (uint32_t)(128 * s), tmem + D1 + 16u * j, tmem + D1 + 16u * j + 8u,
+                tc::kmajor_desc(w1t + bo, 128u, 2 * C * 16u), tc::kmajor_desc(w1t + LO + bo, 128u, 2 * C * 16u), i3,
+                j > 0);
+      }
+      tc::mma_commit(&bars.d3_full[s]);
+      last = &bars.d3_full[s];
+      last_par = n & 1u;
+      last_seen = false;
+    }
+    if (last && !last_seen) tc::mbar_wait_for(last, last_par, WAIT_NS);   // no MMA in flight when tensor memory is freed
+  } else if (ok && warp >= W_CVT && warp < W_E1) {
+    const int q = warp & 3, r = 32 * q + lane;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!warp_wait(&bars.stg_full[s], n & 1u, err, 7)) break;
+      if (!warp_wait(&bars.a_empty[s], (n & 1u) ^ 1u, err, 8)) break;
+      tc::tc_after_sync();
+      const uint8_t* st = ring + s * SB;
+      const uint32_t A = tmem + lq + (uint32_t)(128 * s);
+#pragma unroll
+      for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+          const uint8_t* rowp = st + x * XB + b * BOX_BYTES + r * 128;
+          uint32_t hi[16], lo[16];
+#pragma unroll
+          for (int c = 0; c < 8; ++c) {
+            const float4 v = *reinterpret_cast<const float4*>(rowp + ((c ^ (r & 7)) << 4));
+            tc::split_pack(v.x, v.y, hi[2 * c], lo[2 * c]);
+            tc::split_pack(v.z, v.w, hi[2 * c + 1], lo[2 * c + 1]);
+          }
+          tc::tmem_st16u(A + (uint32_t)(x * C + 16 * b), hi);
+          tc::tmem_st16u(A + (uint32_t)(x * C + C / 2 + 16 * b), lo);
+        }
+      tc::mbar_arrive(&bars.stg_empty[s]);
+      tc::tmem_wait_st();
+      tc::tc_before_sync();
+      tc::mbar_arrive(&bars.a_full[s]);
+    }
+  } else if (ok && warp >= W_E1 && warp < W_E2) {
+    const int q = warp & 3, hf = (warp - W_E1) >> 2;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      if (!warp_wait(&bars.d_full, (uint32_t)i & 1u, err, 9)) break;
+      tc::tc_after_sync();
+#pragma unroll 1
+      for (int j = hf; j < 2 * C / 16; j += 2) {
+        uint32_t h[16], gb[16];
+        tc::tmem_ld16u(tmem + lq + D1 + 16u * j, h);
+        tc::tmem_ld16u(tmem + lq + D2 + 16u * j, gb);
+        tc::tmem_wait_ld();
+        uint32_t hi[8], lo[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const float g0 = __uint_as_float(gb[2 * e]) * gelu_grad_tc(__uint_as_float(h[2 * e]));
+          const float g1 = __uint_as_float(gb[2 * e + 1]) * gelu_grad_tc(__uint_as_float(h[2 * e + 1]));
+          tc::split_pack(g0, g1, hi[e], lo[e]);
+        }
+        tc::tmem_st8u(tmem + lq + D1 + 16u * j, hi);
+        tc::tmem_st8u(tmem + lq + D1 + 16u * j + 8u, lo);
+      }
+      tc::tmem_wait_st();
+      tc::tc_before_sync();
+      tc::mbar_arrive(&bars.g_full);
+    }
+  } else if (ok && warp >= W_E2) {
+    const int q = warp & 3, r = 32 * q + lane;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      const long v = tile_of(i) * TM + r;
+      const bool live = v < V;
+      float4 bv[C / 4];
+#pragma unroll
+      for (int c = 0; c < C / 4; ++c)
+        bv[c] = (base && live) ? __ldg(reinterpret_cast<const float4*>(base + v * C) + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (!warp_wait(&bars.d3_full[s], n & 1u, err, 10)) break;
+      tc::tc_after_sync();
+#pragma unroll
+      for (int k = 0; k < C / 16; ++k) {
+        uint32_t d[16];
+        tc::tmem_ld16u(tmem + lq + (uint32_t)(128 * s + 16 * k), d);
+        tc::tmem_wait_ld();
+        if (k == C / 16 - 1) {   // the stage's tensor memory is free once D3 is in registers
+          tc::tc_before_sync();
+          tc::mbar_arrive(&bars.a_empty[s]);
+        }
+        if (live) {
+          float4* o = reinterpret_cast<float4*>(abar + v * C + 16 * k);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const float4 b4 = bv[4 * k + e];
+            o[e] = make_float4(b4.x + __uint_as_float(d[4 * e]), b4.y + __uint_as_float(d[4 * e + 1]),
+                               b4.z + __uint_as_float(d[4 * e + 2]), b4.w + __uint_as_float(d[4 * e + 3]));
+          }
+        }
+      }
+    }
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  if (warp == 0) tc::tmem_free(tmem, 512);
+}
+
+int g_sms = 0;
+int sms() {
+  if (!g_sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sms <= 0) g_sms = 152;
+  }
+  return g_sms;
+}
+
+// [V][C] FP32 rows as [128 voxels][32 channels] boxes with the 128-byte swizzle; rows past V read as zero
+bool row_map(CUtensorMap* map, const float* p, long V, int C) {
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tc::tensor_map_encoder();
+  if (!encode) return false;
+  cuuint64_t gdim[2] = {(cuuint64_t)C, (cuuint64_t)V};
+  cuuint64_t gstr[1] = {(cuuint64_t)C * 4};
+  cuuint32_t box[2] = {32u, (cuuint32_t)TM};
+  cuuint32_t estr[2] = {1u, 1u};
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(p), gdim, gstr, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int C>
+int launch_mlp2_bwd(const float* a, const float* pb, const float* base, long V, const void* wpack, float* abar,
+                    int* err, cudaStream_t s) {
+  CUtensorMap ma, mp;
+  if (!row_map(&ma, a, V, C) || !row_map(&mp, pb, V, C)) return FFNO_EINVAL;
+  const size_t smem = 1024 + 3 * (size_t)mat_bytes(2 * C, C) + 2 * (size_t)(2 * (C / 32) * BOX_BYTES);
+  if (cudaFuncSetAttribute(k_mlp2_bwd_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return FFNO_ELAUNCH;
+  const long nt = (V + TM - 1) / TM;
+  const int grid = (int)(nt < sms() ? nt : sms());
+  k_mlp2_bwd_ws<C><<<grid, NTHREADS, smem, s>>>(ma, mp, base, V, static_cast<const uint8_t*>(wpack), abar, err);
+  return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
+}
+
+}  // namespace
+
+namespace ffno {
+namespace ws {
+
+bool mlp2_bwd_supported(int C) { return C == 32 || C == 64; }
+
+int mlp2_bwd(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack, float* a_bar,
+             int* err, cudaStream_t stream) {
+  if (V < 1 || V > 0x7fffffffL - TM || (reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(pre_bar)) % 16)
+    return FFNO_EINVAL;
+  if (C == 64) return launch_mlp2_bwd<64>(a, pre_bar, base, V, wpack, a_bar, err, stream);
+  if (C == 32) return launch_mlp2_bwd<32>(a, pre_bar, base, V, wpack, a_bar, err, stream);
+  return FFNO_EINVAL;
+}
+
+}  // namespace ws
+}  // namespace ffno

@@ -645,19 +645,6 @@ __global__ void __launch_bounds__(XT, 1)
   if (warp == 0) tc::tmem_free(tmem, 512);
 }
 
-// cuTensorMapEncodeTiled through the runtime's driver entry point (the library does not link the driver directly)
-PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      f = nullptr;
-    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-  }();
-  return fn;
-}
-
 int g_sms = 0;
 int sms() {
   if (!g_sms) {
@@ -761,7 +748,7 @@ int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, 
   cuuint32_t box[4] = {(cuuint32_t)CB, d[0].box, d[1].box, d[2].box};
   cuuint32_t estr[4] = {1, 1, 1, 1};
   CUtensorMap map;
-  const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tc::tensor_map_encoder();
   if (!encode) return FFNO_ELAUNCH;
   if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(in), gdim, gstr, box, estr,
                              CU_TENSOR_MAP_INTERLEAVE_NONE,

@@ -151,8 +151,9 @@ def test_fuse_fwd_tc(C):
     _close(b, a)
 
 
-@pytest.mark.parametrize("C", [16, 32, 64])
-def test_mlp2_bwd_tc(C):
+@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (32, 152 * 128 * 5 + 77), (64, 152 * 128 * 5 + 77)])
+def test_mlp2_bwd_tc(C, V):
+    """Also at a voxel count that sends several tiles through every CTA's two-stage ring, with a ragged last tile."""
     nat = _nat()
     a, pb, base = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3)
     w1, w2 = _rand(2 * C, C, seed=4, scale=C ** -0.5), _rand(C, 2 * C, seed=5, scale=(2 * C) ** -0.5)
