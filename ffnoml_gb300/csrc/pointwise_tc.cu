@@ -1195,6 +1195,8 @@ int ffno_mlp2_fwd_tc(int mode, const float* in, const float* prev_pre, const flo
   if (mode && (!prev_pre || !prev_coefs || !xout)) return FFNO_EINVAL;
   if (nparts != grid_tc(V)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
+  if (ws::mlp2_fwd_supported(C))
+    return ws::mlp2_fwd(mode, in, prev_pre, prev_coefs, res, xout, V, C, wpack, dw, pre, partials, nparts, err, s);
   const auto* w = static_cast<const uint8_t*>(wpack);
   TC_DISPATCH(C, {
     const size_t smem = mat_bytes(2 * CC, CC) + mat_bytes(CC, 2 * CC) + 2 * tile_bytes(2 * CC);

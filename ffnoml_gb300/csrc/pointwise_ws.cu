@@ -59,6 +59,24 @@ __device__ __forceinline__ void mma3_ta(uint32_t d, uint32_t a_hi, uint32_t a_lo
   tc::mma_bf16_ta(d, a_lo, b_hi, idesc, 1u);
 }
 
+__device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
+  return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+}
+
+// barrier of the four epilogue-2 warps (named barrier 1)
+__device__ __forceinline__ void e2_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+// The same barrier returning whether p holds in all four warps, so that they leave their tile loop together.
+__device__ __forceinline__ bool e2_sync_and(bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.and.pred po, 1, 128, pi;\n selp.u32 %0, 1, 0, po;\n}"
+      : "=r"(r)
+      : "r"((uint32_t)p)
+      : "memory");
+  return r != 0;
+}
+
 template <int C>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_mlp2_bwd_ws(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_pb,
@@ -268,6 +286,291 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) tc::tmem_free(tmem, 512);
 }
 
+// ================================================================================================ forward
+// The ffno_mlp2_fwd contract: pre = W2 gelu(W1 x) with x = in (MODE 0) or x = in + res act(GN(prev)) written to xout
+// (MODE 1: act = GELU, MODE 2: identity), and the depth-weighted GroupNorm partials of pre (one per CTA, its tiles
+// merged in order with Chan's update, so the statistics do not depend on timing). Roles as in the backward:
+//   warp 0 TMA ring of in [and prev]; warp 1 MMA: GEMM1 D1[t % 2] = x W1^T (N = 2C), and GEMM2 D2 = H W2^T (N = C)
+//   one tile behind, so that epilogue 1 of a tile overlaps GEMM1 of the next; warps 2-5 conversion with the residual
+//   prologue (xout); warps 6-13 epilogue 1: H = gelu(D1), split over D1; warps 14-17 epilogue 2: pre and statistics.
+// Tensor memory: A stages at 0 and 128 ([x hi | x lo], D2 of the stage's tile over them), D1 buffers at 256 and 384.
+template <int C, int MODE>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_mlp2_fwd_ws(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_prev,
+                  const float* __restrict__ pc, float res, float* __restrict__ xout, long V,
+                  const uint8_t* __restrict__ wpack, const float* __restrict__ dw, float* __restrict__ pre,
+                  double* __restrict__ partials, int* __restrict__ err) {
+  static_assert(C == 32 || C == 64, "widths 32 and 64");
+  constexpr uint32_t B1 = mat_bytes(2 * C, C);   // w1 (2C x C); w2 (C x 2C) has the same size
+  constexpr uint32_t WB = 2 * B1;
+  constexpr int NB = C / 32, NX = MODE == 0 ? 1 : 2, CPG = C / GMAX;
+  constexpr uint32_t XB = NB * BOX_BYTES, SB = NX * XB;
+  static_assert(WB % 1024 == 0, "the ring must stay 1024-byte aligned (128-byte swizzle)");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint8_t* ring = smem + WB;
+  __shared__ uint64_t stg_full[2], stg_empty[2], a_full[2], a_empty[2], d1_full[2], h_full[2], d2_full[2], wbar;
+  __shared__ uint32_t tslot;
+  __shared__ float cf[3 * C];                 // GroupNorm coefficients of prev: mean, gamma rstd, beta
+  __shared__ float red[4][GMAX + 1], gmean[GMAX], wsum;
+  __shared__ double acc[GMAX * 3];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) tc::tmem_alloc(&tslot, 512);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; ++s) {
+      tc::mbar_init(&stg_full[s], 1);
+      tc::mbar_init(&stg_empty[s], 128);
+      tc::mbar_init(&a_full[s], 128);
+      tc::mbar_init(&a_empty[s], 128);
+      tc::mbar_init(&d1_full[s], 1);
+      tc::mbar_init(&h_full[s], 256);
+      tc::mbar_init(&d2_full[s], 1);
+    }
+    tc::mbar_init(&wbar, 1);
+    tc::mbar_init_fence();
+  }
+  if (MODE != 0)
+    for (int e = threadIdx.x; e < 3 * C; e += NTHREADS) cf[e] = pc[e];
+  if (threadIdx.x < GMAX * 3) acc[threadIdx.x] = 0.0;
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  const uint32_t tmem = tslot;
+  if (threadIdx.x == 0) {
+    tc::mbar_arrive_expect_tx(&wbar, WB);
+    for (uint32_t off = 0; off < WB; off += 32768u)
+      tc::bulk_g2s(smem + off, wpack + off, WB - off < 32768u ? WB - off : 32768u, &wbar);
+  }
+  const bool ok = __syncthreads_and(tc::mbar_wait_for(&wbar, 0, WAIT_NS)) != 0;
+  if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+
+  const long nt = (V + TM - 1) / TM;
+  const int niter = (long)blockIdx.x < nt ? (int)((nt - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  auto tile_of = [&](int i) { return (long)blockIdx.x + (long)i * gridDim.x; };
+
+  if (ok && warp == W_TMA && lane == 0) {
+    int issued[2] = {0, 0};
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!wait_or_flag(&stg_empty[s], (n & 1u) ^ 1u, err, 3)) break;
+      const int row = (int)(tile_of(i) * TM);
+      tc::mbar_arrive_expect_tx(&stg_full[s], SB);
+      uint8_t* st = ring + s * SB;
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        tc::tma_load_2d(st + b * BOX_BYTES, &map_in, 32 * b, row, &stg_full[s]);
+        if (MODE != 0) tc::tma_load_2d(st + XB + b * BOX_BYTES, &map_prev, 32 * b, row, &stg_full[s]);
+      }
+      ++issued[s];
+    }
+    for (int s = 0; s < 2; ++s)
+      if (issued[s]) tc::mbar_wait_for(&stg_full[s], (uint32_t)(issued[s] - 1) & 1u, WAIT_NS);
+  } else if (ok && warp == W_MMA && lane == 0) {
+    const uint32_t i1 = tc::idesc_bf16(128, 2 * C), i2 = tc::idesc_bf16(128, C);
+    const uint32_t w1 = tc::smem_u32(smem), w2 = w1 + B1, LO = B1 / 2;
+    uint64_t* last = nullptr;
+    uint32_t last_par = 0;
+    bool alive = true;
+    auto gemm2 = [&](int j) {   // D2 (A stage j % 2) = H(j) (in D1[j % 2]) W2^T, K = 2C
+      const uint32_t h = tmem + 256u + 128u * (j & 1);
+#pragma unroll 1
+      for (int k = 0; k < 2 * C / 16; ++k)
+        mma3_ta(tmem + 128u * (j & 1), h + 16u * k, h + 16u * k + 8u, tc::kmajor_desc(w2 + 256u * k, 128u, 2 * C * 16u),
+                tc::kmajor_desc(w2 + LO + 256u * k, 128u, 2 * C * 16u), i2, k > 0);
+      tc::mma_commit(&d2_full[j & 1]);
+      last = &d2_full[j & 1];
+      last_par = ((uint32_t)j >> 1) & 1u;
+    };
+    for (int i = 0; i < niter && alive; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      // a_full implies the stage's previous D2 was read, hence GEMM2 of tile i-2 (reader of D1[s]) is complete
+      if (!wait_or_flag(&a_full[s], n & 1u, err, 4)) {
+        alive = false;
+        break;
+      }
+      tc::tc_after_sync();
+      const uint32_t A = tmem + 128u * s, D = tmem + 256u + 128u * s;
+#pragma unroll 1
+      for (int k = 0; k < C / 16; ++k)
+        mma3_ta(D, A + 8u * k, A + C / 2 + 8u * k, tc::kmajor_desc(w1 + 256u * k, 128u, C * 16u),
+                tc::kmajor_desc(w1 + LO + 256u * k, 128u, C * 16u), i1, k > 0);
+      tc::mma_commit(&d1_full[s]);
+      last = &d1_full[s];
+      last_par = n & 1u;
+      if (i >= 1) {
+        if (!wait_or_flag(&h_full[(i - 1) & 1], ((uint32_t)(i - 1) >> 1) & 1u, err, 5)) { alive = false; break; }
+        tc::tc_after_sync();
+        gemm2(i - 1);
+      }
+    }
+    if (alive && niter >= 1) {
+      const int j = niter - 1;
+      if (wait_or_flag(&h_full[j & 1], ((uint32_t)j >> 1) & 1u, err, 6)) {
+        tc::tc_after_sync();
+        gemm2(j);
+      }
+    }
+    if (last) tc::mbar_wait_for(last, last_par, WAIT_NS);   // no MMA in flight when tensor memory is freed
+  } else if (ok && warp >= W_CVT && warp < W_E1) {
+    const int q = warp & 3, r = 32 * q + lane;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!warp_wait(&stg_full[s], n & 1u, err, 7)) break;
+      if (!warp_wait(&a_empty[s], (n & 1u) ^ 1u, err, 8)) break;
+      tc::tc_after_sync();
+      const uint8_t* st = ring + s * SB;
+      const uint32_t A = tmem + lq + 128u * s;
+      const long v = tile_of(i) * TM + r;
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        const uint8_t* rin = st + b * BOX_BYTES + r * 128;
+        uint32_t hi[16], lo[16];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const uint32_t o = (uint32_t)((c ^ (r & 7)) << 4);
+          float4 x = *reinterpret_cast<const float4*>(rin + o);
+          if (MODE != 0) {
+            const float4 p = *reinterpret_cast<const float4*>(rin + XB + o);
+            const int k = 32 * b + 4 * c;
+            float y[4] = {p.x, p.y, p.z, p.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              y[e] = (y[e] - cf[k + e]) * cf[C + k + e] + cf[2 * C + k + e];
+              if (MODE == 1) y[e] = gelu_tc(y[e]);
+            }
+            x = make_float4(fmaf(res, y[0], x.x), fmaf(res, y[1], x.y), fmaf(res, y[2], x.z), fmaf(res, y[3], x.w));
+            if (v < V) *reinterpret_cast<float4*>(xout + v * C + k) = x;
+          }
+          tc::split_pack(x.x, x.y, hi[2 * c], lo[2 * c]);
+          tc::split_pack(x.z, x.w, hi[2 * c + 1], lo[2 * c + 1]);
+        }
+        tc::tmem_st16u(A + (uint32_t)(16 * b), hi);
+        tc::tmem_st16u(A + (uint32_t)(C / 2 + 16 * b), lo);
+      }
+      tc::mbar_arrive(&stg_empty[s]);
+      tc::tmem_wait_st();
+      tc::tc_before_sync();
+      tc::mbar_arrive(&a_full[s]);
+    }
+  } else if (ok && warp >= W_E1 && warp < W_E2) {
+    const int q = warp & 3, hf = (warp - W_E1) >> 2;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!warp_wait(&d1_full[s], n & 1u, err, 9)) break;
+      tc::tc_after_sync();
+      const uint32_t D = tmem + lq + 256u + 128u * s;
+#pragma unroll 1
+      for (int j = hf; j < 2 * C / 16; j += 2) {
+        uint32_t h[16];
+        tc::tmem_ld16u(D + 16u * j, h);
+        tc::tmem_wait_ld();
+        uint32_t hi[8], lo[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          tc::split_pack(gelu_tc(__uint_as_float(h[2 * e])), gelu_tc(__uint_as_float(h[2 * e + 1])), hi[e], lo[e]);
+        tc::tmem_st8u(D + 16u * j, hi);
+        tc::tmem_st8u(D + 16u * j + 8u, lo);
+      }
+      tc::tmem_wait_st();
+      tc::tc_before_sync();
+      tc::mbar_arrive(&h_full[s]);
+    }
+  } else if (ok && warp >= W_E2) {
+    const int q = warp & 3, r = 32 * q + lane, wl = warp - W_E2;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      const long v = tile_of(i) * TM + r;
+      const bool live = v < V;
+      const float w = live ? __ldg(dw + v) : 0.f;
+      if (!e2_sync_and(tc::mbar_wait_for(&d2_full[s], n & 1u, WAIT_NS))) {
+        if (lane == 0) atomicExch(err, 10);
+        break;
+      }
+      tc::tc_after_sync();
+      float o[C];
+#pragma unroll
+      for (int k = 0; k < C / 16; ++k) {
+        uint32_t d[16];
+        tc::tmem_ld16u(tmem + lq + 128u * s + 16u * k, d);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int e = 0; e < 16; ++e) o[16 * k + e] = __uint_as_float(d[e]);
+      }
+      tc::tc_before_sync();
+      tc::mbar_arrive(&a_empty[s]);   // D2 is in registers: the stage may take the tile after next
+      if (live)
+#pragma unroll
+        for (int k = 0; k < C / 4; ++k)
+          *reinterpret_cast<float4*>(pre + v * C + 4 * k) = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+      // depth-weighted statistics of the tile: per group, sum then centred sum of squares over its 128 rows
+      float ws = w;
+#pragma unroll
+      for (int m = 16; m; m >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, m);
+#pragma unroll
+      for (int g = 0; g < GMAX; ++g) {
+        float t = 0.f;
+#pragma unroll
+        for (int c = 0; c < CPG; ++c) t += o[g * CPG + c];
+        t *= w;
+#pragma unroll
+        for (int m = 16; m; m >>= 1) t += __shfl_xor_sync(0xffffffffu, t, m);
+        if (lane == 0) red[wl][g] = t;
+      }
+      if (lane == 0) red[wl][GMAX] = ws;
+      e2_sync();
+      if (threadIdx.x - 32 * W_E2 < GMAX) {
+        const int g = threadIdx.x - 32 * W_E2;
+        const float wt = ((red[0][GMAX] + red[1][GMAX]) + (red[2][GMAX] + red[3][GMAX])) * CPG;
+        gmean[g] = wt > 0.f ? ((red[0][g] + red[1][g]) + (red[2][g] + red[3][g])) / wt : 0.f;
+        if (g == 0) wsum = wt;
+      }
+      e2_sync();
+#pragma unroll
+      for (int g = 0; g < GMAX; ++g) {
+        const float mg = gmean[g];
+        float t = 0.f;
+#pragma unroll
+        for (int c = 0; c < CPG; ++c) {
+          const float e = o[g * CPG + c] - mg;
+          t = fmaf(e, e, t);
+        }
+        t *= w;
+#pragma unroll
+        for (int m = 16; m; m >>= 1) t += __shfl_xor_sync(0xffffffffu, t, m);
+        if (lane == 0) red[wl][g] = t;
+      }
+      e2_sync();
+      if (threadIdx.x - 32 * W_E2 < GMAX) {
+        const int g = threadIdx.x - 32 * W_E2;
+        GroupAcc a{acc[3 * g], acc[3 * g + 1], acc[3 * g + 2]};
+        chan_merge(a, (double)wsum, (double)gmean[g], (double)((red[0][g] + red[1][g]) + (red[2][g] + red[3][g])));
+        acc[3 * g] = a.w;
+        acc[3 * g + 1] = a.mean;
+        acc[3 * g + 2] = a.m2;
+      }
+      e2_sync();
+    }
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  if (threadIdx.x < GMAX) {
+    double* o = partials + ((long)blockIdx.x * GMAX + threadIdx.x) * 3;
+    o[0] = acc[3 * threadIdx.x];
+    o[1] = acc[3 * threadIdx.x + 1];
+    o[2] = acc[3 * threadIdx.x + 2];
+  }
+  if (warp == 0) tc::tmem_free(tmem, 512);
+}
+
 int g_sms = 0;
 int sms() {
   if (!g_sms) {
@@ -306,10 +609,43 @@ int launch_mlp2_bwd(const float* a, const float* pb, const float* base, long V, 
   return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
 }
 
+template <int C, int MODE>
+int launch_mlp2_fwd(const float* in, const float* prev, const float* pc, float res, float* xout, long V,
+                    const void* wpack, const float* dw, float* pre, double* partials, int nparts, int* err,
+                    cudaStream_t s) {
+  CUtensorMap mi, mp;
+  if (!row_map(&mi, in, V, C)) return FFNO_EINVAL;
+  if (MODE != 0 ? !row_map(&mp, prev, V, C) : !row_map(&mp, in, V, C)) return FFNO_EINVAL;
+  const size_t smem = 1024 + 2 * (size_t)mat_bytes(2 * C, C) + 2 * (size_t)((MODE == 0 ? 1 : 2) * (C / 32) * BOX_BYTES);
+  if (cudaFuncSetAttribute(k_mlp2_fwd_ws<C, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return FFNO_ELAUNCH;
+  k_mlp2_fwd_ws<C, MODE><<<nparts, NTHREADS, smem, s>>>(mi, mp, pc, res, xout, V, static_cast<const uint8_t*>(wpack),
+                                                         dw, pre, partials, err);
+  return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
+}
+
 }  // namespace
 
 namespace ffno {
 namespace ws {
+
+bool mlp2_fwd_supported(int C) { return C == 32 || C == 64; }
+
+int mlp2_fwd(int mode, const float* in, const float* prev_pre, const float* prev_coefs, float res, float* xout, long V,
+             int C, const void* wpack, const float* dw, float* pre, double* partials, int nparts, int* err,
+             cudaStream_t stream) {
+  if (V < 1 || V > 0x7fffffffL - TM || nparts < 1 || reinterpret_cast<uintptr_t>(in) % 16 ||
+      (mode && reinterpret_cast<uintptr_t>(prev_pre) % 16))
+    return FFNO_EINVAL;
+#define L(CC, MM)                                                                                                \
+  if (C == CC && mode == MM)                                                                                     \
+    return launch_mlp2_fwd<CC, MM>(in, prev_pre, prev_coefs, res, xout, V, wpack, dw, pre, partials, nparts, err, \
+                                   stream);
+  L(64, 0) L(64, 1) L(64, 2) L(32, 0) L(32, 1) L(32, 2)
+#undef L
+  return FFNO_EINVAL;
+}
 
 bool mlp2_bwd_supported(int C) { return C == 32 || C == 64; }
 

@@ -65,9 +65,10 @@ def _coefs(C, seed):
     return c.reshape(-1).cuda().contiguous()
 
 
-@pytest.mark.parametrize("C", [16, 32, 64])
+@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (64, 152 * 128 * 5 + 77)])
 @pytest.mark.parametrize("mode", [0, 1, 2])
-def test_mlp2_fwd_tc(C, mode):
+def test_mlp2_fwd_tc(C, V, mode):
+    """Also at a voxel count that sends several tiles through every CTA's two-stage ring, with a ragged last tile."""
     nat = _nat()
     x, prev = _rand(V, C, seed=1), _rand(V, C, seed=2)
     pc = _coefs(C, 3)
