@@ -293,7 +293,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 //   warp 0 TMA ring of in [and prev]; warp 1 MMA: GEMM1 D1[t % 2] = x W1^T (N = 2C), and GEMM2 D2 = H W2^T (N = C)
 //   one tile behind, so that epilogue 1 of a tile overlaps GEMM1 of the next; warps 2-5 conversion with the residual
 //   prologue (xout); warps 6-13 epilogue 1: H = gelu(D1), split over D1; warps 14-17 epilogue 2: pre and statistics.
-// Tensor memory: A stages at 0 and 128 ([x hi | x lo], D2 of the stage's tile over them), D1 buffers at 256 and 384.
+// Tensor memory: four A stages of C columns from column 0 ([x hi | x lo], D2 of the stage's tile over them: a stage is
+// held from conversion to epilogue 2), D1 buffers at 256 and 384.
 template <int C, int MODE>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_mlp2_fwd_ws(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_prev,
@@ -309,7 +310,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* ring = smem + WB;
-  __shared__ uint64_t stg_full[2], stg_empty[2], a_full[2], a_empty[2], d1_full[2], h_full[2], d2_full[2], wbar;
+  constexpr int NA = 4;   // A stages
+  __shared__ uint64_t stg_full[2], stg_empty[2], a_full[NA], a_empty[NA], d2_full[NA], d1_full[2], h_full[2], wbar;
   __shared__ uint32_t tslot;
   __shared__ float cf[3 * C];                 // GroupNorm coefficients of prev: mean, gamma rstd, beta
   __shared__ float red[4][GMAX + 1], gmean[GMAX], wsum;
@@ -320,10 +322,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     for (int s = 0; s < 2; ++s) {
       tc::mbar_init(&stg_full[s], 1);
       tc::mbar_init(&stg_empty[s], 128);
-      tc::mbar_init(&a_full[s], 128);
-      tc::mbar_init(&a_empty[s], 128);
       tc::mbar_init(&d1_full[s], 1);
       tc::mbar_init(&h_full[s], 256);
+    }
+    for (int s = 0; s < NA; ++s) {
+      tc::mbar_init(&a_full[s], 128);
+      tc::mbar_init(&a_empty[s], 128);
       tc::mbar_init(&d2_full[s], 1);
     }
     tc::mbar_init(&wbar, 1);
@@ -372,26 +376,30 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     uint64_t* last = nullptr;
     uint32_t last_par = 0;
     bool alive = true;
-    auto gemm2 = [&](int j) {   // D2 (A stage j % 2) = H(j) (in D1[j % 2]) W2^T, K = 2C
+    auto gemm2 = [&](int j) {   // D2 (A stage j % NA) = H(j) (in D1[j % 2]) W2^T, K = 2C
       const uint32_t h = tmem + 256u + 128u * (j & 1);
 #pragma unroll 1
       for (int k = 0; k < 2 * C / 16; ++k)
-        mma3_ta(tmem + 128u * (j & 1), h + 16u * k, h + 16u * k + 8u, tc::kmajor_desc(w2 + 256u * k, 128u, 2 * C * 16u),
-                tc::kmajor_desc(w2 + LO + 256u * k, 128u, 2 * C * 16u), i2, k > 0);
-      tc::mma_commit(&d2_full[j & 1]);
-      last = &d2_full[j & 1];
-      last_par = ((uint32_t)j >> 1) & 1u;
+        mma3_ta(tmem + (uint32_t)(C * (j % NA)), h + 16u * k, h + 16u * k + 8u,
+                tc::kmajor_desc(w2 + 256u * k, 128u, 2 * C * 16u), tc::kmajor_desc(w2 + LO + 256u * k, 128u, 2 * C * 16u),
+                i2, k > 0);
+      tc::mma_commit(&d2_full[j % NA]);
+      last = &d2_full[j % NA];
+      last_par = (uint32_t)(j / NA) & 1u;
     };
     for (int i = 0; i < niter && alive; ++i) {
-      const int s = i & 1;
+      const int s = i & 1, sa = i % NA;
       const uint32_t n = (uint32_t)i >> 1;
-      // a_full implies the stage's previous D2 was read, hence GEMM2 of tile i-2 (reader of D1[s]) is complete
-      if (!wait_or_flag(&a_full[s], n & 1u, err, 4)) {
+      if (!wait_or_flag(&a_full[sa], (uint32_t)(i / NA) & 1u, err, 4)) {
         alive = false;
         break;
       }
+      if (i >= 2 && !wait_or_flag(&d2_full[(i - 2) % NA], (uint32_t)((i - 2) / NA) & 1u, err, 11)) {
+        alive = false;   // GEMM2 of tile i-2, the last reader of D1[s], has completed
+        break;
+      }
       tc::tc_after_sync();
-      const uint32_t A = tmem + 128u * s, D = tmem + 256u + 128u * s;
+      const uint32_t A = tmem + (uint32_t)(C * sa), D = tmem + 256u + 128u * s;
 #pragma unroll 1
       for (int k = 0; k < C / 16; ++k)
         mma3_ta(D, A + 8u * k, A + C / 2 + 8u * k, tc::kmajor_desc(w1 + 256u * k, 128u, C * 16u),
@@ -419,18 +427,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     for (int i = 0; i < niter; ++i) {
       const int s = i & 1;
       const uint32_t n = (uint32_t)i >> 1;
+      const int sa = i % NA;
       if (!warp_wait(&stg_full[s], n & 1u, err, 7)) break;
-      if (!warp_wait(&a_empty[s], (n & 1u) ^ 1u, err, 8)) break;
+      if (!warp_wait(&a_empty[sa], ((uint32_t)(i / NA) & 1u) ^ 1u, err, 8)) break;
       tc::tc_after_sync();
       const uint8_t* st = ring + s * SB;
-      const uint32_t A = tmem + lq + 128u * s;
+      const uint32_t A = tmem + lq + (uint32_t)(C * sa);
       const long v = tile_of(i) * TM + r;
-#pragma unroll
-      for (int b = 0; b < NB; ++b) {
+#pragma unroll 1
+      for (int bh = 0; bh < 2 * NB; ++bh) {   // half boxes: 16 channels, 8 hi and 8 lo columns
+        const int b = bh >> 1;
         const uint8_t* rin = st + b * BOX_BYTES + r * 128;
-        uint32_t hi[16], lo[16];
+        uint32_t hi[8], lo[8];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
+        for (int cc = 0; cc < 4; ++cc) {
+          const int c = 4 * (bh & 1) + cc;
           const uint32_t o = (uint32_t)((c ^ (r & 7)) << 4);
           float4 x = *reinterpret_cast<const float4*>(rin + o);
           if (MODE != 0) {
@@ -445,16 +456,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             x = make_float4(fmaf(res, y[0], x.x), fmaf(res, y[1], x.y), fmaf(res, y[2], x.z), fmaf(res, y[3], x.w));
             if (v < V) *reinterpret_cast<float4*>(xout + v * C + k) = x;
           }
-          tc::split_pack(x.x, x.y, hi[2 * c], lo[2 * c]);
-          tc::split_pack(x.z, x.w, hi[2 * c + 1], lo[2 * c + 1]);
+          tc::split_pack(x.x, x.y, hi[2 * cc], lo[2 * cc]);
+          tc::split_pack(x.z, x.w, hi[2 * cc + 1], lo[2 * cc + 1]);
         }
-        tc::tmem_st16u(A + (uint32_t)(16 * b), hi);
-        tc::tmem_st16u(A + (uint32_t)(C / 2 + 16 * b), lo);
+        tc::tmem_st8u(A + (uint32_t)(8 * bh), hi);
+        tc::tmem_st8u(A + (uint32_t)(C / 2 + 8 * bh), lo);
       }
       tc::mbar_arrive(&stg_empty[s]);
       tc::tmem_wait_st();
       tc::tc_before_sync();
-      tc::mbar_arrive(&a_full[s]);
+      tc::mbar_arrive(&a_full[sa]);
     }
   } else if (ok && warp >= W_E1 && warp < W_E2) {
     const int q = warp & 3, hf = (warp - W_E1) >> 2;
@@ -485,41 +496,43 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int q = warp & 3, r = 32 * q + lane, wl = warp - W_E2;
     const uint32_t lq = (uint32_t)(32 * q) << 16;
     for (int i = 0; i < niter; ++i) {
-      const int s = i & 1;
-      const uint32_t n = (uint32_t)i >> 1;
+      const int sa = i % NA;
       const long v = tile_of(i) * TM + r;
       const bool live = v < V;
       const float w = live ? __ldg(dw + v) : 0.f;
-      if (!e2_sync_and(tc::mbar_wait_for(&d2_full[s], n & 1u, WAIT_NS))) {
+      if (!e2_sync_and(tc::mbar_wait_for(&d2_full[sa], (uint32_t)(i / NA) & 1u, WAIT_NS))) {
         if (lane == 0) atomicExch(err, 10);
         break;
       }
       tc::tc_after_sync();
-      float o[C];
+      // pass 1: pre to HBM and the weighted group sums (CPG = C / 8 channels per group; a 16-column chunk holds
+      // 16 / CPG groups)
+      const uint32_t D = tmem + lq + (uint32_t)(C * sa);
+      float gs[GMAX];
 #pragma unroll
       for (int k = 0; k < C / 16; ++k) {
         uint32_t d[16];
-        tc::tmem_ld16u(tmem + lq + 128u * s + 16u * k, d);
+        tc::tmem_ld16u(D + 16u * k, d);
         tc::tmem_wait_ld();
+        if (live)
 #pragma unroll
-        for (int e = 0; e < 16; ++e) o[16 * k + e] = __uint_as_float(d[e]);
+          for (int e = 0; e < 4; ++e)
+            *reinterpret_cast<float4*>(pre + v * C + 16 * k + 4 * e) =
+                make_float4(__uint_as_float(d[4 * e]), __uint_as_float(d[4 * e + 1]), __uint_as_float(d[4 * e + 2]),
+                            __uint_as_float(d[4 * e + 3]));
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          const int g = (16 * k + e) / CPG;
+          if (e % CPG == 0) gs[g] = 0.f;
+          gs[g] += __uint_as_float(d[e]);
+        }
       }
-      tc::tc_before_sync();
-      tc::mbar_arrive(&a_empty[s]);   // D2 is in registers: the stage may take the tile after next
-      if (live)
-#pragma unroll
-        for (int k = 0; k < C / 4; ++k)
-          *reinterpret_cast<float4*>(pre + v * C + 4 * k) = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
-      // depth-weighted statistics of the tile: per group, sum then centred sum of squares over its 128 rows
       float ws = w;
 #pragma unroll
       for (int m = 16; m; m >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, m);
 #pragma unroll
       for (int g = 0; g < GMAX; ++g) {
-        float t = 0.f;
-#pragma unroll
-        for (int c = 0; c < CPG; ++c) t += o[g * CPG + c];
-        t *= w;
+        float t = w * gs[g];
 #pragma unroll
         for (int m = 16; m; m >>= 1) t += __shfl_xor_sync(0xffffffffu, t, m);
         if (lane == 0) red[wl][g] = t;
@@ -533,16 +546,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (g == 0) wsum = wt;
       }
       e2_sync();
+      // pass 2 (D2 read again from tensor memory): centred sums of squares
+#pragma unroll
+      for (int k = 0; k < C / 16; ++k) {
+        uint32_t d[16];
+        tc::tmem_ld16u(D + 16u * k, d);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          const int g = (16 * k + e) / CPG;
+          if (e % CPG == 0) gs[g] = 0.f;
+          const float x = __uint_as_float(d[e]) - gmean[g];
+          gs[g] = fmaf(x, x, gs[g]);
+        }
+      }
+      tc::tc_before_sync();
+      tc::mbar_arrive(&a_empty[sa]);   // D2 has been read: the stage may take a new tile
 #pragma unroll
       for (int g = 0; g < GMAX; ++g) {
-        const float mg = gmean[g];
-        float t = 0.f;
-#pragma unroll
-        for (int c = 0; c < CPG; ++c) {
-          const float e = o[g * CPG + c] - mg;
-          t = fmaf(e, e, t);
-        }
-        t *= w;
+        float t = w * gs[g];
 #pragma unroll
         for (int m = 16; m; m >>= 1) t += __shfl_xor_sync(0xffffffffu, t, m);
         if (lane == 0) red[wl][g] = t;

@@ -281,10 +281,11 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 
 __device__ __forceinline__ float bf16_round(float a) { return __bfloat162float(__float2bfloat16_rn(a)); }
 
-// Split-BF16 pair of two values: hi = bf16(a), lo = bf16(a - hi), packed as (a, b) pairs.
+// Split-BF16 pair of two values: hi = bf16(a), lo = bf16(a - hi), packed as (a, b) pairs. Two paired conversions:
+// the rounded hi values are read back out of the packed word with integer shifts.
 __device__ __forceinline__ void split_pack(float a, float b, uint32_t& hi, uint32_t& lo) {
-  const float ah = bf16_round(a), bh = bf16_round(b);
-  hi = pack_bf16(ah, bh);
+  hi = pack_bf16(a, b);
+  const float ah = __uint_as_float(hi << 16), bh = __uint_as_float(hi & 0xffff0000u);
   lo = pack_bf16(a - ah, b - bh);
 }
 
