@@ -195,8 +195,9 @@ def test_gate_bwd_tc(C):
     _close(z1, z0, 1e-5)
 
 
-@pytest.mark.parametrize("C", [16, 32, 64])
-def test_fuse_bwd_tc(C):
+@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (64, 152 * 128 * 5 + 77)])
+def test_fuse_bwd_tc(C, V):
+    """Also at a voxel count that sends several tiles through every CTA of the warp-specialised stage b."""
     nat = _nat()
     x, sp, vp = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3)
     sc, vc = _coefs(C, 4), _coefs(C, 5)
