@@ -1308,9 +1308,6 @@ int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const flo
                        float* vert_bar, int* err, ffno_stream_t stream) {
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
-  if (ws::fuse_bwd_b_supported(C))
-    return ws::fuse_bwd_b(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, hg, fused_pre_bar, hf_bar, base, V, C,
-                          wpack, x_bar, spec_bar, vert_bar, err, s);
   TC_DISPATCH(C, {
     const size_t smem =
         mat_bytes(2 * CC, 2 * CC) + mat_bytes(CC, 2 * CC) + mat_bytes(3 * CC, CC) + 2 * tile_bytes(CC);

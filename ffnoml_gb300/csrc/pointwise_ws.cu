@@ -593,300 +593,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) tc::tmem_free(tmem, 512);
 }
 
-// ============================================================================================ fuse backward
-// The ffno_fuse_bwd_b_tc contract (stage b of the branch-fusion backward): with B_bar = hfb Wf1 + [F_bar, F_bar] / 2,
-// g the branch gates and s = gelu(GN(pre)) the branch activations,
-//   spec_bar / vert_bar = B_bar g + A_bar[C:2C] / A_bar[2C:3C],   q = B_bar s g (1 - g),
-//   hg_bar = (q Wg2) * gelu'(hg),   A_bar = hg_bar Wg1,   x_bar = base + A_bar[:C].
-// Roles: warp 0 TMA of hfb (one ring stage of [128][2C]) and L2 prefetch of the tile's other rows; warp 1 MMA;
-// warps 2-5 conversion of hfb into tensor memory; warps 6-13 epilogue 1 (direct branch gradients to HBM, q split
-// over D1); warps 14-17 epilogue 2 (hg_bar split over D2) and epilogue 3 (x_bar, and A_bar added into the branch
-// gradients, which are still in L2). The MMA thread issues GEMM1 of the next tile between GEMM2 and GEMM3 of the
-// current one, so epilogue 1 of a tile overlaps epilogues 2 and 3 of the previous.
-// Tensor memory: A1 (hfb hi | lo) at 0, D1 (2C) at 128, D2 (C) at 256, D3 (3C) at 320.
-template <int C>
-__global__ void __launch_bounds__(NTHREADS, 1)
-    k_fuse_bwd_b_ws(const __grid_constant__ CUtensorMap map_hfb, const float* __restrict__ sp,
-                    const float* __restrict__ sc, const float* __restrict__ vp, const float* __restrict__ vc,
-                    const float* __restrict__ gates, const float* __restrict__ hg, const float* __restrict__ fb,
-                    const float* __restrict__ base, long V, const uint8_t* __restrict__ wpack,
-                    float* __restrict__ xbar, float* __restrict__ sbar, float* __restrict__ vbar,
-                    int* __restrict__ err) {
-  static_assert(C == 32 || C == 64, "widths 32 and 64");
-  constexpr uint32_t BF1 = mat_bytes(2 * C, 2 * C), BG2 = mat_bytes(C, 2 * C), BG1 = mat_bytes(3 * C, C);
-  constexpr uint32_t WB = BF1 + BG2 + BG1;
-  constexpr int NB = 2 * C / 32;                 // boxes of one hfb row block
-  constexpr uint32_t SB = NB * BOX_BYTES;
-  constexpr uint32_t A1 = 0, DD1 = 128, DD2 = 256, DD3 = 320;
-  static_assert(WB % 1024 == 0, "the ring must stay 1024-byte aligned (128-byte swizzle)");
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = align1024(smem_raw);
-  uint8_t* ring = smem + WB;
-  __shared__ uint64_t stg_full, stg_empty, a1_full, a1_free, d1_full, q_full, d2_full, hg_full, d3_full, d3_empty, wbar;
-  __shared__ uint32_t tslot;
-  __shared__ float cfs[3 * C], cfv[3 * C];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp == 0) tc::tmem_alloc(&tslot, 512);
-  if (threadIdx.x == 0) {
-    tc::mbar_init(&stg_full, 1);
-    tc::mbar_init(&stg_empty, 128);
-    tc::mbar_init(&a1_full, 128);
-    tc::mbar_init(&a1_free, 1);
-    tc::mbar_init(&d1_full, 1);
-    tc::mbar_init(&q_full, 256);
-    tc::mbar_init(&d2_full, 1);
-    tc::mbar_init(&hg_full, 128);
-    tc::mbar_init(&d3_full, 1);
-    tc::mbar_init(&d3_empty, 128);
-    tc::mbar_init(&wbar, 1);
-    tc::mbar_init_fence();
-  }
-  for (int e = threadIdx.x; e < 3 * C; e += NTHREADS) {
-    cfs[e] = sc[e];
-    cfv[e] = vc[e];
-  }
-  tc::tc_before_sync();
-  __syncthreads();
-  tc::tc_after_sync();
-  const uint32_t tmem = tslot;
-  if (threadIdx.x == 0) {
-    tc::mbar_arrive_expect_tx(&wbar, WB);
-    for (uint32_t off = 0; off < WB; off += 32768u)
-      tc::bulk_g2s(smem + off, wpack + off, WB - off < 32768u ? WB - off : 32768u, &wbar);
-  }
-  const bool ok = __syncthreads_and(tc::mbar_wait_for(&wbar, 0, WAIT_NS)) != 0;
-  if (!ok && threadIdx.x == 0) atomicExch(err, 1);
-
-  const long nt = (V + TM - 1) / TM;
-  const int niter = (long)blockIdx.x < nt ? (int)((nt - 1 - blockIdx.x) / gridDim.x + 1) : 0;
-  auto tile_of = [&](int i) { return (long)blockIdx.x + (long)i * gridDim.x; };
-
-  if (ok && warp == W_TMA && lane == 0) {
-    int issued = 0;
-    for (int i = 0; i < niter; ++i) {
-      if (i > 0 && !wait_or_flag(&stg_empty, (uint32_t)(i - 1) & 1u, err, 3)) break;
-      const long v0 = tile_of(i) * TM;
-      tc::mbar_arrive_expect_tx(&stg_full, SB);
-#pragma unroll
-      for (int b = 0; b < NB; ++b) tc::tma_load_2d(ring + b * BOX_BYTES, &map_hfb, 32 * b, (int)v0, &stg_full);
-      ++issued;
-      const uint32_t rows = (uint32_t)((V - v0) < TM ? (V - v0) : TM);
-      tc::prefetch_l2(fb + v0 * C, rows * C * 4);
-      tc::prefetch_l2(gates + v0 * 2 * C, rows * 2 * C * 4);
-      tc::prefetch_l2(sp + v0 * C, rows * C * 4);
-      tc::prefetch_l2(vp + v0 * C, rows * C * 4);
-      tc::prefetch_l2(hg + v0 * C, rows * C * 4);
-      if (base) tc::prefetch_l2(base + v0 * C, rows * C * 4);
-    }
-    if (issued) tc::mbar_wait_for(&stg_full, (uint32_t)(issued - 1) & 1u, WAIT_NS);
-  } else if (ok && warp == W_MMA && lane == 0) {
-    const uint32_t i1 = tc::idesc_bf16(128, 2 * C), i2 = tc::idesc_bf16(128, C), i3 = tc::idesc_bf16(128, 3 * C);
-    const uint32_t wf1t = tc::smem_u32(smem), wg2t = wf1t + BF1, wg1t = wg2t + BG2;
-    uint64_t* last = nullptr;
-    uint32_t last_par = 0;
-    auto gemm1 = [&](int i) {   // D1 = hfb Wf1t^T (K = 2C, N = 2C)
-#pragma unroll 1
-      for (int k = 0; k < 2 * C / 16; ++k)
-        mma3_ta(tmem + DD1, tmem + A1 + 8u * k, tmem + A1 + C + 8u * k,
-                tc::kmajor_desc(wf1t + 256u * k, 128u, 2 * C * 16u),
-                tc::kmajor_desc(wf1t + BF1 / 2 + 256u * k, 128u, 2 * C * 16u), i1, k > 0);
-      tc::mma_commit(&d1_full);
-      tc::mma_commit(&a1_free);
-      last = &a1_free;
-      last_par = (uint32_t)i & 1u;
-    };
-    bool alive = niter > 0;
-    if (alive) {
-      alive = wait_or_flag(&a1_full, 0u, err, 4);
-      if (alive) {
-        tc::tc_after_sync();
-        gemm1(0);
-      }
-    }
-    for (int i = 0; i < niter && alive; ++i) {
-      const uint32_t par = (uint32_t)i & 1u;
-      // GEMM2: D2 = q Wg2t^T (K = 2C, N = C); D2 is free once GEMM3 of the previous tile has completed
-      if (!wait_or_flag(&q_full, par, err, 5)) break;
-      if (i > 0 && !wait_or_flag(&d3_full, par ^ 1u, err, 6)) break;
-      tc::tc_after_sync();
-#pragma unroll 1
-      for (int k = 0; k < 2 * C / 16; ++k)
-        mma3_ta(tmem + DD2, tmem + DD1 + 16u * k, tmem + DD1 + 16u * k + 8u,
-                tc::kmajor_desc(wg2t + 256u * k, 128u, 2 * C * 16u),
-                tc::kmajor_desc(wg2t + BG2 / 2 + 256u * k, 128u, 2 * C * 16u), i2, k > 0);
-      tc::mma_commit(&d2_full);
-      last = &d2_full;
-      last_par = par;
-      // GEMM1 of the next tile once GEMM2 (the reader of q in D1) has completed
-      if (i + 1 < niter) {
-        if (!wait_or_flag(&d2_full, par, err, 7)) break;
-        if (!wait_or_flag(&a1_full, par ^ 1u, err, 8)) break;
-        tc::tc_after_sync();
-        gemm1(i + 1);
-      }
-      // GEMM3: D3 = hg_bar Wg1t^T (K = C, N = 3C) once epilogue 3 of the previous tile has read D3
-      if (!wait_or_flag(&hg_full, par, err, 9)) break;
-      if (i > 0 && !wait_or_flag(&d3_empty, par ^ 1u, err, 10)) break;
-      tc::tc_after_sync();
-#pragma unroll 1
-      for (int k = 0; k < C / 16; ++k)
-        mma3_ta(tmem + DD3, tmem + DD2 + 16u * k, tmem + DD2 + 16u * k + 8u,
-                tc::kmajor_desc(wg1t + 256u * k, 128u, C * 16u), tc::kmajor_desc(wg1t + BG1 / 2 + 256u * k, 128u, C * 16u),
-                i3, k > 0);
-      tc::mma_commit(&d3_full);
-      last = &d3_full;
-      last_par = par;
-    }
-    if (last) tc::mbar_wait_for(last, last_par, WAIT_NS);   // no MMA in flight when tensor memory is freed
-  } else if (ok && warp >= W_CVT && warp < W_E1) {
-    const int q = warp & 3, r = 32 * q + lane;
-    const uint32_t lq = (uint32_t)(32 * q) << 16;
-    for (int i = 0; i < niter; ++i) {
-      const uint32_t par = (uint32_t)i & 1u;
-      if (!warp_wait(&stg_full, par, err, 11)) break;
-      if (i > 0 && !warp_wait(&a1_free, par ^ 1u, err, 12)) break;   // GEMM1 of the previous tile has read A1
-      tc::tc_after_sync();
-      const uint32_t A = tmem + lq + A1;
-#pragma unroll 1
-      for (int bh = 0; bh < 2 * NB; ++bh) {   // 16 channels of hfb: 8 hi and 8 lo columns
-        const uint8_t* rin = ring + (bh >> 1) * BOX_BYTES + r * 128;
-        uint32_t hi[8], lo[8];
-#pragma unroll
-        for (int cc = 0; cc < 4; ++cc) {
-          const int c = 4 * (bh & 1) + cc;
-          const float4 x = *reinterpret_cast<const float4*>(rin + ((c ^ (r & 7)) << 4));
-          tc::split_pack(x.x, x.y, hi[2 * cc], lo[2 * cc]);
-          tc::split_pack(x.z, x.w, hi[2 * cc + 1], lo[2 * cc + 1]);
-        }
-        tc::tmem_st8u(A + 8u * bh, hi);
-        tc::tmem_st8u(A + C + 8u * bh, lo);
-      }
-      tc::mbar_arrive(&stg_empty);
-      tc::tmem_wait_st();
-      tc::tc_before_sync();
-      tc::mbar_arrive(&a1_full);
-    }
-  } else if (ok && warp >= W_E1 && warp < W_E2) {
-    const int q = warp & 3, hf = (warp - W_E1) >> 2, r = 32 * q + lane;
-    const uint32_t lq = (uint32_t)(32 * q) << 16;
-    for (int i = 0; i < niter; ++i) {
-      if (!warp_wait(&d1_full, (uint32_t)i & 1u, err, 13)) break;
-      tc::tc_after_sync();
-      const long v = tile_of(i) * TM + r;
-      const bool live = v < V;
-#pragma unroll 1
-      for (int j = hf; j < 2 * C / 16; j += 2) {
-        const int kh = j / (C / 16), cc = 16 * (j % (C / 16));
-        const float* pre = kh == 0 ? sp : vp;
-        const float* cf = kh == 0 ? cfs : cfv;
-        float* gout = kh == 0 ? sbar : vbar;
-        uint32_t bb[16];
-        tc::tmem_ld16u(tmem + lq + DD1 + 16u * j, bb);
-        float4 f4[4], g4[4], p4[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const bool in = live;
-          f4[e] = in ? __ldg(reinterpret_cast<const float4*>(fb + v * C + cc) + e) : make_float4(0.f, 0.f, 0.f, 0.f);
-          g4[e] = in ? __ldg(reinterpret_cast<const float4*>(gates + v * 2 * C + kh * C + cc) + e)
-                     : make_float4(0.f, 0.f, 0.f, 0.f);
-          p4[e] = in ? __ldg(reinterpret_cast<const float4*>(pre + v * C + cc) + e) : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        tc::tmem_wait_ld();
-        uint32_t hi[8], lo[8];
-        float qv[16];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float ff[4] = {f4[e].x, f4[e].y, f4[e].z, f4[e].w}, gg[4] = {g4[e].x, g4[e].y, g4[e].z, g4[e].w},
-                      pp[4] = {p4[e].x, p4[e].y, p4[e].z, p4[e].w};
-          float o[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const int c = cc + 4 * e + u;
-            const float sv = gelu_tc((pp[u] - cf[c]) * cf[C + c] + cf[2 * C + c]);
-            const float b = __uint_as_float(bb[4 * e + u]) + 0.5f * ff[u];
-            o[u] = b * gg[u];
-            qv[4 * e + u] = live ? b * sv * gg[u] * (1.f - gg[u]) : 0.f;
-          }
-          if (live) *reinterpret_cast<float4*>(gout + v * C + cc + 4 * e) = make_float4(o[0], o[1], o[2], o[3]);
-        }
-#pragma unroll
-        for (int e = 0; e < 8; ++e) tc::split_pack(qv[2 * e], qv[2 * e + 1], hi[e], lo[e]);
-        tc::tmem_st8u(tmem + lq + DD1 + 16u * j, hi);
-        tc::tmem_st8u(tmem + lq + DD1 + 16u * j + 8u, lo);
-      }
-      __threadfence();   // the direct branch gradients are in L2 before epilogue 3 of this tile adds to them
-      tc::tmem_wait_st();
-      tc::tc_before_sync();
-      tc::mbar_arrive(&q_full);
-    }
-  } else if (ok && warp >= W_E2) {
-    const int q = warp & 3, r = 32 * q + lane;
-    const uint32_t lq = (uint32_t)(32 * q) << 16;
-    for (int i = 0; i < niter; ++i) {
-      const uint32_t par = (uint32_t)i & 1u;
-      const long v = tile_of(i) * TM + r;
-      const bool live = v < V;
-      if (!warp_wait(&d2_full, par, err, 14)) break;
-      tc::tc_after_sync();
-#pragma unroll 1
-      for (int j = 0; j < C / 16; ++j) {
-        uint32_t hb[16];
-        tc::tmem_ld16u(tmem + lq + DD2 + 16u * j, hb);
-        float4 h4[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-          h4[e] = live ? __ldg(reinterpret_cast<const float4*>(hg + v * C + 16 * j) + e) : make_float4(0.f, 0.f, 0.f, 0.f);
-        tc::tmem_wait_ld();
-        uint32_t hi[8], lo[8];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float g0 = __uint_as_float(hb[4 * e]) * gelu_grad_tc(h4[e].x);
-          const float g1 = __uint_as_float(hb[4 * e + 1]) * gelu_grad_tc(h4[e].y);
-          const float g2 = __uint_as_float(hb[4 * e + 2]) * gelu_grad_tc(h4[e].z);
-          const float g3 = __uint_as_float(hb[4 * e + 3]) * gelu_grad_tc(h4[e].w);
-          tc::split_pack(g0, g1, hi[2 * e], lo[2 * e]);
-          tc::split_pack(g2, g3, hi[2 * e + 1], lo[2 * e + 1]);
-        }
-        tc::tmem_st8u(tmem + lq + DD2 + 16u * j, hi);
-        tc::tmem_st8u(tmem + lq + DD2 + 16u * j + 8u, lo);
-      }
-      tc::tmem_wait_st();
-      tc::tc_before_sync();
-      tc::mbar_arrive(&hg_full);
-      if (!warp_wait(&d3_full, par, err, 15)) break;
-      tc::tc_after_sync();
-#pragma unroll 1
-      for (int j = 0; j < 3 * C / 16; ++j) {
-        uint32_t d[16];
-        tc::tmem_ld16u(tmem + lq + DD3 + 16u * j, d);
-        tc::tmem_wait_ld();
-        if (j == 3 * C / 16 - 1) {
-          tc::tc_before_sync();
-          tc::mbar_arrive(&d3_empty);
-        }
-        if (!live) continue;
-        const int part = j / (C / 16), cc = 16 * (j % (C / 16));
-        float* dst = part == 0 ? xbar : part == 1 ? sbar : vbar;
-        const float* add = part == 0 ? base : dst;
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          float4 o = make_float4(__uint_as_float(d[4 * e]), __uint_as_float(d[4 * e + 1]), __uint_as_float(d[4 * e + 2]),
-                                 __uint_as_float(d[4 * e + 3]));
-          if (add) {
-            const float4 a4 = *(reinterpret_cast<const float4*>(add + v * C + cc) + e);
-            o = make_float4(o.x + a4.x, o.y + a4.y, o.z + a4.z, o.w + a4.w);
-          }
-          *(reinterpret_cast<float4*>(dst + v * C + cc) + e) = o;
-        }
-      }
-    }
-  }
-  tc::tc_before_sync();
-  __syncthreads();
-  tc::tc_after_sync();
-  if (warp == 0) tc::tmem_free(tmem, 512);
-}
-
 int g_sms = 0;
 int sms() {
   if (!g_sms) {
@@ -941,43 +647,10 @@ int launch_mlp2_fwd(const float* in, const float* prev, const float* pc, float r
   return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
 }
 
-template <int C>
-int launch_fuse_bwd_b(const float* sp, const float* sc, const float* vp, const float* vc, const float* gates,
-                      const float* hg, const float* fb, const float* hfb, const float* base, long V, const void* wpack,
-                      float* xbar, float* sbar, float* vbar, int* err, cudaStream_t s) {
-  CUtensorMap mh;
-  if (!row_map(&mh, hfb, V, 2 * C)) return FFNO_EINVAL;
-  const size_t smem = 1024 + (size_t)mat_bytes(2 * C, 2 * C) + mat_bytes(C, 2 * C) + mat_bytes(3 * C, C) +
-                      (size_t)(2 * C / 32) * BOX_BYTES;
-  if (cudaFuncSetAttribute(k_fuse_bwd_b_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return FFNO_ELAUNCH;
-  const long nt = (V + TM - 1) / TM;
-  const int grid = (int)(nt < sms() ? nt : sms());
-  k_fuse_bwd_b_ws<C><<<grid, NTHREADS, smem, s>>>(mh, sp, sc, vp, vc, gates, hg, fb, base, V,
-                                                  static_cast<const uint8_t*>(wpack), xbar, sbar, vbar, err);
-  return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
-}
-
 }  // namespace
 
 namespace ffno {
 namespace ws {
-
-bool fuse_bwd_b_supported(int C) { return C == 32 || C == 64; }
-
-int fuse_bwd_b(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
-               const float* gates, const float* hg, const float* fused_pre_bar, const float* hf_bar, const float* base,
-               long V, int C, const void* wpack, float* x_bar, float* spec_bar, float* vert_bar, int* err,
-               cudaStream_t stream) {
-  if (V < 1 || V > 0x7fffffffL - TM || reinterpret_cast<uintptr_t>(hf_bar) % 16) return FFNO_EINVAL;
-  if (C == 64)
-    return launch_fuse_bwd_b<64>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, hg, fused_pre_bar, hf_bar, base,
-                                 V, wpack, x_bar, spec_bar, vert_bar, err, stream);
-  if (C == 32)
-    return launch_fuse_bwd_b<32>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, hg, fused_pre_bar, hf_bar, base,
-                                 V, wpack, x_bar, spec_bar, vert_bar, err, stream);
-  return FFNO_EINVAL;
-}
 
 bool mlp2_fwd_supported(int C) { return C == 32 || C == 64; }
 

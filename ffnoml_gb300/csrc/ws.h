@@ -10,11 +10,6 @@ bool mlp2_fwd_supported(int C);
 int mlp2_fwd(int mode, const float* in, const float* prev_pre, const float* prev_coefs, float res, float* xout, long V,
              int C, const void* wpack, const float* dw, float* pre, double* partials, int nparts, int* err,
              cudaStream_t stream);
-bool fuse_bwd_b_supported(int C);
-int fuse_bwd_b(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
-               const float* gates, const float* hg, const float* fused_pre_bar, const float* hf_bar, const float* base,
-               long V, int C, const void* wpack, float* x_bar, float* spec_bar, float* vert_bar, int* err,
-               cudaStream_t stream);
 bool mlp2_bwd_supported(int C);
 int mlp2_bwd(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack, float* a_bar,
              int* err, cudaStream_t stream);
