@@ -26,6 +26,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
+from . import table_store
 from . import tables as tb
 
 EPS = 1e-5  # nn.GroupNorm default, DepthWeightedGroupNorm's eps (models/ffno_model.py:77-95)
@@ -170,6 +171,7 @@ class Packed:
         self.b2 = dev(b2)
         self.head = self._head_params(model)
         self.freq_params = {k: v.detach().cpu() for k, v in model.state_dict().items() if ".freq_" in k}
+        self.freq_key = table_store.freq_key(self.freq_params)
 
     @staticmethod
     def _tc_block(pk, b, device):
@@ -328,6 +330,8 @@ class Executor:
         self._plane_freq = {}
         self._height = {}
         self._lock = threading.RLock()        # caches are shared by concurrent service slots
+        # shape-constant tables persist across processes in a TableStore ($FFNO_GB300_TABLE_CACHE, or assigned)
+        self.tables = table_store.default_store()
         self._tls = threading.local()         # per-thread mode (a JVP forces the FP32 kernels)
         # A forward for the VJP keeps every block's intermediates instead of recomputing them in the backward when
         # they fit in half the free device memory (models/ffno_model.py:786-791 recomputes each block under
@@ -357,7 +361,8 @@ class Executor:
     def _plane_locked(self, H, W, device):
         key = (H, W, str(device))
         if key not in self._plane:
-            twf, thf, thi, twi = tb.plane_dft(H, W)
+            t = table_store.plane_arrays(self.tables, H, W)
+            twf, thf, thi, twi = t["twf"], t["thf"], t["thi"], t["twi"]
             f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device=device)
             # forward tables and the transposes the VJP applies (rows/cols swapped)
             self._plane[key] = dict(twf=f(twf), thf=f(thf), thi=f(thi), twi=f(twi), twf_t=f(twf.T), thf_t=f(thf.T),
@@ -372,10 +377,9 @@ class Executor:
     def _plane_freq_locked(self, pk, H, W, dx, dy, device):
         key = (H, W, float(dx), float(dy))
         if key not in self._plane_freq:
-            feats = tb.plane_features(H, W, dx, dy)
-            rank = self.model.freq_mix_rank
-            self._plane_freq[key] = [FreqTables(*tb.freq_tables(pk.freq_params, f"blocks.{i}.spec", feats, rank), device)
-                                     for i in range(self.model.n_layers)]
+            n, rank = self.model.n_layers, self.model.freq_mix_rank
+            t = table_store.plane_freq_arrays(self.tables, pk.freq_params, pk.freq_key, n, rank, H, W, dx, dy)
+            self._plane_freq[key] = [FreqTables(*gv, device) for gv in table_store.freq_list(t, n)]
         return self._plane_freq[key]
 
     def height(self, pk, geo, device):
@@ -385,11 +389,11 @@ class Executor:
     def _height_locked(self, pk, geo, device):
         key = (geo.column.tobytes(), float(geo.length), geo.k.numel())
         if key not in self._height:
-            live, tzf, tzi = tb.height_tables(geo.column, geo.length, geo.k)
-            feats = tb.height_features(geo.k[:live], self.model.z_feature_wavelength)
-            rank = self.model.freq_mix_rank
-            per_block = [FreqTables(*tb.freq_tables(pk.freq_params, f"blocks.{i}.vertical", feats, rank), device)
-                         for i in range(self.model.n_layers)]
+            n, rank = self.model.n_layers, self.model.freq_mix_rank
+            t = table_store.height_arrays(self.tables, pk.freq_params, pk.freq_key, n, rank, geo.column, geo.length,
+                                          geo.k, self.model.z_feature_wavelength)
+            live, tzf, tzi = int(t["live"]), t["tzf"], t["tzi"]
+            per_block = [FreqTables(*gv, device) for gv in table_store.freq_list(t, n)]
             f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device=device)
             self._height[key] = dict(live=live, tzf=f(tzf), tzi=f(tzi), tzf_t=f(tzf.T), tzi_t=f(tzi.T),
                                      freq=per_block, np=dict(tzf=tzf, tzi=tzi), device=device)

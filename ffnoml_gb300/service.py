@@ -392,12 +392,14 @@ class Client:
 
 def main():
     """python -m ffnoml_gb300.service manifest.toml — the manifest of ffno_fsdp_service.py ([service] port, token,
-    bind_host; [[models]] name, checkpoint_path, level_names, factory_kwargs), plus optional [service] slots."""
+    bind_host; [[models]] name, checkpoint_path, level_names, factory_kwargs), plus optional [service] slots and
+    table_cache (a directory where the shape-constant tables persist across restarts)."""
     import argparse
     import tomllib
 
     from .factory import create_ffno3d
     from .runtime import GB300Backend
+    from .table_store import TableStore
 
     ap = argparse.ArgumentParser()
     ap.add_argument("manifest")
@@ -405,13 +407,16 @@ def main():
     args = ap.parse_args()
     with open(args.manifest, "rb") as fh:
         cfg = tomllib.load(fh)
+    svc = cfg["service"]
+    store = TableStore(svc["table_cache"]) if svc.get("table_cache") else None
     backends = {}
     for m in sorted(cfg["models"], key=lambda item: item["name"]):
         b = GB300Backend.from_checkpoint(m["checkpoint_path"], create_ffno3d, m["level_names"],
                                          m.get("factory_kwargs", {}))
         b.model.set_precision(args.precision)
+        if store is not None:
+            b.model.executor().tables = store
         backends[str(m["name"])] = b
-    svc = cfg["service"]
     server = Server(backends, svc["token"], svc.get("bind_host", "0.0.0.0"), int(svc["port"]),
                     slots=int(svc.get("slots", 4)), log=lambda s: print(s, flush=True))
     server.serve_forever()
