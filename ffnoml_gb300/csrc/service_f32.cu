@@ -140,4 +140,16 @@ int ffno_si_input_grads(const float* features, const float* x_bar, const float* 
   return FFNO_OK;
 }
 
+// Strided host <-> device block copy (rows of width bytes, each pitch apart on either side) on a stream: the slab and
+// row-slab transfers of the host-RAM streaming forward (ffno_batched_backend.py:147-157 moves the same blocks with
+// tensor slicing).
+int ffno_copy2d(void* dst, long dpitch, const void* src, long spitch, long width, long rows, ffno_stream_t stream) {
+  if (!dst || !src || width < 0 || rows < 0 || dpitch < width || spitch < width) return FFNO_EINVAL;
+  if (!width || !rows) return FFNO_OK;
+  if (cudaMemcpy2DAsync(dst, (size_t)dpitch, src, (size_t)spitch, (size_t)width, (size_t)rows, cudaMemcpyDefault,
+                        (cudaStream_t)stream) != cudaSuccess)
+    return FFNO_ELAUNCH;
+  return FFNO_OK;
+}
+
 }  // extern "C"

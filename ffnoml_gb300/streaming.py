@@ -1,0 +1,314 @@
+"""Host-RAM streaming forward of FFNO3D, for cubes whose activations do not fit in HBM (the reference's
+BatchedFFNOBackend, ffno_batched_backend.py:116-308).
+
+Every operation of the model is local, acts on depth planes, or acts on columns, so it can run over slabs of the cube
+without changing the operator (ffno_batched_backend.py:1-13): the lift, gates, branch post-MLPs, fusion, pw / mlp and
+the head over depth slabs; the horizontal spectral convolution over depth slabs (each plane's rfft2 / mixing / irfft2
+is its own); the height operator over row slabs [D][h0:h1][W] (each column alone). The hidden states live in pinned
+host memory, channels last like the device layout; slabs move with strided copies (ffno_copy2d). A depth-weighted
+GroupNorm gathers every slab's partial statistics (the kernels' per-CTA Chan partials, FP64) into one buffer and
+finalizes once, so the statistics are those of the whole cube; its application is folded into the next stage's
+kernels as in the resident executor, so each GroupNorm costs no extra pass over the cube.
+
+The kernels are the resident path's (split-BF16 tensor cores or FP32, as the model's precision says). Host buffers:
+four hidden states (x, and three rotating buffers for the branch / fusion / pw / mlp intermediates). Shared height
+grids only (per-column grids raise NotImplementedError). Forward only, as in the reference.
+"""
+import copy
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .executor import EPS, Workspace, _descs, _stream
+from .runtime import INPUT_CHANNELS, _check
+
+
+def _pinned(n):
+    return torch.empty(n, dtype=torch.float32, pin_memory=True)
+
+
+class StreamingForward:
+    """FFNO3D forward of one cube held in host memory, `chunk_depth` depth planes and `chunk_rows` rows of columns at
+    a time on the device (ffno_batched_backend.py:117-145 takes the same two chunk sizes)."""
+
+    def __init__(self, model, chunk_depth=16, chunk_rows=16, normalization=None):
+        if chunk_depth < 1 or chunk_rows < 1:
+            raise ValueError("chunk sizes must be positive")
+        self.model = model
+        # mean_X, std_X, mean_Y, std_Y (a checkpoint's normalization_stats; default: the model's buffers)
+        self.normalization = normalization
+        self.ex = model.executor()
+        self.chunk_depth = int(chunk_depth)
+        self.chunk_rows = int(chunk_rows)
+        self.slabs = 0          # device slabs processed by the last call
+
+    # ------------------------------------------------------------------------------------------------ helpers
+    def _view(self, ws, V):
+        """ws's buffers for a smaller cube of V voxels (prefixes of the same buffers)."""
+        if V == ws.V:
+            return ws
+        w = copy.copy(ws)
+        w.V = V
+        w.nparts = nat.lib().ffno_stats_parts(V)
+        w.nparts_tc = nat.lib().ffno_tc_parts(V)
+        w.coefs = dict(ws.coefs)
+        return w
+
+    def _h2d(self, dst, src, offset, n):
+        """n floats of pinned host tensor src from element offset into device tensor dst."""
+        dst.view(-1)[:n].copy_(src[offset:offset + n], non_blocking=True)
+
+    def _d2h(self, dst, offset, src, n):
+        dst[offset:offset + n].copy_(src.reshape(-1)[:n], non_blocking=True)
+
+    def _rows(self, dst, dpitch, src, spitch, width, rows):
+        nat.call("ffno_copy2d", dst, dpitch, src, spitch, width, rows, _stream())
+
+    def _stats(self, ws, tc):
+        """Append this slab's GroupNorm partials to the cube's list."""
+        P = ws.nparts_tc if tc else ws.nparts
+        n = P * self.G * 3
+        self.parts[self.npart * self.G * 3:(self.npart + P) * self.G * 3].copy_(ws.partials[:n])
+        self.npart += P
+
+    def _finalize(self, name, gamma, beta):
+        nat.call("ffno_gn_finalize", self.parts.data_ptr(), self.npart, self.C, self.G, gamma.data_ptr(),
+                 beta.data_ptr(), EPS, self.coefs[name].data_ptr(), self.gstats[name].data_ptr(), _stream())
+        self.npart = 0
+
+    def _depth_slabs(self):
+        for d0 in range(0, self.D, self.chunk_depth):
+            yield d0, min(self.D, d0 + self.chunk_depth)
+
+    def _row_slabs(self):
+        for h0 in range(0, self.H, self.chunk_rows):
+            yield h0, min(self.H, h0 + self.chunk_rows)
+
+    def _load(self, ws, names, d0, d1, hosts):
+        """Depth slab d0:d1 of host hidden states into the named workspace buffers."""
+        n = (d1 - d0) * self.HW * self.C
+        for name, h in zip(names, hosts):
+            self._h2d(getattr(ws, name), h, d0 * self.HW * self.C, n)
+
+    def _store(self, ws, names, d0, d1, hosts):
+        n = (d1 - d0) * self.HW * self.C
+        for name, h in zip(names, hosts):
+            self._d2h(h, d0 * self.HW * self.C, getattr(ws, name), n)
+
+    # ------------------------------------------------------------------------------------------------ forward
+    def __call__(self, features, z_m, dx, dy):
+        """SI features (6, D, H, W) and heights z_m (D, H, W) in metres (host arrays) -> populations (D, H, W, L)
+        in m^-3 (numpy), as BatchedFFNOBackend.predict_si (ffno_batched_backend.py:285-308)."""
+        m, ex = self.model, self.ex
+        features = np.ascontiguousarray(features, dtype=np.float32)
+        z_m = np.ascontiguousarray(z_m, dtype=np.float32)
+        if features.ndim != 4 or features.shape[0] != len(INPUT_CHANNELS) or features.shape[1:] != z_m.shape:
+            raise ValueError(f"expected features (6,D,H,W) and z (D,H,W), got {features.shape}, {z_m.shape}")
+        dev = next(m.parameters()).device
+        D, H, W = z_m.shape
+        C, L = m.width, m.out_channels
+        self.D, self.H, self.W, self.HW, self.C = D, H, W, H * W, C
+        V = D * H * W
+        s = _stream()
+        pk = ex.packed(dev)
+        self.G = pk.groups
+        src = self.normalization or {k: getattr(m, k).detach().cpu().numpy() for k in
+                                     ("mean_X", "std_X", "mean_Y", "std_Y")}
+        norm = {k: torch.as_tensor(np.asarray(src[k], dtype=np.float32), device=dev).contiguous() for k in
+                ("mean_X", "std_X", "mean_Y", "std_Y")}
+        flags = torch.zeros(1, dtype=torch.int32, device=dev)
+        # normalised inputs [6][V] and heights [V] (Mm) stay on the device (7 floats a voxel against C of a hidden
+        # state); converted slab by slab from the pinned host arrays by the resident path's kernel
+        f_host = torch.from_numpy(features).pin_memory()
+        zm_host = torch.from_numpy(z_m).reshape(-1).pin_memory()
+        cd, cr = min(self.chunk_depth, D), min(self.chunk_rows, H)
+        xn = torch.empty(6, V, dtype=torch.float32, device=dev)
+        zmm = torch.empty(1, D, H, W, dtype=torch.float32, device=dev)
+        fs = torch.empty(6, cd * H * W, dtype=torch.float32, device=dev)
+        xs = torch.empty(6, cd * H * W, dtype=torch.float32, device=dev)
+        zin = torch.empty(cd * H * W, dtype=torch.float32, device=dev)
+        for d0, d1 in self._depth_slabs():
+            Vs, o = (d1 - d0) * self.HW, d0 * self.HW
+            self._rows(fs.data_ptr(), Vs * 4, f_host.data_ptr() + o * 4, V * 4, Vs * 4, 6)
+            self._h2d(zin, zm_host, o, Vs)
+            nat.call("ffno_si_inputs", fs.data_ptr(), zin.data_ptr(), Vs, norm["mean_X"].data_ptr(),
+                     norm["std_X"].data_ptr(), xs.data_ptr(), zmm.view(-1)[o:].data_ptr(), flags.data_ptr(), s)
+            self._rows(xn.data_ptr() + o * 4, V * 4, xs.data_ptr(), Vs * 4, Vs * 4, 6)
+        torch.cuda.current_stream().synchronize()
+        _check(flags.item(), "FFNO streaming request")
+        del fs, zin
+        geo = ex.geometry(zmm)
+        if not geo.shared:
+            raise NotImplementedError("the streaming forward runs shared height grids")
+        hgt = ex.height(pk, geo, dev)
+        pln, pfr = ex.plane(H, W, dev), ex.plane_freq(pk, H, W, float(dx), float(dy), dev)
+        live = hgt["live"]
+        dw = torch.empty(V, dtype=torch.float32, device=dev)
+        nat.call("ffno_depth_weights", zmm.data_ptr(), D, H * W, dw.data_ptr(), s)
+        # host hidden states and device workspaces
+        X, A, B, F = (_pinned(V * C) for _ in range(4))
+        pop_host = torch.empty(V * L, dtype=torch.float32, pin_memory=True)
+        wsd = Workspace(cd, H, W, C, live, self.G, dev)
+        wsr = Workspace(D, cr, W, C, live, self.G, dev)
+        nslab = max(-(-D // cd), -(-H // cr))
+        maxp = max(wsd.partials.numel(), wsr.partials.numel()) // (self.G * 3)
+        self.parts = torch.empty(nslab * maxp * self.G * 3, dtype=torch.float64, device=dev)
+        self.npart = 0
+        self.coefs = {n: torch.empty(3 * C, dtype=torch.float32, device=dev) for n in ("lift",) + _NORMS}
+        self.gstats = {n: torch.empty(self.G * 3, dtype=torch.float64, device=dev) for n in ("lift",) + _NORMS}
+        self.slabs = 0
+
+        def slab_inputs(d0, d1):
+            """Normalised model inputs of depth slab d0:d1, contiguous [6][Vs] (in xs)."""
+            Vs = (d1 - d0) * self.HW
+            self._rows(xs.data_ptr(), Vs * 4, xn.data_ptr() + d0 * self.HW * 4, V * 4, Vs * 4, 6)
+            return xs
+
+        def depth_ws(d0, d1):
+            ws = self._view(wsd, (d1 - d0) * self.HW)
+            ws.dw = dw[d0 * self.HW:d1 * self.HW]
+            for n in self.coefs:
+                ws.coefs[n] = self.coefs[n]
+            self.slabs += 1
+            return ws
+
+        # lift: pre-activation and statistics, then GELU(GN(.)) into X
+        for d0, d1 in self._depth_slabs():
+            ws = depth_ws(d0, d1)
+            x = slab_inputs(d0, d1)
+            nat.call("ffno_lift_fwd", x.data_ptr(), m.in_channels, ws.V, C, pk.lift_w.data_ptr(), ws.dw.data_ptr(),
+                     ws.pre.data_ptr(), ws.partials.data_ptr(), ws.nparts, self.G, s)
+            self._store(ws, ["pre"], d0, d1, [A])
+            self._stats(ws, False)
+        self._finalize("lift", pk.lift_g, pk.lift_b)
+        for d0, d1 in self._depth_slabs():
+            ws = depth_ws(d0, d1)
+            self._load(ws, ["pre"], d0, d1, [A])
+            nat.call("ffno_gn_act", ws.pre.data_ptr(), self.coefs["lift"].data_ptr(), ws.V, C, 1, ws.x.data_ptr(), s)
+            self._store(ws, ["x"], d0, d1, [X])
+        for i in range(m.n_layers):
+            self._block(pk, i, wsd, wsr, depth_ws, dw, zmm, hgt, pln, pfr[i], X, A, B, F, dev)
+        # head, and the SI populations of each slab
+        out = torch.empty(L, cd * H * W, dtype=torch.float32, device=dev)
+        pop = torch.empty(cd * H * W, L, dtype=torch.float32, device=dev)
+        for d0, d1 in self._depth_slabs():
+            ws = depth_ws(d0, d1)
+            x = slab_inputs(d0, d1)
+            self._load(ws, ["x"], d0, d1, [X])
+            y = out[:, :ws.V]
+            nat.call("ffno_head_fwd", ws.x.data_ptr(), x.data_ptr(), ws.V, C, pk.p1.data_ptr(), pk.p2.data_ptr(),
+                     pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head, y.data_ptr(), None, s)
+            nat.call("ffno_si_populations", y.data_ptr(), ws.V, L, norm["mean_Y"].data_ptr(), norm["std_Y"].data_ptr(),
+                     pop.data_ptr(), flags.data_ptr(), s)
+            self._d2h(pop_host, d0 * self.HW * L, pop, ws.V * L)
+        torch.cuda.current_stream().synchronize()
+        _check(flags.item(), "FFNO streaming output")
+        if any(int(w.err.item()) for w in (wsd, wsr)):
+            raise RuntimeError("tensor-core kernel timed out")
+        return pop_host.numpy().reshape(D, H, W, L).copy()
+
+    # ------------------------------------------------------------------------------------------------ one block
+    def _block(self, pk, i, wsd, wsr, depth_ws, dw, zmm, hgt, pln, fq, X, A, B, F, dev):
+        m, ex = self.model, self.ex
+        C, D, H, W, HW, Wf = self.C, self.D, self.H, self.W, self.HW, self.W // 2 + 1
+        s = _stream()
+        bp = pk.blocks[i]
+        live = hgt["live"]
+        tc = ex._tc()
+        r_f, r_pw, r_mlp = bp["res"]
+        # horizontal spectral branch over depth slabs -> spec_pre (A)
+        for d0, d1 in self._depth_slabs():
+            ws = depth_ws(d0, d1)
+            Ds = d1 - d0
+            self._load(ws, ["x"], d0, d1, [X])
+            if tc:
+                nat.call("ffno_gate_fwd_tc", ws.x.data_ptr(), ws.V, C, bp["tc_s_gate"].data_ptr(), None, None,
+                         ws.xs.data_ptr(), ws.err.data_ptr(), s)
+            else:
+                nat.call("ffno_gate_fwd", ws.x.data_ptr(), ws.V, C, bp["s_g1"].data_ptr(), bp["s_g2"].data_ptr(), None,
+                         None, ws.xs.data_ptr(), s)
+            d = _descs(Ds, H, W, C, live)
+            ex._xf(pln, "twf", ws.xs, ws.sa, d["wf"], ws)
+            ex._xf(pln, "thf", ws.sa, ws.sb, d["hf"], ws)
+            ex._mix(ws, "s", bp, fq, ws.sb, ws.sa, H * Wf, Ds, C, 2 * H * Wf * C, H * Wf * C, False)
+            ex._xf(pln, "thi", ws.sa, ws.sb, d["hf"], ws)
+            ex._xf(pln, "twi", ws.sb, ws.ys, d["wi"], ws)
+            t = ex._mlp2(ws, 0, ws.ys, None, None, 0.0, None, bp["s_p1"], bp["s_p2"], bp.get("tc_s_post"),
+                         ws.spec_pre)
+            self._store(ws, ["spec_pre"], d0, d1, [A])
+            self._stats(ws, t)
+        self._finalize("spec", bp["spec_g"], bp["spec_b"])
+        # height branch over row slabs [D][h0:h1][W] -> vert_pre (B)
+        hq = hgt["freq"][i]
+        rowb = HW * C * 4
+        for h0, h1 in self._row_slabs():
+            rows = h1 - h0
+            ws = self._view(wsr, D * rows * W)
+            ws.dw = dw.view(D, H, W)[:, h0:h1].contiguous().view(-1)
+            zr = zmm.view(D, H, W)[:, h0:h1].contiguous()
+            width = rows * W * C * 4
+            self._rows(ws.x.data_ptr(), width, X.data_ptr() + h0 * W * C * 4, rowb, width, D)
+            self.slabs += 1
+            if tc:
+                nat.call("ffno_gate_fwd_tc", ws.x.data_ptr(), ws.V, C, bp["tc_v_gate"].data_ptr(), bp["v_zp"].data_ptr(),
+                         zr.data_ptr(), ws.xv.data_ptr(), ws.err.data_ptr(), s)
+            else:
+                nat.call("ffno_gate_fwd", ws.x.data_ptr(), ws.V, C, bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(),
+                         bp["v_zp"].data_ptr(), zr.data_ptr(), ws.xv.data_ptr(), s)
+            d = _descs(D, rows, W, C, live)
+            RW = rows * W
+            ex._xf(hgt, "tzf", ws.xv, ws.va, d["zf"], ws)
+            ex._mix(ws, "v", bp, hq, ws.va, ws.vb, live, RW, RW * C, C, live * RW * C, False)
+            ex._xf(hgt, "tzi", ws.vb, ws.yv, d["zi"], ws)
+            t = ex._mlp2(ws, 0, ws.yv, None, None, 0.0, None, bp["v_p1"], bp["v_p2"], bp.get("tc_v_post"),
+                         ws.vert_pre)
+            self._rows(B.data_ptr() + h0 * W * C * 4, rowb, ws.vert_pre.data_ptr(), width, width, D)
+            self._stats(ws, t)
+        self._finalize("vert", bp["vert_g"], bp["vert_b"])
+        # fusion -> fused_pre (F)
+        for d0, d1 in self._depth_slabs():
+            ws = depth_ws(d0, d1)
+            self._load(ws, ["x", "spec_pre", "vert_pre"], d0, d1, [X, A, B])
+            if tc:
+                ex._fuse1_tc(ws, bp, ws.x, None)
+                nat.call("ffno_fuse2_tc", ws.spec_pre.data_ptr(), self.coefs["spec"].data_ptr(),
+                         ws.vert_pre.data_ptr(), self.coefs["vert"].data_ptr(), ws.gates.data_ptr(), ws.V, C,
+                         bp["tc_fuse2"].data_ptr(), ws.dw.data_ptr(), ws.fused_pre.data_ptr(),
+                         ws.partials.data_ptr(), ws.nparts_tc, self.G, ws.err.data_ptr(), s)
+            else:
+                nat.call("ffno_fuse_fwd", ws.x.data_ptr(), ws.spec_pre.data_ptr(), self.coefs["spec"].data_ptr(),
+                         ws.vert_pre.data_ptr(), self.coefs["vert"].data_ptr(), ws.V, C, bp["bg1"].data_ptr(),
+                         bp["bg2"].data_ptr(), bp["bgb"].data_ptr(), bp["f1"].data_ptr(), bp["f2"].data_ptr(),
+                         ws.dw.data_ptr(), ws.fused_pre.data_ptr(), ws.partials.data_ptr(), ws.nparts, self.G, s)
+            self._store(ws, ["fused_pre"], d0, d1, [F])
+            self._stats(ws, tc)
+        self._finalize("fuse", bp["fuse_g"], bp["fuse_b"])
+        # x1 = x + r_f gelu(GN(fused_pre)) (A), pw_pre (B)
+        for d0, d1 in self._depth_slabs():
+            ws = depth_ws(d0, d1)
+            self._load(ws, ["x", "fused_pre"], d0, d1, [X, F])
+            t = ex._mlp2(ws, 1, ws.x, ws.fused_pre, self.coefs["fuse"], r_f, ws.x1, bp["pw1"], bp["pw2"],
+                         bp.get("tc_pw"), ws.pw_pre)
+            self._store(ws, ["x1", "pw_pre"], d0, d1, [A, B])
+            self._stats(ws, t)
+        self._finalize("pw", bp["pw_g"], bp["pw_b"])
+        # x2 = x1 + r_pw GN(pw_pre) (F), mlp_pre (A, over x1 slab by slab)
+        for d0, d1 in self._depth_slabs():
+            ws = depth_ws(d0, d1)
+            self._load(ws, ["x1", "pw_pre"], d0, d1, [A, B])
+            t = ex._mlp2(ws, 2, ws.x1, ws.pw_pre, self.coefs["pw"], r_pw, ws.x2, bp["m1"], bp["m2"], bp.get("tc_mlp"),
+                         ws.mlp_pre)
+            self._store(ws, ["x2", "mlp_pre"], d0, d1, [F, A])
+            self._stats(ws, t)
+        self._finalize("mlp", bp["mlp_g"], bp["mlp_b"])
+        # block output x = x2 + r_mlp GN(mlp_pre) (X)
+        for d0, d1 in self._depth_slabs():
+            ws = depth_ws(d0, d1)
+            self._load(ws, ["x2", "mlp_pre"], d0, d1, [F, A])
+            nat.call("ffno_resid_out", ws.x2.data_ptr(), ws.mlp_pre.data_ptr(), self.coefs["mlp"].data_ptr(), r_mlp,
+                     ws.V, C, ws.x.data_ptr(), s)
+            self._store(ws, ["x"], d0, d1, [X])
+
+
+_NORMS = ("spec", "vert", "fuse", "pw", "mlp")

@@ -231,6 +231,10 @@ int ffno_outer_noalloc(const float* A, long lda, int Ma, const float* B, long ld
 
 /* _model_inputs + normalisation (:48-58, :274-276): SI features [6][V] (T, vx, vy, vz, log10 ne, log10 rho) and z [V]
  * in metres -> normalised inputs x [6][V] and z_mm [V] in Mm. */
+/* Host-RAM streaming (ffno_batched_backend.py:147-289): strided block copy between pinned host memory and the device,
+ * rows of `width` bytes `spitch` / `dpitch` apart (cudaMemcpy2DAsync, direction from the addresses). */
+int ffno_copy2d(void* dst, long dpitch, const void* src, long spitch, long width, long rows, ffno_stream_t stream);
+
 int ffno_si_inputs(const float* features, const float* z_m, long V, const float* mean_x, const float* std_x,
                    float* x, float* z_mm, int* flags, ffno_stream_t stream);
 /* linear_populations + _canonical_populations (:76-78, :277-292): normalised log10 n y [L][V] -> pop [V][L] m^-3. */

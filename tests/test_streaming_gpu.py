@@ -1,0 +1,46 @@
+"""The host-RAM streaming forward (hidden states in pinned host memory, the cube on the device a depth slab or a slab of
+column rows at a time) against the resident forward through the service backend: the same kernels on the same
+voxels, with GroupNorm statistics merged over the slabs' partials instead of the whole cube's, so the populations
+agree to rounding (ffno_batched_backend.py's own chunking test allows 2e-4)."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _model(width, precision):
+    import bench
+    from ffnoml_gb300 import create_ffno3d
+    torch.manual_seed(3)
+    m = create_ffno3d(6, 12, atoms=["H", "CA"], width=width, n_layers=2, z_min_wavelength=40.0 / 15)
+    with torch.no_grad():
+        for name, p in m.named_parameters():
+            if ".freq_u." in name:
+                p.normal_(0.0, 0.1)
+    m.set_normalization(bench.MEAN_X, bench.STD_X, np.zeros(12), np.ones(12))
+    return m.cuda().eval().set_precision(precision)
+
+
+@pytest.mark.parametrize("width,precision,tol", [(32, "fp32", 1e-4), (64, "fp32", 1e-4), (64, "bf16", 2e-3)])
+def test_streaming_matches_resident(width, precision, tol):
+    import bench
+    from ffnoml_gb300.runtime import GB300Backend
+    from ffnoml_gb300.streaming import StreamingForward
+    model = _model(width, precision)
+    f, z = bench.synthetic_si((37, 24, 20), seed=5)
+    ref = GB300Backend(model, [f"l{i}" for i in range(12)]).predict_local(f, z, 48e3, 48e3)
+    sf = StreamingForward(model, chunk_depth=8, chunk_rows=7)
+    got = sf(f, z, 48e3, 48e3)
+    assert got.shape == ref.shape == (37, 24, 20, 12)
+    assert sf.slabs > 2 * 5 * 6            # several depth slabs and row slabs per block stage
+    err = np.abs(np.log10(got) - np.log10(ref)).max()
+    print(f"w{width} {precision}: max |dlog10 n| streaming vs resident {err:.2e}")
+    assert err < tol
+
+
+def test_streaming_rejects_bad_shapes():
+    from ffnoml_gb300.streaming import StreamingForward
+    sf = StreamingForward(_model(32, "fp32"))
+    with pytest.raises(ValueError):
+        sf(np.zeros((5, 4, 4, 4), np.float32), np.zeros((4, 4, 4), np.float32), 1.0, 1.0)
