@@ -97,9 +97,10 @@ class StreamingForward:
             self._d2h(h, d0 * self.HW * self.C, getattr(ws, name), n)
 
     # ------------------------------------------------------------------------------------------------ forward
-    def __call__(self, features, z_m, dx, dy):
+    def __call__(self, features, z_m, dx, dy, log10=False):
         """SI features (6, D, H, W) and heights z_m (D, H, W) in metres (host arrays) -> populations (D, H, W, L)
-        in m^-3 (numpy), as BatchedFFNOBackend.predict_si (ffno_batched_backend.py:285-308)."""
+        in m^-3 (numpy), as BatchedFFNOBackend.predict_si (ffno_batched_backend.py:285-308); with log10, the
+        de-normalised log10 populations (L, D, H, W) as its predict_log10 (:251-283)."""
         m, ex = self.model, self.ex
         features = np.ascontiguousarray(features, dtype=np.float32)
         z_m = np.ascontiguousarray(z_m, dtype=np.float32)
@@ -196,9 +197,14 @@ class StreamingForward:
             ws = depth_ws(d0, d1)
             x = slab_inputs(d0, d1)
             self._load(ws, ["x"], d0, d1, [X])
-            y = out[:, :ws.V]
+            y = out.view(-1)[:L * ws.V].view(L, ws.V)      # the head writes [L][Vs] contiguously
             nat.call("ffno_head_fwd", ws.x.data_ptr(), x.data_ptr(), ws.V, C, pk.p1.data_ptr(), pk.p2.data_ptr(),
                      pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head, y.data_ptr(), None, s)
+            if log10:   # y std_Y + mean_Y into rows of [L][V]
+                lg = pop.view(-1)[:L * ws.V].view(L, ws.V)
+                torch.addcmul(norm["mean_Y"][:, None], y, norm["std_Y"][:, None], out=lg)
+                self._rows(pop_host.data_ptr() + d0 * self.HW * 4, V * 4, lg.data_ptr(), ws.V * 4, ws.V * 4, L)
+                continue
             nat.call("ffno_si_populations", y.data_ptr(), ws.V, L, norm["mean_Y"].data_ptr(), norm["std_Y"].data_ptr(),
                      pop.data_ptr(), flags.data_ptr(), s)
             self._d2h(pop_host, d0 * self.HW * L, pop, ws.V * L)
@@ -206,6 +212,8 @@ class StreamingForward:
         _check(flags.item(), "FFNO streaming output")
         if any(int(w.err.item()) for w in (wsd, wsr)):
             raise RuntimeError("tensor-core kernel timed out")
+        if log10:
+            return pop_host.numpy().reshape(L, D, H, W).copy()
         return pop_host.numpy().reshape(D, H, W, L).copy()
 
     # ------------------------------------------------------------------------------------------------ one block
@@ -312,3 +320,63 @@ class StreamingForward:
 
 
 _NORMS = ("spec", "vert", "fuse", "pw", "mlp")
+
+
+class StreamingBackend:
+    """The reference's BatchedFFNOBackend interface (ffno_batched_backend.py:116-308) on one GB300: a checkpoint's
+    FFNO3D predicting a whole cube of any size that fits in host RAM. predict_log10 takes model units, predict_si the
+    service's SI units; chunk_depth / chunk_rows are the device slab sizes."""
+
+    def __init__(self, model, level_names, normalization=None, device="cuda", chunk_depth=16, chunk_rows=16,
+                 log=print):
+        if not torch.cuda.is_available():
+            raise RuntimeError("the GB300 streaming backend requires CUDA")
+        self.device = torch.device(device)
+        self.model = model.to(self.device).eval()
+        self.levels = int(model.out_channels)
+        self.level_names = tuple(str(v) for v in level_names)
+        if len(self.level_names) != self.levels:
+            raise RuntimeError("checkpoint Cout differs from configured level_names")
+        self.normalization = normalization or {k: getattr(model, k).detach().cpu().numpy() for k in
+                                               ("mean_X", "std_X", "mean_Y", "std_Y")}
+        self.forward = StreamingForward(self.model, chunk_depth, chunk_rows, self.normalization)
+        self.log = log
+
+    @classmethod
+    def from_checkpoint(cls, checkpoint_path, factory, level_names, factory_kwargs=None, device="cuda", **kw):
+        from .runtime import load_checkpoint
+        ck = load_checkpoint(checkpoint_path)
+        norm, io = ck.get("normalization_stats"), ck.get("io_metadata")
+        if norm is None or io is None:
+            raise RuntimeError("checkpoint must contain normalization_stats and io_metadata")
+        model = factory(Cin=int(io["Cin"]), Cout=int(io["Cout"]), device="cpu", **dict(factory_kwargs or {}))
+        model.load_state_dict(ck["model_state"], strict=True)
+        return cls(model, level_names, normalization=norm, device=device, **kw)
+
+    def predict_si(self, features, z_m, dx, dy):
+        """Linear populations [m^-3], (D, H, W, levels), from SI features (T [K], vx, vy, vz [m/s], log10 ne,
+        log10 rho) and heights z_m [m] (ffno_batched_backend.py:285-308)."""
+        features = np.asarray(features, dtype=np.float32)
+        if features.ndim != 4 or features.shape[0] != len(INPUT_CHANNELS):
+            raise ValueError(f"expected features (6,D,H,W), got {features.shape}")
+        if not (np.isfinite(features).all() and np.isfinite(np.asarray(z_m)).all()):
+            raise ValueError("FFNO request contains NaN or Inf")
+        if not (features[0] > 0).all():
+            raise ValueError("FFNO request temperature must be positive")
+        pop = self.forward(features, z_m, float(dx), float(dy))
+        if not np.isfinite(pop).all() or (pop <= 0).any():
+            raise RuntimeError("FFNO returned non-positive or non-finite populations")
+        return pop
+
+    def predict_log10(self, features, z_scale, dx, dy):
+        """log10 populations (levels, D, H, W) from features in model units (log10 T, velocities in km/s, log10 ne,
+        log10 rho) and z in Mm (ffno_batched_backend.py:251-283)."""
+        f = np.array(features, dtype=np.float64)
+        if f.ndim != 4 or f.shape[0] != len(INPUT_CHANNELS):
+            raise ValueError(f"expected features (6,D,H,W), got {f.shape}")
+        if not (np.isfinite(f).all() and np.isfinite(np.asarray(z_scale)).all()):
+            raise ValueError("FFNO request contains NaN or Inf")
+        f[0] = 10.0 ** f[0]
+        f[1:4] *= 1e3
+        return self.forward(f.astype(np.float32), np.asarray(z_scale, dtype=np.float64) * 1e6, float(dx), float(dy),
+                            log10=True)

@@ -44,3 +44,27 @@ def test_streaming_rejects_bad_shapes():
     sf = StreamingForward(_model(32, "fp32"))
     with pytest.raises(ValueError):
         sf(np.zeros((5, 4, 4, 4), np.float32), np.zeros((4, 4, 4), np.float32), 1.0, 1.0)
+
+
+def test_streaming_backend_log10_and_si():
+    """predict_log10 (model units in, de-normalised log10 n out) against the resident model, and predict_si."""
+    import bench
+    from ffnoml_gb300.streaming import StreamingBackend
+    model = _model(32, "fp32")
+    f, z = bench.synthetic_si((19, 16, 12), seed=7)
+    x, zmm = bench.normalised(f, z)
+    with torch.no_grad():
+        ref = model(torch.from_numpy(x).cuda(), torch.from_numpy(zmm).cuda(), 48e3, 48e3)[0].cpu().numpy()
+    sb = StreamingBackend(model, [f"l{i}" for i in range(12)], chunk_depth=4, chunk_rows=5)
+    units = f.astype(np.float64).copy()
+    units[0] = np.log10(units[0])
+    units[1:4] /= 1e3
+    got = sb.predict_log10(units, z / 1e6, 48e3, 48e3)
+    assert got.shape == (12, 19, 16, 12)
+    assert np.abs(got - ref).max() < 1e-4
+    pop = sb.predict_si(f, z, 48e3, 48e3)
+    assert np.abs(np.log10(pop) - got.transpose(1, 2, 3, 0)).max() < 1e-4
+    with pytest.raises(ValueError):
+        bad = f.copy()
+        bad[0, 0, 0, 0] = -1.0
+        sb.predict_si(bad, z, 48e3, 48e3)
