@@ -39,6 +39,7 @@ MEAN_X = np.array([4.75, 0.0, 0.0, 0.0, 17.5, -8.0], np.float32)
 STD_X = np.array([2.5 / math.sqrt(12), 5.0, 5.0, 5.0, 7.0 / math.sqrt(12), 8.0 / math.sqrt(12)], np.float32)
 CPU_SAMPLE = (32, 16, 16)       # bounded sub-cube per step of the reference arm (same C, L, M)
 CPU_SAMPLE_FULL = (64, 32, 32)  # the cpu_baseline sub-cube (about 10-30 s of fwd+VJP on the host cores)
+STREAM_CHUNKS = (32, 16)        # depth planes / column rows per device slab of the host-RAM streaming forward
 KERNELS_PER_CALL = {"ffno_column_info": 3, "ffno_outer": 2}
 METRIC = "FFNO3D voxels/s fwd & fwd+VJP, BF16 vs FP32 @ |\u0394log n|\u22642e-3; p50/p99 latency"
 
@@ -433,6 +434,25 @@ def run_gb300(args):
                                                                                             cot_np.nbytes),
                "d2h_bytes_per_step": int(f_np.nbytes + z_np.nbytes), "ms_per_step": 1e3 * e2e_s}
 
+    # the host-RAM streaming forward on the same cube (hidden states in pinned host memory, slabs on the device)
+    streaming = None
+    if not args.no_streaming and not args.fwd_only:
+        from ffnoml_gb300.streaming import StreamingForward
+        sfw = StreamingForward(model, chunk_depth=STREAM_CHUNKS[0], chunk_rows=STREAM_CHUNKS[1])
+        sfw(f_np, z_np, DXY, DXY)
+        barrier()
+        t0 = time.perf_counter()
+        n_s = max(1, min(args.steps, 2))
+        for _ in range(n_s):
+            sfw(f_np, z_np, DXY, DXY)
+        barrier()
+        st = max_over_ranks((time.perf_counter() - t0) / n_s, world, dev)
+        streaming = {"value": job_rate(V, world, st), "unit": "voxels/s", "ms_per_step": 1e3 * st, "pass": "forward",
+                     "chunk_depth": STREAM_CHUNKS[0], "chunk_rows": STREAM_CHUNKS[1], "slabs_per_step": sfw.slabs,
+                     "host_hidden_bytes": 4 * V * WIDTH * 4, "h2d_bytes_per_step": int(f_np.nbytes + z_np.nbytes),
+                     "d2h_bytes_per_step": int(V * 12 * 4)}
+        del sfw
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         torch.set_num_threads(len(os.sched_getaffinity(0)))
@@ -467,7 +487,7 @@ def run_gb300(args):
             "kernel_breakdown_ms": breakdown,
             "clocks": clocks, "memory": memory, "gpu_launches": launches * args.steps, "e2e": e2e,
             "cpu_baseline": cpu,
-            "serving": serving,
+            "serving": serving, "streaming": streaming,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -552,6 +572,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-streaming", action="store_true", help="skip the host-RAM streaming forward")
     ap.add_argument("--serve-requests", type=int, default=256)
     args = ap.parse_args()
     args.shape = tuple(int(v) for v in args.shape.split(","))

@@ -96,6 +96,20 @@ class StreamingForward:
         for name, h in zip(names, hosts):
             self._d2h(h, d0 * self.HW * self.C, getattr(ws, name), n)
 
+    def _buffers(self, dev, D, H, W, C, L, cd):
+        """Pinned host hidden states and device inputs, kept while the cube shape repeats (pinning GBs of host
+        memory costs more than a forward)."""
+        key = (str(dev), D, H, W, C, L, cd)
+        if getattr(self, "_bufs_key", None) != key:
+            self._bufs = None
+            V = D * H * W
+            self._bufs = dict(X=_pinned(V * C), A=_pinned(V * C), B=_pinned(V * C), F=_pinned(V * C),
+                              pop=_pinned(V * L), xn=torch.empty(6, V, dtype=torch.float32, device=dev),
+                              zmm=torch.empty(1, D, H, W, dtype=torch.float32, device=dev),
+                              xs=torch.empty(6, cd * H * W, dtype=torch.float32, device=dev))
+            self._bufs_key = key
+        return self._bufs
+
     # ------------------------------------------------------------------------------------------------ forward
     def __call__(self, features, z_m, dx, dy, log10=False):
         """SI features (6, D, H, W) and heights z_m (D, H, W) in metres (host arrays) -> populations (D, H, W, L)
@@ -124,10 +138,9 @@ class StreamingForward:
         f_host = torch.from_numpy(features).pin_memory()
         zm_host = torch.from_numpy(z_m).reshape(-1).pin_memory()
         cd, cr = min(self.chunk_depth, D), min(self.chunk_rows, H)
-        xn = torch.empty(6, V, dtype=torch.float32, device=dev)
-        zmm = torch.empty(1, D, H, W, dtype=torch.float32, device=dev)
+        bufs = self._buffers(dev, D, H, W, C, L, cd)
+        xn, zmm, xs = bufs["xn"], bufs["zmm"], bufs["xs"]
         fs = torch.empty(6, cd * H * W, dtype=torch.float32, device=dev)
-        xs = torch.empty(6, cd * H * W, dtype=torch.float32, device=dev)
         zin = torch.empty(cd * H * W, dtype=torch.float32, device=dev)
         for d0, d1 in self._depth_slabs():
             Vs, o = (d1 - d0) * self.HW, d0 * self.HW
@@ -148,10 +161,16 @@ class StreamingForward:
         dw = torch.empty(V, dtype=torch.float32, device=dev)
         nat.call("ffno_depth_weights", zmm.data_ptr(), D, H * W, dw.data_ptr(), s)
         # host hidden states and device workspaces
-        X, A, B, F = (_pinned(V * C) for _ in range(4))
-        pop_host = torch.empty(V * L, dtype=torch.float32, pin_memory=True)
-        wsd = Workspace(cd, H, W, C, live, self.G, dev)
-        wsr = Workspace(D, cr, W, C, live, self.G, dev)
+        X, A, B, F, pop_host = bufs["X"], bufs["A"], bufs["B"], bufs["F"], bufs["pop"]
+        key = (cd, cr, live)
+        if bufs.get("ws_key") != key:
+            bufs["wsd"] = bufs["wsr"] = None
+            bufs["wsd"] = Workspace(cd, H, W, C, live, self.G, dev)
+            bufs["wsr"] = Workspace(D, cr, W, C, live, self.G, dev)
+            bufs["ws_key"] = key
+        wsd, wsr = bufs["wsd"], bufs["wsr"]
+        wsd.err.zero_()
+        wsr.err.zero_()
         nslab = max(-(-D // cd), -(-H // cr))
         maxp = max(wsd.partials.numel(), wsr.partials.numel()) // (self.G * 3)
         self.parts = torch.empty(nslab * maxp * self.G * 3, dtype=torch.float64, device=dev)
