@@ -88,6 +88,12 @@ PROTOTYPES = {
     "ffno_tc_width_supported": [I],
     "ffno_tc_set_prefetch_tiles": [I],
     "ffno_copy2d": [P, L, P, L, L, L, P],
+    "ffno_mesh_features": [P, P, L, I, P, I, I, P, P, P],
+    "ffno_mesh_features_vjp": [P, P, L, I, P, I, I, P, P, P, P, P],
+    "ffno_mesh_features_jvp": [P, P, L, I, P, I, I, P, P, P, P],
+    "ffno_mesh_backmap": [P, P, I, P, L, I, I, P, P],
+    "ffno_mesh_backmap_vjp": [P, P, I, P, L, I, I, P, P, P, P],
+    "ffno_mesh_backmap_jvp": [P, P, P, I, P, L, I, I, P, P],
     "ffno_mlp2_fwd_tc": [I, P, P, P, F, P, L, I, P, P, P, P, I, I, P, P],
     "ffno_gate_fwd_tc": [P, L, I, P, P, P, P, P, P],
     "ffno_fuse1_tc": [P, P, P, P, P, L, I, P, P, P, P, P, P],

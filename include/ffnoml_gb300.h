@@ -231,6 +231,27 @@ int ffno_outer_noalloc(const float* A, long lda, int Ma, const float* B, long ld
 
 /* _model_inputs + normalisation (:48-58, :274-276): SI features [6][V] (T, vx, vy, vz, log10 ne, log10 rho) and z [V]
  * in metres -> normalised inputs x [6][V] and z_mm [V] in Mm. */
+/* Population-mesh maps, FP64 (FFNOInversion.jl/src/PopulationMesh.jl:182-227 features, :335-360 back-map, :362-408
+ * and :522-573 transposes, :427-518 tangents). atm [6][ncol][nz] = T, vx, vy, vz, log10 ne, log10 rho; z [ncol][nz]
+ * and mesh [nm] decreasing (top first); f / fm_bar / fm_dot [ncol][nm][6]; kind [ncol][nm] (0 inside, 1 above the top,
+ * values held, 2 below the bottom, 3 corona: features left to the caller's hydrostatic extension); pm [L][ncol][nm];
+ * pop [L][ncol][nz]; feature_bar / feature_dot [ncol][nz][6]; z_bar [ncol][nz]. corona != 0: points above a column top
+ * are corona points. */
+int ffno_mesh_features(const double* atm, const double* z, long ncol, int nz, const double* mesh, int nm, int corona,
+                       double* f, int8_t* kind, ffno_stream_t stream);
+int ffno_mesh_features_vjp(const double* atm, const double* z, long ncol, int nz, const double* mesh, int nm,
+                           int corona, const double* f, const double* fm_bar, double* feature_bar, double* z_bar,
+                           ffno_stream_t stream);
+int ffno_mesh_features_jvp(const double* atm, const double* z, long ncol, int nz, const double* mesh, int nm,
+                           int corona, const double* f, const double* feature_dot, double* fm_dot,
+                           ffno_stream_t stream);
+int ffno_mesh_backmap(const double* pm, const double* mesh, int nm, const double* z, long ncol, int nz, int L,
+                      double* pop, ffno_stream_t stream);
+int ffno_mesh_backmap_vjp(const double* pm, const double* mesh, int nm, const double* z, long ncol, int nz, int L,
+                          const double* pop_bar, double* pm_bar, double* z_bar, ffno_stream_t stream);
+int ffno_mesh_backmap_jvp(const double* pm, const double* pm_dot, const double* mesh, int nm, const double* z,
+                          long ncol, int nz, int L, double* pop_dot, ffno_stream_t stream);
+
 /* Host-RAM streaming (ffno_batched_backend.py:147-289): strided block copy between pinned host memory and the device,
  * rows of `width` bytes `spitch` / `dpitch` apart (cudaMemcpy2DAsync, direction from the addresses). */
 int ffno_copy2d(void* dst, long dpitch, const void* src, long spitch, long width, long rows, ffno_stream_t stream);
