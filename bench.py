@@ -296,6 +296,53 @@ def dram_traffic(kernel, nbytes_per_launch):
     return ratio * nbytes_per_launch, rec.get("case")
 
 
+def population_mesh_rate(dev, nz=95, nx=256, ny=256, levels=12, reps=5):
+    """Columns per second of the population-mesh features map plus the back-map (and of their VJP) on a synthetic
+    log-tau cube: nz points per column (log tau500 -6 .. 1.4), heights varying by column, the default fixed mesh."""
+    import torch
+    from ffnoml_gb300.population_mesh import MeshMaps, PopulationMeshConfig, population_mesh
+    g = np.random.default_rng(11)
+    ncol = nx * ny
+    tau = 10.0 ** np.linspace(-6.0, 1.4, nz)
+    scale = 1 + 0.05 * g.random(ncol)
+    z = -1.2e5 * np.log(tau)[None, :] * scale[:, None] + 2e4 * g.random(ncol)[:, None]
+    atm = np.empty((6, ncol, nz))
+    atm[0] = (4300 + 1700 * tau ** 0.25)[None] * scale[:, None]
+    atm[1:4] = g.normal(0, 3e3, (3, ncol, nz))
+    atm[4] = 19 + 0.6 * np.log10(tau)[None] + 0.01 * g.random((ncol, nz))
+    atm[5] = -3.5 + 0.45 * np.log10(tau)[None] + 0.01 * g.random((ncol, nz))
+    mesh = population_mesh(PopulationMeshConfig())
+    maps = MeshMaps(z, mesh, dev)
+    at = torch.as_tensor(atm, device=dev)
+    pm = torch.exp(torch.randn(levels, ncol, len(mesh), dtype=torch.float64, device=dev))
+    pb = torch.randn(levels, ncol, nz, dtype=torch.float64, device=dev)
+
+    def fwd():
+        f, _ = maps.features(at)
+        return f, maps.backmap(pm)
+
+    def vjp(f):
+        maps.backmap_vjp(pm, pb)
+        maps.features_vjp(at, f, torch.ones_like(f))
+
+    f, _ = fwd()
+    vjp(f)
+    torch.cuda.synchronize()
+    a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    a.record()
+    for _ in range(reps):
+        fwd()
+    b.record()
+    for _ in range(reps):
+        vjp(f)
+    c.record()
+    torch.cuda.synchronize()
+    tf, tv = a.elapsed_time(b) / reps, b.elapsed_time(c) / reps
+    return {"value": ncol / (tf / 1e3), "unit": "columns/s", "ms_per_step": tf, "vjp_ms": tv, "columns": ncol,
+            "column_points": nz, "mesh_points": len(mesh), "levels": levels, "dtype": "f64",
+            "workload": f"{nx}x{ny} log-tau columns of {nz} points onto the default fixed mesh and back"}
+
+
 def run_gb300(args):
     import torch
     import torch.distributed as dist
@@ -453,6 +500,11 @@ def run_gb300(args):
                      "d2h_bytes_per_step": int(V * 12 * 4)}
         del sfw
 
+    # population-mesh maps (FP64): a log-tau cube's columns onto the default fixed mesh and the populations back
+    mesh_maps = None
+    if not args.fwd_only:
+        mesh_maps = population_mesh_rate(dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         torch.set_num_threads(len(os.sched_getaffinity(0)))
@@ -487,7 +539,7 @@ def run_gb300(args):
             "kernel_breakdown_ms": breakdown,
             "clocks": clocks, "memory": memory, "gpu_launches": launches * args.steps, "e2e": e2e,
             "cpu_baseline": cpu,
-            "serving": serving, "streaming": streaming,
+            "serving": serving, "streaming": streaming, "population_mesh": mesh_maps,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
