@@ -983,7 +983,8 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_a_tc(const float* __restrict
   pipe_finish(P, tslot, 2 * NCOL);
 }
 
-// Fuse backward, stage b: B_bar = hfb Wf1^T + [F_bar, F_bar] / 2; spec/vert grads B_bar g (+ the gate path);
+// Fuse backward, stage b: B_bar = hfb Wf1^T + [F_bar, F_bar] / 2; spec/vert grads B_bar g (+ the gate path, added by
+// the last GEMM onto the direct gradients kept in tensor memory, so each branch gradient is written once);
 // gate pre-activation grad q = B_bar [spec, vert] g (1 - g); hg_bar = (q Wg2^T) * gelu'(hg); A_bar = hg_bar Wg1^T:
 // x_bar = base + A_bar[:C], spec_bar = B_bar_s g_s + A_bar[C:2C], vert_bar likewise.
 // Weights: [wf1t (2C x 2C), wg2t (C x 2C), wg1t (3C x C)]. All three GEMMs run untransposed (lane = voxel; the
@@ -1005,7 +1006,6 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
   PIPE_PROLOGUE(3 * C, 2)
   const Split T = split_at(smem + B1 + B2 + B3 + pid * RB, TM, C);
   P.ok = load_weights(smem, wpack, B1 + B2 + B3, wcx, err);
-  const Op wg1t = wop(smem + B1 + B2, 3 * C, C);
   const int row = P.feat();
   const int pf = c_pf;
   for (int k = 1; P.ptid == 0 && k < pf; ++k) {
@@ -1041,16 +1041,15 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
     for (int kh = 0; kh < 2; ++kh) {
       const float* pre = kh == 0 ? sp : vp;
       const float* cf = kh == 0 ? sc : vc;
-      float* gout = kh == 0 ? sbar : vbar;
 #pragma unroll 1
       for (int jj = 0; jj < C / 16; ++jj) {
         const int j = kh * (C / 16) + jj;
         if (!owns(j, P.half)) continue;
         const int cc = 16 * jj;
-        float bb[16], q[16];
+        float bb[16], q[16], od[16];
         rld(P, 0, j, bb);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) q[i] = 0.f;
+        for (int i = 0; i < 16; ++i) q[i] = od[i] = 0.f;
         if (v < V) {
 #pragma unroll
           for (int i = 0; i < 16; i += 4) {
@@ -1058,16 +1057,16 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
             const float4 s4 = gn_apply<true>(ld4(pre + v * C + cc + i), gn_coefs(cf, C, cc + i));
             const float ff[4] = {f4.x, f4.y, f4.z, f4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w},
                         ss[4] = {s4.x, s4.y, s4.z, s4.w};
-            float o[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
               const float b = bb[i + u] + 0.5f * ff[u];
-              o[u] = b * gg[u];
+              od[i + u] = b * gg[u];
               q[i + u] = b * ss[u] * gg[u] * (1.f - gg[u]);
             }
-            *reinterpret_cast<float4*>(gout + v * C + cc + i) = make_float4(o[0], o[1], o[2], o[3]);
           }
         }
+        // the direct branch gradient replaces B_bar in its own accumulator columns; GEMM3 adds A_bar onto it
+        tc::tmem_st16(P.tmem + P.lq + (uint32_t)(16 * j), od);
         put16(T, row, cc, C, q);
       }
       if (!pipe_gemms(P, err, Gemm{P.tmem + 2 * C, kop(T, C), wop(smem + B1, C, 2 * C, 0, kh * C), C, kh > 0, C}))
@@ -1090,15 +1089,26 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
       }
       put16(T, row, c0, C, hb);
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, C), wg1t, C, false, 3 * C})) break;
+    // GEMM3: the branch rows of Wg1 accumulate onto the direct gradients (columns 0 .. 2C), the x rows go to the
+    // columns GEMM2 used (2C .. 3C)
+    const Gemm g3x{P.tmem + 2 * C, kop(T, C), wop(smem + B1 + B2, 3 * C, C, 0), C, false, C};
+    if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, C), wop(smem + B1 + B2, 3 * C, C, C), C, true, 2 * C}, &g3x)) break;
 #pragma unroll
     for (int j = 0; j < (3 * C) / 16; ++j) {
       if (!owns(j, P.half)) continue;
-      const int c0 = 16 * j;
       float r[16];
-      rld(P, 0, j, r);
-      if (v < V) {
-        if (c0 < C) {
+      if (j < 2 * C / 16) {   // spec_bar / vert_bar, written once
+        rld(P, 0, j, r);
+        float* g = j < C / 16 ? sbar : vbar;
+        const int cc = 16 * (j % (C / 16));
+        if (v < V)
+#pragma unroll
+          for (int i = 0; i < 16; i += 4)
+            *reinterpret_cast<float4*>(g + v * C + cc + i) = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
+      } else {                // x_bar = base + A_bar[:C]
+        const int c0 = 16 * (j - 2 * C / 16);
+        rld(P, 2 * C, j - 2 * C / 16, r);
+        if (v < V)
 #pragma unroll
           for (int i = 0; i < 16; i += 4) {
             float4 o = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
@@ -1108,17 +1118,6 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
             }
             *reinterpret_cast<float4*>(xbar + v * C + c0 + i) = o;
           }
-        } else {
-          float* g = c0 < 2 * C ? sbar : vbar;
-          const int cc = c0 < 2 * C ? c0 - C : c0 - 2 * C;
-#pragma unroll
-          for (int i = 0; i < 16; i += 4) {
-            float4* pp = reinterpret_cast<float4*>(g + v * C + cc + i);
-            float4 o = *pp;
-            o = make_float4(o.x + r[i], o.y + r[i + 1], o.z + r[i + 2], o.w + r[i + 3]);
-            *pp = o;
-          }
-        }
       }
     }
   }
