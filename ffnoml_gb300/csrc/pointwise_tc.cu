@@ -861,31 +861,27 @@ __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__
     for (int j = 0; j < C / 16; ++j) {
       if (!owns(j, P.half)) continue;
       const int c0 = 16 * j;
-      float g[16], q[16];
+      float g[16], q[16], o[16];
       rld(P, D2, j, g);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) q[i] = 0.f;
+      for (int i = 0; i < 16; ++i) q[i] = o[i] = 0.f;
       if (v < V) {
 #pragma unroll
         for (int i = 0; i < 16; i += 4) {
           const float4 b = ld4(gbar + v * C + c0 + i), xv = ld4(x + v * C + c0 + i);
-          const float bb[4] = {b.x, b.y, b.z, b.w}, xx[4] = {xv.x, xv.y, xv.z, xv.w};
-          float o[4];
+          const float4 bs = base ? ld4(base + v * C + c0 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float bb[4] = {b.x, b.y, b.z, b.w}, xx[4] = {xv.x, xv.y, xv.z, xv.w}, ba[4] = {bs.x, bs.y, bs.z, bs.w};
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             const float s = sigmoid_tc(g[i + u]);
-            o[u] = bb[u] * s;
+            o[i + u] = fmaf(bb[u], s, ba[u]);
             q[i + u] = bb[u] * xx[u] * s * (1.f - s);
             if (zp) zs = fmaf(bb[u], __ldg(zp + c0 + i + u), zs);
           }
-          float4 r = make_float4(o[0], o[1], o[2], o[3]);
-          if (base) {
-            const float4 bs = ld4(base + v * C + c0 + i);
-            r = make_float4(r.x + bs.x, r.y + bs.y, r.z + bs.z, r.w + bs.w);
-          }
-          *reinterpret_cast<float4*>(xbar + v * C + c0 + i) = r;
         }
       }
+      // base + gbar s into the last GEMM's accumulator, which adds the gate-path gradient onto it
+      tc::tmem_st16(P.tmem + P.lq + D4 + (uint32_t)c0, o);
       put16(T, row, c0, C, q);
     }
     if (zp) {   // the two halves of the row add their parts of z_bar in a fixed order
@@ -904,7 +900,7 @@ __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__
       for (int i = 0; i < 16; ++i) hb[i] *= gelu_grad_tc(hp[i]);
       put16(T, row, 16 * j, C, hb);
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem + D4, kop(T, C), g1t, C, false, C})) break;
+    if (!pipe_gemms(P, err, Gemm{P.tmem + D4, kop(T, C), g1t, C, true, C})) break;
 #pragma unroll
     for (int j = 0; j < C / 16; ++j) {
       if (!owns(j, P.half)) continue;
@@ -913,12 +909,8 @@ __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__
       rld(P, D4, j, r);
       if (v < V)
 #pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          float4* pp = reinterpret_cast<float4*>(xbar + v * C + c0 + i);
-          float4 o = *pp;
-          o = make_float4(o.x + r[i], o.y + r[i + 1], o.z + r[i + 2], o.w + r[i + 3]);
-          *pp = o;
-        }
+        for (int i = 0; i < 16; i += 4)
+          *reinterpret_cast<float4*>(xbar + v * C + c0 + i) = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
     }
   }
   pipe_finish(P, tslot, 2 * NCOL);
