@@ -97,22 +97,32 @@ __global__ void __launch_bounds__(256) k_gn_bwd_stats(int mode, const float* __r
   }
   double d1[4] = {0, 0, 0, 0}, d2[4] = {0, 0, 0, 0};   // per element slot (groups of slot j fixed per thread)
   float f1[4] = {0, 0, 0, 0}, f2[4] = {0, 0, 0, 0};
-  int n = 0;
   const long step = (long)gridDim.x * 8 * Ln::VPW;
-  for (long v = ((long)blockIdx.x * 8 + warp) * Ln::VPW + sub; v < V; v += step) {
-    if (!active) break;
-    const float4 pu = __ldg(reinterpret_cast<const float4*>(u + v * C + c));
-    const float4 pp = __ldg(reinterpret_cast<const float4*>(pre + v * C + c));
-    const float uu[4] = {pu.x, pu.y, pu.z, pu.w}, xx[4] = {pp.x, pp.y, pp.z, pp.w};
+  // UN voxels a thread are loaded before any is used (loads in flight); float partials go to double every 4 rounds
+  constexpr int UN = 4;
+  int n = 0;
+  for (long v0 = ((long)blockIdx.x * 8 + warp) * Ln::VPW + sub; active && v0 < V; v0 += UN * step) {
+    float4 pu[UN], pp[UN];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int g = grp[j];
-      const float xh = (xx[j] - k.mean[g]) * k.rstd[g];
-      const float gh = upstream(mode, uu[j], r, xh * gm[j] + bt[j]) * gm[j];
-      f1[j] += gh;
-      f2[j] += gh * xh;
+    for (int e = 0; e < UN; ++e) {
+      const long v = v0 + e * step;
+      pu[e] = v < V ? __ldg(reinterpret_cast<const float4*>(u + v * C + c)) : make_float4(0.f, 0.f, 0.f, 0.f);
+      pp[e] = v < V ? __ldg(reinterpret_cast<const float4*>(pre + v * C + c)) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    if (++n == 16) {
+#pragma unroll
+    for (int e = 0; e < UN; ++e) {
+      if (v0 + e * step >= V) break;
+      const float uu[4] = {pu[e].x, pu[e].y, pu[e].z, pu[e].w}, xx[4] = {pp[e].x, pp[e].y, pp[e].z, pp[e].w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int g = grp[j];
+        const float xh = (xx[j] - k.mean[g]) * k.rstd[g];
+        const float gh = upstream(mode, uu[j], r, xh * gm[j] + bt[j]) * gm[j];
+        f1[j] += gh;
+        f2[j] += gh * xh;
+      }
+    }
+    if (++n == 4) {
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         d1[j] += f1[j];
@@ -205,14 +215,27 @@ __global__ void __launch_bounds__(256) k_gn_bwd_apply(int mode, const float* __r
   }
   const long step = (long)gridDim.x * 8 * Ln::VPW;
   const long first = ((long)blockIdx.x * 8 + warp) * Ln::VPW;
-  for (long vb = first; vb < V; vb += step) {   // warp-uniform loop
-    const long v = vb + sub;
+  constexpr int UN = 2;   // voxel rounds whose loads are issued together
+  for (long vb0 = first; vb0 < V; vb0 += UN * step) {   // warp-uniform loop
+   float4 pus[UN], pps[UN];
+   float wvs[UN];
+#pragma unroll
+   for (int e = 0; e < UN; ++e) {
+    const long v = vb0 + e * step + sub;
+    const bool ok = active && v < V;
+    wvs[e] = ok ? __ldg(dw + v) : 0.f;
+    pus[e] = ok ? __ldg(reinterpret_cast<const float4*>(u + v * C + c)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    pps[e] = ok ? __ldg(reinterpret_cast<const float4*>(pre + v * C + c)) : make_float4(0.f, 0.f, 0.f, 0.f);
+   }
+#pragma unroll
+   for (int e = 0; e < UN; ++e) {
+    if (vb0 + e * step >= V) break;   // warp-uniform
+    const long v = vb0 + e * step + sub;
     const bool ok = active && v < V;
     float wc = 0.f;
     if (ok) {
-      const float wv = __ldg(dw + v);
-      const float4 pu = __ldg(reinterpret_cast<const float4*>(u + v * C + c));
-      const float4 pp = __ldg(reinterpret_cast<const float4*>(pre + v * C + c));
+      const float wv = wvs[e];
+      const float4 pu = pus[e], pp = pps[e];
       const float uu[4] = {pu.x, pu.y, pu.z, pu.w}, xx[4] = {pp.x, pp.y, pp.z, pp.w};
       float o[4];
 #pragma unroll
@@ -234,6 +257,7 @@ __global__ void __launch_bounds__(256) k_gn_bwd_apply(int mode, const float* __r
       for (int off = Ln::LPV / 2; off; off >>= 1) wc += __shfl_xor_sync(0xffffffffu, wc, off);
     }
     if (ok && q == 0) w_bar[v] += wc;
+   }
   }
 }
 

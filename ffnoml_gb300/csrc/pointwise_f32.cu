@@ -175,21 +175,52 @@ __global__ void k_gn_finalize(const double* __restrict__ partials, int nparts, i
 }
 
 // ------------------------------------------------------------------------------------------------ elementwise
-__global__ void k_gn_act(const float* __restrict__ pre, const float* __restrict__ coefs, long n, int C, int act,
+// y = GN(pre) from the finalized coefficients, 4 channels a thread (float4), two float4 in flight per round; the
+// channel index from a 32-bit modulo (n / 4 < 2^31 is checked by the launchers).
+__device__ __forceinline__ float4 gn4(float4 p, const float* __restrict__ cf, int C, int c) {
+  const float4 m = __ldg(reinterpret_cast<const float4*>(cf + c));
+  const float4 sc = __ldg(reinterpret_cast<const float4*>(cf + C + c));
+  const float4 b = __ldg(reinterpret_cast<const float4*>(cf + 2 * C + c));
+  return make_float4((p.x - m.x) * sc.x + b.x, (p.y - m.y) * sc.y + b.y, (p.z - m.z) * sc.z + b.z,
+                     (p.w - m.w) * sc.w + b.w);
+}
+
+__global__ void k_gn_act(const float* __restrict__ pre, const float* __restrict__ coefs, unsigned n4, int C, int act,
                          float* __restrict__ out) {
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(e % C);
-    float y = (pre[e] - coefs[c]) * coefs[C + c] + coefs[2 * C + c];
-    out[e] = act ? gelu(y) : y;
+  const unsigned C4 = (unsigned)C / 4, stride = gridDim.x * blockDim.x;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += 2 * stride) {
+    const unsigned i2 = i + stride;
+    const float4 p0 = __ldg(reinterpret_cast<const float4*>(pre) + i);
+    const float4 p1 = i2 < n4 ? __ldg(reinterpret_cast<const float4*>(pre) + i2) : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 y = gn4(p0, coefs, C, (int)(i % C4) * 4);
+    if (act) y = make_float4(gelu(y.x), gelu(y.y), gelu(y.z), gelu(y.w));
+    reinterpret_cast<float4*>(out)[i] = y;
+    if (i2 < n4) {
+      y = gn4(p1, coefs, C, (int)(i2 % C4) * 4);
+      if (act) y = make_float4(gelu(y.x), gelu(y.y), gelu(y.z), gelu(y.w));
+      reinterpret_cast<float4*>(out)[i2] = y;
+    }
   }
 }
 
 __global__ void k_resid_out(const float* __restrict__ x2, const float* __restrict__ pre,
-                            const float* __restrict__ coefs, float res, long n, int C, float* __restrict__ out) {
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(e % C);
-    const float y = (pre[e] - coefs[c]) * coefs[C + c] + coefs[2 * C + c];
-    out[e] = x2[e] + res * y;
+                            const float* __restrict__ coefs, float res, unsigned n4, int C, float* __restrict__ out) {
+  const unsigned C4 = (unsigned)C / 4, stride = gridDim.x * blockDim.x;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += 2 * stride) {
+    const unsigned i2 = i + stride;
+    const bool two = i2 < n4;
+    const float4 p0 = __ldg(reinterpret_cast<const float4*>(pre) + i);
+    const float4 a0 = __ldg(reinterpret_cast<const float4*>(x2) + i);
+    const float4 p1 = two ? __ldg(reinterpret_cast<const float4*>(pre) + i2) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 a1 = two ? __ldg(reinterpret_cast<const float4*>(x2) + i2) : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 y = gn4(p0, coefs, C, (int)(i % C4) * 4);
+    reinterpret_cast<float4*>(out)[i] =
+        make_float4(fmaf(res, y.x, a0.x), fmaf(res, y.y, a0.y), fmaf(res, y.z, a0.z), fmaf(res, y.w, a0.w));
+    if (two) {
+      y = gn4(p1, coefs, C, (int)(i2 % C4) * 4);
+      reinterpret_cast<float4*>(out)[i2] =
+          make_float4(fmaf(res, y.x, a1.x), fmaf(res, y.y, a1.y), fmaf(res, y.z, a1.z), fmaf(res, y.w, a1.w));
+    }
   }
 }
 
@@ -511,21 +542,31 @@ int ffno_gn_finalize(const double* partials, int nparts, int C, int groups, cons
   return FFNO_OK;
 }
 
+bool elementwise_ok(long V, int C, const void* a, const void* b, const void* c) {
+  return V >= 1 && C >= 4 && C % 4 == 0 && V * (long)C / 4 < 0x7fffffffL &&
+         ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(c)) % 16) == 0;
+}
+
+int elementwise_blocks(long n4) {
+  const long want = (n4 + 511) / 512, cap = (long)num_sms() * 8;
+  return (int)(want < cap ? (want > 0 ? want : 1) : cap);
+}
+
 int ffno_gn_act(const float* pre, const float* coefs, long V, int C, int act, float* out, ffno_stream_t stream) {
-  if (V < 1 || C < 1) return FFNO_EINVAL;
-  const long n = V * C;
-  const int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
-  k_gn_act<<<blocks, 256, 0, (cudaStream_t)stream>>>(pre, coefs, n, C, act, out);
+  if (!pre || !coefs || !out || !elementwise_ok(V, C, pre, coefs, out)) return FFNO_EINVAL;
+  const long n4 = V * C / 4;
+  k_gn_act<<<elementwise_blocks(n4), 256, 0, (cudaStream_t)stream>>>(pre, coefs, (unsigned)n4, C, act, out);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }
 
 int ffno_resid_out(const float* x2, const float* pre, const float* coefs, float res, long V, int C, float* out,
                    ffno_stream_t stream) {
-  if (V < 1 || C < 1) return FFNO_EINVAL;
-  const long n = V * C;
-  const int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
-  k_resid_out<<<blocks, 256, 0, (cudaStream_t)stream>>>(x2, pre, coefs, res, n, C, out);
+  if (!x2 || !pre || !coefs || !out || !elementwise_ok(V, C, x2, pre, out) ||
+      reinterpret_cast<uintptr_t>(coefs) % 16)
+    return FFNO_EINVAL;
+  const long n4 = V * C / 4;
+  k_resid_out<<<elementwise_blocks(n4), 256, 0, (cudaStream_t)stream>>>(x2, pre, coefs, res, (unsigned)n4, C, out);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }
