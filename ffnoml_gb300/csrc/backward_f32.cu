@@ -215,27 +215,14 @@ __global__ void __launch_bounds__(256) k_gn_bwd_apply(int mode, const float* __r
   }
   const long step = (long)gridDim.x * 8 * Ln::VPW;
   const long first = ((long)blockIdx.x * 8 + warp) * Ln::VPW;
-  constexpr int UN = 2;   // voxel rounds whose loads are issued together
-  for (long vb0 = first; vb0 < V; vb0 += UN * step) {   // warp-uniform loop
-   float4 pus[UN], pps[UN];
-   float wvs[UN];
-#pragma unroll
-   for (int e = 0; e < UN; ++e) {
-    const long v = vb0 + e * step + sub;
-    const bool ok = active && v < V;
-    wvs[e] = ok ? __ldg(dw + v) : 0.f;
-    pus[e] = ok ? __ldg(reinterpret_cast<const float4*>(u + v * C + c)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    pps[e] = ok ? __ldg(reinterpret_cast<const float4*>(pre + v * C + c)) : make_float4(0.f, 0.f, 0.f, 0.f);
-   }
-#pragma unroll
-   for (int e = 0; e < UN; ++e) {
-    if (vb0 + e * step >= V) break;   // warp-uniform
-    const long v = vb0 + e * step + sub;
+  for (long vb = first; vb < V; vb += step) {   // warp-uniform loop
+    const long v = vb + sub;
     const bool ok = active && v < V;
     float wc = 0.f;
     if (ok) {
-      const float wv = wvs[e];
-      const float4 pu = pus[e], pp = pps[e];
+      const float wv = __ldg(dw + v);
+      const float4 pu = __ldg(reinterpret_cast<const float4*>(u + v * C + c));
+      const float4 pp = __ldg(reinterpret_cast<const float4*>(pre + v * C + c));
       const float uu[4] = {pu.x, pu.y, pu.z, pu.w}, xx[4] = {pp.x, pp.y, pp.z, pp.w};
       float o[4];
 #pragma unroll
@@ -257,7 +244,6 @@ __global__ void __launch_bounds__(256) k_gn_bwd_apply(int mode, const float* __r
       for (int off = Ln::LPV / 2; off; off >>= 1) wc += __shfl_xor_sync(0xffffffffu, wc, off);
     }
     if (ok && q == 0) w_bar[v] += wc;
-   }
   }
 }
 
