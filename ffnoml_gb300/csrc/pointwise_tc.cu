@@ -658,7 +658,13 @@ __global__ void __launch_bounds__(CT, 1) k_fuse1_tc(const float* __restrict__ x,
 }
 
 // Fuse (second half of _fuse_branches): B = [spec gs, vert gv], pre = gelu(B Wf1) Wf2 + (spec gs + vert gv) / 2, with
-// the GroupNorm partials of pre. Weights: [wf1 (2C x 2C), wf2 (C x 2C)].
+// the GroupNorm partials of pre. Weights: [wf1 (2C x 2C), wf2 (C x 2C)]. The residual (spec gs + vert gv) / 2 is read
+// from the split B tile (hi + lo) into the second accumulator before the hidden layer overwrites the tile, and GEMM2
+// adds onto it, so pre is never recomputed from HBM.
+__device__ __forceinline__ float bf16_at(const uint8_t* p) {
+  return __uint_as_float((uint32_t)(*reinterpret_cast<const uint16_t*>(p)) << 16);
+}
+
 template <int C>
 __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp, const float* __restrict__ sc,
                                                     const float* __restrict__ vp, const float* __restrict__ vc,
@@ -670,7 +676,7 @@ __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp
   constexpr uint32_t B1 = mat_bytes(2 * C, 2 * C), B2 = mat_bytes(C, 2 * C), RB = tile_bytes(2 * C);
   __shared__ float wt[2][TM], wpart[2][4], red[2][4 * GMAX];
   __shared__ double acc[2 * GMAX * 3];
-  PIPE_PROLOGUE(TM, 2)
+  PIPE_PROLOGUE(2 * TM, 2)
   const Split A = split_at(smem + B1 + B2 + pid * RB, TM, 2 * C);
   if (tid < 2 * GMAX * 3) acc[tid] = 0.0;
   P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
@@ -680,9 +686,6 @@ __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp
   const float* src = kf < C ? sp : vp;
   const int ks = kf < C ? kf : kf - C;
   const int f = P.feat();
-  const int fc = f < C ? f : 0;   // this thread's output channel (epilogue) and its GroupNorm coefficients
-  const float sm = __ldg(sc + fc), ss = __ldg(sc + C + fc), sb = __ldg(sc + 2 * C + fc);
-  const float vm = __ldg(vc + fc), vs = __ldg(vc + C + fc), vbb = __ldg(vc + 2 * C + fc);
   const int pf = c_pf;
   for (int k = 1; P.ptid == 0 && k < pf; ++k) {
     const long tp = t0 + k * tstep;
@@ -705,6 +708,24 @@ __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp
       return make_float4(s.x * g.x, s.y * g.y, s.z * g.z, s.w * g.w);
     });
     if (!pipe_gemms(P, err, Gemm{P.tmem, wf1, kop(A, 2 * C), 2 * C, false})) break;
+    if (32 * P.q < C) {   // warps holding output channels: the residual of their lanes, columns of their half
+#pragma unroll 1
+      for (int c = 0; c < 4; ++c) {
+        const int vl0 = 64 * P.half + 16 * c;
+        float r[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          float x = 0.f;
+          if (f < C) {
+            const uint32_t os = tc::kmajor_offset(vl0 + i, f, 2 * C), ov = tc::kmajor_offset(vl0 + i, C + f, 2 * C);
+            x = 0.5f * ((bf16_at(A.hi() + os) + bf16_at(A.lo() + os)) + (bf16_at(A.hi() + ov) + bf16_at(A.lo() + ov)));
+          }
+          r[i] = x;
+        }
+        tc::tmem_st16(P.tmem + P.lq + TM + (uint32_t)vl0, r);
+      }
+    }
+    pipe_sync(P.id);   // the tile is read; the hidden layer may overwrite it
 #pragma unroll 1
     for (int c = 0; c < 4; ++c) {
       float h[16];
@@ -713,30 +734,18 @@ __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp
       for (int i = 0; i < 16; ++i) h[i] = gelu_tc(h[i]);
       if (f < 2 * C) put_mn(A, f, 64 * P.half + 16 * c, h);
     }
-    if (!pipe_gemms(P, err, Gemm{P.tmem, wf2, mop(A), 2 * C, false})) break;
-    // pre = gelu(B Wf1) Wf2 + (spec gs + vert gv) / 2, written to HBM and back to tensor memory for the statistics
+    if (!pipe_gemms(P, err, Gemm{P.tmem + TM, wf2, mop(A), 2 * C, true})) break;
 #pragma unroll 1
     for (int c = 0; c < 4; ++c) {
       float o[16];
-      tld(P, 0, c, o);
+      tld(P, TM, c, o);
       const long vb = v0 + 64 * P.half + 16 * c;
       if (f < C)
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const long v = vb + i;
-          if (v < V) {
-            const float s = gelu_tc((__ldg(sp + v * C + f) - sm) * ss + sb) * __ldg(gates + v * 2 * C + f);
-            const float u = gelu_tc((__ldg(vp + v * C + f) - vm) * vs + vbb) * __ldg(gates + v * 2 * C + C + f);
-            o[i] += 0.5f * (s + u);
-            pre[v * C + f] = o[i];
-          }
-        }
-      tc::tmem_st16(P.tmem + P.lq + (uint32_t)(64 * P.half + 16 * c), o);
+        for (int i = 0; i < 16; ++i)
+          if (vb + i < V) pre[(vb + i) * C + f] = o[i];
     }
-    tc::tc_before_sync();
-    pipe_sync(P.id);
-    tc::tc_after_sync();
-    tile_stats<C>(P, 0, wt[pid], wpart[pid], red[pid], acc + pid * GMAX * 3);
+    tile_stats<C>(P, TM, wt[pid], wpart[pid], red[pid], acc + pid * GMAX * 3);
   }
   write_partial2(partials, acc);
   pipe_finish(P, tslot, 2 * NCOL);
