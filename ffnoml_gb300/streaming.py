@@ -5,7 +5,8 @@ Every operation of the model is local, acts on depth planes, or acts on columns,
 without changing the operator (ffno_batched_backend.py:1-13): the lift, gates, branch post-MLPs, fusion, pw / mlp and
 the head over depth slabs; the horizontal spectral convolution over depth slabs (each plane's rfft2 / mixing / irfft2
 is its own); the height operator over row slabs [D][h0:h1][W] (each column alone). The hidden states live in pinned
-host memory, channels last like the device layout; slabs move with strided copies (ffno_copy2d). A depth-weighted
+host memory, channels last like the device layout; slabs move with strided copies (ffno_copy2d) on two copy streams,
+pipelined over two device buffer sets so that one slab's copies overlap another's kernels. A depth-weighted
 GroupNorm gathers every slab's partial statistics (the kernels' per-CTA Chan partials, FP64) into one buffer and
 finalizes once, so the statistics are those of the whole cube; its application is folded into the next stage's
 kernels as in the resident executor, so each GroupNorm costs no extra pass over the cube.
@@ -26,6 +27,12 @@ from .runtime import INPUT_CHANNELS, _check
 
 def _pinned(n):
     return torch.empty(n, dtype=torch.float32, pin_memory=True)
+
+
+def _record(stream):
+    e = torch.cuda.Event()
+    e.record(stream)
+    return e
 
 
 class StreamingForward:
@@ -96,6 +103,34 @@ class StreamingForward:
         for name, h in zip(names, hosts):
             self._d2h(h, d0 * self.HW * self.C, getattr(ws, name), n)
 
+    def _run(self, items, make, load, compute, store):
+        """One stage over its slabs, pipelined over two device buffer sets: the host -> device copies of slab k (on
+        the h2d stream) overlap the kernels of slab k-1 (the current stream) and the device -> host copies of slab
+        k-2 (the d2h stream); events order every reuse of a buffer set, and the stage ends with the current stream
+        waiting for its last copy back, so the next stage (and a GroupNorm finalize) sees whole host buffers."""
+        comp = torch.cuda.current_stream()
+        self.h2d.wait_event(_record(comp))
+        free = [None, None]
+        for k, item in enumerate(items):
+            b = k & 1
+            ws = make(b, item)
+            self.slabs += 1
+            with torch.cuda.stream(self.h2d):
+                if free[b] is not None:
+                    self.h2d.wait_event(free[b])
+                if load is not None:
+                    load(ws, item)
+                loaded = _record(self.h2d)
+            comp.wait_event(loaded)
+            compute(ws, item)
+            done = _record(comp)
+            with torch.cuda.stream(self.d2h):
+                self.d2h.wait_event(done)
+                if store is not None:
+                    store(ws, item)
+                free[b] = _record(self.d2h)
+        comp.wait_event(_record(self.d2h))
+
     def _buffers(self, dev, D, H, W, C, L, cd):
         """Pinned host hidden states and device inputs, kept while the cube shape repeats (pinning GBs of host
         memory costs more than a forward)."""
@@ -160,95 +195,120 @@ class StreamingForward:
         live = hgt["live"]
         dw = torch.empty(V, dtype=torch.float32, device=dev)
         nat.call("ffno_depth_weights", zmm.data_ptr(), D, H * W, dw.data_ptr(), s)
-        # host hidden states and device workspaces
+        # host hidden states, two device buffer sets per slab kind (the copies of one slab overlap the kernels of
+        # the other), the copy streams
         X, A, B, F, pop_host = bufs["X"], bufs["A"], bufs["B"], bufs["F"], bufs["pop"]
         key = (cd, cr, live)
         if bufs.get("ws_key") != key:
             bufs["wsd"] = bufs["wsr"] = None
-            bufs["wsd"] = Workspace(cd, H, W, C, live, self.G, dev)
-            bufs["wsr"] = Workspace(D, cr, W, C, live, self.G, dev)
+            bufs["wsd"] = [Workspace(cd, H, W, C, live, self.G, dev) for _ in range(2)]
+            bufs["wsr"] = [Workspace(D, cr, W, C, live, self.G, dev) for _ in range(2)]
             bufs["ws_key"] = key
         wsd, wsr = bufs["wsd"], bufs["wsr"]
-        wsd.err.zero_()
-        wsr.err.zero_()
+        for w in wsd + wsr:
+            w.err.zero_()
+        if getattr(self, "h2d", None) is None or self.h2d.device != dev:
+            self.h2d, self.d2h = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
         nslab = max(-(-D // cd), -(-H // cr))
-        maxp = max(wsd.partials.numel(), wsr.partials.numel()) // (self.G * 3)
+        maxp = max(wsd[0].partials.numel(), wsr[0].partials.numel()) // (self.G * 3)
         self.parts = torch.empty(nslab * maxp * self.G * 3, dtype=torch.float64, device=dev)
         self.npart = 0
         self.coefs = {n: torch.empty(3 * C, dtype=torch.float32, device=dev) for n in ("lift",) + _NORMS}
         self.gstats = {n: torch.empty(self.G * 3, dtype=torch.float64, device=dev) for n in ("lift",) + _NORMS}
         self.slabs = 0
+        depth = list(self._depth_slabs())
 
         def slab_inputs(d0, d1):
-            """Normalised model inputs of depth slab d0:d1, contiguous [6][Vs] (in xs)."""
+            """Normalised model inputs of depth slab d0:d1, contiguous [6][Vs] (in xs; the current stream)."""
             Vs = (d1 - d0) * self.HW
             self._rows(xs.data_ptr(), Vs * 4, xn.data_ptr() + d0 * self.HW * 4, V * 4, Vs * 4, 6)
             return xs
 
-        def depth_ws(d0, d1):
-            ws = self._view(wsd, (d1 - d0) * self.HW)
-            ws.dw = dw[d0 * self.HW:d1 * self.HW]
+        def depth_ws(b, it):
+            ws = self._view(wsd[b], (it[1] - it[0]) * self.HW)
+            ws.buf = b
+            ws.dw = dw[it[0] * self.HW:it[1] * self.HW]
             for n in self.coefs:
                 ws.coefs[n] = self.coefs[n]
-            self.slabs += 1
+            return ws
+
+        def row_ws(b, it):
+            rows = it[1] - it[0]
+            ws = self._view(wsr[b], D * rows * W)
+            ws.dw = dw.view(D, H, W)[:, it[0]:it[1]].contiguous().view(-1)
+            ws.zr = zmm.view(D, H, W)[:, it[0]:it[1]].contiguous()
+            for n in self.coefs:
+                ws.coefs[n] = self.coefs[n]
             return ws
 
         # lift: pre-activation and statistics, then GELU(GN(.)) into X
-        for d0, d1 in self._depth_slabs():
-            ws = depth_ws(d0, d1)
-            x = slab_inputs(d0, d1)
+        def lift(ws, it):
+            x = slab_inputs(*it)
             nat.call("ffno_lift_fwd", x.data_ptr(), m.in_channels, ws.V, C, pk.lift_w.data_ptr(), ws.dw.data_ptr(),
-                     ws.pre.data_ptr(), ws.partials.data_ptr(), ws.nparts, self.G, s)
-            self._store(ws, ["pre"], d0, d1, [A])
+                     ws.pre.data_ptr(), ws.partials.data_ptr(), ws.nparts, self.G, _stream())
             self._stats(ws, False)
+
+        self._run(depth, depth_ws, None, lift, lambda ws, it: self._store(ws, ["pre"], it[0], it[1], [A]))
         self._finalize("lift", pk.lift_g, pk.lift_b)
-        for d0, d1 in self._depth_slabs():
-            ws = depth_ws(d0, d1)
-            self._load(ws, ["pre"], d0, d1, [A])
-            nat.call("ffno_gn_act", ws.pre.data_ptr(), self.coefs["lift"].data_ptr(), ws.V, C, 1, ws.x.data_ptr(), s)
-            self._store(ws, ["x"], d0, d1, [X])
+
+        def act(ws, it):
+            nat.call("ffno_gn_act", ws.pre.data_ptr(), self.coefs["lift"].data_ptr(), ws.V, C, 1, ws.x.data_ptr(),
+                     _stream())
+
+        self._run(depth, depth_ws, lambda ws, it: self._load(ws, ["pre"], it[0], it[1], [A]), act,
+                  lambda ws, it: self._store(ws, ["x"], it[0], it[1], [X]))
         for i in range(m.n_layers):
-            self._block(pk, i, wsd, wsr, depth_ws, dw, zmm, hgt, pln, pfr[i], X, A, B, F, dev)
-        # head, and the SI populations of each slab
-        out = torch.empty(L, cd * H * W, dtype=torch.float32, device=dev)
-        pop = torch.empty(cd * H * W, L, dtype=torch.float32, device=dev)
-        for d0, d1 in self._depth_slabs():
-            ws = depth_ws(d0, d1)
-            x = slab_inputs(d0, d1)
-            self._load(ws, ["x"], d0, d1, [X])
-            y = out.view(-1)[:L * ws.V].view(L, ws.V)      # the head writes [L][Vs] contiguously
+            self._block(pk, i, depth_ws, row_ws, hgt, pln, pfr[i], X, A, B, F)
+
+        # head, and the SI populations (or log10 n) of each slab, one output buffer per buffer set
+        outs = [torch.empty(L, cd * H * W, dtype=torch.float32, device=dev) for _ in range(2)]
+        pops = [torch.empty(cd * H * W, L, dtype=torch.float32, device=dev) for _ in range(2)]
+
+        def head(ws, it):
+            b = ws.buf
+            x = slab_inputs(*it)
+            y = outs[b].view(-1)[:L * ws.V].view(L, ws.V)      # the head writes [L][Vs] contiguously
             nat.call("ffno_head_fwd", ws.x.data_ptr(), x.data_ptr(), ws.V, C, pk.p1.data_ptr(), pk.p2.data_ptr(),
-                     pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head, y.data_ptr(), None, s)
-            if log10:   # y std_Y + mean_Y into rows of [L][V]
-                lg = pop.view(-1)[:L * ws.V].view(L, ws.V)
-                torch.addcmul(norm["mean_Y"][:, None], y, norm["std_Y"][:, None], out=lg)
-                self._rows(pop_host.data_ptr() + d0 * self.HW * 4, V * 4, lg.data_ptr(), ws.V * 4, ws.V * 4, L)
-                continue
-            nat.call("ffno_si_populations", y.data_ptr(), ws.V, L, norm["mean_Y"].data_ptr(), norm["std_Y"].data_ptr(),
-                     pop.data_ptr(), flags.data_ptr(), s)
-            self._d2h(pop_host, d0 * self.HW * L, pop, ws.V * L)
+                     pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head, y.data_ptr(), None, _stream())
+            if log10:   # y std_Y + mean_Y
+                torch.addcmul(norm["mean_Y"][:, None], y, norm["std_Y"][:, None],
+                              out=pops[b].view(-1)[:L * ws.V].view(L, ws.V))
+            else:
+                nat.call("ffno_si_populations", y.data_ptr(), ws.V, L, norm["mean_Y"].data_ptr(),
+                         norm["std_Y"].data_ptr(), pops[b].data_ptr(), flags.data_ptr(), _stream())
+
+        def head_out(ws, it):
+            b = ws.buf
+            if log10:   # rows of [L][V]
+                self._rows(pop_host.data_ptr() + it[0] * self.HW * 4, V * 4, pops[b].data_ptr(), ws.V * 4, ws.V * 4,
+                           L)
+            else:
+                self._d2h(pop_host, it[0] * self.HW * L, pops[b], ws.V * L)
+
+        self._run(depth, depth_ws, lambda ws, it: self._load(ws, ["x"], it[0], it[1], [X]), head, head_out)
         torch.cuda.current_stream().synchronize()
         _check(flags.item(), "FFNO streaming output")
-        if any(int(w.err.item()) for w in (wsd, wsr)):
+        if any(int(w.err.item()) for w in wsd + wsr):
             raise RuntimeError("tensor-core kernel timed out")
         if log10:
             return pop_host.numpy().reshape(L, D, H, W).copy()
         return pop_host.numpy().reshape(D, H, W, L).copy()
 
     # ------------------------------------------------------------------------------------------------ one block
-    def _block(self, pk, i, wsd, wsr, depth_ws, dw, zmm, hgt, pln, fq, X, A, B, F, dev):
-        m, ex = self.model, self.ex
+    def _block(self, pk, i, depth_ws, row_ws, hgt, pln, fq, X, A, B, F):
+        ex = self.ex
         C, D, H, W, HW, Wf = self.C, self.D, self.H, self.W, self.HW, self.W // 2 + 1
-        s = _stream()
         bp = pk.blocks[i]
         live = hgt["live"]
         tc = ex._tc()
         r_f, r_pw, r_mlp = bp["res"]
+        depth = list(self._depth_slabs())
+        ld = lambda names, hosts: (lambda ws, it: self._load(ws, names, it[0], it[1], hosts))
+        st = lambda names, hosts: (lambda ws, it: self._store(ws, names, it[0], it[1], hosts))
+
         # horizontal spectral branch over depth slabs -> spec_pre (A)
-        for d0, d1 in self._depth_slabs():
-            ws = depth_ws(d0, d1)
-            Ds = d1 - d0
-            self._load(ws, ["x"], d0, d1, [X])
+        def spectral(ws, it):
+            s, Ds = _stream(), it[1] - it[0]
             if tc:
                 nat.call("ffno_gate_fwd_tc", ws.x.data_ptr(), ws.V, C, bp["tc_s_gate"].data_ptr(), None, None,
                          ws.xs.data_ptr(), ws.err.data_ptr(), s)
@@ -261,42 +321,46 @@ class StreamingForward:
             ex._mix(ws, "s", bp, fq, ws.sb, ws.sa, H * Wf, Ds, C, 2 * H * Wf * C, H * Wf * C, False)
             ex._xf(pln, "thi", ws.sa, ws.sb, d["hf"], ws)
             ex._xf(pln, "twi", ws.sb, ws.ys, d["wi"], ws)
-            t = ex._mlp2(ws, 0, ws.ys, None, None, 0.0, None, bp["s_p1"], bp["s_p2"], bp.get("tc_s_post"),
-                         ws.spec_pre)
-            self._store(ws, ["spec_pre"], d0, d1, [A])
-            self._stats(ws, t)
+            self._stats(ws, ex._mlp2(ws, 0, ws.ys, None, None, 0.0, None, bp["s_p1"], bp["s_p2"], bp.get("tc_s_post"),
+                                     ws.spec_pre))
+
+        self._run(depth, depth_ws, ld(["x"], [X]), spectral, st(["spec_pre"], [A]))
         self._finalize("spec", bp["spec_g"], bp["spec_b"])
-        # height branch over row slabs [D][h0:h1][W] -> vert_pre (B)
+
+        # height branch over row slabs [D][h0:h1][W] -> vert_pre (B): strided copies of D rows each
         hq = hgt["freq"][i]
         rowb = HW * C * 4
-        for h0, h1 in self._row_slabs():
-            rows = h1 - h0
-            ws = self._view(wsr, D * rows * W)
-            ws.dw = dw.view(D, H, W)[:, h0:h1].contiguous().view(-1)
-            zr = zmm.view(D, H, W)[:, h0:h1].contiguous()
-            width = rows * W * C * 4
-            self._rows(ws.x.data_ptr(), width, X.data_ptr() + h0 * W * C * 4, rowb, width, D)
-            self.slabs += 1
+
+        def rows_in(ws, it):
+            width = (it[1] - it[0]) * W * C * 4
+            self._rows(ws.x.data_ptr(), width, X.data_ptr() + it[0] * W * C * 4, rowb, width, D)
+
+        def rows_out(ws, it):
+            width = (it[1] - it[0]) * W * C * 4
+            self._rows(B.data_ptr() + it[0] * W * C * 4, rowb, ws.vert_pre.data_ptr(), width, width, D)
+
+        def vertical(ws, it):
+            s, rows = _stream(), it[1] - it[0]
             if tc:
                 nat.call("ffno_gate_fwd_tc", ws.x.data_ptr(), ws.V, C, bp["tc_v_gate"].data_ptr(), bp["v_zp"].data_ptr(),
-                         zr.data_ptr(), ws.xv.data_ptr(), ws.err.data_ptr(), s)
+                         ws.zr.data_ptr(), ws.xv.data_ptr(), ws.err.data_ptr(), s)
             else:
                 nat.call("ffno_gate_fwd", ws.x.data_ptr(), ws.V, C, bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(),
-                         bp["v_zp"].data_ptr(), zr.data_ptr(), ws.xv.data_ptr(), s)
+                         bp["v_zp"].data_ptr(), ws.zr.data_ptr(), ws.xv.data_ptr(), s)
             d = _descs(D, rows, W, C, live)
             RW = rows * W
             ex._xf(hgt, "tzf", ws.xv, ws.va, d["zf"], ws)
             ex._mix(ws, "v", bp, hq, ws.va, ws.vb, live, RW, RW * C, C, live * RW * C, False)
             ex._xf(hgt, "tzi", ws.vb, ws.yv, d["zi"], ws)
-            t = ex._mlp2(ws, 0, ws.yv, None, None, 0.0, None, bp["v_p1"], bp["v_p2"], bp.get("tc_v_post"),
-                         ws.vert_pre)
-            self._rows(B.data_ptr() + h0 * W * C * 4, rowb, ws.vert_pre.data_ptr(), width, width, D)
-            self._stats(ws, t)
+            self._stats(ws, ex._mlp2(ws, 0, ws.yv, None, None, 0.0, None, bp["v_p1"], bp["v_p2"], bp.get("tc_v_post"),
+                                     ws.vert_pre))
+
+        self._run(list(self._row_slabs()), row_ws, rows_in, vertical, rows_out)
         self._finalize("vert", bp["vert_g"], bp["vert_b"])
+
         # fusion -> fused_pre (F)
-        for d0, d1 in self._depth_slabs():
-            ws = depth_ws(d0, d1)
-            self._load(ws, ["x", "spec_pre", "vert_pre"], d0, d1, [X, A, B])
+        def fusion(ws, it):
+            s = _stream()
             if tc:
                 ex._fuse1_tc(ws, bp, ws.x, None)
                 nat.call("ffno_fuse2_tc", ws.spec_pre.data_ptr(), self.coefs["spec"].data_ptr(),
@@ -308,34 +372,33 @@ class StreamingForward:
                          ws.vert_pre.data_ptr(), self.coefs["vert"].data_ptr(), ws.V, C, bp["bg1"].data_ptr(),
                          bp["bg2"].data_ptr(), bp["bgb"].data_ptr(), bp["f1"].data_ptr(), bp["f2"].data_ptr(),
                          ws.dw.data_ptr(), ws.fused_pre.data_ptr(), ws.partials.data_ptr(), ws.nparts, self.G, s)
-            self._store(ws, ["fused_pre"], d0, d1, [F])
             self._stats(ws, tc)
+
+        self._run(depth, depth_ws, ld(["x", "spec_pre", "vert_pre"], [X, A, B]), fusion, st(["fused_pre"], [F]))
         self._finalize("fuse", bp["fuse_g"], bp["fuse_b"])
+
         # x1 = x + r_f gelu(GN(fused_pre)) (A), pw_pre (B)
-        for d0, d1 in self._depth_slabs():
-            ws = depth_ws(d0, d1)
-            self._load(ws, ["x", "fused_pre"], d0, d1, [X, F])
-            t = ex._mlp2(ws, 1, ws.x, ws.fused_pre, self.coefs["fuse"], r_f, ws.x1, bp["pw1"], bp["pw2"],
-                         bp.get("tc_pw"), ws.pw_pre)
-            self._store(ws, ["x1", "pw_pre"], d0, d1, [A, B])
-            self._stats(ws, t)
+        def pw(ws, it):
+            self._stats(ws, ex._mlp2(ws, 1, ws.x, ws.fused_pre, self.coefs["fuse"], r_f, ws.x1, bp["pw1"], bp["pw2"],
+                                     bp.get("tc_pw"), ws.pw_pre))
+
+        self._run(depth, depth_ws, ld(["x", "fused_pre"], [X, F]), pw, st(["x1", "pw_pre"], [A, B]))
         self._finalize("pw", bp["pw_g"], bp["pw_b"])
+
         # x2 = x1 + r_pw GN(pw_pre) (F), mlp_pre (A, over x1 slab by slab)
-        for d0, d1 in self._depth_slabs():
-            ws = depth_ws(d0, d1)
-            self._load(ws, ["x1", "pw_pre"], d0, d1, [A, B])
-            t = ex._mlp2(ws, 2, ws.x1, ws.pw_pre, self.coefs["pw"], r_pw, ws.x2, bp["m1"], bp["m2"], bp.get("tc_mlp"),
-                         ws.mlp_pre)
-            self._store(ws, ["x2", "mlp_pre"], d0, d1, [F, A])
-            self._stats(ws, t)
+        def mlp(ws, it):
+            self._stats(ws, ex._mlp2(ws, 2, ws.x1, ws.pw_pre, self.coefs["pw"], r_pw, ws.x2, bp["m1"], bp["m2"],
+                                     bp.get("tc_mlp"), ws.mlp_pre))
+
+        self._run(depth, depth_ws, ld(["x1", "pw_pre"], [A, B]), mlp, st(["x2", "mlp_pre"], [F, A]))
         self._finalize("mlp", bp["mlp_g"], bp["mlp_b"])
+
         # block output x = x2 + r_mlp GN(mlp_pre) (X)
-        for d0, d1 in self._depth_slabs():
-            ws = depth_ws(d0, d1)
-            self._load(ws, ["x2", "mlp_pre"], d0, d1, [F, A])
+        def out(ws, it):
             nat.call("ffno_resid_out", ws.x2.data_ptr(), ws.mlp_pre.data_ptr(), self.coefs["mlp"].data_ptr(), r_mlp,
-                     ws.V, C, ws.x.data_ptr(), s)
-            self._store(ws, ["x"], d0, d1, [X])
+                     ws.V, C, ws.x.data_ptr(), _stream())
+
+        self._run(depth, depth_ws, ld(["x2", "mlp_pre"], [F, A]), out, st(["x"], [X]))
 
 
 _NORMS = ("spec", "vert", "fuse", "pw", "mlp")
