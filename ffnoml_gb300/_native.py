@@ -34,6 +34,7 @@ class HeadParams(ctypes.Structure):
         ("mean_y", F * FFNO_MAX_LEVELS), ("std_y", F * FFNO_MAX_LEVELS),
         ("log_g", D * FFNO_MAX_LEVELS), ("ev", D * FFNO_MAX_LEVELS), ("ndxi", D * FFNO_MAX_LEVELS),
         ("dion", D * FFNO_MAX_LEVELS),
+        ("math32", I),
     ]
 
 

@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(NT) k_lift_bwd(const float* __restrict__ pb, i
 
 // ------------------------------------------------------------------------------------------------ head backward
 
-template <int C, int NHP>
+template <int C, int NHP, typename T>
 __global__ void __launch_bounds__(NT) k_head_bwd(const float* __restrict__ x, const float* __restrict__ xin,
                                                  const float* __restrict__ ybar, long V, const float* __restrict__ p1,
                                                  const float* __restrict__ p2, const float* __restrict__ b2,
@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(NT) k_head_bwd(const float* __restrict__ x, co
   float* SG = SP + BM * LH;   // gelu(hidden), later the hidden gradient
   float* SO = SG + BM * LH;   // head channels, later their gradient
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const double lnc = ln_ccon();
+  const T lnc = (T)ln_ccon(), LN10 = (T)kLN10;
   const long nt = ntiles(V, BM);
   for (long t = blockIdx.x; t < nt; t += gridDim.x) {
     const long v0 = t * BM;
@@ -634,42 +634,42 @@ __global__ void __launch_bounds__(NT) k_head_bwd(const float* __restrict__ x, co
       float* o = SO + r * LO;
       if (v < V) {
         const int tc = hp.temperature_channel, ec = hp.ne_channel, rc = hp.rho_channel;
-        const double lt = (double)__ldg(xin + (long)tc * V + v) * (double)hp.std_x[tc] + (double)hp.mean_x[tc];
-        const double lne = (double)__ldg(xin + (long)ec * V + v) * (double)hp.std_x[ec] + (double)hp.mean_x[ec];
-        const double tk = exp10(lt);
-        const double ne = exp10(lne - 6.0);
-        const double conl = lnc + (lne - 6.0) * kLN10 - 1.5 * lt * kLN10;
-        const double dxi = 4.98e-4 * 5040.0 / tk * sqrt(ne * kBK * tk);
-        const double ek_t = (kEE / kBK) / tk;
-        double gsum = 0.0, ltb = 0.0, lneb = 0.0;
+        const T lt = (T)__ldg(xin + (long)tc * V + v) * (T)hp.std_x[tc] + (T)hp.mean_x[tc];
+        const T lne = (T)__ldg(xin + (long)ec * V + v) * (T)hp.std_x[ec] + (T)hp.mean_x[ec];
+        const T tk = mexp10(lt);
+        const T ne = mexp10(lne - (T)6);
+        const T conl = lnc + (lne - (T)6) * LN10 - (T)1.5 * lt * LN10;
+        const T dxi = (T)(4.98e-4 * 5040.0) / tk * msqrt(ne * (T)kBK * tk);
+        const T ek_t = (T)(kEE / kBK) / tk;
+        T gsum = 0, ltb = 0, lneb = 0;
         int hc = 0, lvl = 0;
         for (int s = 0; s < hp.nspecies; ++s) {
           const int L = hp.levels[s];
-          double logit[FFNO_MAX_LEVELS], gl[FFNO_MAX_LEVELS];
-          double mx = -1e300;
+          T logit[FFNO_MAX_LEVELS], gl[FFNO_MAX_LEVELS];
+          T mx = (T)-1e30;
           for (int i = 0; i < L; ++i) {
             const int g = lvl + i;
-            logit[i] = (double)o[hc + i] + hp.log_g[g] - ek_t * (hp.ev[g] - dxi * hp.ndxi[g]) - hp.dion[g] * conl;
+            logit[i] = (T)o[hc + i] + (T)hp.log_g[g] - ek_t * ((T)hp.ev[g] - dxi * (T)hp.ndxi[g]) - (T)hp.dion[g] * conl;
             mx = fmax(mx, logit[i]);
           }
-          double se = 0.0;
-          for (int i = 0; i < L; ++i) se += exp(logit[i] - mx);
-          double G = 0.0;
+          T se = 0;
+          for (int i = 0; i < L; ++i) se += mexp(logit[i] - mx);
+          T G = 0;
           for (int i = 0; i < L; ++i) {
-            gl[i] = (double)__ldg(ybar + (long)(lvl + i) * V + v) / (double)hp.std_y[lvl + i];
+            gl[i] = (T)__ldg(ybar + (long)(lvl + i) * V + v) / (T)hp.std_y[lvl + i];
             G += gl[i];
           }
           gsum += G;
-          const double tb = (double)hp.total_bound;
-          const double th = tanh((double)o[hc + L] / tb);
-          const float ubar = (float)(G * (1.0 - th * th));
+          const T tb = (T)hp.total_bound;
+          const T th = mtanh((T)o[hc + L] / tb);
+          const float ubar = (float)(G * ((T)1 - th * th));
           for (int i = 0; i < L; ++i) {
             const int g = lvl + i;
-            const double p = exp(logit[i] - mx) / se;
-            const double lb = (gl[i] - p * G) / kLN10;
+            const T p = mexp(logit[i] - mx) / se;
+            const T lb = (gl[i] - p * G) / LN10;
             o[hc + i] = (float)lb;
-            ltb += lb * kLN10 * (ek_t * (hp.ev[g] - 1.5 * dxi * hp.ndxi[g]) + 1.5 * hp.dion[g]);
-            lneb += lb * kLN10 * (0.5 * ek_t * dxi * hp.ndxi[g] - hp.dion[g]);
+            ltb += lb * LN10 * (ek_t * ((T)hp.ev[g] - (T)1.5 * dxi * (T)hp.ndxi[g]) + (T)1.5 * (T)hp.dion[g]);
+            lneb += lb * LN10 * ((T)0.5 * ek_t * dxi * (T)hp.ndxi[g] - (T)hp.dion[g]);
           }
           o[hc + L] = ubar;
           hc += L + 1;
@@ -677,10 +677,10 @@ __global__ void __launch_bounds__(NT) k_head_bwd(const float* __restrict__ x, co
         }
         for (int c = hc; c < NHP; ++c) o[c] = 0.f;
         for (int k = 0; k < hp.in_channels; ++k) {
-          double val = 0.0;
-          if (k == tc) val += ltb * (double)hp.std_x[tc];
-          if (k == ec) val += lneb * (double)hp.std_x[ec];
-          if (k == rc) val += gsum * (double)hp.std_x[rc];
+          T val = 0;
+          if (k == tc) val += ltb * (T)hp.std_x[tc];
+          if (k == ec) val += lneb * (T)hp.std_x[ec];
+          if (k == rc) val += gsum * (T)hp.std_x[rc];
           xinbar[(long)k * V + v] = (float)val;
         }
       } else {
@@ -970,9 +970,15 @@ int ffno_head_bwd(const float* x, const float* x_in, const float* y_bar, long V,
 #define L(CC, NN)                                                                                        \
   if (C == CC && nhp == NN) {                                                                            \
     const size_t smem = (BM * (CC + 1) + 2 * BM * (2 * CC + 1) + BM * (NN + 1)) * sizeof(float);         \
-    if (!smem_attr(k_head_bwd<CC, NN>, smem)) return FFNO_ELAUNCH;                                       \
-    k_head_bwd<CC, NN><<<grid_of(V, BM, 2), NT, smem, s>>>(x, x_in, y_bar, V, p1, p2, b2, p2t, p1t, *params, \
-                                                           x_bar, x_in_bar);                             \
+    if (params->math32) {                                                                               \
+      if (!smem_attr(k_head_bwd<CC, NN, float>, smem)) return FFNO_ELAUNCH;                             \
+      k_head_bwd<CC, NN, float><<<grid_of(V, BM, 2), NT, smem, s>>>(x, x_in, y_bar, V, p1, p2, b2, p2t, p1t, \
+                                                                    *params, x_bar, x_in_bar);          \
+    } else {                                                                                            \
+      if (!smem_attr(k_head_bwd<CC, NN, double>, smem)) return FFNO_ELAUNCH;                            \
+      k_head_bwd<CC, NN, double><<<grid_of(V, BM, 2), NT, smem, s>>>(x, x_in, y_bar, V, p1, p2, b2, p2t, p1t, \
+                                                                     *params, x_bar, x_in_bar);         \
+    }                                                                                                   \
   }
     default:
       L(16, 16) L(16, 32) L(32, 16) L(32, 32) L(64, 16) L(64, 32) L(96, 16) L(96, 32)

@@ -53,6 +53,18 @@ __device__ __forceinline__ float gelu_grad_tc(float x) {
 }
 __device__ __forceinline__ float sigmoid_tc(float x) { return __fdividef(1.f, 1.f + __expf(-x)); }
 
+// Math of the level-fraction head in the scalar type of the caller: FP64 (the reference's arithmetic) or FP32.
+__device__ __forceinline__ double mexp10(double x) { return exp10(x); }
+__device__ __forceinline__ float mexp10(float x) { return exp10f(x); }
+__device__ __forceinline__ double mexp(double x) { return exp(x); }
+__device__ __forceinline__ float mexp(float x) { return expf(x); }
+__device__ __forceinline__ double mlog(double x) { return log(x); }
+__device__ __forceinline__ float mlog(float x) { return logf(x); }
+__device__ __forceinline__ double msqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float msqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double mtanh(double x) { return tanh(x); }
+__device__ __forceinline__ float mtanh(float x) { return tanhf(x); }
+
 // MULTI3D constants, cgs (models/ffno_model.py:111-112)
 constexpr double kEE = 1.602189e-12, kBK = 1.380662e-16;
 constexpr double kLN10 = 2.302585092994045684;

@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(NT) k_fuse(const float* __restrict__ x, const 
 
 // ------------------------------------------------------------------------------------------------ head
 
-template <int C, int NHP>
+template <int C, int NHP, typename T>
 __global__ void __launch_bounds__(NT) k_head(const float* __restrict__ x, const float* __restrict__ xin, long V,
                                              const float* __restrict__ p1, const float* __restrict__ p2,
                                              const float* __restrict__ b2, int nh, ffno_head_params hp,
@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(NT) k_head(const float* __restrict__ x, const 
   float* hs = as + BM * LA;
   float* os = hs + BM * LH;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const double lnc = ln_ccon();
+  const T lnc = (T)ln_ccon(), LN10 = (T)kLN10;
   const long nt = ntiles_of(V);
   for (long t = blockIdx.x; t < nt; t += gridDim.x) {
     const long v0 = t * BM;
@@ -453,35 +453,35 @@ __global__ void __launch_bounds__(NT) k_head(const float* __restrict__ x, const 
         if (head_out)
           for (int c = 0; c < nh; ++c) head_out[(long)c * V + v] = o[c];
         const int tc = hp.temperature_channel, ec = hp.ne_channel, rc = hp.rho_channel;
-        const double lt = (double)__ldg(xin + (long)tc * V + v) * (double)hp.std_x[tc] + (double)hp.mean_x[tc];
-        const double lne = (double)__ldg(xin + (long)ec * V + v) * (double)hp.std_x[ec] + (double)hp.mean_x[ec];
-        const double lrho = (double)__ldg(xin + (long)rc * V + v) * (double)hp.std_x[rc] + (double)hp.mean_x[rc];
-        const double tk = exp10(lt);
-        const double ne = exp10(lne - 6.0);  // cm^-3
-        const double conl = lnc + (lne - 6.0) * kLN10 - 1.5 * lt * kLN10;
-        const double dxi = 4.98e-4 * 5040.0 / tk * sqrt(ne * kBK * tk);
-        const double ek_t = (kEE / kBK) / tk;
+        const T lt = (T)__ldg(xin + (long)tc * V + v) * (T)hp.std_x[tc] + (T)hp.mean_x[tc];
+        const T lne = (T)__ldg(xin + (long)ec * V + v) * (T)hp.std_x[ec] + (T)hp.mean_x[ec];
+        const T lrho = (T)__ldg(xin + (long)rc * V + v) * (T)hp.std_x[rc] + (T)hp.mean_x[rc];
+        const T tk = mexp10(lt);
+        const T ne = mexp10(lne - (T)6);  // cm^-3
+        const T conl = lnc + (lne - (T)6) * LN10 - (T)1.5 * lt * LN10;
+        const T dxi = (T)(4.98e-4 * 5040.0) / tk * msqrt(ne * (T)kBK * tk);
+        const T ek_t = (T)(kEE / kBK) / tk;
         int hc = 0, lvl = 0;
         for (int s = 0; s < hp.nspecies; ++s) {
           const int L = hp.levels[s];
-          double logit[FFNO_MAX_LEVELS];
-          double mx = -1e300;
+          T logit[FFNO_MAX_LEVELS];
+          T mx = (T)-1e30;
           for (int i = 0; i < L; ++i) {
             const int g = lvl + i;
-            const double lte = hp.log_g[g] - ek_t * (hp.ev[g] - dxi * hp.ndxi[g]) - hp.dion[g] * conl;
-            logit[i] = (double)o[hc + i] + lte;
+            const T lte = (T)hp.log_g[g] - ek_t * ((T)hp.ev[g] - dxi * (T)hp.ndxi[g]) - (T)hp.dion[g] * conl;
+            logit[i] = (T)o[hc + i] + lte;
             mx = fmax(mx, logit[i]);
           }
           float se = 0.f;
           for (int i = 0; i < L; ++i) se += expf((float)(logit[i] - mx));
-          const double lse = (double)logf(se);
-          const double tb = (double)hp.total_bound;
-          const double tot = tb * tanh((double)o[hc + L] / tb);
-          const double base = lrho - (double)hp.log10_particle_mass[s] + tot;
+          const T lse = (T)logf(se);
+          const T tb = (T)hp.total_bound;
+          const T tot = tb * mtanh((T)o[hc + L] / tb);
+          const T base = lrho - (T)hp.log10_particle_mass[s] + tot;
           for (int i = 0; i < L; ++i) {
             const int g = lvl + i;
-            const double l10 = base + (logit[i] - mx - lse) / kLN10;
-            out[(long)g * V + v] = (float)((l10 - (double)hp.mean_y[g]) / (double)hp.std_y[g]);
+            const T l10 = base + (logit[i] - mx - lse) / LN10;
+            out[(long)g * V + v] = (float)((l10 - (T)hp.mean_y[g]) / (T)hp.std_y[g]);
           }
           hc += L + 1;
           lvl += L;
@@ -660,8 +660,13 @@ int ffno_head_fwd(const float* x, const float* x_in, long V, int C, const float*
 #define L(CC, NN)                                                                                       \
   if (C == CC && nhp == NN) {                                                                           \
     const size_t smem = (BM * (CC + 1) + BM * (2 * CC + 1) + BM * (NN + 1)) * sizeof(float);            \
-    if (!set_smem(k_head<CC, NN>, smem)) return FFNO_ELAUNCH;                                           \
-    k_head<CC, NN><<<grid_for(V, 2), NT, smem, s>>>(x, x_in, V, p1, p2, b2, nh, *params, out, head_out); \
+    if (params->math32) {                                                                               \
+      if (!set_smem(k_head<CC, NN, float>, smem)) return FFNO_ELAUNCH;                                  \
+      k_head<CC, NN, float><<<grid_for(V, 2), NT, smem, s>>>(x, x_in, V, p1, p2, b2, nh, *params, out, head_out); \
+    } else {                                                                                            \
+      if (!set_smem(k_head<CC, NN, double>, smem)) return FFNO_ELAUNCH;                                 \
+      k_head<CC, NN, double><<<grid_for(V, 2), NT, smem, s>>>(x, x_in, V, p1, p2, b2, nh, *params, out, head_out); \
+    }                                                                                                   \
   }
     default:
       L(16, 16) L(16, 32) L(32, 16) L(32, 32) L(64, 16) L(64, 32) L(96, 16) L(96, 32)

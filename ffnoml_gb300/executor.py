@@ -170,6 +170,10 @@ class Packed:
         b2[:nh] = model.proj2.bias.detach().float()
         self.b2 = dev(b2)
         self.head = self._head_params(model)
+        # the split-BF16 path evaluates the LTE weights and log-softmax in FP32 (its tolerance is 2e-3 dex; FP32
+        # rounding there is ~1e-6 dex), the FP32 path in FP64 as the reference does
+        self.head32 = nat.HeadParams.from_buffer_copy(self.head)
+        self.head32.math32 = 1
         self.freq_params = {k: v.detach().cpu() for k, v in model.state_dict().items() if ".freq_" in k}
         self.freq_key = table_store.freq_key(self.freq_params)
 
@@ -653,6 +657,10 @@ class Executor:
             nat.call("ffno_spectral_mix", inp.data_ptr(), out.data_ptr(), F, nb, sf, sb, s_im, m.width, w.data_ptr(),
                      g.data_ptr(), _ptr(u), _ptr(v), m.freq_mix_rank, s)
 
+    def _hp(self, pk):
+        """The head's parameters: FP32 LTE math on the split-BF16 path, FP64 on the FP32 path."""
+        return pk.head32 if self._tc() else pk.head
+
     def _tc(self):
         """Whether the split-BF16 tensor-core kernels run (precision 'bf16' at a width they support; never inside a
         JVP, which is FP32)."""
@@ -682,7 +690,7 @@ class Executor:
         m = self.model
         V = x.shape[0]
         nat.call("ffno_head_fwd", x.data_ptr(), xin.data_ptr(), V, m.width, pk.p1.data_ptr(), pk.p2.data_ptr(),
-                 pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head, out.data_ptr(), None, _stream())
+                 pk.b2.data_ptr(), pk.nh, pk.nhp, self._hp(pk), out.data_ptr(), None, _stream())
 
     # -------------------------------------------------------------------------------------------- JVP
     def jvp(self, x, z_scale, dx, dy, x_dot):
@@ -722,7 +730,8 @@ class Executor:
                     self._block_jvp(pk, ws, tw, i, tw.xp, D, H, W, hgt_b, pln, pfr[i])
                 self._head(pk, ws.x, xin, y[b])
                 nat.call("ffno_head_jvp", ws.x.data_ptr(), tw.x.data_ptr(), xin.data_ptr(), xin_dot.data_ptr(), V, C,
-                         pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.nhp, pk.head, out[b].data_ptr(), s)
+                         pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.nhp, self._hp(pk),
+                         out[b].data_ptr(), s)
             self._check(ws)
         finally:
             self._tls.fp32 = False
@@ -824,7 +833,7 @@ class Executor:
             # head
             nat.call("ffno_head_bwd", inputs[-1].data_ptr(), xin.data_ptr(), ybar[b].data_ptr(), V, C,
                      pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.p2t.data_ptr(), pk.p1t.data_ptr(),
-                     pk.nhp, pk.head, gb.xbar.data_ptr(), xbar_in[b].data_ptr(), s)
+                     pk.nhp, self._hp(pk), gb.xbar.data_ptr(), xbar_in[b].data_ptr(), s)
             cached = state.get("blocks")
             for i in reversed(range(m.n_layers)):
                 if cached and cached[b][i] is not None:

@@ -52,6 +52,8 @@ typedef struct {
   float mean_x[8], std_x[8];
   float mean_y[FFNO_MAX_LEVELS], std_y[FFNO_MAX_LEVELS];
   double log_g[FFNO_MAX_LEVELS], ev[FFNO_MAX_LEVELS], ndxi[FFNO_MAX_LEVELS], dion[FFNO_MAX_LEVELS];
+  int math32; /* nonzero: the LTE weights and log-softmax in FP32 (the split-BF16 path's tolerance); 0: FP64 as the
+                 reference computes them */
 } ffno_head_params;
 
 /* library version string */
