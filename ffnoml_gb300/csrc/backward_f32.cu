@@ -590,8 +590,8 @@ __global__ void __launch_bounds__(NT) k_head_bwd(const float* __restrict__ x, co
                                                  const float* __restrict__ ybar, long V, const float* __restrict__ p1,
                                                  const float* __restrict__ p2, const float* __restrict__ b2,
                                                  const float* __restrict__ p2t, const float* __restrict__ p1t,
-                                                 ffno_head_params hp, float* __restrict__ xbar,
-                                                 float* __restrict__ xinbar) {
+                                                 const __grid_constant__ ffno_head_params hp,
+                                                 float* __restrict__ xbar, float* __restrict__ xinbar) {
   extern __shared__ float sm[];
   constexpr int LA = C + 1, LH = 2 * C + 1, LO = NHP + 1;
   float* SA = sm;
@@ -599,7 +599,6 @@ __global__ void __launch_bounds__(NT) k_head_bwd(const float* __restrict__ x, co
   float* SG = SP + BM * LH;   // gelu(hidden), later the hidden gradient
   float* SO = SG + BM * LH;   // head channels, later their gradient
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const T lnc = (T)ln_ccon(), LN10 = (T)kLN10;
   const long nt = ntiles(V, BM);
   for (long t = blockIdx.x; t < nt; t += gridDim.x) {
     const long v0 = t * BM;
@@ -633,56 +632,7 @@ __global__ void __launch_bounds__(NT) k_head_bwd(const float* __restrict__ x, co
       const long v = v0 + r;
       float* o = SO + r * LO;
       if (v < V) {
-        const int tc = hp.temperature_channel, ec = hp.ne_channel, rc = hp.rho_channel;
-        const T lt = (T)__ldg(xin + (long)tc * V + v) * (T)hp.std_x[tc] + (T)hp.mean_x[tc];
-        const T lne = (T)__ldg(xin + (long)ec * V + v) * (T)hp.std_x[ec] + (T)hp.mean_x[ec];
-        const T tk = mexp10(lt);
-        const T ne = mexp10(lne - (T)6);
-        const T conl = lnc + (lne - (T)6) * LN10 - (T)1.5 * lt * LN10;
-        const T dxi = (T)(4.98e-4 * 5040.0) / tk * msqrt(ne * (T)kBK * tk);
-        const T ek_t = (T)(kEE / kBK) / tk;
-        T gsum = 0, ltb = 0, lneb = 0;
-        int hc = 0, lvl = 0;
-        for (int s = 0; s < hp.nspecies; ++s) {
-          const int L = hp.levels[s];
-          T logit[FFNO_MAX_LEVELS], gl[FFNO_MAX_LEVELS];
-          T mx = (T)-1e30;
-          for (int i = 0; i < L; ++i) {
-            const int g = lvl + i;
-            logit[i] = (T)o[hc + i] + (T)hp.log_g[g] - ek_t * ((T)hp.ev[g] - dxi * (T)hp.ndxi[g]) - (T)hp.dion[g] * conl;
-            mx = fmax(mx, logit[i]);
-          }
-          T se = 0;
-          for (int i = 0; i < L; ++i) se += mexp(logit[i] - mx);
-          T G = 0;
-          for (int i = 0; i < L; ++i) {
-            gl[i] = (T)__ldg(ybar + (long)(lvl + i) * V + v) / (T)hp.std_y[lvl + i];
-            G += gl[i];
-          }
-          gsum += G;
-          const T tb = (T)hp.total_bound;
-          const T th = mtanh((T)o[hc + L] / tb);
-          const float ubar = (float)(G * ((T)1 - th * th));
-          for (int i = 0; i < L; ++i) {
-            const int g = lvl + i;
-            const T p = mexp(logit[i] - mx) / se;
-            const T lb = (gl[i] - p * G) / LN10;
-            o[hc + i] = (float)lb;
-            ltb += lb * LN10 * (ek_t * ((T)hp.ev[g] - (T)1.5 * dxi * (T)hp.ndxi[g]) + (T)1.5 * (T)hp.dion[g]);
-            lneb += lb * LN10 * ((T)0.5 * ek_t * dxi * (T)hp.ndxi[g] - (T)hp.dion[g]);
-          }
-          o[hc + L] = ubar;
-          hc += L + 1;
-          lvl += L;
-        }
-        for (int c = hc; c < NHP; ++c) o[c] = 0.f;
-        for (int k = 0; k < hp.in_channels; ++k) {
-          T val = 0;
-          if (k == tc) val += ltb * (T)hp.std_x[tc];
-          if (k == ec) val += lneb * (T)hp.std_x[ec];
-          if (k == rc) val += gsum * (T)hp.std_x[rc];
-          xinbar[(long)k * V + v] = (float)val;
-        }
+        head_voxel_bwd<T>(hp, o, NHP, head_inputs(hp, xin, V, v), ybar, V, v, xinbar);
       } else {
         for (int c = 0; c < NHP; ++c) o[c] = 0.f;
       }

@@ -76,6 +76,126 @@ __device__ __forceinline__ double ln_ccon() {
   return log(0.5 * a * a * a);
 }
 
+// ------------------------------------------------------------------------------------------ level-fraction head
+// One voxel of FFNO3D.head_output after proj2 (models/ffno_model.py:729-748): per species, logits = head channels + the
+// LTE Boltzmann/Saha log-weights of (T, ne), log-softmax over the levels, plus the bounded total b tanh(u / b),
+// log10 rho and the particle mass; normalised with mean_Y / std_Y. o: the voxel's head channels (species s: its L
+// level logits, then its total channel). The LTE math and the log-softmax run in T (double: the reference's FP64;
+// float: FP32), except the forward's sum of the max-shifted exponentials, which lie in (0, 1] and are summed in FP32
+// (relative error of the log-sum about 1e-7).
+struct HeadInputs {
+  float lt, lne, lrho;   // log10 T, log10 ne (SI), log10 rho of the voxel (denormalised)
+};
+
+__device__ __forceinline__ HeadInputs head_inputs(const ffno_head_params& hp, const float* __restrict__ xin, long V,
+                                                  long v) {
+  const int tc = hp.temperature_channel, ec = hp.ne_channel, rc = hp.rho_channel;
+  return HeadInputs{__ldg(xin + (long)tc * V + v), __ldg(xin + (long)ec * V + v), __ldg(xin + (long)rc * V + v)};
+}
+
+template <typename T>
+struct Lte {
+  T lt, lne, conl, dxi, ek_t;
+  __device__ __forceinline__ Lte(const ffno_head_params& hp, const HeadInputs& in) {
+    const int tc = hp.temperature_channel, ec = hp.ne_channel;
+    const T LN10 = (T)kLN10;
+    lt = (T)in.lt * (T)hp.std_x[tc] + (T)hp.mean_x[tc];
+    lne = (T)in.lne * (T)hp.std_x[ec] + (T)hp.mean_x[ec];
+    const T tk = mexp10(lt);
+    const T ne = mexp10(lne - (T)6);  // cm^-3
+    conl = (T)ln_ccon() + (lne - (T)6) * LN10 - (T)1.5 * lt * LN10;
+    dxi = (T)(4.98e-4 * 5040.0) / tk * msqrt(ne * (T)kBK * tk);
+    ek_t = (T)(kEE / kBK) / tk;
+  }
+  // the LTE log-weight of level g
+  __device__ __forceinline__ T weight(const ffno_head_params& hp, int g) const {
+    return (T)hp.log_g[g] - ek_t * ((T)hp.ev[g] - dxi * (T)hp.ndxi[g]) - (T)hp.dion[g] * conl;
+  }
+};
+
+// Forward: out[g * V + v] = the normalised log10 population of level g.
+template <typename T>
+__device__ __forceinline__ void head_voxel_fwd(const ffno_head_params& hp, const float* o, const HeadInputs& in,
+                                               float* __restrict__ out, long V, long v) {
+  const Lte<T> e(hp, in);
+  const T LN10 = (T)kLN10;
+  const T lrho = (T)in.lrho * (T)hp.std_x[hp.rho_channel] + (T)hp.mean_x[hp.rho_channel];
+  int hc = 0, lvl = 0;
+  for (int s = 0; s < hp.nspecies; ++s) {
+    const int L = hp.levels[s];
+    T logit[FFNO_MAX_LEVELS];
+    T mx = (T)-1e30;
+    for (int i = 0; i < L; ++i) {
+      logit[i] = (T)o[hc + i] + e.weight(hp, lvl + i);
+      mx = fmax(mx, logit[i]);
+    }
+    float se = 0.f;
+    for (int i = 0; i < L; ++i) se += expf((float)(logit[i] - mx));
+    const T lse = (T)logf(se);
+    const T tb = (T)hp.total_bound;
+    const T base = lrho - (T)hp.log10_particle_mass[s] + tb * mtanh((T)o[hc + L] / tb);
+    for (int i = 0; i < L; ++i) {
+      const int g = lvl + i;
+      const T l10 = base + (logit[i] - mx - lse) / LN10;
+      out[(long)g * V + v] = (float)((l10 - (T)hp.mean_y[g]) / (T)hp.std_y[g]);
+    }
+    hc += L + 1;
+    lvl += L;
+  }
+}
+
+// Backward: with ybar[g * V + v] the cotangent of the normalised output, overwrites o[0..nhp) with the gradient of the
+// head channels (zero past the last species) and writes x_in_bar[k * V + v] for every input channel k.
+template <typename T>
+__device__ __forceinline__ void head_voxel_bwd(const ffno_head_params& hp, float* o, int nhp, const HeadInputs& in,
+                                               const float* __restrict__ ybar, long V, long v,
+                                               float* __restrict__ xinbar) {
+  const Lte<T> e(hp, in);
+  const T LN10 = (T)kLN10;
+  T gsum = 0, ltb = 0, lneb = 0;
+  int hc = 0, lvl = 0;
+  for (int s = 0; s < hp.nspecies; ++s) {
+    const int L = hp.levels[s];
+    T logit[FFNO_MAX_LEVELS], gl[FFNO_MAX_LEVELS];
+    T mx = (T)-1e30;
+    for (int i = 0; i < L; ++i) {
+      logit[i] = (T)o[hc + i] + e.weight(hp, lvl + i);
+      mx = fmax(mx, logit[i]);
+    }
+    T se = 0;
+    for (int i = 0; i < L; ++i) se += mexp(logit[i] - mx);
+    T G = 0;
+    for (int i = 0; i < L; ++i) {
+      gl[i] = (T)__ldg(ybar + (long)(lvl + i) * V + v) / (T)hp.std_y[lvl + i];
+      G += gl[i];
+    }
+    gsum += G;
+    const T tb = (T)hp.total_bound;
+    const T th = mtanh((T)o[hc + L] / tb);
+    const float ubar = (float)(G * ((T)1 - th * th));
+    for (int i = 0; i < L; ++i) {
+      const int g = lvl + i;
+      const T p = mexp(logit[i] - mx) / se;
+      const T lb = (gl[i] - p * G) / LN10;
+      o[hc + i] = (float)lb;
+      ltb += lb * LN10 * (e.ek_t * ((T)hp.ev[g] - (T)1.5 * e.dxi * (T)hp.ndxi[g]) + (T)1.5 * (T)hp.dion[g]);
+      lneb += lb * LN10 * ((T)0.5 * e.ek_t * e.dxi * (T)hp.ndxi[g] - (T)hp.dion[g]);
+    }
+    o[hc + L] = ubar;
+    hc += L + 1;
+    lvl += L;
+  }
+  for (int c = hc; c < nhp; ++c) o[c] = 0.f;
+  const int tc = hp.temperature_channel, ec = hp.ne_channel, rc = hp.rho_channel;
+  for (int k = 0; k < hp.in_channels; ++k) {
+    T val = 0;
+    if (k == tc) val += ltb * (T)hp.std_x[tc];
+    if (k == ec) val += lneb * (T)hp.std_x[ec];
+    if (k == rc) val += gsum * (T)hp.std_x[rc];
+    xinbar[(long)k * V + v] = (float)val;
+  }
+}
+
 // acc[i][j] = sum_k A[(ty + 16 i) * lda + k] * W[k * N + tx + 16 j] for i < RM rows per thread (a tile of 16 RM
 // rows); A in shared memory, W (row-major K x N) in global memory (read through L1; every CTA reads the same small
 // weight matrix).

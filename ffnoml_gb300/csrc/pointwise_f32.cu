@@ -412,15 +412,15 @@ __global__ void __launch_bounds__(NT) k_fuse(const float* __restrict__ x, const 
 template <int C, int NHP, typename T>
 __global__ void __launch_bounds__(NT) k_head(const float* __restrict__ x, const float* __restrict__ xin, long V,
                                              const float* __restrict__ p1, const float* __restrict__ p2,
-                                             const float* __restrict__ b2, int nh, ffno_head_params hp,
-                                             float* __restrict__ out, float* __restrict__ head_out) {
+                                             const float* __restrict__ b2, int nh,
+                                             const __grid_constant__ ffno_head_params hp, float* __restrict__ out,
+                                             float* __restrict__ head_out) {
   extern __shared__ float sm[];
   constexpr int LA = C + 1, LH = 2 * C + 1, LO = NHP + 1;
   float* as = sm;
   float* hs = as + BM * LA;
   float* os = hs + BM * LH;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const T lnc = (T)ln_ccon(), LN10 = (T)kLN10;
   const long nt = ntiles_of(V);
   for (long t = blockIdx.x; t < nt; t += gridDim.x) {
     const long v0 = t * BM;
@@ -452,40 +452,7 @@ __global__ void __launch_bounds__(NT) k_head(const float* __restrict__ x, const 
         const float* o = os + r * LO;
         if (head_out)
           for (int c = 0; c < nh; ++c) head_out[(long)c * V + v] = o[c];
-        const int tc = hp.temperature_channel, ec = hp.ne_channel, rc = hp.rho_channel;
-        const T lt = (T)__ldg(xin + (long)tc * V + v) * (T)hp.std_x[tc] + (T)hp.mean_x[tc];
-        const T lne = (T)__ldg(xin + (long)ec * V + v) * (T)hp.std_x[ec] + (T)hp.mean_x[ec];
-        const T lrho = (T)__ldg(xin + (long)rc * V + v) * (T)hp.std_x[rc] + (T)hp.mean_x[rc];
-        const T tk = mexp10(lt);
-        const T ne = mexp10(lne - (T)6);  // cm^-3
-        const T conl = lnc + (lne - (T)6) * LN10 - (T)1.5 * lt * LN10;
-        const T dxi = (T)(4.98e-4 * 5040.0) / tk * msqrt(ne * (T)kBK * tk);
-        const T ek_t = (T)(kEE / kBK) / tk;
-        int hc = 0, lvl = 0;
-        for (int s = 0; s < hp.nspecies; ++s) {
-          const int L = hp.levels[s];
-          T logit[FFNO_MAX_LEVELS];
-          T mx = (T)-1e30;
-          for (int i = 0; i < L; ++i) {
-            const int g = lvl + i;
-            const T lte = (T)hp.log_g[g] - ek_t * ((T)hp.ev[g] - dxi * (T)hp.ndxi[g]) - (T)hp.dion[g] * conl;
-            logit[i] = (T)o[hc + i] + lte;
-            mx = fmax(mx, logit[i]);
-          }
-          float se = 0.f;
-          for (int i = 0; i < L; ++i) se += expf((float)(logit[i] - mx));
-          const T lse = (T)logf(se);
-          const T tb = (T)hp.total_bound;
-          const T tot = tb * mtanh((T)o[hc + L] / tb);
-          const T base = lrho - (T)hp.log10_particle_mass[s] + tot;
-          for (int i = 0; i < L; ++i) {
-            const int g = lvl + i;
-            const T l10 = base + (logit[i] - mx - lse) / LN10;
-            out[(long)g * V + v] = (float)((l10 - (T)hp.mean_y[g]) / (T)hp.std_y[g]);
-          }
-          hc += L + 1;
-          lvl += L;
-        }
+        head_voxel_fwd<T>(hp, o, head_inputs(hp, xin, V, v), out, V, v);
       }
     }
   }

@@ -1125,6 +1125,163 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
   pipe_finish(P, tslot, 2 * NCOL);
 }
 
+// ============================================================================================== head
+// Level-fraction head (FFNO3D proj1 / proj2 and head_output, models/ffno_model.py:712-713, 729-748): o = gelu(x P1)
+// P2 + b2 per voxel (P1: C -> 2C without bias, P2: 2C -> nh padded with zero rows to NHP), then the voxel's LTE
+// log-softmax (head_voxel_fwd). The first GEMM runs transposed (2C outputs), the second untransposed (lane = voxel);
+// the NHP head channels of a voxel reach the thread that owns it through shared memory, rows [128][NHP + 1] over the
+// pipeline's tile region (the hidden tile has been consumed by then).
+__host__ __device__ constexpr uint32_t head_rows_bytes(int NHP) { return (uint32_t)TM * (NHP + 1) * 4; }
+__host__ __device__ constexpr uint32_t head_obar_at(int NHP) { return (head_rows_bytes(NHP) + 1023u) & ~1023u; }
+__host__ __device__ constexpr uint32_t head_region(int C, int NHP, bool bwd) {
+  const uint32_t need = bwd ? head_obar_at(NHP) + tile_bytes(NHP) : head_rows_bytes(NHP);
+  return tile_bytes(2 * C) > need ? tile_bytes(2 * C) : need;
+}
+
+template <int C, int NHP, typename T>
+__global__ void __launch_bounds__(CT, 1) k_head_tc(const float* __restrict__ x, const float* __restrict__ xin, long V,
+                                                   const uint8_t* __restrict__ wpack, const float* __restrict__ b2,
+                                                   int nh, const __grid_constant__ ffno_head_params hp,
+                                                   float* __restrict__ out, float* __restrict__ head_out,
+                                                   int* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(2 * C, C), B2 = mat_bytes(NHP, 2 * C), RB = head_region(C, NHP, false);
+  constexpr int LO = NHP + 1;
+  PIPE_PROLOGUE(TM, 2)
+  uint8_t* region = smem + B1 + B2 + pid * RB;
+  const Split X = split_at(region, TM, C), H = split_at(region, TM, 2 * C);
+  float* os = reinterpret_cast<float*>(region);
+  P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
+  const Op w1 = wop(smem, 2 * C, C), w2 = wop(smem + B1, NHP, 2 * C);
+  const int f = P.feat();
+  const int pf = c_pf;
+  for (int k = 1; P.ptid == 0 && k < pf; ++k) prefetch_rows(x, (t0 + k * tstep) * TM, V, C);
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    if (P.ptid == 0 && pf > 0) prefetch_rows(x, (t + pf * tstep) * TM, V, C);
+    fill_tile<C>(X, v0, V, P.ptid, [&](long v, int k) { return ld4(x + v * C + k); });
+    if (!pipe_gemms(P, err, Gemm{P.tmem, w1, kop(X, C), C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+      float v[16];
+      tld(P, 0, c, v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = gelu_tc(v[i]);
+      if (f < 2 * C) put_mn(H, f, 64 * P.half + 16 * c, v);
+    }
+    if (!pipe_gemms(P, err, Gemm{P.tmem, mop(H), w2, 2 * C, false, NHP})) break;
+#pragma unroll
+    for (int j = 0; j < NHP / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      float r[16];
+      rld(P, 0, j, r);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) os[f * LO + 16 * j + i] = r[i] + __ldg(b2 + 16 * j + i);
+    }
+    pipe_sync(P.id);
+    const long v = v0 + f;
+    if (P.half == 0 && v < V) {
+      const float* o = os + f * LO;
+      if (head_out)
+        for (int c = 0; c < nh; ++c) head_out[(long)c * V + v] = o[c];
+      head_voxel_fwd<T>(hp, o, head_inputs(hp, xin, V, v), out, V, v);
+    }
+    pipe_sync(P.id);   // the rows are read before the next tile's fill overwrites them
+  }
+  pipe_finish(P, tslot, 2 * NCOL);
+}
+
+// Head backward: the forward recomputed (pre = x P1 kept in tensor memory columns 0..127, o = gelu(pre) P2 + b2 at
+// columns 128.. and then as shared rows), o_bar from head_voxel_bwd (which also writes x_in_bar) as a K-major tile,
+// h_bar = (o_bar P2^T) * gelu'(pre) (transposed, columns 128..255), x_bar = h_bar P1^T (untransposed, columns 0..C-1).
+// Weights: [w1 (2C x C), w2 (NHP x 2C), w2t (2C x NHP), w1t (C x 2C)]. The tile region holds in turn the input tile,
+// the hidden tile, the head rows with the o_bar tile behind them, and the hidden-gradient tile.
+template <int C, int NHP, typename T>
+__global__ void __launch_bounds__(CT, 1) k_head_bwd_tc(const float* __restrict__ x, const float* __restrict__ xin,
+                                                       const float* __restrict__ ybar, long V,
+                                                       const uint8_t* __restrict__ wpack, const float* __restrict__ b2,
+                                                       const __grid_constant__ ffno_head_params hp,
+                                                       float* __restrict__ xbar, float* __restrict__ xinbar,
+                                                       int* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(2 * C, C), B2 = mat_bytes(NHP, 2 * C), RB = head_region(C, NHP, true);
+  constexpr int LO = NHP + 1;
+  PIPE_PROLOGUE(2 * TM, 2)
+  uint8_t* region = smem + 2 * B1 + 2 * B2 + pid * RB;
+  const Split X = split_at(region, TM, C), H = split_at(region, TM, 2 * C),
+              Ob = split_at(region + head_obar_at(NHP), TM, NHP);
+  float* os = reinterpret_cast<float*>(region);
+  P.ok = load_weights(smem, wpack, 2 * B1 + 2 * B2, wcx, err);
+  const Op w1 = wop(smem, 2 * C, C), w2 = wop(smem + B1, NHP, 2 * C), w2t = wop(smem + B1 + B2, 2 * C, NHP),
+           w1t = wop(smem + B1 + 2 * B2, C, 2 * C);
+  const int f = P.feat();
+  const int pf = c_pf;
+  for (int k = 1; P.ptid == 0 && k < pf; ++k) prefetch_rows(x, (t0 + k * tstep) * TM, V, C);
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    if (P.ptid == 0 && pf > 0) prefetch_rows(x, (t + pf * tstep) * TM, V, C);
+    fill_tile<C>(X, v0, V, P.ptid, [&](long v, int k) { return ld4(x + v * C + k); });
+    if (!pipe_gemms(P, err, Gemm{P.tmem, w1, kop(X, C), C, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+      float v[16];
+      tld(P, 0, c, v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = gelu_tc(v[i]);
+      if (f < 2 * C) put_mn(H, f, 64 * P.half + 16 * c, v);
+    }
+    if (!pipe_gemms(P, err, Gemm{P.tmem + TM, mop(H), w2, 2 * C, false, NHP})) break;
+#pragma unroll
+    for (int j = 0; j < NHP / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      float r[16];
+      rld(P, TM, j, r);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) os[f * LO + 16 * j + i] = r[i] + __ldg(b2 + 16 * j + i);
+    }
+    pipe_sync(P.id);
+    if (P.half == 0) {
+      const long v = v0 + f;
+      float* o = os + f * LO;
+      if (v < V) {
+        head_voxel_bwd<T>(hp, o, NHP, head_inputs(hp, xin, V, v), ybar, V, v, xinbar);
+      } else {
+        for (int c = 0; c < NHP; ++c) o[c] = 0.f;
+      }
+#pragma unroll
+      for (int j = 0; j < NHP / 16; ++j) {
+        float r[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) r[i] = o[16 * j + i];
+        put16(Ob, f, 16 * j, NHP, r);
+      }
+    }
+    if (!pipe_gemms(P, err, Gemm{P.tmem + TM, w2t, kop(Ob, NHP), NHP, false})) break;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+      float hp_[16], gb[16];
+      tld(P, 0, c, hp_);
+      tld(P, TM, c, gb);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) gb[i] *= gelu_grad_tc(hp_[i]);
+      if (f < 2 * C) put_mn(H, f, 64 * P.half + 16 * c, gb);
+    }
+    if (!pipe_gemms(P, err, Gemm{P.tmem, mop(H), w1t, 2 * C, false, C})) break;
+    const long v = v0 + f;
+#pragma unroll
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      float r[16];
+      rld(P, 0, j, r);
+      if (v < V)
+#pragma unroll
+        for (int i = 0; i < 16; i += 4)
+          *reinterpret_cast<float4*>(xbar + v * C + 16 * j + i) = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
+    }
+  }
+  pipe_finish(P, tslot, 2 * NCOL);
+}
+
 #undef PIPE_PROLOGUE
 
 int g_sms = 0;
@@ -1317,6 +1474,75 @@ int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const flo
                                                     static_cast<const uint8_t*>(wpack), x_bar, spec_bar, vert_bar,
                                                     err);
   })
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+// head parameters the tensor-core head kernels accept: species and levels within the kernels' fixed arrays, and
+// nh = sum (levels + 1) head channels within nhp
+static bool head_ok(const ffno_head_params* hp, int nh, int nhp) {
+  if (!hp || (nhp != 16 && nhp != 32) || hp->nspecies < 1 || hp->nspecies > FFNO_MAX_SPECIES) return false;
+  if (hp->in_channels < 1 || hp->in_channels > 8) return false;
+  int tot = 0, lv = 0;
+  for (int s = 0; s < hp->nspecies; ++s) {
+    if (hp->levels[s] < 1) return false;
+    tot += hp->levels[s] + 1;
+    lv += hp->levels[s];
+  }
+  const int ch[3] = {hp->temperature_channel, hp->ne_channel, hp->rho_channel};
+  for (int c : ch)
+    if (c < 0 || c >= hp->in_channels) return false;
+  return lv <= FFNO_MAX_LEVELS && tot <= nhp && (nh < 0 || tot == nh);
+}
+
+#define HEAD_DISPATCH(KERNEL, SMEM, ...)                                                     \
+  TC_DISPATCH(C, {                                                                           \
+    if (nhp == 16) {                                                                         \
+      constexpr int NN = 16;                                                                 \
+      if (params->math32) {                                                                  \
+        if (!launch_prep(KERNEL<CC, NN, float>, SMEM)) return FFNO_ELAUNCH;                  \
+        KERNEL<CC, NN, float><<<grid_tc(V), CT, SMEM, s>>>(__VA_ARGS__);                     \
+      } else {                                                                               \
+        if (!launch_prep(KERNEL<CC, NN, double>, SMEM)) return FFNO_ELAUNCH;                 \
+        KERNEL<CC, NN, double><<<grid_tc(V), CT, SMEM, s>>>(__VA_ARGS__);                    \
+      }                                                                                      \
+    } else {                                                                                 \
+      constexpr int NN = 32;                                                                 \
+      if (params->math32) {                                                                  \
+        if (!launch_prep(KERNEL<CC, NN, float>, SMEM)) return FFNO_ELAUNCH;                  \
+        KERNEL<CC, NN, float><<<grid_tc(V), CT, SMEM, s>>>(__VA_ARGS__);                     \
+      } else {                                                                               \
+        if (!launch_prep(KERNEL<CC, NN, double>, SMEM)) return FFNO_ELAUNCH;                 \
+        KERNEL<CC, NN, double><<<grid_tc(V), CT, SMEM, s>>>(__VA_ARGS__);                    \
+      }                                                                                      \
+    }                                                                                        \
+  })
+
+int ffno_head_fwd_tc(const float* x, const float* x_in, long V, int C, const void* wpack, const float* b2, int nh,
+                     int nhp, const ffno_head_params* params, float* out, float* head_out, int* err,
+                     ffno_stream_t stream) {
+  if (!tc_width(C) || V < 1 || !x || !x_in || !b2 || !out || !err || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!head_ok(params, nh, nhp)) return FFNO_EINVAL;
+  const uint8_t* w = static_cast<const uint8_t*>(wpack);
+  cudaStream_t s = (cudaStream_t)stream;
+  HEAD_DISPATCH(k_head_tc,
+                mat_bytes(2 * CC, CC) + mat_bytes(NN, 2 * CC) + 2 * (size_t)head_region(CC, NN, false),
+                x, x_in, V, w, b2, nh, *params, out, head_out, err)
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_head_bwd_tc(const float* x, const float* x_in, const float* y_bar, long V, int C, const void* wpack,
+                     const float* b2, int nhp, const ffno_head_params* params, float* x_bar, float* x_in_bar,
+                     int* err, ffno_stream_t stream) {
+  if (!tc_width(C) || V < 1 || !x || !x_in || !y_bar || !b2 || !x_bar || !x_in_bar || !err || !aligned16(wpack))
+    return FFNO_EINVAL;
+  if (!head_ok(params, -1, nhp)) return FFNO_EINVAL;
+  const uint8_t* w = static_cast<const uint8_t*>(wpack);
+  cudaStream_t s = (cudaStream_t)stream;
+  HEAD_DISPATCH(k_head_bwd_tc,
+                2 * mat_bytes(2 * CC, CC) + 2 * mat_bytes(NN, 2 * CC) + 2 * (size_t)head_region(CC, NN, true),
+                x, x_in, y_bar, V, w, b2, *params, x_bar, x_in_bar, err)
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

@@ -174,6 +174,10 @@ class Packed:
         # rounding there is ~1e-6 dex), the FP32 path in FP64 as the reference does
         self.head32 = nat.HeadParams.from_buffer_copy(self.head)
         self.head32.math32 = 1
+        if self.tc:   # proj1 [2C][C] and proj2 [nhp][2C] for the tensor-core head
+            w1, w2 = _w(model.proj1), p2.t()
+            self.tc_head = tc_pack(device, w1, w2)
+            self.tcb_head = tc_pack(device, w1, w2, w2.t(), w1.t())
         self.freq_params = {k: v.detach().cpu() for k, v in model.state_dict().items() if ".freq_" in k}
         self.freq_key = table_store.freq_key(self.freq_params)
 
@@ -536,7 +540,7 @@ class Executor:
                     inputs.append(ws.x.clone())
                 if cache:
                     blocks.append(wb)
-            self._head(pk, ws.x, xin, out[b])
+            self._head(pk, ws.x, xin, out[b], ws.err)
             if keep:
                 saved.append(inputs)
                 states.append(blocks)
@@ -657,10 +661,6 @@ class Executor:
             nat.call("ffno_spectral_mix", inp.data_ptr(), out.data_ptr(), F, nb, sf, sb, s_im, m.width, w.data_ptr(),
                      g.data_ptr(), _ptr(u), _ptr(v), m.freq_mix_rank, s)
 
-    def _hp(self, pk):
-        """The head's parameters: FP32 LTE math on the split-BF16 path, FP64 on the FP32 path."""
-        return pk.head32 if self._tc() else pk.head
-
     def _tc(self):
         """Whether the split-BF16 tensor-core kernels run (precision 'bf16' at a width they support; never inside a
         JVP, which is FP32)."""
@@ -686,11 +686,16 @@ class Executor:
                  G, s)
         return False
 
-    def _head(self, pk, x, xin, out):
+    def _head(self, pk, x, xin, out, err):
+        """The level-fraction head of one cube (or slab): x [V][C], xin [Cin][V] -> out [L][V]."""
         m = self.model
         V = x.shape[0]
+        if self._tc():
+            nat.call("ffno_head_fwd_tc", x.data_ptr(), xin.data_ptr(), V, m.width, pk.tc_head.data_ptr(),
+                     pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head32, out.data_ptr(), None, err.data_ptr(), _stream())
+            return
         nat.call("ffno_head_fwd", x.data_ptr(), xin.data_ptr(), V, m.width, pk.p1.data_ptr(), pk.p2.data_ptr(),
-                 pk.b2.data_ptr(), pk.nh, pk.nhp, self._hp(pk), out.data_ptr(), None, _stream())
+                 pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head, out.data_ptr(), None, _stream())
 
     # -------------------------------------------------------------------------------------------- JVP
     def jvp(self, x, z_scale, dx, dy, x_dot):
@@ -728,9 +733,9 @@ class Executor:
                     tw.xp.copy_(ws.x)
                     self._block(pk, ws, i, z, D, H, W, hgt_b, pln, pfr[i], x_in=tw.xp)
                     self._block_jvp(pk, ws, tw, i, tw.xp, D, H, W, hgt_b, pln, pfr[i])
-                self._head(pk, ws.x, xin, y[b])
+                self._head(pk, ws.x, xin, y[b], ws.err)
                 nat.call("ffno_head_jvp", ws.x.data_ptr(), tw.x.data_ptr(), xin.data_ptr(), xin_dot.data_ptr(), V, C,
-                         pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.nhp, self._hp(pk),
+                         pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.nhp, pk.head,
                          out[b].data_ptr(), s)
             self._check(ws)
         finally:
@@ -811,6 +816,7 @@ class Executor:
         ybar = ybar.contiguous()
         xbar_in = torch.zeros_like(x)
         zbar = torch.zeros_like(z_scale)
+        tc = self._tc()
         ws = gb = None
         if geo.shared:
             live = hgt["live"]
@@ -831,9 +837,14 @@ class Executor:
             self._depth_weights(ws, z, D, HW)
             gb.wbar.zero_()
             # head
-            nat.call("ffno_head_bwd", inputs[-1].data_ptr(), xin.data_ptr(), ybar[b].data_ptr(), V, C,
-                     pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.p2t.data_ptr(), pk.p1t.data_ptr(),
-                     pk.nhp, self._hp(pk), gb.xbar.data_ptr(), xbar_in[b].data_ptr(), s)
+            if tc:
+                nat.call("ffno_head_bwd_tc", inputs[-1].data_ptr(), xin.data_ptr(), ybar[b].data_ptr(), V, C,
+                         pk.tcb_head.data_ptr(), pk.b2.data_ptr(), pk.nhp, pk.head32, gb.xbar.data_ptr(),
+                         xbar_in[b].data_ptr(), ws.err.data_ptr(), s)
+            else:
+                nat.call("ffno_head_bwd", inputs[-1].data_ptr(), xin.data_ptr(), ybar[b].data_ptr(), V, C,
+                         pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.p2t.data_ptr(), pk.p1t.data_ptr(),
+                         pk.nhp, pk.head, gb.xbar.data_ptr(), xbar_in[b].data_ptr(), s)
             cached = state.get("blocks")
             for i in reversed(range(m.n_layers)):
                 if cached and cached[b][i] is not None:

@@ -268,8 +268,7 @@ class StreamingForward:
             b = ws.buf
             x = slab_inputs(*it)
             y = outs[b].view(-1)[:L * ws.V].view(L, ws.V)      # the head writes [L][Vs] contiguously
-            nat.call("ffno_head_fwd", ws.x.data_ptr(), x.data_ptr(), ws.V, C, pk.p1.data_ptr(), pk.p2.data_ptr(),
-                     pk.b2.data_ptr(), pk.nh, pk.nhp, ex._hp(pk), y.data_ptr(), None, _stream())
+            ex._head(pk, ws.x, x, y, ws.err)
             if log10:   # y std_Y + mean_Y
                 torch.addcmul(norm["mean_Y"][:, None], y, norm["std_Y"][:, None],
                               out=pops[b].view(-1)[:L * ws.V].view(L, ws.V))

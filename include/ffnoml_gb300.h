@@ -320,6 +320,16 @@ int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const flo
                        const float* gates, const float* hg, const float* fused_pre_bar, const float* hf_bar,
                        const float* base, long V, int C, const void* wpack, float* x_bar, float* spec_bar,
                        float* vert_bar, int* err, ffno_stream_t stream);
+/* ffno_head_fwd and ffno_head_bwd (FFNO3D proj1 / proj2 and head_output, models/ffno_model.py:712-713, 729-748) with
+ * the proj1 / proj2 GEMMs on tensor cores; b2 [nhp] (zero past nh); the LTE math in FP32 when params->math32, else
+ * FP64. Forward wpack = [w1 (2C x C), w2 (nhp x 2C)]; backward wpack = [w1, w2, w2^T (2C x nhp), w1^T (C x 2C)],
+ * with w2's rows past nh zero. */
+int ffno_head_fwd_tc(const float* x, const float* x_in, long V, int C, const void* wpack, const float* b2, int nh,
+                     int nhp, const ffno_head_params* params, float* out, float* head_out, int* err,
+                     ffno_stream_t stream);
+int ffno_head_bwd_tc(const float* x, const float* x_in, const float* y_bar, long V, int C, const void* wpack,
+                     const float* b2, int nhp, const ffno_head_params* params, float* x_bar, float* x_in_bar,
+                     int* err, ffno_stream_t stream);
 
 /* ffno_xform on tensor cores (split-BF16), same descriptor; M <= 256, every stride and N multiples of 4 floats.
  * tpack: T [M][K] packed per 128-row m-tile (rows past M zero) and, within it, per 64-wide k-chunk (K padded with

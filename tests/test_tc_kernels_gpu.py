@@ -293,3 +293,46 @@ def test_spectral_mix_tc(C, rank, layout):
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     _close(b, a)
+
+
+@pytest.mark.parametrize("name", ["hca_stretched", "w32_m16", "w64_m32"])
+@pytest.mark.parametrize("math32", [0, 1])
+def test_head_tc(name, math32):
+    """ffno_head_fwd_tc / ffno_head_bwd_tc against the FP32 head kernels (LTE math in FP64) on a golden model's head
+    and normalised inputs, tiled to a ragged voxel count; output compared in log10 n."""
+    from golden_io import load, model_config
+    from ffnoml_gb300 import FFNO3D
+    from ffnoml_gb300.executor import Packed
+    nat = _nat()
+    meta, state, a = load(name)
+    model = FFNO3D(**model_config(meta))
+    model.load_state_dict({k: v.float() for k, v in state.items()}, strict=True)
+    C, L = model.width, model.out_channels
+    pk = Packed(model, torch.device("cuda"))
+    hp = nat.HeadParams.from_buffer_copy(pk.head)
+    hp.math32 = math32
+    xin0 = a["x"][0].reshape(6, -1).float()
+    Vn = 5 * 128 + 77
+    xin = xin0.repeat(1, (Vn + xin0.shape[1] - 1) // xin0.shape[1])[:, :Vn].cuda().contiguous()
+    x, ybar = _rand(Vn, C, seed=11), _rand(L, Vn, seed=12)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = _s()
+    ref, out = torch.empty(L, Vn, device="cuda"), torch.empty(L, Vn, device="cuda")
+    nat.call("ffno_head_fwd", x.data_ptr(), xin.data_ptr(), Vn, C, pk.p1.data_ptr(), pk.p2.data_ptr(),
+             pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head, ref.data_ptr(), None, s)
+    nat.call("ffno_head_fwd_tc", x.data_ptr(), xin.data_ptr(), Vn, C, pk.tc_head.data_ptr(), pk.b2.data_ptr(),
+             pk.nh, pk.nhp, hp, out.data_ptr(), None, err.data_ptr(), s)
+    std_y = model.std_Y.detach().float().cuda()[:, None]
+    dlog = ((out - ref) * std_y).abs().max().item()
+    assert dlog < 1e-4, dlog
+    xb_ref, xib_ref = torch.empty(Vn, C, device="cuda"), torch.empty(6, Vn, device="cuda")
+    xb, xib = torch.empty(Vn, C, device="cuda"), torch.empty(6, Vn, device="cuda")
+    nat.call("ffno_head_bwd", x.data_ptr(), xin.data_ptr(), ybar.data_ptr(), Vn, C, pk.p1.data_ptr(),
+             pk.p2.data_ptr(), pk.b2.data_ptr(), pk.p2t.data_ptr(), pk.p1t.data_ptr(), pk.nhp, pk.head,
+             xb_ref.data_ptr(), xib_ref.data_ptr(), s)
+    nat.call("ffno_head_bwd_tc", x.data_ptr(), xin.data_ptr(), ybar.data_ptr(), Vn, C, pk.tcb_head.data_ptr(),
+             pk.b2.data_ptr(), pk.nhp, hp, xb.data_ptr(), xib.data_ptr(), err.data_ptr(), s)
+    torch.cuda.synchronize()
+    assert err.item() == 0
+    _close(xb, xb_ref, 2e-4)
+    _close(xib, xib_ref, 1e-3 if math32 else 2e-4)
