@@ -686,10 +686,10 @@ class Executor:
                  G, s)
         return False
 
-    def _head(self, pk, x, xin, out, err):
-        """The level-fraction head of one cube (or slab): x [V][C], xin [Cin][V] -> out [L][V]."""
+    def _head(self, pk, x, xin, out, err, V=None):
+        """The level-fraction head of V voxels (default: all rows of x): x [V][C], xin [Cin][V] -> out [L][V]."""
         m = self.model
-        V = x.shape[0]
+        V = x.shape[0] if V is None else V
         if self._tc():
             nat.call("ffno_head_fwd_tc", x.data_ptr(), xin.data_ptr(), V, m.width, pk.tc_head.data_ptr(),
                      pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head32, out.data_ptr(), None, err.data_ptr(), _stream())

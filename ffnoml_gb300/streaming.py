@@ -268,7 +268,7 @@ class StreamingForward:
             b = ws.buf
             x = slab_inputs(*it)
             y = outs[b].view(-1)[:L * ws.V].view(L, ws.V)      # the head writes [L][Vs] contiguously
-            ex._head(pk, ws.x, x, y, ws.err)
+            ex._head(pk, ws.x, x, y, ws.err, ws.V)
             if log10:   # y std_Y + mean_Y
                 torch.addcmul(norm["mean_Y"][:, None], y, norm["std_Y"][:, None],
                               out=pops[b].view(-1)[:L * ws.V].view(L, ws.V))
