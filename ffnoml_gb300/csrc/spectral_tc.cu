@@ -645,6 +645,148 @@ __global__ void __launch_bounds__(XT, 1)
   if (warp == 0) tc::tmem_free(tmem, 512);
 }
 
+// ------------------------------------------------------------------------------------------- A B^T split-K
+// part[split][i][j] = sum over the split's range of n of A[i][n] B[j][n], A [Ma][N] and B [Mb][N] FP32 rows (the
+// gradient of a height-transform table: cotangent rows against transform-input rows, summed over every column and
+// channel). One CTA per split, 512 threads. Per chunk of 64 n, the rows of A (TI tiles of 128, rows past Ma zero) and
+// of B (NB rows, past Mb zero) are loaded from HBM, split into hi / lo K-major tiles and multiplied on the tensor cores
+// into accumulators D_t [128][NB] (tile t at tensor-memory column t NB), which sum over all the split's chunks. With
+// two tile buffers (NS = 2) the loads of chunk c + 1 run while the MMAs of chunk c do; a buffer is refilled after the
+// mbarrier of its previous MMAs. Element (i, j) of a split's product is stored at part[split so + i si + j sj], so a
+// caller can put the longer of its two operands on the M side and store the transpose. Every wait is bounded.
+constexpr int OT = 512;    // threads
+constexpr int OKC = 64;    // n per chunk
+constexpr int OFB = 8;     // loads in flight per thread
+
+__host__ __device__ constexpr uint32_t outer_stage_bytes(int TI, int NB) {
+  return (uint32_t)(TI * 128 + NB) * OKC * 2 * 2;
+}
+
+__global__ void __launch_bounds__(OT, 1) k_outer_tc(const float* __restrict__ A, long lda, int Ma,
+                                                    const float* __restrict__ B, long ldb, int Mb, long N, int TI,
+                                                    int NB, int NS, long cps, float* __restrict__ part, long so,
+                                                    long si, long sj, int* __restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+  __shared__ uint64_t bar[2];
+  __shared__ uint32_t tslot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int RA = TI * 128, R = RA + NB;     // rows of a stage: A's tiles, then B
+  const uint32_t half = (uint32_t)R * OKC * 2, stage = 2 * half;
+  uint32_t ncol = 32;
+  while (ncol < (uint32_t)(TI * NB)) ncol <<= 1;
+  if (warp == 0) tc::tmem_alloc(&tslot, ncol);
+  if (tid == 0) {
+    tc::mbar_init(&bar[0], 1);
+    tc::mbar_init(&bar[1], 1);
+    tc::mbar_init_fence();
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  const uint32_t tmem = tslot;
+  const long nchunks = (N + OKC - 1) / OKC;
+  const long c0 = blockIdx.x * cps, c1 = c0 + cps < nchunks ? c0 + cps : nchunks;
+  const long nmine = c1 > c0 ? c1 - c0 : 0;
+  const int NE = R * (OKC / 4);             // float4 pieces of a stage
+  bool ok = true;
+  long c = 0;
+  for (; c < nmine; ++c) {
+    const uint32_t b = (uint32_t)(c % NS);
+    if (c >= NS && !(ok = bounded(tc::mbar_wait(&bar[b], (uint32_t)((c - NS) / NS) & 1u), err, 5))) break;
+    uint8_t* hi = base + b * stage;
+    uint8_t* lo = hi + half;
+    const long n0 = (c0 + c) * OKC;
+    for (int e0 = tid; e0 < NE; e0 += OT * OFB) {
+      float4 v[OFB];
+#pragma unroll
+      for (int u = 0; u < OFB; ++u) {   // issue the loads before converting any of them
+        // piece e = 4 values at byte e * 8 of the canonical K-major stage (conflict-free 8-byte stores): core matrix
+        // e / 16 (8 rows x 8 k), its row (e / 2) % 8 and k half e % 2; a warp reads 8 rows x 64 bytes
+        const int e = e0 + u * OT;
+        const int cm = e >> 4, r = (cm / (OKC / 8)) * 8 + ((e >> 1) & 7), k = (cm % (OKC / 8)) * 8 + (e & 1) * 4;
+        const long n = n0 + k;
+        v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (e < NE && n < N) {
+          if (r < RA) {
+            if (r < Ma) v[u] = __ldg(reinterpret_cast<const float4*>(A + r * lda + n));
+          } else if (r - RA < Mb) {
+            v[u] = __ldg(reinterpret_cast<const float4*>(B + (r - RA) * ldb + n));
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < OFB; ++u) {
+        const int e = e0 + u * OT;
+        if (e >= NE) break;
+        uint32_t h0, l0, h1, l1;
+        tc::split_pack(v[u].x, v[u].y, h0, l0);
+        tc::split_pack(v[u].z, v[u].w, h1, l1);
+        *reinterpret_cast<uint2*>(hi + (size_t)e * 8) = make_uint2(h0, h1);
+        *reinterpret_cast<uint2*>(lo + (size_t)e * 8) = make_uint2(l0, l1);
+      }
+    }
+    tc::fence_async_smem();
+    tc::tc_before_sync();
+    __syncthreads();
+    tc::tc_after_sync();
+    if (tid == 0) {
+      const uint32_t sh = tc::smem_u32(hi), sl = sh + half;
+      const uint32_t bo = (uint32_t)RA * OKC * 2;   // B's rows follow A's tiles (a multiple of 8 rows)
+      for (int t = 0; t < TI; ++t) {
+        const uint32_t ao = (uint32_t)t * 128u * OKC * 2, d = tmem + (uint32_t)(t * NB);
+        tc::gemm_128xN(d, sh + ao, sh + bo, OKC, NB, c > 0);
+        tc::gemm_128xN(d, sh + ao, sl + bo, OKC, NB, true);
+        tc::gemm_128xN(d, sl + ao, sh + bo, OKC, NB, true);
+      }
+      tc::mma_commit(&bar[b]);
+    }
+  }
+  // the last commit covers every MMA issued before it
+  if (ok && nmine > 0) {
+    const long l = nmine - 1;
+    ok = bounded(tc::mbar_wait(&bar[l % NS], (uint32_t)(l / NS) & 1u), err, 6);
+  }
+  tc::tc_after_sync();
+  if (ok) {
+    const int q = warp & 3, g = warp >> 2;
+    for (int t = 0; t < TI; ++t) {
+      const int i = t * 128 + 32 * q + lane;
+      for (int cc = g; cc < NB / 16; cc += 4) {
+        float v[16];
+        if (nmine > 0) {
+          tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(t * NB + 16 * cc), v);
+        } else {
+#pragma unroll
+          for (int m = 0; m < 16; ++m) v[m] = 0.f;
+        }
+        if (i < Ma) {
+          float* o = part + blockIdx.x * so + i * si;
+#pragma unroll
+          for (int m = 0; m < 16; ++m)
+            if (16 * cc + m < Mb) o[(16 * cc + m) * sj] = v[m];
+        }
+      }
+    }
+  } else if (c > 0) {   // leave no MMA in flight before freeing tensor memory
+    const long l = c - 1;
+    tc::mbar_wait(&bar[l % NS], (uint32_t)(l / NS) & 1u);
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  if (warp == 0) tc::tmem_free(tmem, ncol);
+}
+
+__global__ void k_outer_tc_reduce(const float* __restrict__ part, long nsplit, long n, double* __restrict__ out,
+                                  int accumulate) {
+  const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double s = 0.0;
+  for (long p = 0; p < nsplit; ++p) s += (double)part[p * n + e];
+  out[e] = accumulate ? out[e] + s : s;
+}
+
 int g_sms = 0;
 int sms() {
   if (!g_sms) {
@@ -784,6 +926,36 @@ int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, 
     L(16) L(32) L(64)
 #undef L
   }
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_outer_tc(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, float* part, int nsplit,
+                  double* out, int accumulate, int* err, ffno_stream_t stream) {
+  if (!A || !B || !part || !out || !err || Ma < 1 || Mb < 1 || N < 1 || nsplit < 1) return FFNO_EINVAL;
+  if (N % 4 || lda % 4 || ldb % 4 || lda < N || ldb < N || (reinterpret_cast<uintptr_t>(A) % 16) ||
+      (reinterpret_cast<uintptr_t>(B) % 16))
+    return FFNO_EINVAL;   // float4 loads that never straddle the end of a row
+  const bool trans = Mb > Ma;   // the longer operand on the M side (tiles of 128), the shorter as the MMA's N
+  const int MA = trans ? Mb : Ma, MB = trans ? Ma : Mb;
+  const int TI = (MA + 127) / 128, NB = (MB + 15) / 16 * 16;
+  if (NB > 256 || TI * NB > 512) return FFNO_EINVAL;
+  const size_t limit = 227 * 1024 - 1024;
+  int NS = 2;
+  if (1024 + 2 * (size_t)outer_stage_bytes(TI, NB) > limit) NS = 1;
+  const size_t smem = 1024 + NS * (size_t)outer_stage_bytes(TI, NB);
+  if (smem > limit) return FFNO_EINVAL;
+  if (cudaFuncSetAttribute(k_outer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return FFNO_ELAUNCH;
+  const long nchunks = (N + OKC - 1) / OKC;
+  const long cps = (nchunks + nsplit - 1) / nsplit;
+  const long n = (long)Ma * Mb;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (trans)
+    k_outer_tc<<<nsplit, OT, smem, s>>>(B, ldb, Mb, A, lda, Ma, N, TI, NB, NS, cps, part, n, 1, Mb, err);
+  else
+    k_outer_tc<<<nsplit, OT, smem, s>>>(A, lda, Ma, B, ldb, Mb, N, TI, NB, NS, cps, part, n, Mb, 1, err);
+  k_outer_tc_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(part, nsplit, n, out, accumulate);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

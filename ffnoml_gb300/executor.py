@@ -661,6 +661,15 @@ class Executor:
             nat.call("ffno_spectral_mix", inp.data_ptr(), out.data_ptr(), F, nb, sf, sb, s_im, m.width, w.data_ptr(),
                      g.data_ptr(), _ptr(u), _ptr(v), m.freq_mix_rank, s)
 
+    def _outer(self, ws, a, ma, b, mb, n, part, nsplit, out):
+        """out [ma][mb] += a [ma][n] @ b [mb][n]^T (double): a height-transform table's gradient."""
+        if self._tc() and min(ma, mb) <= 256:
+            nat.call("ffno_outer_tc", a.data_ptr(), n, ma, b.data_ptr(), n, mb, n, part.data_ptr(), nsplit,
+                     out.data_ptr(), 1, ws.err.data_ptr(), _stream())
+        else:
+            nat.call("ffno_outer", a.data_ptr(), n, ma, b.data_ptr(), n, mb, n, part.data_ptr(), nsplit,
+                     out.data_ptr(), 1, _stream())
+
     def _tc(self):
         """Whether the split-BF16 tensor-core kernels run (precision 'bf16' at a width they support; never inside a
         JVP, which is FP32)."""
@@ -958,12 +967,10 @@ class Executor:
             nat.call("ffno_xform_pt", hgt["tzf_t"].data_ptr(), 2 * live * D, ws.vb.data_ptr(), gb.xvb.data_ptr(),
                      d["pci"], 0, s)
         else:
-            nat.call("ffno_outer", gb.yvb.data_ptr(), N, D, ws.vb.data_ptr(), N, 2 * live, N, gb.opart.data_ptr(),
-                     gb.osplit_i, tzi_bar.data_ptr(), 1, s)
+            self._outer(ws, gb.yvb, D, ws.vb, 2 * live, N, gb.opart, gb.osplit_i, tzi_bar)
             self._xf(hgt, "tzi_t", gb.yvb, ws.va, d["zf"], ws)
             self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, True)
-            nat.call("ffno_outer", ws.vb.data_ptr(), N, 2 * live, ws.xv.data_ptr(), N, D, N, gb.opart.data_ptr(),
-                     gb.osplit_f, tzf_bar.data_ptr(), 1, s)
+            self._outer(ws, ws.vb, 2 * live, ws.xv, D, N, gb.opart, gb.osplit_f, tzf_bar)
             self._xf(hgt, "tzf_t", ws.vb, gb.xvb, d["zi"], ws)
         # input gates (and z_proj)
         if tc:

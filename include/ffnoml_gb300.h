@@ -349,6 +349,11 @@ int ffno_xform_tcr(const void* tpack, int Mp, int Kp, const float* in, float* ou
 int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, long sb, long s_im, int C,
                          const void* wpack, const float* g, const float* U, const float* Vm, int rank, int* err,
                          ffno_stream_t stream);
+/* ffno_outer with the products on tensor cores (split-BF16, FP32 accumulation per split; the splits reduced in double
+ * in a fixed order). Same part / nsplit contract (ffno_outer_parts); additionally N a multiple of 4 and lda, ldb >= N;
+ * the shorter of Ma, Mb at most 256. */
+int ffno_outer_tc(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, float* part, int nsplit,
+                  double* out, int accumulate, int* err, ffno_stream_t stream);
 
 /* ---- forward-mode derivative (JVP): jvp_local (ffno_fsdp_runtime.py:350-372), the tangent of FFNO3D.forward along
  * an input tangent with the heights fixed. The linear stages reuse the forward entry points on the tangent (the lift

@@ -336,3 +336,26 @@ def test_head_tc(name, math32):
     assert err.item() == 0
     _close(xb, xb_ref, 2e-4)
     _close(xib, xib_ref, 1e-3 if math32 else 2e-4)
+
+
+@pytest.mark.parametrize("Ma,Mb,N,nsplit", [(12, 8, 1000, 3), (256, 64, 65536 + 196, 152), (64, 256, 65536 + 196, 152),
+                                           (300, 40, 8192, 7), (496, 64, 4096, 5), (16, 16, 256, 9)])
+def test_outer_tc(Ma, Mb, N, nsplit):
+    """ffno_outer_tc against a float64 product and against ffno_outer: tile counts 1-4 (one stage at 4), the longer
+    operand on either side, ragged rows and chunks, and more splits than chunks (splits with no work)."""
+    nat = _nat()
+    A, B = _rand(Ma, N, seed=21), _rand(Mb, N, seed=22)
+    ref = A.double() @ B.double().t()
+    part = torch.empty(nsplit * Ma * Mb, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    out = torch.full((Ma, Mb), 0.5, dtype=torch.float64, device="cuda")
+    nat.call("ffno_outer_tc", A.data_ptr(), N, Ma, B.data_ptr(), N, Mb, N, part.data_ptr(), nsplit, out.data_ptr(),
+             1, err.data_ptr(), _s())
+    out32 = torch.empty(Ma, Mb, dtype=torch.float64, device="cuda")
+    part32 = torch.empty(nat.lib().ffno_outer_parts(Ma, Mb, N) * Ma * Mb, device="cuda")
+    nat.call("ffno_outer", A.data_ptr(), N, Ma, B.data_ptr(), N, Mb, N, part32.data_ptr(),
+             nat.lib().ffno_outer_parts(Ma, Mb, N), out32.data_ptr(), 0, _s())
+    torch.cuda.synchronize()
+    assert err.item() == 0
+    _close(out - 0.5, ref, 2e-5)
+    _close(out32, ref, 2e-5)
