@@ -37,6 +37,12 @@ bool smem_attr(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess;
 }
 
+// the same for kernels whose static shared memory would push dynamic + static past the 48 KB default
+template <typename K>
+bool smem_attr_always(K kernel, size_t bytes) {
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess;
+}
+
 bool width_ok(int C) { return C == 16 || C == 32 || C == 64 || C == 96; }
 
 __device__ __forceinline__ float upstream(int mode, float u, float r, float y) {
@@ -1051,7 +1057,7 @@ int ffno_gn_bwd_stats_bulk(int mode, const float* u, float r, const float* pre, 
   switch (C) {
 #define L(CC)                                                                                                 \
   case CC:                                                                                                    \
-    if (!smem_attr(k_gn_bwd_stats_bulk<CC>, GnBulk<CC>::smem())) return FFNO_ELAUNCH;                        \
+    if (!smem_attr_always(k_gn_bwd_stats_bulk<CC>, GnBulk<CC>::smem())) return FFNO_ELAUNCH;                        \
     k_gn_bwd_stats_bulk<CC><<<nparts, 256, GnBulk<CC>::smem(), s>>>(mode, u, r, pre, gamma, beta, gstats, V, \
                                                                       partials, cpg, groups, err);           \
     break;
@@ -1076,7 +1082,7 @@ int ffno_gn_bwd_apply_bulk(int mode, const float* u, float r, const float* pre, 
 #define L(CC)                                                                                                  \
   case CC: {                                                                                                   \
     const int blocks = grid_of(V, GnBulk<CC>::TV, 2);                                                          \
-    if (!smem_attr(k_gn_bwd_apply_bulk<CC>, GnBulk<CC>::smem())) return FFNO_ELAUNCH;                         \
+    if (!smem_attr_always(k_gn_bwd_apply_bulk<CC>, GnBulk<CC>::smem())) return FFNO_ELAUNCH;                         \
     k_gn_bwd_apply_bulk<CC><<<blocks, 256, GnBulk<CC>::smem(), s>>>(mode, u, r, pre, gamma, beta, gstats, sums, \
                                                                       dw, V, pre_bar, w_bar, cpg, groups, eps, err); \
     break;                                                                                                     \
