@@ -71,8 +71,6 @@ PROTOTYPES = {
     "ffno_gn_bwd_stats": [I, P, F, P, P, P, P, L, I, I, P, I, P],
     "ffno_gn_bwd_final": [P, I, I, P, P],
     "ffno_gn_bwd_apply": [I, P, F, P, P, P, P, P, P, L, I, I, F, P, P, P],
-    "ffno_gn_bwd_stats_bulk": [I, P, F, P, P, P, P, L, I, I, P, I, P, P],
-    "ffno_gn_bwd_apply_bulk": [I, P, F, P, P, P, P, P, P, L, I, I, F, P, P, P, P],
     "ffno_mlp2_bwd": [P, P, P, L, I, P, P, P, P, P],
     "ffno_fuse_bwd": [P, P, P, P, P, P, P, L, I, P, P, P, P, P, P, P, P, P, P, P, P],
     "ffno_gate_bwd": [P, P, P, P, L, I, P, P, P, P, P, P, P, P, P, P, P, P],

@@ -6,7 +6,6 @@
 #include <mutex>
 
 #include "common.cuh"
-#include "tc.cuh"
 
 using namespace ffno;
 
@@ -34,12 +33,6 @@ int grid_of(long V, int rows, int per_sm) {
 template <typename K>
 bool smem_attr(K kernel, size_t bytes) {
   if (bytes <= 48 * 1024) return true;
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess;
-}
-
-// the same for kernels whose static shared memory would push dynamic + static past the 48 KB default
-template <typename K>
-bool smem_attr_always(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess;
 }
 
@@ -252,238 +245,6 @@ __global__ void __launch_bounds__(256) k_gn_bwd_apply(int mode, const float* __r
     }
     if (ok && q == 0) w_bar[v] += wc;
   }
-}
-
-// ------------------------------------------------------------------------------------------- GN backward, bulk
-// The two GroupNorm-backward kernels with their u and pre rows streamed by bulk asynchronous copies: a CTA takes the
-// tiles t = blockIdx.x + k gridDim.x of GTV voxels (contiguous [GTV][C] rows in HBM), and one thread keeps GSTG tiles
-// of both tensors in flight in a shared-memory ring (mbarrier completion), so a CTA has 2 GSTG GTV C 4 bytes of loads
-// outstanding without holding them in registers. Same arithmetic per element as k_gn_bwd_stats / k_gn_bwd_apply.
-// Thread layout: lane slot q = tid % (C/4) serves channels 4q..4q+3 (fixed groups), slot tid / (C/4) the voxels
-// slot, slot + VP, ... of each tile (VP = 256 / (C/4) voxels per pass; the remaining threads idle).
-template <int C>
-struct GnBulk {
-  static constexpr int Q = C / 4;
-  static constexpr int VP = 256 / Q;
-  static constexpr int TV = C <= 64 ? 64 : 32;    // voxels per tile
-  static constexpr int STG = 3;                   // tiles in flight per CTA
-  static constexpr uint32_t TB = (uint32_t)TV * C * 4;   // bytes of one tensor's tile
-  static constexpr size_t smem() { return (size_t)STG * 2 * TB; }
-};
-
-__device__ __forceinline__ bool gn_bounded(bool ok, int* err, int code) {
-  const bool all = __syncthreads_and(ok) != 0;
-  if (!all && threadIdx.x == 0) atomicExch(err, code);
-  return all;
-}
-
-// Issue the bulk copies of tile t (its nv voxels) of u and pre into ring stage s.
-template <int C>
-__device__ __forceinline__ void gn_issue(float* ring, uint64_t* full, int s, long t, long V, const float* u,
-                                         const float* pre) {
-  using B = GnBulk<C>;
-  const long v0 = t * B::TV;
-  const long nv = V - v0 < B::TV ? V - v0 : B::TV;
-  const uint32_t bytes = (uint32_t)nv * C * 4;
-  float* st = ring + (size_t)s * 2 * B::TV * C;
-  tc::mbar_arrive_expect_tx(&full[s], 2 * bytes);
-  tc::bulk_g2s(st, u + v0 * C, bytes, &full[s]);
-  tc::bulk_g2s(st + B::TV * C, pre + v0 * C, bytes, &full[s]);
-}
-
-// After a wait ran out at tile i: wait (bounded) for the copies of tiles i .. i + STG - 1 still in flight, so that no
-// bulk copy lands in the shared memory of a finished CTA.
-template <int C>
-__device__ __forceinline__ void gn_drain(uint64_t* full, long i, long mine) {
-  using B = GnBulk<C>;
-  for (long j = i; j < mine && j < i + B::STG; ++j) tc::mbar_wait(&full[j % B::STG], (uint32_t)(j / B::STG) & 1u);
-}
-
-template <int C>
-__global__ void __launch_bounds__(256) k_gn_bwd_stats_bulk(int mode, const float* __restrict__ u, float r,
-                                                           const float* __restrict__ pre,
-                                                           const float* __restrict__ gamma,
-                                                           const float* __restrict__ beta,
-                                                           const double* __restrict__ gst, long V,
-                                                           double* __restrict__ partials, int cpg, int groups,
-                                                           int* __restrict__ err) {
-  using B = GnBulk<C>;
-  extern __shared__ __align__(128) float ring[];
-  __shared__ uint64_t full[B::STG];
-  __shared__ GnConst k;
-  __shared__ double red[8][GMAX][2];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) {
-    for (int s = 0; s < B::STG; ++s) tc::mbar_init(&full[s], 1);
-    tc::mbar_init_fence();
-  }
-  load_gn_const(k, gst, nullptr, groups, 0.f);   // ends with __syncthreads
-  const long nt = (V + B::TV - 1) / B::TV;
-  const long mine = nt > blockIdx.x ? (nt - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  if (tid == 0)
-    for (long i = 0; i < B::STG && i < mine; ++i) gn_issue<C>(ring, full, (int)i, blockIdx.x + i * gridDim.x, V, u, pre);
-  const int q = tid % B::Q, slot = tid / B::Q;
-  const bool active = slot < B::VP;
-  const int c = 4 * q;
-  float gm[4], bt[4];
-  int grp[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    gm[j] = active ? __ldg(gamma + c + j) : 0.f;
-    bt[j] = active ? __ldg(beta + c + j) : 0.f;
-    grp[j] = (c + j) / cpg;
-  }
-  double d1[4] = {0, 0, 0, 0}, d2[4] = {0, 0, 0, 0};
-  bool ok = true;
-  long i = 0;
-  for (; i < mine; ++i) {
-    const int s = (int)(i % B::STG);
-    if (!(ok = gn_bounded(tc::mbar_wait(&full[s], (uint32_t)(i / B::STG) & 1u), err, 1))) break;
-    const long t = blockIdx.x + i * gridDim.x;
-    const int nv = (int)(V - t * B::TV < B::TV ? V - t * B::TV : B::TV);
-    const float* su = ring + (size_t)s * 2 * B::TV * C;
-    const float* sp = su + B::TV * C;
-    float f1[4] = {0, 0, 0, 0}, f2[4] = {0, 0, 0, 0};
-    if (active)
-      for (int vl = slot; vl < nv; vl += B::VP) {
-        const float4 pu = *reinterpret_cast<const float4*>(su + vl * C + c);
-        const float4 pp = *reinterpret_cast<const float4*>(sp + vl * C + c);
-        const float uu[4] = {pu.x, pu.y, pu.z, pu.w}, xx[4] = {pp.x, pp.y, pp.z, pp.w};
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int g = grp[j];
-          const float xh = (xx[j] - k.mean[g]) * k.rstd[g];
-          const float gh = upstream(mode, uu[j], r, xh * gm[j] + bt[j]) * gm[j];
-          f1[j] += gh;
-          f2[j] += gh * xh;
-        }
-      }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      d1[j] += f1[j];
-      d2[j] += f2[j];
-    }
-    __syncthreads();   // every thread has read stage s
-    if (tid == 0 && i + B::STG < mine) gn_issue<C>(ring, full, s, t + (long)B::STG * gridDim.x, V, u, pre);
-  }
-  if (!ok && tid == 0) gn_drain<C>(full, i, mine);
-  for (int g = 0; g < groups; ++g) {
-    double a = 0.0, b = 0.0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      if (active && grp[j] == g) {
-        a += d1[j];
-        b += d2[j];
-      }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      a += __shfl_xor_sync(0xffffffffu, a, o);
-      b += __shfl_xor_sync(0xffffffffu, b, o);
-    }
-    if (lane == 0) {
-      red[warp][g][0] = a;
-      red[warp][g][1] = b;
-    }
-  }
-  __syncthreads();
-  if (tid < groups) {
-    double a = 0.0, b = 0.0;
-    for (int w = 0; w < 8; ++w) {
-      a += red[w][tid][0];
-      b += red[w][tid][1];
-    }
-    partials[((long)blockIdx.x * groups + tid) * 2] = a;
-    partials[((long)blockIdx.x * groups + tid) * 2 + 1] = b;
-  }
-}
-
-template <int C>
-__global__ void __launch_bounds__(256) k_gn_bwd_apply_bulk(int mode, const float* __restrict__ u, float r,
-                                                           const float* __restrict__ pre,
-                                                           const float* __restrict__ gamma,
-                                                           const float* __restrict__ beta,
-                                                           const double* __restrict__ gst,
-                                                           const double* __restrict__ sums,
-                                                           const float* __restrict__ dw, long V,
-                                                           float* __restrict__ pre_bar, float* __restrict__ w_bar,
-                                                           int cpg, int groups, float eps, int* __restrict__ err) {
-  using B = GnBulk<C>;
-  extern __shared__ __align__(128) float ring[];
-  __shared__ uint64_t full[B::STG];
-  __shared__ GnConst k;
-  __shared__ float wsum[256];
-  const int tid = threadIdx.x;
-  if (tid == 0) {
-    for (int s = 0; s < B::STG; ++s) tc::mbar_init(&full[s], 1);
-    tc::mbar_init_fence();
-  }
-  load_gn_const(k, gst, sums, groups, eps);   // ends with __syncthreads
-  const long nt = (V + B::TV - 1) / B::TV;
-  const long mine = nt > blockIdx.x ? (nt - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  if (tid == 0)
-    for (long i = 0; i < B::STG && i < mine; ++i) gn_issue<C>(ring, full, (int)i, blockIdx.x + i * gridDim.x, V, u, pre);
-  const int q = tid % B::Q, slot = tid / B::Q;
-  const bool active = slot < B::VP;
-  const int c = 4 * q;
-  float gm[4], bt[4];
-  int grp[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    gm[j] = active ? __ldg(gamma + c + j) : 0.f;
-    bt[j] = active ? __ldg(beta + c + j) : 0.f;
-    grp[j] = (c + j) / cpg;
-  }
-  bool ok = true;
-  long i = 0;
-  for (; i < mine; ++i) {
-    const int s = (int)(i % B::STG);
-    if (!(ok = gn_bounded(tc::mbar_wait(&full[s], (uint32_t)(i / B::STG) & 1u), err, 1))) break;
-    const long t = blockIdx.x + i * gridDim.x, v0 = t * B::TV;
-    const int nv = (int)(V - v0 < B::TV ? V - v0 : B::TV);
-    const float* su = ring + (size_t)s * 2 * B::TV * C;
-    const float* sp = su + B::TV * C;
-    for (int vb = 0; vb < nv; vb += B::VP) {   // block-uniform passes of VP voxels
-      const int vl = vb + slot;
-      const bool live = active && vl < nv;
-      float wc = 0.f;
-      if (live) {
-        const long v = v0 + vl;
-        const float wv = __ldg(dw + v);
-        const float4 pu = *reinterpret_cast<const float4*>(su + vl * C + c);
-        const float4 pp = *reinterpret_cast<const float4*>(sp + vl * C + c);
-        const float uu[4] = {pu.x, pu.y, pu.z, pu.w}, xx[4] = {pp.x, pp.y, pp.z, pp.w};
-        float o[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int g = grp[j];
-          const float xh = (xx[j] - k.mean[g]) * k.rstd[g];
-          const float gh = upstream(mode, uu[j], r, xh * gm[j] + bt[j]) * gm[j];
-          o[j] = k.rstd[g] * (gh - wv * k.invT[g] * (k.s1[g] + xh * k.s2[g]));
-          wc += k.invT[g] * (-k.s1[g] * xh - 0.5f * k.s2[g] * (xh * xh - k.vr2[g]));
-        }
-        *reinterpret_cast<float4*>(pre_bar + v * C + c) = make_float4(o[0], o[1], o[2], o[3]);
-      }
-      // the voxel's Q channel slots are consecutive threads: a shuffle tree inside the warp when Q divides 32, else
-      // a sum over shared memory (both in a fixed order)
-      if constexpr (32 % B::Q == 0) {
-#pragma unroll
-        for (int off = B::Q / 2; off; off >>= 1) wc += __shfl_xor_sync(0xffffffffu, wc, off);
-        if (live && q == 0) w_bar[v0 + vl] += wc;
-      } else {
-        wsum[tid] = wc;
-        __syncthreads();
-        if (live && q == 0) {
-          float w = 0.f;
-          for (int e = 0; e < B::Q; ++e) w += wsum[tid + e];
-          w_bar[v0 + vl] += w;
-        }
-        __syncthreads();
-      }
-    }
-    __syncthreads();   // every thread has read stage s
-    if (tid == 0 && i + B::STG < mine) gn_issue<C>(ring, full, s, t + (long)B::STG * gridDim.x, V, u, pre);
-  }
-  if (!ok && tid == 0) gn_drain<C>(full, i, mine);
 }
 
 // ------------------------------------------------------------------------------------------------ MLP backward
@@ -1040,53 +801,6 @@ int ffno_gn_bwd_stats(int mode, const float* u, float r, const float* pre, const
   const int cpg = C / groups;
   switch (C) {
 #define L(CC) case CC: k_gn_bwd_stats<CC><<<nparts, 256, 0, s>>>(mode, u, r, pre, gamma, beta, gstats, V, partials, cpg, groups); break;
-    L(16) L(32) L(64) L(96)
-#undef L
-  }
-  FFNO_CHECK_LAUNCH();
-  return FFNO_OK;
-}
-
-int ffno_gn_bwd_stats_bulk(int mode, const float* u, float r, const float* pre, const float* gamma,
-                           const float* beta, const double* gstats, long V, int C, int groups, double* partials,
-                           int nparts, int* err, ffno_stream_t stream) {
-  if (!width_ok(C) || V < 1 || groups < 1 || groups > GMAX || C % groups || nparts < 1 || !err) return FFNO_EINVAL;
-  if ((reinterpret_cast<uintptr_t>(u) % 16) || (reinterpret_cast<uintptr_t>(pre) % 16)) return FFNO_EINVAL;
-  cudaStream_t s = (cudaStream_t)stream;
-  const int cpg = C / groups;
-  switch (C) {
-#define L(CC)                                                                                                 \
-  case CC:                                                                                                    \
-    if (!smem_attr_always(k_gn_bwd_stats_bulk<CC>, GnBulk<CC>::smem())) return FFNO_ELAUNCH;                        \
-    k_gn_bwd_stats_bulk<CC><<<nparts, 256, GnBulk<CC>::smem(), s>>>(mode, u, r, pre, gamma, beta, gstats, V, \
-                                                                      partials, cpg, groups, err);           \
-    break;
-    L(16) L(32) L(64) L(96)
-#undef L
-  }
-  FFNO_CHECK_LAUNCH();
-  return FFNO_OK;
-}
-
-int ffno_gn_bwd_apply_bulk(int mode, const float* u, float r, const float* pre, const float* gamma,
-                           const float* beta, const double* gstats, const double* sums, const float* dw, long V,
-                           int C, int groups, float eps, float* pre_bar, float* w_bar, int* err,
-                           ffno_stream_t stream) {
-  if (!width_ok(C) || V < 1 || groups < 1 || groups > GMAX || C % groups || !err) return FFNO_EINVAL;
-  if ((reinterpret_cast<uintptr_t>(u) % 16) || (reinterpret_cast<uintptr_t>(pre) % 16) ||
-      (reinterpret_cast<uintptr_t>(pre_bar) % 16))
-    return FFNO_EINVAL;
-  cudaStream_t s = (cudaStream_t)stream;
-  const int cpg = C / groups;
-  switch (C) {
-#define L(CC)                                                                                                  \
-  case CC: {                                                                                                   \
-    const int blocks = grid_of(V, GnBulk<CC>::TV, 2);                                                          \
-    if (!smem_attr_always(k_gn_bwd_apply_bulk<CC>, GnBulk<CC>::smem())) return FFNO_ELAUNCH;                         \
-    k_gn_bwd_apply_bulk<CC><<<blocks, 256, GnBulk<CC>::smem(), s>>>(mode, u, r, pre, gamma, beta, gstats, sums, \
-                                                                      dw, V, pre_bar, w_bar, cpg, groups, eps, err); \
-    break;                                                                                                     \
-  }
     L(16) L(32) L(64) L(96)
 #undef L
   }

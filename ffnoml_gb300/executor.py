@@ -887,13 +887,12 @@ class Executor:
         m = self.model
         C, V, s = m.width, ws.V, _stream()
         G = self._packed.groups
-        nat.call("ffno_gn_bwd_stats_bulk", mode, u.data_ptr(), r, pre.data_ptr(), gamma.data_ptr(),
-                 beta.data_ptr(), ws.gstats[name].data_ptr(), V, C, G, gb.bpart.data_ptr(), ws.nparts,
-                 ws.err.data_ptr(), s)
+        nat.call("ffno_gn_bwd_stats", mode, u.data_ptr(), r, pre.data_ptr(), gamma.data_ptr(), beta.data_ptr(),
+                 ws.gstats[name].data_ptr(), V, C, G, gb.bpart.data_ptr(), ws.nparts, s)
         nat.call("ffno_gn_bwd_final", gb.bpart.data_ptr(), ws.nparts, G, gb.sums.data_ptr(), s)
-        nat.call("ffno_gn_bwd_apply_bulk", mode, u.data_ptr(), r, pre.data_ptr(), gamma.data_ptr(),
-                 beta.data_ptr(), ws.gstats[name].data_ptr(), gb.sums.data_ptr(), ws.dw.data_ptr(), V, C, G, EPS,
-                 pbar.data_ptr(), gb.wbar.data_ptr(), ws.err.data_ptr(), s)
+        nat.call("ffno_gn_bwd_apply", mode, u.data_ptr(), r, pre.data_ptr(), gamma.data_ptr(), beta.data_ptr(),
+                 ws.gstats[name].data_ptr(), gb.sums.data_ptr(), ws.dw.data_ptr(), V, C, G, EPS, pbar.data_ptr(),
+                 gb.wbar.data_ptr(), s)
 
     def _block_bwd(self, pk, ws, gb, i, x, z, zbar, D, H, W, hgt, pln, fq, tzf_bar, tzi_bar):
         """gb.xbar (gradient of the block output) -> gb.xbar (gradient of the block input x); accumulates the

@@ -170,16 +170,6 @@ int ffno_gn_bwd_final(const double* partials, int nparts, int groups, double* su
 int ffno_gn_bwd_apply(int mode, const float* u, float r, const float* pre, const float* gamma, const float* beta,
                       const double* gstats, const double* sums, const float* dw, long V, int C, int groups, float eps,
                       float* pre_bar, float* w_bar, ffno_stream_t stream);
-/* ffno_gn_bwd_stats / ffno_gn_bwd_apply with u and pre streamed into shared memory by bulk asynchronous copies (the
- * same results up to the order of the float partial sums); u, pre and pre_bar 16-byte aligned; err as for the
- * tensor-core kernels (set if a bounded wait ran out). */
-int ffno_gn_bwd_stats_bulk(int mode, const float* u, float r, const float* pre, const float* gamma,
-                           const float* beta, const double* gstats, long V, int C, int groups, double* partials,
-                           int nparts, int* err, ffno_stream_t stream);
-int ffno_gn_bwd_apply_bulk(int mode, const float* u, float r, const float* pre, const float* gamma,
-                           const float* beta, const double* gstats, const double* sums, const float* dw, long V,
-                           int C, int groups, float eps, float* pre_bar, float* w_bar, int* err,
-                           ffno_stream_t stream);
 
 /* Backward of pre = gelu(a @ w1) @ w2 (the C -> 2C -> C MLPs): a_bar = base + ((pre_bar @ w2t) * gelu'(a @ w1)) @ w1t,
  * recomputing a @ w1; w2t [C][2C], w1t [2C][C] are the transposed weights; base may be NULL. */
