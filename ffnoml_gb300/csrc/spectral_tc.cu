@@ -16,7 +16,7 @@ using namespace ffno;
 
 namespace {
 
-constexpr int XT = 256;    // threads of the mixing kernel
+constexpr int XT = 512;    // threads of the mixing kernel
 constexpr int XKC = 64;    // k per chunk of the streamed table pack
 constexpr int XMT = 2;     // max m tiles of 128 (a transform call has at most 256 output rows)
 
@@ -399,10 +399,10 @@ __global__ void __launch_bounds__(RT, 1)
 //   * MMAs: D^T [2C (padded to 128) x 128 b] = W X^T (W resident in shared memory as the A operand) and the low-rank
 //     projections T [128 b x 16] = X Vblk^T, into double-buffered tensor memory, so the epilogue of item i-1 runs
 //     while the MMAs of item i do.
-//   * Epilogue: thread = output channel p (TMEM lane; lanes < C hold re, lanes C..2C-1 im of the same channels),
-//     columns = rows b. The re and im lanes of a channel swap their values through shared memory (a shuffle when
-//     C = 16) to apply g_f; y = g_f D + sum_r U_f[p][r] t[b][r]; one warp's stores cover 32 consecutive channels of
-//     one row.
+//   * Epilogue: thread = output slot p (TMEM lane). W's output rows are packed so that warp quadrant q holds the re
+//     parts of channels 16q..16q+15 (lanes 0-15) and their im parts (lanes 16-31): the re and im lanes of a channel
+//     swap their values with one shuffle to apply g_f; y = g_f D + sum_r U_f[c][r] t[b][r]; 16 warps, each over 32
+//     rows b of its lane quadrant; one warp's stores cover 16 consecutive channels of the re and of the im part.
 constexpr int MIX_RANK_TC = 8;   // low-rank terms carried by the tensor-core mixing (larger ranks use k_mix)
 
 struct MixGeom {
@@ -410,7 +410,6 @@ struct MixGeom {
   int o1, o2, o3;      // logical dimension (0 f, 1 b, 2 re/im) of tensor-map dimensions 1..3
 };
 
-__device__ __forceinline__ void pair_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
 
 template <int C>
 __global__ void __launch_bounds__(XT, 1)
@@ -427,7 +426,6 @@ __global__ void __launch_bounds__(XT, 1)
   constexpr uint32_t WB = 128u * K2 * 2;    // one split half (hi or lo) of a 128-row operand
   constexpr uint32_t WP = (uint32_t)K2 * K2 * 2;   // one split half of the packed [2C][2C] weight
   constexpr int NT = 16;                    // low-rank operand rows
-  constexpr int PW = C / 32;                // warp distance between the re and im lanes of a channel (0: same warp)
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
   uint8_t* sW = base;                  // hi [0, WB), lo [WB, 2 WB)
@@ -435,7 +433,6 @@ __global__ void __launch_bounds__(XT, 1)
   uint8_t* sS = base + 4 * WB;         // staging, 1024-byte aligned (WB is a multiple of 1024)
   uint8_t* sV = sS + NH * HALF;        // hi [NT][K2], lo after
   float* sT = reinterpret_cast<float*>(sV + 2u * NT * K2 * 2);   // [128 b][16], 16-byte chunks swizzled by b
-  float4* sE = reinterpret_cast<float4*>(sT + 128 * 16);          // exchange: [8 warps][4][32 lanes] float4
   __shared__ uint64_t bar_w, bar_s, bar_m[2];
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, q = warp & 3, wg = warp >> 2;
@@ -481,10 +478,9 @@ __global__ void __launch_bounds__(XT, 1)
   float ucur[MIX_RANK_TC], uprev[MIX_RANK_TC];
   long pf = 0, pb0 = 0;
   float pgr = 0.f, pgi = 0.f;
-  const int p = 32 * q + lane;            // output channel slot of this thread in the epilogue
+  const int p = 32 * q + lane;            // output slot of this thread in the epilogue (its TMEM lane)
   const bool live = p < 2 * C;
-  const int part = p >= C ? 1 : 0, pc = p - part * C;
-  const int pair_id = 1 + 2 * wg + (PW ? q % PW : 0);
+  const int part = lane >> 4, pc = 16 * q + (lane & 15);   // re / im part and channel of slot p
 
   auto epilogue = [&](uint32_t buf, long f, long b0, float gr, float gi) {
     if (rank) {
@@ -500,31 +496,14 @@ __global__ void __launch_bounds__(XT, 1)
       __syncthreads();
     }
     float* ob = out + f * sf + part * s_im + pc;
-    const float ga = part ? gr : gr, gb = part ? gi : -gi;   // y = ga * own + gb * partner
+    const float ga = gr, gb = part ? gi : -gi;   // y = ga * own + gb * partner
 #pragma unroll 1
-    for (int cch = 0; cch < 4; ++cch) {
-      const int col = 64 * wg + 16 * cch;
+    for (int cch = 0; cch < 2; ++cch) {
+      const int col = 32 * wg + 16 * cch;
       float v[16], w[16];
       tc::tmem_ld16(tmem + lq + buf * 128u + (uint32_t)col, v);
-      if (PW == 0) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) w[i] = __shfl_xor_sync(0xffffffffu, v[i], 16);
-      } else if (live) {
-        float4* mine = sE + warp * 128;
-        const float4* theirs = sE + (part ? warp - PW : warp + PW) * 128;
-#pragma unroll
-        for (int m = 0; m < 4; ++m) mine[m * 32 + lane] = make_float4(v[4 * m], v[4 * m + 1], v[4 * m + 2], v[4 * m + 3]);
-        pair_sync(pair_id);
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          const float4 t4 = theirs[m * 32 + lane];
-          w[4 * m] = t4.x;
-          w[4 * m + 1] = t4.y;
-          w[4 * m + 2] = t4.z;
-          w[4 * m + 3] = t4.w;
-        }
-        pair_sync(pair_id);
-      }
+      for (int i = 0; i < 16; ++i) w[i] = __shfl_xor_sync(0xffffffffu, v[i], 16);
       if (live) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
@@ -697,6 +676,17 @@ __global__ void __launch_bounds__(OT, 1) k_outer_tc(const float* __restrict__ A,
     uint8_t* hi = base + b * stage;
     uint8_t* lo = hi + half;
     const long n0 = (c0 + c) * OKC;
+    if (c + 1 < nmine) {   // the rows of the next chunk into L2 while this one loads
+      const long n1 = n0 + OKC;
+      const uint32_t bytes = (uint32_t)((N - n1 < OKC ? N - n1 : OKC) * 4);
+      for (int r = tid; r < R; r += OT) {
+        if (r < RA) {
+          if (r < Ma) tc::prefetch_l2(A + r * lda + n1, bytes);
+        } else if (r - RA < Mb) {
+          tc::prefetch_l2(B + (r - RA) * ldb + n1, bytes);
+        }
+      }
+    }
     for (int e0 = tid; e0 < NE; e0 += OT * OFB) {
       float4 v[OFB];
 #pragma unroll
@@ -783,7 +773,8 @@ __global__ void k_outer_tc_reduce(const float* __restrict__ part, long nsplit, l
   const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (e >= n) return;
   double s = 0.0;
-  for (long p = 0; p < nsplit; ++p) s += (double)part[p * n + e];
+#pragma unroll 8
+  for (long p = 0; p < nsplit; ++p) s += (double)part[p * n + e];   // loads issued ahead, sums in order
   out[e] = accumulate ? out[e] + s : s;
 }
 
@@ -910,8 +901,7 @@ int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, 
   const long items = F * ((nb + 127) / 128);
   const long grid = items < sms() ? items : sms();
   const size_t K2 = 2 * (size_t)C;
-  size_t smem = 1024 + 4 * 128 * K2 * 2 + (size_t)(C / CB) * 256 * CB * 4 + 2 * 16 * K2 * 2 + 128 * 16 * 4 +
-                8 * 128 * 16;
+  size_t smem = 1024 + 4 * 128 * K2 * 2 + (size_t)(C / CB) * 256 * CB * 4 + 2 * 16 * K2 * 2 + 128 * 16 * 4;
   if (smem < 120 * 1024) smem = 120 * 1024;   // one CTA per SM: each CTA holds all 512 tensor-memory columns
   cudaStream_t s = (cudaStream_t)stream;
   switch (C) {

@@ -68,6 +68,15 @@ def _w(conv):
     return conv.weight.detach()[:, :, 0, 0, 0].float()
 
 
+def mix_pack(device, m):
+    """Split-BF16 pack of a spectral-mixing matrix m [2C out][2C in] (outputs re 0..C-1 then im 0..C-1) with its output
+    rows in the order of ffno_spectral_mix_tc's tensor-memory lanes: slot p = 32 q + l holds part l // 16 (re, im) of
+    channel 16 q + l % 16."""
+    C = m.shape[0] // 2
+    perm = [((p % 32) // 16) * C + 16 * (p // 32) + p % 16 for p in range(2 * C)]
+    return tc_pack(device, m[perm])
+
+
 def tc_pack(device, *mats):
     """Split-BF16 packs of matrices [R][K] back to back: per matrix hi = bf16(M) then lo = bf16(M - hi), each in the
     canonical K-major order (the layout the tensor-core kernels bulk-copy into shared memory)."""
@@ -201,8 +210,8 @@ class Packed:
         pk["tcb_fuse_b"] = tc_pack(device, f0.t(), bg2.t(), bg0.t())
         for name, conv in (("s", s), ("v", v)):
             wb = _wbig(conv.weight_real, conv.weight_imag)
-            pk[f"tc_{name}_mix"] = tc_pack(device, wb.t())      # out = xhat @ wbig -> matrix wbig^T
-            pk[f"tcb_{name}_mix"] = tc_pack(device, wb)         # adjoint: xhat_bar = y_bar @ wbig^T
+            pk[f"tc_{name}_mix"] = mix_pack(device, wb.t())      # out = xhat @ wbig -> matrix wbig^T
+            pk[f"tcb_{name}_mix"] = mix_pack(device, wb)         # adjoint: xhat_bar = y_bar @ wbig^T
 
     @staticmethod
     def _head_params(model):

@@ -344,7 +344,8 @@ int ffno_xform_tc(const void* tpack, const float* in, float* out, const ffno_xfo
 int ffno_xform_tcr_max_table_bytes(void);
 int ffno_xform_tcr(const void* tpack, int Mp, int Kp, const float* in, float* out, const ffno_xform_desc* desc,
                    int accumulate, int* err, ffno_stream_t stream);
-/* ffno_spectral_mix on tensor cores (split-BF16); wpack = [wbig^T (2C x 2C)]; C = 16, 32, 64; strides multiples of 4
+/* ffno_spectral_mix on tensor cores (split-BF16); wpack = [wbig^T (2C x 2C)] with its output rows reordered so that
+ * row p = 32 q + l is part l / 16 (0 re, 1 im) of channel 16 q + l % 16; C = 16, 32, 64; strides multiples of 4
  * floats. */
 int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, long sb, long s_im, int C,
                          const void* wpack, const float* g, const float* U, const float* Vm, int rank, int* err,

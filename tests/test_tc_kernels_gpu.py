@@ -269,7 +269,7 @@ def test_xform_tc_matches_fp32(which, C, kind):
 @pytest.mark.parametrize("rank", [0, 3, 8])
 @pytest.mark.parametrize("layout", ["horizontal", "height"])
 def test_spectral_mix_tc(C, rank, layout):
-    from ffnoml_gb300.executor import tc_pack
+    from ffnoml_gb300.executor import mix_pack
     nat = _nat()
     F, nb = 37, 150
     if layout == "horizontal":
@@ -288,7 +288,7 @@ def test_spectral_mix_tc(C, rank, layout):
     nat.call("ffno_spectral_mix", x.data_ptr(), a.data_ptr(), F, nb, sf, sb, s_im, C, wbig.data_ptr(), gg.data_ptr(),
              ptr(U), ptr(Vm), rank, _s())
     nat.call("ffno_spectral_mix_tc", x.data_ptr(), b.data_ptr(), F, nb, sf, sb, s_im, C,
-             _hold(tc_pack(torch.device("cuda"), wbig.t().cpu())), gg.data_ptr(), ptr(U), ptr(Vm), rank,
+             _hold(mix_pack(torch.device("cuda"), wbig.t().cpu())), gg.data_ptr(), ptr(U), ptr(Vm), rank,
              err.data_ptr(), _s())
     torch.cuda.synchronize()
     assert int(err.item()) == 0
