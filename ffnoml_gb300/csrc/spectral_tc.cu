@@ -398,11 +398,13 @@ __global__ void __launch_bounds__(RT, 1)
 //     [16][2C] operand (rows 0..7 act on the re half, rows 8..15 on the im half).
 //   * MMAs: D^T [2C (padded to 128) x 128 b] = W X^T (W resident in shared memory as the A operand) and the low-rank
 //     projections T [128 b x 16] = X Vblk^T, into double-buffered tensor memory, so the epilogue of item i-1 runs
-//     while the MMAs of item i do.
+//     while the MMAs of item i do. After that epilogue, T of item i goes back to shared memory as a split K-major
+//     tile and the low-rank term D2^T [slots x 128 b] = Ublk T^T (Ublk: U_f block-diagonal by re / im part, K = 16)
+//     lands in a third accumulator, read by the epilogue of item i.
 //   * Epilogue: thread = output slot p (TMEM lane). W's output rows are packed so that warp quadrant q holds the re
 //     parts of channels 16q..16q+15 (lanes 0-15) and their im parts (lanes 16-31): the re and im lanes of a channel
-//     swap their values with one shuffle to apply g_f; y = g_f D + sum_r U_f[c][r] t[b][r]; 16 warps, each over 32
-//     rows b of its lane quadrant; one warp's stores cover 16 consecutive channels of the re and of the im part.
+//     swap their values with one shuffle to apply g_f; y = g_f D + D2; 16 warps, each over 32 rows b of its lane
+//     quadrant; one warp's stores cover 16 consecutive channels of the re and of the im part.
 constexpr int MIX_RANK_TC = 8;   // low-rank terms carried by the tensor-core mixing (larger ranks use k_mix)
 
 struct MixGeom {
@@ -425,15 +427,18 @@ __global__ void __launch_bounds__(XT, 1)
   constexpr bool SWZ = (CB == 32);
   constexpr uint32_t WB = 128u * K2 * 2;    // one split half (hi or lo) of a 128-row operand
   constexpr uint32_t WP = (uint32_t)K2 * K2 * 2;   // one split half of the packed [2C][2C] weight
-  constexpr int NT = 16;                    // low-rank operand rows
+  constexpr int NT = 16;                    // low-rank operand rows / columns
+  constexpr uint32_t LB = 128u * NT * 2;    // one split half of a [128][16] operand
+  constexpr uint32_t TD2 = 384;             // tensor-memory column of the low-rank accumulator
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
   uint8_t* sW = base;                  // hi [0, WB), lo [WB, 2 WB)
   uint8_t* sX = base + 2 * WB;
   uint8_t* sS = base + 4 * WB;         // staging, 1024-byte aligned (WB is a multiple of 1024)
-  uint8_t* sV = sS + NH * HALF;        // hi [NT][K2], lo after
-  float* sT = reinterpret_cast<float*>(sV + 2u * NT * K2 * 2);   // [128 b][16], 16-byte chunks swizzled by b
-  __shared__ uint64_t bar_w, bar_s, bar_m[2];
+  uint8_t* sV = sS + NH * HALF;        // Vblk [16][K2]: hi, then lo
+  uint8_t* sU = sV + 2u * NT * K2 * 2; // Ublk [128 slots][16]: hi, then lo
+  uint8_t* sT = sU + 2u * LB;          // T [128 b][16]: hi, then lo
+  __shared__ uint64_t bar_w, bar_s, bar_m[2], bar_r;
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, q = warp & 3, wg = warp >> 2;
   if (warp == 0) tc::tmem_alloc(&tslot, 512);
@@ -442,6 +447,7 @@ __global__ void __launch_bounds__(XT, 1)
     tc::mbar_init(&bar_s, 1);
     tc::mbar_init(&bar_m[0], 1);
     tc::mbar_init(&bar_m[1], 1);
+    tc::mbar_init(&bar_r, 1);
     tc::mbar_init_fence();
   }
   // zero the padding rows 2C..127 of W (hi and lo); they are contiguous at the end of each half
@@ -475,33 +481,23 @@ __global__ void __launch_bounds__(XT, 1)
   }
   bool ok = bounded(tc::mbar_wait(&bar_w, 0), err, 1);
   bool load_pending = it < items;         // the load of the next item to process is in flight
-  float ucur[MIX_RANK_TC], uprev[MIX_RANK_TC];
+  uint32_t n1 = 0, n2 = 0;                // commits issued on bar_m (main products) and bar_r (low-rank term)
   long pf = 0, pb0 = 0;
   float pgr = 0.f, pgi = 0.f;
   const int p = 32 * q + lane;            // output slot of this thread in the epilogue (its TMEM lane)
   const bool live = p < 2 * C;
   const int part = lane >> 4, pc = 16 * q + (lane & 15);   // re / im part and channel of slot p
 
+  // y = g_f D + (U_f t) for the rows of item (f, b0) from accumulator buffer buf and the low-rank accumulator
   auto epilogue = [&](uint32_t buf, long f, long b0, float gr, float gi) {
-    if (rank) {
-      if (wg == 0) {   // low-rank rows t[b][0..16) from tensor memory (lane = b) to shared memory
-        const int bl = 32 * q + lane;
-        float t[16];
-        tc::tmem_ld16(tmem + lq + 256u + buf * 16u, t);
-#pragma unroll
-        for (int m = 0; m < 4; ++m)
-          *reinterpret_cast<float4*>(sT + bl * 16 + ((m ^ (bl & 3)) << 2)) =
-              make_float4(t[4 * m], t[4 * m + 1], t[4 * m + 2], t[4 * m + 3]);
-      }
-      __syncthreads();
-    }
     float* ob = out + f * sf + part * s_im + pc;
     const float ga = gr, gb = part ? gi : -gi;   // y = ga * own + gb * partner
 #pragma unroll 1
     for (int cch = 0; cch < 2; ++cch) {
       const int col = 32 * wg + 16 * cch;
-      float v[16], w[16];
+      float v[16], w[16], r[16];
       tc::tmem_ld16(tmem + lq + buf * 128u + (uint32_t)col, v);
+      if (rank) tc::tmem_ld16(tmem + lq + TD2 + (uint32_t)col, r);
 #pragma unroll
       for (int i = 0; i < 16; ++i) w[i] = __shfl_xor_sync(0xffffffffu, v[i], 16);
       if (live) {
@@ -510,20 +506,7 @@ __global__ void __launch_bounds__(XT, 1)
           const long b = b0 + col + i;
           if (b < nb) {
             float y = fmaf(ga, v[i], gb * w[i]);
-            if (rank) {
-              const int bl = col + i;
-              const float* tr = sT + bl * 16;
-#pragma unroll
-              for (int m = 0; m < 2; ++m) {
-                if (4 * m < rank) {
-                  const float4 tv = *reinterpret_cast<const float4*>(tr + (((2 * part + m) ^ (bl & 3)) << 2));
-                  y = fmaf(uprev[4 * m], tv.x, y);
-                  if (4 * m + 1 < rank) y = fmaf(uprev[4 * m + 1], tv.y, y);
-                  if (4 * m + 2 < rank) y = fmaf(uprev[4 * m + 2], tv.z, y);
-                  if (4 * m + 3 < rank) y = fmaf(uprev[4 * m + 3], tv.w, y);
-                }
-              }
-            }
+            if (rank) y += r[i];
             ob[b * sb] = y;
           }
         }
@@ -537,16 +520,19 @@ __global__ void __launch_bounds__(XT, 1)
   uint32_t j = 0;
   for (; ok && it < items; it += gridDim.x, ++j) {
     const long f = it / nbt, b0 = (it % nbt) * 128;
+    const uint32_t buf = j & 1u;
+    // staged rows of item j; the MMAs of item j-1 (sX free) and its low-rank product (sU, sT free, D2 ready)
     const bool w1 = tc::mbar_wait(&bar_s, j & 1u);
-    const bool w2 = j ? tc::mbar_wait(&bar_m[(j - 1) & 1u], ((j - 1) >> 1) & 1u) : true;
-    if (!(ok = bounded(w1 && w2, err, 2))) break;
+    const bool w2 = n1 ? tc::mbar_wait(&bar_m[(n1 - 1) & 1u], ((n1 - 1) >> 1) & 1u) : true;
+    const bool w3 = n2 ? tc::mbar_wait(&bar_r, (n2 - 1) & 1u) : true;
+    if (!(ok = bounded(w1 && w2 && w3, err, 2))) break;
     load_pending = false;
     tc::tc_after_sync();
     // split the staged rows into X
     for (int e = tid; e < 128 * NH * CPR; e += XT) {
       const int c4 = e % CPR, rest = e / CPR;
-      const int b = rest & 127, h = rest >> 7;
-      const int rre = b * geo.mul_b, rim = rre + geo.mul_ri;
+      const int bb = rest & 127, h = rest >> 7;
+      const int rre = bb * geo.mul_b, rim = rre + geo.mul_ri;
       const uint8_t* hb = sS + h * HALF;
       const float4 xr = *reinterpret_cast<const float4*>(hb + rre * ROWB + ((SWZ ? (c4 ^ (rre & 7)) : c4) << 4));
       const float4 xi = *reinterpret_cast<const float4*>(hb + rim * ROWB + ((SWZ ? (c4 ^ (rim & 7)) : c4) << 4));
@@ -554,12 +540,12 @@ __global__ void __launch_bounds__(XT, 1)
       uint32_t h0, l0, h1, l1;
       tc::split_pack(xr.x, xr.y, h0, l0);
       tc::split_pack(xr.z, xr.w, h1, l1);
-      *reinterpret_cast<uint2*>(sX + tc::kmajor_offset(b, k, K2)) = make_uint2(h0, h1);
-      *reinterpret_cast<uint2*>(sX + WB + tc::kmajor_offset(b, k, K2)) = make_uint2(l0, l1);
+      *reinterpret_cast<uint2*>(sX + tc::kmajor_offset(bb, k, K2)) = make_uint2(h0, h1);
+      *reinterpret_cast<uint2*>(sX + WB + tc::kmajor_offset(bb, k, K2)) = make_uint2(l0, l1);
       tc::split_pack(xi.x, xi.y, h0, l0);
       tc::split_pack(xi.z, xi.w, h1, l1);
-      *reinterpret_cast<uint2*>(sX + tc::kmajor_offset(b, C + k, K2)) = make_uint2(h0, h1);
-      *reinterpret_cast<uint2*>(sX + WB + tc::kmajor_offset(b, C + k, K2)) = make_uint2(l0, l1);
+      *reinterpret_cast<uint2*>(sX + tc::kmajor_offset(bb, C + k, K2)) = make_uint2(h0, h1);
+      *reinterpret_cast<uint2*>(sX + WB + tc::kmajor_offset(bb, C + k, K2)) = make_uint2(l0, l1);
     }
     if (rank) {
       // block-diagonal V_f: rows 0..r-1 act on the re half, rows 8..8+r-1 on the im half, the others are zero
@@ -578,9 +564,22 @@ __global__ void __launch_bounds__(XT, 1)
         *reinterpret_cast<uint32_t*>(sV + tc::kmajor_offset(n, k, K2)) = hi;
         *reinterpret_cast<uint32_t*>(sV + (uint32_t)NT * K2 * 2 + tc::kmajor_offset(n, k, K2)) = lo;
       }
-#pragma unroll
-      for (int r = 0; r < MIX_RANK_TC; ++r)
-        ucur[r] = (live && r < rank) ? __ldg(U + (f * C + pc) * (long)rank + r) : 0.f;
+      // block-diagonal U_f by output slot: slot p (part, channel pc) takes U_f[pc][0..r) in columns 8 part + r
+      for (int e = tid; e < 128 * NT / 2; e += XT) {
+        const int ps = e / (NT / 2), k = (e % (NT / 2)) * 2;
+        const int sp = (ps & 31) >> 4, sc = 16 * (ps >> 5) + (ps & 15);
+        float u0 = 0.f, u1 = 0.f;
+        if (ps < 2 * C && (k >> 3) == sp) {
+          const int r = k & 7;
+          const float* ur = U + (f * C + sc) * (long)rank;
+          if (r < rank) u0 = __ldg(ur + r);
+          if (r + 1 < rank) u1 = __ldg(ur + r + 1);
+        }
+        uint32_t hi, lo;
+        tc::split_pack(u0, u1, hi, lo);
+        *reinterpret_cast<uint32_t*>(sU + tc::kmajor_offset(ps, k, NT)) = hi;
+        *reinterpret_cast<uint32_t*>(sU + LB + tc::kmajor_offset(ps, k, NT)) = lo;
+      }
     }
     tc::fence_async_smem();
     tc::tc_before_sync();
@@ -589,7 +588,6 @@ __global__ void __launch_bounds__(XT, 1)
     load_pending = it + gridDim.x < items;
     if (tid == 0) {
       if (load_pending) issue_load(it + gridDim.x);
-      const uint32_t buf = j & 1u;
       const uint32_t w_hi = tc::smem_u32(sW), x_hi = tc::smem_u32(sX);
       tc::gemm3_128xN(tmem + buf * 128u, w_hi, w_hi + WB, x_hi, x_hi + WB, K2, 128);
       if (rank) {
@@ -598,17 +596,48 @@ __global__ void __launch_bounds__(XT, 1)
       }
       tc::mma_commit(&bar_m[buf]);
     }
-    if (j) epilogue((j - 1) & 1u, pf, pb0, pgr, pgi);
+    ++n1;
+    if (j) epilogue((j - 1) & 1u, pf, pb0, pgr, pgi);   // ends with a barrier: D2 has been read
+    if (rank) {
+      // t = X V_f^T of item j (lanes = rows b) into a split K-major tile, then D2 = Ublk T^T
+      if (!(ok = bounded(tc::mbar_wait(&bar_m[buf], (j >> 1) & 1u), err, 4))) {
+        ++j;
+        break;
+      }
+      tc::tc_after_sync();
+      if (wg == 0) {
+        float t[16];
+        tc::tmem_ld16(tmem + lq + 256u + buf * 16u, t);
+        const int bl = 32 * q + lane;
+        uint32_t h[8], l[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) tc::split_pack(t[2 * i], t[2 * i + 1], h[i], l[i]);
+        const uint32_t o0 = tc::kmajor_offset(bl, 0, NT), o1 = tc::kmajor_offset(bl, 8, NT);
+        *reinterpret_cast<uint4*>(sT + o0) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4*>(sT + o1) = make_uint4(h[4], h[5], h[6], h[7]);
+        *reinterpret_cast<uint4*>(sT + LB + o0) = make_uint4(l[0], l[1], l[2], l[3]);
+        *reinterpret_cast<uint4*>(sT + LB + o1) = make_uint4(l[4], l[5], l[6], l[7]);
+      }
+      tc::fence_async_smem();
+      tc::tc_before_sync();
+      __syncthreads();
+      tc::tc_after_sync();
+      if (tid == 0) {
+        const uint32_t u_hi = tc::smem_u32(sU), t_hi = tc::smem_u32(sT);
+        tc::gemm3_128xN(tmem + TD2, u_hi, u_hi + LB, t_hi, t_hi + LB, NT, 128);
+        tc::mma_commit(&bar_r);
+      }
+      ++n2;
+    }
     pf = f;
     pb0 = b0;
     pgr = __ldg(g + 2 * f);
     pgi = __ldg(g + 2 * f + 1);
-#pragma unroll
-    for (int r = 0; r < MIX_RANK_TC; ++r) uprev[r] = ucur[r];
   }
   if (ok && j) {
-    const bool w = tc::mbar_wait(&bar_m[(j - 1) & 1u], ((j - 1) >> 1) & 1u);
-    if ((ok = bounded(w, err, 3))) {
+    const bool w1 = tc::mbar_wait(&bar_m[(n1 - 1) & 1u], ((n1 - 1) >> 1) & 1u);
+    const bool w2 = n2 ? tc::mbar_wait(&bar_r, (n2 - 1) & 1u) : true;
+    if ((ok = bounded(w1 && w2, err, 3))) {
       tc::tc_after_sync();
       epilogue((j - 1) & 1u, pf, pb0, pgr, pgi);
     }
@@ -616,7 +645,8 @@ __global__ void __launch_bounds__(XT, 1)
   if (!ok) {   // leave no bulk copy or MMA in flight before freeing tensor memory
     tc::mbar_wait(&bar_w, 0);
     if (load_pending) tc::mbar_wait(&bar_s, j & 1u);
-    if (j) tc::mbar_wait(&bar_m[(j - 1) & 1u], ((j - 1) >> 1) & 1u);
+    if (n1) tc::mbar_wait(&bar_m[(n1 - 1) & 1u], ((n1 - 1) >> 1) & 1u);
+    if (n2) tc::mbar_wait(&bar_r, (n2 - 1) & 1u);
   }
   tc::tc_before_sync();
   __syncthreads();
@@ -676,17 +706,6 @@ __global__ void __launch_bounds__(OT, 1) k_outer_tc(const float* __restrict__ A,
     uint8_t* hi = base + b * stage;
     uint8_t* lo = hi + half;
     const long n0 = (c0 + c) * OKC;
-    if (c + 1 < nmine) {   // the rows of the next chunk into L2 while this one loads
-      const long n1 = n0 + OKC;
-      const uint32_t bytes = (uint32_t)((N - n1 < OKC ? N - n1 : OKC) * 4);
-      for (int r = tid; r < R; r += OT) {
-        if (r < RA) {
-          if (r < Ma) tc::prefetch_l2(A + r * lda + n1, bytes);
-        } else if (r - RA < Mb) {
-          tc::prefetch_l2(B + (r - RA) * ldb + n1, bytes);
-        }
-      }
-    }
     for (int e0 = tid; e0 < NE; e0 += OT * OFB) {
       float4 v[OFB];
 #pragma unroll
@@ -901,7 +920,7 @@ int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, 
   const long items = F * ((nb + 127) / 128);
   const long grid = items < sms() ? items : sms();
   const size_t K2 = 2 * (size_t)C;
-  size_t smem = 1024 + 4 * 128 * K2 * 2 + (size_t)(C / CB) * 256 * CB * 4 + 2 * 16 * K2 * 2 + 128 * 16 * 4;
+  size_t smem = 1024 + 4 * 128 * K2 * 2 + (size_t)(C / CB) * 256 * CB * 4 + 2 * 16 * K2 * 2 + 4 * 128 * 16 * 2;
   if (smem < 120 * 1024) smem = 120 * 1024;   // one CTA per SM: each CTA holds all 512 tensor-memory columns
   cudaStream_t s = (cudaStream_t)stream;
   switch (C) {
