@@ -41,6 +41,7 @@ constexpr int RT = 256;                     // threads per pipeline
 constexpr int RKC = 64;                     // data rows k per chunk
 constexpr uint32_t RSB = 128u * RKC * 2;    // one split half of a data stage
 constexpr int RT_MAXK = 512;                // largest padded K of a resident table
+constexpr int XFB = 8;                      // data loads in flight per thread (a whole 64-row chunk per pipeline)
 
 __device__ __forceinline__ void rt_sync(int pipe) { asm volatile("bar.sync %0, %1;" ::"r"(1 + pipe), "n"(RT) : "memory"); }
 __device__ __forceinline__ bool rt_sync_and(int pipe, bool p) {
@@ -127,17 +128,17 @@ __global__ void __launch_bounds__(2 * RT, 1)
       // fill: piece e = 4 consecutive columns of one row k; lanes take 8 rows x 2 column pairs, so a warp reads 8
       // rows x 64 contiguous bytes and writes conflict-free 8-byte slots of the MN-major tile. Row k of piece e is
       // 8 (e / 256) + (lane & 7); its columns nf..nf+3 depend on the thread only.
-      for (int e0 = ptid; e0 < kc * 32; e0 += 4 * RT) {
-        float4 v[4];
+      for (int e0 = ptid; e0 < kc * 32; e0 += XFB * RT) {
+        float4 v[XFB];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < XFB; ++u) {
           const int e = e0 + u * RT;
           const int k = k0 + 8 * (e >> 8) + (lane & 7);
           v[u] = (e < kc * 32 && k < d.K && fv) ? __ldg(reinterpret_cast<const float4*>(fsrc + row_in[k]))
                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < XFB; ++u) {
           const int e = e0 + u * RT;
           if (e >= kc * 32) break;
           uint32_t h0, l0, h1, l1;
@@ -297,17 +298,17 @@ __global__ void __launch_bounds__(RT, 1)
           tc::bulk_g2s(tt + (uint32_t)MT * part + mt * part, src + part, part, &bar_t[s]);
         }
       }
-      for (int e0 = tid; e0 < kc * 32; e0 += 4 * RT) {
-        float4 v[4];
+      for (int e0 = tid; e0 < kc * 32; e0 += XFB * RT) {
+        float4 v[XFB];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < XFB; ++u) {
           const int e = e0 + u * RT;
           const int k = k0 + 8 * (e >> 8) + (lane & 7);
           v[u] = (e < kc * 32 && k < d.K && fv) ? __ldg(reinterpret_cast<const float4*>(fsrc + row_in[k]))
                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < XFB; ++u) {
           const int e = e0 + u * RT;
           if (e >= kc * 32) break;
           uint32_t h0, l0, h1, l1;
