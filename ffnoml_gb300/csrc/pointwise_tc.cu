@@ -1376,6 +1376,7 @@ int ffno_gate_fwd_tc(const float* x, long V, int C, const void* wpack, const flo
                      int* err, ffno_stream_t stream) {
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
+  if (ws::gate_fwd_supported(C)) return ws::gate_fwd(x, V, C, wpack, zp, z, out, err, s);
   TC_DISPATCH(C, {
     const size_t smem = 2 * mat_bytes(CC, CC) + 2 * tile_bytes(CC);
     if (!launch_prep(k_gate_tc<CC>, smem)) return FFNO_ELAUNCH;

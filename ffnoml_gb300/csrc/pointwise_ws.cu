@@ -593,6 +593,232 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) tc::tmem_free(tmem, 512);
 }
 
+// ================================================================================================ input gate
+// The ffno_gate_fwd_tc contract: out = x sigmoid(gelu(x G1^T) G2^T) [+ zp z], G1, G2: [C][C]. Roles as in the forward
+// MLP: warp 0 TMA ring of x; warp 1 MMA: GEMM1 D1[t % 2] = x G1^T, and GEMM2 D2 = H G2^T one tile behind; warps 2-5
+// conversion into the A stages; warps 6-13 epilogue 1: H = gelu(D1), split over D1; warps 14-17 epilogue 2: the gate
+// applied to the tile's x rows (loaded from HBM before D2 is waited for) and the z_proj term. Tensor memory: four A
+// stages of C columns from column 0 (D2 of a stage's tile over them), D1 buffers at 256 and 256 + C.
+template <int C>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_gate_fwd_ws(const __grid_constant__ CUtensorMap map_x, const float* __restrict__ x, long V,
+                  const uint8_t* __restrict__ wpack, const float* __restrict__ zp, const float* __restrict__ z,
+                  float* __restrict__ out, int* __restrict__ err) {
+  static_assert(C == 32 || C == 64, "widths 32 and 64");
+  constexpr uint32_t B1 = mat_bytes(C, C);       // each of g1, g2
+  constexpr uint32_t WB = 2 * B1;
+  constexpr int NB = C / 32;
+  constexpr uint32_t SB = NB * BOX_BYTES;        // one ring stage: x
+  constexpr int NA = 4;                          // A stages
+  static_assert(WB % 1024 == 0, "the ring must stay 1024-byte aligned (128-byte swizzle)");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint8_t* ring = smem + WB;
+  __shared__ uint64_t stg_full[2], stg_empty[2], a_full[NA], a_empty[NA], d2_full[NA], d1_full[2], h_full[2], wbar;
+  __shared__ uint32_t tslot;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) tc::tmem_alloc(&tslot, 512);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; ++s) {
+      tc::mbar_init(&stg_full[s], 1);
+      tc::mbar_init(&stg_empty[s], 128);
+      tc::mbar_init(&d1_full[s], 1);
+      tc::mbar_init(&h_full[s], 256);
+    }
+    for (int s = 0; s < NA; ++s) {
+      tc::mbar_init(&a_full[s], 128);
+      tc::mbar_init(&a_empty[s], 128);
+      tc::mbar_init(&d2_full[s], 1);
+    }
+    tc::mbar_init(&wbar, 1);
+    tc::mbar_init_fence();
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  const uint32_t tmem = tslot;
+  if (threadIdx.x == 0) {
+    tc::mbar_arrive_expect_tx(&wbar, WB);
+    tc::bulk_g2s(smem, wpack, WB, &wbar);
+  }
+  const bool ok = __syncthreads_and(tc::mbar_wait_for(&wbar, 0, WAIT_NS)) != 0;
+  if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+
+  const long nt = (V + TM - 1) / TM;
+  const int niter = (long)blockIdx.x < nt ? (int)((nt - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  auto tile_of = [&](int i) { return (long)blockIdx.x + (long)i * gridDim.x; };
+  constexpr uint32_t D1C = 256;
+
+  if (ok && warp == W_TMA && lane == 0) {
+    int issued[2] = {0, 0};
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!wait_or_flag(&stg_empty[s], (n & 1u) ^ 1u, err, 3)) break;
+      const int row = (int)(tile_of(i) * TM);
+      tc::mbar_arrive_expect_tx(&stg_full[s], SB);
+      uint8_t* st = ring + s * SB;
+#pragma unroll
+      for (int b = 0; b < NB; ++b) tc::tma_load_2d(st + b * BOX_BYTES, &map_x, 32 * b, row, &stg_full[s]);
+      ++issued[s];
+    }
+    for (int s = 0; s < 2; ++s)
+      if (issued[s]) tc::mbar_wait_for(&stg_full[s], (uint32_t)(issued[s] - 1) & 1u, WAIT_NS);
+  } else if (ok && warp == W_MMA && lane == 0) {
+    const uint32_t id = tc::idesc_bf16(128, C);
+    const uint32_t g1 = tc::smem_u32(smem), g2 = g1 + B1, LO = B1 / 2;
+    uint64_t* last = nullptr;
+    uint32_t last_par = 0;
+    bool alive = true;
+    auto gemm2 = [&](int j) {   // D2 (A stage j % NA) = H(j) (in D1[j % 2]) G2^T, K = C
+      const uint32_t h = tmem + D1C + (uint32_t)(C * (j & 1));
+#pragma unroll 1
+      for (int k = 0; k < C / 16; ++k)
+        mma3_ta(tmem + (uint32_t)(C * (j % NA)), h + 16u * k, h + 16u * k + 8u,
+                tc::kmajor_desc(g2 + 256u * k, 128u, C * 16u), tc::kmajor_desc(g2 + LO + 256u * k, 128u, C * 16u),
+                id, k > 0);
+      tc::mma_commit(&d2_full[j % NA]);
+      last = &d2_full[j % NA];
+      last_par = (uint32_t)(j / NA) & 1u;
+    };
+    for (int i = 0; i < niter && alive; ++i) {
+      const int s = i & 1, sa = i % NA;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!wait_or_flag(&a_full[sa], (uint32_t)(i / NA) & 1u, err, 4)) {
+        alive = false;
+        break;
+      }
+      if (i >= 2 && !wait_or_flag(&d2_full[(i - 2) % NA], (uint32_t)((i - 2) / NA) & 1u, err, 11)) {
+        alive = false;   // GEMM2 of tile i-2, the last reader of D1[s], has completed
+        break;
+      }
+      tc::tc_after_sync();
+      const uint32_t A = tmem + (uint32_t)(C * sa), D = tmem + D1C + (uint32_t)(C * s);
+#pragma unroll 1
+      for (int k = 0; k < C / 16; ++k)
+        mma3_ta(D, A + 8u * k, A + C / 2 + 8u * k, tc::kmajor_desc(g1 + 256u * k, 128u, C * 16u),
+                tc::kmajor_desc(g1 + LO + 256u * k, 128u, C * 16u), id, k > 0);
+      tc::mma_commit(&d1_full[s]);
+      last = &d1_full[s];
+      last_par = n & 1u;
+      if (i >= 1) {
+        if (!wait_or_flag(&h_full[(i - 1) & 1], ((uint32_t)(i - 1) >> 1) & 1u, err, 5)) { alive = false; break; }
+        tc::tc_after_sync();
+        gemm2(i - 1);
+      }
+    }
+    if (alive && niter >= 1) {
+      const int j = niter - 1;
+      if (wait_or_flag(&h_full[j & 1], ((uint32_t)j >> 1) & 1u, err, 6)) {
+        tc::tc_after_sync();
+        gemm2(j);
+      }
+    }
+    if (last) tc::mbar_wait_for(last, last_par, WAIT_NS);   // no MMA in flight when tensor memory is freed
+  } else if (ok && warp >= W_CVT && warp < W_E1) {
+    const int q = warp & 3, r = 32 * q + lane;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      const int sa = i % NA;
+      if (!warp_wait(&stg_full[s], n & 1u, err, 7)) break;
+      if (!warp_wait(&a_empty[sa], ((uint32_t)(i / NA) & 1u) ^ 1u, err, 8)) break;
+      tc::tc_after_sync();
+      const uint8_t* st = ring + s * SB;
+      const uint32_t A = tmem + lq + (uint32_t)(C * sa);
+#pragma unroll 1
+      for (int bh = 0; bh < 2 * NB; ++bh) {   // half boxes: 16 channels, 8 hi and 8 lo columns
+        const uint8_t* rin = st + (bh >> 1) * BOX_BYTES + r * 128;
+        uint32_t hi[8], lo[8];
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+          const int c = 4 * (bh & 1) + cc;
+          const float4 v = *reinterpret_cast<const float4*>(rin + ((c ^ (r & 7)) << 4));
+          tc::split_pack(v.x, v.y, hi[2 * cc], lo[2 * cc]);
+          tc::split_pack(v.z, v.w, hi[2 * cc + 1], lo[2 * cc + 1]);
+        }
+        tc::tmem_st8u(A + (uint32_t)(8 * bh), hi);
+        tc::tmem_st8u(A + (uint32_t)(C / 2 + 8 * bh), lo);
+      }
+      tc::mbar_arrive(&stg_empty[s]);
+      tc::tmem_wait_st();
+      tc::tc_before_sync();
+      tc::mbar_arrive(&a_full[sa]);
+    }
+  } else if (ok && warp >= W_E1 && warp < W_E2) {
+    const int q = warp & 3, hf = (warp - W_E1) >> 2;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!warp_wait(&d1_full[s], n & 1u, err, 9)) break;
+      tc::tc_after_sync();
+      const uint32_t D = tmem + lq + D1C + (uint32_t)(C * s);
+#pragma unroll 1
+      for (int j = hf; j < C / 16; j += 2) {
+        uint32_t h[16];
+        tc::tmem_ld16u(D + 16u * j, h);
+        tc::tmem_wait_ld();
+        uint32_t hi[8], lo[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          tc::split_pack(gelu_tc(__uint_as_float(h[2 * e])), gelu_tc(__uint_as_float(h[2 * e + 1])), hi[e], lo[e]);
+        tc::tmem_st8u(D + 16u * j, hi);
+        tc::tmem_st8u(D + 16u * j + 8u, lo);
+      }
+      tc::tmem_wait_st();
+      tc::tc_before_sync();
+      tc::mbar_arrive(&h_full[s]);
+    }
+  } else if (ok && warp >= W_E2) {
+    const int q = warp & 3, r = 32 * q + lane;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int sa = i % NA;
+      const long v = tile_of(i) * TM + r;
+      const bool live = v < V;
+      float4 xv[C / 4];
+#pragma unroll
+      for (int c = 0; c < C / 4; ++c)
+        xv[c] = live ? __ldg(reinterpret_cast<const float4*>(x + v * C) + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float zv = (zp && live) ? __ldg(z + v) : 0.f;
+      if (!warp_wait(&d2_full[sa], (uint32_t)(i / NA) & 1u, err, 10)) break;
+      tc::tc_after_sync();
+#pragma unroll
+      for (int k = 0; k < C / 16; ++k) {
+        uint32_t d[16];
+        tc::tmem_ld16u(tmem + lq + (uint32_t)(C * sa + 16 * k), d);
+        tc::tmem_wait_ld();
+        if (k == C / 16 - 1) {   // the stage's tensor memory is free once D2 is in registers
+          tc::tc_before_sync();
+          tc::mbar_arrive(&a_empty[sa]);
+        }
+        if (live) {
+          float4* o = reinterpret_cast<float4*>(out + v * C + 16 * k);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const float4 x4 = xv[4 * k + e];
+            float4 y = make_float4(x4.x * sigmoid_tc(__uint_as_float(d[4 * e])),
+                                   x4.y * sigmoid_tc(__uint_as_float(d[4 * e + 1])),
+                                   x4.z * sigmoid_tc(__uint_as_float(d[4 * e + 2])),
+                                   x4.w * sigmoid_tc(__uint_as_float(d[4 * e + 3])));
+            if (zp) {
+              const float4 zz = __ldg(reinterpret_cast<const float4*>(zp + 16 * k + 4 * e));
+              y = make_float4(fmaf(zz.x, zv, y.x), fmaf(zz.y, zv, y.y), fmaf(zz.z, zv, y.z), fmaf(zz.w, zv, y.w));
+            }
+            o[e] = y;
+          }
+        }
+      }
+    }
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  if (warp == 0) tc::tmem_free(tmem, 512);
+}
+
 int g_sms = 0;
 int sms() {
   if (!g_sms) {
@@ -647,10 +873,36 @@ int launch_mlp2_fwd(const float* in, const float* prev, const float* pc, float r
   return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
 }
 
+template <int C>
+int launch_gate_fwd(const float* x, long V, const void* wpack, const float* zp, const float* z, float* out, int* err,
+                    cudaStream_t s) {
+  CUtensorMap mx;
+  if (!row_map(&mx, x, V, C)) return FFNO_EINVAL;
+  const size_t smem = 1024 + 2 * (size_t)mat_bytes(C, C) + 2 * (size_t)((C / 32) * BOX_BYTES);
+  if (cudaFuncSetAttribute(k_gate_fwd_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return FFNO_ELAUNCH;
+  const long nt = (V + TM - 1) / TM;
+  const int grid = (int)(nt < sms() ? nt : sms());
+  k_gate_fwd_ws<C><<<grid, NTHREADS, smem, s>>>(mx, x, V, static_cast<const uint8_t*>(wpack), zp, z, out, err);
+  return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
+}
+
 }  // namespace
 
 namespace ffno {
 namespace ws {
+
+bool gate_fwd_supported(int C) { return C == 32 || C == 64; }
+
+int gate_fwd(const float* x, long V, int C, const void* wpack, const float* zp, const float* z, float* out, int* err,
+             cudaStream_t stream) {
+  if (V < 1 || V > 0x7fffffffL - TM || reinterpret_cast<uintptr_t>(x) % 16 || reinterpret_cast<uintptr_t>(out) % 16 ||
+      (zp && reinterpret_cast<uintptr_t>(zp) % 16))
+    return FFNO_EINVAL;
+  if (C == 64) return launch_gate_fwd<64>(x, V, wpack, zp, z, out, err, stream);
+  if (C == 32) return launch_gate_fwd<32>(x, V, wpack, zp, z, out, err, stream);
+  return FFNO_EINVAL;
+}
 
 bool mlp2_fwd_supported(int C) { return C == 32 || C == 64; }
 

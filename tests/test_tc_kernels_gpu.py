@@ -102,9 +102,10 @@ def test_mlp2_fwd_tc(C, V, mode):
     assert torch.allclose(outs[1][2], outs[0][2], rtol=1e-4, atol=1e-6)
 
 
-@pytest.mark.parametrize("C", [16, 32, 64])
+@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (64, 152 * 128 * 5 + 77)])
 @pytest.mark.parametrize("with_z", [False, True])
-def test_gate_fwd_tc(C, with_z):
+def test_gate_fwd_tc(C, V, with_z):
+    """Widths 32 and 64 run the warp-specialised kernel; also at a voxel count that cycles every CTA's ring."""
     nat = _nat()
     x = _rand(V, C, seed=1)
     g1, g2 = _rand(C, C, seed=2, scale=C ** -0.5), _rand(C, C, seed=3, scale=C ** -0.5)
