@@ -1435,6 +1435,7 @@ int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long
                      const float* zp, float* x_bar, float* z_bar, int* err, ffno_stream_t stream) {
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z_bar)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
+  if (ws::gate_bwd_supported(C)) return ws::gate_bwd(x, g_bar, base, V, C, wpack, zp, x_bar, z_bar, err, s);
   TC_DISPATCH(C, {
     const size_t smem = 4 * mat_bytes(CC, CC) + 4 * tile_bytes(CC);
     if (!launch_prep(k_gate_bwd_tc<CC>, smem)) return FFNO_ELAUNCH;

@@ -819,6 +819,305 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) tc::tmem_free(tmem, 512);
 }
 
+// ============================================================================================ input gate, VJP
+// The ffno_gate_bwd_tc contract: x_bar = base + d/dx [x sigmoid(gelu(x G1^T) G2^T)] applied to g_bar, z_bar[v] +=
+// g_bar . zp when zp. Per tile (lane = voxel, all products untransposed, K = N = C):
+//   GEMM1 h = x G1^T;  E1: H = gelu(h);  GEMM2 s = H G2^T;  E2: o = base + g_bar sig(s) (stored into the GEMM4
+//   accumulator), Q = g_bar x sig(s) (1 - sig(s));  GEMM3 t = Q G2;  E3: G = t gelu'(h);  GEMM4 acc += G G1;  E4: x_bar.
+// Roles: warp 0 TMA ring of x and g_bar (two stages; a stage is held until E2 has read it); warp 1 MMA; warps 2-5
+// conversion of x into tensor memory; warps 6-9 E1 and E3; warps 10-13 E2 and E4. Tiles go through in pairs, one per
+// tensor-memory slot of 4C columns ([x split, then s, then t] [h] [H, then Q, then G] [o + G G1]), and every role
+// works through a pair stage by stage (both tiles' GEMM1, both E1, both GEMM2, ...), so that the MMAs of one tile run
+// while the epilogue warps work on the other.
+template <int C>
+__global__ void __launch_bounds__(448, 1)
+    k_gate_bwd_ws(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_g,
+                  const float* __restrict__ base, long V, const uint8_t* __restrict__ wpack,
+                  const float* __restrict__ zp, float* __restrict__ xbar, float* __restrict__ zbar,
+                  int* __restrict__ err) {
+  static_assert(C == 32 || C == 64, "widths 32 and 64");
+  constexpr int GW_TMA = 0, GW_MMA = 1, GW_CVT = 2, GW_E13 = 6, GW_E24 = 10;
+  constexpr uint32_t B1 = mat_bytes(C, C);       // each of g1, g2, g2t, g1t
+  constexpr uint32_t WB = 4 * B1;
+  constexpr int NB = C / 32;
+  constexpr uint32_t XB = NB * BOX_BYTES;        // one tensor's FP32 tile
+  constexpr uint32_t SB = 2 * XB;                // one ring stage: x, g_bar
+  static_assert(WB % 1024 == 0, "the ring must stay 1024-byte aligned (128-byte swizzle)");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint8_t* ring = smem + WB;
+  __shared__ uint64_t stg_full[2], stg_empty[2], a_full[2], ra_free[2], d1_full[2], h_full[2], d2_full[2],
+      q_full[2], d3_full[2], g_full[2], d4_full[2], wbar;
+  __shared__ uint32_t tslot;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) tc::tmem_alloc(&tslot, 512);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; ++s) {
+      tc::mbar_init(&stg_full[s], 1);
+      tc::mbar_init(&stg_empty[s], 128);
+      tc::mbar_init(&a_full[s], 128);
+      tc::mbar_init(&ra_free[s], 128);
+      tc::mbar_init(&d1_full[s], 1);
+      tc::mbar_init(&h_full[s], 128);
+      tc::mbar_init(&d2_full[s], 1);
+      tc::mbar_init(&q_full[s], 128);
+      tc::mbar_init(&d3_full[s], 1);
+      tc::mbar_init(&g_full[s], 128);
+      tc::mbar_init(&d4_full[s], 1);
+    }
+    tc::mbar_init(&wbar, 1);
+    tc::mbar_init_fence();
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  const uint32_t tmem = tslot;
+  if (threadIdx.x == 0) {
+    tc::mbar_arrive_expect_tx(&wbar, WB);
+    for (uint32_t off = 0; off < WB; off += 32768u)
+      tc::bulk_g2s(smem + off, wpack + off, WB - off < 32768u ? WB - off : 32768u, &wbar);
+  }
+  const bool ok = __syncthreads_and(tc::mbar_wait_for(&wbar, 0, WAIT_NS)) != 0;
+  if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+
+  const long nt = (V + TM - 1) / TM;
+  const int niter = (long)blockIdx.x < nt ? (int)((nt - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  const int npair = (niter + 1) / 2;
+  auto tile_of = [&](int i) { return (long)blockIdx.x + (long)i * gridDim.x; };
+  // tensor-memory regions of slot t
+  auto RA = [&](int t) { return tmem + (uint32_t)(4 * C * t); };
+  auto RD1 = [&](int t) { return tmem + (uint32_t)(4 * C * t + C); };
+  auto RH = [&](int t) { return tmem + (uint32_t)(4 * C * t + 2 * C); };
+  auto RD4 = [&](int t) { return tmem + (uint32_t)(4 * C * t + 3 * C); };
+
+  if (ok && warp == GW_TMA && lane == 0) {
+    int issued[2] = {0, 0};
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!wait_or_flag(&stg_empty[s], (n & 1u) ^ 1u, err, 3)) break;
+      const int row = (int)(tile_of(i) * TM);
+      tc::mbar_arrive_expect_tx(&stg_full[s], SB);
+      uint8_t* st = ring + s * SB;
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        tc::tma_load_2d(st + b * BOX_BYTES, &map_x, 32 * b, row, &stg_full[s]);
+        tc::tma_load_2d(st + XB + b * BOX_BYTES, &map_g, 32 * b, row, &stg_full[s]);
+      }
+      ++issued[s];
+    }
+    for (int s = 0; s < 2; ++s)
+      if (issued[s]) tc::mbar_wait_for(&stg_full[s], (uint32_t)(issued[s] - 1) & 1u, WAIT_NS);
+  } else if (ok && warp == GW_MMA && lane == 0) {
+    const uint32_t id = tc::idesc_bf16(128, C);
+    const uint32_t g1 = tc::smem_u32(smem), g2 = g1 + B1, g2t = g1 + 2 * B1, g1t = g1 + 3 * B1, LO = B1 / 2;
+    auto bd = [&](uint32_t w, int k) { return tc::kmajor_desc(w + 256u * k, 128u, C * 16u); };
+    // D (+)= A W^T with A in tensor memory as [hi 8 | lo 8] column pairs per 16-wide k chunk
+    auto gemm_il = [&](uint32_t d, uint32_t a, uint32_t w, bool acc) {
+#pragma unroll 1
+      for (int k = 0; k < C / 16; ++k) mma3_ta(d, a + 16u * k, a + 16u * k + 8u, bd(w, k), bd(w + LO, k), id, acc || k > 0);
+    };
+    uint64_t* last = nullptr;
+    uint32_t last_par = 0;
+    bool alive = true;
+    for (int p = 0; p < npair && alive; ++p) {
+      const uint32_t par = (uint32_t)p & 1u;
+      const int nin = (2 * p + 1 < niter) ? 2 : 1;
+      for (int t = 0; t < nin && alive; ++t) {   // GEMM1: h = x G1^T (x as [hi C/2 | lo C/2])
+        if (!wait_or_flag(&a_full[t], par, err, 4)) { alive = false; break; }
+        tc::tc_after_sync();
+#pragma unroll 1
+        for (int k = 0; k < C / 16; ++k)
+          mma3_ta(RD1(t), RA(t) + 8u * k, RA(t) + C / 2 + 8u * k, bd(g1, k), bd(g1 + LO, k), id, k > 0);
+        tc::mma_commit(&d1_full[t]);
+        last = &d1_full[t];
+        last_par = par;
+      }
+      for (int t = 0; t < nin && alive; ++t) {   // GEMM2: s = H G2^T into the x region
+        if (!wait_or_flag(&h_full[t], par, err, 5)) { alive = false; break; }
+        tc::tc_after_sync();
+        gemm_il(RA(t), RH(t), g2, false);
+        tc::mma_commit(&d2_full[t]);
+        last = &d2_full[t];
+      }
+      for (int t = 0; t < nin && alive; ++t) {   // GEMM3: t = Q G2 into the x region
+        if (!wait_or_flag(&q_full[t], par, err, 6)) { alive = false; break; }
+        tc::tc_after_sync();
+        gemm_il(RA(t), RH(t), g2t, false);
+        tc::mma_commit(&d3_full[t]);
+        last = &d3_full[t];
+      }
+      for (int t = 0; t < nin && alive; ++t) {   // GEMM4: o += G G1
+        if (!wait_or_flag(&g_full[t], par, err, 11)) { alive = false; break; }
+        tc::tc_after_sync();
+        gemm_il(RD4(t), RH(t), g1t, true);
+        tc::mma_commit(&d4_full[t]);
+        last = &d4_full[t];
+      }
+    }
+    if (last) tc::mbar_wait_for(last, last_par, WAIT_NS);   // no MMA in flight when tensor memory is freed
+  } else if (ok && warp >= GW_CVT && warp < GW_E13) {
+    const int q = warp & 3, r = 32 * q + lane;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1, t = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!warp_wait(&stg_full[s], n & 1u, err, 7)) break;
+      if (!warp_wait(&ra_free[t], (n & 1u) ^ 1u, err, 8)) break;   // E3 of tile i-2 has read its t
+      tc::tc_after_sync();
+      const uint8_t* st = ring + s * SB;
+      const uint32_t A = RA(t) + lq;
+#pragma unroll 1
+      for (int bh = 0; bh < 2 * NB; ++bh) {
+        const uint8_t* rin = st + (bh >> 1) * BOX_BYTES + r * 128;
+        uint32_t hi[8], lo[8];
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+          const int c = 4 * (bh & 1) + cc;
+          const float4 v = *reinterpret_cast<const float4*>(rin + ((c ^ (r & 7)) << 4));
+          tc::split_pack(v.x, v.y, hi[2 * cc], lo[2 * cc]);
+          tc::split_pack(v.z, v.w, hi[2 * cc + 1], lo[2 * cc + 1]);
+        }
+        tc::tmem_st8u(A + (uint32_t)(8 * bh), hi);
+        tc::tmem_st8u(A + (uint32_t)(C / 2 + 8 * bh), lo);
+      }
+      tc::tmem_wait_st();
+      tc::tc_before_sync();
+      tc::mbar_arrive(&a_full[t]);
+    }
+  } else if (ok && warp >= GW_E13 && warp < GW_E24) {
+    const int q = warp & 3;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    bool alive = true;
+    for (int p = 0; p < npair && alive; ++p) {
+      const uint32_t par = (uint32_t)p & 1u;
+      const int nin = (2 * p + 1 < niter) ? 2 : 1;
+      for (int t = 0; t < nin && alive; ++t) {   // E1: H = gelu(h)
+        if (!warp_wait(&d1_full[t], par, err, 9)) { alive = false; break; }
+        tc::tc_after_sync();
+#pragma unroll 1
+        for (int k = 0; k < C / 16; ++k) {
+          uint32_t h[16];
+          tc::tmem_ld16u(RD1(t) + lq + 16u * k, h);
+          tc::tmem_wait_ld();
+          uint32_t hi[8], lo[8];
+#pragma unroll
+          for (int e = 0; e < 8; ++e)
+            tc::split_pack(gelu_tc(__uint_as_float(h[2 * e])), gelu_tc(__uint_as_float(h[2 * e + 1])), hi[e], lo[e]);
+          tc::tmem_st8u(RH(t) + lq + 16u * k, hi);
+          tc::tmem_st8u(RH(t) + lq + 16u * k + 8u, lo);
+        }
+        tc::tmem_wait_st();
+        tc::tc_before_sync();
+        tc::mbar_arrive(&h_full[t]);
+      }
+      for (int t = 0; t < nin && alive; ++t) {   // E3: G = t gelu'(h)
+        if (!warp_wait(&d3_full[t], par, err, 12)) { alive = false; break; }
+        tc::tc_after_sync();
+#pragma unroll 1
+        for (int k = 0; k < C / 16; ++k) {
+          uint32_t tv[16], h[16];
+          tc::tmem_ld16u(RA(t) + lq + 16u * k, tv);
+          tc::tmem_ld16u(RD1(t) + lq + 16u * k, h);
+          tc::tmem_wait_ld();
+          uint32_t hi[8], lo[8];
+#pragma unroll
+          for (int e = 0; e < 8; ++e)
+            tc::split_pack(__uint_as_float(tv[2 * e]) * gelu_grad_tc(__uint_as_float(h[2 * e])),
+                           __uint_as_float(tv[2 * e + 1]) * gelu_grad_tc(__uint_as_float(h[2 * e + 1])), hi[e], lo[e]);
+          tc::tmem_st8u(RH(t) + lq + 16u * k, hi);
+          tc::tmem_st8u(RH(t) + lq + 16u * k + 8u, lo);
+        }
+        tc::tmem_wait_st();
+        tc::tc_before_sync();
+        tc::mbar_arrive(&g_full[t]);
+        tc::mbar_arrive(&ra_free[t]);
+      }
+    }
+  } else if (ok && warp >= GW_E24) {
+    const int q = warp & 3, r = 32 * q + lane;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    bool alive = true;
+    for (int p = 0; p < npair && alive; ++p) {
+      const uint32_t par = (uint32_t)p & 1u;
+      const int nin = (2 * p + 1 < niter) ? 2 : 1;
+      for (int t = 0; t < nin && alive; ++t) {   // E2: the gate's local terms
+        const int i = 2 * p + t;
+        const long v = tile_of(i) * TM + r;
+        const bool live = v < V;
+        float4 bv[C / 4];
+#pragma unroll
+        for (int c = 0; c < C / 4; ++c)
+          bv[c] = (base && live) ? __ldg(reinterpret_cast<const float4*>(base + v * C) + c)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (!warp_wait(&d2_full[t], par, err, 10)) { alive = false; break; }
+        tc::tc_after_sync();
+        const uint8_t* st = ring + t * SB;   // stage of tile i (i & 1 == t)
+        float zs = 0.f;
+#pragma unroll
+        for (int k = 0; k < C / 16; ++k) {
+          uint32_t d[16];
+          tc::tmem_ld16u(RA(t) + lq + 16u * k, d);
+          tc::tmem_wait_ld();
+          float o[16];
+          uint32_t hi[8], lo[8];
+          const uint8_t* rx = st + (k >> 1) * BOX_BYTES + r * 128;
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) {
+            const uint32_t off = (uint32_t)(((4 * (k & 1) + cc) ^ (r & 7)) << 4);
+            const float4 xv = *reinterpret_cast<const float4*>(rx + off);
+            const float4 gv = *reinterpret_cast<const float4*>(rx + XB + off);
+            const float xx[4] = {xv.x, xv.y, xv.z, xv.w}, gg[4] = {gv.x, gv.y, gv.z, gv.w};
+            const float4 b4 = bv[4 * k + cc];
+            const float bb[4] = {b4.x, b4.y, b4.z, b4.w};
+            float qv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const float sg = sigmoid_tc(__uint_as_float(d[4 * cc + u]));
+              o[4 * cc + u] = fmaf(gg[u], sg, bb[u]);
+              qv[u] = gg[u] * xx[u] * sg * (1.f - sg);
+              if (zp) zs = fmaf(gg[u], __ldg(zp + 16 * k + 4 * cc + u), zs);
+            }
+            tc::split_pack(qv[0], qv[1], hi[2 * cc], lo[2 * cc]);
+            tc::split_pack(qv[2], qv[3], hi[2 * cc + 1], lo[2 * cc + 1]);
+          }
+          tc::tmem_st16(RD4(t) + lq + 16u * k, o);
+          tc::tmem_st8u(RH(t) + lq + 16u * k, hi);
+          tc::tmem_st8u(RH(t) + lq + 16u * k + 8u, lo);
+        }
+        tc::tmem_wait_st();
+        tc::mbar_arrive(&stg_empty[t]);
+        tc::tc_before_sync();
+        tc::mbar_arrive(&q_full[t]);
+        if (zp && live) zbar[v] += zs;
+      }
+      for (int t = 0; t < nin && alive; ++t) {   // E4: x_bar
+        const int i = 2 * p + t;
+        const long v = tile_of(i) * TM + r;
+        if (!warp_wait(&d4_full[t], par, err, 13)) { alive = false; break; }
+        tc::tc_after_sync();
+#pragma unroll
+        for (int k = 0; k < C / 16; ++k) {
+          uint32_t d[16];
+          tc::tmem_ld16u(RD4(t) + lq + 16u * k, d);
+          tc::tmem_wait_ld();
+          if (v < V) {
+            float4* o = reinterpret_cast<float4*>(xbar + v * C + 16 * k);
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              o[e] = make_float4(__uint_as_float(d[4 * e]), __uint_as_float(d[4 * e + 1]),
+                                 __uint_as_float(d[4 * e + 2]), __uint_as_float(d[4 * e + 3]));
+          }
+        }
+      }
+    }
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  if (warp == 0) tc::tmem_free(tmem, 512);
+}
+
 int g_sms = 0;
 int sms() {
   if (!g_sms) {
@@ -887,10 +1186,37 @@ int launch_gate_fwd(const float* x, long V, const void* wpack, const float* zp, 
   return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
 }
 
+template <int C>
+int launch_gate_bwd(const float* x, const float* gbar, const float* base, long V, const void* wpack, const float* zp,
+                    float* xbar, float* zbar, int* err, cudaStream_t s) {
+  CUtensorMap mx, mg;
+  if (!row_map(&mx, x, V, C) || !row_map(&mg, gbar, V, C)) return FFNO_EINVAL;
+  const size_t smem = 1024 + 4 * (size_t)mat_bytes(C, C) + 2 * (size_t)(2 * (C / 32) * BOX_BYTES);
+  if (cudaFuncSetAttribute(k_gate_bwd_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return FFNO_ELAUNCH;
+  const long nt = (V + TM - 1) / TM;
+  const int grid = (int)(nt < sms() ? nt : sms());
+  k_gate_bwd_ws<C><<<grid, 448, smem, s>>>(mx, mg, base, V, static_cast<const uint8_t*>(wpack), zp, xbar, zbar, err);
+  return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
+}
+
 }  // namespace
 
 namespace ffno {
 namespace ws {
+
+bool gate_bwd_supported(int C) { return C == 32 || C == 64; }
+
+int gate_bwd(const float* x, const float* g_bar, const float* base, long V, int C, const void* wpack, const float* zp,
+             float* x_bar, float* z_bar, int* err, cudaStream_t stream) {
+  if (V < 1 || V > 0x7fffffffL - TM ||
+      (reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(g_bar) | reinterpret_cast<uintptr_t>(x_bar)) % 16 ||
+      (base && reinterpret_cast<uintptr_t>(base) % 16))
+    return FFNO_EINVAL;
+  if (C == 64) return launch_gate_bwd<64>(x, g_bar, base, V, wpack, zp, x_bar, z_bar, err, stream);
+  if (C == 32) return launch_gate_bwd<32>(x, g_bar, base, V, wpack, zp, x_bar, z_bar, err, stream);
+  return FFNO_EINVAL;
+}
 
 bool gate_fwd_supported(int C) { return C == 32 || C == 64; }
 

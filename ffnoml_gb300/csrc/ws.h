@@ -13,6 +13,9 @@ int mlp2_fwd(int mode, const float* in, const float* prev_pre, const float* prev
 bool gate_fwd_supported(int C);
 int gate_fwd(const float* x, long V, int C, const void* wpack, const float* zp, const float* z, float* out, int* err,
              cudaStream_t stream);
+bool gate_bwd_supported(int C);
+int gate_bwd(const float* x, const float* g_bar, const float* base, long V, int C, const void* wpack, const float* zp,
+             float* x_bar, float* z_bar, int* err, cudaStream_t stream);
 bool mlp2_bwd_supported(int C);
 int mlp2_bwd(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack, float* a_bar,
              int* err, cudaStream_t stream);

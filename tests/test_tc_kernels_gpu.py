@@ -171,8 +171,10 @@ def test_mlp2_bwd_tc(C, V):
     _close(r1, r0)
 
 
-@pytest.mark.parametrize("C", [16, 32, 64])
-def test_gate_bwd_tc(C):
+@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (32, 2 * 128 + 5), (64, 152 * 128 * 5 + 77)])
+def test_gate_bwd_tc(C, V):
+    """Widths 32 and 64 run the warp-specialised kernel (tiles in pairs): also one CTA with an odd tile count and
+    every CTA with a ragged last pair; the second call writes x_bar over its own base."""
     nat = _nat()
     x, xsb, xvb, base = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3), _rand(V, C, seed=4)
     s1, s2 = _rand(C, C, seed=5, scale=C ** -0.5), _rand(C, C, seed=6, scale=C ** -0.5)
