@@ -1406,6 +1406,9 @@ int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* v
                   int nparts, int groups, int* err, ffno_stream_t stream) {
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || groups != GMAX || nparts != grid_tc(V)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
+  if (ws::fuse2_supported(C))
+    return ws::fuse2(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, V, C, wpack, dw, pre, partials, nparts, err,
+                     s);
   TC_DISPATCH(C, {
     const size_t smem = mat_bytes(2 * CC, 2 * CC) + mat_bytes(CC, 2 * CC) + 2 * tile_bytes(2 * CC);
     if (!launch_prep(k_fuse2_tc<CC>, smem)) return FFNO_ELAUNCH;

@@ -819,6 +819,326 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) tc::tmem_free(tmem, 512);
 }
 
+// ================================================================================================ fuse, second half
+// The ffno_fuse2_tc contract: B = [gelu(GN_s(spec_pre)) g_s, gelu(GN_v(vert_pre)) g_v] (g = the branch gates [V][2C]),
+// pre = gelu(B Wf1^T) Wf2^T + (B[:, :C] + B[:, C:]) / 2, with the depth-weighted GroupNorm partials of pre.
+// Roles: warp 0 TMA: per tile 2 NB phases of 32 channels (spec_pre boxes, then vert_pre boxes), each a pre box and the
+// matching gates box, through a three-stage ring; warp 1 MMA: GEMM1 D1 = B Wf1^T (N = K = 2C) and, one tile behind,
+// GEMM2 D2 += H Wf2^T (N = C); warps 2-5 conversion: B split into the tile's A stage and the FP32 residual
+// (B[:, c] + B[:, C + c]) / 2 into its D2 buffer (GEMM2 accumulates onto it); warps 6-13 epilogue 1: H = gelu(D1),
+// split over D1; warps 14-17 epilogue 2: pre and its statistics, as in the forward MLP. Tensor memory (8C columns):
+// A stages at 0 and 2C, D1 at 4C, D2 buffers at 6C and 7C.
+template <int C>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_fuse2_ws(const __grid_constant__ CUtensorMap map_sp, const __grid_constant__ CUtensorMap map_vp,
+               const __grid_constant__ CUtensorMap map_g, const float* __restrict__ sc, const float* __restrict__ vc,
+               long V, const uint8_t* __restrict__ wpack, const float* __restrict__ dw, float* __restrict__ pre,
+               double* __restrict__ partials, int* __restrict__ err) {
+  static_assert(C == 32 || C == 64, "widths 32 and 64");
+  constexpr uint32_t B1 = mat_bytes(2 * C, 2 * C), B2 = mat_bytes(C, 2 * C);
+  constexpr uint32_t WB = B1 + B2;
+  constexpr int NB = C / 32, NPH = 2 * NB, NS = 3, CPG = C / GMAX;
+  constexpr uint32_t SB = 2 * BOX_BYTES;         // one ring stage: a pre box and its gates box
+  constexpr uint32_t TA = 0, TD1 = 4 * C, TD2 = 6 * C;
+  static_assert(WB % 1024 == 0, "the ring must stay 1024-byte aligned (128-byte swizzle)");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint8_t* ring = smem + WB;
+  __shared__ uint64_t stg_full[NS], stg_empty[NS], a_full[2], a_empty[2], d2_free[2], d2_full[2], d1_full, h_full,
+      wbar;
+  __shared__ uint32_t tslot;
+  __shared__ float cf[2][3 * C];              // GroupNorm coefficients of spec and vert: mean, gamma rstd, beta
+  __shared__ float red[4][GMAX + 1], gmean[GMAX], wsum;
+  __shared__ double acc[GMAX * 3];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) tc::tmem_alloc(&tslot, 512);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; ++s) {
+      tc::mbar_init(&stg_full[s], 1);
+      tc::mbar_init(&stg_empty[s], 128);
+    }
+    for (int s = 0; s < 2; ++s) {
+      tc::mbar_init(&a_full[s], 128);
+      tc::mbar_init(&a_empty[s], 1);
+      tc::mbar_init(&d2_free[s], 128);
+      tc::mbar_init(&d2_full[s], 1);
+    }
+    tc::mbar_init(&d1_full, 1);
+    tc::mbar_init(&h_full, 256);
+    tc::mbar_init(&wbar, 1);
+    tc::mbar_init_fence();
+  }
+  for (int e = threadIdx.x; e < 3 * C; e += NTHREADS) {
+    cf[0][e] = sc[e];
+    cf[1][e] = vc[e];
+  }
+  if (threadIdx.x < GMAX * 3) acc[threadIdx.x] = 0.0;
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  const uint32_t tmem = tslot;
+  if (threadIdx.x == 0) {
+    tc::mbar_arrive_expect_tx(&wbar, WB);
+    for (uint32_t off = 0; off < WB; off += 32768u)
+      tc::bulk_g2s(smem + off, wpack + off, WB - off < 32768u ? WB - off : 32768u, &wbar);
+  }
+  const bool ok = __syncthreads_and(tc::mbar_wait_for(&wbar, 0, WAIT_NS)) != 0;
+  if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+
+  const long nt = (V + TM - 1) / TM;
+  const int niter = (long)blockIdx.x < nt ? (int)((nt - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  auto tile_of = [&](int i) { return (long)blockIdx.x + (long)i * gridDim.x; };
+
+  if (ok && warp == W_TMA && lane == 0) {
+    int issued[NS] = {0, 0, 0};
+    bool alive = true;
+    for (int i = 0; i < niter && alive; ++i) {
+      const int row = (int)(tile_of(i) * TM);
+      for (int ph = 0; ph < NPH; ++ph) {
+        const int u = i * NPH + ph, st = u % NS;
+        const uint32_t n = (uint32_t)(u / NS);
+        if (!wait_or_flag(&stg_empty[st], (n & 1u) ^ 1u, err, 3)) {
+          alive = false;
+          break;
+        }
+        tc::mbar_arrive_expect_tx(&stg_full[st], SB);
+        uint8_t* sp = ring + st * SB;
+        tc::tma_load_2d(sp, ph < NB ? &map_sp : &map_vp, 32 * (ph % NB), row, &stg_full[st]);
+        tc::tma_load_2d(sp + BOX_BYTES, &map_g, 32 * ph, row, &stg_full[st]);
+        ++issued[st];
+      }
+    }
+    for (int s = 0; s < NS; ++s)
+      if (issued[s]) tc::mbar_wait_for(&stg_full[s], (uint32_t)(issued[s] - 1) & 1u, WAIT_NS);
+  } else if (ok && warp == W_MMA && lane == 0) {
+    const uint32_t i1 = tc::idesc_bf16(128, 2 * C), i2 = tc::idesc_bf16(128, C);
+    const uint32_t w1 = tc::smem_u32(smem), w2 = w1 + B1;
+    uint64_t* last = nullptr;
+    uint32_t last_par = 0;
+    bool alive = true;
+    auto gemm2 = [&](int j) {   // D2[j % 2] += H(j) Wf2^T, H in D1 as [hi 8 | lo 8] per 16-wide k chunk, K = 2C
+#pragma unroll 1
+      for (int k = 0; k < 2 * C / 16; ++k)
+        mma3_ta(tmem + TD2 + (uint32_t)(C * (j & 1)), tmem + TD1 + 16u * k, tmem + TD1 + 16u * k + 8u,
+                tc::kmajor_desc(w2 + 256u * k, 128u, 2 * C * 16u),
+                tc::kmajor_desc(w2 + B2 / 2 + 256u * k, 128u, 2 * C * 16u), i2, true);
+      tc::mma_commit(&d2_full[j & 1]);
+      last = &d2_full[j & 1];
+      last_par = ((uint32_t)j >> 1) & 1u;
+    };
+    for (int i = 0; i < niter && alive; ++i) {
+      const int s = i & 1;
+      if (!wait_or_flag(&a_full[s], ((uint32_t)i >> 1) & 1u, err, 4)) {
+        alive = false;
+        break;
+      }
+      if (i >= 1) {   // GEMM2 of the previous tile reads D1 before GEMM1 of this one overwrites it
+        if (!wait_or_flag(&h_full, (uint32_t)(i - 1) & 1u, err, 5)) {
+          alive = false;
+          break;
+        }
+        tc::tc_after_sync();
+        gemm2(i - 1);
+      }
+      tc::tc_after_sync();
+      const uint32_t A = tmem + TA + (uint32_t)(2 * C * s);
+#pragma unroll 1
+      for (int k = 0; k < 2 * C / 16; ++k)
+        mma3_ta(tmem + TD1, A + 8u * k, A + C + 8u * k, tc::kmajor_desc(w1 + 256u * k, 128u, 2 * C * 16u),
+                tc::kmajor_desc(w1 + B1 / 2 + 256u * k, 128u, 2 * C * 16u), i1, k > 0);
+      tc::mma_commit(&d1_full);
+      tc::mma_commit(&a_empty[s]);
+      last = &a_empty[s];
+      last_par = ((uint32_t)i >> 1) & 1u;
+    }
+    if (alive && niter >= 1) {
+      const int j = niter - 1;
+      if (wait_or_flag(&h_full, (uint32_t)j & 1u, err, 6)) {
+        tc::tc_after_sync();
+        gemm2(j);
+      }
+    }
+    if (last) tc::mbar_wait_for(last, last_par, WAIT_NS);   // no MMA in flight when tensor memory is freed
+  } else if (ok && warp >= W_CVT && warp < W_E1) {
+    const int q = warp & 3, r = 32 * q + lane;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    bool alive = true;
+    for (int i = 0; i < niter && alive; ++i) {
+      const int s = i & 1;
+      const uint32_t n2 = ((uint32_t)i >> 1) & 1u;
+      if (!warp_wait(&a_empty[s], n2 ^ 1u, err, 7)) break;    // GEMM1 of tile i-2 has read the A stage
+      if (!warp_wait(&d2_free[s], n2 ^ 1u, err, 8)) break;    // epilogue 2 of tile i-2 has read D2[s]
+      tc::tc_after_sync();
+      const uint32_t A = tmem + lq + TA + (uint32_t)(2 * C * s), D2 = tmem + lq + TD2 + (uint32_t)(C * s);
+      for (int ph = 0; ph < NPH; ++ph) {
+        const int u = i * NPH + ph, st = u % NS;
+        if (!warp_wait(&stg_full[st], (uint32_t)(u / NS) & 1u, err, 12)) {
+          alive = false;
+          break;
+        }
+        const int br = ph / NB, c0 = 32 * (ph % NB);   // branch (0 spec, 1 vert) and its first channel
+        const float* k = cf[br];
+        const uint8_t* rp = ring + st * SB + r * 128;
+        float b[32];
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+          const uint32_t o = (uint32_t)((cc ^ (r & 7)) << 4);
+          const float4 p = *reinterpret_cast<const float4*>(rp + o);
+          const float4 g = *reinterpret_cast<const float4*>(rp + BOX_BYTES + o);
+          const float pp[4] = {p.x, p.y, p.z, p.w}, gg[4] = {g.x, g.y, g.z, g.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int c = c0 + 4 * cc + e;
+            b[4 * cc + e] = gelu_tc((pp[e] - k[c]) * k[C + c] + k[2 * C + c]) * gg[e];
+          }
+        }
+        tc::mbar_arrive(&stg_empty[st]);
+        uint32_t hi[16], lo[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) tc::split_pack(b[2 * e], b[2 * e + 1], hi[e], lo[e]);
+        const uint32_t kc = (uint32_t)((br * C + c0) / 2);   // first column of this phase's channel pairs
+        tc::tmem_st16u(A + kc, hi);
+        tc::tmem_st16u(A + (uint32_t)C + kc, lo);
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {   // residual (B[c] + B[C + c]) / 2 in D2
+          float rr[16];
+          if (br == 0) {
+#pragma unroll
+            for (int e = 0; e < 16; ++e) rr[e] = 0.5f * b[16 * hh + e];
+          } else {
+            tc::tmem_ld16(D2 + (uint32_t)(c0 + 16 * hh), rr);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) rr[e] = fmaf(0.5f, b[16 * hh + e], rr[e]);
+          }
+          tc::tmem_st16(D2 + (uint32_t)(c0 + 16 * hh), rr);
+        }
+      }
+      if (!alive) break;
+      tc::tmem_wait_st();
+      tc::tc_before_sync();
+      tc::mbar_arrive(&a_full[s]);
+    }
+  } else if (ok && warp >= W_E1 && warp < W_E2) {
+    const int q = warp & 3, hf = (warp - W_E1) >> 2;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      if (!warp_wait(&d1_full, (uint32_t)i & 1u, err, 9)) break;
+      tc::tc_after_sync();
+      const uint32_t D = tmem + lq + TD1;
+#pragma unroll 1
+      for (int j = hf; j < 2 * C / 16; j += 2) {
+        uint32_t h[16];
+        tc::tmem_ld16u(D + 16u * j, h);
+        tc::tmem_wait_ld();
+        uint32_t hi[8], lo[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          tc::split_pack(gelu_tc(__uint_as_float(h[2 * e])), gelu_tc(__uint_as_float(h[2 * e + 1])), hi[e], lo[e]);
+        tc::tmem_st8u(D + 16u * j, hi);
+        tc::tmem_st8u(D + 16u * j + 8u, lo);
+      }
+      tc::tmem_wait_st();
+      tc::tc_before_sync();
+      tc::mbar_arrive(&h_full);
+    }
+  } else if (ok && warp >= W_E2) {
+    const int q = warp & 3, r = 32 * q + lane, wl = warp - W_E2;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const long v = tile_of(i) * TM + r;
+      const bool live = v < V;
+      const float w = live ? __ldg(dw + v) : 0.f;
+      if (!e2_sync_and(tc::mbar_wait_for(&d2_full[s], ((uint32_t)i >> 1) & 1u, WAIT_NS))) {
+        if (lane == 0) atomicExch(err, 10);
+        break;
+      }
+      tc::tc_after_sync();
+      const uint32_t D = tmem + lq + TD2 + (uint32_t)(C * s);
+      float gs[GMAX];
+#pragma unroll
+      for (int k = 0; k < C / 16; ++k) {
+        uint32_t d[16];
+        tc::tmem_ld16u(D + 16u * k, d);
+        tc::tmem_wait_ld();
+        if (live)
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            *reinterpret_cast<float4*>(pre + v * C + 16 * k + 4 * e) =
+                make_float4(__uint_as_float(d[4 * e]), __uint_as_float(d[4 * e + 1]), __uint_as_float(d[4 * e + 2]),
+                            __uint_as_float(d[4 * e + 3]));
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          const int g = (16 * k + e) / CPG;
+          if (e % CPG == 0) gs[g] = 0.f;
+          gs[g] += __uint_as_float(d[e]);
+        }
+      }
+      float ws = w;
+#pragma unroll
+      for (int m = 16; m; m >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, m);
+#pragma unroll
+      for (int g = 0; g < GMAX; ++g) {
+        float t = w * gs[g];
+#pragma unroll
+        for (int m = 16; m; m >>= 1) t += __shfl_xor_sync(0xffffffffu, t, m);
+        if (lane == 0) red[wl][g] = t;
+      }
+      if (lane == 0) red[wl][GMAX] = ws;
+      e2_sync();
+      if (threadIdx.x - 32 * W_E2 < GMAX) {
+        const int g = threadIdx.x - 32 * W_E2;
+        const float wt = ((red[0][GMAX] + red[1][GMAX]) + (red[2][GMAX] + red[3][GMAX])) * CPG;
+        gmean[g] = wt > 0.f ? ((red[0][g] + red[1][g]) + (red[2][g] + red[3][g])) / wt : 0.f;
+        if (g == 0) wsum = wt;
+      }
+      e2_sync();
+#pragma unroll
+      for (int k = 0; k < C / 16; ++k) {
+        uint32_t d[16];
+        tc::tmem_ld16u(D + 16u * k, d);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          const int g = (16 * k + e) / CPG;
+          if (e % CPG == 0) gs[g] = 0.f;
+          const float x = __uint_as_float(d[e]) - gmean[g];
+          gs[g] = fmaf(x, x, gs[g]);
+        }
+      }
+      tc::tc_before_sync();
+      tc::mbar_arrive(&d2_free[s]);   // D2[s] has been read: conversion may write the residual of tile i + 2
+#pragma unroll
+      for (int g = 0; g < GMAX; ++g) {
+        float t = w * gs[g];
+#pragma unroll
+        for (int m = 16; m; m >>= 1) t += __shfl_xor_sync(0xffffffffu, t, m);
+        if (lane == 0) red[wl][g] = t;
+      }
+      e2_sync();
+      if (threadIdx.x - 32 * W_E2 < GMAX) {
+        const int g = threadIdx.x - 32 * W_E2;
+        GroupAcc a{acc[3 * g], acc[3 * g + 1], acc[3 * g + 2]};
+        chan_merge(a, (double)wsum, (double)gmean[g], (double)((red[0][g] + red[1][g]) + (red[2][g] + red[3][g])));
+        acc[3 * g] = a.w;
+        acc[3 * g + 1] = a.mean;
+        acc[3 * g + 2] = a.m2;
+      }
+      e2_sync();
+    }
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  if (threadIdx.x < GMAX) {
+    double* o = partials + ((long)blockIdx.x * GMAX + threadIdx.x) * 3;
+    o[0] = acc[3 * threadIdx.x];
+    o[1] = acc[3 * threadIdx.x + 1];
+    o[2] = acc[3 * threadIdx.x + 2];
+  }
+  if (warp == 0) tc::tmem_free(tmem, 512);
+}
+
 // ============================================================================================ input gate, VJP
 // The ffno_gate_bwd_tc contract: x_bar = base + d/dx [x sigmoid(gelu(x G1^T) G2^T)] applied to g_bar, z_bar[v] +=
 // g_bar . zp when zp. Per tile (lane = voxel, all products untransposed, K = N = C):
@@ -1200,10 +1520,42 @@ int launch_gate_bwd(const float* x, const float* gbar, const float* base, long V
   return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
 }
 
+template <int C>
+int launch_fuse2(const float* sp, const float* sc, const float* vp, const float* vc, const float* gates, long V,
+                 const void* wpack, const float* dw, float* pre, double* partials, int nparts, int* err,
+                 cudaStream_t s) {
+  CUtensorMap ms, mv, mg;
+  if (!row_map(&ms, sp, V, C) || !row_map(&mv, vp, V, C) || !row_map(&mg, gates, V, 2 * C)) return FFNO_EINVAL;
+  const size_t smem = 1024 + (size_t)mat_bytes(2 * C, 2 * C) + mat_bytes(C, 2 * C) + 3 * (size_t)(2 * BOX_BYTES);
+  if (cudaFuncSetAttribute(k_fuse2_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return FFNO_ELAUNCH;
+  k_fuse2_ws<C><<<nparts, NTHREADS, smem, s>>>(ms, mv, mg, sc, vc, V, static_cast<const uint8_t*>(wpack), dw, pre,
+                                                partials, err);
+  return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
+}
+
 }  // namespace
 
 namespace ffno {
 namespace ws {
+
+bool fuse2_supported(int C) { return C == 32 || C == 64; }
+
+int fuse2(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
+          const float* gates, long V, int C, const void* wpack, const float* dw, float* pre, double* partials,
+          int nparts, int* err, cudaStream_t stream) {
+  if (V < 1 || V > 0x7fffffffL - TM || nparts < 1 ||
+      (reinterpret_cast<uintptr_t>(spec_pre) | reinterpret_cast<uintptr_t>(vert_pre) |
+       reinterpret_cast<uintptr_t>(gates) | reinterpret_cast<uintptr_t>(pre)) % 16)
+    return FFNO_EINVAL;
+  if (C == 64)
+    return launch_fuse2<64>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, V, wpack, dw, pre, partials, nparts,
+                            err, stream);
+  if (C == 32)
+    return launch_fuse2<32>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, V, wpack, dw, pre, partials, nparts,
+                            err, stream);
+  return FFNO_EINVAL;
+}
 
 bool gate_bwd_supported(int C) { return C == 32 || C == 64; }
 

@@ -128,8 +128,9 @@ def _fuse_weights(C):
             _rand(C, 2 * C, seed=15, scale=(2 * C) ** -0.5))
 
 
-@pytest.mark.parametrize("C", [16, 32, 64])
-def test_fuse_fwd_tc(C):
+@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (32, 152 * 128 * 3 + 77), (64, 152 * 128 * 5 + 77)])
+def test_fuse_fwd_tc(C, V):
+    """fuse2 at widths 32 and 64 is the warp-specialised kernel (three-stage ring of 32-channel phases)."""
     nat = _nat()
     x, sp, vp = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3)
     sc, vc = _coefs(C, 4), _coefs(C, 5)
