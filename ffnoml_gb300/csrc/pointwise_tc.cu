@@ -1391,6 +1391,8 @@ int ffno_fuse1_tc(const float* x, const float* spec_pre, const float* spec_coefs
                   float* hg, int* err, ffno_stream_t stream) {
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || !gates) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
+  if (ws::fuse1_supported(C))
+    return ws::fuse1(x, spec_pre, spec_coefs, vert_pre, vert_coefs, V, C, wpack, bias, gates, hg, err, s);
   TC_DISPATCH(C, {
     const size_t smem = mat_bytes(CC, 3 * CC) + mat_bytes(2 * CC, CC) + 2 * tile_bytes(CC);
     if (!launch_prep(k_fuse1_tc<CC>, smem)) return FFNO_ELAUNCH;

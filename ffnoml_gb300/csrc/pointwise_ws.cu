@@ -819,6 +819,255 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) tc::tmem_free(tmem, 512);
 }
 
+// ================================================================================================ fuse, first half
+// The ffno_fuse1_tc contract: gates [V][2C] = sigmoid(gelu(A Wg1^T) Wg2^T + bias), A = [x, gelu(GN_s(spec_pre)),
+// gelu(GN_v(vert_pre))] (K = 3C), and hg [V][C] = A Wg1^T when hg is not NULL. Roles as in the forward MLP: warp 0 TMA,
+// 3 NB phases of 32 channels per tile (x, spec_pre, vert_pre boxes) through a four-stage ring; warp 1 MMA: GEMM1
+// D1[t % 2] = A Wg1^T (N = C), and GEMM2 D2 = H Wg2^T (N = 2C) one tile behind, over the tile's A stage; warps 2-5
+// conversion; warps 6-13 epilogue 1: hg to HBM, H = gelu(D1) split over D1; warps 14-17 epilogue 2: the gates.
+// Tensor memory: A stages of 3C columns at 0 and 3C, D1 buffers at 6C and 7C.
+template <int C>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_fuse1_ws(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_sp,
+               const __grid_constant__ CUtensorMap map_vp, const float* __restrict__ sc, const float* __restrict__ vc,
+               long V, const uint8_t* __restrict__ wpack, const float* __restrict__ bias, float* __restrict__ gates,
+               float* __restrict__ hg, int* __restrict__ err) {
+  static_assert(C == 32 || C == 64, "widths 32 and 64");
+  constexpr uint32_t B1 = mat_bytes(C, 3 * C), B2 = mat_bytes(2 * C, C);
+  constexpr uint32_t WB = B1 + B2;
+  constexpr int NB = C / 32, NPH = 3 * NB, NS = 4;
+  constexpr uint32_t SB = BOX_BYTES;             // one ring stage: one box
+  constexpr uint32_t TD1 = 6 * C;
+  static_assert(WB % 1024 == 0, "the ring must stay 1024-byte aligned (128-byte swizzle)");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint8_t* ring = smem + WB;
+  __shared__ uint64_t stg_full[NS], stg_empty[NS], a_full[2], a_empty[2], d1_full[2], h_full[2], d2_full[2], wbar;
+  __shared__ uint32_t tslot;
+  __shared__ float cf[2][3 * C], bs[2 * C];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) tc::tmem_alloc(&tslot, 512);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; ++s) {
+      tc::mbar_init(&stg_full[s], 1);
+      tc::mbar_init(&stg_empty[s], 128);
+    }
+    for (int s = 0; s < 2; ++s) {
+      tc::mbar_init(&a_full[s], 128);
+      tc::mbar_init(&a_empty[s], 128);
+      tc::mbar_init(&d1_full[s], 1);
+      tc::mbar_init(&h_full[s], 256);
+      tc::mbar_init(&d2_full[s], 1);
+    }
+    tc::mbar_init(&wbar, 1);
+    tc::mbar_init_fence();
+  }
+  for (int e = threadIdx.x; e < 3 * C; e += NTHREADS) {
+    cf[0][e] = sc[e];
+    cf[1][e] = vc[e];
+  }
+  for (int e = threadIdx.x; e < 2 * C; e += NTHREADS) bs[e] = bias[e];
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  const uint32_t tmem = tslot;
+  if (threadIdx.x == 0) {
+    tc::mbar_arrive_expect_tx(&wbar, WB);
+    for (uint32_t off = 0; off < WB; off += 32768u)
+      tc::bulk_g2s(smem + off, wpack + off, WB - off < 32768u ? WB - off : 32768u, &wbar);
+  }
+  const bool ok = __syncthreads_and(tc::mbar_wait_for(&wbar, 0, WAIT_NS)) != 0;
+  if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+
+  const long nt = (V + TM - 1) / TM;
+  const int niter = (long)blockIdx.x < nt ? (int)((nt - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  auto tile_of = [&](int i) { return (long)blockIdx.x + (long)i * gridDim.x; };
+
+  if (ok && warp == W_TMA && lane == 0) {
+    int issued[NS] = {0, 0, 0, 0};
+    bool alive = true;
+    for (int i = 0; i < niter && alive; ++i) {
+      const int row = (int)(tile_of(i) * TM);
+      for (int ph = 0; ph < NPH; ++ph) {
+        const int u = i * NPH + ph, st = u % NS;
+        const uint32_t n = (uint32_t)(u / NS);
+        if (!wait_or_flag(&stg_empty[st], (n & 1u) ^ 1u, err, 3)) {
+          alive = false;
+          break;
+        }
+        tc::mbar_arrive_expect_tx(&stg_full[st], SB);
+        const int t = ph / NB;
+        tc::tma_load_2d(ring + st * SB, t == 0 ? &map_x : (t == 1 ? &map_sp : &map_vp), 32 * (ph % NB), row,
+                        &stg_full[st]);
+        ++issued[st];
+      }
+    }
+    for (int s = 0; s < NS; ++s)
+      if (issued[s]) tc::mbar_wait_for(&stg_full[s], (uint32_t)(issued[s] - 1) & 1u, WAIT_NS);
+  } else if (ok && warp == W_MMA && lane == 0) {
+    const uint32_t i1 = tc::idesc_bf16(128, C), i2 = tc::idesc_bf16(128, 2 * C);
+    const uint32_t w1 = tc::smem_u32(smem), w2 = w1 + B1;
+    uint64_t* last = nullptr;
+    uint32_t last_par = 0;
+    bool alive = true;
+    auto gemm2 = [&](int j) {   // D2 (over A stage j % 2) = H(j) Wg2^T, H in D1[j % 2] as [hi 8 | lo 8], K = C
+      const uint32_t h = tmem + TD1 + (uint32_t)(C * (j & 1));
+#pragma unroll 1
+      for (int k = 0; k < C / 16; ++k)
+        mma3_ta(tmem + (uint32_t)(3 * C * (j & 1)), h + 16u * k, h + 16u * k + 8u,
+                tc::kmajor_desc(w2 + 256u * k, 128u, C * 16u), tc::kmajor_desc(w2 + B2 / 2 + 256u * k, 128u, C * 16u),
+                i2, k > 0);
+      tc::mma_commit(&d2_full[j & 1]);
+      last = &d2_full[j & 1];
+      last_par = ((uint32_t)j >> 1) & 1u;
+    };
+    for (int i = 0; i < niter && alive; ++i) {
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
+      if (!wait_or_flag(&a_full[s], n & 1u, err, 4)) {
+        alive = false;
+        break;
+      }
+      if (i >= 2 && !wait_or_flag(&d2_full[s], ((uint32_t)(i - 2) >> 1) & 1u, err, 11)) {
+        alive = false;   // GEMM2 of tile i-2, the last reader of D1[s], has completed
+        break;
+      }
+      tc::tc_after_sync();
+      const uint32_t A = tmem + (uint32_t)(3 * C * s), D = tmem + TD1 + (uint32_t)(C * s);
+#pragma unroll 1
+      for (int k = 0; k < 3 * C / 16; ++k)
+        mma3_ta(D, A + 8u * k, A + 3 * C / 2 + 8u * k, tc::kmajor_desc(w1 + 256u * k, 128u, 3 * C * 16u),
+                tc::kmajor_desc(w1 + B1 / 2 + 256u * k, 128u, 3 * C * 16u), i1, k > 0);
+      tc::mma_commit(&d1_full[s]);
+      last = &d1_full[s];
+      last_par = n & 1u;
+      if (i >= 1) {
+        if (!wait_or_flag(&h_full[(i - 1) & 1], ((uint32_t)(i - 1) >> 1) & 1u, err, 5)) { alive = false; break; }
+        tc::tc_after_sync();
+        gemm2(i - 1);
+      }
+    }
+    if (alive && niter >= 1) {
+      const int j = niter - 1;
+      if (wait_or_flag(&h_full[j & 1], ((uint32_t)j >> 1) & 1u, err, 6)) {
+        tc::tc_after_sync();
+        gemm2(j);
+      }
+    }
+    if (last) tc::mbar_wait_for(last, last_par, WAIT_NS);   // no MMA in flight when tensor memory is freed
+  } else if (ok && warp >= W_CVT && warp < W_E1) {
+    const int q = warp & 3, r = 32 * q + lane;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    bool alive = true;
+    for (int i = 0; i < niter && alive; ++i) {
+      const int s = i & 1;
+      if (!warp_wait(&a_empty[s], (((uint32_t)i >> 1) & 1u) ^ 1u, err, 7)) break;   // D2 of tile i-2 read
+      tc::tc_after_sync();
+      const uint32_t A = tmem + lq + (uint32_t)(3 * C * s);
+      for (int ph = 0; ph < NPH; ++ph) {
+        const int u = i * NPH + ph, st = u % NS;
+        if (!warp_wait(&stg_full[st], (uint32_t)(u / NS) & 1u, err, 8)) {
+          alive = false;
+          break;
+        }
+        const int t = ph / NB, c0 = 32 * (ph % NB);
+        const uint8_t* rp = ring + st * SB + r * 128;
+        uint32_t hi[16], lo[16];
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+          const float4 p = *reinterpret_cast<const float4*>(rp + ((cc ^ (r & 7)) << 4));
+          float y[4] = {p.x, p.y, p.z, p.w};
+          if (t > 0) {
+            const float* k = cf[t - 1];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int c = c0 + 4 * cc + e;
+              y[e] = gelu_tc((y[e] - k[c]) * k[C + c] + k[2 * C + c]);
+            }
+          }
+          tc::split_pack(y[0], y[1], hi[2 * cc], lo[2 * cc]);
+          tc::split_pack(y[2], y[3], hi[2 * cc + 1], lo[2 * cc + 1]);
+        }
+        tc::mbar_arrive(&stg_empty[st]);
+        const uint32_t kc = (uint32_t)((t * C + c0) / 2);
+        tc::tmem_st16u(A + kc, hi);
+        tc::tmem_st16u(A + (uint32_t)(3 * C / 2) + kc, lo);
+      }
+      if (!alive) break;
+      tc::tmem_wait_st();
+      tc::tc_before_sync();
+      tc::mbar_arrive(&a_full[s]);
+    }
+  } else if (ok && warp >= W_E1 && warp < W_E2) {
+    const int q = warp & 3, hf = (warp - W_E1) >> 2, r = 32 * q + lane;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const long v = tile_of(i) * TM + r;
+      if (!warp_wait(&d1_full[s], ((uint32_t)i >> 1) & 1u, err, 9)) break;
+      tc::tc_after_sync();
+      const uint32_t D = tmem + lq + TD1 + (uint32_t)(C * s);
+#pragma unroll 1
+      for (int j = hf; j < C / 16; j += 2) {
+        uint32_t h[16];
+        tc::tmem_ld16u(D + 16u * j, h);
+        tc::tmem_wait_ld();
+        if (hg && v < V) {
+          float4* o = reinterpret_cast<float4*>(hg + v * C + 16 * j);
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            o[e] = make_float4(__uint_as_float(h[4 * e]), __uint_as_float(h[4 * e + 1]), __uint_as_float(h[4 * e + 2]),
+                               __uint_as_float(h[4 * e + 3]));
+        }
+        uint32_t hi[8], lo[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          tc::split_pack(gelu_tc(__uint_as_float(h[2 * e])), gelu_tc(__uint_as_float(h[2 * e + 1])), hi[e], lo[e]);
+        tc::tmem_st8u(D + 16u * j, hi);
+        tc::tmem_st8u(D + 16u * j + 8u, lo);
+      }
+      tc::tmem_wait_st();
+      tc::tc_before_sync();
+      tc::mbar_arrive(&h_full[s]);
+    }
+  } else if (ok && warp >= W_E2) {
+    const int q = warp & 3, r = 32 * q + lane;
+    const uint32_t lq = (uint32_t)(32 * q) << 16;
+    for (int i = 0; i < niter; ++i) {
+      const int s = i & 1;
+      const long v = tile_of(i) * TM + r;
+      if (!warp_wait(&d2_full[s], ((uint32_t)i >> 1) & 1u, err, 10)) break;
+      tc::tc_after_sync();
+      const uint32_t D = tmem + lq + (uint32_t)(3 * C * s);
+#pragma unroll
+      for (int k = 0; k < 2 * C / 16; ++k) {
+        uint32_t d[16];
+        tc::tmem_ld16u(D + 16u * k, d);
+        tc::tmem_wait_ld();
+        if (k == 2 * C / 16 - 1) {   // the A stage is free once D2 is in registers
+          tc::tc_before_sync();
+          tc::mbar_arrive(&a_empty[s]);
+        }
+        if (v < V) {
+          float4* o = reinterpret_cast<float4*>(gates + v * 2 * C + 16 * k);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int c = 16 * k + 4 * e;
+            o[e] = make_float4(sigmoid_tc(__uint_as_float(d[4 * e]) + bs[c]),
+                               sigmoid_tc(__uint_as_float(d[4 * e + 1]) + bs[c + 1]),
+                               sigmoid_tc(__uint_as_float(d[4 * e + 2]) + bs[c + 2]),
+                               sigmoid_tc(__uint_as_float(d[4 * e + 3]) + bs[c + 3]));
+          }
+        }
+      }
+    }
+  }
+  tc::tc_before_sync();
+  __syncthreads();
+  tc::tc_after_sync();
+  if (warp == 0) tc::tmem_free(tmem, 512);
+}
+
 // ================================================================================================ fuse, second half
 // The ffno_fuse2_tc contract: B = [gelu(GN_s(spec_pre)) g_s, gelu(GN_v(vert_pre)) g_v] (g = the branch gates [V][2C]),
 // pre = gelu(B Wf1^T) Wf2^T + (B[:, :C] + B[:, C:]) / 2, with the depth-weighted GroupNorm partials of pre.
@@ -1534,10 +1783,42 @@ int launch_fuse2(const float* sp, const float* sc, const float* vp, const float*
   return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
 }
 
+template <int C>
+int launch_fuse1(const float* x, const float* sp, const float* sc, const float* vp, const float* vc, long V,
+                 const void* wpack, const float* bias, float* gates, float* hg, int* err, cudaStream_t s) {
+  CUtensorMap mx, ms, mv;
+  if (!row_map(&mx, x, V, C) || !row_map(&ms, sp, V, C) || !row_map(&mv, vp, V, C)) return FFNO_EINVAL;
+  const size_t smem = 1024 + (size_t)mat_bytes(C, 3 * C) + mat_bytes(2 * C, C) + 4 * (size_t)BOX_BYTES;
+  if (cudaFuncSetAttribute(k_fuse1_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return FFNO_ELAUNCH;
+  const long nt = (V + TM - 1) / TM;
+  const int grid = (int)(nt < sms() ? nt : sms());
+  k_fuse1_ws<C><<<grid, NTHREADS, smem, s>>>(mx, ms, mv, sc, vc, V, static_cast<const uint8_t*>(wpack), bias, gates,
+                                              hg, err);
+  return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
+}
+
 }  // namespace
 
 namespace ffno {
 namespace ws {
+
+bool fuse1_supported(int C) { return C == 32 || C == 64; }
+
+int fuse1(const float* x, const float* spec_pre, const float* spec_coefs, const float* vert_pre,
+          const float* vert_coefs, long V, int C, const void* wpack, const float* bias, float* gates, float* hg,
+          int* err, cudaStream_t stream) {
+  if (V < 1 || V > 0x7fffffffL - TM || !bias ||
+      (reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(spec_pre) | reinterpret_cast<uintptr_t>(vert_pre) |
+       reinterpret_cast<uintptr_t>(gates)) % 16 ||
+      (hg && reinterpret_cast<uintptr_t>(hg) % 16))
+    return FFNO_EINVAL;
+  if (C == 64)
+    return launch_fuse1<64>(x, spec_pre, spec_coefs, vert_pre, vert_coefs, V, wpack, bias, gates, hg, err, stream);
+  if (C == 32)
+    return launch_fuse1<32>(x, spec_pre, spec_coefs, vert_pre, vert_coefs, V, wpack, bias, gates, hg, err, stream);
+  return FFNO_EINVAL;
+}
 
 bool fuse2_supported(int C) { return C == 32 || C == 64; }
 

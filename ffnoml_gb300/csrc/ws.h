@@ -10,6 +10,10 @@ bool mlp2_fwd_supported(int C);
 int mlp2_fwd(int mode, const float* in, const float* prev_pre, const float* prev_coefs, float res, float* xout, long V,
              int C, const void* wpack, const float* dw, float* pre, double* partials, int nparts, int* err,
              cudaStream_t stream);
+bool fuse1_supported(int C);
+int fuse1(const float* x, const float* spec_pre, const float* spec_coefs, const float* vert_pre,
+          const float* vert_coefs, long V, int C, const void* wpack, const float* bias, float* gates, float* hg,
+          int* err, cudaStream_t stream);
 bool fuse2_supported(int C);
 int fuse2(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
           const float* gates, long V, int C, const void* wpack, const float* dw, float* pre, double* partials,
