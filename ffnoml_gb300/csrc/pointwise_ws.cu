@@ -305,24 +305,27 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                      float eps, const float* __restrict__ dw, float* __restrict__ wbar, const float* __restrict__ base,
                      long V, const uint8_t* __restrict__ wpack, float* __restrict__ abar, int* __restrict__ err) {
   static_assert(C == 32 || C == 64, "widths 32 and 64");
-  constexpr uint32_t B1 = mat_bytes(2 * C, C);   // each of w1 (2C x C), w2t (2C x C), w1t (C x 2C)
-  constexpr uint32_t WB = 3 * B1;
-  constexpr int NB = C / 32, CPG = C / GMAX;
+  constexpr uint32_t B1 = mat_bytes(2 * C, C);   // each of w1 (2C x C), w2t (2C x C); GEMM3 reads w1 as MN-major W1^T
+  constexpr uint32_t WB = 2 * B1;
+  constexpr int NB = C / 32, CPG = C / GMAX, NS = 3;
   constexpr uint32_t SB = 3 * BOX_BYTES;         // one ring stage: 32 channels of a, u, pre
   static_assert(WB % 1024 == 0, "the ring must stay 1024-byte aligned (128-byte swizzle)");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* ring = smem + WB;
   __shared__ Bars bars;
+  __shared__ uint64_t rfull[NS], rempty[NS];
   __shared__ uint32_t tslot;
   __shared__ GnBwdConst kc;
   __shared__ float gm[C], bt[C];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp == 0) tc::tmem_alloc(&tslot, 512);
   if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; ++s) {
+      tc::mbar_init(&rfull[s], 1);
+      tc::mbar_init(&rempty[s], 128);
+    }
     for (int s = 0; s < 2; ++s) {
-      tc::mbar_init(&bars.stg_full[s], 1);
-      tc::mbar_init(&bars.stg_empty[s], 128);
       tc::mbar_init(&bars.a_full[s], 128);
       tc::mbar_init(&bars.a_empty[s], 128);
       tc::mbar_init(&bars.d3_full[s], 1);
@@ -363,30 +366,30 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   auto tile_of = [&](int i) { return (long)blockIdx.x + (long)i * gridDim.x; };
 
   if (ok && warp == W_TMA && lane == 0) {
-    int issued[2] = {0, 0};
+    int issued[NS] = {0, 0, 0};
     bool alive = true;
     for (int i = 0; i < niter && alive; ++i) {
       const int row = (int)(tile_of(i) * TM);
       for (int ph = 0; ph < NB; ++ph) {
-        const int u = i * NB + ph, st = u & 1;
-        const uint32_t n = (uint32_t)u >> 1;
-        if (!wait_or_flag(&bars.stg_empty[st], (n & 1u) ^ 1u, err, 3)) {
+        const int u = i * NB + ph, st = u % NS;
+        const uint32_t n = (uint32_t)(u / NS);
+        if (!wait_or_flag(&rempty[st], (n & 1u) ^ 1u, err, 3)) {
           alive = false;
           break;
         }
-        tc::mbar_arrive_expect_tx(&bars.stg_full[st], SB);
+        tc::mbar_arrive_expect_tx(&rfull[st], SB);
         uint8_t* sp = ring + st * SB;
-        tc::tma_load_2d(sp, &map_a, 32 * ph, row, &bars.stg_full[st]);
-        tc::tma_load_2d(sp + BOX_BYTES, &map_u, 32 * ph, row, &bars.stg_full[st]);
-        tc::tma_load_2d(sp + 2 * BOX_BYTES, &map_p, 32 * ph, row, &bars.stg_full[st]);
+        tc::tma_load_2d(sp, &map_a, 32 * ph, row, &rfull[st]);
+        tc::tma_load_2d(sp + BOX_BYTES, &map_u, 32 * ph, row, &rfull[st]);
+        tc::tma_load_2d(sp + 2 * BOX_BYTES, &map_p, 32 * ph, row, &rfull[st]);
         ++issued[st];
       }
     }
-    for (int s = 0; s < 2; ++s)   // every copy has landed before the CTA may exit
-      if (issued[s]) tc::mbar_wait_for(&bars.stg_full[s], (uint32_t)(issued[s] - 1) & 1u, WAIT_NS);
+    for (int s = 0; s < NS; ++s)   // every copy has landed before the CTA may exit
+      if (issued[s]) tc::mbar_wait_for(&rfull[s], (uint32_t)(issued[s] - 1) & 1u, WAIT_NS);
   } else if (ok && warp == W_MMA && lane == 0) {
-    const uint32_t i12 = tc::idesc_bf16(128, 2 * C), i3 = tc::idesc_bf16(128, C);
-    const uint32_t w1 = tc::smem_u32(smem), w2t = w1 + B1, w1t = w1 + 2 * B1, LO = B1 / 2;
+    const uint32_t i12 = tc::idesc_bf16(128, 2 * C), i3 = tc::idesc_bf16(128, C, true);
+    const uint32_t w1 = tc::smem_u32(smem), w2t = w1 + B1, LO = B1 / 2;
     uint64_t* last = nullptr;
     uint32_t last_par = 0;
     bool last_seen = true;
@@ -417,11 +420,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (!wait_or_flag(&bars.g_full, (uint32_t)i & 1u, err, 6)) break;
       tc::tc_after_sync();
 #pragma unroll 1
-      for (int j = 0; j < 2 * C / 16; ++j) {
-        const uint32_t bo = 256u * j;
+      for (int j = 0; j < 2 * C / 16; ++j) {   // W1 [2C][C] K-major is W1^T MN-major (N = C): 16 k = 2 row groups
+        const uint32_t bo = (uint32_t)(32 * C) * j;
         mma3_ta(tmem + (uint32_t)(128 * s), tmem + D1 + 16u * j, tmem + D1 + 16u * j + 8u,
-                tc::kmajor_desc(w1t + bo, 128u, 2 * C * 16u), tc::kmajor_desc(w1t + LO + bo, 128u, 2 * C * 16u), i3,
-                j > 0);
+                tc::mnmajor_desc(w1 + bo, C * 16u, 128u), tc::mnmajor_desc(w1 + LO + bo, C * 16u, 128u), i3, j > 0);
       }
       tc::mma_commit(&bars.d3_full[s]);
       last = &bars.d3_full[s];
@@ -444,8 +446,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float w = live ? __ldg(dw + v) : 0.f;
       float wc = 0.f;
       for (int ph = 0; ph < NB; ++ph) {
-        const int u = i * NB + ph, st = u & 1;
-        if (!warp_wait(&bars.stg_full[st], ((uint32_t)u >> 1) & 1u, err, 7)) {
+        const int u = i * NB + ph, st = u % NS;
+        if (!warp_wait(&rfull[st], (uint32_t)(u / NS) & 1u, err, 7)) {
           alive = false;
           break;
         }
@@ -483,7 +485,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           tc::tmem_st8u(A + (uint32_t)C + col, phi);
           tc::tmem_st8u(A + (uint32_t)(C + C / 2) + col, plo);
         }
-        tc::mbar_arrive(&bars.stg_empty[st]);
+        tc::mbar_arrive(&rempty[st]);
       }
       if (!alive) break;
       if (live) wbar[v] += wc;
@@ -2077,7 +2079,7 @@ int launch_mlp2_bwd_gn(int mode, const float* u, float r, const float* pre, cons
                        cudaStream_t s) {
   CUtensorMap ma, mu, mp;
   if (!row_map(&ma, a, V, C) || !row_map(&mu, u, V, C) || !row_map(&mp, pre, V, C)) return FFNO_EINVAL;
-  const size_t smem = 1024 + 3 * (size_t)mat_bytes(2 * C, C) + 2 * (size_t)(3 * BOX_BYTES);
+  const size_t smem = 1024 + 2 * (size_t)mat_bytes(2 * C, C) + 3 * (size_t)(3 * BOX_BYTES);
   if (cudaFuncSetAttribute(k_mlp2_bwd_gn_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return FFNO_ELAUNCH;
