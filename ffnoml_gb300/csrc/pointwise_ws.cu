@@ -435,15 +435,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int q = warp & 3, r = 32 * q + lane;
     const uint32_t lq = (uint32_t)(32 * q) << 16;
     bool alive = true;
+    long vn = tile_of(0) * TM + r;
+    float wn = (niter > 0 && vn < V) ? __ldg(dw + vn) : 0.f;   // the row's depth weight, loaded a tile ahead
     for (int i = 0; i < niter && alive; ++i) {
       const int s = i & 1;
       const uint32_t n = (uint32_t)i >> 1;
+      const long v = vn;
+      const bool live = v < V;
+      const float w = wn;
+      vn = tile_of(i + 1) * TM + r;
+      wn = (i + 1 < niter && vn < V) ? __ldg(dw + vn) : 0.f;
       if (!warp_wait(&bars.a_empty[s], (n & 1u) ^ 1u, err, 8)) break;
       tc::tc_after_sync();
       const uint32_t A = tmem + lq + (uint32_t)(128 * s);
-      const long v = tile_of(i) * TM + r;
-      const bool live = v < V;
-      const float w = live ? __ldg(dw + v) : 0.f;
       float wc = 0.f;
       for (int ph = 0; ph < NB; ++ph) {
         const int u = i * NB + ph, st = u % NS;
@@ -488,10 +492,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         tc::mbar_arrive(&rempty[st]);
       }
       if (!alive) break;
-      if (live) wbar[v] += wc;
       tc::tmem_wait_st();
       tc::tc_before_sync();
       tc::mbar_arrive(&bars.a_full[s]);
+      if (live) wbar[v] += wc;   // after the hand-off: its load stays off the MMAs' path
     }
   } else if (ok && warp >= W_E1 && warp < W_E2) {
     const int q = warp & 3, hf = (warp - W_E1) >> 2;
