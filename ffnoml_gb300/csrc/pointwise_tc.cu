@@ -1436,15 +1436,6 @@ int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, lo
   return FFNO_OK;
 }
 
-int ffno_mlp2_bwd_gn_tc(int mode, const float* u, float r, const float* pre, const float* gamma, const float* beta,
-                        const double* gstats, const double* sums, const float* dw, float eps, const float* a,
-                        const float* base, long V, int C, int groups, const void* wpack, float* a_bar, float* w_bar,
-                        int* err, ffno_stream_t stream) {
-  if (!ws::mlp2_bwd_supported(C) || groups != GMAX || !err || !aligned16(wpack)) return FFNO_EINVAL;
-  return ws::mlp2_bwd_gn(mode, u, r, pre, gamma, beta, gstats, sums, dw, eps, a, base, V, C, wpack, a_bar, w_bar, err,
-                         (cudaStream_t)stream);
-}
-
 int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long V, int C, const void* wpack,
                      const float* zp, float* x_bar, float* z_bar, int* err, ffno_stream_t stream) {
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z_bar)) return FFNO_EINVAL;

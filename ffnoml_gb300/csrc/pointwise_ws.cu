@@ -286,284 +286,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) tc::tmem_free(tmem, 512);
 }
 
-// ======================================================================================= GN backward + MLP backward
-// ffno_gn_bwd_apply followed by ffno_mlp2_bwd in one pass: the GroupNorm-backward application is done by the
-// conversion warps on the way into tensor memory, so pre_bar never goes through HBM. Per voxel v and channel c of group
-// g: xh = (pre - mean_g) rstd_g, ghat = r u [gelu'(xh gamma + beta) when mode 1] gamma, pre_bar = rstd_g (ghat -
-// w_v / T_g (S1_g + xh S2_g)), and w_bar[v] += sum_c (1 / T_g) (-S1_g xh - S2_g (xh^2 - var_g rstd_g^2) / 2); then
-// a_bar = base + ((pre_bar W2^T) * gelu'(a W1)) W1^T as in k_mlp2_bwd_ws. The ring carries, per tile, NB phases of 32
-// channels of a, u and pre (two stages); the MMA, epilogue-1 and epilogue-2 roles are those of k_mlp2_bwd_ws.
-struct GnBwdConst {
-  float mean[GMAX], rstd[GMAX], invT[GMAX], s1[GMAX], s2[GMAX], vr2[GMAX];
-};
-
-template <int C>
-__global__ void __launch_bounds__(NTHREADS, 1)
-    k_mlp2_bwd_gn_ws(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_u,
-                     const __grid_constant__ CUtensorMap map_p, int mode, float rr, const float* __restrict__ gamma,
-                     const float* __restrict__ beta, const double* __restrict__ gst, const double* __restrict__ sums,
-                     float eps, const float* __restrict__ dw, float* __restrict__ wbar, const float* __restrict__ base,
-                     long V, const uint8_t* __restrict__ wpack, float* __restrict__ abar, int* __restrict__ err) {
-  static_assert(C == 32 || C == 64, "widths 32 and 64");
-  constexpr uint32_t B1 = mat_bytes(2 * C, C);   // each of w1 (2C x C), w2t (2C x C); GEMM3 reads w1 as MN-major W1^T
-  constexpr uint32_t WB = 2 * B1;
-  constexpr int NB = C / 32, CPG = C / GMAX, NS = 3;
-  constexpr uint32_t SB = 3 * BOX_BYTES;         // one ring stage: 32 channels of a, u, pre
-  static_assert(WB % 1024 == 0, "the ring must stay 1024-byte aligned (128-byte swizzle)");
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = align1024(smem_raw);
-  uint8_t* ring = smem + WB;
-  __shared__ Bars bars;
-  __shared__ uint64_t rfull[NS], rempty[NS];
-  __shared__ uint32_t tslot;
-  __shared__ GnBwdConst kc;
-  __shared__ float gm[C], bt[C];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp == 0) tc::tmem_alloc(&tslot, 512);
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < NS; ++s) {
-      tc::mbar_init(&rfull[s], 1);
-      tc::mbar_init(&rempty[s], 128);
-    }
-    for (int s = 0; s < 2; ++s) {
-      tc::mbar_init(&bars.a_full[s], 128);
-      tc::mbar_init(&bars.a_empty[s], 128);
-      tc::mbar_init(&bars.d3_full[s], 1);
-    }
-    tc::mbar_init(&bars.d_full, 1);
-    tc::mbar_init(&bars.g_full, 256);
-    tc::mbar_init(&bars.w, 1);
-    tc::mbar_init_fence();
-  }
-  if (threadIdx.x < GMAX) {
-    const int g = threadIdx.x;
-    const double rs = gst[3 * g + 1];
-    kc.mean[g] = (float)gst[3 * g];
-    kc.rstd[g] = (float)rs;
-    kc.invT[g] = (float)(1.0 / gst[3 * g + 2]);
-    kc.s1[g] = (float)sums[2 * g];
-    kc.s2[g] = (float)sums[2 * g + 1];
-    kc.vr2[g] = (float)(1.0 - (double)eps * rs * rs);
-  }
-  for (int e = threadIdx.x; e < C; e += NTHREADS) {
-    gm[e] = gamma[e];
-    bt[e] = beta[e];
-  }
-  tc::tc_before_sync();
-  __syncthreads();
-  tc::tc_after_sync();
-  const uint32_t tmem = tslot;
-  if (threadIdx.x == 0) {
-    tc::mbar_arrive_expect_tx(&bars.w, WB);
-    for (uint32_t off = 0; off < WB; off += 32768u)
-      tc::bulk_g2s(smem + off, wpack + off, WB - off < 32768u ? WB - off : 32768u, &bars.w);
-  }
-  const bool ok = __syncthreads_and(tc::mbar_wait_for(&bars.w, 0, WAIT_NS)) != 0;
-  if (!ok && threadIdx.x == 0) atomicExch(err, 1);
-
-  const long nt = (V + TM - 1) / TM;
-  const int niter = (long)blockIdx.x < nt ? (int)((nt - 1 - blockIdx.x) / gridDim.x + 1) : 0;
-  auto tile_of = [&](int i) { return (long)blockIdx.x + (long)i * gridDim.x; };
-
-  if (ok && warp == W_TMA && lane == 0) {
-    int issued[NS] = {0, 0, 0};
-    bool alive = true;
-    for (int i = 0; i < niter && alive; ++i) {
-      const int row = (int)(tile_of(i) * TM);
-      for (int ph = 0; ph < NB; ++ph) {
-        const int u = i * NB + ph, st = u % NS;
-        const uint32_t n = (uint32_t)(u / NS);
-        if (!wait_or_flag(&rempty[st], (n & 1u) ^ 1u, err, 3)) {
-          alive = false;
-          break;
-        }
-        tc::mbar_arrive_expect_tx(&rfull[st], SB);
-        uint8_t* sp = ring + st * SB;
-        tc::tma_load_2d(sp, &map_a, 32 * ph, row, &rfull[st]);
-        tc::tma_load_2d(sp + BOX_BYTES, &map_u, 32 * ph, row, &rfull[st]);
-        tc::tma_load_2d(sp + 2 * BOX_BYTES, &map_p, 32 * ph, row, &rfull[st]);
-        ++issued[st];
-      }
-    }
-    for (int s = 0; s < NS; ++s)   // every copy has landed before the CTA may exit
-      if (issued[s]) tc::mbar_wait_for(&rfull[s], (uint32_t)(issued[s] - 1) & 1u, WAIT_NS);
-  } else if (ok && warp == W_MMA && lane == 0) {
-    const uint32_t i12 = tc::idesc_bf16(128, 2 * C), i3 = tc::idesc_bf16(128, C, true);
-    const uint32_t w1 = tc::smem_u32(smem), w2t = w1 + B1, LO = B1 / 2;
-    uint64_t* last = nullptr;
-    uint32_t last_par = 0;
-    bool last_seen = true;
-    for (int i = 0; i < niter; ++i) {
-      const int s = i & 1;
-      const uint32_t n = (uint32_t)i >> 1;
-      if (!wait_or_flag(&bars.a_full[s], n & 1u, err, 4)) break;
-      if (i > 0) {   // GEMM3 of the previous tile has read G out of D1
-        if (!wait_or_flag(&bars.d3_full[(i - 1) & 1], ((uint32_t)(i - 1) >> 1) & 1u, err, 5)) break;
-        last_seen = true;
-      }
-      tc::tc_after_sync();
-      const uint32_t A = tmem + (uint32_t)(128 * s);
-#pragma unroll 1
-      for (int k = 0; k < C / 16; ++k) {
-        const uint32_t ah = A + 8u * k, al = A + C / 2 + 8u * k;
-        const uint32_t ph = A + C + 8u * k, pl = A + C + C / 2 + 8u * k;
-        const uint32_t bo = 256u * k;
-        mma3_ta(tmem + D1, ah, al, tc::kmajor_desc(w1 + bo, 128u, C * 16u), tc::kmajor_desc(w1 + LO + bo, 128u, C * 16u),
-                i12, k > 0);
-        mma3_ta(tmem + D2, ph, pl, tc::kmajor_desc(w2t + bo, 128u, C * 16u),
-                tc::kmajor_desc(w2t + LO + bo, 128u, C * 16u), i12, k > 0);
-      }
-      tc::mma_commit(&bars.d_full);
-      last = &bars.d_full;
-      last_par = (uint32_t)i & 1u;
-      last_seen = false;
-      if (!wait_or_flag(&bars.g_full, (uint32_t)i & 1u, err, 6)) break;
-      tc::tc_after_sync();
-#pragma unroll 1
-      for (int j = 0; j < 2 * C / 16; ++j) {   // W1 [2C][C] K-major is W1^T MN-major (N = C): 16 k = 2 row groups
-        const uint32_t bo = (uint32_t)(32 * C) * j;
-        mma3_ta(tmem + (uint32_t)(128 * s), tmem + D1 + 16u * j, tmem + D1 + 16u * j + 8u,
-                tc::mnmajor_desc(w1 + bo, C * 16u, 128u), tc::mnmajor_desc(w1 + LO + bo, C * 16u, 128u), i3, j > 0);
-      }
-      tc::mma_commit(&bars.d3_full[s]);
-      last = &bars.d3_full[s];
-      last_par = n & 1u;
-      last_seen = false;
-    }
-    if (last && !last_seen) tc::mbar_wait_for(last, last_par, WAIT_NS);   // no MMA in flight when tensor memory is freed
-  } else if (ok && warp >= W_CVT && warp < W_E1) {
-    const int q = warp & 3, r = 32 * q + lane;
-    const uint32_t lq = (uint32_t)(32 * q) << 16;
-    bool alive = true;
-    long vn = tile_of(0) * TM + r;
-    float wn = (niter > 0 && vn < V) ? __ldg(dw + vn) : 0.f;   // the row's depth weight, loaded a tile ahead
-    for (int i = 0; i < niter && alive; ++i) {
-      const int s = i & 1;
-      const uint32_t n = (uint32_t)i >> 1;
-      const long v = vn;
-      const bool live = v < V;
-      const float w = wn;
-      vn = tile_of(i + 1) * TM + r;
-      wn = (i + 1 < niter && vn < V) ? __ldg(dw + vn) : 0.f;
-      if (!warp_wait(&bars.a_empty[s], (n & 1u) ^ 1u, err, 8)) break;
-      tc::tc_after_sync();
-      const uint32_t A = tmem + lq + (uint32_t)(128 * s);
-      float wc = 0.f;
-      for (int ph = 0; ph < NB; ++ph) {
-        const int u = i * NB + ph, st = u % NS;
-        if (!warp_wait(&rfull[st], (uint32_t)(u / NS) & 1u, err, 7)) {
-          alive = false;
-          break;
-        }
-        const uint8_t* rp = ring + st * SB + r * 128;
-#pragma unroll
-        for (int hh = 0; hh < 2; ++hh) {   // 16 channels at a time: 8 hi and 8 lo columns of a and of pre_bar
-          uint32_t ahi[8], alo[8], phi[8], plo[8];
-#pragma unroll
-          for (int cc = 0; cc < 4; ++cc) {
-            const int c4 = 4 * hh + cc;
-            const uint32_t o = (uint32_t)((c4 ^ (r & 7)) << 4);
-            const float4 av = *reinterpret_cast<const float4*>(rp + o);
-            const float4 uv = *reinterpret_cast<const float4*>(rp + BOX_BYTES + o);
-            const float4 pv = *reinterpret_cast<const float4*>(rp + 2 * BOX_BYTES + o);
-            const float uu[4] = {uv.x, uv.y, uv.z, uv.w}, pp[4] = {pv.x, pv.y, pv.z, pv.w};
-            float pb[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const int c = 32 * ph + 4 * c4 + e, g = c / CPG;
-              const float xh = (pp[e] - kc.mean[g]) * kc.rstd[g];
-              float gh = rr * uu[e];
-              if (mode) gh *= gelu_grad_tc(fmaf(xh, gm[c], bt[c]));
-              gh *= gm[c];
-              pb[e] = kc.rstd[g] * (gh - w * kc.invT[g] * fmaf(xh, kc.s2[g], kc.s1[g]));
-              wc += kc.invT[g] * (-kc.s1[g] * xh - 0.5f * kc.s2[g] * (xh * xh - kc.vr2[g]));
-            }
-            tc::split_pack(av.x, av.y, ahi[2 * cc], alo[2 * cc]);
-            tc::split_pack(av.z, av.w, ahi[2 * cc + 1], alo[2 * cc + 1]);
-            tc::split_pack(pb[0], pb[1], phi[2 * cc], plo[2 * cc]);
-            tc::split_pack(pb[2], pb[3], phi[2 * cc + 1], plo[2 * cc + 1]);
-          }
-          const uint32_t col = (uint32_t)(16 * ph + 8 * hh);   // first column of these 16 channels' pairs
-          tc::tmem_st8u(A + col, ahi);
-          tc::tmem_st8u(A + (uint32_t)(C / 2) + col, alo);
-          tc::tmem_st8u(A + (uint32_t)C + col, phi);
-          tc::tmem_st8u(A + (uint32_t)(C + C / 2) + col, plo);
-        }
-        tc::mbar_arrive(&rempty[st]);
-      }
-      if (!alive) break;
-      tc::tmem_wait_st();
-      tc::tc_before_sync();
-      tc::mbar_arrive(&bars.a_full[s]);
-      if (live) wbar[v] += wc;   // after the hand-off: its load stays off the MMAs' path
-    }
-  } else if (ok && warp >= W_E1 && warp < W_E2) {
-    const int q = warp & 3, hf = (warp - W_E1) >> 2;
-    const uint32_t lq = (uint32_t)(32 * q) << 16;
-    for (int i = 0; i < niter; ++i) {
-      if (!warp_wait(&bars.d_full, (uint32_t)i & 1u, err, 9)) break;
-      tc::tc_after_sync();
-#pragma unroll 1
-      for (int j = hf; j < 2 * C / 16; j += 2) {
-        uint32_t h[16], gb[16];
-        tc::tmem_ld16u(tmem + lq + D1 + 16u * j, h);
-        tc::tmem_ld16u(tmem + lq + D2 + 16u * j, gb);
-        tc::tmem_wait_ld();
-        uint32_t hi[8], lo[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-          const float g0 = __uint_as_float(gb[2 * e]) * gelu_grad_tc(__uint_as_float(h[2 * e]));
-          const float g1 = __uint_as_float(gb[2 * e + 1]) * gelu_grad_tc(__uint_as_float(h[2 * e + 1]));
-          tc::split_pack(g0, g1, hi[e], lo[e]);
-        }
-        tc::tmem_st8u(tmem + lq + D1 + 16u * j, hi);
-        tc::tmem_st8u(tmem + lq + D1 + 16u * j + 8u, lo);
-      }
-      tc::tmem_wait_st();
-      tc::tc_before_sync();
-      tc::mbar_arrive(&bars.g_full);
-    }
-  } else if (ok && warp >= W_E2) {
-    const int q = warp & 3, r = 32 * q + lane;
-    const uint32_t lq = (uint32_t)(32 * q) << 16;
-    for (int i = 0; i < niter; ++i) {
-      const int s = i & 1;
-      const uint32_t n = (uint32_t)i >> 1;
-      const long v = tile_of(i) * TM + r;
-      const bool live = v < V;
-      float4 bv[C / 4];
-#pragma unroll
-      for (int c = 0; c < C / 4; ++c)
-        bv[c] = (base && live) ? __ldg(reinterpret_cast<const float4*>(base + v * C) + c) : make_float4(0.f, 0.f, 0.f, 0.f);
-      if (!warp_wait(&bars.d3_full[s], n & 1u, err, 10)) break;
-      tc::tc_after_sync();
-#pragma unroll
-      for (int k = 0; k < C / 16; ++k) {
-        uint32_t d[16];
-        tc::tmem_ld16u(tmem + lq + (uint32_t)(128 * s + 16 * k), d);
-        tc::tmem_wait_ld();
-        if (k == C / 16 - 1) {   // the stage's tensor memory is free once D3 is in registers
-          tc::tc_before_sync();
-          tc::mbar_arrive(&bars.a_empty[s]);
-        }
-        if (live) {
-          float4* o = reinterpret_cast<float4*>(abar + v * C + 16 * k);
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const float4 b4 = bv[4 * k + e];
-            o[e] = make_float4(b4.x + __uint_as_float(d[4 * e]), b4.y + __uint_as_float(d[4 * e + 1]),
-                               b4.z + __uint_as_float(d[4 * e + 2]), b4.w + __uint_as_float(d[4 * e + 3]));
-          }
-        }
-      }
-    }
-  }
-  tc::tc_before_sync();
-  __syncthreads();
-  tc::tc_after_sync();
-  if (warp == 0) tc::tmem_free(tmem, 512);
-}
-
 // ================================================================================================ forward
 // The ffno_mlp2_fwd contract: pre = W2 gelu(W1 x) with x = in (MODE 0) or x = in + res act(GN(prev)) written to xout
 // (MODE 1: act = GELU, MODE 2: identity), and the depth-weighted GroupNorm partials of pre (one per CTA, its tiles
@@ -2076,47 +1798,10 @@ int launch_fuse1(const float* x, const float* sp, const float* sc, const float* 
   return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
 }
 
-template <int C>
-int launch_mlp2_bwd_gn(int mode, const float* u, float r, const float* pre, const float* gamma, const float* beta,
-                       const double* gstats, const double* sums, const float* dw, float eps, const float* a,
-                       const float* base, long V, const void* wpack, float* a_bar, float* w_bar, int* err,
-                       cudaStream_t s) {
-  CUtensorMap ma, mu, mp;
-  if (!row_map(&ma, a, V, C) || !row_map(&mu, u, V, C) || !row_map(&mp, pre, V, C)) return FFNO_EINVAL;
-  const size_t smem = 1024 + 2 * (size_t)mat_bytes(2 * C, C) + 3 * (size_t)(3 * BOX_BYTES);
-  if (cudaFuncSetAttribute(k_mlp2_bwd_gn_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess)
-    return FFNO_ELAUNCH;
-  const long nt = (V + TM - 1) / TM;
-  const int grid = (int)(nt < sms() ? nt : sms());
-  k_mlp2_bwd_gn_ws<C><<<grid, NTHREADS, smem, s>>>(ma, mu, mp, mode, r, gamma, beta, gstats, sums, eps, dw, w_bar,
-                                                    base, V, static_cast<const uint8_t*>(wpack), a_bar, err);
-  return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
-}
-
 }  // namespace
 
 namespace ffno {
 namespace ws {
-
-int mlp2_bwd_gn(int mode, const float* u, float r, const float* pre, const float* gamma, const float* beta,
-                const double* gstats, const double* sums, const float* dw, float eps, const float* a,
-                const float* base, long V, int C, const void* wpack, float* a_bar, float* w_bar, int* err,
-                cudaStream_t stream) {
-  if (V < 1 || V > 0x7fffffffL - TM || (mode != 0 && mode != 1) || !gamma || !beta || !gstats || !sums || !dw ||
-      !w_bar ||
-      (reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(pre) |
-       reinterpret_cast<uintptr_t>(a_bar)) % 16 ||
-      (base && reinterpret_cast<uintptr_t>(base) % 16))
-    return FFNO_EINVAL;
-  if (C == 64)
-    return launch_mlp2_bwd_gn<64>(mode, u, r, pre, gamma, beta, gstats, sums, dw, eps, a, base, V, wpack, a_bar, w_bar,
-                                  err, stream);
-  if (C == 32)
-    return launch_mlp2_bwd_gn<32>(mode, u, r, pre, gamma, beta, gstats, sums, dw, eps, a, base, V, wpack, a_bar, w_bar,
-                                  err, stream);
-  return FFNO_EINVAL;
-}
 
 bool fuse1_supported(int C) { return C == 32 || C == 64; }
 

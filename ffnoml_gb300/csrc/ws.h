@@ -24,10 +24,6 @@ int gate_fwd(const float* x, long V, int C, const void* wpack, const float* zp, 
 bool gate_bwd_supported(int C);
 int gate_bwd(const float* x, const float* g_bar, const float* base, long V, int C, const void* wpack, const float* zp,
              float* x_bar, float* z_bar, int* err, cudaStream_t stream);
-int mlp2_bwd_gn(int mode, const float* u, float r, const float* pre, const float* gamma, const float* beta,
-                const double* gstats, const double* sums, const float* dw, float eps, const float* a,
-                const float* base, long V, int C, const void* wpack, float* a_bar, float* w_bar, int* err,
-                cudaStream_t stream);
 bool mlp2_bwd_supported(int C);
 int mlp2_bwd(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack, float* a_bar,
              int* err, cudaStream_t stream);

@@ -896,19 +896,12 @@ class Executor:
         m = self.model
         C, V, s = m.width, ws.V, _stream()
         G = self._packed.groups
-        self._gn_bwd_sums(ws, gb, mode, u, r, pre, gamma, beta, name)
-        nat.call("ffno_gn_bwd_apply", mode, u.data_ptr(), r, pre.data_ptr(), gamma.data_ptr(), beta.data_ptr(),
-                 ws.gstats[name].data_ptr(), gb.sums.data_ptr(), ws.dw.data_ptr(), V, C, G, EPS, pbar.data_ptr(),
-                 gb.wbar.data_ptr(), s)
-
-    def _gn_bwd_sums(self, ws, gb, mode, u, r, pre, gamma, beta, name):
-        """The GroupNorm backward's per-group sums S1, S2 into gb.sums."""
-        m = self.model
-        C, V, s = m.width, ws.V, _stream()
-        G = self._packed.groups
         nat.call("ffno_gn_bwd_stats", mode, u.data_ptr(), r, pre.data_ptr(), gamma.data_ptr(), beta.data_ptr(),
                  ws.gstats[name].data_ptr(), V, C, G, gb.bpart.data_ptr(), ws.nparts, s)
         nat.call("ffno_gn_bwd_final", gb.bpart.data_ptr(), ws.nparts, G, gb.sums.data_ptr(), s)
+        nat.call("ffno_gn_bwd_apply", mode, u.data_ptr(), r, pre.data_ptr(), gamma.data_ptr(), beta.data_ptr(),
+                 ws.gstats[name].data_ptr(), gb.sums.data_ptr(), ws.dw.data_ptr(), V, C, G, EPS, pbar.data_ptr(),
+                 gb.wbar.data_ptr(), s)
 
     def _block_bwd(self, pk, ws, gb, i, x, z, zbar, D, H, W, hgt, pln, fq, tzf_bar, tzi_bar):
         """gb.xbar (gradient of the block output) -> gb.xbar (gradient of the block input x); accumulates the
@@ -931,24 +924,12 @@ class Executor:
                 nat.call("ffno_mlp2_bwd", a.data_ptr(), pb.data_ptr(), _ptr(base), V, C, bp[w1].data_ptr(),
                          bp[w2t].data_ptr(), bp[w1t].data_ptr(), out.data_ptr(), s)
 
-        def gn_mlp_bwd(mode, u, r, pre, name, a, base, out, w1, w2t, w1t, pack):
-            """GroupNorm backward of `name` (upstream u) then the MLP backward that produced its input pre; on the
-            tensor cores at widths 32 / 64 the GroupNorm application runs inside the MLP backward's conversion."""
-            gamma, beta = bp[name + "_g"], bp[name + "_b"]
-            if tc and C in (32, 64):
-                self._gn_bwd_sums(ws, gb, mode, u, r, pre, gamma, beta, name)
-                nat.call("ffno_mlp2_bwd_gn_tc", mode, u.data_ptr(), r, pre.data_ptr(), gamma.data_ptr(),
-                         beta.data_ptr(), ws.gstats[name].data_ptr(), gb.sums.data_ptr(), ws.dw.data_ptr(), EPS,
-                         a.data_ptr(), _ptr(base), V, C, pk.groups, bp[pack].data_ptr(), out.data_ptr(),
-                         gb.wbar.data_ptr(), err, s)
-            else:
-                self._gn_bwd(ws, gb, mode, u, r, pre, gamma, beta, name, gb.pbar)
-                mlp_bwd(a, gb.pbar, base, out, w1, w2t, w1t, pack)
-
         # out = x2 + r_mlp GN(mlp_pre); mlp_pre = mlp(x2)
-        gn_mlp_bwd(0, gb.xbar, r_mlp, ws.mlp_pre, "mlp", ws.x2, gb.xbar, gb.g2, "m1", "m2t", "m1t", "tcb_mlp")
+        self._gn_bwd(ws, gb, 0, gb.xbar, r_mlp, ws.mlp_pre, bp["mlp_g"], bp["mlp_b"], "mlp", gb.pbar)
+        mlp_bwd(ws.x2, gb.pbar, gb.xbar, gb.g2, "m1", "m2t", "m1t", "tcb_mlp")
         # x2 = x1 + r_pw GN(pw_pre); pw_pre = pw(x1)
-        gn_mlp_bwd(0, gb.g2, r_pw, ws.pw_pre, "pw", ws.x1, gb.g2, gb.g1, "pw1", "pw2t", "pw1t", "tcb_pw")
+        self._gn_bwd(ws, gb, 0, gb.g2, r_pw, ws.pw_pre, bp["pw_g"], bp["pw_b"], "pw", gb.pbar)
+        mlp_bwd(ws.x1, gb.pbar, gb.g2, gb.g1, "pw1", "pw2t", "pw1t", "tcb_pw")
         # x1 = x + r_f gelu(GN(fused_pre)); fused_pre = fuse(x, spec, vert)
         self._gn_bwd(ws, gb, 1, gb.g1, r_f, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], "fuse", gb.pbar)
         if tc:
@@ -971,8 +952,10 @@ class Executor:
                      bp["f2t"].data_ptr(), bp["f1t"].data_ptr(), bp["bg2t"].data_ptr(), bp["bg1t"].data_ptr(),
                      gb.xacc.data_ptr(), gb.sbar.data_ptr(), gb.vbar.data_ptr(), s)
         # spec = gelu(GN(spec_pre)), spec_pre = post_s(ys); vert likewise
-        gn_mlp_bwd(1, gb.sbar, 1.0, ws.spec_pre, "spec", ws.ys, None, gb.ysb, "s_p1", "s_p2t", "s_p1t", "tcb_s_post")
-        gn_mlp_bwd(1, gb.vbar, 1.0, ws.vert_pre, "vert", ws.yv, None, gb.yvb, "v_p1", "v_p2t", "v_p1t", "tcb_v_post")
+        self._gn_bwd(ws, gb, 1, gb.sbar, 1.0, ws.spec_pre, bp["spec_g"], bp["spec_b"], "spec", gb.pbar)
+        mlp_bwd(ws.ys, gb.pbar, None, gb.ysb, "s_p1", "s_p2t", "s_p1t", "tcb_s_post")
+        self._gn_bwd(ws, gb, 1, gb.vbar, 1.0, ws.vert_pre, bp["vert_g"], bp["vert_b"], "vert", gb.pbar)
+        mlp_bwd(ws.yv, gb.pbar, None, gb.yvb, "v_p1", "v_p2t", "v_p1t", "tcb_v_post")
         # horizontal transposes: ys = twi thi mix thf twf xs  ->  xs_bar = twf^T thf^T mix^T thi^T twi^T ys_bar
         self._xf(pln, "twi_t", gb.ysb, ws.sa, d["wf"], ws)
         self._xf(pln, "thi_t", ws.sa, ws.sb, d["hf"], ws)

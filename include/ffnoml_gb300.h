@@ -306,13 +306,6 @@ int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* v
 /* ffno_mlp2_bwd; wpack = [w1 (2C x C), w2^T (2C x C), w1^T (C x 2C)]. */
 int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack,
                      float* a_bar, int* err, ffno_stream_t stream);
-/* ffno_gn_bwd_apply (mode, u, r, pre, gamma, beta, gstats, sums, dw, eps; accumulating w_bar) followed by
- * ffno_mlp2_bwd_tc (a, base, wpack, a_bar) in one pass, pre_bar never stored; widths 32 and 64, groups = 8. The
- * statistics sums come from ffno_gn_bwd_stats + ffno_gn_bwd_final as before. */
-int ffno_mlp2_bwd_gn_tc(int mode, const float* u, float r, const float* pre, const float* gamma, const float* beta,
-                        const double* gstats, const double* sums, const float* dw, float eps, const float* a,
-                        const float* base, long V, int C, int groups, const void* wpack, float* a_bar, float* w_bar,
-                        int* err, ffno_stream_t stream);
 /* One branch of ffno_gate_bwd: x_bar = base + d/dx applied to g_bar, z_bar += g_bar . zp if zp; wpack = [g1, g2,
  * g2^T, g1^T]. base may equal x_bar. */
 int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long V, int C, const void* wpack,

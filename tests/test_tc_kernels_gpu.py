@@ -363,35 +363,3 @@ def test_outer_tc(Ma, Mb, N, nsplit):
     assert err.item() == 0
     _close(out - 0.5, ref, 2e-5)
     _close(out32, ref, 2e-5)
-
-
-@pytest.mark.parametrize("C,V", [(32, V), (64, V), (64, 152 * 128 * 5 + 77)])
-@pytest.mark.parametrize("mode,with_base", [(0, True), (1, False)])
-def test_mlp2_bwd_gn_tc(C, V, mode, with_base):
-    """The fused GroupNorm-backward application + MLP backward against ffno_gn_bwd_apply then ffno_mlp2_bwd (FP32):
-    a_bar and the depth-weight gradient w_bar."""
-    nat = _nat()
-    a, u, pre = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3, scale=2.0)
-    base = _rand(V, C, seed=4) if with_base else None
-    gamma, beta = 1 + 0.1 * _rand(C, seed=5), 0.1 * _rand(C, seed=6)
-    dw = (1 + 0.2 * _rand(V, seed=7)).abs().contiguous()
-    w1, w2 = _rand(2 * C, C, seed=8, scale=C ** -0.5), _rand(C, 2 * C, seed=9, scale=(2 * C) ** -0.5)
-    gst = torch.stack([0.1 * torch.randn(G, dtype=torch.float64), 0.5 + torch.rand(G, dtype=torch.float64),
-                       torch.full((G,), float(V), dtype=torch.float64)], 1).reshape(-1).cuda().contiguous()
-    sums = torch.randn(2 * G, dtype=torch.float64).cuda() * 10
-    err = torch.zeros(1, dtype=torch.int32, device="cuda")
-    ptr = lambda t: None if t is None else t.data_ptr()
-    pb = torch.empty(V, C, device="cuda")
-    r0, r1 = torch.empty(V, C, device="cuda"), torch.empty(V, C, device="cuda")
-    wb0, wb1 = torch.full((V,), 0.25, device="cuda"), torch.full((V,), 0.25, device="cuda")
-    nat.call("ffno_gn_bwd_apply", mode, u.data_ptr(), 0.7, pre.data_ptr(), gamma.data_ptr(), beta.data_ptr(),
-             gst.data_ptr(), sums.data_ptr(), dw.data_ptr(), V, C, G, 1e-5, pb.data_ptr(), wb0.data_ptr(), _s())
-    nat.call("ffno_mlp2_bwd", a.data_ptr(), pb.data_ptr(), ptr(base), V, C, _hold(w1.t().contiguous()),
-             _hold(w2.contiguous()), _hold(w1.contiguous()), r0.data_ptr(), _s())
-    nat.call("ffno_mlp2_bwd_gn_tc", mode, u.data_ptr(), 0.7, pre.data_ptr(), gamma.data_ptr(), beta.data_ptr(),
-             gst.data_ptr(), sums.data_ptr(), dw.data_ptr(), 1e-5, a.data_ptr(), ptr(base), V, C, G,
-             _pack(w1, w2.t(), w1.t()).data_ptr(), r1.data_ptr(), wb1.data_ptr(), err.data_ptr(), _s())
-    torch.cuda.synchronize()
-    assert int(err.item()) == 0
-    _close(r1, r0)
-    _close(wb1 - 0.25, wb0 - 0.25, 1e-5)
