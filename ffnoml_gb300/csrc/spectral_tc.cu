@@ -91,88 +91,63 @@ __global__ void __launch_bounds__(2 * RT, 1)
   const uint32_t t_hi = tc::smem_u32(sT), t_lo = t_hi + TB;
   uint32_t g = 0;                                            // chunks issued by this pipeline
   const int n_ep = 32 * q + lane;                            // epilogue column of this thread
-  // every fill piece of this thread covers the same 4 columns nf..nf+3 (see the piece mapping below)
-  const int nf = 8 * (2 * ((ptid >> 5) & 7) + (lane >> 4)) + 4 * ((lane >> 3) & 1);
-  auto item_of = [&](long itx, long& bfirst, long& n0) {
+  for (long it = 2L * blockIdx.x + pipe; ok && it < items; it += 2L * gridDim.x) {
+    long bfirst, n0;
     if (nbi > 1) {
-      bfirst = itx * nbi;
+      bfirst = it * nbi;
       n0 = 0;
     } else {
-      bfirst = itx / ntn;
-      n0 = (itx % ntn) * 128;
+      bfirst = it / ntn;
+      n0 = (it % ntn) * 128;
     }
-  };
-  // this thread's source columns in item itx
-  auto item_src = [&](long itx, const float*& src, bool& valid) {
-    long bfirst, n0, b, c;
-    item_of(itx, bfirst, n0);
-    if (nbi > 1) {
-      b = bfirst + (nf >> nshift);
-      c = nf & ((1 << nshift) - 1);
-    } else {
-      b = bfirst;
-      c = n0 + nf;
+    // every fill piece of this thread covers the same 4 columns nf..nf+3 (see the piece mapping below)
+    const int nf = 8 * (2 * ((ptid >> 5) & 7) + (lane >> 4)) + 4 * ((lane >> 3) & 1);
+    long foff = 0;
+    bool fv;
+    {
+      long b, c;
+      if (nbi > 1) {
+        b = bfirst + (nf >> nshift);
+        c = nf & ((1 << nshift) - 1);
+      } else {
+        b = bfirst;
+        c = n0 + nf;
+      }
+      fv = b < d.nb && c < d.N;
+      if (fv) foff = (b / d.nb2) * d.in_b1 + (b % d.nb2) * d.in_b2 + c;
     }
-    valid = b < d.nb && c < d.N;
-    src = in + (valid ? (b / d.nb2) * d.in_b1 + (b % d.nb2) * d.in_b2 + c : 0);
-  };
-  // fill: piece e = 4 consecutive columns of one row k; lanes take 8 rows x 2 column pairs, so a warp reads 8 rows x
-  // 64 contiguous bytes and writes conflict-free 8-byte slots of the MN-major tile. Row k of piece e is
-  // 8 (e / 256) + (lane & 7); its columns nf..nf+3 depend on the thread only. XFB RT pieces cover a whole chunk.
-  static_assert(XFB * RT == RKC * 32, "one round of loads per chunk");
-  auto load_chunk = [&](const float* src, bool valid, int k0, int kc, float4 (&v)[XFB]) {
-#pragma unroll
-    for (int u = 0; u < XFB; ++u) {
-      const int e = ptid + u * RT;
-      const int k = k0 + 8 * (e >> 8) + (lane & 7);
-      v[u] = (e < kc * 32 && k < d.K && valid) ? __ldg(reinterpret_cast<const float4*>(src + row_in[k]))
-                                               : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-  };
-  auto store_chunk = [&](uint8_t* st, int kc, const float4 (&v)[XFB]) {
-#pragma unroll
-    for (int u = 0; u < XFB; ++u) {
-      const int e = ptid + u * RT;
-      if (e >= kc * 32) break;
-      uint32_t h0, l0, h1, l1;
-      tc::split_pack(v[u].x, v[u].y, h0, l0);
-      tc::split_pack(v[u].z, v[u].w, h1, l1);
-      const uint32_t o = tc::mnmajor_offset(nf, 8 * (e >> 8) + (lane & 7), 128);
-      *reinterpret_cast<uint2*>(st + o) = make_uint2(h0, h1);
-      *reinterpret_cast<uint2*>(st + RSB + o) = make_uint2(l0, l1);
-    }
-  };
-  auto chunk_rows = [&](int ch) { return (Kp - ch * RKC) < RKC ? (Kp - ch * RKC) : RKC; };
-  // the loads of a chunk are issued one chunk ahead: while the previous chunk's MMAs are issued, and across an item
-  // boundary while the previous item's epilogue runs
-  float4 vb[XFB];
-  const float* fsrc = in;
-  bool fv = false;
-  const long it0 = 2L * blockIdx.x + pipe;
-  if (it0 < items) {
-    item_src(it0, fsrc, fv);
-    load_chunk(fsrc, fv, 0, chunk_rows(0), vb);
-  }
-  for (long it = it0; ok && it < items; it += 2L * gridDim.x) {
-    long bfirst, n0;
-    item_of(it, bfirst, n0);
-    const long itn = it + 2L * gridDim.x;
-    const float* nsrc = fsrc;
-    bool nvalid = false;
+    const float* fsrc = in + foff;
     for (int ch = 0; ch < nch; ++ch, ++g) {
       const int s = (int)(g & 1u);
-      const int k0 = ch * RKC, kc = chunk_rows(ch);
+      const int k0 = ch * RKC, kc = (Kp - k0) < RKC ? (Kp - k0) : RKC;
       if (g >= 2) {
         const bool w = tc::mbar_wait(&bar_m[pipe][s], ((g - 2) >> 1) & 1u);
         if (!(ok = rt_sync_and(pipe, w))) break;
       }
       uint8_t* st = sD + (uint32_t)(pipe * 2 + s) * 2u * RSB;
-      store_chunk(st, kc, vb);
-      if (ch + 1 < nch) {
-        load_chunk(fsrc, fv, k0 + RKC, chunk_rows(ch + 1), vb);
-      } else if (itn < items) {
-        item_src(itn, nsrc, nvalid);
-        load_chunk(nsrc, nvalid, 0, chunk_rows(0), vb);
+      // fill: piece e = 4 consecutive columns of one row k; lanes take 8 rows x 2 column pairs, so a warp reads 8
+      // rows x 64 contiguous bytes and writes conflict-free 8-byte slots of the MN-major tile. Row k of piece e is
+      // 8 (e / 256) + (lane & 7); its columns nf..nf+3 depend on the thread only.
+      for (int e0 = ptid; e0 < kc * 32; e0 += XFB * RT) {
+        float4 v[XFB];
+#pragma unroll
+        for (int u = 0; u < XFB; ++u) {
+          const int e = e0 + u * RT;
+          const int k = k0 + 8 * (e >> 8) + (lane & 7);
+          v[u] = (e < kc * 32 && k < d.K && fv) ? __ldg(reinterpret_cast<const float4*>(fsrc + row_in[k]))
+                                                : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < XFB; ++u) {
+          const int e = e0 + u * RT;
+          if (e >= kc * 32) break;
+          uint32_t h0, l0, h1, l1;
+          tc::split_pack(v[u].x, v[u].y, h0, l0);
+          tc::split_pack(v[u].z, v[u].w, h1, l1);
+          const uint32_t o = tc::mnmajor_offset(nf, 8 * (e >> 8) + (lane & 7), 128);
+          *reinterpret_cast<uint2*>(st + o) = make_uint2(h0, h1);
+          *reinterpret_cast<uint2*>(st + RSB + o) = make_uint2(l0, l1);
+        }
       }
       tc::fence_async_smem();
       tc::tc_before_sync();
@@ -192,8 +167,6 @@ __global__ void __launch_bounds__(2 * RT, 1)
       }
     }
     if (!ok) break;
-    fsrc = nsrc;
-    fv = nvalid;
     {
       const uint32_t gl = g - 1;
       const bool w = tc::mbar_wait(&bar_m[pipe][gl & 1u], (gl >> 1) & 1u);
@@ -282,57 +255,34 @@ __global__ void __launch_bounds__(RT, 1)
   bool ok = true;
   uint32_t g = 0;
   const int n_ep = 32 * q + lane;
-  const int nf = 8 * (2 * ((tid >> 5) & 7) + (lane >> 4)) + 4 * ((lane >> 3) & 1);
-  auto item_of = [&](long itx, long& bfirst, long& n0) {
-    if (nbi > 1) {
-      bfirst = itx * nbi;
-      n0 = 0;
-    } else {
-      bfirst = itx / ntn;
-      n0 = (itx % ntn) * 128;
-    }
-  };
-  auto item_src = [&](long itx, const float*& src, bool& valid) {
-    long bfirst, n0, b, c;
-    item_of(itx, bfirst, n0);
-    if (nbi > 1) {
-      b = bfirst + (nf >> nshift);
-      c = nf & ((1 << nshift) - 1);
-    } else {
-      b = bfirst;
-      c = n0 + nf;
-    }
-    valid = b < d.nb && c < d.N;
-    src = in + (valid ? (b / d.nb2) * d.in_b1 + (b % d.nb2) * d.in_b2 + c : 0);
-  };
-  static_assert(XFB * RT == RKC * 32, "one round of loads per chunk");
-  auto load_chunk = [&](const float* src, bool valid, int k0, int kc, float4 (&v)[XFB]) {
-#pragma unroll
-    for (int u = 0; u < XFB; ++u) {
-      const int e = tid + u * RT;
-      const int k = k0 + 8 * (e >> 8) + (lane & 7);
-      v[u] = (e < kc * 32 && k < d.K && valid) ? __ldg(reinterpret_cast<const float4*>(src + row_in[k]))
-                                               : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-  };
-  auto chunk_rows = [&](int ch) { return (Kp - ch * RKC) < RKC ? (Kp - ch * RKC) : RKC; };
-  // data loads issued one chunk ahead, across item boundaries too (as in k_xform_rt)
-  float4 vb[XFB];
-  const float* fsrc = in;
-  bool fv = false;
-  if ((long)blockIdx.x < items) {
-    item_src(blockIdx.x, fsrc, fv);
-    load_chunk(fsrc, fv, 0, chunk_rows(0), vb);
-  }
   for (long it = blockIdx.x; ok && it < items; it += gridDim.x) {
     long bfirst, n0;
-    item_of(it, bfirst, n0);
-    const long itn = it + gridDim.x;
-    const float* nsrc = fsrc;
-    bool nvalid = false;
+    if (nbi > 1) {
+      bfirst = it * nbi;
+      n0 = 0;
+    } else {
+      bfirst = it / ntn;
+      n0 = (it % ntn) * 128;
+    }
+    const int nf = 8 * (2 * ((tid >> 5) & 7) + (lane >> 4)) + 4 * ((lane >> 3) & 1);
+    long foff = 0;
+    bool fv;
+    {
+      long b, c;
+      if (nbi > 1) {
+        b = bfirst + (nf >> nshift);
+        c = nf & ((1 << nshift) - 1);
+      } else {
+        b = bfirst;
+        c = n0 + nf;
+      }
+      fv = b < d.nb && c < d.N;
+      if (fv) foff = (b / d.nb2) * d.in_b1 + (b % d.nb2) * d.in_b2 + c;
+    }
+    const float* fsrc = in + foff;
     for (int ch = 0; ch < nch; ++ch, ++g) {
       const int s = (int)(g & 1u);
-      const int k0 = ch * RKC, kc = chunk_rows(ch);
+      const int k0 = ch * RKC, kc = (Kp - k0) < RKC ? (Kp - k0) : RKC;
       if (g >= 2) {
         const bool w = tc::mbar_wait(&bar_m[s], ((g - 2) >> 1) & 1u);
         if (!(ok = bounded(w, err, 3))) break;
@@ -348,22 +298,26 @@ __global__ void __launch_bounds__(RT, 1)
           tc::bulk_g2s(tt + (uint32_t)MT * part + mt * part, src + part, part, &bar_t[s]);
         }
       }
+      for (int e0 = tid; e0 < kc * 32; e0 += XFB * RT) {
+        float4 v[XFB];
 #pragma unroll
-      for (int u = 0; u < XFB; ++u) {
-        const int e = tid + u * RT;
-        if (e >= kc * 32) break;
-        uint32_t h0, l0, h1, l1;
-        tc::split_pack(vb[u].x, vb[u].y, h0, l0);
-        tc::split_pack(vb[u].z, vb[u].w, h1, l1);
-        const uint32_t o = tc::mnmajor_offset(nf, 8 * (e >> 8) + (lane & 7), 128);
-        *reinterpret_cast<uint2*>(st + o) = make_uint2(h0, h1);
-        *reinterpret_cast<uint2*>(st + RSB + o) = make_uint2(l0, l1);
-      }
-      if (ch + 1 < nch) {
-        load_chunk(fsrc, fv, k0 + RKC, chunk_rows(ch + 1), vb);
-      } else if (itn < items) {
-        item_src(itn, nsrc, nvalid);
-        load_chunk(nsrc, nvalid, 0, chunk_rows(0), vb);
+        for (int u = 0; u < XFB; ++u) {
+          const int e = e0 + u * RT;
+          const int k = k0 + 8 * (e >> 8) + (lane & 7);
+          v[u] = (e < kc * 32 && k < d.K && fv) ? __ldg(reinterpret_cast<const float4*>(fsrc + row_in[k]))
+                                                : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < XFB; ++u) {
+          const int e = e0 + u * RT;
+          if (e >= kc * 32) break;
+          uint32_t h0, l0, h1, l1;
+          tc::split_pack(v[u].x, v[u].y, h0, l0);
+          tc::split_pack(v[u].z, v[u].w, h1, l1);
+          const uint32_t o = tc::mnmajor_offset(nf, 8 * (e >> 8) + (lane & 7), 128);
+          *reinterpret_cast<uint2*>(st + o) = make_uint2(h0, h1);
+          *reinterpret_cast<uint2*>(st + RSB + o) = make_uint2(l0, l1);
+        }
       }
       tc::fence_async_smem();
       const bool wt = tc::mbar_wait(&bar_t[s], (g >> 1) & 1u);
@@ -385,8 +339,6 @@ __global__ void __launch_bounds__(RT, 1)
       }
     }
     if (!ok) break;
-    fsrc = nsrc;
-    fv = nvalid;
     {
       const uint32_t gl = g - 1;
       const bool w = tc::mbar_wait(&bar_m[gl & 1u], (gl >> 1) & 1u);
