@@ -98,8 +98,8 @@ __global__ void __launch_bounds__(256) k_gn_bwd_stats(int mode, const float* __r
   double d1[4] = {0, 0, 0, 0}, d2[4] = {0, 0, 0, 0};   // per element slot (groups of slot j fixed per thread)
   float f1[4] = {0, 0, 0, 0}, f2[4] = {0, 0, 0, 0};
   const long step = (long)gridDim.x * 8 * Ln::VPW;
-  // UN voxels a thread are loaded before any is used (loads in flight); float partials go to double every 16 voxels
-  constexpr int UN = 8;
+  // UN voxels a thread are loaded before any is used (loads in flight); float partials go to double every 4 rounds
+  constexpr int UN = 4;
   int n = 0;
   for (long v0 = ((long)blockIdx.x * 8 + warp) * Ln::VPW + sub; active && v0 < V; v0 += UN * step) {
     float4 pu[UN], pp[UN];
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(256) k_gn_bwd_stats(int mode, const float* __r
         f2[j] += gh * xh;
       }
     }
-    if (++n * UN == 16) {
+    if (++n == 4) {
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         d1[j] += f1[j];
