@@ -78,18 +78,15 @@ struct TaGemm {
   }
 };
 
-// Issue g with the first MMAs of h (may be NULL) interleaved one to one, commit g_bar (it also covers those MMAs of
-// h), then the rest of h and commit h_bar.
-__device__ __forceinline__ void issue_pair(const TaGemm& g, uint64_t* g_bar, const TaGemm* h, uint64_t* h_bar) {
-  int th = 0;
-  for (int t = 0; t < g.n; ++t) {
-    g.issue(t);
-    if (h && th < h->n) h->issue(th++);
-  }
-  tc::mma_commit(g_bar);
-  if (h) {
-    for (; th < h->n; ++th) h->issue(th);
-    tc::mma_commit(h_bar);
+// Issue g and, interleaved in proportion, h (may be NULL).
+__device__ __forceinline__ void issue_pair(const TaGemm& g, const TaGemm* h) {
+  const int ng = g.n, nh = h ? h->n : 0;
+  int tg = 0, th = 0;
+  while (tg < ng || th < nh) {
+    if (tg < ng && (th >= nh || tg * nh <= th * ng))
+      g.issue(tg++);
+    else
+      h->issue(th++);
   }
 }
 
@@ -432,32 +429,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         alive = false;   // GEMM2 of tile i-2, the last reader of D1[s], has completed
         break;
       }
-      tc::tc_after_sync();
-      const TaGemm a = g1(i);
-      // GEMM2 of the previous tile goes along with this GEMM1 when its H is already there (independent accumulators),
-      // else after it
-      const uint32_t hp = ((uint32_t)(i - 1) >> 1) & 1u;
-      if (i >= 1 && tc::mbar_test_wait(&h_full[(i - 1) & 1], hp)) {
-        tc::tc_after_sync();
-        const TaGemm b = g2(i - 1);
-        issue_pair(a, &d1_full[s], &b, &d2_full[(i - 1) % NA]);
-        last = &d2_full[(i - 1) % NA];
-        last_par = (uint32_t)((i - 1) / NA) & 1u;
-        continue;
+      if (i >= 1 && !wait_or_flag(&h_full[(i - 1) & 1], ((uint32_t)(i - 1) >> 1) & 1u, err, 5)) {
+        alive = false;
+        break;
       }
-      issue_pair(a, &d1_full[s], nullptr, nullptr);
-      last = &d1_full[s];
-      last_par = n & 1u;
+      tc::tc_after_sync();
+      // GEMM1 of this tile interleaved with GEMM2 of the previous one (independent accumulators)
+      const TaGemm a = g1(i);
       if (i >= 1) {
-        if (!wait_or_flag(&h_full[(i - 1) & 1], hp, err, 5)) {
-          alive = false;
-          break;
-        }
-        tc::tc_after_sync();
         const TaGemm b = g2(i - 1);
-        issue_pair(b, &d2_full[(i - 1) % NA], nullptr, nullptr);
+        issue_pair(a, &b);
+        tc::mma_commit(&d1_full[s]);
+        tc::mma_commit(&d2_full[(i - 1) % NA]);
         last = &d2_full[(i - 1) % NA];
         last_par = (uint32_t)((i - 1) / NA) & 1u;
+      } else {
+        issue_pair(a, nullptr);
+        tc::mma_commit(&d1_full[s]);
+        last = &d1_full[s];
+        last_par = n & 1u;
       }
     }
     if (alive && niter >= 1) {
@@ -465,7 +455,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (wait_or_flag(&h_full[j & 1], ((uint32_t)j >> 1) & 1u, err, 6)) {
         tc::tc_after_sync();
         const TaGemm b = g2(j);
-        issue_pair(b, &d2_full[j % NA], nullptr, nullptr);
+        issue_pair(b, nullptr);
+        tc::mma_commit(&d2_full[j % NA]);
         last = &d2_full[j % NA];
         last_par = (uint32_t)(j / NA) & 1u;
       }
