@@ -59,37 +59,6 @@ __device__ __forceinline__ void mma3_ta(uint32_t d, uint32_t a_hi, uint32_t a_lo
   tc::mma_bf16_ta(d, a_lo, b_hi, idesc, 1u);
 }
 
-// One split-BF16 GEMM D (+)= A B^T with its A operand in tensor memory, as n = 3 K / 16 MMAs: MMA t is k step t / 3,
-// product t % 3 (A hi B hi, A hi B lo, A lo B hi). A chain of MMAs into one accumulator issues at one MMA per ~96
-// cycles (each waits for the previous accumulation); two independent chains interleaved keep the tensor core at its
-// full rate, so the MMA roles issue two GEMMs of different accumulators together wherever their data allow.
-struct TaGemm {
-  uint32_t d, idesc;
-  uint32_t a_hi, a_lo, a_step;   // tensor-memory columns of k step 0 (hi, lo) and the column step per k step
-  uint32_t b_hi, b_lo, b_step;   // shared addresses of the K-major B (hi, lo) at k step 0 and the byte step per k step
-  uint32_t sbo;                  // B's 8-row group stride
-  int n;
-  bool acc;                      // accumulate onto D from the first MMA
-  __device__ __forceinline__ void issue(int t) const {
-    const int k = t / 3, p = t - 3 * k;
-    const uint32_t a = (p == 2 ? a_lo : a_hi) + a_step * (uint32_t)k;
-    const uint32_t b = (p == 1 ? b_lo : b_hi) + b_step * (uint32_t)k;
-    tc::mma_bf16_ta(d, a, tc::kmajor_desc(b, 128u, sbo), idesc, (acc || t > 0) ? 1u : 0u);
-  }
-};
-
-// Issue g and, interleaved in proportion, h (may be NULL).
-__device__ __forceinline__ void issue_pair(const TaGemm& g, const TaGemm* h) {
-  const int ng = g.n, nh = h ? h->n : 0;
-  int tg = 0, th = 0;
-  while (tg < ng || th < nh) {
-    if (tg < ng && (th >= nh || tg * nh <= th * ng))
-      g.issue(tg++);
-    else
-      h->issue(th++);
-  }
-}
-
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
 }
@@ -407,16 +376,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     uint64_t* last = nullptr;
     uint32_t last_par = 0;
     bool alive = true;
-    // GEMM1 of tile i: D1[i % 2] = x W1^T (x split as [hi C/2 | lo C/2] columns of A stage i % NA); GEMM2 of tile j:
-    // D2 (over A stage j % NA) = H(j) W2^T, H in D1[j % 2] as [hi 8 | lo 8] per 16-wide k chunk
-    auto g1 = [&](int i) {
-      const uint32_t A = tmem + (uint32_t)(C * (i % NA));
-      return TaGemm{tmem + 256u + 128u * (i & 1), i1, A, A + C / 2, 8u, w1, w1 + LO, 256u, C * 16u, 3 * C / 16, false};
-    };
-    auto g2 = [&](int j) {
+    auto gemm2 = [&](int j) {   // D2 (A stage j % NA) = H(j) (in D1[j % 2]) W2^T, K = 2C
       const uint32_t h = tmem + 256u + 128u * (j & 1);
-      return TaGemm{tmem + (uint32_t)(C * (j % NA)), i2, h, h + 8u, 16u, w2, w2 + LO, 256u, 2 * C * 16u, 3 * 2 * C / 16,
-                    false};
+#pragma unroll 1
+      for (int k = 0; k < 2 * C / 16; ++k)
+        mma3_ta(tmem + (uint32_t)(C * (j % NA)), h + 16u * k, h + 16u * k + 8u,
+                tc::kmajor_desc(w2 + 256u * k, 128u, 2 * C * 16u), tc::kmajor_desc(w2 + LO + 256u * k, 128u, 2 * C * 16u),
+                i2, k > 0);
+      tc::mma_commit(&d2_full[j % NA]);
+      last = &d2_full[j % NA];
+      last_par = (uint32_t)(j / NA) & 1u;
     };
     for (int i = 0; i < niter && alive; ++i) {
       const int s = i & 1, sa = i % NA;
@@ -429,36 +398,26 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         alive = false;   // GEMM2 of tile i-2, the last reader of D1[s], has completed
         break;
       }
-      if (i >= 1 && !wait_or_flag(&h_full[(i - 1) & 1], ((uint32_t)(i - 1) >> 1) & 1u, err, 5)) {
-        alive = false;
-        break;
-      }
       tc::tc_after_sync();
-      // GEMM1 of this tile interleaved with GEMM2 of the previous one (independent accumulators)
-      const TaGemm a = g1(i);
+      const uint32_t A = tmem + (uint32_t)(C * sa), D = tmem + 256u + 128u * s;
+#pragma unroll 1
+      for (int k = 0; k < C / 16; ++k)
+        mma3_ta(D, A + 8u * k, A + C / 2 + 8u * k, tc::kmajor_desc(w1 + 256u * k, 128u, C * 16u),
+                tc::kmajor_desc(w1 + LO + 256u * k, 128u, C * 16u), i1, k > 0);
+      tc::mma_commit(&d1_full[s]);
+      last = &d1_full[s];
+      last_par = n & 1u;
       if (i >= 1) {
-        const TaGemm b = g2(i - 1);
-        issue_pair(a, &b);
-        tc::mma_commit(&d1_full[s]);
-        tc::mma_commit(&d2_full[(i - 1) % NA]);
-        last = &d2_full[(i - 1) % NA];
-        last_par = (uint32_t)((i - 1) / NA) & 1u;
-      } else {
-        issue_pair(a, nullptr);
-        tc::mma_commit(&d1_full[s]);
-        last = &d1_full[s];
-        last_par = n & 1u;
+        if (!wait_or_flag(&h_full[(i - 1) & 1], ((uint32_t)(i - 1) >> 1) & 1u, err, 5)) { alive = false; break; }
+        tc::tc_after_sync();
+        gemm2(i - 1);
       }
     }
     if (alive && niter >= 1) {
       const int j = niter - 1;
       if (wait_or_flag(&h_full[j & 1], ((uint32_t)j >> 1) & 1u, err, 6)) {
         tc::tc_after_sync();
-        const TaGemm b = g2(j);
-        issue_pair(b, nullptr);
-        tc::mma_commit(&d2_full[j % NA]);
-        last = &d2_full[j % NA];
-        last_par = (uint32_t)(j / NA) & 1u;
+        gemm2(j);
       }
     }
     if (last) tc::mbar_wait_for(last, last_par, WAIT_NS);   // no MMA in flight when tensor memory is freed
