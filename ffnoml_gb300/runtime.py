@@ -7,7 +7,9 @@ m^-3. The model sees D = nz, H = nx, W = ny. Weights and tables stay resident; h
 pinned staging buffers that are reused per shape.
 """
 import hashlib
+import os
 import threading
+from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
 import numpy as np
@@ -26,6 +28,28 @@ def load_checkpoint(path, map_location="cpu"):
         return torch.load(path, map_location=map_location, weights_only=True)
     except Exception:
         return torch.load(path, map_location=map_location, weights_only=False)
+
+
+_POOL = None
+_POOL_LOCK = threading.Lock()
+
+
+def _host_copy(dst, src):
+    """dst[...] = src for large host arrays, in chunks on a few threads (numpy releases the GIL while copying)."""
+    d, v = dst.reshape(-1), np.ascontiguousarray(src, dtype=np.float32).reshape(-1)
+    n = d.size
+    parts = min(8, os.cpu_count() or 1, max(1, n >> 22))
+    if parts <= 1:
+        np.copyto(d, v)
+        return
+    global _POOL
+    with _POOL_LOCK:
+        if _POOL is None:
+            _POOL = ThreadPoolExecutor(max_workers=8, thread_name_prefix="ffno-host-copy")
+    step = -(-n // parts)
+    futures = [_POOL.submit(np.copyto, d[i:i + step], v[i:i + step]) for i in range(0, n, step)]
+    for f in futures:
+        f.result()
 
 
 def _check(flags, what):
@@ -67,10 +91,30 @@ class GB300Backend:
 
     @property
     def _flags(self):
+        """This thread's status words on the device: [0] the request's inputs, [1] the results."""
         loc = self._local
         if not hasattr(loc, "flags"):
-            loc.flags = torch.zeros(1, dtype=torch.int32, device=self.device)
+            loc.flags = torch.zeros(2, dtype=torch.int32, device=self.device)
         return loc.flags
+
+    def _out_flags(self):
+        return self._flags.data_ptr() + 4
+
+    def _guarded(self, fn):
+        """Run the model part of a call; if it fails on a request whose inputs are invalid, report the inputs."""
+        try:
+            return fn()
+        except Exception:
+            torch.cuda.current_stream().synchronize()
+            _check(self._flags.tolist()[0], "FFNO request")
+            raise
+
+    def _finish(self):
+        """Wait for the call's work; raise on invalid inputs; return the results' status word."""
+        torch.cuda.current_stream().synchronize()
+        req, out = self._flags.tolist()
+        _check(req, "FFNO request")
+        return out
 
     @property
     def _staging(self):
@@ -111,7 +155,7 @@ class GB300Backend:
 
     def _upload(self, key, array):
         host, dev = self._stage(key, array.shape)
-        host.numpy()[...] = array
+        _host_copy(host.numpy(), array)
         dev.copy_(host, non_blocking=True)
         return dev
 
@@ -119,6 +163,13 @@ class GB300Backend:
         host, _ = self._stage(key + "_out", tensor.shape)
         host.copy_(tensor, non_blocking=True)
         return host
+
+    @staticmethod
+    def _result(host):
+        """A fresh numpy copy of a pinned result buffer (the buffer is reused by the next call)."""
+        out = np.empty(tuple(host.shape), dtype=np.float32)
+        _host_copy(out, host.numpy())
+        return out
 
     def _validate(self, features, z_scale):
         features = np.asarray(features, dtype=np.float32)
@@ -137,9 +188,9 @@ class GB300Backend:
         x = torch.empty(1, 6, nz, nx, ny, dtype=torch.float32, device=self.device)
         zmm = torch.empty(1, nz, nx, ny, dtype=torch.float32, device=self.device)
         self._flags.zero_()
+        # the request's status word is read once with the results (_finish): no synchronisation before the model
         nat.call("ffno_si_inputs", f_dev.data_ptr(), z_dev.data_ptr(), V, self.mean_x.data_ptr(),
                  self.std_x.data_ptr(), x.data_ptr(), zmm.data_ptr(), self._flags.data_ptr(), _stream())
-        _check(self._flags.item(), "FFNO request")
         return f_dev, x, zmm, V
 
     # ------------------------------------------------------------------------------------------------ API
@@ -150,15 +201,14 @@ class GB300Backend:
         _, x, zmm, V = self._prepare(features, z_scale)
         L = self.model.out_channels
         with torch.no_grad():
-            y = self.model(x, zmm, float(dx), float(dy))
+            y = self._guarded(lambda: self.model(x, zmm, float(dx), float(dy)))
         pop = torch.empty(*z_scale.shape, L, dtype=torch.float32, device=self.device)
         nat.call("ffno_si_populations", y.data_ptr(), V, L, self.mean_y.data_ptr(), self.std_y.data_ptr(),
-                 pop.data_ptr(), self._flags.data_ptr(), _stream())
+                 pop.data_ptr(), self._out_flags(), _stream())
         host = self._download("pop", pop)
-        torch.cuda.current_stream().synchronize()
-        _check(self._flags.item(), "FFNO output")
+        _check(self._finish(), "FFNO output")
         self.call_count += 1
-        return host.numpy().copy()
+        return self._result(host)
 
     def jvp_local(self, features, z_scale, dx, dy, feature_tangent):
         """Forward-mode derivative of the populations along feature_tangent (6,nz,nx,ny) in the SI units of features
@@ -174,22 +224,21 @@ class GB300Backend:
         t_dev = self._upload("tangent", tangent)
         x_dot = torch.empty_like(x)
         nat.call("ffno_si_input_tangent", f_dev.data_ptr(), t_dev.data_ptr(), V, self.std_x.data_ptr(),
-                 x_dot.data_ptr(), self._flags.data_ptr(), _stream())
-        y, y_dot = self.model.executor().jvp(x, zmm, float(dx), float(dy), x_dot)
+                 x_dot.data_ptr(), self._out_flags(), _stream())
+        y, y_dot = self._guarded(lambda: self.model.executor().jvp(x, zmm, float(dx), float(dy), x_dot))
         L = self.model.out_channels
         pop_dot = torch.empty(*z_scale.shape, L, dtype=torch.float32, device=self.device)
         nat.call("ffno_si_population_tangent", y.data_ptr(), y_dot.data_ptr(), V, L, self.mean_y.data_ptr(),
-                 self.std_y.data_ptr(), pop_dot.data_ptr(), self._flags.data_ptr(), _stream())
+                 self.std_y.data_ptr(), pop_dot.data_ptr(), self._out_flags(), _stream())
         host = self._download("pop_dot", pop_dot)
-        torch.cuda.current_stream().synchronize()
-        flags = int(self._flags.item())
+        flags = self._finish()
         if flags & 1:
             raise ValueError("FFNO JVP tangent contains NaN or Inf")
         if flags & 8:
             raise RuntimeError("FFNO JVP returned NaN or Inf")
         _check(flags, "FFNO JVP")
         self.call_count += 1
-        return host.numpy().copy()
+        return self._result(host)
 
     def vjp_local(self, features, z_scale, dx, dy, population_cotangent):
         """Input VJP along the population cotangent (nz,nx,ny,L): {"features": (6,nz,nx,ny), "z_scale": (nz,nx,ny)}
@@ -201,23 +250,30 @@ class GB300Backend:
         if tuple(cot.shape) != expected:
             raise ValueError(f"local population_cotangent has shape {cot.shape}; expected {expected}")
         f_dev, x, zmm, V = self._prepare(features, z_scale)
-        cot_dev = self._upload("cot", cot)
+        # the cotangent is not needed before the forward: its host copy into pinned staging runs on another thread
+        # while the forward does
+        cot_host, cot_dev = self._stage("cot", cot.shape)
+        copier = threading.Thread(target=_host_copy, args=(cot_host.numpy(), cot), daemon=True)
+        copier.start()
         ex = self.model.executor()
-        y, state = ex.forward(x, zmm, float(dx), float(dy), keep=True)
+        try:
+            y, state = self._guarded(lambda: ex.forward(x, zmm, float(dx), float(dy), keep=True))
+        finally:
+            copier.join()
+        cot_dev.copy_(cot_host, non_blocking=True)
         ybar = torch.empty_like(y)
         nat.call("ffno_si_population_cotangent", y.data_ptr(), cot_dev.data_ptr(), V, L, self.mean_y.data_ptr(),
-                 self.std_y.data_ptr(), ybar.data_ptr(), self._flags.data_ptr(), _stream())
-        xbar, zbar = ex.backward(state, ybar)
+                 self.std_y.data_ptr(), ybar.data_ptr(), self._out_flags(), _stream())
+        xbar, zbar = self._guarded(lambda: ex.backward(state, ybar))
         fbar = torch.empty(6, *z_scale.shape, dtype=torch.float32, device=self.device)
         zbar_m = torch.empty(*z_scale.shape, dtype=torch.float32, device=self.device)
         nat.call("ffno_si_input_grads", f_dev.data_ptr(), xbar.data_ptr(), zbar.data_ptr(), V,
-                 self.std_x.data_ptr(), fbar.data_ptr(), zbar_m.data_ptr(), self._flags.data_ptr(), _stream())
+                 self.std_x.data_ptr(), fbar.data_ptr(), zbar_m.data_ptr(), self._out_flags(), _stream())
         hf = self._download("fbar", fbar)
         hz = self._download("zbar", zbar_m)
-        torch.cuda.current_stream().synchronize()
-        flags = int(self._flags.item())
+        flags = self._finish()
         if flags & 1:
             raise ValueError("FFNO VJP cotangent contains NaN or Inf")
         _check(flags, "FFNO VJP")
         self.call_count += 1
-        return {"features": hf.numpy().copy(), "z_scale": hz.numpy().copy()}
+        return {"features": self._result(hf), "z_scale": self._result(hz)}
