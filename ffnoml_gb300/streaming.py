@@ -22,7 +22,7 @@ import torch
 
 from . import _native as nat
 from .executor import EPS, Workspace, _descs, _stream
-from .runtime import INPUT_CHANNELS, _check
+from .runtime import INPUT_CHANNELS, _check, _host_copy
 
 
 def _pinned(n):
@@ -139,7 +139,7 @@ class StreamingForward:
             self._bufs = None
             V = D * H * W
             self._bufs = dict(X=_pinned(V * C), A=_pinned(V * C), B=_pinned(V * C), F=_pinned(V * C),
-                              pop=_pinned(V * L), xn=torch.empty(6, V, dtype=torch.float32, device=dev),
+                              pop=_pinned(V * L), f_in=_pinned(6 * V), z_in=_pinned(V), xn=torch.empty(6, V, dtype=torch.float32, device=dev),
                               zmm=torch.empty(1, D, H, W, dtype=torch.float32, device=dev),
                               xs=torch.empty(6, cd * H * W, dtype=torch.float32, device=dev))
             self._bufs_key = key
@@ -170,10 +170,12 @@ class StreamingForward:
         flags = torch.zeros(1, dtype=torch.int32, device=dev)
         # normalised inputs [6][V] and heights [V] (Mm) stay on the device (7 floats a voxel against C of a hidden
         # state); converted slab by slab from the pinned host arrays by the resident path's kernel
-        f_host = torch.from_numpy(features).pin_memory()
-        zm_host = torch.from_numpy(z_m).reshape(-1).pin_memory()
         cd, cr = min(self.chunk_depth, D), min(self.chunk_rows, H)
         bufs = self._buffers(dev, D, H, W, C, L, cd)
+        # the request into pinned buffers kept with the hidden states (pinning on every call costs more than copying)
+        f_host, zm_host = bufs["f_in"], bufs["z_in"]
+        _host_copy(f_host.numpy(), features)
+        _host_copy(zm_host.numpy(), z_m)
         xn, zmm, xs = bufs["xn"], bufs["zmm"], bufs["xs"]
         fs = torch.empty(6, cd * H * W, dtype=torch.float32, device=dev)
         zin = torch.empty(cd * H * W, dtype=torch.float32, device=dev)
@@ -289,9 +291,9 @@ class StreamingForward:
         _check(flags.item(), "FFNO streaming output")
         if any(int(w.err.item()) for w in wsd + wsr):
             raise RuntimeError("tensor-core kernel timed out")
-        if log10:
-            return pop_host.numpy().reshape(L, D, H, W).copy()
-        return pop_host.numpy().reshape(D, H, W, L).copy()
+        out = np.empty((L, D, H, W) if log10 else (D, H, W, L), dtype=np.float32)
+        _host_copy(out, pop_host.numpy()[:V * L])
+        return out
 
     # ------------------------------------------------------------------------------------------------ one block
     def _block(self, pk, i, depth_ws, row_ws, hgt, pln, fq, X, A, B, F):
