@@ -292,8 +292,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 // merged in order with Chan's update, so the statistics do not depend on timing). Roles as in the backward:
 //   warp 0 TMA ring of in [and prev]; warp 1 MMA: GEMM1 D1[t % 2] = x W1^T (N = 2C), and GEMM2 D2 = H W2^T (N = C)
 //   one tile behind, so that epilogue 1 of a tile overlaps GEMM1 of the next; warps 2-5 conversion with the residual
-//   prologue (xout); warps 6-13 epilogue 1: H = gelu(D1), split over D1, then pre of the previous tile to HBM;
-//   warps 14-17 epilogue 2: the statistics of pre.
+//   prologue (xout); warps 6-13 epilogue 1: H = gelu(D1), split over D1; warps 14-17 epilogue 2: pre and statistics.
 // Tensor memory: four A stages of C columns from column 0 ([x hi | x lo], D2 of the stage's tile over them: a stage is
 // held from conversion to epilogue 2), D1 buffers at 256 and 384.
 template <int C, int MODE>
@@ -328,7 +327,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
     for (int s = 0; s < NA; ++s) {
       tc::mbar_init(&a_full[s], 128);
-      tc::mbar_init(&a_empty[s], 128 + 256);   // epilogue 2 (statistics) and epilogue 1 (stores of pre)
+      tc::mbar_init(&a_empty[s], 128);
       tc::mbar_init(&d2_full[s], 1);
     }
     tc::mbar_init(&wbar, 1);
@@ -469,33 +468,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       tc::mbar_arrive(&a_full[sa]);
     }
   } else if (ok && warp >= W_E1 && warp < W_E2) {
-    const int q = warp & 3, hf = (warp - W_E1) >> 2, r = 32 * q + lane;
+    const int q = warp & 3, hf = (warp - W_E1) >> 2;
     const uint32_t lq = (uint32_t)(32 * q) << 16;
-    // pre of tile j to HBM (this warp's half of the 16-column chunks), then its A stage's share of the release
-    auto store_pre = [&](int j) -> bool {
-      const int sj = j % NA;
-      if (!warp_wait(&d2_full[sj], (uint32_t)(j / NA) & 1u, err, 12)) return false;
-      tc::tc_after_sync();
-      const long v = tile_of(j) * TM + r;
-      const uint32_t D = tmem + lq + (uint32_t)(C * sj);
-#pragma unroll 1
-      for (int k = hf; k < C / 16; k += 2) {
-        uint32_t d[16];
-        tc::tmem_ld16u(D + 16u * k, d);
-        tc::tmem_wait_ld();
-        if (v < V)
-#pragma unroll
-          for (int e = 0; e < 4; ++e)
-            *reinterpret_cast<float4*>(pre + v * C + 16 * k + 4 * e) =
-                make_float4(__uint_as_float(d[4 * e]), __uint_as_float(d[4 * e + 1]), __uint_as_float(d[4 * e + 2]),
-                            __uint_as_float(d[4 * e + 3]));
-      }
-      tc::tc_before_sync();
-      tc::mbar_arrive(&a_empty[sj]);
-      return true;
-    };
-    bool alive = true;
-    for (int i = 0; i < niter && alive; ++i) {
+    for (int i = 0; i < niter; ++i) {
       const int s = i & 1;
       const uint32_t n = (uint32_t)i >> 1;
       if (!warp_wait(&d1_full[s], n & 1u, err, 9)) break;
@@ -516,9 +491,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       tc::tmem_wait_st();
       tc::tc_before_sync();
       tc::mbar_arrive(&h_full[s]);
-      if (i >= 1) alive = store_pre(i - 1);   // GEMM2 of the previous tile was issued before GEMM1 of this one
     }
-    if (alive && niter >= 1) store_pre(niter - 1);
   } else if (ok && warp >= W_E2) {
     const int q = warp & 3, r = 32 * q + lane, wl = warp - W_E2;
     const uint32_t lq = (uint32_t)(32 * q) << 16;
@@ -532,8 +505,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         break;
       }
       tc::tc_after_sync();
-      // pass 1 (pre goes to HBM from the epilogue-1 warps): the weighted group sums (CPG = C / 8 channels per group;
-      // a 16-column chunk holds 16 / CPG groups)
+      // pass 1: pre to HBM and the weighted group sums (CPG = C / 8 channels per group; a 16-column chunk holds
+      // 16 / CPG groups)
       const uint32_t D = tmem + lq + (uint32_t)(C * sa);
       float gs[GMAX];
 #pragma unroll
@@ -541,6 +514,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         uint32_t d[16];
         tc::tmem_ld16u(D + 16u * k, d);
         tc::tmem_wait_ld();
+        if (live)
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            *reinterpret_cast<float4*>(pre + v * C + 16 * k + 4 * e) =
+                make_float4(__uint_as_float(d[4 * e]), __uint_as_float(d[4 * e + 1]), __uint_as_float(d[4 * e + 2]),
+                            __uint_as_float(d[4 * e + 3]));
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
           const int g = (16 * k + e) / CPG;
