@@ -598,8 +598,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 // MLP: warp 0 TMA ring of x; warp 1 MMA: GEMM1 D1[t % 2] = x G1^T, and GEMM2 D2 = H G2^T one tile behind; warps 2-5
 // conversion into the A stages; warps 6-13 epilogue 1: H = gelu(D1), split over D1; warps 14-17 epilogue 2: the gate
 // applied to the tile's x rows (read from the TMA ring, four stages, each held until then) and the z_proj term.
-// Tensor memory: four A stages of C columns from column 0 (D2 of a stage's tile over them), D1 buffers at 256 and
-// 256 + C.
+// Tensor memory: four A
+// stages of C columns from column 0 (D2 of a stage's tile over them), D1 buffers at 256 and 256 + C.
 template <int C>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_gate_fwd_ws(const __grid_constant__ CUtensorMap map_x, long V,
