@@ -1,0 +1,33 @@
+"""Bitwise determinism of the split-BF16 forward and input VJP at a cube where every persistent CTA of the
+warp-specialised kernels walks many tiles (their rings and tensor-memory stages wrap many times): a race between roles
+shows up as a few voxels that differ between two runs. Also the BF16 forward against the FP32 drop-in on that cube."""
+import os
+import sys
+
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+
+def test_bf16_forward_and_vjp_are_deterministic():
+    import bench
+    model = bench.build_model().cuda().eval()
+    f_np, z_np = bench.synthetic_si((64, 64, 64), seed=1)
+    x_np, z_mm = bench.normalised(f_np, z_np)
+    x, z = torch.from_numpy(x_np).cuda(), torch.from_numpy(z_mm).cuda()
+    cot = torch.randn(1, 12, 64, 64, 64, generator=torch.Generator().manual_seed(3)).cuda()
+    ex = model.executor()
+    runs = []
+    for _ in range(2):
+        y, state = ex.forward(x, z, bench.DXY, bench.DXY, keep=True)
+        xb, zb = ex.backward(state, cot)
+        runs.append((y.clone(), xb.clone(), zb.clone()))
+    for a, b in zip(runs[0], runs[1]):
+        assert torch.equal(a, b)
+    model.set_precision("fp32")
+    y32 = ex.forward(x, z, bench.DXY, bench.DXY)[0]
+    model.set_precision("bf16")
+    assert float((runs[0][0] - y32).abs().max()) < 2e-3
