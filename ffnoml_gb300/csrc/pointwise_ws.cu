@@ -1627,8 +1627,11 @@ __global__ void __launch_bounds__(448, 1)
           bv[c] = (base && live) ? __ldg(reinterpret_cast<const float4*>(base + v * C) + c)
                                  : make_float4(0.f, 0.f, 0.f, 0.f);
         if (!warp_wait(&d2_full[t], par, err, 10)) { alive = false; break; }
+        // x and g_bar of tile i in its ring stage (i & 1 == t): this warp waits on the stage's TMA barrier itself
+        // (its phase cannot move on before this epilogue releases the stage), which makes the copy visible to it
+        if (!warp_wait(&stg_full[t], par, err, 14)) { alive = false; break; }
         tc::tc_after_sync();
-        const uint8_t* st = ring + t * SB;   // stage of tile i (i & 1 == t)
+        const uint8_t* st = ring + t * SB;
         float zs = 0.f;
 #pragma unroll
         for (int k = 0; k < C / 16; ++k) {
