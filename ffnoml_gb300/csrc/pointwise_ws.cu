@@ -597,12 +597,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 // The ffno_gate_fwd_tc contract: out = x sigmoid(gelu(x G1^T) G2^T) [+ zp z], G1, G2: [C][C]. Roles as in the forward
 // MLP: warp 0 TMA ring of x; warp 1 MMA: GEMM1 D1[t % 2] = x G1^T, and GEMM2 D2 = H G2^T one tile behind; warps 2-5
 // conversion into the A stages; warps 6-13 epilogue 1: H = gelu(D1), split over D1; warps 14-17 epilogue 2: the gate
-// applied to the tile's x rows (read from the TMA ring, four stages, each held until then) and the z_proj term.
-// Tensor memory: four A stages of C columns from column 0 (D2 of a stage's tile over them), D1 buffers at 256 and
-// 256 + C.
+// applied to the tile's x rows (loaded from HBM before D2 is waited for) and the z_proj term. Tensor memory: four A
+// stages of C columns from column 0 (D2 of a stage's tile over them), D1 buffers at 256 and 256 + C.
 template <int C>
 __global__ void __launch_bounds__(NTHREADS, 1)
-    k_gate_fwd_ws(const __grid_constant__ CUtensorMap map_x, long V,
+    k_gate_fwd_ws(const __grid_constant__ CUtensorMap map_x, const float* __restrict__ x, long V,
                   const uint8_t* __restrict__ wpack, const float* __restrict__ zp, const float* __restrict__ z,
                   float* __restrict__ out, int* __restrict__ err) {
   static_assert(C == 32 || C == 64, "widths 32 and 64");
@@ -611,21 +610,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   constexpr int NB = C / 32;
   constexpr uint32_t SB = NB * BOX_BYTES;        // one ring stage: x
   constexpr int NA = 4;                          // A stages
-  constexpr int NS = 4;                          // ring stages: a stage is held until epilogue 2 has read x
   static_assert(WB % 1024 == 0, "the ring must stay 1024-byte aligned (128-byte swizzle)");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* ring = smem + WB;
-  __shared__ uint64_t stg_full[NS], stg_empty[NS], a_full[NA], a_empty[NA], d2_full[NA], d1_full[2], h_full[2], wbar;
+  __shared__ uint64_t stg_full[2], stg_empty[2], a_full[NA], a_empty[NA], d2_full[NA], d1_full[2], h_full[2], wbar;
   __shared__ uint32_t tslot;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp == 0) tc::tmem_alloc(&tslot, 512);
   if (threadIdx.x == 0) {
-    for (int s = 0; s < NS; ++s) {
+    for (int s = 0; s < 2; ++s) {
       tc::mbar_init(&stg_full[s], 1);
       tc::mbar_init(&stg_empty[s], 128);
-    }
-    for (int s = 0; s < 2; ++s) {
       tc::mbar_init(&d1_full[s], 1);
       tc::mbar_init(&h_full[s], 256);
     }
@@ -654,10 +650,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   constexpr uint32_t D1C = 256;
 
   if (ok && warp == W_TMA && lane == 0) {
-    int issued[NS] = {0, 0, 0, 0};
+    int issued[2] = {0, 0};
     for (int i = 0; i < niter; ++i) {
-      const int s = i % NS;
-      const uint32_t n = (uint32_t)(i / NS);
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
       if (!wait_or_flag(&stg_empty[s], (n & 1u) ^ 1u, err, 3)) break;
       const int row = (int)(tile_of(i) * TM);
       tc::mbar_arrive_expect_tx(&stg_full[s], SB);
@@ -666,7 +662,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (int b = 0; b < NB; ++b) tc::tma_load_2d(st + b * BOX_BYTES, &map_x, 32 * b, row, &stg_full[s]);
       ++issued[s];
     }
-    for (int s = 0; s < NS; ++s)
+    for (int s = 0; s < 2; ++s)
       if (issued[s]) tc::mbar_wait_for(&stg_full[s], (uint32_t)(issued[s] - 1) & 1u, WAIT_NS);
   } else if (ok && warp == W_MMA && lane == 0) {
     const uint32_t id = tc::idesc_bf16(128, C);
@@ -723,9 +719,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int q = warp & 3, r = 32 * q + lane;
     const uint32_t lq = (uint32_t)(32 * q) << 16;
     for (int i = 0; i < niter; ++i) {
-      const int s = i % NS;
+      const int s = i & 1;
+      const uint32_t n = (uint32_t)i >> 1;
       const int sa = i % NA;
-      if (!warp_wait(&stg_full[s], (uint32_t)(i / NS) & 1u, err, 7)) break;
+      if (!warp_wait(&stg_full[s], n & 1u, err, 7)) break;
       if (!warp_wait(&a_empty[sa], ((uint32_t)(i / NA) & 1u) ^ 1u, err, 8)) break;
       tc::tc_after_sync();
       const uint8_t* st = ring + s * SB;
@@ -744,6 +741,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         tc::tmem_st8u(A + (uint32_t)(8 * bh), hi);
         tc::tmem_st8u(A + (uint32_t)(C / 2 + 8 * bh), lo);
       }
+      tc::mbar_arrive(&stg_empty[s]);
       tc::tmem_wait_st();
       tc::tc_before_sync();
       tc::mbar_arrive(&a_full[sa]);
@@ -777,16 +775,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int q = warp & 3, r = 32 * q + lane;
     const uint32_t lq = (uint32_t)(32 * q) << 16;
     for (int i = 0; i < niter; ++i) {
-      const int sa = i % NA, st = i % NS;
+      const int sa = i % NA;
       const long v = tile_of(i) * TM + r;
       const bool live = v < V;
+      float4 xv[C / 4];
+#pragma unroll
+      for (int c = 0; c < C / 4; ++c)
+        xv[c] = live ? __ldg(reinterpret_cast<const float4*>(x + v * C) + c) : make_float4(0.f, 0.f, 0.f, 0.f);
       const float zv = (zp && live) ? __ldg(z + v) : 0.f;
       if (!warp_wait(&d2_full[sa], (uint32_t)(i / NA) & 1u, err, 10)) break;
-      // the tile's x rows, still in the ring: this warp waits on the stage's TMA barrier itself (its phase cannot move
-      // on before this epilogue releases the stage), which makes the bulk copy's data visible to it
-      if (!warp_wait(&stg_full[st], (uint32_t)(i / NS) & 1u, err, 13)) break;
       tc::tc_after_sync();
-      const uint8_t* rx = ring + st * SB + r * 128;
 #pragma unroll
       for (int k = 0; k < C / 16; ++k) {
         uint32_t d[16];
@@ -796,16 +794,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           tc::tc_before_sync();
           tc::mbar_arrive(&a_empty[sa]);
         }
-        float4 xk[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-          xk[e] = *reinterpret_cast<const float4*>(rx + (k >> 1) * BOX_BYTES + (((4 * (k & 1) + e) ^ (r & 7)) << 4));
-        if (k == C / 16 - 1) tc::mbar_arrive(&stg_empty[st]);   // x has been read: the ring stage may refill
         if (live) {
           float4* o = reinterpret_cast<float4*>(out + v * C + 16 * k);
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
-            const float4 x4 = xk[e];
+            const float4 x4 = xv[4 * k + e];
             float4 y = make_float4(x4.x * sigmoid_tc(__uint_as_float(d[4 * e])),
                                    x4.y * sigmoid_tc(__uint_as_float(d[4 * e + 1])),
                                    x4.z * sigmoid_tc(__uint_as_float(d[4 * e + 2])),
@@ -1756,12 +1749,12 @@ int launch_gate_fwd(const float* x, long V, const void* wpack, const float* zp, 
                     cudaStream_t s) {
   CUtensorMap mx;
   if (!row_map(&mx, x, V, C)) return FFNO_EINVAL;
-  const size_t smem = 1024 + 2 * (size_t)mat_bytes(C, C) + 4 * (size_t)((C / 32) * BOX_BYTES);
+  const size_t smem = 1024 + 2 * (size_t)mat_bytes(C, C) + 2 * (size_t)((C / 32) * BOX_BYTES);
   if (cudaFuncSetAttribute(k_gate_fwd_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return FFNO_ELAUNCH;
   const long nt = (V + TM - 1) / TM;
   const int grid = (int)(nt < sms() ? nt : sms());
-  k_gate_fwd_ws<C><<<grid, NTHREADS, smem, s>>>(mx, V, static_cast<const uint8_t*>(wpack), zp, z, out, err);
+  k_gate_fwd_ws<C><<<grid, NTHREADS, smem, s>>>(mx, x, V, static_cast<const uint8_t*>(wpack), zp, z, out, err);
   return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
 }
 
