@@ -3,7 +3,7 @@ import pytest
 import torch
 
 from golden_io import CASES, load, model_config
-from oracle.ffno_oracle import OracleFFNO3D, lte_tables, vjp
+from oracle.ffno_oracle import OracleFFNO3D, jvp, lte_tables, vjp
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -48,3 +48,31 @@ def test_lte_debye_stage_table():
     assert ndxi_h == [0.0, 1.0] and dion_h == [0.0, 1.0]
     _, _, ndxi_ca, dion_ca = lte_tables(dict(g=[2.0, 1.0], ev=[0.0, 11.9], ion=[2, 3]), 2)
     assert ndxi_ca == [0.0, 3.0] and dion_ca == [0.0, 1.0]
+
+
+@pytest.mark.parametrize("name", ["h_uniform", "batch2"])
+def test_oracle_jvp_matches_central_differences(name):
+    # the forward-mode derivative along a random direction against (f(x + h d) - f(x - h d)) / 2h in float64
+    meta, state, a = load(name)
+    oracle = OracleFFNO3D(state, model_config(meta), torch.float64)
+    x, z = a["x"].double(), a["z"].double()
+    d = torch.randn(x.shape, generator=torch.Generator().manual_seed(3), dtype=torch.float64)
+    _, yd = jvp(oracle, x, z, meta["dx"], meta["dy"], d)
+    h = 1e-5
+    with torch.no_grad():
+        fd = (oracle.forward(x + h * d, z, meta["dx"], meta["dy"])
+              - oracle.forward(x - h * d, z, meta["dx"], meta["dy"])) / (2 * h)
+    assert ((yd - fd).abs().max() / yd.abs().max()).item() < 1e-6
+
+
+@pytest.mark.parametrize("name", ["tall_box", "per_column"])
+def test_oracle_jvp_is_the_transpose_of_the_vjp(name):
+    # <cot, J d> == <J^T cot, d>: the forward- and reverse-mode derivatives of the oracle are one Jacobian
+    meta, state, a = load(name)
+    oracle = OracleFFNO3D(state, model_config(meta), torch.float64)
+    x, z = a["x"].double(), a["z"].double()
+    d = torch.randn(x.shape, generator=torch.Generator().manual_seed(5), dtype=torch.float64)
+    _, yd = jvp(oracle, x, z, meta["dx"], meta["dy"], d)
+    _, xb, _ = vjp(oracle, x, z, meta["dx"], meta["dy"], a["cot"].double())
+    lhs, rhs = (a["cot"].double() * yd).sum().item(), (xb * d).sum().item()
+    assert abs(lhs - rhs) <= 1e-10 * max(abs(lhs), abs(rhs))
