@@ -76,3 +76,16 @@ def test_tall_columns_take_a_longer_box():
     assert abs(length - 30.0) < 1e-12 and k.numel() == 61
     length, k = tb.height_box(9.0, 20.0, 0.5, 41)
     assert length == 20.0 and k.numel() == 41
+
+
+@pytest.mark.parametrize("ion", [[1, 1, 2], [2, 2, 3], [1, 2, 3], [3, 3, 4], [2, 3, 5]])
+def test_lte_level_tables_match_the_oracle(ion):
+    from ffnoml_gb300 import lte
+    atom = dict(g=[2.0, 8.0, 1.0], ev=[0.0, 10.2, 13.6], ion=ion)
+    assert lte.tables(atom, 3) == orc.lte_tables(atom, 3)
+
+
+def test_lte_level_tables_refuse_a_level_count_mismatch():
+    from ffnoml_gb300 import lte
+    with pytest.raises(ValueError):
+        lte.tables(dict(g=[2.0, 1.0], ev=[0.0, 13.6], ion=[1, 2]), 3)
