@@ -36,6 +36,8 @@ _POOL_LOCK = threading.Lock()
 
 def _host_copy(dst, src):
     """dst[...] = src for large host arrays, in chunks on a few threads (numpy releases the GIL while copying)."""
+    if not dst.flags.c_contiguous or dst.dtype != np.float32 or dst.size != np.size(src):
+        raise ValueError("host copy needs a C-contiguous float32 destination of the source's size")
     d, v = dst.reshape(-1), np.ascontiguousarray(src, dtype=np.float32).reshape(-1)
     n = d.size
     parts = min(8, os.cpu_count() or 1, max(1, n >> 22))

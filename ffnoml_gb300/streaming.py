@@ -139,7 +139,8 @@ class StreamingForward:
             self._bufs = None
             V = D * H * W
             self._bufs = dict(X=_pinned(V * C), A=_pinned(V * C), B=_pinned(V * C), F=_pinned(V * C),
-                              pop=_pinned(V * L), f_in=_pinned(6 * V), z_in=_pinned(V), xn=torch.empty(6, V, dtype=torch.float32, device=dev),
+                              pop=_pinned(V * L), f_in=_pinned(6 * V), z_in=_pinned(V),
+                              xn=torch.empty(6, V, dtype=torch.float32, device=dev),
                               zmm=torch.empty(1, D, H, W, dtype=torch.float32, device=dev),
                               xs=torch.empty(6, cd * H * W, dtype=torch.float32, device=dev))
             self._bufs_key = key

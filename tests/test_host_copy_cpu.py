@@ -25,3 +25,17 @@ def test_host_copy_shapes_and_types():
     d2 = np.empty((40, 30, 20), np.float32)
     _host_copy(d2, t)
     assert np.array_equal(d2, t)
+
+
+def test_host_copy_refuses_a_destination_it_cannot_fill_in_place():
+    src = np.ones((4, 5), np.float32)
+    for dst in (np.empty((5, 4), np.float32).T, np.empty((4, 5), np.float64), np.empty((2, 9), np.float32)):
+        with pytest.raises(ValueError):
+            _host_copy(dst, src)
+
+
+def test_host_copy_flattens_into_a_flat_buffer():
+    src = np.arange(24, dtype=np.float32).reshape(2, 3, 4)
+    dst = np.empty(24, np.float32)                        # the streaming forward's flat pinned buffers
+    _host_copy(dst, src)
+    assert np.array_equal(dst, src.reshape(-1))
