@@ -796,6 +796,7 @@ extern "C" {
 int ffno_gn_bwd_stats(int mode, const float* u, float r, const float* pre, const float* gamma, const float* beta,
                       const double* gstats, long V, int C, int groups, double* partials, int nparts,
                       ffno_stream_t stream) {
+  if (!u || !pre || !gamma || !beta || !gstats || !partials) return FFNO_EINVAL;
   if (!width_ok(C) || V < 1 || groups < 1 || groups > GMAX || C % groups || nparts < 1) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   const int cpg = C / groups;
@@ -809,7 +810,7 @@ int ffno_gn_bwd_stats(int mode, const float* u, float r, const float* pre, const
 }
 
 int ffno_gn_bwd_final(const double* partials, int nparts, int groups, double* sums, ffno_stream_t stream) {
-  if (nparts < 1 || groups < 1 || groups > GMAX) return FFNO_EINVAL;
+  if (!partials || !sums || nparts < 1 || groups < 1 || groups > GMAX) return FFNO_EINVAL;
   k_gn_bwd_final<<<1, 512, 0, (cudaStream_t)stream>>>(partials, nparts, groups, sums);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
@@ -818,6 +819,7 @@ int ffno_gn_bwd_final(const double* partials, int nparts, int groups, double* su
 int ffno_gn_bwd_apply(int mode, const float* u, float r, const float* pre, const float* gamma, const float* beta,
                       const double* gstats, const double* sums, const float* dw, long V, int C, int groups, float eps,
                       float* pre_bar, float* w_bar, ffno_stream_t stream) {
+  if (!u || !pre || !gamma || !beta || !gstats || !dw || !pre_bar || !w_bar) return FFNO_EINVAL;
   if (!width_ok(C) || V < 1 || groups < 1 || groups > GMAX || C % groups) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   const int cpg = C / groups;
@@ -833,7 +835,7 @@ int ffno_gn_bwd_apply(int mode, const float* u, float r, const float* pre, const
 
 int ffno_mlp2_bwd(const float* a, const float* pre_bar, const float* base, long V, int C, const float* w1,
                   const float* w2t, const float* w1t, float* a_bar, ffno_stream_t stream) {
-  if (!width_ok(C) || V < 1) return FFNO_EINVAL;
+  if (!a || !pre_bar || !w1 || !w2t || !w1t || !a_bar || !width_ok(C) || V < 1) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   switch (C) {
 #define L(CC)                                                                                   \
@@ -855,6 +857,9 @@ int ffno_fuse_bwd(const float* x, const float* spec_pre, const float* spec_coefs
                   const float* wg1, const float* wg2, const float* bg2, const float* wf1, const float* wf2t,
                   const float* wf1t, const float* wg2t, const float* wg1t, float* x_bar, float* spec_bar,
                   float* vert_bar, ffno_stream_t stream) {
+  if (!x || !spec_pre || !spec_coefs || !vert_pre || !vert_coefs || !fused_pre_bar || !wg1 || !wg2 || !bg2 || !wf1 ||
+      !wf2t || !wf1t || !wg2t || !wg1t || !x_bar || !spec_bar || !vert_bar)
+    return FFNO_EINVAL;
   if (!width_ok(C) || V < 1) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   switch (C) {
@@ -879,6 +884,8 @@ int ffno_gate_bwd(const float* x, const float* xs_bar, const float* xv_bar, cons
                   const float* s_w1, const float* s_w2, const float* s_w2t, const float* s_w1t, const float* v_w1,
                   const float* v_w2, const float* v_w2t, const float* v_w1t, const float* zp, float* x_bar,
                   float* z_bar, ffno_stream_t stream) {
+  if (!x || !xs_bar || !xv_bar || !s_w1 || !s_w2 || !s_w2t || !s_w1t || !v_w1 || !v_w2 || !v_w2t || !v_w1t || !x_bar)
+    return FFNO_EINVAL;
   if (!width_ok(C) || V < 1 || (zp && !z_bar)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   switch (C) {
@@ -899,7 +906,7 @@ int ffno_gate_bwd(const float* x, const float* xs_bar, const float* xv_bar, cons
 
 int ffno_lift_bwd(const float* pre_bar, int cin, long V, int C, const float* w_lift, float* x_in_bar,
                   ffno_stream_t stream) {
-  if (!width_ok(C) || V < 1 || cin < 1 || cin > 8) return FFNO_EINVAL;
+  if (!pre_bar || !w_lift || !x_in_bar || !width_ok(C) || V < 1 || cin < 1 || cin > 8) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   switch (C) {
 #define L(CC) case CC: k_lift_bwd<CC><<<grid_of(V, BM, 4), NT, 0, s>>>(pre_bar, cin, V, w_lift, x_in_bar); break;
@@ -913,6 +920,7 @@ int ffno_lift_bwd(const float* pre_bar, int cin, long V, int C, const float* w_l
 int ffno_head_bwd(const float* x, const float* x_in, const float* y_bar, long V, int C, const float* p1,
                   const float* p2, const float* b2, const float* p2t, const float* p1t, int nhp,
                   const ffno_head_params* params, float* x_bar, float* x_in_bar, ffno_stream_t stream) {
+  if (!x || !x_in || !y_bar || !p1 || !p2 || !b2 || !p2t || !p1t || !x_bar || !x_in_bar) return FFNO_EINVAL;
   if (!width_ok(C) || V < 1 || !params || (nhp != 16 && nhp != 32)) return FFNO_EINVAL;
   if (params->nspecies < 1 || params->nspecies > FFNO_MAX_SPECIES || params->in_channels > 8) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;

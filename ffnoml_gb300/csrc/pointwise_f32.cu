@@ -488,6 +488,7 @@ int ffno_column_info(const float* z, int D, long HW, float* out, ffno_stream_t s
 
 int ffno_lift_fwd(const float* x_in, int cin, long V, int C, const float* w_lift, const float* dw, float* pre,
                   double* partials, int nparts, int groups, ffno_stream_t stream) {
+  if (!x_in || !w_lift || !dw || !pre || !partials) return FFNO_EINVAL;
   if (!width_ok(C) || cin < 1 || cin > 8 || V < 1 || groups < 1 || groups > GMAX || C % groups) return FFNO_EINVAL;
   if (nparts != ffno_stats_parts(V)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
@@ -503,6 +504,7 @@ int ffno_lift_fwd(const float* x_in, int cin, long V, int C, const float* w_lift
 
 int ffno_gn_finalize(const double* partials, int nparts, int C, int groups, const float* gamma, const float* beta,
                      float eps, float* coefs, double* gstats, ffno_stream_t stream) {
+  if (!partials || !gamma || !beta || !coefs) return FFNO_EINVAL;
   if (nparts < 1 || C < 1 || groups < 1 || groups > GMAX || C % groups) return FFNO_EINVAL;
   k_gn_finalize<<<1, 512, 0, (cudaStream_t)stream>>>(partials, nparts, C, groups, gamma, beta, eps, coefs, gstats);
   FFNO_CHECK_LAUNCH();
@@ -540,7 +542,7 @@ int ffno_resid_out(const float* x2, const float* pre, const float* coefs, float 
 
 int ffno_gate_fwd(const float* x, long V, int C, const float* w1, const float* w2, const float* zp, const float* z,
                   float* out, ffno_stream_t stream) {
-  if (!width_ok(C) || V < 1 || (zp && !z)) return FFNO_EINVAL;
+  if (!x || !w1 || !w2 || !out || !width_ok(C) || V < 1 || (zp && !z)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   const size_t smem = 2 * BM * (C + 1) * sizeof(float);
   switch (C) {
@@ -559,6 +561,7 @@ int ffno_gate_fwd(const float* x, long V, int C, const float* w1, const float* w
 int ffno_mlp2_fwd(int mode, const float* in, const float* prev_pre, const float* prev_coefs, float res, float* xout,
                   long V, int C, const float* w1, const float* w2, const float* dw, float* pre, double* partials,
                   int nparts, int groups, ffno_stream_t stream) {
+  if (!in || !w1 || !w2 || !dw || !pre || !partials) return FFNO_EINVAL;
   if (!width_ok(C) || V < 1 || mode < 0 || mode > 2 || groups < 1 || groups > GMAX || C % groups) return FFNO_EINVAL;
   if (mode && (!prev_pre || !prev_coefs || !xout)) return FFNO_EINVAL;
   if (nparts != ffno_stats_parts(V)) return FFNO_EINVAL;
@@ -594,6 +597,9 @@ int ffno_fuse_fwd(const float* x, const float* spec_pre, const float* spec_coefs
                   const float* vert_coefs, long V, int C, const float* wg1, const float* wg2, const float* bg2,
                   const float* wf1, const float* wf2, const float* dw, float* pre, double* partials, int nparts,
                   int groups, ffno_stream_t stream) {
+  if (!x || !spec_pre || !spec_coefs || !vert_pre || !vert_coefs || !wg1 || !wg2 || !bg2 || !wf1 || !wf2 || !dw ||
+      !pre || !partials)
+    return FFNO_EINVAL;
   if (!width_ok(C) || V < 1 || groups < 1 || groups > GMAX || C % groups) return FFNO_EINVAL;
   if (nparts != ffno_stats_parts(V)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
@@ -617,6 +623,7 @@ int ffno_fuse_fwd(const float* x, const float* spec_pre, const float* spec_coefs
 int ffno_head_fwd(const float* x, const float* x_in, long V, int C, const float* p1, const float* p2, const float* b2,
                   int nh, int nhp, const ffno_head_params* params, float* out, float* head_out,
                   ffno_stream_t stream) {
+  if (!x || !x_in || !p1 || !p2 || !b2 || !out) return FFNO_EINVAL;
   if (!width_ok(C) || V < 1 || !params || (nhp != 16 && nhp != 32) || nh > nhp) return FFNO_EINVAL;
   if (params->nspecies < 1 || params->nspecies > FFNO_MAX_SPECIES) return FFNO_EINVAL;
   int tot = 0;

@@ -1348,6 +1348,7 @@ int ffno_tc_set_prefetch_tiles(int tiles) {
 int ffno_mlp2_fwd_tc(int mode, const float* in, const float* prev_pre, const float* prev_coefs, float res, float* xout,
                      long V, int C, const void* wpack, const float* dw, float* pre, double* partials, int nparts,
                      int groups, int* err, ffno_stream_t stream) {
+  if (!in || !wpack || !dw || !pre || !partials) return FFNO_EINVAL;
   if (!tc_width(C) || V < 1 || mode < 0 || mode > 2 || groups != GMAX || !err || !aligned16(wpack)) return FFNO_EINVAL;
   if (mode && (!prev_pre || !prev_coefs || !xout)) return FFNO_EINVAL;
   if (nparts != grid_tc(V)) return FFNO_EINVAL;
@@ -1374,7 +1375,7 @@ int ffno_mlp2_fwd_tc(int mode, const float* in, const float* prev_pre, const flo
 
 int ffno_gate_fwd_tc(const float* x, long V, int C, const void* wpack, const float* zp, const float* z, float* out,
                      int* err, ffno_stream_t stream) {
-  if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z)) return FFNO_EINVAL;
+  if (!x || !wpack || !out || !tc_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   if (ws::gate_fwd_supported(C)) return ws::gate_fwd(x, V, C, wpack, zp, z, out, err, s);
   TC_DISPATCH(C, {
@@ -1389,6 +1390,7 @@ int ffno_gate_fwd_tc(const float* x, long V, int C, const void* wpack, const flo
 int ffno_fuse1_tc(const float* x, const float* spec_pre, const float* spec_coefs, const float* vert_pre,
                   const float* vert_coefs, long V, int C, const void* wpack, const float* bias, float* gates,
                   float* hg, int* err, ffno_stream_t stream) {
+  if (!x || !spec_pre || !spec_coefs || !vert_pre || !vert_coefs || !wpack || !bias) return FFNO_EINVAL;
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || !gates) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   if (ws::fuse1_supported(C))
@@ -1406,6 +1408,8 @@ int ffno_fuse1_tc(const float* x, const float* spec_pre, const float* spec_coefs
 int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
                   const float* gates, long V, int C, const void* wpack, const float* dw, float* pre, double* partials,
                   int nparts, int groups, int* err, ffno_stream_t stream) {
+  if (!spec_pre || !spec_coefs || !vert_pre || !vert_coefs || !gates || !wpack || !dw || !pre || !partials)
+    return FFNO_EINVAL;
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || groups != GMAX || nparts != grid_tc(V)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   if (ws::fuse2_supported(C))
@@ -1423,7 +1427,7 @@ int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* v
 
 int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack,
                      float* a_bar, int* err, ffno_stream_t stream) {
-  if (!tc_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!a || !pre_bar || !wpack || !a_bar || !tc_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   if (ws::mlp2_bwd_supported(C)) return ws::mlp2_bwd(a, pre_bar, base, V, C, wpack, a_bar, err, s);
   TC_DISPATCH(C, {
@@ -1438,6 +1442,7 @@ int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, lo
 
 int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long V, int C, const void* wpack,
                      const float* zp, float* x_bar, float* z_bar, int* err, ffno_stream_t stream) {
+  if (!x || !g_bar || !wpack || !x_bar) return FFNO_EINVAL;
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z_bar)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   if (ws::gate_bwd_supported(C)) return ws::gate_bwd(x, g_bar, base, V, C, wpack, zp, x_bar, z_bar, err, s);
@@ -1454,6 +1459,8 @@ int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long
 int ffno_fuse_bwd_a_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
                        const float* gates, const float* fused_pre_bar, long V, int C, const void* wpack,
                        float* hf_bar, int* err, ffno_stream_t stream) {
+  if (!spec_pre || !spec_coefs || !vert_pre || !vert_coefs || !gates || !fused_pre_bar || !wpack || !hf_bar)
+    return FFNO_EINVAL;
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   TC_DISPATCH(C, {
@@ -1470,6 +1477,9 @@ int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const flo
                        const float* gates, const float* hg, const float* fused_pre_bar, const float* hf_bar,
                        const float* base, long V, int C, const void* wpack, float* x_bar, float* spec_bar,
                        float* vert_bar, int* err, ffno_stream_t stream) {
+  if (!spec_pre || !spec_coefs || !vert_pre || !vert_coefs || !gates || !hg || !fused_pre_bar || !hf_bar || !wpack ||
+      !x_bar || !spec_bar || !vert_bar)
+    return FFNO_EINVAL;
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   TC_DISPATCH(C, {
@@ -1528,7 +1538,7 @@ static bool head_ok(const ffno_head_params* hp, int nh, int nhp) {
 int ffno_head_fwd_tc(const float* x, const float* x_in, long V, int C, const void* wpack, const float* b2, int nh,
                      int nhp, const ffno_head_params* params, float* out, float* head_out, int* err,
                      ffno_stream_t stream) {
-  if (!tc_width(C) || V < 1 || !x || !x_in || !b2 || !out || !err || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!tc_width(C) || V < 1 || !x || !x_in || !wpack || !b2 || !out || !err || !aligned16(wpack)) return FFNO_EINVAL;
   if (!head_ok(params, nh, nhp)) return FFNO_EINVAL;
   const uint8_t* w = static_cast<const uint8_t*>(wpack);
   cudaStream_t s = (cudaStream_t)stream;
@@ -1542,7 +1552,8 @@ int ffno_head_fwd_tc(const float* x, const float* x_in, long V, int C, const voi
 int ffno_head_bwd_tc(const float* x, const float* x_in, const float* y_bar, long V, int C, const void* wpack,
                      const float* b2, int nhp, const ffno_head_params* params, float* x_bar, float* x_in_bar,
                      int* err, ffno_stream_t stream) {
-  if (!tc_width(C) || V < 1 || !x || !x_in || !y_bar || !b2 || !x_bar || !x_in_bar || !err || !aligned16(wpack))
+  if (!tc_width(C) || V < 1 || !x || !x_in || !y_bar || !wpack || !b2 || !x_bar || !x_in_bar || !err ||
+      !aligned16(wpack))
     return FFNO_EINVAL;
   if (!head_ok(params, -1, nhp)) return FFNO_EINVAL;
   const uint8_t* w = static_cast<const uint8_t*>(wpack);

@@ -108,7 +108,7 @@ extern "C" {
 
 int ffno_si_inputs(const float* features, const float* z_m, long V, const float* mean_x, const float* std_x,
                    float* x, float* z_mm, int* flags, ffno_stream_t stream) {
-  if (!features || !z_m || !x || !z_mm || !flags || V < 1) return FFNO_EINVAL;
+  if (!features || !z_m || !mean_x || !std_x || !x || !z_mm || !flags || V < 1) return FFNO_EINVAL;
   k_si_inputs<<<grid1d(V), 256, 0, (cudaStream_t)stream>>>(features, z_m, V, mean_x, std_x, x, z_mm, flags);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
@@ -116,7 +116,7 @@ int ffno_si_inputs(const float* features, const float* z_m, long V, const float*
 
 int ffno_si_populations(const float* y, long V, int L, const float* mean_y, const float* std_y, float* pop,
                         int* flags, ffno_stream_t stream) {
-  if (!y || !pop || !flags || V < 1 || L < 1) return FFNO_EINVAL;
+  if (!y || !mean_y || !std_y || !pop || !flags || V < 1 || L < 1) return FFNO_EINVAL;
   k_si_populations<<<grid1d(V), 256, 0, (cudaStream_t)stream>>>(y, V, L, mean_y, std_y, pop, flags);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
@@ -124,7 +124,7 @@ int ffno_si_populations(const float* y, long V, int L, const float* mean_y, cons
 
 int ffno_si_population_cotangent(const float* y, const float* pop_bar, long V, int L, const float* mean_y,
                                  const float* std_y, float* y_bar, int* flags, ffno_stream_t stream) {
-  if (!y || !pop_bar || !y_bar || !flags || V < 1 || L < 1) return FFNO_EINVAL;
+  if (!y || !pop_bar || !mean_y || !std_y || !y_bar || !flags || V < 1 || L < 1) return FFNO_EINVAL;
   k_si_population_cotangent<<<grid1d(V), 256, 0, (cudaStream_t)stream>>>(y, pop_bar, V, L, mean_y, std_y, y_bar,
                                                                          flags);
   FFNO_CHECK_LAUNCH();
@@ -133,7 +133,7 @@ int ffno_si_population_cotangent(const float* y, const float* pop_bar, long V, i
 
 int ffno_si_input_grads(const float* features, const float* x_bar, const float* z_bar_mm, long V, const float* std_x,
                         float* features_bar, float* z_bar_m, int* flags, ffno_stream_t stream) {
-  if (!features || !x_bar || !z_bar_mm || !features_bar || !z_bar_m || !flags || V < 1) return FFNO_EINVAL;
+  if (!features || !x_bar || !z_bar_mm || !std_x || !features_bar || !z_bar_m || !flags || V < 1) return FFNO_EINVAL;
   k_si_input_grads<<<grid1d(V), 256, 0, (cudaStream_t)stream>>>(features, x_bar, z_bar_mm, V, std_x, features_bar,
                                                                 z_bar_m, flags);
   FFNO_CHECK_LAUNCH();
