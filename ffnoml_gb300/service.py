@@ -10,7 +10,9 @@ Wire protocol (ffno_fsdp_service.py:22, 156-343; FFNOInversion.jl/src/FSDPServic
   MEMORY\\n -> OK MEMORY <n>\\n + one line per GPU: host, local rank, peak allocated, reserved, total (bytes)
   SHUTDOWN\\n -> BYE\\n
 A request that fails validation is answered with ERROR <message>\\n once its arrays have been read (as
-ffno_batched_service.py:74-77 does), and the connection stays usable.
+ffno_batched_service.py:74-77 does), and the connection stays usable. A header whose sizes do not parse, or whose
+arrays would exceed `max_request_bytes` (default: the host's physical memory), is answered with ERROR and the
+connection is closed (its arrays are not read); so is a command line longer than 64 KiB.
 
 Continuous batching: each connection has a reader that parses requests as they arrive and hands them to the scheduler
 without waiting for earlier replies, and a writer that sends replies in request order. The scheduler admits requests
@@ -20,6 +22,7 @@ their kernels overlap on the device. Weights and the shape-constant tables stay 
 `slots` is reported as the world size in READY (at least 2, so the Julia client accepts the service).
 """
 import collections
+import hmac
 import os
 import queue
 import socket
@@ -31,6 +34,7 @@ import torch
 
 PROTOCOL_VERSION = 2
 OPERATIONS = ("PREDICT", "VJP", "JVP")
+MAX_LINE = 1 << 16
 
 
 # ---------------------------------------------------------------------------------------------------- wire helpers
@@ -56,8 +60,9 @@ def array_bytes(value):
     return np.asfortranarray(value, dtype="<f4").tobytes(order="F")
 
 
-def readline(stream):
-    """One \\n-terminated line from a socket (bytes, without the terminator); b'' at end of stream."""
+def readline(stream, limit=MAX_LINE):
+    """One \\n-terminated line from a socket (bytes, without the terminator); b'' at end of stream. A line longer
+    than `limit` bytes raises ConnectionError (no command of the protocol comes near it)."""
     out = bytearray()
     while True:
         ch = stream.recv(1)
@@ -65,7 +70,22 @@ def readline(stream):
             return bytes(out) if out else b""
         if ch == b"\n":
             return bytes(out)
+        if len(out) >= limit:
+            raise ConnectionError("command line too long")
         out += ch
+
+
+def request_bytes(op, nz, nx, ny, levels):
+    """Bytes of the arrays that follow a request header."""
+    per_voxel = 7 + {"PREDICT": 0, "VJP": levels, "JVP": 6}[op]
+    return 4 * nz * nx * ny * per_voxel
+
+
+def host_memory_bytes():
+    try:
+        return os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
+    except (ValueError, OSError, AttributeError):
+        return 1 << 62
 
 
 # ---------------------------------------------------------------------------------------------------- scheduling
@@ -214,9 +234,10 @@ class Server:
     """The protocol-v2 server. backends: name -> object with predict_local / vjp_local / level_names / model."""
 
     def __init__(self, backends, token, host="127.0.0.1", port=0, slots=4, memory_fraction=0.8, budget_bytes=None,
-                 device=None, log=None):
+                 device=None, log=None, max_request_bytes=None):
         self.backends = dict(backends)
         self.token = str(token)
+        self.max_request_bytes = int(max_request_bytes or host_memory_bytes())
         self.slots = max(2, int(slots))
         self.scheduler = Scheduler(self.backends, self.slots, memory_fraction, budget_bytes, device)
         self.listener = socket.socket(socket.AF_INET, socket.SOCK_STREAM)
@@ -289,8 +310,9 @@ class Server:
         wt = threading.Thread(target=writer, daemon=True)
         wt.start()
         try:
-            hello = readline(conn).decode().split()
-            if len(hello) != 2 or hello[0] != "HELLO" or hello[1] != self.token:
+            hello = readline(conn).decode(errors="replace").split()
+            if len(hello) != 2 or hello[0] != "HELLO" or not hmac.compare_digest(hello[1].encode(),
+                                                                                   self.token.encode()):
                 conn.sendall(b"ERROR invalid handshake\n")
                 return
             conn.sendall(f"READY {PROTOCOL_VERSION} {self.slots} {len(self.backends)} FULL_SHARD_H_SLAB\n".encode())
@@ -298,7 +320,7 @@ class Server:
                 line = readline(conn)
                 if not line:
                     break
-                fields = line.decode().strip().split()
+                fields = line.decode(errors="replace").strip().split()
                 if not fields:
                     continue
                 op = fields[0]
@@ -318,6 +340,10 @@ class Server:
                     dx, dy = float(dx), float(dy)
                     if min(nz, nx, ny, levels) < 1:
                         raise ValueError("sizes must be positive")
+                    nbytes = request_bytes(op, nz, nx, ny, levels)
+                    if nbytes > self.max_request_bytes:
+                        raise ValueError(f"request arrays of {nbytes} bytes exceed the limit of "
+                                         f"{self.max_request_bytes}")
                 except ValueError as exc:
                     replies.put(f"ERROR invalid command: {exc}\n".encode())
                     break                                   # the arrays' length is unknown: the stream is lost
@@ -392,8 +418,8 @@ class Client:
 
 def main():
     """python -m ffnoml_gb300.service manifest.toml — the manifest of ffno_fsdp_service.py ([service] port, token,
-    bind_host; [[models]] name, checkpoint_path, level_names, factory_kwargs), plus optional [service] slots and
-    table_cache (a directory where the shape-constant tables persist across restarts)."""
+    bind_host; [[models]] name, checkpoint_path, level_names, factory_kwargs), plus optional [service] slots,
+    table_cache (a directory where the shape-constant tables persist across restarts) and max_request_bytes."""
     import argparse
     import tomllib
 
@@ -418,7 +444,8 @@ def main():
             b.model.executor().tables = store
         backends[str(m["name"])] = b
     server = Server(backends, svc["token"], svc.get("bind_host", "0.0.0.0"), int(svc["port"]),
-                    slots=int(svc.get("slots", 4)), log=lambda s: print(s, flush=True))
+                    slots=int(svc.get("slots", 4)), log=lambda s: print(s, flush=True),
+                    max_request_bytes=svc.get("max_request_bytes"))
     server.serve_forever()
 
 

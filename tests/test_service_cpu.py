@@ -145,3 +145,54 @@ def test_jvp_request_round_trip():
     np.testing.assert_allclose(got[..., 2], 3 * t.sum(axis=0), rtol=1e-6)
     c.close()
     srv.shutdown()
+
+
+def _raw(port):
+    import socket
+    s = socket.create_connection(("127.0.0.1", port), timeout=30)
+    return s, s.makefile("rb")
+
+
+def test_oversized_request_is_refused_before_its_arrays():
+    srv = Server({"H": FakeBackend()}, "tok", port=0, slots=2, budget_bytes=1 << 40, device="cpu",
+                 max_request_bytes=1 << 20)
+    srv.start()
+    s, rd = _raw(srv.port)
+    s.sendall(b"HELLO tok\n")
+    assert rd.readline().startswith(b"READY 2")
+    s.sendall(b"PREDICT H 1000 1000 1000 6 1.0 1.0\n")   # 28 GB of arrays announced: refused, connection closed
+    line = rd.readline()
+    assert line.startswith(b"ERROR") and b"exceed the limit" in line
+    assert rd.readline() == b""
+    s.close()
+    c = Client(srv.port, "tok")                          # the server keeps serving other connections
+    f, z = _inputs((4, 3, 2), 5)
+    assert c.request("PREDICT", "H", f, z, 1.0, 1.0, 6).shape == (4, 3, 2, 6)
+    c.close()
+    srv.shutdown()
+
+
+def test_endless_command_line_closes_the_connection():
+    srv = _server(FakeBackend())
+    s, rd = _raw(srv.port)
+    s.sendall(b"HELLO tok\n")
+    assert rd.readline().startswith(b"READY 2")
+    try:
+        s.sendall(b"A" * (1 << 17))
+    except OSError:
+        pass                                             # the server may close while the line is still arriving
+    try:
+        assert rd.readline() == b""                      # closed (or reset: the rest of the line was never read)
+    except ConnectionResetError:
+        pass
+    s.close()
+    srv.shutdown()
+
+
+def test_handshake_with_undecodable_bytes_is_refused():
+    srv = _server(FakeBackend())
+    s, rd = _raw(srv.port)
+    s.sendall(b"HELLO \xff\xfe\n")
+    assert rd.readline().startswith(b"ERROR invalid handshake")
+    s.close()
+    srv.shutdown()
