@@ -9,6 +9,7 @@ pinned staging buffers that are reused per shape.
 import hashlib
 import os
 import threading
+import warnings
 from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
@@ -21,13 +22,40 @@ from .executor import _stream
 INPUT_CHANNELS = ("temperature", "vx", "vy", "vz", "log10_ne", "log10_rho")
 
 
+def _numpy_globals():
+    """numpy's array/dtype/scalar reconstruction functions and classes, for the weights-only unpickler (checkpoints
+    whose normalisation statistics or metadata hold numpy values)."""
+    found = []
+    for mod_name, names in (("numpy._core.multiarray", ("_reconstruct", "scalar")),
+                            ("numpy.core.multiarray", ("_reconstruct", "scalar")),
+                            ("numpy", ("ndarray", "dtype"))):
+        try:
+            mod = __import__(mod_name, fromlist=list(names))
+        except ImportError:
+            continue
+        found += [getattr(mod, n) for n in names if hasattr(mod, n)]
+    found += [getattr(np.dtypes, n) for n in dir(getattr(np, "dtypes", object)) if n.endswith("DType")]
+    return [g for g in found if g is not None]
+
+
 def load_checkpoint(path, map_location="cpu"):
-    """The training checkpoint dict (model_state, normalization_stats, io_metadata), weights_only first
-    (train_utils.load_checkpoint, train_utils.py:20-92)."""
+    """The training checkpoint dict (model_state, normalization_stats, io_metadata), as the reference's
+    train_utils.load_checkpoint (train_utils.py:20-92) loads it: weights-only, then weights-only with numpy's
+    reconstruction types allowed, and only then a full unpickle, with a warning (load only trusted checkpoints)."""
     try:
         return torch.load(path, map_location=map_location, weights_only=True)
     except Exception:
-        return torch.load(path, map_location=map_location, weights_only=False)
+        pass
+    safe = getattr(torch.serialization, "safe_globals", None)
+    if safe is not None:
+        try:
+            with safe(_numpy_globals()):
+                return torch.load(path, map_location=map_location, weights_only=True)
+        except Exception:
+            pass
+    warnings.warn(f"checkpoint {path} cannot be loaded weights-only; falling back to torch.load(weights_only=False), "
+                  "which runs the file's pickled code: load only trusted checkpoints", RuntimeWarning, stacklevel=2)
+    return torch.load(path, map_location=map_location, weights_only=False)
 
 
 _POOL = None
