@@ -76,3 +76,23 @@ def test_oracle_jvp_is_the_transpose_of_the_vjp(name):
     _, xb, _ = vjp(oracle, x, z, meta["dx"], meta["dy"], a["cot"].double())
     lhs, rhs = (a["cot"].double() * yd).sum().item(), (xb * d).sum().item()
     assert abs(lhs - rhs) <= 1e-10 * max(abs(lhs), abs(rhs))
+
+
+def test_oracle_si_level_matches_the_reference_service_conversions():
+    # tests/golden/si_hca.npz: the reference's _model_inputs / linear_populations around its FFNO3D, float64
+    from oracle.ffno_oracle import jvp_si
+    meta, state, a = load("si_hca")
+    oracle = OracleFFNO3D(state, model_config(meta), torch.float64)
+    f, z, dx, dy = a["features"][None], a["z_m"][None], meta["dx"], meta["dy"]
+    canon = lambda t: t[0].permute(1, 2, 3, 0)                  # (nz, nx, ny, L) as predict_local returns it
+    fr, zr = f.clone().requires_grad_(True), z.clone().requires_grad_(True)
+    pops = canon(oracle.forward_si(fr, zr, dx, dy))
+    assert ((pops - a["pops"]).abs() / a["pops"]).max().item() < 1e-10
+    fb, zb = torch.autograd.grad(pops, (fr, zr), a["cot"])
+    for got, ref in ((fb[0], a["features_bar"]), (zb[0], a["z_bar"])):
+        for c in range(ref.shape[0] if ref.dim() == 4 else 1):     # per feature: their units differ by decades
+            g, r = (got[c], ref[c]) if ref.dim() == 4 else (got, ref)
+            assert ((g - r).abs().max() / r.abs().max()).item() < 1e-9
+    _, pdot = jvp_si(oracle, f, z, dx, dy, a["tangent"][None])
+    # per element, relative to the population (the tangent of ln n): populations span 34 decades
+    assert ((canon(pdot) - a["pops_dot"]).abs() / a["pops"]).max().item() < 1e-9
