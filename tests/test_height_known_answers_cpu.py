@@ -1,7 +1,8 @@
 """The reference's own known answers for the height operator (its tests/test_height_operator.py), restated against
 the oracle (oracle/ffno_oracle.py) and the host table builders the product uses (ffnoml_gb300/tables.py): Filon
 weights exact for piecewise-linear columns and symmetric under flipping the grid, the taper following the column
-spacing, frequency features independent of the band limit, and the same populations on any vertical grid."""
+spacing, frequency features independent of the band limit, the same populations on any vertical grid, the
+depth-weighted GroupNorm with unit weights equal to GroupNorm, and the per-column path equal to the shared-grid one."""
 import math
 
 import numpy as np
@@ -114,3 +115,37 @@ def test_same_populations_on_any_vertical_grid():
         got = populations(z).reshape(-1, len(z))
         worst = max(worst, (got - want).abs().max().item() / scale)
     assert worst < 5e-3
+
+
+def _small_oracle(seed=0):
+    from ffnoml_gb300 import FFNO3D
+    cfg = dict(in_channels=6, out_channels=6, width=16, n_layers=1, hidden_spectral=16, hidden_vertical=16,
+               species=[ATOMS["H"]], z_reference_length=40.0, z_min_wavelength=0.04, z_feature_wavelength=0.3,
+               freq_mix_rank=2)
+    torch.manual_seed(seed)
+    module = FFNO3D(**cfg)
+    state = {k: v.clone() for k, v in module.state_dict().items()}
+    for k in state:                                           # the low-rank term live, as the reference's test has it
+        if ".freq_u." in k:
+            state[k] = torch.randn(state[k].shape, generator=torch.Generator().manual_seed(seed + 1)) * 0.1
+    return orc.OracleFFNO3D(state, cfg, torch.float64)
+
+
+def test_weighted_groupnorm_with_unit_weights_is_groupnorm():
+    o = _small_oracle()
+    x = torch.randn(2, 16, 7, 3, 4, generator=torch.Generator().manual_seed(2), dtype=torch.float64)
+    got = o._wgn("lift.1", x, torch.ones(2, 1, 7, 3, 4, dtype=torch.float64))
+    want = torch.nn.functional.group_norm(x, o.groups, o.p["lift.1.weight"], o.p["lift.1.bias"], eps=1e-5)
+    assert (got - want).abs().max().item() < 1e-12
+
+
+def test_shared_grid_equals_per_column_path():
+    """The height operator on one shared column grid, and on the same grid with one column moved by 1e-9 Mm (which
+    takes the per-column path): the same output."""
+    o = _small_oracle()
+    x = torch.randn(1, 16, 300, 2, 3, generator=torch.Generator().manual_seed(3), dtype=torch.float64)
+    z = torch.linspace(6.0, 0.0, 300, dtype=torch.float64)[None, :, None, None].expand(1, 300, 2, 3).clone()
+    prefix = "blocks.0.vertical"
+    shared = o.vertical(prefix, x, z)
+    z[0, 150, 1, 2] += 1e-9
+    assert (o.vertical(prefix, x, z) - shared).abs().max().item() < 1e-6
