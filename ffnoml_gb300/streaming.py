@@ -404,6 +404,10 @@ class StreamingForward:
 
 
 _NORMS = ("spec", "vert", "fuse", "pw", "mlp")
+# the service's float32 populations are 10^clamp(log10 n, +-37) (the device kernel clamps); a value within 1e-6 dex
+# of a bound was limited
+LOG10_POPULATION_LIMIT = 37.0
+_LIMITED_HI, _LIMITED_LO = 10.0 ** (LOG10_POPULATION_LIMIT - 1e-6), 10.0 ** (1e-6 - LOG10_POPULATION_LIMIT)
 
 
 class StreamingBackend:
@@ -448,6 +452,9 @@ class StreamingBackend:
         if not (features[0] > 0).all():
             raise ValueError("FFNO request temperature must be positive")
         pop = self.forward(features, z_m, float(dx), float(dy))
+        limited = int(np.count_nonzero((pop >= _LIMITED_HI) | (pop <= _LIMITED_LO)))
+        if limited:
+            self.log(f"STREAMING {limited} predicted populations beyond 10^+-{LOG10_POPULATION_LIMIT:g} limited to it")
         if not np.isfinite(pop).all() or (pop <= 0).any():
             raise RuntimeError("FFNO returned non-positive or non-finite populations")
         return pop
