@@ -1,0 +1,53 @@
+"""GB300Backend's request validation (ffno_fsdp_runtime.py:245-258, 306-320, 350-365: the same ValueErrors) runs on
+the host before any device work: the device steps are replaced by a stub that fails the test if reached."""
+import types
+
+import numpy as np
+import pytest
+
+from ffnoml_gb300.runtime import GB300Backend
+
+
+def _backend(levels=12):
+    be = GB300Backend.__new__(GB300Backend)                  # no device: the host checks alone
+    be.model = types.SimpleNamespace(out_channels=levels)
+
+    def no_device(*args, **kw):
+        raise AssertionError("device work before the request was validated")
+    be._prepare = be._upload = be._stage = no_device
+    return be
+
+
+def _request(shape=(8, 5, 4)):
+    g = np.random.default_rng(1)
+    f = g.normal(size=(6,) + shape).astype(np.float32)
+    f[0] = 5000.0
+    return f, np.linspace(1e6, 0.0, shape[0])[:, None, None] * np.ones(shape, np.float32)
+
+
+@pytest.mark.parametrize("op", ["predict", "vjp", "jvp"])
+def test_feature_and_height_shapes_are_checked(op):
+    be, (f, z) = _backend(), _request()
+    call = {"predict": lambda ff, zz: be.predict_local(ff, zz, 48e3, 48e3),
+            "vjp": lambda ff, zz: be.vjp_local(ff, zz, 48e3, 48e3, np.zeros(zz.shape + (12,), np.float32)),
+            "jvp": lambda ff, zz: be.jvp_local(ff, zz, 48e3, 48e3, np.zeros_like(ff))}[op]
+    with pytest.raises(ValueError, match=r"features must have shape"):
+        call(f[:5], z)
+    with pytest.raises(ValueError, match=r"z_scale must have shape"):
+        call(f, z[:-1])
+
+
+def test_cotangent_shape_is_checked():
+    be, (f, z) = _backend(), _request()
+    with pytest.raises(ValueError, match=r"population_cotangent has shape .*expected \(8, 5, 4, 12\)"):
+        be.vjp_local(f, z, 48e3, 48e3, np.zeros((8, 5, 4, 6), np.float32))
+
+
+def test_tangent_shape_and_values_are_checked():
+    be, (f, z) = _backend(), _request()
+    with pytest.raises(ValueError, match=r"feature_tangent has shape"):
+        be.jvp_local(f, z, 48e3, 48e3, np.zeros((6, 8, 5, 3), np.float32))
+    t = np.zeros_like(f)
+    t[3, 2, 1, 0] = np.inf
+    with pytest.raises(ValueError, match=r"NaN or Inf"):
+        be.jvp_local(f, z, 48e3, 48e3, t)
