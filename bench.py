@@ -37,8 +37,8 @@ ATOMS = ["H", "CA"]
 DXY = 48e3
 MEAN_X = np.array([4.75, 0.0, 0.0, 0.0, 17.5, -8.0], np.float32)
 STD_X = np.array([2.5 / math.sqrt(12), 5.0, 5.0, 5.0, 7.0 / math.sqrt(12), 8.0 / math.sqrt(12)], np.float32)
-CPU_SAMPLE = (32, 16, 16)       # bounded sub-cube per step of the reference arm (same C, L, M)
-CPU_SAMPLE_FULL = (64, 32, 32)  # the cpu_baseline sub-cube (about 10-30 s of fwd+VJP on the host cores)
+CPU_SAMPLE = (64, 32, 32)       # sub-cube per step of the reference arm and of cpu_baseline (same C, L, M)
+CONFIG4 = (496, 252, 252)       # the full-volume inversion step (31.5 M voxels)
 STREAM_CHUNKS = (32, 16)        # depth planes / column rows per device slab of the host-RAM streaming forward
 KERNELS_PER_CALL = {"ffno_column_info": 3, "ffno_outer": 2}
 METRIC = "FFNO3D voxels/s fwd & fwd+VJP, BF16 vs FP32 @ |\u0394log n|\u22642e-3; p50/p99 latency"
@@ -48,11 +48,11 @@ def model_config():
     return dict(width=WIDTH, n_layers=LAYERS, z_min_wavelength=40.0 / (MODES - 1))
 
 
-def build_model(seed=0):
+def build_model(seed=0, **overrides):
     import torch
     from ffnoml_gb300 import create_ffno3d
     torch.manual_seed(seed)
-    m = create_ffno3d(6, 12, atoms=ATOMS, **model_config())
+    m = create_ffno3d(6, 12, atoms=ATOMS, **dict(model_config(), **overrides))
     with torch.no_grad():
         for name, p in m.named_parameters():
             if ".freq_u." in name:
@@ -190,7 +190,8 @@ def run_reference(args):
     model = build_model()
     state = {k: v.detach().clone() for k, v in model.state_dict().items()}
     rate, dt, cores = cpu_rate(state, CPU_SAMPLE, steps=args.steps, warmup=args.warmup)
-    sample = f"{CPU_SAMPLE[0]}x{CPU_SAMPLE[1]}x{CPU_SAMPLE[2]} sub-cube of the same model per step, fwd+VJP"
+    sample = (f"{CPU_SAMPLE[0]}x{CPU_SAMPLE[1]}x{CPU_SAMPLE[2]} sub-cube of the same model per step, fwd+VJP; "
+              "the full cube's rate is extrapolated as this per-voxel rate")
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "voxels/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
@@ -505,15 +506,35 @@ def run_gb300(args):
     if not args.fwd_only:
         mesh_maps = population_mesh_rate(dev)
 
+    # production variant P: the same model with the height operator at its production band limit (M = 1001, 340
+    # live modes at D = 256), fwd+VJP at the headline precision on the same cube
+    variant_p = None
+    if not args.no_variant_p and not args.fwd_only:
+        mp = build_model(z_min_wavelength=0.04).to(dev).set_precision(args.precision)
+        exp = mp.executor()
+        ms_p, _ = timed(lambda: exp.backward(exp.forward(x, z, DXY, DXY, keep=True)[1], cot), 2, 1)
+        hp = exp.height(exp.packed(dev), exp.geometry(z), dev)
+        variant_p = {"value": job_rate(V, world, ms_p / 1e3), "unit": "voxels/s", "ms_per_step": ms_p,
+                     "modes": mp.blocks[0].vertical.modes, "live_modes": int(hp["live"]), "pass": "fwd+vjp"}
+        del mp, exp, hp
+        torch.cuda.empty_cache()
+
+    # config 4: the full-volume inversion step [1,6,496,252,252] on this GPU (block states recomputed), with the BF16
+    # forward against the FP32 forward on the whole cube
+    config4 = None
+    if not args.no_config4 and not args.fwd_only:
+        config4 = config4_run(model, ex, dev, world, rank, timed)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         torch.set_num_threads(len(os.sched_getaffinity(0)))
         state = {k: v.detach().cpu().clone() for k, v in model.state_dict().items()}
-        S = CPU_SAMPLE_FULL
+        S = CPU_SAMPLE
         rate, dt, cores = cpu_rate(state, S, steps=1, warmup=0)
         cpu = {"value": rate, "unit": "voxels/s", "cores": cores, "kind": "port",
                "sample": f"{S[0]}x{S[1]}x{S[2]} sub-cube of the same model, one fwd+VJP "
-                         f"({dt:.1f} s), oracle port of the reference FFNO3D in float32 torch"}
+                         f"({dt:.1f} s), oracle port of the reference FFNO3D in float32 torch; the full cube's rate "
+                         "is extrapolated as this per-voxel rate"}
 
     serving = None
     if rank == 0 and not args.no_serve:
@@ -540,10 +561,50 @@ def run_gb300(args):
             "clocks": clocks, "memory": memory, "gpu_launches": launches * args.steps, "e2e": e2e,
             "cpu_baseline": cpu,
             "serving": serving, "streaming": streaming, "population_mesh": mesh_maps,
+            "variant_p": variant_p, "config4": config4,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def config4_run(model, ex, dev, world, rank, timed):
+    """fwd+VJP of the full-volume cube at the model's precision (2 timed steps), its peak device memory, and the
+    largest |d log10 n| between the BF16 and the FP32 forward on the whole cube."""
+    import torch
+    D, H, W = CONFIG4
+    V = D * H * W
+    torch.cuda.empty_cache()
+    f_np, z_np = synthetic_si(CONFIG4, seed=11 + rank)
+    x_np, z_mm = normalised(f_np, z_np)
+    del f_np, z_np
+    x = torch.from_numpy(x_np).to(dev)
+    z = torch.from_numpy(z_mm).to(dev)
+    del x_np, z_mm
+    cot = torch.randn((1, 12, D, H, W), generator=torch.Generator(dev).manual_seed(12 + rank), device=dev)
+    precision = model.precision
+    out = {"shape": list(CONFIG4), "voxels": V}
+    try:
+        torch.cuda.reset_peak_memory_stats(dev)
+        ms, _ = timed(lambda: ex.backward(ex.forward(x, z, DXY, DXY, keep=True)[1], cot), 2, 1)
+        out.update({"value": job_rate(V, world, ms / 1e3), "unit": "voxels/s", "ms_per_step": ms,
+                    "pass": "fwd+vjp", "precision": precision, "block_states": "kept" if ex.last_cached else
+                    "recomputed per block", "peak_allocated_gib": torch.cuda.max_memory_allocated(dev) / 2 ** 30})
+        if precision == "bf16":
+            with torch.no_grad():
+                y16 = ex.forward(x, z, DXY, DXY)[0]
+                model.set_precision("fp32")
+                try:
+                    y32 = ex.forward(x, z, DXY, DXY)[0]
+                finally:
+                    model.set_precision(precision)
+                out["max_abs_dlog10n_bf16_vs_fp32"] = float((y16 - y32).abs().max())
+            del y16, y32
+    except torch.cuda.OutOfMemoryError as e:
+        out["error"] = "out of device memory: " + str(e).splitlines()[0]
+    del x, z, cot
+    torch.cuda.empty_cache()
+    return out
 
 
 def serving_stream(model, n_requests, rate, seed=7, slots=4, connections=8):
@@ -625,6 +686,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-streaming", action="store_true", help="skip the host-RAM streaming forward")
+    ap.add_argument("--no-config4", action="store_true", help="skip the full-volume [1,6,496,252,252] step")
+    ap.add_argument("--no-variant-p", action="store_true", help="skip the production band limit (M = 1001) step")
     ap.add_argument("--serve-requests", type=int, default=256)
     args = ap.parse_args()
     args.shape = tuple(int(v) for v in args.shape.split(","))

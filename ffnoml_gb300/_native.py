@@ -77,6 +77,10 @@ PROTOTYPES = {
     "ffno_lift_bwd": [P, I, L, I, P, P, P],
     "ffno_head_bwd": [P, P, P, L, I, P, P, P, P, P, I, ctypes.POINTER(HeadParams), P, P, P],
     "ffno_depth_weights_bwd": [P, P, I, L, P, P],
+    "ffno_proj_fwd": [P, L, I, P, P, P, I, I, P, P],
+    "ffno_head_output": [P, P, L, I, ctypes.POINTER(HeadParams), P, P],
+    "ffno_proj_bwd": [P, P, L, I, P, P, P, P, P, I, I, P, P],
+    "ffno_head_output_bwd": [P, P, P, L, I, ctypes.POINTER(HeadParams), P, P, P],
     "ffno_outer_parts": [I, I, L],
     "ffno_outer": [P, L, I, P, L, I, L, P, I, P, I, P],
     "ffno_outer_noalloc": [P, L, I, P, L, I, L, P, I, P],

@@ -585,12 +585,14 @@ __global__ void __launch_bounds__(NT) k_lift_bwd(const float* __restrict__ pb, i
 
 // ------------------------------------------------------------------------------------------------ head backward
 
-template <int C, int NHP, typename T>
+// kLte = false: the VJP of FFNO3D._run_head alone (models/ffno_model.py:790-798); ybar is then the gradient of the
+// nh head channels [nh][V] and xin / xinbar are not used.
+template <int C, int NHP, typename T, bool kLte = true>
 __global__ void __launch_bounds__(NT) k_head_bwd(const float* __restrict__ x, const float* __restrict__ xin,
                                                  const float* __restrict__ ybar, long V, const float* __restrict__ p1,
                                                  const float* __restrict__ p2, const float* __restrict__ b2,
                                                  const float* __restrict__ p2t, const float* __restrict__ p1t,
-                                                 const __grid_constant__ ffno_head_params hp,
+                                                 const __grid_constant__ ffno_head_params hp, int nh,
                                                  float* __restrict__ xbar, float* __restrict__ xinbar) {
   extern __shared__ float sm[];
   constexpr int LA = C + 1, LH = 2 * C + 1, LO = NHP + 1;
@@ -632,7 +634,11 @@ __global__ void __launch_bounds__(NT) k_head_bwd(const float* __restrict__ x, co
       const long v = v0 + r;
       float* o = SO + r * LO;
       if (v < V) {
-        head_voxel_bwd<T>(hp, o, NHP, head_inputs(hp, xin, V, v), ybar, V, v, xinbar);
+        if constexpr (kLte) {
+          head_voxel_bwd<T>(hp, o, NHP, head_inputs(hp, xin, V, v), ybar, V, v, xinbar);
+        } else {
+          for (int c = 0; c < NHP; ++c) o[c] = c < nh ? __ldg(ybar + (long)c * V + v) : 0.f;
+        }
       } else {
         for (int c = 0; c < NHP; ++c) o[c] = 0.f;
       }
@@ -661,6 +667,21 @@ __global__ void __launch_bounds__(NT) k_head_bwd(const float* __restrict__ x, co
         for (int j = 0; j < C / 16; ++j) xbar[v * C + tx + 16 * j] = acc[i][j];
       }
     }
+  }
+}
+
+// VJP of FFNO3D.head_output on precomputed head channels: one thread per voxel; head_bar [nh][V] and x_in_bar
+// [cin][V] are written (the T, ne and rho channels carry the LTE and total terms, the others are zero).
+template <typename T>
+__global__ void __launch_bounds__(256) k_head_output_bwd(const float* __restrict__ head, const float* __restrict__ xin,
+                                                         const float* __restrict__ ybar, long V, int nh,
+                                                         const __grid_constant__ ffno_head_params hp,
+                                                         float* __restrict__ hbar, float* __restrict__ xinbar) {
+  float o[FFNO_MAX_LEVELS + FFNO_MAX_SPECIES];
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < V; v += (long)gridDim.x * blockDim.x) {
+    for (int c = 0; c < nh; ++c) o[c] = __ldg(head + (long)c * V + v);
+    head_voxel_bwd<T>(hp, o, nh, head_inputs(hp, xin, V, v), ybar, V, v, xinbar);
+    for (int c = 0; c < nh; ++c) hbar[(long)c * V + v] = o[c];
   }
 }
 
@@ -931,11 +952,11 @@ int ffno_head_bwd(const float* x, const float* x_in, const float* y_bar, long V,
     if (params->math32) {                                                                               \
       if (!smem_attr(k_head_bwd<CC, NN, float>, smem)) return FFNO_ELAUNCH;                             \
       k_head_bwd<CC, NN, float><<<grid_of(V, BM, 2), NT, smem, s>>>(x, x_in, y_bar, V, p1, p2, b2, p2t, p1t, \
-                                                                    *params, x_bar, x_in_bar);          \
+                                                                    *params, NN, x_bar, x_in_bar);          \
     } else {                                                                                            \
       if (!smem_attr(k_head_bwd<CC, NN, double>, smem)) return FFNO_ELAUNCH;                            \
       k_head_bwd<CC, NN, double><<<grid_of(V, BM, 2), NT, smem, s>>>(x, x_in, y_bar, V, p1, p2, b2, p2t, p1t, \
-                                                                     *params, x_bar, x_in_bar);         \
+                                                                     *params, NN, x_bar, x_in_bar);         \
     }                                                                                                   \
   }
     default:
@@ -1028,6 +1049,53 @@ int ffno_outer_noalloc(const float* A, long lda, int Ma, const float* B, long ld
   // every partial sum the reduction reads is written first by k_outer: nothing in the scratch has to start at zero
   k_outer<<<(unsigned)((long)ti * tj * nsplit), NT, 0, s>>>(A, lda, Ma, B, ldb, Mb, N, chunk, ti, tj, scratch);
   k_outer_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(scratch, nsplit, n, out, accumulate);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_proj_bwd(const float* x, const float* head_bar, long V, int C, const float* p1, const float* p2,
+                  const float* b2, const float* p2t, const float* p1t, int nh, int nhp, float* x_bar,
+                  ffno_stream_t stream) {
+  if (!x || !head_bar || !p1 || !p2 || !b2 || !p2t || !p1t || !x_bar) return FFNO_EINVAL;
+  if (!width_ok(C) || V < 1 || (nhp != 16 && nhp != 32) || nh < 1 || nh > nhp) return FFNO_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  ffno_head_params none{};
+  switch (C) {
+#define L(CC, NN)                                                                                        \
+  if (C == CC && nhp == NN) {                                                                            \
+    const size_t smem = (BM * (CC + 1) + 2 * BM * (2 * CC + 1) + BM * (NN + 1)) * sizeof(float);         \
+    if (!smem_attr(k_head_bwd<CC, NN, float, false>, smem)) return FFNO_ELAUNCH;                         \
+    k_head_bwd<CC, NN, float, false><<<grid_of(V, BM, 2), NT, smem, s>>>(x, nullptr, head_bar, V, p1, p2, b2, \
+                                                                         p2t, p1t, none, nh, x_bar, nullptr); \
+  }
+    default:
+      L(16, 16) L(16, 32) L(32, 16) L(32, 32) L(64, 16) L(64, 32) L(96, 16) L(96, 32)
+#undef L
+  }
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_head_output_bwd(const float* head, const float* x_in, const float* y_bar, long V, int nh,
+                         const ffno_head_params* params, float* head_bar, float* x_in_bar, ffno_stream_t stream) {
+  if (!head || !x_in || !y_bar || !params || !head_bar || !x_in_bar) return FFNO_EINVAL;
+  if (V < 1 || params->nspecies < 1 || params->nspecies > FFNO_MAX_SPECIES || params->in_channels > 8)
+    return FFNO_EINVAL;
+  int tot = 0, lv = 0;
+  for (int s = 0; s < params->nspecies; ++s) {
+    if (params->levels[s] < 1) return FFNO_EINVAL;
+    tot += params->levels[s] + 1;
+    lv += params->levels[s];
+  }
+  if (tot != nh || lv > FFNO_MAX_LEVELS) return FFNO_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long want = (V + 255) / 256, cap = 8L * sms();   // 8 CTAs of 256 threads per SM, grid-stride
+  const long blocks = want < cap ? want : cap;
+  if (params->math32)
+    k_head_output_bwd<float><<<(unsigned)blocks, 256, 0, s>>>(head, x_in, y_bar, V, nh, *params, head_bar, x_in_bar);
+  else
+    k_head_output_bwd<double><<<(unsigned)blocks, 256, 0, s>>>(head, x_in, y_bar, V, nh, *params, head_bar,
+                                                               x_in_bar);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

@@ -80,9 +80,10 @@ __device__ __forceinline__ double ln_ccon() {
 // One voxel of FFNO3D.head_output after proj2 (models/ffno_model.py:729-748): per species, logits = head channels + the
 // LTE Boltzmann/Saha log-weights of (T, ne), log-softmax over the levels, plus the bounded total b tanh(u / b),
 // log10 rho and the particle mass; normalised with mean_Y / std_Y. o: the voxel's head channels (species s: its L
-// level logits, then its total channel). The LTE math and the log-softmax run in T (double: the reference's FP64;
-// float: FP32), except the forward's sum of the max-shifted exponentials, which lie in (0, 1] and are summed in FP32
-// (relative error of the log-sum about 1e-7).
+// level logits, then its total channel). The LTE math and the log-softmax run entirely in T: double is the
+// reference's FP64 (torch.log_softmax on float64 logits, :741); float is the split-BF16 path's FP32, where the sum of
+// the max-shifted exponentials (each in (0, 1]) is compensated (below), so that the level shares of a voxel add up
+// to 1 within a few FP32 roundings.
 struct HeadInputs {
   float lt, lne, lrho;   // log10 T, log10 ne (SI), log10 rho of the voxel (denormalised)
 };
@@ -113,6 +114,28 @@ struct Lte {
   }
 };
 
+// sum_i exp(logit[i] - mx), i < L. FP64: a plain sum (the reference's float64 logsumexp). FP32: Neumaier's
+// improved Kahan-Babuska summation (A. Neumaier, "Rundungsfehleranalyse einiger Verfahren zur Summation endlicher
+// Summen", ZAMM 54 (1974) 39-51): the rounding error of every addition is carried in c and added once at the end,
+// so the result is the exactly rounded sum of the rounded terms up to O(L u^2).
+template <typename T>
+__device__ __forceinline__ T shifted_exp_sum(const T* logit, int L, T mx) {
+  T s = 0;
+  for (int i = 0; i < L; ++i) s += mexp(logit[i] - mx);
+  return s;
+}
+template <>
+__device__ __forceinline__ float shifted_exp_sum<float>(const float* logit, int L, float mx) {
+  float s = 0.f, c = 0.f;
+  for (int i = 0; i < L; ++i) {
+    const float t = expf(logit[i] - mx);
+    const float u = s + t;
+    c += fabsf(s) >= fabsf(t) ? (s - u) + t : (t - u) + s;
+    s = u;
+  }
+  return s + c;
+}
+
 // Forward: out[g * V + v] = the normalised log10 population of level g.
 template <typename T>
 __device__ __forceinline__ void head_voxel_fwd(const ffno_head_params& hp, const float* o, const HeadInputs& in,
@@ -129,9 +152,7 @@ __device__ __forceinline__ void head_voxel_fwd(const ffno_head_params& hp, const
       logit[i] = (T)o[hc + i] + e.weight(hp, lvl + i);
       mx = fmax(mx, logit[i]);
     }
-    float se = 0.f;
-    for (int i = 0; i < L; ++i) se += expf((float)(logit[i] - mx));
-    const T lse = (T)logf(se);
+    const T lse = mlog(shifted_exp_sum<T>(logit, L, mx));
     const T tb = (T)hp.total_bound;
     const T base = lrho - (T)hp.log10_particle_mass[s] + tb * mtanh((T)o[hc + L] / tb);
     for (int i = 0; i < L; ++i) {
@@ -162,8 +183,7 @@ __device__ __forceinline__ void head_voxel_bwd(const ffno_head_params& hp, float
       logit[i] = (T)o[hc + i] + e.weight(hp, lvl + i);
       mx = fmax(mx, logit[i]);
     }
-    T se = 0;
-    for (int i = 0; i < L; ++i) se += mexp(logit[i] - mx);
+    const T se = shifted_exp_sum<T>(logit, L, mx);
     T G = 0;
     for (int i = 0; i < L; ++i) {
       gl[i] = (T)__ldg(ybar + (long)(lvl + i) * V + v) / (T)hp.std_y[lvl + i];

@@ -409,7 +409,8 @@ __global__ void __launch_bounds__(NT) k_fuse(const float* __restrict__ x, const 
 
 // ------------------------------------------------------------------------------------------------ head
 
-template <int C, int NHP, typename T>
+// kLte = false: FFNO3D._run_head alone (models/ffno_model.py:790-798), the head channels into head_out, no LTE head.
+template <int C, int NHP, typename T, bool kLte = true>
 __global__ void __launch_bounds__(NT) k_head(const float* __restrict__ x, const float* __restrict__ xin, long V,
                                              const float* __restrict__ p1, const float* __restrict__ p2,
                                              const float* __restrict__ b2, int nh,
@@ -452,9 +453,23 @@ __global__ void __launch_bounds__(NT) k_head(const float* __restrict__ x, const 
         const float* o = os + r * LO;
         if (head_out)
           for (int c = 0; c < nh; ++c) head_out[(long)c * V + v] = o[c];
-        head_voxel_fwd<T>(hp, o, head_inputs(hp, xin, V, v), out, V, v);
+        if constexpr (kLte) head_voxel_fwd<T>(hp, o, head_inputs(hp, xin, V, v), out, V, v);
       }
     }
+  }
+}
+
+// FFNO3D.head_output on head channels that are already computed (models/ffno_model.py:730-749): one thread per voxel,
+// the head channels read channels-first (consecutive voxels of one channel plane per warp: coalesced), the levels
+// written channels-first. Bound by HBM: (nh + 3 + levels) * 4 bytes a voxel.
+template <typename T>
+__global__ void __launch_bounds__(256) k_head_output(const float* __restrict__ head, const float* __restrict__ xin,
+                                                     long V, int nh, const __grid_constant__ ffno_head_params hp,
+                                                     float* __restrict__ out) {
+  float o[FFNO_MAX_LEVELS + FFNO_MAX_SPECIES];
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < V; v += (long)gridDim.x * blockDim.x) {
+    for (int c = 0; c < nh; ++c) o[c] = __ldg(head + (long)c * V + v);
+    head_voxel_fwd<T>(hp, o, head_inputs(hp, xin, V, v), out, V, v);
   }
 }
 
@@ -646,6 +661,51 @@ int ffno_head_fwd(const float* x, const float* x_in, long V, int C, const float*
       L(16, 16) L(16, 32) L(32, 16) L(32, 32) L(64, 16) L(64, 32) L(96, 16) L(96, 32)
 #undef L
   }
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_proj_fwd(const float* x, long V, int C, const float* p1, const float* p2, const float* b2, int nh, int nhp,
+                  float* head, ffno_stream_t stream) {
+  if (!x || !p1 || !p2 || !b2 || !head) return FFNO_EINVAL;
+  if (!width_ok(C) || V < 1 || (nhp != 16 && nhp != 32) || nh < 1 || nh > nhp) return FFNO_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  ffno_head_params none{};
+  switch (C) {
+#define L(CC, NN)                                                                                       \
+  if (C == CC && nhp == NN) {                                                                           \
+    const size_t smem = (BM * (CC + 1) + BM * (2 * CC + 1) + BM * (NN + 1)) * sizeof(float);            \
+    if (!set_smem(k_head<CC, NN, float, false>, smem)) return FFNO_ELAUNCH;                             \
+    k_head<CC, NN, float, false><<<grid_for(V, 2), NT, smem, s>>>(x, nullptr, V, p1, p2, b2, nh, none,  \
+                                                                  nullptr, head);                       \
+  }
+    default:
+      L(16, 16) L(16, 32) L(32, 16) L(32, 32) L(64, 16) L(64, 32) L(96, 16) L(96, 32)
+#undef L
+  }
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_head_output(const float* head, const float* x_in, long V, int nh, const ffno_head_params* params,
+                     float* out, ffno_stream_t stream) {
+  if (!head || !x_in || !out || !params) return FFNO_EINVAL;
+  if (V < 1 || params->nspecies < 1 || params->nspecies > FFNO_MAX_SPECIES || params->in_channels > 8)
+    return FFNO_EINVAL;
+  int tot = 0, lv = 0;
+  for (int s = 0; s < params->nspecies; ++s) {
+    if (params->levels[s] < 1) return FFNO_EINVAL;
+    tot += params->levels[s] + 1;
+    lv += params->levels[s];
+  }
+  if (tot != nh || lv > FFNO_MAX_LEVELS) return FFNO_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long want = (V + 255) / 256, cap = 8L * num_sms();   // 8 CTAs of 256 threads per SM, grid-stride
+  const long blocks = want < cap ? want : cap;
+  if (params->math32)
+    k_head_output<float><<<(unsigned)blocks, 256, 0, s>>>(head, x_in, V, nh, *params, out);
+  else
+    k_head_output<double><<<(unsigned)blocks, 256, 0, s>>>(head, x_in, V, nh, *params, out);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

@@ -1115,3 +1115,238 @@ def _spacing(v):
             raise ValueError("spacing must be scalar.")
         return float(v.detach().item())
     raise TypeError(f"Unsupported spacing type: {type(v)}")
+
+
+# ------------------------------------------------------------------------------------------------ module pieces
+# FFNO3D._run_lift, _run_head and head_output (models/ffno_model.py:785-798, 730-749) on their own, for the reference's
+# callers that compose the model from them (ffno_batched_backend.py:280-283, FFNONet.py:1419, 1478). Each runs the
+# CUDA kernels of the whole-model path and is differentiable through the same hand-written backward kernels. The
+# lift output (the hidden state [B, C, D, H, W]) is a channels-first view of channels-last storage, the layout the
+# kernels use; _run_head takes such a view without a copy.
+
+class _LiftSpace:
+    """The buffers of one cube's lift (a Workspace's lift-related subset)."""
+
+    def __init__(self, V, C, groups, device):
+        f32 = dict(dtype=torch.float32, device=device)
+        self.V = V
+        self.nparts = nat.lib().ffno_stats_parts(V)
+        self.dw = torch.empty(V, **f32)
+        self.pre = torch.empty(V, C, **f32)
+        self.partials = torch.empty(max(self.nparts, 1) * groups * 3, dtype=torch.float64, device=device)
+        self.coefs = {"lift": torch.empty(3 * C, **f32)}
+        self.gstats = {"lift": torch.empty(groups * 3, dtype=torch.float64, device=device)}
+
+
+def _check_cuda_f32(*ts):
+    for t in ts:
+        if not t.is_cuda:
+            raise RuntimeError("ffnoml_gb300 runs on CUDA tensors only")
+        if t.dtype != torch.float32:
+            raise TypeError("ffnoml_gb300 FFNO3D takes float32 inputs")
+
+
+def _channels_last(h):
+    """[B, C, D, H, W] -> its channels-last storage [B, D, H, W, C] (no copy when h is already a view of it)."""
+    cl = h.permute(0, 2, 3, 4, 1)
+    return cl if cl.is_contiguous() else cl.contiguous()
+
+
+def run_lift(ex, x, z_scale):
+    """_run_lift forward: x [B, Cin, D, H, W], z_scale [B, D, H, W] -> (hidden [B, C, D, H, W] view, per-cube lift
+    spaces for the backward)."""
+    m = ex.model
+    _check_cuda_f32(x, z_scale)
+    if x.dim() != 5 or x.shape[1] != m.in_channels or z_scale.shape != (x.shape[0],) + tuple(x.shape[2:]):
+        raise ValueError(f"x must be [B, {m.in_channels}, D, H, W] and z_scale [B, D, H, W]; got {tuple(x.shape)}, "
+                         f"{tuple(z_scale.shape)}")
+    x, z_scale = x.contiguous(), z_scale.contiguous()
+    pk = ex.packed(x.device)
+    B, _, D, H, W = x.shape
+    V, C = D * H * W, m.width
+    out = torch.empty(B, D, H, W, C, dtype=torch.float32, device=x.device)
+    spaces = []
+    for b in range(B):
+        ls = _LiftSpace(V, C, pk.groups, x.device)
+        nat.call("ffno_depth_weights", z_scale[b].data_ptr(), D, H * W, ls.dw.data_ptr(), _stream())
+        ex._lift(pk, _LiftOut(ls, out[b]), x[b])
+        spaces.append(ls)
+    return out.permute(0, 4, 1, 2, 3), spaces
+
+
+class _LiftOut:
+    """A lift space whose output row buffer is a given [V][C] view (what Executor._lift writes to as ws.x)."""
+
+    def __init__(self, ls, x):
+        self.__dict__.update(ls.__dict__)
+        self.x = x
+
+
+def run_lift_bwd(ex, x, z_scale, spaces, hbar):
+    """_run_lift backward: hbar [B, C, D, H, W] -> (x_bar [B, Cin, D, H, W], z_bar [B, D, H, W])."""
+    m = ex.model
+    pk = ex.packed(x.device)
+    B, Cin, D, H, W = x.shape
+    V, C, HW = D * H * W, m.width, H * W
+    z_scale = z_scale.contiguous()
+    hb = _channels_last(hbar.float())
+    xbar = torch.zeros(B, Cin, D, H, W, dtype=torch.float32, device=x.device)
+    zbar = torch.zeros(B, D, H, W, dtype=torch.float32, device=x.device)
+    s = _stream()
+    G = pk.groups
+    for b, ls in enumerate(spaces):
+        bpart = torch.empty(max(ls.nparts, 1) * G * 2, dtype=torch.float64, device=x.device)
+        sums = torch.empty(G * 2, dtype=torch.float64, device=x.device)
+        pbar = torch.empty(V, C, dtype=torch.float32, device=x.device)
+        wbar = torch.zeros(V, dtype=torch.float32, device=x.device)
+        u = hb[b]
+        nat.call("ffno_gn_bwd_stats", 1, u.data_ptr(), 1.0, ls.pre.data_ptr(), pk.lift_g.data_ptr(),
+                 pk.lift_b.data_ptr(), ls.gstats["lift"].data_ptr(), V, C, G, bpart.data_ptr(), ls.nparts, s)
+        nat.call("ffno_gn_bwd_final", bpart.data_ptr(), ls.nparts, G, sums.data_ptr(), s)
+        nat.call("ffno_gn_bwd_apply", 1, u.data_ptr(), 1.0, ls.pre.data_ptr(), pk.lift_g.data_ptr(),
+                 pk.lift_b.data_ptr(), ls.gstats["lift"].data_ptr(), sums.data_ptr(), ls.dw.data_ptr(), V, C, G, EPS,
+                 pbar.data_ptr(), wbar.data_ptr(), s)
+        nat.call("ffno_lift_bwd", pbar.data_ptr(), Cin, V, C, pk.lift_w.data_ptr(), xbar[b].data_ptr(), s)
+        nat.call("ffno_depth_weights_bwd", z_scale[b].data_ptr(), wbar.data_ptr(), D, HW, zbar[b].data_ptr(), s)
+    return xbar, zbar
+
+
+def run_head(ex, h):
+    """_run_head forward: hidden [B, C, D, H, W] -> head channels [B, nh, D, H, W] = proj2(gelu(proj1(h)))."""
+    m = ex.model
+    _check_cuda_f32(h)
+    if h.dim() != 5 or h.shape[1] != m.width:
+        raise ValueError(f"expected the hidden state [B, {m.width}, D, H, W], got {tuple(h.shape)}")
+    pk = ex.packed(h.device)
+    cl = _channels_last(h)
+    B, D, H, W, C = cl.shape
+    V = D * H * W
+    out = torch.empty(B, pk.nh, D, H, W, dtype=torch.float32, device=h.device)
+    for b in range(B):
+        nat.call("ffno_proj_fwd", cl[b].data_ptr(), V, C, pk.p1.data_ptr(), pk.p2.data_ptr(), pk.b2.data_ptr(), pk.nh,
+                 pk.nhp, out[b].data_ptr(), _stream())
+    return out
+
+
+def run_head_bwd(ex, h, gbar):
+    """_run_head backward: gbar [B, nh, D, H, W] -> h_bar [B, C, D, H, W] (a channels-first view)."""
+    pk = ex.packed(h.device)
+    cl = _channels_last(h)
+    B, D, H, W, C = cl.shape
+    V = D * H * W
+    gbar = gbar.float().contiguous()
+    hbar = torch.empty(B, D, H, W, C, dtype=torch.float32, device=h.device)
+    for b in range(B):
+        nat.call("ffno_proj_bwd", cl[b].data_ptr(), gbar[b].data_ptr(), V, C, pk.p1.data_ptr(), pk.p2.data_ptr(),
+                 pk.b2.data_ptr(), pk.p2t.data_ptr(), pk.p1t.data_ptr(), pk.nh, pk.nhp, hbar[b].data_ptr(),
+                 _stream())
+    return hbar.permute(0, 4, 1, 2, 3)
+
+
+def _head_params_for(ex, device):
+    pk = ex.packed(device)
+    return pk, (pk.head32 if ex.model.precision == "bf16" else pk.head)
+
+
+def head_output(ex, head, x_in):
+    """head_output forward: head channels [B, nh, D, H, W], normalised inputs x_in [B, Cin, D, H, W] -> normalised
+    log10 n [B, L, D, H, W]. The FP32 path evaluates the LTE weights and log-softmax in FP64 as the reference does;
+    precision 'bf16' in FP32 with a compensated sum."""
+    m = ex.model
+    _check_cuda_f32(head, x_in)
+    pk, hp = _head_params_for(ex, head.device)
+    if head.dim() != 5 or head.shape[1] != pk.nh or x_in.dim() != 5 or x_in.shape[1] != m.in_channels or \
+            head.shape[0] != x_in.shape[0] or head.shape[2:] != x_in.shape[2:]:
+        raise ValueError(f"head_output takes head [B, {pk.nh}, D, H, W] and x_in [B, {m.in_channels}, D, H, W]; got "
+                         f"{tuple(head.shape)}, {tuple(x_in.shape)}")
+    head, x_in = head.contiguous(), x_in.contiguous()
+    B = head.shape[0]
+    V = head[0, 0].numel()
+    out = torch.empty(B, m.out_channels, *head.shape[2:], dtype=torch.float32, device=head.device)
+    for b in range(B):
+        nat.call("ffno_head_output", head[b].data_ptr(), x_in[b].data_ptr(), V, pk.nh, hp, out[b].data_ptr(),
+                 _stream())
+    return out
+
+
+def head_output_bwd(ex, head, x_in, ybar):
+    pk, hp = _head_params_for(ex, head.device)
+    head, x_in, ybar = head.contiguous(), x_in.contiguous(), ybar.float().contiguous()
+    B = head.shape[0]
+    V = head[0, 0].numel()
+    hbar = torch.empty_like(head)
+    xbar = torch.empty_like(x_in)
+    for b in range(B):
+        nat.call("ffno_head_output_bwd", head[b].data_ptr(), x_in[b].data_ptr(), ybar[b].data_ptr(), V, pk.nh, hp,
+                 hbar[b].data_ptr(), xbar[b].data_ptr(), _stream())
+    return hbar, xbar
+
+
+class _LiftFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, z_scale, ex):
+        h, spaces = run_lift(ex, x, z_scale)
+        ctx.ex, ctx.spaces = ex, spaces
+        ctx.save_for_backward(x, z_scale)
+        return h
+
+    @staticmethod
+    def backward(ctx, hbar):
+        x, z_scale = ctx.saved_tensors
+        xbar, zbar = run_lift_bwd(ctx.ex, x, z_scale, ctx.spaces, hbar)
+        ctx.spaces = None
+        return xbar, zbar, None
+
+
+class _HeadFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, h, ex):
+        ctx.ex = ex
+        ctx.save_for_backward(h)
+        return run_head(ex, h)
+
+    @staticmethod
+    def backward(ctx, gbar):
+        (h,) = ctx.saved_tensors
+        return run_head_bwd(ctx.ex, h, gbar), None
+
+
+class _HeadOutputFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, head, x_in, ex):
+        ctx.ex = ex
+        ctx.save_for_backward(head, x_in)
+        return head_output(ex, head, x_in)
+
+    @staticmethod
+    def backward(ctx, ybar):
+        head, x_in = ctx.saved_tensors
+        hbar, xbar = head_output_bwd(ctx.ex, head, x_in, ybar)
+        return hbar, xbar, None
+
+
+def _needs_grad(*ts):
+    return torch.is_grad_enabled() and any(t.requires_grad for t in ts)
+
+
+def lift_apply(model, x, z_scale):
+    if z_scale.ndim == 5:
+        z_scale = z_scale[:, 0]
+    ex = model.executor()
+    if _needs_grad(x, z_scale):
+        return _LiftFunction.apply(x, z_scale, ex)
+    return run_lift(ex, x, z_scale)[0]
+
+
+def head_apply(model, h):
+    ex = model.executor()
+    if _needs_grad(h):
+        return _HeadFunction.apply(h, ex)
+    return run_head(ex, h)
+
+
+def head_output_apply(model, head, x_in):
+    ex = model.executor()
+    if _needs_grad(head, x_in):
+        return _HeadOutputFunction.apply(head, x_in, ex)
+    return head_output(ex, head, x_in)

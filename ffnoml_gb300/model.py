@@ -225,8 +225,36 @@ class FFNO3D(nn.Module):
             self._executor = Executor(self)
         return self._executor
 
-    def forward(self, x, z_scale, dx, dy, collect_stats=False, branch_mask=None):
+    def _check_mode(self, collect_stats=False, branch_mask=None):
         if collect_stats or branch_mask is not None:
             raise NotImplementedError("collect_stats / branch_mask are training diagnostics outside this path")
+        if self.training and any(isinstance(mod, nn.Dropout) and mod.p > 0 for mod in self.modules()):
+            # the reference applies its dropout layers in training mode (models/ffno_model.py:519-521, 155); this
+            # path computes the inference operator only, so it refuses rather than return eval-mode results
+            raise RuntimeError("this FFNO3D has dropout layers and is in training mode; the GB300 path computes the "
+                               "inference operator only: call model.eval() first")
+
+    def head_output(self, head, x_in):
+        """Normalised log10 populations from the head channels [B, L+S, D, H, W] and the normalised inputs x_in
+        [B, Cin, D, H, W] (models/ffno_model.py:730-749), on the GPU; differentiable in both."""
+        from .executor import head_output_apply
+        return head_output_apply(self, head, x_in)
+
+    def _run_lift(self, x, z_scale, collect_stats=False):
+        """gelu(DepthWeightedGroupNorm(lift(x), depth_weights(z_scale))) (models/ffno_model.py:782-788): the hidden
+        state [B, width, D, H, W], a channels-first view of channels-last storage; differentiable in x and z_scale."""
+        self._check_mode(collect_stats)
+        from .executor import lift_apply
+        return lift_apply(self, x, z_scale)
+
+    def _run_head(self, x, collect_stats=False):
+        """proj2(gelu(proj1(x))) (models/ffno_model.py:790-798): the head channels [B, L+S, D, H, W] of the hidden
+        state x [B, width, D, H, W]; differentiable in x."""
+        self._check_mode(collect_stats)
+        from .executor import head_apply
+        return head_apply(self, x)
+
+    def forward(self, x, z_scale, dx, dy, collect_stats=False, branch_mask=None):
+        self._check_mode(collect_stats, branch_mask)
         from .executor import ffno_apply
         return ffno_apply(self, x, z_scale, dx, dy)

@@ -52,8 +52,9 @@ typedef struct {
   float mean_x[8], std_x[8];
   float mean_y[FFNO_MAX_LEVELS], std_y[FFNO_MAX_LEVELS];
   double log_g[FFNO_MAX_LEVELS], ev[FFNO_MAX_LEVELS], ndxi[FFNO_MAX_LEVELS], dion[FFNO_MAX_LEVELS];
-  int math32; /* nonzero: the LTE weights and log-softmax in FP32 (the split-BF16 path's tolerance); 0: FP64 as the
-                 reference computes them */
+  int math32; /* nonzero: the LTE weights and log-softmax in FP32 with a compensated (Neumaier) sum of the level
+                 exponentials, so that a voxel's level shares add up to 1 within 1e-6 (the split-BF16 path);
+                 0: all of it in FP64, as the reference computes it */
 } ffno_head_params;
 
 /* library version string */
@@ -118,6 +119,17 @@ int ffno_resid_out(const float* x2, const float* pre, const float* coefs, float 
  * log10 n. If head_out is not NULL the raw head channels are also written there channels-first [nh][V]. */
 int ffno_head_fwd(const float* x, const float* x_in, long V, int C, const float* p1, const float* p2, const float* b2,
                   int nh, int nhp, const ffno_head_params* params, float* out, float* head_out, ffno_stream_t stream);
+
+/* FFNO3D._run_head alone (models/ffno_model.py:790-798; the drop-in module's _run_head): head [nh][V] channels-first
+ * = gelu(x @ p1) @ p2 + b2 for x [V][C]; p2, b2 padded to nhp = 16 or 32 columns, nh <= nhp. */
+int ffno_proj_fwd(const float* x, long V, int C, const float* p1, const float* p2, const float* b2, int nh, int nhp,
+                  float* head, ffno_stream_t stream);
+
+/* FFNO3D.head_output (models/ffno_model.py:730-749) on head channels that are already computed: head [nh][V]
+ * channels-first (per species its level logits, then its total channel), x_in [cin][V] the normalised inputs ->
+ * out [levels][V] normalised log10 n. One thread per voxel: coalesced loads and stores of the channel planes. */
+int ffno_head_output(const float* head, const float* x_in, long V, int nh, const ffno_head_params* params,
+                     float* out, ffno_stream_t stream);
 
 /* Batched transform GEMM: out[b][m][n] = sum_k T[m][k] * in[b][k][n], the DFT-as-contraction of both spectral
  * operators (rfft2/irfft2 of SpectralConv2dFull.forward :441-448; the Filon height transform and its inverse of
@@ -203,6 +215,17 @@ int ffno_head_bwd(const float* x, const float* x_in, const float* y_bar, long V,
                   const float* p2, const float* b2, const float* p2t, const float* p1t, int nhp,
                   const ffno_head_params* params, float* x_bar, float* x_in_bar, ffno_stream_t stream);
 
+/* VJP of ffno_proj_fwd: x_bar [V][C] (written) from head_bar [nh][V]; p2t [nhp][2C] and p1t [2C][C] as for
+ * ffno_head_bwd. */
+int ffno_proj_bwd(const float* x, const float* head_bar, long V, int C, const float* p1, const float* p2,
+                  const float* b2, const float* p2t, const float* p1t, int nh, int nhp, float* x_bar,
+                  ffno_stream_t stream);
+
+/* VJP of ffno_head_output given y_bar [levels][V]: head_bar [nh][V] and x_in_bar [cin][V], both written (x_in_bar
+ * is non-zero only on the T, ne and rho channels). */
+int ffno_head_output_bwd(const float* head, const float* x_in, const float* y_bar, long V, int nh,
+                         const ffno_head_params* params, float* head_bar, float* x_in_bar, ffno_stream_t stream);
+
 /* Backward of ffno_depth_weights: z_bar [D][HW] += d w / d z applied to w_bar. */
 int ffno_depth_weights_bwd(const float* z, const float* w_bar, int D, long HW, float* z_bar, ffno_stream_t stream);
 
@@ -221,8 +244,11 @@ int ffno_outer(const float* A, long lda, int Ma, const float* B, long ldb, int M
  * larger requests return FFNO_ETOOBIG without touching the device. Allocates nothing. The first call on each device
  * looks up the array's device address (with that device current); make that first call before any stream capture.
  * Every call shares the one array, so calls that overlap on the GPU (other streams, other threads) race; nothing in it
- * needs to start at zero. Same result as ffno_outer with the same nsplit; fewer splits when the array is too small
- * for the usual count (the sums are then added in a different order). */
+ * needs to start at zero. The result equals ffno_outer's with nsplit = ffno_outer_parts(Ma, Mb, N) bit for bit while
+ * Ma * Mb * ffno_outer_parts(Ma, Mb, N) <= 4 Mi; above that the array holds fewer splits, so the partial sums are
+ * added in another order (the same value to rounding, not the same bits). The looked-up address belongs to the
+ * device's current context: after cudaDeviceReset on a device, do not call this entry point on it again in the same
+ * process. */
 int ffno_outer_noalloc(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, double* out,
                        int accumulate, ffno_stream_t stream);
 

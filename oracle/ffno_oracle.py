@@ -326,26 +326,26 @@ class OracleFFNO3D:
         y = torch.cat(outs, dim=1)
         return (y - p["mean_Y"][None, :, None, None, None]) / p["std_Y"][None, :, None, None, None]
 
+    def lift(self, x, z_scale):
+        """FFNO3D._lift (models/ffno_model.py:782-783): gelu(weighted GroupNorm(lift conv(x)))."""
+        return F.gelu(self._wgn("lift.1", pointwise(x, self.p["lift.0.weight"]), level_weights(z_scale)))
+
+    def proj(self, x):
+        """The projection of FFNO3D._run_head (models/ffno_model.py:790-798): proj2(gelu(proj1(x)))."""
+        p = self.p
+        return pointwise(F.gelu(pointwise(x, p["proj1.weight"])), p["proj2.weight"], p["proj2.bias"])
+
     def forward(self, x, z_scale, dx, dy):
         """FFNO3D.forward (models/ffno_model.py:800-832): normalised inputs -> normalised log10 populations."""
-        p = self.p
         x_in = x
         use_ckpt = self.checkpoint_blocks and torch.is_grad_enabled()
-
-        def lift(x, z):
-            return F.gelu(self._wgn("lift.1", pointwise(x, p["lift.0.weight"]), level_weights(z)))
-
-        x = checkpoint(lift, x, z_scale, use_reentrant=False) if use_ckpt else lift(x, z_scale)
+        x = checkpoint(self.lift, x, z_scale, use_reentrant=False) if use_ckpt else self.lift(x, z_scale)
         for i in range(self.n_layers):
             if use_ckpt:
                 x = checkpoint(lambda a, b, i=i: self.block(i, a, b, dx, dy), x, z_scale, use_reentrant=False)
             else:
                 x = self.block(i, x, z_scale, dx, dy)
-
-        def proj(x):
-            return pointwise(F.gelu(pointwise(x, p["proj1.weight"])), p["proj2.weight"], p["proj2.bias"])
-
-        h = checkpoint(proj, x, use_reentrant=False) if use_ckpt else proj(x)
+        h = checkpoint(self.proj, x, use_reentrant=False) if use_ckpt else self.proj(x)
         return self.head(h, x_in)
 
     __call__ = forward

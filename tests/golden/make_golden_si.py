@@ -2,8 +2,8 @@
 (harshmathur1990/FFNOML ffno_fsdp_runtime.py: _model_inputs, linear_populations, and the composition of
 _forward_linear / _canonical_populations, :265-292) around the reference's own FFNO3D, in float64 on CPU.
 
-Run in a container that has the reference checked out (default /root/reference, override with FFNOML_REFERENCE):
-    python tests/golden/make_golden_si.py
+Run where the reference is checked out, naming its directory in FFNOML_REFERENCE or with --reference:
+    FFNOML_REFERENCE=<reference checkout> python tests/golden/make_golden_si.py
 The fixture is committed; the tests read it and never import the reference.
 
 It holds the seeded model's state dict, its config (json), SI inputs (features (6, nz, nx, ny): T [K], vx, vy, vz
@@ -21,8 +21,7 @@ import torch.autograd.forward_ad as fwAD
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from make_golden import ATOM, MEAN_X, STD_X, build, synthetic  # noqa: E402
-from make_golden import REF  # noqa: E402,F401  (puts the reference on sys.path)
+from make_golden import ATOM, MEAN_X, STD_X, build, synthetic  # noqa: E402  (puts the reference on sys.path)
 from ffno_fsdp_runtime import _model_inputs, linear_populations  # noqa: E402
 
 CONFIG = dict(width=16, n_layers=2, hidden_spectral=16, hidden_vertical=16, freq_mix_rank=4, z_min_wavelength=0.5,

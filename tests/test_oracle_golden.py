@@ -96,3 +96,23 @@ def test_oracle_si_level_matches_the_reference_service_conversions():
     _, pdot = jvp_si(oracle, f, z, dx, dy, a["tangent"][None])
     # per element, relative to the population (the tangent of ln n): populations span 34 decades
     assert ((canon(pdot) - a["pops_dot"]).abs() / a["pops"]).max().item() < 1e-9
+
+
+# ------------------------------------------------------------------------------------------------ recipe fixtures
+def _recipe_oracle(meta, dtype):
+    from golden_io import recipe_model
+    state = {k: v.detach().clone() for k, v in recipe_model(meta, device="cpu").state_dict().items()}
+    return OracleFFNO3D(state, model_config(meta), dtype)
+
+
+@pytest.mark.parametrize("name", ["cfg0", "cfg3_fd", "w96_p_d64", "w96_p_d256", "w64_p_d256"])
+def test_oracle_matches_reference_at_benchmark_architectures(name):
+    """The oracle against the reference's float64 forward and VJP on the benchmark models (the recipe's weights are
+    reproduced bit for bit first: recipe_model checks the fixture's digest)."""
+    from golden_io import load_recipe
+    meta, a = load_recipe(name)
+    oracle = _recipe_oracle(meta, torch.float64)
+    y, xb, zb = vjp(oracle, a["x"], a["z"], meta["dx"], meta["dy"], a["cot"])
+    assert (y - a["y64"]).abs().max().item() < 1e-10
+    assert ((xb - a["xbar"]).abs().max() / a["xbar"].abs().max()).item() < 1e-9
+    assert ((zb - a["zbar"]).abs().max() / a["zbar"].abs().max()).item() < 1e-8

@@ -22,6 +22,7 @@ def _model(precision):
             if ".freq_u." in n:
                 p.normal_(0.0, 0.1)
     m.set_normalization(MEAN_X, STD_X, np.zeros(12), np.ones(12))
+    m.eval()
     return m.set_precision(precision)
 
 
