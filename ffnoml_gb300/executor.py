@@ -98,33 +98,40 @@ def _split_kmajor(m):
     return torch.cat([pack_kmajor(hi.float()).reshape(-1), pack_kmajor(lo.float()).reshape(-1)])
 
 
+XFORM_TC_MAX_K = 512     # the longest contraction one tensor-core transform call takes (RT_MAXK in spectral_tc.cu)
+
+
 class TcXform:
     """A transform table T [M][K] (float64 numpy) packed for the tensor-core transforms, in slices of at most 256 rows
-    (one kernel call each): per slice the streamed pack of ffno_xform_tc (split-BF16 per 128-row m-tile and 64-wide
-    k-chunk) and, when the slice fits in shared memory, the resident pack of ffno_xform_tcr (the whole [Mp][Kp] table
-    as one canonical operand, Mp and Kp rounded up to 16)."""
+    and 512 columns (one kernel call each; the column slices of one row slice accumulate into the same output rows):
+    per slice the streamed pack of ffno_xform_tc (split-BF16 per 128-row m-tile and 64-wide k-chunk) and, when the
+    slice fits in shared memory, the resident pack of ffno_xform_tcr (the whole [Mp][Kp] table as one canonical
+    operand, Mp and Kp rounded up to 16). A production height grid (M = 1001: 680 table rows at D = 256) takes both
+    kinds of slices."""
 
     def __init__(self, T, device):
         T = np.asarray(T, dtype=np.float64)
         self.M, self.K = T.shape
-        Kp = (self.K + 15) // 16 * 16
         limit = nat.lib().ffno_xform_tcr_max_table_bytes()
         self.slices = []
         for r0 in range(0, self.M, 256):
             rows = min(256, self.M - r0)
             mt = (rows + 127) // 128
-            pad = np.zeros((mt * 128, Kp))
-            pad[:rows, :self.K] = T[r0:r0 + rows]
-            parts = [_split_kmajor(pad[t * 128:(t + 1) * 128, k0:min(Kp, k0 + 64)])
-                     for t in range(mt) for k0 in range(0, Kp, 64)]
-            packed = torch.cat(parts).to(device).contiguous()
-            if packed.numel() * 2 != nat.lib().ffno_xform_tc_pack_bytes(rows, self.K):
-                raise RuntimeError("transform pack size mismatch")
-            res = None
-            Mp = (rows + 15) // 16 * 16
-            if 4 * Mp * Kp <= limit:
-                res = (_split_kmajor(pad[:Mp]).to(device).contiguous(), Mp, Kp)
-            self.slices.append((r0, rows, packed, res))
+            for c0 in range(0, self.K, XFORM_TC_MAX_K):
+                cols = min(XFORM_TC_MAX_K, self.K - c0)
+                Kp = (cols + 15) // 16 * 16
+                pad = np.zeros((mt * 128, Kp))
+                pad[:rows, :cols] = T[r0:r0 + rows, c0:c0 + cols]
+                parts = [_split_kmajor(pad[t * 128:(t + 1) * 128, k0:min(Kp, k0 + 64)])
+                         for t in range(mt) for k0 in range(0, Kp, 64)]
+                packed = torch.cat(parts).to(device).contiguous()
+                if packed.numel() * 2 != nat.lib().ffno_xform_tc_pack_bytes(rows, cols):
+                    raise RuntimeError("transform pack size mismatch")
+                res = None
+                Mp = (rows + 15) // 16 * 16
+                if 4 * Mp * Kp <= limit:
+                    res = (_split_kmajor(pad[:Mp]).to(device).contiguous(), Mp, Kp)
+                self.slices.append((r0, rows, c0, cols, packed, res))
 
 
 class Packed:
@@ -432,17 +439,21 @@ class Executor:
             nat.call("ffno_xform", tabs[name].data_ptr(), inp.data_ptr(), out.data_ptr(), desc, 0, s, tag=name)
             return
         tx = self.tc_table(tabs, name)
-        if len(tx.slices) > 1 and desc.out_split < desc.M:
+        if tx.M > 256 and desc.out_split < desc.M:
             raise ValueError("a transform taller than 256 rows needs single-level output addressing")
-        for r0, rows, packed, res in tx.slices:
+        if tx.K > XFORM_TC_MAX_K and desc.in_split < desc.K:
+            raise ValueError("a transform longer than 512 columns needs single-level input addressing")
+        for r0, rows, c0, cols, packed, res in tx.slices:
             d = nat.XformDesc.from_buffer_copy(desc)
-            d.M = rows
+            d.M, d.K = rows, cols
+            src = inp.data_ptr() + 4 * c0 * desc.in_lo
             dst = out.data_ptr() + 4 * r0 * desc.out_lo
+            acc = 1 if c0 else 0
             if res is not None:
-                nat.call("ffno_xform_tcr", res[0].data_ptr(), res[1], res[2], inp.data_ptr(), dst, d, 0,
-                         ws.err.data_ptr(), s, tag=name)
+                nat.call("ffno_xform_tcr", res[0].data_ptr(), res[1], res[2], src, dst, d, acc, ws.err.data_ptr(), s,
+                         tag=name)
             else:
-                nat.call("ffno_xform_tc", packed.data_ptr(), inp.data_ptr(), dst, d, 0, ws.err.data_ptr(), s, tag=name)
+                nat.call("ffno_xform_tc", packed.data_ptr(), src, dst, d, acc, ws.err.data_ptr(), s, tag=name)
 
     # -------------------------------------------------------------------------------------------- geometry
     def geometry(self, z_scale):
@@ -671,8 +682,12 @@ class Executor:
                      g.data_ptr(), _ptr(u), _ptr(v), m.freq_mix_rank, s)
 
     def _outer(self, ws, a, ma, b, mb, n, part, nsplit, out):
-        """out [ma][mb] += a [ma][n] @ b [mb][n]^T (double): a height-transform table's gradient."""
-        if self._tc() and min(ma, mb) <= 256:
+        """out [ma][mb] += a [ma][n] @ b [mb][n]^T (double): a height-transform table's gradient. The tensor-core
+        kernel holds the longer side in 128-row tiles and the shorter (rounded up to 16) as the MMA's N, at most 512
+        accumulator columns in all; larger products (production height grids) run on the FP32 kernel."""
+        lo, hi = min(ma, mb), max(ma, mb)
+        fits = (lo + 15) // 16 * 16 <= 256 and (hi + 127) // 128 * ((lo + 15) // 16 * 16) <= 512
+        if self._tc() and fits:
             nat.call("ffno_outer_tc", a.data_ptr(), n, ma, b.data_ptr(), n, mb, n, part.data_ptr(), nsplit,
                      out.data_ptr(), 1, ws.err.data_ptr(), _stream())
         else:

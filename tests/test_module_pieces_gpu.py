@@ -121,15 +121,19 @@ def _share_setup(V, seed, nh_std=1.0):
 
 def _share_sums(y, head, model):
     """Per voxel and species sum_i 10^(log10 n_i) / (rho / m 10^s), from the normalised outputs y [12][V] and the head
-    channels [14][V] (float64 arithmetic)."""
+    channels [14][V]: log10 n_i = y_i std_Y + mean_Y and log10 rho - log10 m with the model's own float32 buffers,
+    in float64 arithmetic."""
     y = y.double().cpu()
     head = head.double().cpu()
+    mean_y, std_y = model.mean_Y.double().cpu()[:, None], model.std_Y.double().cpu()[:, None]
+    log10_n = y * std_y + mean_y
+    log10_rho = float(model.mean_X[5].double())          # the inputs' normalised rho channel is 0
     tb = model.total_bound
     sums = []
     for s in range(2):
         u = head[7 * s + 6]
-        tot = tb * torch.tanh(u / tb)
-        sums.append(torch.pow(10.0, y[6 * s:6 * s + 6] - tot[None]).sum(0))
+        base = log10_rho - float(model.log10_particle_mass[s].double()) + tb * torch.tanh(u / tb)
+        sums.append(torch.pow(10.0, log10_n[6 * s:6 * s + 6] - base[None]).sum(0))
     return torch.stack(sums)
 
 

@@ -254,16 +254,15 @@ def test_xform_tc_matches_fp32(which, C, kind):
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     nat.call("ffno_xform", Tf.data_ptr(), x.data_ptr(), a.data_ptr(), d, 0, _s())
     tx = TcXform(T, torch.device("cuda"))
-    for r0, rows, packed, res in tx.slices:
+    for r0, rows, c0, cols, packed, res in tx.slices:
         dd = nat.XformDesc.from_buffer_copy(d)
-        dd.M = rows
+        dd.M, dd.K = rows, cols
+        src, dst, acc = x.data_ptr() + 4 * c0 * d.in_lo, b.data_ptr() + 4 * r0 * d.out_lo, 1 if c0 else 0
         if kind == "resident":
             assert res is not None
-            nat.call("ffno_xform_tcr", _hold(res[0]), res[1], res[2], x.data_ptr(), b.data_ptr() + 4 * r0 * d.out_lo,
-                     dd, 0, err.data_ptr(), _s())
+            nat.call("ffno_xform_tcr", _hold(res[0]), res[1], res[2], src, dst, dd, acc, err.data_ptr(), _s())
         else:
-            nat.call("ffno_xform_tc", _hold(packed), x.data_ptr(), b.data_ptr() + 4 * r0 * d.out_lo, dd, 0,
-                     err.data_ptr(), _s())
+            nat.call("ffno_xform_tc", _hold(packed), src, dst, dd, acc, err.data_ptr(), _s())
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     _close(b, a)

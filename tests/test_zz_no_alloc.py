@@ -53,8 +53,12 @@ def test_noalloc_outer_with_fewer_splits_than_outer(Ma, Mb, N):
     ref, got, exact, nsplit = _outer_pair(Ma, Mb, N, 4)
     assert Ma * Mb <= CAPACITY
     scale = exact.abs().max()
-    assert ((got - ref).abs().max() / scale).item() < 1e-6
-    assert ((got - exact).abs().max() / scale).item() < 1e-5
+    # both are float32 sums over N terms per split (fewer, longer splits here): each within float32 summation error
+    # of the float64 product, so within twice that of each other
+    e_got = ((got - exact).abs().max() / scale).item()
+    e_ref = ((ref - exact).abs().max() / scale).item()
+    assert e_got < 5e-5 and e_ref < 5e-5
+    assert ((got - ref).abs().max() / scale).item() < 1e-4
 
 
 def test_noalloc_outer_refuses_oversized_products():
