@@ -539,6 +539,8 @@ def run_gb300(args):
     serving = None
     if rank == 0 and not args.no_serve:
         serving = serving_stream(model, args.serve_requests, 40.0)
+        # inversion requests are VJPs: the same size mix at a rate the device can follow
+        serving["vjp_stream"] = serving_stream(model, max(16, args.serve_requests // 4), 5.0, seed=17, op="VJP")
 
     flops_vox = algorithmic_flops_per_voxel(WIDTH, LAYERS, D, H, W, MODES, 12, 2)
     if rank == 0:
@@ -607,10 +609,11 @@ def config4_run(model, ex, dev, world, rank, timed):
     return out
 
 
-def serving_stream(model, n_requests, rate, seed=7, slots=4, connections=8):
+def serving_stream(model, n_requests, rate, seed=7, slots=4, connections=8, op="PREDICT"):
     """The mixed-size request stream: Poisson arrivals at `rate` per second, D in {128, 192, 256}, H = W in
-    {32, 64, 96, 128}, PREDICT over the protocol-v2 service (each request on one of `connections` client connections).
-    Returns p50 / p99 latency (send to reply) and aggregate voxels/s."""
+    {32, 64, 96, 128}, PREDICT (or VJP, with a seeded population cotangent) over the protocol-v2 service (each request
+    on one of `connections` client connections). Returns p50 / p99 latency (send to reply), aggregate voxels/s, and
+    the server's mean queue wait and service time per request."""
     import threading
     import queue as q
 
@@ -625,28 +628,38 @@ def serving_stream(model, n_requests, rate, seed=7, slots=4, connections=8):
     gaps = g.exponential(1.0 / rate, n_requests)
     inputs = {}
     for sh in set(sizes):
-        inputs[sh] = synthetic_si(sh, seed=11)
+        f, z = synthetic_si(sh, seed=11)
+        extra = ()
+        if op == "VJP":
+            extra = (np.random.default_rng(13).normal(size=sh + (12,)).astype(np.float32) * np.float32(1e-15),)
+        inputs[sh] = (f, z) + extra
     # warm every shape once (tables and packs are built on first use)
     c = Client(srv.port, "bench")
     for sh in set(sizes):
-        c.request("PREDICT", "HCA", inputs[sh][0], inputs[sh][1], DXY, DXY, 12)
+        c.request(op, "HCA", inputs[sh][0], inputs[sh][1], DXY, DXY, 12, *inputs[sh][2:])
     c.close()
+    srv.scheduler.completed.clear()
     work = q.Queue()
     lat = [None] * n_requests
 
+    # each shape's request bytes are encoded once: the clients (threads of this process, like the server) only send
+    # bytes and read the reply's bytes, so that the measured time is the server's
+    encoded = {sh: Client.encode(op, "HCA", a[0], a[1], DXY, DXY, 12, *a[2:]) for sh, a in inputs.items()}
+    reply_floats = {sh: (7 if op == "VJP" else 12) * sh[0] * sh[1] * sh[2] for sh in inputs}
+
     def client_loop():
         cl = Client(srv.port, "bench")
+        into = bytearray(4 * max(reply_floats.values()))
         while True:
             item = work.get()
             if item is None:
                 break
             i, t_send = item
-            f, z = inputs[sizes[i]]
             wait = t_send - time.perf_counter()
             if wait > 0:
                 time.sleep(wait)
             t0 = time.perf_counter()
-            cl.request("PREDICT", "HCA", f, z, DXY, DXY, 12)
+            cl.request_raw(encoded[sizes[i]], 4 * reply_floats[sizes[i]], into)
             lat[i] = time.perf_counter() - t0
         cl.close()
 
@@ -663,12 +676,19 @@ def serving_stream(model, n_requests, rate, seed=7, slots=4, connections=8):
     for t_ in threads:
         t_.join()
     elapsed = time.perf_counter() - t_begin
+    done = list(srv.scheduler.completed)
     srv.shutdown()
     vox = sum(d * h * w for d, h, w in sizes)
     lat_ms = np.array(lat) * 1e3
-    return {"requests": n_requests, "rate_per_s": rate, "slots": slots, "op": "PREDICT",
+    wait_ms = [1e3 * (r.t_start - r.t_arrive) for r in done if r.t_start]
+    serve_ms = [1e3 * (r.t_done - r.t_start) for r in done if r.t_start]
+    return {"requests": n_requests, "rate_per_s": rate, "slots": slots, "op": op,
             "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
-            "voxels_per_s": vox / elapsed, "wall_s": elapsed}
+            "voxels_per_s": vox / elapsed, "wall_s": elapsed,
+            "offered_voxels_per_s": vox / float(np.sum(gaps)),
+            "server_mean_queue_ms": float(np.mean(wait_ms)) if wait_ms else None,
+            "server_mean_service_ms": float(np.mean(serve_ms)) if serve_ms else None,
+            "server_busy_slot_s": float(np.sum(serve_ms)) / 1e3 if serve_ms else None}
 
 
 def main():

@@ -39,7 +39,10 @@ bool smem_attr(K kernel, size_t bytes) {
 bool width_ok(int C) { return C == 16 || C == 32 || C == 64 || C == 96; }
 
 __device__ __forceinline__ float upstream(int mode, float u, float r, float y) {
-  // gradient w.r.t. the GroupNorm output y given the upstream u: r u (mode 0) or r u gelu'(y) (mode 1: GELU after GN)
+  // gradient w.r.t. the GroupNorm output y given the upstream u: r u (mode 0), r u gelu'(y) (mode 1: GELU after GN,
+  // erf-based), or r u gelu'(y) with the tensor-core kernels' activation (mode 2: the split-BF16 path, whose forward
+  // applies that GELU after these GroupNorms)
+  if (mode == 2) return r * u * gelu_grad_tc(y);
   return mode ? r * u * gelu_grad(y) : r * u;
 }
 
@@ -818,6 +821,7 @@ int ffno_gn_bwd_stats(int mode, const float* u, float r, const float* pre, const
                       const double* gstats, long V, int C, int groups, double* partials, int nparts,
                       ffno_stream_t stream) {
   if (!u || !pre || !gamma || !beta || !gstats || !partials) return FFNO_EINVAL;
+  if (mode < 0 || mode > 2) return FFNO_EINVAL;
   if (!width_ok(C) || V < 1 || groups < 1 || groups > GMAX || C % groups || nparts < 1) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   const int cpg = C / groups;
@@ -841,6 +845,7 @@ int ffno_gn_bwd_apply(int mode, const float* u, float r, const float* pre, const
                       const double* gstats, const double* sums, const float* dw, long V, int C, int groups, float eps,
                       float* pre_bar, float* w_bar, ffno_stream_t stream) {
   if (!u || !pre || !gamma || !beta || !gstats || !dw || !pre_bar || !w_bar) return FFNO_EINVAL;
+  if (mode < 0 || mode > 2) return FFNO_EINVAL;
   if (!width_ok(C) || V < 1 || groups < 1 || groups > GMAX || C % groups) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   const int cpg = C / groups;

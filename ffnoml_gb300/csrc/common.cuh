@@ -80,10 +80,10 @@ __device__ __forceinline__ double ln_ccon() {
 // One voxel of FFNO3D.head_output after proj2 (models/ffno_model.py:729-748): per species, logits = head channels + the
 // LTE Boltzmann/Saha log-weights of (T, ne), log-softmax over the levels, plus the bounded total b tanh(u / b),
 // log10 rho and the particle mass; normalised with mean_Y / std_Y. o: the voxel's head channels (species s: its L
-// level logits, then its total channel). The LTE math and the log-softmax run entirely in T: double is the
-// reference's FP64 (torch.log_softmax on float64 logits, :741); float is the split-BF16 path's FP32, where the sum of
-// the max-shifted exponentials (each in (0, 1]) is compensated (below), so that the level shares of a voxel add up
-// to 1 within a few FP32 roundings.
+// level logits, then its total channel). The LTE math and the log-softmax run in T: double is the reference's FP64
+// (torch.log_softmax on float64 logits, :741); float is the split-BF16 path's FP32, where the sum of the max-shifted
+// exponentials (each in (0, 1]) is compensated (below), so that the level shares of a voxel add up to 1 within a few
+// FP32 roundings. The total term and the final sum of log10 n are FP64 in both.
 struct HeadInputs {
   float lt, lne, lrho;   // log10 T, log10 ne (SI), log10 rho of the voxel (denormalised)
 };
@@ -141,8 +141,10 @@ template <typename T>
 __device__ __forceinline__ void head_voxel_fwd(const ffno_head_params& hp, const float* o, const HeadInputs& in,
                                                float* __restrict__ out, long V, long v) {
   const Lte<T> e(hp, in);
-  const T LN10 = (T)kLN10;
-  const T lrho = (T)in.lrho * (T)hp.std_x[hp.rho_channel] + (T)hp.mean_x[hp.rho_channel];
+  // the total term and the assembly of log10 n (log10 rho - log10 m + s ~ 20, minus mean_Y) stay in FP64 for both
+  // T: in FP32 their rounding (~1e-6 dex at that magnitude) would shift every level share of the voxel alike; they
+  // are a handful of FP64 operations a voxel
+  const double lrho = (double)in.lrho * (double)hp.std_x[hp.rho_channel] + (double)hp.mean_x[hp.rho_channel];
   int hc = 0, lvl = 0;
   for (int s = 0; s < hp.nspecies; ++s) {
     const int L = hp.levels[s];
@@ -153,12 +155,12 @@ __device__ __forceinline__ void head_voxel_fwd(const ffno_head_params& hp, const
       mx = fmax(mx, logit[i]);
     }
     const T lse = mlog(shifted_exp_sum<T>(logit, L, mx));
-    const T tb = (T)hp.total_bound;
-    const T base = lrho - (T)hp.log10_particle_mass[s] + tb * mtanh((T)o[hc + L] / tb);
+    const double tb = (double)hp.total_bound;
+    const double base = lrho - (double)hp.log10_particle_mass[s] + tb * tanh((double)o[hc + L] / tb);
     for (int i = 0; i < L; ++i) {
       const int g = lvl + i;
-      const T l10 = base + (logit[i] - mx - lse) / LN10;
-      out[(long)g * V + v] = (float)((l10 - (T)hp.mean_y[g]) / (T)hp.std_y[g]);
+      const double l10 = base + ((double)(logit[i] - mx) - (double)lse) / kLN10;
+      out[(long)g * V + v] = (float)((l10 - (double)hp.mean_y[g]) / (double)hp.std_y[g]);
     }
     hc += L + 1;
     lvl += L;

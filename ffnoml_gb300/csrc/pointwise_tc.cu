@@ -944,22 +944,22 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_a_tc(const float* __restrict
   const float* src = kf < C ? sp : vp;
   const int ks = kf < C ? kf : kf - C;
   const int f = P.feat();
+  // L2 prefetch: the first phase's rows (spec, vert, gates) one tile ahead, F_bar (read after the first GEMM) at
+  // the start of its own tile, so that no prefetched line has to outlive a whole tile step of all pipelines
   const int pf = c_pf;
-  for (int k = 1; P.ptid == 0 && k < pf; ++k) {
-    const long tp = t0 + k * tstep;
-    prefetch_rows(sp, tp * TM, V, C);
-    prefetch_rows(vp, tp * TM, V, C);
-    prefetch_rows(gates, tp * TM, V, 2 * C);
-    prefetch_rows(fb, tp * TM, V, C);
+  if (P.ptid == 0 && pf > 0) {
+    prefetch_rows(sp, t0 * TM, V, C);
+    prefetch_rows(vp, t0 * TM, V, C);
+    prefetch_rows(gates, t0 * TM, V, 2 * C);
   }
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
     if (P.ptid == 0 && pf > 0) {
-      const long tp = t + pf * tstep;
-      prefetch_rows(sp, tp * TM, V, C);
-      prefetch_rows(vp, tp * TM, V, C);
-      prefetch_rows(gates, tp * TM, V, 2 * C);
-      prefetch_rows(fb, tp * TM, V, C);
+      prefetch_rows(fb, v0, V, C);
+      const long tn = (t + tstep) * TM;
+      prefetch_rows(sp, tn, V, C);
+      prefetch_rows(vp, tn, V, C);
+      prefetch_rows(gates, tn, V, 2 * C);
     }
     fill_tile<2 * C>(Bt, v0, V, P.ptid, [&](long v, int k) {
       const float4 g = ld4(gates + v * 2 * C + k);
@@ -1008,28 +1008,21 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
   const Split T = split_at(smem + B1 + B2 + B3 + pid * RB, TM, C);
   P.ok = load_weights(smem, wpack, B1 + B2 + B3, wcx, err);
   const int row = P.feat();
+  // L2 prefetch: hfb (the first phase's operand) one tile ahead; the rows the later phases read (F_bar, gates, both
+  // pre-activations, hg, base) at the start of their own tile, while the first GEMMs run, so that no prefetched line
+  // has to outlive a whole tile step of all pipelines (one tile step reads 9 C floats a voxel: ~90 MB at C = 64)
   const int pf = c_pf;
-  for (int k = 1; P.ptid == 0 && k < pf; ++k) {
-    const long tp = t0 + k * tstep;
-    prefetch_rows(hfb, tp * TM, V, 2 * C);
-    prefetch_rows(fb, tp * TM, V, C);
-    prefetch_rows(gates, tp * TM, V, 2 * C);
-    prefetch_rows(sp, tp * TM, V, C);
-    prefetch_rows(vp, tp * TM, V, C);
-    prefetch_rows(hg, tp * TM, V, C);
-    prefetch_rows(base, tp * TM, V, C);
-  }
+  if (P.ptid == 0 && pf > 0) prefetch_rows(hfb, t0 * TM, V, 2 * C);
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
     if (P.ptid == 0 && pf > 0) {
-      const long tp = t + pf * tstep;
-      prefetch_rows(hfb, tp * TM, V, 2 * C);
-      prefetch_rows(fb, tp * TM, V, C);
-      prefetch_rows(gates, tp * TM, V, 2 * C);
-      prefetch_rows(sp, tp * TM, V, C);
-      prefetch_rows(vp, tp * TM, V, C);
-      prefetch_rows(hg, tp * TM, V, C);
-      prefetch_rows(base, tp * TM, V, C);
+      prefetch_rows(fb, v0, V, C);
+      prefetch_rows(gates, v0, V, 2 * C);
+      prefetch_rows(sp, v0, V, C);
+      prefetch_rows(vp, v0, V, C);
+      prefetch_rows(hg, v0, V, C);
+      prefetch_rows(base, v0, V, C);
+      prefetch_rows(hfb, (t + tstep) * TM, V, 2 * C);
     }
     const long v = v0 + row;
     // B_bar (without the F_bar term) = hfb Wf1^T over the spec and vert halves of hfb

@@ -97,6 +97,30 @@ __global__ void k_si_input_grads(const float* __restrict__ feat, const float* __
   if (bad) atomicOr(flags, bad);
 }
 
+// out = in with its four axes reversed: in C-order [s0][s1][s2][s3], out C-order [s3][s2][s1][s0], i.e. the same
+// array in Fortran order (the layout of the protocol's arrays, FFNOInversion.jl/src/FSDPService.jl). For a fixed i1
+// the input is a [s0][s2 s3] matrix (rows contiguous) and the output, for each (i3, i2), a run of s0 contiguous
+// values: a 32 x 32 shared-memory tile over (i0, k = i2 s3 + i3) reads and writes whole warp-wide runs.
+__global__ void __launch_bounds__(256) k_reverse4(const float* __restrict__ in, long s0, long s1, long s2, long s3,
+                                                  float* __restrict__ out) {
+  __shared__ float tile[32][33];
+  const long K = s2 * s3;
+  const long k0 = (long)blockIdx.x * 32, r0 = (long)blockIdx.y * 32, i1 = blockIdx.z;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int r = ty; r < 32; r += 8) {
+    const long i0 = r0 + r, k = k0 + tx;
+    if (i0 < s0 && k < K) tile[r][tx] = in[(i0 * s1 + i1) * K + k];
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const long k = k0 + r, i0 = r0 + tx;
+    if (i0 < s0 && k < K) {
+      const long i2 = k / s3, i3 = k - i2 * s3;
+      out[((i3 * s2 + i2) * s1 + i1) * s0 + i0] = tile[tx][r];
+    }
+  }
+}
+
 unsigned grid1d(long n) {
   long b = (n + 255) / 256;
   return (unsigned)(b < 4096 ? (b > 0 ? b : 1) : 4096);
@@ -136,6 +160,15 @@ int ffno_si_input_grads(const float* features, const float* x_bar, const float* 
   if (!features || !x_bar || !z_bar_mm || !std_x || !features_bar || !z_bar_m || !flags || V < 1) return FFNO_EINVAL;
   k_si_input_grads<<<grid1d(V), 256, 0, (cudaStream_t)stream>>>(features, x_bar, z_bar_mm, V, std_x, features_bar,
                                                                 z_bar_m, flags);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_reverse_axes4(const float* in, long s0, long s1, long s2, long s3, float* out, ffno_stream_t stream) {
+  if (!in || !out || in == out || s0 < 1 || s1 < 1 || s2 < 1 || s3 < 1) return FFNO_EINVAL;
+  const long kt = (s2 * s3 + 31) / 32, rt = (s0 + 31) / 32;
+  if (kt > 0x7fffffffL || rt > 65535 || s1 > 65535) return FFNO_EINVAL;
+  k_reverse4<<<dim3((unsigned)kt, (unsigned)rt, (unsigned)s1), 256, 0, (cudaStream_t)stream>>>(in, s0, s1, s2, s3, out);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

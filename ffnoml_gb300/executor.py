@@ -457,7 +457,9 @@ class Executor:
 
     # -------------------------------------------------------------------------------------------- geometry
     def geometry(self, z_scale):
-        """Per-batch height analysis (HeightSpectralConv.box and shared-grid test, models/ffno_model.py:248-269)."""
+        """Per-batch height analysis (HeightSpectralConv.box and shared-grid test, models/ffno_model.py:248-269) of
+        the device heights: a column-analysis kernel, whose two numbers per sample are read back (a synchronisation
+        with the stream)."""
         B, D = z_scale.shape[0], z_scale.shape[1]
         HW = z_scale.shape[2] * z_scale.shape[3]
         info = torch.empty(B, 2, dtype=torch.float32, device=z_scale.device)
@@ -468,19 +470,39 @@ class Executor:
         host = torch.cat([info.reshape(-1), col.reshape(-1)]).cpu()
         info_h = host[:2 * B].reshape(B, 2)
         cols32 = host[2 * B:].reshape(B, D).numpy()
+        columns = lambda: z_scale.reshape(B, D, HW).transpose(1, 2).double().cpu().numpy()
+        return self._geometry(bool((info_h[:, 0] > 0.5).all()), float(info_h[:, 1].max()), cols32, columns)
+
+    def geometry_host(self, z_mm):
+        """The same analysis of heights held on the host (float32 numpy [B, D, H, W] in Mm, the values the device
+        holds), without touching the device: the service backend decides it once per request, before the model
+        runs, so no read-back synchronises the request's stream."""
+        z = np.asarray(z_mm, dtype=np.float32)
+        B, D = z.shape[0], z.shape[1]
+        zc = z.reshape(B, D, -1).transpose(0, 2, 1)              # [B][HW][D] view
+        return self.geometry_columns(zc, lambda: zc.astype(np.float64))
+
+    def geometry_columns(self, zc, columns):
+        """geometry_host from columns: zc [B][N][D] float32, every sample's N = H*W columns in any order with column
+        (0, 0) first; columns() -> [B][H*W][D] float64 in the model's h*W + w order (built only for per-column
+        grids)."""
+        mn = zc.min(axis=2)
+        span = float((zc.max(axis=2) - mn).max())
+        shifted = zc - mn[:, :, None]                      # float32, as ffno_column_info compares them
+        shared_each = all(bool((shifted[b] == shifted[b, :1, :]).all()) for b in range(zc.shape[0]))
+        return self._geometry(shared_each, span, np.ascontiguousarray(zc[:, 0, :]), columns)
+
+    def _geometry(self, shared_each, span, cols32, columns):
+        """Geometry from the per-sample test, the span and every sample's column 0; columns() gives every sample's
+        columns [B][H*W][D] (float64), gathered only when the grids are not shared."""
         cols = cols32.astype(np.float64)
-        shared_each = bool((info_h[:, 0] > 0.5).all())
-        span = float(info_h[:, 1].max())
         shifted32 = cols32 - cols32.min(axis=1, keepdims=True)       # the test in the model's float32
         shared = shared_each and bool((shifted32 == shifted32[:1]).all())
         shifted = cols - cols.min(axis=1, keepdims=True)
         m = self.model
         modes = int(math.floor(m.z_reference_length / m.z_min_wavelength)) + 1
         length, k = tb.height_box(span, m.z_reference_length, m.z_min_wavelength, modes)
-        columns = None
-        if not shared:
-            columns = z_scale.reshape(B, D, HW).transpose(1, 2).double().cpu().numpy()
-        return Geometry(shared, span, shifted[0], cols[0], length, k, columns)
+        return Geometry(shared, span, shifted[0], cols[0], length, k, None if shared else columns())
 
     def height_percol(self, pk, geo, b, device):
         """Per-column tables of sample b when the height grids differ (cached by the sample's heights)."""
@@ -504,7 +526,7 @@ class Executor:
             return self._height[key]
 
     # -------------------------------------------------------------------------------------------- setup
-    def _setup(self, x, z_scale, dx, dy):
+    def _setup(self, x, z_scale, dx, dy, geo=None):
         m = self.model
         if not x.is_cuda or not z_scale.is_cuda:
             raise RuntimeError("ffnoml_gb300 runs on CUDA tensors only")
@@ -521,7 +543,8 @@ class Executor:
             raise ValueError("the height operator needs at least two levels")
         device = x.device
         pk = self.packed(device)
-        geo = self.geometry(z_scale)
+        if geo is None:
+            geo = self.geometry(z_scale)
         hgt = self.height(pk, geo, device) if geo.shared else None
         B, _, D, H, W = x.shape
         pln = self.plane(H, W, device)
@@ -529,13 +552,14 @@ class Executor:
         return pk, geo, hgt, pln, pfr
 
     # -------------------------------------------------------------------------------------------- forward
-    def forward(self, x, z_scale, dx, dy, keep=False):
+    def forward(self, x, z_scale, dx, dy, keep=False, geo=None):
         """x [B, Cin, D, H, W], z_scale [B, D, H, W] (Mm), float32 CUDA -> [B, L, D, H, W] float32. With keep=True
-        also returns the state the VJP needs (block inputs per cube)."""
+        also returns the state the VJP needs (block inputs per cube). geo: the heights' analysis when the caller
+        already has it (geometry_host), else it is computed on the device."""
         m = self.model
         x = x.contiguous()
         z_scale = z_scale.contiguous()
-        pk, geo, hgt, pln, pfr = self._setup(x, z_scale, dx, dy)
+        pk, geo, hgt, pln, pfr = self._setup(x, z_scale, dx, dy, geo)
         B, _, D, H, W = x.shape
         out = torch.empty(B, m.out_channels, D, H, W, dtype=torch.float32, device=x.device)
         saved, states = [], []
@@ -841,7 +865,7 @@ class Executor:
         """Input VJP: ybar [B, L, D, H, W] -> (x_bar [B, Cin, D, H, W], z_bar [B, D, H, W])."""
         m = self.model
         x, z_scale, dx, dy = state["x"], state["z"], state["dx"], state["dy"]
-        pk, geo, hgt, pln, pfr = self._setup(x, z_scale, dx, dy)
+        pk, geo, hgt, pln, pfr = self._setup(x, z_scale, dx, dy, state.get("geo"))
         B, Cin, D, H, W = x.shape
         C, V, HW = m.width, D * H * W, H * W
         dev = x.device
@@ -945,8 +969,10 @@ class Executor:
         # x2 = x1 + r_pw GN(pw_pre); pw_pre = pw(x1)
         self._gn_bwd(ws, gb, 0, gb.g2, r_pw, ws.pw_pre, bp["pw_g"], bp["pw_b"], "pw", gb.pbar)
         mlp_bwd(ws.x1, gb.pbar, gb.g2, gb.g1, "pw1", "pw2t", "pw1t", "tcb_pw")
+        # GELU after a GroupNorm: the tensor-core forward applies the A&S activation (mode 2), the FP32 one erf's
+        act = 2 if tc else 1
         # x1 = x + r_f gelu(GN(fused_pre)); fused_pre = fuse(x, spec, vert)
-        self._gn_bwd(ws, gb, 1, gb.g1, r_f, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], "fuse", gb.pbar)
+        self._gn_bwd(ws, gb, act, gb.g1, r_f, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], "fuse", gb.pbar)
         if tc:
             hg = ws.hg                     # gates and hidden layer kept from the forward, else recomputed
             if hg is None:
@@ -967,9 +993,9 @@ class Executor:
                      bp["f2t"].data_ptr(), bp["f1t"].data_ptr(), bp["bg2t"].data_ptr(), bp["bg1t"].data_ptr(),
                      gb.xacc.data_ptr(), gb.sbar.data_ptr(), gb.vbar.data_ptr(), s)
         # spec = gelu(GN(spec_pre)), spec_pre = post_s(ys); vert likewise
-        self._gn_bwd(ws, gb, 1, gb.sbar, 1.0, ws.spec_pre, bp["spec_g"], bp["spec_b"], "spec", gb.pbar)
+        self._gn_bwd(ws, gb, act, gb.sbar, 1.0, ws.spec_pre, bp["spec_g"], bp["spec_b"], "spec", gb.pbar)
         mlp_bwd(ws.ys, gb.pbar, None, gb.ysb, "s_p1", "s_p2t", "s_p1t", "tcb_s_post")
-        self._gn_bwd(ws, gb, 1, gb.vbar, 1.0, ws.vert_pre, bp["vert_g"], bp["vert_b"], "vert", gb.pbar)
+        self._gn_bwd(ws, gb, act, gb.vbar, 1.0, ws.vert_pre, bp["vert_g"], bp["vert_b"], "vert", gb.pbar)
         mlp_bwd(ws.yv, gb.pbar, None, gb.yvb, "v_p1", "v_p2t", "v_p1t", "tcb_v_post")
         # horizontal transposes: ys = twi thi mix thf twf xs  ->  xs_bar = twf^T thf^T mix^T thi^T twi^T ys_bar
         self._xf(pln, "twi_t", gb.ysb, ws.sa, d["wf"], ws)

@@ -183,6 +183,14 @@ class GB300Backend:
             self._staging[k] = (host, dev)
         return self._staging[k]
 
+    def _dev_buffer(self, key, n):
+        """A device float32 buffer of n values for this thread, grown as needed and reused across calls."""
+        t = self._staging.get(("dev", key))
+        if t is None or t.numel() < n:
+            t = torch.empty(max(n, 5 * (0 if t is None else t.numel()) // 4), dtype=torch.float32, device=self.device)
+            self._staging[("dev", key)] = t
+        return t[:n]
+
     def _upload(self, key, array):
         host, dev = self._stage(key, array.shape)
         _host_copy(host.numpy(), array)
@@ -213,6 +221,11 @@ class GB300Backend:
     def _prepare(self, features, z_scale):
         nz, nx, ny = z_scale.shape
         V = nz * nx * ny
+        # the heights' analysis from the host copy, in the device's float32 values (z / 1e6 with IEEE division, as
+        # ffno_si_inputs computes it), so that the model's stream is not synchronised to read it back
+        z_mm = z_scale / np.float32(1e6)
+        # (heights that are not finite are left to the device path, which reports them through the request's flags)
+        self._local.geo = self.model.executor().geometry_host(z_mm[None]) if np.isfinite(z_mm).all() else None
         f_dev = self._upload("features", features)
         z_dev = self._upload("z", z_scale)
         x = torch.empty(1, 6, nz, nx, ny, dtype=torch.float32, device=self.device)
@@ -223,6 +236,134 @@ class GB300Backend:
                  self.std_x.data_ptr(), x.data_ptr(), zmm.data_ptr(), self._flags.data_ptr(), _stream())
         return f_dev, x, zmm, V
 
+    # ------------------------------------------------------------------------------------------------ wire layout
+    # The service's arrays are little-endian float32 in Fortran order (ffno_fsdp_service.py:219-322). The *_wire
+    # methods take a request's arrays as they arrived, back to back in one host buffer (pinned, for the copy engine),
+    # and write the reply's arrays in that order into `out`: no host-side transpose or copy; the layouts change on the
+    # device (ffno_reverse_axes4: Fortran order is the C order of the reversed shape). They validate like their
+    # *_local twins and raise the same errors.
+    def _wire_in(self, buf, shape, n_extra):
+        """Device arrays of a request buffer [6V features | V z | n_extra V]: the model's SI features [6][V], z [V]
+        (C order) and the extra array [V][n_extra] (a cotangent (nz, nx, ny, L)) or [n_extra][V] (a feature
+        tangent), with the host geometry of the heights."""
+        nz, nx, ny = shape
+        V = nz * nx * ny
+        n = V * (7 + n_extra)
+        if buf.numel() < n:
+            raise ValueError("request buffer shorter than its arrays")
+        raw = self._dev_buffer("wire_in", n)
+        raw.copy_(buf[:n], non_blocking=True)
+        s = _stream()
+        f = torch.empty(6, V, dtype=torch.float32, device=self.device)
+        z = torch.empty(V, dtype=torch.float32, device=self.device)
+        nat.call("ffno_reverse_axes4", raw.data_ptr(), ny, nx, nz, 6, f.data_ptr(), s)
+        nat.call("ffno_reverse_axes4", raw.data_ptr() + 24 * V, 1, ny, nx, nz, z.data_ptr(), s)
+        extra = None
+        if n_extra:
+            extra = torch.empty(n_extra * V, dtype=torch.float32, device=self.device)
+            src = raw.data_ptr() + 28 * V
+            if n_extra == 6:    # a feature tangent (6, nz, nx, ny)
+                nat.call("ffno_reverse_axes4", src, ny, nx, nz, 6, extra.data_ptr(), s)
+            else:               # a population cotangent (nz, nx, ny, L)
+                nat.call("ffno_reverse_axes4", src, n_extra, ny, nx, nz, extra.data_ptr(), s)
+        # the heights' analysis on the host, in the device's float32 values: the wire z is [ny][nx][nz], columns
+        # contiguous, column (0, 0) first
+        zw = buf[6 * V:7 * V].numpy().reshape(ny, nx, nz) / np.float32(1e6)
+        if np.isfinite(zw).all():
+            geo = self.model.executor().geometry_columns(zw.reshape(1, ny * nx, nz),
+                                                         lambda: zw.transpose(1, 0, 2).reshape(1, nx * ny, nz)
+                                                         .astype(np.float64))
+        else:
+            geo = None
+        return f, z, extra, geo, V
+
+    def _wire_model_inputs(self, f, z, V, shape):
+        nz, nx, ny = shape
+        x = torch.empty(1, 6, nz, nx, ny, dtype=torch.float32, device=self.device)
+        zmm = torch.empty(1, nz, nx, ny, dtype=torch.float32, device=self.device)
+        self._flags.zero_()
+        nat.call("ffno_si_inputs", f.data_ptr(), z.data_ptr(), V, self.mean_x.data_ptr(), self.std_x.data_ptr(),
+                 x.data_ptr(), zmm.data_ptr(), self._flags.data_ptr(), _stream())
+        return x, zmm
+
+    def _wire_out(self, arrays, out):
+        """Device arrays (each with its C-order shape, reversed into Fortran order on the device) -> out (host),
+        back to back."""
+        total = sum(a.numel() for a, _ in arrays)
+        if out.numel() < total:
+            raise ValueError("reply buffer shorter than the reply's arrays")
+        dev = self._dev_buffer("wire_out", total)
+        off = 0
+        for a, shape in arrays:
+            s0, s1, s2, s3 = shape
+            nat.call("ffno_reverse_axes4", a.data_ptr(), s0, s1, s2, s3, dev.data_ptr() + 4 * off, _stream())
+            off += a.numel()
+        out[:total].copy_(dev, non_blocking=True)
+
+    def predict_wire(self, buf, shape, dx, dy, out):
+        """PREDICT on a request buffer [features | z] in wire layout: populations (nz, nx, ny, L) in wire layout into
+        out. Returns the number of floats written."""
+        f, z, _, geo, V = self._wire_in(buf, shape, 0)
+        x, zmm = self._wire_model_inputs(f, z, V, shape)
+        L = self.model.out_channels
+        with torch.no_grad():
+            y = self._guarded(lambda: self.model.executor().forward(x, zmm, float(dx), float(dy), geo=geo)[0])
+        pop = torch.empty(V, L, dtype=torch.float32, device=self.device)
+        nat.call("ffno_si_populations", y.data_ptr(), V, L, self.mean_y.data_ptr(), self.std_y.data_ptr(),
+                 pop.data_ptr(), self._out_flags(), _stream())
+        self._wire_out([(pop, (shape[0], shape[1], shape[2], L))], out)
+        _check(self._finish(), "FFNO output")
+        self.call_count += 1
+        return V * L
+
+    def vjp_wire(self, buf, shape, dx, dy, out):
+        """VJP on a request buffer [features | z | population cotangent] in wire layout: features_bar (6, nz, nx, ny)
+        then z_bar (nz, nx, ny) in wire layout into out. Returns the number of floats written."""
+        L = self.model.out_channels
+        f, z, cot, geo, V = self._wire_in(buf, shape, L)
+        x, zmm = self._wire_model_inputs(f, z, V, shape)
+        ex = self.model.executor()
+        y, state = self._guarded(lambda: ex.forward(x, zmm, float(dx), float(dy), keep=True, geo=geo))
+        ybar = torch.empty_like(y)
+        nat.call("ffno_si_population_cotangent", y.data_ptr(), cot.data_ptr(), V, L, self.mean_y.data_ptr(),
+                 self.std_y.data_ptr(), ybar.data_ptr(), self._out_flags(), _stream())
+        xbar, zbar = self._guarded(lambda: ex.backward(state, ybar))
+        fbar = torch.empty(6, V, dtype=torch.float32, device=self.device)
+        zbar_m = torch.empty(V, dtype=torch.float32, device=self.device)
+        nat.call("ffno_si_input_grads", f.data_ptr(), xbar.data_ptr(), zbar.data_ptr(), V, self.std_x.data_ptr(),
+                 fbar.data_ptr(), zbar_m.data_ptr(), self._out_flags(), _stream())
+        nz, nx, ny = shape
+        self._wire_out([(fbar, (6, nz, nx, ny)), (zbar_m, (1, nz, nx, ny))], out)
+        flags = self._finish()
+        if flags & 1:
+            raise ValueError("FFNO VJP cotangent contains NaN or Inf")
+        _check(flags, "FFNO VJP")
+        self.call_count += 1
+        return 7 * V
+
+    def jvp_wire(self, buf, shape, dx, dy, out):
+        """JVP on a request buffer [features | z | feature tangent] in wire layout: the population tangent
+        (nz, nx, ny, L) in wire layout into out. Returns the number of floats written."""
+        f, z, tangent, _, V = self._wire_in(buf, shape, 6)
+        x, zmm = self._wire_model_inputs(f, z, V, shape)
+        x_dot = torch.empty_like(x)
+        nat.call("ffno_si_input_tangent", f.data_ptr(), tangent.data_ptr(), V, self.std_x.data_ptr(),
+                 x_dot.data_ptr(), self._out_flags(), _stream())
+        y, y_dot = self._guarded(lambda: self.model.executor().jvp(x, zmm, float(dx), float(dy), x_dot))
+        L = self.model.out_channels
+        pop_dot = torch.empty(V, L, dtype=torch.float32, device=self.device)
+        nat.call("ffno_si_population_tangent", y.data_ptr(), y_dot.data_ptr(), V, L, self.mean_y.data_ptr(),
+                 self.std_y.data_ptr(), pop_dot.data_ptr(), self._out_flags(), _stream())
+        self._wire_out([(pop_dot, (shape[0], shape[1], shape[2], L))], out)
+        flags = self._finish()
+        if flags & 1:
+            raise ValueError("FFNO JVP tangent contains NaN or Inf")
+        if flags & 8:
+            raise RuntimeError("FFNO JVP returned NaN or Inf")
+        _check(flags, "FFNO JVP")
+        self.call_count += 1
+        return V * L
+
     # ------------------------------------------------------------------------------------------------ API
     def predict_local(self, features, z_scale, dx, dy):
         """(6,nz,nx,ny) SI features, (nz,nx,ny) heights [m] -> (nz,nx,ny,L) populations [m^-3]
@@ -231,7 +372,8 @@ class GB300Backend:
         _, x, zmm, V = self._prepare(features, z_scale)
         L = self.model.out_channels
         with torch.no_grad():
-            y = self._guarded(lambda: self.model(x, zmm, float(dx), float(dy)))
+            y = self._guarded(lambda: self.model.executor().forward(x, zmm, float(dx), float(dy),
+                                                                    geo=self._local.geo)[0])
         pop = torch.empty(*z_scale.shape, L, dtype=torch.float32, device=self.device)
         nat.call("ffno_si_populations", y.data_ptr(), V, L, self.mean_y.data_ptr(), self.std_y.data_ptr(),
                  pop.data_ptr(), self._out_flags(), _stream())
@@ -287,7 +429,8 @@ class GB300Backend:
         copier.start()
         ex = self.model.executor()
         try:
-            y, state = self._guarded(lambda: ex.forward(x, zmm, float(dx), float(dy), keep=True))
+            y, state = self._guarded(lambda: ex.forward(x, zmm, float(dx), float(dy), keep=True,
+                                                        geo=self._local.geo))
         finally:
             copier.join()
         cot_dev.copy_(cot_host, non_blocking=True)

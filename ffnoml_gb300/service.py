@@ -50,6 +50,16 @@ def read_exact(stream, count):
     return bytes(buf)
 
 
+def read_into(stream, view):
+    """Fill a writable byte memoryview from the socket."""
+    off, count = 0, len(view)
+    while off < count:
+        n = stream.recv_into(view[off:])
+        if n == 0:
+            raise EOFError("client disconnected during array transfer")
+        off += n
+
+
 def read_array(stream, shape):
     count = int(np.prod(shape))
     raw = read_exact(stream, count * 4)
@@ -88,13 +98,50 @@ def host_memory_bytes():
         return 1 << 62
 
 
+# ---------------------------------------------------------------------------------------------------- host buffers
+class HostBuffers:
+    """A pool of host float32 buffers for request and reply arrays: pinned (page-locked) when CUDA is available, so
+    that the copy engine moves them without staging. A request's arrays are received straight into one buffer and
+    a reply's arrays are sent straight from one, in the protocol's own layout; buffers are kept by size class (powers
+    of two) for reuse, at most `keep` free ones a class."""
+
+    def __init__(self, keep=4):
+        self.keep = keep
+        self.free = collections.defaultdict(list)
+        self.lock = threading.Lock()
+        self.pinned = torch.cuda.is_available()
+
+    def acquire(self, n):
+        size = 1 << max(20, (int(n) - 1).bit_length())
+        with self.lock:
+            if self.free[size]:
+                return self.free[size].pop()
+        return torch.empty(size, dtype=torch.float32, pin_memory=self.pinned)
+
+    def release(self, buf):
+        if buf is None:
+            return
+        with self.lock:
+            if len(self.free[buf.numel()]) < self.keep:
+                self.free[buf.numel()].append(buf)
+
+
+def _bytes_view(buf, n):
+    """The first n floats of a host buffer as a writable byte memoryview."""
+    return memoryview(buf.numpy()[:n]).cast("B")
+
+
 # ---------------------------------------------------------------------------------------------------- scheduling
 class Request:
-    def __init__(self, op, name, shape, levels, dx, dy, arrays):
+    """One request: its header fields and its arrays as received, back to back in a host buffer (wire layout:
+    features (6, nz, nx, ny), z (nz, nx, ny), then the cotangent or tangent, each little-endian float32 in Fortran
+    order)."""
+
+    def __init__(self, op, name, shape, levels, dx, dy, buf, pool=None):
         self.op, self.name, self.shape, self.levels, self.dx, self.dy = op, name, shape, levels, dx, dy
-        self.arrays = arrays
+        self.buf, self.pool = buf, pool
         self.done = threading.Event()
-        self.reply = None            # bytes to send
+        self.reply = None            # bytes to send, or (header bytes, host buffer, float count)
         self.t_arrive = time.perf_counter()
         self.t_start = self.t_done = None
 
@@ -102,6 +149,24 @@ class Request:
     def voxels(self):
         nz, nx, ny = self.shape
         return nz * nx * ny
+
+    @property
+    def arrays(self):
+        """The request's arrays as numpy views (Fortran order) over its buffer."""
+        nz, nx, ny = self.shape
+        V = nz * nx * ny
+        a = self.buf.numpy()
+        out = [a[:6 * V].reshape((6, nz, nx, ny), order="F"), a[6 * V:7 * V].reshape((nz, nx, ny), order="F")]
+        if self.op == "VJP":
+            out.append(a[7 * V:(7 + self.levels) * V].reshape((nz, nx, ny, self.levels), order="F"))
+        elif self.op == "JVP":
+            out.append(a[7 * V:13 * V].reshape((6, nz, nx, ny), order="F"))
+        return out
+
+    def release(self):
+        if self.pool is not None:
+            self.pool.release(self.buf)
+        self.buf = None
 
     def finish(self, reply):
         self.reply = reply
@@ -118,8 +183,9 @@ def workspace_bytes(op, voxels, width, levels):
 class Scheduler:
     """FIFO admission into `slots` GPU workers under an HBM budget."""
 
-    def __init__(self, backends, slots=4, memory_fraction=0.8, budget_bytes=None, device=None):
+    def __init__(self, backends, slots=4, memory_fraction=0.8, budget_bytes=None, device=None, pool=None):
         self.backends = backends
+        self.pool = pool
         self.slots = max(1, int(slots))
         # a VJP recomputes each block in its backward: its workspace stays within the admission estimate while
         # other requests run beside it
@@ -193,11 +259,12 @@ class Scheduler:
                 if ctx is None:
                     raise RuntimeError(f"service slot unavailable: {self.failed}")
                 with ctx():
-                    reply = execute(self.backends, req)
+                    reply = execute(self.backends, req, self.pool)
             except Exception as exc:  # reported to the client, the service stays up
                 reply = f"ERROR {type(exc).__name__}: {exc}".replace("\n", " ").encode() + b"\n"
             finally:
                 self._release(cost)
+                req.release()
             req.finish(reply)
             with self.cv:
                 self.completed.append(req)
@@ -210,8 +277,10 @@ class Scheduler:
             w.join(timeout=30)
 
 
-def execute(backends, req):
-    """Run one request on the current stream; returns the reply bytes."""
+def execute(backends, req, pool=None):
+    """Run one request on the current stream; returns the reply: bytes, or (header bytes, host buffer, float count)
+    when the backend takes the wire layout (GB300Backend.*_wire: the arrays are reordered on the device, so the host
+    neither transposes nor copies them)."""
     if req.name not in backends:
         raise KeyError(f"unknown model {req.name!r}")
     backend = backends[req.name]
@@ -219,6 +288,16 @@ def execute(backends, req):
         raise ValueError("request level count differs from the model")
     nz, nx, ny = req.shape
     head = f"OK {req.op} {nz} {nx} {ny} {req.levels}\n".encode()
+    wire = getattr(backend, req.op.lower() + "_wire", None)
+    if wire is not None and pool is not None:
+        V = nz * nx * ny
+        out = pool.acquire(7 * V if req.op == "VJP" else req.levels * V)
+        try:
+            n = wire(req.buf, req.shape, req.dx, req.dy, out)
+        except BaseException:
+            pool.release(out)
+            raise
+        return head, out, n
     if req.op == "PREDICT":
         pop = backend.predict_local(req.arrays[0], req.arrays[1], req.dx, req.dy)
         return head + array_bytes(pop)
@@ -239,7 +318,8 @@ class Server:
         self.token = str(token)
         self.max_request_bytes = int(max_request_bytes or host_memory_bytes())
         self.slots = max(2, int(slots))
-        self.scheduler = Scheduler(self.backends, self.slots, memory_fraction, budget_bytes, device)
+        self.pool = HostBuffers()
+        self.scheduler = Scheduler(self.backends, self.slots, memory_fraction, budget_bytes, device, self.pool)
         self.listener = socket.socket(socket.AF_INET, socket.SOCK_STREAM)
         self.listener.setsockopt(socket.SOL_SOCKET, socket.SO_REUSEADDR, 1)
         self.listener.bind((host, int(port)))
@@ -303,7 +383,15 @@ class Server:
                 else:
                     data = item
                 try:
-                    conn.sendall(data)
+                    if isinstance(data, tuple):          # header, then the arrays straight from the host buffer
+                        head, buf, n = data
+                        try:
+                            conn.sendall(head)
+                            conn.sendall(_bytes_view(buf, n))
+                        finally:
+                            self.pool.release(buf)
+                    else:
+                        conn.sendall(data)
                 except OSError:
                     return
 
@@ -347,12 +435,14 @@ class Server:
                 except ValueError as exc:
                     replies.put(f"ERROR invalid command: {exc}\n".encode())
                     break                                   # the arrays' length is unknown: the stream is lost
-                arrays = [read_array(conn, (6, nz, nx, ny)), read_array(conn, (nz, nx, ny))]
-                if op == "VJP":
-                    arrays.append(read_array(conn, (nz, nx, ny, levels)))
-                elif op == "JVP":
-                    arrays.append(read_array(conn, (6, nz, nx, ny)))
-                req = Request(op, name, (nz, nx, ny), levels, dx, dy, arrays)
+                n = nbytes // 4
+                buf = self.pool.acquire(n)
+                try:
+                    read_into(conn, _bytes_view(buf, n))
+                except BaseException:
+                    self.pool.release(buf)
+                    raise
+                req = Request(op, name, (nz, nx, ny), levels, dx, dy, buf, self.pool)
                 replies.put(req)
                 self.scheduler.submit(req)
         except (EOFError, ConnectionError, OSError):
@@ -400,6 +490,24 @@ class Client:
     def request(self, op, name, features, z, dx, dy, levels, extra=None):
         self.send(op, name, features, z, dx, dy, levels, extra)
         return self.receive(op, z.shape, levels)
+
+    @staticmethod
+    def encode(op, name, features, z, dx, dy, levels, extra=None):
+        """A request's bytes (header and arrays), for a client that sends the same request many times."""
+        nz, nx, ny = z.shape
+        msg = f"{op} {name} {nz} {nx} {ny} {levels} {dx} {dy}\n".encode() + array_bytes(features) + array_bytes(z)
+        return msg + (array_bytes(extra) if extra is not None else b"")
+
+    def request_raw(self, msg, reply_bytes, into=None):
+        """Send encoded request bytes; return the reply's header fields, its arrays' bytes read into `into` (a
+        writable buffer of at least reply_bytes, reused by the caller)."""
+        self.sock.sendall(msg)
+        head = readline(self.sock).decode().split()
+        if not head or head[0] != "OK":
+            raise RuntimeError(" ".join(head))
+        view = memoryview(into if into is not None else bytearray(reply_bytes))[:reply_bytes]
+        read_into(self.sock, view)
+        return head
 
     def memory(self):
         self.sock.sendall(b"MEMORY\n")

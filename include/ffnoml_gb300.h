@@ -168,7 +168,9 @@ int ffno_spectral_mix(const float* in, float* out, long F, long nb, long sf, lon
 /* ------------------------------------------------------------------------------------------------------------------
  * Input VJP (the hand-written replacement of torch.autograd.backward through FFNO3D.forward under per-block
  * checkpointing, ffno_fsdp_runtime.py:306-348 and models/ffno_model.py:751-780). u is the gradient arriving at a
- * GroupNorm's consumer: mode 0 means dL/dy = r*u (y = GN(pre)), mode 1 means dL/dy = r*u*gelu'(y) (GELU after GN).
+ * GroupNorm's consumer: mode 0 means dL/dy = r*u (y = GN(pre)), mode 1 means dL/dy = r*u*gelu'(y) (GELU after GN),
+ * mode 2 the same with the tensor-core kernels' GELU (the normal CDF of Abramowitz & Stegun 7.1.26), for the
+ * GroupNorms whose GELU the split-BF16 forward applied with it.
  * ------------------------------------------------------------------------------------------------------------------ */
 
 /* Per-group sums S1 = sum ghat, S2 = sum ghat*xhat of the GroupNorm backward, ghat = dL/dy * gamma, as partials
@@ -279,6 +281,12 @@ int ffno_mesh_backmap_vjp(const double* pm, const double* mesh, int nm, const do
                           const double* pop_bar, double* pm_bar, double* z_bar, ffno_stream_t stream);
 int ffno_mesh_backmap_jvp(const double* pm, const double* pm_dot, const double* mesh, int nm, const double* z,
                           long ncol, int nz, int L, double* pop_dot, ffno_stream_t stream);
+
+/* Reverses the four axes of an array: in C-order [s0][s1][s2][s3] -> out C-order [s3][s2][s1][s0], i.e. the same
+ * array in Fortran order. The protocol's arrays (FFNOInversion.jl/src/FSDPService.jl: features (6, nz, nx, ny), z,
+ * populations (nz, nx, ny, L), in Fortran order; ffno_fsdp_service.py:219-322) go between their wire layout and the
+ * model's with it on the device. in and out must not overlap; s1 and ceil(s0 / 32) at most 65535. */
+int ffno_reverse_axes4(const float* in, long s0, long s1, long s2, long s3, float* out, ffno_stream_t stream);
 
 /* Host-RAM streaming (ffno_batched_backend.py:147-289): strided block copy between pinned host memory and the device,
  * rows of `width` bytes `spitch` / `dpitch` apart (cudaMemcpy2DAsync, direction from the addresses). */

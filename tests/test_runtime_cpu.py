@@ -51,3 +51,28 @@ def test_tangent_shape_and_values_are_checked():
     t[3, 2, 1, 0] = np.inf
     with pytest.raises(ValueError, match=r"NaN or Inf"):
         be.jvp_local(f, z, 48e3, 48e3, t)
+
+
+def test_host_geometry_decides_the_shared_grid_like_the_column_kernel():
+    """Executor.geometry_host (the service backend's per-request analysis, no device read-back): every column equal
+    to column 0 after subtracting its own minimum, in float32, gives the shared path; one column apart, or two
+    samples whose columns differ, gives the per-column path with every column's heights."""
+    import numpy as np
+    from ffnoml_gb300 import create_ffno3d
+    from ffnoml_gb300.executor import Executor
+    ex = Executor(create_ffno3d(6, 6, atoms=["H"], width=16, n_layers=1, hidden_spectral=16, hidden_vertical=16,
+                                z_min_wavelength=0.5))
+    D, H, W = 12, 5, 4
+    col = np.linspace(14.0, -1.0, D, dtype=np.float32)
+    z = np.broadcast_to(col[:, None, None], (D, H, W)).copy()[None]
+    g = ex.geometry_host(z)
+    assert g.shared and g.columns is None and abs(g.span - 15.0) < 1e-6
+    assert np.allclose(g.column_raw, col)
+    bent = z.copy()
+    bent[0, 3, 2, 1] += np.float32(0.25)
+    g = ex.geometry_host(bent)
+    assert not g.shared and g.columns.shape == (1, H * W, D)
+    assert g.columns[0, 2 * W + 1, 3] == np.float32(col[3] + np.float32(0.25))
+    two = np.concatenate([z, z * np.float32(0.5)])
+    g = ex.geometry_host(two)
+    assert not g.shared and g.columns.shape == (2, H * W, D)

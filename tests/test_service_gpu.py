@@ -105,3 +105,51 @@ def test_results_are_the_same_alone_and_in_a_mix(served):
     [t.join() for t in ts]
     for a, b in zip(alone, mixed):
         assert np.array_equal(a, b)
+
+
+@pytest.fixture(scope="module")
+def served_bf16():
+    from ffnoml_gb300.runtime import GB300Backend
+    from ffnoml_gb300.service import Server
+    backend = GB300Backend(_model("bf16"), [f"l{i}" for i in range(12)])
+    srv = Server({"HCA": backend}, "tok", slots=4)
+    srv.start()
+    yield srv
+    srv.shutdown()
+
+
+def test_bf16_results_are_the_same_alone_and_in_a_mix(served_bf16):
+    """The service's default precision (split-BF16 tensor cores): PREDICT and VJP requests of uneven sizes give the
+    same bits alone and while other requests run on the device beside them (each request has its own workspace and
+    the kernels' reductions run in a fixed order)."""
+    from ffnoml_gb300.service import Client
+    srv = served_bf16
+    shapes = [(40, 32, 32), (24, 48, 40), (64, 16, 24), (16, 24, 16), (32, 40, 40)]
+    reqs = []
+    for i, s in enumerate(shapes):
+        f, z = _request(s, 30 + i)
+        op = "VJP" if i % 2 else "PREDICT"
+        cot = (np.random.default_rng(40 + i).normal(size=s + (12,)) * 1e-15).astype(np.float32) if op == "VJP" else None
+        reqs.append((op, f, z, cot))
+
+    def ask(cl, op, f, z, cot):
+        out = cl.request(op, "HCA", f, z, 48e3, 48e3, 12, cot)
+        return [out] if op == "PREDICT" else [out["features"], out["z_scale"]]
+
+    c = Client(srv.port, "tok")
+    alone = [ask(c, *r) for r in reqs]
+    c.close()
+    mixed = [None] * len(reqs)
+
+    def run(i):
+        cl = Client(srv.port, "tok")
+        for _ in range(3):
+            mixed[i] = ask(cl, *reqs[i])
+        cl.close()
+
+    ts = [threading.Thread(target=run, args=(i,)) for i in range(len(reqs))]
+    [t.start() for t in ts]
+    [t.join() for t in ts]
+    for i, (a, b) in enumerate(zip(alone, mixed)):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), (i, reqs[i][0])

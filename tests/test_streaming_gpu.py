@@ -68,3 +68,58 @@ def test_streaming_backend_log10_and_si():
         bad = f.copy()
         bad[0, 0, 0, 0] = -1.0
         sb.predict_si(bad, z, 48e3, 48e3)
+
+
+def _rel_per_channel(got, ref):
+    """max over the feature channels of max |got - ref| / max |ref| (their SI units differ by decades)."""
+    return max(float(np.abs(got[c] - ref[c]).max() / np.abs(ref[c]).max()) for c in range(ref.shape[0]))
+
+
+@pytest.mark.parametrize("width,precision,tol", [(32, "fp32", 1e-4), (64, "fp32", 1e-4), (64, "bf16", 1e-2)])
+def test_streaming_vjp_matches_resident(width, precision, tol):
+    """The streaming VJP (block inputs in pinned host memory, blocks recomputed and back-propagated slab by slab)
+    against the resident VJP through the service backend: the same kernels on the same voxels; only the GroupNorm
+    sums' merge order differs."""
+    import bench
+    from ffnoml_gb300.runtime import GB300Backend
+    from ffnoml_gb300.streaming import StreamingVJP
+    model = _model(width, precision)
+    f, z = bench.synthetic_si((23, 14, 10), seed=9)
+    cot = np.random.default_rng(10).normal(size=(23, 14, 10, 12)).astype(np.float32)
+    pop = GB300Backend(model, [f"l{i}" for i in range(12)]).predict_local(f, z, 48e3, 48e3)
+    cot = cot / pop                          # the cotangent of ln n, as the inversion's gradients scale
+    ref = GB300Backend(model, [f"l{i}" for i in range(12)]).vjp_local(f, z, 48e3, 48e3, cot)
+    sv = StreamingVJP(model, chunk_depth=6, chunk_rows=4)
+    got = sv(f, z, 48e3, 48e3, cot)
+    assert got["features"].shape == (6, 23, 14, 10) and got["z_scale"].shape == (23, 14, 10)
+    ef = _rel_per_channel(got["features"], ref["features"])
+    ez = float(np.abs(got["z_scale"] - ref["z_scale"]).max() / np.abs(ref["z_scale"]).max())
+    print(f"w{width} {precision}: streaming vs resident VJP: features {ef:.2e}, z {ez:.2e}, {sv.slabs} slabs")
+    assert ef < tol
+    assert ez < 10 * tol
+
+
+def test_streaming_vjp_against_the_float64_oracle():
+    """The streaming VJP in FP32 against the float64 oracle's SI-level VJP (its forward_si through autograd)."""
+    import bench
+    from ffnoml_gb300.config import species_of
+    from ffnoml_gb300.streaming import StreamingBackend
+    from oracle.ffno_oracle import OracleFFNO3D
+    model = _model(32, "fp32")
+    f, z = bench.synthetic_si((17, 10, 12), seed=11)
+    state = {k: v.detach().cpu().clone() for k, v in model.state_dict().items()}
+    cfg = dict(width=32, n_layers=2, z_min_wavelength=40.0 / 15, species=species_of(["H", "CA"]), in_channels=6,
+               out_channels=12)
+    oracle = OracleFFNO3D({k: v.double() for k, v in state.items()}, cfg, torch.float64)
+    fr = torch.from_numpy(f.astype(np.float64))[None].requires_grad_(True)
+    zr = torch.from_numpy(z.astype(np.float64))[None].requires_grad_(True)
+    pops = oracle.forward_si(fr, zr, 48e3, 48e3)[0].permute(1, 2, 3, 0)
+    cot = (np.random.default_rng(12).normal(size=pops.shape) / pops.detach().numpy()).astype(np.float32)
+    fb, zb = torch.autograd.grad(pops, (fr, zr), torch.from_numpy(cot.astype(np.float64)))
+    sb = StreamingBackend(model, [f"l{i}" for i in range(12)], chunk_depth=5, chunk_rows=3)
+    got = sb.vjp_local(f, z, 48e3, 48e3, cot)
+    ef = _rel_per_channel(got["features"], fb[0].numpy())
+    ez = float(np.abs(got["z_scale"] - zb[0].numpy()).max() / np.abs(zb[0].numpy()).max())
+    print(f"streaming VJP vs float64 oracle: features {ef:.2e}, z {ez:.2e}")
+    assert ef < 1e-4
+    assert ez < 1e-3
