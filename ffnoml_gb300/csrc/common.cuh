@@ -68,6 +68,7 @@ __device__ __forceinline__ float mtanh(float x) { return tanhf(x); }
 // MULTI3D constants, cgs (models/ffno_model.py:111-112)
 constexpr double kEE = 1.602189e-12, kBK = 1.380662e-16;
 constexpr double kLN10 = 2.302585092994045684;
+constexpr double kINV_LN10 = 0.434294481903251827651;
 
 __device__ __forceinline__ double ln_ccon() {
   // log(0.5 * (HH / sqrt(2 pi EM) / sqrt(BK))^3), MULTI3D's Saha constant (models/ffno_model.py:112)
@@ -159,8 +160,9 @@ __device__ __forceinline__ void head_voxel_fwd(const ffno_head_params& hp, const
     const double base = lrho - (double)hp.log10_particle_mass[s] + tb * tanh((double)o[hc + L] / tb);
     for (int i = 0; i < L; ++i) {
       const int g = lvl + i;
-      const double l10 = base + ((double)(logit[i] - mx) - (double)lse) / kLN10;
-      out[(long)g * V + v] = (float)((l10 - (double)hp.mean_y[g]) / (double)hp.std_y[g]);
+      const double l10 = base + ((double)(logit[i] - mx) - (double)lse) * kINV_LN10;
+      // the large terms cancel in FP64; the difference (a few units) is normalised in FP32
+      out[(long)g * V + v] = (float)(l10 - (double)hp.mean_y[g]) / hp.std_y[g];
     }
     hc += L + 1;
     lvl += L;
