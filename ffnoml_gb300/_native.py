@@ -94,6 +94,8 @@ PROTOTYPES = {
     "ffno_tc_set_prefetch_tiles": [I],
     "ffno_copy2d": [P, L, P, L, L, L, P],
     "ffno_reverse_axes4": [P, L, L, L, L, P, P],
+    "ffno_shear_levels": [P, I, L, L, P, P, P, P, I, P, P],
+    "ffno_mesh_refine": [P, L, I, D, D, D, D, D, P, P],
     "ffno_mesh_features": [P, P, L, I, P, I, I, P, P, P],
     "ffno_mesh_features_vjp": [P, P, L, I, P, I, I, P, P, P, P, P],
     "ffno_mesh_features_jvp": [P, P, L, I, P, I, I, P, P, P, P],

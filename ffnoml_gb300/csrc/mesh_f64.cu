@@ -231,6 +231,66 @@ bool dims_ok(long ncol, int nz, int nm) {
   return ncol >= 1 && nz >= 2 && nm >= 1 && ncol * (long)(nz > nm ? nz : nm) < (long)0x7fffffff * 256L;
 }
 
+// ------------------------------------------------------------------------------------------------ adaptive mesh
+// The spacing each probe interval needs (adaptive_population_mesh, FFNOInversion.jl/src/PopulationMesh.jl:213-262):
+// for column c and interval i of features f [ncol][n][6] (T, v, log10 ne, log10 rho on probe heights dz apart),
+// r = max(|ln(T_i / T_{i+1})| / lnT_step, |d log10 ne| / log_ne_step, |d log10 rho| / log_rho_step, |d v| / v_step),
+// and need[i] = min(need[i], dz / r) over the columns with r > 0. The minimum of positive doubles is taken on their
+// bit patterns (which order as the values), so the result does not depend on the order of the columns.
+__global__ void k_mesh_refine(const double* __restrict__ f, long ncol, int n, double dz, double lnT_step,
+                              double ne_step, double rho_step, double v_step, unsigned long long* __restrict__ need) {
+  const long total = ncol * (long)(n - 1);
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const long col = e / (n - 1);
+    const int i = (int)(e - col * (n - 1));
+    const double* a = f + (col * n + i) * 6;
+    const double* b = a + 6;
+    double r = fabs(log(a[0] / b[0])) / lnT_step;
+    r = fmax(r, fabs(a[4] - b[4]) / ne_step);
+    r = fmax(r, fabs(a[5] - b[5]) / rho_step);
+    for (int v = 1; v <= 3; ++v) r = fmax(r, fabs(a[v] - b[v]) / v_step);
+    if (r > 0.0) atomicMin(need + i, (unsigned long long)__double_as_longlong(dz / r));
+  }
+}
+
+// ------------------------------------------------------------------------------------------------ inclined views
+// The periodic bilinear shear of an inclined view between Cartesian mesh columns and the footprint rays
+// (FFNOInversion.jl/src/ViewAngle.jl:93-145): level k of A [nz][nx][ny] is read at the fractional cell offset
+// (i0[k] + wx[k], j0[k] + wy[k]), the same for every cell of the level:
+//   out[k][i][j] = (1 - wy)((1 - wx) A[k][ia][ja] + wx A[k][ib][ja]) + wy((1 - wx) A[k][ia][jb] + wx A[k][ib][jb]),
+//   ia = (i + i0) mod nx, ib = (ia + 1) mod nx, ja = (j + j0) mod ny, jb = (ja + 1) mod ny.
+// Its transpose (ViewAngle.jl:147-162, a scatter there) is a gather here, one thread per output value and no atomics:
+//   out[k][p][q] = (1 - wy)(1 - wx) A[k][p - i0][q - j0] + (1 - wy) wx A[k][p - 1 - i0][q - j0]
+//                + wy (1 - wx) A[k][p - i0][q - 1 - j0] + wy wx A[k][p - 1 - i0][q - 1 - j0]   (indices mod nx, ny).
+__device__ __forceinline__ long pmod(long a, long n) {
+  const long r = a % n;
+  return r < 0 ? r + n : r;
+}
+
+__global__ void k_shear_levels(const double* __restrict__ A, int nz, long nx, long ny, const int* __restrict__ i0,
+                               const int* __restrict__ j0, const double* __restrict__ wx,
+                               const double* __restrict__ wy, int transpose, double* __restrict__ out) {
+  const long n = (long)nz * nx * ny;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const long j = e % ny, t = e / ny, i = t % nx;
+    const int k = (int)(t / nx);
+    const double ax = wx[k], ay = wy[k];
+    const double* a = A + (long)k * nx * ny;
+    double v;
+    if (!transpose) {
+      const long ia = pmod(i + i0[k], nx), ib = (ia + 1) % nx, ja = pmod(j + j0[k], ny), jb = (ja + 1) % ny;
+      v = (1.0 - ay) * ((1.0 - ax) * a[ia * ny + ja] + ax * a[ib * ny + ja]) +
+          ay * ((1.0 - ax) * a[ia * ny + jb] + ax * a[ib * ny + jb]);
+    } else {
+      const long pa = pmod(i - i0[k], nx), pb = pmod(i - 1 - i0[k], nx), qa = pmod(j - j0[k], ny),
+                 qb = pmod(j - 1 - j0[k], ny);
+      v = (1.0 - ay) * ((1.0 - ax) * a[pa * ny + qa] + ax * a[pb * ny + qa]) +
+          ay * ((1.0 - ax) * a[pa * ny + qb] + ax * a[pb * ny + qb]);
+    }
+    out[e] = v;
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -286,6 +346,30 @@ int ffno_mesh_backmap_vjp(const double* pm, const double* mesh, int nm, const do
   if (!pm || !mesh || !z || !pop_bar || !pm_bar || !z_bar || L < 1 || !dims_ok(ncol, nz, nm)) return FFNO_EINVAL;
   k_mesh_backmap_vjp<<<blocks_for(ncol), 256, 0, (cudaStream_t)stream>>>(pm, mesh, nm, z, ncol, nz, L, pop_bar,
                                                                            pm_bar, z_bar);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_shear_levels(const double* A, int nz, long nx, long ny, const int* i0, const int* j0, const double* wx,
+                      const double* wy, int transpose, double* out, ffno_stream_t stream) {
+  if (!A || !i0 || !j0 || !wx || !wy || !out || A == out || nz < 1 || nx < 1 || ny < 1) return FFNO_EINVAL;
+  const long n = (long)nz * nx * ny;
+  const long blocks = (n + 255) / 256 < 8L * 152 ? (n + 255) / 256 : 8L * 152;
+  k_shear_levels<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(A, nz, nx, ny, i0, j0, wx, wy, transpose, out);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_mesh_refine(const double* f, long ncol, int n, double dz, double lnT_step, double log_ne_step,
+                     double log_rho_step, double velocity_step, double* need, ffno_stream_t stream) {
+  if (!f || !need || ncol < 1 || n < 2 || !(dz > 0) || !(lnT_step > 0) || !(log_ne_step > 0) || !(log_rho_step > 0) ||
+      !(velocity_step > 0))
+    return FFNO_EINVAL;
+  const long total = ncol * (long)(n - 1);
+  const long blocks = (total + 255) / 256 < 8L * 152 ? (total + 255) / 256 : 8L * 152;
+  k_mesh_refine<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(f, ncol, n, dz, lnT_step, log_ne_step, log_rho_step,
+                                                                    velocity_step,
+                                                                    reinterpret_cast<unsigned long long*>(need));
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

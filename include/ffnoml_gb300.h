@@ -282,6 +282,22 @@ int ffno_mesh_backmap_vjp(const double* pm, const double* mesh, int nm, const do
 int ffno_mesh_backmap_jvp(const double* pm, const double* pm_dot, const double* mesh, int nm, const double* z,
                           long ncol, int nz, int L, double* pop_dot, ffno_stream_t stream);
 
+/* The spacing each probe interval of an adaptive population mesh needs (FFNOInversion.jl/src/PopulationMesh.jl:
+ * 213-262): f [ncol][n][6] the mesh features of every column on n probe heights dz apart (ffno_mesh_features);
+ * need [n - 1] holds positive spacings (the maximum spacing) on entry and, on return, for each interval the minimum
+ * over the columns of dz / r, r the largest of |ln(T ratio)| / lnT_step, |d log10 ne| / log_ne_step,
+ * |d log10 rho| / log_rho_step and |d v| / velocity_step over the interval (columns with r = 0 leave it). */
+int ffno_mesh_refine(const double* f, long ncol, int n, double dz, double lnT_step, double log_ne_step,
+                     double log_rho_step, double velocity_step, double* need, ffno_stream_t stream);
+
+/* Periodic bilinear shear of an inclined view between Cartesian mesh columns and footprint rays
+ * (FFNOInversion.jl/src/ViewAngle.jl:93-162, used by PopulationMesh.jl:296-317): A and out [nz][nx][ny] FP64 (level k
+ * a contiguous plane), per level the integer cell offsets i0, j0 [nz] and fractions wx, wy [nz] in [0, 1). transpose = 0:
+ * out[k][i][j] = bilinear read of A at ((i + i0 + wx) mod nx, (j + j0 + wy) mod ny); transpose = 1: its transpose
+ * (adjoint), written, not accumulated. A and out must not overlap. */
+int ffno_shear_levels(const double* A, int nz, long nx, long ny, const int* i0, const int* j0, const double* wx,
+                      const double* wy, int transpose, double* out, ffno_stream_t stream);
+
 /* Reverses the four axes of an array: in C-order [s0][s1][s2][s3] -> out C-order [s3][s2][s1][s0], i.e. the same
  * array in Fortran order. The protocol's arrays (FFNOInversion.jl/src/FSDPService.jl: features (6, nz, nx, ny), z,
  * populations (nz, nx, ny, L), in Fortran order; ffno_fsdp_service.py:219-322) go between their wire layout and the

@@ -187,3 +187,119 @@ def features_jvp(atm, z, mesh, f, fd, corona=False):
                 out[col, m, c] = ad[c, 0] if kd == TOP else (1 - w) * ad[c, k] + w * ad[c, k + 1]
             out[col, m, 0] *= f[col, m, 0]
     return out
+
+
+# ------------------------------------------------------------------------------------------------ inclined views
+VIEW_Z_REF_M = 0.0      # the ray origin of the shear (FFNOInversion.jl/src/ViewAngle.jl:9)
+
+
+def slant(mu, azimuth_deg):
+    """t = tan(theta) (cos phi, sin phi) of an inclined view, mu = cos(theta) (FFNOInversion.jl/src/Types.jl:64-66);
+    (0, 0) for mu = 1."""
+    if mu >= 1.0:
+        return 0.0, 0.0
+    s = np.sqrt(1.0 - mu * mu) / mu
+    return s * np.cos(np.deg2rad(azimuth_deg)), s * np.sin(np.deg2rad(azimuth_deg))
+
+
+def shear_plan(z, dx, dy, t, s):
+    """Per level k: the integer cell offsets (i0, j0) and the fractions (wx, wy) of the shear s (t_x (z_k - z_ref)/dx,
+    t_y (z_k - z_ref)/dy) (ViewAngle.jl:107-115)."""
+    z = np.asarray(z, dtype=np.float64)
+    fx = s * t[0] * (z - VIEW_Z_REF_M) / dx
+    fy = s * t[1] * (z - VIEW_Z_REF_M) / dy
+    i0, j0 = np.floor(fx).astype(np.int64), np.floor(fy).astype(np.int64)
+    return i0, j0, fx - i0, fy - j0
+
+
+def shear_levels(A, plan):
+    """out[k, i, j] = the periodic bilinear read of level k of A (nz, nx, ny) at the level's offset (ViewAngle.jl:
+    132-145), by loops as the reference writes it."""
+    i0, j0, wx, wy = plan
+    nz, nx, ny = A.shape
+    out = np.empty_like(A, dtype=np.float64)
+    for k in range(nz):
+        for i in range(nx):
+            ia = (i + i0[k]) % nx
+            ib = (ia + 1) % nx
+            for j in range(ny):
+                ja = (j + j0[k]) % ny
+                jb = (ja + 1) % ny
+                out[k, i, j] = (1 - wy[k]) * ((1 - wx[k]) * A[k, ia, ja] + wx[k] * A[k, ib, ja]) + \
+                    wy[k] * ((1 - wx[k]) * A[k, ia, jb] + wx[k] * A[k, ib, jb])
+    return out
+
+
+def shear_levels_transpose(out_bar, plan):
+    """The transpose of shear_levels as the reference's scatter (ViewAngle.jl:147-162), into a zero array."""
+    i0, j0, wx, wy = plan
+    nz, nx, ny = out_bar.shape
+    A_bar = np.zeros_like(out_bar, dtype=np.float64)
+    for k in range(nz):
+        for i in range(nx):
+            ia = (i + i0[k]) % nx
+            ib = (ia + 1) % nx
+            for j in range(ny):
+                ja = (j + j0[k]) % ny
+                jb = (ja + 1) % ny
+                g = out_bar[k, i, j]
+                A_bar[k, ia, ja] += (1 - wy[k]) * (1 - wx[k]) * g
+                A_bar[k, ib, ja] += (1 - wy[k]) * wx[k] * g
+                A_bar[k, ia, jb] += wy[k] * (1 - wx[k]) * g
+                A_bar[k, ib, jb] += wy[k] * wx[k] * g
+    return A_bar
+
+
+# ------------------------------------------------------------------------------------------------ adaptive mesh
+def adaptive_mesh(atm, z, mesh_top, mesh_bottom, min_spacing_m, max_spacing_m, growth, lnT_step, log_ne_step,
+                  log_rho_step, velocity_step_m_s, extend=True, fill=None):
+    """adaptive_population_mesh (PopulationMesh.jl:213-262): atm [6][ncol][nz], z [ncol][nz] top first. Probe
+    heights below a column are filled by fill(f, kind) (a stand-in for the hydrostatic extension), else refused."""
+    top, bottom = (float(mesh_top), float(mesh_bottom)) if extend else (float(z[:, 0].max()), float(z[:, -1].min()))
+    n = max(2, int(np.ceil(2 * (top - bottom) / min_spacing_m)) + 1)
+    probe = np.linspace(top, bottom, n)
+    dz = probe[0] - probe[1]
+    f, kind = features(atm, z, probe)
+    if (kind >= DEEP).any():
+        if fill is None:
+            raise ValueError("probe heights below a column need the hydrostatic extension")
+        fill(f, kind)
+    need = np.full(n - 1, float(max_spacing_m))
+    for col in range(f.shape[0]):
+        g = f[col]
+        r = np.maximum.reduce([np.abs(np.log(g[:-1, 0] / g[1:, 0])) / lnT_step,
+                               np.abs(g[:-1, 4] - g[1:, 4]) / log_ne_step,
+                               np.abs(g[:-1, 5] - g[1:, 5]) / log_rho_step] +
+                              [np.abs(g[:-1, v] - g[1:, v]) / velocity_step_m_s for v in (1, 2, 3)])
+        pos = r > 0
+        need[pos] = np.minimum(need[pos], dz / r[pos])
+    h = np.clip(np.concatenate([[need[0]], np.minimum(need[:-1], need[1:]), [need[-1]]]), min_spacing_m,
+                max_spacing_m)
+    a = (growth - 1) * dz
+    for i in range(1, n):
+        h[i] = min(h[i], h[i - 1] + a)
+    for i in range(n - 2, -1, -1):
+        h[i] = min(h[i], h[i + 1] + a)
+
+    def spacing(zz):
+        u = min(max((top - zz) / dz, 0.0), n - 1)
+        i = min(int(np.floor(u)), n - 2)
+        return h[i] + (u - i) * (h[i + 1] - h[i])
+
+    def lowest(zz, s):
+        lo = min(max(int(np.floor((top - zz) / dz)) + 2, 1), n)
+        hi = min(max(int(np.ceil((top - zz + s) / dz)), 1), n)
+        window = h[lo - 1:hi]
+        return min(spacing(zz), spacing(zz - s), window.min() if window.size else np.inf)
+
+    mesh = [top]
+    while True:
+        zz = mesh[-1]
+        step = spacing(zz)
+        for _ in range(3):
+            step = lowest(zz, step)
+        if zz - step <= bottom + step / 2:
+            mesh.append(bottom)
+            break
+        mesh.append(zz - step)
+    return np.array(mesh)

@@ -196,3 +196,45 @@ def test_layout_round_trip():
     assert np.array_equal(pmesh.uncolumns(c, 3, 4), a)
     b = rng.normal(size=(2, 12, 5))
     assert np.array_equal(pmesh.uncolumns(b, 3, 4)[1, 4, 1, 2], b[1, 1 + 3 * 2, 4])
+
+
+# ------------------------------------------------------------------------------------------------ inclined views
+def test_shear_transpose_is_its_adjoint_and_zero_slant_is_the_identity():
+    """The oracle's shear (ViewAngle.jl:132-145) and its scatter transpose (:147-162): <S A, B> = <A, S^T B> for both
+    directions of an inclined view, and a vertical view reads every level in place."""
+    g = np.random.default_rng(5)
+    z = np.linspace(2.2e6, -1.3e6, 6)
+    A, B = g.normal(size=(6, 7, 4)), g.normal(size=(6, 7, 4))
+    t = pmo.slant(0.55, 35.0)
+    for s in (-1, 1):
+        plan = pmo.shear_plan(z, 48e3, 30e3, t, s)
+        assert (plan[0] < 0).any() or (plan[1] < 0).any() or s == 1
+        lhs = np.sum(pmo.shear_levels(A, plan) * B)
+        rhs = np.sum(A * pmo.shear_levels_transpose(B, plan))
+        assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    ident = pmo.shear_plan(z, 48e3, 30e3, pmo.slant(1.0, 35.0), 1)
+    assert np.array_equal(pmo.shear_levels(A, ident), A)
+
+
+def _hold_bottom(atm):
+    """The stand-in hydrostatic extension: points below a column take its bottom values."""
+    def fill(f, kind):
+        for col in range(f.shape[0]):
+            f[col, kind[col] == pmo.DEEP] = atm[:, col, -1]
+    return fill
+
+
+def test_adaptive_mesh_oracle_properties():
+    """adaptive_population_mesh (PopulationMesh.jl:213-262): top first from the highest top to the lowest bottom
+    (extend = false), every step within [min_spacing_m, max_spacing_m] (the last one may be shorter), neighbouring
+    steps within the growth factor's reach, and finer where the features change faster."""
+    f, z = mesh_test_atmosphere(nx=4, ny=3)
+    a, zc = atm_cols(f), cols(z)
+    kw = dict(min_spacing_m=1e4, max_spacing_m=1e5, growth=1.2, log_ne_step=0.1, log_rho_step=0.1,
+              velocity_step_m_s=1e3, extend=False, fill=_hold_bottom(a))
+    m = pmo.adaptive_mesh(a, zc, 1.4e7, -1e6, lnT_step=0.05, **kw)
+    d = -np.diff(m)
+    assert m[0] == zc[:, 0].max() and m[-1] == zc[:, -1].min() and (d > 0).all()
+    assert d[:-1].min() >= 1e4 * (1 - 1e-12) and d.max() <= 1e5 * (1 + 1e-12)
+    fine = pmo.adaptive_mesh(a, zc, 1.4e7, -1e6, lnT_step=0.01, **kw)
+    assert len(fine) > len(m)

@@ -9,8 +9,8 @@ import torch
 
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
 import population_mesh_oracle as pmo  # noqa: E402
-from test_population_mesh_cpu import (_grads, _mesh_inside, atm_cols, chain, cols, inner_jvp, inner_pm,  # noqa: E402
-                                      inner_vjp, mesh_test_atmosphere)
+from test_population_mesh_cpu import (_grads, _hold_bottom, _mesh_inside, atm_cols, chain, cols, inner_jvp,  # noqa: E402
+                                      inner_pm, inner_vjp, mesh_test_atmosphere)
 
 pytestmark = pytest.mark.gpu
 
@@ -148,4 +148,77 @@ def test_points_below_columns_need_an_extension():
     fd = (obj(f + h * tang) - obj(f - h * tang)) / (2 * h)
     assert abs(np.sum(fbar * tang) - fd) < 1e-6 * abs(fd)
     pd = model.jvp(f, z, 48e3, 48e3, tang)
+    assert abs(np.sum(bar * pd) - fd) < 1e-6 * abs(fd)
+
+
+# ------------------------------------------------------------------------------------------------ inclined views
+@pytest.mark.parametrize("shape,s", [((6, 7, 4), -1), ((6, 7, 4), 1), ((5, 1, 9), -1), ((4, 12, 1), 1)])
+def test_shear_kernel_matches_oracle(shape, s):
+    from ffnoml_gb300.population_mesh import ShearPlan
+    g = np.random.default_rng(7)
+    nz = shape[0]
+    z = np.linspace(2.2e6, -1.3e6, nz)
+    t = pmo.slant(0.45, 200.0)
+    A = g.normal(size=shape)
+    plan = ShearPlan(z, 48e3, 30e3, t, s, "cuda")
+    ref = pmo.shear_plan(z, 48e3, 30e3, t, s)
+    assert np.array_equal(plan.i0.cpu().numpy(), ref[0]) and np.array_equal(plan.j0.cpu().numpy(), ref[1])
+    At = torch.as_tensor(A, device="cuda")
+    _close(plan.apply(At).cpu().numpy(), pmo.shear_levels(A, ref), 1e-14)
+    _close(plan.apply(At, transpose=True).cpu().numpy(), pmo.shear_levels_transpose(A, ref), 1e-14)
+
+
+def test_adaptive_mesh_matches_oracle():
+    """The GPU adaptive mesh (probe features and the per-interval spacing on the device, the walk on the host) against
+    the oracle's restatement of adaptive_population_mesh."""
+    from ffnoml_gb300.population_mesh import PopulationMeshConfig, adaptive_population_mesh
+    f, z = mesh_test_atmosphere(nx=6, ny=5)
+    a, zc = atm_cols(f), cols(z)
+    cfg = PopulationMeshConfig(adaptive=True, extend=False, lnT_step=0.02)
+    ref = pmo.adaptive_mesh(a, zc, cfg.top_m, cfg.bottom_m, cfg.min_spacing_m, cfg.max_spacing_m, cfg.growth,
+                            cfg.lnT_step, cfg.log_ne_step, cfg.log_rho_step, cfg.velocity_step_m_s, extend=False,
+                            fill=_hold_bottom(a))
+
+    class Hold:
+        def fill(self, fh, kind, atm, zz, mesh):
+            _hold_bottom(atm)(fh, kind)
+
+    got = adaptive_population_mesh(cfg, a, zc, extension=Hold(), chunk_bytes=1 << 16)    # several column chunks
+    assert got.shape == ref.shape
+    _close(got, ref, 1e-12)
+
+
+def test_inclined_view_chain():
+    """MeshPopulationModel on an inclined view: the ray mesh features sheared to Cartesian columns for the inner
+    model and its populations sheared back (PopulationMesh.jl:296-334), against the same chain composed from the
+    oracle; its VJP and JVP against central differences."""
+    from ffnoml_gb300.population_mesh import MeshPopulationModel, PopulationMeshConfig, ViewGeometry, uncolumns
+    f, z = mesh_test_atmosphere(nx=6, ny=5)
+    mesh = _mesh_inside()
+    view = ViewGeometry(mu=0.5, azimuth_deg=30.0)
+    model = MeshPopulationModel(_Toy(mesh), PopulationMeshConfig(heights_m=tuple(mesh)), view=view)
+    nz, nx, ny = z.shape
+    dx, dy = 48e3, 40e3
+    out = model.predict(f, z, dx, dy)
+    # the oracle chain: ray features on the mesh -> Cartesian (ln T and the others sheared, s = -1) -> toy inner
+    # model -> ray populations (ln n sheared, s = +1) -> back-map
+    fm, _ = pmo.features(atm_cols(f), cols(z), mesh)                       # [col][m][6]
+    grid = lambda c: uncolumns(c[None], nx, ny)[0]                          # [col][m] -> (m, nx, ny)
+    t = pmo.slant(0.5, 30.0)
+    sm, sp = pmo.shear_plan(mesh, dx, dy, t, -1), pmo.shear_plan(mesh, dx, dy, t, 1)
+    fc = [np.exp(pmo.shear_levels(np.log(grid(fm[:, :, 0])), sm))] + \
+         [pmo.shear_levels(grid(fm[:, :, c]), sm) for c in range(1, 6)]
+    fc_cols = np.stack([cols(v) for v in fc], axis=-1)                      # [col][m][6]
+    pc = inner_pm(fc_cols, mesh)                                            # [L][col][m]
+    pr = np.stack([cols(np.exp(pmo.shear_levels(np.log(grid(pc[l])), sp))) for l in range(pc.shape[0])])
+    ref = pmo.backmap(pr, mesh, cols(z))
+    _close(out, np.moveaxis(uncolumns(ref, nx, ny), 0, -1), 1e-10)
+    bar = np.random.default_rng(8).normal(size=out.shape)
+    fbar, zbar = model.vjp(f, z, dx, dy, bar)
+    tang = np.random.default_rng(9).normal(size=f.shape) * np.r_[1.0, 1e2, 1e2, 1e2, 0.01, 0.01][:, None, None, None]
+    h = 1e-5
+    obj = lambda g: np.sum(bar * model.predict(g, z, dx, dy))
+    fd = (obj(f + h * tang) - obj(f - h * tang)) / (2 * h)
+    assert abs(np.sum(fbar * tang) - fd) < 1e-6 * abs(fd)
+    pd = model.jvp(f, z, dx, dy, tang)
     assert abs(np.sum(bar * pd) - fd) < 1e-6 * abs(fd)
