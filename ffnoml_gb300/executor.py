@@ -13,9 +13,11 @@ Per cube (batch element), a block is (FFNOBlock3dBalanced.forward, models/ffno_m
   x2 = x1 + r_pw GN(pw_pre);      mlp_pre = mlp(x2)                  -> statistics
   out = x2 + r_mlp GN(mlp_pre)
 
-The input VJP keeps only the block inputs from the forward pass and recomputes each block's intermediates before
-back-propagating through it (the reference's per-block activation checkpointing, models/ffno_model.py:751-780).
-Parameter gradients are not computed: the service's VJP discards them (ffno_fsdp_runtime.py:319-344).
+For the input VJP the forward keeps every block's intermediates when they fit in half the free device memory
+(cache_states, the default) and the backward consumes them block by block; otherwise (or with cache_states off, as
+the service runs it) it keeps only the block inputs and recomputes each block's intermediates before back-propagating
+through it (the reference's per-block activation checkpointing, models/ffno_model.py:751-780). Both give the same
+bits. Parameter gradients are not computed: the service's VJP discards them (ffno_fsdp_runtime.py:319-344).
 """
 import copy
 import hashlib
