@@ -33,7 +33,7 @@ int grid_of(long V, int rows, int per_sm) {
 template <typename K>
 bool smem_attr(K kernel, size_t bytes) {
   if (bytes <= 48 * 1024) return true;
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess;
+  return ffno::smem_cap_ok(kernel, bytes);
 }
 
 bool width_ok(int C) { return C == 16 || C == 32 || C == 64 || C == 96; }

@@ -411,6 +411,21 @@ __device__ __forceinline__ void write_partial(double* partials, int groups, cons
   }
 }
 
+// The dynamic shared memory a kernel may take is a process-wide attribute of that kernel. The service launches the
+// same kernels from several host threads with different sizes (one request per thread), and a thread that lowered the
+// attribute to its own size between another thread's setting and that thread's launch made the launch fail. So the
+// attribute is set once per kernel and device, under a lock, to the most the kernel can have there (the opt-in maximum
+// per block less the kernel's static shared memory), and each launch only checks its own size against that cap.
+bool smem_cap_lookup(const void* kernel, size_t* cap);
+
+template <typename K>
+inline bool smem_cap_ok(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return true;
+  size_t cap = 0;
+  if (!smem_cap_lookup(reinterpret_cast<const void*>(kernel), &cap)) return false;
+  return bytes <= cap;
+}
+
 }  // namespace ffno
 
 #define FFNO_CHECK_LAUNCH()                                   \

@@ -33,7 +33,7 @@ int grid_for(long V, int per_sm) {
 template <typename K>
 bool set_smem(K kernel, size_t bytes) {
   if (bytes <= 48 * 1024) return true;
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess;
+  return ffno::smem_cap_ok(kernel, bytes);
 }
 
 // ------------------------------------------------------------------------------------------------ depth weights

@@ -1297,7 +1297,7 @@ int grid_tc(long V) {
 template <typename K>
 bool launch_prep(K kernel, size_t bytes) {
   if (bytes > 227 * 1024 - 1024) return false;   // leave room for the kernels' static shared memory
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess;
+  return ffno::smem_cap_ok(kernel, bytes);
 }
 
 bool tc_width(int C) { return C == 16 || C == 32 || C == 64; }

@@ -1720,7 +1720,7 @@ int launch_mlp2_bwd(const float* a, const float* pb, const float* base, long V, 
   CUtensorMap ma, mp;
   if (!row_map(&ma, a, V, C) || !row_map(&mp, pb, V, C)) return FFNO_EINVAL;
   const size_t smem = 1024 + 3 * (size_t)mat_bytes(2 * C, C) + 2 * (size_t)(2 * (C / 32) * BOX_BYTES);
-  if (cudaFuncSetAttribute(k_mlp2_bwd_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!ffno::smem_cap_ok(k_mlp2_bwd_ws<C>, smem))
     return FFNO_ELAUNCH;
   const long nt = (V + TM - 1) / TM;
   const int grid = (int)(nt < sms() ? nt : sms());
@@ -1736,9 +1736,7 @@ int launch_mlp2_fwd(const float* in, const float* prev, const float* pc, float r
   if (!row_map(&mi, in, V, C)) return FFNO_EINVAL;
   if (MODE != 0 ? !row_map(&mp, prev, V, C) : !row_map(&mp, in, V, C)) return FFNO_EINVAL;
   const size_t smem = 1024 + 2 * (size_t)mat_bytes(2 * C, C) + 2 * (size_t)((MODE == 0 ? 1 : 2) * (C / 32) * BOX_BYTES);
-  if (cudaFuncSetAttribute(k_mlp2_fwd_ws<C, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess)
-    return FFNO_ELAUNCH;
+  if (!ffno::smem_cap_ok(k_mlp2_fwd_ws<C, MODE>, smem)) return FFNO_ELAUNCH;
   k_mlp2_fwd_ws<C, MODE><<<nparts, NTHREADS, smem, s>>>(mi, mp, pc, res, xout, V, static_cast<const uint8_t*>(wpack),
                                                          dw, pre, partials, err);
   return cudaGetLastError() == cudaSuccess ? FFNO_OK : FFNO_ELAUNCH;
@@ -1750,7 +1748,7 @@ int launch_gate_fwd(const float* x, long V, const void* wpack, const float* zp, 
   CUtensorMap mx;
   if (!row_map(&mx, x, V, C)) return FFNO_EINVAL;
   const size_t smem = 1024 + 2 * (size_t)mat_bytes(C, C) + 2 * (size_t)((C / 32) * BOX_BYTES);
-  if (cudaFuncSetAttribute(k_gate_fwd_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!ffno::smem_cap_ok(k_gate_fwd_ws<C>, smem))
     return FFNO_ELAUNCH;
   const long nt = (V + TM - 1) / TM;
   const int grid = (int)(nt < sms() ? nt : sms());
@@ -1764,7 +1762,7 @@ int launch_gate_bwd(const float* x, const float* gbar, const float* base, long V
   CUtensorMap mx, mg;
   if (!row_map(&mx, x, V, C) || !row_map(&mg, gbar, V, C)) return FFNO_EINVAL;
   const size_t smem = 1024 + 4 * (size_t)mat_bytes(C, C) + 2 * (size_t)(2 * (C / 32) * BOX_BYTES);
-  if (cudaFuncSetAttribute(k_gate_bwd_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!ffno::smem_cap_ok(k_gate_bwd_ws<C>, smem))
     return FFNO_ELAUNCH;
   const long nt = (V + TM - 1) / TM;
   const int grid = (int)(nt < sms() ? nt : sms());
@@ -1779,7 +1777,7 @@ int launch_fuse2(const float* sp, const float* sc, const float* vp, const float*
   CUtensorMap ms, mv, mg;
   if (!row_map(&ms, sp, V, C) || !row_map(&mv, vp, V, C) || !row_map(&mg, gates, V, 2 * C)) return FFNO_EINVAL;
   const size_t smem = 1024 + (size_t)mat_bytes(2 * C, 2 * C) + mat_bytes(C, 2 * C) + 3 * (size_t)(2 * BOX_BYTES);
-  if (cudaFuncSetAttribute(k_fuse2_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!ffno::smem_cap_ok(k_fuse2_ws<C>, smem))
     return FFNO_ELAUNCH;
   k_fuse2_ws<C><<<nparts, NTHREADS, smem, s>>>(ms, mv, mg, sc, vc, V, static_cast<const uint8_t*>(wpack), dw, pre,
                                                 partials, err);
@@ -1792,7 +1790,7 @@ int launch_fuse1(const float* x, const float* sp, const float* sc, const float* 
   CUtensorMap mx, ms, mv;
   if (!row_map(&mx, x, V, C) || !row_map(&ms, sp, V, C) || !row_map(&mv, vp, V, C)) return FFNO_EINVAL;
   const size_t smem = 1024 + (size_t)mat_bytes(C, 3 * C) + mat_bytes(2 * C, C) + 4 * (size_t)BOX_BYTES;
-  if (cudaFuncSetAttribute(k_fuse1_ws<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!ffno::smem_cap_ok(k_fuse1_ws<C>, smem))
     return FFNO_ELAUNCH;
   const long nt = (V + TM - 1) / TM;
   const int grid = (int)(nt < sms() ? nt : sms());

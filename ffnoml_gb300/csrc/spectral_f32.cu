@@ -238,7 +238,7 @@ int ffno_spectral_mix(const float* in, float* out, long F, long nb, long sf, lon
   case CC: {                                                                                               \
     const size_t smem = (BM * (2 * CC + 1) + 2 * CC * 16 + BM * 32) * sizeof(float);                        \
     if (smem > 48 * 1024 &&                                                                                \
-        cudaFuncSetAttribute(k_mix<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) \
+        !ffno::smem_cap_ok(k_mix<CC>, smem)) \
       return FFNO_ELAUNCH;                                                                                 \
     k_mix<CC><<<(unsigned)blocks, NT, smem, s>>>(in, out, F, nb, sf, sb, s_im, wbig, g, U, Vm, rank);       \
     break;                                                                                                 \

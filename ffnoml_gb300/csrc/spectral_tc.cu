@@ -838,7 +838,7 @@ int ffno_xform_tc(const void* tpack, const float* in, float* out, const ffno_xfo
   const long ntn = (d.N + 127) / 128;
   const long items = nbi > 1 ? (d.nb + nbi - 1) / nbi : d.nb * ntn;
   const size_t smem = 1024 + 4 * (size_t)RSB + 2 * 2 * (size_t)MT * 128 * RKC * 2;
-  if (cudaFuncSetAttribute(k_xform_st, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!ffno::smem_cap_ok(k_xform_st, smem))
     return FFNO_ELAUNCH;
   const long grid = items < sms() ? items : sms();
   k_xform_st<<<(unsigned)grid, RT, smem, (cudaStream_t)stream>>>(static_cast<const uint8_t*>(tpack), MT, Kp, in, out,
@@ -864,7 +864,7 @@ int ffno_xform_tcr(const void* tpack, int Mp, int Kp, const float* in, float* ou
   const long ntn = (d.N + 127) / 128;
   const long items = nbi > 1 ? (d.nb + nbi - 1) / nbi : d.nb * ntn;
   const size_t smem = 1024 + (((size_t)Mp * Kp * 4 + 1023) & ~(size_t)1023) + 4 * 2 * (size_t)RSB;
-  if (cudaFuncSetAttribute(k_xform_rt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!ffno::smem_cap_ok(k_xform_rt, smem))
     return FFNO_ELAUNCH;
   const long pairs = (items + 1) / 2;
   const long grid = pairs < sms() ? pairs : sms();
@@ -927,7 +927,7 @@ int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, 
   switch (C) {
 #define L(CC)                                                                                                     \
   case CC: {                                                                                                      \
-    if (cudaFuncSetAttribute(k_mix_tc<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) \
+    if (!ffno::smem_cap_ok(k_mix_tc<CC>, smem)) \
       return FFNO_ELAUNCH;                                                                                        \
     k_mix_tc<CC><<<(unsigned)grid, XT, smem, s>>>(map, out, F, nb, sf, sb, s_im, static_cast<const uint8_t*>(wpack), \
                                                  g, U, Vm, rank, geo, err);                                       \
@@ -955,7 +955,7 @@ int ffno_outer_tc(const float* A, long lda, int Ma, const float* B, long ldb, in
   if (1024 + 2 * (size_t)outer_stage_bytes(TI, NB) > limit) NS = 1;
   const size_t smem = 1024 + NS * (size_t)outer_stage_bytes(TI, NB);
   if (smem > limit) return FFNO_EINVAL;
-  if (cudaFuncSetAttribute(k_outer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!ffno::smem_cap_ok(k_outer_tc, smem))
     return FFNO_ELAUNCH;
   const long nchunks = (N + OKC - 1) / OKC;
   const long cps = (nchunks + nsplit - 1) / nsplit;

@@ -66,7 +66,7 @@ extern "C" int ffno_tc_selftest(const float* A, const float* B, int K, int N, in
                                 ffno_stream_t stream) {
   if (!A || !B || !D || !status || K < 16 || K % 16 || K > 256 || N < 16 || N % 16 || N > 256) return FFNO_EINVAL;
   const size_t smem = (size_t)(128 + N) * K * 2 + 1024;
-  if (cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!ffno::smem_cap_ok(k_tc_selftest, smem))
     return FFNO_ELAUNCH;
   k_tc_selftest<<<1, 128, smem, (cudaStream_t)stream>>>(A, B, K, N, b_mn, D, status);
   FFNO_CHECK_LAUNCH();
