@@ -70,12 +70,10 @@ constexpr double kEE = 1.602189e-12, kBK = 1.380662e-16;
 constexpr double kLN10 = 2.302585092994045684;
 constexpr double kINV_LN10 = 0.434294481903251827651;
 
-__device__ __forceinline__ double ln_ccon() {
-  // log(0.5 * (HH / sqrt(2 pi EM) / sqrt(BK))^3), MULTI3D's Saha constant (models/ffno_model.py:112)
-  const double hh = 6.626176e-27, em = 9.109534e-28, pi = 3.14159265359;
-  const double a = hh / sqrt(2.0 * pi * em) / sqrt(kBK);
-  return log(0.5 * a * a * a);
-}
+// log(0.5 * (HH / sqrt(2 pi EM) / sqrt(BK))^3) with HH = 6.626176e-27, EM = 9.109534e-28, BK = 1.380662e-16 and
+// pi = 3.14159265359: MULTI3D's Saha constant (models/ffno_model.py:112), evaluated once in 40-digit arithmetic (a
+// CPU test recomputes it from the formula); as a literal it costs no FP64 log and square roots per voxel
+constexpr double kLN_CCON = -36.113482555935598575;
 
 // ------------------------------------------------------------------------------------------ level-fraction head
 // One voxel of FFNO3D.head_output after proj2 (models/ffno_model.py:729-748): per species, logits = head channels + the
@@ -84,7 +82,7 @@ __device__ __forceinline__ double ln_ccon() {
 // level logits, then its total channel). The LTE math and the log-softmax run in T: double is the reference's FP64
 // (torch.log_softmax on float64 logits, :741); float is the split-BF16 path's FP32, where the sum of the max-shifted
 // exponentials (each in (0, 1]) is compensated (below), so that the level shares of a voxel add up to 1 within a few
-// FP32 roundings. The total term and the final sum of log10 n are FP64 in both.
+// FP32 roundings. The final sum of log10 n is FP64 in both.
 struct HeadInputs {
   float lt, lne, lrho;   // log10 T, log10 ne (SI), log10 rho of the voxel (denormalised)
 };
@@ -105,7 +103,7 @@ struct Lte {
     lne = (T)in.lne * (T)hp.std_x[ec] + (T)hp.mean_x[ec];
     const T tk = mexp10(lt);
     const T ne = mexp10(lne - (T)6);  // cm^-3
-    conl = (T)ln_ccon() + (lne - (T)6) * LN10 - (T)1.5 * lt * LN10;
+    conl = (T)kLN_CCON + (lne - (T)6) * LN10 - (T)1.5 * lt * LN10;
     dxi = (T)(4.98e-4 * 5040.0) / tk * msqrt(ne * (T)kBK * tk);
     ek_t = (T)(kEE / kBK) / tk;
   }
@@ -142,9 +140,9 @@ template <typename T>
 __device__ __forceinline__ void head_voxel_fwd(const ffno_head_params& hp, const float* o, const HeadInputs& in,
                                                float* __restrict__ out, long V, long v) {
   const Lte<T> e(hp, in);
-  // the total term and the assembly of log10 n (log10 rho - log10 m + s ~ 20, minus mean_Y) stay in FP64 for both
-  // T: in FP32 their rounding (~1e-6 dex at that magnitude) would shift every level share of the voxel alike; they
-  // are a handful of FP64 operations a voxel
+  // the assembly of log10 n (log10 rho - log10 m + total ~ 20, minus mean_Y) stays in FP64 for both T: in FP32 its
+  // rounding (~1e-6 dex at that magnitude) would move every level of the voxel; the bounded total b tanh(u / b) is
+  // evaluated in T (FP32: within a few ulp of b, the same shift for all levels of the species, so no level share moves)
   const double lrho = (double)in.lrho * (double)hp.std_x[hp.rho_channel] + (double)hp.mean_x[hp.rho_channel];
   int hc = 0, lvl = 0;
   for (int s = 0; s < hp.nspecies; ++s) {
@@ -156,8 +154,8 @@ __device__ __forceinline__ void head_voxel_fwd(const ffno_head_params& hp, const
       mx = fmax(mx, logit[i]);
     }
     const T lse = mlog(shifted_exp_sum<T>(logit, L, mx));
-    const double tb = (double)hp.total_bound;
-    const double base = lrho - (double)hp.log10_particle_mass[s] + tb * tanh((double)o[hc + L] / tb);
+    const T tb = (T)hp.total_bound;
+    const double base = lrho - (double)hp.log10_particle_mass[s] + (double)(tb * mtanh((T)o[hc + L] / tb));
     for (int i = 0; i < L; ++i) {
       const int g = lvl + i;
       const double l10 = base + ((double)(logit[i] - mx) - (double)lse) * kINV_LN10;

@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(NT) k_head_jvp(const float* __restrict__ x, co
   float* os = hds + BM * LH;
   float* ods = os + BM * LO;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const double lnc = ln_ccon();
+  const double lnc = kLN_CCON;
   const long nt = (V + BM - 1) / BM;
   for (long t = blockIdx.x; t < nt; t += gridDim.x) {
     const long v0 = t * BM;

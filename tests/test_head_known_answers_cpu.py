@@ -171,3 +171,15 @@ def test_level_2_follows_boltzmann_in_temperature():
     expected = (1.602189e-12 / 1.380662e-16) * ATOMS["H"]["multi3d_lte"]["ev"][1] / t * float(STD_X[0])
     assert g[:, 1:].abs().max().item() < 1e-6 * np.abs(expected).max()
     assert np.abs(g[:, 0].numpy() - expected).max() / np.abs(expected).max() < 1e-4
+
+
+def test_kernel_saha_constant_matches_its_formula():
+    """The kernels carry MULTI3D's Saha constant as a literal; it is the formula's value (the oracle evaluates it
+    with math.log and math.sqrt)."""
+    import os
+    import re
+    from oracle.ffno_oracle import LN_CCON
+    src = open(os.path.join(os.path.dirname(__file__), "..", "ffnoml_gb300", "csrc", "common.cuh")).read()
+    m = re.search(r"kLN_CCON = (-?[0-9.eE+-]+);", src)
+    assert m is not None
+    assert abs(float(m.group(1)) - LN_CCON) <= 4e-16 * abs(LN_CCON)
