@@ -79,6 +79,42 @@ def synthetic_si(shape, seed=1):
     return f, z
 
 
+def per_column_heights(z):
+    """Heights [1, D, H, W] (Mm) of the same span with every column's grid its own: each column stretched by up to
+    +-2 % and shifted, so that no two columns share their tables."""
+    import torch
+    _, D, H, W = z.shape
+    hh = torch.arange(H, dtype=torch.float32, device=z.device)[:, None]
+    ww = torch.arange(W, dtype=torch.float32, device=z.device)[None, :]
+    stretch = 1.0 + 0.02 * torch.sin(0.37 * hh + 0.23 * ww)
+    shift = 0.05 * torch.cos(0.11 * hh - 0.19 * ww)
+    return (z * stretch[None, None] + shift[None, None]).contiguous()
+
+
+def per_column_run(model, x, z, cot, dev, world, timed):
+    """fwd+VJP with per-column heights, and the time to build the per-column tables (device kernels, host prep)."""
+    import torch
+    ex = model.executor()
+    zc = per_column_heights(z)
+    geo = ex.geometry(zc)
+    pk = ex.packed(dev)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    hgt = ex.height_percol(pk, geo, 0, dev)
+    torch.cuda.synchronize(dev)
+    build_s = time.perf_counter() - t0
+    ms, _ = timed(lambda: ex.backward(ex.forward(x, zc, DXY, DXY, keep=True)[1], cot), 2, 1)
+    V = x.shape[2] * x.shape[3] * x.shape[4]
+    out = {"value": job_rate(V, world, ms / 1e3), "unit": "voxels/s", "ms_per_step": ms, "pass": "fwd+vjp",
+           "columns": int(x.shape[3] * x.shape[4]), "live_modes": int(hgt["live"]),
+           "tables_build_ms": 1e3 * build_s, "tables": "device (ffno_percol_tables), gradient ffno_percol_tables_vjp"}
+    del hgt
+    for key in [key for key in ex._height if key[0] == "percol"]:
+        del ex._height[key]
+    torch.cuda.empty_cache()
+    return out
+
+
 def normalised(f, z):
     """Model-unit, normalised inputs [1, 6, D, H, W] and z [1, D, H, W] in Mm (ffno_fsdp_runtime._model_inputs)."""
     m = f.astype(np.float64).copy()
@@ -519,6 +555,13 @@ def run_gb300(args):
         del mp, exp, hp
         torch.cuda.empty_cache()
 
+    # per-column height grids (every column its own heights: the height operator's non-shared path) on the same
+    # cube: the per-column tables built on the device once (timed alone), then fwd+VJP steps with them, the tables'
+    # gradient for every column included
+    per_column = None
+    if not args.no_per_column and not args.fwd_only:
+        per_column = per_column_run(model, x, z, cot, dev, world, timed)
+
     # config 4: the full-volume inversion step [1,6,496,252,252] on this GPU (block states recomputed), with the BF16
     # forward against the FP32 forward on the whole cube
     config4 = None
@@ -563,7 +606,7 @@ def run_gb300(args):
             "clocks": clocks, "memory": memory, "gpu_launches": launches * args.steps, "e2e": e2e,
             "cpu_baseline": cpu,
             "serving": serving, "streaming": streaming, "population_mesh": mesh_maps,
-            "variant_p": variant_p, "config4": config4,
+            "variant_p": variant_p, "per_column": per_column, "config4": config4,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -708,6 +751,7 @@ def main():
     ap.add_argument("--no-streaming", action="store_true", help="skip the host-RAM streaming forward")
     ap.add_argument("--no-config4", action="store_true", help="skip the full-volume [1,6,496,252,252] step")
     ap.add_argument("--no-variant-p", action="store_true", help="skip the production band limit (M = 1001) step")
+    ap.add_argument("--no-per-column", action="store_true", help="skip the per-column height grid step")
     ap.add_argument("--serve-requests", type=int, default=256)
     args = ap.parse_args()
     args.shape = tuple(int(v) for v in args.shape.split(","))

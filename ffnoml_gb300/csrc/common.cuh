@@ -82,7 +82,7 @@ constexpr double kLN_CCON = -36.113482555935598575;
 // level logits, then its total channel). The LTE math and the log-softmax run in T: double is the reference's FP64
 // (torch.log_softmax on float64 logits, :741); float is the split-BF16 path's FP32, where the sum of the max-shifted
 // exponentials (each in (0, 1]) is compensated (below), so that the level shares of a voxel add up to 1 within a few
-// FP32 roundings. The final sum of log10 n is FP64 in both.
+// FP32 roundings. The total term and the final sum of log10 n are FP64 in both.
 struct HeadInputs {
   float lt, lne, lrho;   // log10 T, log10 ne (SI), log10 rho of the voxel (denormalised)
 };
@@ -140,9 +140,9 @@ template <typename T>
 __device__ __forceinline__ void head_voxel_fwd(const ffno_head_params& hp, const float* o, const HeadInputs& in,
                                                float* __restrict__ out, long V, long v) {
   const Lte<T> e(hp, in);
-  // the assembly of log10 n (log10 rho - log10 m + total ~ 20, minus mean_Y) stays in FP64 for both T: in FP32 its
-  // rounding (~1e-6 dex at that magnitude) would move every level of the voxel; the bounded total b tanh(u / b) is
-  // evaluated in T (FP32: within a few ulp of b, the same shift for all levels of the species, so no level share moves)
+  // the total term and the assembly of log10 n (log10 rho - log10 m + s ~ 20, minus mean_Y) stay in FP64 for both
+  // T: in FP32 their rounding (~1e-6 dex at that magnitude, and a few ulp of b for tanh) would move every level of
+  // the voxel against its total, past the 1e-6 bar on the level shares' sum; they are a handful of FP64 operations
   const double lrho = (double)in.lrho * (double)hp.std_x[hp.rho_channel] + (double)hp.mean_x[hp.rho_channel];
   int hc = 0, lvl = 0;
   for (int s = 0; s < hp.nspecies; ++s) {
@@ -154,8 +154,8 @@ __device__ __forceinline__ void head_voxel_fwd(const ffno_head_params& hp, const
       mx = fmax(mx, logit[i]);
     }
     const T lse = mlog(shifted_exp_sum<T>(logit, L, mx));
-    const T tb = (T)hp.total_bound;
-    const double base = lrho - (double)hp.log10_particle_mass[s] + (double)(tb * mtanh((T)o[hc + L] / tb));
+    const double tb = (double)hp.total_bound;
+    const double base = lrho - (double)hp.log10_particle_mass[s] + tb * tanh((double)o[hc + L] / tb);
     for (int i = 0; i < L; ++i) {
       const int g = lvl + i;
       const double l10 = base + ((double)(logit[i] - mx) - (double)lse) * kINV_LN10;

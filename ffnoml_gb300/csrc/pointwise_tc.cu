@@ -87,6 +87,9 @@ __device__ __forceinline__ void prefetch_rows(const float* base, long n0, long V
 
 __device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
+__device__ __forceinline__ void ld8(const float* p, float (&o)[8]) { tc::ld8(p, o); }
+__device__ __forceinline__ void st8(float* p, const float* v) { tc::st8(p, v); }
+
 // GroupNorm coefficients (mean, gamma * rstd, beta) of 4 consecutive channels, and their application (+ GELU)
 struct Gn4 {
   float4 m, s, b;
@@ -1046,16 +1049,22 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
         for (int i = 0; i < 16; ++i) q[i] = od[i] = 0.f;
         if (v < V) {
 #pragma unroll
-          for (int i = 0; i < 16; i += 4) {
-            const float4 f4 = ld4(fb + v * C + cc + i), g4 = ld4(gates + v * 2 * C + kh * C + cc + i);
-            const float4 s4 = gn_apply<true>(ld4(pre + v * C + cc + i), gn_coefs(cf, C, cc + i));
-            const float ff[4] = {f4.x, f4.y, f4.z, f4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w},
-                        ss[4] = {s4.x, s4.y, s4.z, s4.w};
+          for (int i = 0; i < 16; i += 8) {
+            float ff[8], gg[8], pp[8];
+            ld8(fb + v * C + cc + i, ff);
+            ld8(gates + v * 2 * C + kh * C + cc + i, gg);
+            ld8(pre + v * C + cc + i, pp);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const float b = bb[i + u] + 0.5f * ff[u];
-              od[i + u] = b * gg[u];
-              q[i + u] = b * ss[u] * gg[u] * (1.f - gg[u]);
+            for (int h = 0; h < 8; h += 4) {
+              const float4 s4 = gn_apply<true>(make_float4(pp[h], pp[h + 1], pp[h + 2], pp[h + 3]),
+                                               gn_coefs(cf, C, cc + i + h));
+              const float ss[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                const float b = bb[i + h + u] + 0.5f * ff[h + u];
+                od[i + h + u] = b * gg[h + u];
+                q[i + h + u] = b * ss[u] * gg[h + u] * (1.f - gg[h + u]);
+              }
             }
           }
         }
@@ -1071,16 +1080,17 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
     for (int j = 0; j < C / 16; ++j) {
       if (!owns(j, P.half)) continue;
       const int c0 = 16 * j;
-      float hb[16];
+      float hb[16], h8[16];
       rld(P, 2 * C, j, hb);
+      if (v < V) {
+        ld8(hg + v * C + c0, *reinterpret_cast<float(*)[8]>(h8));
+        ld8(hg + v * C + c0 + 8, *reinterpret_cast<float(*)[8]>(h8 + 8));
+      } else {
 #pragma unroll
-      for (int i = 0; i < 16; i += 4) {
-        const float4 h4 = v < V ? ld4(hg + v * C + c0 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-        hb[i] *= gelu_grad_tc(h4.x);
-        hb[i + 1] *= gelu_grad_tc(h4.y);
-        hb[i + 2] *= gelu_grad_tc(h4.z);
-        hb[i + 3] *= gelu_grad_tc(h4.w);
+        for (int i = 0; i < 16; ++i) h8[i] = 0.f;
       }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) hb[i] *= gelu_grad_tc(h8[i]);
       put16(T, row, c0, C, hb);
     }
     // GEMM3: the branch rows of Wg1 accumulate onto the direct gradients (columns 0 .. 2C), the x rows go to the
@@ -1095,23 +1105,24 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
         rld(P, 0, j, r);
         float* g = j < C / 16 ? sbar : vbar;
         const int cc = 16 * (j % (C / 16));
-        if (v < V)
-#pragma unroll
-          for (int i = 0; i < 16; i += 4)
-            *reinterpret_cast<float4*>(g + v * C + cc + i) = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
+        if (v < V) {
+          st8(g + v * C + cc, r);
+          st8(g + v * C + cc + 8, r + 8);
+        }
       } else {                // x_bar = base + A_bar[:C]
         const int c0 = 16 * (j - 2 * C / 16);
         rld(P, 2 * C, j - 2 * C / 16, r);
-        if (v < V)
+        if (v < V) {
+          if (base) {
+            float b8[16];
+            ld8(base + v * C + c0, *reinterpret_cast<float(*)[8]>(b8));
+            ld8(base + v * C + c0 + 8, *reinterpret_cast<float(*)[8]>(b8 + 8));
 #pragma unroll
-          for (int i = 0; i < 16; i += 4) {
-            float4 o = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
-            if (base) {
-              const float4 b4 = ld4(base + v * C + c0 + i);
-              o = make_float4(o.x + b4.x, o.y + b4.y, o.z + b4.z, o.w + b4.w);
-            }
-            *reinterpret_cast<float4*>(xbar + v * C + c0 + i) = o;
+            for (int i = 0; i < 16; ++i) r[i] += b8[i];
           }
+          st8(xbar + v * C + c0, r);
+          st8(xbar + v * C + c0 + 8, r + 8);
+        }
       }
     }
   }
@@ -1302,6 +1313,7 @@ bool launch_prep(K kernel, size_t bytes) {
 
 bool tc_width(int C) { return C == 16 || C == 32 || C == 64; }
 bool aligned16(const void* p) { return p && (reinterpret_cast<uintptr_t>(p) % 16) == 0; }
+bool aligned32(const void* p) { return p && (reinterpret_cast<uintptr_t>(p) % 32) == 0; }
 
 }  // namespace
 
@@ -1474,6 +1486,11 @@ int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const flo
       !x_bar || !spec_bar || !vert_bar)
     return FFNO_EINVAL;
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
+  // the epilogues move 32 bytes of a row per request
+  if (!aligned32(spec_pre) || !aligned32(vert_pre) || !aligned32(gates) || !aligned32(hg) ||
+      !aligned32(fused_pre_bar) || (base && !aligned32(base)) || !aligned32(x_bar) || !aligned32(spec_bar) ||
+      !aligned32(vert_bar))
+    return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   TC_DISPATCH(C, {
     const size_t smem =

@@ -253,10 +253,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const uint32_t n = (uint32_t)i >> 1;
       const long v = tile_of(i) * TM + r;
       const bool live = v < V;
-      float4 bv[C / 4];
+      float bv[C];
 #pragma unroll
-      for (int c = 0; c < C / 4; ++c)
-        bv[c] = (base && live) ? __ldg(reinterpret_cast<const float4*>(base + v * C) + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int c = 0; c < C; c += 8) {
+        if (base && live) {
+          tc::ld8(base + v * C + c, bv + c);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 8; ++e) bv[c + e] = 0.f;
+        }
+      }
       if (!warp_wait(&bars.d3_full[s], n & 1u, err, 10)) break;
       tc::tc_after_sync();
 #pragma unroll
@@ -269,13 +275,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           tc::mbar_arrive(&bars.a_empty[s]);
         }
         if (live) {
-          float4* o = reinterpret_cast<float4*>(abar + v * C + 16 * k);
+          float o[16];
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const float4 b4 = bv[4 * k + e];
-            o[e] = make_float4(b4.x + __uint_as_float(d[4 * e]), b4.y + __uint_as_float(d[4 * e + 1]),
-                               b4.z + __uint_as_float(d[4 * e + 2]), b4.w + __uint_as_float(d[4 * e + 3]));
-          }
+          for (int e = 0; e < 16; ++e) o[e] = bv[16 * k + e] + __uint_as_float(d[e]);
+          tc::st8(abar + v * C + 16 * k, o);
+          tc::st8(abar + v * C + 16 * k + 8, o + 8);
         }
       }
     }
@@ -439,6 +443,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int b = bh >> 1;
         const uint8_t* rin = st + b * BOX_BYTES + r * 128;
         uint32_t hi[8], lo[8];
+        float xs[16];   // the half box's 16 channels of x, stored to xout in two 32-byte requests
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) {
           const int c = 4 * (bh & 1) + cc;
@@ -454,10 +459,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               if (MODE == 1) y[e] = gelu_tc(y[e]);
             }
             x = make_float4(fmaf(res, y[0], x.x), fmaf(res, y[1], x.y), fmaf(res, y[2], x.z), fmaf(res, y[3], x.w));
-            if (v < V) *reinterpret_cast<float4*>(xout + v * C + k) = x;
+            xs[4 * cc] = x.x;
+            xs[4 * cc + 1] = x.y;
+            xs[4 * cc + 2] = x.z;
+            xs[4 * cc + 3] = x.w;
           }
           tc::split_pack(x.x, x.y, hi[2 * cc], lo[2 * cc]);
           tc::split_pack(x.z, x.w, hi[2 * cc + 1], lo[2 * cc + 1]);
+        }
+        if (MODE != 0 && v < V) {
+          float* xo = xout + v * C + 32 * b + 16 * (bh & 1);
+          tc::st8(xo, xs);
+          tc::st8(xo + 8, xs + 8);
         }
         tc::tmem_st8u(A + (uint32_t)(8 * bh), hi);
         tc::tmem_st8u(A + (uint32_t)(C / 2 + 8 * bh), lo);
@@ -514,12 +527,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         uint32_t d[16];
         tc::tmem_ld16u(D + 16u * k, d);
         tc::tmem_wait_ld();
-        if (live)
+        if (live) {
+          float o[16];
 #pragma unroll
-          for (int e = 0; e < 4; ++e)
-            *reinterpret_cast<float4*>(pre + v * C + 16 * k + 4 * e) =
-                make_float4(__uint_as_float(d[4 * e]), __uint_as_float(d[4 * e + 1]), __uint_as_float(d[4 * e + 2]),
-                            __uint_as_float(d[4 * e + 3]));
+          for (int e = 0; e < 16; ++e) o[e] = __uint_as_float(d[e]);
+          tc::st8(pre + v * C + 16 * k, o);
+          tc::st8(pre + v * C + 16 * k + 8, o + 8);
+        }
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
           const int g = (16 * k + e) / CPG;
@@ -778,10 +792,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int sa = i % NA;
       const long v = tile_of(i) * TM + r;
       const bool live = v < V;
-      float4 xv[C / 4];
+      float xv[C];
 #pragma unroll
-      for (int c = 0; c < C / 4; ++c)
-        xv[c] = live ? __ldg(reinterpret_cast<const float4*>(x + v * C) + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int c = 0; c < C; c += 8) {
+        if (live) {
+          tc::ld8(x + v * C + c, xv + c);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 8; ++e) xv[c + e] = 0.f;
+        }
+      }
       const float zv = (zp && live) ? __ldg(z + v) : 0.f;
       if (!warp_wait(&d2_full[sa], (uint32_t)(i / NA) & 1u, err, 10)) break;
       tc::tc_after_sync();
@@ -795,20 +815,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           tc::mbar_arrive(&a_empty[sa]);
         }
         if (live) {
-          float4* o = reinterpret_cast<float4*>(out + v * C + 16 * k);
+          float y[16];
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const float4 x4 = xv[4 * k + e];
-            float4 y = make_float4(x4.x * sigmoid_tc(__uint_as_float(d[4 * e])),
-                                   x4.y * sigmoid_tc(__uint_as_float(d[4 * e + 1])),
-                                   x4.z * sigmoid_tc(__uint_as_float(d[4 * e + 2])),
-                                   x4.w * sigmoid_tc(__uint_as_float(d[4 * e + 3])));
-            if (zp) {
-              const float4 zz = __ldg(reinterpret_cast<const float4*>(zp + 16 * k + 4 * e));
-              y = make_float4(fmaf(zz.x, zv, y.x), fmaf(zz.y, zv, y.y), fmaf(zz.z, zv, y.z), fmaf(zz.w, zv, y.w));
-            }
-            o[e] = y;
-          }
+          for (int e = 0; e < 16; ++e) y[e] = xv[16 * k + e] * sigmoid_tc(__uint_as_float(d[e]));
+          if (zp)
+#pragma unroll
+            for (int e = 0; e < 16; ++e) y[e] = fmaf(__ldg(zp + 16 * k + e), zv, y[e]);
+          tc::st8(out + v * C + 16 * k, y);
+          tc::st8(out + v * C + 16 * k + 8, y + 8);
         }
       }
     }
@@ -1013,11 +1027,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         tc::tmem_ld16u(D + 16u * j, h);
         tc::tmem_wait_ld();
         if (hg && v < V) {
-          float4* o = reinterpret_cast<float4*>(hg + v * C + 16 * j);
+          float o[16];
 #pragma unroll
-          for (int e = 0; e < 4; ++e)
-            o[e] = make_float4(__uint_as_float(h[4 * e]), __uint_as_float(h[4 * e + 1]), __uint_as_float(h[4 * e + 2]),
-                               __uint_as_float(h[4 * e + 3]));
+          for (int e = 0; e < 16; ++e) o[e] = __uint_as_float(h[e]);
+          tc::st8(hg + v * C + 16 * j, o);
+          tc::st8(hg + v * C + 16 * j + 8, o + 8);
         }
         uint32_t hi[8], lo[8];
 #pragma unroll
@@ -1049,15 +1063,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           tc::mbar_arrive(&a_empty[s]);
         }
         if (v < V) {
-          float4* o = reinterpret_cast<float4*>(gates + v * 2 * C + 16 * k);
+          float o[16];
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int c = 16 * k + 4 * e;
-            o[e] = make_float4(sigmoid_tc(__uint_as_float(d[4 * e]) + bs[c]),
-                               sigmoid_tc(__uint_as_float(d[4 * e + 1]) + bs[c + 1]),
-                               sigmoid_tc(__uint_as_float(d[4 * e + 2]) + bs[c + 2]),
-                               sigmoid_tc(__uint_as_float(d[4 * e + 3]) + bs[c + 3]));
-          }
+          for (int e = 0; e < 16; ++e) o[e] = sigmoid_tc(__uint_as_float(d[e]) + bs[16 * k + e]);
+          tc::st8(gates + v * 2 * C + 16 * k, o);
+          tc::st8(gates + v * 2 * C + 16 * k + 8, o + 8);
         }
       }
     }
@@ -1310,12 +1320,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         uint32_t d[16];
         tc::tmem_ld16u(D + 16u * k, d);
         tc::tmem_wait_ld();
-        if (live)
+        if (live) {
+          float o[16];
 #pragma unroll
-          for (int e = 0; e < 4; ++e)
-            *reinterpret_cast<float4*>(pre + v * C + 16 * k + 4 * e) =
-                make_float4(__uint_as_float(d[4 * e]), __uint_as_float(d[4 * e + 1]), __uint_as_float(d[4 * e + 2]),
-                            __uint_as_float(d[4 * e + 3]));
+          for (int e = 0; e < 16; ++e) o[e] = __uint_as_float(d[e]);
+          tc::st8(pre + v * C + 16 * k, o);
+          tc::st8(pre + v * C + 16 * k + 8, o + 8);
+        }
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
           const int g = (16 * k + e) / CPG;
@@ -1614,11 +1625,16 @@ __global__ void __launch_bounds__(448, 1)
         const int i = 2 * p + t;
         const long v = tile_of(i) * TM + r;
         const bool live = v < V;
-        float4 bv[C / 4];
+        float bv[C];
 #pragma unroll
-        for (int c = 0; c < C / 4; ++c)
-          bv[c] = (base && live) ? __ldg(reinterpret_cast<const float4*>(base + v * C) + c)
-                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int c = 0; c < C; c += 8) {
+          if (base && live) {
+            tc::ld8(base + v * C + c, bv + c);
+          } else {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) bv[c + e] = 0.f;
+          }
+        }
         if (!warp_wait(&d2_full[t], par, err, 10)) { alive = false; break; }
         // x and g_bar of tile i in its ring stage (i & 1 == t): this warp waits on the stage's TMA barrier itself
         // (its phase cannot move on before this epilogue releases the stage), which makes the copy visible to it
@@ -1640,8 +1656,7 @@ __global__ void __launch_bounds__(448, 1)
             const float4 xv = *reinterpret_cast<const float4*>(rx + off);
             const float4 gv = *reinterpret_cast<const float4*>(rx + XB + off);
             const float xx[4] = {xv.x, xv.y, xv.z, xv.w}, gg[4] = {gv.x, gv.y, gv.z, gv.w};
-            const float4 b4 = bv[4 * k + cc];
-            const float bb[4] = {b4.x, b4.y, b4.z, b4.w};
+            const float* bb = bv + 16 * k + 4 * cc;
             float qv[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
@@ -1674,11 +1689,11 @@ __global__ void __launch_bounds__(448, 1)
           tc::tmem_ld16u(RD4(t) + lq + 16u * k, d);
           tc::tmem_wait_ld();
           if (v < V) {
-            float4* o = reinterpret_cast<float4*>(xbar + v * C + 16 * k);
+            float o[16];
 #pragma unroll
-            for (int e = 0; e < 4; ++e)
-              o[e] = make_float4(__uint_as_float(d[4 * e]), __uint_as_float(d[4 * e + 1]),
-                                 __uint_as_float(d[4 * e + 2]), __uint_as_float(d[4 * e + 3]));
+            for (int e = 0; e < 16; ++e) o[e] = __uint_as_float(d[e]);
+            tc::st8(xbar + v * C + 16 * k, o);
+            tc::st8(xbar + v * C + 16 * k + 8, o + 8);
           }
         }
       }
@@ -1804,6 +1819,9 @@ int launch_fuse1(const float* x, const float* sp, const float* sc, const float* 
 namespace ffno {
 namespace ws {
 
+// the epilogues read and write a voxel's row 32 bytes per request (rows of 32 or 64 floats keep that alignment)
+static bool rows32(const void* p) { return p && reinterpret_cast<uintptr_t>(p) % 32 == 0; }
+
 bool fuse1_supported(int C) { return C == 32 || C == 64; }
 
 int fuse1(const float* x, const float* spec_pre, const float* spec_coefs, const float* vert_pre,
@@ -1812,7 +1830,7 @@ int fuse1(const float* x, const float* spec_pre, const float* spec_coefs, const 
   if (V < 1 || V > 0x7fffffffL - TM || !bias ||
       (reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(spec_pre) | reinterpret_cast<uintptr_t>(vert_pre) |
        reinterpret_cast<uintptr_t>(gates)) % 16 ||
-      (hg && reinterpret_cast<uintptr_t>(hg) % 16))
+      (hg && reinterpret_cast<uintptr_t>(hg) % 16) || !rows32(gates) || (hg && !rows32(hg)))
     return FFNO_EINVAL;
   if (C == 64)
     return launch_fuse1<64>(x, spec_pre, spec_coefs, vert_pre, vert_coefs, V, wpack, bias, gates, hg, err, stream);
@@ -1828,7 +1846,7 @@ int fuse2(const float* spec_pre, const float* spec_coefs, const float* vert_pre,
           int nparts, int* err, cudaStream_t stream) {
   if (V < 1 || V > 0x7fffffffL - TM || nparts < 1 ||
       (reinterpret_cast<uintptr_t>(spec_pre) | reinterpret_cast<uintptr_t>(vert_pre) |
-       reinterpret_cast<uintptr_t>(gates) | reinterpret_cast<uintptr_t>(pre)) % 16)
+       reinterpret_cast<uintptr_t>(gates) | reinterpret_cast<uintptr_t>(pre)) % 16 || !rows32(pre))
     return FFNO_EINVAL;
   if (C == 64)
     return launch_fuse2<64>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, V, wpack, dw, pre, partials, nparts,
@@ -1845,7 +1863,7 @@ int gate_bwd(const float* x, const float* g_bar, const float* base, long V, int 
              float* x_bar, float* z_bar, int* err, cudaStream_t stream) {
   if (V < 1 || V > 0x7fffffffL - TM ||
       (reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(g_bar) | reinterpret_cast<uintptr_t>(x_bar)) % 16 ||
-      (base && reinterpret_cast<uintptr_t>(base) % 16))
+      (base && reinterpret_cast<uintptr_t>(base) % 16) || !rows32(x_bar) || (base && !rows32(base)))
     return FFNO_EINVAL;
   if (C == 64) return launch_gate_bwd<64>(x, g_bar, base, V, wpack, zp, x_bar, z_bar, err, stream);
   if (C == 32) return launch_gate_bwd<32>(x, g_bar, base, V, wpack, zp, x_bar, z_bar, err, stream);
@@ -1857,7 +1875,7 @@ bool gate_fwd_supported(int C) { return C == 32 || C == 64; }
 int gate_fwd(const float* x, long V, int C, const void* wpack, const float* zp, const float* z, float* out, int* err,
              cudaStream_t stream) {
   if (V < 1 || V > 0x7fffffffL - TM || reinterpret_cast<uintptr_t>(x) % 16 || reinterpret_cast<uintptr_t>(out) % 16 ||
-      (zp && reinterpret_cast<uintptr_t>(zp) % 16))
+      (zp && reinterpret_cast<uintptr_t>(zp) % 16) || !rows32(x) || !rows32(out))
     return FFNO_EINVAL;
   if (C == 64) return launch_gate_fwd<64>(x, V, wpack, zp, z, out, err, stream);
   if (C == 32) return launch_gate_fwd<32>(x, V, wpack, zp, z, out, err, stream);
@@ -1870,7 +1888,7 @@ int mlp2_fwd(int mode, const float* in, const float* prev_pre, const float* prev
              int C, const void* wpack, const float* dw, float* pre, double* partials, int nparts, int* err,
              cudaStream_t stream) {
   if (V < 1 || V > 0x7fffffffL - TM || nparts < 1 || reinterpret_cast<uintptr_t>(in) % 16 ||
-      (mode && reinterpret_cast<uintptr_t>(prev_pre) % 16))
+      (mode && reinterpret_cast<uintptr_t>(prev_pre) % 16) || !rows32(pre) || (mode && !rows32(xout)))
     return FFNO_EINVAL;
 #define L(CC, MM)                                                                                                \
   if (C == CC && mode == MM)                                                                                     \
@@ -1885,7 +1903,8 @@ bool mlp2_bwd_supported(int C) { return C == 32 || C == 64; }
 
 int mlp2_bwd(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack, float* a_bar,
              int* err, cudaStream_t stream) {
-  if (V < 1 || V > 0x7fffffffL - TM || (reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(pre_bar)) % 16)
+  if (V < 1 || V > 0x7fffffffL - TM || (reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(pre_bar)) % 16 ||
+      !rows32(a_bar) || (base && !rows32(base)))
     return FFNO_EINVAL;
   if (C == 64) return launch_mlp2_bwd<64>(a, pre_bar, base, V, wpack, a_bar, err, stream);
   if (C == 32) return launch_mlp2_bwd<32>(a, pre_bar, base, V, wpack, a_bar, err, stream);

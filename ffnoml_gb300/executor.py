@@ -516,15 +516,24 @@ class Executor:
                 old = [k for k in self._height if k[0] == "percol"]
                 for k in old[:-1]:
                     del self._height[k]
-                live, tzf, tzi = tb.percolumn_tables(cols, geo.length, geo.k)
+                # the tables of every column are built on the device (ffno_percol_tables, FP64); the host decides
+                # the live modes, the tapers and their derivative, and the median spacing's index
+                live, fcol, dfcol, med = tb.percolumn_prep(cols, geo.length, geo.k)
+                ncol, D = cols.shape
+                f64 = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=device)
+                zc, kk, fd, dfd = f64(cols), f64(geo.k.numpy()[:live]), f64(fcol), f64(dfcol)
+                medd = torch.as_tensor(med, dtype=torch.int32, device=device)
+                t32 = lambda *shape: torch.empty(*shape, dtype=torch.float32, device=device)
+                tzf, tzi = t32(ncol, 2 * live, D), t32(ncol, D, 2 * live)
+                tzf_t, tzi_t = t32(ncol, D, 2 * live), t32(ncol, 2 * live, D)
+                nat.call("ffno_percol_tables", zc.data_ptr(), D, ncol, kk.data_ptr(), live, fd.data_ptr(),
+                         tzf.data_ptr(), tzi.data_ptr(), tzf_t.data_ptr(), tzi_t.data_ptr(), _stream())
                 feats = tb.height_features(geo.k[:live], self.model.z_feature_wavelength)
                 rank = self.model.freq_mix_rank
                 per_block = [FreqTables(*tb.freq_tables(pk.freq_params, f"blocks.{i}.vertical", feats, rank), device)
                              for i in range(self.model.n_layers)]
-                f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device=device)
-                self._height[key] = dict(live=live, percol=True, tzf=f(tzf), tzi=f(tzi),
-                                         tzf_t=f(tzf.transpose(0, 2, 1)), tzi_t=f(tzi.transpose(0, 2, 1)),
-                                         freq=per_block, columns=cols)
+                self._height[key] = dict(live=live, percol=True, tzf=tzf, tzi=tzi, tzf_t=tzf_t, tzi_t=tzi_t,
+                                         freq=per_block, columns=cols, z=zc, k=kk, f=fd, df=dfd, med=medd)
             return self._height[key]
 
     # -------------------------------------------------------------------------------------------- setup
@@ -881,6 +890,14 @@ class Executor:
             live = hgt["live"]
             tzf_bar = torch.zeros(2 * live, D, dtype=torch.float64, device=dev)
             tzi_bar = torch.zeros(D, 2 * live, dtype=torch.float64, device=dev)
+            host_f = torch.empty(tzf_bar.shape, dtype=torch.float64, pin_memory=True)
+            host_i = torch.empty(tzi_bar.shape, dtype=torch.float64, pin_memory=True)
+            copied = torch.cuda.Event()
+
+            def tables_out():
+                host_f.copy_(tzf_bar, non_blocking=True)
+                host_i.copy_(tzi_bar, non_blocking=True)
+                copied.record()     # on the current stream, which every kernel of this backward runs on
         for b in range(B):
             hgt_b = hgt if geo.shared else self.height_percol(pk, geo, b, dev)
             live = hgt_b["live"]
@@ -914,22 +931,27 @@ class Executor:
                 else:
                     wb = ws
                     self._block(pk, ws, i, z, D, H, W, hgt_b, pln, pfr[i], x_in=inputs[i])
-                self._block_bwd(pk, wb, gb, i, inputs[i], z, zbar[b], D, H, W, hgt_b, pln, pfr[i], tzf_bar, tzi_bar)
+                # the shared tables' gradients are complete after the last block's height-table products: copy them
+                # out there, so that their host-side finish overlaps the rest of the backward
+                done = tables_out if geo.shared and b == B - 1 and i == 0 else None
+                self._block_bwd(pk, wb, gb, i, inputs[i], z, zbar[b], D, H, W, hgt_b, pln, pfr[i], tzf_bar, tzi_bar,
+                                done)
             # lift: x0 = gelu(GN(pre0))
             self._lift(pk, ws, xin)
             self._gn_bwd(ws, gb, 1, gb.xbar, 1.0, ws.pre, pk.lift_g, pk.lift_b, "lift", gb.pbar)
             nat.call("ffno_lift_bwd", gb.pbar.data_ptr(), Cin, V, C, pk.lift_w.data_ptr(), xbar_in[b].data_ptr(), s)
             nat.call("ffno_depth_weights_bwd", z.data_ptr(), gb.wbar.data_ptr(), D, HW, zbar[b].data_ptr(), s)
             if not geo.shared:
-                # every column's own tables depend on that column's heights
-                gcols = tb.percolumn_tables_vjp(geo.columns[b], geo.length, geo.k, live, tzf_bar.cpu().numpy(),
-                                                tzi_bar.cpu().numpy())                     # [HW][D]
-                zbar[b] += torch.as_tensor(gcols.T.reshape(D, H, W), dtype=torch.float32, device=dev)
+                # every column's own tables depend on that column's heights (ffno_percol_tables_vjp, FP64)
+                nat.call("ffno_percol_tables_vjp", hgt_b["z"].data_ptr(), D, HW, hgt_b["k"].data_ptr(), live,
+                         hgt_b["f"].data_ptr(), hgt_b["df"].data_ptr(), hgt_b["med"].data_ptr(), tzf_bar.data_ptr(),
+                         tzi_bar.data_ptr(), zbar[b].data_ptr(), s)
         if geo.shared:
-            # the height tables depend on the shared column (sample 0, column (0, 0)): their gradient goes there
-            gcol = tb.height_tables_vjp(geo.column_raw, geo.length, geo.k, live, tzf_bar.cpu().numpy(),
-                                        tzi_bar.cpu().numpy())
-            zbar[0, :, 0, 0] += torch.as_tensor(gcol, dtype=torch.float32, device=dev)
+            # the height tables depend on the shared column (sample 0, column (0, 0)): their gradient goes there,
+            # finished on the host (float64 autograd through the table builder) while the device runs the lift
+            copied.synchronize()
+            gcol = tb.height_tables_vjp(geo.column_raw, geo.length, geo.k, live, host_f.numpy(), host_i.numpy())
+            zbar[0, :, 0, 0] += torch.as_tensor(gcol, dtype=torch.float32).to(dev)
         self._check(ws)
         return xbar_in, zbar
 
@@ -944,7 +966,7 @@ class Executor:
                  ws.gstats[name].data_ptr(), gb.sums.data_ptr(), ws.dw.data_ptr(), V, C, G, EPS, pbar.data_ptr(),
                  gb.wbar.data_ptr(), s)
 
-    def _block_bwd(self, pk, ws, gb, i, x, z, zbar, D, H, W, hgt, pln, fq, tzf_bar, tzi_bar):
+    def _block_bwd(self, pk, ws, gb, i, x, z, zbar, D, H, W, hgt, pln, fq, tzf_bar, tzi_bar, tables_done=None):
         """gb.xbar (gradient of the block output) -> gb.xbar (gradient of the block input x); accumulates the
         depth-weight gradient in gb.wbar, the z_proj gradient in zbar and the height-table gradients."""
         m = self.model
@@ -1023,6 +1045,8 @@ class Executor:
             self._xf(hgt, "tzi_t", gb.yvb, ws.va, d["zf"], ws)
             self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, True)
             self._outer(ws, ws.vb, 2 * live, ws.xv, D, N, gb.opart, gb.osplit_f, tzf_bar)
+            if tables_done:
+                tables_done()
             self._xf(hgt, "tzf_t", ws.vb, gb.xvb, d["zi"], ws)
         # input gates (and z_proj)
         if tc:

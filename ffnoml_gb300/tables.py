@@ -140,7 +140,8 @@ def percolumn_tables(z_raw, length, k):
     """Per-column tables when the columns' height grids differ (the reference's non-shared path,
     models/ffno_model.py:276-280, 306-308): z_raw [ncol, D] heights of each column (unshifted). Returns live modes M'
     (the largest live count over the columns), tzf [ncol][2M'][D] and tzi [ncol][D][2M'] with each column's own
-    taper, float64."""
+    taper, float64. The executor builds these tables on the device (ffno_percol_tables); this host statement is what
+    the kernel is tested against."""
     z = np.asarray(z_raw, dtype=np.float64)
     z = z - z.min(axis=-1, keepdims=True)
     tap = column_tapers(z, k)
@@ -154,6 +155,32 @@ def percolumn_tables(z_raw, length, k):
     tzf = np.concatenate([q_re.transpose(0, 2, 1), q_im.transpose(0, 2, 1)], axis=1)
     tzi = np.concatenate([np.cos(ph) * f[:, None], -np.sin(ph) * f[:, None]], axis=2)
     return live, tzf, tzi
+
+
+def percolumn_prep(z_raw, length, k):
+    """What the per-column table kernels (ffno_percol_tables / _vjp) take besides the heights: live modes M' (the
+    largest live count over the columns), f [ncol][M'] = factor * taper / length per column and mode, df [ncol][M'] =
+    d f / d dz (dz the column's median spacing: the taper's only dependence on the heights) and med [ncol] (int32), the
+    index of the median spacing as torch.median returns it (the index autograd differentiates through), float64."""
+    z = np.asarray(z_raw, dtype=np.float64)
+    z = z - z.min(axis=-1, keepdims=True)           # spacings of the shifted heights, bit for bit as autograd sees them
+    sp = torch.from_numpy(np.abs(z[..., 1:] - z[..., :-1]))
+    dz_t, med = sp.median(dim=-1)
+    dz = dz_t.numpy()[:, None]
+    kk = k.numpy()[None]
+    kn = math.pi / dz
+    u_raw = (kk - 2 * kn / 3) / (kn / 3)
+    u = np.clip(u_raw, 0.0, 1.0)
+    tap = 0.5 * (1 + np.cos(math.pi * u))
+    live = max(1, int((tap > 0).sum(axis=-1).max()))
+    factor = np.full(live, 2.0)
+    factor[0] = 1.0
+    f = factor[None] * tap[:, :live] / length
+    # d tap / d dz = -pi/2 sin(pi u) * du/d dz with du/d dz = 3 k / pi where the clamp passes (0 <= u_raw <= 1)
+    inside = (u_raw >= 0.0) & (u_raw <= 1.0)
+    dtap = np.where(inside, -0.5 * math.pi * np.sin(math.pi * u) * 3 * kk / math.pi, 0.0)
+    df = factor[None] * dtap[:, :live] / length
+    return live, np.ascontiguousarray(f), np.ascontiguousarray(df), med.numpy().astype(np.int32)
 
 
 def height_tables(column, length, k):
@@ -218,7 +245,8 @@ def _filon_torch(z, k):
 
 def percolumn_tables_vjp(z_raw, length, k, live, tzf_bar, tzi_bar):
     """Gradient w.r.t. z_raw [ncol, D] of percolumn_tables along (tzf_bar [ncol][2M'][D], tzi_bar [ncol][D][2M']),
-    by float64 autograd: each column's shift by its minimum, Filon weights, phases and taper."""
+    by float64 autograd: each column's shift by its minimum, Filon weights, phases and taper. The executor runs this
+    gradient on the device (ffno_percol_tables_vjp); this host statement is what the kernel is tested against."""
     with torch.enable_grad():
         zr = torch.as_tensor(np.asarray(z_raw, dtype=np.float64)).requires_grad_(True)
         z = zr - zr.amin(dim=-1, keepdim=True)

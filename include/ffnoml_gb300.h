@@ -362,7 +362,9 @@ int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long
                      const float* zp, float* x_bar, float* z_bar, int* err, ffno_stream_t stream);
 /* ffno_fuse_bwd in two stages after ffno_fuse1_tc has recomputed gates and hg:
  * a: hf_bar [V][2C] = (fused_pre_bar wf2) * gelu'(B wf1^T); wpack = [wf1 (2C x 2C), wf2^T (2C x C)]
- * b: the rest, writing x_bar, spec_bar, vert_bar; wpack = [wf1^T (2C x 2C), wg2^T (C x 2C), wg1^T (3C x C)]. */
+ * b: the rest, writing x_bar, spec_bar, vert_bar; wpack = [wf1^T (2C x 2C), wg2^T (C x 2C), wg1^T (3C x C)]; its
+ *    per-voxel arrays (spec_pre, vert_pre, gates, hg, fused_pre_bar, base, x_bar, spec_bar, vert_bar) must be
+ *    32-byte aligned (FFNO_EINVAL otherwise). */
 int ffno_fuse_bwd_a_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
                        const float* gates, const float* fused_pre_bar, long V, int C, const void* wpack,
                        float* hf_bar, int* err, ffno_stream_t stream);
@@ -405,6 +407,23 @@ int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, 
  * the shorter of Ma, Mb at most 256. */
 int ffno_outer_tc(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, float* part, int nsplit,
                   double* out, int accumulate, int* err, ffno_stream_t stream);
+
+/* ---- per-column height tables (HeightSpectralConv's non-shared path, models/ffno_model.py:276-280, 306-308), FP64
+ * arithmetic. Column c has heights z_raw[c][0..D) (unshifted); k[0..live) the live wavenumbers; f[c][m] = factor_m
+ * taper_m / length with the column's own taper. Writes the FP32 tables tzf [ncol][2 live][D] (Filon weights, real rows
+ * then imaginary rows), tzi [ncol][D][2 live] (cos, -sin of z_j k_m times f) and their transposes tzf_t
+ * [ncol][D][2 live], tzi_t [ncol][2 live][D], z_j = z_raw[c][j] - min_j z_raw[c][j]. */
+#define FFNO_PERCOL_MAX_D 4096
+#define FFNO_PERCOL_MAX_LIVE 2048
+int ffno_percol_tables(const double* z_raw, int D, long ncol, const double* k, int live, const double* f, float* tzf,
+                       float* tzi, float* tzf_t, float* tzi_t, ffno_stream_t stream);
+/* Its gradient: z_bar[j * ncol + c] += d/dz_raw[c][j] of sum(tzf_bar * tzf) + sum(tzi_bar * tzi) (FP64 bars in the
+ * layouts of tzf and tzi). df[c][m] = d f[c][m] / d dz_c, dz_c the median spacing of column c, which is spacing
+ * med[c] (|z_raw[c][med + 1] - z_raw[c][med]|, the index torch.median returns); the minimum's gradient is shared
+ * evenly by tied minima. */
+int ffno_percol_tables_vjp(const double* z_raw, int D, long ncol, const double* k, int live, const double* f,
+                           const double* df, const int* med, const double* tzf_bar, const double* tzi_bar,
+                           float* z_bar, ffno_stream_t stream);
 
 /* ---- forward-mode derivative (JVP): jvp_local (ffno_fsdp_runtime.py:350-372), the tangent of FFNO3D.forward along
  * an input tangent with the heights fixed. The linear stages reuse the forward entry points on the tangent (the lift

@@ -1,0 +1,106 @@
+"""The per-column height tables built on the device (ffno_percol_tables) and their gradient (ffno_percol_tables_vjp)
+against the float64 host statements in ffnoml_gb300/tables.py (numpy Filon weights; torch autograd through the same
+table builder), on columns that run up and down, with tied minima, zero-length intervals and modes inside the taper's
+transition band, so that every term of the gradient is exercised."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _columns(ncol, D, seed):
+    g = np.random.default_rng(seed)
+    steps = g.uniform(0.25, 0.7, (ncol, D))            # median spacing ~0.47: k in (4.5, 6.7) falls in the taper band
+    cols = 14.0 - np.cumsum(steps, axis=1)              # descending columns (heights from the top)
+    cols[1] = cols[1][::-1].copy()                      # an ascending one
+    cols[2, 5] = cols[2, 6]                             # a zero-length interval
+    cols[3, -1] = cols[3, -2] = cols[3].min() - 0.5     # two tied minima
+    cols[4] = np.sort(g.uniform(-1.0, 14.0, D))[::-1]   # irregular spacing
+    return np.ascontiguousarray(cols)
+
+
+def _k(length, n):
+    return torch.arange(0, n, dtype=torch.float64) * 2 * math.pi / (2 * length)
+
+
+def _device_tables(cols, length, k):
+    from ffnoml_gb300 import _native as nat
+    from ffnoml_gb300 import tables as tb
+    live, f, df, med = tb.percolumn_prep(cols, length, k)
+    ncol, D = cols.shape
+    dev = torch.device("cuda")
+    d64 = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    z, kk, fd, dfd = d64(cols), d64(k.numpy()[:live]), d64(f), d64(df)
+    medd = torch.as_tensor(med, dtype=torch.int32, device=dev)
+    out = [torch.empty(s, dtype=torch.float32, device=dev)
+           for s in ((ncol, 2 * live, D), (ncol, D, 2 * live), (ncol, D, 2 * live), (ncol, 2 * live, D))]
+    s = torch.cuda.current_stream().cuda_stream
+    nat.call("ffno_percol_tables", z.data_ptr(), D, ncol, kk.data_ptr(), live, fd.data_ptr(),
+             *[t.data_ptr() for t in out], s)
+    torch.cuda.synchronize()
+    return live, out, (z, kk, fd, dfd, medd)
+
+
+@pytest.mark.parametrize("D,ncol,nk", [(40, 9, 33), (256, 5, 65), (37, 6, 12)])
+def test_tables_match_host_float64(D, ncol, nk):
+    from ffnoml_gb300 import tables as tb
+    length = 15.0
+    cols = _columns(ncol, D, D)
+    k = _k(length, nk)
+    live, (tzf, tzi, tzf_t, tzi_t), _ = _device_tables(cols, length, k)
+    live0, tzf0, tzi0 = tb.percolumn_tables(cols, length, k)
+    assert live == live0
+    for got, ref in ((tzf, tzf0), (tzi, tzi0), (tzf_t, tzf0.transpose(0, 2, 1)), (tzi_t, tzi0.transpose(0, 2, 1))):
+        got = got.cpu().numpy().astype(np.float64)
+        # both are the float32 rounding of float64 values that agree to ~1e-15: equal or one float32 ulp apart
+        assert np.all(np.abs(got - ref) <= 1.2e-7 * np.abs(ref) + 1e-12 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("D,ncol,nk", [(40, 9, 33), (256, 5, 65), (37, 6, 12)])
+def test_gradient_matches_host_autograd(D, ncol, nk):
+    from ffnoml_gb300 import _native as nat
+    from ffnoml_gb300 import tables as tb
+    length = 15.0
+    cols = _columns(ncol, D, D + 1)
+    k = _k(length, nk)
+    live, _, (z, kk, fd, dfd, medd) = _device_tables(cols, length, k)
+    _, f, df, _ = tb.percolumn_prep(cols, length, k)
+    assert np.any(df != 0.0)                             # the taper term is live in this case
+    g = np.random.default_rng(D + 2)
+    fb = g.normal(size=(ncol, 2 * live, D))
+    ib = g.normal(size=(ncol, D, 2 * live))
+    ref = tb.percolumn_tables_vjp(cols, length, k, live, fb, ib)          # [ncol][D], float64
+    zbar = torch.zeros(D, ncol, dtype=torch.float32, device="cuda")
+    dev = lambda a: torch.as_tensor(a, dtype=torch.float64, device="cuda").contiguous()
+    nat.call("ffno_percol_tables_vjp", z.data_ptr(), D, ncol, kk.data_ptr(), live, fd.data_ptr(), dfd.data_ptr(),
+             medd.data_ptr(), dev(fb).data_ptr(), dev(ib).data_ptr(), zbar.data_ptr(),
+             torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    got = zbar.cpu().numpy().T.astype(np.float64)                      # [ncol][D]
+    want = ref.astype(np.float32).astype(np.float64)
+    # float64 sums in other orders, then rounded to float32: equal to within two float32 ulps of the entry
+    assert np.all(np.abs(got - want) <= 2.4e-7 * np.abs(want) + 1e-9 * np.abs(want).max()), \
+        np.max(np.abs(got - want) / (np.abs(want) + 1e-30))
+
+
+def test_gradient_accumulates_into_z_bar():
+    """The kernel adds to z_bar (the executor accumulates the samples' other height gradients there first)."""
+    from ffnoml_gb300 import _native as nat
+    length, D, ncol = 15.0, 24, 4
+    cols = _columns(ncol, D, 5)
+    k = _k(length, 20)
+    live, _, (z, kk, fd, dfd, medd) = _device_tables(cols, length, k)
+    fb = torch.randn(ncol, 2 * live, D, dtype=torch.float64, device="cuda")
+    ib = torch.randn(ncol, D, 2 * live, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    args = lambda zb: (z.data_ptr(), D, ncol, kk.data_ptr(), live, fd.data_ptr(), dfd.data_ptr(), medd.data_ptr(),
+                       fb.data_ptr(), ib.data_ptr(), zb.data_ptr(), s)
+    a = torch.zeros(D, ncol, device="cuda")
+    nat.call("ffno_percol_tables_vjp", *args(a))
+    b = torch.full((D, ncol), 2.5, device="cuda")
+    nat.call("ffno_percol_tables_vjp", *args(b))
+    torch.cuda.synchronize()
+    assert torch.equal(b, (a + 2.5))
