@@ -18,7 +18,8 @@ def _columns(ncol, D, seed):
     cols[1] = cols[1][::-1].copy()                      # an ascending one
     cols[2, 5] = cols[2, 6]                             # a zero-length interval
     cols[3, -1] = cols[3, -2] = cols[3].min() - 0.5     # two tied minima
-    cols[4] = np.sort(g.uniform(-1.0, 14.0, D))[::-1]   # irregular spacing
+    if ncol > 4:
+        cols[4] = np.sort(g.uniform(-1.0, 14.0, D))[::-1]   # irregular spacing
     return np.ascontiguousarray(cols)
 
 
@@ -74,10 +75,11 @@ def test_gradient_matches_host_autograd(D, ncol, nk):
     ib = g.normal(size=(ncol, D, 2 * live))
     ref = tb.percolumn_tables_vjp(cols, length, k, live, fb, ib)          # [ncol][D], float64
     zbar = torch.zeros(D, ncol, dtype=torch.float32, device="cuda")
-    dev = lambda a: torch.as_tensor(a, dtype=torch.float64, device="cuda").contiguous()
+    # device copies held until the kernel has run (a temporary's memory may be handed to the next allocation)
+    fbd = torch.as_tensor(fb, dtype=torch.float64, device="cuda").contiguous()
+    ibd = torch.as_tensor(ib, dtype=torch.float64, device="cuda").contiguous()
     nat.call("ffno_percol_tables_vjp", z.data_ptr(), D, ncol, kk.data_ptr(), live, fd.data_ptr(), dfd.data_ptr(),
-             medd.data_ptr(), dev(fb).data_ptr(), dev(ib).data_ptr(), zbar.data_ptr(),
-             torch.cuda.current_stream().cuda_stream)
+             medd.data_ptr(), fbd.data_ptr(), ibd.data_ptr(), zbar.data_ptr(), torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     got = zbar.cpu().numpy().T.astype(np.float64)                      # [ncol][D]
     want = ref.astype(np.float32).astype(np.float64)
