@@ -6,6 +6,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "tc.cuh"
 
 using namespace ffno;
 
@@ -47,13 +48,34 @@ __device__ __forceinline__ float upstream(int mode, float u, float r, float y) {
 }
 
 // ------------------------------------------------------------------------------------------------ GN backward
-// Lane layout of the two GroupNorm-backward kernels: each voxel's C channels are C/4 float4s held by LPV consecutive
-// lanes (LPV = C/4, or 24 lanes of a warp for C = 96); a warp covers VPW voxels per step.
-template <int C>
+// Lane layout of the two GroupNorm-backward kernels: each voxel's C channels are held VW at a time by LPV consecutive
+// lanes (C = 96: VW = 4 and 24 lanes of a warp); a warp covers VPW voxels per step. The application uses VW = 8 (one
+// 32-byte request a lane) for C <= 64; the statistics keep VW = 4, whose per-slot double accumulators would
+// otherwise take more registers than two CTAs of an SM have.
+template <int C, int W>
 struct GnLanes {
-  static constexpr int LPV = C / 4;
+  static constexpr int VW = C <= 64 ? W : 4;
+  static constexpr int LPV = C / VW;
   static constexpr int VPW = LPV <= 32 ? 32 / LPV : 1;
 };
+
+template <int VW>
+__device__ __forceinline__ void ldv(const float* p, float (&o)[VW]) {
+  if constexpr (VW == 8) {
+    ffno::tc::ld8(p, o);
+  } else {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(p));
+    o[0] = a.x, o[1] = a.y, o[2] = a.z, o[3] = a.w;
+  }
+}
+template <int VW>
+__device__ __forceinline__ void stv(float* p, const float (&v)[VW]) {
+  if constexpr (VW == 8) {
+    ffno::tc::st8(p, v);
+  } else {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+}
 
 // Per-group constants of one GroupNorm, as floats in shared memory: mean, rstd, 1/T, S1, S2, var*rstd^2.
 struct GnConst {
@@ -82,52 +104,60 @@ __global__ void __launch_bounds__(256) k_gn_bwd_stats(int mode, const float* __r
                                                       const float* __restrict__ beta,
                                                       const double* __restrict__ gst, long V,
                                                       double* __restrict__ partials, int cpg, int groups) {
-  using Ln = GnLanes<C>;
+  using Ln = GnLanes<C, 4>;
   __shared__ GnConst k;
   __shared__ double red[8][GMAX][2];
   load_gn_const(k, gst, nullptr, groups, 0.f);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / Ln::LPV, q = lane % Ln::LPV;
   const bool active = sub < Ln::VPW;
-  const int c = 4 * q;
-  float gm[4], bt[4];
-  int grp[4];
+  constexpr int VW = Ln::VW;
+  const int c = VW * q;
+  float gm[VW], bt[VW];
+  int grp[VW];
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < VW; ++j) {
     gm[j] = active ? __ldg(gamma + c + j) : 0.f;
     bt[j] = active ? __ldg(beta + c + j) : 0.f;
     grp[j] = (c + j) / cpg;
   }
-  double d1[4] = {0, 0, 0, 0}, d2[4] = {0, 0, 0, 0};   // per element slot (groups of slot j fixed per thread)
-  float f1[4] = {0, 0, 0, 0}, f2[4] = {0, 0, 0, 0};
+  double d1[VW], d2[VW];   // per element slot (groups of slot j fixed per thread)
+  float f1[VW], f2[VW];
+#pragma unroll
+  for (int j = 0; j < VW; ++j) d1[j] = d2[j] = 0.0, f1[j] = f2[j] = 0.f;
   const long step = (long)gridDim.x * 8 * Ln::VPW;
-  // UN voxels a thread are loaded before any is used (loads in flight); float partials go to double every 4 rounds
-  constexpr int UN = 4;
+  // UN voxels a thread are loaded before any is used (128 bytes in flight); float partials go to double every 4
+  // rounds
+  constexpr int UN = 16 / VW;
   int n = 0;
   for (long v0 = ((long)blockIdx.x * 8 + warp) * Ln::VPW + sub; active && v0 < V; v0 += UN * step) {
-    float4 pu[UN], pp[UN];
+    float pu[UN][VW], pp[UN][VW];
 #pragma unroll
     for (int e = 0; e < UN; ++e) {
       const long v = v0 + e * step;
-      pu[e] = v < V ? __ldg(reinterpret_cast<const float4*>(u + v * C + c)) : make_float4(0.f, 0.f, 0.f, 0.f);
-      pp[e] = v < V ? __ldg(reinterpret_cast<const float4*>(pre + v * C + c)) : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (v < V) {
+        ldv<VW>(u + v * C + c, pu[e]);
+        ldv<VW>(pre + v * C + c, pp[e]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < VW; ++j) pu[e][j] = pp[e][j] = 0.f;
+      }
     }
 #pragma unroll
     for (int e = 0; e < UN; ++e) {
       if (v0 + e * step >= V) break;
-      const float uu[4] = {pu[e].x, pu[e].y, pu[e].z, pu[e].w}, xx[4] = {pp[e].x, pp[e].y, pp[e].z, pp[e].w};
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < VW; ++j) {
         const int g = grp[j];
-        const float xh = (xx[j] - k.mean[g]) * k.rstd[g];
-        const float gh = upstream(mode, uu[j], r, xh * gm[j] + bt[j]) * gm[j];
+        const float xh = (pp[e][j] - k.mean[g]) * k.rstd[g];
+        const float gh = upstream(mode, pu[e][j], r, xh * gm[j] + bt[j]) * gm[j];
         f1[j] += gh;
         f2[j] += gh * xh;
       }
     }
-    if (++n == 4) {
+    if (++n == 16 / UN) {
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < VW; ++j) {
         d1[j] += f1[j];
         d2[j] += f2[j];
         f1[j] = f2[j] = 0.f;
@@ -136,7 +166,7 @@ __global__ void __launch_bounds__(256) k_gn_bwd_stats(int mode, const float* __r
     }
   }
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < VW; ++j) {
     d1[j] += f1[j];
     d2[j] += f2[j];
   }
@@ -144,7 +174,7 @@ __global__ void __launch_bounds__(256) k_gn_bwd_stats(int mode, const float* __r
   for (int g = 0; g < groups; ++g) {
     double a = 0.0, b = 0.0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < VW; ++j)
       if (active && grp[j] == g) {
         a += d1[j];
         b += d2[j];
@@ -194,24 +224,25 @@ __global__ void k_gn_bwd_final(const double* __restrict__ partials, int nparts, 
 
 // pre_bar = rstd (ghat - (w / T)(S1 + xhat S2)); w_bar[v] += sum_c (1/T)(-S1 xhat - S2 (xhat^2 - var rstd^2) / 2).
 template <int C>
-__global__ void __launch_bounds__(256) k_gn_bwd_apply(int mode, const float* __restrict__ u, float r,
+__global__ void __launch_bounds__(256, 4) k_gn_bwd_apply(int mode, const float* __restrict__ u, float r,
                                                       const float* __restrict__ pre, const float* __restrict__ gamma,
                                                       const float* __restrict__ beta,
                                                       const double* __restrict__ gst, const double* __restrict__ sums,
                                                       const float* __restrict__ dw, long V,
                                                       float* __restrict__ pre_bar, float* __restrict__ w_bar, int cpg,
                                                       int groups, float eps) {
-  using Ln = GnLanes<C>;
+  using Ln = GnLanes<C, 8>;
   __shared__ GnConst k;
   load_gn_const(k, gst, sums, groups, eps);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / Ln::LPV, q = lane % Ln::LPV;
   const bool active = sub < Ln::VPW;
-  const int c = 4 * q;
-  float gm[4], bt[4];
-  int grp[4];
+  constexpr int VW = Ln::VW;
+  const int c = VW * q;
+  float gm[VW], bt[VW];
+  int grp[VW];
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < VW; ++j) {
     gm[j] = active ? __ldg(gamma + c + j) : 0.f;
     bt[j] = active ? __ldg(beta + c + j) : 0.f;
     grp[j] = (c + j) / cpg;
@@ -224,19 +255,18 @@ __global__ void __launch_bounds__(256) k_gn_bwd_apply(int mode, const float* __r
     float wc = 0.f;
     if (ok) {
       const float wv = __ldg(dw + v);
-      const float4 pu = __ldg(reinterpret_cast<const float4*>(u + v * C + c));
-      const float4 pp = __ldg(reinterpret_cast<const float4*>(pre + v * C + c));
-      const float uu[4] = {pu.x, pu.y, pu.z, pu.w}, xx[4] = {pp.x, pp.y, pp.z, pp.w};
-      float o[4];
+      float uu[VW], xx[VW], o[VW];
+      ldv<VW>(u + v * C + c, uu);
+      ldv<VW>(pre + v * C + c, xx);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < VW; ++j) {
         const int g = grp[j];
         const float xh = (xx[j] - k.mean[g]) * k.rstd[g];
         const float gh = upstream(mode, uu[j], r, xh * gm[j] + bt[j]) * gm[j];
         o[j] = k.rstd[g] * (gh - wv * k.invT[g] * (k.s1[g] + xh * k.s2[g]));
         wc += k.invT[g] * (-k.s1[g] * xh - 0.5f * k.s2[g] * (xh * xh - k.vr2[g]));
       }
-      *reinterpret_cast<float4*>(pre_bar + v * C + c) = make_float4(o[0], o[1], o[2], o[3]);
+      stv<VW>(pre_bar + v * C + c, o);
     }
     // sum over the LPV lanes of this voxel (segments of a power-of-two LPV, or the whole warp for C = 96)
     if (Ln::LPV >= 32 || (Ln::LPV & (Ln::LPV - 1))) {
@@ -847,6 +877,10 @@ int ffno_gn_bwd_apply(int mode, const float* u, float r, const float* pre, const
   if (!u || !pre || !gamma || !beta || !gstats || !dw || !pre_bar || !w_bar) return FFNO_EINVAL;
   if (mode < 0 || mode > 2) return FFNO_EINVAL;
   if (!width_ok(C) || V < 1 || groups < 1 || groups > GMAX || C % groups) return FFNO_EINVAL;
+  // a lane moves 32 bytes of a row per request for C <= 64, 16 bytes for C = 96
+  const uintptr_t al = C <= 64 ? 32 : 16;
+  if ((reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(pre) | reinterpret_cast<uintptr_t>(pre_bar)) % al)
+    return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   const int cpg = C / groups;
   const int blocks = grid_of(V, 8 * 8, 4);

@@ -243,6 +243,46 @@ __device__ __forceinline__ void fill_tile(Split t, long v0, long V, int ptid, F 
   }
 }
 
+// fill_tile with 8 columns a piece: f(v, k, o) writes columns k..k+7 of voxel v into o (32-byte loads; a warp's
+// request covers 8 rows x 128 bytes). The pieces land in the same K-major layout, hi and lo in one 16-byte store each.
+// Thread t always serves columns fill_col8<KW>(t) .. + 7; half as many pieces in flight as fill_tile, the same bytes.
+template <int KW>
+__device__ __forceinline__ int fill_col8(int ptid) {
+  return ((ptid >> 3) % (KW / 8)) * 8;
+}
+template <int KW, typename F>
+__device__ __forceinline__ void fill_tile8(Split t, long v0, long V, int ptid, F f) {
+  static_assert(32 % (KW / 8) == 0, "fill columns must be fixed per thread");
+  constexpr int NE = TM * KW / 8;
+  constexpr int FB8 = FB / 2;
+  for (int e0 = ptid; e0 < NE; e0 += PT * FB8) {
+    float a[FB8][8];
+#pragma unroll
+    for (int u = 0; u < FB8; ++u) {   // issue the loads of FB8 pieces before converting any of them
+      const int e = e0 + u * PT;
+      const int r8 = e & 7, q = e >> 3;
+      const int kb = q % (KW / 8), rb = q / (KW / 8);
+      const long v = v0 + rb * 8 + r8;
+      if (e < NE && v < V) {
+        f(v, kb * 8, a[u]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[u][i] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < FB8; ++u) {
+      const int e = e0 + u * PT;
+      if (e >= NE) break;
+      uint32_t h[4], l[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) tc::split_pack(a[u][2 * i], a[u][2 * i + 1], h[i], l[i]);
+      *reinterpret_cast<uint4*>(t.hi() + (size_t)e * 16) = make_uint4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<uint4*>(t.lo() + (size_t)e * 16) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+  }
+}
+
 // The tile's depth weights into shared memory (wt[128]) and their warp partial sums (wpart[4]); threads ptid < 128.
 __device__ __forceinline__ void load_tile_weights(const Pipe& p, const float* __restrict__ dw, long v0, long V,
                                                   float* wt, float* wpart) {
@@ -684,10 +724,11 @@ __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp
   if (tid < 2 * GMAX * 3) acc[tid] = 0.0;
   P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
   const Op wf1 = wop(smem, 2 * C, 2 * C), wf2 = wop(smem + B1, C, 2 * C);
-  const int kf = fill_col<2 * C>(P.ptid);
-  const Gn4 gk = kf < C ? gn_coefs(sc, C, kf) : gn_coefs(vc, C, kf - C);
-  const float* src = kf < C ? sp : vp;
+  const int kf = fill_col8<2 * C>(P.ptid);
+  const float* cfk = kf < C ? sc : vc;
   const int ks = kf < C ? kf : kf - C;
+  const Gn4 gk0 = gn_coefs(cfk, C, ks), gk1 = gn_coefs(cfk, C, ks + 4);
+  const float* src = kf < C ? sp : vp;
   const int f = P.feat();
   const int pf = c_pf;
   for (int k = 1; P.ptid == 0 && k < pf; ++k) {
@@ -705,10 +746,14 @@ __global__ void __launch_bounds__(CT, 1) k_fuse2_tc(const float* __restrict__ sp
       prefetch_rows(gates, tp * TM, V, 2 * C);
     }
     load_tile_weights(P, dw, v0, V, wt[pid], wpart[pid]);
-    fill_tile<2 * C>(A, v0, V, P.ptid, [&](long v, int k) {
-      const float4 g = ld4(gates + v * 2 * C + k);
-      const float4 s = gn_apply<true>(ld4(src + v * C + ks), gk);
-      return make_float4(s.x * g.x, s.y * g.y, s.z * g.z, s.w * g.w);
+    fill_tile8<2 * C>(A, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) {
+      float g[8], p[8];
+      ld8(gates + v * 2 * C + k, g);
+      ld8(src + v * C + ks, p);
+      const float4 s0 = gn_apply<true>(make_float4(p[0], p[1], p[2], p[3]), gk0);
+      const float4 s1 = gn_apply<true>(make_float4(p[4], p[5], p[6], p[7]), gk1);
+      o[0] = s0.x * g[0], o[1] = s0.y * g[1], o[2] = s0.z * g[2], o[3] = s0.w * g[3];
+      o[4] = s1.x * g[4], o[5] = s1.y * g[5], o[6] = s1.z * g[6], o[7] = s1.w * g[7];
     });
     if (!pipe_gemms(P, err, Gemm{P.tmem, wf1, kop(A, 2 * C), 2 * C, false})) break;
     if (32 * P.q < C) {   // warps holding output channels: the residual of their lanes, columns of their half
@@ -942,10 +987,11 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_a_tc(const float* __restrict
   const Split Bt = split_at(smem + B1 + B2 + pid * RB, TM, 2 * C), Ft = split_at(smem + B1 + B2 + pid * RB, TM, C);
   P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
   const Op wf1 = wop(smem, 2 * C, 2 * C), wf2t = wop(smem + B1, 2 * C, C);
-  const int kf = fill_col<2 * C>(P.ptid);
-  const Gn4 gk = kf < C ? gn_coefs(sc, C, kf) : gn_coefs(vc, C, kf - C);
-  const float* src = kf < C ? sp : vp;
+  const int kf = fill_col8<2 * C>(P.ptid);
+  const float* cfk = kf < C ? sc : vc;
   const int ks = kf < C ? kf : kf - C;
+  const Gn4 gk0 = gn_coefs(cfk, C, ks), gk1 = gn_coefs(cfk, C, ks + 4);
+  const float* src = kf < C ? sp : vp;
   const int f = P.feat();
   // L2 prefetch: the first phase's rows (spec, vert, gates) one tile ahead, F_bar (read after the first GEMM) at
   // the start of its own tile, so that no prefetched line has to outlive a whole tile step of all pipelines
@@ -964,13 +1010,17 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_a_tc(const float* __restrict
       prefetch_rows(vp, tn, V, C);
       prefetch_rows(gates, tn, V, 2 * C);
     }
-    fill_tile<2 * C>(Bt, v0, V, P.ptid, [&](long v, int k) {
-      const float4 g = ld4(gates + v * 2 * C + k);
-      const float4 s = gn_apply<true>(ld4(src + v * C + ks), gk);
-      return make_float4(s.x * g.x, s.y * g.y, s.z * g.z, s.w * g.w);
+    fill_tile8<2 * C>(Bt, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) {
+      float g[8], p[8];
+      ld8(gates + v * 2 * C + k, g);
+      ld8(src + v * C + ks, p);
+      const float4 s0 = gn_apply<true>(make_float4(p[0], p[1], p[2], p[3]), gk0);
+      const float4 s1 = gn_apply<true>(make_float4(p[4], p[5], p[6], p[7]), gk1);
+      o[0] = s0.x * g[0], o[1] = s0.y * g[1], o[2] = s0.z * g[2], o[3] = s0.w * g[3];
+      o[4] = s1.x * g[4], o[5] = s1.y * g[5], o[6] = s1.z * g[6], o[7] = s1.w * g[7];
     });
     if (!pipe_gemms(P, err, Gemm{P.tmem, wf1, kop(Bt, 2 * C), 2 * C, false})) break;
-    fill_tile<C>(Ft, v0, V, P.ptid, [&](long v, int k) { return ld4(fb + v * C + k); });
+    fill_tile8<C>(Ft, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(fb + v * C + k, o); });
     if (!pipe_gemms(P, err, Gemm{P.tmem + TM, wf2t, kop(Ft, C), C, false})) break;
 #pragma unroll 1
     for (int c = 0; c < 4; ++c) {
@@ -1030,7 +1080,7 @@ __global__ void __launch_bounds__(CT, 1) k_fuse_bwd_b_tc(const float* __restrict
     const long v = v0 + row;
     // B_bar (without the F_bar term) = hfb Wf1^T over the spec and vert halves of hfb
     for (int kh = 0; kh < 2; ++kh) {
-      fill_tile<C>(T, v0, V, P.ptid, [&](long vv, int k) { return ld4(hfb + vv * 2 * C + kh * C + k); });
+      fill_tile8<C>(T, v0, V, P.ptid, [&](long vv, int k, float (&o)[8]) { ld8(hfb + vv * 2 * C + kh * C + k, o); });
       if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, C), wop(smem, 2 * C, 2 * C, 0, kh * C), C, kh > 0, 2 * C})) break;
     }
     if (!P.ok) break;
@@ -1420,6 +1470,7 @@ int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* v
   if (ws::fuse2_supported(C))
     return ws::fuse2(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, V, C, wpack, dw, pre, partials, nparts, err,
                      s);
+  if (!aligned32(spec_pre) || !aligned32(vert_pre) || !aligned32(gates)) return FFNO_EINVAL;   // 32-byte fills
   TC_DISPATCH(C, {
     const size_t smem = mat_bytes(2 * CC, 2 * CC) + mat_bytes(CC, 2 * CC) + 2 * tile_bytes(2 * CC);
     if (!launch_prep(k_fuse2_tc<CC>, smem)) return FFNO_ELAUNCH;
@@ -1467,6 +1518,9 @@ int ffno_fuse_bwd_a_tc(const float* spec_pre, const float* spec_coefs, const flo
   if (!spec_pre || !spec_coefs || !vert_pre || !vert_coefs || !gates || !fused_pre_bar || !wpack || !hf_bar)
     return FFNO_EINVAL;
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
+  // the operand fills read 32 bytes of a row per request
+  if (!aligned32(spec_pre) || !aligned32(vert_pre) || !aligned32(gates) || !aligned32(fused_pre_bar))
+    return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   TC_DISPATCH(C, {
     const size_t smem = mat_bytes(2 * CC, 2 * CC) + mat_bytes(2 * CC, CC) + 2 * tile_bytes(2 * CC);
@@ -1488,8 +1542,8 @@ int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const flo
   if (!tc_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
   // the epilogues move 32 bytes of a row per request
   if (!aligned32(spec_pre) || !aligned32(vert_pre) || !aligned32(gates) || !aligned32(hg) ||
-      !aligned32(fused_pre_bar) || (base && !aligned32(base)) || !aligned32(x_bar) || !aligned32(spec_bar) ||
-      !aligned32(vert_bar))
+      !aligned32(fused_pre_bar) || !aligned32(hf_bar) || (base && !aligned32(base)) || !aligned32(x_bar) ||
+      !aligned32(spec_bar) || !aligned32(vert_bar))
     return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   TC_DISPATCH(C, {

@@ -180,7 +180,8 @@ int ffno_gn_bwd_stats(int mode, const float* u, float r, const float* pre, const
                       ffno_stream_t stream);
 /* partials -> sums [groups][2] doubles (fixed order). */
 int ffno_gn_bwd_final(const double* partials, int nparts, int groups, double* sums, ffno_stream_t stream);
-/* pre_bar = rstd (ghat - (w/T)(S1 + xhat S2)); w_bar[v] += the depth-weight gradient of this GroupNorm's statistics. */
+/* pre_bar = rstd (ghat - (w/T)(S1 + xhat S2)); w_bar[v] += the depth-weight gradient of this GroupNorm's statistics.
+ * u, pre and pre_bar 32-byte aligned for C <= 64 (16-byte for C = 96), FFNO_EINVAL otherwise. */
 int ffno_gn_bwd_apply(int mode, const float* u, float r, const float* pre, const float* gamma, const float* beta,
                       const double* gstats, const double* sums, const float* dw, long V, int C, int groups, float eps,
                       float* pre_bar, float* w_bar, ffno_stream_t stream);
@@ -361,9 +362,10 @@ int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, lo
 int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long V, int C, const void* wpack,
                      const float* zp, float* x_bar, float* z_bar, int* err, ffno_stream_t stream);
 /* ffno_fuse_bwd in two stages after ffno_fuse1_tc has recomputed gates and hg:
- * a: hf_bar [V][2C] = (fused_pre_bar wf2) * gelu'(B wf1^T); wpack = [wf1 (2C x 2C), wf2^T (2C x C)]
+ * a: hf_bar [V][2C] = (fused_pre_bar wf2) * gelu'(B wf1^T); wpack = [wf1 (2C x 2C), wf2^T (2C x C)]; spec_pre,
+ *    vert_pre, gates and fused_pre_bar 32-byte aligned (FFNO_EINVAL otherwise)
  * b: the rest, writing x_bar, spec_bar, vert_bar; wpack = [wf1^T (2C x 2C), wg2^T (C x 2C), wg1^T (3C x C)]; its
- *    per-voxel arrays (spec_pre, vert_pre, gates, hg, fused_pre_bar, base, x_bar, spec_bar, vert_bar) must be
+ *    per-voxel arrays (spec_pre, vert_pre, gates, hg, fused_pre_bar, hf_bar, base, x_bar, spec_bar, vert_bar) must be
  *    32-byte aligned (FFNO_EINVAL otherwise). */
 int ffno_fuse_bwd_a_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
                        const float* gates, const float* fused_pre_bar, long V, int C, const void* wpack,
