@@ -199,27 +199,70 @@ int ffno_xform_pt(const float* T, long t_b, const float* in, float* out, const f
   return FFNO_OK;
 }
 
-// out[col][i][j] (+)= sum_c A[i*rs + col*C + c] * B[j*rs + col*C + c] (double), one CTA per column: the per-column
-// height-table gradients.
-__global__ void k_col_outer(const float* __restrict__ A, int Ra, const float* __restrict__ B, int Rb, long ncol, int C,
-                            long rs, double* __restrict__ out, int accumulate) {
+// out[col][i][j] (+)= sum_c A[i*rs + col*C + c] * B[j*rs + col*C + c], one CTA per column: the per-column
+// height-table gradients. Output tiles of 64 rows of A x 64 rows of B: both row blocks staged in shared memory
+// (coalesced row loads, rows padded to C + 1 floats), 4 x 4 outputs a thread summed over the C channels in FP32, then
+// added to the FP64 output (which accumulates the blocks of a VJP).
+constexpr int OT = 64;
+
+__global__ void __launch_bounds__(256) k_col_outer(const float* __restrict__ A, int Ra, const float* __restrict__ B,
+                                                   int Rb, long ncol, int C, long rs, double* __restrict__ out,
+                                                   int accumulate) {
+  extern __shared__ float osm[];
+  const int LD = C + 1;
+  float* as = osm;             // [OT][C + 1]
+  float* bs = osm + OT * LD;   // [OT][C + 1]
   const long col = blockIdx.x;
   if (col >= ncol) return;
-  for (int e = threadIdx.x; e < Ra * Rb; e += blockDim.x) {
-    const int i = e / Rb, j = e % Rb;
-    const float* a = A + (long)i * rs + col * C;
-    const float* b = B + (long)j * rs + col * C;
-    double s = 0.0;
-    for (int c = 0; c < C; ++c) s += (double)a[c] * (double)b[c];
-    double* o = out + (col * Ra + i) * (long)Rb + j;
-    *o = accumulate ? *o + s : s;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  for (int i0 = 0; i0 < Ra; i0 += OT) {
+    for (int j0 = 0; j0 < Rb; j0 += OT) {
+      __syncthreads();   // the previous tile's reads are done
+      for (int e = threadIdx.x; e < OT * C; e += blockDim.x) {
+        const int r = e / C, c = e % C;
+        as[r * LD + c] = i0 + r < Ra ? __ldg(A + (long)(i0 + r) * rs + col * C + c) : 0.f;
+        bs[r * LD + c] = j0 + r < Rb ? __ldg(B + (long)(j0 + r) * rs + col * C + c) : 0.f;
+      }
+      __syncthreads();
+      float acc[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+      for (int c = 0; c < C; ++c) {
+        float a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = as[(ty + 16 * i) * LD + c];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = bs[(tx + 16 * j) * LD + c];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int ii = i0 + ty + 16 * i;
+        if (ii >= Ra) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int jj = j0 + tx + 16 * j;
+          if (jj >= Rb) continue;
+          double* o = out + (col * Ra + ii) * (long)Rb + jj;
+          *o = accumulate ? *o + (double)acc[i][j] : (double)acc[i][j];
+        }
+      }
+    }
   }
 }
 
 int ffno_col_outer(const float* A, int Ra, const float* B, int Rb, long ncol, int C, long row_stride, double* out,
                    int accumulate, ffno_stream_t stream) {
-  if (!A || !B || !out || Ra < 1 || Rb < 1 || ncol < 1 || C < 1 || ncol > 0x7fffffffL) return FFNO_EINVAL;
-  k_col_outer<<<(unsigned)ncol, 256, 0, (cudaStream_t)stream>>>(A, Ra, B, Rb, ncol, C, row_stride, out, accumulate);
+  if (!A || !B || !out || Ra < 1 || Rb < 1 || ncol < 1 || C < 1 || C > 512 || ncol > 0x7fffffffL) return FFNO_EINVAL;
+  const size_t smem = (size_t)2 * OT * (C + 1) * sizeof(float);
+  if (smem > 48 * 1024 && !ffno::smem_cap_ok(k_col_outer, smem)) return FFNO_ELAUNCH;
+  k_col_outer<<<(unsigned)ncol, 256, smem, (cudaStream_t)stream>>>(A, Ra, B, Rb, ncol, C, row_stride, out,
+                                                                  accumulate);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

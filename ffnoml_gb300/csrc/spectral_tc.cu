@@ -41,7 +41,6 @@ constexpr int RT = 256;                     // threads per pipeline
 constexpr int RKC = 64;                     // data rows k per chunk
 constexpr uint32_t RSB = 128u * RKC * 2;    // one split half of a data stage
 constexpr int RT_MAXK = 512;                // largest padded K of a resident table
-constexpr int XFB = 8;                      // data loads in flight per thread (a whole 64-row chunk per pipeline)
 
 __device__ __forceinline__ void rt_sync(int pipe) { asm volatile("bar.sync %0, %1;" ::"r"(1 + pipe), "n"(RT) : "memory"); }
 __device__ __forceinline__ bool rt_sync_and(int pipe, bool p) {
@@ -52,6 +51,44 @@ __device__ __forceinline__ bool rt_sync_and(int pipe, bool p) {
       : "r"((uint32_t)p), "r"(1 + pipe), "n"(RT)
       : "memory");
   return r != 0;
+}
+
+// Fill of one data stage (rows k0 .. k0 + kc of the chunk, 128 columns) from FP32 HBM into the split MN-major tile.
+// A piece is 8 consecutive columns of one row (one 32-byte load). Lanes take 8 rows (lane & 7) x 4 column octets
+// (lane >> 3) and warps (w & 3) four groups of octets, so a warp reads 8 rows x 128 contiguous bytes, and each 8-lane
+// phase of its 16-byte stores covers 8 rows of one octet: 128 contiguous bytes of the tile, free of bank conflicts.
+// Row k0 + kr of piece u is kr = 8 (2u + (w >> 2)) + (lane & 7); the columns nf..nf+7 depend on the thread only.
+constexpr int XFB8 = 4;   // pieces a thread: 4 x 32 bytes in flight, the whole 64-row chunk per pipeline
+static_assert(XFB8 * RT * 8 == RKC * 128, "the pieces of a pipeline cover a whole chunk");
+
+__device__ __forceinline__ int xf_fill_col(int ptid, int lane) { return 8 * (4 * ((ptid >> 5) & 3) + (lane >> 3)); }
+
+__device__ __forceinline__ void xf_fill_chunk(uint8_t* st, const float* fsrc, bool fv, const long* row_in, int K,
+                                              int k0, int kc, int ptid, int lane, int nf) {
+  const int w = (ptid >> 5) & 7;
+  float v[XFB8][8];
+#pragma unroll
+  for (int u = 0; u < XFB8; ++u) {   // every load of the chunk issued before any is converted
+    const int kr = 8 * (2 * u + (w >> 2)) + (lane & 7);
+    const int k = k0 + kr;
+    if (kr < kc && k < K && fv) {
+      tc::ld8(fsrc + row_in[k], v[u]);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[u][i] = 0.f;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < XFB8; ++u) {
+    const int kr = 8 * (2 * u + (w >> 2)) + (lane & 7);
+    if (kr >= kc) break;
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) tc::split_pack(v[u][2 * i], v[u][2 * i + 1], h[i], l[i]);
+    const uint32_t o = tc::mnmajor_offset(nf, kr, 128);
+    *reinterpret_cast<uint4*>(st + o) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(st + RSB + o) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
 }
 
 __global__ void __launch_bounds__(2 * RT, 1)
@@ -100,8 +137,8 @@ __global__ void __launch_bounds__(2 * RT, 1)
       bfirst = it / ntn;
       n0 = (it % ntn) * 128;
     }
-    // every fill piece of this thread covers the same 4 columns nf..nf+3 (see the piece mapping below)
-    const int nf = 8 * (2 * ((ptid >> 5) & 7) + (lane >> 4)) + 4 * ((lane >> 3) & 1);
+    // every fill piece of this thread covers the same 8 columns nf..nf+7 (see the piece mapping below)
+    const int nf = xf_fill_col(ptid, lane);
     long foff = 0;
     bool fv;
     {
@@ -125,30 +162,7 @@ __global__ void __launch_bounds__(2 * RT, 1)
         if (!(ok = rt_sync_and(pipe, w))) break;
       }
       uint8_t* st = sD + (uint32_t)(pipe * 2 + s) * 2u * RSB;
-      // fill: piece e = 4 consecutive columns of one row k; lanes take 8 rows x 2 column pairs, so a warp reads 8
-      // rows x 64 contiguous bytes and writes conflict-free 8-byte slots of the MN-major tile. Row k of piece e is
-      // 8 (e / 256) + (lane & 7); its columns nf..nf+3 depend on the thread only.
-      for (int e0 = ptid; e0 < kc * 32; e0 += XFB * RT) {
-        float4 v[XFB];
-#pragma unroll
-        for (int u = 0; u < XFB; ++u) {
-          const int e = e0 + u * RT;
-          const int k = k0 + 8 * (e >> 8) + (lane & 7);
-          v[u] = (e < kc * 32 && k < d.K && fv) ? __ldg(reinterpret_cast<const float4*>(fsrc + row_in[k]))
-                                                : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-#pragma unroll
-        for (int u = 0; u < XFB; ++u) {
-          const int e = e0 + u * RT;
-          if (e >= kc * 32) break;
-          uint32_t h0, l0, h1, l1;
-          tc::split_pack(v[u].x, v[u].y, h0, l0);
-          tc::split_pack(v[u].z, v[u].w, h1, l1);
-          const uint32_t o = tc::mnmajor_offset(nf, 8 * (e >> 8) + (lane & 7), 128);
-          *reinterpret_cast<uint2*>(st + o) = make_uint2(h0, h1);
-          *reinterpret_cast<uint2*>(st + RSB + o) = make_uint2(l0, l1);
-        }
-      }
+      xf_fill_chunk(st, fsrc, fv, row_in, d.K, k0, kc, ptid, lane, nf);
       tc::fence_async_smem();
       tc::tc_before_sync();
       rt_sync(pipe);
@@ -264,7 +278,7 @@ __global__ void __launch_bounds__(RT, 1)
       bfirst = it / ntn;
       n0 = (it % ntn) * 128;
     }
-    const int nf = 8 * (2 * ((tid >> 5) & 7) + (lane >> 4)) + 4 * ((lane >> 3) & 1);
+    const int nf = xf_fill_col(tid, lane);
     long foff = 0;
     bool fv;
     {
@@ -298,27 +312,7 @@ __global__ void __launch_bounds__(RT, 1)
           tc::bulk_g2s(tt + (uint32_t)MT * part + mt * part, src + part, part, &bar_t[s]);
         }
       }
-      for (int e0 = tid; e0 < kc * 32; e0 += XFB * RT) {
-        float4 v[XFB];
-#pragma unroll
-        for (int u = 0; u < XFB; ++u) {
-          const int e = e0 + u * RT;
-          const int k = k0 + 8 * (e >> 8) + (lane & 7);
-          v[u] = (e < kc * 32 && k < d.K && fv) ? __ldg(reinterpret_cast<const float4*>(fsrc + row_in[k]))
-                                                : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-#pragma unroll
-        for (int u = 0; u < XFB; ++u) {
-          const int e = e0 + u * RT;
-          if (e >= kc * 32) break;
-          uint32_t h0, l0, h1, l1;
-          tc::split_pack(v[u].x, v[u].y, h0, l0);
-          tc::split_pack(v[u].z, v[u].w, h1, l1);
-          const uint32_t o = tc::mnmajor_offset(nf, 8 * (e >> 8) + (lane & 7), 128);
-          *reinterpret_cast<uint2*>(st + o) = make_uint2(h0, h1);
-          *reinterpret_cast<uint2*>(st + RSB + o) = make_uint2(l0, l1);
-        }
-      }
+      xf_fill_chunk(st, fsrc, fv, row_in, d.K, k0, kc, tid, lane, nf);
       tc::fence_async_smem();
       const bool wt = tc::mbar_wait(&bar_t[s], (g >> 1) & 1u);
       tc::tc_before_sync();
@@ -825,8 +819,8 @@ int ffno_xform_tc(const void* tpack, const float* in, float* out, const ffno_xfo
   if (d.nb < 1 || d.nb2 < 1 || d.K < 1 || d.M < 1 || d.M > 128 * XMT || d.N < 1 || d.in_split < 1 ||
       d.out_split < 1)
     return FFNO_EINVAL;
-  if (d.N % 4 || d.in_lo % 4 || d.in_hi % 4 || d.in_b1 % 4 || d.in_b2 % 4) return FFNO_EINVAL;  // float4 loads
-  if (reinterpret_cast<uintptr_t>(in) % 16) return FFNO_EINVAL;
+  if (d.N % 8 || d.in_lo % 8 || d.in_hi % 8 || d.in_b1 % 8 || d.in_b2 % 8) return FFNO_EINVAL;  // 32-byte loads
+  if (reinterpret_cast<uintptr_t>(in) % 32) return FFNO_EINVAL;
   const int Kp = (d.K + 15) / 16 * 16;
   if (Kp > RT_MAXK) return FFNO_EINVAL;
   const int MT = (d.M + 127) / 128;
@@ -854,8 +848,8 @@ int ffno_xform_tcr(const void* tpack, int Mp, int Kp, const float* in, float* ou
   if (d.nb < 1 || d.nb2 < 1 || d.K < 1 || d.M < 1 || d.N < 1 || d.in_split < 1 || d.out_split < 1) return FFNO_EINVAL;
   if (Mp % 16 || Mp < d.M || Mp > 256 || Kp % 16 || Kp < d.K || Kp > RT_MAXK) return FFNO_EINVAL;
   if ((size_t)Mp * Kp * 4 > ffno_xform_tcr_max_table_bytes()) return FFNO_EINVAL;
-  if (d.N % 4 || d.in_lo % 4 || d.in_hi % 4 || d.in_b1 % 4 || d.in_b2 % 4) return FFNO_EINVAL;   // float4 loads
-  if (reinterpret_cast<uintptr_t>(in) % 16) return FFNO_EINVAL;
+  if (d.N % 8 || d.in_lo % 8 || d.in_hi % 8 || d.in_b1 % 8 || d.in_b2 % 8) return FFNO_EINVAL;   // 32-byte loads
+  if (reinterpret_cast<uintptr_t>(in) % 32) return FFNO_EINVAL;
   int nbi = 1, nshift = 0;
   if (d.N < 128 && 128 % d.N == 0) {
     nbi = 128 / (int)d.N;

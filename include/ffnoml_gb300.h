@@ -152,7 +152,8 @@ int ffno_xform(const float* T, const float* in, float* out, const ffno_xform_des
 int ffno_xform_pt(const float* T, long t_b, const float* in, float* out, const ffno_xform_desc* desc, int accumulate,
                   ffno_stream_t stream);
 /* Per-column table gradients: out [ncol][Ra][Rb] (double; = or +=) with out[col][i][j] = sum_c A[i][col][c] *
- * B[j][col][c], A and B laid [rows][ncol][C] with row stride row_stride floats. */
+ * B[j][col][c], A and B laid [rows][ncol][C] with row stride row_stride floats; each sum over the C <= 512 channels
+ * in FP32, added to out in FP64. */
 int ffno_col_outer(const float* A, int Ra, const float* B, int Rb, long ncol, int C, long row_stride, double* out,
                    int accumulate, ffno_stream_t stream);
 
@@ -385,7 +386,8 @@ int ffno_head_bwd_tc(const float* x, const float* x_in, const float* y_bar, long
                      const float* b2, int nhp, const ffno_head_params* params, float* x_bar, float* x_in_bar,
                      int* err, ffno_stream_t stream);
 
-/* ffno_xform on tensor cores (split-BF16), same descriptor; M <= 256, every stride and N multiples of 4 floats.
+/* ffno_xform on tensor cores (split-BF16), same descriptor; M <= 256, N and the input strides multiples of 8 floats,
+ * the input pointer 32-byte aligned (rows are read 32 bytes a request).
  * tpack: T [M][K] packed per 128-row m-tile (rows past M zero) and, within it, per 64-wide k-chunk (K padded with
  * zeros to a multiple of 16; the last chunk narrower), each chunk its hi then lo half in the canonical K-major order
  * with the chunk's own width; ffno_xform_tc_pack_bytes gives the size. */
@@ -394,7 +396,7 @@ int ffno_xform_tc(const void* tpack, const float* in, float* out, const ffno_xfo
                   ffno_stream_t stream);
 /* ffno_xform on tensor cores with the whole table resident in shared memory (the split table [Mp][Kp] packed as one
  * canonical K-major operand, hi then lo; Mp a multiple of 16 <= 256, Kp a multiple of 16, 4 Mp Kp <=
- * ffno_xform_tcr_max_table_bytes()). N, the input strides and the input pointer must be float4-aligned. */
+ * ffno_xform_tcr_max_table_bytes()). N and the input strides multiples of 8 floats, the input pointer 32-byte aligned. */
 int ffno_xform_tcr_max_table_bytes(void);
 int ffno_xform_tcr(const void* tpack, int Mp, int Kp, const float* in, float* out, const ffno_xform_desc* desc,
                    int accumulate, int* err, ffno_stream_t stream);

@@ -69,7 +69,8 @@ def test_gradient_matches_host_autograd(D, ncol, nk):
     k = _k(length, nk)
     live, _, (z, kk, fd, dfd, medd) = _device_tables(cols, length, k)
     _, f, df, _ = tb.percolumn_prep(cols, length, k)
-    assert np.any(df != 0.0)                             # the taper term is live in this case
+    # with 33 or more modes some reach the taper's transition band, so its term is live; 12 modes stay below it
+    assert np.any(df != 0.0) == (nk >= 33)
     g = np.random.default_rng(D + 2)
     fb = g.normal(size=(ncol, 2 * live, D))
     ib = g.normal(size=(ncol, D, 2 * live))
@@ -106,3 +107,27 @@ def test_gradient_accumulates_into_z_bar():
     nat.call("ffno_percol_tables_vjp", *args(b))
     torch.cuda.synchronize()
     assert torch.equal(b, (a + 2.5))
+
+
+@pytest.mark.parametrize("Ra,Rb,C,ncol", [(70, 130, 64, 5), (256, 64, 16, 3), (37, 12, 96, 4)])
+def test_column_outer_products(Ra, Rb, C, ncol):
+    """ffno_col_outer: out[col][i][j] (+)= sum_c A[i][col][c] B[j][col][c] with row stride rs, ragged against the
+    64 x 64 output tiles, against float64; each sum over the C channels is FP32 (bounded by C ulps of sum |a b|)."""
+    from ffnoml_gb300 import _native as nat
+    g = torch.Generator().manual_seed(Ra + Rb + C)
+    rs = (ncol + 1) * C                                 # a row holds ncol columns and a spare one
+    A = torch.randn(Ra, rs, generator=g).cuda()
+    B = torch.randn(Rb, rs, generator=g).cuda()
+    out = torch.randn(ncol, Ra, Rb, generator=g, dtype=torch.float64).cuda()
+    base = out.clone()
+    s = torch.cuda.current_stream().cuda_stream
+    nat.call("ffno_col_outer", A.data_ptr(), Ra, B.data_ptr(), Rb, ncol, C, rs, out.data_ptr(), 1, s)
+    torch.cuda.synchronize()
+    a = A[:, :ncol * C].double().reshape(Ra, ncol, C)
+    b = B[:, :ncol * C].double().reshape(Rb, ncol, C)
+    ref = torch.einsum("icx,jcx->cij", a, b)
+    bound = C * 2.0 ** -23 * torch.einsum("icx,jcx->cij", a.abs(), b.abs())
+    assert torch.all((out - base - ref).abs() <= bound + 1e-12)
+    nat.call("ffno_col_outer", A.data_ptr(), Ra, B.data_ptr(), Rb, ncol, C, rs, out.data_ptr(), 0, s)
+    torch.cuda.synchronize()
+    assert torch.all((out - ref).abs() <= bound + 1e-12)
