@@ -201,6 +201,107 @@ __global__ void __launch_bounds__(256) k_gn_bwd_stats(int mode, const float* __r
   }
 }
 
+// The statistics for eight groups and C <= 64 (cpg = C / 8 channels a group): lanes of 8 channels (one 32-byte request
+// a lane and tensor), whose channels fall in NG = 8 / cpg groups, so the partials are kept per group (one double pair
+// at C = 64) instead of per channel slot. Same partials layout and fixed reduction order as k_gn_bwd_stats.
+template <int C>
+__global__ void __launch_bounds__(256) k_gn_bwd_stats8(int mode, const float* __restrict__ u, float r,
+                                                       const float* __restrict__ pre, const float* __restrict__ gamma,
+                                                       const float* __restrict__ beta,
+                                                       const double* __restrict__ gst, long V,
+                                                       double* __restrict__ partials) {
+  static_assert(C == 16 || C == 32 || C == 64, "eight groups of C / 8 channels");
+  using Ln = GnLanes<C, 8>;
+  constexpr int VW = 8, CPG = C / GMAX, NG = VW / CPG;
+  __shared__ GnConst k;
+  __shared__ double red[8][GMAX][2];
+  load_gn_const(k, gst, nullptr, GMAX, 0.f);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / Ln::LPV, q = lane % Ln::LPV;   // every lane is active: LPV divides 32
+  const int c = VW * q, g0 = c / CPG;
+  float gm[VW], bt[VW];
+#pragma unroll
+  for (int j = 0; j < VW; ++j) {
+    gm[j] = __ldg(gamma + c + j);
+    bt[j] = __ldg(beta + c + j);
+  }
+  double d1[NG], d2[NG];
+  float f1[NG], f2[NG];
+#pragma unroll
+  for (int l = 0; l < NG; ++l) d1[l] = d2[l] = 0.0, f1[l] = f2[l] = 0.f;
+  const long step = (long)gridDim.x * 8 * Ln::VPW;
+  constexpr int UN = 2;   // voxels a thread loaded before any is used: 128 bytes in flight
+  int n = 0;
+  for (long v0 = ((long)blockIdx.x * 8 + warp) * Ln::VPW + sub; v0 < V; v0 += UN * step) {
+    float pu[UN][VW], pp[UN][VW];
+#pragma unroll
+    for (int e = 0; e < UN; ++e) {
+      const long v = v0 + e * step;
+      if (v < V) {
+        ffno::tc::ld8(u + v * C + c, pu[e]);
+        ffno::tc::ld8(pre + v * C + c, pp[e]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < VW; ++j) pu[e][j] = pp[e][j] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < UN; ++e) {
+      if (v0 + e * step >= V) break;
+#pragma unroll
+      for (int j = 0; j < VW; ++j) {
+        const int l = j / CPG, g = g0 + l;
+        const float xh = (pp[e][j] - k.mean[g]) * k.rstd[g];
+        const float gh = upstream(mode, pu[e][j], r, xh * gm[j] + bt[j]) * gm[j];
+        f1[l] += gh;
+        f2[l] += gh * xh;
+      }
+    }
+    if (++n == 8) {   // float partials go to double every 16 voxels, as in k_gn_bwd_stats
+#pragma unroll
+      for (int l = 0; l < NG; ++l) {
+        d1[l] += f1[l];
+        d2[l] += f2[l];
+        f1[l] = f2[l] = 0.f;
+      }
+      n = 0;
+    }
+  }
+#pragma unroll
+  for (int l = 0; l < NG; ++l) {
+    d1[l] += f1[l];
+    d2[l] += f2[l];
+  }
+  for (int g = 0; g < GMAX; ++g) {
+    double a = 0.0, b = 0.0;
+#pragma unroll
+    for (int l = 0; l < NG; ++l)
+      if (g0 + l == g) {
+        a += d1[l];
+        b += d2[l];
+      }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+      red[warp][g][0] = a;
+      red[warp][g][1] = b;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < GMAX) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < 8; ++w) {
+      a += red[w][threadIdx.x][0];
+      b += red[w][threadIdx.x][1];
+    }
+    partials[((long)blockIdx.x * GMAX + threadIdx.x) * 2] = a;
+    partials[((long)blockIdx.x * GMAX + threadIdx.x) * 2 + 1] = b;
+  }
+}
+
 __global__ void k_gn_bwd_final(const double* __restrict__ partials, int nparts, int groups, double* __restrict__ sums) {
   // one warp per group: strided partial sums per lane, then a fixed shuffle tree (deterministic)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -855,6 +956,16 @@ int ffno_gn_bwd_stats(int mode, const float* u, float r, const float* pre, const
   if (!width_ok(C) || V < 1 || groups < 1 || groups > GMAX || C % groups || nparts < 1) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   const int cpg = C / groups;
+  if (groups == GMAX && C <= 64 &&
+      (reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(pre)) % 32 == 0) {   // 32-byte lanes
+    switch (C) {
+#define L(CC) case CC: k_gn_bwd_stats8<CC><<<nparts, 256, 0, s>>>(mode, u, r, pre, gamma, beta, gstats, V, partials); break;
+      L(16) L(32) L(64)
+#undef L
+    }
+    FFNO_CHECK_LAUNCH();
+    return FFNO_OK;
+  }
   switch (C) {
 #define L(CC) case CC: k_gn_bwd_stats<CC><<<nparts, 256, 0, s>>>(mode, u, r, pre, gamma, beta, gstats, V, partials, cpg, groups); break;
     L(16) L(32) L(64) L(96)
