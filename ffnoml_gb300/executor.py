@@ -481,8 +481,13 @@ class Executor:
         runs, so no read-back synchronises the request's stream."""
         z = np.asarray(z_mm, dtype=np.float32)
         B, D = z.shape[0], z.shape[1]
-        zc = z.reshape(B, D, -1).transpose(0, 2, 1)              # [B][HW][D] view
-        return self.geometry_columns(zc, lambda: zc.astype(np.float64))
+        zd = z.reshape(B, D, -1)                                  # [B][D][HW]: reductions over D run along rows
+        mn = zd.min(axis=1)                                       # [B][HW]
+        span = float((zd.max(axis=1) - mn).max())
+        shifted = zd - mn[:, None, :]                             # float32, as ffno_column_info compares them
+        shared_each = all(bool((shifted[b] == shifted[b, :, :1]).all()) for b in range(B))
+        zc = zd.transpose(0, 2, 1)                                # [B][HW][D] view
+        return self._geometry(shared_each, span, np.ascontiguousarray(zc[:, 0, :]), lambda: zc.astype(np.float64))
 
     def geometry_columns(self, zc, columns):
         """geometry_host from columns: zc [B][N][D] float32, every sample's N = H*W columns in any order with column
@@ -599,10 +604,19 @@ class Executor:
             if keep:
                 saved.append(inputs)
                 states.append(blocks)
-        self._check(ws)
-        state = dict(x=x, z=z_scale, dx=dx, dy=dy, inputs=saved, geo=geo, blocks=states if cache else None) \
-            if keep else None
+        if not keep:
+            self._check(ws)
+            return out, None
+        # a forward kept for the VJP leaves its error flag to the backward, which reads it with its own at the end
+        # (one synchronisation for both passes; the flag is sticky): callers that may not run the backward call
+        # check_forward
+        state = dict(x=x, z=z_scale, dx=dx, dy=dy, inputs=saved, geo=geo, blocks=states if cache else None,
+                     err=ws.err)
         return out, state
+
+    def check_forward(self, state):
+        """Raise if the forward that made `state` (forward(keep=True)) ran out of a bounded wait."""
+        self._check_flag(state["err"])
 
     @staticmethod
     def _fits(nbytes, device):
@@ -613,7 +627,11 @@ class Executor:
 
     @staticmethod
     def _check(ws):
-        if m_err := int(ws.err.item()):
+        Executor._check_flag(ws.err)
+
+    @staticmethod
+    def _check_flag(err):
+        if m_err := int(err.item()):
             raise nat.NativeError(f"a tensor-core kernel's bounded wait ran out (code {m_err})")
 
     def _depth_weights(self, ws, z, D, HW):
@@ -953,6 +971,8 @@ class Executor:
             gcol = tb.height_tables_vjp(geo.column_raw, geo.length, geo.k, live, host_f.numpy(), host_i.numpy())
             zbar[0, :, 0, 0] += torch.as_tensor(gcol, dtype=torch.float32).to(dev)
         self._check(ws)
+        if state.get("err") is not None:
+            self._check_flag(state["err"])
         return xbar_in, zbar
 
     def _gn_bwd(self, ws, gb, mode, u, r, pre, gamma, beta, name, pbar):
@@ -1138,6 +1158,7 @@ class _FFNOFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, z_scale, executor, dx, dy):
         y, state = executor.forward(x, z_scale, dx, dy, keep=True)
+        executor.check_forward(state)        # the caller may never run the backward
         ctx.executor = executor
         ctx.state = state
         return y
