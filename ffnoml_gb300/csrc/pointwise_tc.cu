@@ -1213,7 +1213,7 @@ __global__ void __launch_bounds__(CT, 1) k_head_tc(const float* __restrict__ x, 
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
     if (P.ptid == 0 && pf > 0) prefetch_rows(x, (t + pf * tstep) * TM, V, C);
-    fill_tile<C>(X, v0, V, P.ptid, [&](long v, int k) { return ld4(x + v * C + k); });
+    fill_tile8<C>(X, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(x + v * C + k, o); });
     if (!pipe_gemms(P, err, Gemm{P.tmem, w1, kop(X, C), C, false})) break;
 #pragma unroll 1
     for (int c = 0; c < 4; ++c) {
@@ -1274,7 +1274,7 @@ __global__ void __launch_bounds__(CT, 1) k_head_bwd_tc(const float* __restrict__
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
     if (P.ptid == 0 && pf > 0) prefetch_rows(x, (t + pf * tstep) * TM, V, C);
-    fill_tile<C>(X, v0, V, P.ptid, [&](long v, int k) { return ld4(x + v * C + k); });
+    fill_tile8<C>(X, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(x + v * C + k, o); });
     if (!pipe_gemms(P, err, Gemm{P.tmem, w1, kop(X, C), C, false})) break;
 #pragma unroll 1
     for (int c = 0; c < 4; ++c) {
@@ -1603,6 +1603,7 @@ int ffno_head_fwd_tc(const float* x, const float* x_in, long V, int C, const voi
                      int nhp, const ffno_head_params* params, float* out, float* head_out, int* err,
                      ffno_stream_t stream) {
   if (!tc_width(C) || V < 1 || !x || !x_in || !wpack || !b2 || !out || !err || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!aligned32(x)) return FFNO_EINVAL;   // the hidden rows are read 32 bytes a request
   if (!head_ok(params, nh, nhp)) return FFNO_EINVAL;
   const uint8_t* w = static_cast<const uint8_t*>(wpack);
   cudaStream_t s = (cudaStream_t)stream;
@@ -1617,7 +1618,7 @@ int ffno_head_bwd_tc(const float* x, const float* x_in, const float* y_bar, long
                      const float* b2, int nhp, const ffno_head_params* params, float* x_bar, float* x_in_bar,
                      int* err, ffno_stream_t stream) {
   if (!tc_width(C) || V < 1 || !x || !x_in || !y_bar || !wpack || !b2 || !x_bar || !x_in_bar || !err ||
-      !aligned16(wpack))
+      !aligned16(wpack) || !aligned32(x))
     return FFNO_EINVAL;
   if (!head_ok(params, -1, nhp)) return FFNO_EINVAL;
   const uint8_t* w = static_cast<const uint8_t*>(wpack);

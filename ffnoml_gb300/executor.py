@@ -590,14 +590,18 @@ class Executor:
                 self.last_cached = cache
             xin, z = x[b], z_scale[b]
             self._depth_weights(ws, z, D, H * W)
+            # a kept forward writes the lift output and every block output straight into the saved block inputs
+            # (block i reads inputs[i] and writes inputs[i + 1] through ws.x), so nothing is copied to keep them
+            inputs = [torch.empty_like(ws.x) for _ in range(m.n_layers + 1)] if keep else None
+            if keep:
+                ws.x = inputs[0]
             self._lift(pk, ws, xin)
-            inputs = [ws.x.clone()] if keep else None
             blocks = [] if cache else None
             for i in range(m.n_layers):
-                wb = ws.fork(self._tc()) if cache else ws
-                self._block(pk, wb, i, z, D, H, W, hgt_b, pln, pfr[i])
                 if keep:
-                    inputs.append(ws.x.clone())
+                    ws.x = inputs[i + 1]
+                wb = ws.fork(self._tc()) if cache else ws
+                self._block(pk, wb, i, z, D, H, W, hgt_b, pln, pfr[i], x_in=inputs[i] if keep else None)
                 if cache:
                     blocks.append(wb)
             self._head(pk, ws.x, xin, out[b], ws.err)

@@ -202,12 +202,19 @@ class GB300Backend:
             dev.copy_(torch.from_numpy(src))
         return dev
 
+    def _download(self, key, tensor):
+        """Queue the copy of a result into this thread's pinned buffer for it (reused across calls)."""
+        host, _ = self._stage(key + "_out", tensor.shape)
+        host.copy_(tensor, non_blocking=True)
+        return host
+
     @staticmethod
-    def _fetch(tensor):
-        """The call's result as a fresh numpy array: the copy waits for the stream's work and writes the device data
-        straight into the array's (pageable) memory."""
-        out = np.empty(tuple(tensor.shape), dtype=np.float32)
-        torch.from_numpy(out).copy_(tensor)
+    def _result(host):
+        """A fresh numpy copy of a pinned result buffer (the buffer is reused by the next call). The fresh array's
+        pages are first written here, on several host threads; a device copy straight into it would fault them in
+        one at a time inside the copy."""
+        out = np.empty(tuple(host.shape), dtype=np.float32)
+        _host_copy(out, host.numpy())
         return out
 
     def _validate(self, features, z_scale):
@@ -378,10 +385,10 @@ class GB300Backend:
         pop = torch.empty(*z_scale.shape, L, dtype=torch.float32, device=self.device)
         nat.call("ffno_si_populations", y.data_ptr(), V, L, self.mean_y.data_ptr(), self.std_y.data_ptr(),
                  pop.data_ptr(), self._out_flags(), _stream())
-        out = self._fetch(pop)
+        host = self._download("pop", pop)
         _check(self._finish(), "FFNO output")
         self.call_count += 1
-        return out
+        return self._result(host)
 
     def jvp_local(self, features, z_scale, dx, dy, feature_tangent):
         """Forward-mode derivative of the populations along feature_tangent (6,nz,nx,ny) in the SI units of features
@@ -403,7 +410,7 @@ class GB300Backend:
         pop_dot = torch.empty(*z_scale.shape, L, dtype=torch.float32, device=self.device)
         nat.call("ffno_si_population_tangent", y.data_ptr(), y_dot.data_ptr(), V, L, self.mean_y.data_ptr(),
                  self.std_y.data_ptr(), pop_dot.data_ptr(), self._out_flags(), _stream())
-        out = self._fetch(pop_dot)
+        host = self._download("pop_dot", pop_dot)
         flags = self._finish()
         if flags & 1:
             raise ValueError("FFNO JVP tangent contains NaN or Inf")
@@ -411,7 +418,7 @@ class GB300Backend:
             raise RuntimeError("FFNO JVP returned NaN or Inf")
         _check(flags, "FFNO JVP")
         self.call_count += 1
-        return out
+        return self._result(host)
 
     def vjp_local(self, features, z_scale, dx, dy, population_cotangent):
         """Input VJP along the population cotangent (nz,nx,ny,L): {"features": (6,nz,nx,ny), "z_scale": (nz,nx,ny)}
@@ -443,10 +450,10 @@ class GB300Backend:
         zbar_m = torch.empty(*z_scale.shape, dtype=torch.float32, device=self.device)
         nat.call("ffno_si_input_grads", f_dev.data_ptr(), xbar.data_ptr(), zbar.data_ptr(), V,
                  self.std_x.data_ptr(), fbar.data_ptr(), zbar_m.data_ptr(), self._out_flags(), _stream())
-        hf, hz = self._fetch(fbar), self._fetch(zbar_m)
+        hf, hz = self._download("fbar", fbar), self._download("zbar", zbar_m)
         flags = self._finish()
         if flags & 1:
             raise ValueError("FFNO VJP cotangent contains NaN or Inf")
         _check(flags, "FFNO VJP")
         self.call_count += 1
-        return {"features": hf, "z_scale": hz}
+        return {"features": self._result(hf), "z_scale": self._result(hz)}
