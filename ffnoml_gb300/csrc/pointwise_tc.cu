@@ -75,8 +75,9 @@ __device__ __forceinline__ bool load_weights(void* dst, const void* src, uint32_
 }
 
 // Tiles of L2 prefetch lookahead per pipeline: at tile t a pipeline prefetches the inputs of its tile t + c_pf steps
-// ahead (0: none). Set by ffno_tc_set_prefetch_tiles.
-__constant__ int c_pf = 1;
+// ahead (0: none, the default: with 32-byte row requests the prefetched lines only added DRAM traffic). Set by
+// ffno_tc_set_prefetch_tiles.
+__constant__ int c_pf = 0;
 
 // L2 prefetch of rows [n0, n0 + 128) of a [V][width] FP32 array, by one thread
 __device__ __forceinline__ void prefetch_rows(const float* base, long n0, long V, int width) {

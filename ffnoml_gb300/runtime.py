@@ -192,14 +192,12 @@ class GB300Backend:
         return t[:n]
 
     def _upload(self, key, array):
-        """A device copy of a host array, in a device buffer reused across calls. The copy reads the caller's memory
-        directly: on a GB300 node the GPU reaches pageable host memory at nearly the pinned rate (about 170 against
-        210 GB/s), so staging through a pinned buffer would only add a host copy before the model can start."""
-        dev = self._dev_buffer(key, array.size).view(array.shape)
-        src = np.ascontiguousarray(array, dtype=np.float32)
-        with warnings.catch_warnings():   # read-only caller arrays are only read
-            warnings.simplefilter("ignore", UserWarning)
-            dev.copy_(torch.from_numpy(src))
+        """A device copy of a host array: the array is copied into this thread's pinned buffer on several host
+        threads, then to the device by the copy engine. (A copy straight from the caller's pageable memory measured
+        slower per call on a GB300 node: 15 against 3 ms for a request's 117 MB of inputs.)"""
+        host, dev = self._stage(key, array.shape)
+        _host_copy(host.numpy(), array)
+        dev.copy_(host, non_blocking=True)
         return dev
 
     def _download(self, key, tensor):

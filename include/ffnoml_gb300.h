@@ -335,7 +335,7 @@ int ffno_si_input_grads(const float* features, const float* x_bar, const float* 
 int ffno_tc_parts(long V);
 int ffno_tc_width_supported(int C);
 /* L2 prefetch lookahead of the tensor-core pointwise kernels on the current device, in tiles of 128 voxels per
- * pipeline (0..4; default 1): a tuning knob, synchronous, not to be called while those kernels run. */
+ * pipeline (0..4; default 0): a tuning knob, synchronous, not to be called while those kernels run. */
 int ffno_tc_set_prefetch_tiles(int tiles);
 
 /* ffno_mlp2_fwd; wpack = [w1 (2C x C), w2 (C x 2C)]. */
