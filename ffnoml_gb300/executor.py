@@ -482,12 +482,17 @@ class Executor:
         z = np.asarray(z_mm, dtype=np.float32)
         B, D = z.shape[0], z.shape[1]
         zd = z.reshape(B, D, -1)                                  # [B][D][HW]: reductions over D run along rows
+        zc = zd.transpose(0, 2, 1)                                # [B][HW][D] view
+        col0 = np.ascontiguousarray(zc[:, 0, :])                  # [B][D]
+        if bool((zd == zd[:, :, :1]).all()):
+            # every column equals its sample's column (0, 0): shared grids, one pass over the heights
+            span = float((col0.max(axis=1) - col0.min(axis=1)).max())
+            return self._geometry(True, span, col0, lambda: zc.astype(np.float64))
         mn = zd.min(axis=1)                                       # [B][HW]
         span = float((zd.max(axis=1) - mn).max())
         shifted = zd - mn[:, None, :]                             # float32, as ffno_column_info compares them
         shared_each = all(bool((shifted[b] == shifted[b, :, :1]).all()) for b in range(B))
-        zc = zd.transpose(0, 2, 1)                                # [B][HW][D] view
-        return self._geometry(shared_each, span, np.ascontiguousarray(zc[:, 0, :]), lambda: zc.astype(np.float64))
+        return self._geometry(shared_each, span, col0, lambda: zc.astype(np.float64))
 
     def geometry_columns(self, zc, columns):
         """geometry_host from columns: zc [B][N][D] float32, every sample's N = H*W columns in any order with column
