@@ -40,7 +40,7 @@ STD_X = np.array([2.5 / math.sqrt(12), 5.0, 5.0, 5.0, 7.0 / math.sqrt(12), 8.0 /
 CPU_SAMPLE = (64, 32, 32)       # sub-cube per step of the reference arm and of cpu_baseline (same C, L, M)
 CONFIG4 = (496, 252, 252)       # the full-volume inversion step (31.5 M voxels)
 STREAM_CHUNKS = (32, 16)        # depth planes / column rows per device slab of the host-RAM streaming forward
-KERNELS_PER_CALL = {"ffno_column_info": 3, "ffno_outer": 2}
+KERNELS_PER_CALL = {"ffno_column_info": 3, "ffno_outer": 2, "ffno_outer_tc": 2, "ffno_outer_tc_ld": 2}
 METRIC = "FFNO3D voxels/s fwd & fwd+VJP, BF16 vs FP32 @ |\u0394log n|\u22642e-3; p50/p99 latency"
 
 
@@ -555,6 +555,13 @@ def run_gb300(args):
         del mp, exp, hp
         torch.cuda.empty_cache()
 
+    # the production model (width 96, 4 blocks, hidden 128, M = 1001, H: the reference's MODEL_CONFIG defaults) on the
+    # same cube, fwd+VJP in both precisions: at width 96 the "bf16" form runs the transforms and table gradients on
+    # the tensor cores and the channel kernels in FP32
+    production = None
+    if not args.no_production and not args.fwd_only:
+        production = production_run(x, z, dev, world, timed)
+
     # per-column height grids (every column its own heights: the height operator's non-shared path) on the same
     # cube: the per-column tables built on the device once (timed alone), then fwd+VJP steps with them, the tables'
     # gradient for every column included
@@ -606,11 +613,62 @@ def run_gb300(args):
             "clocks": clocks, "memory": memory, "gpu_launches": launches * args.steps, "e2e": e2e,
             "cpu_baseline": cpu,
             "serving": serving, "streaming": streaming, "population_mesh": mesh_maps,
-            "variant_p": variant_p, "per_column": per_column, "config4": config4,
+            "variant_p": variant_p, "per_column": per_column, "config4": config4, "production": production,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def entry_breakdown(step, top):
+    """CUDA-event milliseconds per entry point (tagged per call site) over one run of step(): the `top` largest."""
+    import torch
+    from ffnoml_gb300 import _native as nat
+    nat.counter.timing = []
+    step()
+    torch.cuda.synchronize()
+    per = {}
+    for name, e0, e1, _ in nat.counter.timing:
+        per[name] = per.get(name, 0.0) + e0.elapsed_time(e1)
+    nat.counter.timing = None
+    return {k: round(v, 2) for k, v in sorted(per.items(), key=lambda kv: -kv[1])[:top]}
+
+
+def production_run(x, z, dev, world, timed):
+    """fwd+VJP of the production model (create_ffno3d defaults: width 96, 4 blocks, M = 1001, H atom) on the cube
+    x, z, 2 timed steps in FP32 and in "bf16" (transforms and height-table gradients on tensor cores, channel kernels
+    FP32 at this width), with the largest |d log10 n| between the two forwards."""
+    import torch
+    from ffnoml_gb300 import create_ffno3d
+    torch.manual_seed(5)
+    m = create_ffno3d(6, 6).to(dev).eval()
+    with torch.no_grad():
+        for name, p in m.named_parameters():
+            if ".freq_u." in name:
+                p.normal_(0.0, 0.1)
+    m.set_normalization(MEAN_X, STD_X, np.zeros(6), np.ones(6))
+    D, H, W = x.shape[2:]
+    V = D * H * W
+    cot = torch.randn((1, 6, D, H, W), generator=torch.Generator(dev).manual_seed(21), device=dev)
+    ex = m.executor()
+    out = {"model": "width 96, 4 blocks, hidden 128, M = 1001, H (6 levels)", "shape": [D, H, W]}
+    ys = {}
+    step = lambda: ex.backward(ex.forward(x, z, DXY, DXY, keep=True)[1], cot)
+    for prec in ("fp32", "bf16"):
+        m.set_precision(prec)
+        ms, _ = timed(step, 2, 1)
+        out[prec] = {"value": job_rate(V, world, ms / 1e3), "unit": "voxels/s", "ms_per_step": ms, "pass": "fwd+vjp",
+                     "top_entries_ms": entry_breakdown(step, 8)}
+        with torch.no_grad():
+            ys[prec] = ex.forward(x, z, DXY, DXY)[0]
+    hp = ex.height(ex.packed(dev), ex.geometry(z), dev)
+    out["live_modes"] = int(hp["live"])
+    out["channel_kernels_on_tensor_cores"] = bool(ex.packed(dev).tc)
+    out["bf16_speedup"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
+    out["max_abs_dlog10n_bf16_vs_fp32"] = float((ys["bf16"] - ys["fp32"]).abs().max())
+    del m, ex, ys, hp, cot
+    torch.cuda.empty_cache()
+    return out
 
 
 def config4_run(model, ex, dev, world, rank, timed):
@@ -751,6 +809,8 @@ def main():
     ap.add_argument("--no-streaming", action="store_true", help="skip the host-RAM streaming forward")
     ap.add_argument("--no-config4", action="store_true", help="skip the full-volume [1,6,496,252,252] step")
     ap.add_argument("--no-variant-p", action="store_true", help="skip the production band limit (M = 1001) step")
+    ap.add_argument("--no-production", action="store_true",
+                    help="skip the production model (width 96, M = 1001) steps")
     ap.add_argument("--no-per-column", action="store_true", help="skip the per-column height grid step")
     ap.add_argument("--serve-requests", type=int, default=256)
     args = ap.parse_args()

@@ -113,6 +113,7 @@ PROTOTYPES = {
     "ffno_fuse_bwd_a_tc": [P, P, P, P, P, P, L, I, P, P, P, P],
     "ffno_fuse_bwd_b_tc": [P, P, P, P, P, P, P, P, P, L, I, P, P, P, P, P, P],
     "ffno_outer_tc": [P, L, I, P, L, I, L, P, I, P, I, P, P],
+    "ffno_outer_tc_ld": [P, L, I, P, L, I, L, P, I, P, L, I, P, P],
     "ffno_head_fwd_tc": [P, P, L, I, P, P, I, I, ctypes.POINTER(HeadParams), P, P, P, P],
     "ffno_head_bwd_tc": [P, P, P, L, I, P, P, I, ctypes.POINTER(HeadParams), P, P, P, P],
     "ffno_gn_jvp_stats": [P, P, P, P, L, I, I, P, I, P],

@@ -782,14 +782,16 @@ __global__ void __launch_bounds__(OT, 1) k_outer_tc(const float* __restrict__ A,
   if (warp == 0) tc::tmem_free(tmem, ncol);
 }
 
-__global__ void k_outer_tc_reduce(const float* __restrict__ part, long nsplit, long n, double* __restrict__ out,
-                                  int accumulate) {
+// part [nsplit][rows][cols] -> out rows of stride ldo (ldo = cols: out is the contiguous [rows][cols] product)
+__global__ void k_outer_tc_reduce(const float* __restrict__ part, long nsplit, long n, long cols, long ldo,
+                                  double* __restrict__ out, int accumulate) {
   const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (e >= n) return;
   double s = 0.0;
 #pragma unroll 8
   for (long p = 0; p < nsplit; ++p) s += (double)part[p * n + e];   // loads issued ahead, sums in order
-  out[e] = accumulate ? out[e] + s : s;
+  double* o = out + (e / cols) * ldo + e % cols;
+  *o = accumulate ? *o + s : s;
 }
 
 int g_sms = 0;
@@ -936,7 +938,12 @@ int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, 
 
 int ffno_outer_tc(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, float* part, int nsplit,
                   double* out, int accumulate, int* err, ffno_stream_t stream) {
-  if (!A || !B || !part || !out || !err || Ma < 1 || Mb < 1 || N < 1 || nsplit < 1) return FFNO_EINVAL;
+  return ffno_outer_tc_ld(A, lda, Ma, B, ldb, Mb, N, part, nsplit, out, Mb, accumulate, err, stream);
+}
+
+int ffno_outer_tc_ld(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, float* part,
+                     int nsplit, double* out, long ldo, int accumulate, int* err, ffno_stream_t stream) {
+  if (!A || !B || !part || !out || !err || Ma < 1 || Mb < 1 || N < 1 || nsplit < 1 || ldo < Mb) return FFNO_EINVAL;
   if (N % 4 || lda % 4 || ldb % 4 || lda < N || ldb < N || (reinterpret_cast<uintptr_t>(A) % 16) ||
       (reinterpret_cast<uintptr_t>(B) % 16))
     return FFNO_EINVAL;   // float4 loads that never straddle the end of a row
@@ -959,7 +966,7 @@ int ffno_outer_tc(const float* A, long lda, int Ma, const float* B, long ldb, in
     k_outer_tc<<<nsplit, OT, smem, s>>>(B, ldb, Mb, A, lda, Ma, N, TI, NB, NS, cps, part, n, 1, Mb, err);
   else
     k_outer_tc<<<nsplit, OT, smem, s>>>(A, lda, Ma, B, ldb, Mb, N, TI, NB, NS, cps, part, n, Mb, 1, err);
-  k_outer_tc_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(part, nsplit, n, out, accumulate);
+  k_outer_tc_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(part, nsplit, n, Mb, ldo, out, accumulate);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

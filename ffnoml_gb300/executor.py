@@ -421,8 +421,16 @@ class Executor:
             live, tzf, tzi = int(t["live"]), t["tzf"], t["tzi"]
             per_block = [FreqTables(*gv, device) for gv in table_store.freq_list(t, n)]
             f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device=device)
+            # what the tables' gradient w.r.t. the shared column takes (ffno_percol_tables_vjp with one column):
+            # the column, its live wavenumbers, mode factors, their derivative in the median spacing and its index
+            vlive, fcol, dfcol, med = tb.percolumn_prep(np.asarray(geo.column, np.float64)[None], geo.length, geo.k)
+            if vlive != live:
+                raise RuntimeError("height table live-mode counts disagree")
+            f64 = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=device)
+            vjp = dict(z=f64(np.asarray(geo.column, np.float64)[None]), k=f64(geo.k.numpy()[:live]), f=f64(fcol),
+                       df=f64(dfcol), med=torch.as_tensor(med, dtype=torch.int32, device=device))
             self._height[key] = dict(live=live, tzf=f(tzf), tzi=f(tzi), tzf_t=f(tzf.T), tzi_t=f(tzi.T),
-                                     freq=per_block, np=dict(tzf=tzf, tzi=tzi), device=device)
+                                     freq=per_block, np=dict(tzf=tzf, tzi=tzi), vjp=vjp, device=device)
         return self._height[key]
 
     def tc_table(self, tabs, name):
@@ -437,7 +445,7 @@ class Executor:
     def _xf(self, tabs, name, inp, out, desc, ws):
         """out = T_name applied by ffno_xform (FP32) or ffno_xform_tc (split-BF16 tensor cores)."""
         s = _stream()
-        if not self._tc():
+        if not self._tc_xf():
             nat.call("ffno_xform", tabs[name].data_ptr(), inp.data_ptr(), out.data_ptr(), desc, 0, s, tag=name)
             return
         tx = self.tc_table(tabs, name)
@@ -746,20 +754,39 @@ class Executor:
     def _outer(self, ws, a, ma, b, mb, n, part, nsplit, out):
         """out [ma][mb] += a [ma][n] @ b [mb][n]^T (double): a height-transform table's gradient. The tensor-core
         kernel holds the longer side in 128-row tiles and the shorter (rounded up to 16) as the MMA's N, at most 512
-        accumulator columns in all; larger products (production height grids) run on the FP32 kernel."""
-        lo, hi = min(ma, mb), max(ma, mb)
-        fits = (lo + 15) // 16 * 16 <= 256 and (hi + 127) // 128 * ((lo + 15) // 16 * 16) <= 512
-        if self._tc() and fits:
-            nat.call("ffno_outer_tc", a.data_ptr(), n, ma, b.data_ptr(), n, mb, n, part.data_ptr(), nsplit,
-                     out.data_ptr(), 1, ws.err.data_ptr(), _stream())
-        else:
-            nat.call("ffno_outer", a.data_ptr(), n, ma, b.data_ptr(), n, mb, n, part.data_ptr(), nsplit,
-                     out.data_ptr(), 1, _stream())
+        accumulator columns in all; a longer product (a production height grid: 2 M' = 680 rows at D = 256) runs as
+        slices of the longer side, each its own call into its rows or columns of out. A shorter side above 256 runs on
+        the FP32 kernel."""
+        plan = _outer_tc_slices(ma, mb)
+        s = _stream()
+        if self._tc_xf() and plan is not None:
+            if len(plan) == 1:
+                nat.call("ffno_outer_tc", a.data_ptr(), n, ma, b.data_ptr(), n, mb, n, part.data_ptr(), nsplit,
+                         out.data_ptr(), 1, ws.err.data_ptr(), s)
+                return
+            for r0, rows in plan:
+                if ma >= mb:      # slices of a: rows r0 .. r0 + rows of out
+                    pa, sa, pb, sb, po = a.data_ptr() + 4 * r0 * n, rows, b.data_ptr(), mb, out.data_ptr() + 8 * r0 * mb
+                else:             # slices of b: columns r0 .. r0 + rows of out
+                    pa, sa, pb, sb, po = a.data_ptr(), ma, b.data_ptr() + 4 * r0 * n, rows, out.data_ptr() + 8 * r0
+                ns = max(1, min(_sm_count(out.device), part.numel() // (sa * sb), (n + 1023) // 1024))
+                nat.call("ffno_outer_tc_ld", pa, n, sa, pb, n, sb, n, part.data_ptr(), ns, po, mb, 1,
+                         ws.err.data_ptr(), s)
+            return
+        nat.call("ffno_outer", a.data_ptr(), n, ma, b.data_ptr(), n, mb, n, part.data_ptr(), nsplit,
+                 out.data_ptr(), 1, s)
 
     def _tc(self):
         """Whether the split-BF16 tensor-core kernels run (precision 'bf16' at a width they support; never inside a
         JVP, which is FP32)."""
         return self.model.precision == "bf16" and self._packed.tc and not getattr(self._tls, "fp32", False)
+
+    def _tc_xf(self):
+        """Whether the transforms and the height-table gradients run on the split-BF16 tensor-core kernels: precision
+        'bf16' at any width (their operands are tables and data columns, not channel matrices), never inside a JVP.
+        At a width the channel kernels do not support (96, the production model) the rest of the model stays on the
+        FP32 kernels."""
+        return self.model.precision == "bf16" and not getattr(self._tls, "fp32", False)
 
     def _fuse1_tc(self, ws, bp, x, hg):
         m = self.model
@@ -917,14 +944,6 @@ class Executor:
             live = hgt["live"]
             tzf_bar = torch.zeros(2 * live, D, dtype=torch.float64, device=dev)
             tzi_bar = torch.zeros(D, 2 * live, dtype=torch.float64, device=dev)
-            host_f = torch.empty(tzf_bar.shape, dtype=torch.float64, pin_memory=True)
-            host_i = torch.empty(tzi_bar.shape, dtype=torch.float64, pin_memory=True)
-            copied = torch.cuda.Event()
-
-            def tables_out():
-                host_f.copy_(tzf_bar, non_blocking=True)
-                host_i.copy_(tzi_bar, non_blocking=True)
-                copied.record()     # on the current stream, which every kernel of this backward runs on
         for b in range(B):
             hgt_b = hgt if geo.shared else self.height_percol(pk, geo, b, dev)
             live = hgt_b["live"]
@@ -958,11 +977,7 @@ class Executor:
                 else:
                     wb = ws
                     self._block(pk, ws, i, z, D, H, W, hgt_b, pln, pfr[i], x_in=inputs[i])
-                # the shared tables' gradients are complete after the last block's height-table products: copy them
-                # out there, so that their host-side finish overlaps the rest of the backward
-                done = tables_out if geo.shared and b == B - 1 and i == 0 else None
-                self._block_bwd(pk, wb, gb, i, inputs[i], z, zbar[b], D, H, W, hgt_b, pln, pfr[i], tzf_bar, tzi_bar,
-                                done)
+                self._block_bwd(pk, wb, gb, i, inputs[i], z, zbar[b], D, H, W, hgt_b, pln, pfr[i], tzf_bar, tzi_bar)
             # lift: x0 = gelu(GN(pre0))
             self._lift(pk, ws, xin)
             self._gn_bwd(ws, gb, 1, gb.xbar, 1.0, ws.pre, pk.lift_g, pk.lift_b, "lift", gb.pbar)
@@ -975,10 +990,14 @@ class Executor:
                          tzi_bar.data_ptr(), zbar[b].data_ptr(), s)
         if geo.shared:
             # the height tables depend on the shared column (sample 0, column (0, 0)): their gradient goes there,
-            # finished on the host (float64 autograd through the table builder) while the device runs the lift
-            copied.synchronize()
-            gcol = tb.height_tables_vjp(geo.column_raw, geo.length, geo.k, live, host_f.numpy(), host_i.numpy())
-            zbar[0, :, 0, 0] += torch.as_tensor(gcol, dtype=torch.float32).to(dev)
+            # on the device in FP64 (the per-column table gradient with one column), so the backward never waits
+            # for the host
+            hv = hgt["vjp"]
+            gcol = torch.zeros(D, dtype=torch.float32, device=dev)
+            nat.call("ffno_percol_tables_vjp", hv["z"].data_ptr(), D, 1, hv["k"].data_ptr(), hgt["live"],
+                     hv["f"].data_ptr(), hv["df"].data_ptr(), hv["med"].data_ptr(), tzf_bar.data_ptr(),
+                     tzi_bar.data_ptr(), gcol.data_ptr(), s)
+            zbar[0, :, 0, 0] += gcol
         self._check(ws)
         if state.get("err") is not None:
             self._check_flag(state["err"])
@@ -995,7 +1014,7 @@ class Executor:
                  ws.gstats[name].data_ptr(), gb.sums.data_ptr(), ws.dw.data_ptr(), V, C, G, EPS, pbar.data_ptr(),
                  gb.wbar.data_ptr(), s)
 
-    def _block_bwd(self, pk, ws, gb, i, x, z, zbar, D, H, W, hgt, pln, fq, tzf_bar, tzi_bar, tables_done=None):
+    def _block_bwd(self, pk, ws, gb, i, x, z, zbar, D, H, W, hgt, pln, fq, tzf_bar, tzi_bar):
         """gb.xbar (gradient of the block output) -> gb.xbar (gradient of the block input x); accumulates the
         depth-weight gradient in gb.wbar, the z_proj gradient in zbar and the height-table gradients."""
         m = self.model
@@ -1074,8 +1093,6 @@ class Executor:
             self._xf(hgt, "tzi_t", gb.yvb, ws.va, d["zf"], ws)
             self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, True)
             self._outer(ws, ws.vb, 2 * live, ws.xv, D, N, gb.opart, gb.osplit_f, tzf_bar)
-            if tables_done:
-                tables_done()
             self._xf(hgt, "tzf_t", ws.vb, gb.xvb, d["zi"], ws)
         # input gates (and z_proj)
         if tc:
@@ -1108,7 +1125,11 @@ class _GradBuffers:
         lib = nat.lib()
         self.osplit_i = lib.ffno_outer_parts(D, 2 * live, N)
         self.osplit_f = lib.ffno_outer_parts(2 * live, D, N)
-        self.opart = torch.empty(max(self.osplit_i, self.osplit_f) * D * 2 * live, **f32)
+        need = max(self.osplit_i, self.osplit_f) * D * 2 * live
+        plan = _outer_tc_slices(D, 2 * live)
+        if plan is not None and len(plan) > 1:      # one split per SM for each sliced tensor-core call
+            need = max(need, _sm_count(device) * max(r for _, r in plan) * min(D, 2 * live))
+        self.opart = torch.empty(need, **f32)
 
 
 class _TangentBuffers:
@@ -1131,6 +1152,32 @@ class _TangentBuffers:
         self.parts = torch.empty(max(nparts, 1) * groups * 2, dtype=torch.float64, device=device)
         self.sums = torch.empty(groups * 2, dtype=torch.float64, device=device)
         self.scratch_parts = torch.empty(max(nparts, 1) * groups * 3, dtype=torch.float64, device=device)
+
+
+def _outer_tc_slices(ma, mb):
+    """The calls ffno_outer_tc makes of an [ma][mb] product: (first row, rows) of the longer side per call, TI tiles of
+    128 rows each, NB = the shorter side rounded up to 16 (the MMA's N), with TI NB <= 512 accumulator columns and
+    one k-chunk stage of (128 TI + NB) x 64 split-BF16 operands within shared memory ((128 TI + NB) <= 900); None when
+    the shorter side exceeds 256."""
+    lo, hi = min(ma, mb), max(ma, mb)
+    nb = (lo + 15) // 16 * 16
+    if nb > 256:
+        return None
+    rows = 128 * min(512 // nb, (900 - nb) // 128)
+    return [(r0, min(rows, hi - r0)) for r0 in range(0, hi, rows)]
+
+
+_SMS = {}
+
+
+def _sm_count(device):
+    device = torch.device(device)
+    if device.type != "cuda":
+        return 1
+    idx = device.index if device.index is not None else torch.cuda.current_device()
+    if idx not in _SMS:
+        _SMS[idx] = torch.cuda.get_device_properties(idx).multi_processor_count
+    return _SMS[idx]
 
 
 def _descs(D, H, W, C, live):

@@ -411,6 +411,10 @@ int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, 
  * the shorter of Ma, Mb at most 256. */
 int ffno_outer_tc(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, float* part, int nsplit,
                   double* out, int accumulate, int* err, ffno_stream_t stream);
+/* ffno_outer_tc writing out rows of stride ldo >= Mb (a block of columns of a wider product): the gradient of a
+ * production height table (2 M' up to ~1300 rows) taken in slices of the longer operand that fit the accumulator. */
+int ffno_outer_tc_ld(const float* A, long lda, int Ma, const float* B, long ldb, int Mb, long N, float* part,
+                     int nsplit, double* out, long ldo, int accumulate, int* err, ffno_stream_t stream);
 
 /* ---- per-column height tables (HeightSpectralConv's non-shared path, models/ffno_model.py:276-280, 306-308), FP64
  * arithmetic. Column c has heights z_raw[c][0..D) (unshifted); k[0..live) the live wavenumbers; f[c][m] = factor_m

@@ -362,3 +362,33 @@ def test_outer_tc(Ma, Mb, N, nsplit):
     assert err.item() == 0
     _close(out - 0.5, ref, 2e-5)
     _close(out32, ref, 2e-5)
+
+
+@pytest.mark.parametrize("ma,mb,calls", [(256, 680, 3), (680, 256, 3), (64, 1300, 2), (200, 200, 1)])
+def test_outer_tc_in_slices(ma, mb, calls):
+    """The executor's height-table gradient product at production sizes (2 M' = 680 rows at D = 256): sliced calls of
+    ffno_outer_tc_ld along the longer side, into rows of out (ma longer) or into columns at row stride mb (mb longer),
+    accumulated onto what out holds, against a float64 product; and the unsliced single call at (200, 200)."""
+    from ffnoml_gb300.executor import Executor, _outer_tc_slices
+
+    class _WS:
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    class _Model:
+        precision = "bf16"
+
+    ex = Executor.__new__(Executor)
+    ex.model = _Model()
+    import threading
+    ex._tls = threading.local()
+    N = 16384 * 4 + 96
+    a, b = _rand(ma, N, seed=31), _rand(mb, N, seed=32)
+    ref = a.double() @ b.double().t()
+    plan = _outer_tc_slices(ma, mb)
+    assert plan is not None and len(plan) == calls
+    part = torch.empty(152 * max(r for _, r in plan) * min(ma, mb), device="cuda")
+    out = torch.full((ma, mb), 0.25, dtype=torch.float64, device="cuda")
+    ex._outer(_WS, a, ma, b, mb, N, part, 64, out)      # 64 splits for the single call (the sliced ones pick theirs)
+    torch.cuda.synchronize()
+    assert _WS.err.item() == 0
+    _close(out - 0.25, ref, 2e-5)
