@@ -13,7 +13,8 @@ kernels as in the resident executor, so each GroupNorm costs no extra pass over 
 
 The kernels are the resident path's (split-BF16 tensor cores or FP32, as the model's precision says). Host buffers:
 four hidden states (x, and three rotating buffers for the branch / fusion / pw / mlp intermediates). Shared height
-grids only (per-column grids raise NotImplementedError).
+grids use one pair of height tables; per-column grids (every column its own heights) keep every column's tables on the
+device and each row slab uses its own columns' tables.
 
 StreamingVJP adds the input VJP, which the reference's batched backend does not have: every block's input is kept in
 pinned host memory during the forward, and the backward recomputes each block slab by slab before running the resident
@@ -25,7 +26,6 @@ import numpy as np
 import torch
 
 from . import _native as nat
-from . import tables as tb
 from .executor import EPS, Workspace, _descs, _GradBuffers, _stream
 from .runtime import INPUT_CHANNELS, _check, _host_copy
 
@@ -202,9 +202,9 @@ class StreamingForward:
         _check(flags.item(), "FFNO streaming request")
         del fs, zin
         geo = ex.geometry(zmm)
-        if not geo.shared:
-            raise NotImplementedError("the streaming path runs shared height grids")
-        hgt = ex.height(pk, geo, dev)
+        # shared grids: one table pair; per-column grids: every column's tables on the device ([HW][2M'][D] and
+        # [HW][D][2M'], built by ffno_percol_tables), which each row slab addresses from its first column
+        hgt = ex.height(pk, geo, dev) if geo.shared else ex.height_percol(pk, geo, 0, dev)
         pln, pfr = ex.plane(H, W, dev), ex.plane_freq(pk, H, W, float(dx), float(dy), dev)
         live = hgt["live"]
         dw = torch.empty(V, dtype=torch.float32, device=dev)
@@ -327,6 +327,26 @@ class StreamingForward:
         _host_copy(out, pop_host.numpy()[:V * L])
         return out
 
+    def _vert_forward(self, cx, ws, it, bp, hq):
+        """The height operator's transforms and mode mixing on row slab it = (h0, h1): ws.xv -> ws.yv (ws.va: the
+        modes, ws.vb: the mixed modes), with the shared tables or the slab's columns' own tables."""
+        ex, hgt, live = self.ex, cx.hgt, cx.live
+        D, W, C = self.D, self.W, self.C
+        rows = it[1] - it[0]
+        RW, s = rows * W, _stream()
+        d = _descs(D, rows, W, C, live)
+        if hgt.get("percol"):
+            c0 = it[0] * W
+            nat.call("ffno_xform_pt", hgt["tzf"].data_ptr() + 4 * c0 * 2 * live * D, 2 * live * D, ws.xv.data_ptr(),
+                     ws.va.data_ptr(), d["pcf"], 0, s)
+            ex._mix(ws, "v", bp, hq, ws.va, ws.vb, live, RW, RW * C, C, live * RW * C, False)
+            nat.call("ffno_xform_pt", hgt["tzi"].data_ptr() + 4 * c0 * 2 * live * D, 2 * live * D, ws.vb.data_ptr(),
+                     ws.yv.data_ptr(), d["pci"], 0, s)
+        else:
+            ex._xf(hgt, "tzf", ws.xv, ws.va, d["zf"], ws)
+            ex._mix(ws, "v", bp, hq, ws.va, ws.vb, live, RW, RW * C, C, live * RW * C, False)
+            ex._xf(hgt, "tzi", ws.vb, ws.yv, d["zi"], ws)
+
     @staticmethod
     def _check_err(cx):
         if any(int(w.err.item()) for w in cx.wsd + cx.wsr):
@@ -391,11 +411,7 @@ class StreamingForward:
             else:
                 nat.call("ffno_gate_fwd", ws.x.data_ptr(), ws.V, C, bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(),
                          bp["v_zp"].data_ptr(), ws.zr.data_ptr(), ws.xv.data_ptr(), s)
-            d = _descs(D, rows, W, C, live)
-            RW = rows * W
-            ex._xf(hgt, "tzf", ws.xv, ws.va, d["zf"], ws)
-            ex._mix(ws, "v", bp, hq, ws.va, ws.vb, live, RW, RW * C, C, live * RW * C, False)
-            ex._xf(hgt, "tzi", ws.vb, ws.yv, d["zi"], ws)
+            self._vert_forward(cx, ws, it, bp, hq)
             self._stats(ws, ex._mlp2(ws, 0, ws.yv, None, None, 0.0, None, bp["v_p1"], bp["v_p2"], bp.get("tc_v_post"),
                                      ws.vert_pre))
 
@@ -460,9 +476,9 @@ class StreamingVJP(StreamingForward):
     (S1 = sum g, S2 = sum g xhat), so each one is a statistics pass over depth slabs (every slab's per-CTA partials
     gathered, reduced once in a fixed order) followed by the pass that applies it. The pointwise and horizontal stages
     run over depth slabs, the height branch over row slabs [D][h0:h1][W]; the height tables' gradients accumulate over
-    the row slabs (FP64) and reach the shared column as in the resident path. Per voxel the device keeps the
-    normalised inputs, heights, depth weights and their gradients (15 floats); every [V][C] state stays on the host.
-    Shared height grids only."""
+    the row slabs (FP64; per column for per-column grids) and reach the heights as in the resident path. Per voxel the
+    device keeps the normalised inputs, heights, depth weights and their gradients (15 floats); every [V][C] state
+    stays on the host."""
 
     _INTER = ("spec_pre", "vert_pre", "fused_pre", "x1", "pw_pre", "x2", "mlp_pre")
 
@@ -505,8 +521,10 @@ class StreamingVJP(StreamingForward):
         zbar_rows = torch.zeros(V, **f32)
         xin_bar = torch.zeros(6, V, **f32)
         live = cx.live
-        tzf_bar = torch.zeros(2 * live, D, dtype=torch.float64, device=dev)
-        tzi_bar = torch.zeros(D, 2 * live, dtype=torch.float64, device=dev)
+        # the height tables' gradients: one pair for a shared grid, one per column for per-column grids
+        ncol = 1 if cx.geo.shared else HW
+        tzf_bar = torch.zeros(ncol, 2 * live, D, dtype=torch.float64, device=dev)
+        tzi_bar = torch.zeros(ncol, D, 2 * live, dtype=torch.float64, device=dev)
         nparts = [w.nparts for w in cx.wsd] + [w.nparts for w in cx.wsr]
         gbd = [_GradBuffers(cd, H, W, C, live, G, max(nparts), dev) for _ in range(2)]
         gbr = [_GradBuffers(D, cr, W, C, live, G, max(nparts), dev) for _ in range(2)]
@@ -576,9 +594,20 @@ class StreamingVJP(StreamingForward):
             width = rows * W * 4
             self._rows(zbar.data_ptr() + h0 * W * 4, HW * 4, zbar_rows.data_ptr() + D * h0 * W * 4, width, width, D)
         nat.call("ffno_depth_weights_bwd", cx.zmm.data_ptr(), wbar.data_ptr(), D, HW, zbar.data_ptr(), s)
-        gcol = tb.height_tables_vjp(cx.geo.column_raw, cx.geo.length, cx.geo.k, live, tzf_bar.cpu().numpy(),
-                                    tzi_bar.cpu().numpy())
-        zbar.view(D, H, W)[:, 0, 0] += torch.as_tensor(gcol, dtype=torch.float32, device=dev)
+        if cx.geo.shared:
+            # the shared tables depend on column (0, 0): their gradient goes there (ffno_percol_tables_vjp with one
+            # column, FP64, on the device)
+            hv, gcol = cx.hgt["vjp"], torch.zeros(D, **f32)
+            nat.call("ffno_percol_tables_vjp", hv["z"].data_ptr(), D, 1, hv["k"].data_ptr(), live, hv["f"].data_ptr(),
+                     hv["df"].data_ptr(), hv["med"].data_ptr(), tzf_bar.data_ptr(), tzi_bar.data_ptr(),
+                     gcol.data_ptr(), s)
+            zbar.view(D, H, W)[:, 0, 0] += gcol
+        else:
+            # every column's own tables depend on that column's heights
+            hp = cx.hgt
+            nat.call("ffno_percol_tables_vjp", hp["z"].data_ptr(), D, HW, hp["k"].data_ptr(), live, hp["f"].data_ptr(),
+                     hp["df"].data_ptr(), hp["med"].data_ptr(), tzf_bar.data_ptr(), tzi_bar.data_ptr(),
+                     zbar.data_ptr(), s)
         # SI units: the feature and height gradients of ffno_fsdp_runtime's conversions, slab by slab
         fs = torch.empty(6, cd * HW, **f32)
         fb = torch.empty(6, cd * HW, **f32)
@@ -802,17 +831,34 @@ class StreamingVJP(StreamingForward):
             else:
                 nat.call("ffno_gate_fwd", ws.x.data_ptr(), ws.V, C, bp["v_g1"].data_ptr(), bp["v_g2"].data_ptr(),
                          bp["v_zp"].data_ptr(), ws.zr.data_ptr(), ws.xv.data_ptr(), s)
-            ex._xf(cx.hgt, "tzf", ws.xv, ws.va, d["zf"], ws)
-            ex._mix(ws, "v", bp, hq, ws.va, ws.vb, live, RW, RW * C, C, live * RW * C, False)
-            ex._xf(cx.hgt, "tzi", ws.vb, ws.yv, d["zi"], ws)
+            self._vert_forward(cx, ws, it, bp, hq)
             self._mlp_bwd(bp, ws.yv, gb.pbar, None, gb.yvb, "v_p1", "v_p2t", "v_p1t", "tcb_v_post", ws.V, ws.err)
-            # split counts for this slab's own N (the buffer holds the counts of the largest slab, which are larger)
-            lib = nat.lib()
-            ex._outer(ws, gb.yvb, D, ws.vb, 2 * live, N, gb.opart, lib.ffno_outer_parts(D, 2 * live, N), self.tzi_bar)
-            ex._xf(cx.hgt, "tzi_t", gb.yvb, ws.va, d["zf"], ws)
-            ex._mix(ws, "v", bp, hq, ws.va, ws.vb, live, RW, RW * C, C, live * RW * C, True)
-            ex._outer(ws, ws.vb, 2 * live, ws.xv, D, N, gb.opart, lib.ffno_outer_parts(2 * live, D, N), self.tzf_bar)
-            ex._xf(cx.hgt, "tzf_t", ws.vb, gb.xvb, d["zi"], ws)
+            hgt = cx.hgt
+            if hgt.get("percol"):
+                # the slab's columns' tables and their gradients, from its first column on
+                c0 = it[0] * W
+                tab = 4 * c0 * 2 * live * D
+                bar = 8 * c0 * 2 * live * D
+                nat.call("ffno_col_outer", gb.yvb.data_ptr(), D, ws.vb.data_ptr(), 2 * live, RW, C, N,
+                         self.tzi_bar.data_ptr() + bar, 1, s)
+                nat.call("ffno_xform_pt", hgt["tzi_t"].data_ptr() + tab, 2 * live * D, gb.yvb.data_ptr(),
+                         ws.va.data_ptr(), d["pcf"], 0, s)
+                ex._mix(ws, "v", bp, hq, ws.va, ws.vb, live, RW, RW * C, C, live * RW * C, True)
+                nat.call("ffno_col_outer", ws.vb.data_ptr(), 2 * live, ws.xv.data_ptr(), D, RW, C, N,
+                         self.tzf_bar.data_ptr() + bar, 1, s)
+                nat.call("ffno_xform_pt", hgt["tzf_t"].data_ptr() + tab, 2 * live * D, ws.vb.data_ptr(),
+                         gb.xvb.data_ptr(), d["pci"], 0, s)
+            else:
+                # split counts for this slab's own N (the buffer holds the counts of the largest slab, which are
+                # larger)
+                lib = nat.lib()
+                ex._outer(ws, gb.yvb, D, ws.vb, 2 * live, N, gb.opart, lib.ffno_outer_parts(D, 2 * live, N),
+                          self.tzi_bar)
+                ex._xf(hgt, "tzi_t", gb.yvb, ws.va, d["zf"], ws)
+                ex._mix(ws, "v", bp, hq, ws.va, ws.vb, live, RW, RW * C, C, live * RW * C, True)
+                ex._outer(ws, ws.vb, 2 * live, ws.xv, D, N, gb.opart, lib.ffno_outer_parts(2 * live, D, N),
+                          self.tzf_bar)
+                ex._xf(hgt, "tzf_t", ws.vb, gb.xvb, d["zi"], ws)
             if tc:
                 nat.call("ffno_gate_bwd_tc", ws.x.data_ptr(), gb.xvb.data_ptr(), gb.xacc.data_ptr(), ws.V, C,
                          bp["tcb_v_gate"].data_ptr(), bp["v_zp"].data_ptr(), gb.xacc.data_ptr(), zrow.data_ptr(),

@@ -123,3 +123,35 @@ def test_streaming_vjp_against_the_float64_oracle():
     print(f"streaming VJP vs float64 oracle: features {ef:.2e}, z {ez:.2e}")
     assert ef < 1e-4
     assert ez < 1e-3
+
+
+def _per_column_si(shape, seed):
+    """SI features and heights [m] whose columns each have their own grid (stretched and shifted per column)."""
+    import bench
+    f, z = bench.synthetic_si(shape, seed=seed)
+    zc = bench.per_column_heights(torch.from_numpy(z / 1e6)[None])[0].numpy() * 1e6
+    return f, zc.astype(np.float32)
+
+
+@pytest.mark.parametrize("precision,tol,vtol", [("fp32", 1e-4, 1e-4), ("bf16", 2e-3, 1e-2)])
+def test_streaming_per_column_grids_match_resident(precision, tol, vtol):
+    """Per-column height grids (every column its own tables): the streaming forward and VJP, row slabs addressing
+    their own columns' tables and table gradients, against the resident path through the service backend."""
+    from ffnoml_gb300.runtime import GB300Backend
+    from ffnoml_gb300.streaming import StreamingForward, StreamingVJP
+    model = _model(32, precision)
+    f, z = _per_column_si((21, 12, 10), seed=13)
+    ex = model.executor()
+    assert not ex.geometry_host((z / np.float32(1e6))[None]).shared
+    names = [f"l{i}" for i in range(12)]
+    ref = GB300Backend(model, names).predict_local(f, z, 48e3, 48e3)
+    got = StreamingForward(model, chunk_depth=6, chunk_rows=5)(f, z, 48e3, 48e3)
+    err = np.abs(np.log10(got) - np.log10(ref)).max()
+    cot = (np.random.default_rng(14).normal(size=ref.shape) / ref).astype(np.float32)
+    vref = GB300Backend(model, names).vjp_local(f, z, 48e3, 48e3, cot)
+    vgot = StreamingVJP(model, chunk_depth=6, chunk_rows=5)(f, z, 48e3, 48e3, cot)
+    ef = _rel_per_channel(vgot["features"], vref["features"])
+    ez = float(np.abs(vgot["z_scale"] - vref["z_scale"]).max() / np.abs(vref["z_scale"]).max())
+    print(f"per-column {precision}: forward {err:.2e}, VJP features {ef:.2e}, z {ez:.2e}")
+    assert err < tol
+    assert ef < vtol and ez < 10 * vtol
