@@ -581,10 +581,12 @@ class Executor:
         return pk, geo, hgt, pln, pfr
 
     # -------------------------------------------------------------------------------------------- forward
-    def forward(self, x, z_scale, dx, dy, keep=False, geo=None):
+    def forward(self, x, z_scale, dx, dy, keep=False, geo=None, errs=None):
         """x [B, Cin, D, H, W], z_scale [B, D, H, W] (Mm), float32 CUDA -> [B, L, D, H, W] float32. With keep=True
         also returns the state the VJP needs (block inputs per cube). geo: the heights' analysis when the caller
-        already has it (geometry_host), else it is computed on the device."""
+        already has it (geometry_host), else it is computed on the device. errs: a list that receives the device
+        error flag instead of it being read here (a read waits for the stream); the caller checks it with
+        check_flags after its own synchronisation."""
         m = self.model
         x = x.contiguous()
         z_scale = z_scale.contiguous()
@@ -622,7 +624,10 @@ class Executor:
                 saved.append(inputs)
                 states.append(blocks)
         if not keep:
-            self._check(ws)
+            if errs is None:
+                self._check(ws)
+            else:
+                errs.append(ws.err)
             return out, None
         # a forward kept for the VJP leaves its error flag to the backward, which reads it with its own at the end
         # (one synchronisation for both passes; the flag is sticky): callers that may not run the backward call
@@ -634,6 +639,13 @@ class Executor:
     def check_forward(self, state):
         """Raise if the forward that made `state` (forward(keep=True)) ran out of a bounded wait."""
         self._check_flag(state["err"])
+
+    @staticmethod
+    def check_flags(errs):
+        """Raise if any error flag collected by forward / backward(errs=...) is set (reads them: waits for their
+        streams)."""
+        for e in errs:
+            Executor._check_flag(e)
 
     @staticmethod
     def _fits(nbytes, device):
@@ -926,8 +938,9 @@ class Executor:
         self._gn_jvp(ws, tw, ws.mlp_pre, tw.mlp, bp["mlp_g"], bp["mlp_b"], "mlp", 0, tw.x2, r_mlp, tw.x)
 
     # -------------------------------------------------------------------------------------------- VJP
-    def backward(self, state, ybar):
-        """Input VJP: ybar [B, L, D, H, W] -> (x_bar [B, Cin, D, H, W], z_bar [B, D, H, W])."""
+    def backward(self, state, ybar, errs=None):
+        """Input VJP: ybar [B, L, D, H, W] -> (x_bar [B, Cin, D, H, W], z_bar [B, D, H, W]). errs: as in forward
+        (the backward's flag and that of the forward that made the state)."""
         m = self.model
         x, z_scale, dx, dy = state["x"], state["z"], state["dx"], state["dy"]
         pk, geo, hgt, pln, pfr = self._setup(x, z_scale, dx, dy, state.get("geo"))
@@ -998,9 +1011,11 @@ class Executor:
                      hv["f"].data_ptr(), hv["df"].data_ptr(), hv["med"].data_ptr(), tzf_bar.data_ptr(),
                      tzi_bar.data_ptr(), gcol.data_ptr(), s)
             zbar[0, :, 0, 0] += gcol
-        self._check(ws)
-        if state.get("err") is not None:
-            self._check_flag(state["err"])
+        flags = [ws.err] + ([state["err"]] if state.get("err") is not None else [])
+        if errs is None:
+            self.check_flags(flags)
+        else:
+            errs.extend(flags)
         return xbar_in, zbar
 
     def _gn_bwd(self, ws, gb, mode, u, r, pre, gamma, beta, name, pbar):

@@ -68,18 +68,49 @@ def _host_copy(dst, src):
         raise ValueError("host copy needs a C-contiguous float32 destination of the source's size")
     d, v = dst.reshape(-1), np.ascontiguousarray(src, dtype=np.float32).reshape(-1)
     n = d.size
-    parts = min(8, os.cpu_count() or 1, max(1, n >> 22))
+    parts = min(_THREADS, os.cpu_count() or 1, max(1, n >> 20))      # pieces of at least 4 MB
     if parts <= 1:
         np.copyto(d, v)
         return
+    step = -(-n // parts)
+    futures = [_pool().submit(np.copyto, d[i:i + step], v[i:i + step]) for i in range(0, n, step)]
+    for f in futures:
+        f.result()
+
+
+_THREADS = 16      # host threads for copies and scans of request arrays (one GB300 node's Grace has 72 cores)
+
+
+def _pool():
     global _POOL
     with _POOL_LOCK:
         if _POOL is None:
-            _POOL = ThreadPoolExecutor(max_workers=8, thread_name_prefix="ffno-host-copy")
+            _POOL = ThreadPoolExecutor(max_workers=_THREADS, thread_name_prefix="ffno-host-copy")
+    return _POOL
+
+
+def _heights_scan(z, columns_first=False):
+    """(every height finite, every column equal to column (0, 0)) of float32 heights: z (D, H, W), or with
+    columns_first z (N, D), one column a row (the wire layout). In chunks on a few threads (numpy releases the GIL
+    inside the comparisons)."""
+    if columns_first:
+        zr = z.reshape(z.shape[0], -1)         # [N][D]: chunks of columns against the first
+        ref = lambda a, b: zr[:1]
+    else:
+        zr = z.reshape(z.shape[0], -1)         # [D][HW]: chunks of depths against column 0 at those depths
+        ref = lambda a, b: zr[a:b, :1]
+
+    def scan(a, b):
+        part = zr[a:b]
+        return bool(np.isfinite(part).all()), bool((part == ref(a, b)).all())
+
+    n = zr.shape[0]
+    parts = min(_THREADS, os.cpu_count() or 1, max(1, zr.size >> 20), n)
+    if parts <= 1:
+        return scan(0, n)
     step = -(-n // parts)
-    futures = [_POOL.submit(np.copyto, d[i:i + step], v[i:i + step]) for i in range(0, n, step)]
-    for f in futures:
-        f.result()
+    res = [f.result() for f in [_pool().submit(scan, a, min(n, a + step)) for a in range(0, n, step)]]
+    return all(r[0] for r in res), all(r[1] for r in res)
 
 
 def _check(flags, what):
@@ -228,12 +259,21 @@ class GB300Backend:
         nz, nx, ny = z_scale.shape
         V = nz * nx * ny
         # the heights' analysis from the host copy, in the device's float32 values (z / 1e6 with IEEE division, as
-        # ffno_si_inputs computes it), so that the model's stream is not synchronised to read it back
-        z_mm = z_scale / np.float32(1e6)
-        # (heights that are not finite are left to the device path, which reports them through the request's flags)
-        self._local.geo = self.model.executor().geometry_host(z_mm[None]) if np.isfinite(z_mm).all() else None
-        f_dev = self._upload("features", features)
-        z_dev = self._upload("z", z_scale)
+        # ffno_si_inputs computes it), so that the model's stream is not synchronised to read it back. Columns equal
+        # in metres are equal in Mm, so when every column equals column (0, 0) only that column is divided; otherwise
+        # the analysis runs on the divided heights. (Heights that are not finite are left to the device path, which
+        # reports them through the request's flags.)
+        found = []
+        scan = threading.Thread(target=lambda: found.append(self._scan_heights(z_scale)), daemon=True)
+        scan.start()                     # beside the uploads' host copies
+        try:
+            f_dev = self._upload("features", features)
+            z_dev = self._upload("z", z_scale)
+        finally:
+            scan.join()
+        if not found:
+            raise RuntimeError("the heights' analysis failed")
+        self._local.geo = found[0]
         x = torch.empty(1, 6, nz, nx, ny, dtype=torch.float32, device=self.device)
         zmm = torch.empty(1, nz, nx, ny, dtype=torch.float32, device=self.device)
         self._flags.zero_()
@@ -241,6 +281,18 @@ class GB300Backend:
         nat.call("ffno_si_inputs", f_dev.data_ptr(), z_dev.data_ptr(), V, self.mean_x.data_ptr(),
                  self.std_x.data_ptr(), x.data_ptr(), zmm.data_ptr(), self._flags.data_ptr(), _stream())
         return f_dev, x, zmm, V
+
+    def _scan_heights(self, z_scale):
+        """The geometry of heights z_scale (D, H, W) in metres (None if any is not finite)."""
+        finite, same = _heights_scan(z_scale)
+        ex = self.model.executor()
+        if not finite:
+            geo = None
+        elif same:
+            geo = ex.geometry_host((z_scale[:, :1, :1] / np.float32(1e6))[None])
+        else:
+            geo = ex.geometry_host((z_scale / np.float32(1e6))[None])
+        return geo
 
     # ------------------------------------------------------------------------------------------------ wire layout
     # The service's arrays are little-endian float32 in Fortran order (ffno_fsdp_service.py:219-322). The *_wire
@@ -274,13 +326,17 @@ class GB300Backend:
                 nat.call("ffno_reverse_axes4", src, n_extra, ny, nx, nz, extra.data_ptr(), s)
         # the heights' analysis on the host, in the device's float32 values: the wire z is [ny][nx][nz], columns
         # contiguous, column (0, 0) first
-        zw = buf[6 * V:7 * V].numpy().reshape(ny, nx, nz) / np.float32(1e6)
-        if np.isfinite(zw).all():
-            geo = self.model.executor().geometry_columns(zw.reshape(1, ny * nx, nz),
-                                                         lambda: zw.transpose(1, 0, 2).reshape(1, nx * ny, nz)
-                                                         .astype(np.float64))
-        else:
+        zraw = buf[6 * V:7 * V].numpy().reshape(ny * nx, nz)
+        finite, same = _heights_scan(zraw, columns_first=True)
+        ex = self.model.executor()
+        if not finite:
             geo = None
+        elif same:      # every column equals column (0, 0) in metres, so in Mm too: only that column is divided
+            geo = ex.geometry_columns((zraw[:1] / np.float32(1e6))[None], None)
+        else:
+            zw = zraw.reshape(ny, nx, nz) / np.float32(1e6)
+            geo = ex.geometry_columns(zw.reshape(1, ny * nx, nz),
+                                      lambda: zw.transpose(1, 0, 2).reshape(1, nx * ny, nz).astype(np.float64))
         return f, z, extra, geo, V
 
     def _wire_model_inputs(self, f, z, V, shape):
@@ -312,13 +368,15 @@ class GB300Backend:
         f, z, _, geo, V = self._wire_in(buf, shape, 0)
         x, zmm = self._wire_model_inputs(f, z, V, shape)
         L = self.model.out_channels
+        ex, errs = self.model.executor(), []
         with torch.no_grad():
-            y = self._guarded(lambda: self.model.executor().forward(x, zmm, float(dx), float(dy), geo=geo)[0])
+            y = self._guarded(lambda: ex.forward(x, zmm, float(dx), float(dy), geo=geo, errs=errs)[0])
         pop = torch.empty(V, L, dtype=torch.float32, device=self.device)
         nat.call("ffno_si_populations", y.data_ptr(), V, L, self.mean_y.data_ptr(), self.std_y.data_ptr(),
                  pop.data_ptr(), self._out_flags(), _stream())
         self._wire_out([(pop, (shape[0], shape[1], shape[2], L))], out)
         _check(self._finish(), "FFNO output")
+        ex.check_flags(errs)
         self.call_count += 1
         return V * L
 
@@ -333,7 +391,8 @@ class GB300Backend:
         ybar = torch.empty_like(y)
         nat.call("ffno_si_population_cotangent", y.data_ptr(), cot.data_ptr(), V, L, self.mean_y.data_ptr(),
                  self.std_y.data_ptr(), ybar.data_ptr(), self._out_flags(), _stream())
-        xbar, zbar = self._guarded(lambda: ex.backward(state, ybar))
+        errs = []
+        xbar, zbar = self._guarded(lambda: ex.backward(state, ybar, errs=errs))
         fbar = torch.empty(6, V, dtype=torch.float32, device=self.device)
         zbar_m = torch.empty(V, dtype=torch.float32, device=self.device)
         nat.call("ffno_si_input_grads", f.data_ptr(), xbar.data_ptr(), zbar.data_ptr(), V, self.std_x.data_ptr(),
@@ -344,6 +403,7 @@ class GB300Backend:
         if flags & 1:
             raise ValueError("FFNO VJP cotangent contains NaN or Inf")
         _check(flags, "FFNO VJP")
+        ex.check_flags(errs)
         self.call_count += 1
         return 7 * V
 
@@ -377,14 +437,15 @@ class GB300Backend:
         features, z_scale = self._validate(features, z_scale)
         _, x, zmm, V = self._prepare(features, z_scale)
         L = self.model.out_channels
+        ex, errs = self.model.executor(), []
         with torch.no_grad():
-            y = self._guarded(lambda: self.model.executor().forward(x, zmm, float(dx), float(dy),
-                                                                    geo=self._local.geo)[0])
+            y = self._guarded(lambda: ex.forward(x, zmm, float(dx), float(dy), geo=self._local.geo, errs=errs)[0])
         pop = torch.empty(*z_scale.shape, L, dtype=torch.float32, device=self.device)
         nat.call("ffno_si_populations", y.data_ptr(), V, L, self.mean_y.data_ptr(), self.std_y.data_ptr(),
                  pop.data_ptr(), self._out_flags(), _stream())
         host = self._download("pop", pop)
         _check(self._finish(), "FFNO output")
+        ex.check_flags(errs)
         self.call_count += 1
         return self._result(host)
 
@@ -443,7 +504,8 @@ class GB300Backend:
         ybar = torch.empty_like(y)
         nat.call("ffno_si_population_cotangent", y.data_ptr(), cot_dev.data_ptr(), V, L, self.mean_y.data_ptr(),
                  self.std_y.data_ptr(), ybar.data_ptr(), self._out_flags(), _stream())
-        xbar, zbar = self._guarded(lambda: ex.backward(state, ybar))
+        errs = []
+        xbar, zbar = self._guarded(lambda: ex.backward(state, ybar, errs=errs))
         fbar = torch.empty(6, *z_scale.shape, dtype=torch.float32, device=self.device)
         zbar_m = torch.empty(*z_scale.shape, dtype=torch.float32, device=self.device)
         nat.call("ffno_si_input_grads", f_dev.data_ptr(), xbar.data_ptr(), zbar.data_ptr(), V,
@@ -453,5 +515,6 @@ class GB300Backend:
         if flags & 1:
             raise ValueError("FFNO VJP cotangent contains NaN or Inf")
         _check(flags, "FFNO VJP")
+        ex.check_flags(errs)
         self.call_count += 1
         return {"features": self._result(hf), "z_scale": self._result(hz)}

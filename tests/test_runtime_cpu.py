@@ -76,3 +76,41 @@ def test_host_geometry_decides_the_shared_grid_like_the_column_kernel():
     two = np.concatenate([z, z * np.float32(0.5)])
     g = ex.geometry_host(two)
     assert not g.shared and g.columns.shape == (2, H * W, D)
+
+
+def _geo_fields(g):
+    return (g.shared, g.span, np.asarray(g.column).tobytes(), np.asarray(g.column_raw).tobytes(), g.length,
+            g.k.numpy().tobytes(), None if g.columns is None else np.asarray(g.columns).tobytes())
+
+
+@pytest.mark.parametrize("kind", ["shared", "per_column", "shifted", "rounding", "nonfinite"])
+def test_heights_scan_gives_the_exact_geometry(kind):
+    """The request's height analysis (_heights_scan on the heights in metres, column (0, 0) alone divided when every
+    column equals it) gives the geometry of the analysis of all heights divided by 1e6, in the backend's layout and in
+    the wire layout (columns first); non-finite heights are reported as such."""
+    import torch
+    from ffnoml_gb300 import create_ffno3d
+    from ffnoml_gb300.runtime import _heights_scan
+    ex = create_ffno3d(6, 12, atoms=["H", "CA"], width=32, n_layers=2).executor()
+    D, H, W = 40, 6, 5
+    z = (np.linspace(14.0, -1.0, D, dtype=np.float32)[:, None, None] * np.ones((D, H, W), np.float32)) * 1e6
+    if kind == "per_column":
+        z = z * (1.0 + 0.01 * np.arange(H * W, dtype=np.float32).reshape(1, H, W))
+    elif kind == "shifted":         # every column the same grid shifted: shared after the shift, not equal in metres
+        z = z + 1e4 * np.arange(H * W, dtype=np.float32).reshape(1, H, W)
+    elif kind == "rounding":        # columns differing in metres by one ULP, which the division may merge
+        z[:, 2, 3] = np.nextafter(z[:, 2, 3], np.float32(np.inf))
+    elif kind == "nonfinite":
+        z[7, 1, 1] = np.inf
+    z = z.astype(np.float32)
+    finite, same = _heights_scan(z)
+    zw = np.ascontiguousarray(z.transpose(2, 1, 0)).reshape(W * H, D)
+    assert (finite, same) == _heights_scan(zw, columns_first=True)
+    assert finite == (kind != "nonfinite")
+    assert same == (kind == "shared")
+    if not finite:
+        return
+    exact = ex.geometry_host((z / np.float32(1e6))[None])
+    fast = ex.geometry_host((z[:, :1, :1] / np.float32(1e6))[None]) if same else exact
+    assert _geo_fields(fast)[:6] == _geo_fields(exact)[:6]
+    assert fast.columns is None or np.array_equal(fast.columns, exact.columns)
