@@ -17,7 +17,7 @@ using namespace ffno;
 namespace {
 
 constexpr int XT = 512;    // threads of the mixing kernel
-constexpr int XKC = 64;    // k per chunk of the streamed table pack
+constexpr int XKC = 32;    // k per chunk of the streamed table pack (and data rows per chunk of k_xform_st)
 constexpr int XMT = 2;     // max m tiles of 128 (a transform call has at most 256 output rows)
 
 // one (m-tile, k-chunk) block of the streamed table pack: 128 rows x kc, split hi + lo
@@ -58,17 +58,21 @@ __device__ __forceinline__ bool rt_sync_and(int pipe, bool p) {
 // (lane >> 3) and warps (w & 3) four groups of octets, so a warp reads 8 rows x 128 contiguous bytes, and each 8-lane
 // phase of its 16-byte stores covers 8 rows of one octet: 128 contiguous bytes of the tile, free of bank conflicts.
 // Row k0 + kr of piece u is kr = 8 (2u + (w >> 2)) + (lane & 7); the columns nf..nf+7 depend on the thread only.
-constexpr int XFB8 = 4;   // pieces a thread: 4 x 32 bytes in flight, the whole 64-row chunk per pipeline
+// NP pieces a thread: NP x 32 bytes in flight, the whole chunk of 16 NP rows per pipeline (NP = 4: the 64-row chunks
+// of k_xform_rt; NP = 2: the 32-row chunks of k_xform_st). hb: bytes of one split half of the stage.
+constexpr int XFB8 = 4;
 static_assert(XFB8 * RT * 8 == RKC * 128, "the pieces of a pipeline cover a whole chunk");
+static_assert(2 * RT * 8 == XKC * 128, "the pieces of a pipeline cover a whole streamed chunk");
 
 __device__ __forceinline__ int xf_fill_col(int ptid, int lane) { return 8 * (4 * ((ptid >> 5) & 3) + (lane >> 3)); }
 
-__device__ __forceinline__ void xf_fill_chunk(uint8_t* st, const float* fsrc, bool fv, const long* row_in, int K,
-                                              int k0, int kc, int ptid, int lane, int nf) {
+template <int NP>
+__device__ __forceinline__ void xf_fill_chunk(uint8_t* st, uint32_t hb, const float* fsrc, bool fv,
+                                              const long* row_in, int K, int k0, int kc, int ptid, int lane, int nf) {
   const int w = (ptid >> 5) & 7;
-  float v[XFB8][8];
+  float v[NP][8];
 #pragma unroll
-  for (int u = 0; u < XFB8; ++u) {   // every load of the chunk issued before any is converted
+  for (int u = 0; u < NP; ++u) {   // every load of the chunk issued before any is converted
     const int kr = 8 * (2 * u + (w >> 2)) + (lane & 7);
     const int k = k0 + kr;
     if (kr < kc && k < K && fv) {
@@ -79,7 +83,7 @@ __device__ __forceinline__ void xf_fill_chunk(uint8_t* st, const float* fsrc, bo
     }
   }
 #pragma unroll
-  for (int u = 0; u < XFB8; ++u) {
+  for (int u = 0; u < NP; ++u) {
     const int kr = 8 * (2 * u + (w >> 2)) + (lane & 7);
     if (kr >= kc) break;
     uint32_t h[4], l[4];
@@ -87,7 +91,7 @@ __device__ __forceinline__ void xf_fill_chunk(uint8_t* st, const float* fsrc, bo
     for (int i = 0; i < 4; ++i) tc::split_pack(v[u][2 * i], v[u][2 * i + 1], h[i], l[i]);
     const uint32_t o = tc::mnmajor_offset(nf, kr, 128);
     *reinterpret_cast<uint4*>(st + o) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4*>(st + RSB + o) = make_uint4(l[0], l[1], l[2], l[3]);
+    *reinterpret_cast<uint4*>(st + hb + o) = make_uint4(l[0], l[1], l[2], l[3]);
   }
 }
 
@@ -162,7 +166,7 @@ __global__ void __launch_bounds__(2 * RT, 1)
         if (!(ok = rt_sync_and(pipe, w))) break;
       }
       uint8_t* st = sD + (uint32_t)(pipe * 2 + s) * 2u * RSB;
-      xf_fill_chunk(st, fsrc, fv, row_in, d.K, k0, kc, ptid, lane, nf);
+      xf_fill_chunk<XFB8>(st, RSB, fsrc, fv, row_in, d.K, k0, kc, ptid, lane, nf);
       tc::fence_async_smem();
       tc::tc_before_sync();
       rt_sync(pipe);
@@ -232,17 +236,18 @@ __global__ void __launch_bounds__(2 * RT, 1)
 
 // ------------------------------------------------------------------------------------------- streamed table
 // The transposed transform GEMM of k_xform_rt for tables too large to keep resident (the H transforms, K = M = 2H):
-// per 64-row k-chunk the table slice [MT * 128][kc] (from the m-tile / k-chunk pack of ffno_xform_tc) arrives by
-// bulk copies into the stage next to the data chunk, both double-buffered against the MMAs. One pipeline of 256
-// threads per CTA (the table stages fill shared memory).
-__global__ void __launch_bounds__(RT, 1)
+// per 32-row k-chunk the table slice [MT * 128][kc] (from the m-tile / k-chunk pack of ffno_xform_tc) arrives by
+// bulk copies into the stage next to the data chunk, both double-buffered against the MMAs. Chunks of 32 rows k keep
+// a CTA's stages near 100 KB, so that two CTAs of 256 threads share an SM (each with 256 tensor-memory columns).
+constexpr uint32_t SSB = 128u * XKC * 2;    // one split half of a data stage of k_xform_st
+__global__ void __launch_bounds__(RT, 2)
     k_xform_st(const uint8_t* __restrict__ tpack, int MT, int Kp, const float* __restrict__ in, float* __restrict__ out,
                ffno_xform_desc d, int nbi, int nshift, long ntn, long items, int accumulate, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
-  const uint32_t TSB = (uint32_t)MT * 128u * RKC * 2;        // one split half of a table stage
-  uint8_t* sD = base;                                        // [stage][hi | lo], 2 * RSB each
-  uint8_t* sT = base + 4 * RSB;                              // [stage][hi | lo], 2 * TSB each
+  const uint32_t TSB = (uint32_t)MT * 128u * XKC * 2;        // one split half of a table stage
+  uint8_t* sD = base;                                        // [stage][hi | lo], 2 * SSB each
+  uint8_t* sT = base + 4 * SSB;                              // [stage][hi | lo], 2 * TSB each
   __shared__ uint64_t bar_t[2], bar_m[2];
   __shared__ uint32_t tslot;
   __shared__ long row_in[RT_MAXK], row_out[256];
@@ -263,7 +268,7 @@ __global__ void __launch_bounds__(RT, 1)
   tc::tc_after_sync();
   const uint32_t tmem = tslot;
   const uint32_t lq = (uint32_t)(32 * q) << 16;
-  const int nch = (Kp + RKC - 1) / RKC;
+  const int nch = (Kp + XKC - 1) / XKC;
   const uint32_t idesc = tc::idesc_bf16_ab(128, Mp, true, false);
   const uint32_t mt_bytes = (uint32_t)128 * Kp * 2 * 2;
   bool ok = true;
@@ -296,12 +301,12 @@ __global__ void __launch_bounds__(RT, 1)
     const float* fsrc = in + foff;
     for (int ch = 0; ch < nch; ++ch, ++g) {
       const int s = (int)(g & 1u);
-      const int k0 = ch * RKC, kc = (Kp - k0) < RKC ? (Kp - k0) : RKC;
+      const int k0 = ch * XKC, kc = (Kp - k0) < XKC ? (Kp - k0) : XKC;
       if (g >= 2) {
         const bool w = tc::mbar_wait(&bar_m[s], ((g - 2) >> 1) & 1u);
         if (!(ok = bounded(w, err, 3))) break;
       }
-      uint8_t* st = sD + (uint32_t)s * 2u * RSB;
+      uint8_t* st = sD + (uint32_t)s * 2u * SSB;
       uint8_t* tt = sT + (uint32_t)s * 2u * TSB;
       if (tid == 0) {   // the table slice of this chunk: m-tiles stacked, hi then lo
         const uint32_t part = 128u * kc * 2;
@@ -312,14 +317,14 @@ __global__ void __launch_bounds__(RT, 1)
           tc::bulk_g2s(tt + (uint32_t)MT * part + mt * part, src + part, part, &bar_t[s]);
         }
       }
-      xf_fill_chunk(st, fsrc, fv, row_in, d.K, k0, kc, tid, lane, nf);
+      xf_fill_chunk<2>(st, SSB, fsrc, fv, row_in, d.K, k0, kc, tid, lane, nf);
       tc::fence_async_smem();
       const bool wt = tc::mbar_wait(&bar_t[s], (g >> 1) & 1u);
       tc::tc_before_sync();
       if (!(ok = bounded(wt, err, 1))) break;
       tc::tc_after_sync();
       if (tid == 0) {
-        const uint32_t x_hi = tc::smem_u32(st), x_lo = x_hi + RSB;
+        const uint32_t x_hi = tc::smem_u32(st), x_lo = x_hi + SSB;
         const uint32_t t_hi = tc::smem_u32(tt), t_lo = t_hi + (uint32_t)MT * 128u * kc * 2;
         const uint32_t as[3] = {x_hi, x_hi, x_lo}, bs[3] = {t_hi, t_lo, t_hi};
 #pragma unroll
@@ -833,10 +838,10 @@ int ffno_xform_tc(const void* tpack, const float* in, float* out, const ffno_xfo
   }
   const long ntn = (d.N + 127) / 128;
   const long items = nbi > 1 ? (d.nb + nbi - 1) / nbi : d.nb * ntn;
-  const size_t smem = 1024 + 4 * (size_t)RSB + 2 * 2 * (size_t)MT * 128 * RKC * 2;
+  const size_t smem = 1024 + 4 * (size_t)SSB + 2 * 2 * (size_t)MT * 128 * XKC * 2;
   if (!ffno::smem_cap_ok(k_xform_st, smem))
     return FFNO_ELAUNCH;
-  const long grid = items < sms() ? items : sms();
+  const long grid = items < 2L * sms() ? items : 2L * sms();   // two CTAs per SM
   k_xform_st<<<(unsigned)grid, RT, smem, (cudaStream_t)stream>>>(static_cast<const uint8_t*>(tpack), MT, Kp, in, out,
                                                                 d, nbi, nshift, ntn, items, accumulate, err);
   FFNO_CHECK_LAUNCH();

@@ -101,12 +101,13 @@ def _split_kmajor(m):
 
 
 XFORM_TC_MAX_K = 512     # the longest contraction one tensor-core transform call takes (RT_MAXK in spectral_tc.cu)
+XFORM_TC_KCHUNK = 32     # k per block of the streamed table pack (XKC in spectral_tc.cu)
 
 
 class TcXform:
     """A transform table T [M][K] (float64 numpy) packed for the tensor-core transforms, in slices of at most 256 rows
     and 512 columns (one kernel call each; the column slices of one row slice accumulate into the same output rows):
-    per slice the streamed pack of ffno_xform_tc (split-BF16 per 128-row m-tile and 64-wide k-chunk) and, when the
+    per slice the streamed pack of ffno_xform_tc (split-BF16 per 128-row m-tile and 32-wide k-chunk) and, when the
     slice fits in shared memory, the resident pack of ffno_xform_tcr (the whole [Mp][Kp] table as one canonical
     operand, Mp and Kp rounded up to 16). A production height grid (M = 1001: 680 table rows at D = 256) takes both
     kinds of slices."""
@@ -124,8 +125,8 @@ class TcXform:
                 Kp = (cols + 15) // 16 * 16
                 pad = np.zeros((mt * 128, Kp))
                 pad[:rows, :cols] = T[r0:r0 + rows, c0:c0 + cols]
-                parts = [_split_kmajor(pad[t * 128:(t + 1) * 128, k0:min(Kp, k0 + 64)])
-                         for t in range(mt) for k0 in range(0, Kp, 64)]
+                parts = [_split_kmajor(pad[t * 128:(t + 1) * 128, k0:min(Kp, k0 + XFORM_TC_KCHUNK)])
+                         for t in range(mt) for k0 in range(0, Kp, XFORM_TC_KCHUNK)]
                 packed = torch.cat(parts).to(device).contiguous()
                 if packed.numel() * 2 != nat.lib().ffno_xform_tc_pack_bytes(rows, cols):
                     raise RuntimeError("transform pack size mismatch")

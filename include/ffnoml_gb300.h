@@ -388,7 +388,7 @@ int ffno_head_bwd_tc(const float* x, const float* x_in, const float* y_bar, long
 
 /* ffno_xform on tensor cores (split-BF16), same descriptor; M <= 256, N and the input strides multiples of 8 floats,
  * the input pointer 32-byte aligned (rows are read 32 bytes a request).
- * tpack: T [M][K] packed per 128-row m-tile (rows past M zero) and, within it, per 64-wide k-chunk (K padded with
+ * tpack: T [M][K] packed per 128-row m-tile (rows past M zero) and, within it, per 32-wide k-chunk (K padded with
  * zeros to a multiple of 16; the last chunk narrower), each chunk its hi then lo half in the canonical K-major order
  * with the chunk's own width; ffno_xform_tc_pack_bytes gives the size. */
 int ffno_xform_tc_pack_bytes(int M, int K);
