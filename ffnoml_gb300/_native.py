@@ -69,6 +69,7 @@ PROTOTYPES = {
     "ffno_col_outer": [P, I, P, I, L, I, L, P, I, P],
     "ffno_percol_tables": [P, I, L, P, I, P, P, P, P, P, P],
     "ffno_percol_tables_vjp": [P, I, L, P, I, P, P, P, P, P, P, P],
+    "ffno_column_tables_vjp": [P, I, P, I, P, P, I, P, P, P, P, L, P],
     "ffno_spectral_mix": [P, P, L, L, L, L, L, I, P, P, P, P, I, P],
     "ffno_gn_bwd_stats": [I, P, F, P, P, P, P, L, I, I, P, I, P],
     "ffno_gn_bwd_final": [P, I, I, P, P],

@@ -264,6 +264,106 @@ __global__ void __launch_bounds__(HT) k_percol_tables_vjp(const double* __restri
 
 size_t vjp_smem(int D, int live) { return (size_t)(2 * D + live + 2 * HT * (HCH + 1)) * sizeof(double); }
 
+// ---------------------------------------------------------------------------------------- one column, many CTAs
+// The same gradient for one column (a shared height grid), spread over the (mode, node) pairs: k_column_terms writes
+// every pair's terms (node j's lower-end sum, node j + 1's upper-end term, d L / d f_m) to scratch; k_column_finish
+// sums them in a fixed order (per node over the modes, per mode over the nodes) and finishes as k_percol_tables_vjp
+// does. scratch: [3][M'][D] doubles.
+constexpr int CT1 = 256;
+
+__device__ __forceinline__ double column_min(const double* __restrict__ zr, int D, double* red) {
+  double mn = INFINITY;
+  for (int j = threadIdx.x; j < D; j += blockDim.x) mn = fmin(mn, zr[j]);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mn;
+  __syncthreads();
+  double m = red[0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmin(m, red[w]);
+  return m;
+}
+
+__global__ void __launch_bounds__(CT1) k_column_terms(const double* __restrict__ zr, int D,
+                                                      const double* __restrict__ k, int live,
+                                                      const double* __restrict__ f,
+                                                      const double* __restrict__ tzf_bar,
+                                                      const double* __restrict__ tzi_bar, double* __restrict__ terms) {
+  __shared__ double red[CT1 / 32];
+  const double zmin = column_min(zr, D, red);
+  const long e = (long)blockIdx.x * CT1 + threadIdx.x;
+  if (e >= (long)live * D) return;
+  const int m = (int)(e / D), j = (int)(e % D);
+  const long M2 = 2L * live;
+  const double km = k[m], fm = f[m];
+  const double zj = zr[j] - zmin;
+  double sn, cs;
+  sincos(zj * km, &sn, &cs);
+  const double gc = tzi_bar[(long)j * M2 + m], gs = tzi_bar[(long)j * M2 + live + m];
+  double lo = fm * km * (-gc * sn - gs * cs), up = 0.0;
+  if (j + 1 < D) {
+    double dza, dzb;
+    filon_terms_vjp(zj, zr[j + 1] - zmin, km, tzf_bar[(long)m * D + j], tzf_bar[(long)(live + m) * D + j],
+                    tzf_bar[(long)m * D + j + 1], tzf_bar[(long)(live + m) * D + j + 1], dza, dzb);
+    lo += dza;
+    up = dzb;
+  }
+  const long n = (long)live * D;
+  terms[e] = lo;
+  terms[n + e] = up;
+  terms[2 * n + e] = gc * cs - gs * sn;
+}
+
+__global__ void __launch_bounds__(CT1) k_column_finish(const double* __restrict__ zr, int D, int live,
+                                                       const double* __restrict__ df, int med,
+                                                       const double* __restrict__ terms, float* __restrict__ z_bar,
+                                                       long z_stride) {
+  extern __shared__ double gz[];   // [D]
+  __shared__ double red[CT1 / 32];
+  __shared__ double share, gtap;
+  const double zmin = column_min(zr, D, red);
+  const long n = (long)live * D;
+  for (int j = threadIdx.x; j < D; j += CT1) {
+    double g = 0.0;
+    for (int m = 0; m < live; ++m) g += terms[(long)m * D + j];
+    if (j > 0)
+      for (int m = 0; m < live; ++m) g += terms[n + (long)m * D + j - 1];
+    gz[j] = g;
+  }
+  // d L / d f_m per mode, weighted by d f_m / d dz, summed over the modes in order by one warp
+  if (threadIdx.x < 32) {
+    double t = 0.0;
+    for (int m = threadIdx.x; m < live; m += 32) {
+      double dl = 0.0;
+      for (int j = 0; j < D; ++j) dl += terms[2 * n + (long)m * D + j];
+      t += dl * df[m];
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) gtap = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // the taper through the median spacing |z_p+1 - z_p|
+    const double d = zr[med + 1] - zr[med];
+    const double sg = d > 0 ? 1.0 : (d < 0 ? -1.0 : 0.0);
+    gz[med + 1] += gtap * sg;
+    gz[med] -= gtap * sg;
+    // the shift by the minimum: its gradient (minus the sum) shared evenly by the tied minima
+    double tot = 0.0;
+    int nt = 0;
+    for (int j = 0; j < D; ++j) {
+      tot += gz[j];
+      nt += zr[j] == zmin;
+    }
+    share = tot / nt;
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < D; j += CT1) {
+    const double g = gz[j] - (zr[j] == zmin ? share : 0.0);
+    z_bar[(long)j * z_stride] += (float)g;
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -276,6 +376,20 @@ int ffno_percol_tables(const double* z_raw, int D, long ncol, const double* k, i
   if (!ffno::smem_cap_ok(k_percol_tables, smem)) return FFNO_ELAUNCH;
   k_percol_tables<<<(unsigned)ncol, HT, smem, (cudaStream_t)stream>>>(z_raw, D, ncol, k, live, f, tzf, tzi, tzf_t,
                                                                      tzi_t);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_column_tables_vjp(const double* z_raw, int D, const double* k, int live, const double* f, const double* df,
+                           int med, const double* tzf_bar, const double* tzi_bar, double* scratch, float* z_bar,
+                           long z_stride, ffno_stream_t stream) {
+  if (!z_raw || !k || !f || !df || !tzf_bar || !tzi_bar || !scratch || !z_bar || D < 2 || live < 1 || z_stride < 1)
+    return FFNO_EINVAL;
+  if (D > FFNO_PERCOL_MAX_D || live > FFNO_PERCOL_MAX_LIVE || med < 0 || med > D - 2) return FFNO_EINVAL;
+  const long n = (long)live * D;
+  cudaStream_t s = (cudaStream_t)stream;
+  k_column_terms<<<(unsigned)((n + CT1 - 1) / CT1), CT1, 0, s>>>(z_raw, D, k, live, f, tzf_bar, tzi_bar, scratch);
+  k_column_finish<<<1, CT1, (size_t)D * sizeof(double), s>>>(z_raw, D, live, df, med, scratch, z_bar, z_stride);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

@@ -429,7 +429,7 @@ class Executor:
                 raise RuntimeError("height table live-mode counts disagree")
             f64 = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=device)
             vjp = dict(z=f64(np.asarray(geo.column, np.float64)[None]), k=f64(geo.k.numpy()[:live]), f=f64(fcol),
-                       df=f64(dfcol), med=torch.as_tensor(med, dtype=torch.int32, device=device))
+                       df=f64(dfcol), med=torch.as_tensor(med, dtype=torch.int32, device=device), med_i=int(med[0]))
             self._height[key] = dict(live=live, tzf=f(tzf), tzi=f(tzi), tzf_t=f(tzf.T), tzi_t=f(tzi.T),
                                      freq=per_block, np=dict(tzf=tzf, tzi=tzi), vjp=vjp, device=device)
         return self._height[key]
@@ -958,21 +958,6 @@ class Executor:
             live = hgt["live"]
             tzf_bar = torch.zeros(2 * live, D, dtype=torch.float64, device=dev)
             tzi_bar = torch.zeros(D, 2 * live, dtype=torch.float64, device=dev)
-            # the height tables depend on the shared column (sample 0, column (0, 0)): their gradient goes there, on
-            # the device in FP64 (the per-column table gradient with one column). It starts on a second stream as
-            # soon as the last block's table products are done, so it runs beside the rest of the backward.
-            gcol = torch.zeros(D, dtype=torch.float32, device=dev)
-            side = torch.cuda.Stream(dev)
-            products_done, gcol_done = torch.cuda.Event(), torch.cuda.Event()
-
-            def tables_out():
-                products_done.record()
-                side.wait_event(products_done)
-                hv = hgt["vjp"]
-                nat.call("ffno_percol_tables_vjp", hv["z"].data_ptr(), D, 1, hv["k"].data_ptr(), hgt["live"],
-                         hv["f"].data_ptr(), hv["df"].data_ptr(), hv["med"].data_ptr(), tzf_bar.data_ptr(),
-                         tzi_bar.data_ptr(), gcol.data_ptr(), side.cuda_stream)
-                gcol_done.record(side)
         for b in range(B):
             hgt_b = hgt if geo.shared else self.height_percol(pk, geo, b, dev)
             live = hgt_b["live"]
@@ -1006,9 +991,7 @@ class Executor:
                 else:
                     wb = ws
                     self._block(pk, ws, i, z, D, H, W, hgt_b, pln, pfr[i], x_in=inputs[i])
-                done = tables_out if geo.shared and b == B - 1 and i == 0 else None
-                self._block_bwd(pk, wb, gb, i, inputs[i], z, zbar[b], D, H, W, hgt_b, pln, pfr[i], tzf_bar, tzi_bar,
-                                done)
+                self._block_bwd(pk, wb, gb, i, inputs[i], z, zbar[b], D, H, W, hgt_b, pln, pfr[i], tzf_bar, tzi_bar)
             # lift: x0 = gelu(GN(pre0))
             self._lift(pk, ws, xin)
             self._gn_bwd(ws, gb, 1, gb.xbar, 1.0, ws.pre, pk.lift_g, pk.lift_b, "lift", gb.pbar)
@@ -1020,8 +1003,9 @@ class Executor:
                          hgt_b["f"].data_ptr(), hgt_b["df"].data_ptr(), hgt_b["med"].data_ptr(), tzf_bar.data_ptr(),
                          tzi_bar.data_ptr(), zbar[b].data_ptr(), s)
         if geo.shared:
-            torch.cuda.current_stream(dev).wait_event(gcol_done)
-            zbar[0, :, 0, 0] += gcol
+            # the height tables depend on the shared column (sample 0, column (0, 0)): their gradient goes there, on
+            # the device in FP64, spread over the column's (mode, node) pairs
+            self._column_tables_vjp(hgt, D, tzf_bar, tzi_bar, zbar[0], H * W)
         flags = [ws.err] + ([state["err"]] if state.get("err") is not None else [])
         if errs is None:
             self.check_flags(flags)
@@ -1040,7 +1024,17 @@ class Executor:
                  ws.gstats[name].data_ptr(), gb.sums.data_ptr(), ws.dw.data_ptr(), V, C, G, EPS, pbar.data_ptr(),
                  gb.wbar.data_ptr(), s)
 
-    def _block_bwd(self, pk, ws, gb, i, x, z, zbar, D, H, W, hgt, pln, fq, tzf_bar, tzi_bar, tables_done=None):
+    @staticmethod
+    def _column_tables_vjp(hgt, D, tzf_bar, tzi_bar, zbar, stride):
+        """z_bar[j * stride] += the gradient of the shared grid's height tables (along tzf_bar, tzi_bar) w.r.t. its
+        column's heights (ffno_column_tables_vjp)."""
+        hv, live = hgt["vjp"], hgt["live"]
+        scratch = torch.empty(3 * live * D, dtype=torch.float64, device=tzf_bar.device)
+        nat.call("ffno_column_tables_vjp", hv["z"].data_ptr(), D, hv["k"].data_ptr(), live, hv["f"].data_ptr(),
+                 hv["df"].data_ptr(), hv["med_i"], tzf_bar.data_ptr(), tzi_bar.data_ptr(), scratch.data_ptr(),
+                 zbar.data_ptr(), stride, _stream())
+
+    def _block_bwd(self, pk, ws, gb, i, x, z, zbar, D, H, W, hgt, pln, fq, tzf_bar, tzi_bar):
         """gb.xbar (gradient of the block output) -> gb.xbar (gradient of the block input x); accumulates the
         depth-weight gradient in gb.wbar, the z_proj gradient in zbar and the height-table gradients."""
         m = self.model
@@ -1119,8 +1113,6 @@ class Executor:
             self._xf(hgt, "tzi_t", gb.yvb, ws.va, d["zf"], ws)
             self._mix(ws, "v", bp, hq, ws.va, ws.vb, live, HW, HW * C, C, live * HW * C, True)
             self._outer(ws, ws.vb, 2 * live, ws.xv, D, N, gb.opart, gb.osplit_f, tzf_bar)
-            if tables_done:
-                tables_done()
             self._xf(hgt, "tzf_t", ws.vb, gb.xvb, d["zi"], ws)
         # input gates (and z_proj)
         if tc:

@@ -595,13 +595,8 @@ class StreamingVJP(StreamingForward):
             self._rows(zbar.data_ptr() + h0 * W * 4, HW * 4, zbar_rows.data_ptr() + D * h0 * W * 4, width, width, D)
         nat.call("ffno_depth_weights_bwd", cx.zmm.data_ptr(), wbar.data_ptr(), D, HW, zbar.data_ptr(), s)
         if cx.geo.shared:
-            # the shared tables depend on column (0, 0): their gradient goes there (ffno_percol_tables_vjp with one
-            # column, FP64, on the device)
-            hv, gcol = cx.hgt["vjp"], torch.zeros(D, **f32)
-            nat.call("ffno_percol_tables_vjp", hv["z"].data_ptr(), D, 1, hv["k"].data_ptr(), live, hv["f"].data_ptr(),
-                     hv["df"].data_ptr(), hv["med"].data_ptr(), tzf_bar.data_ptr(), tzi_bar.data_ptr(),
-                     gcol.data_ptr(), s)
-            zbar.view(D, H, W)[:, 0, 0] += gcol
+            # the shared tables depend on column (0, 0): their gradient goes there (FP64, on the device)
+            ex._column_tables_vjp(cx.hgt, D, tzf_bar, tzi_bar, zbar, HW)
         else:
             # every column's own tables depend on that column's heights
             hp = cx.hgt

@@ -432,6 +432,12 @@ int ffno_percol_tables(const double* z_raw, int D, long ncol, const double* k, i
 int ffno_percol_tables_vjp(const double* z_raw, int D, long ncol, const double* k, int live, const double* f,
                            const double* df, const int* med, const double* tzf_bar, const double* tzi_bar,
                            float* z_bar, ffno_stream_t stream);
+/* The same gradient for one column (a shared height grid: models/ffno_model.py:266-275, 302-305), spread over its
+ * (mode, node) pairs instead of one CTA: z_bar[j * z_stride] += d/dz_raw[j]; med is the median spacing's index;
+ * scratch holds 3 * live * D doubles. Sums run in a fixed order. */
+int ffno_column_tables_vjp(const double* z_raw, int D, const double* k, int live, const double* f, const double* df,
+                           int med, const double* tzf_bar, const double* tzi_bar, double* scratch, float* z_bar,
+                           long z_stride, ffno_stream_t stream);
 
 /* ---- forward-mode derivative (JVP): jvp_local (ffno_fsdp_runtime.py:350-372), the tangent of FFNO3D.forward along
  * an input tangent with the heights fixed. The linear stages reuse the forward entry points on the tangent (the lift

@@ -131,3 +131,37 @@ def test_column_outer_products(Ra, Rb, C, ncol):
     nat.call("ffno_col_outer", A.data_ptr(), Ra, B.data_ptr(), Rb, ncol, C, rs, out.data_ptr(), 0, s)
     torch.cuda.synchronize()
     assert torch.all((out - ref).abs() <= bound + 1e-12)
+
+
+@pytest.mark.parametrize("D,nk", [(40, 33), (256, 65), (37, 12), (256, 700)])
+def test_one_column_gradient_matches_per_column_kernel(D, nk):
+    """ffno_column_tables_vjp (one column over many CTAs, the shared height grid's path) against
+    ffno_percol_tables_vjp on the same column, for columns that run up and down, with a zero-length interval, tied
+    minima and irregular spacing, written at a stride into z_bar."""
+    from ffnoml_gb300 import _native as nat
+    length = 15.0
+    cols = _columns(5, D, D + 1)
+    k = _k(length, nk)
+    dev = torch.device("cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    g = np.random.default_rng(D + nk)
+    for c in range(cols.shape[0]):
+        col = cols[c:c + 1]
+        live, _, (z, kk, fd, dfd, medd) = _device_tables(col, length, k)
+        fbar = torch.as_tensor(g.normal(size=(1, 2 * live, D)), device=dev)
+        ibar = torch.as_tensor(g.normal(size=(1, D, 2 * live)), device=dev)
+        ref = torch.zeros(D, dtype=torch.float32, device=dev)
+        nat.call("ffno_percol_tables_vjp", z.data_ptr(), D, 1, kk.data_ptr(), live, fd.data_ptr(), dfd.data_ptr(),
+                 medd.data_ptr(), fbar.data_ptr(), ibar.data_ptr(), ref.data_ptr(), s)
+        stride = 7
+        got = torch.full((D * stride,), 0.5, dtype=torch.float32, device=dev)
+        got.view(D, stride)[:, 0] = 0.0
+        scratch = torch.empty(3 * live * D, dtype=torch.float64, device=dev)
+        nat.call("ffno_column_tables_vjp", z.data_ptr(), D, kk.data_ptr(), live, fd.data_ptr(), dfd.data_ptr(),
+                 int(medd[0].item()), fbar.data_ptr(), ibar.data_ptr(), scratch.data_ptr(), got.data_ptr(), stride, s)
+        torch.cuda.synchronize()
+        g2 = got.view(D, stride)
+        assert torch.all(g2[:, 1:] == 0.5)
+        # FP64 sums in another order, rounded to float32: within a few float32 ulps of the largest entry
+        err = (g2[:, 0].double() - ref.double()).abs().max().item()
+        assert err <= 1e-6 * ref.abs().max().item() + 1e-30, (c, err)
