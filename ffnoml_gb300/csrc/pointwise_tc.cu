@@ -1337,6 +1337,185 @@ __global__ void __launch_bounds__(CT, 1) k_head_bwd_tc(const float* __restrict__
   pipe_finish(P, tslot, 2 * NCOL);
 }
 
+// ============================================================================================== width 96
+// The production model's width (96): a channel MLP's split weights take 144 KB, so a CTA runs one 256-thread pipeline
+// and every GEMM runs untransposed (lane = voxel row; the 16-column chunks of a row alternate between its two threads,
+// as in the other row-oriented kernels). The 2C = 192 hidden features pass through one [128][96] operand tile in two
+// K-halves. The backward reads its transposed weights out of the forward's matrices: a K-major [R][K] matrix read as
+// an MN-major operand is its transpose ([K][R]), so one 144 KB pack serves all three of its GEMMs.
+constexpr int C96 = 96;
+
+// the transpose of the K-major weight matrix [R][K] at p, as the MN-major operand [N = K][K' = R] from k' = r0
+__device__ __forceinline__ Op wop_t(const uint8_t* p, int R, int K, int r0 = 0) {
+  const uint32_t h = tc::smem_u32(p) + (uint32_t)(r0 / 8) * (uint32_t)K * 16u;
+  return Op{h, h + (uint32_t)R * K * 2, (uint32_t)K * 16u, 128u, (uint32_t)K * 32u, true};
+}
+
+// fill_tile8 for 96 columns (12 octets a row, so a thread's columns change from piece to piece)
+template <typename F>
+__device__ __forceinline__ void fill96(Split t, long v0, long V, int ptid, F f) {
+  constexpr int KB = C96 / 8, NE = TM * KB, FB8 = FB / 2;
+  for (int e0 = ptid; e0 < NE; e0 += PT * FB8) {
+    float a[FB8][8];
+#pragma unroll
+    for (int u = 0; u < FB8; ++u) {   // the loads of FB8 pieces issued before any is converted
+      const int e = e0 + u * PT;
+      const int r8 = e & 7, q = e >> 3;
+      const long v = v0 + (q / KB) * 8 + r8;
+      if (e < NE && v < V) {
+        f(v, (q % KB) * 8, a[u]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[u][i] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < FB8; ++u) {
+      const int e = e0 + u * PT;
+      if (e >= NE) break;
+      uint32_t h[4], l[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) tc::split_pack(a[u][2 * i], a[u][2 * i + 1], h[i], l[i]);
+      *reinterpret_cast<uint4*>(t.hi() + (size_t)e * 16) = make_uint4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<uint4*>(t.lo() + (size_t)e * 16) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+  }
+}
+
+// The ffno_mlp2_fwd_tc contract at C = 96: pre = gelu(X W1^T) W2^T with X = in (+ res GN(prev) [gelu] in modes 1 and
+// 2, written to xout), and the GroupNorm partials of pre. Weights [w1 (2C x C), w2 (C x 2C)]. Tensor memory: D1 (2C
+// columns) at 0, D2 (C) at 2C.
+template <int MODE>
+__global__ void __launch_bounds__(PT, 1) k_mlp2_tc96(const float* __restrict__ in, const float* __restrict__ prev,
+                                                     const float* __restrict__ pc, float res, float* __restrict__ xout,
+                                                     long V, const uint8_t* __restrict__ wpack,
+                                                     const float* __restrict__ dw, float* __restrict__ pre,
+                                                     double* __restrict__ partials, int* __restrict__ err) {
+  constexpr int C = C96;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(2 * C, C), B2 = mat_bytes(C, 2 * C);
+  __shared__ float red[(PT / 32) * (GMAX + 1)], gm[GMAX], wsum;
+  __shared__ double acc[GMAX * 3];
+  PIPE_PROLOGUE(3 * C, 1)
+  const Split T = split_at(smem + B1 + B2, TM, C);   // the input tile, then each K-half of the hidden layer
+  if (tid < GMAX * 3) acc[tid] = 0.0;
+  P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
+  const Op w1 = wop(smem, 2 * C, C);
+  const int row = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    fill96(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) {
+      ld8(in + v * C + k, o);
+      if (MODE != 0) {
+        float p[8];
+        ld8(prev + v * C + k, p);
+        const float4 y0 = gn_apply<MODE == 1>(make_float4(p[0], p[1], p[2], p[3]), gn_coefs(pc, C, k));
+        const float4 y1 = gn_apply<MODE == 1>(make_float4(p[4], p[5], p[6], p[7]), gn_coefs(pc, C, k + 4));
+        const float y[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+#pragma unroll
+        for (int i = 0; i < 8; ++i) o[i] = fmaf(res, y[i], o[i]);
+        st8(xout + v * C + k, o);
+      }
+    });
+    if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, C), w1, C, false, 2 * C})) break;
+    for (int h = 0; h < 2; ++h) {
+#pragma unroll 1
+      for (int j = 6 * h; j < 6 * h + 6; ++j) {
+        if (!owns(j, P.half)) continue;
+        float v[16];
+        rld(P, 0, j, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = gelu_tc(v[i]);
+        put16(T, row, 16 * j - C * h, C, v);
+      }
+      if (!pipe_gemms(P, err, Gemm{P.tmem + 2 * C, kop(T, C), wop(smem + B1, C, 2 * C, 0, C * h), C, h > 0, C}))
+        break;
+    }
+    if (!P.ok) break;
+    const long v = v0 + row;
+    const float w = v < V ? __ldg(dw + v) : 0.f;
+    float vals[C];
+#pragma unroll
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      float r[16];
+      rld(P, 2 * C, j, r);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) vals[16 * j + i] = r[i];
+      if (v < V) {
+        st8(pre + v * C + 16 * j, r);
+        st8(pre + v * C + 16 * j + 8, r + 8);
+      }
+    }
+    row_stats<C>(P, vals, w, red, gm, &wsum, acc);
+  }
+  __syncthreads();
+  if (tid < GMAX) {
+    double* o = partials + ((long)blockIdx.x * GMAX + tid) * 3;
+    o[0] = acc[3 * tid];
+    o[1] = acc[3 * tid + 1];
+    o[2] = acc[3 * tid + 2];
+  }
+  pipe_finish(P, tslot, NCOL);
+}
+
+// The ffno_mlp2_bwd_tc contract at C = 96: a_bar = base + ((pre_bar W2) * gelu'(a W1^T)) W1, from the forward's pack
+// [w1 (2C x C), w2 (C x 2C)]: W2 and W1 as MN-major operands give the second and third GEMMs' transposes. Tensor
+// memory: D1 = a W1^T (2C) at 0, D2 = pre_bar W2 (2C) at 2C, D3 (C) at 4C.
+__global__ void __launch_bounds__(PT, 1) k_mlp2_bwd_tc96(const float* __restrict__ a, const float* __restrict__ pb,
+                                                         const float* __restrict__ base, long V,
+                                                         const uint8_t* __restrict__ wpack, float* __restrict__ abar,
+                                                         int* __restrict__ err) {
+  constexpr int C = C96;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(2 * C, C), B2 = mat_bytes(C, 2 * C);
+  PIPE_PROLOGUE(5 * C, 1)
+  const Split T = split_at(smem + B1 + B2, TM, C);
+  P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
+  const Op w1 = wop(smem, 2 * C, C), w2t = wop_t(smem + B1, C, 2 * C);
+  const int row = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    fill96(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(a + v * C + k, o); });
+    if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, C), w1, C, false, 2 * C})) break;
+    fill96(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(pb + v * C + k, o); });
+    if (!pipe_gemms(P, err, Gemm{P.tmem + 2 * C, kop(T, C), w2t, C, false, 2 * C})) break;
+    for (int h = 0; h < 2; ++h) {
+#pragma unroll 1
+      for (int j = 6 * h; j < 6 * h + 6; ++j) {
+        if (!owns(j, P.half)) continue;
+        float hp[16], gb[16];
+        rld(P, 0, j, hp);
+        rld(P, 2 * C, j, gb);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) gb[i] *= gelu_grad_tc(hp[i]);
+        put16(T, row, 16 * j - C * h, C, gb);
+      }
+      if (!pipe_gemms(P, err, Gemm{P.tmem + 4 * C, kop(T, C), wop_t(smem, 2 * C, C, C * h), C, h > 0, C})) break;
+    }
+    if (!P.ok) break;
+    const long v = v0 + row;
+#pragma unroll
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      float r[16];
+      rld(P, 4 * C, j, r);
+      if (v < V) {
+        if (base) {
+          float b[16];
+          ld8(base + v * C + 16 * j, *reinterpret_cast<float(*)[8]>(b));
+          ld8(base + v * C + 16 * j + 8, *reinterpret_cast<float(*)[8]>(b + 8));
+#pragma unroll
+          for (int i = 0; i < 16; ++i) r[i] += b[i];
+        }
+        st8(abar + v * C + 16 * j, r);
+        st8(abar + v * C + 16 * j + 8, r + 8);
+      }
+    }
+  }
+  pipe_finish(P, tslot, NCOL);
+}
+
 #undef PIPE_PROLOGUE
 
 int g_sms = 0;
@@ -1363,6 +1542,7 @@ bool launch_prep(K kernel, size_t bytes) {
 }
 
 bool tc_width(int C) { return C == 16 || C == 32 || C == 64; }
+bool mlp_width(int C) { return tc_width(C) || C == C96; }   // the channel MLPs also at the production width
 bool aligned16(const void* p) { return p && (reinterpret_cast<uintptr_t>(p) % 16) == 0; }
 bool aligned32(const void* p) { return p && (reinterpret_cast<uintptr_t>(p) % 32) == 0; }
 
@@ -1374,6 +1554,8 @@ extern "C" {
 int ffno_tc_parts(long V) { return grid_tc(V); }
 
 int ffno_tc_width_supported(int C) { return tc_width(C) ? 1 : 0; }
+
+int ffno_tc_mlp2_width_supported(int C) { return mlp_width(C) ? 1 : 0; }
 
 int ffno_tc_set_prefetch_tiles(int tiles) {
   if (tiles < 0 || tiles > 4) return FFNO_EINVAL;
@@ -1405,10 +1587,24 @@ int ffno_mlp2_fwd_tc(int mode, const float* in, const float* prev_pre, const flo
                      long V, int C, const void* wpack, const float* dw, float* pre, double* partials, int nparts,
                      int groups, int* err, ffno_stream_t stream) {
   if (!in || !wpack || !dw || !pre || !partials) return FFNO_EINVAL;
-  if (!tc_width(C) || V < 1 || mode < 0 || mode > 2 || groups != GMAX || !err || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!mlp_width(C) || V < 1 || mode < 0 || mode > 2 || groups != GMAX || !err || !aligned16(wpack)) return FFNO_EINVAL;
   if (mode && (!prev_pre || !prev_coefs || !xout)) return FFNO_EINVAL;
   if (nparts != grid_tc(V)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
+  if (C == C96) {   // rows are moved 32 bytes a request
+    if (!aligned32(in) || !aligned32(pre) || (mode && (!aligned32(prev_pre) || !aligned32(xout)))) return FFNO_EINVAL;
+    const auto* w = static_cast<const uint8_t*>(wpack);
+    const size_t smem = mat_bytes(2 * C96, C96) + mat_bytes(C96, 2 * C96) + tile_bytes(C96);
+#define L96(M)                                                                                                    \
+  if (mode == M) {                                                                                              \
+    if (!launch_prep(k_mlp2_tc96<M>, smem)) return FFNO_ELAUNCH;                                                \
+    k_mlp2_tc96<M><<<nparts, PT, smem, s>>>(in, prev_pre, prev_coefs, res, xout, V, w, dw, pre, partials, err); \
+  }
+    L96(0) L96(1) L96(2)
+#undef L96
+    FFNO_CHECK_LAUNCH();
+    return FFNO_OK;
+  }
   if (ws::mlp2_fwd_supported(C))
     return ws::mlp2_fwd(mode, in, prev_pre, prev_coefs, res, xout, V, C, wpack, dw, pre, partials, nparts, err, s);
   const auto* w = static_cast<const uint8_t*>(wpack);
@@ -1484,8 +1680,16 @@ int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* v
 
 int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack,
                      float* a_bar, int* err, ffno_stream_t stream) {
-  if (!a || !pre_bar || !wpack || !a_bar || !tc_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!a || !pre_bar || !wpack || !a_bar || !mlp_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
+  if (C == C96) {
+    if (!aligned32(a) || !aligned32(pre_bar) || !aligned32(a_bar) || (base && !aligned32(base))) return FFNO_EINVAL;
+    const size_t smem = mat_bytes(2 * C96, C96) + mat_bytes(C96, 2 * C96) + tile_bytes(C96);
+    if (!launch_prep(k_mlp2_bwd_tc96, smem)) return FFNO_ELAUNCH;
+    k_mlp2_bwd_tc96<<<grid_tc(V), PT, smem, s>>>(a, pre_bar, base, V, static_cast<const uint8_t*>(wpack), a_bar, err);
+    FFNO_CHECK_LAUNCH();
+    return FFNO_OK;
+  }
   if (ws::mlp2_bwd_supported(C)) return ws::mlp2_bwd(a, pre_bar, base, V, C, wpack, a_bar, err, s);
   TC_DISPATCH(C, {
     const size_t smem = 3 * mat_bytes(2 * CC, CC) + 2 * tile_bytes(2 * CC);

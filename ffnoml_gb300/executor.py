@@ -148,6 +148,8 @@ class Packed:
         self.lift_g, self.lift_b = dev(model.lift[1].weight.detach()), dev(model.lift[1].bias.detach())
         self.groups = model.lift[1].num_groups
         self.tc = bool(nat.lib().ffno_tc_width_supported(C)) and self.groups == 8
+        # the channel MLPs (the post-MLPs of both branches, pw, mlp) also run on tensor cores at width 96
+        self.tc_mlp = bool(nat.lib().ffno_tc_mlp2_width_supported(C)) and self.groups == 8
         self.blocks = []
         for b in model.blocks:
             s, v = b.spec, b.vertical
@@ -173,6 +175,8 @@ class Packed:
             pk["res"] = (float(b.res_fused.detach()), float(b.res_pw.detach()), float(b.res_mlp.detach()))
             if self.tc:
                 self._tc_block(pk, b, device)
+            elif self.tc_mlp:
+                self._tc_mlp_block(pk, b, device)
             self.blocks.append(pk)
         nh = model.proj2.out_channels
         self.nh = nh
@@ -222,6 +226,15 @@ class Packed:
             wb = _wbig(conv.weight_real, conv.weight_imag)
             pk[f"tc_{name}_mix"] = mix_pack(device, wb.t())      # out = xhat @ wbig -> matrix wbig^T
             pk[f"tcb_{name}_mix"] = mix_pack(device, wb)         # adjoint: xhat_bar = y_bar @ wbig^T
+
+    @staticmethod
+    def _tc_mlp_block(pk, b, device):
+        """Split-BF16 packs of one block's channel MLPs at width 96: [w1, w2] for the forward, and the same pack for
+        the backward (its kernel reads the transposes out of it)."""
+        s, v = b.spec, b.vertical
+        for name, (c1, c2) in dict(s_post=(s.post[0], s.post[2]), v_post=(v.post[0], v.post[2]),
+                                   pw=(b.pw[0], b.pw[2]), mlp=(b.mlp.net[0], b.mlp.net[3])).items():
+            pk["tc_" + name] = pk["tcb_" + name] = tc_pack(device, _w(c1), _w(c2))
 
     @staticmethod
     def _head_params(model):
@@ -794,6 +807,10 @@ class Executor:
         JVP, which is FP32)."""
         return self.model.precision == "bf16" and self._packed.tc and not getattr(self._tls, "fp32", False)
 
+    def _tc_mlp(self):
+        """Whether the channel MLPs run on the split-BF16 tensor-core kernels: wherever _tc() does, and at width 96."""
+        return self.model.precision == "bf16" and self._packed.tc_mlp and not getattr(self._tls, "fp32", False)
+
     def _tc_xf(self):
         """Whether the transforms and the height-table gradients run on the split-BF16 tensor-core kernels: precision
         'bf16' at any width (their operands are tables and data columns, not channel matrices), never inside a JVP.
@@ -811,7 +828,7 @@ class Executor:
         """ffno_mlp2_fwd (FP32) or its tensor-core twin; returns whether the tensor-core path ran."""
         m = self.model
         C, V, s, G = m.width, ws.V, _stream(), self._packed.groups
-        if self._tc():
+        if self._tc_mlp():
             nat.call("ffno_mlp2_fwd_tc", mode, inp.data_ptr(), _ptr(prev), _ptr(pcoefs), res, _ptr(xout), V, C,
                      pack.data_ptr(), ws.dw.data_ptr(), pre.data_ptr(), ws.partials.data_ptr(), ws.nparts_tc, G,
                      ws.err.data_ptr(), s)
@@ -1044,11 +1061,11 @@ class Executor:
         r_f, r_pw, r_mlp = bp["res"]
         live = hgt["live"]
         d = _descs(D, H, W, C, live)
-        tc = self._tc()
+        tc, tc_mlp = self._tc(), self._tc_mlp()
         err = ws.err.data_ptr()
 
         def mlp_bwd(a, pb, base, out, w1, w2t, w1t, pack):
-            if tc:
+            if tc_mlp:
                 nat.call("ffno_mlp2_bwd_tc", a.data_ptr(), pb.data_ptr(), _ptr(base), V, C, bp[pack].data_ptr(),
                          out.data_ptr(), err, s)
             else:
@@ -1061,10 +1078,12 @@ class Executor:
         # x2 = x1 + r_pw GN(pw_pre); pw_pre = pw(x1)
         self._gn_bwd(ws, gb, 0, gb.g2, r_pw, ws.pw_pre, bp["pw_g"], bp["pw_b"], "pw", gb.pbar)
         mlp_bwd(ws.x1, gb.pbar, gb.g2, gb.g1, "pw1", "pw2t", "pw1t", "tcb_pw")
-        # GELU after a GroupNorm: the tensor-core forward applies the A&S activation (mode 2), the FP32 one erf's
+        # GELU after a GroupNorm: the tensor-core forward applies the A&S activation (mode 2), the FP32 one erf's; the
+        # fuse norm's GELU is applied by the pw MLP's prologue, the spec / vert norms' by the fusion
         act = 2 if tc else 1
         # x1 = x + r_f gelu(GN(fused_pre)); fused_pre = fuse(x, spec, vert)
-        self._gn_bwd(ws, gb, act, gb.g1, r_f, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], "fuse", gb.pbar)
+        self._gn_bwd(ws, gb, 2 if tc_mlp else 1, gb.g1, r_f, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], "fuse",
+                     gb.pbar)
         if tc:
             hg = ws.hg                     # gates and hidden layer kept from the forward, else recomputed
             if hg is None:

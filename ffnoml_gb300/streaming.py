@@ -670,7 +670,7 @@ class StreamingVJP(StreamingForward):
                  pbar.data_ptr(), self.wbar[o:].data_ptr(), _stream())
 
     def _mlp_bwd(self, bp, a, pb, base, out, w1, w2t, w1t, pack, V, err):
-        if self.ex._tc():
+        if self.ex._tc_mlp():
             nat.call("ffno_mlp2_bwd_tc", a.data_ptr(), pb.data_ptr(), None if base is None else base.data_ptr(), V,
                      self.C, bp[pack].data_ptr(), out.data_ptr(), err.data_ptr(), _stream())
         else:
@@ -688,7 +688,8 @@ class StreamingVJP(StreamingForward):
         C, D, H, W, HW, Wf = self.C, self.D, self.H, self.W, self.HW, self.W // 2 + 1
         live, tc, s = cx.live, ex._tc(), _stream()
         r_f, r_pw, r_mlp = bp["res"]
-        act = 2 if tc else 1      # GELU after the spec / vert / fuse GroupNorms, as the forward applied it
+        act = 2 if tc else 1      # GELU after the spec / vert GroupNorms, as the forward applied it
+        act_f = 2 if ex._tc_mlp() else 1   # after the fuse GroupNorm (applied by the pw MLP's prologue)
         depth = list(self._depth_slabs())
         gbd, gbr = self.gbd, self.gbr
         Gout, GA, T1, T2, T3 = hb["G"], hb["GA"], hb["T1"], hb["T2"], hb["T3"]
@@ -722,11 +723,11 @@ class StreamingVJP(StreamingForward):
                   [S["pw_pre"], S["x1"]])), pw_stage, self._st_gb(gbd, "g2", T2))
         # x1 = x + r_f gelu(GN(fused_pre)), fused_pre = fuse(x, spec, vert) -> x_bar so far (GA), spec_bar (T1),
         # vert_bar (T3)
-        self._gn_bwd_stats("fuse", act, r_f, T2, S["fused_pre"], bp["fuse_g"], bp["fuse_b"])
+        self._gn_bwd_stats("fuse", act_f, r_f, T2, S["fused_pre"], bp["fuse_g"], bp["fuse_b"])
 
         def fuse_stage(ws, it):
             gb = gbd[ws.buf]
-            self._gn_apply("fuse", act, r_f, ws, gb.xbar, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], gb.pbar, it)
+            self._gn_apply("fuse", act_f, r_f, ws, gb.xbar, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], gb.pbar, it)
             cs, cv = self.coefs["spec"].data_ptr(), self.coefs["vert"].data_ptr()
             if tc:
                 ex._fuse1_tc(ws, bp, ws.x, gb.hg)

@@ -334,11 +334,14 @@ int ffno_si_input_grads(const float* features, const float* x_bar, const float* 
  * ------------------------------------------------------------------------------------------------------------------ */
 int ffno_tc_parts(long V);
 int ffno_tc_width_supported(int C);
+/* Widths of ffno_mlp2_fwd_tc / ffno_mlp2_bwd_tc: also C = 96, the production model's width (the channel MLPs there
+ * run on tensor cores while the gates, fusion, mixing and head keep their FP32 entry points). */
+int ffno_tc_mlp2_width_supported(int C);
 /* L2 prefetch lookahead of the tensor-core pointwise kernels on the current device, in tiles of 128 voxels per
  * pipeline (0..4; default 0): a tuning knob, synchronous, not to be called while those kernels run. */
 int ffno_tc_set_prefetch_tiles(int tiles);
 
-/* ffno_mlp2_fwd; wpack = [w1 (2C x C), w2 (C x 2C)]. */
+/* ffno_mlp2_fwd; wpack = [w1 (2C x C), w2 (C x 2C)]. C = 96 also (in, pre, prev_pre, xout 32-byte aligned). */
 int ffno_mlp2_fwd_tc(int mode, const float* in, const float* prev_pre, const float* prev_coefs, float res, float* xout,
                      long V, int C, const void* wpack, const float* dw, float* pre, double* partials, int nparts,
                      int groups, int* err, ffno_stream_t stream);
@@ -355,7 +358,8 @@ int ffno_fuse1_tc(const float* x, const float* spec_pre, const float* spec_coefs
 int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
                   const float* gates, long V, int C, const void* wpack, const float* dw, float* pre, double* partials,
                   int nparts, int groups, int* err, ffno_stream_t stream);
-/* ffno_mlp2_bwd; wpack = [w1 (2C x C), w2^T (2C x C), w1^T (C x 2C)]. */
+/* ffno_mlp2_bwd; wpack = [w1 (2C x C), w2^T (2C x C), w1^T (C x 2C)]; at C = 96 the forward's pack [w1 (2C x C),
+ * w2 (C x 2C)] (the kernel reads the transposes out of it; a, pre_bar, base, a_bar 32-byte aligned). */
 int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack,
                      float* a_bar, int* err, ffno_stream_t stream);
 /* One branch of ffno_gate_bwd: x_bar = base + d/dx applied to g_bar, z_bar += g_bar . zp if zp; wpack = [g1, g2,

@@ -53,8 +53,9 @@ def test_bf16_forward_and_vjp_against_reference_float64(name):
     y, xb, zb = _run(model, a, meta)
     err = (y - a["y64"]).abs().max().item()
     ex = _rel(xb, a["xbar"])
-    print(f"{name} bf16: max |d log10 n| {err:.2e}, x_bar rel {ex:.2e}, channel kernels on tensor cores: "
-          f"{model.executor()._packed.tc}, transforms on tensor cores: {model.executor()._tc_xf()}")
+    ex_ = model.executor()
+    print(f"{name} bf16: max |d log10 n| {err:.2e}, x_bar rel {ex:.2e}, tensor cores: every kernel family "
+          f"{ex_._packed.tc}, channel MLPs {ex_._tc_mlp()}, transforms {ex_._tc_xf()}")
     assert err <= 2e-3
     assert ex <= 1e-2
 

@@ -65,10 +65,12 @@ def _coefs(C, seed):
     return c.reshape(-1).cuda().contiguous()
 
 
-@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (64, 152 * 128 * 5 + 77)])
+@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (64, 152 * 128 * 5 + 77), (96, V),
+                                 (96, 152 * 128 * 3 + 77)])
 @pytest.mark.parametrize("mode", [0, 1, 2])
 def test_mlp2_fwd_tc(C, V, mode):
-    """Also at a voxel count that sends several tiles through every CTA's two-stage ring, with a ragged last tile."""
+    """Also at a voxel count that sends several tiles through every CTA's two-stage ring, with a ragged last tile; and
+    at width 96 (one pipeline a CTA, the hidden layer in two K-halves, GroupNorm groups of 12 channels)."""
     nat = _nat()
     x, prev = _rand(V, C, seed=1), _rand(V, C, seed=2)
     pc = _coefs(C, 3)
@@ -154,9 +156,11 @@ def test_fuse_fwd_tc(C, V):
     _close(b, a)
 
 
-@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (32, 152 * 128 * 5 + 77), (64, 152 * 128 * 5 + 77)])
+@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (32, 152 * 128 * 5 + 77), (64, 152 * 128 * 5 + 77),
+                                 (96, V), (96, 152 * 128 * 3 + 77)])
 def test_mlp2_bwd_tc(C, V):
-    """Also at a voxel count that sends several tiles through every CTA's two-stage ring, with a ragged last tile."""
+    """Also at a voxel count that sends several tiles through every CTA's two-stage ring, with a ragged last tile. At
+    width 96 the pack is the forward's [w1, w2]: the kernel reads W2 and W1 as MN-major operands (their transposes)."""
     nat = _nat()
     a, pb, base = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3)
     w1, w2 = _rand(2 * C, C, seed=4, scale=C ** -0.5), _rand(C, 2 * C, seed=5, scale=(2 * C) ** -0.5)
@@ -165,8 +169,9 @@ def test_mlp2_bwd_tc(C, V):
     # FP32 kernel wants w1 [C][2C] (in x out), w2t = W2^T laid [C][2C], w1t [2C][C]
     nat.call("ffno_mlp2_bwd", a.data_ptr(), pb.data_ptr(), base.data_ptr(), V, C, _hold(w1.t().contiguous()),
              _hold(w2.contiguous()), _hold(w1.contiguous()), r0.data_ptr(), _s())
-    nat.call("ffno_mlp2_bwd_tc", a.data_ptr(), pb.data_ptr(), base.data_ptr(), V, C,
-             _pack(w1, w2.t(), w1.t()).data_ptr(), r1.data_ptr(), err.data_ptr(), _s())
+    pack = _pack(w1, w2) if C == 96 else _pack(w1, w2.t(), w1.t())
+    nat.call("ffno_mlp2_bwd_tc", a.data_ptr(), pb.data_ptr(), base.data_ptr(), V, C, pack.data_ptr(), r1.data_ptr(),
+             err.data_ptr(), _s())
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     _close(r1, r0)
