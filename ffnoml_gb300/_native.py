@@ -94,7 +94,7 @@ PROTOTYPES = {
     "ffno_tc_selftest": [P, P, I, I, I, P, P, P],
     "ffno_tc_parts": [L],
     "ffno_tc_width_supported": [I],
-    "ffno_tc_mlp2_width_supported": [I],
+    "ffno_tc_channel_width_supported": [I],
     "ffno_tc_set_prefetch_tiles": [I],
     "ffno_copy2d": [P, L, P, L, L, L, P],
     "ffno_reverse_axes4": [P, L, L, L, L, P, P],

@@ -284,6 +284,55 @@ __device__ __forceinline__ void fill_tile8(Split t, long v0, long V, int ptid, F
   }
 }
 
+// The production model's width: rows of 12 octets, weights read as transposes (below and in the width-96 kernels).
+constexpr int C96 = 96;
+
+// the transpose of the K-major weight matrix [R][K] at p, as the MN-major operand [N = K][K' = R] from k' = r0
+__device__ __forceinline__ Op wop_t(const uint8_t* p, int R, int K, int r0 = 0) {
+  const uint32_t h = tc::smem_u32(p) + (uint32_t)(r0 / 8) * (uint32_t)K * 16u;
+  return Op{h, h + (uint32_t)R * K * 2, (uint32_t)K * 16u, 128u, (uint32_t)K * 32u, true};
+}
+
+// fill_tile8 for 96 columns (12 octets a row, so a thread's columns change from piece to piece)
+template <typename F>
+__device__ __forceinline__ void fill96(Split t, long v0, long V, int ptid, F f) {
+  constexpr int KB = C96 / 8, NE = TM * KB, FB8 = FB / 2;
+  for (int e0 = ptid; e0 < NE; e0 += PT * FB8) {
+    float a[FB8][8];
+#pragma unroll
+    for (int u = 0; u < FB8; ++u) {   // the loads of FB8 pieces issued before any is converted
+      const int e = e0 + u * PT;
+      const int r8 = e & 7, q = e >> 3;
+      const long v = v0 + (q / KB) * 8 + r8;
+      if (e < NE && v < V) {
+        f(v, (q % KB) * 8, a[u]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[u][i] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < FB8; ++u) {
+      const int e = e0 + u * PT;
+      if (e >= NE) break;
+      uint32_t h[4], l[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) tc::split_pack(a[u][2 * i], a[u][2 * i + 1], h[i], l[i]);
+      *reinterpret_cast<uint4*>(t.hi() + (size_t)e * 16) = make_uint4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<uint4*>(t.lo() + (size_t)e * 16) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+  }
+}
+
+// Plain FP32 rows [V][C] of src into a split K-major tile [128][C]; every width, 96 included (12 octets a row).
+template <int C>
+__device__ __forceinline__ void fill_rows(Split t, long v0, long V, int ptid, const float* __restrict__ src) {
+  if constexpr (C == 96)
+    fill96(t, v0, V, ptid, [&](long v, int k, float (&o)[8]) { ld8(src + v * C + k, o); });
+  else
+    fill_tile<C>(t, v0, V, ptid, [&](long v, int k) { return ld4(src + v * C + k); });
+}
+
 // The tile's depth weights into shared memory (wt[128]) and their warp partial sums (wpart[4]); threads ptid < 128.
 __device__ __forceinline__ void load_tile_weights(const Pipe& p, const float* __restrict__ dw, long v0, long V,
                                                   float* wt, float* wpart) {
@@ -587,7 +636,7 @@ __global__ void __launch_bounds__(CT, 1) k_gate_tc(const float* __restrict__ x, 
       const long tp = t + pf * tstep;
       prefetch_rows(x, tp * TM, V, C);
     }
-    fill_tile<C>(X, v0, V, P.ptid, [&](long v, int k) { return ld4(x + v * C + k); });
+    fill_rows<C>(X, v0, V, P.ptid, x);
     if (!pipe_gemms(P, err, Gemm{P.tmem, kop(X, C), g1, C, false, C})) break;
 #pragma unroll
     for (int j = 0; j < C / 16; ++j) {
@@ -870,20 +919,24 @@ __global__ void __launch_bounds__(CT, 1) k_mlp2_bwd_tc(const float* __restrict__
 
 // One input gate's backward: x_bar = base + d/dx [x sigmoid(gelu(x G1) G2)] applied to gbar; with zp, z_bar[v] +=
 // sum_c gbar zp. Weights: [g1, g2, g2t, g1t] (each C x C). All four GEMMs have C outputs and run untransposed.
-template <int C>
-__global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__ x, const float* __restrict__ gbar,
-                                                       const float* __restrict__ base, long V,
-                                                       const uint8_t* __restrict__ wpack, const float* __restrict__ zp,
-                                                       float* __restrict__ xbar, float* __restrict__ zbar,
-                                                       int* __restrict__ err) {
+// At C = 96 (one pipeline a CTA: tensor memory holds 4C columns) the pack is [g1, g2] and the transposes are read out
+// of it as MN-major operands.
+template <int C, int NP = 2>
+__global__ void __launch_bounds__(NP * PT, 1) k_gate_bwd_tc(const float* __restrict__ x, const float* __restrict__ gbar,
+                                                            const float* __restrict__ base, long V,
+                                                            const uint8_t* __restrict__ wpack,
+                                                            const float* __restrict__ zp, float* __restrict__ xbar,
+                                                            float* __restrict__ zbar, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  constexpr uint32_t B1 = mat_bytes(C, C), RB = 2 * tile_bytes(C);
-  __shared__ float zsh[2][TM];
-  PIPE_PROLOGUE(4 * C, 2)
-  const Split X = split_at(smem + 4 * B1 + pid * RB, TM, C), T = split_at(smem + 4 * B1 + pid * RB + tile_bytes(C), TM, C);
-  P.ok = load_weights(smem, wpack, 4 * B1, wcx, err);
-  const Op g1 = wop(smem, C, C), g2 = wop(smem + B1, C, C), g2t = wop(smem + 2 * B1, C, C),
-           g1t = wop(smem + 3 * B1, C, C);
+  constexpr bool TW = C == 96;                   // transposes from the forward's matrices
+  constexpr uint32_t B1 = mat_bytes(C, C), RB = 2 * tile_bytes(C), WB = (TW ? 2 : 4) * B1;
+  __shared__ float zsh[NP][TM];
+  PIPE_PROLOGUE(4 * C, NP)
+  const Split X = split_at(smem + WB + pid * RB, TM, C), T = split_at(smem + WB + pid * RB + tile_bytes(C), TM, C);
+  P.ok = load_weights(smem, wpack, WB, wcx, err);
+  const Op g1 = wop(smem, C, C), g2 = wop(smem + B1, C, C);
+  const Op g2t = TW ? wop_t(smem + B1, C, C) : wop(smem + 2 * B1, C, C);
+  const Op g1t = TW ? wop_t(smem, C, C) : wop(smem + 3 * B1, C, C);
   const uint32_t D1 = 0, D2 = C, D3 = 2 * C, D4 = 3 * C;
   const int row = P.feat();
   const int pf = c_pf;
@@ -902,7 +955,7 @@ __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__
       prefetch_rows(base, tp * TM, V, C);
     }
     const long v = v0 + row;
-    fill_tile<C>(X, v0, V, P.ptid, [&](long vv, int k) { return ld4(x + vv * C + k); });
+    fill_rows<C>(X, v0, V, P.ptid, x);
     if (!pipe_gemms(P, err, Gemm{P.tmem + D1, kop(X, C), g1, C, false, C})) break;
 #pragma unroll
     for (int j = 0; j < C / 16; ++j) {
@@ -971,7 +1024,7 @@ __global__ void __launch_bounds__(CT, 1) k_gate_bwd_tc(const float* __restrict__
           *reinterpret_cast<float4*>(xbar + v * C + c0 + i) = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
     }
   }
-  pipe_finish(P, tslot, 2 * NCOL);
+  pipe_finish(P, tslot, NP * NCOL);
 }
 
 // Fuse backward, stage a: hf_bar_pre = (F_bar Wf2^T) * gelu'(B Wf1) with B = [spec gs, vert gv], F_bar =
@@ -1343,45 +1396,6 @@ __global__ void __launch_bounds__(CT, 1) k_head_bwd_tc(const float* __restrict__
 // as in the other row-oriented kernels). The 2C = 192 hidden features pass through one [128][96] operand tile in two
 // K-halves. The backward reads its transposed weights out of the forward's matrices: a K-major [R][K] matrix read as
 // an MN-major operand is its transpose ([K][R]), so one 144 KB pack serves all three of its GEMMs.
-constexpr int C96 = 96;
-
-// the transpose of the K-major weight matrix [R][K] at p, as the MN-major operand [N = K][K' = R] from k' = r0
-__device__ __forceinline__ Op wop_t(const uint8_t* p, int R, int K, int r0 = 0) {
-  const uint32_t h = tc::smem_u32(p) + (uint32_t)(r0 / 8) * (uint32_t)K * 16u;
-  return Op{h, h + (uint32_t)R * K * 2, (uint32_t)K * 16u, 128u, (uint32_t)K * 32u, true};
-}
-
-// fill_tile8 for 96 columns (12 octets a row, so a thread's columns change from piece to piece)
-template <typename F>
-__device__ __forceinline__ void fill96(Split t, long v0, long V, int ptid, F f) {
-  constexpr int KB = C96 / 8, NE = TM * KB, FB8 = FB / 2;
-  for (int e0 = ptid; e0 < NE; e0 += PT * FB8) {
-    float a[FB8][8];
-#pragma unroll
-    for (int u = 0; u < FB8; ++u) {   // the loads of FB8 pieces issued before any is converted
-      const int e = e0 + u * PT;
-      const int r8 = e & 7, q = e >> 3;
-      const long v = v0 + (q / KB) * 8 + r8;
-      if (e < NE && v < V) {
-        f(v, (q % KB) * 8, a[u]);
-      } else {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) a[u][i] = 0.f;
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < FB8; ++u) {
-      const int e = e0 + u * PT;
-      if (e >= NE) break;
-      uint32_t h[4], l[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) tc::split_pack(a[u][2 * i], a[u][2 * i + 1], h[i], l[i]);
-      *reinterpret_cast<uint4*>(t.hi() + (size_t)e * 16) = make_uint4(h[0], h[1], h[2], h[3]);
-      *reinterpret_cast<uint4*>(t.lo() + (size_t)e * 16) = make_uint4(l[0], l[1], l[2], l[3]);
-    }
-  }
-}
-
 // The ffno_mlp2_fwd_tc contract at C = 96: pre = gelu(X W1^T) W2^T with X = in (+ res GN(prev) [gelu] in modes 1 and
 // 2, written to xout), and the GroupNorm partials of pre. Weights [w1 (2C x C), w2 (C x 2C)]. Tensor memory: D1 (2C
 // columns) at 0, D2 (C) at 2C.
@@ -1542,7 +1556,7 @@ bool launch_prep(K kernel, size_t bytes) {
 }
 
 bool tc_width(int C) { return C == 16 || C == 32 || C == 64; }
-bool mlp_width(int C) { return tc_width(C) || C == C96; }   // the channel MLPs also at the production width
+bool chan_width(int C) { return tc_width(C) || C == C96; }   // channel MLPs and input gates: also width 96
 bool aligned16(const void* p) { return p && (reinterpret_cast<uintptr_t>(p) % 16) == 0; }
 bool aligned32(const void* p) { return p && (reinterpret_cast<uintptr_t>(p) % 32) == 0; }
 
@@ -1555,7 +1569,7 @@ int ffno_tc_parts(long V) { return grid_tc(V); }
 
 int ffno_tc_width_supported(int C) { return tc_width(C) ? 1 : 0; }
 
-int ffno_tc_mlp2_width_supported(int C) { return mlp_width(C) ? 1 : 0; }
+int ffno_tc_channel_width_supported(int C) { return chan_width(C) ? 1 : 0; }
 
 int ffno_tc_set_prefetch_tiles(int tiles) {
   if (tiles < 0 || tiles > 4) return FFNO_EINVAL;
@@ -1587,7 +1601,7 @@ int ffno_mlp2_fwd_tc(int mode, const float* in, const float* prev_pre, const flo
                      long V, int C, const void* wpack, const float* dw, float* pre, double* partials, int nparts,
                      int groups, int* err, ffno_stream_t stream) {
   if (!in || !wpack || !dw || !pre || !partials) return FFNO_EINVAL;
-  if (!mlp_width(C) || V < 1 || mode < 0 || mode > 2 || groups != GMAX || !err || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!chan_width(C) || V < 1 || mode < 0 || mode > 2 || groups != GMAX || !err || !aligned16(wpack)) return FFNO_EINVAL;
   if (mode && (!prev_pre || !prev_coefs || !xout)) return FFNO_EINVAL;
   if (nparts != grid_tc(V)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
@@ -1627,9 +1641,17 @@ int ffno_mlp2_fwd_tc(int mode, const float* in, const float* prev_pre, const flo
 
 int ffno_gate_fwd_tc(const float* x, long V, int C, const void* wpack, const float* zp, const float* z, float* out,
                      int* err, ffno_stream_t stream) {
-  if (!x || !wpack || !out || !tc_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z)) return FFNO_EINVAL;
+  if (!x || !wpack || !out || !chan_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   if (ws::gate_fwd_supported(C)) return ws::gate_fwd(x, V, C, wpack, zp, z, out, err, s);
+  if (C == C96) {
+    if (!aligned32(x)) return FFNO_EINVAL;   // rows are read 32 bytes a request
+    const size_t smem = 2 * mat_bytes(C96, C96) + 2 * tile_bytes(C96);
+    if (!launch_prep(k_gate_tc<C96>, smem)) return FFNO_ELAUNCH;
+    k_gate_tc<C96><<<grid_tc(V), CT, smem, s>>>(x, V, static_cast<const uint8_t*>(wpack), zp, z, out, err);
+    FFNO_CHECK_LAUNCH();
+    return FFNO_OK;
+  }
   TC_DISPATCH(C, {
     const size_t smem = 2 * mat_bytes(CC, CC) + 2 * tile_bytes(CC);
     if (!launch_prep(k_gate_tc<CC>, smem)) return FFNO_ELAUNCH;
@@ -1680,7 +1702,7 @@ int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* v
 
 int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack,
                      float* a_bar, int* err, ffno_stream_t stream) {
-  if (!a || !pre_bar || !wpack || !a_bar || !mlp_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!a || !pre_bar || !wpack || !a_bar || !chan_width(C) || V < 1 || !err || !aligned16(wpack)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   if (C == C96) {
     if (!aligned32(a) || !aligned32(pre_bar) || !aligned32(a_bar) || (base && !aligned32(base))) return FFNO_EINVAL;
@@ -1704,9 +1726,18 @@ int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, lo
 int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long V, int C, const void* wpack,
                      const float* zp, float* x_bar, float* z_bar, int* err, ffno_stream_t stream) {
   if (!x || !g_bar || !wpack || !x_bar) return FFNO_EINVAL;
-  if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z_bar)) return FFNO_EINVAL;
+  if (!chan_width(C) || V < 1 || !err || !aligned16(wpack) || (zp && !z_bar)) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   if (ws::gate_bwd_supported(C)) return ws::gate_bwd(x, g_bar, base, V, C, wpack, zp, x_bar, z_bar, err, s);
+  if (C == C96) {
+    if (!aligned32(x)) return FFNO_EINVAL;
+    const size_t smem = 2 * mat_bytes(C96, C96) + 2 * tile_bytes(C96);   // one pipeline; pack [g1, g2]
+    if (!launch_prep(k_gate_bwd_tc<C96, 1>, smem)) return FFNO_ELAUNCH;
+    k_gate_bwd_tc<C96, 1><<<grid_tc(V), PT, smem, s>>>(x, g_bar, base, V, static_cast<const uint8_t*>(wpack), zp,
+                                                       x_bar, z_bar, err);
+    FFNO_CHECK_LAUNCH();
+    return FFNO_OK;
+  }
   TC_DISPATCH(C, {
     const size_t smem = 4 * mat_bytes(CC, CC) + 4 * tile_bytes(CC);
     if (!launch_prep(k_gate_bwd_tc<CC>, smem)) return FFNO_ELAUNCH;

@@ -148,8 +148,9 @@ class Packed:
         self.lift_g, self.lift_b = dev(model.lift[1].weight.detach()), dev(model.lift[1].bias.detach())
         self.groups = model.lift[1].num_groups
         self.tc = bool(nat.lib().ffno_tc_width_supported(C)) and self.groups == 8
-        # the channel MLPs (the post-MLPs of both branches, pw, mlp) also run on tensor cores at width 96
-        self.tc_mlp = bool(nat.lib().ffno_tc_mlp2_width_supported(C)) and self.groups == 8
+        # the channel MLPs (the post-MLPs of both branches, pw, mlp) and the input gates also run on tensor cores at
+        # width 96
+        self.tc_chan = bool(nat.lib().ffno_tc_channel_width_supported(C)) and self.groups == 8
         self.blocks = []
         for b in model.blocks:
             s, v = b.spec, b.vertical
@@ -175,8 +176,8 @@ class Packed:
             pk["res"] = (float(b.res_fused.detach()), float(b.res_pw.detach()), float(b.res_mlp.detach()))
             if self.tc:
                 self._tc_block(pk, b, device)
-            elif self.tc_mlp:
-                self._tc_mlp_block(pk, b, device)
+            elif self.tc_chan:
+                self._tc_chan_block(pk, b, device)
             self.blocks.append(pk)
         nh = model.proj2.out_channels
         self.nh = nh
@@ -228,12 +229,14 @@ class Packed:
             pk[f"tcb_{name}_mix"] = mix_pack(device, wb)         # adjoint: xhat_bar = y_bar @ wbig^T
 
     @staticmethod
-    def _tc_mlp_block(pk, b, device):
-        """Split-BF16 packs of one block's channel MLPs at width 96: [w1, w2] for the forward, and the same pack for
-        the backward (its kernel reads the transposes out of it)."""
+    def _tc_chan_block(pk, b, device):
+        """Split-BF16 packs of one block's channel MLPs and input gates at width 96: [w1, w2] for the forward, and the
+        same pack for the backward (its kernels read the transposes out of it)."""
         s, v = b.spec, b.vertical
         for name, (c1, c2) in dict(s_post=(s.post[0], s.post[2]), v_post=(v.post[0], v.post[2]),
-                                   pw=(b.pw[0], b.pw[2]), mlp=(b.mlp.net[0], b.mlp.net[3])).items():
+                                   pw=(b.pw[0], b.pw[2]), mlp=(b.mlp.net[0], b.mlp.net[3]),
+                                   s_gate=(s.input_gate[0], s.input_gate[2]),
+                                   v_gate=(v.input_gate[0], v.input_gate[2])).items():
             pk["tc_" + name] = pk["tcb_" + name] = tc_pack(device, _w(c1), _w(c2))
 
     @staticmethod
@@ -705,7 +708,7 @@ class Executor:
         x = ws.x if x_in is None else x_in
         live = hgt["live"]
         d = _descs(D, H, W, C, live)
-        if self._tc():
+        if self._tc_chan():
             nat.call("ffno_gate_fwd_tc", x.data_ptr(), V, C, bp["tc_s_gate"].data_ptr(), None, None, ws.xs.data_ptr(),
                      ws.err.data_ptr(), s)
             nat.call("ffno_gate_fwd_tc", x.data_ptr(), V, C, bp["tc_v_gate"].data_ptr(), bp["v_zp"].data_ptr(),
@@ -807,9 +810,10 @@ class Executor:
         JVP, which is FP32)."""
         return self.model.precision == "bf16" and self._packed.tc and not getattr(self._tls, "fp32", False)
 
-    def _tc_mlp(self):
-        """Whether the channel MLPs run on the split-BF16 tensor-core kernels: wherever _tc() does, and at width 96."""
-        return self.model.precision == "bf16" and self._packed.tc_mlp and not getattr(self._tls, "fp32", False)
+    def _tc_chan(self):
+        """Whether the channel MLPs and input gates run on the split-BF16 tensor-core kernels: wherever _tc() does,
+        and at width 96."""
+        return self.model.precision == "bf16" and self._packed.tc_chan and not getattr(self._tls, "fp32", False)
 
     def _tc_xf(self):
         """Whether the transforms and the height-table gradients run on the split-BF16 tensor-core kernels: precision
@@ -828,7 +832,7 @@ class Executor:
         """ffno_mlp2_fwd (FP32) or its tensor-core twin; returns whether the tensor-core path ran."""
         m = self.model
         C, V, s, G = m.width, ws.V, _stream(), self._packed.groups
-        if self._tc_mlp():
+        if self._tc_chan():
             nat.call("ffno_mlp2_fwd_tc", mode, inp.data_ptr(), _ptr(prev), _ptr(pcoefs), res, _ptr(xout), V, C,
                      pack.data_ptr(), ws.dw.data_ptr(), pre.data_ptr(), ws.partials.data_ptr(), ws.nparts_tc, G,
                      ws.err.data_ptr(), s)
@@ -1061,11 +1065,11 @@ class Executor:
         r_f, r_pw, r_mlp = bp["res"]
         live = hgt["live"]
         d = _descs(D, H, W, C, live)
-        tc, tc_mlp = self._tc(), self._tc_mlp()
+        tc, tc_chan = self._tc(), self._tc_chan()
         err = ws.err.data_ptr()
 
         def mlp_bwd(a, pb, base, out, w1, w2t, w1t, pack):
-            if tc_mlp:
+            if tc_chan:
                 nat.call("ffno_mlp2_bwd_tc", a.data_ptr(), pb.data_ptr(), _ptr(base), V, C, bp[pack].data_ptr(),
                          out.data_ptr(), err, s)
             else:
@@ -1082,7 +1086,7 @@ class Executor:
         # fuse norm's GELU is applied by the pw MLP's prologue, the spec / vert norms' by the fusion
         act = 2 if tc else 1
         # x1 = x + r_f gelu(GN(fused_pre)); fused_pre = fuse(x, spec, vert)
-        self._gn_bwd(ws, gb, 2 if tc_mlp else 1, gb.g1, r_f, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], "fuse",
+        self._gn_bwd(ws, gb, 2 if tc_chan else 1, gb.g1, r_f, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], "fuse",
                      gb.pbar)
         if tc:
             hg = ws.hg                     # gates and hidden layer kept from the forward, else recomputed
@@ -1134,7 +1138,7 @@ class Executor:
             self._outer(ws, ws.vb, 2 * live, ws.xv, D, N, gb.opart, gb.osplit_f, tzf_bar)
             self._xf(hgt, "tzf_t", ws.vb, gb.xvb, d["zi"], ws)
         # input gates (and z_proj)
-        if tc:
+        if tc_chan:
             nat.call("ffno_gate_bwd_tc", x.data_ptr(), gb.xsb.data_ptr(), gb.xacc.data_ptr(), V, C,
                      bp["tcb_s_gate"].data_ptr(), None, gb.xbar.data_ptr(), None, err, s)
             nat.call("ffno_gate_bwd_tc", x.data_ptr(), gb.xvb.data_ptr(), gb.xbar.data_ptr(), V, C,

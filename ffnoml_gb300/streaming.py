@@ -363,7 +363,7 @@ class StreamingForward:
         C, D, H, W, HW, Wf = self.C, self.D, self.H, self.W, self.HW, self.W // 2 + 1
         bp = pk.blocks[i]
         live = hgt["live"]
-        tc = ex._tc()
+        tc, tcg = ex._tc(), ex._tc_chan()      # every kernel family / the channel MLPs and input gates
         r_f, r_pw, r_mlp = bp["res"]
         depth = list(self._depth_slabs())
         ld = lambda names, hosts: (lambda ws, it: self._load(ws, names, it[0], it[1], hosts))
@@ -372,7 +372,7 @@ class StreamingForward:
         # horizontal spectral branch over depth slabs -> spec_pre (A)
         def spectral(ws, it):
             s, Ds = _stream(), it[1] - it[0]
-            if tc:
+            if tcg:
                 nat.call("ffno_gate_fwd_tc", ws.x.data_ptr(), ws.V, C, bp["tc_s_gate"].data_ptr(), None, None,
                          ws.xs.data_ptr(), ws.err.data_ptr(), s)
             else:
@@ -405,7 +405,7 @@ class StreamingForward:
 
         def vertical(ws, it):
             s, rows = _stream(), it[1] - it[0]
-            if tc:
+            if tcg:
                 nat.call("ffno_gate_fwd_tc", ws.x.data_ptr(), ws.V, C, bp["tc_v_gate"].data_ptr(), bp["v_zp"].data_ptr(),
                          ws.zr.data_ptr(), ws.xv.data_ptr(), ws.err.data_ptr(), s)
             else:
@@ -670,7 +670,7 @@ class StreamingVJP(StreamingForward):
                  pbar.data_ptr(), self.wbar[o:].data_ptr(), _stream())
 
     def _mlp_bwd(self, bp, a, pb, base, out, w1, w2t, w1t, pack, V, err):
-        if self.ex._tc_mlp():
+        if self.ex._tc_chan():
             nat.call("ffno_mlp2_bwd_tc", a.data_ptr(), pb.data_ptr(), None if base is None else base.data_ptr(), V,
                      self.C, bp[pack].data_ptr(), out.data_ptr(), err.data_ptr(), _stream())
         else:
@@ -686,10 +686,10 @@ class StreamingVJP(StreamingForward):
         pk = cx.pk
         bp = pk.blocks[i]
         C, D, H, W, HW, Wf = self.C, self.D, self.H, self.W, self.HW, self.W // 2 + 1
-        live, tc, s = cx.live, ex._tc(), _stream()
+        live, tc, tcg, s = cx.live, ex._tc(), ex._tc_chan(), _stream()
         r_f, r_pw, r_mlp = bp["res"]
         act = 2 if tc else 1      # GELU after the spec / vert GroupNorms, as the forward applied it
-        act_f = 2 if ex._tc_mlp() else 1   # after the fuse GroupNorm (applied by the pw MLP's prologue)
+        act_f = 2 if ex._tc_chan() else 1   # after the fuse GroupNorm (applied by the pw MLP's prologue)
         depth = list(self._depth_slabs())
         gbd, gbr = self.gbd, self.gbr
         Gout, GA, T1, T2, T3 = hb["G"], hb["GA"], hb["T1"], hb["T2"], hb["T3"]
@@ -760,7 +760,7 @@ class StreamingVJP(StreamingForward):
         def spec_stage(ws, it):
             gb, Ds = gbd[ws.buf], it[1] - it[0]
             d = _descs(Ds, H, W, C, live)
-            if tc:
+            if tcg:
                 nat.call("ffno_gate_fwd_tc", ws.x.data_ptr(), ws.V, C, bp["tc_s_gate"].data_ptr(), None, None,
                          ws.xs.data_ptr(), ws.err.data_ptr(), s)
             else:
@@ -778,7 +778,7 @@ class StreamingVJP(StreamingForward):
             ex._mix(ws, "s", bp, fq, ws.sb, ws.sa, H * Wf, Ds, C, 2 * H * Wf * C, H * Wf * C, True)
             ex._xf(cx.pln, "thf_t", ws.sa, ws.sb, d["hf"], ws)
             ex._xf(cx.pln, "twf_t", ws.sb, gb.xsb, d["wi"], ws)
-            if tc:
+            if tcg:
                 nat.call("ffno_gate_bwd_tc", ws.x.data_ptr(), gb.xsb.data_ptr(), gb.xacc.data_ptr(), ws.V, C,
                          bp["tcb_s_gate"].data_ptr(), None, gb.xacc.data_ptr(), None, ws.err.data_ptr(), s)
             else:
@@ -821,7 +821,7 @@ class StreamingVJP(StreamingForward):
             N = RW * C
             d = _descs(D, rows, W, C, live)
             zrow = self.zbar_rows[D * it[0] * W:]
-            if tc:
+            if tcg:
                 nat.call("ffno_gate_fwd_tc", ws.x.data_ptr(), ws.V, C, bp["tc_v_gate"].data_ptr(), bp["v_zp"].data_ptr(),
                          ws.zr.data_ptr(), ws.xv.data_ptr(), ws.err.data_ptr(), s)
             else:
@@ -855,7 +855,7 @@ class StreamingVJP(StreamingForward):
                 ex._outer(ws, ws.vb, 2 * live, ws.xv, D, N, gb.opart, lib.ffno_outer_parts(2 * live, D, N),
                           self.tzf_bar)
                 ex._xf(hgt, "tzf_t", ws.vb, gb.xvb, d["zi"], ws)
-            if tc:
+            if tcg:
                 nat.call("ffno_gate_bwd_tc", ws.x.data_ptr(), gb.xvb.data_ptr(), gb.xacc.data_ptr(), ws.V, C,
                          bp["tcb_v_gate"].data_ptr(), bp["v_zp"].data_ptr(), gb.xacc.data_ptr(), zrow.data_ptr(),
                          ws.err.data_ptr(), s)

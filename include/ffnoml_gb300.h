@@ -334,9 +334,10 @@ int ffno_si_input_grads(const float* features, const float* x_bar, const float* 
  * ------------------------------------------------------------------------------------------------------------------ */
 int ffno_tc_parts(long V);
 int ffno_tc_width_supported(int C);
-/* Widths of ffno_mlp2_fwd_tc / ffno_mlp2_bwd_tc: also C = 96, the production model's width (the channel MLPs there
- * run on tensor cores while the gates, fusion, mixing and head keep their FP32 entry points). */
-int ffno_tc_mlp2_width_supported(int C);
+/* Widths of ffno_mlp2_fwd_tc / ffno_mlp2_bwd_tc and ffno_gate_fwd_tc / ffno_gate_bwd_tc: also C = 96, the production
+ * model's width (the channel MLPs and input gates there run on tensor cores while the fusion, mixing and head keep
+ * their FP32 entry points). */
+int ffno_tc_channel_width_supported(int C);
 /* L2 prefetch lookahead of the tensor-core pointwise kernels on the current device, in tiles of 128 voxels per
  * pipeline (0..4; default 0): a tuning knob, synchronous, not to be called while those kernels run. */
 int ffno_tc_set_prefetch_tiles(int tiles);
@@ -345,7 +346,7 @@ int ffno_tc_set_prefetch_tiles(int tiles);
 int ffno_mlp2_fwd_tc(int mode, const float* in, const float* prev_pre, const float* prev_coefs, float res, float* xout,
                      long V, int C, const void* wpack, const float* dw, float* pre, double* partials, int nparts,
                      int groups, int* err, ffno_stream_t stream);
-/* ffno_gate_fwd for one branch; wpack = [g1, g2] (C x C). */
+/* ffno_gate_fwd for one branch; wpack = [g1, g2] (C x C). C = 96 also (x 32-byte aligned). */
 int ffno_gate_fwd_tc(const float* x, long V, int C, const void* wpack, const float* zp, const float* z, float* out,
                      int* err, ffno_stream_t stream);
 /* First stage of ffno_fuse_fwd: gates [V][2C] = sigmoid(gelu([x, spec, vert] wg1^T) wg2^T + bias), and (if hg is not
@@ -363,7 +364,7 @@ int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* v
 int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack,
                      float* a_bar, int* err, ffno_stream_t stream);
 /* One branch of ffno_gate_bwd: x_bar = base + d/dx applied to g_bar, z_bar += g_bar . zp if zp; wpack = [g1, g2,
- * g2^T, g1^T]. base may equal x_bar. */
+ * g2^T, g1^T], at C = 96 the forward's [g1, g2] (x 32-byte aligned). base may equal x_bar. */
 int ffno_gate_bwd_tc(const float* x, const float* g_bar, const float* base, long V, int C, const void* wpack,
                      const float* zp, float* x_bar, float* z_bar, int* err, ffno_stream_t stream);
 /* ffno_fuse_bwd in two stages after ffno_fuse1_tc has recomputed gates and hg:

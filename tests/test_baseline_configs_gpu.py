@@ -55,7 +55,7 @@ def test_bf16_forward_and_vjp_against_reference_float64(name):
     ex = _rel(xb, a["xbar"])
     ex_ = model.executor()
     print(f"{name} bf16: max |d log10 n| {err:.2e}, x_bar rel {ex:.2e}, tensor cores: every kernel family "
-          f"{ex_._packed.tc}, channel MLPs {ex_._tc_mlp()}, transforms {ex_._tc_xf()}")
+          f"{ex_._packed.tc}, channel MLPs and gates {ex_._tc_chan()}, transforms {ex_._tc_xf()}")
     assert err <= 2e-3
     assert ex <= 1e-2
 

@@ -104,10 +104,12 @@ def test_mlp2_fwd_tc(C, V, mode):
     assert torch.allclose(outs[1][2], outs[0][2], rtol=1e-4, atol=1e-6)
 
 
-@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (64, 152 * 128 * 5 + 77)])
+@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (64, 152 * 128 * 5 + 77), (96, V),
+                                 (96, 152 * 128 * 3 + 77)])
 @pytest.mark.parametrize("with_z", [False, True])
 def test_gate_fwd_tc(C, V, with_z):
-    """Widths 32 and 64 run the warp-specialised kernel; also at a voxel count that cycles every CTA's ring."""
+    """Widths 32 and 64 run the warp-specialised kernel; also at a voxel count that cycles every CTA's ring; width 96
+    the two-pipeline kernel with rows of 12 octets."""
     nat = _nat()
     x = _rand(V, C, seed=1)
     g1, g2 = _rand(C, C, seed=2, scale=C ** -0.5), _rand(C, C, seed=3, scale=C ** -0.5)
@@ -177,10 +179,12 @@ def test_mlp2_bwd_tc(C, V):
     _close(r1, r0)
 
 
-@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (32, 2 * 128 + 5), (64, 152 * 128 * 5 + 77)])
+@pytest.mark.parametrize("C,V", [(16, V), (32, V), (64, V), (32, 2 * 128 + 5), (64, 152 * 128 * 5 + 77), (96, V),
+                                 (96, 152 * 128 * 3 + 77)])
 def test_gate_bwd_tc(C, V):
     """Widths 32 and 64 run the warp-specialised kernel (tiles in pairs): also one CTA with an odd tile count and
-    every CTA with a ragged last pair; the second call writes x_bar over its own base."""
+    every CTA with a ragged last pair; the second call writes x_bar over its own base. Width 96: one pipeline a CTA,
+    the pack [g1, g2] (the transposes read out of it)."""
     nat = _nat()
     x, xsb, xvb, base = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3), _rand(V, C, seed=4)
     s1, s2 = _rand(C, C, seed=5, scale=C ** -0.5), _rand(C, C, seed=6, scale=C ** -0.5)
@@ -193,11 +197,11 @@ def test_gate_bwd_tc(C, V):
     Nn = lambda m: _hold(m.contiguous())
     nat.call("ffno_gate_bwd", x.data_ptr(), xsb.data_ptr(), xvb.data_ptr(), base.data_ptr(), V, C, T(s1), T(s2),
              Nn(s2), Nn(s1), T(v1), T(v2), Nn(v2), Nn(v1), zp.data_ptr(), r0.data_ptr(), z0.data_ptr(), _s())
-    nat.call("ffno_gate_bwd_tc", x.data_ptr(), xsb.data_ptr(), base.data_ptr(), V, C,
-             _pack(s1, s2, s2.t(), s1.t()).data_ptr(), None, r1.data_ptr(), None, err.data_ptr(), _s())
-    nat.call("ffno_gate_bwd_tc", x.data_ptr(), xvb.data_ptr(), r1.data_ptr(), V, C,
-             _pack(v1, v2, v2.t(), v1.t()).data_ptr(), zp.data_ptr(), r1.data_ptr(), z1.data_ptr(), err.data_ptr(),
-             _s())
+    pk = (lambda g1, g2: _pack(g1, g2)) if C == 96 else (lambda g1, g2: _pack(g1, g2, g2.t(), g1.t()))
+    nat.call("ffno_gate_bwd_tc", x.data_ptr(), xsb.data_ptr(), base.data_ptr(), V, C, pk(s1, s2).data_ptr(), None,
+             r1.data_ptr(), None, err.data_ptr(), _s())
+    nat.call("ffno_gate_bwd_tc", x.data_ptr(), xvb.data_ptr(), r1.data_ptr(), V, C, pk(v1, v2).data_ptr(),
+             zp.data_ptr(), r1.data_ptr(), z1.data_ptr(), err.data_ptr(), _s())
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     _close(r1, r0)
