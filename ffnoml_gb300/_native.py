@@ -95,6 +95,11 @@ PROTOTYPES = {
     "ffno_tc_parts": [L],
     "ffno_tc_width_supported": [I],
     "ffno_tc_channel_width_supported": [I],
+    "ffno_fuse_hidden_tc": [P, P, P, P, P, L, I, P, P, P, P],
+    "ffno_fuse_out_tc": [P, P, P, P, P, P, L, I, P, P, P, P, I, I, P, P],
+    "ffno_fuse_bwd_h_tc": [P, P, L, I, P, P, P, P],
+    "ffno_fuse_bwd_q_tc": [P, P, P, P, P, P, P, L, I, P, P, P, P, P, P],
+    "ffno_fuse_bwd_x_tc": [P, P, P, L, I, P, P, P, P, P, P],
     "ffno_tc_set_prefetch_tiles": [I],
     "ffno_copy2d": [P, L, P, L, L, L, P],
     "ffno_reverse_axes4": [P, L, L, L, L, P, P],

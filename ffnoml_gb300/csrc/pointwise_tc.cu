@@ -287,16 +287,17 @@ __device__ __forceinline__ void fill_tile8(Split t, long v0, long V, int ptid, F
 // The production model's width: rows of 12 octets, weights read as transposes (below and in the width-96 kernels).
 constexpr int C96 = 96;
 
-// the transpose of the K-major weight matrix [R][K] at p, as the MN-major operand [N = K][K' = R] from k' = r0
-__device__ __forceinline__ Op wop_t(const uint8_t* p, int R, int K, int r0 = 0) {
-  const uint32_t h = tc::smem_u32(p) + (uint32_t)(r0 / 8) * (uint32_t)K * 16u;
+// the transpose of the K-major weight matrix [R][K] at p, as the MN-major operand [N = K][K' = R] from k' = r0 and
+// n = n0 (multiples of 8)
+__device__ __forceinline__ Op wop_t(const uint8_t* p, int R, int K, int r0 = 0, int n0 = 0) {
+  const uint32_t h = tc::smem_u32(p) + (uint32_t)(r0 / 8) * (uint32_t)K * 16u + (uint32_t)(n0 / 8) * 128u;
   return Op{h, h + (uint32_t)R * K * 2, (uint32_t)K * 16u, 128u, (uint32_t)K * 32u, true};
 }
 
-// fill_tile8 for 96 columns (12 octets a row, so a thread's columns change from piece to piece)
-template <typename F>
-__device__ __forceinline__ void fill96(Split t, long v0, long V, int ptid, F f) {
-  constexpr int KB = C96 / 8, NE = TM * KB, FB8 = FB / 2;
+// fill_tile8 for KW = 48 or 96 columns (6 or 12 octets a row, so a thread's columns change from piece to piece)
+template <int KW, typename F>
+__device__ __forceinline__ void fill_oct(Split t, long v0, long V, int ptid, F f) {
+  constexpr int KB = KW / 8, NE = TM * KB, FB8 = FB / 2;
   for (int e0 = ptid; e0 < NE; e0 += PT * FB8) {
     float a[FB8][8];
 #pragma unroll
@@ -325,6 +326,11 @@ __device__ __forceinline__ void fill96(Split t, long v0, long V, int ptid, F f) 
 }
 
 // Plain FP32 rows [V][C] of src into a split K-major tile [128][C]; every width, 96 included (12 octets a row).
+template <typename F>
+__device__ __forceinline__ void fill96(Split t, long v0, long V, int ptid, F f) {
+  fill_oct<C96>(t, v0, V, ptid, f);
+}
+
 template <int C>
 __device__ __forceinline__ void fill_rows(Split t, long v0, long V, int ptid, const float* __restrict__ src) {
   if constexpr (C == 96)
@@ -1530,6 +1536,362 @@ __global__ void __launch_bounds__(PT, 1) k_mlp2_bwd_tc96(const float* __restrict
   pipe_finish(P, tslot, NCOL);
 }
 
+// ---------------------------------------------------------------------------------------- width 96: branch fusion
+// _fuse_branches at C = 96, where its four weight matrices (332 KB split) exceed shared memory: the forward as three
+// kernels (the gates and their hidden pre-activation; the fuse hidden pre-activation hf = B Wf1^T; the output with
+// its residual and GroupNorm partials), the backward as three (hf_bar; the branch gradients and the gate
+// pre-activation gradient q; the input gradients), each holding at most 184 KB of weights. Every GEMM is K-sliced by
+// 48 columns through one [128][48] tile; the backward reads its transposed weights out of the forward's packs.
+constexpr int KS = 48;
+
+// gelu(GN(p)) of 8 consecutive channels k..k+7 of one branch (cf: the GroupNorm coefficients)
+__device__ __forceinline__ void branch8(const float* __restrict__ cf, int k, const float (&p)[8], float (&o)[8]) {
+  const float4 a = gn_apply<true>(make_float4(p[0], p[1], p[2], p[3]), gn_coefs(cf, C96, k));
+  const float4 b = gn_apply<true>(make_float4(p[4], p[5], p[6], p[7]), gn_coefs(cf, C96, k + 4));
+  o[0] = a.x, o[1] = a.y, o[2] = a.z, o[3] = a.w, o[4] = b.x, o[5] = b.y, o[6] = b.z, o[7] = b.w;
+}
+
+// gates [V][2C] = sigmoid(gelu(A Wg1^T) Wg2^T + bias), A = [x, gelu(GN_s(sp)), gelu(GN_v(vp))]; hg = A Wg1^T if not
+// NULL. Weights [wg1 (C x 3C), wg2 (2C x C)]. Tensor memory: D1 (C) at 0, D2 (2C) at C.
+__global__ void __launch_bounds__(PT, 1) k_fuse1_tc96(const float* __restrict__ x, const float* __restrict__ sp,
+                                                      const float* __restrict__ sc, const float* __restrict__ vp,
+                                                      const float* __restrict__ vc, long V,
+                                                      const uint8_t* __restrict__ wpack,
+                                                      const float* __restrict__ bias, float* __restrict__ gates,
+                                                      float* __restrict__ hg, int* __restrict__ err) {
+  constexpr int C = C96;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(C, 3 * C), B2 = mat_bytes(2 * C, C);
+  PIPE_PROLOGUE(3 * C, 1)
+  const Split T = split_at(smem + B1 + B2, TM, KS);
+  P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
+  const int row = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    for (int sl = 0; sl < 6; ++sl) {   // K-slices of A: x, then the spec branch, then the vert branch
+      const int part = sl / 2, k0 = (sl % 2) * KS;
+      fill_oct<KS>(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) {
+        if (part == 0) {
+          ld8(x + v * C + k0 + k, o);
+        } else {
+          float p[8];
+          ld8((part == 1 ? sp : vp) + v * C + k0 + k, p);
+          branch8(part == 1 ? sc : vc, k0 + k, p, o);
+        }
+      });
+      if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, KS), wop(smem, C, 3 * C, 0, sl * KS), KS, sl > 0, C})) break;
+    }
+    if (!P.ok) break;
+    const long v = v0 + row;
+    for (int h = 0; h < 2; ++h) {   // the hidden layer: hg out, gelu(hg) into the tile, K-half h of GEMM2
+#pragma unroll 1
+      for (int j = 3 * h; j < 3 * h + 3; ++j) {
+        if (!owns(j, P.half)) continue;
+        float hv[16];
+        rld(P, 0, j, hv);
+        if (hg && v < V) {
+          st8(hg + v * C + 16 * j, hv);
+          st8(hg + v * C + 16 * j + 8, hv + 8);
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) hv[i] = gelu_tc(hv[i]);
+        put16(T, row, 16 * j - KS * h, KS, hv);
+      }
+      if (!pipe_gemms(P, err, Gemm{P.tmem + C, kop(T, KS), wop(smem + B1, 2 * C, C, 0, KS * h), KS, h > 0, 2 * C}))
+        break;
+    }
+    if (!P.ok) break;
+#pragma unroll 1
+    for (int j = 0; j < 2 * C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      float g[16];
+      rld(P, C, j, g);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) g[i] = sigmoid_tc(g[i] + __ldg(bias + 16 * j + i));
+      if (v < V) {
+        st8(gates + v * 2 * C + 16 * j, g);
+        st8(gates + v * 2 * C + 16 * j + 8, g + 8);
+      }
+    }
+  }
+  pipe_finish(P, tslot, NCOL);
+}
+
+// hf [V][2C] = B Wf1^T, B = [gelu(GN_s(sp)) g_s, gelu(GN_v(vp)) g_v]. Weights [wf1 (2C x 2C)].
+__global__ void __launch_bounds__(PT, 1) k_fuse_hidden_tc96(const float* __restrict__ sp, const float* __restrict__ sc,
+                                                            const float* __restrict__ vp, const float* __restrict__ vc,
+                                                            const float* __restrict__ gates, long V,
+                                                            const uint8_t* __restrict__ wpack,
+                                                            float* __restrict__ hf, int* __restrict__ err) {
+  constexpr int C = C96;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(2 * C, 2 * C);
+  PIPE_PROLOGUE(2 * C, 1)
+  const Split T = split_at(smem + B1, TM, KS);
+  P.ok = load_weights(smem, wpack, B1, wcx, err);
+  const int row = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    for (int sl = 0; sl < 4; ++sl) {
+      const int part = sl / 2, k0 = (sl % 2) * KS;
+      fill_oct<KS>(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) {
+        float p[8], g[8];
+        ld8((part == 0 ? sp : vp) + v * C + k0 + k, p);
+        ld8(gates + v * 2 * C + part * C + k0 + k, g);
+        branch8(part == 0 ? sc : vc, k0 + k, p, o);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) o[i] *= g[i];
+      });
+      if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, KS), wop(smem, 2 * C, 2 * C, 0, sl * KS), KS, sl > 0, 2 * C}))
+        break;
+    }
+    if (!P.ok) break;
+    const long v = v0 + row;
+#pragma unroll 1
+    for (int j = 0; j < 2 * C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      float r[16];
+      rld(P, 0, j, r);
+      if (v < V) {
+        st8(hf + v * 2 * C + 16 * j, r);
+        st8(hf + v * 2 * C + 16 * j + 8, r + 8);
+      }
+    }
+  }
+  pipe_finish(P, tslot, NCOL);
+}
+
+// pre [V][C] = gelu(hf) Wf2^T + (B_s + B_v) / 2 with the GroupNorm partials of pre. Weights [wf2 (C x 2C)].
+__global__ void __launch_bounds__(PT, 1) k_fuse_out_tc96(const float* __restrict__ sp, const float* __restrict__ sc,
+                                                         const float* __restrict__ vp, const float* __restrict__ vc,
+                                                         const float* __restrict__ gates, const float* __restrict__ hf,
+                                                         long V, const uint8_t* __restrict__ wpack,
+                                                         const float* __restrict__ dw, float* __restrict__ pre,
+                                                         double* __restrict__ partials, int* __restrict__ err) {
+  constexpr int C = C96;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(C, 2 * C);
+  __shared__ float red[(PT / 32) * (GMAX + 1)], gm[GMAX], wsum;
+  __shared__ double acc[GMAX * 3];
+  PIPE_PROLOGUE(C, 1)
+  const Split T = split_at(smem + B1, TM, KS);
+  if (tid < GMAX * 3) acc[tid] = 0.0;
+  P.ok = load_weights(smem, wpack, B1, wcx, err);
+  const int row = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    for (int sl = 0; sl < 4; ++sl) {
+      fill_oct<KS>(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) {
+        ld8(hf + v * 2 * C + sl * KS + k, o);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) o[i] = gelu_tc(o[i]);
+      });
+      if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, KS), wop(smem, C, 2 * C, 0, sl * KS), KS, sl > 0, C})) break;
+    }
+    if (!P.ok) break;
+    const long v = v0 + row;
+    const float w = v < V ? __ldg(dw + v) : 0.f;
+    float vals[C];
+#pragma unroll
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      float r[16];
+      rld(P, 0, j, r);
+      if (v < V) {
+#pragma unroll
+        for (int e = 0; e < 16; e += 8) {
+          float ps[8], pv[8], gs[8], gv[8], bs[8], bv[8];
+          ld8(sp + v * C + 16 * j + e, ps);
+          ld8(vp + v * C + 16 * j + e, pv);
+          ld8(gates + v * 2 * C + 16 * j + e, gs);
+          ld8(gates + v * 2 * C + C + 16 * j + e, gv);
+          branch8(sc, 16 * j + e, ps, bs);
+          branch8(vc, 16 * j + e, pv, bv);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) r[e + i] += 0.5f * (bs[i] * gs[i] + bv[i] * gv[i]);
+        }
+        st8(pre + v * C + 16 * j, r);
+        st8(pre + v * C + 16 * j + 8, r + 8);
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) vals[16 * j + i] = r[i];
+    }
+    row_stats<C>(P, vals, w, red, gm, &wsum, acc);
+  }
+  __syncthreads();
+  if (tid < GMAX) {
+    double* o = partials + ((long)blockIdx.x * GMAX + tid) * 3;
+    o[0] = acc[3 * tid];
+    o[1] = acc[3 * tid + 1];
+    o[2] = acc[3 * tid + 2];
+  }
+  pipe_finish(P, tslot, NCOL);
+}
+
+// hfb [V][2C] = (fb Wf2) * gelu'(hf), fb = fused_pre_bar. Weights [wf2 (C x 2C)], read as its transpose.
+__global__ void __launch_bounds__(PT, 1) k_fuse_bwd_h_tc96(const float* __restrict__ fb, const float* __restrict__ hf,
+                                                           long V, const uint8_t* __restrict__ wpack,
+                                                           float* __restrict__ hfb, int* __restrict__ err) {
+  constexpr int C = C96;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(C, 2 * C);
+  PIPE_PROLOGUE(2 * C, 1)
+  const Split T = split_at(smem + B1, TM, KS);
+  P.ok = load_weights(smem, wpack, B1, wcx, err);
+  const int row = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    for (int sl = 0; sl < 2; ++sl) {
+      fill_oct<KS>(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(fb + v * C + sl * KS + k, o); });
+      if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, KS), wop_t(smem, C, 2 * C, sl * KS), KS, sl > 0, 2 * C})) break;
+    }
+    if (!P.ok) break;
+    const long v = v0 + row;
+#pragma unroll 1
+    for (int j = 0; j < 2 * C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      float r[16], h[16];
+      rld(P, 0, j, r);
+      if (v < V) {
+        ld8(hf + v * 2 * C + 16 * j, *reinterpret_cast<float(*)[8]>(h));
+        ld8(hf + v * 2 * C + 16 * j + 8, *reinterpret_cast<float(*)[8]>(h + 8));
+#pragma unroll
+        for (int i = 0; i < 16; ++i) r[i] *= gelu_grad_tc(h[i]);
+        st8(hfb + v * 2 * C + 16 * j, r);
+        st8(hfb + v * 2 * C + 16 * j + 8, r + 8);
+      }
+    }
+  }
+  pipe_finish(P, tslot, NCOL);
+}
+
+// B_bar = hfb Wf1 + [fb, fb] / 2; sbar = B_bar_s g_s, vbar = B_bar_v g_v; q [V][2C] = B_bar [s, v] g (1 - g), with
+// s = gelu(GN_s(sp)), v = gelu(GN_v(vp)). q may be hfb itself. Weights [wf1 (2C x 2C)], read as its transpose.
+__global__ void __launch_bounds__(PT, 1) k_fuse_bwd_q_tc96(const float* __restrict__ sp, const float* __restrict__ sc,
+                                                           const float* __restrict__ vp, const float* __restrict__ vc,
+                                                           const float* __restrict__ gates,
+                                                           const float* __restrict__ fb, const float* hfb, long V,
+                                                           const uint8_t* __restrict__ wpack,
+                                                           float* __restrict__ sbar, float* __restrict__ vbar,
+                                                           float* q, int* __restrict__ err) {
+  constexpr int C = C96;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(2 * C, 2 * C);
+  PIPE_PROLOGUE(2 * C, 1)
+  const Split T = split_at(smem + B1, TM, KS);
+  P.ok = load_weights(smem, wpack, B1, wcx, err);
+  const int row = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    for (int sl = 0; sl < 4; ++sl) {
+      fill_oct<KS>(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(hfb + v * 2 * C + sl * KS + k, o); });
+      if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, KS), wop_t(smem, 2 * C, 2 * C, sl * KS), KS, sl > 0, 2 * C}))
+        break;
+    }
+    if (!P.ok) break;
+    const long v = v0 + row;
+#pragma unroll 1
+    for (int j = 0; j < 2 * C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      const int part = j / (C / 16), c0 = 16 * (j % (C / 16));
+      float r[16];
+      rld(P, 0, j, r);
+      if (v < V) {
+        float dr[16], qq[16];
+#pragma unroll
+        for (int e = 0; e < 16; e += 8) {
+          float f[8], g[8], p[8], b[8];
+          ld8(fb + v * C + c0 + e, f);
+          ld8(gates + v * 2 * C + part * C + c0 + e, g);
+          ld8((part == 0 ? sp : vp) + v * C + c0 + e, p);
+          branch8(part == 0 ? sc : vc, c0 + e, p, b);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const float bb = r[e + i] + 0.5f * f[i];
+            dr[e + i] = bb * g[i];
+            qq[e + i] = bb * b[i] * g[i] * (1.f - g[i]);
+          }
+        }
+        float* dst = part == 0 ? sbar : vbar;
+        st8(dst + v * C + c0, dr);
+        st8(dst + v * C + c0 + 8, dr + 8);
+        st8(q + v * 2 * C + 16 * j, qq);
+        st8(q + v * 2 * C + 16 * j + 8, qq + 8);
+      }
+    }
+  }
+  pipe_finish(P, tslot, NCOL);
+}
+
+// hg_bar = (q Wg2) * gelu'(hg); A_bar = hg_bar Wg1: x_bar = base + A_bar[:C], sbar += A_bar[C:2C], vbar +=
+// A_bar[2C:]. Weights [wg1 (C x 3C), wg2 (2C x C)] (the gates' pack), read as their transposes. Tensor memory: D3
+// (C) at 0, D4 (3C, two accumulators of 144) at C.
+__global__ void __launch_bounds__(PT, 1) k_fuse_bwd_x_tc96(const float* __restrict__ q, const float* __restrict__ hg,
+                                                           const float* __restrict__ base, long V,
+                                                           const uint8_t* __restrict__ wpack,
+                                                           float* __restrict__ xbar, float* __restrict__ sbar,
+                                                           float* __restrict__ vbar, int* __restrict__ err) {
+  constexpr int C = C96;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(C, 3 * C), B2 = mat_bytes(2 * C, C);
+  PIPE_PROLOGUE(4 * C, 1)
+  const Split T = split_at(smem + B1 + B2, TM, KS);
+  P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
+  const int row = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    for (int sl = 0; sl < 4; ++sl) {
+      fill_oct<KS>(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(q + v * 2 * C + sl * KS + k, o); });
+      if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, KS), wop_t(smem + B1, 2 * C, C, sl * KS), KS, sl > 0, C})) break;
+    }
+    if (!P.ok) break;
+    const long v = v0 + row;
+    for (int h = 0; h < 2; ++h) {
+#pragma unroll 1
+      for (int j = 3 * h; j < 3 * h + 3; ++j) {
+        if (!owns(j, P.half)) continue;
+        float d[16], hv[16];
+        rld(P, 0, j, d);
+        if (v < V) {
+          ld8(hg + v * C + 16 * j, *reinterpret_cast<float(*)[8]>(hv));
+          ld8(hg + v * C + 16 * j + 8, *reinterpret_cast<float(*)[8]>(hv + 8));
+#pragma unroll
+          for (int i = 0; i < 16; ++i) d[i] *= gelu_grad_tc(hv[i]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) d[i] = 0.f;
+        }
+        put16(T, row, 16 * j - KS * h, KS, d);
+      }
+      const Gemm g4b{P.tmem + C + 144, kop(T, KS), wop_t(smem, C, 3 * C, KS * h, 144), KS, h > 0, 144};
+      if (!pipe_gemms(P, err, Gemm{P.tmem + C, kop(T, KS), wop_t(smem, C, 3 * C, KS * h, 0), KS, h > 0, 144}, &g4b))
+        break;
+    }
+    if (!P.ok) break;
+#pragma unroll 1
+    for (int j = 0; j < 3 * C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      const int part = j / (C / 16), c0 = 16 * (j % (C / 16));
+      float r[16];
+      rld(P, C, j, r);
+      if (v < V) {
+        const float* add = part == 0 ? base : (part == 1 ? sbar : vbar);
+        float* dst = part == 0 ? xbar : (part == 1 ? sbar : vbar);
+        if (add) {
+          float b[16];
+          ld8(add + v * C + c0, *reinterpret_cast<float(*)[8]>(b));
+          ld8(add + v * C + c0 + 8, *reinterpret_cast<float(*)[8]>(b + 8));
+#pragma unroll
+          for (int i = 0; i < 16; ++i) r[i] += b[i];
+        }
+        st8(dst + v * C + c0, r);
+        st8(dst + v * C + c0 + 8, r + 8);
+      }
+    }
+  }
+  pipe_finish(P, tslot, NCOL);
+}
+
 #undef PIPE_PROLOGUE
 
 int g_sms = 0;
@@ -1665,8 +2027,18 @@ int ffno_fuse1_tc(const float* x, const float* spec_pre, const float* spec_coefs
                   const float* vert_coefs, long V, int C, const void* wpack, const float* bias, float* gates,
                   float* hg, int* err, ffno_stream_t stream) {
   if (!x || !spec_pre || !spec_coefs || !vert_pre || !vert_coefs || !wpack || !bias) return FFNO_EINVAL;
-  if (!tc_width(C) || V < 1 || !err || !aligned16(wpack) || !gates) return FFNO_EINVAL;
+  if (!chan_width(C) || V < 1 || !err || !aligned16(wpack) || !gates) return FFNO_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
+  if (C == C96) {
+    if (!aligned32(x) || !aligned32(spec_pre) || !aligned32(vert_pre) || !aligned32(gates) || (hg && !aligned32(hg)))
+      return FFNO_EINVAL;
+    const size_t smem = mat_bytes(C96, 3 * C96) + mat_bytes(2 * C96, C96) + tile_bytes(KS);
+    if (!launch_prep(k_fuse1_tc96, smem)) return FFNO_ELAUNCH;
+    k_fuse1_tc96<<<grid_tc(V), PT, smem, s>>>(x, spec_pre, spec_coefs, vert_pre, vert_coefs, V,
+                                             static_cast<const uint8_t*>(wpack), bias, gates, hg, err);
+    FFNO_CHECK_LAUNCH();
+    return FFNO_OK;
+  }
   if (ws::fuse1_supported(C))
     return ws::fuse1(x, spec_pre, spec_coefs, vert_pre, vert_coefs, V, C, wpack, bias, gates, hg, err, s);
   TC_DISPATCH(C, {
@@ -1696,6 +2068,87 @@ int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* v
     k_fuse2_tc<CC><<<nparts, CT, smem, s>>>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, V,
                                            static_cast<const uint8_t*>(wpack), dw, pre, partials, err);
   })
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_fuse_hidden_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
+                        const float* gates, long V, int C, const void* wpack, float* hf, int* err,
+                        ffno_stream_t stream) {
+  if (!spec_pre || !spec_coefs || !vert_pre || !vert_coefs || !gates || !wpack || !hf || !err) return FFNO_EINVAL;
+  if (C != C96 || V < 1 || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!aligned32(spec_pre) || !aligned32(vert_pre) || !aligned32(gates) || !aligned32(hf)) return FFNO_EINVAL;
+  const size_t smem = mat_bytes(2 * C96, 2 * C96) + tile_bytes(KS);
+  if (!launch_prep(k_fuse_hidden_tc96, smem)) return FFNO_ELAUNCH;
+  k_fuse_hidden_tc96<<<grid_tc(V), PT, smem, (cudaStream_t)stream>>>(spec_pre, spec_coefs, vert_pre, vert_coefs,
+                                                                     gates, V, static_cast<const uint8_t*>(wpack), hf,
+                                                                     err);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_fuse_out_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
+                     const float* gates, const float* hf, long V, int C, const void* wpack, const float* dw,
+                     float* pre, double* partials, int nparts, int groups, int* err, ffno_stream_t stream) {
+  if (!spec_pre || !spec_coefs || !vert_pre || !vert_coefs || !gates || !hf || !wpack || !dw || !pre || !partials ||
+      !err)
+    return FFNO_EINVAL;
+  if (C != C96 || V < 1 || !aligned16(wpack) || groups != GMAX || nparts != grid_tc(V)) return FFNO_EINVAL;
+  if (!aligned32(spec_pre) || !aligned32(vert_pre) || !aligned32(gates) || !aligned32(hf) || !aligned32(pre))
+    return FFNO_EINVAL;
+  const size_t smem = mat_bytes(C96, 2 * C96) + tile_bytes(KS);
+  if (!launch_prep(k_fuse_out_tc96, smem)) return FFNO_ELAUNCH;
+  k_fuse_out_tc96<<<nparts, PT, smem, (cudaStream_t)stream>>>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates, hf, V,
+                                                              static_cast<const uint8_t*>(wpack), dw, pre, partials,
+                                                              err);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_fuse_bwd_h_tc(const float* fused_pre_bar, const float* hf, long V, int C, const void* wpack, float* hf_bar,
+                       int* err, ffno_stream_t stream) {
+  if (!fused_pre_bar || !hf || !wpack || !hf_bar || !err) return FFNO_EINVAL;
+  if (C != C96 || V < 1 || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!aligned32(fused_pre_bar) || !aligned32(hf) || !aligned32(hf_bar)) return FFNO_EINVAL;
+  const size_t smem = mat_bytes(C96, 2 * C96) + tile_bytes(KS);
+  if (!launch_prep(k_fuse_bwd_h_tc96, smem)) return FFNO_ELAUNCH;
+  k_fuse_bwd_h_tc96<<<grid_tc(V), PT, smem, (cudaStream_t)stream>>>(fused_pre_bar, hf, V,
+                                                                    static_cast<const uint8_t*>(wpack), hf_bar, err);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_fuse_bwd_q_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
+                       const float* gates, const float* fused_pre_bar, const float* hf_bar, long V, int C,
+                       const void* wpack, float* spec_bar, float* vert_bar, float* q, int* err, ffno_stream_t stream) {
+  if (!spec_pre || !spec_coefs || !vert_pre || !vert_coefs || !gates || !fused_pre_bar || !hf_bar || !wpack ||
+      !spec_bar || !vert_bar || !q || !err)
+    return FFNO_EINVAL;
+  if (C != C96 || V < 1 || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!aligned32(spec_pre) || !aligned32(vert_pre) || !aligned32(gates) || !aligned32(fused_pre_bar) ||
+      !aligned32(hf_bar) || !aligned32(spec_bar) || !aligned32(vert_bar) || !aligned32(q))
+    return FFNO_EINVAL;
+  const size_t smem = mat_bytes(2 * C96, 2 * C96) + tile_bytes(KS);
+  if (!launch_prep(k_fuse_bwd_q_tc96, smem)) return FFNO_ELAUNCH;
+  k_fuse_bwd_q_tc96<<<grid_tc(V), PT, smem, (cudaStream_t)stream>>>(spec_pre, spec_coefs, vert_pre, vert_coefs, gates,
+                                                                    fused_pre_bar, hf_bar, V,
+                                                                    static_cast<const uint8_t*>(wpack), spec_bar,
+                                                                    vert_bar, q, err);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+
+int ffno_fuse_bwd_x_tc(const float* q, const float* hg, const float* base, long V, int C, const void* wpack,
+                       float* x_bar, float* spec_bar, float* vert_bar, int* err, ffno_stream_t stream) {
+  if (!q || !hg || !wpack || !x_bar || !spec_bar || !vert_bar || !err) return FFNO_EINVAL;
+  if (C != C96 || V < 1 || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!aligned32(q) || !aligned32(hg) || (base && !aligned32(base)) || !aligned32(x_bar) || !aligned32(spec_bar) ||
+      !aligned32(vert_bar))
+    return FFNO_EINVAL;
+  const size_t smem = mat_bytes(C96, 3 * C96) + mat_bytes(2 * C96, C96) + tile_bytes(KS);
+  if (!launch_prep(k_fuse_bwd_x_tc96, smem)) return FFNO_ELAUNCH;
+  k_fuse_bwd_x_tc96<<<grid_tc(V), PT, smem, (cudaStream_t)stream>>>(q, hg, base, V, static_cast<const uint8_t*>(wpack),
+                                                                    x_bar, spec_bar, vert_bar, err);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;
 }

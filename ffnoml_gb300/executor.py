@@ -230,14 +230,18 @@ class Packed:
 
     @staticmethod
     def _tc_chan_block(pk, b, device):
-        """Split-BF16 packs of one block's channel MLPs and input gates at width 96: [w1, w2] for the forward, and the
-        same pack for the backward (its kernels read the transposes out of it)."""
+        """Split-BF16 packs of one block's channel MLPs, input gates and branch fusion at width 96: [w1, w2] for the
+        forward, and the same packs for the backward (its kernels read the transposes out of them)."""
         s, v = b.spec, b.vertical
         for name, (c1, c2) in dict(s_post=(s.post[0], s.post[2]), v_post=(v.post[0], v.post[2]),
                                    pw=(b.pw[0], b.pw[2]), mlp=(b.mlp.net[0], b.mlp.net[3]),
                                    s_gate=(s.input_gate[0], s.input_gate[2]),
                                    v_gate=(v.input_gate[0], v.input_gate[2])).items():
             pk["tc_" + name] = pk["tcb_" + name] = tc_pack(device, _w(c1), _w(c2))
+        # the branch fusion: the gates' [wg1, wg2] (also read transposed by the backward), [wf1], [wf2]
+        pk["tc_fuse1"] = tc_pack(device, _w(b.branch_gate[0]), _w(b.branch_gate[2]))
+        pk["tc_f1"] = tc_pack(device, _w(b.fuse[0]))
+        pk["tc_f2"] = tc_pack(device, _w(b.fuse[2]))
 
     @staticmethod
     def _head_params(model):
@@ -320,6 +324,7 @@ class Workspace:
         spec_len = D * 2 * H * Wf * C
         self.sa, self.sb = nb(spec_len), nb(spec_len)
         self.gates = nb(V, 2 * C)     # branch gates between the two tensor-core fuse stages
+        self.hf = nb(V, 2 * C) if C == 96 else None   # the width-96 fusion's hidden pre-activation
         self.va, self.vb = nb(2 * live * HW * C), nb(2 * live * HW * C)
         self.hg = None                # the gate MLP's hidden pre-activation, kept only by a caching forward
 
@@ -329,7 +334,8 @@ class Workspace:
     def state_bytes(self, gates):
         """Device bytes of one block's cached intermediates (gates: also the branch gates and the gate MLP's hidden
         layer of the tensor-core fuse)."""
-        n = sum(getattr(self, n).numel() for n in self.CACHED) + (3 * self.x.numel() if gates else 0)
+        extra = 3 * self.x.numel() + (self.hf.numel() if self.hf is not None else 0)
+        n = sum(getattr(self, n).numel() for n in self.CACHED) + (extra if gates else 0)
         return 4 * n + 2 * len(NORMS) * 8 * 64
 
     def fork(self, gates):
@@ -341,6 +347,8 @@ class Workspace:
         if gates:
             w.gates = torch.empty_like(self.gates)
             w.hg = torch.empty_like(self.x)
+            if self.hf is not None:
+                w.hf = torch.empty_like(self.hf)
         w.ys = w.xs
         w.coefs = dict(self.coefs)
         w.gstats = dict(self.gstats)
@@ -355,7 +363,7 @@ class Workspace:
         for n in self.CACHED + ("ys",):
             setattr(w, n, getattr(state, n))
         if state.hg is not None:
-            w.gates, w.hg = state.gates, state.hg
+            w.gates, w.hg, w.hf = state.gates, state.hg, state.hf
         w.coefs = dict(self.coefs)
         w.gstats = dict(self.gstats)
         for n in NORMS:
@@ -618,7 +626,8 @@ class Executor:
             if ws is None or ws.live != hgt_b["live"]:
                 ws = Workspace(D, H, W, m.width, hgt_b["live"], pk.groups, x.device)
             if keep and cache is None:
-                cache = self.cache_states and self._fits(B * m.n_layers * ws.state_bytes(self._tc()), x.device)
+                cache = self.cache_states and self._fits(B * m.n_layers * ws.state_bytes(self._keeps_gates()),
+                                                         x.device)
                 self.last_cached = cache
             xin, z = x[b], z_scale[b]
             self._depth_weights(ws, z, D, H * W)
@@ -632,7 +641,7 @@ class Executor:
             for i in range(m.n_layers):
                 if keep:
                     ws.x = inputs[i + 1]
-                wb = ws.fork(self._tc()) if cache else ws
+                wb = ws.fork(self._keeps_gates()) if cache else ws
                 self._block(pk, wb, i, z, D, H, W, hgt_b, pln, pfr[i], x_in=inputs[i] if keep else None)
                 if cache:
                     blocks.append(wb)
@@ -750,6 +759,16 @@ class Executor:
                      ws.dw.data_ptr(), ws.fused_pre.data_ptr(), ws.partials.data_ptr(), ws.nparts_tc, G,
                      ws.err.data_ptr(), s)
             self._finalize(ws, "fuse", bp["fuse_g"], bp["fuse_b"], True)
+        elif self._tc_fuse96():
+            self._fuse1_tc(ws, bp, x, ws.hg)
+            sp, cs, vp, cv = (ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(), ws.vert_pre.data_ptr(),
+                              ws.coefs["vert"].data_ptr())
+            nat.call("ffno_fuse_hidden_tc", sp, cs, vp, cv, ws.gates.data_ptr(), V, C, bp["tc_f1"].data_ptr(),
+                     ws.hf.data_ptr(), ws.err.data_ptr(), s)
+            nat.call("ffno_fuse_out_tc", sp, cs, vp, cv, ws.gates.data_ptr(), ws.hf.data_ptr(), V, C,
+                     bp["tc_f2"].data_ptr(), ws.dw.data_ptr(), ws.fused_pre.data_ptr(), ws.partials.data_ptr(),
+                     ws.nparts_tc, G, ws.err.data_ptr(), s)
+            self._finalize(ws, "fuse", bp["fuse_g"], bp["fuse_b"], True)
         else:
             nat.call("ffno_fuse_fwd", x.data_ptr(), ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(),
                      ws.vert_pre.data_ptr(), ws.coefs["vert"].data_ptr(), V, C, bp["bg1"].data_ptr(),
@@ -814,6 +833,15 @@ class Executor:
         """Whether the channel MLPs and input gates run on the split-BF16 tensor-core kernels: wherever _tc() does,
         and at width 96."""
         return self.model.precision == "bf16" and self._packed.tc_chan and not getattr(self._tls, "fp32", False)
+
+    def _tc_fuse96(self):
+        """Whether the branch fusion runs on the width-96 tensor-core kernels (gates, hidden layer, output; three
+        backward kernels)."""
+        return self._tc_chan() and not self._packed.tc and self.model.width == 96
+
+    def _keeps_gates(self):
+        """Whether a caching forward keeps the fusion's gates and hidden layers (the tensor-core fusion)."""
+        return self._tc() or self._tc_fuse96()
 
     def _tc_xf(self):
         """Whether the transforms and the height-table gradients run on the split-BF16 tensor-core kernels: precision
@@ -1065,7 +1093,7 @@ class Executor:
         r_f, r_pw, r_mlp = bp["res"]
         live = hgt["live"]
         d = _descs(D, H, W, C, live)
-        tc, tc_chan = self._tc(), self._tc_chan()
+        tc, tc_chan, fuse96 = self._tc(), self._tc_chan(), self._tc_fuse96()
         err = ws.err.data_ptr()
 
         def mlp_bwd(a, pb, base, out, w1, w2t, w1t, pack):
@@ -1084,7 +1112,7 @@ class Executor:
         mlp_bwd(ws.x1, gb.pbar, gb.g2, gb.g1, "pw1", "pw2t", "pw1t", "tcb_pw")
         # GELU after a GroupNorm: the tensor-core forward applies the A&S activation (mode 2), the FP32 one erf's; the
         # fuse norm's GELU is applied by the pw MLP's prologue, the spec / vert norms' by the fusion
-        act = 2 if tc else 1
+        act = 2 if tc or fuse96 else 1
         # x1 = x + r_f gelu(GN(fused_pre)); fused_pre = fuse(x, spec, vert)
         self._gn_bwd(ws, gb, 2 if tc_chan else 1, gb.g1, r_f, ws.fused_pre, bp["fuse_g"], bp["fuse_b"], "fuse",
                      gb.pbar)
@@ -1101,6 +1129,21 @@ class Executor:
                      ws.gates.data_ptr(), hg.data_ptr(), gb.pbar.data_ptr(), gb.hfb.data_ptr(), gb.g1.data_ptr(),
                      V, C, bp["tcb_fuse_b"].data_ptr(), gb.xacc.data_ptr(), gb.sbar.data_ptr(), gb.vbar.data_ptr(),
                      err, s)
+        elif fuse96:
+            sp, cs, vp, cv = (ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(), ws.vert_pre.data_ptr(),
+                              ws.coefs["vert"].data_ptr())
+            # the gates and hf are this block's (kept from the forward, or just recomputed into ws by it); the gate
+            # hidden layer hg is kept only by a caching forward, else recomputed here
+            hg, hf = ws.hg, ws.hf
+            if hg is None:
+                hg = gb.hg
+                self._fuse1_tc(ws, bp, x, hg)
+            nat.call("ffno_fuse_bwd_h_tc", gb.pbar.data_ptr(), hf.data_ptr(), V, C, bp["tc_f2"].data_ptr(),
+                     gb.hfb.data_ptr(), err, s)
+            nat.call("ffno_fuse_bwd_q_tc", sp, cs, vp, cv, ws.gates.data_ptr(), gb.pbar.data_ptr(), gb.hfb.data_ptr(),
+                     V, C, bp["tc_f1"].data_ptr(), gb.sbar.data_ptr(), gb.vbar.data_ptr(), gb.hfb.data_ptr(), err, s)
+            nat.call("ffno_fuse_bwd_x_tc", gb.hfb.data_ptr(), hg.data_ptr(), gb.g1.data_ptr(), V, C,
+                     bp["tc_fuse1"].data_ptr(), gb.xacc.data_ptr(), gb.sbar.data_ptr(), gb.vbar.data_ptr(), err, s)
         else:
             nat.call("ffno_fuse_bwd", x.data_ptr(), ws.spec_pre.data_ptr(), ws.coefs["spec"].data_ptr(),
                      ws.vert_pre.data_ptr(), ws.coefs["vert"].data_ptr(), gb.pbar.data_ptr(), gb.g1.data_ptr(), V, C,

@@ -350,7 +350,8 @@ int ffno_mlp2_fwd_tc(int mode, const float* in, const float* prev_pre, const flo
 int ffno_gate_fwd_tc(const float* x, long V, int C, const void* wpack, const float* zp, const float* z, float* out,
                      int* err, ffno_stream_t stream);
 /* First stage of ffno_fuse_fwd: gates [V][2C] = sigmoid(gelu([x, spec, vert] wg1^T) wg2^T + bias), and (if hg is not
- * NULL) the hidden pre-activation hg [V][C]; wpack = [wg1 (C x 3C), wg2 (2C x C)]. */
+ * NULL) the hidden pre-activation hg [V][C]; wpack = [wg1 (C x 3C), wg2 (2C x C)]. C = 96 also (rows 32-byte
+ * aligned). */
 int ffno_fuse1_tc(const float* x, const float* spec_pre, const float* spec_coefs, const float* vert_pre,
                   const float* vert_coefs, long V, int C, const void* wpack, const float* bias, float* gates,
                   float* hg, int* err, ffno_stream_t stream);
@@ -359,6 +360,32 @@ int ffno_fuse1_tc(const float* x, const float* spec_pre, const float* spec_coefs
 int ffno_fuse2_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
                   const float* gates, long V, int C, const void* wpack, const float* dw, float* pre, double* partials,
                   int nparts, int groups, int* err, ffno_stream_t stream);
+/* The branch fusion at C = 96 (ffno_fuse_fwd / ffno_fuse_bwd, models/ffno_model.py:524-534), whose weights exceed
+ * shared memory for the two-stage form: ffno_fuse1_tc (C = 96 also) for the gates and hg, then
+ *   ffno_fuse_hidden_tc: hf [V][2C] = B wf1^T, B = [gelu(GN_s(spec_pre)) g_s, gelu(GN_v(vert_pre)) g_v]; wpack = [wf1
+ *     (2C x 2C)];
+ *   ffno_fuse_out_tc: pre [V][C] = gelu(hf) wf2^T + (B_s + B_v) / 2 with GroupNorm partials (nparts =
+ *     ffno_tc_parts(V)); wpack = [wf2 (C x 2C)].
+ * The backward given fused_pre_bar (fb), gates, hg and hf:
+ *   ffno_fuse_bwd_h_tc: hf_bar [V][2C] = (fb wf2) * gelu'(hf); wpack = [wf2];
+ *   ffno_fuse_bwd_q_tc: B_bar = hf_bar wf1 + [fb, fb] / 2, spec_bar = B_bar_s g_s, vert_bar = B_bar_v g_v, q [V][2C] =
+ *     B_bar [s, v] g (1 - g) (q may be hf_bar); wpack = [wf1];
+ *   ffno_fuse_bwd_x_tc: hg_bar = (q wg2) * gelu'(hg), A_bar = hg_bar wg1: x_bar = base + A_bar[:C], spec_bar +=
+ *     A_bar[C:2C], vert_bar += A_bar[2C:]; wpack = ffno_fuse1_tc's [wg1 (C x 3C), wg2 (2C x C)].
+ * C = 96 only; row pointers 32-byte aligned. The backward kernels read the transposed weights out of the packs. */
+int ffno_fuse_hidden_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
+                        const float* gates, long V, int C, const void* wpack, float* hf, int* err,
+                        ffno_stream_t stream);
+int ffno_fuse_out_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
+                     const float* gates, const float* hf, long V, int C, const void* wpack, const float* dw,
+                     float* pre, double* partials, int nparts, int groups, int* err, ffno_stream_t stream);
+int ffno_fuse_bwd_h_tc(const float* fused_pre_bar, const float* hf, long V, int C, const void* wpack, float* hf_bar,
+                       int* err, ffno_stream_t stream);
+int ffno_fuse_bwd_q_tc(const float* spec_pre, const float* spec_coefs, const float* vert_pre, const float* vert_coefs,
+                       const float* gates, const float* fused_pre_bar, const float* hf_bar, long V, int C,
+                       const void* wpack, float* spec_bar, float* vert_bar, float* q, int* err, ffno_stream_t stream);
+int ffno_fuse_bwd_x_tc(const float* q, const float* hg, const float* base, long V, int C, const void* wpack,
+                       float* x_bar, float* spec_bar, float* vert_bar, int* err, ffno_stream_t stream);
 /* ffno_mlp2_bwd; wpack = [w1 (2C x C), w2^T (2C x C), w1^T (C x 2C)]; at C = 96 the forward's pack [w1 (2C x C),
  * w2 (C x 2C)] (the kernel reads the transposes out of it; a, pre_bar, base, a_bar 32-byte aligned). */
 int ffno_mlp2_bwd_tc(const float* a, const float* pre_bar, const float* base, long V, int C, const void* wpack,

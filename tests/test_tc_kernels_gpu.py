@@ -401,3 +401,62 @@ def test_outer_tc_in_slices(ma, mb, calls):
     torch.cuda.synchronize()
     assert _WS.err.item() == 0
     _close(out - 0.25, ref, 2e-5)
+
+
+@pytest.mark.parametrize("V", [V, 152 * 128 * 3 + 77])
+def test_fuse_tc96(V):
+    """The branch fusion at width 96 on tensor cores (gates, hidden pre-activation, output; backward in three
+    kernels that read their transposed weights out of the forward's packs) against the FP32 fusion kernels."""
+    nat = _nat()
+    C = 96
+    x, sp, vp = _rand(V, C, seed=1), _rand(V, C, seed=2), _rand(V, C, seed=3)
+    sc, vc = _coefs(C, 4), _coefs(C, 5)
+    fb, base = _rand(V, C, seed=6), _rand(V, C, seed=7)
+    bg0, bg2, bb, f0, f2 = _fuse_weights(C)
+    dw = (1 + 0.1 * _rand(V, seed=8)).contiguous()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    T = lambda m: _hold(m.t().contiguous())
+    Nn = lambda m: _hold(m.contiguous())
+    # forward
+    P0, P1 = nat.lib().ffno_stats_parts(V), nat.lib().ffno_tc_parts(V)
+    part0 = torch.empty(P0 * G * 3, dtype=torch.float64, device="cuda")
+    part1 = torch.empty(P1 * G * 3, dtype=torch.float64, device="cuda")
+    a, b = torch.empty(V, C, device="cuda"), torch.empty(V, C, device="cuda")
+    nat.call("ffno_fuse_fwd", x.data_ptr(), sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), V, C, T(bg0),
+             T(bg2), bb.data_ptr(), T(f0), T(f2), dw.data_ptr(), a.data_ptr(), part0.data_ptr(), P0, G, _s())
+    gates, hg, hf = (torch.empty(V, 2 * C, device="cuda"), torch.empty(V, C, device="cuda"),
+                     torch.empty(V, 2 * C, device="cuda"))
+    g_pack, f1_pack, f2_pack = _pack(bg0, bg2), _pack(f0), _pack(f2)
+    nat.call("ffno_fuse1_tc", x.data_ptr(), sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), V, C,
+             g_pack.data_ptr(), bb.data_ptr(), gates.data_ptr(), hg.data_ptr(), err.data_ptr(), _s())
+    nat.call("ffno_fuse_hidden_tc", sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), gates.data_ptr(), V,
+             C, f1_pack.data_ptr(), hf.data_ptr(), err.data_ptr(), _s())
+    nat.call("ffno_fuse_out_tc", sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), gates.data_ptr(),
+             hf.data_ptr(), V, C, f2_pack.data_ptr(), dw.data_ptr(), b.data_ptr(), part1.data_ptr(), P1, G,
+             err.data_ptr(), _s())
+    ones, zeros = torch.ones(C, device="cuda"), torch.zeros(C, device="cuda")
+    st = []
+    for part, P in ((part0, P0), (part1, P1)):
+        coefs, gst = torch.empty(3 * C, device="cuda"), torch.empty(G * 3, dtype=torch.float64, device="cuda")
+        nat.call("ffno_gn_finalize", part.data_ptr(), P, C, G, ones.data_ptr(), zeros.data_ptr(), 1e-5,
+                 coefs.data_ptr(), gst.data_ptr(), _s())
+        st.append(gst)
+    # backward
+    o = [torch.empty(V, C, device="cuda") for _ in range(6)]
+    nat.call("ffno_fuse_bwd", x.data_ptr(), sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), fb.data_ptr(),
+             base.data_ptr(), V, C, T(bg0), T(bg2), bb.data_ptr(), T(f0), Nn(f2), Nn(f0), Nn(bg2), Nn(bg0),
+             o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(), _s())
+    hfb = torch.empty(V, 2 * C, device="cuda")
+    nat.call("ffno_fuse_bwd_h_tc", fb.data_ptr(), hf.data_ptr(), V, C, f2_pack.data_ptr(), hfb.data_ptr(),
+             err.data_ptr(), _s())
+    nat.call("ffno_fuse_bwd_q_tc", sp.data_ptr(), sc.data_ptr(), vp.data_ptr(), vc.data_ptr(), gates.data_ptr(),
+             fb.data_ptr(), hfb.data_ptr(), V, C, f1_pack.data_ptr(), o[4].data_ptr(), o[5].data_ptr(),
+             hfb.data_ptr(), err.data_ptr(), _s())
+    nat.call("ffno_fuse_bwd_x_tc", hfb.data_ptr(), hg.data_ptr(), base.data_ptr(), V, C, g_pack.data_ptr(),
+             o[3].data_ptr(), o[4].data_ptr(), o[5].data_ptr(), err.data_ptr(), _s())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    _close(b, a)
+    assert torch.allclose(st[1], st[0], rtol=1e-4, atol=1e-6)
+    for i in range(3):
+        _close(o[3 + i], o[i])
