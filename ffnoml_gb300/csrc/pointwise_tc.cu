@@ -1892,6 +1892,100 @@ __global__ void __launch_bounds__(PT, 1) k_fuse_bwd_x_tc96(const float* __restri
   pipe_finish(P, tslot, NCOL);
 }
 
+// ---------------------------------------------------------------------------------------- width 96: mixing
+// ffno_spectral_mix at C = 96 (SpectralConv2dFull.mix_spectrum, HeightSpectralConv's mode mixing): for frequency f and
+// row b, x = [re | im] (2C), out = g_f (x M) + [U_f t_re, U_f t_im], t = [V_f x_re, V_f x_im], with M the pack (wbig
+// for the mixing, wbig^T for its adjoint) read through its transpose view. An item is 128 rows b of one frequency; x
+// arrives in four K-slices of 48 through one tile, and each slice feeds x M (N = 2C) and the projections t (N = 16:
+// a block-diagonal [16][2C] operand built from V_f per item); the epilogue applies g_f and U_f (FP32, U_f in shared
+// memory). Tensor memory: x M at 0 (2C columns), t at 2C (16).
+constexpr int MIXR = 8;   // the low-rank terms this kernel carries (the model's freq_mix_rank)
+
+__global__ void __launch_bounds__(PT, 1) k_mix_tc96(const float* __restrict__ in, float* __restrict__ out, long F,
+                                                    long nb, long sf, long sb, long s_im,
+                                                    const uint8_t* __restrict__ wpack, const float* __restrict__ g,
+                                                    const float* __restrict__ U, const float* __restrict__ Vm,
+                                                    int rank, int* __restrict__ err) {
+  constexpr int C = C96, K2 = 2 * C;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(K2, K2), VB = mat_bytes(16, K2);
+  __shared__ float us[C * MIXR];
+  const long nbt = (nb + TM - 1) / TM;
+  const long V = F * nbt * TM;   // the prologue's tiles are the items: (frequency, block of 128 rows) pairs
+  PIPE_PROLOGUE(K2 + 16, 1)
+  const Split T = split_at(smem + B1, TM, KS);
+  uint8_t* vblk = smem + B1 + tile_bytes(KS);           // [16][2C] split, K-major
+  P.ok = load_weights(smem, wpack, B1, wcx, err);
+  const int row = P.feat();
+  for (long it = t0; P.ok && it < nt; it += tstep) {
+    const long f = it / nbt, b0 = (it % nbt) * TM;
+    if (rank) {   // this frequency's U_f into shared memory, V_f as the block-diagonal split operand
+      pipe_sync(P.id);   // the previous item's epilogue has read U_f
+      for (int e = P.ptid; e < C * rank; e += PT) us[(e / rank) * MIXR + e % rank] = __ldg(U + f * C * rank + e);
+      for (int e = P.ptid; e < 16 * K2; e += PT) {
+        const int n = e / K2, k = e % K2, r = n % 8, part = n / 8;
+        float v = 0.f;
+        if (r < rank && k / C == part) v = __ldg(Vm + (f * rank + r) * C + k % C);
+        uint32_t h, l;
+        tc::split_pack(v, 0.f, h, l);
+        const uint32_t o = tc::kmajor_offset(n, k, K2);
+        *reinterpret_cast<uint16_t*>(vblk + o) = (uint16_t)(h & 0xffffu);
+        *reinterpret_cast<uint16_t*>(vblk + VB / 2 + o) = (uint16_t)(l & 0xffffu);
+      }
+    }
+    const float* fin = in + f * sf;
+    for (int sl = 0; sl < 4; ++sl) {
+      const int part = sl / 2, k0 = (sl % 2) * KS;
+      fill_oct<KS>(T, b0, nb, P.ptid, [&](long b, int k, float (&o)[8]) { ld8(fin + b * sb + part * s_im + k0 + k, o); });
+      const Op vo = wop(vblk, 16, K2, 0, sl * KS);
+      const Gemm gt{P.tmem + K2, kop(T, KS), vo, KS, sl > 0, 16};
+      if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, KS), wop_t(smem, K2, K2, sl * KS), KS, sl > 0, K2},
+                      rank ? &gt : nullptr))
+        break;
+    }
+    if (!P.ok) break;
+    const long b = b0 + row;
+    const float gr = __ldg(g + 2 * f), gi = __ldg(g + 2 * f + 1);
+    float t[16];
+    if (rank) rld(P, K2, 0, t);
+#pragma unroll 1
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      float ar[16], ai[16];
+      rld(P, 0, j, ar);
+      rld(P, 0, j + C / 16, ai);
+      float yr[16], yi[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        yr[i] = ar[i] * gr - ai[i] * gi;
+        yi[i] = ar[i] * gi + ai[i] * gr;
+      }
+      if (rank) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const float* u = us + (16 * j + i) * MIXR;
+          float lr = 0.f, li = 0.f;
+#pragma unroll
+          for (int r = 0; r < MIXR; ++r) {
+            lr = fmaf(u[r], t[r], lr);
+            li = fmaf(u[r], t[8 + r], li);
+          }
+          yr[i] += lr;
+          yi[i] += li;
+        }
+      }
+      if (b < nb) {
+        float* fo = out + f * sf + b * sb + 16 * j;
+        st8(fo, yr);
+        st8(fo + 8, yr + 8);
+        st8(fo + s_im, yi);
+        st8(fo + s_im + 8, yi + 8);
+      }
+    }
+  }
+  pipe_finish(P, tslot, NCOL);
+}
+
 #undef PIPE_PROLOGUE
 
 int g_sms = 0;
@@ -1923,6 +2017,23 @@ bool aligned16(const void* p) { return p && (reinterpret_cast<uintptr_t>(p) % 16
 bool aligned32(const void* p) { return p && (reinterpret_cast<uintptr_t>(p) % 32) == 0; }
 
 }  // namespace
+
+// The width-96 mixing, launched by ffno_spectral_mix_tc (spectral_tc.cu) after its argument checks.
+namespace ffno {
+int launch_mix_tc96(const float* in, float* out, long F, long nb, long sf, long sb, long s_im, const void* wpack,
+                    const float* g, const float* U, const float* Vm, int rank, int* err, cudaStream_t s) {
+  if (rank > MIXR) return FFNO_EINVAL;
+  if (sf % 8 || sb % 8 || s_im % 8 || !aligned32(in) || !aligned32(out)) return FFNO_EINVAL;   // 32-byte rows
+  const size_t smem = mat_bytes(2 * C96, 2 * C96) + tile_bytes(KS) + mat_bytes(16, 2 * C96);
+  if (!launch_prep(k_mix_tc96, smem)) return FFNO_ELAUNCH;
+  const long items = F * ((nb + TM - 1) / TM);
+  const long grid = items < sms() ? items : sms();
+  k_mix_tc96<<<(unsigned)grid, PT, smem, s>>>(in, out, F, nb, sf, sb, s_im, static_cast<const uint8_t*>(wpack), g, U,
+                                              Vm, rank, err);
+  FFNO_CHECK_LAUNCH();
+  return FFNO_OK;
+}
+}  // namespace ffno
 
 // ====================================================================================================== C ABI
 extern "C" {

@@ -14,6 +14,11 @@
 
 using namespace ffno;
 
+namespace ffno {
+int launch_mix_tc96(const float* in, float* out, long F, long nb, long sf, long sb, long s_im, const void* wpack,
+                    const float* g, const float* U, const float* Vm, int rank, int* err, cudaStream_t s);
+}
+
 namespace {
 
 constexpr int XT = 512;    // threads of the mixing kernel
@@ -886,6 +891,8 @@ int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, 
   if (rank > MIX_RANK_TC) return FFNO_EINVAL;
   if (sf < 1 || sb < 1 || s_im < 1 || sf % 4 || sb % 4 || s_im % 4) return FFNO_EINVAL;
   if (F > 0x7fffffffL || nb > 0x7fffffffL) return FFNO_EINVAL;
+  if (C == 96)   // the production width: its own row-oriented kernel (pointwise_tc.cu); wpack = [M (2C x 2C)]
+    return ffno::launch_mix_tc96(in, out, F, nb, sf, sb, s_im, wpack, g, U, Vm, rank, err, (cudaStream_t)stream);
   if (C != 16 && C != 32 && C != 64) return FFNO_EINVAL;
   // tensor map over (channel, then f / b / re-im sorted by stride); boxes of (min(C, 32), 1, 128, 2)
   struct Dim { int logical; uint64_t extent, stride; uint32_t box; } d[3] = {

@@ -238,6 +238,11 @@ class Packed:
                                    s_gate=(s.input_gate[0], s.input_gate[2]),
                                    v_gate=(v.input_gate[0], v.input_gate[2])).items():
             pk["tc_" + name] = pk["tcb_" + name] = tc_pack(device, _w(c1), _w(c2))
+        # the mixing: wbig for the operator, wbig^T for its adjoint
+        for name, conv in (("s", s), ("v", v)):
+            wb = _wbig(conv.weight_real, conv.weight_imag)
+            pk[f"tc_{name}_mix"] = tc_pack(device, wb)
+            pk[f"tcb_{name}_mix"] = tc_pack(device, wb.t())
         # the branch fusion: the gates' [wg1, wg2] (also read transposed by the backward), [wf1], [wf2]
         pk["tc_fuse1"] = tc_pack(device, _w(b.branch_gate[0]), _w(b.branch_gate[2]))
         pk["tc_f1"] = tc_pack(device, _w(b.fuse[0]))
@@ -790,7 +795,7 @@ class Executor:
         m = self.model
         s = _stream()
         g, u, v = (fq.g_adj, fq.u_adj, fq.v_adj) if adjoint else (fq.g, fq.u, fq.v)
-        if self._tc() and m.freq_mix_rank <= MIX_RANK_TC:
+        if (self._tc() or self._tc_fuse96()) and m.freq_mix_rank <= MIX_RANK_TC:
             w = bp[("tcb_" if adjoint else "tc_") + branch + "_mix"]
             nat.call("ffno_spectral_mix_tc", inp.data_ptr(), out.data_ptr(), F, nb, sf, sb, s_im, m.width,
                      w.data_ptr(), g.data_ptr(), _ptr(u), _ptr(v), m.freq_mix_rank, ws.err.data_ptr(), s)
@@ -835,8 +840,8 @@ class Executor:
         return self.model.precision == "bf16" and self._packed.tc_chan and not getattr(self._tls, "fp32", False)
 
     def _tc_fuse96(self):
-        """Whether the branch fusion runs on the width-96 tensor-core kernels (gates, hidden layer, output; three
-        backward kernels)."""
+        """Whether the branch fusion (gates, hidden layer, output; three backward kernels) and the mixing run on the
+        width-96 tensor-core kernels."""
         return self._tc_chan() and not self._packed.tc and self.model.width == 96
 
     def _keeps_gates(self):

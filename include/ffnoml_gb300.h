@@ -434,7 +434,8 @@ int ffno_xform_tcr(const void* tpack, int Mp, int Kp, const float* in, float* ou
                    int accumulate, int* err, ffno_stream_t stream);
 /* ffno_spectral_mix on tensor cores (split-BF16); wpack = [wbig^T (2C x 2C)] with its output rows reordered so that
  * row p = 32 q + l is part l / 16 (0 re, 1 im) of channel 16 q + l % 16; C = 16, 32, 64; strides multiples of 4
- * floats. */
+ * floats. At C = 96: wpack = [M (2C x 2C)], out = g (x M) + the low-rank term, M = wbig (or wbig^T for the adjoint),
+ * rank <= 8, strides multiples of 8 floats, in and out 32-byte aligned. */
 int ffno_spectral_mix_tc(const float* in, float* out, long F, long nb, long sf, long sb, long s_im, int C,
                          const void* wpack, const float* g, const float* U, const float* Vm, int rank, int* err,
                          ffno_stream_t stream);

@@ -277,10 +277,11 @@ def test_xform_tc_matches_fp32(which, C, kind):
     _close(b, a)
 
 
-@pytest.mark.parametrize("C", [16, 32, 64])
+@pytest.mark.parametrize("C", [16, 32, 64, 96])
 @pytest.mark.parametrize("rank", [0, 3, 8])
 @pytest.mark.parametrize("layout", ["horizontal", "height"])
 def test_spectral_mix_tc(C, rank, layout):
+    """Width 96 runs its own row-oriented kernel: the pack is wbig itself (out = g (x wbig) + the low-rank term)."""
     from ffnoml_gb300.executor import mix_pack
     nat = _nat()
     F, nb = 37, 150
@@ -299,9 +300,9 @@ def test_spectral_mix_tc(C, rank, layout):
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     nat.call("ffno_spectral_mix", x.data_ptr(), a.data_ptr(), F, nb, sf, sb, s_im, C, wbig.data_ptr(), gg.data_ptr(),
              ptr(U), ptr(Vm), rank, _s())
-    nat.call("ffno_spectral_mix_tc", x.data_ptr(), b.data_ptr(), F, nb, sf, sb, s_im, C,
-             _hold(mix_pack(torch.device("cuda"), wbig.t().cpu())), gg.data_ptr(), ptr(U), ptr(Vm), rank,
-             err.data_ptr(), _s())
+    pack = _pack(wbig).data_ptr() if C == 96 else _hold(mix_pack(torch.device("cuda"), wbig.t().cpu()))
+    nat.call("ffno_spectral_mix_tc", x.data_ptr(), b.data_ptr(), F, nb, sf, sb, s_im, C, pack, gg.data_ptr(), ptr(U),
+             ptr(Vm), rank, err.data_ptr(), _s())
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     _close(b, a)
