@@ -556,8 +556,8 @@ def run_gb300(args):
         torch.cuda.empty_cache()
 
     # the production model (width 96, 4 blocks, hidden 128, M = 1001, H: the reference's MODEL_CONFIG defaults) on the
-    # same cube, fwd+VJP in both precisions: at width 96 the "bf16" form runs the transforms, table gradients,
-    # channel MLPs and input gates on the tensor cores, the fusion, mixing and head in FP32
+    # same cube, fwd+VJP in both precisions: at width 96 the "bf16" form runs every kernel family on the tensor cores
+    # (width-96 forms of the channel kernels)
     production = None
     if not args.no_production and not args.fwd_only:
         production = production_run(x, z, dev, world, timed)
@@ -636,9 +636,8 @@ def entry_breakdown(step, top):
 
 def production_run(x, z, dev, world, timed):
     """fwd+VJP of the production model (create_ffno3d defaults: width 96, 4 blocks, M = 1001, H atom) on the cube
-    x, z, 2 timed steps in FP32 and in "bf16" (transforms, height-table gradients, channel MLPs and input gates on
-    tensor cores, the fusion, mixing and head FP32 at this width), with the largest |d log10 n| between the two
-    forwards."""
+    x, z, 2 timed steps in FP32 and in "bf16" (every kernel family on tensor cores, the channel kernels in their
+    width-96 forms), with the largest |d log10 n| between the two forwards."""
     import torch
     from ffnoml_gb300 import create_ffno3d
     torch.manual_seed(5)
@@ -664,8 +663,9 @@ def production_run(x, z, dev, world, timed):
             ys[prec] = ex.forward(x, z, DXY, DXY)[0]
     hp = ex.height(ex.packed(dev), ex.geometry(z), dev)
     out["live_modes"] = int(hp["live"])
-    out["tensor_cores"] = {"every_kernel_family": bool(ex.packed(dev).tc),
-                           "channel_mlps_and_gates": bool(ex.packed(dev).tc_chan), "transforms": True}
+    m.set_precision("bf16")
+    out["tensor_cores"] = {"width_16_64_kernels": bool(ex.packed(dev).tc), "width_96_kernels": bool(ex._tc_fuse96()),
+                           "transforms": bool(ex._tc_xf())}
     out["bf16_speedup"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
     out["max_abs_dlog10n_bf16_vs_fp32"] = float((ys["bf16"] - ys["fp32"]).abs().max())
     del m, ex, ys, hp, cot

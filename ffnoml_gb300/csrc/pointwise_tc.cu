@@ -1986,6 +1986,161 @@ __global__ void __launch_bounds__(PT, 1) k_mix_tc96(const float* __restrict__ in
   pipe_finish(P, tslot, NCOL);
 }
 
+// ---------------------------------------------------------------------------------------- width 96: head
+// The level-fraction head at C = 96 (proj1 -> GELU -> proj2, head_output): o = gelu(x P1^T) P2^T + b2 (row-oriented,
+// the hidden layer in four K-slices of 48 through the tile), then the voxel's LTE log-softmax (head_voxel_fwd) by
+// the row's first thread. Weights [P1 (2C x C), P2 (NHP x 2C)]. Tensor memory: the hidden layer (2C) at 0, o at 2C.
+template <int NHP, typename T>
+__global__ void __launch_bounds__(PT, 1) k_head_tc96(const float* __restrict__ x, const float* __restrict__ xin, long V,
+                                                     const uint8_t* __restrict__ wpack, const float* __restrict__ b2,
+                                                     int nh, const __grid_constant__ ffno_head_params hp,
+                                                     float* __restrict__ out, float* __restrict__ head_out,
+                                                     int* __restrict__ err) {
+  constexpr int C = C96;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(2 * C, C), B2 = mat_bytes(NHP, 2 * C);
+  PIPE_PROLOGUE(2 * C + NHP, 1)
+  const Split T_ = split_at(smem + B1 + B2, TM, KS);
+  P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
+  const int row = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    for (int sl = 0; sl < 2; ++sl) {
+      fill_oct<KS>(T_, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(x + v * C + sl * KS + k, o); });
+      if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T_, KS), wop(smem, 2 * C, C, 0, sl * KS), KS, sl > 0, 2 * C})) break;
+    }
+    if (!P.ok) break;
+    for (int sl = 0; sl < 4; ++sl) {
+#pragma unroll 1
+      for (int j = 3 * sl; j < 3 * sl + 3; ++j) {
+        if (!owns(j, P.half)) continue;
+        float h[16];
+        rld(P, 0, j, h);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) h[i] = gelu_tc(h[i]);
+        put16(T_, row, 16 * j - KS * sl, KS, h);
+      }
+      if (!pipe_gemms(P, err, Gemm{P.tmem + 2 * C, kop(T_, KS), wop(smem + B1, NHP, 2 * C, 0, sl * KS), KS, sl > 0,
+                                   NHP}))
+        break;
+    }
+    if (!P.ok) break;
+    const long v = v0 + row;
+    if (P.half == 0) {   // whole warps (tensor-memory loads are warp-collective); rows past the cube skip the head
+      float o[NHP];
+#pragma unroll
+      for (int j = 0; j < NHP / 16; ++j) {
+        float r[16];
+        rld(P, 2 * C, j, r);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) o[16 * j + i] = r[i] + __ldg(b2 + 16 * j + i);
+      }
+      if (v < V) {
+        if (head_out)
+          for (int c = 0; c < nh; ++c) head_out[(long)c * V + v] = o[c];
+        head_voxel_fwd<T>(hp, o, head_inputs(hp, xin, V, v), out, V, v);
+      }
+    }
+  }
+  pipe_finish(P, tslot, NCOL);
+}
+
+// Its backward: the forward recomputed (the hidden pre-activation kept in tensor memory), o_bar from head_voxel_bwd
+// (which writes x_in_bar), h_bar = (o_bar P2) * gelu'(pre), x_bar = h_bar P1, both products reading the transposes
+// out of the forward's pack [P1, P2]. Tensor memory: pre (2C) at 0, o (NHP) at 2C, o_bar P2 (2C) at 2C + NHP, x_bar
+// (C) at 4C + NHP.
+template <int NHP, typename T>
+__global__ void __launch_bounds__(PT, 1) k_head_bwd_tc96(const float* __restrict__ x, const float* __restrict__ xin,
+                                                         const float* __restrict__ ybar, long V,
+                                                         const uint8_t* __restrict__ wpack,
+                                                         const float* __restrict__ b2,
+                                                         const __grid_constant__ ffno_head_params hp,
+                                                         float* __restrict__ xbar, float* __restrict__ xinbar,
+                                                         int* __restrict__ err) {
+  constexpr int C = C96;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t B1 = mat_bytes(2 * C, C), B2 = mat_bytes(NHP, 2 * C);
+  constexpr uint32_t DO = 2 * C, D3 = 2 * C + NHP, D4 = 4 * C + NHP;
+  static_assert(D4 + C <= 512, "tensor memory");
+  PIPE_PROLOGUE(D4 + C, 1)
+  const Split T_ = split_at(smem + B1 + B2, TM, KS), Ob = split_at(smem + B1 + B2, TM, NHP);
+  P.ok = load_weights(smem, wpack, B1 + B2, wcx, err);
+  const int row = P.feat();
+  for (long t = t0; P.ok && t < nt; t += tstep) {
+    const long v0 = t * TM;
+    for (int sl = 0; sl < 2; ++sl) {
+      fill_oct<KS>(T_, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(x + v * C + sl * KS + k, o); });
+      if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T_, KS), wop(smem, 2 * C, C, 0, sl * KS), KS, sl > 0, 2 * C})) break;
+    }
+    if (!P.ok) break;
+    for (int sl = 0; sl < 4; ++sl) {
+#pragma unroll 1
+      for (int j = 3 * sl; j < 3 * sl + 3; ++j) {
+        if (!owns(j, P.half)) continue;
+        float h[16];
+        rld(P, 0, j, h);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) h[i] = gelu_tc(h[i]);
+        put16(T_, row, 16 * j - KS * sl, KS, h);
+      }
+      if (!pipe_gemms(P, err, Gemm{P.tmem + DO, kop(T_, KS), wop(smem + B1, NHP, 2 * C, 0, sl * KS), KS, sl > 0,
+                                   NHP}))
+        break;
+    }
+    if (!P.ok) break;
+    const long v = v0 + row;
+    if (P.half == 0) {
+      float o[NHP];
+#pragma unroll
+      for (int j = 0; j < NHP / 16; ++j) {
+        float r[16];
+        rld(P, DO, j, r);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) o[16 * j + i] = r[i] + __ldg(b2 + 16 * j + i);
+      }
+      if (v < V) {
+        head_voxel_bwd<T>(hp, o, NHP, head_inputs(hp, xin, V, v), ybar, V, v, xinbar);
+      } else {
+#pragma unroll
+        for (int c = 0; c < NHP; ++c) o[c] = 0.f;
+      }
+#pragma unroll
+      for (int j = 0; j < NHP / 16; ++j) {
+        float r[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) r[i] = o[16 * j + i];
+        put16(Ob, row, 16 * j, NHP, r);
+      }
+    }
+    if (!pipe_gemms(P, err, Gemm{P.tmem + D3, kop(Ob, NHP), wop_t(smem + B1, NHP, 2 * C), NHP, false, 2 * C})) break;
+    for (int sl = 0; sl < 4; ++sl) {
+#pragma unroll 1
+      for (int j = 3 * sl; j < 3 * sl + 3; ++j) {
+        if (!owns(j, P.half)) continue;
+        float hp_[16], gb[16];
+        rld(P, 0, j, hp_);
+        rld(P, D3, j, gb);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) gb[i] *= gelu_grad_tc(hp_[i]);
+        put16(T_, row, 16 * j - KS * sl, KS, gb);
+      }
+      if (!pipe_gemms(P, err, Gemm{P.tmem + D4, kop(T_, KS), wop_t(smem, 2 * C, C, sl * KS), KS, sl > 0, C})) break;
+    }
+    if (!P.ok) break;
+#pragma unroll
+    for (int j = 0; j < C / 16; ++j) {
+      if (!owns(j, P.half)) continue;
+      float r[16];
+      rld(P, D4, j, r);
+      if (v < V) {
+        st8(xbar + v * C + 16 * j, r);
+        st8(xbar + v * C + 16 * j + 8, r + 8);
+      }
+    }
+  }
+  pipe_finish(P, tslot, NCOL);
+}
+
 #undef PIPE_PROLOGUE
 
 int g_sms = 0;
@@ -2399,14 +2554,39 @@ static bool head_ok(const ffno_head_params* hp, int nh, int nhp) {
     }                                                                                        \
   })
 
+#define HEAD96(KERNEL, SMEM, ...)                                                                    \
+  if (nhp == 16) {                                                                                  \
+    if (params->math32) {                                                                           \
+      if (!launch_prep(KERNEL<16, float>, SMEM)) return FFNO_ELAUNCH;                               \
+      KERNEL<16, float><<<grid_tc(V), PT, SMEM, s>>>(__VA_ARGS__);                                  \
+    } else {                                                                                        \
+      if (!launch_prep(KERNEL<16, double>, SMEM)) return FFNO_ELAUNCH;                              \
+      KERNEL<16, double><<<grid_tc(V), PT, SMEM, s>>>(__VA_ARGS__);                                 \
+    }                                                                                               \
+  } else {                                                                                          \
+    if (params->math32) {                                                                           \
+      if (!launch_prep(KERNEL<32, float>, SMEM)) return FFNO_ELAUNCH;                               \
+      KERNEL<32, float><<<grid_tc(V), PT, SMEM, s>>>(__VA_ARGS__);                                  \
+    } else {                                                                                        \
+      if (!launch_prep(KERNEL<32, double>, SMEM)) return FFNO_ELAUNCH;                              \
+      KERNEL<32, double><<<grid_tc(V), PT, SMEM, s>>>(__VA_ARGS__);                                 \
+    }                                                                                               \
+  }
+
 int ffno_head_fwd_tc(const float* x, const float* x_in, long V, int C, const void* wpack, const float* b2, int nh,
                      int nhp, const ffno_head_params* params, float* out, float* head_out, int* err,
                      ffno_stream_t stream) {
-  if (!tc_width(C) || V < 1 || !x || !x_in || !wpack || !b2 || !out || !err || !aligned16(wpack)) return FFNO_EINVAL;
+  if (!chan_width(C) || V < 1 || !x || !x_in || !wpack || !b2 || !out || !err || !aligned16(wpack)) return FFNO_EINVAL;
   if (!aligned32(x)) return FFNO_EINVAL;   // the hidden rows are read 32 bytes a request
   if (!head_ok(params, nh, nhp)) return FFNO_EINVAL;
   const uint8_t* w = static_cast<const uint8_t*>(wpack);
   cudaStream_t s = (cudaStream_t)stream;
+  if (C == C96) {
+    HEAD96(k_head_tc96, mat_bytes(2 * C96, C96) + mat_bytes(nhp, 2 * C96) + tile_bytes(KS),
+           x, x_in, V, w, b2, nh, *params, out, head_out, err)
+    FFNO_CHECK_LAUNCH();
+    return FFNO_OK;
+  }
   HEAD_DISPATCH(k_head_tc,
                 mat_bytes(2 * CC, CC) + mat_bytes(NN, 2 * CC) + 2 * (size_t)head_region(CC, NN, false),
                 x, x_in, V, w, b2, nh, *params, out, head_out, err)
@@ -2417,12 +2597,19 @@ int ffno_head_fwd_tc(const float* x, const float* x_in, long V, int C, const voi
 int ffno_head_bwd_tc(const float* x, const float* x_in, const float* y_bar, long V, int C, const void* wpack,
                      const float* b2, int nhp, const ffno_head_params* params, float* x_bar, float* x_in_bar,
                      int* err, ffno_stream_t stream) {
-  if (!tc_width(C) || V < 1 || !x || !x_in || !y_bar || !wpack || !b2 || !x_bar || !x_in_bar || !err ||
+  if (!chan_width(C) || V < 1 || !x || !x_in || !y_bar || !wpack || !b2 || !x_bar || !x_in_bar || !err ||
       !aligned16(wpack) || !aligned32(x))
     return FFNO_EINVAL;
   if (!head_ok(params, -1, nhp)) return FFNO_EINVAL;
   const uint8_t* w = static_cast<const uint8_t*>(wpack);
   cudaStream_t s = (cudaStream_t)stream;
+  if (C == C96) {   // the pack is the forward's [P1, P2]
+    if (!aligned32(x_bar)) return FFNO_EINVAL;
+    HEAD96(k_head_bwd_tc96, mat_bytes(2 * C96, C96) + mat_bytes(nhp, 2 * C96) + tile_bytes(KS),
+           x, x_in, y_bar, V, w, b2, *params, x_bar, x_in_bar, err)
+    FFNO_CHECK_LAUNCH();
+    return FFNO_OK;
+  }
   HEAD_DISPATCH(k_head_bwd_tc,
                 2 * mat_bytes(2 * CC, CC) + 2 * mat_bytes(NN, 2 * CC) + 2 * (size_t)head_region(CC, NN, true),
                 x, x_in, y_bar, V, w, b2, *params, x_bar, x_in_bar, err)

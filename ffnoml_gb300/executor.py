@@ -202,6 +202,8 @@ class Packed:
             w1, w2 = _w(model.proj1), p2.t()
             self.tc_head = tc_pack(device, w1, w2)
             self.tcb_head = tc_pack(device, w1, w2, w2.t(), w1.t())
+        elif self.tc_chan and C == 96:   # width 96: the backward reads the transposes out of the forward's pack
+            self.tc_head = self.tcb_head = tc_pack(device, _w(model.proj1), p2.t())
         self.freq_params = {k: v.detach().cpu() for k, v in model.state_dict().items() if ".freq_" in k}
         self.freq_key = table_store.freq_key(self.freq_params)
 
@@ -840,8 +842,8 @@ class Executor:
         return self.model.precision == "bf16" and self._packed.tc_chan and not getattr(self._tls, "fp32", False)
 
     def _tc_fuse96(self):
-        """Whether the branch fusion (gates, hidden layer, output; three backward kernels) and the mixing run on the
-        width-96 tensor-core kernels."""
+        """Whether the branch fusion (gates, hidden layer, output; three backward kernels), the mixing and the head
+        run on the width-96 tensor-core kernels."""
         return self._tc_chan() and not self._packed.tc and self.model.width == 96
 
     def _keeps_gates(self):
@@ -879,7 +881,7 @@ class Executor:
         """The level-fraction head of V voxels (default: all rows of x): x [V][C], xin [Cin][V] -> out [L][V]."""
         m = self.model
         V = x.shape[0] if V is None else V
-        if self._tc():
+        if self._tc() or self._tc_fuse96():
             nat.call("ffno_head_fwd_tc", x.data_ptr(), xin.data_ptr(), V, m.width, pk.tc_head.data_ptr(),
                      pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head32, out.data_ptr(), None, err.data_ptr(), _stream())
             return
@@ -1027,7 +1029,7 @@ class Executor:
             self._depth_weights(ws, z, D, HW)
             gb.wbar.zero_()
             # head
-            if tc:
+            if tc or self._tc_fuse96():
                 nat.call("ffno_head_bwd_tc", inputs[-1].data_ptr(), xin.data_ptr(), ybar[b].data_ptr(), V, C,
                          pk.tcb_head.data_ptr(), pk.b2.data_ptr(), pk.nhp, pk.head32, gb.xbar.data_ptr(),
                          xbar_in[b].data_ptr(), ws.err.data_ptr(), s)

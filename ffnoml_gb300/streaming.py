@@ -555,7 +555,7 @@ class StreamingVJP(StreamingForward):
             nat.call("ffno_si_population_cotangent", y.data_ptr(), cot_dev[b].data_ptr(), Vs, L,
                      cx.norm["mean_Y"].data_ptr(), cx.norm["std_Y"].data_ptr(), ybar.data_ptr(), cx.flags.data_ptr(), s)
             gb = gbd[b]
-            if tc:
+            if tc or ex._tc_fuse96():
                 nat.call("ffno_head_bwd_tc", ws.x.data_ptr(), x.data_ptr(), ybar.data_ptr(), Vs, C,
                          pk.tcb_head.data_ptr(), pk.b2.data_ptr(), pk.nhp, pk.head32, gb.xbar.data_ptr(),
                          xib.data_ptr(), ws.err.data_ptr(), s)

@@ -410,7 +410,9 @@ int ffno_fuse_bwd_b_tc(const float* spec_pre, const float* spec_coefs, const flo
 /* ffno_head_fwd and ffno_head_bwd (FFNO3D proj1 / proj2 and head_output, models/ffno_model.py:712-713, 729-748) with
  * the proj1 / proj2 GEMMs on tensor cores; b2 [nhp] (zero past nh); the LTE math in FP32 when params->math32, else
  * FP64. Forward wpack = [w1 (2C x C), w2 (nhp x 2C)]; backward wpack = [w1, w2, w2^T (2C x nhp), w1^T (C x 2C)],
- * with w2's rows past nh zero. x (the hidden state [V][C]) 32-byte aligned (FFNO_EINVAL otherwise). */
+ * with w2's rows past nh zero. x (the hidden state [V][C]) 32-byte aligned (FFNO_EINVAL otherwise). C = 96 also,
+ * where the backward takes the forward's pack [w1, w2] (reading the transposes out of it) and x_bar is 32-byte
+ * aligned too. */
 int ffno_head_fwd_tc(const float* x, const float* x_in, long V, int C, const void* wpack, const float* b2, int nh,
                      int nhp, const ffno_head_params* params, float* out, float* head_out, int* err,
                      ffno_stream_t stream);

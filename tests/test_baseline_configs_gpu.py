@@ -54,8 +54,8 @@ def test_bf16_forward_and_vjp_against_reference_float64(name):
     err = (y - a["y64"]).abs().max().item()
     ex = _rel(xb, a["xbar"])
     ex_ = model.executor()
-    print(f"{name} bf16: max |d log10 n| {err:.2e}, x_bar rel {ex:.2e}, tensor cores: every kernel family "
-          f"{ex_._packed.tc}, channel MLPs and gates {ex_._tc_chan()}, transforms {ex_._tc_xf()}")
+    print(f"{name} bf16: max |d log10 n| {err:.2e}, x_bar rel {ex:.2e}, tensor cores: widths 16-64 kernels "
+          f"{ex_._packed.tc}, width-96 kernels {ex_._tc_fuse96()}, transforms {ex_._tc_xf()}")
     assert err <= 2e-3
     assert ex <= 1e-2
 

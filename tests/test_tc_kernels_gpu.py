@@ -461,3 +461,51 @@ def test_fuse_tc96(V):
     assert torch.allclose(st[1], st[0], rtol=1e-4, atol=1e-6)
     for i in range(3):
         _close(o[3 + i], o[i])
+
+
+@pytest.mark.parametrize("math32", [0, 1])
+@pytest.mark.parametrize("atoms", [["H"], ["H", "CA"]])
+def test_head_tc96(math32, atoms):
+    """The head at width 96 (one pipeline, the hidden layer in K-slices, the backward reading the transposes out of
+    the forward's pack) against the FP32 head kernels, for the one- and two-species heads (7 and 14 head channels,
+    padded to 16), at a ragged voxel count."""
+    import bench
+    from ffnoml_gb300 import create_ffno3d
+    from ffnoml_gb300.executor import Packed
+    nat = _nat()
+    torch.manual_seed(4)
+    L = 6 * len(atoms)
+    model = create_ffno3d(6, L, atoms=atoms, n_layers=1)
+    with torch.no_grad():
+        model.proj2.weight.normal_(0.0, 0.3)
+        model.proj2.bias.normal_(0.0, 0.3)
+    model.set_normalization(bench.MEAN_X, bench.STD_X, np.zeros(L), np.ones(L))
+    C = model.width
+    assert C == 96
+    pk = Packed(model.eval(), torch.device("cuda"))
+    hp = nat.HeadParams.from_buffer_copy(pk.head)
+    hp.math32 = math32
+    Vn = 5 * 128 + 77
+    f, z = bench.synthetic_si((Vn, 1, 1), seed=13)
+    xn, _ = bench.normalised(f, z)
+    xin = torch.from_numpy(xn.reshape(6, Vn)).cuda().contiguous()
+    x, ybar = _rand(Vn, C, seed=11), _rand(L, Vn, seed=12)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = _s()
+    ref, out = torch.empty(L, Vn, device="cuda"), torch.empty(L, Vn, device="cuda")
+    nat.call("ffno_head_fwd", x.data_ptr(), xin.data_ptr(), Vn, C, pk.p1.data_ptr(), pk.p2.data_ptr(),
+             pk.b2.data_ptr(), pk.nh, pk.nhp, pk.head, ref.data_ptr(), None, s)
+    nat.call("ffno_head_fwd_tc", x.data_ptr(), xin.data_ptr(), Vn, C, pk.tc_head.data_ptr(), pk.b2.data_ptr(),
+             pk.nh, pk.nhp, hp, out.data_ptr(), None, err.data_ptr(), s)
+    assert (out - ref).abs().max().item() < 1e-4
+    xb_ref, xib_ref = torch.empty(Vn, C, device="cuda"), torch.empty(6, Vn, device="cuda")
+    xb, xib = torch.empty(Vn, C, device="cuda"), torch.empty(6, Vn, device="cuda")
+    nat.call("ffno_head_bwd", x.data_ptr(), xin.data_ptr(), ybar.data_ptr(), Vn, C, pk.p1.data_ptr(),
+             pk.p2.data_ptr(), pk.b2.data_ptr(), pk.p2t.data_ptr(), pk.p1t.data_ptr(), pk.nhp, pk.head,
+             xb_ref.data_ptr(), xib_ref.data_ptr(), s)
+    nat.call("ffno_head_bwd_tc", x.data_ptr(), xin.data_ptr(), ybar.data_ptr(), Vn, C, pk.tcb_head.data_ptr(),
+             pk.b2.data_ptr(), pk.nhp, hp, xb.data_ptr(), xib.data_ptr(), err.data_ptr(), s)
+    torch.cuda.synchronize()
+    assert err.item() == 0
+    _close(xb, xb_ref, 2e-4)
+    _close(xib, xib_ref, 1e-3 if math32 else 2e-4)
