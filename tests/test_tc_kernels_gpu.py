@@ -404,7 +404,7 @@ def test_outer_tc_in_slices(ma, mb, calls):
     _close(out - 0.25, ref, 2e-5)
 
 
-@pytest.mark.parametrize("V", [V, 152 * 128 * 3 + 77])
+@pytest.mark.parametrize("V", [V, 152 * 128 * 3 + 77, 600_000])
 def test_fuse_tc96(V):
     """The branch fusion at width 96 on tensor cores (gates, hidden pre-activation, output; backward in three
     kernels that read their transposed weights out of the forward's packs) against the FP32 fusion kernels."""
