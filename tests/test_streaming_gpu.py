@@ -22,7 +22,8 @@ def _model(width, precision):
     return m.cuda().eval().set_precision(precision)
 
 
-@pytest.mark.parametrize("width,precision,tol", [(32, "fp32", 1e-4), (64, "fp32", 1e-4), (64, "bf16", 2e-3)])
+@pytest.mark.parametrize("width,precision,tol", [(32, "fp32", 1e-4), (64, "fp32", 1e-4), (64, "bf16", 2e-3),
+                                                 (96, "bf16", 2e-3)])
 def test_streaming_matches_resident(width, precision, tol):
     import bench
     from ffnoml_gb300.runtime import GB300Backend
@@ -75,7 +76,8 @@ def _rel_per_channel(got, ref):
     return max(float(np.abs(got[c] - ref[c]).max() / np.abs(ref[c]).max()) for c in range(ref.shape[0]))
 
 
-@pytest.mark.parametrize("width,precision,tol", [(32, "fp32", 1e-4), (64, "fp32", 1e-4), (64, "bf16", 1e-2)])
+@pytest.mark.parametrize("width,precision,tol", [(32, "fp32", 1e-4), (64, "fp32", 1e-4), (64, "bf16", 1e-2),
+                                                 (96, "bf16", 1e-2)])
 def test_streaming_vjp_matches_resident(width, precision, tol):
     """The streaming VJP (block inputs in pinned host memory, blocks recomputed and back-propagated slab by slab)
     against the resident VJP through the service backend: the same kernels on the same voxels; only the GroupNorm
