@@ -1424,6 +1424,11 @@ __global__ void __launch_bounds__(PT, 1) k_mlp2_tc96(const float* __restrict__ i
   const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
+    if (P.ptid == 0) {   // the next tile's rows into L2 while this one runs (one tile step: 152 x 48 KB a tensor)
+      const long tn = (t + tstep) * TM;
+      prefetch_rows(in, tn, V, C);
+      prefetch_rows(MODE != 0 ? prev : nullptr, tn, V, C);
+    }
     fill96(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) {
       ld8(in + v * C + k, o);
       if (MODE != 0) {
@@ -1496,6 +1501,12 @@ __global__ void __launch_bounds__(PT, 1) k_mlp2_bwd_tc96(const float* __restrict
   const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
+    if (P.ptid == 0) {   // the next tile's rows into L2 while this one runs (one tile step: 152 x 48 KB a tensor)
+      const long tn = (t + tstep) * TM;
+      prefetch_rows(a, tn, V, C);
+      prefetch_rows(pb, tn, V, C);
+      prefetch_rows(base, tn, V, C);
+    }
     fill96(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(a + v * C + k, o); });
     if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, C), w1, C, false, 2 * C})) break;
     fill96(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(pb + v * C + k, o); });
@@ -1568,6 +1579,12 @@ __global__ void __launch_bounds__(PT, 1) k_fuse1_tc96(const float* __restrict__ 
   const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
+    if (P.ptid == 0) {   // the next tile's rows into L2 while this one runs (one tile step: 152 x 48 KB a tensor)
+      const long tn = (t + tstep) * TM;
+      prefetch_rows(x, tn, V, C);
+      prefetch_rows(sp, tn, V, C);
+      prefetch_rows(vp, tn, V, C);
+    }
     for (int sl = 0; sl < 6; ++sl) {   // K-slices of A: x, then the spec branch, then the vert branch
       const int part = sl / 2, k0 = (sl % 2) * KS;
       fill_oct<KS>(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) {
@@ -1632,6 +1649,12 @@ __global__ void __launch_bounds__(PT, 1) k_fuse_hidden_tc96(const float* __restr
   const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
+    if (P.ptid == 0) {   // the next tile's rows into L2 while this one runs (one tile step: 152 x 48 KB a tensor)
+      const long tn = (t + tstep) * TM;
+      prefetch_rows(sp, tn, V, C);
+      prefetch_rows(vp, tn, V, C);
+      prefetch_rows(gates, tn, V, 2 * C);
+    }
     for (int sl = 0; sl < 4; ++sl) {
       const int part = sl / 2, k0 = (sl % 2) * KS;
       fill_oct<KS>(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) {
@@ -1680,6 +1703,13 @@ __global__ void __launch_bounds__(PT, 1) k_fuse_out_tc96(const float* __restrict
   const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
+    if (P.ptid == 0) {   // the next tile's rows into L2 while this one runs (one tile step: 152 x 48 KB a tensor)
+      const long tn = (t + tstep) * TM;
+      prefetch_rows(hf, tn, V, 2 * C);
+      prefetch_rows(sp, tn, V, C);
+      prefetch_rows(vp, tn, V, C);
+      prefetch_rows(gates, tn, V, 2 * C);
+    }
     for (int sl = 0; sl < 4; ++sl) {
       fill_oct<KS>(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) {
         ld8(hf + v * 2 * C + sl * KS + k, o);
@@ -1741,6 +1771,11 @@ __global__ void __launch_bounds__(PT, 1) k_fuse_bwd_h_tc96(const float* __restri
   const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
+    if (P.ptid == 0) {   // the next tile's rows into L2 while this one runs (one tile step: 152 x 48 KB a tensor)
+      const long tn = (t + tstep) * TM;
+      prefetch_rows(fb, tn, V, C);
+      prefetch_rows(hf, tn, V, 2 * C);
+    }
     for (int sl = 0; sl < 2; ++sl) {
       fill_oct<KS>(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(fb + v * C + sl * KS + k, o); });
       if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, KS), wop_t(smem, C, 2 * C, sl * KS), KS, sl > 0, 2 * C})) break;
@@ -1840,6 +1875,12 @@ __global__ void __launch_bounds__(PT, 1) k_fuse_bwd_x_tc96(const float* __restri
   const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
+    if (P.ptid == 0) {   // the next tile's rows into L2 while this one runs (one tile step: 152 x 48 KB a tensor)
+      const long tn = (t + tstep) * TM;
+      prefetch_rows(q, tn, V, 2 * C);
+      prefetch_rows(hg, tn, V, C);
+      prefetch_rows(base, tn, V, C);
+    }
     for (int sl = 0; sl < 4; ++sl) {
       fill_oct<KS>(T, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(q + v * 2 * C + sl * KS + k, o); });
       if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T, KS), wop_t(smem + B1, 2 * C, C, sl * KS), KS, sl > 0, C})) break;
@@ -2005,6 +2046,10 @@ __global__ void __launch_bounds__(PT, 1) k_head_tc96(const float* __restrict__ x
   const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
+    if (P.ptid == 0) {   // the next tile's rows into L2 while this one runs (one tile step: 152 x 48 KB a tensor)
+      const long tn = (t + tstep) * TM;
+      prefetch_rows(x, tn, V, C);
+    }
     for (int sl = 0; sl < 2; ++sl) {
       fill_oct<KS>(T_, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(x + v * C + sl * KS + k, o); });
       if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T_, KS), wop(smem, 2 * C, C, 0, sl * KS), KS, sl > 0, 2 * C})) break;
@@ -2068,6 +2113,10 @@ __global__ void __launch_bounds__(PT, 1) k_head_bwd_tc96(const float* __restrict
   const int row = P.feat();
   for (long t = t0; P.ok && t < nt; t += tstep) {
     const long v0 = t * TM;
+    if (P.ptid == 0) {   // the next tile's rows into L2 while this one runs (one tile step: 152 x 48 KB a tensor)
+      const long tn = (t + tstep) * TM;
+      prefetch_rows(x, tn, V, C);
+    }
     for (int sl = 0; sl < 2; ++sl) {
       fill_oct<KS>(T_, v0, V, P.ptid, [&](long v, int k, float (&o)[8]) { ld8(x + v * C + sl * KS + k, o); });
       if (!pipe_gemms(P, err, Gemm{P.tmem, kop(T_, KS), wop(smem, 2 * C, C, 0, sl * KS), KS, sl > 0, 2 * C})) break;
