@@ -1936,42 +1936,51 @@ __global__ void __launch_bounds__(PT, 1) k_fuse_bwd_x_tc96(const float* __restri
 // ---------------------------------------------------------------------------------------- width 96: mixing
 // ffno_spectral_mix at C = 96 (SpectralConv2dFull.mix_spectrum, HeightSpectralConv's mode mixing): for frequency f and
 // row b, x = [re | im] (2C), out = g_f (x M) + [U_f t_re, U_f t_im], t = [V_f x_re, V_f x_im], with M the pack (wbig
-// for the mixing, wbig^T for its adjoint) read through its transpose view. An item is 128 rows b of one frequency; x
-// arrives in four K-slices of 48 through one tile, and each slice feeds x M (N = 2C) and the projections t (N = 16:
-// a block-diagonal [16][2C] operand built from V_f per item); the epilogue applies g_f and U_f (FP32, U_f in shared
-// memory). Tensor memory: x M at 0 (2C columns), t at 2C (16).
+// for the mixing, wbig^T for its adjoint) read through its transpose view. An item is 128 rows b of one frequency; two
+// pipelines a CTA take alternate items and share M. x arrives in four K-slices of 48 through the pipeline's tile, and
+// each slice feeds x M (N = 2C) and the projections t (N = 16: a block-diagonal [16][2C] operand whose rows 0..7 hold
+// V_f on the re half and rows 8..15 on the im half; its zero blocks and the rows beyond the rank are written once, the
+// rest per item); the epilogue applies g_f and U_f (FP32, U_f in shared memory). Tensor memory per pipeline: x M at 0
+// (2C columns), t at 2C (16).
 constexpr int MIXR = 8;   // the low-rank terms this kernel carries (the model's freq_mix_rank)
 
-__global__ void __launch_bounds__(PT, 1) k_mix_tc96(const float* __restrict__ in, float* __restrict__ out, long F,
+__global__ void __launch_bounds__(CT, 1) k_mix_tc96(const float* __restrict__ in, float* __restrict__ out, long F,
                                                     long nb, long sf, long sb, long s_im,
                                                     const uint8_t* __restrict__ wpack, const float* __restrict__ g,
                                                     const float* __restrict__ U, const float* __restrict__ Vm,
                                                     int rank, int* __restrict__ err) {
   constexpr int C = C96, K2 = 2 * C;
   extern __shared__ __align__(1024) uint8_t smem[];
-  constexpr uint32_t B1 = mat_bytes(K2, K2), VB = mat_bytes(16, K2);
-  __shared__ float us[C * MIXR];
+  constexpr uint32_t B1 = mat_bytes(K2, K2), VB = mat_bytes(16, K2), RB = tile_bytes(KS) + VB;
+  __shared__ float us_all[2][C * MIXR];
   const long nbt = (nb + TM - 1) / TM;
   const long V = F * nbt * TM;   // the prologue's tiles are the items: (frequency, block of 128 rows) pairs
-  PIPE_PROLOGUE(K2 + 16, 1)
-  const Split T = split_at(smem + B1, TM, KS);
-  uint8_t* vblk = smem + B1 + tile_bytes(KS);           // [16][2C] split, K-major
+  PIPE_PROLOGUE(K2 + 16, 2)
+  const Split T = split_at(smem + B1 + pid * RB, TM, KS);
+  uint8_t* vblk = smem + B1 + pid * RB + tile_bytes(KS);   // [16][2C] split, K-major
+  float* us = us_all[pid];
+  for (int e = P.ptid; e < (int)(VB / 16); e += PT) reinterpret_cast<uint4*>(vblk)[e] = make_uint4(0u, 0u, 0u, 0u);
+  for (int e = P.ptid; e < C * MIXR; e += PT) us[e] = 0.f;
   P.ok = load_weights(smem, wpack, B1, wcx, err);
   const int row = P.feat();
   for (long it = t0; P.ok && it < nt; it += tstep) {
     const long f = it / nbt, b0 = (it % nbt) * TM;
-    if (rank) {   // this frequency's U_f into shared memory, V_f as the block-diagonal split operand
-      pipe_sync(P.id);   // the previous item's epilogue has read U_f
-      for (int e = P.ptid; e < C * rank; e += PT) us[(e / rank) * MIXR + e % rank] = __ldg(U + f * C * rank + e);
-      for (int e = P.ptid; e < 16 * K2; e += PT) {
-        const int n = e / K2, k = e % K2, r = n % 8, part = n / 8;
-        float v = 0.f;
-        if (r < rank && k / C == part) v = __ldg(Vm + (f * rank + r) * C + k % C);
+    if (rank) {   // this frequency's U_f and V_f into shared memory
+      pipe_sync(P.id);   // the previous item's epilogue has read U_f (its MMAs, which read V_f, have completed)
+      const float* uf = U + f * C * rank;
+      const float* vf = Vm + f * rank * C;
+#pragma unroll 4
+      for (int e = P.ptid; e < C * rank; e += PT) us[(e / rank) * MIXR + e % rank] = __ldg(uf + e);
+#pragma unroll 4
+      for (int e = P.ptid; e < rank * C; e += PT) {
+        const int r = e / C, k = e % C;
         uint32_t h, l;
-        tc::split_pack(v, 0.f, h, l);
-        const uint32_t o = tc::kmajor_offset(n, k, K2);
-        *reinterpret_cast<uint16_t*>(vblk + o) = (uint16_t)(h & 0xffffu);
-        *reinterpret_cast<uint16_t*>(vblk + VB / 2 + o) = (uint16_t)(l & 0xffffu);
+        tc::split_pack(__ldg(vf + e), 0.f, h, l);
+        const uint32_t o0 = tc::kmajor_offset(r, k, K2), o1 = tc::kmajor_offset(8 + r, C + k, K2);
+        *reinterpret_cast<uint16_t*>(vblk + o0) = (uint16_t)(h & 0xffffu);
+        *reinterpret_cast<uint16_t*>(vblk + VB / 2 + o0) = (uint16_t)(l & 0xffffu);
+        *reinterpret_cast<uint16_t*>(vblk + o1) = (uint16_t)(h & 0xffffu);
+        *reinterpret_cast<uint16_t*>(vblk + VB / 2 + o1) = (uint16_t)(l & 0xffffu);
       }
     }
     const float* fin = in + f * sf;
@@ -1992,14 +2001,14 @@ __global__ void __launch_bounds__(PT, 1) k_mix_tc96(const float* __restrict__ in
 #pragma unroll 1
     for (int j = 0; j < C / 16; ++j) {
       if (!owns(j, P.half)) continue;
-      float ar[16], ai[16];
-      rld(P, 0, j, ar);
-      rld(P, 0, j + C / 16, ai);
       float yr[16], yi[16];
+      rld(P, 0, j, yr);
+      rld(P, 0, j + C / 16, yi);
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
-        yr[i] = ar[i] * gr - ai[i] * gi;
-        yi[i] = ar[i] * gi + ai[i] * gr;
+        const float ar = yr[i], ai = yi[i];
+        yr[i] = ar * gr - ai * gi;
+        yi[i] = ar * gi + ai * gr;
       }
       if (rank) {
 #pragma unroll
@@ -2024,7 +2033,7 @@ __global__ void __launch_bounds__(PT, 1) k_mix_tc96(const float* __restrict__ in
       }
     }
   }
-  pipe_finish(P, tslot, NCOL);
+  pipe_finish(P, tslot, 2 * NCOL);
 }
 
 // ---------------------------------------------------------------------------------------- width 96: head
@@ -2228,11 +2237,12 @@ int launch_mix_tc96(const float* in, float* out, long F, long nb, long sf, long 
                     const float* g, const float* U, const float* Vm, int rank, int* err, cudaStream_t s) {
   if (rank > MIXR) return FFNO_EINVAL;
   if (sf % 8 || sb % 8 || s_im % 8 || !aligned32(in) || !aligned32(out)) return FFNO_EINVAL;   // 32-byte rows
-  const size_t smem = mat_bytes(2 * C96, 2 * C96) + tile_bytes(KS) + mat_bytes(16, 2 * C96);
+  const size_t smem = mat_bytes(2 * C96, 2 * C96) + 2 * (tile_bytes(KS) + mat_bytes(16, 2 * C96));
   if (!launch_prep(k_mix_tc96, smem)) return FFNO_ELAUNCH;
   const long items = F * ((nb + TM - 1) / TM);
-  const long grid = items < sms() ? items : sms();
-  k_mix_tc96<<<(unsigned)grid, PT, smem, s>>>(in, out, F, nb, sf, sb, s_im, static_cast<const uint8_t*>(wpack), g, U,
+  const long pairs = (items + 1) / 2;   // two pipelines a CTA
+  const long grid = pairs < sms() ? pairs : sms();
+  k_mix_tc96<<<(unsigned)grid, CT, smem, s>>>(in, out, F, nb, sf, sb, s_im, static_cast<const uint8_t*>(wpack), g, U,
                                               Vm, rank, err);
   FFNO_CHECK_LAUNCH();
   return FFNO_OK;

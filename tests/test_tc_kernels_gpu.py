@@ -280,11 +280,13 @@ def test_xform_tc_matches_fp32(which, C, kind):
 @pytest.mark.parametrize("C", [16, 32, 64, 96])
 @pytest.mark.parametrize("rank", [0, 3, 8])
 @pytest.mark.parametrize("layout", ["horizontal", "height"])
-def test_spectral_mix_tc(C, rank, layout):
-    """Width 96 runs its own row-oriented kernel: the pack is wbig itself (out = g (x wbig) + the low-rank term)."""
+@pytest.mark.parametrize("nb", [150, 100])
+def test_spectral_mix_tc(C, rank, layout, nb):
+    """Width 96 runs its own row-oriented kernel: the pack is wbig itself (out = g (x wbig) + the low-rank term). With
+    nb = 100 the 37 items (frequency, 128-row block) are odd in number, so one CTA's second pipeline has no item."""
     from ffnoml_gb300.executor import mix_pack
     nat = _nat()
-    F, nb = 37, 150
+    F = 37
     if layout == "horizontal":
         sf, sb, s_im = C, 2 * F * C, F * C        # [b][2][F][C]
     else:
