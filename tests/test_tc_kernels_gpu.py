@@ -310,6 +310,28 @@ def test_spectral_mix_tc(C, rank, layout, nb):
     _close(b, a)
 
 
+def test_spectral_mix_tc96_large():
+    """The width-96 mixing on a height-layout spectrum larger than L2 ([2][64][16384][96] FP32, 0.8 GB each way),
+    rank 8: every CTA runs many items on both pipelines; against the FP32 kernel."""
+    nat = _nat()
+    C, F, nb, rank = 96, 64, 16384, 8
+    sf, sb, s_im = nb * C, C, F * nb * C
+    x = torch.randn(nb * 2 * F * C, generator=torch.Generator("cuda").manual_seed(1), device="cuda")
+    wr, wi = _rand(C, C, seed=2, scale=C ** -0.5), _rand(C, C, seed=3, scale=C ** -0.5)
+    wbig = torch.cat([torch.cat([wr, wi], 1), torch.cat([-wi, wr], 1)], 0).contiguous()
+    gg, U, Vm = _rand(F, 2, seed=4), _rand(F, C, rank, seed=5), _rand(F, rank, C, seed=6)
+    a, b = torch.empty_like(x), torch.empty_like(x)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nat.call("ffno_spectral_mix", x.data_ptr(), a.data_ptr(), F, nb, sf, sb, s_im, C, wbig.data_ptr(), gg.data_ptr(),
+             U.data_ptr(), Vm.data_ptr(), rank, _s())
+    pack = _pack(wbig)
+    nat.call("ffno_spectral_mix_tc", x.data_ptr(), b.data_ptr(), F, nb, sf, sb, s_im, C, pack.data_ptr(),
+             gg.data_ptr(), U.data_ptr(), Vm.data_ptr(), rank, err.data_ptr(), _s())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    _close(b, a)
+
+
 @pytest.mark.parametrize("name", ["hca_stretched", "w32_m16", "w64_m32"])
 @pytest.mark.parametrize("math32", [0, 1])
 def test_head_tc(name, math32):
