@@ -39,6 +39,8 @@ MEAN_X = np.array([4.75, 0.0, 0.0, 0.0, 17.5, -8.0], np.float32)
 STD_X = np.array([2.5 / math.sqrt(12), 5.0, 5.0, 5.0, 7.0 / math.sqrt(12), 8.0 / math.sqrt(12)], np.float32)
 CPU_SAMPLE = (64, 32, 32)       # sub-cube per step of the reference arm and of cpu_baseline (same C, L, M)
 CONFIG4 = (496, 252, 252)       # the full-volume inversion step (31.5 M voxels)
+CONFIG0 = (64, 32, 32)          # the CPU-runnable forward: width 32, 4 blocks, M = 16, H
+CONFIG3 = (256, 96, 96)         # the differentiation case: the width-64 model's fwd+VJP
 STREAM_CHUNKS = (32, 16)        # depth planes / column rows per device slab of the host-RAM streaming forward
 KERNELS_PER_CALL = {"ffno_column_info": 3, "ffno_outer": 2, "ffno_outer_tc": 2, "ffno_outer_tc_ld": 2}
 METRIC = "FFNO3D voxels/s fwd & fwd+VJP, BF16 vs FP32 @ |\u0394log n|\u22642e-3; p50/p99 latency"
@@ -215,6 +217,22 @@ def cpu_rate(model_state, shape, steps=1, warmup=0):
     dt = time.perf_counter() - t0
     vox = shape[0] * shape[1] * shape[2]
     return vox * steps / dt, dt, torch.get_num_threads()
+
+
+def cpu_forward_rate(model_state, cfg, shape, steps=1):
+    """Forward voxels/s of the oracle port (float32 torch on the host cores, no autograd) on a whole cube."""
+    import torch
+    from oracle.ffno_oracle import OracleFFNO3D
+    oracle = OracleFFNO3D(model_state, cfg, torch.float32, checkpoint_blocks=True)
+    f, z = synthetic_si(shape, seed=3)
+    x, zz = normalised(f, z)
+    x, zz = torch.from_numpy(x), torch.from_numpy(zz)
+    with torch.no_grad():
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            oracle.forward(x, zz, DXY, DXY)
+        dt = time.perf_counter() - t0
+    return shape[0] * shape[1] * shape[2] * steps / dt, dt, torch.get_num_threads()
 
 
 def run_reference(args):
@@ -575,6 +593,12 @@ def run_gb300(args):
     if not args.no_config4 and not args.fwd_only:
         config4 = config4_run(model, ex, dev, world, rank, timed)
 
+    # configs 0 and 3 of the benchmark table: the small width-32 forward (with the oracle port's forward of the same
+    # cube on the host cores) and the width-64 model's fwd+VJP on [1,6,256,96,96]
+    configs = None
+    if not args.no_configs and not args.fwd_only:
+        configs = configs_run(model, dev, world, rank, timed, with_cpu=not args.no_cpu_baseline)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         torch.set_num_threads(len(os.sched_getaffinity(0)))
@@ -614,6 +638,7 @@ def run_gb300(args):
             "cpu_baseline": cpu,
             "serving": serving, "streaming": streaming, "population_mesh": mesh_maps,
             "variant_p": variant_p, "per_column": per_column, "config4": config4, "production": production,
+            "configs": configs,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -671,6 +696,56 @@ def production_run(x, z, dev, world, timed):
     del m, ex, ys, hp, cot
     torch.cuda.empty_cache()
     return out
+
+
+def configs_run(model, dev, world, rank, timed, with_cpu):
+    """Config 0 (width 32, 4 blocks, M = 16, H; [1,6,64,32,32]): the forward on this GPU in FP32 and BF16 (20 timed
+    steps) and, on rank 0, the oracle port's FP32 forward of the same whole cube on the host cores. Config 3 (the
+    headline model on [1,6,256,96,96], cotangent N(0, 1)): fwd+VJP at the model's precision (3 timed steps)."""
+    import torch
+    from ffnoml_gb300 import create_ffno3d
+    from ffnoml_gb300.config import species_of
+    cfg0 = dict(width=32, n_layers=4, z_min_wavelength=40.0 / 15)
+    torch.manual_seed(20)
+    m0 = create_ffno3d(6, 6, atoms=["H"], **cfg0)
+    with torch.no_grad():
+        for name, p in m0.named_parameters():
+            if ".freq_u." in name:
+                p.normal_(0.0, 0.1)
+    m0.set_normalization(MEAN_X, STD_X, np.zeros(6), np.ones(6))
+    state0 = {k: v.detach().clone() for k, v in m0.state_dict().items()}
+    m0 = m0.eval().to(dev)
+    ex0 = m0.executor()
+    V0 = CONFIG0[0] * CONFIG0[1] * CONFIG0[2]
+    f_np, z_np = synthetic_si(CONFIG0, seed=21 + rank)
+    x_np, z_mm = normalised(f_np, z_np)
+    x0, z0 = torch.from_numpy(x_np).to(dev), torch.from_numpy(z_mm).to(dev)
+    c0 = {"shape": list(CONFIG0), "model": "width 32, 4 blocks, M = 16, H (6 levels)", "pass": "forward"}
+    for prec in ("fp32", "bf16"):
+        m0.set_precision(prec)
+        ms, _ = timed(lambda: ex0.forward(x0, z0, DXY, DXY), 20, 3)
+        c0[prec] = {"value": job_rate(V0, world, ms / 1e3), "unit": "voxels/s", "ms_per_step": ms}
+    if with_cpu and rank == 0:
+        torch.set_num_threads(len(os.sched_getaffinity(0)))
+        cfg = dict(cfg0, species=species_of(["H"]), in_channels=6, out_channels=6)
+        rate, dt, cores = cpu_forward_rate(state0, cfg, CONFIG0, steps=2)
+        c0["cpu"] = {"value": rate, "unit": "voxels/s", "cores": cores, "kind": "port", "seconds": dt,
+                     "sample": "the whole cube, two forwards, oracle port of the reference FFNO3D in float32 torch"}
+    del m0, ex0, x0, z0
+    D, H, W = CONFIG3
+    V3 = D * H * W
+    f_np, z_np = synthetic_si(CONFIG3, seed=31 + rank)
+    x_np, z_mm = normalised(f_np, z_np)
+    x3, z3 = torch.from_numpy(x_np).to(dev), torch.from_numpy(z_mm).to(dev)
+    cot3 = torch.randn((1, 12, D, H, W), generator=torch.Generator(dev).manual_seed(32 + rank), device=dev)
+    ex = model.executor()
+    ms, _ = timed(lambda: ex.backward(ex.forward(x3, z3, DXY, DXY, keep=True)[1], cot3), 3, 1)
+    c3 = {"shape": list(CONFIG3), "model": f"width {WIDTH}, {LAYERS} blocks, M = {MODES}, H + Ca II",
+          "pass": "fwd+vjp", "precision": model.precision, "value": job_rate(V3, world, ms / 1e3), "unit": "voxels/s",
+          "ms_per_step": ms}
+    del x3, z3, cot3
+    torch.cuda.empty_cache()
+    return {"config0": c0, "config3": c3}
 
 
 def config4_run(model, ex, dev, world, rank, timed):
@@ -814,6 +889,7 @@ def main():
     ap.add_argument("--no-production", action="store_true",
                     help="skip the production model (width 96, M = 1001) steps")
     ap.add_argument("--no-per-column", action="store_true", help="skip the per-column height grid step")
+    ap.add_argument("--no-configs", action="store_true", help="skip the config 0 forward and the config 3 fwd+VJP")
     ap.add_argument("--serve-requests", type=int, default=256)
     args = ap.parse_args()
     args.shape = tuple(int(v) for v in args.shape.split(","))
