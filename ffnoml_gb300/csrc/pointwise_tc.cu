@@ -1963,19 +1963,36 @@ __global__ void __launch_bounds__(CT, 1) k_mix_tc96(const float* __restrict__ in
   for (int e = P.ptid; e < C * MIXR; e += PT) us[e] = 0.f;
   P.ok = load_weights(smem, wpack, B1, wcx, err);
   const int row = P.feat();
+  // the per-frequency values of the pipeline's next item (g_f; this thread's U_f and V_f elements e = ptid + u PT,
+  // e < C rank <= 3 PT), loaded one item ahead so that their latency stays off the item's path
+  static_assert(C * MIXR <= 3 * PT, "three U_f and V_f elements a thread");
+  float un[3], vn[3], grn = 0.f, gin = 0.f;
+  auto load_freq = [&](long it2) {
+    const long f2 = it2 / nbt;
+    grn = __ldg(g + 2 * f2);
+    gin = __ldg(g + 2 * f2 + 1);
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      const int e = P.ptid + u * PT;
+      const bool in = rank && e < C * rank;
+      un[u] = in ? __ldg(U + f2 * C * rank + e) : 0.f;
+      vn[u] = in ? __ldg(Vm + f2 * rank * C + e) : 0.f;
+    }
+  };
+  if (t0 < nt) load_freq(t0);
   for (long it = t0; P.ok && it < nt; it += tstep) {
     const long f = it / nbt, b0 = (it % nbt) * TM;
+    const float gr = grn, gi = gin;
     if (rank) {   // this frequency's U_f and V_f into shared memory
       pipe_sync(P.id);   // the previous item's epilogue has read U_f (its MMAs, which read V_f, have completed)
-      const float* uf = U + f * C * rank;
-      const float* vf = Vm + f * rank * C;
-#pragma unroll 4
-      for (int e = P.ptid; e < C * rank; e += PT) us[(e / rank) * MIXR + e % rank] = __ldg(uf + e);
-#pragma unroll 4
-      for (int e = P.ptid; e < rank * C; e += PT) {
-        const int r = e / C, k = e % C;
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        const int e = P.ptid + u * PT;
+        if (e >= C * rank) break;
+        us[(e / rank) * MIXR + e % rank] = un[u];
+        const int r = e / C, k = e % C;   // V_f element (r, k)
         uint32_t h, l;
-        tc::split_pack(__ldg(vf + e), 0.f, h, l);
+        tc::split_pack(vn[u], 0.f, h, l);
         const uint32_t o0 = tc::kmajor_offset(r, k, K2), o1 = tc::kmajor_offset(8 + r, C + k, K2);
         *reinterpret_cast<uint16_t*>(vblk + o0) = (uint16_t)(h & 0xffffu);
         *reinterpret_cast<uint16_t*>(vblk + VB / 2 + o0) = (uint16_t)(l & 0xffffu);
@@ -1983,6 +2000,7 @@ __global__ void __launch_bounds__(CT, 1) k_mix_tc96(const float* __restrict__ in
         *reinterpret_cast<uint16_t*>(vblk + VB / 2 + o1) = (uint16_t)(l & 0xffffu);
       }
     }
+    if (it + tstep < nt) load_freq(it + tstep);
     const float* fin = in + f * sf;
     for (int sl = 0; sl < 4; ++sl) {
       const int part = sl / 2, k0 = (sl % 2) * KS;
@@ -1995,7 +2013,6 @@ __global__ void __launch_bounds__(CT, 1) k_mix_tc96(const float* __restrict__ in
     }
     if (!P.ok) break;
     const long b = b0 + row;
-    const float gr = __ldg(g + 2 * f), gi = __ldg(g + 2 * f + 1);
     float t[16];
     if (rank) rld(P, K2, 0, t);
 #pragma unroll 1
