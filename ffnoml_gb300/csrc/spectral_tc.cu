@@ -522,6 +522,40 @@ __global__ void __launch_bounds__(XT, 1)
     tc::tc_after_sync();
   };
 
+  // this thread's elements of an item's block-diagonal V_f (pairs e = tid + i XT < NT K2 / 2) and U_f (pairs
+  // e = tid + i XT < 128 NT / 2) operands, loaded one item ahead so that their latency stays off the item's path
+  static_assert(NT * K2 / 2 <= 2 * XT && 128 * NT / 2 == 2 * XT, "two V_f and two U_f pairs a thread");
+  float vn[2][2] = {}, un[2][2] = {};
+  auto load_vu = [&](long it2) {
+    const long f2 = it2 / nbt;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int e = tid + i * XT;
+      const int n = e / (K2 / 2), k = (e % (K2 / 2)) * 2;
+      const int kp = k >= C ? 1 : 0, c = k - kp * C;
+      const int r = n & 7;
+      vn[i][0] = vn[i][1] = 0.f;
+      if (e < NT * K2 / 2 && r < rank && (n >> 3) == kp) {
+        const float* vr = Vm + (f2 * rank + r) * (long)C + c;
+        vn[i][0] = __ldg(vr);
+        vn[i][1] = __ldg(vr + 1);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int e = tid + i * XT;
+      const int ps = e / (NT / 2), k = (e % (NT / 2)) * 2;
+      const int sp = (ps & 31) >> 4, sc = 16 * (ps >> 5) + (ps & 15);
+      un[i][0] = un[i][1] = 0.f;
+      if (ps < 2 * C && (k >> 3) == sp) {
+        const int r = k & 7;
+        const float* ur = U + (f2 * C + sc) * (long)rank;
+        if (r < rank) un[i][0] = __ldg(ur + r);
+        if (r + 1 < rank) un[i][1] = __ldg(ur + r + 1);
+      }
+    }
+  };
+  if (rank && it < items) load_vu(it);
   uint32_t j = 0;
   for (; ok && it < items; it += gridDim.x, ++j) {
     const long f = it / nbt, b0 = (it % nbt) * 128;
@@ -554,34 +588,23 @@ __global__ void __launch_bounds__(XT, 1)
     }
     if (rank) {
       // block-diagonal V_f: rows 0..r-1 act on the re half, rows 8..8+r-1 on the im half, the others are zero
-      for (int e = tid; e < NT * K2 / 2; e += XT) {
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int e = tid + i * XT;
+        if (e >= NT * K2 / 2) break;
         const int n = e / (K2 / 2), k = (e % (K2 / 2)) * 2;
-        const int kp = k >= C ? 1 : 0, c = k - kp * C;
-        const int r = n & 7;
-        float v0 = 0.f, v1 = 0.f;
-        if (r < rank && (n >> 3) == kp) {
-          const float* vr = Vm + (f * rank + r) * (long)C + c;
-          v0 = __ldg(vr);
-          v1 = __ldg(vr + 1);
-        }
         uint32_t hi, lo;
-        tc::split_pack(v0, v1, hi, lo);
+        tc::split_pack(vn[i][0], vn[i][1], hi, lo);
         *reinterpret_cast<uint32_t*>(sV + tc::kmajor_offset(n, k, K2)) = hi;
         *reinterpret_cast<uint32_t*>(sV + (uint32_t)NT * K2 * 2 + tc::kmajor_offset(n, k, K2)) = lo;
       }
       // block-diagonal U_f by output slot: slot p (part, channel pc) takes U_f[pc][0..r) in columns 8 part + r
-      for (int e = tid; e < 128 * NT / 2; e += XT) {
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int e = tid + i * XT;
         const int ps = e / (NT / 2), k = (e % (NT / 2)) * 2;
-        const int sp = (ps & 31) >> 4, sc = 16 * (ps >> 5) + (ps & 15);
-        float u0 = 0.f, u1 = 0.f;
-        if (ps < 2 * C && (k >> 3) == sp) {
-          const int r = k & 7;
-          const float* ur = U + (f * C + sc) * (long)rank;
-          if (r < rank) u0 = __ldg(ur + r);
-          if (r + 1 < rank) u1 = __ldg(ur + r + 1);
-        }
         uint32_t hi, lo;
-        tc::split_pack(u0, u1, hi, lo);
+        tc::split_pack(un[i][0], un[i][1], hi, lo);
         *reinterpret_cast<uint32_t*>(sU + tc::kmajor_offset(ps, k, NT)) = hi;
         *reinterpret_cast<uint32_t*>(sU + LB + tc::kmajor_offset(ps, k, NT)) = lo;
       }
@@ -591,6 +614,7 @@ __global__ void __launch_bounds__(XT, 1)
     __syncthreads();
     tc::tc_after_sync();
     load_pending = it + gridDim.x < items;
+    if (rank && load_pending) load_vu(it + gridDim.x);   // the next item's V_f and U_f, used after its rows land
     if (tid == 0) {
       if (load_pending) issue_load(it + gridDim.x);
       const uint32_t w_hi = tc::smem_u32(sW), x_hi = tc::smem_u32(sX);
